@@ -1,0 +1,598 @@
+/*
+ * oracle.c -- CPU restatement of FrameLab's reconstruction hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY. This file is the checker the GPU library is
+ * compared against; nothing in the product library links, loads or calls it.
+ * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use it.
+ *
+ * Two families of functions:
+ *
+ *  (1) *_f32: restatements of the reference's own single-precision CPU
+ *      kernels, written so that every float operation (operands, order,
+ *      rounding) is the one the reference performs. Compiled with
+ *      -ffp-contract=off they reproduce the reference bit for bit; that claim
+ *      is pinned by tests/test_oracle_pin.py against the reference sources
+ *      compiled unmodified into oracle/_ref (Makefile in this directory) and
+ *      by the committed fixtures in tests/golden/.
+ *
+ *  (2) *_f64: exact-arithmetic (FP64) Siddon model of the same geometry:
+ *      exact ray/voxel intersection lengths, its transpose, and the count of
+ *      voxels each ray crosses. This is the "FP64 oracle" every error figure
+ *      is quoted against.
+ *
+ * Conventions (reference's own, matlab/mex/src/Ax_cone_mf_cpu_siddon.cpp):
+ *   volume index  iz*ny*nx + iy*nx + ix  (x fastest), voxel xy pitch 1,
+ *   x/y planes at integers -n/2 .. n/2, z planes at (k - nz/2)*dz;
+ *   sinogram index iv*na*nb + ib*na + ia (detector column fastest);
+ *   source  (-SO cos phi, -SO sin phi, sd_z[iv]),
+ *   detector (OD cos phi - y_det sin phi, OD sin phi + y_det cos phi,
+ *             z_det[ib] + sd_z[iv]);  outputs multiplied by `scale`.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* ------------------------------------------------------------------------- */
+/* (1a) Siddon forward, FP32, reference arithmetic                            */
+/* ------------------------------------------------------------------------- */
+
+/*
+ * One axis of plane crossings, generated lazily in ascending alpha order.
+ * The reference fills arrays alpha_x[] etc. with (i - p1)/d for
+ * i = -n/2..n/2 (ascending when p1 < p2, descending i when p1 > p2) and merges
+ * them with sort_alpha() (sort_alpha.cpp:15-60), dropping a value of one list
+ * that equals the current head of the other. Here the lists are produced on
+ * the fly and merged by always taking the smallest head; a value that the
+ * reference de-duplicates becomes a zero-length segment whose contribution is
+ * 0*x = +0, so the running sum is bit-identical for finite volumes.
+ */
+typedef struct {
+    int active;     /* p1 != p2 : the ray crosses this family of planes */
+    int i, iend;    /* current and one-past-last plane index (stepping by di) */
+    int di;         /* +1 when p1 < p2, -1 when p1 > p2 */
+    int zaxis;      /* 1: alpha = (i*dz0 - p1)/d ; 0: alpha = (i - p1)/d */
+    float p1, d, dz0;
+    float head;     /* alpha of plane i */
+} orc_axis;
+
+static float orc_axis_alpha(const orc_axis *a, int i)
+{
+    if (a->zaxis) {
+        float zi = (float)i * a->dz0;            /* Ax_cone_mf_cpu_siddon.cpp:69 */
+        return (zi - a->p1) / a->d;
+    }
+    return ((float)i - a->p1) / a->d;            /* Ax_fan_mf_cpu_siddon.cpp:44 */
+}
+
+static void orc_axis_init(orc_axis *a, float p1, float p2, int n, int zaxis, float dz0)
+{
+    int n2 = n / 2;
+    a->zaxis = zaxis; a->dz0 = dz0; a->p1 = p1; a->d = p2 - p1;
+    a->active = (p1 != p2);
+    if (!a->active) return;
+    if (p1 < p2) { a->i = -n2; a->iend = n2 + 1; a->di = 1; }
+    else         { a->i = n2;  a->iend = -n2 - 1; a->di = -1; }
+    a->head = orc_axis_alpha(a, a->i);
+}
+
+static int orc_axis_more(const orc_axis *a) { return a->active && a->i != a->iend; }
+
+static void orc_axis_pop(orc_axis *a)
+{
+    a->i += a->di;
+    if (a->i != a->iend) a->head = orc_axis_alpha(a, a->i);
+}
+
+/* index of the axis holding the smallest head, or -1 when all are exhausted */
+static int orc_pick(orc_axis *ax, int naxes)
+{
+    int best = -1;
+    for (int k = 0; k < naxes; k++)
+        if (orc_axis_more(&ax[k]) && (best < 0 || ax[k].head < ax[best].head)) best = k;
+    return best;
+}
+
+/*
+ * Fan-beam Siddon projection of views [v0, v1).
+ * Restates Ax_fan_mf_cpu_siddon (Ax_fan_mf_cpu_siddon.cpp:19-93).
+ */
+void orc_fan_siddon_f32(const float *X, float *y, float SO, float OD, float scale,
+                        int nx, int ny, int v0, int v1, const float *sd_phi, int nd,
+                        const float *y_det, const int *id_X)
+{
+    int nx2 = nx / 2, ny2 = ny / 2;
+    long n = (long)nx * ny;
+    for (int iv = v0; iv < v1; iv++) {
+        const float *x = X + (long)id_X[iv] * n;
+        /* C++ <math.h> resolves cos(float) to the float overload (cosf) */
+        float cphi = cosf(sd_phi[iv]), sphi = sinf(sd_phi[iv]);
+        float x1 = cphi * (-SO), y1 = sphi * (-SO);
+        for (int id = 0; id < nd; id++) {
+            float x2 = cphi * OD - sphi * y_det[id];
+            float y2 = sphi * OD + cphi * y_det[id];
+            float dx = x2 - x1, dy = y2 - y1;
+            orc_axis ax[2];
+            orc_axis_init(&ax[0], x1, x2, nx, 0, 1.0f);
+            orc_axis_init(&ax[1], y1, y2, ny, 0, 1.0f);
+            float total = (float)sqrt(dx * dx + dy * dy);
+            float acc = 0.0f;
+            int k = orc_pick(ax, 2);
+            if (k >= 0) {
+                float prev = ax[k].head;
+                orc_axis_pop(&ax[k]);
+                while ((k = orc_pick(ax, 2)) >= 0) {
+                    float next = ax[k].head;
+                    orc_axis_pop(&ax[k]);
+                    float ac = 0.5f * (prev + next);
+                    int tx = (int)floorf(x1 + ac * dx + (float)nx2);
+                    if (tx >= 0 && tx < nx) {
+                        int ty = (int)floorf(y1 + ac * dy + (float)ny2);
+                        if (ty >= 0 && ty < ny) {
+                            float seg = (next - prev) * total;
+                            acc += seg * x[ty * nx + tx];
+                        }
+                    }
+                    prev = next;
+                }
+            }
+            y[(long)iv * nd + id] = acc * scale;
+        }
+    }
+}
+
+/*
+ * Cone-beam Siddon projection of views [v0, v1).
+ * Restates Ax_cone_mf_cpu_siddon (Ax_cone_mf_cpu_siddon.cpp:19-134).
+ */
+void orc_cone_siddon_f32(const float *X, float *y, float SO, float OD, float scale,
+                         int nx, int ny, int nz, int v0, int v1, const float *sd_phi,
+                         const float *sd_z, int na, int nb, const float *y_det,
+                         const float *z_det, const int *id_X, float dz0)
+{
+    int nx2 = nx / 2, ny2 = ny / 2, nz2 = nz / 2;
+    long n = (long)nx * ny * nz, nd = (long)na * nb;
+    for (int iv = v0; iv < v1; iv++) {
+        const float *x = X + (long)id_X[iv] * n;
+        /* C++ <math.h> resolves cos(float) to the float overload (cosf) */
+        float cphi = cosf(sd_phi[iv]), sphi = sinf(sd_phi[iv]);
+        float x1 = cphi * (-SO), y1 = sphi * (-SO), z1 = sd_z[iv];
+        for (int ib = 0; ib < nb; ib++) {
+            for (int ia = 0; ia < na; ia++) {
+                float x2 = cphi * OD - sphi * y_det[ia];
+                float y2 = sphi * OD + cphi * y_det[ia];
+                float z2 = z_det[ib] + sd_z[iv];
+                float dx = x2 - x1, dy = y2 - y1, dz = z2 - z1;
+                orc_axis ax[3];
+                orc_axis_init(&ax[0], x1, x2, nx, 0, 1.0f);
+                orc_axis_init(&ax[1], y1, y2, ny, 0, 1.0f);
+                orc_axis_init(&ax[2], z1, z2, nz, 1, dz0);
+                float total = (float)sqrt(dx * dx + dy * dy + dz * dz);
+                float acc = 0.0f;
+                int k = orc_pick(ax, 3);
+                if (k >= 0) {
+                    float prev = ax[k].head;
+                    orc_axis_pop(&ax[k]);
+                    while ((k = orc_pick(ax, 3)) >= 0) {
+                        float next = ax[k].head;
+                        orc_axis_pop(&ax[k]);
+                        float ac = (prev + next) / 2;
+                        int tx = (int)floorf(x1 + ac * dx + (float)nx2);
+                        if (tx >= 0 && tx < nx) {
+                            int ty = (int)floorf(y1 + ac * dy + (float)ny2);
+                            if (ty >= 0 && ty < ny) {
+                                int tz = (int)floorf((z1 + ac * dz) / dz0 + (float)nz2);
+                                if (tz >= 0 && tz < nz) {
+                                    float seg = (next - prev) * total;
+                                    acc += seg * x[((long)tz * ny + ty) * nx + tx];
+                                }
+                            }
+                        }
+                        prev = next;
+                    }
+                }
+                y[(long)iv * nd + (long)ib * na + ia] = acc * scale;
+            }
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------- */
+/* (1b) Chord-length backprojectors, FP32, reference arithmetic               */
+/* ------------------------------------------------------------------------- */
+
+static float orc_absf(float v) { return v > 0 ? v : -v; }
+
+/*
+ * Chord of the line a*x + b*y = c through the unit pixel centred at (x, y).
+ * Restates find_l (find_l.cpp:18-45): the distance of the centre to the line
+ * decides between the full chord 1/max(|a|,|b|) and the corner-clipped one.
+ */
+float orc_chord_unit_pixel(float a, float b, float c, float x, float y)
+{
+    float aa = orc_absf(a), bb = orc_absf(b);
+    float ha = aa / 2, hb = bb / 2;
+    float reach = ha + hb;
+    float off = c - a * x - b * y;
+    float d = orc_absf(off);
+    if (!(d < reach)) return 0.0f;
+    float flat = orc_absf(ha - hb);
+    float full = (ha < hb) ? (float)1.0 / bb : (float)1.0 / aa;
+    return (d <= flat) ? full : (reach - d) / (aa * bb);
+}
+
+/*
+ * Chord of the segment line through a (w x h) rectangle centred at (x, y).
+ * Restates the 2-D helper of find_l_3d.cpp:19-92: faces perpendicular to the
+ * dominant direction are tried first; the first two hits define the chord.
+ */
+static float orc_chord_rect(float px, float py, float qx, float qy, float w, float h,
+                            float x, float y)
+{
+    float a = qx - px, b = qy - py;
+    float hw = w / 2, hh = h / 2;
+    if (a == 0) return (orc_absf(px - x) <= hw) ? h : 0.0f;
+    if (b == 0) return (orc_absf(py - y) <= hh) ? w : 0.0f;
+    float rx = px - x, ry = py - y;
+    float hx[2], hy[2];
+    int nh = 0;
+    /* families: 0 = faces x = -+hw, 1 = faces y = -+hh */
+    int first = (orc_absf(a) > orc_absf(b)) ? 0 : 1;
+    for (int pass = 0; pass < 2; pass++) {
+        int fam = (pass == 0) ? first : 1 - first;
+        if (pass == 1 && nh >= 2) break;
+        for (int side = 0; side < 2; side++) {
+            if (pass == 1 && side == 1 && nh >= 2) break;
+            if (fam == 0) {
+                float s = b / a, t = s * (-rx) + ry, u = s * hw;
+                float yy = side ? t + u : t - u;
+                if (orc_absf(yy) <= hh) { hx[nh] = side ? hw : -hw; hy[nh] = yy; nh++; }
+            } else {
+                float s = a / b, t = s * (-ry) + rx, u = s * hh;
+                float xx = side ? t + u : t - u;
+                if (orc_absf(xx) <= hw) { hy[nh] = side ? hh : -hh; hx[nh] = xx; nh++; }
+            }
+        }
+    }
+    if (nh != 2) return 0.0f;
+    float ex = hx[1] - hx[0], ey = hy[1] - hy[0];
+    return (float)sqrt(ex * ex + ey * ey);
+}
+
+/*
+ * Chord of the line through P=(px,py,pz) and Q=(qx,qy,qz) with the box of
+ * size (w,h,t) centred at (x,y,z). Restates find_l_3d (find_l_3d.cpp:94-182):
+ * the two face families perpendicular to x and y are tried in order of the
+ * dominant xy direction, the z faces last; the first two hits give the chord.
+ */
+float orc_chord_box(float px, float py, float pz, float qx, float qy, float qz,
+                    float w, float h, float t, float x, float y, float z)
+{
+    float a = qx - px, b = qy - py, c = qz - pz;
+    float hw = w / 2, hh = h / 2, ht = t / 2;
+    if (a == 0) return orc_chord_rect(py, pz, qy, qz, h, t, y, z);
+    if (b == 0) return orc_chord_rect(px, pz, qx, qz, w, t, x, z);
+    float rx = px - x, ry = py - y, rz = pz - z;
+    float hx[2], hy[2], hz[2];
+    int nh = 0;
+    /* families: 0 = x faces, 1 = y faces, 2 = z faces */
+    int order[3];
+    if (orc_absf(a) > orc_absf(b)) { order[0] = 0; order[1] = 1; }
+    else                           { order[0] = 1; order[1] = 0; }
+    order[2] = 2;
+    for (int pass = 0; pass < 3; pass++) {
+        if (pass > 0 && nh >= 2) break;
+        int fam = order[pass];
+        float u0, v0, u1, v1;   /* the two in-face coordinates, centre and half-span */
+        float lim0, lim1;
+        if (fam == 0) {
+            float s = b / a; u0 = s * (-rx) + ry; u1 = s * hw;
+            s = c / a;       v0 = s * (-rx) + rz; v1 = s * hw;
+            lim0 = hh; lim1 = ht;
+        } else if (fam == 1) {
+            float s = a / b; u0 = s * (-ry) + rx; u1 = s * hh;
+            s = c / b;       v0 = s * (-ry) + rz; v1 = s * hh;
+            lim0 = hw; lim1 = ht;
+        } else {
+            float s = a / c; u0 = s * (-rz) + rx; u1 = s * ht;
+            s = b / c;       v0 = s * (-rz) + ry; v1 = s * ht;
+            lim0 = hw; lim1 = hh;
+        }
+        for (int side = 0; side < 2; side++) {
+            if (pass > 0 && side == 1 && nh >= 2) break;
+            float uu = side ? u0 + u1 : u0 - u1;
+            float vv = side ? v0 + v1 : v0 - v1;
+            if (orc_absf(uu) <= lim0 && orc_absf(vv) <= lim1) {
+                if (fam == 0)      { hx[nh] = side ? hw : -hw; hy[nh] = uu; hz[nh] = vv; }
+                else if (fam == 1) { hx[nh] = uu; hy[nh] = side ? hh : -hh; hz[nh] = vv; }
+                else               { hx[nh] = uu; hy[nh] = vv; hz[nh] = side ? ht : -ht; }
+                nh++;
+            }
+        }
+    }
+    if (nh != 2) return 0.0f;
+    float ex = hx[1] - hx[0], ey = hy[1] - hy[0], ez = hz[1] - hz[0];
+    return (float)sqrt(ex * ex + ey * ey + ez * ez);
+}
+
+/*
+ * Fan-beam backprojection for image rows [iy0, iy1).
+ * Restates Atx_fan_mf_cpu_new (Atx_fan_mf_cpu_new.cpp:21-63).
+ */
+void orc_fan_adj_f32(float *x, const float *Y, float SO, float OD, float scale, int nx,
+                     int ny, int nd, float dy_det, float y_os, int nt, const int *id_Y,
+                     const int *Nv, int tmp_size, const float *cos_phi,
+                     const float *sin_phi, const float *cos_det, const float *sin_det,
+                     int iy0, int iy1)
+{
+    int nd2 = nd / 2, nx2 = nx / 2, ny2 = ny / 2;
+    float SD = SO + OD;
+    long n = (long)nx * ny;
+    for (int iy = iy0; iy < iy1; iy++) {
+        float yc = (float)(iy + 0.5 - ny2);
+        for (int ix = 0; ix < nx; ix++) {
+            float xc = (float)(ix + 0.5 - nx2);
+            for (int it = 0; it < nt; it++) {
+                float acc = 0.0f;
+                for (int j = 0; j < Nv[it]; j++) {
+                    int iv = id_Y[it * tmp_size + j];
+                    const float *yv = Y + (long)iv * nd;
+                    float c = cos_phi[iv], s = sin_phi[iv];
+                    float xr = c * xc + s * yc;
+                    float yr = -s * xc + c * yc;
+                    float g = SD / ((xr + SO) * dy_det);
+                    int hi = (int)floor((yr + 1) * g - y_os + nd2);
+                    int lo = (int)floor((yr - 1) * g - y_os + nd2);
+                    if (lo < 0) lo = 0;
+                    if (hi > nd - 1) hi = nd - 1;
+                    for (int id = lo; id <= hi; id++) {
+                        float Px = -(sin_det[id] * c + cos_det[id] * s);
+                        float Py = cos_det[id] * c - sin_det[id] * s;
+                        float Pd = SO * sin_det[id];
+                        float l = orc_chord_unit_pixel(Px, Py, Pd, xc, yc);
+                        if (l > 0) acc += l * yv[id];
+                    }
+                }
+                x[it * n + (long)iy * nx + ix] = acc * scale;
+            }
+        }
+    }
+}
+
+/*
+ * Cone-beam backprojection for volume slices [iz0, iz1).
+ * Restates Atx_cone_mf_cpu_new (Atx_cone_mf_cpu_new.cpp:23-85), including its
+ * unit-cube chord (it passes voxel size 1,1,1 whatever dz is) and its
+ * z window half-width sqrt(1 + dz^2/2).
+ */
+void orc_cone_adj_f32(float *x, const float *Y, float SO, float OD, float scale, int nx,
+                      int ny, int nz, const float *sd_z, const float *y_det,
+                      const float *z_det, float dy_det, float y_os, float dz_det, float dz,
+                      int nt, const int *id_Y, const int *Nv, int tmp_size,
+                      const float *cos_phi, const float *sin_phi, int na, int nb, int iz0,
+                      int iz1)
+{
+    float SD = SO + OD;
+    int na2 = na / 2, nb2 = nb / 2, nx2 = nx / 2, ny2 = ny / 2, nz2 = nz / 2;
+    long n = (long)nx * ny * nz, nd = (long)na * nb;
+    float d = (float)sqrt(1 + dz * dz / 2);
+    for (int iz = iz0; iz < iz1; iz++) {
+        float zc = (float)(iz + 0.5 - nz2) * dz;
+        for (int iy = 0; iy < ny; iy++) {
+            float yc = (float)(iy + 0.5 - ny2);
+            for (int ix = 0; ix < nx; ix++) {
+                float xc = (float)(ix + 0.5 - nx2);
+                long idx = ((long)iz * ny + iy) * nx + ix;
+                for (int it = 0; it < nt; it++) {
+                    float acc = 0.0f;
+                    for (int j = 0; j < Nv[it]; j++) {
+                        int iv = id_Y[it * tmp_size + j];
+                        const float *yv = Y + (long)iv * nd;
+                        float c = cos_phi[iv], s = sin_phi[iv];
+                        float xr = c * xc + s * yc;
+                        float yr = -s * xc + c * yc;
+                        float g = SD / ((xr + SO) * dy_det);
+                        int amax = (int)floor((yr + 1) * g - y_os + na2);
+                        int amin = (int)floor((yr - 1) * g - y_os + na2);
+                        g = SD / ((xr + SO) * dz_det);
+                        int bmax = (int)floor((zc + d) * g + nb2);
+                        int bmin = (int)floor((zc - d) * g + nb2);
+                        if (amin < 0) amin = 0;
+                        if (amax > na - 1) amax = na - 1;
+                        if (bmin < 0) bmin = 0;
+                        if (bmax > nb - 1) bmax = nb - 1;
+                        for (int ib = bmin; ib <= bmax; ib++) {
+                            for (int ia = amin; ia <= amax; ia++) {
+                                float x1 = c * (-SO), y1 = s * (-SO), z1 = sd_z[iv];
+                                float x2 = c * OD - s * y_det[ia];
+                                float y2 = s * OD + c * y_det[ia];
+                                float z2 = z_det[ib] + sd_z[iv];
+                                float l = orc_chord_box(x1, y1, z1, x2, y2, z2, 1.0f, 1.0f,
+                                                        1.0f, xc, yc, zc);
+                                acc += l * yv[(long)ib * na + ia];
+                            }
+                        }
+                    }
+                    x[it * n + idx] = acc * scale;
+                }
+            }
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------- */
+/* (2) Exact (FP64) Siddon model                                              */
+/* ------------------------------------------------------------------------- */
+
+/*
+ * Geometry of one ray in FP64 from the FP32 parameters: source S, detector D.
+ * The detector column positions y_det are points on the flat panel
+ * (Ax_cone_mf_cpu_siddon.cpp:38-45); an equiangular detector is described by
+ * the flat-panel points SD*tan(gamma) of its bins, which define the same rays.
+ */
+typedef struct {
+    int nx, ny, nz;
+    double dz;          /* z voxel pitch in xy units */
+} orc_grid;
+
+/*
+ * Calls visit(ctx, voxel_index, length_in_voxel_units) for every voxel the
+ * segment S->D crosses with positive length, in order along the ray.
+ * Planes: x = k - nx/2 (k = 0..nx), y likewise, z = (k - nz/2)*dz.
+ * Returns the number of voxels visited.
+ */
+typedef void (*orc_visit_fn)(void *ctx, long vox, double len);
+
+static long orc_exact_walk(const orc_grid *g, const double S[3], const double D[3],
+                           orc_visit_fn visit, void *ctx)
+{
+    int n[3] = {g->nx, g->ny, g->nz};
+    double pitch[3] = {1.0, 1.0, g->dz};
+    double lo[3], d[3], amin = 0.0, amax = 1.0;
+    for (int a = 0; a < 3; a++) {
+        lo[a] = -(n[a] / 2) * pitch[a];
+        d[a] = D[a] - S[a];
+        double hi = lo[a] + n[a] * pitch[a];
+        if (d[a] == 0.0) {
+            if (S[a] < lo[a] || S[a] >= hi) return 0;
+        } else {
+            double t0 = (lo[a] - S[a]) / d[a], t1 = (hi - S[a]) / d[a];
+            if (t0 > t1) { double tt = t0; t0 = t1; t1 = tt; }
+            if (t0 > amin) amin = t0;
+            if (t1 < amax) amax = t1;
+        }
+    }
+    if (!(amin < amax)) return 0;
+    double len = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    /* voxel containing the midpoint of the first step; then step plane by plane */
+    int idx[3], step[3];
+    double next[3];
+    double am = amin;
+    for (int a = 0; a < 3; a++) {
+        double p = S[a] + (am + 1e-12 * (amax - amin)) * d[a];
+        int k = (int)floor((p - lo[a]) / pitch[a]);
+        if (k < 0) k = 0;
+        if (k >= n[a]) k = n[a] - 1;
+        idx[a] = k;
+        if (d[a] > 0) {
+            step[a] = 1; next[a] = (lo[a] + (k + 1) * pitch[a] - S[a]) / d[a];
+        } else if (d[a] < 0) {
+            step[a] = -1; next[a] = (lo[a] + k * pitch[a] - S[a]) / d[a];
+        } else {
+            step[a] = 0; next[a] = INFINITY;
+        }
+    }
+    long count = 0;
+    double acur = amin;
+    while (acur < amax) {
+        int a = 0;
+        if (next[1] < next[a]) a = 1;
+        if (next[2] < next[a]) a = 2;
+        double anext = next[a] < amax ? next[a] : amax;
+        double seg = (anext - acur) * len;
+        if (seg > 0) {
+            long vox = ((long)idx[2] * g->ny + idx[1]) * g->nx + idx[0];
+            if (visit) visit(ctx, vox, seg);
+            count++;
+        }
+        acur = anext;
+        if (acur >= amax) break;
+        idx[a] += step[a];
+        if (idx[a] < 0 || idx[a] >= n[a]) break;
+        /* next crossing recomputed from the plane index (no drift) */
+        int k1 = idx[a] + (step[a] > 0 ? 1 : 0);
+        next[a] = (lo[a] + k1 * pitch[a] - S[a]) / d[a];
+    }
+    return count;
+}
+
+typedef struct { const double *x; double acc; } orc_fwd_ctx;
+static void orc_fwd_visit(void *c, long vox, double len)
+{
+    orc_fwd_ctx *f = (orc_fwd_ctx *)c;
+    f->acc += len * f->x[vox];
+}
+
+typedef struct { double *x; double w; } orc_adj_ctx;
+static void orc_adj_visit(void *c, long vox, double len)
+{
+    orc_adj_ctx *f = (orc_adj_ctx *)c;
+    f->x[vox] += len * f->w;
+}
+
+static void orc_ray_points(double SO, double OD, double phi, double sz, double ydet,
+                           double zdet, double S[3], double D[3])
+{
+    double c = cos(phi), s = sin(phi);
+    S[0] = -SO * c; S[1] = -SO * s; S[2] = sz;
+    D[0] = OD * c - ydet * s; D[1] = OD * s + ydet * c; D[2] = zdet + sz;
+}
+
+/*
+ * Exact cone (nz >= 1; a fan is nz = 1, nb = 1, z_det = {0}, dz = 1) forward
+ * projection of views [v0, v1): y = scale * sum(len * x).
+ */
+void orc_exact_forward_f64(const double *X, double *y, double SO, double OD, double scale,
+                           int nx, int ny, int nz, double dz, int v0, int v1,
+                           const float *sd_phi, const float *sd_z, int na, int nb,
+                           const float *y_det, const float *z_det)
+{
+    orc_grid g = {nx, ny, nz, dz};
+    long nd = (long)na * nb;
+    for (int iv = v0; iv < v1; iv++) {
+        double sz = sd_z ? (double)sd_z[iv] : 0.0;
+        for (int ib = 0; ib < nb; ib++) {
+            for (int ia = 0; ia < na; ia++) {
+                double S[3], D[3];
+                orc_ray_points(SO, OD, (double)sd_phi[iv], sz, (double)y_det[ia],
+                               z_det ? (double)z_det[ib] : 0.0, S, D);
+                orc_fwd_ctx f = {X, 0.0};
+                orc_exact_walk(&g, S, D, orc_fwd_visit, &f);
+                y[(long)iv * nd + (long)ib * na + ia] = scale * f.acc;
+            }
+        }
+    }
+}
+
+/* Exact transpose: X += scale * sum over rays of views [v0, v1) (len * y). */
+void orc_exact_adjoint_f64(double *X, const double *y, double SO, double OD, double scale,
+                           int nx, int ny, int nz, double dz, int v0, int v1,
+                           const float *sd_phi, const float *sd_z, int na, int nb,
+                           const float *y_det, const float *z_det)
+{
+    orc_grid g = {nx, ny, nz, dz};
+    long nd = (long)na * nb;
+    for (int iv = v0; iv < v1; iv++) {
+        double sz = sd_z ? (double)sd_z[iv] : 0.0;
+        for (int ib = 0; ib < nb; ib++) {
+            for (int ia = 0; ia < na; ia++) {
+                double S[3], D[3];
+                orc_ray_points(SO, OD, (double)sd_phi[iv], sz, (double)y_det[ia],
+                               z_det ? (double)z_det[ib] : 0.0, S, D);
+                orc_adj_ctx f = {X, scale * y[(long)iv * nd + (long)ib * na + ia]};
+                orc_exact_walk(&g, S, D, orc_adj_visit, &f);
+            }
+        }
+    }
+}
+
+/* Number of voxels crossed with positive length, per ray of views [v0, v1). */
+void orc_exact_count(int64_t *cnt, double SO, double OD, int nx, int ny, int nz, double dz,
+                     int v0, int v1, const float *sd_phi, const float *sd_z, int na, int nb,
+                     const float *y_det, const float *z_det)
+{
+    orc_grid g = {nx, ny, nz, dz};
+    long nd = (long)na * nb;
+    for (int iv = v0; iv < v1; iv++) {
+        double sz = sd_z ? (double)sd_z[iv] : 0.0;
+        for (int ib = 0; ib < nb; ib++) {
+            for (int ia = 0; ia < na; ia++) {
+                double S[3], D[3];
+                orc_ray_points(SO, OD, (double)sd_phi[iv], sz, (double)y_det[ia],
+                               z_det ? (double)z_det[ib] : 0.0, S, D);
+                cnt[(long)(iv - v0) * nd + (long)ib * na + ia] =
+                    orc_exact_walk(&g, S, D, NULL, NULL);
+            }
+        }
+    }
+}

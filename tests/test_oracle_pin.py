@@ -1,0 +1,82 @@
+"""Pins the oracle restatement against the reference's own CPU kernels.
+
+The reference sources (compiled unmodified into oracle/_ref) are only present
+where the reference checkout exists; elsewhere the committed fixtures in
+tests/golden/ (generated from oracle/_ref by tests/golden/make_golden.py) pin
+the restatement instead.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+from framelab_gb300 import geometry as G
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+need_ref = pytest.mark.skipif(not O.have_ref(), reason="reference sources not built here")
+
+
+def _rand_fan(rng, n, nd, nv):
+    return G.fan_para(n, n, nd, nv, L=(2, 2), SO=rng.uniform(2, 6), OD=rng.uniform(2, 6),
+                      Ly=rng.uniform(3, 8))
+
+
+def _rand_cone(rng, n, na, nb, nv, scan="circle"):
+    kw = {}
+    if scan != "circle":
+        kw = dict(scan=scan, zmax=0.5, rps=1.0, vtab=1.0, fps=max(nv, 4))
+    return G.cone_para(n, n, n, na, nb, nv, L=(2, 2, 2), SO=rng.uniform(3, 6),
+                       OD=rng.uniform(3, 6), Ly=rng.uniform(3, 8), Lz=rng.uniform(3, 8), **kw)
+
+
+@need_ref
+@pytest.mark.parametrize("seed", range(8))
+def test_fan_restatement_is_bit_exact(seed):
+    rng = np.random.default_rng(seed)
+    n = [8, 16, 32, 64][seed % 4]
+    p = _rand_fan(rng, n, [12, 24, 50, 33][seed % 4], [5, 7, 16][seed % 3])
+    X = rng.standard_normal(n * n).astype(np.float32)
+    assert np.array_equal(O.fan_siddon_f32(X, p), O.ref_fan_siddon(X, p))
+    Y = rng.standard_normal(len(p["y_det"]) * len(p["sd_phi"])).astype(np.float32)
+    assert np.array_equal(O.fan_adj_f32(Y, p), O.ref_fan_adj(Y, p))
+
+
+@need_ref
+@pytest.mark.parametrize("seed", range(6))
+def test_cone_restatement_is_bit_exact(seed):
+    rng = np.random.default_rng(100 + seed)
+    n = [8, 16, 24][seed % 3]
+    scan = "helix" if seed % 2 else "circle"
+    p = _rand_cone(rng, n, [12, 20][seed % 2], [10, 14][seed % 2], [3, 5, 9][seed % 3], scan)
+    X = rng.standard_normal(n ** 3).astype(np.float32)
+    assert np.array_equal(O.cone_siddon_f32(X, p), O.ref_cone_siddon(X, p))
+    Y = rng.standard_normal(len(p["y_det"]) * len(p["z_det"]) * len(p["sd_phi"])).astype(np.float32)
+    assert np.array_equal(O.cone_adj_f32(Y, p), O.ref_cone_adj(Y, p))
+
+
+def _golden_cases():
+    return sorted(glob.glob(os.path.join(GOLDEN, "*.npz")))
+
+
+def test_golden_fixtures_exist():
+    assert len(_golden_cases()) >= 4
+
+
+@pytest.mark.parametrize("path", _golden_cases(), ids=os.path.basename)
+def test_restatement_matches_golden(path):
+    from tests.golden.fixtures import load_case
+    case = load_case(path)
+    p, kind = case["para"], case["kind"]
+    if kind == "fan_siddon":
+        out = O.fan_siddon_f32(case["x"], p)
+    elif kind == "fan_adj":
+        out = O.fan_adj_f32(case["x"], p)
+    elif kind == "cone_siddon":
+        out = O.cone_siddon_f32(case["x"], p)
+    elif kind == "cone_adj":
+        out = O.cone_adj_f32(case["x"], p)
+    else:
+        pytest.skip(f"no restatement yet for {kind}")
+    assert np.array_equal(out, case["y"]), kind
