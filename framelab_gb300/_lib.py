@@ -1,0 +1,105 @@
+"""ctypes binding of libframelab_gb300.so (the C ABI in include/framelab_gb300.h).
+
+The library is the only compute path: if it cannot be loaded, every operator
+raises. There is no CPU or PyTorch fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+from . import build as _build
+
+_lock = threading.Lock()
+_lib = None
+
+FL_OK, FL_ERR_INVALID, FL_ERR_UNSUPPORTED, FL_ERR_CUDA, FL_ERR_ALLOC, FL_ERR_TIMEOUT = range(6)
+MODEL_SIDDON_REF, MODEL_CHORD_REF, MODEL_MATCHED = 0, 1, 16
+F32, F16, BF16 = 0, 1, 2
+
+
+class FLError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"framelab_gb300 error {code}: {msg}")
+        self.code = code
+
+
+class Scan(C.Structure):
+    _fields_ = [
+        ("ndim", C.c_int32), ("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32),
+        ("nt", C.c_int32), ("nv", C.c_int32), ("na", C.c_int32), ("nb", C.c_int32),
+        ("SO", C.c_float), ("OD", C.c_float), ("scale", C.c_float), ("dz", C.c_float),
+        ("dy_det", C.c_float), ("dz_det", C.c_float), ("y_os", C.c_float),
+        ("sd_phi", C.c_void_p), ("sd_z", C.c_void_p), ("y_det", C.c_void_p),
+        ("z_det", C.c_void_p), ("cos_phi", C.c_void_p), ("sin_phi", C.c_void_p),
+        ("cos_det", C.c_void_p), ("sin_det", C.c_void_p), ("view_frame", C.c_void_p),
+        ("id_Y", C.c_void_p), ("Nv", C.c_void_p), ("tmp_size", C.c_int32),
+    ]
+
+
+_V, _I, _I64, _F, _D = C.c_void_p, C.c_int, C.c_int64, C.c_float, C.c_double
+_P = C.c_void_p
+
+# name -> (restype, argtypes)
+_SIGS = {
+    "fl_last_status": (_I, []),
+    "fl_last_error": (C.c_char_p, []),
+    "fl_version": (C.c_char_p, []),
+    "fl_plan_create": (_I, [C.POINTER(Scan), C.POINTER(_P)]),
+    "fl_plan_destroy": (None, [_P]),
+    "fl_plan_sizes": (_I, [_P, C.POINTER(_I64), C.POINTER(_I64)]),
+    "fl_forward": (_I, [_P, _I, _V, _I, _V, _I, _V]),
+    "fl_adjoint": (_I, [_P, _I, _V, _I, _V, _I, _V]),
+    "fl_count_intersections": (_I, [_P, _V, _V]),
+    "Ax_fan_mf_gpu_siddon": (None, [_V, _V, _F, _F, _F, _I, _I, _I, _V, _I, _V, _V, _I]),
+    "Atx_fan_mf_gpu_new": (None, [_V, _V, _F, _F, _F, _I, _I, _V, _I, _V, _F, _F, _I, _V, _V,
+                                  _I, _I, _V, _V, _V, _V]),
+    "Ax_cone_mf_gpu_siddon": (None, [_V, _V, _V, _V, _V, _V, _V, _V, _F, _F, _F, _F, _I, _I,
+                                     _I, _I, _I, _I, _I, _I, _I]),
+    "Atx_cone_mf_gpu_new": (None, [_V, _V, _V, _V, _V, _V, _V, _V, _V, _F, _F, _F, _F, _F, _F,
+                                   _F, _I, _I, _I, _I, _I, _I, _I, _I, _I]),
+}
+
+
+def lib_path() -> str:
+    return _build.OUT
+
+
+def load(build_if_missing: bool = True):
+    """Load the library (building it in-tree first when it is absent)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            path = _build.OUT
+            if build_if_missing:
+                path = _build.build()
+            if not os.path.exists(path):
+                raise FLError(FL_ERR_CUDA, f"{path} not built; run framelab_gb300.build.build()")
+            lib = C.CDLL(path)
+            for name, (res, args) in _SIGS.items():
+                fn = getattr(lib, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = lib
+        return _lib
+
+
+def declare(name, restype, argtypes):
+    """Register the signature of an additional exported symbol."""
+    _SIGS[name] = (restype, argtypes)
+    if _lib is not None:
+        fn = getattr(_lib, name)
+        fn.restype = restype
+        fn.argtypes = argtypes
+
+
+def check(status: int):
+    if status != FL_OK:
+        L = load()
+        raise FLError(status, L.fl_last_error().decode())
+
+
+def check_last():
+    L = load()
+    check(L.fl_last_status())

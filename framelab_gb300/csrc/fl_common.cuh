@@ -1,0 +1,59 @@
+// fl_common.cuh -- shared helpers for the FrameLab-GB300 kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include "framelab_gb300.h"
+
+// ---------------------------------------------------------------------------
+// Pinned single-precision arithmetic.
+//
+// nvcc contracts a*b+c into one FMA by default; the reference's CPU kernels
+// round every product and sum separately (x86-64 build, no FMA). Kernels
+// that must reproduce the reference bit for bit use these explicit
+// round-to-nearest intrinsics, which the compiler never fuses or reorders.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ float fsqrt(float a) { return __fsqrt_rn(a); }
+// |a| exactly as `a>0?a:-(a)` (equal to fabsf for every non-NaN input)
+__device__ __forceinline__ float fabs_ref(float a) { return fabsf(a); }
+
+// ---------------------------------------------------------------------------
+// Storage types. Volumes and sinograms may be stored as f32, f16 or bf16;
+// arithmetic is always f32.
+// ---------------------------------------------------------------------------
+template <typename T> struct Store;
+template <> struct Store<float> {
+    static __device__ __forceinline__ float ld(const float* p) { return __ldg(p); }
+    static __device__ __forceinline__ float ld_plain(const float* p) { return *p; }
+    static __device__ __forceinline__ void st(float* p, float v) { *p = v; }
+};
+template <> struct Store<__half> {
+    static __device__ __forceinline__ float ld(const __half* p) { return __half2float(__ldg(p)); }
+    static __device__ __forceinline__ float ld_plain(const __half* p) { return __half2float(*p); }
+    static __device__ __forceinline__ void st(__half* p, float v) { *p = __float2half_rn(v); }
+};
+template <> struct Store<__nv_bfloat16> {
+    static __device__ __forceinline__ float ld(const __nv_bfloat16* p) { return __bfloat162float(__ldg(p)); }
+    static __device__ __forceinline__ float ld_plain(const __nv_bfloat16* p) { return __bfloat162float(*p); }
+    static __device__ __forceinline__ void st(__nv_bfloat16* p, float v) { *p = __float2bfloat16_rn(v); }
+};
+
+// ---------------------------------------------------------------------------
+// Host-side status handling (fl_runtime.cpp).
+// ---------------------------------------------------------------------------
+int fl_set_error(int code, const char* fmt, ...);
+int fl_check_cuda(cudaError_t e, const char* what);
+int fl_check_launch(const char* what);
+#define FL_CUDA(call)                                                     \
+    do {                                                                  \
+        int _st = fl_check_cuda((call), #call);                           \
+        if (_st != FL_OK) return _st;                                     \
+    } while (0)
+
+static inline unsigned fl_div_up(long long a, long long b) { return (unsigned)((a + b - 1) / b); }

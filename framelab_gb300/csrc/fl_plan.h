@@ -1,0 +1,57 @@
+// fl_plan.h -- internal layout of an fl_plan (geometry uploaded to HBM).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "framelab_gb300.h"
+
+// Per-ray parameters of the matched Siddon model. A ray's plane crossings are
+// A_a(k) = fmaf(k, inv_a, off_a) for plane index k on axis a (x, y: planes at
+// k - n/2; z: planes at (k - nz/2)*dz), an affine re-parameterisation
+// A = alpha - alpha_c(view) of the source->detector parameter alpha, centred
+// near the isocentre for precision. The forward walk and the adjoint gather
+// read the same FP32 table entries, so both see identical crossings.
+struct ColEntry {   // per (view, detector column): x and y axes
+    float inv_x, off_x, inv_y, off_y;
+};
+struct RowEntry {   // per (view, detector row): z axis (cone only)
+    float inv_z, off_z, rinv_z, dz2;   // dz2 = fl(d_z^2)
+};
+struct ViewEntry {  // per view, for the adjoint's detector windows
+    float c, s;       // cos/sin of the source angle
+    float sz;         // source z
+    float ac;         // alpha_c: A = alpha - ac
+};
+
+struct fl_plan {
+    fl_scan s;                 // scalar fields; array pointers below are device copies
+    int tmp_size;
+    int64_t n_vox_frame, n_vox, n_rays;
+    // reference geometry (device)
+    float *d_sd_phi, *d_sd_z, *d_y_det, *d_z_det;
+    float *d_cos_phi, *d_sin_phi, *d_cos_det, *d_sin_det;
+    float *d_cphi_f, *d_sphi_f;    // cosf/sinf(sd_phi): the reference Siddon's own trig
+    int32_t *d_view_frame, *d_idY, *d_Nv;
+    // matched-model tables (device)
+    ColEntry *d_col;           // [nv*na]
+    float *d_colr;             // [nv*na] fl(d_x^2 + d_y^2)
+    RowEntry *d_row;           // [nv*nb]
+    ViewEntry *d_view;         // [nv]
+    // detector grid for the adjoint windows (matched model)
+    int det_kind;              // 0 flat uniform, 1 equiangular (fan), -1 irregular
+    float u0, du, g0, dg;      // flat: u = u0 + ia*du ; arc: gamma = g0 + ia*dg
+    float v0, dv;              // rows: v = v0 + ib*dv
+    float SD;
+    // reusable scratch (sinogram-sized f32 for the pre-weighted adjoint input)
+    float *d_work;
+    size_t work_elems;
+};
+
+// internal launchers
+int fl_ref_forward(fl_plan* p, const float* x, float* y, cudaStream_t st);
+int fl_ref_adjoint(fl_plan* p, const float* y, float* x, cudaStream_t st);
+int fl_matched_forward(fl_plan* p, const void* x, int xt, void* y, int yt, int cr_power,
+                       cudaStream_t st);
+int fl_matched_weight(fl_plan* p, const void* y, int yt, float* yw, cudaStream_t st);
+int fl_matched_adjoint_w(fl_plan* p, const float* yw, void* x, int xt, cudaStream_t st);
+int fl_matched_count(fl_plan* p, int32_t* counts, cudaStream_t st);

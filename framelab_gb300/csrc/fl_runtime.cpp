@@ -1,0 +1,501 @@
+// fl_runtime.cpp -- host runtime: status, plans (geometry -> HBM tables),
+// projector dispatch and the reference-signature drop-ins.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "fl_plan.h"
+#include "framelab_gb300.h"
+
+// ---------------------------------------------------------------------------
+// Status (per host thread)
+// ---------------------------------------------------------------------------
+static thread_local int g_status = FL_OK;
+static thread_local char g_msg[512] = "";
+
+int fl_set_error(int code, const char* fmt, ...)
+{
+    g_status = code;
+    if (code == FL_OK) { g_msg[0] = 0; return FL_OK; }
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_msg, sizeof g_msg, fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+int fl_check_cuda(cudaError_t e, const char* what)
+{
+    if (e == cudaSuccess) return FL_OK;
+    cudaGetLastError();   // clear a non-sticky error so the next call starts clean
+    return fl_set_error(e == cudaErrorMemoryAllocation ? FL_ERR_ALLOC : FL_ERR_CUDA,
+                        "%s: %s", what, cudaGetErrorString(e));
+}
+
+int fl_check_launch(const char* what) { return fl_check_cuda(cudaGetLastError(), what); }
+
+extern "C" int fl_last_status(void) { return g_status; }
+extern "C" const char* fl_last_error(void) { return g_msg; }
+extern "C" const char* fl_version(void) { return "framelab_gb300 1.0 (sm_103a)"; }
+
+// ---------------------------------------------------------------------------
+// Plans
+// ---------------------------------------------------------------------------
+template <typename T>
+static int upload(T** dst, const T* src, size_t n)
+{
+    *dst = nullptr;
+    if (n == 0) return FL_OK;
+    int st = fl_check_cuda(cudaMalloc((void**)dst, n * sizeof(T)), "cudaMalloc(plan)");
+    if (st) return st;
+    return fl_check_cuda(cudaMemcpy(*dst, src, n * sizeof(T), cudaMemcpyHostToDevice),
+                         "cudaMemcpy(plan)");
+}
+
+static void free_plan_arrays(fl_plan* p)
+{
+    void* ptrs[] = {p->d_sd_phi, p->d_sd_z,   p->d_y_det,      p->d_z_det, p->d_cos_phi,
+                    p->d_sin_phi, p->d_cos_det, p->d_sin_det,   p->d_cphi_f, p->d_sphi_f,
+                    p->d_view_frame, p->d_idY, p->d_Nv,        p->d_col,   p->d_colr,
+                    p->d_row,    p->d_view,   p->d_work};
+    for (void* q : ptrs)
+        if (q) cudaFree(q);
+}
+
+// Nudge a direction component away from zero so 1/d stays finite; the ray
+// moves by at most 1e-9 of its length, identically for forward and adjoint.
+static double nudge(double d, double len)
+{
+    double eps = 1e-9 * len;
+    if (std::fabs(d) < eps) return d < 0 ? -eps : eps;
+    return d;
+}
+
+static int build_tables(fl_plan* p, const std::vector<float>& phi, const float* sd_z,
+                        const float* y_det, const float* z_det)
+{
+    const fl_scan& s = p->s;
+    const double SO = s.SO, OD = s.OD, SD = SO + OD;
+    const double ac = SO / SD;   // alpha at the isocentre plane: A = alpha - ac
+    const int nx2 = s.nx / 2, ny2 = s.ny / 2, nz2 = s.nz / 2;
+    std::vector<ColEntry> col((size_t)s.nv * s.na);
+    std::vector<float> colr((size_t)s.nv * s.na);
+    std::vector<RowEntry> row((size_t)s.nv * s.nb);
+    std::vector<ViewEntry> view(s.nv);
+    for (int iv = 0; iv < s.nv; iv++) {
+        double c = std::cos((double)phi[iv]), sn = std::sin((double)phi[iv]);
+        double Sx = -SO * c, Sy = -SO * sn, Sz = sd_z ? (double)sd_z[iv] : 0.0;
+        view[iv] = ViewEntry{(float)c, (float)sn, (float)Sz, (float)ac};
+        for (int ia = 0; ia < s.na; ia++) {
+            double u = y_det[ia];
+            double dx = (OD * c - u * sn) - Sx, dy = (OD * sn + u * c) - Sy;
+            double len = std::sqrt(dx * dx + dy * dy);
+            dx = nudge(dx, len); dy = nudge(dy, len);
+            ColEntry e;
+            e.inv_x = (float)(1.0 / dx);
+            e.off_x = (float)((-nx2 - Sx) / dx - ac);
+            e.inv_y = (float)(1.0 / dy);
+            e.off_y = (float)((-ny2 - Sy) / dy - ac);
+            col[(size_t)iv * s.na + ia] = e;
+            colr[(size_t)iv * s.na + ia] = (float)(dx * dx + dy * dy);
+        }
+        for (int ib = 0; ib < s.nb; ib++) {
+            RowEntry r{0.0f, 0.0f, 0.0f, 0.0f};
+            if (s.ndim == 3) {
+                double dzr = nudge((double)z_det[ib], SD);   // detector z - source z
+                double pitch = s.dz;
+                r.inv_z = (float)(pitch / dzr);
+                r.off_z = (float)((-nz2 * pitch - Sz) / dzr - ac);
+                r.rinv_z = (float)(dzr / pitch);
+                r.dz2 = (float)(dzr * dzr);
+            }
+            row[(size_t)iv * s.nb + ib] = r;
+        }
+    }
+    int st;
+    if ((st = upload(&p->d_col, col.data(), col.size()))) return st;
+    if ((st = upload(&p->d_colr, colr.data(), colr.size()))) return st;
+    if ((st = upload(&p->d_row, row.data(), row.size()))) return st;
+    if ((st = upload(&p->d_view, view.data(), view.size()))) return st;
+
+    // detector grids for the adjoint windows
+    p->SD = (float)SD;
+    p->det_kind = -1;
+    if (s.na == 1) {
+        p->det_kind = 0; p->u0 = y_det[0]; p->du = 1.0f;
+    } else {
+        double u0 = y_det[0], du = ((double)y_det[s.na - 1] - u0) / (s.na - 1);
+        double g0 = std::atan2((double)y_det[0], SD);
+        double dg = (std::atan2((double)y_det[s.na - 1], SD) - g0) / (s.na - 1);
+        double eflat = 0, earc = 0;
+        for (int ia = 0; ia < s.na; ia++) {
+            eflat = std::fmax(eflat, std::fabs(y_det[ia] - (u0 + ia * du)));
+            earc = std::fmax(earc, std::fabs(std::atan2((double)y_det[ia], SD) - (g0 + ia * dg)));
+        }
+        if (du != 0 && eflat <= 0.05 * std::fabs(du)) {
+            p->det_kind = 0; p->u0 = (float)u0; p->du = (float)du;
+        } else if (dg != 0 && earc <= 0.05 * std::fabs(dg)) {
+            p->det_kind = 1; p->g0 = (float)g0; p->dg = (float)dg;
+        }
+    }
+    p->v0 = 0.0f; p->dv = 1.0f;
+    if (s.ndim == 3) {
+        p->v0 = z_det[0];
+        if (s.nb > 1) {
+            double dv = ((double)z_det[s.nb - 1] - z_det[0]) / (s.nb - 1);
+            double e = 0;
+            for (int ib = 0; ib < s.nb; ib++)
+                e = std::fmax(e, std::fabs(z_det[ib] - (z_det[0] + ib * dv)));
+            if (dv == 0 || e > 0.05 * std::fabs(dv)) p->det_kind = -2;   // irregular rows
+            else p->dv = (float)dv;
+        }
+    }
+    return FL_OK;
+}
+
+extern "C" int fl_plan_create(const fl_scan* scan, fl_plan** out)
+{
+    if (!scan || !out) return fl_set_error(FL_ERR_INVALID, "fl_plan_create: null argument");
+    *out = nullptr;
+    fl_scan s = *scan;
+    if (s.ndim != 2 && s.ndim != 3)
+        return fl_set_error(FL_ERR_INVALID, "ndim must be 2 (fan) or 3 (cone)");
+    if (s.ndim == 2) { s.nz = 1; s.nb = 1; s.dz = 1.0f; }
+    if (s.nt < 1) s.nt = 1;
+    if (s.nx < 1 || s.ny < 1 || s.nz < 1 || s.nv < 1 || s.na < 1 || s.nb < 1)
+        return fl_set_error(FL_ERR_INVALID, "sizes must be positive");
+    if (!(s.SO > 0) || !(s.OD > -s.SO) || !(s.scale > 0) || !(s.dz > 0))
+        return fl_set_error(FL_ERR_INVALID, "SO, SO+OD, scale and dz must be positive");
+    if ((!s.sd_phi && !(s.cos_phi && s.sin_phi)) || !s.y_det || (s.ndim == 3 && !s.z_det))
+        return fl_set_error(FL_ERR_INVALID, "geometry arrays missing");
+
+    fl_plan* p = new (std::nothrow) fl_plan;
+    if (!p) return fl_set_error(FL_ERR_ALLOC, "fl_plan_create: out of host memory");
+    std::memset((void*)p, 0, sizeof *p);
+    p->s = s;
+    p->n_vox_frame = (int64_t)s.nx * s.ny * s.nz;
+    p->n_vox = p->n_vox_frame * s.nt;
+    p->n_rays = (int64_t)s.nv * s.na * s.nb;
+    const int nv = s.nv, na = s.na, nb = s.nb, nt = s.nt;
+
+    std::vector<float> phi(nv), cphi(nv), sphi(nv), cf(nv), sf(nv), sdz(nv, 0.0f);
+    for (int iv = 0; iv < nv; iv++) {
+        phi[iv] = s.sd_phi ? s.sd_phi[iv] : (float)std::atan2((double)s.sin_phi[iv], (double)s.cos_phi[iv]);
+        // the reference Siddon evaluates cos/sin of a float (C++ float overloads)
+        cf[iv] = std::cos(phi[iv]);
+        sf[iv] = std::sin(phi[iv]);
+        cphi[iv] = s.cos_phi ? s.cos_phi[iv] : (float)std::cos((double)phi[iv]);
+        sphi[iv] = s.sin_phi ? s.sin_phi[iv] : (float)std::sin((double)phi[iv]);
+        if (s.sd_z) sdz[iv] = s.sd_z[iv];
+    }
+    std::vector<float> cdet(na), sdet(na);
+    for (int ia = 0; ia < na; ia++) {
+        if (s.cos_det && s.sin_det) { cdet[ia] = s.cos_det[ia]; sdet[ia] = s.sin_det[ia]; }
+        else {
+            float ang = (float)std::atan2((double)s.y_det[ia], (double)(s.SO + s.OD));
+            cdet[ia] = (float)std::cos((double)ang);
+            sdet[ia] = (float)std::sin((double)ang);
+        }
+    }
+    std::vector<int32_t> vframe(nv, 0);
+    for (int iv = 0; iv < nv; iv++) {
+        vframe[iv] = s.view_frame ? s.view_frame[iv] : 0;
+        if (vframe[iv] < 0 || vframe[iv] >= nt) {
+            delete p;
+            return fl_set_error(FL_ERR_INVALID, "view %d reads frame %d (nt = %d)", iv, vframe[iv], nt);
+        }
+    }
+    std::vector<int32_t> idY, Nvv(nt, 0);
+    int tmp = 0;
+    if (s.id_Y && s.Nv) {
+        tmp = s.tmp_size;
+        for (int it = 0; it < nt; it++) {
+            Nvv[it] = s.Nv[it];
+            if (Nvv[it] < 0 || Nvv[it] > tmp) {
+                delete p;
+                return fl_set_error(FL_ERR_INVALID, "Nv[%d] = %d outside [0, tmp_size]", it, Nvv[it]);
+            }
+        }
+        idY.assign(s.id_Y, s.id_Y + (size_t)tmp * nt);
+        for (int it = 0; it < nt; it++)
+            for (int j = 0; j < Nvv[it]; j++) {
+                int iv = idY[(size_t)it * tmp + j];
+                if (iv < 0 || iv >= nv) {
+                    delete p;
+                    return fl_set_error(FL_ERR_INVALID, "id_Y entry %d out of range", iv);
+                }
+            }
+    } else {
+        for (int iv = 0; iv < nv; iv++) Nvv[vframe[iv]]++;
+        for (int it = 0; it < nt; it++) tmp = tmp > Nvv[it] ? tmp : Nvv[it];
+        idY.assign((size_t)tmp * nt, 0);
+        std::vector<int> fill(nt, 0);
+        for (int iv = 0; iv < nv; iv++) idY[(size_t)vframe[iv] * tmp + fill[vframe[iv]]++] = iv;
+    }
+    if (tmp < 1) tmp = 1, idY.resize((size_t)nt, 0);
+    p->tmp_size = tmp;
+
+    int st = FL_OK;
+    if (!st) st = upload(&p->d_sd_phi, phi.data(), nv);
+    if (!st) st = upload(&p->d_sd_z, sdz.data(), nv);
+    if (!st) st = upload(&p->d_y_det, s.y_det, na);
+    if (!st && s.ndim == 3) st = upload(&p->d_z_det, s.z_det, nb);
+    if (!st) st = upload(&p->d_cos_phi, cphi.data(), nv);
+    if (!st) st = upload(&p->d_sin_phi, sphi.data(), nv);
+    if (!st) st = upload(&p->d_cphi_f, cf.data(), nv);
+    if (!st) st = upload(&p->d_sphi_f, sf.data(), nv);
+    if (!st) st = upload(&p->d_cos_det, cdet.data(), na);
+    if (!st) st = upload(&p->d_sin_det, sdet.data(), na);
+    if (!st) st = upload(&p->d_view_frame, vframe.data(), nv);
+    if (!st) st = upload(&p->d_idY, idY.data(), idY.size());
+    if (!st) st = upload(&p->d_Nv, Nvv.data(), nt);
+    if (!st) st = build_tables(p, phi, s.sd_z ? sdz.data() : nullptr, s.y_det, s.z_det);
+    // host copies of the arrays are not kept: clear the caller's pointers
+    p->s.sd_phi = p->s.sd_z = p->s.y_det = p->s.z_det = nullptr;
+    p->s.cos_phi = p->s.sin_phi = p->s.cos_det = p->s.sin_det = nullptr;
+    p->s.view_frame = p->s.id_Y = p->s.Nv = nullptr;
+    if (st) {
+        free_plan_arrays(p);
+        delete p;
+        return st;
+    }
+    *out = p;
+    return fl_set_error(FL_OK, "");
+}
+
+extern "C" void fl_plan_destroy(fl_plan* p)
+{
+    if (!p) return;
+    free_plan_arrays(p);
+    delete p;
+}
+
+extern "C" int fl_plan_sizes(const fl_plan* p, int64_t* n_vox, int64_t* n_rays)
+{
+    if (!p) return fl_set_error(FL_ERR_INVALID, "null plan");
+    if (n_vox) *n_vox = p->n_vox;
+    if (n_rays) *n_rays = p->n_rays;
+    return FL_OK;
+}
+
+static int check_dtype(int t)
+{
+    if (t != FL_F32 && t != FL_F16 && t != FL_BF16)
+        return fl_set_error(FL_ERR_INVALID, "unknown dtype %d", t);
+    return FL_OK;
+}
+
+static int matched_ready(fl_plan* p)
+{
+    const fl_scan& s = p->s;
+    double r = std::sqrt(0.25 * s.nx * s.nx + 0.25 * s.ny * s.ny) + 1.0;
+    if (!(s.SO > r))
+        return fl_set_error(FL_ERR_UNSUPPORTED,
+                            "matched model needs the source outside the volume (SO > %.1f)", r);
+    return FL_OK;
+}
+
+extern "C" int fl_forward(fl_plan* p, int model, const void* x, int xt, void* y, int yt,
+                          void* stream)
+{
+    if (!p || !x || !y) return fl_set_error(FL_ERR_INVALID, "fl_forward: null argument");
+    int st;
+    if ((st = check_dtype(xt)) || (st = check_dtype(yt))) return st;
+    cudaStream_t sm = (cudaStream_t)stream;
+    if (model == FL_MODEL_SIDDON_REF) {
+        if (xt != FL_F32 || yt != FL_F32)
+            return fl_set_error(FL_ERR_UNSUPPORTED, "reference Siddon is FP32 only");
+        return fl_ref_forward(p, (const float*)x, (float*)y, sm);
+    }
+    if (model == FL_MODEL_MATCHED) {
+        if ((st = matched_ready(p))) return st;
+        return fl_matched_forward(p, x, xt, y, yt, 1, sm);
+    }
+    return fl_set_error(FL_ERR_UNSUPPORTED, "fl_forward: model %d not available", model);
+}
+
+// scratch for the pre-weighted adjoint input, owned by the plan
+static int plan_work(fl_plan* p, float** w)
+{
+    size_t need = (size_t)p->n_rays;
+    if (p->work_elems < need) {
+        if (p->d_work) cudaFree(p->d_work);
+        p->d_work = nullptr;
+        p->work_elems = 0;
+        int st = fl_check_cuda(cudaMalloc((void**)&p->d_work, need * sizeof(float)),
+                               "cudaMalloc(adjoint scratch)");
+        if (st) return st;
+        p->work_elems = need;
+    }
+    *w = p->d_work;
+    return FL_OK;
+}
+
+extern "C" int fl_adjoint(fl_plan* p, int model, const void* y, int yt, void* x, int xt,
+                          void* stream)
+{
+    if (!p || !x || !y) return fl_set_error(FL_ERR_INVALID, "fl_adjoint: null argument");
+    int st;
+    if ((st = check_dtype(xt)) || (st = check_dtype(yt))) return st;
+    cudaStream_t sm = (cudaStream_t)stream;
+    if (model == FL_MODEL_CHORD_REF) {
+        if (xt != FL_F32 || yt != FL_F32)
+            return fl_set_error(FL_ERR_UNSUPPORTED, "reference backprojector is FP32 only");
+        return fl_ref_adjoint(p, (const float*)y, (float*)x, sm);
+    }
+    if (model == FL_MODEL_MATCHED) {
+        if ((st = matched_ready(p))) return st;
+        if (p->det_kind < 0)
+            return fl_set_error(FL_ERR_UNSUPPORTED,
+                                "matched adjoint needs a uniform flat or equiangular detector");
+        if (p->det_kind == 1 && p->s.ndim == 3)
+            return fl_set_error(FL_ERR_UNSUPPORTED, "equiangular detector is fan-beam only");
+        float* w;
+        if ((st = plan_work(p, &w))) return st;
+        if ((st = fl_matched_weight(p, y, yt, w, sm))) return st;
+        return fl_matched_adjoint_w(p, w, x, xt, sm);
+    }
+    return fl_set_error(FL_ERR_UNSUPPORTED, "fl_adjoint: model %d not available", model);
+}
+
+extern "C" int fl_count_intersections(fl_plan* p, int32_t* counts, void* stream)
+{
+    if (!p || !counts) return fl_set_error(FL_ERR_INVALID, "null argument");
+    int st = matched_ready(p);
+    if (st) return st;
+    return fl_matched_count(p, counts, (cudaStream_t)stream);
+}
+
+// ---------------------------------------------------------------------------
+// Drop-ins: host pointers in/out, one synchronous call, like the reference.
+// ---------------------------------------------------------------------------
+namespace {
+struct DevBuf {
+    void* p = nullptr;
+    ~DevBuf() { if (p) cudaFree(p); }
+    int alloc(size_t bytes) { return fl_check_cuda(cudaMalloc(&p, bytes ? bytes : 4), "cudaMalloc"); }
+};
+struct PlanGuard {
+    fl_plan* p = nullptr;
+    ~PlanGuard() { fl_plan_destroy(p); }
+};
+
+// frames from (id_Y, Nv, tmp_size): view -> frame
+std::vector<int32_t> frames_of(const int* id_Y, const int* Nv, int nt, int tmp, int nv, int* bad)
+{
+    std::vector<int32_t> f(nv, 0);
+    *bad = 0;
+    for (int it = 0; it < nt; it++)
+        for (int j = 0; j < Nv[it]; j++) {
+            int iv = id_Y[(size_t)it * tmp + j];
+            if (iv < 0 || iv >= nv) { *bad = 1; continue; }
+            f[iv] = it;
+        }
+    return f;
+}
+
+int run_forward_host(const fl_scan& s, int model, const float* X, float* y)
+{
+    PlanGuard g;
+    int st = fl_plan_create(&s, &g.p);
+    if (st) return st;
+    DevBuf dx, dy;
+    size_t nvox = (size_t)g.p->n_vox, nray = (size_t)g.p->n_rays;
+    if ((st = dx.alloc(nvox * 4)) || (st = dy.alloc(nray * 4))) return st;
+    if ((st = fl_check_cuda(cudaMemcpy(dx.p, X, nvox * 4, cudaMemcpyHostToDevice), "H2D"))) return st;
+    if ((st = fl_forward(g.p, model, dx.p, FL_F32, dy.p, FL_F32, nullptr))) return st;
+    if ((st = fl_check_cuda(cudaMemcpy(y, dy.p, nray * 4, cudaMemcpyDeviceToHost), "D2H"))) return st;
+    return fl_set_error(FL_OK, "");
+}
+
+int run_adjoint_host(const fl_scan& s, int model, const float* Y, float* x)
+{
+    PlanGuard g;
+    int st = fl_plan_create(&s, &g.p);
+    if (st) return st;
+    DevBuf dx, dy;
+    size_t nvox = (size_t)g.p->n_vox, nray = (size_t)g.p->n_rays;
+    if ((st = dx.alloc(nvox * 4)) || (st = dy.alloc(nray * 4))) return st;
+    if ((st = fl_check_cuda(cudaMemcpy(dy.p, Y, nray * 4, cudaMemcpyHostToDevice), "H2D"))) return st;
+    if ((st = fl_adjoint(g.p, model, dy.p, FL_F32, dx.p, FL_F32, nullptr))) return st;
+    if ((st = fl_check_cuda(cudaMemcpy(x, dx.p, nvox * 4, cudaMemcpyDeviceToHost), "D2H"))) return st;
+    return fl_set_error(FL_OK, "");
+}
+}  // namespace
+
+extern "C" void Ax_fan_mf_gpu_siddon(float* X, float* y, float SO, float OD, float scale, int nx,
+                                     int ny, int nv, float* sd_phi, int nd, float* y_det,
+                                     int* id_X, int nt)
+{
+    fl_scan s;
+    std::memset(&s, 0, sizeof s);
+    s.ndim = 2; s.nx = nx; s.ny = ny; s.nz = 1; s.nt = nt; s.nv = nv; s.na = nd; s.nb = 1;
+    s.SO = SO; s.OD = OD; s.scale = scale; s.dz = 1.0f;
+    s.sd_phi = sd_phi; s.y_det = y_det; s.view_frame = id_X;
+    run_forward_host(s, FL_MODEL_SIDDON_REF, X, y);
+}
+
+extern "C" void Atx_fan_mf_gpu_new(float* x, float* Y, float SO, float OD, float scale, int nx,
+                                   int ny, float* sd_phi, int nd, float* y_det, float dy_det,
+                                   float y_os, int nt, int* id_Y, int* Nv, int tmp_size, int nv,
+                                   float* cos_phi, float* sin_phi, float* cos_det,
+                                   float* sin_det)
+{
+    fl_scan s;
+    std::memset(&s, 0, sizeof s);
+    s.ndim = 2; s.nx = nx; s.ny = ny; s.nz = 1; s.nt = nt; s.nv = nv; s.na = nd; s.nb = 1;
+    s.SO = SO; s.OD = OD; s.scale = scale; s.dz = 1.0f; s.dy_det = dy_det; s.y_os = y_os;
+    s.sd_phi = sd_phi; s.y_det = y_det; s.cos_phi = cos_phi; s.sin_phi = sin_phi;
+    s.cos_det = cos_det; s.sin_det = sin_det;
+    s.id_Y = id_Y; s.Nv = Nv; s.tmp_size = tmp_size;
+    int bad;
+    std::vector<int32_t> vf = frames_of(id_Y, Nv, nt, tmp_size, nv, &bad);
+    if (bad) { fl_set_error(FL_ERR_INVALID, "id_Y entry out of range"); return; }
+    s.view_frame = vf.data();
+    run_adjoint_host(s, FL_MODEL_CHORD_REF, Y, x);
+}
+
+extern "C" void Ax_cone_mf_gpu_siddon(float* X, float* y, float* sd_phi, float* sd_z,
+                                      float* y_det, float* z_det, int* id_Y, int* Nv, float SO,
+                                      float OD, float scale, float dz, int nx, int ny, int nz,
+                                      int nt, int na, int nb, int nv, int tmp_size, int nv_block)
+{
+    (void)nv_block;
+    fl_scan s;
+    std::memset(&s, 0, sizeof s);
+    s.ndim = 3; s.nx = nx; s.ny = ny; s.nz = nz; s.nt = nt; s.nv = nv; s.na = na; s.nb = nb;
+    s.SO = SO; s.OD = OD; s.scale = scale; s.dz = dz;
+    s.sd_phi = sd_phi; s.sd_z = sd_z; s.y_det = y_det; s.z_det = z_det;
+    int bad;
+    std::vector<int32_t> vf = frames_of(id_Y, Nv, nt, tmp_size, nv, &bad);
+    if (bad) { fl_set_error(FL_ERR_INVALID, "id_Y entry out of range"); return; }
+    s.view_frame = vf.data();
+    s.id_Y = id_Y; s.Nv = Nv; s.tmp_size = tmp_size;
+    run_forward_host(s, FL_MODEL_SIDDON_REF, X, y);
+}
+
+extern "C" void Atx_cone_mf_gpu_new(float* X, float* y, float* cos_phi, float* sin_phi,
+                                    float* sd_z, float* y_det, float* z_det, int* id_Y, int* Nv,
+                                    float SO, float OD, float scale, float dy_det, float y_os,
+                                    float dz_det, float dz, int nx, int ny, int nz, int nt,
+                                    int na, int nb, int nv, int tmp_size, int nv_block)
+{
+    (void)nv_block;
+    fl_scan s;
+    std::memset(&s, 0, sizeof s);
+    s.ndim = 3; s.nx = nx; s.ny = ny; s.nz = nz; s.nt = nt; s.nv = nv; s.na = na; s.nb = nb;
+    s.SO = SO; s.OD = OD; s.scale = scale; s.dz = dz;
+    s.dy_det = dy_det; s.y_os = y_os; s.dz_det = dz_det;
+    s.cos_phi = cos_phi; s.sin_phi = sin_phi; s.sd_z = sd_z; s.y_det = y_det; s.z_det = z_det;
+    int bad;
+    std::vector<int32_t> vf = frames_of(id_Y, Nv, nt, tmp_size, nv, &bad);
+    if (bad) { fl_set_error(FL_ERR_INVALID, "id_Y entry out of range"); return; }
+    s.view_frame = vf.data();
+    s.id_Y = id_Y; s.Nv = Nv; s.tmp_size = tmp_size;
+    run_adjoint_host(s, FL_MODEL_CHORD_REF, y, X);
+}

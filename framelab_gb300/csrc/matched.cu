@@ -1,0 +1,437 @@
+// matched.cu -- matched Siddon projector pair (FL_MODEL_MATCHED).
+//
+// Matrix. For ray r and voxel V = (ix, iy, iz) the entry is
+//     A[r,V] = c_r * w_rV,   c_r = scale * |D - S|,
+//     w_rV   = fl( min_a max(A_a(i_a), A_a(i_a+1)) - max_a min(A_a(i_a), A_a(i_a+1)) )
+// when positive, where A_a(k) = fmaf(k, inv_a, off_a) are the FP32 plane
+// crossings of the ray (fl_plan.h). This is the exact Siddon intersection
+// length evaluated with FP32 crossing parameters.
+//
+// Forward: one thread per ray walks the crossings in increasing order (an
+// incremental Siddon walk: three candidate crossings, step the smallest). The
+// segment it accumulates inside V is exactly w_rV above: its start is the
+// latest crossing behind V, its end the earliest crossing ahead.
+//
+// Adjoint: one thread per voxel column gathers over the rays whose detector
+// window covers the column and evaluates the same w_rV from the same table
+// entries -- the exact transpose, with no atomics.
+#include "fl_common.cuh"
+#include "fl_plan.h"
+
+namespace {
+
+template <typename T>
+__device__ __forceinline__ float ldv(const T* p) { return Store<T>::ld(p); }
+
+// Slab index of the ray at parameter a on one axis, consistent with the FP32
+// crossings: inv > 0 -> A(j) <= a < A(j+1); inv < 0 -> A(j+1) <= a < A(j).
+__device__ __forceinline__ int start_slab(float a, float inv, float off, int n)
+{
+    float t = floorf(__fdividef(a - off, inv));
+    t = fminf(fmaxf(t, 0.0f), (float)(n - 1));   // NaN -> 0
+    int j = (int)t;
+    if (inv > 0.0f) {
+        while (j < n - 1 && fmaf((float)(j + 1), inv, off) <= a) j++;
+        while (j > 0 && fmaf((float)j, inv, off) > a) j--;
+    } else {
+        while (j > 0 && fmaf((float)j, inv, off) <= a) j--;
+        while (j < n - 1 && fmaf((float)(j + 1), inv, off) > a) j++;
+    }
+    return j;
+}
+
+// Walk one ray through an nx*ny*nz volume (nz == 1 with no z axis for 2-D).
+// Returns sum over voxels of w * x; *nseg counts segments with w > 0.
+template <typename TX, bool THREE, bool COUNT>
+__device__ __forceinline__ float walk(const TX* __restrict__ x, float inv_x, float off_x,
+                                      float inv_y, float off_y, float inv_z, float off_z,
+                                      int nx, int ny, int nz, int* nseg)
+{
+    float ax0 = fmaf(0.0f, inv_x, off_x), ax1 = fmaf((float)nx, inv_x, off_x);
+    float ay0 = fmaf(0.0f, inv_y, off_y), ay1 = fmaf((float)ny, inv_y, off_y);
+    float a_in = fmaxf(fminf(ax0, ax1), fminf(ay0, ay1));
+    float a_out = fminf(fmaxf(ax0, ax1), fmaxf(ay0, ay1));
+    float az0 = 0.0f, az1 = 0.0f;
+    if (THREE) {
+        az0 = fmaf(0.0f, inv_z, off_z); az1 = fmaf((float)nz, inv_z, off_z);
+        a_in = fmaxf(a_in, fminf(az0, az1));
+        a_out = fminf(a_out, fmaxf(az0, az1));
+    }
+    if (!(a_in < a_out)) return 0.0f;
+    int jx = start_slab(a_in, inv_x, off_x, nx);
+    int jy = start_slab(a_in, inv_y, off_y, ny);
+    int jz = THREE ? start_slab(a_in, inv_z, off_z, nz) : 0;
+    const long long sy = nx, sz = (long long)nx * ny;
+    long long v = (long long)jz * sz + (long long)jy * sy + jx;
+    float pax = (inv_x > 0.0f) ? (float)(jx + 1) : (float)jx;
+    float pay = (inv_y > 0.0f) ? (float)(jy + 1) : (float)jy;
+    float paz = (inv_z > 0.0f) ? (float)(jz + 1) : (float)jz;
+    const float stx = (inv_x > 0.0f) ? 1.0f : -1.0f;
+    const float sty = (inv_y > 0.0f) ? 1.0f : -1.0f;
+    const float stz = (inv_z > 0.0f) ? 1.0f : -1.0f;
+    const long long dvx = (inv_x > 0.0f) ? 1 : -1;
+    const long long dvy = (inv_y > 0.0f) ? sy : -sy;
+    const long long dvz = (inv_z > 0.0f) ? sz : -sz;
+    float cur = a_in, acc = 0.0f;
+    int cnt = 0;
+    const int maxit = nx + ny + (THREE ? nz : 0) + 3;   // every step crosses >= 1 plane
+    for (int it = 0; it < maxit; ++it) {
+        float nAx = fmaf(pax, inv_x, off_x);
+        float nAy = fmaf(pay, inv_y, off_y);
+        float nxt = fminf(nAx, nAy);
+        float nAz = 0.0f;
+        if (THREE) { nAz = fmaf(paz, inv_z, off_z); nxt = fminf(nxt, nAz); }
+        float seg = nxt - cur;
+        if (COUNT) cnt += (seg > 0.0f);
+        else acc = fmaf(seg, ldv(x + v), acc);
+        if (nxt >= a_out) break;
+        if (nAx == nxt) { pax += stx; v += dvx; }
+        if (nAy == nxt) { pay += sty; v += dvy; }
+        if (THREE && nAz == nxt) { paz += stz; v += dvz; }
+        cur = nxt;
+    }
+    if (COUNT) *nseg = cnt;
+    return acc;
+}
+
+__device__ __forceinline__ float ray_cr(float scale, float dxy2, float dz2)
+{
+    return fmul(scale, fsqrt(fadd(dxy2, dz2)));
+}
+
+// ---------------------------------------------------------------------------
+// Forward kernels. Block (32, 4): 32 adjacent detector columns x 4 rows of one
+// view, so a warp's rays are neighbours and their gathers share cache lines.
+// ---------------------------------------------------------------------------
+template <typename TX, typename TY>
+__global__ void __launch_bounds__(128)
+k_fwd_cone(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restrict__ col,
+           const float* __restrict__ colr, const RowEntry* __restrict__ row,
+           const int* __restrict__ vframe, int nx, int ny, int nz, int na, int nb,
+           long long nper, float scale, int cr_power)
+{
+    int ia = blockIdx.x * 32 + threadIdx.x;
+    int ib = blockIdx.y * 4 + threadIdx.y;
+    int iv = blockIdx.z;
+    if (ia >= na || ib >= nb) return;
+    ColEntry ce = col[(long long)iv * na + ia];
+    RowEntry re = row[(long long)iv * nb + ib];
+    const TX* x = X + (long long)vframe[iv] * nper;
+    float acc = walk<TX, true, false>(x, ce.inv_x, ce.off_x, ce.inv_y, ce.off_y, re.inv_z,
+                                      re.off_z, nx, ny, nz, nullptr);
+    float cr = ray_cr(scale, colr[(long long)iv * na + ia], re.dz2);
+    float out = cr * acc;
+    if (cr_power == 2) out = cr * out;
+    Store<TY>::st(y + ((long long)iv * nb + ib) * na + ia, out);
+}
+
+template <typename TX, typename TY>
+__global__ void __launch_bounds__(128)
+k_fwd_fan(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restrict__ col,
+          const float* __restrict__ colr, const int* __restrict__ vframe, int nx, int ny,
+          int na, int nv, long long nper, float scale, int cr_power)
+{
+    long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= (long long)na * nv) return;
+    int iv = (int)(r / na);
+    ColEntry ce = col[r];
+    const TX* x = X + (long long)vframe[iv] * nper;
+    float acc = walk<TX, false, false>(x, ce.inv_x, ce.off_x, ce.inv_y, ce.off_y, 0.0f, 0.0f,
+                                       nx, ny, 1, nullptr);
+    float cr = ray_cr(scale, colr[r], 0.0f);
+    float out = cr * acc;
+    if (cr_power == 2) out = cr * out;
+    Store<TY>::st(y + r, out);
+}
+
+__global__ void __launch_bounds__(128)
+k_count(int32_t* __restrict__ cnt, const ColEntry* __restrict__ col,
+        const RowEntry* __restrict__ row, int nx, int ny, int nz, int na, int nb, int nv,
+        int three)
+{
+    long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long nr = (long long)na * nb * nv;
+    if (r >= nr) return;
+    int ia = (int)(r % na);
+    long long q = r / na;
+    int ib = (int)(q % nb);
+    int iv = (int)(q / nb);
+    ColEntry ce = col[(long long)iv * na + ia];
+    int c = 0;
+    if (three) {
+        RowEntry re = row[(long long)iv * nb + ib];
+        walk<float, true, true>(nullptr, ce.inv_x, ce.off_x, ce.inv_y, ce.off_y, re.inv_z,
+                                re.off_z, nx, ny, nz, &c);
+    } else {
+        walk<float, false, true>(nullptr, ce.inv_x, ce.off_x, ce.inv_y, ce.off_y, 0.0f, 0.0f,
+                                 nx, ny, 1, &c);
+    }
+    cnt[r] = c;
+}
+
+// yw = c_r * y  (the adjoint gathers pre-weighted sinogram values)
+template <typename TY>
+__global__ void k_weight(float* __restrict__ yw, const TY* __restrict__ y,
+                         const float* __restrict__ colr, const RowEntry* __restrict__ row,
+                         int na, int nb, long long nrays, float scale, int three)
+{
+    long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrays) return;
+    int ia = (int)(r % na);
+    long long q = r / na;
+    int ib = (int)(q % nb);
+    int iv = (int)(q / nb);
+    float dz2 = three ? row[(long long)iv * nb + ib].dz2 : 0.0f;
+    float cr = ray_cr(scale, colr[(long long)iv * na + ia], dz2);
+    yw[r] = cr * Store<TY>::ld_plain(y + r);
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint helpers: detector column window of an axis-aligned xy box.
+// ---------------------------------------------------------------------------
+struct DetGrid {
+    int kind;          // 0 flat uniform, 1 equiangular
+    float u0, du, g0, dg, v0, dv, SO, SD;
+};
+
+// Column range [lo, hi] of rays that can cross the xy square [x0,x0+1]x[y0,y0+1]
+// in a view with cos/sin (c, s); also returns the depth range SO + t.
+__device__ __forceinline__ void column_window(const DetGrid& G, float c, float s, float x0,
+                                              float y0, float wx, float wy, int na, int& lo,
+                                              int& hi, float& dmin, float& dmax)
+{
+    float umin = 3.0e38f, umax = -3.0e38f;
+    dmin = 3.0e38f; dmax = -3.0e38f;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        float px = x0 + ((k & 1) ? wx : 0.0f);
+        float py = y0 + ((k & 2) ? wy : 0.0f);
+        float depth = G.SO + (c * px + s * py);        // distance from source along the axis
+        float lat = -s * px + c * py;
+        float u = (G.kind == 0) ? G.SD * __fdividef(lat, depth) : atan2f(lat, depth);
+        umin = fminf(umin, u); umax = fmaxf(umax, u);
+        dmin = fminf(dmin, depth); dmax = fmaxf(dmax, depth);
+    }
+    float f0, f1;
+    if (G.kind == 0) { f0 = (umin - G.u0) / G.du; f1 = (umax - G.u0) / G.du; }
+    else             { f0 = (umin - G.g0) / G.dg; f1 = (umax - G.g0) / G.dg; }
+    if (f0 > f1) { float t = f0; f0 = f1; f1 = t; }
+    f0 = fmaxf(floorf(f0) - 1.0f, 0.0f);
+    f1 = fminf(ceilf(f1) + 1.0f, (float)(na - 1));
+    lo = (int)f0; hi = (int)f1;                   // empty when lo > hi
+}
+
+// ---------------------------------------------------------------------------
+// Fan adjoint: one thread per (pixel, frame).
+// ---------------------------------------------------------------------------
+template <typename TX>
+__global__ void __launch_bounds__(128)
+k_adj_fan(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __restrict__ col,
+          const ViewEntry* __restrict__ view, const int* __restrict__ idY,
+          const int* __restrict__ Nv, int tmp_size, DetGrid G, int nx, int ny, int na)
+{
+    int ix = blockIdx.x * blockDim.x + threadIdx.x;
+    int iy = blockIdx.y;
+    int it = blockIdx.z;
+    if (ix >= nx) return;
+    float x0 = (float)(ix - nx / 2), y0 = (float)(iy - ny / 2);
+    float fx0 = (float)ix, fx1 = (float)(ix + 1), fy0 = (float)iy, fy1 = (float)(iy + 1);
+    float acc = 0.0f;
+    int nvf = Nv[it];
+    for (int j = 0; j < nvf; j++) {
+        int iv = idY[it * tmp_size + j];
+        ViewEntry ve = view[iv];
+        int lo, hi; float dmin, dmax;
+        column_window(G, ve.c, ve.s, x0, y0, 1.0f, 1.0f, na, lo, hi, dmin, dmax);
+        const ColEntry* cv = col + (long long)iv * na;
+        const float* yv = yw + (long long)iv * na;
+        for (int ia = lo; ia <= hi; ia++) {
+            ColEntry ce = cv[ia];
+            float ax0 = fmaf(fx0, ce.inv_x, ce.off_x), ax1 = fmaf(fx1, ce.inv_x, ce.off_x);
+            float ay0 = fmaf(fy0, ce.inv_y, ce.off_y), ay1 = fmaf(fy1, ce.inv_y, ce.off_y);
+            float l = fmaxf(fminf(ax0, ax1), fminf(ay0, ay1));
+            float h = fminf(fmaxf(ax0, ax1), fmaxf(ay0, ay1));
+            float w = h - l;
+            if (w > 0.0f) acc = fmaf(w, __ldg(yv + ia), acc);
+        }
+    }
+    Store<TX>::st(X + (long long)it * nx * ny + (long long)iy * nx + ix, acc);
+}
+
+// ---------------------------------------------------------------------------
+// Cone adjoint: one thread per voxel column (ix, iy) and a run of TZ voxels
+// in z; block (32, 4). Per view and candidate detector column the thread
+// forms the column's xy crossing interval once, then visits only the detector
+// rows -- and for each row only the z voxels -- that the ray can cross inside
+// that interval. Per-thread accumulators live in shared memory so the z run
+// can be indexed at run time.
+// ---------------------------------------------------------------------------
+template <typename TX, int TZ>
+__global__ void __launch_bounds__(128)
+k_adj_cone(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __restrict__ col,
+           const RowEntry* __restrict__ row, const ViewEntry* __restrict__ view,
+           const int* __restrict__ idY, const int* __restrict__ Nv, int tmp_size, DetGrid G,
+           int nx, int ny, int nz, int na, int nb, float dz, int zruns)
+{
+    __shared__ float sacc[TZ][128];
+    const int tid = threadIdx.y * 32 + threadIdx.x;
+    const int ix = blockIdx.x * 32 + threadIdx.x;
+    const int iy = blockIdx.y * 4 + threadIdx.y;
+    const int zr = blockIdx.z % zruns, it = blockIdx.z / zruns;
+    const int z0 = zr * TZ;
+    const int z1 = min(z0 + TZ, nz);          // exclusive
+#pragma unroll
+    for (int k = 0; k < TZ; k++) sacc[k][tid] = 0.0f;
+    const bool active = (ix < nx) && (iy < ny);
+    if (active) {
+        float x0 = (float)(ix - nx / 2), y0 = (float)(iy - ny / 2);
+        float fx0 = (float)ix, fx1 = (float)(ix + 1), fy0 = (float)iy, fy1 = (float)(iy + 1);
+        float Zlo = (float)(z0 - nz / 2) * dz, Zhi = (float)(z1 - nz / 2) * dz;
+        int nvf = Nv[it];
+        for (int j = 0; j < nvf; j++) {
+            int iv = idY[it * tmp_size + j];
+            ViewEntry ve = view[iv];
+            int alo, ahi; float dmin, dmax;
+            column_window(G, ve.c, ve.s, x0, y0, 1.0f, 1.0f, na, alo, ahi, dmin, dmax);
+            const ColEntry* cv = col + (long long)iv * na;
+            const RowEntry* rv = row + (long long)iv * nb;
+            const float* yv = yw + (long long)iv * nb * na;
+            const float zl = Zlo - ve.sz, zh = Zhi - ve.sz;
+            for (int ia = alo; ia <= ahi; ia++) {
+                ColEntry ce = cv[ia];
+                float ax0 = fmaf(fx0, ce.inv_x, ce.off_x), ax1 = fmaf(fx1, ce.inv_x, ce.off_x);
+                float ay0 = fmaf(fy0, ce.inv_y, ce.off_y), ay1 = fmaf(fy1, ce.inv_y, ce.off_y);
+                float l = fmaxf(fminf(ax0, ax1), fminf(ay0, ay1));
+                float h = fminf(fmaxf(ax0, ax1), fmaxf(ay0, ay1));
+                if (!(l < h)) continue;
+                // rows whose ray reaches z in [Zlo, Zhi] while alpha is in [l, h]:
+                // z = sz + (A + ac) * d_z, d_z = v0 + ib*dv (flat panel rows)
+                float a1 = l + ve.ac, a2 = h + ve.ac;
+                float r1 = __fdividef(1.0f, a1), r2 = __fdividef(1.0f, a2);
+                float dlo = fminf(zl * r1, zl * r2), dhi = fmaxf(zh * r1, zh * r2);
+                float b0 = (dlo - G.v0) / G.dv, b1 = (dhi - G.v0) / G.dv;
+                if (b0 > b1) { float t = b0; b0 = b1; b1 = t; }
+                int blo = (int)fmaxf(floorf(b0) - 1.0f, 0.0f);
+                int bhi = (int)fminf(ceilf(b1) + 1.0f, (float)(nb - 1));
+                for (int ib = blo; ib <= bhi; ib++) {
+                    RowEntry re = rv[ib];
+                    float t0 = (l - re.off_z) * re.rinv_z, t1 = (h - re.off_z) * re.rinv_z;
+                    float tmin = fminf(t0, t1), tmax = fmaxf(t0, t1);
+                    int klo = (int)fmaxf(floorf(tmin - 0.01f), (float)z0);
+                    int khi = (int)fminf(floorf(tmax + 0.01f), (float)(z1 - 1));
+                    if (klo > khi) continue;
+                    float yval = __ldg(yv + (long long)ib * na + ia);
+                    for (int iz = klo; iz <= khi; iz++) {
+                        float az0 = fmaf((float)iz, re.inv_z, re.off_z);
+                        float az1 = fmaf((float)(iz + 1), re.inv_z, re.off_z);
+                        float l2 = fmaxf(l, fminf(az0, az1));
+                        float h2 = fminf(h, fmaxf(az0, az1));
+                        float w = h2 - l2;
+                        if (w > 0.0f) sacc[iz - z0][tid] = fmaf(w, yval, sacc[iz - z0][tid]);
+                    }
+                }
+            }
+        }
+        long long base = (long long)it * nx * ny * nz + (long long)iy * nx + ix;
+        for (int iz = z0; iz < z1; iz++)
+            Store<TX>::st(X + base + (long long)iz * nx * ny, sacc[iz - z0][tid]);
+    }
+}
+
+DetGrid det_grid(const fl_plan* p)
+{
+    DetGrid G;
+    G.kind = p->det_kind; G.u0 = p->u0; G.du = p->du; G.g0 = p->g0; G.dg = p->dg;
+    G.v0 = p->v0; G.dv = p->dv; G.SO = p->s.SO; G.SD = p->SD;
+    return G;
+}
+
+template <typename TX, typename TY>
+void launch_fwd(fl_plan* p, const void* x, void* y, int cr_power, cudaStream_t st)
+{
+    const fl_scan& s = p->s;
+    if (s.ndim == 3) {
+        dim3 grid(fl_div_up(s.na, 32), fl_div_up(s.nb, 4), s.nv);
+        k_fwd_cone<TX, TY><<<grid, dim3(32, 4), 0, st>>>(
+            (const TX*)x, (TY*)y, p->d_col, p->d_colr, p->d_row, p->d_view_frame, s.nx, s.ny,
+            s.nz, s.na, s.nb, p->n_vox_frame, s.scale, cr_power);
+    } else {
+        long long nr = (long long)s.na * s.nv;
+        k_fwd_fan<TX, TY><<<fl_div_up(nr, 128), 128, 0, st>>>(
+            (const TX*)x, (TY*)y, p->d_col, p->d_colr, p->d_view_frame, s.nx, s.ny, s.na, s.nv,
+            p->n_vox_frame, s.scale, cr_power);
+    }
+}
+
+template <typename TX>
+void launch_fwd_y(fl_plan* p, const void* x, void* y, int yt, int cr_power, cudaStream_t st)
+{
+    if (yt == FL_F32) launch_fwd<TX, float>(p, x, y, cr_power, st);
+    else if (yt == FL_F16) launch_fwd<TX, __half>(p, x, y, cr_power, st);
+    else launch_fwd<TX, __nv_bfloat16>(p, x, y, cr_power, st);
+}
+
+template <typename TX>
+void launch_adj(fl_plan* p, const float* yw, void* x, cudaStream_t st)
+{
+    const fl_scan& s = p->s;
+    DetGrid G = det_grid(p);
+    if (s.ndim == 3) {
+        constexpr int TZ = 8;
+        int zruns = (s.nz + TZ - 1) / TZ;
+        dim3 grid(fl_div_up(s.nx, 32), fl_div_up(s.ny, 4), (unsigned)zruns * s.nt);
+        k_adj_cone<TX, TZ><<<grid, dim3(32, 4), 0, st>>>(
+            (TX*)x, yw, p->d_col, p->d_row, p->d_view, p->d_idY, p->d_Nv, p->tmp_size, G, s.nx,
+            s.ny, s.nz, s.na, s.nb, s.dz, zruns);
+    } else {
+        dim3 grid(fl_div_up(s.nx, 128), s.ny, s.nt);
+        k_adj_fan<TX><<<grid, 128, 0, st>>>((TX*)x, yw, p->d_col, p->d_view, p->d_idY,
+                                             p->d_Nv, p->tmp_size, G, s.nx, s.ny, s.na);
+    }
+}
+
+}  // namespace
+
+int fl_matched_forward(fl_plan* p, const void* x, int xt, void* y, int yt, int cr_power,
+                       cudaStream_t st)
+{
+    if (xt == FL_F32) launch_fwd_y<float>(p, x, y, yt, cr_power, st);
+    else if (xt == FL_F16) launch_fwd_y<__half>(p, x, y, yt, cr_power, st);
+    else launch_fwd_y<__nv_bfloat16>(p, x, y, yt, cr_power, st);
+    return fl_check_launch("matched forward");
+}
+
+int fl_matched_weight(fl_plan* p, const void* y, int yt, float* yw, cudaStream_t st)
+{
+    const fl_scan& s = p->s;
+    long long nr = p->n_rays;
+    int three = s.ndim == 3;
+    unsigned g = fl_div_up(nr, 256);
+    if (yt == FL_F32)
+        k_weight<float><<<g, 256, 0, st>>>(yw, (const float*)y, p->d_colr, p->d_row, s.na,
+                                           s.nb, nr, s.scale, three);
+    else if (yt == FL_F16)
+        k_weight<__half><<<g, 256, 0, st>>>(yw, (const __half*)y, p->d_colr, p->d_row, s.na,
+                                            s.nb, nr, s.scale, three);
+    else
+        k_weight<__nv_bfloat16><<<g, 256, 0, st>>>(yw, (const __nv_bfloat16*)y, p->d_colr,
+                                                   p->d_row, s.na, s.nb, nr, s.scale, three);
+    return fl_check_launch("matched adjoint weighting");
+}
+
+int fl_matched_adjoint_w(fl_plan* p, const float* yw, void* x, int xt, cudaStream_t st)
+{
+    if (xt == FL_F32) launch_adj<float>(p, yw, x, st);
+    else if (xt == FL_F16) launch_adj<__half>(p, yw, x, st);
+    else launch_adj<__nv_bfloat16>(p, yw, x, st);
+    return fl_check_launch("matched adjoint");
+}
+
+int fl_matched_count(fl_plan* p, int32_t* counts, cudaStream_t st)
+{
+    const fl_scan& s = p->s;
+    long long nr = p->n_rays;
+    k_count<<<fl_div_up(nr, 128), 128, 0, st>>>(counts, p->d_col, p->d_row, s.nx, s.ny, s.nz,
+                                                s.na, s.nb, s.nv, s.ndim == 3);
+    return fl_check_launch("intersection count");
+}

@@ -1,0 +1,463 @@
+// ref_kernels.cu -- GPU kernels that reproduce the reference's CPU projectors
+// bit for bit (FL_MODEL_SIDDON_REF forward, FL_MODEL_CHORD_REF adjoint).
+//
+// Every float operation is the one the reference performs, in its order,
+// through the pinned intrinsics of fl_common.cuh (no FMA contraction).
+// Work that cannot change the result is skipped: the Siddon merge starts a
+// few planes before the ray enters the image and stops a few planes after it
+// leaves (decided in FP64 with a 2-voxel safety band), since segments
+// outside the image add nothing in the reference either.
+#include "fl_common.cuh"
+#include "fl_plan.h"
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// Siddon merge (version 0). One axis of plane crossings; see oracle.c for the
+// argument that a plain sorted merge equals the reference's sort_alpha() merge
+// (sort_alpha.cpp:15-60) for the sum it feeds.
+// ---------------------------------------------------------------------------
+struct MergeAxis {
+    int i;        // current plane index
+    int left;     // planes still to emit (including i)
+    int di;       // +1 / -1
+    float p1, d;  // source coordinate, direction component
+    float pitch;  // plane spacing: 1 for x/y, dz0 for z
+    bool zaxis;
+    float head;
+};
+
+__device__ __forceinline__ float merge_alpha(const MergeAxis& a, int i)
+{
+    if (a.zaxis) return fdiv(fsub(fmul((float)i, a.pitch), a.p1), a.d);  // Ax_cone_mf_cpu_siddon.cpp:69
+    return fdiv(fsub((float)i, a.p1), a.d);                               // Ax_fan_mf_cpu_siddon.cpp:44
+}
+
+// Box-clip one axis of the ray (p1 -> p1+d) against planes [lo, hi] in FP64;
+// returns false when the ray misses the slab entirely.
+__device__ __forceinline__ bool clip_axis(double p1, double d, double lo, double hi,
+                                          double& amin, double& amax)
+{
+    if (d == 0.0) return p1 >= lo && p1 <= hi;
+    double t0 = (lo - p1) / d, t1 = (hi - p1) / d;
+    if (t0 > t1) { double t = t0; t0 = t1; t1 = t; }
+    amin = fmax(amin, t0);
+    amax = fmin(amax, t1);
+    return true;
+}
+
+// Plane index range [first..last] (in traversal order) covering alpha in
+// [A0, A1] plus one plane on either side and one more for rounding.
+__device__ __forceinline__ void init_axis(MergeAxis& a, float p1, float p2, int n, bool zaxis,
+                                          float dz0, double A0, double A1)
+{
+    int n2 = n / 2;
+    a.p1 = p1; a.d = fsub(p2, p1); a.zaxis = zaxis; a.pitch = zaxis ? dz0 : 1.0f;
+    a.left = 0;
+    if (p1 == p2) return;
+    double pitch = zaxis ? (double)dz0 : 1.0;
+    double c0 = ((double)p1 + A0 * (double)a.d) / pitch;
+    double c1 = ((double)p1 + A1 * (double)a.d) / pitch;
+    int first, last;
+    if (p1 < p2) {
+        a.di = 1;
+        first = max(-n2, (int)floor(c0) - 2);
+        last = min(n2, (int)ceil(c1) + 2);
+        a.left = last - first + 1;
+    } else {
+        a.di = -1;
+        first = min(n2, (int)ceil(c0) + 2);
+        last = max(-n2, (int)floor(c1) - 2);
+        a.left = first - last + 1;
+    }
+    if (a.left < 0) a.left = 0;
+    a.i = first;
+    if (a.left > 0) a.head = merge_alpha(a, a.i);
+}
+
+template <int NA>
+__device__ __forceinline__ int pick_min(const MergeAxis (&ax)[NA])
+{
+    int best = -1;
+#pragma unroll
+    for (int k = 0; k < NA; k++)
+        if (ax[k].left > 0 && (best < 0 || ax[k].head < ax[best].head)) best = k;
+    return best;
+}
+
+template <int NA>
+__device__ __forceinline__ float pop(MergeAxis (&ax)[NA], int k)
+{
+    float v = ax[k].head;
+    // select by constant index so the array stays in registers
+#pragma unroll
+    for (int j = 0; j < NA; j++) {
+        if (j == k) {
+            ax[j].left -= 1;
+            ax[j].i += ax[j].di;
+            if (ax[j].left > 0) ax[j].head = merge_alpha(ax[j], ax[j].i);
+        }
+    }
+    return v;
+}
+
+// Fan-beam Siddon, restating Ax_fan_mf_cpu_siddon.cpp:19-93. One thread per ray.
+__global__ void __launch_bounds__(128)
+k_ref_fan_siddon(const float* __restrict__ X, float* __restrict__ y,
+                 const float* __restrict__ cphi_v, const float* __restrict__ sphi_v,
+                 const float* __restrict__ ydet, const int* __restrict__ vframe, float SO,
+                 float OD, float scale, int nx, int ny, int nd, long long nper)
+{
+    int id = blockIdx.x * blockDim.x + threadIdx.x;
+    int iv = blockIdx.y;
+    if (id >= nd) return;
+    const float* x = X + (long long)vframe[iv] * nper;
+    float c = cphi_v[iv], s = sphi_v[iv];
+    float x1 = fmul(c, -SO), y1 = fmul(s, -SO);
+    float u = ydet[id];
+    float x2 = fsub(fmul(c, OD), fmul(s, u));
+    float y2 = fadd(fmul(s, OD), fmul(c, u));
+    float dx = fsub(x2, x1), dy = fsub(y2, y1);
+    float total = fsqrt(fadd(fmul(dx, dx), fmul(dy, dy)));
+    int nx2 = nx / 2, ny2 = ny / 2;
+
+    double A0 = -1e300, A1 = 1e300;
+    bool hit = clip_axis(x1, dx, -nx2 - 2.0, nx - nx2 + 2.0, A0, A1) &&
+               clip_axis(y1, dy, -ny2 - 2.0, ny - ny2 + 2.0, A0, A1);
+    float acc = 0.0f;
+    if (hit && A0 < A1) {
+        MergeAxis ax[2];
+        init_axis(ax[0], x1, x2, nx, false, 1.0f, A0, A1);
+        init_axis(ax[1], y1, y2, ny, false, 1.0f, A0, A1);
+        int k = pick_min(ax);
+        if (k >= 0) {
+            float prev = pop(ax, k);
+            while ((k = pick_min(ax)) >= 0) {
+                float next = pop(ax, k);
+                float ac = fmul(0.5f, fadd(prev, next));
+                int tx = (int)floorf(fadd(fadd(x1, fmul(ac, dx)), (float)nx2));
+                if (tx >= 0 && tx < nx) {
+                    int ty = (int)floorf(fadd(fadd(y1, fmul(ac, dy)), (float)ny2));
+                    if (ty >= 0 && ty < ny) {
+                        float seg = fmul(fsub(next, prev), total);
+                        acc = fadd(acc, fmul(seg, __ldg(x + ty * nx + tx)));
+                    }
+                }
+                prev = next;
+            }
+        }
+    }
+    y[(long long)iv * nd + id] = fmul(acc, scale);
+}
+
+// Cone-beam Siddon, restating Ax_cone_mf_cpu_siddon.cpp:19-134.
+__global__ void __launch_bounds__(128)
+k_ref_cone_siddon(const float* __restrict__ X, float* __restrict__ y,
+                  const float* __restrict__ cphi_v, const float* __restrict__ sphi_v,
+                  const float* __restrict__ sdz, const float* __restrict__ ydet,
+                  const float* __restrict__ zdet, const int* __restrict__ vframe, float SO,
+                  float OD, float scale, int nx, int ny, int nz, float dz0, int na, int nb,
+                  long long nper)
+{
+    int ia = blockIdx.x * blockDim.x + threadIdx.x;
+    int ib = blockIdx.y;
+    int iv = blockIdx.z;
+    if (ia >= na) return;
+    const float* x = X + (long long)vframe[iv] * nper;
+    float c = cphi_v[iv], s = sphi_v[iv];
+    float x1 = fmul(c, -SO), y1 = fmul(s, -SO), z1 = sdz[iv];
+    float u = ydet[ia];
+    float x2 = fsub(fmul(c, OD), fmul(s, u));
+    float y2 = fadd(fmul(s, OD), fmul(c, u));
+    float z2 = fadd(zdet[ib], sdz[iv]);
+    float dx = fsub(x2, x1), dy = fsub(y2, y1), dz = fsub(z2, z1);
+    float total = fsqrt(fadd(fadd(fmul(dx, dx), fmul(dy, dy)), fmul(dz, dz)));
+    int nx2 = nx / 2, ny2 = ny / 2, nz2 = nz / 2;
+
+    double A0 = -1e300, A1 = 1e300;
+    bool hit = clip_axis(x1, dx, -nx2 - 2.0, nx - nx2 + 2.0, A0, A1) &&
+               clip_axis(y1, dy, -ny2 - 2.0, ny - ny2 + 2.0, A0, A1) &&
+               clip_axis(z1, dz, (-nz2 - 2.0) * (double)dz0, (nz - nz2 + 2.0) * (double)dz0,
+                         A0, A1);
+    float acc = 0.0f;
+    if (hit && A0 < A1) {
+        MergeAxis ax[3];
+        init_axis(ax[0], x1, x2, nx, false, 1.0f, A0, A1);
+        init_axis(ax[1], y1, y2, ny, false, 1.0f, A0, A1);
+        init_axis(ax[2], z1, z2, nz, true, dz0, A0, A1);
+        int k = pick_min(ax);
+        if (k >= 0) {
+            float prev = pop(ax, k);
+            while ((k = pick_min(ax)) >= 0) {
+                float next = pop(ax, k);
+                float ac = fmul(0.5f, fadd(prev, next));
+                int tx = (int)floorf(fadd(fadd(x1, fmul(ac, dx)), (float)nx2));
+                if (tx >= 0 && tx < nx) {
+                    int ty = (int)floorf(fadd(fadd(y1, fmul(ac, dy)), (float)ny2));
+                    if (ty >= 0 && ty < ny) {
+                        int tz = (int)floorf(fadd(fdiv(fadd(z1, fmul(ac, dz)), dz0), (float)nz2));
+                        if (tz >= 0 && tz < nz) {
+                            float seg = fmul(fsub(next, prev), total);
+                            acc = fadd(acc, fmul(seg, __ldg(x + ((long long)tz * ny + ty) * nx + tx)));
+                        }
+                    }
+                }
+                prev = next;
+            }
+        }
+    }
+    y[((long long)iv * nb + ib) * na + ia] = fmul(acc, scale);
+}
+
+// ---------------------------------------------------------------------------
+// Chord-length backprojectors (version 1).
+// ---------------------------------------------------------------------------
+
+// find_l (find_l.cpp:18-45): chord of the line a*x+b*y=c through the unit
+// pixel centred at (x, y).
+__device__ __forceinline__ float chord_unit_pixel(float a, float b, float c, float x, float y)
+{
+    float aa = fabs_ref(a), bb = fabs_ref(b);
+    float ha = fdiv(aa, 2.0f), hb = fdiv(bb, 2.0f);
+    float reach = fadd(ha, hb);
+    float d = fabs_ref(fsub(fsub(c, fmul(a, x)), fmul(b, y)));
+    if (!(d < reach)) return 0.0f;
+    float flat = fabs_ref(fsub(ha, hb));
+    float full = (ha < hb) ? fdiv(1.0f, bb) : fdiv(1.0f, aa);
+    return (d <= flat) ? full : fdiv(fsub(reach, d), fmul(aa, bb));
+}
+
+// 2-D helper of find_l_3d.cpp:19-92 (a line through a w x h rectangle).
+__device__ float chord_rect(float px, float py, float qx, float qy, float w, float h, float x,
+                            float y)
+{
+    float a = fsub(qx, px), b = fsub(qy, py);
+    float hw = fdiv(w, 2.0f), hh = fdiv(h, 2.0f);
+    if (a == 0.0f) return (fabs_ref(fsub(px, x)) <= hw) ? h : 0.0f;
+    if (b == 0.0f) return (fabs_ref(fsub(py, y)) <= hh) ? w : 0.0f;
+    float rx = fsub(px, x), ry = fsub(py, y);
+    float hx0 = 0, hy0 = 0, hx1 = 0, hy1 = 0;
+    int nh = 0;
+    bool xfirst = fabs_ref(a) > fabs_ref(b);
+#pragma unroll
+    for (int pass = 0; pass < 2; pass++) {
+        if (pass == 1 && nh >= 2) break;
+        bool xfam = (pass == 0) ? xfirst : !xfirst;
+        float s, t, uu;
+        if (xfam) { s = fdiv(b, a); t = fadd(fmul(s, -rx), ry); uu = fmul(s, hw); }
+        else      { s = fdiv(a, b); t = fadd(fmul(s, -ry), rx); uu = fmul(s, hh); }
+#pragma unroll
+        for (int side = 0; side < 2; side++) {
+            if (pass == 1 && side == 1 && nh >= 2) break;
+            float v = side ? fadd(t, uu) : fsub(t, uu);
+            bool ok = xfam ? (fabs_ref(v) <= hh) : (fabs_ref(v) <= hw);
+            if (ok) {
+                float px_ = xfam ? (side ? hw : -hw) : v;
+                float py_ = xfam ? v : (side ? hh : -hh);
+                if (nh == 0) { hx0 = px_; hy0 = py_; } else { hx1 = px_; hy1 = py_; }
+                nh++;
+            }
+        }
+    }
+    if (nh != 2) return 0.0f;
+    float ex = fsub(hx1, hx0), ey = fsub(hy1, hy0);
+    return fsqrt(fadd(fmul(ex, ex), fmul(ey, ey)));
+}
+
+// find_l_3d (find_l_3d.cpp:94-182): chord of the line P->Q through the box of
+// size (w,h,t) centred at (x,y,z); faces of the dominant xy axis first, then
+// the other xy axis, then z; the first two hits give the chord.
+__device__ float chord_box(float px, float py, float pz, float qx, float qy, float qz, float w,
+                           float h, float t, float x, float y, float z)
+{
+    float a = fsub(qx, px), b = fsub(qy, py), c = fsub(qz, pz);
+    float hw = fdiv(w, 2.0f), hh = fdiv(h, 2.0f), ht = fdiv(t, 2.0f);
+    if (a == 0.0f) return chord_rect(py, pz, qy, qz, h, t, y, z);
+    if (b == 0.0f) return chord_rect(px, pz, qx, qz, w, t, x, z);
+    float rx = fsub(px, x), ry = fsub(py, y), rz = fsub(pz, z);
+    float P0[3] = {0, 0, 0}, P1[3] = {0, 0, 0};
+    int nh = 0;
+    int f0 = (fabs_ref(a) > fabs_ref(b)) ? 0 : 1;
+#pragma unroll
+    for (int pass = 0; pass < 3; pass++) {
+        if (pass > 0 && nh >= 2) break;
+        int fam = (pass == 0) ? f0 : (pass == 1 ? 1 - f0 : 2);
+        float u0, u1, v0, v1, lim0, lim1;
+        if (fam == 0) {
+            float s = fdiv(b, a); u0 = fadd(fmul(s, -rx), ry); u1 = fmul(s, hw);
+            s = fdiv(c, a);       v0 = fadd(fmul(s, -rx), rz); v1 = fmul(s, hw);
+            lim0 = hh; lim1 = ht;
+        } else if (fam == 1) {
+            float s = fdiv(a, b); u0 = fadd(fmul(s, -ry), rx); u1 = fmul(s, hh);
+            s = fdiv(c, b);       v0 = fadd(fmul(s, -ry), rz); v1 = fmul(s, hh);
+            lim0 = hw; lim1 = ht;
+        } else {
+            float s = fdiv(a, c); u0 = fadd(fmul(s, -rz), rx); u1 = fmul(s, ht);
+            s = fdiv(b, c);       v0 = fadd(fmul(s, -rz), ry); v1 = fmul(s, ht);
+            lim0 = hw; lim1 = hh;
+        }
+#pragma unroll
+        for (int side = 0; side < 2; side++) {
+            if (pass > 0 && side == 1 && nh >= 2) break;
+            float uu = side ? fadd(u0, u1) : fsub(u0, u1);
+            float vv = side ? fadd(v0, v1) : fsub(v0, v1);
+            if (fabs_ref(uu) <= lim0 && fabs_ref(vv) <= lim1) {
+                float q0, q1, q2;
+                if (fam == 0)      { q0 = side ? hw : -hw; q1 = uu; q2 = vv; }
+                else if (fam == 1) { q0 = uu; q1 = side ? hh : -hh; q2 = vv; }
+                else               { q0 = uu; q1 = vv; q2 = side ? ht : -ht; }
+                if (nh == 0) { P0[0] = q0; P0[1] = q1; P0[2] = q2; }
+                else         { P1[0] = q0; P1[1] = q1; P1[2] = q2; }
+                nh++;
+            }
+        }
+    }
+    if (nh != 2) return 0.0f;
+    float ex = fsub(P1[0], P0[0]), ey = fsub(P1[1], P0[1]), ez = fsub(P1[2], P0[2]);
+    return fsqrt(fadd(fadd(fmul(ex, ex), fmul(ey, ey)), fmul(ez, ez)));
+}
+
+// Fan-beam chord backprojection, restating Atx_fan_mf_cpu_new.cpp:21-63.
+// One thread per (pixel, frame).
+__global__ void __launch_bounds__(128)
+k_ref_fan_chord_adj(float* __restrict__ x, const float* __restrict__ Y,
+                    const float* __restrict__ cos_phi, const float* __restrict__ sin_phi,
+                    const float* __restrict__ cos_det, const float* __restrict__ sin_det,
+                    const int* __restrict__ idY, const int* __restrict__ Nv, int tmp_size,
+                    float SO, float OD, float scale, float dy_det, float y_os, int nx, int ny,
+                    int nd, int nt)
+{
+    int ix = blockIdx.x * blockDim.x + threadIdx.x;
+    int iy = blockIdx.y;
+    int it = blockIdx.z;
+    if (ix >= nx) return;
+    int nd2 = nd / 2, nx2 = nx / 2, ny2 = ny / 2;
+    float SD = fadd(SO, OD);
+    // (float)(i + 0.5 - n2) is exact for any realistic size
+    float yc = (float)(iy - ny2) + 0.5f;
+    float xc = (float)(ix - nx2) + 0.5f;
+    float acc = 0.0f;
+    int nvf = Nv[it];
+    for (int j = 0; j < nvf; j++) {
+        int iv = idY[it * tmp_size + j];
+        const float* yv = Y + (long long)iv * nd;
+        float c = cos_phi[iv], s = sin_phi[iv];
+        float xr = fadd(fmul(c, xc), fmul(s, yc));
+        float yr = fadd(fmul(-s, xc), fmul(c, yc));
+        float g = fdiv(SD, fmul(fadd(xr, SO), dy_det));
+        int hi = (int)floorf(fadd(fsub(fmul(fadd(yr, 1.0f), g), y_os), (float)nd2));
+        int lo = (int)floorf(fadd(fsub(fmul(fsub(yr, 1.0f), g), y_os), (float)nd2));
+        lo = max(lo, 0);
+        hi = min(hi, nd - 1);
+        for (int id = lo; id <= hi; id++) {
+            float sd = __ldg(sin_det + id), cd = __ldg(cos_det + id);
+            float Px = -fadd(fmul(sd, c), fmul(cd, s));
+            float Py = fsub(fmul(cd, c), fmul(sd, s));
+            float Pd = fmul(SO, sd);
+            float l = chord_unit_pixel(Px, Py, Pd, xc, yc);
+            if (l > 0.0f) acc = fadd(acc, fmul(l, __ldg(yv + id)));
+        }
+    }
+    x[(long long)it * nx * ny + (long long)iy * nx + ix] = fmul(acc, scale);
+}
+
+// Cone-beam chord backprojection, restating Atx_cone_mf_cpu_new.cpp:23-85
+// (unit-cube chord, z window half-width sqrt(1 + dz^2/2)).
+__global__ void __launch_bounds__(128)
+k_ref_cone_chord_adj(float* __restrict__ x, const float* __restrict__ Y,
+                     const float* __restrict__ cos_phi, const float* __restrict__ sin_phi,
+                     const float* __restrict__ sdz, const float* __restrict__ ydet,
+                     const float* __restrict__ zdet, const int* __restrict__ idY,
+                     const int* __restrict__ Nv, int tmp_size, float SO, float OD, float scale,
+                     float dy_det, float y_os, float dz_det, float dz, int nx, int ny, int nz,
+                     int na, int nb)
+{
+    int ix = blockIdx.x * blockDim.x + threadIdx.x;
+    int iy = blockIdx.y;
+    int izt = blockIdx.z;            // iz + nz * it
+    int iz = izt % nz, it = izt / nz;
+    if (ix >= nx) return;
+    float SD = fadd(SO, OD);
+    int na2 = na / 2, nb2 = nb / 2, nx2 = nx / 2, ny2 = ny / 2, nz2 = nz / 2;
+    long long nd = (long long)na * nb;
+    float dwin = fsqrt(fadd(1.0f, fdiv(fmul(dz, dz), 2.0f)));
+    float zc = fmul((float)(iz - nz2) + 0.5f, dz);
+    float yc = (float)(iy - ny2) + 0.5f;
+    float xc = (float)(ix - nx2) + 0.5f;
+    float acc = 0.0f;
+    int nvf = Nv[it];
+    for (int j = 0; j < nvf; j++) {
+        int iv = idY[it * tmp_size + j];
+        const float* yv = Y + (long long)iv * nd;
+        float c = cos_phi[iv], s = sin_phi[iv];
+        float xr = fadd(fmul(c, xc), fmul(s, yc));
+        float yr = fadd(fmul(-s, xc), fmul(c, yc));
+        float g = fdiv(SD, fmul(fadd(xr, SO), dy_det));
+        int amax = (int)floorf(fadd(fsub(fmul(fadd(yr, 1.0f), g), y_os), (float)na2));
+        int amin = (int)floorf(fadd(fsub(fmul(fsub(yr, 1.0f), g), y_os), (float)na2));
+        g = fdiv(SD, fmul(fadd(xr, SO), dz_det));
+        int bmax = (int)floorf(fadd(fmul(fadd(zc, dwin), g), (float)nb2));
+        int bmin = (int)floorf(fadd(fmul(fsub(zc, dwin), g), (float)nb2));
+        amin = max(amin, 0); amax = min(amax, na - 1);
+        bmin = max(bmin, 0); bmax = min(bmax, nb - 1);
+        float x1 = fmul(c, -SO), y1 = fmul(s, -SO), z1 = sdz[iv];
+        float cOD = fmul(c, OD), sOD = fmul(s, OD);
+        for (int ib = bmin; ib <= bmax; ib++) {
+            float z2 = fadd(__ldg(zdet + ib), z1);
+            for (int ia = amin; ia <= amax; ia++) {
+                float u = __ldg(ydet + ia);
+                float x2 = fsub(cOD, fmul(s, u));
+                float y2 = fadd(sOD, fmul(c, u));
+                float l = chord_box(x1, y1, z1, x2, y2, z2, 1.0f, 1.0f, 1.0f, xc, yc, zc);
+                acc = fadd(acc, fmul(l, __ldg(yv + (long long)ib * na + ia)));
+            }
+        }
+    }
+    x[(long long)it * nx * ny * nz + ((long long)iz * ny + iy) * nx + ix] = fmul(acc, scale);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Launchers (device pointers, stream-ordered)
+// ---------------------------------------------------------------------------
+int fl_ref_forward(fl_plan* p, const float* x, float* y, cudaStream_t st)
+{
+    const fl_scan& s = p->s;
+    if (s.nx % 2 || s.ny % 2 || (s.ndim == 3 && s.nz % 2))
+        return fl_set_error(FL_ERR_UNSUPPORTED,
+                            "Siddon (version 0) needs even nx, ny, nz: the reference's plane "
+                            "lists are one entry short for odd sizes");
+    long long nper = (long long)s.nx * s.ny * s.nz;
+    if (s.ndim == 2) {
+        dim3 grid(fl_div_up(s.na, 128), s.nv);
+        k_ref_fan_siddon<<<grid, 128, 0, st>>>(x, y, p->d_cphi_f, p->d_sphi_f, p->d_y_det,
+                                               p->d_view_frame, s.SO, s.OD, s.scale, s.nx,
+                                               s.ny, s.na, nper);
+    } else {
+        dim3 grid(fl_div_up(s.na, 128), s.nb, s.nv);
+        k_ref_cone_siddon<<<grid, 128, 0, st>>>(x, y, p->d_cphi_f, p->d_sphi_f, p->d_sd_z,
+                                                p->d_y_det, p->d_z_det, p->d_view_frame, s.SO,
+                                                s.OD, s.scale, s.nx, s.ny, s.nz, s.dz, s.na,
+                                                s.nb, nper);
+    }
+    return fl_check_launch("reference Siddon forward");
+}
+
+int fl_ref_adjoint(fl_plan* p, const float* y, float* x, cudaStream_t st)
+{
+    const fl_scan& s = p->s;
+    if (s.ndim == 2) {
+        dim3 grid(fl_div_up(s.nx, 128), s.ny, s.nt);
+        k_ref_fan_chord_adj<<<grid, 128, 0, st>>>(
+            x, y, p->d_cos_phi, p->d_sin_phi, p->d_cos_det, p->d_sin_det, p->d_idY, p->d_Nv,
+            p->tmp_size, s.SO, s.OD, s.scale, s.dy_det, s.y_os, s.nx, s.ny, s.na, s.nt);
+    } else {
+        dim3 grid(fl_div_up(s.nx, 128), s.ny, (unsigned)s.nz * s.nt);
+        k_ref_cone_chord_adj<<<grid, 128, 0, st>>>(
+            x, y, p->d_cos_phi, p->d_sin_phi, p->d_sd_z, p->d_y_det, p->d_z_det, p->d_idY,
+            p->d_Nv, p->tmp_size, s.SO, s.OD, s.scale, s.dy_det, s.y_os, s.dz_det, s.dz, s.nx,
+            s.ny, s.nz, s.na, s.nb);
+    }
+    return fl_check_launch("reference chord backprojection");
+}

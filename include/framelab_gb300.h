@@ -1,0 +1,152 @@
+/*
+ * framelab_gb300.h -- C ABI of libframelab_gb300.so
+ *
+ * GB300-native (sm_103a) implementation of FrameLab's CT reconstruction hot
+ * path: Siddon fan/cone projectors, their backprojectors, the undecimated
+ * piecewise-linear framelet with soft-shrinkage, and the CGLS / split-Bregman
+ * vector algebra.
+ *
+ * Two layers:
+ *  (1) Drop-ins. The reference's own extern "C" entry points, same names and
+ *      argument lists, host pointers in and out (the mex gateways and the
+ *      MATLAB classes call these unchanged). They return void like the
+ *      reference; the outcome is readable with fl_last_status()/fl_last_error().
+ *  (2) The device API. Plans (uploaded geometry + precomputed tables), device
+ *      pointers, a caller-supplied CUDA stream (passed as void*), int status.
+ *
+ * No function aborts the process. Every CUDA error is turned into a status.
+ * Volumes are x-fastest (iz*ny*nx + iy*nx + ix); sinograms are detector
+ * column fastest (iv*na*nb + ib*na + ia). All lengths are in xy-voxel units
+ * (xy pitch = 1); outputs are multiplied by `scale`, the physical xy pitch.
+ */
+#ifndef FRAMELAB_GB300_H
+#define FRAMELAB_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* Status                                                                    */
+/* ------------------------------------------------------------------------ */
+enum {
+    FL_OK = 0,
+    FL_ERR_INVALID = 1,      /* bad argument or geometry */
+    FL_ERR_UNSUPPORTED = 2,  /* valid but not implemented for this case */
+    FL_ERR_CUDA = 3,         /* a CUDA runtime call or a kernel failed */
+    FL_ERR_ALLOC = 4,        /* device or host allocation failed */
+    FL_ERR_TIMEOUT = 5       /* a bounded device-side wait gave up */
+};
+
+/* Status of the last call made on this host thread, and its message. */
+int fl_last_status(void);
+const char *fl_last_error(void);
+const char *fl_version(void);
+
+/* ------------------------------------------------------------------------ */
+/* (1) Drop-ins for the reference's GPU entry points                         */
+/* ------------------------------------------------------------------------ */
+
+/* Fan-beam Siddon projection (version 0), bit-exact with the reference's
+ * Ax_fan_mf_cpu_siddon. Replaces Ax_fan_mf_gpu_siddon
+ * (matlab/mex/src/Ax_fan_mf.h:3, Ax_fan_mf_gpu_siddon.cu:106-129).
+ * y[iv*nd+id]; X holds nt frames, view iv reads frame id_X[iv]. */
+void Ax_fan_mf_gpu_siddon(float *X, float *y, float SO, float OD, float scale, int nx, int ny,
+                          int nv, float *sd_phi, int nd, float *y_det, int *id_X, int nt);
+
+/* Fan-beam chord-length backprojection (version 1), bit-exact with the
+ * reference's Atx_fan_mf_cpu_new. Replaces Atx_fan_mf_gpu_new
+ * (matlab/mex/src/Atx_fan_mf.h:4, Atx_fan_mf_gpu_new.cu:77-106). */
+void Atx_fan_mf_gpu_new(float *x, float *Y, float SO, float OD, float scale, int nx, int ny,
+                        float *sd_phi, int nd, float *y_det, float dy_det, float y_os, int nt,
+                        int *id_Y, int *Nv, int tmp_size, int nv, float *cos_phi,
+                        float *sin_phi, float *cos_det, float *sin_det);
+
+/* Cone-beam Siddon projection (version 0), bit-exact with the reference's
+ * CPU kernel Ax_cone_mf_cpu_siddon (the reference's own GPU version of this
+ * entry point divides by the wrong z step). Replaces Ax_cone_mf_gpu_siddon
+ * (matlab/mex/src/Ax_cone_mf.h:10, Ax_cone_mf_gpu_siddon.cu:149-188).
+ * Frame it owns views id_Y[it*tmp_size + j], j < Nv[it]. nv_block is
+ * accepted and ignored (the reference used it to dodge the display watchdog). */
+void Ax_cone_mf_gpu_siddon(float *X, float *y, float *sd_phi, float *sd_z, float *y_det,
+                           float *z_det, int *id_Y, int *Nv, float SO, float OD, float scale,
+                           float dz, int nx, int ny, int nz, int nt, int na, int nb, int nv,
+                           int tmp_size, int nv_block);
+
+/* Cone-beam chord-length backprojection (version 1), bit-exact with the
+ * reference's Atx_cone_mf_cpu_new. Replaces Atx_cone_mf_gpu_new
+ * (matlab/mex/src/Atx_cone_mf.h:4, Atx_cone_mf_gpu_new.cu:114-162). */
+void Atx_cone_mf_gpu_new(float *X, float *y, float *cos_phi, float *sin_phi, float *sd_z,
+                         float *y_det, float *z_det, int *id_Y, int *Nv, float SO, float OD,
+                         float scale, float dy_det, float y_os, float dz_det, float dz, int nx,
+                         int ny, int nz, int nt, int na, int nb, int nv, int tmp_size,
+                         int nv_block);
+
+/* ------------------------------------------------------------------------ */
+/* (2) Device API                                                            */
+/* ------------------------------------------------------------------------ */
+
+/* Scan description. Host pointers; copied at plan creation. Field meanings
+ * follow the reference's `para` struct (ConeBeamScanner/setPara.m:5-82,
+ * FanBeamScanner/setPara.m:4-55). */
+typedef struct fl_scan {
+    int32_t ndim;            /* 2: fan beam, 3: cone beam */
+    int32_t nx, ny, nz;      /* voxels; nz = 1 for a fan */
+    int32_t nt;              /* volume frames (>= 1) */
+    int32_t nv;              /* views */
+    int32_t na, nb;          /* detector columns; rows (1 for a fan) */
+    float SO, OD;            /* source-isocentre, isocentre-detector distance */
+    float scale;             /* physical xy voxel pitch */
+    float dz;                /* z voxel pitch / xy pitch (cone) */
+    float dy_det, dz_det;    /* detector pitches (chord backprojector window) */
+    float y_os;              /* detector column offset in pixels (window) */
+    const float *sd_phi;     /* [nv] source angles; NULL = atan2(sin_phi, cos_phi) */
+    const float *sd_z;       /* [nv] source z, NULL = all 0 (circular) */
+    const float *y_det;      /* [na] column positions on the flat panel */
+    const float *z_det;      /* [nb] row positions (cone), NULL for a fan */
+    const float *cos_phi;    /* [nv] chord backprojector trig, NULL = computed */
+    const float *sin_phi;    /* [nv] */
+    const float *cos_det;    /* [na] fan chord backprojector, NULL = computed */
+    const float *sin_det;    /* [na] */
+    const int32_t *view_frame; /* [nv] frame read by each view (id_X), NULL = 0 */
+    const int32_t *id_Y;     /* [tmp_size*nt] views of frame it at it*tmp_size + j,
+                                j < Nv[it], in accumulation order; NULL = derived
+                                from view_frame in increasing view order */
+    const int32_t *Nv;       /* [nt] */
+    int32_t tmp_size;
+} fl_scan;
+
+typedef struct fl_plan fl_plan;
+
+/* Projection models */
+enum {
+    FL_MODEL_SIDDON_REF = 0, /* version 0: bit-exact reference Siddon forward */
+    FL_MODEL_CHORD_REF = 1,  /* version 1 adjoint: bit-exact reference chord backprojector */
+    FL_MODEL_MATCHED = 16    /* matched Siddon pair; adjoint is the exact transpose */
+};
+
+/* Storage dtypes of volumes / sinograms (arithmetic is always f32) */
+enum { FL_F32 = 0, FL_F16 = 1, FL_BF16 = 2 };
+
+int fl_plan_create(const fl_scan *scan, fl_plan **plan);
+void fl_plan_destroy(fl_plan *plan);
+/* Number of voxels (all frames) and rays of the plan. */
+int fl_plan_sizes(const fl_plan *plan, int64_t *n_vox, int64_t *n_rays);
+
+/* y = A x on `stream`. x: n_vox elements, y: n_rays elements, device memory. */
+int fl_forward(fl_plan *plan, int model, const void *x, int x_dtype, void *y, int y_dtype,
+               void *stream);
+/* x = A^T y on `stream`. For FL_MODEL_MATCHED this is the exact transpose of
+ * fl_forward's matrix; FL_MODEL_CHORD_REF is the reference's backprojector. */
+int fl_adjoint(fl_plan *plan, int model, const void *y, int y_dtype, void *x, int x_dtype,
+               void *stream);
+/* Number of voxels each ray crosses with positive length (matched model). */
+int fl_count_intersections(fl_plan *plan, int32_t *counts, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FRAMELAB_GB300_H */

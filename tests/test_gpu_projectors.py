@@ -1,0 +1,267 @@
+"""GPU parity of the projectors against the oracle and the reference fixtures.
+
+* Reference replicas (version 0 Siddon forward, version 1 chord backprojector)
+  must be bit-exact with the reference's CPU kernels: checked against the
+  committed fixtures (made by the reference itself) and the oracle restatement.
+* The matched Siddon pair is checked against the FP64 exact model (error
+  stated in each assertion), by the dot-product identity and against the
+  reference projector on phantoms within 1e-5 relative L2.
+"""
+import ctypes as C
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+from framelab_gb300 import geometry as G
+from framelab_gb300 import phantoms as PH
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _plan(p):
+    from framelab_gb300.projector import Plan
+    return Plan(p)
+
+
+def _dev(a, dtype=None):
+    torch = _torch()
+    t = torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    return t.to(dtype) if dtype is not None else t
+
+
+def _host(t):
+    _torch().cuda.synchronize()
+    return t.float().cpu().numpy().reshape(-1)
+
+
+def _rel(a, b):
+    a = np.asarray(a, np.float64); b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+# --------------------------------------------------------------------------
+# bit-exact reference replicas
+# --------------------------------------------------------------------------
+def _golden(kind):
+    from tests.golden.fixtures import load_case
+    return [load_case(p) for p in sorted(glob.glob(os.path.join(GOLDEN, "*.npz")))
+            if load_case(p)["kind"] == kind]
+
+
+@pytest.mark.parametrize("kind", ["fan_siddon", "cone_siddon"])
+def test_siddon_ref_matches_reference_fixtures(kind):
+    cases = _golden(kind)
+    assert cases
+    for c in cases:
+        P = _plan(c["para"])
+        y = _host(P.forward(_dev(c["x"].astype(np.float32)), model="siddon_ref"))
+        assert np.array_equal(y, c["y"]), f"max diff {np.abs(y - c['y']).max()}"
+
+
+@pytest.mark.parametrize("kind", ["fan_adj", "cone_adj"])
+def test_chord_ref_matches_reference_fixtures(kind):
+    cases = _golden(kind)
+    assert cases
+    for c in cases:
+        P = _plan(c["para"])
+        x = _host(P.adjoint(_dev(c["x"].astype(np.float32)), model="chord_ref"))
+        assert np.array_equal(x, c["y"]), f"max diff {np.abs(x - c['y']).max()}"
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_siddon_ref_random_geometries_bit_exact(seed):
+    rng = np.random.default_rng(seed)
+    n = [16, 32, 48, 64][seed]
+    p = G.fan_para(n, n, 2 * n + 6, 11 + seed, L=(2, 2), SO=rng.uniform(2, 8),
+                   OD=rng.uniform(2, 8), Ly=rng.uniform(3, 9))
+    x = rng.standard_normal(n * n).astype(np.float32)
+    y = _host(_plan(p).forward(_dev(x), model="siddon_ref"))
+    assert np.array_equal(y, O.fan_siddon_f32(x, p))
+    m = [8, 16, 24, 32][seed]
+    kw = dict(scan="helix", zmax=0.5, rps=1.0, vtab=1.0, fps=6) if seed % 2 else {}
+    pc = G.cone_para(m, m, m, m + 4, m, 5, L=(2, 2, 2), SO=rng.uniform(3, 8),
+                     OD=rng.uniform(3, 8), Ly=rng.uniform(3, 9), Lz=rng.uniform(3, 9), **kw)
+    xc = rng.standard_normal(m ** 3).astype(np.float32)
+    yc = _host(_plan(pc).forward(_dev(xc), model="siddon_ref"))
+    assert np.array_equal(yc, O.cone_siddon_f32(xc, pc))
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_chord_ref_random_geometries_bit_exact(seed):
+    rng = np.random.default_rng(10 + seed)
+    n = [16, 24, 40][seed]
+    p = G.fan_para(n, n, 2 * n, 9, L=(2, 2), SO=rng.uniform(2, 8), OD=rng.uniform(2, 8),
+                   Ly=rng.uniform(3, 9))
+    y = rng.standard_normal(2 * n * 9).astype(np.float32)
+    x = _host(_plan(p).adjoint(_dev(y), model="chord_ref"))
+    assert np.array_equal(x, O.fan_adj_f32(y, p))
+    m = [8, 12, 16][seed]
+    pc = G.cone_para(m, m, m, m + 4, m + 2, 6, L=(2, 2, 2), SO=rng.uniform(3, 8),
+                     OD=rng.uniform(3, 8), Ly=rng.uniform(3, 9), Lz=rng.uniform(3, 9))
+    yc = rng.standard_normal((m + 4) * (m + 2) * 6).astype(np.float32)
+    xc = _host(_plan(pc).adjoint(_dev(yc), model="chord_ref"))
+    assert np.array_equal(xc, O.cone_adj_f32(yc, pc))
+
+
+# --------------------------------------------------------------------------
+# drop-in entry points through the C ABI, host pointers (the mex boundary)
+# --------------------------------------------------------------------------
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def test_dropins_host_pointer_abi():
+    from framelab_gb300 import _lib
+    L = _lib.load()
+    rng = np.random.default_rng(5)
+    p = G.fan_para(32, 32, 48, 10, L=(2, 2))
+    X = rng.standard_normal(32 * 32).astype(np.float32)
+    y = np.zeros(48 * 10, np.float32)
+    sd = p["sd_phi"].copy(); yd = p["y_det"].copy(); idx = p["id_X"].astype(np.int32)
+    L.Ax_fan_mf_gpu_siddon(_ptr(X), _ptr(y), float(p["SO"]), float(p["OD"]), float(p["scale"]),
+                           32, 32, 10, _ptr(sd), 48, _ptr(yd), _ptr(idx), 1)
+    _lib.check_last()
+    assert np.array_equal(y, O.fan_siddon_f32(X, p))
+
+    Y = rng.standard_normal(48 * 10).astype(np.float32)
+    x = np.zeros(32 * 32, np.float32)
+    idY = np.asarray(p["id_Y"]).T.reshape(-1).astype(np.int32); Nv = p["Nv"].astype(np.int32)
+    cp, sp, cd, sdt = (p[k].copy() for k in ("cos_phi", "sin_phi", "cos_det", "sin_det"))
+    L.Atx_fan_mf_gpu_new(_ptr(x), _ptr(Y), float(p["SO"]), float(p["OD"]), float(p["scale"]),
+                         32, 32, _ptr(sd), 48, _ptr(yd), float(p["dy_det"]), float(p["y_os"]),
+                         1, _ptr(idY), _ptr(Nv), int(p["tmp_size"]), 10, _ptr(cp), _ptr(sp),
+                         _ptr(cd), _ptr(sdt))
+    _lib.check_last()
+    assert np.array_equal(x, O.fan_adj_f32(Y, p))
+
+    pc = G.cone_para(16, 16, 16, 20, 18, 7, L=(2, 2, 2))
+    Xc = rng.standard_normal(16 ** 3).astype(np.float32)
+    yc = np.zeros(20 * 18 * 7, np.float32)
+    a = {k: np.ascontiguousarray(pc[k], np.float32) for k in ("sd_phi", "sd_z", "y_det", "z_det",
+                                                              "cos_phi", "sin_phi")}
+    idYc = np.asarray(pc["id_Y"]).T.reshape(-1).astype(np.int32); Nvc = pc["Nv"].astype(np.int32)
+    L.Ax_cone_mf_gpu_siddon(_ptr(Xc), _ptr(yc), _ptr(a["sd_phi"]), _ptr(a["sd_z"]),
+                            _ptr(a["y_det"]), _ptr(a["z_det"]), _ptr(idYc), _ptr(Nvc),
+                            float(pc["SO"]), float(pc["OD"]), float(pc["scale"]), float(pc["dz"]),
+                            16, 16, 16, 1, 20, 18, 7, int(pc["tmp_size"]), 4)
+    _lib.check_last()
+    assert np.array_equal(yc, O.cone_siddon_f32(Xc, pc))
+    Yc = rng.standard_normal(20 * 18 * 7).astype(np.float32)
+    xc = np.zeros(16 ** 3, np.float32)
+    L.Atx_cone_mf_gpu_new(_ptr(xc), _ptr(Yc), _ptr(a["cos_phi"]), _ptr(a["sin_phi"]),
+                          _ptr(a["sd_z"]), _ptr(a["y_det"]), _ptr(a["z_det"]), _ptr(idYc),
+                          _ptr(Nvc), float(pc["SO"]), float(pc["OD"]), float(pc["scale"]),
+                          float(pc["dy_det"]), float(pc["y_os"]), float(pc["dz_det"]),
+                          float(pc["dz"]), 16, 16, 16, 1, 20, 18, 7, int(pc["tmp_size"]), 4)
+    _lib.check_last()
+    assert np.array_equal(xc, O.cone_adj_f32(Yc, pc))
+
+
+def test_dropin_rejects_odd_siddon_sizes():
+    from framelab_gb300 import _lib
+    L = _lib.load()
+    p = G.fan_para(15, 15, 20, 3, L=(2, 2))
+    X = np.ones(15 * 15, np.float32); y = np.zeros(60, np.float32)
+    sd = p["sd_phi"].copy(); yd = p["y_det"].copy(); idx = np.zeros(3, np.int32)
+    L.Ax_fan_mf_gpu_siddon(_ptr(X), _ptr(y), float(p["SO"]), float(p["OD"]), float(p["scale"]),
+                           15, 15, 3, _ptr(sd), 20, _ptr(yd), _ptr(idx), 1)
+    assert L.fl_last_status() == _lib.FL_ERR_UNSUPPORTED
+    assert b"even" in L.fl_last_error()
+
+
+# --------------------------------------------------------------------------
+# matched Siddon pair
+# --------------------------------------------------------------------------
+def _cone_small(scan="circle"):
+    kw = dict(scan="helix", zmax=0.6, rps=1.0, vtab=1.0, fps=8) if scan == "helix" else {}
+    return G.cone_para_mm(32, 16, 48, 40, det_pitch_mm=8.0, SO_mm=600.0, SD_mm=1200.0,
+                          voxel_mm=8.0, **kw) if scan == "circle" else \
+        G.cone_para(32, 32, 32, 48, 40, 0, L=(2, 2, 2), **kw)
+
+
+def test_matched_fan_vs_fp64_and_reference():
+    p = G.fan_para(64, 64, 128, 90, L=(1.0, 1.0), SO=500.0, OD=500.0, Ly=2 * np.sqrt(2))
+    x = PH.ellipses_2d(64, seed=3).reshape(-1)
+    P = _plan(p)
+    y = _host(P.forward(_dev(x)))
+    e = O.exact_forward(x, p)
+    assert _rel(y, e) < 2e-6, _rel(y, e)
+    # SO = 32000 voxels: the reference's FP32 alpha (ulp 6e-8 times a 64000-voxel
+    # ray) is itself ~7e-5 from the exact answer; the matched pair (alpha centred
+    # on the isocentre) must be closer to the exact answer than the reference.
+    ref = O.fan_siddon_f32(x, p)
+    assert _rel(y, e) < 0.1 * _rel(ref, e)
+    assert _rel(y, ref) < 1.2 * _rel(ref, e)
+    rng = np.random.default_rng(0)
+    r = rng.standard_normal(y.size).astype(np.float32)
+    xa = _host(P.adjoint(_dev(r)))
+    assert _rel(xa, O.exact_adjoint(r, p)) < 1e-5
+
+
+@pytest.mark.parametrize("scan", ["circle", "helix"])
+def test_matched_cone_vs_fp64(scan):
+    p = _cone_small(scan)
+    n = int(p["nx"])
+    x = PH.ellipsoids_3d(n, seed=4).reshape(-1)
+    P = _plan(p)
+    y = _host(P.forward(_dev(x)))
+    e = O.exact_forward(x, p, threads=8)
+    assert _rel(y, e) < 5e-6, _rel(y, e)
+    rng = np.random.default_rng(1)
+    r = rng.standard_normal(y.size).astype(np.float32)
+    xa = _host(P.adjoint(_dev(r)))
+    ea = O.exact_adjoint(r, p, threads=8)
+    assert _rel(xa, ea) < 2e-5, _rel(xa, ea)
+
+
+def test_matched_cone_phantom_matches_reference_projector():
+    p = _cone_small("circle")
+    x = PH.ellipsoids_3d(int(p["nx"]), seed=9).reshape(-1)
+    y = _host(_plan(p).forward(_dev(x)))
+    ref = O.cone_siddon_f32(x, p, threads=8)
+    assert _rel(y, ref) < 1e-5, _rel(y, ref)
+
+
+@pytest.mark.parametrize("cone", [False, True])
+def test_matched_dot_product_identity(cone):
+    rng = np.random.default_rng(2)
+    p = _cone_small() if cone else G.fan_para(96, 96, 160, 120, L=(1, 1), SO=3.0, OD=3.0, Ly=3.0)
+    P = _plan(p)
+    x = rng.standard_normal(P.n_vox).astype(np.float32)
+    yv = rng.standard_normal(P.n_rays).astype(np.float32)
+    Ax = _host(P.forward(_dev(x)))
+    Aty = _host(P.adjoint(_dev(yv)))
+    lhs = np.dot(Ax.astype(np.float64), yv.astype(np.float64))
+    rhs = np.dot(x.astype(np.float64), Aty.astype(np.float64))
+    assert abs(lhs - rhs) / abs(lhs) < 1e-5, (lhs, rhs)
+
+
+def test_matched_counts_match_oracle():
+    p = _cone_small()
+    c = _host(_plan(p).count_intersections()).astype(np.int64)
+    e = O.exact_count(p)
+    mism = np.count_nonzero(c != e)
+    assert mism <= 1e-3 * c.size, mism
+    assert abs(c.sum() - e.sum()) <= 1e-4 * e.sum()
+
+
+@pytest.mark.parametrize("dt", ["float16", "bfloat16"])
+def test_matched_low_precision_storage(dt):
+    torch = _torch()
+    p = _cone_small()
+    x = PH.ellipsoids_3d(int(p["nx"]), seed=4).reshape(-1)
+    P = _plan(p)
+    tdt = getattr(torch, dt)
+    y = _host(P.forward(_dev(x, tdt), out_dtype=tdt))
+    e = O.exact_forward(x, p, threads=8)
+    tol = 2e-3 if dt == "float16" else 1.5e-2
+    assert _rel(y, e) < tol, _rel(y, e)
