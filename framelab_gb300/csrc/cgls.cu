@@ -1,0 +1,532 @@
+// cgls.cu -- CGLS on the normal equations (A^T A + lam I) u = b and the vector
+// algebra it needs (solveCGLS.m:6-31, ObjectData.objdot/plus/mtimes).
+//
+// Inner products and the step lengths alpha/beta are FP64. Two drivers:
+//  * FL_CGLS_PLAIN: FP32 storage, one kernel per vector operation, every
+//    scalar brought back to the host (the reference's loop, with the
+//    projector on the GPU).
+//  * FL_CGLS_MIXED: the search direction is also kept as scaled FP16 for the
+//    projector's gathers (FP32 accumulation along each ray); axpy/dot work is
+//    fused into three kernels that keep alpha, beta and gamma in device memory;
+//    one iteration is captured as a CUDA graph and replayed. Every `refresh`
+//    iterations the residual is recomputed in FP32 from u (r = (A^T A + lam) u - b).
+// Both stop early once gamma < tol, like the reference; in the graph this is a
+// device flag that turns the remaining replays into no-ops.
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "fl_common.cuh"
+#include "fl_plan.h"
+
+struct CgScalars {
+    double gamma;      // <r, r>
+    double alpha, beta;
+    double tol;
+    float lam;
+    float p_scale;     // p16 = p * p_scale
+    float p_unscale;   // 1 / p_scale (forward applies it to the gathered sum)
+    int done;          // 1 once gamma < tol
+    int iter;          // iterations completed
+    unsigned ticket;   // last-block detection for the fused reductions
+};
+
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block sum -> partials[blockIdx.x]; returns true in the block that arrives
+// last, after which `total` holds the sum of all partials (fixed order, so the
+// result is the same on every run).
+__device__ bool grid_sum(double v, double* partials, unsigned* ticket, double& total)
+{
+    __shared__ double sw[kThreads / 32];
+    __shared__ bool last;
+    v = warp_sum(v);
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) sw[w] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double b = 0.0;
+        for (int k = 0; k < kThreads / 32; k++) b += sw[k];
+        partials[blockIdx.x] = b;
+        __threadfence();
+        unsigned t = atomicAdd(ticket, 1u);
+        last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    double s = 0.0;
+    for (int k = threadIdx.x; k < (int)gridDim.x; k += kThreads) s += ((volatile double*)partials)[k];
+    s = warp_sum(s);
+    if (lane == 0) sw[w] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int k = 0; k < kThreads / 32; k++) t += sw[k];
+        total = t;
+        *ticket = 0u;
+    }
+    return true;
+}
+
+__global__ void __launch_bounds__(kThreads)
+k_dot(const float* __restrict__ a, const float* __restrict__ b, long long n,
+      double* __restrict__ partials, unsigned* ticket, double* out)
+{
+    double s = 0.0;
+    for (long long i = (long long)blockIdx.x * kThreads + threadIdx.x; i < n;
+         i += (long long)gridDim.x * kThreads)
+        s += (double)a[i] * (double)b[i];
+    double tot;
+    if (grid_sum(s, partials, ticket, tot) && threadIdx.x == 0) *out = tot;
+}
+
+// y = a*x + b*y (plain driver's building block)
+__global__ void k_axpby(float* __restrict__ y, const float* __restrict__ x, float a, float b,
+                        long long n)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        y[i] = a * x[i] + b * y[i];
+}
+
+// r = q - b (q may be null: r = -b); p = -r; gamma = <r, r>
+__global__ void __launch_bounds__(kThreads)
+k_cg_init(const float* __restrict__ bvec, const float* __restrict__ q, float* __restrict__ r,
+          float* __restrict__ p, long long n, CgScalars* S, double* partials)
+{
+    double s = 0.0;
+    for (long long i = (long long)blockIdx.x * kThreads + threadIdx.x; i < n;
+         i += (long long)gridDim.x * kThreads) {
+        float ri = (q ? q[i] : 0.0f) - bvec[i];
+        r[i] = ri;
+        p[i] = -ri;
+        s += (double)ri * ri;
+    }
+    double tot;
+    if (grid_sum(s, partials, &S->ticket, tot) && threadIdx.x == 0) {
+        S->gamma = tot;
+        S->done = 0;
+        S->iter = 0;
+        double rms = sqrt(tot / (double)n);
+        S->p_scale = rms > 0 ? (float)(1.0 / (8.0 * rms)) : 1.0f;
+        S->p_unscale = 1.0f / S->p_scale;
+    }
+}
+
+// p16 = p * p_scale
+__global__ void k_cg_p16(const float* __restrict__ p, __half* __restrict__ p16, long long n,
+                         const CgScalars* S)
+{
+    if (S->done) return;
+    float sc = S->p_scale;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        p16[i] = __float2half_rn(p[i] * sc);
+}
+
+// q += lam p ; alpha = gamma / <p, q>
+__global__ void __launch_bounds__(kThreads)
+k_cg_pq(const float* __restrict__ p, float* __restrict__ q, long long n, CgScalars* S,
+        double* partials)
+{
+    if (S->done) return;
+    float lam = S->lam;
+    double s = 0.0;
+    for (long long i = (long long)blockIdx.x * kThreads + threadIdx.x; i < n;
+         i += (long long)gridDim.x * kThreads) {
+        float pi = p[i];
+        float qi = fmaf(lam, pi, q[i]);
+        q[i] = qi;
+        s += (double)pi * qi;
+    }
+    double tot;
+    if (grid_sum(s, partials, &S->ticket, tot) && threadIdx.x == 0) S->alpha = S->gamma / tot;
+}
+
+// u += alpha p ; r += alpha q ; gamma' = <r, r> ; beta = gamma'/gamma ; stop test
+__global__ void __launch_bounds__(kThreads)
+k_cg_update(float* __restrict__ u, float* __restrict__ r, const float* __restrict__ p,
+            const float* __restrict__ q, long long n, CgScalars* S, double* partials,
+            double* hist, int hist_cap)
+{
+    if (S->done) return;
+    float a = (float)S->alpha;
+    double s = 0.0;
+    for (long long i = (long long)blockIdx.x * kThreads + threadIdx.x; i < n;
+         i += (long long)gridDim.x * kThreads) {
+        u[i] = fmaf(a, p[i], u[i]);
+        float ri = fmaf(a, q[i], r[i]);
+        r[i] = ri;
+        s += (double)ri * ri;
+    }
+    double tot;
+    if (grid_sum(s, partials, &S->ticket, tot) && threadIdx.x == 0) {
+        S->beta = tot / S->gamma;
+        S->gamma = tot;
+        if (hist && S->iter < hist_cap) hist[S->iter] = tot;
+        S->iter += 1;
+        double rms = sqrt(tot / (double)n);
+        S->p_scale = rms > 0 ? (float)(1.0 / (8.0 * rms)) : 1.0f;
+        S->p_unscale = 1.0f / S->p_scale;
+        if (tot < S->tol) S->done = 1;
+    }
+}
+
+// p = -r + beta p ; p16 = p * p_scale (mixed)
+__global__ void k_cg_dir(const float* __restrict__ r, float* __restrict__ p,
+                         __half* __restrict__ p16, long long n, const CgScalars* S)
+{
+    if (S->done) return;
+    float b = (float)S->beta, sc = S->p_scale;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        float pi = fmaf(b, p[i], -r[i]);
+        p[i] = pi;
+        if (p16) p16[i] = __float2half_rn(pi * sc);
+    }
+}
+
+// residual refresh: r = q - b, gamma = <r, r> (keeps p, beta)
+__global__ void __launch_bounds__(kThreads)
+k_cg_refresh(const float* __restrict__ bvec, const float* __restrict__ q, float* __restrict__ r,
+             long long n, CgScalars* S, double* partials)
+{
+    if (S->done) return;
+    double s = 0.0;
+    for (long long i = (long long)blockIdx.x * kThreads + threadIdx.x; i < n;
+         i += (long long)gridDim.x * kThreads) {
+        float ri = q[i] - bvec[i];
+        r[i] = ri;
+        s += (double)ri * ri;
+    }
+    double tot;
+    if (grid_sum(s, partials, &S->ticket, tot) && threadIdx.x == 0) S->gamma = tot;
+}
+
+int sm_count()
+{
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1)
+            n = 132;
+    }
+    return n;
+}
+
+unsigned grid_for(long long n)
+{
+    long long want = (n + kThreads - 1) / kThreads;
+    long long cap = 4LL * sm_count();
+    return (unsigned)(want < cap ? (want > 0 ? want : 1) : cap);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Shared scratch for the stand-alone FP64 dot product (per device, grown once)
+// ---------------------------------------------------------------------------
+namespace {
+struct DotScratch {
+    double* partials = nullptr;
+    unsigned* ticket = nullptr;
+    int cap = 0;
+};
+DotScratch g_dot[64];
+}
+
+extern "C" int fl_dot(const float* a, const float* b, int64_t n, double* out, void* stream)
+{
+    if (!a || !b || !out || n < 0) return fl_set_error(FL_ERR_INVALID, "fl_dot: bad argument");
+    int dev = 0;
+    FL_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return fl_set_error(FL_ERR_UNSUPPORTED, "device index %d", dev);
+    DotScratch& d = g_dot[dev];
+    unsigned g = grid_for(n);
+    if (d.cap < (int)g) {
+        if (d.partials) cudaFree(d.partials);
+        if (d.ticket) cudaFree(d.ticket);
+        d.partials = nullptr; d.ticket = nullptr; d.cap = 0;
+        FL_CUDA(cudaMalloc((void**)&d.partials, sizeof(double) * 4 * sm_count()));
+        FL_CUDA(cudaMalloc((void**)&d.ticket, sizeof(unsigned)));
+        FL_CUDA(cudaMemset(d.ticket, 0, sizeof(unsigned)));
+        d.cap = 4 * sm_count();
+    }
+    k_dot<<<g, kThreads, 0, (cudaStream_t)stream>>>(a, b, n, d.partials, d.ticket, out);
+    return fl_check_launch("fl_dot");
+}
+
+// ---------------------------------------------------------------------------
+// CGLS workspace
+// ---------------------------------------------------------------------------
+struct fl_cgls {
+    fl_plan* plan;
+    int mode;
+    long long n, nr;
+    float *r, *p, *q, *tmp;     // tmp: sinogram (C^2 W p in the mixed driver)
+    __half* p16;
+    CgScalars* S;
+    double* partials;
+    double* hist;
+    int hist_cap;
+    unsigned grid;
+    cudaStream_t cs;            // capture/replay stream
+    cudaEvent_t ev0, ev1;
+    cudaGraphExec_t exec;
+    bool captured;
+    const float* cap_u;         // pointers baked into the captured graph
+    float* cap_uw;
+    float *hb, *hu;             // device copies for the host-buffer entry point
+};
+
+static void cgls_free(fl_cgls* c)
+{
+    void* ptrs[] = {c->r, c->p, c->q, c->tmp, c->p16, c->S, c->partials, c->hist, c->hb, c->hu};
+    for (void* q : ptrs)
+        if (q) cudaFree(q);
+    if (c->exec) cudaGraphExecDestroy(c->exec);
+    if (c->cs) cudaStreamDestroy(c->cs);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+}
+
+extern "C" int fl_cgls_create(fl_plan* plan, int mode, fl_cgls** out)
+{
+    if (!plan || !out) return fl_set_error(FL_ERR_INVALID, "fl_cgls_create: null argument");
+    if (mode != FL_CGLS_PLAIN && mode != FL_CGLS_MIXED)
+        return fl_set_error(FL_ERR_INVALID, "unknown CGLS mode %d", mode);
+    int st = fl_matched_ready(plan);
+    if (st) return st;
+    *out = nullptr;
+    fl_cgls* c = new (std::nothrow) fl_cgls;
+    if (!c) return fl_set_error(FL_ERR_ALLOC, "out of host memory");
+    std::memset((void*)c, 0, sizeof *c);
+    c->plan = plan; c->mode = mode;
+    c->n = plan->n_vox; c->nr = plan->n_rays;
+    c->grid = grid_for(c->n);
+    c->hist_cap = 4096;
+    auto M = [&](void** ptr, size_t bytes) {
+        return st ? st : (st = fl_check_cuda(cudaMalloc(ptr, bytes), "cudaMalloc(cgls)"));
+    };
+    M((void**)&c->r, c->n * 4); M((void**)&c->p, c->n * 4); M((void**)&c->q, c->n * 4);
+    M((void**)&c->tmp, c->nr * 4);
+    if (mode == FL_CGLS_MIXED) M((void**)&c->p16, c->n * 2);
+    M((void**)&c->S, sizeof(CgScalars));
+    M((void**)&c->partials, sizeof(double) * c->grid);
+    M((void**)&c->hist, sizeof(double) * c->hist_cap);
+    if (!st) st = fl_check_cuda(cudaMemset(c->S, 0, sizeof(CgScalars)), "cudaMemset");
+    if (!st) st = fl_check_cuda(cudaStreamCreateWithFlags(&c->cs, cudaStreamNonBlocking), "stream");
+    if (!st) st = fl_check_cuda(cudaEventCreateWithFlags(&c->ev0, cudaEventDisableTiming), "event");
+    if (!st) st = fl_check_cuda(cudaEventCreateWithFlags(&c->ev1, cudaEventDisableTiming), "event");
+    if (st) { cgls_free(c); delete c; return st; }
+    *out = c;
+    return fl_set_error(FL_OK, "");
+}
+
+extern "C" void fl_cgls_destroy(fl_cgls* c)
+{
+    if (!c) return;
+    cgls_free(c);
+    delete c;
+}
+
+// q = (A^T A + lam I) x with FP32 storage (matched model)
+static int normal_apply(fl_cgls* c, const float* x, float* q, float lam, cudaStream_t s)
+{
+    fl_plan* P = c->plan;
+    int st;
+    if ((st = fl_matched_forward(P, x, FL_F32, c->tmp, FL_F32, 2, nullptr, nullptr, s))) return st;
+    if ((st = fl_matched_adjoint_w(P, c->tmp, q, FL_F32, nullptr, s))) return st;
+    if (lam != 0.0f) {
+        k_axpby<<<c->grid, kThreads, 0, s>>>(q, x, lam, 1.0f, c->n);
+        if ((st = fl_check_launch("normal_apply"))) return st;
+    }
+    return FL_OK;
+}
+
+extern "C" int fl_normal_apply(fl_plan* plan, const float* x, float* q, float lam, void* stream)
+{
+    if (!plan || !x || !q) return fl_set_error(FL_ERR_INVALID, "fl_normal_apply: null argument");
+    int st = fl_matched_ready(plan);
+    if (st) return st;
+    float* w;
+    if ((st = fl_plan_work(plan, &w))) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    if ((st = fl_matched_forward(plan, x, FL_F32, w, FL_F32, 2, nullptr, nullptr, s))) return st;
+    if ((st = fl_matched_adjoint_w(plan, w, q, FL_F32, nullptr, s))) return st;
+    if (lam != 0.0f) {
+        k_axpby<<<grid_for(plan->n_vox), kThreads, 0, s>>>(q, x, lam, 1.0f, plan->n_vox);
+        return fl_check_launch("fl_normal_apply");
+    }
+    return FL_OK;
+}
+
+static int plain_dot(fl_cgls* c, const float* a, const float* b, double* host, cudaStream_t s)
+{
+    int st = fl_dot(a, b, c->n, &c->S->alpha, s);   // S->alpha used as a scratch slot
+    if (st) return st;
+    FL_CUDA(cudaMemcpyAsync(host, &c->S->alpha, sizeof(double), cudaMemcpyDeviceToHost, s));
+    return fl_check_cuda(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+}
+
+static int solve_plain(fl_cgls* c, const float* b, float* u, float lam, int iters, double tol,
+                       int flags, double* hist, int* done_iters, cudaStream_t s)
+{
+    const long long n = c->n;
+    const unsigned g = c->grid;
+    int st;
+    // r = A_loc(u0) - b ; p = -r
+    if (!(flags & FL_CGLS_ZERO_START)) {
+        if ((st = normal_apply(c, u, c->q, lam, s))) return st;
+        FL_CUDA(cudaMemcpyAsync(c->r, c->q, n * 4, cudaMemcpyDeviceToDevice, s));
+        k_axpby<<<g, kThreads, 0, s>>>(c->r, b, -1.0f, 1.0f, n);
+    } else {
+        FL_CUDA(cudaMemsetAsync(c->r, 0, n * 4, s));
+        k_axpby<<<g, kThreads, 0, s>>>(c->r, b, -1.0f, 1.0f, n);
+    }
+    FL_CUDA(cudaMemsetAsync(c->p, 0, n * 4, s));
+    k_axpby<<<g, kThreads, 0, s>>>(c->p, c->r, -1.0f, 0.0f, n);
+    if ((st = fl_check_launch("cgls init"))) return st;
+    double gamma;
+    if ((st = plain_dot(c, c->r, c->r, &gamma, s))) return st;
+    int it = 0;
+    while (it < iters) {
+        it++;
+        if ((st = normal_apply(c, c->p, c->q, lam, s))) return st;
+        double pq;
+        if ((st = plain_dot(c, c->p, c->q, &pq, s))) return st;
+        float alpha = (float)(gamma / pq);
+        k_axpby<<<g, kThreads, 0, s>>>(u, c->p, alpha, 1.0f, n);
+        k_axpby<<<g, kThreads, 0, s>>>(c->r, c->q, alpha, 1.0f, n);
+        double gnew;
+        if ((st = plain_dot(c, c->r, c->r, &gnew, s))) return st;
+        float beta = (float)(gnew / gamma);
+        k_axpby<<<g, kThreads, 0, s>>>(c->p, c->r, -1.0f, beta, n);
+        if ((st = fl_check_launch("cgls iteration"))) return st;
+        gamma = gnew;
+        if (hist) hist[it - 1] = gnew;
+        if (gamma < tol) break;
+    }
+    if (done_iters) *done_iters = it;
+    return FL_OK;
+}
+
+// one mixed iteration: fwd(p16) -> tmp -> adj -> q ; fused updates
+static int mixed_iteration(fl_cgls* c, float* u, cudaStream_t s)
+{
+    fl_plan* P = c->plan;
+    CgScalars* S = c->S;
+    int st;
+    if ((st = fl_matched_forward(P, c->p16, FL_F16, c->tmp, FL_F32, 2, &S->done, &S->p_unscale, s)))
+        return st;
+    if ((st = fl_matched_adjoint_w(P, c->tmp, c->q, FL_F32, &S->done, s))) return st;
+    k_cg_pq<<<c->grid, kThreads, 0, s>>>(c->p, c->q, c->n, S, c->partials);
+    k_cg_update<<<c->grid, kThreads, 0, s>>>(u, c->r, c->p, c->q, c->n, S, c->partials, c->hist,
+                                             c->hist_cap);
+    k_cg_dir<<<c->grid, kThreads, 0, s>>>(c->r, c->p, c->p16, c->n, S);
+    return fl_check_launch("cgls mixed iteration");
+}
+
+static int solve_mixed(fl_cgls* c, const float* b, float* u, float lam, int iters, double tol,
+                       int refresh, int flags, double* hist, int* done_iters, cudaStream_t us)
+{
+    cudaStream_t s = c->cs;
+    int st;
+    FL_CUDA(cudaEventRecord(c->ev0, us));
+    FL_CUDA(cudaStreamWaitEvent(s, c->ev0, 0));
+    CgScalars init;
+    std::memset(&init, 0, sizeof init);
+    init.tol = tol; init.lam = lam;
+    FL_CUDA(cudaMemcpyAsync(c->S, &init, sizeof init, cudaMemcpyHostToDevice, s));
+    const float* q0 = nullptr;
+    if (!(flags & FL_CGLS_ZERO_START)) {
+        if ((st = normal_apply(c, u, c->q, lam, s))) return st;
+        q0 = c->q;
+    }
+    k_cg_init<<<c->grid, kThreads, 0, s>>>(b, q0, c->r, c->p, c->n, c->S, c->partials);
+    k_cg_p16<<<c->grid, kThreads, 0, s>>>(c->p, c->p16, c->n, c->S);
+    if ((st = fl_check_launch("cgls mixed init"))) return st;
+
+    if (!c->captured || c->cap_uw != u) {
+        if (c->exec) { cudaGraphExecDestroy(c->exec); c->exec = nullptr; }
+        cudaGraph_t g;
+        FL_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        int cst = mixed_iteration(c, u, s);
+        cudaError_t e = cudaStreamEndCapture(s, &g);
+        if (cst) return cst;
+        FL_CUDA(e);
+        e = cudaGraphInstantiate(&c->exec, g, 0);
+        cudaGraphDestroy(g);
+        FL_CUDA(e);
+        c->captured = true;
+        c->cap_uw = u;
+    }
+    for (int it = 0; it < iters; it++) {
+        FL_CUDA(cudaGraphLaunch(c->exec, s));
+        if (refresh > 0 && (it + 1) % refresh == 0 && it + 1 < iters) {
+            if ((st = normal_apply(c, u, c->q, lam, s))) return st;
+            k_cg_refresh<<<c->grid, kThreads, 0, s>>>(b, c->q, c->r, c->n, c->S, c->partials);
+            if ((st = fl_check_launch("cgls refresh"))) return st;
+        }
+    }
+    CgScalars fin;
+    FL_CUDA(cudaMemcpyAsync(&fin, c->S, sizeof fin, cudaMemcpyDeviceToHost, s));
+    std::vector<double> h(c->hist_cap);
+    int nh = iters < c->hist_cap ? iters : c->hist_cap;
+    if (hist && nh > 0)
+        FL_CUDA(cudaMemcpyAsync(h.data(), c->hist, sizeof(double) * nh, cudaMemcpyDeviceToHost, s));
+    FL_CUDA(cudaEventRecord(c->ev1, s));
+    FL_CUDA(cudaStreamWaitEvent(us, c->ev1, 0));
+    FL_CUDA(cudaStreamSynchronize(s));
+    if (hist) for (int k = 0; k < nh && k < fin.iter; k++) hist[k] = h[k];
+    if (done_iters) *done_iters = fin.iter;
+    return FL_OK;
+}
+
+extern "C" int fl_cgls_solve(fl_cgls* c, const float* b, float* u, float lam, int iters,
+                             double tol, int refresh, int flags, double* gamma_history,
+                             int* iters_done, void* stream)
+{
+    if (!c || !b || !u || iters < 0)
+        return fl_set_error(FL_ERR_INVALID, "fl_cgls_solve: bad argument");
+    int st = (c->mode == FL_CGLS_PLAIN)
+                 ? solve_plain(c, b, u, lam, iters, tol, flags, gamma_history, iters_done,
+                               (cudaStream_t)stream)
+                 : solve_mixed(c, b, u, lam, iters, tol, refresh, flags, gamma_history, iters_done,
+                               (cudaStream_t)stream);
+    if (st) return st;
+    return fl_set_error(FL_OK, "");
+}
+
+extern "C" int fl_cgls_solve_host(fl_cgls* c, const float* b_host, float* u_host, float lam,
+                                  int iters, double tol, int refresh, int flags,
+                                  double* gamma_history, int* iters_done, void* stream)
+{
+    if (!c || !b_host || !u_host || iters < 0)
+        return fl_set_error(FL_ERR_INVALID, "fl_cgls_solve_host: bad argument");
+    cudaStream_t s = (cudaStream_t)stream;
+    size_t bytes = (size_t)c->n * sizeof(float);
+    if (!c->hb) FL_CUDA(cudaMalloc((void**)&c->hb, bytes));
+    if (!c->hu) FL_CUDA(cudaMalloc((void**)&c->hu, bytes));
+    FL_CUDA(cudaMemcpyAsync(c->hb, b_host, bytes, cudaMemcpyHostToDevice, s));
+    if (!(flags & FL_CGLS_ZERO_START))
+        FL_CUDA(cudaMemcpyAsync(c->hu, u_host, bytes, cudaMemcpyHostToDevice, s));
+    else
+        FL_CUDA(cudaMemsetAsync(c->hu, 0, bytes, s));
+    int st = fl_cgls_solve(c, c->hb, c->hu, lam, iters, tol, refresh, flags, gamma_history,
+                           iters_done, stream);
+    if (st) return st;
+    FL_CUDA(cudaMemcpyAsync(u_host, c->hu, bytes, cudaMemcpyDeviceToHost, s));
+    return fl_check_cuda(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+}

@@ -50,8 +50,14 @@ struct fl_plan {
 // internal launchers
 int fl_ref_forward(fl_plan* p, const float* x, float* y, cudaStream_t st);
 int fl_ref_adjoint(fl_plan* p, const float* y, float* x, cudaStream_t st);
+// skip: optional device flag; when *skip != 0 the kernels return at once
+// (lets a captured CGLS iteration become a no-op after convergence).
+// xscale: optional device factor applied to the gathered sum (scaled storage).
 int fl_matched_forward(fl_plan* p, const void* x, int xt, void* y, int yt, int cr_power,
-                       cudaStream_t st);
+                       const int* skip, const float* xscale, cudaStream_t st);
 int fl_matched_weight(fl_plan* p, const void* y, int yt, float* yw, cudaStream_t st);
-int fl_matched_adjoint_w(fl_plan* p, const float* yw, void* x, int xt, cudaStream_t st);
+int fl_matched_adjoint_w(fl_plan* p, const float* yw, void* x, int xt, const int* skip,
+                         cudaStream_t st);
+int fl_plan_work(fl_plan* p, float** w);
+int fl_matched_ready(fl_plan* p);
 int fl_matched_count(fl_plan* p, int32_t* counts, cudaStream_t st);

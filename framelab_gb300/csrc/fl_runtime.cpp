@@ -290,7 +290,7 @@ static int check_dtype(int t)
     return FL_OK;
 }
 
-static int matched_ready(fl_plan* p)
+int fl_matched_ready(fl_plan* p)
 {
     const fl_scan& s = p->s;
     double r = std::sqrt(0.25 * s.nx * s.nx + 0.25 * s.ny * s.ny) + 1.0;
@@ -313,14 +313,14 @@ extern "C" int fl_forward(fl_plan* p, int model, const void* x, int xt, void* y,
         return fl_ref_forward(p, (const float*)x, (float*)y, sm);
     }
     if (model == FL_MODEL_MATCHED) {
-        if ((st = matched_ready(p))) return st;
-        return fl_matched_forward(p, x, xt, y, yt, 1, sm);
+        if ((st = fl_matched_ready(p))) return st;
+        return fl_matched_forward(p, x, xt, y, yt, 1, nullptr, nullptr, sm);
     }
     return fl_set_error(FL_ERR_UNSUPPORTED, "fl_forward: model %d not available", model);
 }
 
 // scratch for the pre-weighted adjoint input, owned by the plan
-static int plan_work(fl_plan* p, float** w)
+int fl_plan_work(fl_plan* p, float** w)
 {
     size_t need = (size_t)p->n_rays;
     if (p->work_elems < need) {
@@ -349,16 +349,16 @@ extern "C" int fl_adjoint(fl_plan* p, int model, const void* y, int yt, void* x,
         return fl_ref_adjoint(p, (const float*)y, (float*)x, sm);
     }
     if (model == FL_MODEL_MATCHED) {
-        if ((st = matched_ready(p))) return st;
+        if ((st = fl_matched_ready(p))) return st;
         if (p->det_kind < 0)
             return fl_set_error(FL_ERR_UNSUPPORTED,
                                 "matched adjoint needs a uniform flat or equiangular detector");
         if (p->det_kind == 1 && p->s.ndim == 3)
             return fl_set_error(FL_ERR_UNSUPPORTED, "equiangular detector is fan-beam only");
         float* w;
-        if ((st = plan_work(p, &w))) return st;
+        if ((st = fl_plan_work(p, &w))) return st;
         if ((st = fl_matched_weight(p, y, yt, w, sm))) return st;
-        return fl_matched_adjoint_w(p, w, x, xt, sm);
+        return fl_matched_adjoint_w(p, w, x, xt, nullptr, sm);
     }
     return fl_set_error(FL_ERR_UNSUPPORTED, "fl_adjoint: model %d not available", model);
 }
@@ -366,7 +366,7 @@ extern "C" int fl_adjoint(fl_plan* p, int model, const void* y, int yt, void* x,
 extern "C" int fl_count_intersections(fl_plan* p, int32_t* counts, void* stream)
 {
     if (!p || !counts) return fl_set_error(FL_ERR_INVALID, "null argument");
-    int st = matched_ready(p);
+    int st = fl_matched_ready(p);
     if (st) return st;
     return fl_matched_count(p, counts, (cudaStream_t)stream);
 }

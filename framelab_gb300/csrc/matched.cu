@@ -108,8 +108,10 @@ __global__ void __launch_bounds__(128)
 k_fwd_cone(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restrict__ col,
            const float* __restrict__ colr, const RowEntry* __restrict__ row,
            const int* __restrict__ vframe, int nx, int ny, int nz, int na, int nb,
-           long long nper, float scale, int cr_power)
+           long long nper, float scale, int cr_power, const int* __restrict__ skip,
+           const float* __restrict__ xscale)
 {
+    if (skip && *skip) return;
     int ia = blockIdx.x * 32 + threadIdx.x;
     int ib = blockIdx.y * 4 + threadIdx.y;
     int iv = blockIdx.z;
@@ -120,6 +122,7 @@ k_fwd_cone(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restr
     float acc = walk<TX, true, false>(x, ce.inv_x, ce.off_x, ce.inv_y, ce.off_y, re.inv_z,
                                       re.off_z, nx, ny, nz, nullptr);
     float cr = ray_cr(scale, colr[(long long)iv * na + ia], re.dz2);
+    if (xscale) acc *= *xscale;
     float out = cr * acc;
     if (cr_power == 2) out = cr * out;
     Store<TY>::st(y + ((long long)iv * nb + ib) * na + ia, out);
@@ -129,8 +132,10 @@ template <typename TX, typename TY>
 __global__ void __launch_bounds__(128)
 k_fwd_fan(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restrict__ col,
           const float* __restrict__ colr, const int* __restrict__ vframe, int nx, int ny,
-          int na, int nv, long long nper, float scale, int cr_power)
+          int na, int nv, long long nper, float scale, int cr_power,
+          const int* __restrict__ skip, const float* __restrict__ xscale)
 {
+    if (skip && *skip) return;
     long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= (long long)na * nv) return;
     int iv = (int)(r / na);
@@ -139,6 +144,7 @@ k_fwd_fan(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restri
     float acc = walk<TX, false, false>(x, ce.inv_x, ce.off_x, ce.inv_y, ce.off_y, 0.0f, 0.0f,
                                        nx, ny, 1, nullptr);
     float cr = ray_cr(scale, colr[r], 0.0f);
+    if (xscale) acc *= *xscale;
     float out = cr * acc;
     if (cr_power == 2) out = cr * out;
     Store<TY>::st(y + r, out);
@@ -228,8 +234,10 @@ template <typename TX>
 __global__ void __launch_bounds__(128)
 k_adj_fan(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __restrict__ col,
           const ViewEntry* __restrict__ view, const int* __restrict__ idY,
-          const int* __restrict__ Nv, int tmp_size, DetGrid G, int nx, int ny, int na)
+          const int* __restrict__ Nv, int tmp_size, DetGrid G, int nx, int ny, int na,
+          const int* __restrict__ skip)
 {
+    if (skip && *skip) return;
     int ix = blockIdx.x * blockDim.x + threadIdx.x;
     int iy = blockIdx.y;
     int it = blockIdx.z;
@@ -271,8 +279,10 @@ __global__ void __launch_bounds__(128)
 k_adj_cone(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __restrict__ col,
            const RowEntry* __restrict__ row, const ViewEntry* __restrict__ view,
            const int* __restrict__ idY, const int* __restrict__ Nv, int tmp_size, DetGrid G,
-           int nx, int ny, int nz, int na, int nb, float dz, int zruns)
+           int nx, int ny, int nz, int na, int nb, float dz, int zruns,
+           const int* __restrict__ skip)
 {
+    if (skip && *skip) return;
     __shared__ float sacc[TZ][128];
     const int tid = threadIdx.y * 32 + threadIdx.x;
     const int ix = blockIdx.x * 32 + threadIdx.x;
@@ -347,32 +357,34 @@ DetGrid det_grid(const fl_plan* p)
 }
 
 template <typename TX, typename TY>
-void launch_fwd(fl_plan* p, const void* x, void* y, int cr_power, cudaStream_t st)
+void launch_fwd(fl_plan* p, const void* x, void* y, int cr_power, const int* skip,
+                const float* xscale, cudaStream_t st)
 {
     const fl_scan& s = p->s;
     if (s.ndim == 3) {
         dim3 grid(fl_div_up(s.na, 32), fl_div_up(s.nb, 4), s.nv);
         k_fwd_cone<TX, TY><<<grid, dim3(32, 4), 0, st>>>(
             (const TX*)x, (TY*)y, p->d_col, p->d_colr, p->d_row, p->d_view_frame, s.nx, s.ny,
-            s.nz, s.na, s.nb, p->n_vox_frame, s.scale, cr_power);
+            s.nz, s.na, s.nb, p->n_vox_frame, s.scale, cr_power, skip, xscale);
     } else {
         long long nr = (long long)s.na * s.nv;
         k_fwd_fan<TX, TY><<<fl_div_up(nr, 128), 128, 0, st>>>(
             (const TX*)x, (TY*)y, p->d_col, p->d_colr, p->d_view_frame, s.nx, s.ny, s.na, s.nv,
-            p->n_vox_frame, s.scale, cr_power);
+            p->n_vox_frame, s.scale, cr_power, skip, xscale);
     }
 }
 
 template <typename TX>
-void launch_fwd_y(fl_plan* p, const void* x, void* y, int yt, int cr_power, cudaStream_t st)
+void launch_fwd_y(fl_plan* p, const void* x, void* y, int yt, int cr_power, const int* skip,
+                  const float* xscale, cudaStream_t st)
 {
-    if (yt == FL_F32) launch_fwd<TX, float>(p, x, y, cr_power, st);
-    else if (yt == FL_F16) launch_fwd<TX, __half>(p, x, y, cr_power, st);
-    else launch_fwd<TX, __nv_bfloat16>(p, x, y, cr_power, st);
+    if (yt == FL_F32) launch_fwd<TX, float>(p, x, y, cr_power, skip, xscale, st);
+    else if (yt == FL_F16) launch_fwd<TX, __half>(p, x, y, cr_power, skip, xscale, st);
+    else launch_fwd<TX, __nv_bfloat16>(p, x, y, cr_power, skip, xscale, st);
 }
 
 template <typename TX>
-void launch_adj(fl_plan* p, const float* yw, void* x, cudaStream_t st)
+void launch_adj(fl_plan* p, const float* yw, void* x, const int* skip, cudaStream_t st)
 {
     const fl_scan& s = p->s;
     DetGrid G = det_grid(p);
@@ -382,22 +394,22 @@ void launch_adj(fl_plan* p, const float* yw, void* x, cudaStream_t st)
         dim3 grid(fl_div_up(s.nx, 32), fl_div_up(s.ny, 4), (unsigned)zruns * s.nt);
         k_adj_cone<TX, TZ><<<grid, dim3(32, 4), 0, st>>>(
             (TX*)x, yw, p->d_col, p->d_row, p->d_view, p->d_idY, p->d_Nv, p->tmp_size, G, s.nx,
-            s.ny, s.nz, s.na, s.nb, s.dz, zruns);
+            s.ny, s.nz, s.na, s.nb, s.dz, zruns, skip);
     } else {
         dim3 grid(fl_div_up(s.nx, 128), s.ny, s.nt);
         k_adj_fan<TX><<<grid, 128, 0, st>>>((TX*)x, yw, p->d_col, p->d_view, p->d_idY,
-                                             p->d_Nv, p->tmp_size, G, s.nx, s.ny, s.na);
+                                             p->d_Nv, p->tmp_size, G, s.nx, s.ny, s.na, skip);
     }
 }
 
 }  // namespace
 
 int fl_matched_forward(fl_plan* p, const void* x, int xt, void* y, int yt, int cr_power,
-                       cudaStream_t st)
+                       const int* skip, const float* xscale, cudaStream_t st)
 {
-    if (xt == FL_F32) launch_fwd_y<float>(p, x, y, yt, cr_power, st);
-    else if (xt == FL_F16) launch_fwd_y<__half>(p, x, y, yt, cr_power, st);
-    else launch_fwd_y<__nv_bfloat16>(p, x, y, yt, cr_power, st);
+    if (xt == FL_F32) launch_fwd_y<float>(p, x, y, yt, cr_power, skip, xscale, st);
+    else if (xt == FL_F16) launch_fwd_y<__half>(p, x, y, yt, cr_power, skip, xscale, st);
+    else launch_fwd_y<__nv_bfloat16>(p, x, y, yt, cr_power, skip, xscale, st);
     return fl_check_launch("matched forward");
 }
 
@@ -419,11 +431,12 @@ int fl_matched_weight(fl_plan* p, const void* y, int yt, float* yw, cudaStream_t
     return fl_check_launch("matched adjoint weighting");
 }
 
-int fl_matched_adjoint_w(fl_plan* p, const float* yw, void* x, int xt, cudaStream_t st)
+int fl_matched_adjoint_w(fl_plan* p, const float* yw, void* x, int xt, const int* skip,
+                         cudaStream_t st)
 {
-    if (xt == FL_F32) launch_adj<float>(p, yw, x, st);
-    else if (xt == FL_F16) launch_adj<__half>(p, yw, x, st);
-    else launch_adj<__nv_bfloat16>(p, yw, x, st);
+    if (xt == FL_F32) launch_adj<float>(p, yw, x, skip, st);
+    else if (xt == FL_F16) launch_adj<__half>(p, yw, x, skip, st);
+    else launch_adj<__nv_bfloat16>(p, yw, x, skip, st);
     return fl_check_launch("matched adjoint");
 }
 

@@ -146,6 +146,46 @@ int fl_adjoint(fl_plan *plan, int model, const void *y, int y_dtype, void *x, in
 /* Number of voxels each ray crosses with positive length (matched model). */
 int fl_count_intersections(fl_plan *plan, int32_t *counts, void *stream);
 
+/* ------------------------------------------------------------------------ */
+/* Vector algebra and CGLS (solveCGLS.m:6-31, ObjectData.m:96-125)           */
+/* ------------------------------------------------------------------------ */
+
+/* *out (device double) = sum a[i]*b[i], accumulated in FP64. Replaces
+ * ObjectData.objdot (ObjectData.m:118-121). Uses a per-device scratch buffer
+ * allocated on first use; calls that overlap on the GPU (different streams)
+ * must not share a device. */
+int fl_dot(const float *a, const float *b, int64_t n, double *out, void *stream);
+
+/* q = (A^T A + lam I) x for the matched model, FP32 (the operator
+ * A_loc of solveCGLS.m:7). x, q: n_vox device floats. */
+int fl_normal_apply(fl_plan *plan, const float *x, float *q, float lam, void *stream);
+
+typedef struct fl_cgls fl_cgls;
+enum { FL_CGLS_PLAIN = 0, FL_CGLS_MIXED = 1 };
+enum { FL_CGLS_ZERO_START = 1 };   /* u0 == 0: skip the initial A_loc(u0) */
+
+/* CGLS workspace bound to a plan (matched model). Allocates r, p, q, a
+ * sinogram temporary (and an FP16 copy of p in FL_CGLS_MIXED). */
+int fl_cgls_create(fl_plan *plan, int mode, fl_cgls **cg);
+void fl_cgls_destroy(fl_cgls *cg);
+
+/* Solve (A^T A + lam I) u = b by CGLS (Optimizers.CGLS/solveCGLS): u holds
+ * u0 on entry and the result on return; at most `iters` iterations, stop once
+ * gamma = <r,r> < tol. FL_CGLS_MIXED recomputes the FP32 residual every
+ * `refresh` iterations (0 = never). gamma_history (host, optional, >= iters
+ * doubles) receives gamma after each iteration; *iters_done the count.
+ * Returns when the result is in u (the call synchronises with `stream`). */
+int fl_cgls_solve(fl_cgls *cg, const float *b, float *u, float lam, int iters, double tol,
+                  int refresh, int flags, double *gamma_history, int *iters_done,
+                  void *stream);
+
+/* The same solve with host buffers (the mex-style boundary): b and u0 are
+ * copied to the device (u0 skipped with FL_CGLS_ZERO_START), the result is
+ * copied back into u. Device copies are kept in the workspace for reuse. */
+int fl_cgls_solve_host(fl_cgls *cg, const float *b_host, float *u_host, float lam, int iters,
+                       double tol, int refresh, int flags, double *gamma_history,
+                       int *iters_done, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
