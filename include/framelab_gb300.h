@@ -146,6 +146,21 @@ int fl_adjoint(fl_plan *plan, int model, const void *y, int y_dtype, void *x, in
 /* Number of voxels each ray crosses with positive length (matched model). */
 int fl_count_intersections(fl_plan *plan, int32_t *counts, void *stream);
 
+/* No counterpart in the reference. The matched-model backprojection of
+ * fl_adjoint without any device allocation, for callers that cannot call
+ * cudaMalloc when they backproject: work being captured into a CUDA graph, a
+ * host application whose own pool allocator owns the GPU's memory, a loop
+ * that must not block on the allocator. The sinogram pre-weighting scratch
+ * that fl_adjoint allocates in the plan is instead a fixed array of
+ * FL_ADJOINT_NOALLOC_MAX_RAYS floats (8 MiB) inside the library, held on every
+ * GPU that loads it until the process exits; plans with more rays are refused
+ * with FL_ERR_INVALID. The first call on each device looks up that array's
+ * device address once (make it before any stream capture). All calls share the
+ * array: calls that can overlap on the GPU race and must be serialised. */
+#define FL_ADJOINT_NOALLOC_MAX_RAYS (1 << 21)
+int fl_adjoint_noalloc(fl_plan *plan, const void *y, int y_dtype, void *x, int x_dtype,
+                       void *stream);
+
 /* ------------------------------------------------------------------------ */
 /* Vector algebra and CGLS (solveCGLS.m:6-31, ObjectData.m:96-125)           */
 /* ------------------------------------------------------------------------ */
