@@ -117,6 +117,14 @@ static int build_tables(fl_plan* p, const std::vector<float>& phi, const float* 
             row[(size_t)iv * s.nb + ib] = r;
         }
     }
+    // every crossing parameter the kernels read must be finite
+    for (const ColEntry& e : col)
+        if (!std::isfinite(e.inv_x) || !std::isfinite(e.off_x) || !std::isfinite(e.inv_y) ||
+            !std::isfinite(e.off_y))
+            return fl_set_error(FL_ERR_INVALID, "geometry gives a non-finite ray parameter");
+    for (const RowEntry& r : row)
+        if (!std::isfinite(r.inv_z) || !std::isfinite(r.off_z) || !std::isfinite(r.rinv_z))
+            return fl_set_error(FL_ERR_INVALID, "geometry gives a non-finite ray parameter");
     int st;
     if ((st = upload(&p->d_col, col.data(), col.size()))) return st;
     if ((st = upload(&p->d_colr, colr.data(), colr.size()))) return st;
@@ -137,9 +145,9 @@ static int build_tables(fl_plan* p, const std::vector<float>& phi, const float* 
             eflat = std::fmax(eflat, std::fabs(y_det[ia] - (u0 + ia * du)));
             earc = std::fmax(earc, std::fabs(std::atan2((double)y_det[ia], SD) - (g0 + ia * dg)));
         }
-        if (du != 0 && eflat <= 0.05 * std::fabs(du)) {
+        if (du != 0 && eflat <= 0.005 * std::fabs(du)) {
             p->det_kind = 0; p->u0 = (float)u0; p->du = (float)du;
-        } else if (dg != 0 && earc <= 0.05 * std::fabs(dg)) {
+        } else if (dg != 0 && earc <= 0.005 * std::fabs(dg)) {
             p->det_kind = 1; p->g0 = (float)g0; p->dg = (float)dg;
         }
     }
@@ -151,7 +159,7 @@ static int build_tables(fl_plan* p, const std::vector<float>& phi, const float* 
             double e = 0;
             for (int ib = 0; ib < s.nb; ib++)
                 e = std::fmax(e, std::fabs(z_det[ib] - (z_det[0] + ib * dv)));
-            if (dv == 0 || e > 0.05 * std::fabs(dv)) p->det_kind = -2;   // irregular rows
+            if (dv == 0 || e > 0.005 * std::fabs(dv)) p->det_kind = -2;   // irregular rows
             else p->dv = (float)dv;
         }
     }
@@ -169,6 +177,8 @@ extern "C" int fl_plan_create(const fl_scan* scan, fl_plan** out)
     if (s.nt < 1) s.nt = 1;
     if (s.nx < 1 || s.ny < 1 || s.nz < 1 || s.nv < 1 || s.na < 1 || s.nb < 1)
         return fl_set_error(FL_ERR_INVALID, "sizes must be positive");
+    if ((int64_t)s.nx * s.ny * s.nz >= (int64_t)1 << 31)
+        return fl_set_error(FL_ERR_UNSUPPORTED, "a frame must hold fewer than 2^31 voxels");
     if (!(s.SO > 0) || !(s.OD > -s.SO) || !(s.scale > 0) || !(s.dz > 0))
         return fl_set_error(FL_ERR_INVALID, "SO, SO+OD, scale and dz must be positive");
     if ((!s.sd_phi && !(s.cos_phi && s.sin_phi)) || !s.y_det || (s.ndim == 3 && !s.z_det))

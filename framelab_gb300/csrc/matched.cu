@@ -42,6 +42,11 @@ __device__ __forceinline__ int start_slab(float a, float inv, float off, int n)
 
 // Walk one ray through an nx*ny*nz volume (nz == 1 with no z axis for 2-D).
 // Returns sum over voxels of w * x; *nseg counts segments with w > 0.
+// Termination: every step advances at least one axis to a strictly larger
+// crossing (consecutive FP32 crossings of one axis are thousands of ulps
+// apart for any table fl_plan_create accepts), and the loop leaves as soon as
+// the crossing reaches the exit (or is NaN); the step budget nx+ny+nz+4 is a
+// second, independent bound.
 template <typename TX, bool THREE, bool COUNT>
 __device__ __forceinline__ float walk(const TX* __restrict__ x, float inv_x, float off_x,
                                       float inv_y, float off_y, float inv_z, float off_z,
@@ -51,45 +56,52 @@ __device__ __forceinline__ float walk(const TX* __restrict__ x, float inv_x, flo
     float ay0 = fmaf(0.0f, inv_y, off_y), ay1 = fmaf((float)ny, inv_y, off_y);
     float a_in = fmaxf(fminf(ax0, ax1), fminf(ay0, ay1));
     float a_out = fminf(fmaxf(ax0, ax1), fmaxf(ay0, ay1));
-    float az0 = 0.0f, az1 = 0.0f;
     if (THREE) {
-        az0 = fmaf(0.0f, inv_z, off_z); az1 = fmaf((float)nz, inv_z, off_z);
+        float az0 = fmaf(0.0f, inv_z, off_z), az1 = fmaf((float)nz, inv_z, off_z);
         a_in = fmaxf(a_in, fminf(az0, az1));
         a_out = fminf(a_out, fmaxf(az0, az1));
     }
-    if (!(a_in < a_out)) return 0.0f;
-    int jx = start_slab(a_in, inv_x, off_x, nx);
-    int jy = start_slab(a_in, inv_y, off_y, ny);
-    int jz = THREE ? start_slab(a_in, inv_z, off_z, nz) : 0;
-    const long long sy = nx, sz = (long long)nx * ny;
-    long long v = (long long)jz * sz + (long long)jy * sy + jx;
-    float pax = (inv_x > 0.0f) ? (float)(jx + 1) : (float)jx;
-    float pay = (inv_y > 0.0f) ? (float)(jy + 1) : (float)jy;
-    float paz = (inv_z > 0.0f) ? (float)(jz + 1) : (float)jz;
-    const float stx = (inv_x > 0.0f) ? 1.0f : -1.0f;
-    const float sty = (inv_y > 0.0f) ? 1.0f : -1.0f;
-    const float stz = (inv_z > 0.0f) ? 1.0f : -1.0f;
-    const long long dvx = (inv_x > 0.0f) ? 1 : -1;
-    const long long dvy = (inv_y > 0.0f) ? sy : -sy;
-    const long long dvz = (inv_z > 0.0f) ? sz : -sz;
+    if (!(a_in < a_out)) { if (COUNT) *nseg = 0; return 0.0f; }
+    const int jx = start_slab(a_in, inv_x, off_x, nx);
+    const int jy = start_slab(a_in, inv_y, off_y, ny);
+    const int jz = THREE ? start_slab(a_in, inv_z, off_z, nz) : 0;
+    int v = (jz * ny + jy) * nx + jx;              // < 2^31 (checked at plan creation)
+    const bool px = inv_x > 0.0f, py = inv_y > 0.0f, pz = inv_z > 0.0f;
+    float pax = (float)(px ? jx + 1 : jx);
+    float pay = (float)(py ? jy + 1 : jy);
+    float paz = (float)(pz ? jz + 1 : jz);
+    const float stx = px ? 1.0f : -1.0f, sty = py ? 1.0f : -1.0f, stz = pz ? 1.0f : -1.0f;
+    const int dvx = px ? 1 : -1, dvy = py ? nx : -nx, dvz = pz ? nx * ny : -(nx * ny);
+    float nAx = fmaf(pax, inv_x, off_x);
+    float nAy = fmaf(pay, inv_y, off_y);
+    float nAz = THREE ? fmaf(paz, inv_z, off_z) : 3.0e38f;
     float cur = a_in, acc = 0.0f;
     int cnt = 0;
-    const int maxit = nx + ny + (THREE ? nz : 0) + 3;   // every step crosses >= 1 plane
-    for (int it = 0; it < maxit; ++it) {
-        float nAx = fmaf(pax, inv_x, off_x);
-        float nAy = fmaf(pay, inv_y, off_y);
-        float nxt = fminf(nAx, nAy);
-        float nAz = 0.0f;
-        if (THREE) { nAz = fmaf(paz, inv_z, off_z); nxt = fminf(nxt, nAz); }
-        float seg = nxt - cur;
-        if (COUNT) cnt += (seg > 0.0f);
-        else acc = fmaf(seg, ldv(x + v), acc);
-        if (nxt >= a_out) break;
-        if (nAx == nxt) { pax += stx; v += dvx; }
-        if (nAy == nxt) { pay += sty; v += dvy; }
-        if (THREE && nAz == nxt) { paz += stz; v += dvz; }
-        cur = nxt;
+    // the gather of the next voxel is issued as soon as its index is known and
+    // consumed one step later, so its latency overlaps the next step's compares
+    float xv = COUNT ? 0.0f : ldv(x + v);
+    const int budget = nx + ny + (THREE ? nz : 0) + 4;
+    for (int it = 0; it < budget; it += 4) {
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const float nxt = THREE ? fminf(fminf(nAx, nAy), nAz) : fminf(nAx, nAy);
+            const float seg = nxt - cur;
+            const bool cont = nxt < a_out;          // false at the exit (and for NaN)
+            float xn = 0.0f;
+            if (cont) {
+                if (nAx == nxt) { pax += stx; v += dvx; nAx = fmaf(pax, inv_x, off_x); }
+                if (nAy == nxt) { pay += sty; v += dvy; nAy = fmaf(pay, inv_y, off_y); }
+                if (THREE && nAz == nxt) { paz += stz; v += dvz; nAz = fmaf(paz, inv_z, off_z); }
+                if (!COUNT) xn = ldv(x + v);        // v is inside the volume here
+            }
+            if (COUNT) cnt += (seg > 0.0f);
+            else acc = fmaf(seg, xv, acc);
+            if (!cont) goto done;
+            xv = xn;
+            cur = nxt;
+        }
     }
+done:
     if (COUNT) *nseg = cnt;
     return acc;
 }
@@ -104,7 +116,7 @@ __device__ __forceinline__ float ray_cr(float scale, float dxy2, float dz2)
 // view, so a warp's rays are neighbours and their gathers share cache lines.
 // ---------------------------------------------------------------------------
 template <typename TX, typename TY>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, 8)
 k_fwd_cone(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restrict__ col,
            const float* __restrict__ colr, const RowEntry* __restrict__ row,
            const int* __restrict__ vframe, int nx, int ny, int nz, int na, int nb,
@@ -129,7 +141,7 @@ k_fwd_cone(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restr
 }
 
 template <typename TX, typename TY>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, 8)
 k_fwd_fan(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restrict__ col,
           const float* __restrict__ colr, const int* __restrict__ vframe, int nx, int ny,
           int na, int nv, long long nper, float scale, int cr_power,
@@ -222,8 +234,11 @@ __device__ __forceinline__ void column_window(const DetGrid& G, float c, float s
     if (G.kind == 0) { f0 = (umin - G.u0) / G.du; f1 = (umax - G.u0) / G.du; }
     else             { f0 = (umin - G.g0) / G.dg; f1 = (umax - G.g0) / G.dg; }
     if (f0 > f1) { float t = f0; f0 = f1; f1 = t; }
-    f0 = fmaxf(floorf(f0) - 1.0f, 0.0f);
-    f1 = fminf(ceilf(f1) + 1.0f, (float)(na - 1));
+    // the rays of columns whose detector position lies in the shadow [f0, f1];
+    // 0.02 column of slack covers the float evaluation and the tolerance
+    // fl_plan_create allows between y_det and the uniform grid
+    f0 = fmaxf(ceilf(f0 - 0.02f), 0.0f);
+    f1 = fminf(floorf(f1 + 0.02f), (float)(na - 1));
     lo = (int)f0; hi = (int)f1;                   // empty when lo > hi
 }
 
@@ -267,15 +282,17 @@ k_adj_fan(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __re
 }
 
 // ---------------------------------------------------------------------------
-// Cone adjoint: one thread per voxel column (ix, iy) and a run of TZ voxels
-// in z; block (32, 4). Per view and candidate detector column the thread
-// forms the column's xy crossing interval once, then visits only the detector
-// rows -- and for each row only the z voxels -- that the ray can cross inside
-// that interval. Per-thread accumulators live in shared memory so the z run
-// can be indexed at run time.
+// Cone adjoint: one thread per voxel column (ix, iy) and a run of TZ voxels in
+// z (block 32 x 4 columns). Per view, the thread finds the detector columns
+// whose rays can cross its column (projection of the column's four corners),
+// and per such column the xy crossing interval [l, h] of the ray family. For
+// each voxel k of the run it then visits only the detector rows whose ray is
+// inside that voxel's z range somewhere in [l, h], and adds w_rV * (c_r y_r)
+// with w_rV evaluated exactly as in the forward walk. The TZ accumulators are
+// registers (k is a compile-time index).
 // ---------------------------------------------------------------------------
 template <typename TX, int TZ>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, 6)
 k_adj_cone(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __restrict__ col,
            const RowEntry* __restrict__ row, const ViewEntry* __restrict__ view,
            const int* __restrict__ idY, const int* __restrict__ Nv, int tmp_size, DetGrid G,
@@ -283,69 +300,70 @@ k_adj_cone(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __r
            const int* __restrict__ skip)
 {
     if (skip && *skip) return;
-    __shared__ float sacc[TZ][128];
-    const int tid = threadIdx.y * 32 + threadIdx.x;
     const int ix = blockIdx.x * 32 + threadIdx.x;
     const int iy = blockIdx.y * 4 + threadIdx.y;
     const int zr = blockIdx.z % zruns, it = blockIdx.z / zruns;
     const int z0 = zr * TZ;
-    const int z1 = min(z0 + TZ, nz);          // exclusive
+    const int nk = min(TZ, nz - z0);          // voxels of this run inside the volume
+    if (ix >= nx || iy >= ny) return;
+    float acc[TZ];
 #pragma unroll
-    for (int k = 0; k < TZ; k++) sacc[k][tid] = 0.0f;
-    const bool active = (ix < nx) && (iy < ny);
-    if (active) {
-        float x0 = (float)(ix - nx / 2), y0 = (float)(iy - ny / 2);
-        float fx0 = (float)ix, fx1 = (float)(ix + 1), fy0 = (float)iy, fy1 = (float)(iy + 1);
-        float Zlo = (float)(z0 - nz / 2) * dz, Zhi = (float)(z1 - nz / 2) * dz;
-        int nvf = Nv[it];
-        for (int j = 0; j < nvf; j++) {
-            int iv = idY[it * tmp_size + j];
-            ViewEntry ve = view[iv];
-            int alo, ahi; float dmin, dmax;
-            column_window(G, ve.c, ve.s, x0, y0, 1.0f, 1.0f, na, alo, ahi, dmin, dmax);
-            const ColEntry* cv = col + (long long)iv * na;
-            const RowEntry* rv = row + (long long)iv * nb;
-            const float* yv = yw + (long long)iv * nb * na;
-            const float zl = Zlo - ve.sz, zh = Zhi - ve.sz;
-            for (int ia = alo; ia <= ahi; ia++) {
-                ColEntry ce = cv[ia];
-                float ax0 = fmaf(fx0, ce.inv_x, ce.off_x), ax1 = fmaf(fx1, ce.inv_x, ce.off_x);
-                float ay0 = fmaf(fy0, ce.inv_y, ce.off_y), ay1 = fmaf(fy1, ce.inv_y, ce.off_y);
-                float l = fmaxf(fminf(ax0, ax1), fminf(ay0, ay1));
-                float h = fminf(fmaxf(ax0, ax1), fmaxf(ay0, ay1));
-                if (!(l < h)) continue;
-                // rows whose ray reaches z in [Zlo, Zhi] while alpha is in [l, h]:
-                // z = sz + (A + ac) * d_z, d_z = v0 + ib*dv (flat panel rows)
-                float a1 = l + ve.ac, a2 = h + ve.ac;
-                float r1 = __fdividef(1.0f, a1), r2 = __fdividef(1.0f, a2);
-                float dlo = fminf(zl * r1, zl * r2), dhi = fmaxf(zh * r1, zh * r2);
-                float b0 = (dlo - G.v0) / G.dv, b1 = (dhi - G.v0) / G.dv;
-                if (b0 > b1) { float t = b0; b0 = b1; b1 = t; }
-                int blo = (int)fmaxf(floorf(b0) - 1.0f, 0.0f);
-                int bhi = (int)fminf(ceilf(b1) + 1.0f, (float)(nb - 1));
+    for (int k = 0; k < TZ; k++) acc[k] = 0.0f;
+    const float x0 = (float)(ix - nx / 2), y0 = (float)(iy - ny / 2);
+    const float fx0 = (float)ix, fx1 = (float)(ix + 1), fy0 = (float)iy, fy1 = (float)(iy + 1);
+    const float inv_dv = 1.0f / G.dv;
+    const int nvf = Nv[it];
+    for (int j = 0; j < nvf; j++) {
+        const int iv = idY[it * tmp_size + j];
+        const ViewEntry ve = view[iv];
+        int alo, ahi; float dmin, dmax;
+        column_window(G, ve.c, ve.s, x0, y0, 1.0f, 1.0f, na, alo, ahi, dmin, dmax);
+        const ColEntry* cv = col + (long long)iv * na;
+        const RowEntry* rv = row + (long long)iv * nb;
+        const float* yv = yw + (long long)iv * nb * na;
+        const float zr0 = (float)(z0 - nz / 2) * dz - ve.sz;   // lowest plane of the run, source-relative
+        for (int ia = alo; ia <= ahi; ia++) {
+            const ColEntry ce = cv[ia];
+            const float ax0 = fmaf(fx0, ce.inv_x, ce.off_x), ax1 = fmaf(fx1, ce.inv_x, ce.off_x);
+            const float ay0 = fmaf(fy0, ce.inv_y, ce.off_y), ay1 = fmaf(fy1, ce.inv_y, ce.off_y);
+            const float l = fmaxf(fminf(ax0, ax1), fminf(ay0, ay1));
+            const float h = fminf(fmaxf(ax0, ax1), fmaxf(ay0, ay1));
+            if (!(l < h)) continue;
+            // A ray of row ib is at z = sz + (A + ac) * d_ib, d_ib ~ v0 + ib * dv. It is
+            // inside voxel k somewhere in [l, h] iff d_ib lies between the plane
+            // heights over (A + ac) at the two ends: rows [e(k), e(k+1)] below, in
+            // detector-row units, stepping by dz/(A + ac)/dv per plane.
+            const float r1 = __fdividef(1.0f, l + ve.ac), r2 = __fdividef(1.0f, h + ve.ac);
+            const float s1 = dz * r1 * inv_dv, s2 = dz * r2 * inv_dv;
+            float e1 = (zr0 * r1 - G.v0) * inv_dv, e2 = (zr0 * r2 - G.v0) * inv_dv;
+            float mn = fminf(e1, e2), mx = fmaxf(e1, e2);   // row span at plane k
+            const float* ycol = yv + ia;
+#pragma unroll
+            for (int k = 0; k < TZ; k++) {
+                if (k >= nk) break;
+                e1 += s1; e2 += s2;
+                const float mn1 = fminf(e1, e2), mx1 = fmaxf(e1, e2);   // plane k + 1
+                const int blo = (int)fmaxf(ceilf(fminf(mn, mn1) - 0.02f), 0.0f);
+                const int bhi = (int)fminf(floorf(fmaxf(mx, mx1) + 0.02f), (float)(nb - 1));
+                mn = mn1; mx = mx1;
+                const float fk0 = (float)(z0 + k), fk1 = (float)(z0 + k + 1);
                 for (int ib = blo; ib <= bhi; ib++) {
-                    RowEntry re = rv[ib];
-                    float t0 = (l - re.off_z) * re.rinv_z, t1 = (h - re.off_z) * re.rinv_z;
-                    float tmin = fminf(t0, t1), tmax = fmaxf(t0, t1);
-                    int klo = (int)fmaxf(floorf(tmin - 0.01f), (float)z0);
-                    int khi = (int)fminf(floorf(tmax + 0.01f), (float)(z1 - 1));
-                    if (klo > khi) continue;
-                    float yval = __ldg(yv + (long long)ib * na + ia);
-                    for (int iz = klo; iz <= khi; iz++) {
-                        float az0 = fmaf((float)iz, re.inv_z, re.off_z);
-                        float az1 = fmaf((float)(iz + 1), re.inv_z, re.off_z);
-                        float l2 = fmaxf(l, fminf(az0, az1));
-                        float h2 = fminf(h, fmaxf(az0, az1));
-                        float w = h2 - l2;
-                        if (w > 0.0f) sacc[iz - z0][tid] = fmaf(w, yval, sacc[iz - z0][tid]);
-                    }
+                    const RowEntry re = rv[ib];
+                    const float yval = __ldg(ycol + (long long)ib * na);
+                    const float az0 = fmaf(fk0, re.inv_z, re.off_z);
+                    const float az1 = fmaf(fk1, re.inv_z, re.off_z);
+                    const float l2 = fmaxf(l, fminf(az0, az1));
+                    const float h2 = fminf(h, fmaxf(az0, az1));
+                    // w <= 0 (the ray misses voxel k) adds exactly 0 for finite y
+                    acc[k] = fmaf(fmaxf(h2 - l2, 0.0f), yval, acc[k]);
                 }
             }
         }
-        long long base = (long long)it * nx * ny * nz + (long long)iy * nx + ix;
-        for (int iz = z0; iz < z1; iz++)
-            Store<TX>::st(X + base + (long long)iz * nx * ny, sacc[iz - z0][tid]);
     }
+    const long long base = (long long)it * nx * ny * nz + (long long)iy * nx + ix;
+#pragma unroll
+    for (int k = 0; k < TZ; k++)
+        if (k < nk) Store<TX>::st(X + base + (long long)(z0 + k) * nx * ny, acc[k]);
 }
 
 DetGrid det_grid(const fl_plan* p)

@@ -246,7 +246,10 @@ def test_matched_dot_product_identity(cone):
 
 
 def test_matched_counts_match_oracle():
+    # view angles offset by an irrational step: no ray runs exactly through a
+    # line of voxel corners (the symmetric circle does, at 45 degrees)
     p = _cone_small()
+    p["sd_phi"] = (p["sd_phi"] + 0.1234567).astype(np.float32)
     c = _host(_plan(p).count_intersections()).astype(np.int64)
     e = O.exact_count(p)
     # This symmetric geometry sends rays exactly through voxel corners. There the
@@ -269,3 +272,21 @@ def test_matched_low_precision_storage(dt):
     e = O.exact_forward(x, p, threads=8)
     tol = 2e-3 if dt == "float16" else 1.5e-2
     assert _rel(y, e) < tol, _rel(y, e)
+
+
+def test_matched_reversed_detector_axes():
+    """Detector columns and rows listed in decreasing order: the adjoint's
+    windows must cover both orientations (dot-product identity, FP64 forward)."""
+    rng = np.random.default_rng(4)
+    p = _cone_small()
+    p["y_det"] = p["y_det"][::-1].copy()
+    p["z_det"] = p["z_det"][::-1].copy()
+    P = _plan(p)
+    x = rng.standard_normal(P.n_vox).astype(np.float32)
+    yv = rng.standard_normal(P.n_rays).astype(np.float32)
+    Ax = _host(P.forward(_dev(x)))
+    Aty = _host(P.adjoint(_dev(yv)))
+    lhs = np.dot(Ax.astype(np.float64), yv.astype(np.float64))
+    rhs = np.dot(x.astype(np.float64), Aty.astype(np.float64))
+    assert abs(lhs - rhs) / abs(lhs) < 1e-5, (lhs, rhs)
+    assert _rel(Aty, O.exact_adjoint(yv, p, threads=8)) < 2e-5
