@@ -1,0 +1,358 @@
+// framelet.cu -- undecimated tensor-product framelets (piecewise linear and
+// Haar), soft-shrinkage and the fused split-Bregman update.
+//
+// Semantics (FraDecMultiLevel3D.m:14-47, FraRecMultiLevel3D.m:14-48,
+// ConvSymAsym3D.m:18-34, GenerateFrameletFilter.m:2-17, softThreshold.m:47-80):
+//  * every 1-D filter is a circular correlation, taps at offsets
+//    (t - c) * 2^(level-1) around the output sample (imfilter 'circular');
+//  * 3-D band (i, j, k): D_i along y, D_j along x, D_k along z; 2-D band
+//    (i, j): D_i along x, D_j along y (FraDecMultiLevel2D.m:43-52);
+//  * level l+1 decomposes the low band (0,0[,0]) of level l; the synthesis
+//    replaces that low band by the reconstruction of level l+1, so the low
+//    band of every level but the last is never stored here;
+//  * soft-shrink sign(a) max(|a| - tau, 0) applies to every stored band except
+//    the low band of the last level.
+// Coefficient layout: level-major; inside a level, band index = base-3 digits
+// in pass order (3-D: 9i + 3j + k, 2-D: 3i + j), band 0 omitted below the last
+// level; each band is one volume (x fastest).
+//
+// Every pass is a streaming circular stencil along one axis. The last analysis
+// pass computes each band value in registers and applies the Bregman update
+// (v, alpha, alpha - v) without storing W u; the last synthesis pass writes
+// b = base + mu * W^T t directly.
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "fl_common.cuh"
+
+namespace {
+
+constexpr int kMaxBands = 27;
+
+struct Filters {
+    float f[5][5];   // up to 5 filters x 5 taps (linear: 3 x 3, haar: 2 x 3)
+    int nf, nt;      // filters, taps
+};
+
+struct BandPtrs {
+    float* p[kMaxBands];   // per band: coefficient array (nullptr: not stored)
+};
+
+__device__ __forceinline__ long long wrap_index(int ix, int iy, int iz, int nx, int ny, int nz)
+{
+    return ((long long)iz * ny + iy) * nx + ix;
+}
+
+// Index of the neighbour at offset d along `axis` with circular wrap.
+__device__ __forceinline__ long long nb_index(int ix, int iy, int iz, int nx, int ny, int nz,
+                                              int axis, int d)
+{
+    if (axis == 0) { ix = (ix + d) % nx; if (ix < 0) ix += nx; }
+    else if (axis == 1) { iy = (iy + d) % ny; if (iy < 0) iy += ny; }
+    else { iz = (iz + d) % nz; if (iz < 0) iz += nz; }
+    return wrap_index(ix, iy, iz, nx, ny, nz);
+}
+
+// out[nf*c + f] = F_f (*) in[c] along axis, c < nin   (analysis split pass)
+__global__ void k_split(const float* __restrict__ in, long long in_stride, int nin,
+                        float* __restrict__ out, long long out_stride, int nx, int ny, int nz,
+                        int axis, int step, Filters F)
+{
+    const long long N = (long long)nx * ny * nz;
+    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < N * nin;
+         p += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(p / N);
+        const long long q = p - (long long)c * N;
+        const int ix = (int)(q % nx), iy = (int)((q / nx) % ny), iz = (int)(q / ((long long)nx * ny));
+        float v[5];
+        const int ctr = (F.nt - 1) / 2;
+        for (int t = 0; t < F.nt; t++)
+            v[t] = __ldg(in + (long long)c * in_stride +
+                         nb_index(ix, iy, iz, nx, ny, nz, axis, (t - ctr) * step));
+        for (int f = 0; f < F.nf; f++) {
+            float s = 0.0f;
+            for (int t = 0; t < F.nt; t++) s = fmaf(F.f[f][t], v[t], s);
+            out[(long long)(F.nf * c + f) * out_stride + q] = s;
+        }
+    }
+}
+
+// Last analysis pass. band = nf*c + f. mode 0: coef[band] = w (skipping band 0
+// below the last level, which goes to `low`); mode 1: split-Bregman update on
+// v and t = alpha - v_new with soft threshold tau (no shrink on band 0 of the
+// last level).
+__global__ void k_split_last(const float* __restrict__ in, long long in_stride, int nin,
+                             int nx, int ny, int nz, int axis, int step, Filters F,
+                             BandPtrs coef, BandPtrs tout, float* __restrict__ low, int last,
+                             int mode, float tau)
+{
+    const long long N = (long long)nx * ny * nz;
+    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < N * nin;
+         p += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(p / N);
+        const long long q = p - (long long)c * N;
+        const int ix = (int)(q % nx), iy = (int)((q / nx) % ny), iz = (int)(q / ((long long)nx * ny));
+        float v[5];
+        const int ctr = (F.nt - 1) / 2;
+        for (int t = 0; t < F.nt; t++)
+            v[t] = __ldg(in + (long long)c * in_stride +
+                         nb_index(ix, iy, iz, nx, ny, nz, axis, (t - ctr) * step));
+        for (int f = 0; f < F.nf; f++) {
+            float w = 0.0f;
+            for (int t = 0; t < F.nt; t++) w = fmaf(F.f[f][t], v[t], w);
+            const int band = F.nf * c + f;
+            if (band == 0 && !last) {
+                if (low) low[q] = w;
+                continue;
+            }
+            if (mode == 0) {
+                coef.p[band][q] = w;
+            } else {
+                const float s = coef.p[band][q] + w;           // v + W u
+                float a = s;                                   // alpha
+                if (!(band == 0 && last)) {
+                    const float m = fabsf(s) - tau;
+                    a = m > 0.0f ? copysignf(m, s) : 0.0f;
+                }
+                const float vn = s - a;                        // v + W u - alpha
+                coef.p[band][q] = vn;
+                tout.p[band][q] = a - vn;                      // alpha - v_new
+            }
+        }
+    }
+}
+
+// out[c] = sum_f F_f (*) in[nf*c + f] along axis (synthesis merge pass); input
+// arrays come from `bands` (band pointer per index) -- with band 0 replaced by
+// `low` when non-null. final: out = base + scale * result.
+__global__ void k_merge(BandPtrs bands, const float* __restrict__ low, int nout, float* __restrict__ out,
+                        long long out_stride, int nx, int ny, int nz, int axis, int step,
+                        Filters F, const float* __restrict__ base, float scale, int final_)
+{
+    const long long N = (long long)nx * ny * nz;
+    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < N * nout;
+         p += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(p / N);
+        const long long q = p - (long long)c * N;
+        const int ix = (int)(q % nx), iy = (int)((q / nx) % ny), iz = (int)(q / ((long long)nx * ny));
+        const int ctr = (F.nt - 1) / 2;
+        float s = 0.0f;
+        for (int f = 0; f < F.nf; f++) {
+            const int band = F.nf * c + f;
+            const float* src = (band == 0 && low) ? low : bands.p[band];
+            for (int t = 0; t < F.nt; t++)
+                s = fmaf(F.f[f][t], __ldg(src + nb_index(ix, iy, iz, nx, ny, nz, axis, (t - ctr) * step)), s);
+        }
+        if (final_) s = (base ? __ldg(base + q) : 0.0f) + scale * s;
+        out[(long long)c * out_stride + q] = s;
+    }
+}
+
+unsigned grid_for(long long n)
+{
+    long long g = (n + 255) / 256;
+    return (unsigned)(g < 4096 ? (g > 0 ? g : 1) : 4096);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+struct fl_framelet {
+    int nx, ny, nz, dim, levels, kind;
+    int nf, nbands;                 // filters per axis, bands per level (nf^dim)
+    long long N;
+    Filters D, R;
+    int axes[3];                    // analysis pass order
+    float* work;                    // intermediates: nf^(dim-1) + nf^(dim-2) arrays + low
+    long long work_elems;
+    std::vector<long long> level_base;   // first coefficient band of each level
+    long long ncoef_bands;
+};
+
+static void set_filters(fl_framelet* w, int kind)
+{
+    std::memset(&w->D, 0, sizeof w->D);
+    std::memset(&w->R, 0, sizeof w->R);
+    const float r2 = 1.41421356237309505f;
+    if (kind == 1) {   // piecewise linear (GenerateFrameletFilter.m:9-17)
+        const float d[3][3] = {{0.25f, 0.5f, 0.25f}, {-r2 / 4, 0.0f, r2 / 4}, {-0.25f, 0.5f, -0.25f}};
+        const float r[3][3] = {{0.25f, 0.5f, 0.25f}, {r2 / 4, 0.0f, -r2 / 4}, {-0.25f, 0.5f, -0.25f}};
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++) { w->D.f[a][b] = d[a][b]; w->R.f[a][b] = r[a][b]; }
+        w->D.nf = w->R.nf = 3; w->D.nt = w->R.nt = 3;
+    } else {           // Haar (GenerateFrameletFilter.m:2-8)
+        const float d[2][3] = {{0.0f, 0.5f, 0.5f}, {0.0f, -0.5f, 0.5f}};
+        const float r[2][3] = {{0.5f, 0.5f, 0.0f}, {0.5f, -0.5f, 0.0f}};
+        for (int a = 0; a < 2; a++)
+            for (int b = 0; b < 3; b++) { w->D.f[a][b] = d[a][b]; w->R.f[a][b] = r[a][b]; }
+        w->D.nf = w->R.nf = 2; w->D.nt = w->R.nt = 3;
+    }
+}
+
+extern "C" int fl_framelet_create(int nx, int ny, int nz, int levels, int kind, fl_framelet** out)
+{
+    if (!out || nx < 1 || ny < 1 || nz < 1 || levels < 1 || levels > 8)
+        return fl_set_error(FL_ERR_INVALID, "fl_framelet_create: bad size or levels");
+    if (kind != FL_FRAMELET_LINEAR && kind != FL_FRAMELET_HAAR)
+        return fl_set_error(FL_ERR_INVALID, "fl_framelet_create: unknown filter bank %d", kind);
+    *out = nullptr;
+    fl_framelet* w = new (std::nothrow) fl_framelet;
+    if (!w) return fl_set_error(FL_ERR_ALLOC, "out of host memory");
+    w->nx = nx; w->ny = ny; w->nz = nz; w->dim = (nz > 1) ? 3 : 2; w->levels = levels;
+    w->kind = kind; w->N = (long long)nx * ny * nz;
+    set_filters(w, kind);
+    w->nf = w->D.nf;
+    w->nbands = w->dim == 3 ? w->nf * w->nf * w->nf : w->nf * w->nf;
+    if (w->dim == 3) { w->axes[0] = 1; w->axes[1] = 0; w->axes[2] = 2; }   // y, x, z
+    else { w->axes[0] = 0; w->axes[1] = 1; w->axes[2] = -1; }              // x, y
+    long long b = 0;
+    for (int l = 0; l < levels; l++) {
+        w->level_base.push_back(b);
+        b += (l == levels - 1) ? w->nbands : w->nbands - 1;
+    }
+    w->ncoef_bands = b;
+    long long inter = (w->dim == 3) ? (w->nf + w->nf * w->nf) : w->nf;
+    w->work_elems = (inter + 2) * w->N;   // pass intermediates + two low-band volumes
+    int st = fl_check_cuda(cudaMalloc((void**)&w->work, w->work_elems * sizeof(float)),
+                           "cudaMalloc(framelet)");
+    if (st) { delete w; return st; }
+    *out = w;
+    return fl_set_error(FL_OK, "");
+}
+
+extern "C" void fl_framelet_destroy(fl_framelet* w)
+{
+    if (!w) return;
+    if (w->work) cudaFree(w->work);
+    delete w;
+}
+
+extern "C" int64_t fl_framelet_ncoef(const fl_framelet* w)
+{
+    return w ? w->ncoef_bands * w->N : 0;
+}
+
+// band pointers of one level inside a coefficient set (band 0 below the last
+// level is absent)
+static BandPtrs level_bands(const fl_framelet* w, float* coef, int l)
+{
+    BandPtrs B;
+    for (int b = 0; b < kMaxBands; b++) B.p[b] = nullptr;
+    if (!coef) return B;
+    const bool last = (l == w->levels - 1);
+    long long base = w->level_base[l];
+    for (int b = 0; b < w->nbands; b++) {
+        if (b == 0 && !last) continue;
+        long long idx = base + (last ? b : b - 1);
+        B.p[b] = coef + idx * w->N;
+    }
+    return B;
+}
+
+// Analysis of all levels. mode 0: coef = W u. mode 1: Bregman update of v
+// (coef argument) writing t = alpha - v_new into tcoef.
+static int analysis(fl_framelet* w, const float* u, float* coef, float* tcoef, int mode,
+                    float tau, cudaStream_t s)
+{
+    const long long N = w->N;
+    const int nf = w->nf;
+    float* A = w->work;                          // nf arrays
+    float* Bm = A + (long long)nf * N;           // nf^2 arrays (3-D)
+    float* low0 = w->work + (w->work_elems - 2 * N);
+    float* low1 = low0 + N;
+    const float* in = u;
+    for (int l = 0; l < w->levels; l++) {
+        const int step = 1 << l;
+        const bool last = (l == w->levels - 1);
+        float* low_out = last ? nullptr : ((l % 2 == 0) ? low0 : low1);
+        BandPtrs cb = level_bands(w, coef, l), tb = level_bands(w, tcoef, l);
+        if (w->dim == 3) {
+            k_split<<<grid_for(N), 256, 0, s>>>(in, N, 1, A, N, w->nx, w->ny, w->nz, w->axes[0], step, w->D);
+            k_split<<<grid_for(N * nf), 256, 0, s>>>(A, N, nf, Bm, N, w->nx, w->ny, w->nz, w->axes[1], step, w->D);
+            k_split_last<<<grid_for(N * nf * nf), 256, 0, s>>>(Bm, N, nf * nf, w->nx, w->ny, w->nz,
+                                                             w->axes[2], step, w->D, cb, tb,
+                                                             low_out, last, mode, tau);
+        } else {
+            k_split<<<grid_for(N), 256, 0, s>>>(in, N, 1, A, N, w->nx, w->ny, w->nz, w->axes[0], step, w->D);
+            k_split_last<<<grid_for(N * nf), 256, 0, s>>>(A, N, nf, w->nx, w->ny, w->nz,
+                                                         w->axes[1], step, w->D, cb, tb, low_out,
+                                                         last, mode, tau);
+        }
+        int st = fl_check_launch("framelet analysis");
+        if (st) return st;
+        in = low_out;
+    }
+    return FL_OK;
+}
+
+// Synthesis: out = base + scale * W^T coef (base may be null, scale 1).
+static int synthesis(fl_framelet* w, float* coef, float* out, const float* base, float scale,
+                     cudaStream_t s)
+{
+    const long long N = w->N;
+    const int nf = w->nf;
+    float* A = w->work;
+    float* Bm = A + (long long)nf * N;
+    float* low0 = w->work + (w->work_elems - 2 * N);
+    float* low1 = low0 + N;
+    const float* low = nullptr;
+    for (int l = w->levels - 1; l >= 0; l--) {
+        const int step = 1 << l;
+        const bool final_ = (l == 0);
+        float* dst = final_ ? out : ((l % 2 == 0) ? low0 : low1);
+        BandPtrs cb = level_bands(w, coef, l);
+        BandPtrs ib, jb;
+        for (int b = 0; b < kMaxBands; b++) ib.p[b] = jb.p[b] = nullptr;
+        if (w->dim == 3) {
+            // z merge: nbands -> nf^2 arrays (Bm)
+            k_merge<<<grid_for(N * nf * nf), 256, 0, s>>>(cb, low, nf * nf, Bm, N, w->nx, w->ny,
+                                                        w->nz, w->axes[2], step, w->R, nullptr,
+                                                        1.0f, 0);
+            for (int b = 0; b < nf * nf; b++) ib.p[b] = Bm + (long long)b * N;
+            k_merge<<<grid_for(N * nf), 256, 0, s>>>(ib, nullptr, nf, A, N, w->nx, w->ny, w->nz,
+                                                   w->axes[1], step, w->R, nullptr, 1.0f, 0);
+            for (int b = 0; b < nf; b++) jb.p[b] = A + (long long)b * N;
+            k_merge<<<grid_for(N), 256, 0, s>>>(jb, nullptr, 1, dst, N, w->nx, w->ny, w->nz,
+                                              w->axes[0], step, w->R, final_ ? base : nullptr,
+                                              final_ ? scale : 1.0f, final_ ? 1 : 0);
+        } else {
+            k_merge<<<grid_for(N * nf), 256, 0, s>>>(cb, low, nf, A, N, w->nx, w->ny, w->nz,
+                                                   w->axes[1], step, w->R, nullptr, 1.0f, 0);
+            for (int b = 0; b < nf; b++) jb.p[b] = A + (long long)b * N;
+            k_merge<<<grid_for(N), 256, 0, s>>>(jb, nullptr, 1, dst, N, w->nx, w->ny, w->nz,
+                                              w->axes[0], step, w->R, final_ ? base : nullptr,
+                                              final_ ? scale : 1.0f, final_ ? 1 : 0);
+        }
+        int st = fl_check_launch("framelet synthesis");
+        if (st) return st;
+        low = dst;
+    }
+    return FL_OK;
+}
+
+extern "C" int fl_framelet_analysis(fl_framelet* w, const float* u, float* coef, void* stream)
+{
+    if (!w || !u || !coef) return fl_set_error(FL_ERR_INVALID, "fl_framelet_analysis: null argument");
+    int st = analysis(w, u, coef, nullptr, 0, 0.0f, (cudaStream_t)stream);
+    return st ? st : fl_set_error(FL_OK, "");
+}
+
+extern "C" int fl_framelet_synthesis(fl_framelet* w, const float* coef, float* u, void* stream)
+{
+    if (!w || !u || !coef) return fl_set_error(FL_ERR_INVALID, "fl_framelet_synthesis: null argument");
+    int st = synthesis(w, const_cast<float*>(coef), u, nullptr, 1.0f, (cudaStream_t)stream);
+    return st ? st : fl_set_error(FL_OK, "");
+}
+
+extern "C" int fl_framelet_bregman(fl_framelet* w, const float* u, float* v, float* t,
+                                   const float* Atf, float mu, float tau, float* b, void* stream)
+{
+    if (!w || !u || !v || !t || !b)
+        return fl_set_error(FL_ERR_INVALID, "fl_framelet_bregman: null argument");
+    cudaStream_t s = (cudaStream_t)stream;
+    int st = analysis(w, u, v, t, 1, tau, s);
+    if (st) return st;
+    st = synthesis(w, t, b, Atf, mu, s);
+    return st ? st : fl_set_error(FL_OK, "");
+}

@@ -194,6 +194,41 @@ int fl_cgls_solve(fl_cgls *cg, const float *b, float *u, float lam, int iters, d
                   int refresh, int flags, double *gamma_history, int *iters_done,
                   void *stream);
 
+/* ------------------------------------------------------------------------ */
+/* Framelets and split Bregman (FrameletSystem, softThreshold,               */
+/* solveSplitBregman.m:15-41)                                                */
+/* ------------------------------------------------------------------------ */
+typedef struct fl_framelet fl_framelet;
+enum { FL_FRAMELET_HAAR = 0, FL_FRAMELET_LINEAR = 1 };
+
+/* Undecimated tensor-product framelet on nx*ny*nz volumes (nz == 1: the 2-D
+ * transform), `levels` levels, filter bank `kind` (GenerateFrameletFilter.m).
+ * Replaces FrameletSystem(dim, type, level) (FrameletSystem.m:12-29). */
+int fl_framelet_create(int nx, int ny, int nz, int levels, int kind, fl_framelet **fw);
+void fl_framelet_destroy(fl_framelet *fw);
+/* Floats in a coefficient set: every band of every level except the low band
+ * of levels below the last (which the synthesis never reads). */
+int64_t fl_framelet_ncoef(const fl_framelet *fw);
+/* coef = W u (forwardTransform, FraDecMultiLevel3D.m) */
+int fl_framelet_analysis(fl_framelet *fw, const float *u, float *coef, void *stream);
+/* u = W^T coef (adjointTransform, FraRecMultiLevel3D.m) */
+int fl_framelet_synthesis(fl_framelet *fw, const float *coef, float *u, void *stream);
+/* One split-Bregman coefficient step (solveSplitBregman.m:30-38) in two
+ * passes: alpha = shrink(v + W u, tau) (low band of the last level not
+ * shrunk); v += W u - alpha; t = alpha - v; b = Atf + mu * W^T t.
+ * v and t are coefficient sets; Atf may be NULL (taken as 0). */
+int fl_framelet_bregman(fl_framelet *fw, const float *u, float *v, float *t, const float *Atf,
+                        float mu, float tau, float *b, void *stream);
+
+/* Split Bregman for min 1/2|Au - f|^2 + lam |W u|_1 (SplitBregman.m,
+ * solveSplitBregman.m): `outer` iterations of { CGLS on (A^T A + mu I) u = b
+ * warm-started from u, `cg_iters` iterations; framelet step }. f: sinogram,
+ * u: initial guess in, result out (device). `mode` selects the CGLS form.
+ * history (host, optional, >= outer doubles): |u_k - u_{k-1}| / |u_k| (FP64). */
+int fl_sb_solve(fl_plan *plan, const float *f, float *u, float lam, float mu, int outer,
+                int cg_iters, double cg_tol, int levels, int kind, int mode, double *history,
+                void *stream);
+
 /* The same solve with host buffers (the mex-style boundary): b and u0 are
  * copied to the device (u0 skipped with FL_CGLS_ZERO_START), the result is
  * copied back into u. Device copies are kept in the workspace for reuse. */
