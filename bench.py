@@ -6,11 +6,14 @@ Workload (default ``cone512``): 512^3 ellipsoid phantom, 720 views over 2*pi,
 1200 mm, 0.5 mm voxels. A step is one CGLS iteration on (A^T A + lam I) u = b,
 b = A^T A x_true, with the matched Siddon projector pair:
 
-* ``value``: the mixed form (FP16 storage of the projected direction, FP32
-  accumulation, fused FP64 reductions, CUDA-graph replay, FP32 residual
-  refresh every 10 iterations), inputs resident in HBM;
-* ``detail.plain_iter_per_s``: the plain FP32 form, host-synchronised scalars;
-* ``e2e``: the mixed form through the host-buffer C-ABI call
+* ``value``: the graph form (FP32 storage, fused updates with FP64 reductions
+  and device-side alpha/beta, one iteration replayed as a CUDA graph), inputs
+  resident in HBM;
+* ``detail.mixed_iter_per_s``: the same with an FP16 copy of the projected
+  direction (FP32 accumulation, FP32 residual refresh every 10 iterations);
+* ``detail.plain_iter_per_s``: plain FP32, one kernel per vector operation,
+  scalars synchronised to the host every iteration;
+* ``e2e``: the graph form through the host-buffer C-ABI call
   (fl_cgls_solve_host: b and u0 copied in, u copied out, inside the timing);
 * ``roofline``: the dominant projector kernel, algorithmic bytes
   (sum over rays of voxels crossed x voxel bytes + rays x sinogram bytes,
@@ -179,7 +182,7 @@ def main():
               "global_batch": world, "l2": "working set > L2 (volume and sinogram >= 64 MiB "
                                             "per operand; 512^3: 0.5 GiB + 2.2 GiB)",
               "parallelism": f"replicas{world}"}
-    metric = "CGLS iter/s (cone-beam, matched Siddon pair, mixed FP16-storage/graph form)"
+    metric = "CGLS iter/s (cone-beam, matched Siddon pair, fused FP32 graph form)"
 
     if a.impl == "reference":
         if rank != 0:
@@ -228,6 +231,7 @@ def main():
         return t
 
     legs = set(a.only.split(",")) if a.only else {"mixed", "plain", "e2e", "kernels"}
+    legs.add("graph")
     p = para_of(w)
     P = Plan(p)
     n = w["n"]
@@ -252,34 +256,42 @@ def main():
         barrier()
         return out, tmax(e0.elapsed_time(e1) / 1000.0)
 
-    # ---- mixed form (headline) ----
-    cg_m = NativeCGLS(P, "mixed")
+    # ---- graph form (headline) ----
+    cg_g = NativeCGLS(P, "graph")
     if W:
-        cg_m.solve(b, lam=lam, iters=W, refresh=REFRESH)
+        cg_g.solve(b, lam=lam, iters=W)
     clocks = ClockSampler(local)
     with clocks:
-        u_m, t_m = timed(lambda: cg_m.solve(b, lam=lam, iters=K, refresh=REFRESH))
-    value = world * K / t_m
-    detail["mixed_iter_per_s_per_gpu"] = K / t_m
-    detail["mixed_gamma_last"] = cg_m.history[-1] if cg_m.history else None
+        u_g, t_g = timed(lambda: cg_g.solve(b, lam=lam, iters=K))
+    value = world * K / t_g
+    detail["graph_iter_per_s_per_gpu"] = K / t_g
+    xt = x_true.double()
 
-    # ---- plain FP32 form ----
+    def rel(a_, b_):
+        return (torch.linalg.vector_norm((a_ - b_).double()) /
+                torch.linalg.vector_norm(b_.double())).item()
+
+    detail["graph_vs_truth_rel_l2"] = rel(u_g, xt)
+
+    # ---- mixed (FP16 direction) and plain FP32 forms ----
+    if "mixed" in legs:
+        cg_m = NativeCGLS(P, "mixed")
+        if W:
+            cg_m.solve(b, lam=lam, iters=W, refresh=REFRESH)
+        u_m, t_m = timed(lambda: cg_m.solve(b, lam=lam, iters=K, refresh=REFRESH))
+        detail["mixed_iter_per_s"] = world * K / t_m
+        detail["mixed_vs_graph_rel_l2"] = rel(u_m, u_g)
+        del cg_m, u_m
     if "plain" in legs:
         cg_p = NativeCGLS(P, "plain")
         if W:
             cg_p.solve(b, lam=lam, iters=W)
         u_p, t_p = timed(lambda: cg_p.solve(b, lam=lam, iters=K))
         detail["plain_iter_per_s"] = world * K / t_p
-        detail["mixed_over_plain"] = t_p / t_m
-        num = torch.linalg.vector_norm((u_m - u_p).double()).item()
-        den = torch.linalg.vector_norm(u_p.double()).item()
-        detail["mixed_vs_plain_rel_l2"] = num / den if den else None
-        detail["plain_gamma_last"] = cg_p.history[-1] if cg_p.history else None
-        xt = x_true.double()
-        detail["mixed_vs_truth_rel_l2"] = (torch.linalg.vector_norm(u_m.double() - xt) /
-                                           torch.linalg.vector_norm(xt)).item()
-        detail["plain_vs_truth_rel_l2"] = (torch.linalg.vector_norm(u_p.double() - xt) /
-                                           torch.linalg.vector_norm(xt)).item()
+        detail["graph_over_plain"] = t_p / t_g
+        detail["mixed_over_plain"] = (detail["mixed_iter_per_s"] / detail["plain_iter_per_s"]
+                                      if "mixed_iter_per_s" in detail else None)
+        detail["graph_vs_plain_rel_l2"] = rel(u_g, u_p)
         del cg_p, u_p
 
     # ---- e2e: host buffers through the C ABI ----
@@ -289,8 +301,8 @@ def main():
         bh.copy_(b.cpu())
         uh = torch.zeros(b.numel(), dtype=torch.float32, pin_memory=True)
         bn, un = bh.numpy(), uh.numpy()
-        cg_m.solve_host(bn, un, lam=lam, iters=max(W, 1), refresh=REFRESH)
-        _, t_e = timed(lambda: cg_m.solve_host(bn, un, lam=lam, iters=K, refresh=REFRESH))
+        cg_g.solve_host(bn, un, lam=lam, iters=max(W, 1))
+        _, t_e = timed(lambda: cg_g.solve_host(bn, un, lam=lam, iters=K))
         nb = b.numel() * 4
         e2e = {"value": world * K / t_e, "unit": "iter/s",
                "h2d_bytes_per_step": nb / K, "d2h_bytes_per_step": nb / K,
@@ -299,7 +311,7 @@ def main():
 
     # ---- projector kernels: algorithmic bytes and CUDA-event times ----
     roofline = None
-    launches = 5 * K + 2 + (K - 1) // REFRESH * (3 if lam else 2) + (K - 1) // REFRESH
+    launches = 5 * K + 1          # graph form: fwd, adj, 3 fused updates per iteration + init
     if "kernels" in legs:
         from framelab_gb300 import _lib
         L = _lib.load()
@@ -307,7 +319,7 @@ def main():
         n_isect = int(cnt.sum(dtype=torch.int64).item())
         del cnt
         n_rays = P.n_rays
-        p16 = (u_m / (u_m.abs().max() + 1e-30)).half()
+        p32 = (u_g / (u_g.abs().max() + 1e-30)).contiguous()
         ysc = torch.empty(n_rays, device=dev, dtype=torch.float32)
         xo = torch.empty(P.n_vox, device=dev, dtype=torch.float32)
         import ctypes as C
@@ -316,7 +328,7 @@ def main():
 
         def run_fwd():
             for _ in range(reps):
-                _lib.check(L.fl_forward(P.handle, 16, p16.data_ptr(), DTYPES[torch.float16],
+                _lib.check(L.fl_forward(P.handle, 16, p32.data_ptr(), DTYPES[torch.float32],
                                         ysc.data_ptr(), DTYPES[torch.float32], stream.cuda_stream))
 
         def run_adj():
@@ -329,7 +341,7 @@ def main():
         tf /= reps
         ta /= reps
         # adjoint launch = weighting pass + gather kernel; report the gather share via ncu
-        b_fwd = n_isect * 2 + n_rays * 4      # f16 voxel gathers + f32 sinogram writes
+        b_fwd = n_isect * 4 + n_rays * 4      # f32 voxel gathers + f32 sinogram writes
         b_adj = n_isect * 4 + P.n_vox * 4     # f32 sinogram gathers + f32 voxel writes
         peak = None
         try:
@@ -354,7 +366,7 @@ def main():
                 traffic = ent.get("bytes_per_launch")
         roofline = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
                     "frac": ach / peak if peak else None, "traffic": traffic,
-                    "kernel": f"matched {dom} ({'f16' if dom == 'forward' else 'f32'} storage)",
+                    "kernel": f"matched {dom} (f32 storage)",
                     "peak_source": peak_src,
                     "bytes_definition": "sum over rays of voxels crossed x element bytes + "
                                         "one element per ray (forward) / per voxel (adjoint)"}
@@ -366,9 +378,9 @@ def main():
 
     if rank == 0:
         out = {"metric": metric, "value": value, "unit": "iter/s", "n_gpus": world,
-               "steps": K, "warmup": W, "ms_per_step": 1000.0 * t_m / K,
+               "steps": K, "warmup": W, "ms_per_step": 1000.0 * t_g / K,
                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-               "dtype": "f32 (FP16 storage of the projected direction)",
+               "dtype": "f32",
                "data": "synthetic: seeded 12-ellipsoid phantom, noiseless projections",
                "config": config, "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
                "clocks": clocks.summary(), "gpu_launches": launches, "detail": detail}

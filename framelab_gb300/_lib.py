@@ -15,7 +15,7 @@ _lock = threading.Lock()
 _lib = None
 
 FL_OK, FL_ERR_INVALID, FL_ERR_UNSUPPORTED, FL_ERR_CUDA, FL_ERR_ALLOC, FL_ERR_TIMEOUT = range(6)
-MODEL_SIDDON_REF, MODEL_CHORD_REF, MODEL_MATCHED = 0, 1, 16
+MODEL_SIDDON_REF, MODEL_CHORD_REF, MODEL_GAO_REF, MODEL_MATCHED = 0, 1, 2, 16
 F32, F16, BF16 = 0, 1, 2
 
 
@@ -52,6 +52,10 @@ _SIGS = {
     "fl_forward": (_I, [_P, _I, _V, _I, _V, _I, _V]),
     "fl_adjoint": (_I, [_P, _I, _V, _I, _V, _I, _V]),
     "fl_count_intersections": (_I, [_P, _V, _V]),
+    "fl_forward_gao": (_I, [_P, _V, _V, _V, _V]),
+    "Ax_fan_mf_gpu_new": (None, [_V, _V, _F, _F, _F, _I, _I, _I, _V, _I, _V, _V, _I]),
+    "Ax_cone_mf_gpu_new": (None, [_V, _V, _V, _V, _V, _V, _V, _V, _V, _F, _F, _F, _F, _I, _I,
+                                  _I, _I, _I, _I, _I, _I, _I]),
     "Ax_fan_mf_gpu_siddon": (None, [_V, _V, _F, _F, _F, _I, _I, _I, _V, _I, _V, _V, _I]),
     "Atx_fan_mf_gpu_new": (None, [_V, _V, _F, _F, _F, _I, _I, _V, _I, _V, _F, _F, _I, _V, _V,
                                   _I, _I, _V, _V, _V, _V]),

@@ -5,11 +5,13 @@
 //  * FL_CGLS_PLAIN: FP32 storage, one kernel per vector operation, every
 //    scalar brought back to the host (the reference's loop, with the
 //    projector on the GPU).
-//  * FL_CGLS_MIXED: the search direction is also kept as scaled FP16 for the
-//    projector's gathers (FP32 accumulation along each ray); axpy/dot work is
-//    fused into three kernels that keep alpha, beta and gamma in device memory;
-//    one iteration is captured as a CUDA graph and replayed. Every `refresh`
-//    iterations the residual is recomputed in FP32 from u (r = (A^T A + lam) u - b).
+//  * FL_CGLS_GRAPH: FP32 storage; axpy/dot work fused into three kernels that
+//    keep alpha, beta and gamma in device memory; one iteration captured as a
+//    CUDA graph and replayed.
+//  * FL_CGLS_MIXED: as FL_CGLS_GRAPH, and the search direction is also kept as
+//    scaled FP16 for the projector's gathers (FP32 accumulation along each
+//    ray). Every `refresh` iterations the residual is recomputed in FP32 from
+//    u (r = (A^T A + lam) u - b).
 // Both stop early once gamma < tol, like the reference; in the graph this is a
 // device flag that turns the remaining replays into no-ops.
 #include <cstring>
@@ -304,7 +306,7 @@ static void cgls_free(fl_cgls* c)
 extern "C" int fl_cgls_create(fl_plan* plan, int mode, fl_cgls** out)
 {
     if (!plan || !out) return fl_set_error(FL_ERR_INVALID, "fl_cgls_create: null argument");
-    if (mode != FL_CGLS_PLAIN && mode != FL_CGLS_MIXED)
+    if (mode != FL_CGLS_PLAIN && mode != FL_CGLS_MIXED && mode != FL_CGLS_GRAPH)
         return fl_set_error(FL_ERR_INVALID, "unknown CGLS mode %d", mode);
     int st = fl_matched_ready(plan);
     if (st) return st;
@@ -422,14 +424,17 @@ static int solve_plain(fl_cgls* c, const float* b, float* u, float lam, int iter
     return FL_OK;
 }
 
-// one mixed iteration: fwd(p16) -> tmp -> adj -> q ; fused updates
+// one fused iteration: fwd(p or p16) -> tmp -> adj -> q ; fused updates
 static int mixed_iteration(fl_cgls* c, float* u, cudaStream_t s)
 {
     fl_plan* P = c->plan;
     CgScalars* S = c->S;
     int st;
-    if ((st = fl_matched_forward(P, c->p16, FL_F16, c->tmp, FL_F32, 2, &S->done, &S->p_unscale, s)))
-        return st;
+    if (c->p16)
+        st = fl_matched_forward(P, c->p16, FL_F16, c->tmp, FL_F32, 2, &S->done, &S->p_unscale, s);
+    else
+        st = fl_matched_forward(P, c->p, FL_F32, c->tmp, FL_F32, 2, &S->done, nullptr, s);
+    if (st) return st;
     if ((st = fl_matched_adjoint_w(P, c->tmp, c->q, FL_F32, &S->done, s))) return st;
     k_cg_pq<<<c->grid, kThreads, 0, s>>>(c->p, c->q, c->n, S, c->partials);
     k_cg_update<<<c->grid, kThreads, 0, s>>>(u, c->r, c->p, c->q, c->n, S, c->partials, c->hist,
@@ -455,7 +460,7 @@ static int solve_mixed(fl_cgls* c, const float* b, float* u, float lam, int iter
         q0 = c->q;
     }
     k_cg_init<<<c->grid, kThreads, 0, s>>>(b, q0, c->r, c->p, c->n, c->S, c->partials);
-    k_cg_p16<<<c->grid, kThreads, 0, s>>>(c->p, c->p16, c->n, c->S);
+    if (c->p16) k_cg_p16<<<c->grid, kThreads, 0, s>>>(c->p, c->p16, c->n, c->S);
     if ((st = fl_check_launch("cgls mixed init"))) return st;
 
     if (!c->captured || c->cap_uw != u) {
@@ -474,7 +479,7 @@ static int solve_mixed(fl_cgls* c, const float* b, float* u, float lam, int iter
     }
     for (int it = 0; it < iters; it++) {
         FL_CUDA(cudaGraphLaunch(c->exec, s));
-        if (refresh > 0 && (it + 1) % refresh == 0 && it + 1 < iters) {
+        if (c->p16 && refresh > 0 && (it + 1) % refresh == 0 && it + 1 < iters) {
             if ((st = normal_apply(c, u, c->q, lam, s))) return st;
             k_cg_refresh<<<c->grid, kThreads, 0, s>>>(b, c->q, c->r, c->n, c->S, c->partials);
             if ((st = fl_check_launch("cgls refresh"))) return st;

@@ -50,6 +50,7 @@ struct fl_plan {
 // internal launchers
 int fl_ref_forward(fl_plan* p, const float* x, float* y, cudaStream_t st);
 int fl_ref_adjoint(fl_plan* p, const float* y, float* x, cudaStream_t st);
+int fl_ref_gao_forward(fl_plan* p, const float* x, float* y, float* ynorm, cudaStream_t st);
 // skip: optional device flag; when *skip != 0 the kernels return at once
 // (lets a captured CGLS iteration become a no-op after convergence).
 // xscale: optional device factor applied to the gathered sum (scaled storage).

@@ -326,6 +326,11 @@ extern "C" int fl_forward(fl_plan* p, int model, const void* x, int xt, void* y,
         if ((st = fl_matched_ready(p))) return st;
         return fl_matched_forward(p, x, xt, y, yt, 1, nullptr, nullptr, sm);
     }
+    if (model == FL_MODEL_GAO_REF) {
+        if (xt != FL_F32 || yt != FL_F32)
+            return fl_set_error(FL_ERR_UNSUPPORTED, "reference dominant-axis forward is FP32 only");
+        return fl_ref_gao_forward(p, (const float*)x, (float*)y, nullptr, sm);
+    }
     return fl_set_error(FL_ERR_UNSUPPORTED, "fl_forward: model %d not available", model);
 }
 
@@ -371,6 +376,12 @@ extern "C" int fl_adjoint(fl_plan* p, int model, const void* y, int yt, void* x,
         return fl_matched_adjoint_w(p, w, x, xt, nullptr, sm);
     }
     return fl_set_error(FL_ERR_UNSUPPORTED, "fl_adjoint: model %d not available", model);
+}
+
+extern "C" int fl_forward_gao(fl_plan* p, const float* x, float* y, float* ynorm, void* stream)
+{
+    if (!p || !x || !y) return fl_set_error(FL_ERR_INVALID, "fl_forward_gao: null argument");
+    return fl_ref_gao_forward(p, x, y, ynorm, (cudaStream_t)stream);
 }
 
 extern "C" int fl_count_intersections(fl_plan* p, int32_t* counts, void* stream)
@@ -420,6 +431,23 @@ int run_forward_host(const fl_scan& s, int model, const float* X, float* y)
     if ((st = fl_check_cuda(cudaMemcpy(dx.p, X, nvox * 4, cudaMemcpyHostToDevice), "H2D"))) return st;
     if ((st = fl_forward(g.p, model, dx.p, FL_F32, dy.p, FL_F32, nullptr))) return st;
     if ((st = fl_check_cuda(cudaMemcpy(y, dy.p, nray * 4, cudaMemcpyDeviceToHost), "D2H"))) return st;
+    return fl_set_error(FL_OK, "");
+}
+
+int run_gao_host(const fl_scan& s, const float* X, float* y, float* ynorm)
+{
+    PlanGuard g;
+    int st = fl_plan_create(&s, &g.p);
+    if (st) return st;
+    DevBuf dx, dy, dn;
+    size_t nvox = (size_t)g.p->n_vox, nray = (size_t)g.p->n_rays;
+    if ((st = dx.alloc(nvox * 4)) || (st = dy.alloc(nray * 4))) return st;
+    if (ynorm && (st = dn.alloc(nray * 4))) return st;
+    if ((st = fl_check_cuda(cudaMemcpy(dx.p, X, nvox * 4, cudaMemcpyHostToDevice), "H2D"))) return st;
+    if ((st = fl_ref_gao_forward(g.p, (const float*)dx.p, (float*)dy.p, (float*)dn.p, nullptr))) return st;
+    if ((st = fl_check_cuda(cudaMemcpy(y, dy.p, nray * 4, cudaMemcpyDeviceToHost), "D2H"))) return st;
+    if (ynorm && (st = fl_check_cuda(cudaMemcpy(ynorm, dn.p, nray * 4, cudaMemcpyDeviceToHost), "D2H")))
+        return st;
     return fl_set_error(FL_OK, "");
 }
 
@@ -508,4 +536,35 @@ extern "C" void Atx_cone_mf_gpu_new(float* X, float* y, float* cos_phi, float* s
     s.view_frame = vf.data();
     s.id_Y = id_Y; s.Nv = Nv; s.tmp_size = tmp_size;
     run_adjoint_host(s, FL_MODEL_CHORD_REF, y, X);
+}
+
+extern "C" void Ax_fan_mf_gpu_new(float* X, float* y, float SO, float OD, float scale, int nx,
+                                  int ny, int nv, float* sd_phi, int nd, float* y_det,
+                                  int* id_X, int nt)
+{
+    fl_scan s;
+    std::memset(&s, 0, sizeof s);
+    s.ndim = 2; s.nx = nx; s.ny = ny; s.nz = 1; s.nt = nt; s.nv = nv; s.na = nd; s.nb = 1;
+    s.SO = SO; s.OD = OD; s.scale = scale; s.dz = 1.0f;
+    s.sd_phi = sd_phi; s.y_det = y_det; s.view_frame = id_X;
+    run_gao_host(s, X, y, nullptr);
+}
+
+extern "C" void Ax_cone_mf_gpu_new(float* X, float* y, float* yNorm, float* sd_phi, float* sd_z,
+                                   float* y_det, float* z_det, int* id_Y, int* Nv, float SO,
+                                   float OD, float scale, float dz, int nx, int ny, int nz,
+                                   int nt, int na, int nb, int nv, int tmp_size, int nv_block)
+{
+    (void)nv_block;
+    fl_scan s;
+    std::memset(&s, 0, sizeof s);
+    s.ndim = 3; s.nx = nx; s.ny = ny; s.nz = nz; s.nt = nt; s.nv = nv; s.na = na; s.nb = nb;
+    s.SO = SO; s.OD = OD; s.scale = scale; s.dz = dz;
+    s.sd_phi = sd_phi; s.sd_z = sd_z; s.y_det = y_det; s.z_det = z_det;
+    int bad;
+    std::vector<int32_t> vf = frames_of(id_Y, Nv, nt, tmp_size, nv, &bad);
+    if (bad) { fl_set_error(FL_ERR_INVALID, "id_Y entry out of range"); return; }
+    s.view_frame = vf.data();
+    s.id_Y = id_Y; s.Nv = Nv; s.tmp_size = tmp_size;
+    run_gao_host(s, X, y, yNorm);
 }

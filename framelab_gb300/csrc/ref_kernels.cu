@@ -416,6 +416,155 @@ k_ref_cone_chord_adj(float* __restrict__ x, const float* __restrict__ Y,
     x[(long long)it * nx * ny * nz + ((long long)iz * ny + iy) * nx + ix] = fmul(acc, scale);
 }
 
+// ---------------------------------------------------------------------------
+// Dominant-axis forward (version 1): Ax_cone_mf_cpu_new.cpp:23-235 and
+// Ax_fan_mf_cpu_new.cpp:18-122. Per slab of the dominant axis the ray touches
+// at most two cells along the other in-plane axis and two along z; the case
+// analysis (11, 12, 21, 22) and every float operation follow the reference.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float gao_slab(float acc, float p1, float p2, float q1, float q2,
+                                          float l, int ns, int nz, const float* __restrict__ x,
+                                          long long ss, long long zs, long long base)
+{
+    const int c1 = (int)floorf(p1), c2 = (int)floorf(p2);
+    const int k1 = (int)floorf(q1), k2 = (int)floorf(q2);
+#define VOX(c, k) __ldg(x + base + (long long)(k) * zs + (long long)(c) * ss)
+    if (c2 == c1) {
+        if (c1 >= 0 && c1 <= ns - 1) {
+            if (k2 == k1) {
+                if (k1 >= 0 && k1 <= nz - 1) acc = fadd(acc, fmul(l, VOX(c1, k1)));
+            } else if (k1 >= -1 && k1 <= nz - 1) {
+                const float rz = fdiv(fsub((float)k2, q1), fsub(q2, q1));
+                if (k1 > -1) acc = fadd(acc, fmul(fmul(rz, l), VOX(c1, k1)));
+                if (k2 < nz) acc = fadd(acc, fmul(fmul(fsub(1.0f, rz), l), VOX(c1, k2)));
+            }
+        }
+    } else if (c1 >= -1 && c1 <= ns - 1) {
+        const float d = fsub(p2, p1);
+        if (k2 == k1) {
+            if (k1 >= 0 && k1 <= nz - 1) {
+                const float rs = fdiv(fsub((float)c2, p1), d);
+                if (c1 > -1) acc = fadd(acc, fmul(fmul(rs, l), VOX(c1, k1)));
+                if (c2 < ns) acc = fadd(acc, fmul(fmul(fsub(1.0f, rs), l), VOX(c2, k1)));
+            }
+        } else if (k1 >= -1 && k1 <= nz - 1) {
+            const float rs = fdiv(fsub((float)c2, p1), d);
+            const float rz = fdiv(fsub((float)k2, q1), fsub(q2, q1));
+            if (rs > rz) {
+                if (c1 > -1 && k1 > -1) acc = fadd(acc, fmul(fmul(rz, l), VOX(c1, k1)));
+                if (c1 > -1 && k2 < nz) acc = fadd(acc, fmul(fmul(fsub(rs, rz), l), VOX(c1, k2)));
+                if (c2 < ns && k2 < nz) acc = fadd(acc, fmul(fmul(fsub(1.0f, rs), l), VOX(c2, k2)));
+            } else {
+                if (c1 > -1 && k1 > -1) acc = fadd(acc, fmul(fmul(rs, l), VOX(c1, k1)));
+                if (c2 < ns && k1 > -1) acc = fadd(acc, fmul(fmul(fsub(rz, rs), l), VOX(c2, k1)));
+                if (c2 < ns && k2 < nz) acc = fadd(acc, fmul(fmul(fsub(1.0f, rz), l), VOX(c2, k2)));
+            }
+        }
+    }
+#undef VOX
+    return acc;
+}
+
+__global__ void __launch_bounds__(128)
+k_ref_cone_gao(const float* __restrict__ X, float* __restrict__ y, float* __restrict__ ynorm,
+               const float* __restrict__ cphi_v, const float* __restrict__ sphi_v,
+               const float* __restrict__ sdz, const float* __restrict__ ydet,
+               const float* __restrict__ zdet, const int* __restrict__ vframe, float SO,
+               float OD, float scale, int nx, int ny, int nz, float dz, int na, int nb,
+               long long nper)
+{
+    const int ia = blockIdx.x * blockDim.x + threadIdx.x;
+    const int ib = blockIdx.y, iv = blockIdx.z;
+    if (ia >= na) return;
+    const float* x = X + (long long)vframe[iv] * nper;
+    const int nx2 = nx / 2, ny2 = ny / 2, nz2 = nz / 2;
+    const float c = cphi_v[iv], s = sphi_v[iv];
+    const float x1 = fmul(c, -SO), y1 = fmul(s, -SO), z1 = sdz[iv];
+    const float u = ydet[ia];
+    const float x2 = fsub(fmul(c, OD), fmul(s, u));
+    const float y2 = fadd(fmul(s, OD), fmul(c, u));
+    const float z2 = fadd(zdet[ib], sdz[iv]);
+    // norm3 (Ax_cone_mf_cpu_new.cpp:19-20): double sqrt of float differences, returned as float
+    const double ex = (double)fsub(x1, x2), ey = (double)fsub(y1, y2), ez = (double)fsub(z1, z2);
+    const float norm = fmul(__double2float_rn(__dsqrt_rn(
+                                __dadd_rn(__dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)), __dmul_rn(ez, ez)))),
+                            scale);
+    const float tmp = fadd(fmul(fsub(x1, x2), fsub(x1, x2)), fmul(fsub(y1, y2), fsub(y1, y2)));
+    const float zz = fmul(fsub(z1, z2), fsub(z1, z2));
+    const long long zs = (long long)nx * ny;
+    float acc = 0.0f;
+    const bool xdom = fabs_ref(fsub(x1, x2)) > fabs_ref(fsub(y1, y2));
+    // primary axis a (walked), secondary in-plane axis b
+    const float pa = xdom ? x1 : y1, pb = xdom ? y1 : x1;
+    const float s1 = xdom ? fdiv(fsub(y2, y1), fsub(x2, x1)) : fdiv(fsub(x2, x1), fsub(y2, y1));
+    const float s2 = xdom ? fdiv(fsub(z2, z1), fsub(x2, x1)) : fdiv(fsub(z2, z1), fsub(y2, y1));
+    const int np = xdom ? nx : ny, np2 = xdom ? nx2 : ny2;
+    const int ns = xdom ? ny : nx, ns2 = xdom ? ny2 : nx2;
+    const long long ss = xdom ? nx : 1;
+    for (int ip = 0; ip < np; ip++) {
+        const float a1 = (float)(ip - np2), a2 = fadd(a1, 1.0f);
+        const float lo = (s1 >= 0.0f) ? a1 : a2, hi = (s1 >= 0.0f) ? a2 : a1;
+        const float p1 = fadd(fadd(pb, fmul(s1, fsub(lo, pa))), (float)ns2);
+        const float p2 = fadd(fadd(pb, fmul(s1, fsub(hi, pa))), (float)ns2);
+        const float zlo = (s2 >= 0.0f) ? a1 : a2, zhi = (s2 >= 0.0f) ? a2 : a1;
+        const float q1 = fadd(fdiv(fadd(z1, fmul(s2, fsub(zlo, pa))), dz), (float)nz2);
+        const float q2 = fadd(fdiv(fadd(z1, fmul(s2, fsub(zhi, pa))), dz), (float)nz2);
+        const float d = fsub(p2, p1);
+        const float l = fsqrt(fdiv(fmul(fadd(fmul(d, d), 1.0f), fadd(tmp, zz)), tmp));
+        acc = gao_slab(acc, p1, p2, q1, q2, l, ns, nz, x, ss, zs, xdom ? ip : (long long)ip * nx);
+    }
+    const long long r = ((long long)iv * nb + ib) * na + ia;
+    const float out = fmul(acc, scale);
+    y[r] = out;
+    if (ynorm) ynorm[r] = fdiv(out, norm);
+}
+
+__global__ void __launch_bounds__(128)
+k_ref_fan_gao(const float* __restrict__ X, float* __restrict__ y,
+              const float* __restrict__ cphi_v, const float* __restrict__ sphi_v,
+              const float* __restrict__ ydet, const int* __restrict__ vframe, float SO, float OD,
+              float scale, int nx, int ny, int nd, long long nper)
+{
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    const int iv = blockIdx.y;
+    if (id >= nd) return;
+    const float* x = X + (long long)vframe[iv] * nper;
+    const int nx2 = nx / 2, ny2 = ny / 2;
+    const float c = cphi_v[iv], s = sphi_v[iv];
+    const float x1 = fmul(c, -SO), y1 = fmul(s, -SO);
+    const float u = ydet[id];
+    const float x2 = fsub(fmul(c, OD), fmul(s, u));
+    const float y2 = fadd(fmul(s, OD), fmul(c, u));
+    const bool xdom = fabs_ref(fsub(x1, x2)) > fabs_ref(fsub(y1, y2));
+    const float sl = xdom ? fdiv(fsub(y2, y1), fsub(x2, x1)) : fdiv(fsub(x2, x1), fsub(y2, y1));
+    const float pa = xdom ? x1 : y1, pb = xdom ? y1 : x1;
+    const int np = xdom ? nx : ny, np2 = xdom ? nx2 : ny2;
+    const int ns = xdom ? ny : nx, ns2 = xdom ? ny2 : nx2;
+    float acc = 0.0f;
+    for (int ip = 0; ip < np; ip++) {
+        const float a1 = (float)(ip - np2), a2 = fadd(a1, 1.0f);
+        const float lo = (sl >= 0.0f) ? a1 : a2, hi = (sl >= 0.0f) ? a2 : a1;
+        const float p1 = fadd(fadd(pb, fmul(sl, fsub(lo, pa))), (float)ns2);
+        const float p2 = fadd(fadd(pb, fmul(sl, fsub(hi, pa))), (float)ns2);
+        const int c1 = (int)floorf(p1), c2 = (int)floorf(p2);
+#define PIX(cc) __ldg(xdom ? x + (long long)(cc) * nx + ip : x + (long long)ip * nx + (cc))
+        const float d = fsub(p2, p1);
+        const float l = fsqrt(fadd(fmul(d, d), 1.0f));
+        if (c2 == c1) {
+            if (c1 >= 0 && c1 <= ns - 1) acc = fadd(acc, fmul(l, PIX(c1)));
+        } else if (c2 > 0 && c2 < ns) {
+            acc = fadd(acc, fmul(fmul(fdiv(fsub((float)c2, p1), d), l), PIX(c1)));
+            acc = fadd(acc, fmul(fmul(fdiv(fsub(p2, (float)c2), d), l), PIX(c2)));
+        } else {
+            if (c2 == 0) acc = fadd(acc, fmul(fmul(fdiv(fsub(p2, (float)c2), d), l), PIX(c2)));
+            // the reference tests c2 == ny on both branches (Ax_fan_mf_cpu_new.cpp:70,111)
+            if (c2 == ny) acc = fadd(acc, fmul(fmul(fdiv(fsub((float)c2, p1), d), l), PIX(c1)));
+        }
+#undef PIX
+    }
+    y[(long long)iv * nd + id] = fmul(acc, scale);
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -460,4 +609,23 @@ int fl_ref_adjoint(fl_plan* p, const float* y, float* x, cudaStream_t st)
             s.ny, s.nz, s.na, s.nb);
     }
     return fl_check_launch("reference chord backprojection");
+}
+
+int fl_ref_gao_forward(fl_plan* p, const float* x, float* y, float* ynorm, cudaStream_t st)
+{
+    const fl_scan& s = p->s;
+    long long nper = (long long)s.nx * s.ny * s.nz;
+    if (s.ndim == 2) {
+        dim3 grid(fl_div_up(s.na, 128), s.nv);
+        k_ref_fan_gao<<<grid, 128, 0, st>>>(x, y, p->d_cphi_f, p->d_sphi_f, p->d_y_det,
+                                            p->d_view_frame, s.SO, s.OD, s.scale, s.nx, s.ny,
+                                            s.na, nper);
+        if (ynorm) return fl_set_error(FL_ERR_UNSUPPORTED, "yNorm is a cone-beam output");
+    } else {
+        dim3 grid(fl_div_up(s.na, 128), s.nb, s.nv);
+        k_ref_cone_gao<<<grid, 128, 0, st>>>(x, y, ynorm, p->d_cphi_f, p->d_sphi_f, p->d_sd_z,
+                                             p->d_y_det, p->d_z_det, p->d_view_frame, s.SO, s.OD,
+                                             s.scale, s.nx, s.ny, s.nz, s.dz, s.na, s.nb, nper);
+    }
+    return fl_check_launch("reference dominant-axis forward");
 }

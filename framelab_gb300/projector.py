@@ -6,6 +6,7 @@ PyTorch CUDA stream. Models:
 
 * ``"siddon_ref"`` -- version 0, bit-exact with ``Ax_*_mf_cpu_siddon``
 * ``"chord_ref"``  -- version 1 backprojector, bit-exact with ``Atx_*_mf_cpu_new``
+* ``"gao_ref"``    -- version 1 forward, bit-exact with ``Ax_*_mf_cpu_new``
 * ``"matched"``    -- matched Siddon pair; the adjoint is the exact transpose
 """
 from __future__ import annotations
@@ -18,7 +19,7 @@ import torch
 from . import _lib
 
 MODELS = {"siddon_ref": _lib.MODEL_SIDDON_REF, "chord_ref": _lib.MODEL_CHORD_REF,
-          "matched": _lib.MODEL_MATCHED}
+          "gao_ref": _lib.MODEL_GAO_REF, "matched": _lib.MODEL_MATCHED}
 DTYPES = {torch.float32: _lib.F32, torch.float16: _lib.F16, torch.bfloat16: _lib.BF16}
 
 
@@ -134,6 +135,18 @@ class Plan:
         _lib.check(self._L.fl_adjoint(self._h, MODELS[model], y.data_ptr(), DTYPES[y.dtype],
                                       out.data_ptr(), DTYPES[out.dtype], _stream(stream)))
         return out
+
+    def forward_gao(self, x: torch.Tensor, with_norm: bool = True, stream=None):
+        """Version-1 forward (Ax_*_mf_cpu_new); cone beams also return yNorm."""
+        self._check_dev(x, self.n_vox, "x")
+        if x.dtype != torch.float32:
+            raise ValueError("version-1 forward is FP32 only")
+        y = torch.empty(self.sino_shape, device=x.device, dtype=torch.float32)
+        yn = torch.empty_like(y) if (with_norm and self.cone) else None
+        _lib.check(self._L.fl_forward_gao(self._h, x.data_ptr(), y.data_ptr(),
+                                          yn.data_ptr() if yn is not None else None,
+                                          _stream(stream)))
+        return (y, yn) if yn is not None else y
 
     def count_intersections(self, stream=None) -> torch.Tensor:
         c = torch.empty(self.sino_shape, device="cuda", dtype=torch.int32)

@@ -26,7 +26,7 @@ _lib.declare("fl_cgls_solve", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_
 _lib.declare("fl_cgls_solve_host", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_float,
                                              C.c_int, C.c_double, C.c_int, C.c_int, C.c_void_p,
                                              C.POINTER(C.c_int), C.c_void_p])
-MODES = {"plain": 0, "mixed": 1}
+MODES = {"plain": 0, "mixed": 1, "graph": 2}
 ZERO_START = 1
 
 

@@ -76,6 +76,22 @@ void Ax_cone_mf_gpu_siddon(float *X, float *y, float *sd_phi, float *sd_z, float
                            float dz, int nx, int ny, int nz, int nt, int na, int nb, int nv,
                            int tmp_size, int nv_block);
 
+/* Fan-beam dominant-axis projection (version 1, the classes' default),
+ * bit-exact with the reference's Ax_fan_mf_cpu_new. Replaces
+ * Ax_fan_mf_gpu_new (matlab/mex/src/Ax_fan_mf.h:7, Ax_fan_mf_gpu_new.cu:138-164). */
+void Ax_fan_mf_gpu_new(float *X, float *y, float SO, float OD, float scale, int nx, int ny,
+                       int nv, float *sd_phi, int nd, float *y_det, int *id_X, int nt);
+
+/* Cone-beam dominant-axis projection (version 1, the classes' default) and
+ * its normalised twin yNorm = y / (|src - det| scale), bit-exact with the
+ * reference's CPU kernel Ax_cone_mf_cpu_new (its GPU version handles
+ * partially covered border voxels differently). Replaces Ax_cone_mf_gpu_new
+ * (matlab/mex/src/Ax_cone_mf.h:3, Ax_cone_mf_gpu_new.cu:469-521). */
+void Ax_cone_mf_gpu_new(float *X, float *y, float *yNorm, float *sd_phi, float *sd_z,
+                        float *y_det, float *z_det, int *id_Y, int *Nv, float SO, float OD,
+                        float scale, float dz, int nx, int ny, int nz, int nt, int na, int nb,
+                        int nv, int tmp_size, int nv_block);
+
 /* Cone-beam chord-length backprojection (version 1), bit-exact with the
  * reference's Atx_cone_mf_cpu_new. Replaces Atx_cone_mf_gpu_new
  * (matlab/mex/src/Atx_cone_mf.h:4, Atx_cone_mf_gpu_new.cu:114-162). */
@@ -125,6 +141,7 @@ typedef struct fl_plan fl_plan;
 enum {
     FL_MODEL_SIDDON_REF = 0, /* version 0: bit-exact reference Siddon forward */
     FL_MODEL_CHORD_REF = 1,  /* version 1 adjoint: bit-exact reference chord backprojector */
+    FL_MODEL_GAO_REF = 2,    /* version 1 forward: bit-exact reference dominant-axis projector */
     FL_MODEL_MATCHED = 16    /* matched Siddon pair; adjoint is the exact transpose */
 };
 
@@ -143,6 +160,10 @@ int fl_forward(fl_plan *plan, int model, const void *x, int x_dtype, void *y, in
  * fl_forward's matrix; FL_MODEL_CHORD_REF is the reference's backprojector. */
 int fl_adjoint(fl_plan *plan, int model, const void *y, int y_dtype, void *x, int x_dtype,
                void *stream);
+/* Version-1 forward with the cone-beam normalised output (ynorm may be NULL;
+ * fan beams have no ynorm). Replaces the [y, yNorm] of Ax_cone_mf. */
+int fl_forward_gao(fl_plan *plan, const float *x, float *y, float *ynorm, void *stream);
+
 /* Number of voxels each ray crosses with positive length (matched model). */
 int fl_count_intersections(fl_plan *plan, int32_t *counts, void *stream);
 
@@ -176,7 +197,11 @@ int fl_dot(const float *a, const float *b, int64_t n, double *out, void *stream)
 int fl_normal_apply(fl_plan *plan, const float *x, float *q, float lam, void *stream);
 
 typedef struct fl_cgls fl_cgls;
-enum { FL_CGLS_PLAIN = 0, FL_CGLS_MIXED = 1 };
+/* PLAIN: FP32, one kernel per vector operation, scalars on the host.
+ * GRAPH: FP32, fused updates with device-side scalars, CUDA-graph replay.
+ * MIXED: GRAPH plus an FP16 copy of the search direction for the projector
+ *        and an FP32 residual refresh every `refresh` iterations. */
+enum { FL_CGLS_PLAIN = 0, FL_CGLS_MIXED = 1, FL_CGLS_GRAPH = 2 };
 enum { FL_CGLS_ZERO_START = 1 };   /* u0 == 0: skip the initial A_loc(u0) */
 
 /* CGLS workspace bound to a plan (matched model). Allocates r, p, q, a

@@ -337,3 +337,41 @@ def exact_count(p, views=None):
                       I(int(p["ny"])), I(nz), D(dz), I(v0), I(v1), P(sd), P(sz), I(na), I(nb),
                       P(yd), P(zd))
     return c
+
+
+# --------------------------------------------------------------------------
+# dominant-axis forward (version 1), FP32 restatement
+# --------------------------------------------------------------------------
+def cone_gao_f32(X, p, threads=1, views=None):
+    """Ax_cone_mf_cpu_new (Ax_cone_mf_cpu_new.cpp:23-235): returns (y, yNorm)."""
+    L = lib()
+    X = _f(X); sd = _f(p["sd_phi"]); sz = _f(p["sd_z"]); yd = _f(p["y_det"])
+    zd = _f(p["z_det"]); idx = _i(p["id_X"])
+    nv, na, nb = len(sd), len(yd), len(zd)
+    v0, v1 = views or (0, nv)
+    y = np.zeros(nv * na * nb, np.float32)
+    yn = np.zeros(nv * na * nb, np.float32)
+
+    def go(a, b):
+        L.orc_cone_gao_f32(P(X), P(y), P(yn), F(p["SO"]), F(p["OD"]), F(p["scale"]),
+                           I(int(p["nx"])), I(int(p["ny"])), I(int(p["nz"])), I(a), I(b), P(sd),
+                           P(sz), I(na), I(nb), P(yd), P(zd), P(idx), F(p["dz"]))
+    rng = [(v0 + a, v0 + b) for a, b in _split(v1 - v0, threads * 4 if threads > 1 else 1)]
+    _run(go, rng, threads)
+    return y, yn
+
+
+def fan_gao_f32(X, p, threads=1, views=None):
+    """Ax_fan_mf_cpu_new (Ax_fan_mf_cpu_new.cpp:18-122)."""
+    L = lib()
+    X = _f(X); sd = _f(p["sd_phi"]); yd = _f(p["y_det"]); idx = _i(p["id_X"])
+    nv, nd = len(sd), len(yd)
+    v0, v1 = views or (0, nv)
+    y = np.zeros(nv * nd, np.float32)
+
+    def go(a, b):
+        L.orc_fan_gao_f32(P(X), P(y), F(p["SO"]), F(p["OD"]), F(p["scale"]), I(int(p["nx"])),
+                          I(int(p["ny"])), I(a), I(b), P(sd), I(nd), P(yd), P(idx))
+    rng = [(v0 + a, v0 + b) for a, b in _split(v1 - v0, threads * 4 if threads > 1 else 1)]
+    _run(go, rng, threads)
+    return y

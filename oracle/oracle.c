@@ -596,3 +596,185 @@ void orc_exact_count(int64_t *cnt, double SO, double OD, int nx, int ny, int nz,
         }
     }
 }
+
+/* ------------------------------------------------------------------------- */
+/* (1c) Dominant-axis forward projector (version 1), FP32, reference arithmetic */
+/* ------------------------------------------------------------------------- */
+
+/*
+ * One slab of the dominant-axis walk: the ray crosses the slab between
+ * secondary coordinates [p1, p2] (grid units, p1 <= p2) and, in 3-D, z
+ * coordinates [q1, q2]; it touches at most two voxels along each secondary
+ * axis. Restates the case analysis of Ax_cone_mf_cpu_new.cpp:77-155 (cases
+ * 11, 12, 21, 22); `vox(s, z)` maps secondary and z cell to a voxel pointer.
+ */
+typedef struct { const float *x; long sstride, zstride, base; } orc_gao_vox;
+
+static float orc_gao_slab(float acc, float p1, float p2, float q1, float q2, float l, int ns,
+                          int nz, const orc_gao_vox *V)
+{
+    int c1 = (int)floor(p1), c2 = (int)floor(p2);
+    int k1 = (int)floor(q1), k2 = (int)floor(q2);
+#define VOX(s, z) (V->x[V->base + (long)(z) * V->zstride + (long)(s) * V->sstride])
+    if (c2 == c1) {
+        if (c1 >= 0 && c1 <= ns - 1) {
+            if (k2 == k1) {
+                if (k1 >= 0 && k1 <= nz - 1) acc += l * VOX(c1, k1);
+            } else if (k1 >= -1 && k1 <= nz - 1) {
+                float rz = (k2 - q1) / (q2 - q1);
+                if (k1 > -1) acc += rz * l * VOX(c1, k1);
+                if (k2 < nz) acc += (1 - rz) * l * VOX(c1, k2);
+            }
+        }
+    } else if (c1 >= -1 && c1 <= ns - 1) {
+        float d = p2 - p1;
+        if (k2 == k1) {
+            if (k1 >= 0 && k1 <= nz - 1) {
+                float rs = (c2 - p1) / d;
+                if (c1 > -1) acc += rs * l * VOX(c1, k1);
+                if (c2 < ns) acc += (1 - rs) * l * VOX(c2, k1);
+            }
+        } else if (k1 >= -1 && k1 <= nz - 1) {
+            float rs = (c2 - p1) / d, rz = (k2 - q1) / (q2 - q1);
+            if (rs > rz) {
+                if (c1 > -1 && k1 > -1) acc += rz * l * VOX(c1, k1);
+                if (c1 > -1 && k2 < nz) acc += (rs - rz) * l * VOX(c1, k2);
+                if (c2 < ns && k2 < nz) acc += (1 - rs) * l * VOX(c2, k2);
+            } else {
+                if (c1 > -1 && k1 > -1) acc += rs * l * VOX(c1, k1);
+                if (c2 < ns && k1 > -1) acc += (rz - rs) * l * VOX(c2, k1);
+                if (c2 < ns && k2 < nz) acc += (1 - rz) * l * VOX(c2, k2);
+            }
+        }
+    }
+#undef VOX
+    return acc;
+}
+
+/*
+ * Cone-beam dominant-axis projection with its normalised twin, views [v0, v1).
+ * Restates Ax_cone_mf_cpu_new (Ax_cone_mf_cpu_new.cpp:23-235) and its norm3
+ * helper (:19-20: a double sqrt, since pow(float, int) promotes, returned as
+ * float).
+ */
+void orc_cone_gao_f32(const float *X, float *y, float *yNorm, float SO, float OD, float scale,
+                      int nx, int ny, int nz, int v0, int v1, const float *sd_phi,
+                      const float *sd_z, int na, int nb, const float *y_det, const float *z_det,
+                      const int *id_X, float dz)
+{
+    int nx2 = nx / 2, ny2 = ny / 2, nz2 = nz / 2;
+    long n = (long)nx * ny * nz, nd = (long)na * nb;
+    for (int iv = v0; iv < v1; iv++) {
+        float cphi = cosf(sd_phi[iv]), sphi = sinf(sd_phi[iv]);
+        float x1 = cphi * (-SO), y1 = sphi * (-SO), z1 = sd_z[iv];
+        for (int ib = 0; ib < nb; ib++) {
+            for (int ia = 0; ia < na; ia++) {
+                float x2 = cphi * OD - sphi * y_det[ia];
+                float y2 = sphi * OD + cphi * y_det[ia];
+                float z2 = z_det[ib] + sd_z[iv];
+                /* norm3 returns float: sqrt in double (pow(float, int) promotes), rounded
+                   to float on return, then scaled in float */
+                double ex = (double)(x1 - x2), ey = (double)(y1 - y2), ez = (double)(z1 - z2);
+                float norm = (float)sqrt(ex * ex + ey * ey + ez * ez) * scale;
+                float tmp = (x1 - x2) * (x1 - x2) + (y1 - y2) * (y1 - y2);
+                float zz = (z1 - z2) * (z1 - z2);
+                float acc = 0.0f;
+                orc_gao_vox V;
+                V.x = X + (long)id_X[iv] * n;
+                V.zstride = (long)nx * ny;
+                if (orc_absf(x1 - x2) > orc_absf(y1 - y2)) {
+                    float s1 = (y2 - y1) / (x2 - x1), s2 = (z2 - z1) / (x2 - x1);
+                    V.sstride = nx;
+                    for (int ix = 0; ix < nx; ix++) {
+                        float a1 = (float)(ix - nx2), a2 = a1 + 1;
+                        float p1, p2, q1, q2;
+                        if (s1 >= 0) { p1 = y1 + s1 * (a1 - x1) + ny2; p2 = y1 + s1 * (a2 - x1) + ny2; }
+                        else         { p1 = y1 + s1 * (a2 - x1) + ny2; p2 = y1 + s1 * (a1 - x1) + ny2; }
+                        if (s2 >= 0) { q1 = (z1 + s2 * (a1 - x1)) / dz + nz2; q2 = (z1 + s2 * (a2 - x1)) / dz + nz2; }
+                        else         { q1 = (z1 + s2 * (a2 - x1)) / dz + nz2; q2 = (z1 + s2 * (a1 - x1)) / dz + nz2; }
+                        float d = p2 - p1;
+                        float l = sqrtf((d * d + 1) * (tmp + zz) / tmp);
+                        V.base = ix;
+                        acc = orc_gao_slab(acc, p1, p2, q1, q2, l, ny, nz, &V);
+                    }
+                } else {
+                    float s1 = (x2 - x1) / (y2 - y1), s2 = (z2 - z1) / (y2 - y1);
+                    V.sstride = 1;
+                    for (int iy = 0; iy < ny; iy++) {
+                        float a1 = (float)(iy - ny2), a2 = a1 + 1;
+                        float p1, p2, q1, q2;
+                        if (s1 >= 0) { p1 = x1 + s1 * (a1 - y1) + nx2; p2 = x1 + s1 * (a2 - y1) + nx2; }
+                        else         { p1 = x1 + s1 * (a2 - y1) + nx2; p2 = x1 + s1 * (a1 - y1) + nx2; }
+                        if (s2 >= 0) { q1 = (z1 + s2 * (a1 - y1)) / dz + nz2; q2 = (z1 + s2 * (a2 - y1)) / dz + nz2; }
+                        else         { q1 = (z1 + s2 * (a2 - y1)) / dz + nz2; q2 = (z1 + s2 * (a1 - y1)) / dz + nz2; }
+                        float d = p2 - p1;
+                        float l = sqrtf((d * d + 1) * (tmp + zz) / tmp);
+                        V.base = (long)iy * nx;
+                        acc = orc_gao_slab(acc, p1, p2, q1, q2, l, nx, nz, &V);
+                    }
+                }
+                acc = acc * scale;
+                y[(long)iv * nd + (long)ib * na + ia] = acc;
+                yNorm[(long)iv * nd + (long)ib * na + ia] = acc / norm;
+            }
+        }
+    }
+}
+
+/*
+ * Fan-beam dominant-axis projection, views [v0, v1). Restates
+ * Ax_fan_mf_cpu_new (Ax_fan_mf_cpu_new.cpp:18-122), including its y-dominant
+ * edge test against ny where nx is meant (:111; equal for square images).
+ */
+void orc_fan_gao_f32(const float *X, float *y, float SO, float OD, float scale, int nx, int ny,
+                     int v0, int v1, const float *sd_phi, int nd, const float *y_det,
+                     const int *id_X)
+{
+    int nx2 = nx / 2, ny2 = ny / 2;
+    long n = (long)nx * ny;
+    for (int iv = v0; iv < v1; iv++) {
+        const float *x = X + (long)id_X[iv] * n;
+        float cphi = cosf(sd_phi[iv]), sphi = sinf(sd_phi[iv]);
+        float x1 = cphi * (-SO), y1 = sphi * (-SO);
+        for (int id = 0; id < nd; id++) {
+            float x2 = cphi * OD - sphi * y_det[id];
+            float y2 = sphi * OD + cphi * y_det[id];
+            float acc = 0.0f;
+            int xdom = orc_absf(x1 - x2) > orc_absf(y1 - y2);
+            float s = xdom ? (y2 - y1) / (x2 - x1) : (x2 - x1) / (y2 - y1);
+            float pa = xdom ? x1 : y1, pb = xdom ? y1 : x1;   /* primary, secondary start */
+            int np = xdom ? nx : ny, ns = xdom ? ny : nx;
+            int np2 = xdom ? nx2 : ny2, ns2 = xdom ? ny2 : nx2;
+            int nedge = ny;                                     /* the reference's `c2==ny` */
+            for (int ip = 0; ip < np; ip++) {
+                float a1 = (float)(ip - np2), a2 = a1 + 1;
+                float p1, p2;
+                if (s >= 0) { p1 = pb + s * (a1 - pa) + ns2; p2 = pb + s * (a2 - pa) + ns2; }
+                else        { p1 = pb + s * (a2 - pa) + ns2; p2 = pb + s * (a1 - pa) + ns2; }
+                int c1 = (int)floor(p1), c2 = (int)floor(p2);
+#define PIX(c) (xdom ? x[(long)(c) * nx + ip] : x[(long)ip * nx + (c)])
+                if (c2 == c1) {
+                    if (c1 >= 0 && c1 <= ns - 1) {
+                        float d = p2 - p1, l = sqrtf(d * d + 1);
+                        acc += l * PIX(c1);
+                    }
+                } else if (c2 > 0 && c2 < ns) {
+                    float d = p2 - p1, l = sqrtf(d * d + 1);
+                    acc += ((c2 - p1) / d) * l * PIX(c1);
+                    acc += ((p2 - c2) / d) * l * PIX(c2);
+                } else {
+                    if (c2 == 0) {
+                        float d = p2 - p1, l = sqrtf(d * d + 1);
+                        acc += ((p2 - c2) / d) * l * PIX(c2);
+                    }
+                    if (c2 == (xdom ? ny : nedge)) {
+                        float d = p2 - p1, l = sqrtf(d * d + 1);
+                        acc += ((c2 - p1) / d) * l * PIX(c1);
+                    }
+                }
+#undef PIX
+            }
+            y[(long)iv * nd + id] = acc * scale;
+        }
+    }
+}

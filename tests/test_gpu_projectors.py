@@ -290,3 +290,60 @@ def test_matched_reversed_detector_axes():
     rhs = np.dot(x.astype(np.float64), Aty.astype(np.float64))
     assert abs(lhs - rhs) / abs(lhs) < 1e-5, (lhs, rhs)
     assert _rel(Aty, O.exact_adjoint(yv, p, threads=8)) < 2e-5
+
+
+# --------------------------------------------------------------------------
+# version-1 (dominant-axis) forward, the classes' default model
+# --------------------------------------------------------------------------
+def test_gao_ref_matches_reference_fixtures():
+    for c in _golden("fan_new"):
+        y = _host(_plan(c["para"]).forward(_dev(c["x"].astype(np.float32)), model="gao_ref"))
+        assert np.array_equal(y, c["y"])
+    for c in _golden("cone_new"):
+        y, yn = _plan(c["para"]).forward_gao(_dev(c["x"].astype(np.float32)))
+        assert np.array_equal(_host(y), c["y"])
+        assert np.array_equal(_host(yn), c["extra"]["yNorm"])
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_gao_ref_random_geometries_bit_exact(seed):
+    rng = np.random.default_rng(40 + seed)
+    n = [16, 24, 32, 40][seed]
+    p = G.fan_para(n, n, 2 * n + 3, 9, L=(2, 2), SO=rng.uniform(2, 8), OD=rng.uniform(2, 8),
+                   Ly=rng.uniform(3, 9))
+    x = rng.standard_normal(n * n).astype(np.float32)
+    assert np.array_equal(_host(_plan(p).forward(_dev(x), model="gao_ref")), O.fan_gao_f32(x, p))
+    m = [8, 12, 16, 20][seed]
+    kw = dict(scan="helix", zmax=0.5, rps=1.0, vtab=1.0, fps=6) if seed % 2 else {}
+    pc = G.cone_para(m, m, m + 2, m + 4, m, 5, L=(2, 2, 2.4), SO=rng.uniform(3, 8),
+                     OD=rng.uniform(3, 8), Ly=rng.uniform(3, 9), Lz=rng.uniform(3, 9), **kw)
+    xc = rng.standard_normal(m * m * (m + 2)).astype(np.float32)
+    y, yn = _plan(pc).forward_gao(_dev(xc))
+    want, wantn = O.cone_gao_f32(xc, pc)
+    assert np.array_equal(_host(y), want) and np.array_equal(_host(yn), wantn)
+
+
+def test_gao_dropins_host_pointer_abi():
+    from framelab_gb300 import _lib
+    L = _lib.load()
+    rng = np.random.default_rng(6)
+    p = G.fan_para(24, 24, 40, 8, L=(2, 2))
+    X = rng.standard_normal(24 * 24).astype(np.float32)
+    y = np.zeros(40 * 8, np.float32)
+    sd = p["sd_phi"].copy(); yd = p["y_det"].copy(); idx = p["id_X"].astype(np.int32)
+    L.Ax_fan_mf_gpu_new(_ptr(X), _ptr(y), float(p["SO"]), float(p["OD"]), float(p["scale"]),
+                        24, 24, 8, _ptr(sd), 40, _ptr(yd), _ptr(idx), 1)
+    _lib.check_last()
+    assert np.array_equal(y, O.fan_gao_f32(X, p))
+    pc = G.cone_para(16, 16, 16, 20, 18, 6, L=(2, 2, 2))
+    Xc = rng.standard_normal(16 ** 3).astype(np.float32)
+    yc = np.zeros(20 * 18 * 6, np.float32); ycn = np.zeros_like(yc)
+    a = {k: np.ascontiguousarray(pc[k], np.float32) for k in ("sd_phi", "sd_z", "y_det", "z_det")}
+    idYc = np.asarray(pc["id_Y"]).T.reshape(-1).astype(np.int32); Nvc = pc["Nv"].astype(np.int32)
+    L.Ax_cone_mf_gpu_new(_ptr(Xc), _ptr(yc), _ptr(ycn), _ptr(a["sd_phi"]), _ptr(a["sd_z"]),
+                         _ptr(a["y_det"]), _ptr(a["z_det"]), _ptr(idYc), _ptr(Nvc),
+                         float(pc["SO"]), float(pc["OD"]), float(pc["scale"]), float(pc["dz"]),
+                         16, 16, 16, 1, 20, 18, 6, int(pc["tmp_size"]), 4)
+    _lib.check_last()
+    want, wantn = O.cone_gao_f32(Xc, pc)
+    assert np.array_equal(yc, want) and np.array_equal(ycn, wantn)

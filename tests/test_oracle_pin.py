@@ -39,6 +39,7 @@ def test_fan_restatement_is_bit_exact(seed):
     p = _rand_fan(rng, n, [12, 24, 50, 33][seed % 4], [5, 7, 16][seed % 3])
     X = rng.standard_normal(n * n).astype(np.float32)
     assert np.array_equal(O.fan_siddon_f32(X, p), O.ref_fan_siddon(X, p))
+    assert np.array_equal(O.fan_gao_f32(X, p), O.ref_fan_new(X, p))
     Y = rng.standard_normal(len(p["y_det"]) * len(p["sd_phi"])).astype(np.float32)
     assert np.array_equal(O.fan_adj_f32(Y, p), O.ref_fan_adj(Y, p))
 
@@ -52,6 +53,8 @@ def test_cone_restatement_is_bit_exact(seed):
     p = _rand_cone(rng, n, [12, 20][seed % 2], [10, 14][seed % 2], [3, 5, 9][seed % 3], scan)
     X = rng.standard_normal(n ** 3).astype(np.float32)
     assert np.array_equal(O.cone_siddon_f32(X, p), O.ref_cone_siddon(X, p))
+    (a, an), (b, bn) = O.cone_gao_f32(X, p), O.ref_cone_new(X, p)
+    assert np.array_equal(a, b) and np.array_equal(an, bn)
     Y = rng.standard_normal(len(p["y_det"]) * len(p["z_det"]) * len(p["sd_phi"])).astype(np.float32)
     assert np.array_equal(O.cone_adj_f32(Y, p), O.ref_cone_adj(Y, p))
 
@@ -77,6 +80,11 @@ def test_restatement_matches_golden(path):
         out = O.cone_siddon_f32(case["x"], p)
     elif kind == "cone_adj":
         out = O.cone_adj_f32(case["x"], p)
+    elif kind == "fan_new":
+        out = O.fan_gao_f32(case["x"], p)
+    elif kind == "cone_new":
+        out, yn = O.cone_gao_f32(case["x"], p)
+        assert np.array_equal(yn, case["extra"]["yNorm"])
     else:
-        pytest.skip(f"no restatement yet for {kind}")
+        pytest.skip(f"no restatement for {kind}")
     assert np.array_equal(out, case["y"]), kind
