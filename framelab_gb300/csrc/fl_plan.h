@@ -36,6 +36,7 @@ struct fl_plan {
     ColEntry *d_col;           // [nv*na]
     float *d_colr;             // [nv*na] fl(d_x^2 + d_y^2)
     RowEntry *d_row;           // [nv*nb]
+    float2 *d_rowz;            // [nv*nb] (inv_z, off_z): the backprojector's 8-byte copy
     ViewEntry *d_view;         // [nv]
     // detector grid for the adjoint windows (matched model)
     int det_kind;              // 0 flat uniform, 1 equiangular (fan), -1 irregular

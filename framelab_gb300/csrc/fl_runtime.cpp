@@ -62,7 +62,7 @@ static void free_plan_arrays(fl_plan* p)
     void* ptrs[] = {p->d_sd_phi, p->d_sd_z,   p->d_y_det,      p->d_z_det, p->d_cos_phi,
                     p->d_sin_phi, p->d_cos_det, p->d_sin_det,   p->d_cphi_f, p->d_sphi_f,
                     p->d_view_frame, p->d_idY, p->d_Nv,        p->d_col,   p->d_colr,
-                    p->d_row,    p->d_view,   p->d_work};
+                    p->d_row,    p->d_rowz,   p->d_view,       p->d_work};
     for (void* q : ptrs)
         if (q) cudaFree(q);
 }
@@ -129,6 +129,9 @@ static int build_tables(fl_plan* p, const std::vector<float>& phi, const float* 
     if ((st = upload(&p->d_col, col.data(), col.size()))) return st;
     if ((st = upload(&p->d_colr, colr.data(), colr.size()))) return st;
     if ((st = upload(&p->d_row, row.data(), row.size()))) return st;
+    std::vector<float2> rowz(row.size());
+    for (size_t i = 0; i < row.size(); i++) rowz[i] = make_float2(row[i].inv_z, row[i].off_z);
+    if ((st = upload(&p->d_rowz, rowz.data(), rowz.size()))) return st;
     if ((st = upload(&p->d_view, view.data(), view.size()))) return st;
 
     // detector grids for the adjoint windows

@@ -116,7 +116,7 @@ __device__ __forceinline__ float ray_cr(float scale, float dxy2, float dz2)
 // view, so a warp's rays are neighbours and their gathers share cache lines.
 // ---------------------------------------------------------------------------
 template <typename TX, typename TY>
-__global__ void __launch_bounds__(128, 8)
+__global__ void __launch_bounds__(128, 16)
 k_fwd_cone(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restrict__ col,
            const float* __restrict__ colr, const RowEntry* __restrict__ row,
            const int* __restrict__ vframe, int nx, int ny, int nz, int na, int nb,
@@ -294,7 +294,7 @@ k_adj_fan(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __re
 template <typename TX, int TZ>
 __global__ void __launch_bounds__(128, 6)
 k_adj_cone(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __restrict__ col,
-           const RowEntry* __restrict__ row, const ViewEntry* __restrict__ view,
+           const float2* __restrict__ rowz, const ViewEntry* __restrict__ view,
            const int* __restrict__ idY, const int* __restrict__ Nv, int tmp_size, DetGrid G,
            int nx, int ny, int nz, int na, int nb, float dz, int zruns,
            const int* __restrict__ skip)
@@ -319,7 +319,7 @@ k_adj_cone(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __r
         int alo, ahi; float dmin, dmax;
         column_window(G, ve.c, ve.s, x0, y0, 1.0f, 1.0f, na, alo, ahi, dmin, dmax);
         const ColEntry* cv = col + (long long)iv * na;
-        const RowEntry* rv = row + (long long)iv * nb;
+        const float2* rv = rowz + (long long)iv * nb;
         const float* yv = yw + (long long)iv * nb * na;
         const float zr0 = (float)(z0 - nz / 2) * dz - ve.sz;   // lowest plane of the run, source-relative
         for (int ia = alo; ia <= ahi; ia++) {
@@ -343,15 +343,15 @@ k_adj_cone(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __r
                 if (k >= nk) break;
                 e1 += s1; e2 += s2;
                 const float mn1 = fminf(e1, e2), mx1 = fmaxf(e1, e2);   // plane k + 1
-                const int blo = (int)fmaxf(ceilf(fminf(mn, mn1) - 0.02f), 0.0f);
-                const int bhi = (int)fminf(floorf(fmaxf(mx, mx1) + 0.02f), (float)(nb - 1));
+                const int blo = max(__float2int_ru(fminf(mn, mn1) - 0.02f), 0);
+                const int bhi = min(__float2int_rd(fmaxf(mx, mx1) + 0.02f), nb - 1);
                 mn = mn1; mx = mx1;
                 const float fk0 = (float)(z0 + k), fk1 = (float)(z0 + k + 1);
                 for (int ib = blo; ib <= bhi; ib++) {
-                    const RowEntry re = rv[ib];
+                    const float2 re = rv[ib];       // (inv_z, off_z) of row ib
                     const float yval = __ldg(ycol + (long long)ib * na);
-                    const float az0 = fmaf(fk0, re.inv_z, re.off_z);
-                    const float az1 = fmaf(fk1, re.inv_z, re.off_z);
+                    const float az0 = fmaf(fk0, re.x, re.y);
+                    const float az1 = fmaf(fk1, re.x, re.y);
                     const float l2 = fmaxf(l, fminf(az0, az1));
                     const float h2 = fminf(h, fmaxf(az0, az1));
                     // w <= 0 (the ray misses voxel k) adds exactly 0 for finite y
@@ -411,7 +411,7 @@ void launch_adj(fl_plan* p, const float* yw, void* x, const int* skip, cudaStrea
         int zruns = (s.nz + TZ - 1) / TZ;
         dim3 grid(fl_div_up(s.nx, 32), fl_div_up(s.ny, 4), (unsigned)zruns * s.nt);
         k_adj_cone<TX, TZ><<<grid, dim3(32, 4), 0, st>>>(
-            (TX*)x, yw, p->d_col, p->d_row, p->d_view, p->d_idY, p->d_Nv, p->tmp_size, G, s.nx,
+            (TX*)x, yw, p->d_col, p->d_rowz, p->d_view, p->d_idY, p->d_Nv, p->tmp_size, G, s.nx,
             s.ny, s.nz, s.na, s.nb, s.dz, zruns, skip);
     } else {
         dim3 grid(fl_div_up(s.nx, 128), s.ny, s.nt);
