@@ -291,8 +291,44 @@ k_adj_fan(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __re
 // with w_rV evaluated exactly as in the forward walk. The TZ accumulators are
 // registers (k is a compile-time index).
 // ---------------------------------------------------------------------------
+// Candidate rays of one detector column for the TZ voxels of a run. MODE +1:
+// the run lies above the source plane, so every ray that reaches it rises
+// (A_z increasing in k); MODE -1: below, every such ray falls; MODE 0: the run
+// straddles the source plane (general min/max). The other orientation's rays
+// get w <= 0 from the specialised formula, as they miss the run.
+template <int MODE, int TZ>
+__device__ __forceinline__ void adj_rows(float (&acc)[TZ], int nk, int z0, float l, float h,
+                                         float e1, float e2, float s1, float s2,
+                                         const float2* __restrict__ rv,
+                                         const float* __restrict__ ycol, int na, int nb)
+{
+    float mn = fminf(e1, e2), mx = fmaxf(e1, e2);   // row span at plane k
+#pragma unroll
+    for (int k = 0; k < TZ; k++) {
+        if (k >= nk) break;
+        e1 += s1; e2 += s2;
+        const float mn1 = fminf(e1, e2), mx1 = fmaxf(e1, e2);   // plane k + 1
+        const int blo = max(__float2int_ru(fminf(mn, mn1) - 0.02f), 0);
+        const int bhi = min(__float2int_rd(fmaxf(mx, mx1) + 0.02f), nb - 1);
+        mn = mn1; mx = mx1;
+        const float fk0 = (float)(z0 + k), fk1 = (float)(z0 + k + 1);
+        for (int ib = blo; ib <= bhi; ib++) {
+            const float2 re = rv[ib];                 // (inv_z, off_z) of row ib
+            const float yval = __ldg(ycol + (long long)ib * na);
+            const float az0 = fmaf(fk0, re.x, re.y);
+            const float az1 = fmaf(fk1, re.x, re.y);
+            float l2, h2;
+            if (MODE > 0)      { l2 = fmaxf(l, az0); h2 = fminf(h, az1); }
+            else if (MODE < 0) { l2 = fmaxf(l, az1); h2 = fminf(h, az0); }
+            else { l2 = fmaxf(l, fminf(az0, az1)); h2 = fminf(h, fmaxf(az0, az1)); }
+            // w <= 0 (the ray misses voxel k) adds exactly 0 for finite y
+            acc[k] = fmaf(fmaxf(h2 - l2, 0.0f), yval, acc[k]);
+        }
+    }
+}
+
 template <typename TX, int TZ>
-__global__ void __launch_bounds__(128, 6)
+__global__ void __launch_bounds__(128, 8)
 k_adj_cone(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __restrict__ col,
            const float2* __restrict__ rowz, const ViewEntry* __restrict__ view,
            const int* __restrict__ idY, const int* __restrict__ Nv, int tmp_size, DetGrid G,
@@ -321,7 +357,10 @@ k_adj_cone(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __r
         const ColEntry* cv = col + (long long)iv * na;
         const float2* rv = rowz + (long long)iv * nb;
         const float* yv = yw + (long long)iv * nb * na;
-        const float zr0 = (float)(z0 - nz / 2) * dz - ve.sz;   // lowest plane of the run, source-relative
+        // run planes relative to the source: lowest and highest
+        const float zr0 = (float)(z0 - nz / 2) * dz - ve.sz;
+        const float zr1 = (float)(z0 + nk - nz / 2) * dz - ve.sz;
+        const int mode = (zr0 >= 0.0f) ? 1 : ((zr1 <= 0.0f) ? -1 : 0);   // uniform per block
         for (int ia = alo; ia <= ahi; ia++) {
             const ColEntry ce = cv[ia];
             const float ax0 = fmaf(fx0, ce.inv_x, ce.off_x), ax1 = fmaf(fx1, ce.inv_x, ce.off_x);
@@ -331,33 +370,15 @@ k_adj_cone(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __r
             if (!(l < h)) continue;
             // A ray of row ib is at z = sz + (A + ac) * d_ib, d_ib ~ v0 + ib * dv. It is
             // inside voxel k somewhere in [l, h] iff d_ib lies between the plane
-            // heights over (A + ac) at the two ends: rows [e(k), e(k+1)] below, in
-            // detector-row units, stepping by dz/(A + ac)/dv per plane.
+            // heights over (A + ac) at the two ends: in detector-row units the
+            // rows [e(k), e(k+1)], stepping by dz/(A + ac)/dv per plane.
             const float r1 = __fdividef(1.0f, l + ve.ac), r2 = __fdividef(1.0f, h + ve.ac);
             const float s1 = dz * r1 * inv_dv, s2 = dz * r2 * inv_dv;
-            float e1 = (zr0 * r1 - G.v0) * inv_dv, e2 = (zr0 * r2 - G.v0) * inv_dv;
-            float mn = fminf(e1, e2), mx = fmaxf(e1, e2);   // row span at plane k
+            const float e1 = (zr0 * r1 - G.v0) * inv_dv, e2 = (zr0 * r2 - G.v0) * inv_dv;
             const float* ycol = yv + ia;
-#pragma unroll
-            for (int k = 0; k < TZ; k++) {
-                if (k >= nk) break;
-                e1 += s1; e2 += s2;
-                const float mn1 = fminf(e1, e2), mx1 = fmaxf(e1, e2);   // plane k + 1
-                const int blo = max(__float2int_ru(fminf(mn, mn1) - 0.02f), 0);
-                const int bhi = min(__float2int_rd(fmaxf(mx, mx1) + 0.02f), nb - 1);
-                mn = mn1; mx = mx1;
-                const float fk0 = (float)(z0 + k), fk1 = (float)(z0 + k + 1);
-                for (int ib = blo; ib <= bhi; ib++) {
-                    const float2 re = rv[ib];       // (inv_z, off_z) of row ib
-                    const float yval = __ldg(ycol + (long long)ib * na);
-                    const float az0 = fmaf(fk0, re.x, re.y);
-                    const float az1 = fmaf(fk1, re.x, re.y);
-                    const float l2 = fmaxf(l, fminf(az0, az1));
-                    const float h2 = fminf(h, fmaxf(az0, az1));
-                    // w <= 0 (the ray misses voxel k) adds exactly 0 for finite y
-                    acc[k] = fmaf(fmaxf(h2 - l2, 0.0f), yval, acc[k]);
-                }
-            }
+            if (mode > 0) adj_rows<1, TZ>(acc, nk, z0, l, h, e1, e2, s1, s2, rv, ycol, na, nb);
+            else if (mode < 0) adj_rows<-1, TZ>(acc, nk, z0, l, h, e1, e2, s1, s2, rv, ycol, na, nb);
+            else adj_rows<0, TZ>(acc, nk, z0, l, h, e1, e2, s1, s2, rv, ycol, na, nb);
         }
     }
     const long long base = (long long)it * nx * ny * nz + (long long)iy * nx + ix;
