@@ -360,7 +360,10 @@ k_adj_cone(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __r
         // run planes relative to the source: lowest and highest
         const float zr0 = (float)(z0 - nz / 2) * dz - ve.sz;
         const float zr1 = (float)(z0 + nk - nz / 2) * dz - ve.sz;
-        const int mode = (zr0 >= 0.0f) ? 1 : ((zr1 <= 0.0f) ? -1 : 0);   // uniform per block
+        // uniform per block; a run within rounding distance of the source plane
+        // takes the general path
+        const float tol = 1e-3f * dz;
+        const int mode = (zr0 >= tol) ? 1 : ((zr1 <= -tol) ? -1 : 0);
         for (int ia = alo; ia <= ahi; ia++) {
             const ColEntry ce = cv[ia];
             const float ax0 = fmaf(fx0, ce.inv_x, ce.off_x), ax1 = fmaf(fx1, ce.inv_x, ce.off_x);
