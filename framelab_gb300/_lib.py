@@ -15,7 +15,7 @@ _lock = threading.Lock()
 _lib = None
 
 FL_OK, FL_ERR_INVALID, FL_ERR_UNSUPPORTED, FL_ERR_CUDA, FL_ERR_ALLOC, FL_ERR_TIMEOUT = range(6)
-MODEL_SIDDON_REF, MODEL_CHORD_REF, MODEL_GAO_REF, MODEL_MATCHED = 0, 1, 2, 16
+MODEL_SIDDON_REF, MODEL_CHORD_REF, MODEL_GAO_REF, MODEL_FB_REF, MODEL_MATCHED = 0, 1, 2, 3, 16
 F32, F16, BF16 = 0, 1, 2
 
 
@@ -35,6 +35,7 @@ class Scan(C.Structure):
         ("z_det", C.c_void_p), ("cos_phi", C.c_void_p), ("sin_phi", C.c_void_p),
         ("cos_det", C.c_void_p), ("sin_det", C.c_void_p), ("view_frame", C.c_void_p),
         ("id_Y", C.c_void_p), ("Nv", C.c_void_p), ("tmp_size", C.c_int32),
+        ("cos_det2", C.c_void_p), ("sin_det2", C.c_void_p),
     ]
 
 
@@ -59,6 +60,9 @@ _SIGS = {
     "Ax_fan_mf_gpu_siddon": (None, [_V, _V, _F, _F, _F, _I, _I, _I, _V, _I, _V, _V, _I]),
     "Atx_fan_mf_gpu_new": (None, [_V, _V, _F, _F, _F, _I, _I, _V, _I, _V, _F, _F, _I, _V, _V,
                                   _I, _I, _V, _V, _V, _V]),
+    "Ax_fan_mf_gpu_new_fb": (None, [_V, _V, _F, _F, _F, _I, _I, _I, _V, _I, _V, _V, _I, _F]),
+    "Atx_fan_mf_gpu_new_fb": (None, [_V, _V, _F, _F, _F, _I, _I, _V, _I, _V, _F, _I, _V, _V,
+                                     _I, _I, _V, _V, _V, _V]),
     "Ax_cone_mf_gpu_siddon": (None, [_V, _V, _V, _V, _V, _V, _V, _V, _F, _F, _F, _F, _I, _I,
                                      _I, _I, _I, _I, _I, _I, _I]),
     "Atx_cone_mf_gpu_new": (None, [_V, _V, _V, _V, _V, _V, _V, _V, _V, _F, _F, _F, _F, _F, _F,

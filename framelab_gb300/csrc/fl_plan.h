@@ -31,6 +31,8 @@ struct fl_plan {
     float *d_sd_phi, *d_sd_z, *d_y_det, *d_z_det;
     float *d_cos_phi, *d_sin_phi, *d_cos_det, *d_sin_det;
     float *d_cphi_f, *d_sphi_f;    // cosf/sinf(sd_phi): the reference Siddon's own trig
+    float *d_cos_det2, *d_sin_det2; // [na+1] bin-edge trig (finite-beam backprojector)
+    float *d_fb_edges;             // [nv*na*6] finite-beam edge lines (Px, Py, Pd) x 2
     int32_t *d_view_frame, *d_idY, *d_Nv;
     // matched-model tables (device)
     ColEntry *d_col;           // [nv*na]
@@ -52,6 +54,8 @@ struct fl_plan {
 int fl_ref_forward(fl_plan* p, const float* x, float* y, cudaStream_t st);
 int fl_ref_adjoint(fl_plan* p, const float* y, float* x, cudaStream_t st);
 int fl_ref_gao_forward(fl_plan* p, const float* x, float* y, float* ynorm, cudaStream_t st);
+int fl_ref_fb_forward(fl_plan* p, const float* x, float* y, cudaStream_t st);
+int fl_ref_fb_adjoint(fl_plan* p, const float* y, float* x, cudaStream_t st);
 // skip: optional device flag; when *skip != 0 the kernels return at once
 // (lets a captured CGLS iteration become a no-op after convergence).
 // xscale: optional device factor applied to the gathered sum (scaled storage).

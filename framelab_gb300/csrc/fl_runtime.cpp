@@ -62,7 +62,8 @@ static void free_plan_arrays(fl_plan* p)
     void* ptrs[] = {p->d_sd_phi, p->d_sd_z,   p->d_y_det,      p->d_z_det, p->d_cos_phi,
                     p->d_sin_phi, p->d_cos_det, p->d_sin_det,   p->d_cphi_f, p->d_sphi_f,
                     p->d_view_frame, p->d_idY, p->d_Nv,        p->d_col,   p->d_colr,
-                    p->d_row,    p->d_rowz,   p->d_view,       p->d_work};
+                    p->d_row,    p->d_rowz,   p->d_view,       p->d_work,
+                    p->d_cos_det2, p->d_sin_det2, p->d_fb_edges};
     for (void* q : ptrs)
         if (q) cudaFree(q);
 }
@@ -215,6 +216,35 @@ extern "C" int fl_plan_create(const fl_scan* scan, fl_plan** out)
             sdet[ia] = (float)std::sin((double)ang);
         }
     }
+    // finite-beam bin edges: backprojector trig (cos_det2/sin_det2, given or as
+    // setPara-style singles) and the forward's edge lines with the float libm
+    // calls of Ax_fan_mf_cpu_new_fb.cpp:36-46
+    std::vector<float> cdet2(na + 1), sdet2(na + 1), fbe;
+    if (s.ndim == 2) {
+        for (int e = 0; e <= na; e++) {
+            if (s.cos_det2 && s.sin_det2) { cdet2[e] = s.cos_det2[e]; sdet2[e] = s.sin_det2[e]; }
+            else {
+                float u = (e < na) ? s.y_det[e] - s.dy_det / 2 : s.y_det[na - 1] + s.dy_det / 2;
+                float ang = (float)std::atan2((double)u, (double)(s.SO + s.OD));
+                cdet2[e] = (float)std::cos((double)ang);
+                sdet2[e] = (float)std::sin((double)ang);
+            }
+        }
+        if (s.dy_det > 0) {
+            fbe.resize((size_t)nv * na * 6);
+            const float SD = s.SO + s.OD;
+            for (int iv = 0; iv < nv; iv++)
+                for (int ia = 0; ia < na; ia++)
+                    for (int e = 0; e < 2; e++) {
+                        float u = e ? s.y_det[ia] + s.dy_det / 2 : s.y_det[ia] - s.dy_det / 2;
+                        float ang = std::atan2(u, SD);
+                        float* E = &fbe[((size_t)iv * na + ia) * 6 + 3 * e];
+                        E[0] = -std::sin(ang + phi[iv]);
+                        E[1] = std::cos(ang + phi[iv]);
+                        E[2] = s.SO * std::sin(ang);
+                    }
+        }
+    }
     std::vector<int32_t> vframe(nv, 0);
     for (int iv = 0; iv < nv; iv++) {
         vframe[iv] = s.view_frame ? s.view_frame[iv] : 0;
@@ -265,6 +295,9 @@ extern "C" int fl_plan_create(const fl_scan* scan, fl_plan** out)
     if (!st) st = upload(&p->d_cos_det, cdet.data(), na);
     if (!st) st = upload(&p->d_sin_det, sdet.data(), na);
     if (!st) st = upload(&p->d_view_frame, vframe.data(), nv);
+    if (!st && s.ndim == 2) st = upload(&p->d_cos_det2, cdet2.data(), na + 1);
+    if (!st && s.ndim == 2) st = upload(&p->d_sin_det2, sdet2.data(), na + 1);
+    if (!st && !fbe.empty()) st = upload(&p->d_fb_edges, fbe.data(), fbe.size());
     if (!st) st = upload(&p->d_idY, idY.data(), idY.size());
     if (!st) st = upload(&p->d_Nv, Nvv.data(), nt);
     if (!st) st = build_tables(p, phi, s.sd_z ? sdz.data() : nullptr, s.y_det, s.z_det);
@@ -272,6 +305,7 @@ extern "C" int fl_plan_create(const fl_scan* scan, fl_plan** out)
     p->s.sd_phi = p->s.sd_z = p->s.y_det = p->s.z_det = nullptr;
     p->s.cos_phi = p->s.sin_phi = p->s.cos_det = p->s.sin_det = nullptr;
     p->s.view_frame = p->s.id_Y = p->s.Nv = nullptr;
+    p->s.cos_det2 = p->s.sin_det2 = nullptr;
     if (st) {
         free_plan_arrays(p);
         delete p;
@@ -334,6 +368,11 @@ extern "C" int fl_forward(fl_plan* p, int model, const void* x, int xt, void* y,
             return fl_set_error(FL_ERR_UNSUPPORTED, "reference dominant-axis forward is FP32 only");
         return fl_ref_gao_forward(p, (const float*)x, (float*)y, nullptr, sm);
     }
+    if (model == FL_MODEL_FB_REF) {
+        if (xt != FL_F32 || yt != FL_F32)
+            return fl_set_error(FL_ERR_UNSUPPORTED, "reference finite-beam model is FP32 only");
+        return fl_ref_fb_forward(p, (const float*)x, (float*)y, sm);
+    }
     return fl_set_error(FL_ERR_UNSUPPORTED, "fl_forward: model %d not available", model);
 }
 
@@ -365,6 +404,11 @@ extern "C" int fl_adjoint(fl_plan* p, int model, const void* y, int yt, void* x,
         if (xt != FL_F32 || yt != FL_F32)
             return fl_set_error(FL_ERR_UNSUPPORTED, "reference backprojector is FP32 only");
         return fl_ref_adjoint(p, (const float*)y, (float*)x, sm);
+    }
+    if (model == FL_MODEL_FB_REF) {
+        if (xt != FL_F32 || yt != FL_F32)
+            return fl_set_error(FL_ERR_UNSUPPORTED, "reference finite-beam model is FP32 only");
+        return fl_ref_fb_adjoint(p, (const float*)y, (float*)x, sm);
     }
     if (model == FL_MODEL_MATCHED) {
         if ((st = fl_matched_ready(p))) return st;
@@ -570,4 +614,36 @@ extern "C" void Ax_cone_mf_gpu_new(float* X, float* y, float* yNorm, float* sd_p
     s.view_frame = vf.data();
     s.id_Y = id_Y; s.Nv = Nv; s.tmp_size = tmp_size;
     run_gao_host(s, X, y, yNorm);
+}
+
+extern "C" void Ax_fan_mf_gpu_new_fb(float* X, float* y, float SO, float OD, float scale, int nx,
+                                     int ny, int nv, float* sd_phi, int nd, float* y_det,
+                                     int* id_X, int nt, float dy_det)
+{
+    fl_scan s;
+    std::memset(&s, 0, sizeof s);
+    s.ndim = 2; s.nx = nx; s.ny = ny; s.nz = 1; s.nt = nt; s.nv = nv; s.na = nd; s.nb = 1;
+    s.SO = SO; s.OD = OD; s.scale = scale; s.dz = 1.0f; s.dy_det = dy_det;
+    s.sd_phi = sd_phi; s.y_det = y_det; s.view_frame = id_X;
+    run_forward_host(s, FL_MODEL_FB_REF, X, y);
+}
+
+extern "C" void Atx_fan_mf_gpu_new_fb(float* x, float* Y, float SO, float OD, float scale, int nx,
+                                      int ny, float* sd_phi, int nd, float* y_det, float dy_det,
+                                      int nt, int* id_Y, int* Nv, int tmp_size, int nv,
+                                      float* cos_phi, float* sin_phi, float* cos_det,
+                                      float* sin_det)
+{
+    fl_scan s;
+    std::memset(&s, 0, sizeof s);
+    s.ndim = 2; s.nx = nx; s.ny = ny; s.nz = 1; s.nt = nt; s.nv = nv; s.na = nd; s.nb = 1;
+    s.SO = SO; s.OD = OD; s.scale = scale; s.dz = 1.0f; s.dy_det = dy_det;
+    s.sd_phi = sd_phi; s.y_det = y_det; s.cos_phi = cos_phi; s.sin_phi = sin_phi;
+    s.cos_det2 = cos_det; s.sin_det2 = sin_det;
+    s.id_Y = id_Y; s.Nv = Nv; s.tmp_size = tmp_size;
+    int bad;
+    std::vector<int32_t> vf = frames_of(id_Y, Nv, nt, tmp_size, nv, &bad);
+    if (bad) { fl_set_error(FL_ERR_INVALID, "id_Y entry out of range"); return; }
+    s.view_frame = vf.data();
+    run_adjoint_host(s, FL_MODEL_FB_REF, Y, x);
 }

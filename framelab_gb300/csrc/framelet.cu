@@ -1,8 +1,8 @@
-// framelet.cu -- undecimated tensor-product framelets (piecewise linear and
-// Haar), soft-shrinkage and the fused split-Bregman update.
+// framelet.cu -- undecimated tensor-product framelets (Haar, piecewise linear,
+// piecewise cubic), soft-shrinkage and the fused split-Bregman update.
 //
 // Semantics (FraDecMultiLevel3D.m:14-47, FraRecMultiLevel3D.m:14-48,
-// ConvSymAsym3D.m:18-34, GenerateFrameletFilter.m:2-17, softThreshold.m:47-80):
+// ConvSymAsym3D.m:18-34, GenerateFrameletFilter.m:2-30, softThreshold.m:47-80):
 //  * every 1-D filter is a circular correlation, taps at offsets
 //    (t - c) * 2^(level-1) around the output sample (imfilter 'circular');
 //  * 3-D band (i, j, k): D_i along y, D_j along x, D_k along z; 2-D band
@@ -12,9 +12,9 @@
 //    band of every level but the last is never stored here;
 //  * soft-shrink sign(a) max(|a| - tau, 0) applies to every stored band except
 //    the low band of the last level.
-// Coefficient layout: level-major; inside a level, band index = base-3 digits
-// in pass order (3-D: 9i + 3j + k, 2-D: 3i + j), band 0 omitted below the last
-// level; each band is one volume (x fastest).
+// Coefficient layout: level-major; inside a level, band index = base-nf digits
+// in pass order (nf filters per axis; linear 3-D: 9i + 3j + k, 2-D: 3i + j),
+// band 0 omitted below the last level; each band is one volume (x fastest).
 //
 // Every pass is a streaming circular stencil along one axis. The last analysis
 // pass computes each band value in registers and applies the Bregman update
@@ -28,10 +28,10 @@
 
 namespace {
 
-constexpr int kMaxBands = 27;
+constexpr int kMaxBands = 125;   // cubic bank in 3-D: 5^3 bands
 
 struct Filters {
-    float f[5][5];   // up to 5 filters x 5 taps (linear: 3 x 3, haar: 2 x 3)
+    float f[5][5];   // up to 5 filters x 5 taps (linear 3 x 3, haar 2 x 3, cubic 5 x 5)
     int nf, nt;      // filters, taps
 };
 
@@ -181,6 +181,21 @@ static void set_filters(fl_framelet* w, int kind)
         for (int a = 0; a < 3; a++)
             for (int b = 0; b < 3; b++) { w->D.f[a][b] = d[a][b]; w->R.f[a][b] = r[a][b]; }
         w->D.nf = w->R.nf = 3; w->D.nt = w->R.nt = 3;
+    } else if (kind == 3) {   // piecewise cubic (GenerateFrameletFilter.m:18-30)
+        const float r6 = 2.44948974278317810f;
+        const float d[5][5] = {{1 / 16.f, 4 / 16.f, 6 / 16.f, 4 / 16.f, 1 / 16.f},
+                               {-1 / 8.f, -2 / 8.f, 0.f, 2 / 8.f, 1 / 8.f},
+                               {-r6 / 16, 0.f, 2 * r6 / 16, 0.f, -r6 / 16},
+                               {-1 / 8.f, 2 / 8.f, 0.f, -2 / 8.f, 1 / 8.f},
+                               {-1 / 16.f, 4 / 16.f, -6 / 16.f, 4 / 16.f, -1 / 16.f}};
+        const float r[5][5] = {{1 / 16.f, 4 / 16.f, 6 / 16.f, 4 / 16.f, 1 / 16.f},
+                               {1 / 8.f, 2 / 8.f, 0.f, -2 / 8.f, -1 / 8.f},
+                               {-r6 / 16, 0.f, 2 * r6 / 16, 0.f, -r6 / 16},
+                               {1 / 8.f, -2 / 8.f, 0.f, 2 / 8.f, -1 / 8.f},
+                               {-1 / 16.f, 4 / 16.f, -6 / 16.f, 4 / 16.f, -1 / 16.f}};
+        for (int a = 0; a < 5; a++)
+            for (int b = 0; b < 5; b++) { w->D.f[a][b] = d[a][b]; w->R.f[a][b] = r[a][b]; }
+        w->D.nf = w->R.nf = 5; w->D.nt = w->R.nt = 5;
     } else {           // Haar (GenerateFrameletFilter.m:2-8)
         const float d[2][3] = {{0.0f, 0.5f, 0.5f}, {0.0f, -0.5f, 0.5f}};
         const float r[2][3] = {{0.5f, 0.5f, 0.0f}, {0.5f, -0.5f, 0.0f}};
@@ -194,7 +209,7 @@ extern "C" int fl_framelet_create(int nx, int ny, int nz, int levels, int kind, 
 {
     if (!out || nx < 1 || ny < 1 || nz < 1 || levels < 1 || levels > 8)
         return fl_set_error(FL_ERR_INVALID, "fl_framelet_create: bad size or levels");
-    if (kind != FL_FRAMELET_LINEAR && kind != FL_FRAMELET_HAAR)
+    if (kind != FL_FRAMELET_LINEAR && kind != FL_FRAMELET_HAAR && kind != FL_FRAMELET_CUBIC)
         return fl_set_error(FL_ERR_INVALID, "fl_framelet_create: unknown filter bank %d", kind);
     *out = nullptr;
     fl_framelet* w = new (std::nothrow) fl_framelet;

@@ -565,6 +565,142 @@ k_ref_fan_gao(const float* __restrict__ X, float* __restrict__ y,
     y[(long long)iv * nd + id] = fmul(acc, scale);
 }
 
+// ---------------------------------------------------------------------------
+// Finite-size beam fan pair (version 2): Ax_fan_mf_cpu_new_fb.cpp:19-123,
+// Atx_fan_mf_cpu_new_fb.cpp:20-66, find_area.cpp:18-70.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float edge_area(float a, float b, float c, float x, float y, int& sgn)
+{
+    const float aa = fabs_ref(a), bb = fabs_ref(b);
+    const float hx = fdiv(aa, 2.0f), hy = fdiv(bb, 2.0f);
+    const float reach = fadd(hx, hy);
+    const float off = fsub(fsub(c, fmul(a, x)), fmul(b, y));
+    const float d = fabs_ref(off);
+    sgn = off > 0.0f ? 1 : -1;
+    if (!(d < reach)) return 0.5f;
+    const float flat = fabs_ref(fsub(hx, hy));
+    const float inv = (hx < hy) ? fdiv(1.0f, bb) : fdiv(1.0f, aa);
+    if (d <= flat) return fmul(d, inv);
+    const float r = fsub(reach, d);
+    return fsub(0.5f, fdiv(fmul(fmul(0.5f, r), r), fmul(aa, bb)));
+}
+
+__device__ __forceinline__ float beam_area(float a1, float b1, float c1, float a2, float b2,
+                                           float c2, float x, float y)
+{
+    int s1, s2;
+    const float A1 = edge_area(a1, b1, c1, x, y, s1);
+    const float A2 = edge_area(a2, b2, c2, x, y, s2);
+    return fabs_ref(fsub(A1, fmul((float)(s1 * s2), A2)));
+}
+
+// edges: per (view, bin, edge e) the beam-edge line (Px, Py, Pd), evaluated on
+// the host with the float libm calls the reference makes.
+__global__ void __launch_bounds__(128)
+k_ref_fan_fb(const float* __restrict__ X, float* __restrict__ y,
+             const float* __restrict__ cphi_v, const float* __restrict__ sphi_v,
+             const float* __restrict__ ydet, const float* __restrict__ edges,
+             const int* __restrict__ vframe, float SO, float OD, float scale, float dy_det,
+             int nx, int ny, int nd, long long nper)
+{
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    const int iv = blockIdx.y;
+    if (id >= nd) return;
+    const float* x = X + (long long)vframe[iv] * nper;
+    const int nx2 = nx / 2, ny2 = ny / 2;
+    const float c = cphi_v[iv], s = sphi_v[iv];
+    const float x1 = fmul(c, -SO), y1 = fmul(s, -SO);
+    const float hd = fdiv(dy_det, 2.0f);
+    const float u0 = fsub(ydet[id], hd), u1 = fadd(ydet[id], hd);
+    const float x20 = fsub(fmul(c, OD), fmul(s, u0)), y20 = fadd(fmul(s, OD), fmul(c, u0));
+    const float x21 = fsub(fmul(c, OD), fmul(s, u1)), y21 = fadd(fmul(s, OD), fmul(c, u1));
+    const float* E = edges + ((long long)iv * nd + id) * 6;
+    const float Px0 = E[0], Py0 = E[1], Pd0 = E[2], Px1 = E[3], Py1 = E[4], Pd1 = E[5];
+    const bool xdom = fabs_ref(fsub(x1, fdiv(fadd(x20, x21), 2.0f))) >
+                      fabs_ref(fsub(y1, fdiv(fadd(y20, y21), 2.0f)));
+    const float p1 = xdom ? x1 : y1, q1 = xdom ? y1 : x1;
+    const float pe0 = xdom ? x20 : y20, pe1 = xdom ? x21 : y21;
+    const float qe0 = xdom ? y20 : x20, qe1 = xdom ? y21 : x21;
+    const int np = xdom ? nx : ny, nq = xdom ? ny : nx;
+    const int np2 = xdom ? nx2 : ny2, nq2 = xdom ? ny2 : nx2;
+    const bool degen = !(pe0 != p1 && pe1 != p1);
+    float s0 = 0.0f, s1 = 0.0f;
+    if (!degen) { s0 = fdiv(fsub(qe0, q1), fsub(pe0, p1)); s1 = fdiv(fsub(qe1, q1), fsub(pe1, p1)); }
+    float acc = 0.0f;
+    for (int ip = 0; ip < np; ip++) {
+        const float pc = (float)(ip - np2) + 0.5f;
+        const float a1 = (float)(ip - np2), a2 = fadd(a1, 1.0f);
+        int qmin, qmax;
+        if (degen) {
+            if (fabs_ref(fsub(p1, pc)) <= 0.5f) { qmin = 0; qmax = nq - 1; }
+            else { qmin = 1; qmax = 0; }
+        } else {
+            const int c0 = (int)floorf(fadd(fadd(q1, fmul(s0, fsub(a1, p1))), (float)nq2));
+            const int c1 = (int)floorf(fadd(fadd(q1, fmul(s0, fsub(a2, p1))), (float)nq2));
+            const int c2 = (int)floorf(fadd(fadd(q1, fmul(s1, fsub(a1, p1))), (float)nq2));
+            const int c3 = (int)floorf(fadd(fadd(q1, fmul(s1, fsub(a2, p1))), (float)nq2));
+            qmin = nq - 1; qmax = 0;
+            // only in-range crossings move the bounds (Ax_fan_mf_cpu_new_fb.cpp:62-67)
+            const int cc[4] = {c0, c1, c2, c3};
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                if (cc[k] < qmin && cc[k] >= 0) qmin = cc[k];
+                if (cc[k] > qmax && cc[k] <= nq - 1) qmax = cc[k];
+            }
+        }
+        for (int iq = qmin; iq <= qmax; iq++) {
+            const float qc = (float)(iq - nq2) + 0.5f;
+            const float l = beam_area(Px0, Py0, Pd0, Px1, Py1, Pd1, xdom ? pc : qc, xdom ? qc : pc);
+            if (l > 0.0f)
+                acc = fadd(acc, fmul(l, __ldg(xdom ? x + (long long)iq * nx + ip
+                                                  : x + (long long)ip * nx + iq)));
+        }
+    }
+    y[(long long)iv * nd + id] = fmul(acc, scale);
+}
+
+__global__ void __launch_bounds__(128)
+k_ref_fan_fb_adj(float* __restrict__ x, const float* __restrict__ Y,
+                 const float* __restrict__ cos_phi, const float* __restrict__ sin_phi,
+                 const float* __restrict__ cos_e, const float* __restrict__ sin_e,
+                 const int* __restrict__ idY, const int* __restrict__ Nv, int tmp_size,
+                 float SO, float OD, float scale, float dy_det, int nx, int ny, int nd, int nt)
+{
+    const int ix = blockIdx.x * blockDim.x + threadIdx.x;
+    const int iy = blockIdx.y, it = blockIdx.z;
+    if (ix >= nx) return;
+    const int nd2 = nd / 2, nx2 = nx / 2, ny2 = ny / 2;
+    const float SD = fadd(SO, OD);
+    const float yc = (float)(iy - ny2) + 0.5f, xc = (float)(ix - nx2) + 0.5f;
+    float acc = 0.0f;
+    const int nvf = Nv[it];
+    for (int j = 0; j < nvf; j++) {
+        const int iv = idY[it * tmp_size + j];
+        const float* yv = Y + (long long)iv * nd;
+        const float c = cos_phi[iv], s = sin_phi[iv];
+        const float xr = fadd(fmul(c, xc), fmul(s, yc));
+        const float yr = fadd(fmul(-s, xc), fmul(c, yc));
+        const float g = fdiv(SD, fmul(fadd(xr, SO), dy_det));
+        int hi = (int)floorf(fadd(fmul(fadd(yr, 1.0f), g), (float)nd2));
+        int lo = (int)floorf(fadd(fmul(fsub(yr, 1.0f), g), (float)nd2));
+        lo = max(lo, 0);
+        hi = min(hi, nd - 1);
+        for (int id = lo; id <= hi; id++) {
+            const float sd0 = __ldg(sin_e + id), cd0 = __ldg(cos_e + id);
+            const float sd1 = __ldg(sin_e + id + 1), cd1 = __ldg(cos_e + id + 1);
+            const float Px0 = -fadd(fmul(sd0, c), fmul(cd0, s));
+            const float Py0 = fsub(fmul(cd0, c), fmul(sd0, s));
+            const float Pd0 = fmul(SO, sd0);
+            const float Px1 = -fadd(fmul(sd1, c), fmul(cd1, s));
+            const float Py1 = fsub(fmul(cd1, c), fmul(sd1, s));
+            const float Pd1 = fmul(SO, sd1);
+            const float l = beam_area(Px0, Py0, Pd0, Px1, Py1, Pd1, xc, yc);
+            if (l > 0.0f) acc = fadd(acc, fmul(l, __ldg(yv + id)));
+        }
+    }
+    x[(long long)it * nx * ny + (long long)iy * nx + ix] = fmul(acc, scale);
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -628,4 +764,27 @@ int fl_ref_gao_forward(fl_plan* p, const float* x, float* y, float* ynorm, cudaS
                                              s.scale, s.nx, s.ny, s.nz, s.dz, s.na, s.nb, nper);
     }
     return fl_check_launch("reference dominant-axis forward");
+}
+
+int fl_ref_fb_forward(fl_plan* p, const float* x, float* y, cudaStream_t st)
+{
+    const fl_scan& s = p->s;
+    if (s.ndim != 2) return fl_set_error(FL_ERR_UNSUPPORTED, "finite-beam model is fan-beam only");
+    if (!p->d_fb_edges) return fl_set_error(FL_ERR_INVALID, "finite-beam model needs dy_det > 0");
+    dim3 grid(fl_div_up(s.na, 128), s.nv);
+    k_ref_fan_fb<<<grid, 128, 0, st>>>(x, y, p->d_cphi_f, p->d_sphi_f, p->d_y_det, p->d_fb_edges,
+                                       p->d_view_frame, s.SO, s.OD, s.scale, s.dy_det, s.nx,
+                                       s.ny, s.na, (long long)s.nx * s.ny);
+    return fl_check_launch("reference finite-beam forward");
+}
+
+int fl_ref_fb_adjoint(fl_plan* p, const float* y, float* x, cudaStream_t st)
+{
+    const fl_scan& s = p->s;
+    if (s.ndim != 2) return fl_set_error(FL_ERR_UNSUPPORTED, "finite-beam model is fan-beam only");
+    dim3 grid(fl_div_up(s.nx, 128), s.ny, s.nt);
+    k_ref_fan_fb_adj<<<grid, 128, 0, st>>>(x, y, p->d_cos_phi, p->d_sin_phi, p->d_cos_det2,
+                                           p->d_sin_det2, p->d_idY, p->d_Nv, p->tmp_size, s.SO,
+                                           s.OD, s.scale, s.dy_det, s.nx, s.ny, s.na, s.nt);
+    return fl_check_launch("reference finite-beam backprojection");
 }

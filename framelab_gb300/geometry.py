@@ -61,8 +61,15 @@ def fan_para(nx: int, ny: int, nd: int, nv: int, L=(10.0, 10.0), SO=5.0, OD=5.0,
     angle_det = np.arctan2(y_det.astype(np.float64),
                            np.float64(f32(SOs + ODs))).astype(np.float32)
     id_X, id_Y, Nv, tmp = _frame_tables(len(sd_phi))
+    # bin edges for the finite-beam model (version 2): cos_det2/sin_det2, nd + 1
+    # entries, read by Atx_fan_mf.cpp:38-44
+    k = (-nd / 2.0 + np.arange(nd + 1, dtype=np.float64)).astype(np.float32)
+    edges = ((k * dy_det + f32(y_os)) / scale).astype(np.float32)
+    angle_edge = np.arctan2(edges.astype(np.float64),
+                            np.float64(f32(SOs + ODs))).astype(np.float32)
     return dict(
         SO=f32(SOs), OD=f32(ODs), dy_det=f32(dy_det / scale), y_os=f32(0.0),
+        cos_det2=_single_trig(np.cos, angle_edge), sin_det2=_single_trig(np.sin, angle_edge),
         scale=scale, nx=u32(nx), ny=u32(ny), nt=u32(1), sd_phi=sd_phi, y_det=y_det,
         cos_phi=_single_trig(np.cos, sd_phi), sin_phi=_single_trig(np.sin, sd_phi),
         cos_det=_single_trig(np.cos, angle_det), sin_det=_single_trig(np.sin, angle_det),

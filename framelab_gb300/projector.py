@@ -7,6 +7,8 @@ PyTorch CUDA stream. Models:
 * ``"siddon_ref"`` -- version 0, bit-exact with ``Ax_*_mf_cpu_siddon``
 * ``"chord_ref"``  -- version 1 backprojector, bit-exact with ``Atx_*_mf_cpu_new``
 * ``"gao_ref"``    -- version 1 forward, bit-exact with ``Ax_*_mf_cpu_new``
+* ``"fb_ref"``     -- version 2 fan pair (finite-size beam), bit-exact with
+  ``Ax_fan_mf_cpu_new_fb`` / ``Atx_fan_mf_cpu_new_fb``
 * ``"matched"``    -- matched Siddon pair; the adjoint is the exact transpose
 """
 from __future__ import annotations
@@ -19,7 +21,8 @@ import torch
 from . import _lib
 
 MODELS = {"siddon_ref": _lib.MODEL_SIDDON_REF, "chord_ref": _lib.MODEL_CHORD_REF,
-          "gao_ref": _lib.MODEL_GAO_REF, "matched": _lib.MODEL_MATCHED}
+          "gao_ref": _lib.MODEL_GAO_REF, "fb_ref": _lib.MODEL_FB_REF,
+          "matched": _lib.MODEL_MATCHED}
 DTYPES = {torch.float32: _lib.F32, torch.float16: _lib.F16, torch.bfloat16: _lib.BF16}
 
 
@@ -70,6 +73,7 @@ class Plan:
         s.cos_phi, s.sin_phi = ptr("cos_phi"), ptr("sin_phi")
         if not cone:
             s.cos_det, s.sin_det = ptr("cos_det"), ptr("sin_det")
+            s.cos_det2, s.sin_det2 = ptr("cos_det2"), ptr("sin_det2")
         s.view_frame = ptr("id_X", np.int32)
         if "id_Y" in para and "Nv" in para:
             idY = np.asarray(para["id_Y"])

@@ -26,7 +26,7 @@ _lib.declare("fl_framelet_synthesis", C.c_int, [_V, _V, _V, _V])
 _lib.declare("fl_framelet_bregman", C.c_int, [_V, _V, _V, _V, _V, C.c_float, C.c_float, _V, _V])
 _lib.declare("fl_sb_solve", C.c_int, [_V, _V, _V, C.c_float, C.c_float, C.c_int, C.c_int,
                                       C.c_double, C.c_int, C.c_int, C.c_int, _V, _V])
-KINDS = {"haar": 0, "linear": 1}
+KINDS = {"haar": 0, "linear": 1, "cubic": 3}
 
 
 def _stream():

@@ -65,6 +65,23 @@ void Atx_fan_mf_gpu_new(float *x, float *Y, float SO, float OD, float scale, int
                         int *id_Y, int *Nv, int tmp_size, int nv, float *cos_phi,
                         float *sin_phi, float *cos_det, float *sin_det);
 
+/* Fan-beam finite-size-beam projection (version 2), bit-exact with the
+ * reference's Ax_fan_mf_cpu_new_fb (pixel area between the bin's two edge
+ * rays). Replaces Ax_fan_mf_gpu_new_fb (matlab/mex/src/Ax_fan_mf.h:13,
+ * Ax_fan_mf_gpu_new_fb.cu:138-164). */
+void Ax_fan_mf_gpu_new_fb(float *X, float *y, float SO, float OD, float scale, int nx, int ny,
+                          int nv, float *sd_phi, int nd, float *y_det, int *id_X, int nt,
+                          float dy_det);
+
+/* Fan-beam finite-size-beam backprojection (version 2), bit-exact with the
+ * reference's Atx_fan_mf_cpu_new_fb; cos_det/sin_det are the nd + 1 bin-edge
+ * arrays the gateway reads from cos_det2/sin_det2. Replaces
+ * Atx_fan_mf_gpu_new_fb (matlab/mex/src/Atx_fan_mf.h:13, Atx_fan_mf_gpu_new_fb.cu:81-111). */
+void Atx_fan_mf_gpu_new_fb(float *x, float *Y, float SO, float OD, float scale, int nx, int ny,
+                           float *sd_phi, int nd, float *y_det, float dy_det, int nt, int *id_Y,
+                           int *Nv, int tmp_size, int nv, float *cos_phi, float *sin_phi,
+                           float *cos_det, float *sin_det);
+
 /* Cone-beam Siddon projection (version 0), bit-exact with the reference's
  * CPU kernel Ax_cone_mf_cpu_siddon (the reference's own GPU version of this
  * entry point divides by the wrong z step). Replaces Ax_cone_mf_gpu_siddon
@@ -133,6 +150,8 @@ typedef struct fl_scan {
                                 from view_frame in increasing view order */
     const int32_t *Nv;       /* [nt] */
     int32_t tmp_size;
+    const float *cos_det2;   /* [na+1] fan bin-edge trig (finite beam), NULL = computed */
+    const float *sin_det2;   /* [na+1] */
 } fl_scan;
 
 typedef struct fl_plan fl_plan;
@@ -142,6 +161,7 @@ enum {
     FL_MODEL_SIDDON_REF = 0, /* version 0: bit-exact reference Siddon forward */
     FL_MODEL_CHORD_REF = 1,  /* version 1 adjoint: bit-exact reference chord backprojector */
     FL_MODEL_GAO_REF = 2,    /* version 1 forward: bit-exact reference dominant-axis projector */
+    FL_MODEL_FB_REF = 3,     /* version 2 fan pair: bit-exact reference finite-size beam */
     FL_MODEL_MATCHED = 16    /* matched Siddon pair; adjoint is the exact transpose */
 };
 
@@ -224,7 +244,7 @@ int fl_cgls_solve(fl_cgls *cg, const float *b, float *u, float lam, int iters, d
 /* solveSplitBregman.m:15-41)                                                */
 /* ------------------------------------------------------------------------ */
 typedef struct fl_framelet fl_framelet;
-enum { FL_FRAMELET_HAAR = 0, FL_FRAMELET_LINEAR = 1 };
+enum { FL_FRAMELET_HAAR = 0, FL_FRAMELET_LINEAR = 1, FL_FRAMELET_CUBIC = 3 };
 
 /* Undecimated tensor-product framelet on nx*ny*nz volumes (nz == 1: the 2-D
  * transform), `levels` levels, filter bank `kind` (GenerateFrameletFilter.m).

@@ -375,3 +375,62 @@ def fan_gao_f32(X, p, threads=1, views=None):
     rng = [(v0 + a, v0 + b) for a, b in _split(v1 - v0, threads * 4 if threads > 1 else 1)]
     _run(go, rng, threads)
     return y
+
+
+# --------------------------------------------------------------------------
+# finite-size beam fan pair (version 2)
+# --------------------------------------------------------------------------
+def fan_fb_f32(X, p, threads=1):
+    """Ax_fan_mf_cpu_new_fb (Ax_fan_mf_cpu_new_fb.cpp:19-123)."""
+    L = lib()
+    X = _f(X); sd = _f(p["sd_phi"]); yd = _f(p["y_det"]); idx = _i(p["id_X"])
+    nv, nd = len(sd), len(yd)
+    y = np.zeros(nv * nd, np.float32)
+
+    def go(a, b):
+        L.orc_fan_fb_f32(P(X), P(y), F(p["SO"]), F(p["OD"]), F(p["scale"]), I(int(p["nx"])),
+                         I(int(p["ny"])), I(a), I(b), P(sd), I(nd), P(yd), P(idx),
+                         F(p["dy_det"]))
+    _run(go, _split(nv, threads * 4 if threads > 1 else 1), threads)
+    return y
+
+
+def fan_fb_adj_f32(Y, p, threads=1):
+    """Atx_fan_mf_cpu_new_fb (Atx_fan_mf_cpu_new_fb.cpp:20-66), edges cos_det2/sin_det2."""
+    L = lib()
+    Y = _f(Y); cp = _f(p["cos_phi"]); sp = _f(p["sin_phi"]); cd = _f(p["cos_det2"])
+    sdt = _f(p["sin_det2"]); idY = _i(np.asarray(p["id_Y"]).T.reshape(-1)); Nv = _i(p["Nv"])
+    nx, ny, nt = int(p["nx"]), int(p["ny"]), int(p["nt"])
+    nd = len(p["y_det"])
+    x = np.zeros(nx * ny * nt, np.float32)
+
+    def go(a, b):
+        L.orc_fan_fb_adj_f32(P(x), P(Y), F(p["SO"]), F(p["OD"]), F(p["scale"]), I(nx), I(ny),
+                             I(nd), F(p["dy_det"]), I(nt), P(idY), P(Nv), I(int(p["tmp_size"])),
+                             P(cp), P(sp), P(cd), P(sdt), I(a), I(b))
+    _run(go, _split(ny, threads * 4 if threads > 1 else 1), threads)
+    return x
+
+
+def ref_fan_fb(X, p):
+    R = _need_ref()
+    X = _f(X); sd = _f(p["sd_phi"]); yd = _f(p["y_det"]); idx = _i(p["id_X"])
+    y = np.zeros(len(sd) * len(yd), np.float32)
+    R.ref_Ax_fan_mf_cpu_new_fb(P(X), P(y), F(p["SO"]), F(p["OD"]), F(p["scale"]),
+                               I(int(p["nx"])), I(int(p["ny"])), I(len(sd)), P(sd), I(len(yd)),
+                               P(yd), P(idx), F(p["dy_det"]))
+    return y
+
+
+def ref_fan_fb_adj(Y, p):
+    R = _need_ref()
+    Y = _f(Y); sd = _f(p["sd_phi"]); yd = _f(p["y_det"]); cp = _f(p["cos_phi"])
+    sp = _f(p["sin_phi"]); cd = _f(p["cos_det2"]); sdt = _f(p["sin_det2"])
+    idY = _i(np.asarray(p["id_Y"]).T.reshape(-1)); Nv = _i(p["Nv"])
+    nx, ny, nt = int(p["nx"]), int(p["ny"]), int(p["nt"])
+    x = np.zeros(nx * ny * nt, np.float32)
+    R.ref_Atx_fan_mf_cpu_new_fb(P(x), P(Y), F(p["SO"]), F(p["OD"]), F(p["scale"]), I(nx), I(ny),
+                                P(sd), I(len(yd)), P(yd), F(p["dy_det"]), I(nt), P(idY), P(Nv),
+                                I(int(p["tmp_size"])), I(int(p["nv"])), P(cp), P(sp), P(cd),
+                                P(sdt))
+    return x

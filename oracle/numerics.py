@@ -24,10 +24,18 @@ LINEAR_D = [np.array([1, 2, 1]) / 4, -np.array([1, 0, -1]) / 4 * SQ2, np.array([
 LINEAR_R = [np.array([1, 2, 1]) / 4, -np.array([-1, 0, 1]) / 4 * SQ2, np.array([-1, 2, -1]) / 4]
 HAAR_D = [np.array([0, 1, 1]) / 2, -np.array([0, 1, -1]) / 2]
 HAAR_R = [np.array([1, 1, 0]) / 2, -np.array([-1, 1, 0]) / 2]
+SQ6 = np.sqrt(6.0)
+CUBIC_D = [np.array([1, 4, 6, 4, 1]) / 16, -np.array([1, 2, 0, -2, -1]) / 8,
+           np.array([-1, 0, 2, 0, -1]) / 16 * SQ6, np.array([-1, 2, 0, -2, 1]) / 8,
+           -np.array([1, -4, 6, -4, 1]) / 16]
+CUBIC_R = [np.array([1, 4, 6, 4, 1]) / 16, -np.array([-1, -2, 0, 2, 1]) / 8,
+           np.array([-1, 0, 2, 0, -1]) / 16 * SQ6, np.array([1, -2, 0, 2, -1]) / 8,
+           -np.array([1, -4, 6, -4, 1]) / 16]
 
 
 def filters(kind="linear"):
-    return (LINEAR_D, LINEAR_R) if kind == "linear" else (HAAR_D, HAAR_R)
+    return {"linear": (LINEAR_D, LINEAR_R), "haar": (HAAR_D, HAAR_R),
+            "cubic": (CUBIC_D, CUBIC_R)}[kind]
 
 
 def corr_circ(a, m, axis, level):

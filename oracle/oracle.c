@@ -778,3 +778,154 @@ void orc_fan_gao_f32(const float *X, float *y, float SO, float OD, float scale, 
         }
     }
 }
+
+/* ------------------------------------------------------------------------- */
+/* (1d) Finite-size beam fan projector pair (version 2), FP32 reference arithmetic */
+/* ------------------------------------------------------------------------- */
+
+/* Area of the unit pixel at (x, y) on one side of the line a*x + b*y = c,
+   measured from the line (half-plane split), as find_area.cpp:18-70 computes
+   it for each beam edge; returns the area and the side (+1 / -1). */
+static float orc_edge_area(float a, float b, float c, float x, float y, int *sgn)
+{
+    float aa = orc_absf(a), bb = orc_absf(b);
+    float hx = aa / 2, hy = bb / 2;
+    float reach = hx + hy;
+    float off = c - a * x - b * y;
+    float d = orc_absf(off);
+    *sgn = off > 0 ? 1 : -1;
+    if (!(d < reach)) return (float)0.5;
+    float flat = orc_absf(hx - hy);
+    float inv = (hx < hy) ? (float)1.0 / bb : (float)1.0 / aa;
+    if (d <= flat) return d * inv;
+    return (float)0.5 - (float)0.5 * (reach - d) * (reach - d) / (aa * bb);
+}
+
+/* find_area (find_area.cpp:18-70): pixel area between two beam edges. */
+float orc_beam_area(float a1, float b1, float c1, float a2, float b2, float c2, float x,
+                    float y)
+{
+    int s1, s2;
+    float A1 = orc_edge_area(a1, b1, c1, x, y, &s1);
+    float A2 = orc_edge_area(a2, b2, c2, x, y, &s2);
+    float t = A1 - (float)(s1 * s2) * A2;
+    return orc_absf(t);
+}
+
+/*
+ * Finite-beam fan projection of views [v0, v1). Restates Ax_fan_mf_cpu_new_fb
+ * (Ax_fan_mf_cpu_new_fb.cpp:19-123), including its candidate-row bounds that
+ * keep only in-range crossings (a beam half outside the image may skip rows)
+ * and its float trigonometry of the edge angles. Where a beam edge is exactly
+ * parallel to the walked axis and the pixel centre is farther than 0.5 the
+ * reference reads bounds it never set; that degenerate case is empty here.
+ */
+void orc_fan_fb_f32(const float *X, float *y, float SO, float OD, float scale, int nx, int ny,
+                    int v0, int v1, const float *sd_phi, int nd, const float *y_det,
+                    const int *id_X, float dy_det)
+{
+    int nx2 = nx / 2, ny2 = ny / 2;
+    long n = (long)nx * ny;
+    float SD = SO + OD;
+    for (int iv = v0; iv < v1; iv++) {
+        const float *x = X + (long)id_X[iv] * n;
+        float cphi = cosf(sd_phi[iv]), sphi = sinf(sd_phi[iv]);
+        float x1 = cphi * (-SO), y1 = sphi * (-SO);
+        for (int id = 0; id < nd; id++) {
+            float x2[2], y2[2], Px[2], Py[2], Pd[2];
+            for (int e = 0; e < 2; e++) {
+                float u = e ? y_det[id] + dy_det / 2 : y_det[id] - dy_det / 2;
+                x2[e] = cphi * OD - sphi * u;
+                y2[e] = sphi * OD + cphi * u;
+                float ang = atan2f(u, SD);
+                Px[e] = -sinf(ang + sd_phi[iv]);
+                Py[e] = cosf(ang + sd_phi[iv]);
+                Pd[e] = SO * sinf(ang);
+            }
+            float acc = 0.0f;
+            int xdom = orc_absf(x1 - (x2[0] + x2[1]) / 2) > orc_absf(y1 - (y2[0] + y2[1]) / 2);
+            float p1 = xdom ? x1 : y1, q1 = xdom ? y1 : x1;        /* walked, other */
+            float pe0 = xdom ? x2[0] : y2[0], pe1 = xdom ? x2[1] : y2[1];
+            float qe0 = xdom ? y2[0] : x2[0], qe1 = xdom ? y2[1] : x2[1];
+            int np = xdom ? nx : ny, nq = xdom ? ny : nx;
+            int np2 = xdom ? nx2 : ny2, nq2 = xdom ? ny2 : nx2;
+            int degen = !(pe0 != p1 && pe1 != p1);
+            float s0 = 0, s1 = 0;
+            if (!degen) { s0 = (qe0 - q1) / (pe0 - p1); s1 = (qe1 - q1) / (pe1 - p1); }
+            for (int ip = 0; ip < np; ip++) {
+                float pc = (float)(ip + 0.5 - np2);
+                float a1 = (float)(ip - np2), a2 = a1 + 1;
+                int qmin, qmax;
+                if (degen) {
+                    if (orc_absf(p1 - pc) <= 0.5) { qmin = 0; qmax = nq - 1; }
+                    else { qmin = 1; qmax = 0; }
+                } else {
+                    int c[4];
+                    c[0] = (int)floor(q1 + s0 * (a1 - p1) + nq2);
+                    c[1] = (int)floor(q1 + s0 * (a2 - p1) + nq2);
+                    c[2] = (int)floor(q1 + s1 * (a1 - p1) + nq2);
+                    c[3] = (int)floor(q1 + s1 * (a2 - p1) + nq2);
+                    qmin = nq - 1; qmax = 0;
+                    for (int k = 0; k < 4; k++) {
+                        if (c[k] < qmin && c[k] >= 0) qmin = c[k];
+                        if (c[k] > qmax && c[k] <= nq - 1) qmax = c[k];
+                    }
+                }
+                for (int iq = qmin; iq <= qmax; iq++) {
+                    float qc = (float)(iq + 0.5 - nq2);
+                    float xc = xdom ? pc : qc, yc = xdom ? qc : pc;
+                    float l = orc_beam_area(Px[0], Py[0], Pd[0], Px[1], Py[1], Pd[1], xc, yc);
+                    if (l > 0) acc += l * (xdom ? x[(long)iq * nx + ip] : x[(long)ip * nx + iq]);
+                }
+            }
+            y[(long)iv * nd + id] = acc * scale;
+        }
+    }
+}
+
+/*
+ * Finite-beam fan backprojection for image rows [iy0, iy1). Restates
+ * Atx_fan_mf_cpu_new_fb (Atx_fan_mf_cpu_new_fb.cpp:20-66); cos_det/sin_det hold
+ * the nd + 1 bin-edge angles (the gateway's cos_det2/sin_det2).
+ */
+void orc_fan_fb_adj_f32(float *x, const float *Y, float SO, float OD, float scale, int nx,
+                        int ny, int nd, float dy_det, int nt, const int *id_Y, const int *Nv,
+                        int tmp_size, const float *cos_phi, const float *sin_phi,
+                        const float *cos_det, const float *sin_det, int iy0, int iy1)
+{
+    int nd2 = nd / 2, nx2 = nx / 2, ny2 = ny / 2;
+    float SD = SO + OD;
+    long n = (long)nx * ny;
+    for (int iy = iy0; iy < iy1; iy++) {
+        float yc = (float)(iy + 0.5 - ny2);
+        for (int ix = 0; ix < nx; ix++) {
+            float xc = (float)(ix + 0.5 - nx2);
+            for (int it = 0; it < nt; it++) {
+                float acc = 0.0f;
+                for (int j = 0; j < Nv[it]; j++) {
+                    int iv = id_Y[it * tmp_size + j];
+                    const float *yv = Y + (long)iv * nd;
+                    float c = cos_phi[iv], s = sin_phi[iv];
+                    float xr = c * xc + s * yc;
+                    float yr = -s * xc + c * yc;
+                    float g = SD / ((xr + SO) * dy_det);
+                    int hi = (int)floor((yr + 1) * g + nd2);
+                    int lo = (int)floor((yr - 1) * g + nd2);
+                    if (lo < 0) lo = 0;
+                    if (hi > nd - 1) hi = nd - 1;
+                    for (int id = lo; id <= hi; id++) {
+                        float Px0 = -(sin_det[id] * c + cos_det[id] * s);
+                        float Py0 = cos_det[id] * c - sin_det[id] * s;
+                        float Pd0 = SO * sin_det[id];
+                        float Px1 = -(sin_det[id + 1] * c + cos_det[id + 1] * s);
+                        float Py1 = cos_det[id + 1] * c - sin_det[id + 1] * s;
+                        float Pd1 = SO * sin_det[id + 1];
+                        float l = orc_beam_area(Px0, Py0, Pd0, Px1, Py1, Pd1, xc, yc);
+                        if (l > 0) acc += l * yv[id];
+                    }
+                }
+                x[it * n + (long)iy * nx + ix] = acc * scale;
+            }
+        }
+    }
+}

@@ -62,6 +62,12 @@ def main():
     save_case(f"{OUT}/cone_siddon_phantom.npz", "cone_siddon", pm, xm, O.ref_cone_siddon(xm, pm))
     ym = rng.standard_normal(64 * 48 * 12).astype(np.float32)
     save_case(f"{OUT}/cone_adj_mm.npz", "cone_adj", pm, ym, O.ref_cone_adj(ym, pm))
+    # finite-size beam fan pair (version 2) on a phantom and an offset detector
+    pb = G.fan_para(48, 48, 40, 24, L=(2, 2), SO=4.0, OD=3.0, Ly=6.0, y_os=0.21)
+    xb = PH.ellipses_2d(48, seed=5).reshape(-1)
+    save_case(f"{OUT}/fan_fb_phantom.npz", "fan_fb", pb, xb, O.ref_fan_fb(xb, pb))
+    yb = rng.standard_normal(40 * 24).astype(np.float32)
+    save_case(f"{OUT}/fan_fb_adj_rand.npz", "fan_fb_adj", pb, yb, O.ref_fan_fb_adj(yb, pb))
     for f in sorted(os.listdir(OUT)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(OUT, f)))

@@ -10,7 +10,6 @@ pytestmark = pytest.mark.gpu
 
 def _coef_flat(coefs, levels, dim):
     """Oracle coefficient list -> the library's flat layout."""
-    nf = 3
     out = []
     for l, lev in enumerate(coefs):
         last = l == levels - 1
@@ -27,7 +26,7 @@ def _oracle_dec(u, levels, kind="linear"):
 
 
 @pytest.mark.parametrize("levels", [1, 2])
-@pytest.mark.parametrize("kind", ["linear", "haar"])
+@pytest.mark.parametrize("kind", ["linear", "haar", "cubic"])
 def test_framelet_3d_matches_oracle_and_reconstructs(levels, kind):
     import torch
     from framelab_gb300.transforms import FrameletSystem

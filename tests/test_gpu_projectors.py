@@ -347,3 +347,113 @@ def test_gao_dropins_host_pointer_abi():
     _lib.check_last()
     want, wantn = O.cone_gao_f32(Xc, pc)
     assert np.array_equal(yc, want) and np.array_equal(ycn, wantn)
+
+
+# --------------------------------------------------------------------------
+# analytic known answers (testBall.m) through every forward model
+# --------------------------------------------------------------------------
+def test_known_answers_all_models():
+    from tests.known_answers import cone_ball, fan_disc, rel
+    p, x, ex = fan_disc()
+    P = _plan(p)
+    for model in ("siddon_ref", "gao_ref", "matched"):
+        assert rel(_host(P.forward(_dev(x), model=model)), ex) < 5e-3, model
+    for scan in ("circle", "helix"):
+        p, x, ex, exn = cone_ball(scan=scan)
+        P = _plan(p)
+        for model in ("siddon_ref", "matched"):
+            assert rel(_host(P.forward(_dev(x), model=model)), ex) < 3e-2, (scan, model)
+        y, yn = P.forward_gao(_dev(x))
+        assert rel(_host(y), ex) < 3e-2 and rel(_host(yn), exn) < 3e-2, scan
+
+
+def test_multi_frame_views_read_their_frame():
+    """nt = 2 frames; views alternate between them (id_X / id_Y bookkeeping of
+    Ax_cone_mf.cpp:19-24): each view's projection equals the single-frame one."""
+    rng = np.random.default_rng(8)
+    p = G.cone_para(16, 16, 16, 20, 18, 6, L=(2, 2, 2))
+    frames = np.array([0, 1, 0, 1, 1, 0], np.uint32)
+    q = dict(p)
+    q["nt"] = np.uint32(2)
+    q["id_X"] = frames
+    views = [np.where(frames == t)[0] for t in (0, 1)]
+    tmp = max(len(v) for v in views)
+    idY = np.zeros((tmp, 2), np.uint32)
+    for t in (0, 1):
+        idY[:len(views[t]), t] = views[t]
+    q["id_Y"], q["Nv"], q["tmp_size"] = idY, np.array([len(v) for v in views], np.uint32), np.uint32(tmp)
+    X = rng.standard_normal((2, 16 ** 3)).astype(np.float32)
+    P2, P1 = _plan(q), _plan(p)
+    y2 = _host(P2.forward(_dev(X.reshape(-1)), model="matched")).reshape(6, -1)
+    for t in (0, 1):
+        y1 = _host(P1.forward(_dev(X[t]), model="matched")).reshape(6, -1)
+        for v in views[t]:
+            assert np.array_equal(y2[v], y1[v])
+    ysr = _host(P2.forward(_dev(X.reshape(-1)), model="siddon_ref"))
+    assert np.array_equal(ysr, O.cone_siddon_f32(X.reshape(-1), q))
+    yv = rng.standard_normal(6 * 20 * 18).astype(np.float32)
+    xa = _host(P2.adjoint(_dev(yv), model="chord_ref"))
+    assert np.array_equal(xa, O.cone_adj_f32(yv, q))
+
+
+# --------------------------------------------------------------------------
+# finite-size beam fan pair (version 2)
+# --------------------------------------------------------------------------
+def test_fb_ref_matches_reference_fixtures():
+    cases = _golden("fan_fb") + _golden("fan_fb_adj")
+    assert cases
+    for c in cases:
+        P = _plan(c["para"])
+        if c["kind"] == "fan_fb":
+            out = P.forward(_dev(c["x"].astype(np.float32)), model="fb_ref")
+        else:
+            out = P.adjoint(_dev(c["x"].astype(np.float32)), model="fb_ref")
+        assert np.array_equal(_host(out), c["y"]), c["kind"]
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_fb_ref_random_geometries_bit_exact(seed):
+    rng = np.random.default_rng(60 + seed)
+    n = [16, 24, 32, 40][seed]
+    p = G.fan_para(n, n, 2 * n + 3, 11, L=(2, 2), SO=rng.uniform(2, 8), OD=rng.uniform(2, 8),
+                   Ly=rng.uniform(3, 9), y_os=rng.uniform(-0.5, 0.5),
+                   sd_phi=rng.uniform(-4, 4, 11))
+    P = _plan(p)
+    x = rng.standard_normal(n * n).astype(np.float32)
+    assert np.array_equal(_host(P.forward(_dev(x), model="fb_ref")), O.fan_fb_f32(x, p))
+    y = rng.standard_normal(11 * (2 * n + 3)).astype(np.float32)
+    assert np.array_equal(_host(P.adjoint(_dev(y), model="fb_ref")), O.fan_fb_adj_f32(y, p))
+
+
+def test_fb_dropins_host_pointer_abi():
+    from framelab_gb300 import _lib
+    L = _lib.load()
+    rng = np.random.default_rng(9)
+    p = G.fan_para(24, 24, 40, 8, L=(2, 2), y_os=0.13)
+    X = rng.standard_normal(24 * 24).astype(np.float32)
+    y = np.zeros(40 * 8, np.float32)
+    sd = p["sd_phi"].copy(); yd = p["y_det"].copy(); idx = p["id_X"].astype(np.int32)
+    L.Ax_fan_mf_gpu_new_fb(_ptr(X), _ptr(y), float(p["SO"]), float(p["OD"]), float(p["scale"]),
+                           24, 24, 8, _ptr(sd), 40, _ptr(yd), _ptr(idx), 1, float(p["dy_det"]))
+    _lib.check_last()
+    assert np.array_equal(y, O.fan_fb_f32(X, p))
+    Y = rng.standard_normal(40 * 8).astype(np.float32)
+    x = np.zeros(24 * 24, np.float32)
+    arr = {k: np.ascontiguousarray(p[k], np.float32)
+           for k in ("cos_phi", "sin_phi", "cos_det2", "sin_det2")}
+    idY = np.asarray(p["id_Y"]).T.reshape(-1).astype(np.int32); Nv = p["Nv"].astype(np.int32)
+    L.Atx_fan_mf_gpu_new_fb(_ptr(x), _ptr(Y), float(p["SO"]), float(p["OD"]), float(p["scale"]),
+                            24, 24, _ptr(sd), 40, _ptr(yd), float(p["dy_det"]), 1, _ptr(idY),
+                            _ptr(Nv), int(p["tmp_size"]), 8, _ptr(arr["cos_phi"]),
+                            _ptr(arr["sin_phi"]), _ptr(arr["cos_det2"]), _ptr(arr["sin_det2"]))
+    _lib.check_last()
+    assert np.array_equal(x, O.fan_fb_adj_f32(Y, p))
+
+
+def test_fb_ref_known_answer_disc():
+    """The unit disc through the finite-size beam: each bin integrates the
+    chord over its wedge (analytic answer in tests/known_answers.py)."""
+    from tests.known_answers import fan_disc_beam, rel
+    p, x, ex = fan_disc_beam()
+    y = _host(_plan(p).forward(_dev(x), model="fb_ref"))
+    assert rel(y, ex) < 5e-3

@@ -59,6 +59,21 @@ def test_cone_restatement_is_bit_exact(seed):
     assert np.array_equal(O.cone_adj_f32(Y, p), O.ref_cone_adj(Y, p))
 
 
+@need_ref
+@pytest.mark.parametrize("seed", range(8))
+def test_fan_finite_beam_restatement_is_bit_exact(seed):
+    rng = np.random.default_rng(200 + seed)
+    n = [8, 16, 32, 40][seed % 4]
+    p = _rand_fan(rng, n, [12, 24, 50, 33][seed % 4], [5, 7, 16][seed % 3])
+    if seed % 2:                       # an offset detector and arbitrary angles
+        p = G.fan_para(n, n, len(p["y_det"]), 9, L=(2, 2), SO=3.5, OD=4.0, Ly=5.0,
+                       y_os=0.37, sd_phi=rng.uniform(-4, 4, 9))
+    X = rng.standard_normal(n * n).astype(np.float32)
+    assert np.array_equal(O.fan_fb_f32(X, p), O.ref_fan_fb(X, p))
+    Y = rng.standard_normal(len(p["y_det"]) * len(p["sd_phi"])).astype(np.float32)
+    assert np.array_equal(O.fan_fb_adj_f32(Y, p), O.ref_fan_fb_adj(Y, p))
+
+
 def _golden_cases():
     return sorted(glob.glob(os.path.join(GOLDEN, "*.npz")))
 
@@ -82,6 +97,10 @@ def test_restatement_matches_golden(path):
         out = O.cone_adj_f32(case["x"], p)
     elif kind == "fan_new":
         out = O.fan_gao_f32(case["x"], p)
+    elif kind == "fan_fb":
+        out = O.fan_fb_f32(case["x"], p)
+    elif kind == "fan_fb_adj":
+        out = O.fan_fb_adj_f32(case["x"], p)
     elif kind == "cone_new":
         out, yn = O.cone_gao_f32(case["x"], p)
         assert np.array_equal(yn, case["extra"]["yNorm"])
