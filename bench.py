@@ -1,10 +1,10 @@
 #!/usr/bin/env python
-"""Headline benchmark: cone-beam CGLS iterations/s on one GB300.
+"""Benchmarks of the FrameLab hot path on one GB300.
 
-Workload (default ``cone512``): 512^3 ellipsoid phantom, 720 views over 2*pi,
-1024x768 flat panel at 0.5 mm, source-isocentre 600 mm, source-detector
-1200 mm, 0.5 mm voxels. A step is one CGLS iteration on (A^T A + lam I) u = b,
-b = A^T A x_true, with the matched Siddon projector pair:
+Default workload ``cone512`` (the headline): 512^3 ellipsoid phantom, 720
+views over 2*pi, 1024x768 flat panel at 0.5 mm, source-isocentre 600 mm,
+source-detector 1200 mm, 0.5 mm voxels. A step is one CGLS iteration on
+(A^T A + lam I) u = b, b = A^T A x_true, with the matched Siddon projector pair:
 
 * ``value``: the graph form (FP32 storage, fused updates with FP64 reductions
   and device-side alpha/beta, one iteration replayed as a CUDA graph), inputs
@@ -21,13 +21,24 @@ b = A^T A x_true, with the matched Siddon projector pair:
 * ``cpu_baseline``: the reference's CPU projector pair (the oracle's bit-exact
   restatement) timed on a bounded sample on this host and extrapolated.
 
-``--impl reference`` times that CPU path alone as the reference arm.
+Other workloads (``--workload``), same JSON contract:
+* ``cone256`` -- 256^3, 360 views, 512x384 panel at 1 mm (adds the dot-product
+  identity and the FP16-storage error to ``detail``); ``cone128`` for profiling;
+* ``fan256`` -- 256^2 fan beam, 360 views, 512 bins, SO = OD = 500 mm, 20 CGLS;
+* ``fanbatch64`` -- 64 fan slices of uneven size (n in {128..512}, 180..720
+  views, 2n bins) with Gaussian noise, batched CGLS (one launch per operator
+  for all slices); a step is one iteration of all 64 slices;
+* ``sb256`` -- split Bregman (2-level linear framelet, lam 0.01, mu 1, 5 inner
+  CGLS) on 256^3 from 90 Poisson-noisy views; a step is one outer iteration.
+
+``--impl reference`` times the reference's CPU path for the workload alone.
 Multi-GPU: replicas only (independent solves per rank, no collective).
 """
 from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -40,16 +51,22 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+_CONE = dict(SO=600.0, SD=1200.0, lam=0.0)
 WORKLOADS = {
-    # 512^3 cone CGLS with gradients (the large cone-beam configuration)
-    "cone512": dict(n=512, nv=720, na=1024, nb=768, det_mm=0.5, SO=600.0, SD=1200.0,
-                    vox_mm=0.5, lam=0.0),
+    # 512^3 cone CGLS (the large cone-beam configuration)
+    "cone512": dict(kind="cone", n=512, nv=720, na=1024, nb=768, det_mm=0.5, vox_mm=0.5, **_CONE),
     # 256^3 circular cone projector pair
-    "cone256": dict(n=256, nv=360, na=512, nb=384, det_mm=1.0, SO=600.0, SD=1200.0,
-                    vox_mm=1.0, lam=0.0),
+    "cone256": dict(kind="cone", n=256, nv=360, na=512, nb=384, det_mm=1.0, vox_mm=1.0, **_CONE),
     # small case for ncu captures
-    "cone128": dict(n=128, nv=90, na=256, nb=192, det_mm=2.0, SO=600.0, SD=1200.0,
-                    vox_mm=2.0, lam=0.0),
+    "cone128": dict(kind="cone", n=128, nv=90, na=256, nb=192, det_mm=2.0, vox_mm=2.0, **_CONE),
+    # 2-D fan: 256^2 over a 256 mm field, 360 views, 512 bins, SO = OD = 500 mm
+    "fan256": dict(kind="fan", n=256, nv=360, nd=512, SO=500.0, OD=500.0, L=256.0, lam=0.0),
+    # 64 uneven fan slices, same scanner, Gaussian noise 1% of each slice's maximum
+    "fanbatch64": dict(kind="batch", slices=64, sizes=(128, 192, 256, 384, 512),
+                       nv=(180, 720), SO=500.0, OD=500.0, L=256.0, noise=0.01, seed=7),
+    # split Bregman on 256^3 from 90 views, Poisson counts at I0 = 1e5
+    "sb256": dict(kind="sb", n=256, nv=90, na=512, nb=384, det_mm=1.0, vox_mm=1.0, SO=600.0,
+                  SD=1200.0, I0=1e5, pmax=4.0, lam=0.01, mu=1.0, inner=5, levels=2),
 }
 REFRESH = 10
 
@@ -62,34 +79,104 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="cone512", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--only", default="", help="comma list of legs: mixed,plain,e2e,kernels")
+    ap.add_argument("--only", default="", help="comma list of legs: mixed,plain,e2e,kernels,seq")
     return ap.parse_args()
 
 
-def para_of(w):
+# --------------------------------------------------------------------------
+# geometries
+# --------------------------------------------------------------------------
+def cone_para(w, nv=None):
     from framelab_gb300 import geometry as G
-    return G.cone_para_mm(w["n"], w["nv"], w["na"], w["nb"], det_pitch_mm=w["det_mm"],
+    return G.cone_para_mm(w["n"], nv or w["nv"], w["na"], w["nb"], det_pitch_mm=w["det_mm"],
                           SO_mm=w["SO"], SD_mm=w["SD"], voxel_mm=w["vox_mm"])
 
 
+def fan_para(n, nv, nd, w):
+    """Fan scan of an n x n image over an L x L mm field; the detector spans the
+    field's magnified diagonal (2*sqrt(2)*L at magnification 2)."""
+    from framelab_gb300 import geometry as G
+    L = w["L"]
+    return G.fan_para(n, n, nd, nv, L=(L, L), SO=w["SO"], OD=w["OD"],
+                      Ly=math.sqrt(2.0) * L * (w["SO"] + w["OD"]) / w["SO"])
+
+
+def batch_slices(w):
+    rng = np.random.default_rng(w["seed"])
+    ns = rng.choice(np.array(w["sizes"]), w["slices"])
+    nvs = rng.integers(w["nv"][0], w["nv"][1] + 1, w["slices"])
+    return [(int(n), int(v)) for n, v in zip(ns, nvs)]
+
+
+def para_of(w):
+    k = w["kind"]
+    if k in ("cone", "sb"):
+        return cone_para(w)
+    if k == "fan":
+        return fan_para(w["n"], w["nv"], w["nd"], w)
+    return [fan_para(n, v, 2 * n, w) for n, v in batch_slices(w)]
+
+
+def describe(name, w, world):
+    k = w["kind"]
+    if k == "cone":
+        wl = (f"{name}: {w['n']}^3 cone CGLS, {w['nv']} views, {w['na']}x{w['nb']} panel @ "
+              f"{w['det_mm']} mm, SO {w['SO']:.0f} mm, SD {w['SD']:.0f} mm, voxel {w['vox_mm']} mm")
+        metric = "CGLS iter/s (cone-beam, matched Siddon pair, fused FP32 graph form)"
+        vb, sb = 4 * w["n"] ** 3, 4 * w["nv"] * w["na"] * w["nb"]
+        l2 = (f"working set {'>' if 4 * vb + sb > 129e6 else '<'} L2 (4 volume vectors "
+              f"{4 * vb / 2**20:.0f} MiB + sinogram {sb / 2**20:.0f} MiB)")
+        data = "synthetic: seeded 12-ellipsoid phantom, noiseless projections"
+    elif k == "fan":
+        wl = (f"{name}: {w['n']}^2 fan CGLS, {w['nv']} views, {w['nd']} bins, "
+              f"{w['L']:.0f} mm field, SO {w['SO']:.0f} mm, OD {w['OD']:.0f} mm")
+        metric = "CGLS iter/s (fan-beam, matched Siddon pair, fused FP32 graph form)"
+        l2 = ("working set < L2 (256 KiB image, 720 KiB sinogram): the L2-resident "
+              "case the reference's 2-D configuration is")
+        data = "synthetic: seeded 10-ellipse phantom, noiseless projections"
+    elif k == "batch":
+        wl = (f"{name}: {w['slices']} fan slices, n in {list(w['sizes'])}, "
+              f"{w['nv'][0]}..{w['nv'][1]} views, 2n bins, batched CGLS")
+        metric = "batched CGLS iter/s (64 uneven fan slices per iteration)"
+        l2 = "working set > L2 (4 image-sized vectors + sinogram ~ 0.2 GB)"
+        data = ("synthetic: seeded 10-ellipse phantoms, Gaussian noise "
+                f"sigma = {w['noise']} x max(sinogram) per slice")
+    else:
+        wl = (f"{name}: split Bregman, {w['n']}^3, {w['nv']} views, {w['na']}x{w['nb']} "
+              f"panel @ {w['det_mm']} mm, {w['levels']}-level linear framelet, "
+              f"lam {w['lam']}, mu {w['mu']}, {w['inner']} CGLS per outer iteration")
+        metric = "split-Bregman outer iter/s (cone-beam, 2-level linear framelet)"
+        l2 = "working set > L2 (framelet coefficients 2 x 3.4 GiB)"
+        data = (f"synthetic: seeded 12-ellipsoid phantom scaled to max line integral "
+                f"{w['pmax']}, Poisson counts at I0 = {w['I0']:.0e}")
+    config = {"workload": wl, "global_batch": world, "l2": l2,
+              "parallelism": f"replicas{world}"}
+    return metric, config, data
+
+
 # --------------------------------------------------------------------------
-# CPU leg: the reference's CPU projector pair (oracle restatement, bit-exact)
+# CPU legs: the reference's CPU kernels (oracle restatement, bit-exact)
 # --------------------------------------------------------------------------
-def cpu_sample(w, p):
-    """Times Ax_cone_mf_cpu_siddon and Atx_cone_mf_cpu_new (the oracle's bit-exact
-    restatement of the reference's CPU kernels) on a bounded sample with all host
-    threads and extrapolates one CGLS iteration (one forward projection + one
-    backprojection; the vector algebra is negligible next to them).
-    Forward sample: one view per thread, every 16th detector row (a ray depends
-    only on its view, column and row, so these are rays of the full scan).
-    Backprojection sample: one slice per thread, spread over z, x 4 views."""
+def _threads():
+    return max(1, os.cpu_count() or 1)
+
+
+def cone_pair_seconds(w, p, row_step=16, av=4):
+    """Seconds for one forward (Ax_cone_mf_cpu_siddon) + one backprojection
+    (Atx_cone_mf_cpu_new) of the oracle's bit-exact restatement with all host
+    threads, from a bounded sample extrapolated linearly.
+    Forward sample: one view per thread, every `row_step`-th detector row (a ray
+    depends only on its view, column and row, so these are rays of the full
+    scan). Backprojection sample: one slice per thread, spread over z, x `av`
+    views."""
+    import concurrent.futures as cf
     import oracle as O
-    threads = max(1, os.cpu_count() or 1)
-    n, nv, nb = w["n"], w["nv"], w["nb"]
+    threads = _threads()
+    n, nv, nb = w["n"], len(p["sd_phi"]), w["nb"]
     rng = np.random.default_rng(0)
     x = rng.random(n ** 3, dtype=np.float32)
     fv = min(nv, threads)
-    rows = np.arange(0, nb, 16)
+    rows = np.arange(0, nb, row_step)
     q = dict(p)
     q["sd_phi"] = p["sd_phi"][:fv]
     q["sd_z"] = p["sd_z"][:fv]
@@ -99,7 +186,7 @@ def cpu_sample(w, p):
     O.cone_siddon_f32(x, q, threads=threads)
     t_f = time.perf_counter() - t0
     fwd_full = t_f * (nv / fv) * (nb / len(rows))
-    av = 4
+    av = min(av, nv)
     y = rng.random(av * w["na"] * nb, dtype=np.float32)
     r = dict(p)
     for k in ("cos_phi", "sin_phi", "sd_phi", "sd_z"):
@@ -110,17 +197,91 @@ def cpu_sample(w, p):
     zs = min(threads, n)
     zsel = np.linspace(0, n - 1, zs).astype(int)
     t0 = time.perf_counter()
-    import concurrent.futures as cf
     with cf.ThreadPoolExecutor(threads) as ex:
         list(ex.map(lambda z: O.cone_adj_f32(y, r, threads=1, slices=(int(z), int(z) + 1)), zsel))
     t_a = time.perf_counter() - t0
     adj_full = t_a * (n / zs) * (nv / av)
-    it_s = fwd_full + adj_full
-    return dict(value=1.0 / it_s, unit="iter/s", cores=threads, kind="port",
-                sample=(f"Ax_cone_mf_cpu_siddon on {fv}/{nv} views x {len(rows)}/{nb} rows "
-                        f"({t_f:.2f} s) + Atx_cone_mf_cpu_new on {zs}/{n} slices x {av}/{nv} "
-                        f"views ({t_a:.2f} s), {threads} threads, extrapolated linearly to one "
-                        f"forward + backprojection ({it_s:.0f} s per CGLS iteration)"))
+    desc = (f"Ax_cone_mf_cpu_siddon on {fv}/{nv} views x {len(rows)}/{nb} rows ({t_f:.2f} s) + "
+            f"Atx_cone_mf_cpu_new on {zs}/{n} slices x {av}/{nv} views ({t_a:.2f} s)")
+    return fwd_full + adj_full, desc
+
+
+def fan_pair_seconds(p, views=None):
+    """Seconds for one fan forward (Ax_fan_mf_cpu_siddon) + backprojection
+    (Atx_fan_mf_cpu_new), oracle restatement, all host threads; with `views`,
+    on that many views of the scan, extrapolated to all of them."""
+    import oracle as O
+    from framelab_gb300 import geometry as G
+    threads = _threads()
+    nv = len(p["sd_phi"])
+    q = p
+    if views and views < nv:
+        nx, nd = int(p["nx"]), len(p["y_det"])
+        sd = p["sd_phi"][np.linspace(0, nv - 1, views).astype(int)]
+        q = G.fan_para(nx, nx, nd, views, sd_phi=sd)
+        for k in ("SO", "OD", "scale", "y_det", "cos_det", "sin_det", "dy_det"):
+            q[k] = p[k]
+    rng = np.random.default_rng(0)
+    nx, ny = int(q["nx"]), int(q["ny"])
+    x = rng.random(nx * ny, dtype=np.float32)
+    y = rng.random(len(q["sd_phi"]) * len(q["y_det"]), dtype=np.float32)
+    t0 = time.perf_counter()
+    O.fan_siddon_f32(x, q, threads=threads)
+    O.fan_adj_f32(y, q, threads=threads)
+    t = time.perf_counter() - t0
+    return t * nv / len(q["sd_phi"])
+
+
+def framelet_seconds(w, block=64):
+    """Seconds for one framelet analysis + synthesis of the sb workload's
+    volume: the FP64 numpy restatement on a block^3 volume, scaled by voxels."""
+    from oracle import numerics as N
+    rng = np.random.default_rng(0)
+    u = rng.random((block,) * 3)
+    t0 = time.perf_counter()
+    c = N.frame_dec(u, w["levels"], "linear")
+    N.frame_rec(c, "linear")
+    t = time.perf_counter() - t0
+    return t * (w["n"] / block) ** 3, t
+
+
+def cpu_sample(w, p):
+    threads = _threads()
+    k = w["kind"]
+    if k == "cone":
+        s, desc = cone_pair_seconds(w, p)
+        return dict(value=1.0 / s, unit="iter/s", cores=threads, kind="port",
+                    sample=f"{desc}, {threads} threads, extrapolated linearly to one forward + "
+                           f"backprojection ({s:.0f} s per CGLS iteration)")
+    if k == "fan":
+        s = fan_pair_seconds(p)
+        return dict(value=1.0 / s, unit="iter/s", cores=threads, kind="port",
+                    sample=f"Ax_fan_mf_cpu_siddon + Atx_fan_mf_cpu_new on the full scan, "
+                           f"{threads} threads ({s:.2f} s per CGLS iteration)")
+    if k == "batch":
+        sl = batch_slices(w)
+        pick = sorted(range(len(sl)), key=lambda i: sl[i][0])[::4]   # sizes spread
+        tot, smp = 0.0, 0.0
+        per = {}
+        for i in pick:
+            n, v = sl[i]
+            t = fan_pair_seconds(p[i], views=min(v, 128))
+            per[n] = per.get(n, []) + [t / v]                       # seconds per view
+            smp += t * min(v, 128) / v
+        for n, v in sl:
+            near = min(per, key=lambda m: abs(m - n))
+            tot += statistics.mean(per[near]) * v * (n / near) ** 2
+        return dict(value=1.0 / tot, unit="iter/s", cores=threads, kind="port",
+                    sample=f"Ax_fan_mf_cpu_siddon + Atx_fan_mf_cpu_new on 128 views of "
+                           f"{len(pick)} of {len(sl)} slices ({smp:.1f} s), {threads} threads, "
+                           f"scaled per slice by views and pixels ({tot:.1f} s per iteration)")
+    s, desc = cone_pair_seconds(w, p, row_step=4, av=16)
+    tf, t64 = framelet_seconds(w)
+    it = w["inner"] * s + tf
+    return dict(value=1.0 / it, unit="iter/s", cores=threads, kind="port",
+                sample=f"{w['inner']} x ({desc}) + framelet analysis/synthesis on 64^3 "
+                       f"({t64:.2f} s, numpy) scaled by voxels; {threads} threads "
+                       f"({it:.0f} s per outer iteration)")
 
 
 # --------------------------------------------------------------------------
@@ -170,19 +331,329 @@ class ClockSampler:
 
 
 # --------------------------------------------------------------------------
+# GPU legs
+# --------------------------------------------------------------------------
+class Ctx:
+    """Device, stream, replica bookkeeping and the CUDA-event timer."""
+
+    def __init__(self, a, world, rank, local):
+        import torch
+        self.torch = torch
+        self.a, self.world, self.rank, self.local = a, world, rank, local
+        self.dev = torch.device("cuda", local)
+        self.stream = torch.cuda.current_stream()
+        self.K, self.W = a.steps, a.warmup
+        self.legs = set(a.only.split(",")) if a.only else {"mixed", "plain", "e2e", "kernels", "seq"}
+
+    def barrier(self):
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    def tmax(self, t):
+        if self.world > 1:
+            import torch.distributed as dist
+            x = self.torch.tensor([t], device=self.dev, dtype=self.torch.float64)
+            dist.all_reduce(x, op=dist.ReduceOp.MAX)
+            return float(x.item())
+        return t
+
+    def timed(self, fn):
+        """Run fn between CUDA events on the launching stream, synchronised and
+        barriered on both sides; returns (result, max-over-ranks seconds)."""
+        torch = self.torch
+        self.barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(self.stream)
+        out = fn()
+        e1.record(self.stream)
+        torch.cuda.synchronize()
+        self.barrier()
+        return out, self.tmax(e0.elapsed_time(e1) / 1000.0)
+
+    def rel(self, a_, b_):
+        t = self.torch
+        return (t.linalg.vector_norm((a_ - b_).double()) /
+                t.linalg.vector_norm(b_.double())).item()
+
+
+def hbm_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh).get("hbm_gbs"), "measured"
+    except OSError:
+        return 6800.0, "fallback"
+
+
+def traffic_of(workload, dom):
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as fh:
+            ent = json.load(fh).get(workload, {}).get(dom)
+        if ent:
+            return ent.get("bytes_per_launch")
+    return None
+
+
+def projector_roofline(ctx, workload, n_isect, n_rays, n_vox, t_fwd, t_adj, detail, label):
+    """Dominant projector kernel: algorithmic bytes over CUDA-event time."""
+    b_fwd = n_isect * 4 + n_rays * 4      # f32 voxel gathers + f32 sinogram writes
+    b_adj = n_isect * 4 + n_vox * 4       # f32 sinogram gathers + f32 voxel writes
+    peak, src = hbm_peak()
+    detail.update(n_isect=n_isect, mean_isect_per_ray=n_isect / n_rays,
+                  fwd_ms=t_fwd * 1e3, adj_ms=t_adj * 1e3,
+                  fwd_alg_GBps=b_fwd / t_fwd / 1e9, adj_alg_GBps=b_adj / t_adj / 1e9,
+                  fwd_rays_per_s=n_rays / t_fwd, adj_voxel_updates_per_s=n_isect / t_adj)
+    dom = "adjoint" if t_adj > t_fwd else "forward"
+    ach = (b_adj / t_adj if dom == "adjoint" else b_fwd / t_fwd) / 1e9
+    return {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+            "frac": ach / peak if peak else None, "traffic": traffic_of(workload, dom),
+            "kernel": f"{label} {dom} (f32 storage)", "peak_source": src,
+            "bytes_definition": "sum over rays of voxels crossed x element bytes + "
+                                "one element per ray (forward) / per voxel (adjoint)"}
+
+
+def time_pair(ctx, P, x, reps=3):
+    """CUDA-event seconds of one matched forward and one matched adjoint."""
+    from framelab_gb300 import _lib
+    from framelab_gb300.projector import DTYPES
+    torch = ctx.torch
+    L = _lib.load()
+    s = ctx.stream.cuda_stream
+    y = torch.empty(P.n_rays, device=ctx.dev, dtype=torch.float32)
+    xo = torch.empty(P.n_vox, device=ctx.dev, dtype=torch.float32)
+    f32 = DTYPES[torch.float32]
+
+    def fwd():
+        for _ in range(reps):
+            _lib.check(L.fl_forward(P.handle, 16, x.data_ptr(), f32, y.data_ptr(), f32, s))
+
+    def adj():
+        for _ in range(reps):
+            _lib.check(L.fl_adjoint(P.handle, 16, y.data_ptr(), f32, xo.data_ptr(), f32, s))
+    fwd(); adj()
+    _, tf = ctx.timed(fwd)
+    _, ta = ctx.timed(adj)
+    return tf / reps, ta / reps, y, xo
+
+
+def run_single(ctx, name, w, p):
+    """cone / fan: CGLS on one scan (graph headline, mixed, plain, e2e, kernels)."""
+    torch = ctx.torch
+    from framelab_gb300 import phantoms as PH
+    from framelab_gb300.projector import Plan
+    from framelab_gb300.solvers import NativeCGLS, dot
+    K, W, world = ctx.K, ctx.W, ctx.world
+    P = Plan(p)
+    n = w["n"]
+    img = PH.ellipsoids_3d(n, seed=5) if w["kind"] == "cone" else PH.ellipses_2d(n, seed=5)
+    x_true = torch.from_numpy(img.reshape(-1)).to(ctx.dev)
+    f = P.forward(x_true)
+    b = P.adjoint(f).reshape(-1)
+    del f
+    torch.cuda.synchronize()
+    lam = w["lam"]
+    detail = {}
+    cg_g = NativeCGLS(P, "graph")
+    if W:
+        cg_g.solve(b, lam=lam, iters=W)
+    clocks = ClockSampler(ctx.local)
+    with clocks:
+        u_g, t_g = ctx.timed(lambda: cg_g.solve(b, lam=lam, iters=K))
+    detail["graph_iter_per_s_per_gpu"] = K / t_g
+    detail["graph_vs_truth_rel_l2"] = ctx.rel(u_g, x_true)
+    if "mixed" in ctx.legs:
+        cg_m = NativeCGLS(P, "mixed")
+        if W:
+            cg_m.solve(b, lam=lam, iters=W, refresh=REFRESH)
+        u_m, t_m = ctx.timed(lambda: cg_m.solve(b, lam=lam, iters=K, refresh=REFRESH))
+        detail["mixed_iter_per_s"] = world * K / t_m
+        detail["mixed_vs_graph_rel_l2"] = ctx.rel(u_m, u_g)
+        del cg_m, u_m
+    if "plain" in ctx.legs:
+        cg_p = NativeCGLS(P, "plain")
+        if W:
+            cg_p.solve(b, lam=lam, iters=W)
+        u_p, t_p = ctx.timed(lambda: cg_p.solve(b, lam=lam, iters=K))
+        detail["plain_iter_per_s"] = world * K / t_p
+        detail["graph_over_plain"] = t_p / t_g
+        detail["mixed_over_plain"] = (detail["mixed_iter_per_s"] / detail["plain_iter_per_s"]
+                                      if "mixed_iter_per_s" in detail else None)
+        detail["graph_vs_plain_rel_l2"] = ctx.rel(u_g, u_p)
+        del cg_p, u_p
+    e2e = None
+    if "e2e" in ctx.legs:
+        bh = torch.empty(b.numel(), dtype=torch.float32, pin_memory=True)
+        bh.copy_(b.cpu())
+        uh = torch.zeros(b.numel(), dtype=torch.float32, pin_memory=True)
+        bn, un = bh.numpy(), uh.numpy()
+        cg_g.solve_host(bn, un, lam=lam, iters=max(W, 1))
+        _, t_e = ctx.timed(lambda: cg_g.solve_host(bn, un, lam=lam, iters=K))
+        nb = b.numel() * 4
+        e2e = {"value": world * K / t_e, "unit": "iter/s",
+               "h2d_bytes_per_step": nb / K, "d2h_bytes_per_step": nb / K,
+               "call": f"fl_cgls_solve_host, {K} iterations per call: b in, u out "
+                       "(u0 = 0 needs no copy)"}
+    roofline = None
+    if "kernels" in ctx.legs:
+        cnt = P.count_intersections()
+        n_isect = int(cnt.sum(dtype=torch.int64).item())
+        del cnt
+        p32 = (u_g / (u_g.abs().max() + 1e-30)).contiguous()
+        tf, ta, y, xo = time_pair(ctx, P, p32)
+        roofline = projector_roofline(ctx, name, n_isect, P.n_rays, P.n_vox, tf, ta, detail,
+                                      "matched")
+        if name == "cone256":
+            # dot-product identity <A x, y> = <x, A^T y> on N(0,1) vectors (FP64 dots)
+            g = torch.Generator(device=ctx.dev).manual_seed(11)
+            xr = torch.randn(P.n_vox, device=ctx.dev, generator=g)
+            yr = torch.randn(P.n_rays, device=ctx.dev, generator=g)
+            lhs = dot(P.forward(xr), yr)
+            rhs = dot(xr, P.adjoint(yr))
+            detail["dot_test_rel"] = abs(lhs - rhs) / abs(lhs)
+            # FP16 storage of the volume against FP32 storage (same kernel)
+            y32 = P.forward(x_true)
+            y16 = P.forward(x_true.half())
+            detail["fp16_storage_vs_fp32_rel_l2"] = ctx.rel(y16, y32)
+            del xr, yr, y32, y16
+    return dict(value=world * K / t_g, t_step=t_g / K, e2e=e2e, roofline=roofline,
+                launches=5 * K + 1, detail=detail, clocks=clocks.summary(), unit="iter/s")
+
+
+def run_batch(ctx, name, w, paras):
+    """fanbatch: batched CGLS over uneven fan slices (one launch per operator)."""
+    torch = ctx.torch
+    from framelab_gb300 import phantoms as PH
+    from framelab_gb300.batch import FanBatch
+    from framelab_gb300.solvers import NativeCGLS
+    K, W, world = ctx.K, ctx.W, ctx.world
+    B = FanBatch(paras)
+    x_true = B.concat_images([PH.ellipses_2d(P.nx, seed=100 + i)
+                              for i, P in enumerate(B.plans)]).to(ctx.dev)
+    sino = B.forward(x_true)
+    g = torch.Generator(device=ctx.dev).manual_seed(w["seed"])
+    for s in B.sinograms(sino):
+        s += w["noise"] * s.max() * torch.randn(s.shape, device=ctx.dev, generator=g)
+    rhs = B.adjoint(sino)
+    del sino
+    torch.cuda.synchronize()
+    detail = {"slices": len(B), "n_vox": B.n_vox, "n_rays": B.n_rays}
+    if W:
+        B.cgls(rhs, iters=W)
+    clocks = ClockSampler(ctx.local)
+    with clocks:
+        u, t_b = ctx.timed(lambda: B.cgls(rhs, iters=K))
+    detail["slice_iter_per_s"] = len(B) * K / t_b
+    detail["vs_truth_rel_l2"] = ctx.rel(u, x_true)
+    if "seq" in ctx.legs:
+        # the same solves one slice after another (one plan + CGLS per slice)
+        sols = [NativeCGLS(P, "graph") for P in B.plans]
+        parts = [r.reshape(-1).contiguous() for r in B.images(rhs)]
+        for cg, r in zip(sols, parts):
+            cg.solve(r, iters=max(W, 1))
+        us, t_s = ctx.timed(lambda: [cg.solve(r, iters=K) for cg, r in zip(sols, parts)])
+        detail["sequential_iter_per_s"] = K / t_s
+        detail["batched_over_sequential"] = t_s / t_b
+        detail["batched_vs_sequential_rel_l2"] = ctx.rel(u, torch.cat(us))
+        del sols, us
+    e2e = None
+    if "e2e" in ctx.legs:
+        rh = torch.empty(B.n_vox, dtype=torch.float32, pin_memory=True)
+        rh.copy_(rhs.cpu())
+        uh = torch.empty(B.n_vox, dtype=torch.float32, pin_memory=True)
+
+        def host_solve():
+            r = rh.to(ctx.dev, non_blocking=True)
+            uh.copy_(B.cgls(r, iters=K), non_blocking=True)
+        host_solve()
+        _, t_e = ctx.timed(host_solve)
+        nb = B.n_vox * 4
+        e2e = {"value": world * K / t_e, "unit": "iter/s",
+               "h2d_bytes_per_step": nb / K, "d2h_bytes_per_step": nb / K,
+               "call": f"FanBatch.cgls, {K} iterations per call: right-hand sides in "
+                       "(pinned host), solutions out"}
+    roofline = None
+    if "kernels" in ctx.legs:
+        n_isect = sum(int(P.count_intersections().sum(dtype=torch.int64).item())
+                      for P in B.plans)
+        xs = (u / (u.abs().max() + 1e-30)).contiguous()
+        reps = 3
+        y = B.forward(xs)
+        xo = B.adjoint(y)
+        _, tf = ctx.timed(lambda: [B.forward(xs, out=y) for _ in range(reps)])
+        _, ta = ctx.timed(lambda: [B.adjoint(y, out=xo) for _ in range(reps)])
+        roofline = projector_roofline(ctx, name, n_isect, B.n_rays, B.n_vox, tf / reps,
+                                      ta / reps, detail, "batched matched")
+    return dict(value=world * K / t_b, t_step=t_b / K, e2e=e2e, roofline=roofline,
+                launches=5 * K + 1, detail=detail, clocks=clocks.summary(), unit="iter/s")
+
+
+def run_sb(ctx, name, w, p):
+    """sb: split Bregman outer iterations (5 CGLS + framelet step each)."""
+    torch = ctx.torch
+    from framelab_gb300 import phantoms as PH
+    from framelab_gb300.projector import Plan
+    from framelab_gb300.transforms import split_bregman
+    K, W, world = ctx.K, ctx.W, ctx.world
+    P = Plan(p)
+    x = torch.from_numpy(PH.ellipsoids_3d(w["n"], seed=5).reshape(-1)).to(ctx.dev)
+    proj = P.forward(x)
+    s = w["pmax"] / float(proj.max())
+    x_phys = x * s
+    g = torch.Generator(device=ctx.dev).manual_seed(3)
+    counts = torch.poisson(w["I0"] * torch.exp(-proj * s), generator=g)
+    f = -torch.log(counts.clamp(min=1.0) / w["I0"])
+    del proj, counts
+    u0 = torch.zeros(P.n_vox, device=ctx.dev)
+    kw = dict(lam=w["lam"], mu=w["mu"], cg_iters=w["inner"], levels=w["levels"], kind="linear",
+              mode="graph")
+    detail = {}
+    if W:
+        split_bregman(P, f, u0, outer=W, **kw)
+    clocks = ClockSampler(ctx.local)
+    with clocks:
+        (u, hist), t_s = ctx.timed(lambda: split_bregman(P, f, u0, outer=K, **kw))
+    detail["vs_truth_rel_l2"] = ctx.rel(u, x_phys)
+    detail["last_relative_update"] = float(hist[-1]) if len(hist) else None
+    e2e = None
+    if "e2e" in ctx.legs:
+        fh = torch.empty(f.numel(), dtype=torch.float32, pin_memory=True)
+        fh.copy_(f.cpu())
+        uh = torch.empty(P.n_vox, dtype=torch.float32, pin_memory=True)
+
+        def host_solve():
+            fd = fh.to(ctx.dev, non_blocking=True)
+            uh.copy_(split_bregman(P, fd, u0, outer=K, **kw)[0], non_blocking=True)
+        _, t_e = ctx.timed(host_solve)
+        e2e = {"value": world * K / t_e, "unit": "iter/s",
+               "h2d_bytes_per_step": f.numel() * 4 / K, "d2h_bytes_per_step": P.n_vox * 4 / K,
+               "call": f"split_bregman (fl_sb_solve), {K} outer iterations per call: "
+                       "sinogram in (pinned host), volume out"}
+    roofline = None
+    if "kernels" in ctx.legs:
+        cnt = P.count_intersections()
+        n_isect = int(cnt.sum(dtype=torch.int64).item())
+        del cnt
+        tf, ta, _, _ = time_pair(ctx, P, (u / (u.abs().max() + 1e-30)).contiguous())
+        roofline = projector_roofline(ctx, name, n_isect, P.n_rays, P.n_vox, tf, ta, detail,
+                                      "matched")
+    # setup: A^T f (weighting + gather) and W u0 (3 per level); per outer iteration:
+    # warm-start residual (fwd, adj, axpy) + init, inner x (fwd, adj, 3 updates),
+    # Bregman analysis + synthesis (3 + 3 per level), |u_k - u_{k-1}| (diff, 2 dots)
+    launches = 2 + 3 * w["levels"] + K * (4 + 5 * w["inner"] + 6 * w["levels"] + 3)
+    return dict(value=world * K / t_s, t_step=t_s / K, e2e=e2e, roofline=roofline,
+                launches=launches, detail=detail, clocks=clocks.summary(), unit="iter/s")
+
+
+# --------------------------------------------------------------------------
 def main():
     a = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     w = WORKLOADS[a.workload]
-    config = {"workload": f"{a.workload}: {w['n']}^3 cone CGLS, {w['nv']} views, "
-                          f"{w['na']}x{w['nb']} panel @ {w['det_mm']} mm, SO {w['SO']:.0f} mm, "
-                          f"SD {w['SD']:.0f} mm, voxel {w['vox_mm']} mm",
-              "global_batch": world, "l2": "working set > L2 (volume and sinogram >= 64 MiB "
-                                            "per operand; 512^3: 0.5 GiB + 2.2 GiB)",
-              "parallelism": f"replicas{world}"}
-    metric = "CGLS iter/s (cone-beam, matched Siddon pair, fused FP32 graph form)"
+    metric, config, data = describe(a.workload, w, world)
 
     if a.impl == "reference":
         if rank != 0:
@@ -199,7 +670,8 @@ def main():
                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                "dtype": "f32", "data": "synthetic (seeded random volume and sinogram)",
                "impl": "reference", "config": config,
-               "cpu_baseline": {"value": v, "unit": "iter/s", "cores": samples[0]["cores"] if samples else None,
+               "cpu_baseline": {"value": v, "unit": "iter/s",
+                                "cores": samples[0]["cores"] if samples else None,
                                 "kind": "port", "sample": samples[0]["sample"] if samples else ""},
                "e2e": {"value": v, "unit": "iter/s", "h2d_bytes_per_step": 0,
                        "d2h_bytes_per_step": 0},
@@ -212,178 +684,22 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
-    from framelab_gb300 import phantoms as PH
-    from framelab_gb300.projector import Plan
-    from framelab_gb300.solvers import NativeCGLS
-
-    def barrier():
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
-
-    def tmax(t):
-        if world > 1:
-            import torch.distributed as dist
-            x = torch.tensor([t], device=dev, dtype=torch.float64)
-            dist.all_reduce(x, op=dist.ReduceOp.MAX)
-            return float(x.item())
-        return t
-
-    legs = set(a.only.split(",")) if a.only else {"mixed", "plain", "e2e", "kernels"}
-    legs.add("graph")
+    ctx = Ctx(a, world, rank, local)
     p = para_of(w)
-    P = Plan(p)
-    n = w["n"]
-    x_true = torch.from_numpy(PH.ellipsoids_3d(n, seed=5).reshape(-1)).to(dev)
-    f = P.forward(x_true)
-    b = P.adjoint(f).reshape(-1)
-    del f
-    torch.cuda.synchronize()
-    lam = w["lam"]
-    K, W = a.steps, a.warmup
-    stream = torch.cuda.current_stream()
-    detail = {}
-
-    def timed(fn):
-        barrier()
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        out = fn()
-        e1.record(stream)
-        torch.cuda.synchronize()
-        barrier()
-        return out, tmax(e0.elapsed_time(e1) / 1000.0)
-
-    # ---- graph form (headline) ----
-    cg_g = NativeCGLS(P, "graph")
-    if W:
-        cg_g.solve(b, lam=lam, iters=W)
-    clocks = ClockSampler(local)
-    with clocks:
-        u_g, t_g = timed(lambda: cg_g.solve(b, lam=lam, iters=K))
-    value = world * K / t_g
-    detail["graph_iter_per_s_per_gpu"] = K / t_g
-    xt = x_true.double()
-
-    def rel(a_, b_):
-        return (torch.linalg.vector_norm((a_ - b_).double()) /
-                torch.linalg.vector_norm(b_.double())).item()
-
-    detail["graph_vs_truth_rel_l2"] = rel(u_g, xt)
-
-    # ---- mixed (FP16 direction) and plain FP32 forms ----
-    if "mixed" in legs:
-        cg_m = NativeCGLS(P, "mixed")
-        if W:
-            cg_m.solve(b, lam=lam, iters=W, refresh=REFRESH)
-        u_m, t_m = timed(lambda: cg_m.solve(b, lam=lam, iters=K, refresh=REFRESH))
-        detail["mixed_iter_per_s"] = world * K / t_m
-        detail["mixed_vs_graph_rel_l2"] = rel(u_m, u_g)
-        del cg_m, u_m
-    if "plain" in legs:
-        cg_p = NativeCGLS(P, "plain")
-        if W:
-            cg_p.solve(b, lam=lam, iters=W)
-        u_p, t_p = timed(lambda: cg_p.solve(b, lam=lam, iters=K))
-        detail["plain_iter_per_s"] = world * K / t_p
-        detail["graph_over_plain"] = t_p / t_g
-        detail["mixed_over_plain"] = (detail["mixed_iter_per_s"] / detail["plain_iter_per_s"]
-                                      if "mixed_iter_per_s" in detail else None)
-        detail["graph_vs_plain_rel_l2"] = rel(u_g, u_p)
-        del cg_p, u_p
-
-    # ---- e2e: host buffers through the C ABI ----
-    e2e = None
-    if "e2e" in legs:
-        bh = torch.empty(b.numel(), dtype=torch.float32, pin_memory=True)
-        bh.copy_(b.cpu())
-        uh = torch.zeros(b.numel(), dtype=torch.float32, pin_memory=True)
-        bn, un = bh.numpy(), uh.numpy()
-        cg_g.solve_host(bn, un, lam=lam, iters=max(W, 1))
-        _, t_e = timed(lambda: cg_g.solve_host(bn, un, lam=lam, iters=K))
-        nb = b.numel() * 4
-        e2e = {"value": world * K / t_e, "unit": "iter/s",
-               "h2d_bytes_per_step": nb / K, "d2h_bytes_per_step": nb / K,
-               "call": f"fl_cgls_solve_host, {K} iterations per call: b in, u out "
-                       "(u0 = 0 needs no copy)"}
-
-    # ---- projector kernels: algorithmic bytes and CUDA-event times ----
-    roofline = None
-    launches = 5 * K + 1          # graph form: fwd, adj, 3 fused updates per iteration + init
-    if "kernels" in legs:
-        from framelab_gb300 import _lib
-        L = _lib.load()
-        cnt = P.count_intersections()
-        n_isect = int(cnt.sum(dtype=torch.int64).item())
-        del cnt
-        n_rays = P.n_rays
-        p32 = (u_g / (u_g.abs().max() + 1e-30)).contiguous()
-        ysc = torch.empty(n_rays, device=dev, dtype=torch.float32)
-        xo = torch.empty(P.n_vox, device=dev, dtype=torch.float32)
-        import ctypes as C
-        from framelab_gb300.projector import DTYPES
-        reps = 3
-
-        def run_fwd():
-            for _ in range(reps):
-                _lib.check(L.fl_forward(P.handle, 16, p32.data_ptr(), DTYPES[torch.float32],
-                                        ysc.data_ptr(), DTYPES[torch.float32], stream.cuda_stream))
-
-        def run_adj():
-            for _ in range(reps):
-                _lib.check(L.fl_adjoint(P.handle, 16, ysc.data_ptr(), DTYPES[torch.float32],
-                                        xo.data_ptr(), DTYPES[torch.float32], stream.cuda_stream))
-        run_fwd(); run_adj()
-        _, tf = timed(run_fwd)
-        _, ta = timed(run_adj)
-        tf /= reps
-        ta /= reps
-        # adjoint launch = weighting pass + gather kernel; report the gather share via ncu
-        b_fwd = n_isect * 4 + n_rays * 4      # f32 voxel gathers + f32 sinogram writes
-        b_adj = n_isect * 4 + P.n_vox * 4     # f32 sinogram gathers + f32 voxel writes
-        peak = None
-        try:
-            with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
-                peak = json.load(fh).get("hbm_gbs")
-            peak_src = "measured"
-        except OSError:
-            peak, peak_src = 6800.0, "fallback"
-        detail.update(n_isect=n_isect, mean_isect_per_ray=n_isect / n_rays,
-                      fwd_ms=tf * 1e3, adj_ms=ta * 1e3,
-                      fwd_alg_GBps=b_fwd / tf / 1e9, adj_alg_GBps=b_adj / ta / 1e9,
-                      fwd_rays_per_s=n_rays / tf, adj_voxel_updates_per_s=n_isect / ta)
-        dom = "adjoint" if ta > tf else "forward"
-        ach = (b_adj / ta if dom == "adjoint" else b_fwd / tf) / 1e9
-        traffic = None
-        tpath = os.path.join(ROOT, "profiles", "traffic.json")
-        if os.path.exists(tpath):
-            with open(tpath) as fh:
-                tj = json.load(fh)
-            ent = tj.get(a.workload, {}).get(dom)
-            if ent:
-                traffic = ent.get("bytes_per_launch")
-        roofline = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
-                    "frac": ach / peak if peak else None, "traffic": traffic,
-                    "kernel": f"matched {dom} (f32 storage)",
-                    "peak_source": peak_src,
-                    "bytes_definition": "sum over rays of voxels crossed x element bytes + "
-                                        "one element per ray (forward) / per voxel (adjoint)"}
-        launches += 0
+    run = {"cone": run_single, "fan": run_single, "batch": run_batch, "sb": run_sb}[w["kind"]]
+    res = run(ctx, a.workload, w, p)
 
     cpu = None
     if rank == 0 and world == 1 and not a.no_cpu:
         cpu = cpu_sample(w, p)
 
     if rank == 0:
-        out = {"metric": metric, "value": value, "unit": "iter/s", "n_gpus": world,
-               "steps": K, "warmup": W, "ms_per_step": 1000.0 * t_g / K,
+        out = {"metric": metric, "value": res["value"], "unit": res["unit"], "n_gpus": world,
+               "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1000.0 * res["t_step"],
                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-               "dtype": "f32",
-               "data": "synthetic: seeded 12-ellipsoid phantom, noiseless projections",
-               "config": config, "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
-               "clocks": clocks.summary(), "gpu_launches": launches, "detail": detail}
+               "dtype": "f32", "data": data, "config": config, "e2e": res["e2e"],
+               "roofline": res["roofline"], "cpu_baseline": cpu, "clocks": res["clocks"],
+               "gpu_launches": res["launches"], "detail": res["detail"]}
         print(json.dumps(out))
     if world > 1:
         import torch.distributed as dist

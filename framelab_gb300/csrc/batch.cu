@@ -1,0 +1,513 @@
+// batch.cu -- many independent fan-beam scans of different sizes (slices with
+// their own nx, ny, detector and view count) projected and solved together.
+//
+// The slices' matched-model tables stay where their plans put them; a batch
+// holds one descriptor per slice and three work lists:
+//  * rays:   chunks of 128 consecutive rays of one slice (forward, weighting),
+//  * pixels: chunks of 128 pixels of one image row of one slice (adjoint),
+//  * vector: chunks of kVecChunk elements of one slice's image (CGLS algebra).
+// Each operator is ONE launch over its list, whatever the mix of sizes; the ray
+// and pixel lists are ordered by decreasing per-item cost (walk length, view
+// count) so the largest slices start first and the tail is made of the
+// cheapest chunks. The forward and adjoint are the matched model of the
+// single-scan kernels (the same device code, matched_dev.cuh), so each slice's
+// result is bit-identical to its own plan's.
+//
+// CGLS (solveCGLS.m:6-31) runs per slice, all slices in lockstep: every slice
+// has its own FP64 gamma/alpha/beta and stop flag, the inner products are
+// segmented by slice (per-chunk FP64 partials; the last chunk of a slice to
+// finish sums that slice's partials in a fixed order, so results do not depend
+// on scheduling). One iteration = 5 launches (forward with c_r^2, adjoint,
+// q += lam p with <p,q>, updates with <r,r>, direction), captured once as a
+// CUDA graph and replayed. A stopped slice's chunks return at once.
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <numeric>
+#include <vector>
+
+#include "fl_common.cuh"
+#include "fl_plan.h"
+#include "matched_dev.cuh"
+
+namespace {
+
+constexpr int kRayChunk = 128;
+constexpr int kPixChunk = 128;
+constexpr int kVecThreads = 256;
+constexpr int kVecChunk = kVecThreads * 16;
+
+struct BatchSlice {
+    const ColEntry* col;
+    const float* colr;
+    const ViewEntry* view;
+    const int* views;      // the frame's view list (id_Y column 0)
+    int nvf;               // its length (Nv[0])
+    DetGrid G;
+    int nx, ny, na, nv;
+    float scale;
+    long long xoff, yoff;  // offsets of the slice in the concatenated image / sinogram
+    int vc0, vc1;          // its vector chunks [vc0, vc1)
+};
+
+struct BatchScal {
+    double gamma, alpha, beta;
+    int done, iter;
+};
+
+struct VecChunk {
+    int slice, start, len, pad;
+};
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block sum of v into partials[blockIdx.x]; returns true in the last block of
+// the slice to arrive, where `total` is then the slice's sum over its chunks
+// [c0, c1) in a fixed order.
+__device__ bool slice_sum(double v, int slice, int c0, int c1, double* partials,
+                          unsigned* tickets, double& total)
+{
+    __shared__ double sw[kVecThreads / 32];
+    __shared__ bool last;
+    v = warp_sum(v);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) sw[w] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double b = 0.0;
+        for (int k = 0; k < kVecThreads / 32; k++) b += sw[k];
+        partials[blockIdx.x] = b;
+        __threadfence();
+        unsigned t = atomicAdd(tickets + slice, 1u);
+        last = (t == (unsigned)(c1 - c0 - 1));
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    double s = 0.0;
+    for (int k = c0 + threadIdx.x; k < c1; k += kVecThreads) s += ((volatile double*)partials)[k];
+    s = warp_sum(s);
+    if (lane == 0) sw[w] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int k = 0; k < kVecThreads / 32; k++) t += sw[k];
+        total = t;
+        tickets[slice] = 0u;
+    }
+    return true;
+}
+
+// y = c_r^cr_power * (sum of w x along each ray), one block per ray chunk
+__global__ void __launch_bounds__(kRayChunk, 8)
+k_batch_fwd(const float* __restrict__ X, float* __restrict__ Y,
+            const BatchSlice* __restrict__ sl, const int2* __restrict__ chunks, int cr_power,
+            const BatchScal* __restrict__ S)
+{
+    const int2 ch = chunks[blockIdx.x];
+    if (S && S[ch.x].done) return;
+    const BatchSlice& b = sl[ch.x];
+    const int r = ch.y + threadIdx.x;
+    if (r >= b.na * b.nv) return;
+    const ColEntry ce = b.col[r];
+    float acc = walk<float, false, false>(X + b.xoff, ce.inv_x, ce.off_x, ce.inv_y, ce.off_y,
+                                          0.0f, 0.0f, b.nx, b.ny, 1, nullptr);
+    float cr = ray_cr(b.scale, b.colr[r], 0.0f);
+    float out = cr * acc;
+    if (cr_power == 2) out = cr * out;
+    Y[b.yoff + r] = out;
+}
+
+// yw = c_r * y over the ray chunks (input of the stand-alone adjoint)
+__global__ void __launch_bounds__(kRayChunk)
+k_batch_weight(float* __restrict__ YW, const float* __restrict__ Y,
+               const BatchSlice* __restrict__ sl, const int2* __restrict__ chunks)
+{
+    const int2 ch = chunks[blockIdx.x];
+    const BatchSlice& b = sl[ch.x];
+    const int r = ch.y + threadIdx.x;
+    if (r >= b.na * b.nv) return;
+    float cr = ray_cr(b.scale, b.colr[r], 0.0f);
+    YW[b.yoff + r] = cr * Y[b.yoff + r];
+}
+
+// x = A^T (pre-weighted yw), one block per 128-pixel row chunk
+__global__ void __launch_bounds__(kPixChunk)
+k_batch_adj(float* __restrict__ X, const float* __restrict__ YW,
+            const BatchSlice* __restrict__ sl, const int4* __restrict__ chunks,
+            const BatchScal* __restrict__ S)
+{
+    const int4 ch = chunks[blockIdx.x];       // (slice, iy, ix0, -)
+    if (S && S[ch.x].done) return;
+    const BatchSlice& b = sl[ch.x];
+    const int ix = ch.z + threadIdx.x;
+    if (ix >= b.nx) return;
+    float acc = fan_pixel_gather(YW + b.yoff, b.col, b.view, b.views, b.nvf, b.G, ix, ch.y,
+                                 b.nx, b.ny, b.na);
+    X[b.xoff + (long long)ch.y * b.nx + ix] = acc;
+}
+
+// r = q + lam u - b (q null: r = -b) ; p = -r ; gamma = <r, r>
+__global__ void __launch_bounds__(kVecThreads)
+k_batch_init(const float* __restrict__ bvec, const float* __restrict__ q,
+             const float* __restrict__ u, float lam, float* __restrict__ r,
+             float* __restrict__ p, const BatchSlice* __restrict__ sl,
+             const VecChunk* __restrict__ vc, BatchScal* S, double* partials,
+             unsigned* tickets)
+{
+    const VecChunk c = vc[blockIdx.x];
+    const BatchSlice& b = sl[c.slice];
+    const long long o = b.xoff + c.start;
+    double s = 0.0;
+    for (int k = threadIdx.x; k < c.len; k += kVecThreads) {
+        const long long i = o + k;
+        float ri = q ? fmaf(lam, u[i], q[i]) - bvec[i] : -bvec[i];
+        r[i] = ri;
+        p[i] = -ri;
+        s += (double)ri * ri;
+    }
+    double tot;
+    if (slice_sum(s, c.slice, b.vc0, b.vc1, partials, tickets, tot) && threadIdx.x == 0) {
+        BatchScal& z = S[c.slice];
+        z.gamma = tot; z.alpha = 0.0; z.beta = 0.0; z.iter = 0;
+        z.done = 0;
+    }
+}
+
+// q += lam p ; alpha = gamma / <p, q>  (a slice whose <p, q> is zero stops)
+__global__ void __launch_bounds__(kVecThreads)
+k_batch_pq(const float* __restrict__ p, float* __restrict__ q, float lam,
+           const BatchSlice* __restrict__ sl, const VecChunk* __restrict__ vc, BatchScal* S,
+           double* partials, unsigned* tickets)
+{
+    const VecChunk c = vc[blockIdx.x];
+    if (S[c.slice].done) return;
+    const BatchSlice& b = sl[c.slice];
+    const long long o = b.xoff + c.start;
+    double s = 0.0;
+    for (int k = threadIdx.x; k < c.len; k += kVecThreads) {
+        const long long i = o + k;
+        float pi = p[i];
+        float qi = fmaf(lam, pi, q[i]);
+        q[i] = qi;
+        s += (double)pi * qi;
+    }
+    double tot;
+    if (slice_sum(s, c.slice, b.vc0, b.vc1, partials, tickets, tot) && threadIdx.x == 0) {
+        BatchScal& z = S[c.slice];
+        if (tot != 0.0) z.alpha = z.gamma / tot;
+        else { z.alpha = 0.0; z.done = 1; }
+    }
+}
+
+// u += alpha p ; r += alpha q ; gamma' = <r, r> ; beta = gamma'/gamma ; stop test
+__global__ void __launch_bounds__(kVecThreads)
+k_batch_update(float* __restrict__ u, float* __restrict__ r, const float* __restrict__ p,
+               const float* __restrict__ q, double tol, const BatchSlice* __restrict__ sl,
+               const VecChunk* __restrict__ vc, BatchScal* S, double* partials,
+               unsigned* tickets, double* hist, int hist_cap)
+{
+    const VecChunk c = vc[blockIdx.x];
+    if (S[c.slice].done) return;
+    const BatchSlice& b = sl[c.slice];
+    const long long o = b.xoff + c.start;
+    const float a = (float)S[c.slice].alpha;
+    double s = 0.0;
+    for (int k = threadIdx.x; k < c.len; k += kVecThreads) {
+        const long long i = o + k;
+        u[i] = fmaf(a, p[i], u[i]);
+        float ri = fmaf(a, q[i], r[i]);
+        r[i] = ri;
+        s += (double)ri * ri;
+    }
+    double tot;
+    if (slice_sum(s, c.slice, b.vc0, b.vc1, partials, tickets, tot) && threadIdx.x == 0) {
+        BatchScal& z = S[c.slice];
+        z.beta = tot / z.gamma;
+        z.gamma = tot;
+        if (hist && z.iter < hist_cap) hist[(long long)c.slice * hist_cap + z.iter] = tot;
+        z.iter += 1;
+        if (tot < tol) z.done = 1;
+    }
+}
+
+// p = -r + beta p
+__global__ void __launch_bounds__(kVecThreads)
+k_batch_dir(const float* __restrict__ r, float* __restrict__ p,
+            const BatchSlice* __restrict__ sl, const VecChunk* __restrict__ vc,
+            const BatchScal* __restrict__ S)
+{
+    const VecChunk c = vc[blockIdx.x];
+    if (S[c.slice].done) return;
+    const BatchSlice& b = sl[c.slice];
+    const long long o = b.xoff + c.start;
+    const float be = (float)S[c.slice].beta;
+    for (int k = threadIdx.x; k < c.len; k += kVecThreads) {
+        const long long i = o + k;
+        p[i] = fmaf(be, p[i], -r[i]);
+    }
+}
+
+}  // namespace
+
+struct fl_batch {
+    int n;
+    long long n_vox, n_rays;
+    std::vector<long long> xoff, yoff;   // [n + 1]
+    BatchSlice* d_sl;
+    int2* d_rays;  int n_ray_chunks;
+    int4* d_pix;   int n_pix_chunks;
+    VecChunk* d_vec; int n_vec_chunks;
+    float *r, *p, *q, *tmp;
+    BatchScal* S;
+    double* partials;
+    unsigned* tickets;
+    double* hist;
+    int hist_cap;
+    cudaStream_t cs;
+    cudaEvent_t ev0, ev1;
+    cudaGraphExec_t exec;
+    float* cap_u;
+    float cap_lam;
+    double cap_tol;
+};
+
+static void batch_free(fl_batch* b)
+{
+    void* ptrs[] = {b->d_sl, b->d_rays, b->d_pix, b->d_vec, b->r, b->p, b->q, b->tmp,
+                    b->S, b->partials, b->tickets, b->hist};
+    for (void* q : ptrs)
+        if (q) cudaFree(q);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->cs) cudaStreamDestroy(b->cs);
+    if (b->ev0) cudaEventDestroy(b->ev0);
+    if (b->ev1) cudaEventDestroy(b->ev1);
+}
+
+template <typename T>
+static int upload_vec(T** d, const std::vector<T>& h)
+{
+    FL_CUDA(cudaMalloc((void**)d, sizeof(T) * (h.empty() ? 1 : h.size())));
+    if (!h.empty()) FL_CUDA(cudaMemcpy(*d, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice));
+    return FL_OK;
+}
+
+extern "C" int fl_batch_create(fl_plan* const* plans, int32_t n_plans, fl_batch** out)
+{
+    if (!plans || !out || n_plans < 1)
+        return fl_set_error(FL_ERR_INVALID, "fl_batch_create: bad argument");
+    *out = nullptr;
+    std::vector<BatchSlice> sl(n_plans);
+    std::vector<long long> xoff(n_plans + 1, 0), yoff(n_plans + 1, 0);
+    for (int i = 0; i < n_plans; i++) {
+        fl_plan* p = plans[i];
+        if (!p) return fl_set_error(FL_ERR_INVALID, "fl_batch_create: plan %d is null", i);
+        const fl_scan& s = p->s;
+        if (s.ndim != 2)
+            return fl_set_error(FL_ERR_UNSUPPORTED, "fl_batch_create: plan %d is not fan-beam", i);
+        if (s.nt != 1)
+            return fl_set_error(FL_ERR_UNSUPPORTED, "fl_batch_create: plan %d has %d frames "
+                                "(batched slices are single-frame)", i, s.nt);
+        int st = fl_matched_ready(p);
+        if (st) return st;
+        if (p->det_kind < 0)
+            return fl_set_error(FL_ERR_UNSUPPORTED, "fl_batch_create: plan %d needs a uniform "
+                                "flat or equiangular detector", i);
+        int nvf = 0;
+        FL_CUDA(cudaMemcpy(&nvf, p->d_Nv, sizeof(int), cudaMemcpyDeviceToHost));
+        if ((long long)s.na * s.nv >= (1LL << 31) || (long long)s.nx * s.ny >= (1LL << 31))
+            return fl_set_error(FL_ERR_UNSUPPORTED, "fl_batch_create: plan %d too large", i);
+        BatchSlice& b = sl[i];
+        std::memset(&b, 0, sizeof b);
+        b.col = p->d_col; b.colr = p->d_colr; b.view = p->d_view;
+        b.views = p->d_idY; b.nvf = nvf;
+        b.G.kind = p->det_kind; b.G.u0 = p->u0; b.G.du = p->du; b.G.g0 = p->g0; b.G.dg = p->dg;
+        b.G.v0 = p->v0; b.G.dv = p->dv; b.G.SO = s.SO; b.G.SD = p->SD;
+        b.nx = s.nx; b.ny = s.ny; b.na = s.na; b.nv = s.nv; b.scale = s.scale;
+        xoff[i + 1] = xoff[i] + (long long)s.nx * s.ny;
+        yoff[i + 1] = yoff[i] + (long long)s.na * s.nv;
+        b.xoff = xoff[i]; b.yoff = yoff[i];
+    }
+    // work lists, costliest slices first
+    std::vector<int> by_walk(n_plans), by_views(n_plans);
+    std::iota(by_walk.begin(), by_walk.end(), 0);
+    std::iota(by_views.begin(), by_views.end(), 0);
+    std::stable_sort(by_walk.begin(), by_walk.end(), [&](int a, int c) {
+        return sl[a].nx + sl[a].ny > sl[c].nx + sl[c].ny;
+    });
+    std::stable_sort(by_views.begin(), by_views.end(), [&](int a, int c) {
+        return sl[a].nvf > sl[c].nvf;
+    });
+    std::vector<int2> rays;
+    for (int i : by_walk)
+        for (int r = 0; r < sl[i].na * sl[i].nv; r += kRayChunk) rays.push_back(make_int2(i, r));
+    std::vector<int4> pix;
+    for (int i : by_views)
+        for (int iy = 0; iy < sl[i].ny; iy++)
+            for (int ix = 0; ix < sl[i].nx; ix += kPixChunk) pix.push_back(make_int4(i, iy, ix, 0));
+    std::vector<VecChunk> vec;
+    for (int i = 0; i < n_plans; i++) {
+        sl[i].vc0 = (int)vec.size();
+        long long n = (long long)sl[i].nx * sl[i].ny;
+        for (long long k = 0; k < n; k += kVecChunk)
+            vec.push_back(VecChunk{i, (int)k, (int)std::min<long long>(kVecChunk, n - k), 0});
+        sl[i].vc1 = (int)vec.size();
+    }
+    if (rays.size() > 0x7fffffffu || pix.size() > 0x7fffffffu || vec.size() > 0x7fffffffu)
+        return fl_set_error(FL_ERR_UNSUPPORTED, "fl_batch_create: batch too large");
+
+    fl_batch* b = new (std::nothrow) fl_batch;
+    if (!b) return fl_set_error(FL_ERR_ALLOC, "out of host memory");
+    b->n = n_plans; b->n_vox = xoff[n_plans]; b->n_rays = yoff[n_plans];
+    b->xoff = xoff; b->yoff = yoff;
+    b->d_sl = nullptr; b->d_rays = nullptr; b->d_pix = nullptr; b->d_vec = nullptr;
+    b->r = b->p = b->q = b->tmp = nullptr; b->S = nullptr; b->partials = nullptr;
+    b->tickets = nullptr; b->hist = nullptr; b->hist_cap = 4096;
+    b->cs = nullptr; b->ev0 = b->ev1 = nullptr; b->exec = nullptr; b->cap_u = nullptr;
+    b->cap_lam = 0.0f; b->cap_tol = 0.0;
+    b->n_ray_chunks = (int)rays.size(); b->n_pix_chunks = (int)pix.size();
+    b->n_vec_chunks = (int)vec.size();
+    int st = upload_vec(&b->d_sl, sl);
+    if (!st) st = upload_vec(&b->d_rays, rays);
+    if (!st) st = upload_vec(&b->d_pix, pix);
+    if (!st) st = upload_vec(&b->d_vec, vec);
+    auto M = [&](void** ptr, size_t bytes) {
+        if (!st) st = fl_check_cuda(cudaMalloc(ptr, bytes), "cudaMalloc(batch)");
+    };
+    M((void**)&b->r, b->n_vox * 4); M((void**)&b->p, b->n_vox * 4); M((void**)&b->q, b->n_vox * 4);
+    M((void**)&b->tmp, b->n_rays * 4);
+    M((void**)&b->S, sizeof(BatchScal) * n_plans);
+    M((void**)&b->partials, sizeof(double) * b->n_vec_chunks);
+    M((void**)&b->tickets, sizeof(unsigned) * n_plans);
+    M((void**)&b->hist, sizeof(double) * (size_t)b->hist_cap * n_plans);
+    if (!st) st = fl_check_cuda(cudaMemset(b->tickets, 0, sizeof(unsigned) * n_plans), "memset");
+    if (!st) st = fl_check_cuda(cudaMemset(b->S, 0, sizeof(BatchScal) * n_plans), "memset");
+    if (!st) st = fl_check_cuda(cudaStreamCreateWithFlags(&b->cs, cudaStreamNonBlocking), "stream");
+    if (!st) st = fl_check_cuda(cudaEventCreateWithFlags(&b->ev0, cudaEventDisableTiming), "event");
+    if (!st) st = fl_check_cuda(cudaEventCreateWithFlags(&b->ev1, cudaEventDisableTiming), "event");
+    if (st) { batch_free(b); delete b; return st; }
+    *out = b;
+    return fl_set_error(FL_OK, "");
+}
+
+extern "C" void fl_batch_destroy(fl_batch* b)
+{
+    if (!b) return;
+    batch_free(b);
+    delete b;
+}
+
+extern "C" int fl_batch_layout(const fl_batch* b, int64_t* vox_offsets, int64_t* ray_offsets)
+{
+    if (!b) return fl_set_error(FL_ERR_INVALID, "fl_batch_layout: null batch");
+    for (int i = 0; i <= b->n; i++) {
+        if (vox_offsets) vox_offsets[i] = b->xoff[i];
+        if (ray_offsets) ray_offsets[i] = b->yoff[i];
+    }
+    return fl_set_error(FL_OK, "");
+}
+
+static int batch_fwd(fl_batch* b, const float* x, float* y, int cr_power, const BatchScal* S,
+                     cudaStream_t s)
+{
+    k_batch_fwd<<<b->n_ray_chunks, kRayChunk, 0, s>>>(x, y, b->d_sl, b->d_rays, cr_power, S);
+    return fl_check_launch("batched forward");
+}
+
+static int batch_adj_w(fl_batch* b, const float* yw, float* x, const BatchScal* S, cudaStream_t s)
+{
+    k_batch_adj<<<b->n_pix_chunks, kPixChunk, 0, s>>>(x, yw, b->d_sl, b->d_pix, S);
+    return fl_check_launch("batched adjoint");
+}
+
+extern "C" int fl_batch_forward(fl_batch* b, const float* x, float* y, void* stream)
+{
+    if (!b || !x || !y) return fl_set_error(FL_ERR_INVALID, "fl_batch_forward: null argument");
+    int st = batch_fwd(b, x, y, 1, nullptr, (cudaStream_t)stream);
+    return st ? st : fl_set_error(FL_OK, "");
+}
+
+// Uses the batch's sinogram scratch: calls on one batch are stream-ordered.
+extern "C" int fl_batch_adjoint(fl_batch* b, const float* y, float* x, void* stream)
+{
+    if (!b || !x || !y) return fl_set_error(FL_ERR_INVALID, "fl_batch_adjoint: null argument");
+    cudaStream_t s = (cudaStream_t)stream;
+    k_batch_weight<<<b->n_ray_chunks, kRayChunk, 0, s>>>(b->tmp, y, b->d_sl, b->d_rays);
+    int st = fl_check_launch("batched weighting");
+    if (!st) st = batch_adj_w(b, b->tmp, x, nullptr, s);
+    return st ? st : fl_set_error(FL_OK, "");
+}
+
+static int batch_iteration(fl_batch* b, float* u, float lam, double tol, cudaStream_t s)
+{
+    int st = batch_fwd(b, b->p, b->tmp, 2, b->S, s);
+    if (!st) st = batch_adj_w(b, b->tmp, b->q, b->S, s);
+    if (st) return st;
+    const int g = b->n_vec_chunks;
+    k_batch_pq<<<g, kVecThreads, 0, s>>>(b->p, b->q, lam, b->d_sl, b->d_vec, b->S, b->partials,
+                                         b->tickets);
+    k_batch_update<<<g, kVecThreads, 0, s>>>(u, b->r, b->p, b->q, tol, b->d_sl, b->d_vec, b->S,
+                                             b->partials, b->tickets, b->hist, b->hist_cap);
+    k_batch_dir<<<g, kVecThreads, 0, s>>>(b->r, b->p, b->d_sl, b->d_vec, b->S);
+    return fl_check_launch("batched CGLS iteration");
+}
+
+extern "C" int fl_batch_cgls(fl_batch* b, const float* rhs, float* u, float lam, int32_t iters,
+                             double tol, int32_t flags, double* gamma_history,
+                             int32_t* iters_done, void* stream)
+{
+    if (!b || !rhs || !u || iters < 0)
+        return fl_set_error(FL_ERR_INVALID, "fl_batch_cgls: bad argument");
+    cudaStream_t us = (cudaStream_t)stream, s = b->cs;
+    int st;
+    FL_CUDA(cudaEventRecord(b->ev0, us));
+    FL_CUDA(cudaStreamWaitEvent(s, b->ev0, 0));
+    const float* q0 = nullptr;
+    if (!(flags & FL_CGLS_ZERO_START)) {
+        if ((st = batch_fwd(b, u, b->tmp, 2, nullptr, s))) return st;
+        if ((st = batch_adj_w(b, b->tmp, b->q, nullptr, s))) return st;
+        q0 = b->q;
+    }
+    k_batch_init<<<b->n_vec_chunks, kVecThreads, 0, s>>>(rhs, q0, u, lam, b->r, b->p, b->d_sl,
+                                                         b->d_vec, b->S, b->partials, b->tickets);
+    if ((st = fl_check_launch("batched CGLS init"))) return st;
+    if (!b->exec || b->cap_u != u || b->cap_lam != lam || b->cap_tol != tol) {
+        if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
+        cudaGraph_t g;
+        FL_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        int cst = batch_iteration(b, u, lam, tol, s);
+        cudaError_t e = cudaStreamEndCapture(s, &g);
+        if (cst) return cst;
+        FL_CUDA(e);
+        e = cudaGraphInstantiate(&b->exec, g, 0);
+        cudaGraphDestroy(g);
+        FL_CUDA(e);
+        b->cap_u = u; b->cap_lam = lam; b->cap_tol = tol;
+    }
+    for (int it = 0; it < iters; it++) FL_CUDA(cudaGraphLaunch(b->exec, s));
+    std::vector<BatchScal> fin(b->n);
+    FL_CUDA(cudaMemcpyAsync(fin.data(), b->S, sizeof(BatchScal) * b->n, cudaMemcpyDeviceToHost, s));
+    const int nh = std::min(iters, b->hist_cap);
+    std::vector<double> h;
+    if (gamma_history && nh > 0) {
+        h.resize((size_t)b->hist_cap * b->n);
+        FL_CUDA(cudaMemcpyAsync(h.data(), b->hist, sizeof(double) * h.size(),
+                                cudaMemcpyDeviceToHost, s));
+    }
+    FL_CUDA(cudaEventRecord(b->ev1, s));
+    FL_CUDA(cudaStreamWaitEvent(us, b->ev1, 0));
+    FL_CUDA(cudaStreamSynchronize(s));
+    for (int i = 0; i < b->n; i++) {
+        if (iters_done) iters_done[i] = fin[i].iter;
+        if (gamma_history)
+            for (int k = 0; k < iters; k++)
+                gamma_history[(size_t)i * iters + k] =
+                    (k < nh && k < fin[i].iter) ? h[(size_t)i * b->hist_cap + k] : 0.0;
+    }
+    return fl_set_error(FL_OK, "");
+}

@@ -17,99 +17,9 @@
 // entries -- the exact transpose, with no atomics.
 #include "fl_common.cuh"
 #include "fl_plan.h"
+#include "matched_dev.cuh"
 
 namespace {
-
-template <typename T>
-__device__ __forceinline__ float ldv(const T* p) { return Store<T>::ld(p); }
-
-// Slab index of the ray at parameter a on one axis, consistent with the FP32
-// crossings: inv > 0 -> A(j) <= a < A(j+1); inv < 0 -> A(j+1) <= a < A(j).
-__device__ __forceinline__ int start_slab(float a, float inv, float off, int n)
-{
-    float t = floorf(__fdividef(a - off, inv));
-    t = fminf(fmaxf(t, 0.0f), (float)(n - 1));   // NaN -> 0
-    int j = (int)t;
-    if (inv > 0.0f) {
-        while (j < n - 1 && fmaf((float)(j + 1), inv, off) <= a) j++;
-        while (j > 0 && fmaf((float)j, inv, off) > a) j--;
-    } else {
-        while (j > 0 && fmaf((float)j, inv, off) <= a) j--;
-        while (j < n - 1 && fmaf((float)(j + 1), inv, off) > a) j++;
-    }
-    return j;
-}
-
-// Walk one ray through an nx*ny*nz volume (nz == 1 with no z axis for 2-D).
-// Returns sum over voxels of w * x; *nseg counts segments with w > 0.
-// Termination: every step advances at least one axis to a strictly larger
-// crossing (consecutive FP32 crossings of one axis are thousands of ulps
-// apart for any table fl_plan_create accepts), and the loop leaves as soon as
-// the crossing reaches the exit (or is NaN); the step budget nx+ny+nz+4 is a
-// second, independent bound.
-template <typename TX, bool THREE, bool COUNT>
-__device__ __forceinline__ float walk(const TX* __restrict__ x, float inv_x, float off_x,
-                                      float inv_y, float off_y, float inv_z, float off_z,
-                                      int nx, int ny, int nz, int* nseg)
-{
-    float ax0 = fmaf(0.0f, inv_x, off_x), ax1 = fmaf((float)nx, inv_x, off_x);
-    float ay0 = fmaf(0.0f, inv_y, off_y), ay1 = fmaf((float)ny, inv_y, off_y);
-    float a_in = fmaxf(fminf(ax0, ax1), fminf(ay0, ay1));
-    float a_out = fminf(fmaxf(ax0, ax1), fmaxf(ay0, ay1));
-    if (THREE) {
-        float az0 = fmaf(0.0f, inv_z, off_z), az1 = fmaf((float)nz, inv_z, off_z);
-        a_in = fmaxf(a_in, fminf(az0, az1));
-        a_out = fminf(a_out, fmaxf(az0, az1));
-    }
-    if (!(a_in < a_out)) { if (COUNT) *nseg = 0; return 0.0f; }
-    const int jx = start_slab(a_in, inv_x, off_x, nx);
-    const int jy = start_slab(a_in, inv_y, off_y, ny);
-    const int jz = THREE ? start_slab(a_in, inv_z, off_z, nz) : 0;
-    int v = (jz * ny + jy) * nx + jx;              // < 2^31 (checked at plan creation)
-    const bool px = inv_x > 0.0f, py = inv_y > 0.0f, pz = inv_z > 0.0f;
-    float pax = (float)(px ? jx + 1 : jx);
-    float pay = (float)(py ? jy + 1 : jy);
-    float paz = (float)(pz ? jz + 1 : jz);
-    const float stx = px ? 1.0f : -1.0f, sty = py ? 1.0f : -1.0f, stz = pz ? 1.0f : -1.0f;
-    const int dvx = px ? 1 : -1, dvy = py ? nx : -nx, dvz = pz ? nx * ny : -(nx * ny);
-    float nAx = fmaf(pax, inv_x, off_x);
-    float nAy = fmaf(pay, inv_y, off_y);
-    float nAz = THREE ? fmaf(paz, inv_z, off_z) : 3.0e38f;
-    float cur = a_in, acc = 0.0f;
-    int cnt = 0;
-    // the gather of the next voxel is issued as soon as its index is known and
-    // consumed one step later, so its latency overlaps the next step's compares
-    float xv = COUNT ? 0.0f : ldv(x + v);
-    const int budget = nx + ny + (THREE ? nz : 0) + 4;
-    for (int it = 0; it < budget; it += 4) {
-#pragma unroll
-        for (int u = 0; u < 4; u++) {
-            const float nxt = THREE ? fminf(fminf(nAx, nAy), nAz) : fminf(nAx, nAy);
-            const float seg = nxt - cur;
-            const bool cont = nxt < a_out;          // false at the exit (and for NaN)
-            float xn = 0.0f;
-            if (cont) {
-                if (nAx == nxt) { pax += stx; v += dvx; nAx = fmaf(pax, inv_x, off_x); }
-                if (nAy == nxt) { pay += sty; v += dvy; nAy = fmaf(pay, inv_y, off_y); }
-                if (THREE && nAz == nxt) { paz += stz; v += dvz; nAz = fmaf(paz, inv_z, off_z); }
-                if (!COUNT) xn = ldv(x + v);        // v is inside the volume here
-            }
-            if (COUNT) cnt += (seg > 0.0f);
-            else acc = fmaf(seg, xv, acc);
-            if (!cont) goto done;
-            xv = xn;
-            cur = nxt;
-        }
-    }
-done:
-    if (COUNT) *nseg = cnt;
-    return acc;
-}
-
-__device__ __forceinline__ float ray_cr(float scale, float dxy2, float dz2)
-{
-    return fmul(scale, fsqrt(fadd(dxy2, dz2)));
-}
 
 // ---------------------------------------------------------------------------
 // Forward kernels. Block (32, 4): 32 adjacent detector columns x 4 rows of one
@@ -204,43 +114,6 @@ __global__ void k_weight(float* __restrict__ yw, const TY* __restrict__ y,
     yw[r] = cr * Store<TY>::ld_plain(y + r);
 }
 
-// ---------------------------------------------------------------------------
-// Adjoint helpers: detector column window of an axis-aligned xy box.
-// ---------------------------------------------------------------------------
-struct DetGrid {
-    int kind;          // 0 flat uniform, 1 equiangular
-    float u0, du, g0, dg, v0, dv, SO, SD;
-};
-
-// Column range [lo, hi] of rays that can cross the xy square [x0,x0+1]x[y0,y0+1]
-// in a view with cos/sin (c, s); also returns the depth range SO + t.
-__device__ __forceinline__ void column_window(const DetGrid& G, float c, float s, float x0,
-                                              float y0, float wx, float wy, int na, int& lo,
-                                              int& hi, float& dmin, float& dmax)
-{
-    float umin = 3.0e38f, umax = -3.0e38f;
-    dmin = 3.0e38f; dmax = -3.0e38f;
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-        float px = x0 + ((k & 1) ? wx : 0.0f);
-        float py = y0 + ((k & 2) ? wy : 0.0f);
-        float depth = G.SO + (c * px + s * py);        // distance from source along the axis
-        float lat = -s * px + c * py;
-        float u = (G.kind == 0) ? G.SD * __fdividef(lat, depth) : atan2f(lat, depth);
-        umin = fminf(umin, u); umax = fmaxf(umax, u);
-        dmin = fminf(dmin, depth); dmax = fmaxf(dmax, depth);
-    }
-    float f0, f1;
-    if (G.kind == 0) { f0 = (umin - G.u0) / G.du; f1 = (umax - G.u0) / G.du; }
-    else             { f0 = (umin - G.g0) / G.dg; f1 = (umax - G.g0) / G.dg; }
-    if (f0 > f1) { float t = f0; f0 = f1; f1 = t; }
-    // the rays of columns whose detector position lies in the shadow [f0, f1];
-    // 0.02 column of slack covers the float evaluation and the tolerance
-    // fl_plan_create allows between y_det and the uniform grid
-    f0 = fmaxf(ceilf(f0 - 0.02f), 0.0f);
-    f1 = fminf(floorf(f1 + 0.02f), (float)(na - 1));
-    lo = (int)f0; hi = (int)f1;                   // empty when lo > hi
-}
 
 // ---------------------------------------------------------------------------
 // Fan adjoint: one thread per (pixel, frame).
@@ -257,27 +130,7 @@ k_adj_fan(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __re
     int iy = blockIdx.y;
     int it = blockIdx.z;
     if (ix >= nx) return;
-    float x0 = (float)(ix - nx / 2), y0 = (float)(iy - ny / 2);
-    float fx0 = (float)ix, fx1 = (float)(ix + 1), fy0 = (float)iy, fy1 = (float)(iy + 1);
-    float acc = 0.0f;
-    int nvf = Nv[it];
-    for (int j = 0; j < nvf; j++) {
-        int iv = idY[it * tmp_size + j];
-        ViewEntry ve = view[iv];
-        int lo, hi; float dmin, dmax;
-        column_window(G, ve.c, ve.s, x0, y0, 1.0f, 1.0f, na, lo, hi, dmin, dmax);
-        const ColEntry* cv = col + (long long)iv * na;
-        const float* yv = yw + (long long)iv * na;
-        for (int ia = lo; ia <= hi; ia++) {
-            ColEntry ce = cv[ia];
-            float ax0 = fmaf(fx0, ce.inv_x, ce.off_x), ax1 = fmaf(fx1, ce.inv_x, ce.off_x);
-            float ay0 = fmaf(fy0, ce.inv_y, ce.off_y), ay1 = fmaf(fy1, ce.inv_y, ce.off_y);
-            float l = fmaxf(fminf(ax0, ax1), fminf(ay0, ay1));
-            float h = fminf(fmaxf(ax0, ax1), fmaxf(ay0, ay1));
-            float w = h - l;
-            if (w > 0.0f) acc = fmaf(w, __ldg(yv + ia), acc);
-        }
-    }
+    float acc = fan_pixel_gather(yw, col, view, idY + it * tmp_size, Nv[it], G, ix, iy, nx, ny, na);
     Store<TX>::st(X + (long long)it * nx * ny + (long long)iy * nx + ix, acc);
 }
 

@@ -281,6 +281,31 @@ int fl_cgls_solve_host(fl_cgls *cg, const float *b_host, float *u_host, float la
                        double tol, int refresh, int flags, double *gamma_history,
                        int *iters_done, void *stream);
 
+/* ---- batched uneven fan-beam slices ------------------------------------
+ * A batch projects and solves many independent single-frame fan-beam scans of
+ * different sizes at once (matched model): images and sinograms of all slices
+ * are concatenated in plan order (offsets from fl_batch_layout) and every
+ * operator is one launch over all slices. Each slice's forward/adjoint result
+ * is bit-identical to its own plan's. The plans must outlive the batch.
+ * Replaces looping the reference's per-slice Ax_fan_mf / Atx_fan_mf calls
+ * (FanBeamScanner/apply.m:11-20, applyAdjoint.m:21-29) and solveCGLS.m:6-31
+ * over the slices. */
+typedef struct fl_batch fl_batch;
+int fl_batch_create(fl_plan *const *plans, int32_t n_plans, fl_batch **out);
+void fl_batch_destroy(fl_batch *b);
+/* vox_offsets / ray_offsets: [n_plans + 1] each (either may be NULL) */
+int fl_batch_layout(const fl_batch *b, int64_t *vox_offsets, int64_t *ray_offsets);
+int fl_batch_forward(fl_batch *b, const float *x, float *y, void *stream);
+int fl_batch_adjoint(fl_batch *b, const float *y, float *x, void *stream);
+/* CGLS per slice on (A_i^T A_i + lam I) u_i = rhs_i, all slices in lockstep,
+ * each stopping on its own once gamma_i < tol (or <p, q> = 0). u: initial
+ * guess in (ignored with FL_CGLS_ZERO_START), result out (device).
+ * gamma_history (host, optional): [n_plans * iters], row i = slice i's gamma
+ * after each iteration (0 after it stopped); iters_done (host, optional):
+ * [n_plans]. One iteration is a replayed CUDA graph of 5 launches. */
+int fl_batch_cgls(fl_batch *b, const float *rhs, float *u, float lam, int32_t iters, double tol,
+                  int32_t flags, double *gamma_history, int32_t *iters_done, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
