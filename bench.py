@@ -619,11 +619,11 @@ def run_sb(ctx, name, w, p):
     e2e = None
     if "e2e" in ctx.legs:
         fh = torch.empty(f.numel(), dtype=torch.float32, pin_memory=True)
-        fh.copy_(f.cpu())
+        fh.copy_(f.reshape(-1).cpu())
         uh = torch.empty(P.n_vox, dtype=torch.float32, pin_memory=True)
 
         def host_solve():
-            fd = fh.to(ctx.dev, non_blocking=True)
+            fd = fh.to(ctx.dev, non_blocking=True).view_as(f)
             uh.copy_(split_bregman(P, fd, u0, outer=K, **kw)[0], non_blocking=True)
         _, t_e = ctx.timed(host_solve)
         e2e = {"value": world * K / t_e, "unit": "iter/s",

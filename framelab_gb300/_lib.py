@@ -17,6 +17,7 @@ _lib = None
 FL_OK, FL_ERR_INVALID, FL_ERR_UNSUPPORTED, FL_ERR_CUDA, FL_ERR_ALLOC, FL_ERR_TIMEOUT = range(6)
 MODEL_SIDDON_REF, MODEL_CHORD_REF, MODEL_GAO_REF, MODEL_FB_REF, MODEL_MATCHED = 0, 1, 2, 3, 16
 F32, F16, BF16 = 0, 1, 2
+OPT_Z_MIRROR = 1
 
 
 class FLError(RuntimeError):
@@ -50,6 +51,8 @@ _SIGS = {
     "fl_plan_create": (_I, [C.POINTER(Scan), C.POINTER(_P)]),
     "fl_plan_destroy": (None, [_P]),
     "fl_plan_sizes": (_I, [_P, C.POINTER(_I64), C.POINTER(_I64)]),
+    "fl_plan_option": (_I, [_P, _I, _I]),
+    "fl_plan_query": (_I, [_P, _I, C.POINTER(_I)]),
     "fl_forward": (_I, [_P, _I, _V, _I, _V, _I, _V]),
     "fl_adjoint": (_I, [_P, _I, _V, _I, _V, _I, _V]),
     "fl_count_intersections": (_I, [_P, _V, _V]),

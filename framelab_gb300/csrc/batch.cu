@@ -4,7 +4,7 @@
 // The slices' matched-model tables stay where their plans put them; a batch
 // holds one descriptor per slice and three work lists:
 //  * rays:   chunks of 128 consecutive rays of one slice (forward, weighting),
-//  * pixels: chunks of 128 pixels of one image row of one slice (adjoint),
+//  * pixels: chunks of 2 image rows x 256 columns of one slice (adjoint),
 //  * vector: chunks of kVecChunk elements of one slice's image (CGLS algebra).
 // Each operator is ONE launch over its list, whatever the mix of sizes; the ray
 // and pixel lists are ordered by decreasing per-item cost (walk length, view
@@ -136,20 +136,28 @@ k_batch_weight(float* __restrict__ YW, const float* __restrict__ Y,
     YW[b.yoff + r] = cr * Y[b.yoff + r];
 }
 
-// x = A^T (pre-weighted yw), one block per 128-pixel row chunk
+// x = A^T (pre-weighted yw), one block per chunk of 2 image rows x
+// 2*kPixChunk columns, one thread per 2 x 2 pixel block
 __global__ void __launch_bounds__(kPixChunk)
 k_batch_adj(float* __restrict__ X, const float* __restrict__ YW,
             const BatchSlice* __restrict__ sl, const int4* __restrict__ chunks,
             const BatchScal* __restrict__ S)
 {
-    const int4 ch = chunks[blockIdx.x];       // (slice, iy, ix0, -)
+    const int4 ch = chunks[blockIdx.x];       // (slice, iy0, ix0, -)
     if (S && S[ch.x].done) return;
     const BatchSlice& b = sl[ch.x];
-    const int ix = ch.z + threadIdx.x;
-    if (ix >= b.nx) return;
-    float acc = fan_pixel_gather(YW + b.yoff, b.col, b.view, b.views, b.nvf, b.G, ix, ch.y,
-                                 b.nx, b.ny, b.na);
-    X[b.xoff + (long long)ch.y * b.nx + ix] = acc;
+    const int ix0 = ch.z + 2 * threadIdx.x, iy0 = ch.y;
+    if (ix0 >= b.nx) return;
+    float acc[2][2];
+    fan_block_gather<2, 2>(acc, YW + b.yoff, b.col, b.view, b.views, b.nvf, b.G, ix0, iy0,
+                           b.nx, b.ny, b.na);
+    float* xs = X + b.xoff;
+#pragma unroll
+    for (int j = 0; j < 2; j++)
+#pragma unroll
+        for (int i = 0; i < 2; i++)
+            if (iy0 + j < b.ny && ix0 + i < b.nx)
+                xs[(long long)(iy0 + j) * b.nx + ix0 + i] = acc[j][i];
 }
 
 // r = q + lam u - b (q null: r = -b) ; p = -r ; gamma = <r, r>
@@ -348,8 +356,9 @@ extern "C" int fl_batch_create(fl_plan* const* plans, int32_t n_plans, fl_batch*
         for (int r = 0; r < sl[i].na * sl[i].nv; r += kRayChunk) rays.push_back(make_int2(i, r));
     std::vector<int4> pix;
     for (int i : by_views)
-        for (int iy = 0; iy < sl[i].ny; iy++)
-            for (int ix = 0; ix < sl[i].nx; ix += kPixChunk) pix.push_back(make_int4(i, iy, ix, 0));
+        for (int iy = 0; iy < sl[i].ny; iy += 2)
+            for (int ix = 0; ix < sl[i].nx; ix += 2 * kPixChunk)
+                pix.push_back(make_int4(i, iy, ix, 0));
     std::vector<VecChunk> vec;
     for (int i = 0; i < n_plans; i++) {
         sl[i].vc0 = (int)vec.size();

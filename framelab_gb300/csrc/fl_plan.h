@@ -45,6 +45,14 @@ struct fl_plan {
     float u0, du, g0, dg;      // flat: u = u0 + ia*du ; arc: gamma = g0 + ia*dg
     float v0, dv;              // rows: v = v0 + ib*dv
     float SD;
+    // z-mirror symmetry: with the source in the volume's central plane for
+    // every view (sd_z = 0), an even nz, an even nb and z_det exactly
+    // antisymmetric (z_det[nb-1-ib] == -z_det[ib], z_det[0] < 0), the ray of
+    // row nb-1-ib is the mirror image of the ray of row ib. The matched model
+    // then defines A[(v, a, nb-1-b), (x, y, nz-1-z)] = A[(v, a, b), (x, y, z)]
+    // for b < nb/2, so one walk / one weight serves both rays.
+    int zmirror_ok;            // the geometry allows it
+    int zmirror;               // in use (FL_OPT_Z_MIRROR)
     // reusable scratch (sinogram-sized f32 for the pre-weighted adjoint input)
     float *d_work;
     size_t work_elems;

@@ -167,7 +167,39 @@ static int build_tables(fl_plan* p, const std::vector<float>& phi, const float* 
             else p->dv = (float)dv;
         }
     }
+    // z-mirror symmetry (fl_plan.h): exact comparisons, so only a geometry that
+    // is symmetric in its FP32 inputs qualifies
+    p->zmirror_ok = 0;
+    if (s.ndim == 3 && s.nz % 2 == 0 && s.nb % 2 == 0 && z_det[0] < 0.0f) {
+        bool ok = true;
+        for (int iv = 0; iv < s.nv && ok; iv++)
+            if (sd_z && sd_z[iv] != 0.0f) ok = false;
+        for (int ib = 0; ib < s.nb && ok; ib++)
+            if (z_det[s.nb - 1 - ib] != -z_det[ib]) ok = false;
+        p->zmirror_ok = ok ? 1 : 0;
+    }
+    p->zmirror = p->zmirror_ok;
     return FL_OK;
+}
+
+extern "C" int fl_plan_option(fl_plan* p, int option, int value)
+{
+    if (!p) return fl_set_error(FL_ERR_INVALID, "fl_plan_option: null plan");
+    if (option == FL_OPT_Z_MIRROR) {
+        p->zmirror = (value && p->zmirror_ok) ? 1 : 0;
+        return fl_set_error(FL_OK, "");
+    }
+    return fl_set_error(FL_ERR_INVALID, "fl_plan_option: unknown option %d", option);
+}
+
+extern "C" int fl_plan_query(const fl_plan* p, int option, int* value)
+{
+    if (!p || !value) return fl_set_error(FL_ERR_INVALID, "fl_plan_query: null argument");
+    if (option == FL_OPT_Z_MIRROR) {
+        *value = p->zmirror;
+        return fl_set_error(FL_OK, "");
+    }
+    return fl_set_error(FL_ERR_INVALID, "fl_plan_query: unknown option %d", option);
 }
 
 extern "C" int fl_plan_create(const fl_scan* scan, fl_plan** out)

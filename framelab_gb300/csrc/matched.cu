@@ -25,8 +25,11 @@ namespace {
 // Forward kernels. Block (32, 4): 32 adjacent detector columns x 4 rows of one
 // view, so a warp's rays are neighbours and their gathers share cache lines.
 // ---------------------------------------------------------------------------
-template <typename TX, typename TY>
-__global__ void __launch_bounds__(128, 16)
+// MIRROR (scans symmetric about the source plane, fl_plan::zmirror): the
+// block walks only the rows ib < nb/2 and writes each ray's z-mirrored
+// companion, row nb-1-ib, from the same walk.
+template <typename TX, typename TY, bool MIRROR>
+__global__ void __launch_bounds__(128, MIRROR ? 12 : 16)
 k_fwd_cone(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restrict__ col,
            const float* __restrict__ colr, const RowEntry* __restrict__ row,
            const int* __restrict__ vframe, int nx, int ny, int nz, int na, int nb,
@@ -37,17 +40,23 @@ k_fwd_cone(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restr
     int ia = blockIdx.x * 32 + threadIdx.x;
     int ib = blockIdx.y * 4 + threadIdx.y;
     int iv = blockIdx.z;
-    if (ia >= na || ib >= nb) return;
+    if (ia >= na || ib >= (MIRROR ? nb / 2 : nb)) return;
     ColEntry ce = col[(long long)iv * na + ia];
     RowEntry re = row[(long long)iv * nb + ib];
     const TX* x = X + (long long)vframe[iv] * nper;
-    float acc = walk<TX, true, false>(x, ce.inv_x, ce.off_x, ce.inv_y, ce.off_y, re.inv_z,
-                                      re.off_z, nx, ny, nz, nullptr);
+    float accm = 0.0f;
+    float acc = walk<TX, true, false, MIRROR>(x, ce.inv_x, ce.off_x, ce.inv_y, ce.off_y,
+                                              re.inv_z, re.off_z, nx, ny, nz, nullptr, &accm);
     float cr = ray_cr(scale, colr[(long long)iv * na + ia], re.dz2);
-    if (xscale) acc *= *xscale;
+    if (xscale) { acc *= *xscale; accm *= *xscale; }
     float out = cr * acc;
     if (cr_power == 2) out = cr * out;
     Store<TY>::st(y + ((long long)iv * nb + ib) * na + ia, out);
+    if (MIRROR) {
+        float om = cr * accm;
+        if (cr_power == 2) om = cr * om;
+        Store<TY>::st(y + ((long long)iv * nb + (nb - 1 - ib)) * na + ia, om);
+    }
 }
 
 template <typename TX, typename TY>
@@ -118,6 +127,7 @@ __global__ void k_weight(float* __restrict__ yw, const TY* __restrict__ y,
 // ---------------------------------------------------------------------------
 // Fan adjoint: one thread per (pixel, frame).
 // ---------------------------------------------------------------------------
+// Fan adjoint: one thread per 2 x 2 pixel block of one frame.
 template <typename TX>
 __global__ void __launch_bounds__(128)
 k_adj_fan(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __restrict__ col,
@@ -126,12 +136,20 @@ k_adj_fan(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __re
           const int* __restrict__ skip)
 {
     if (skip && *skip) return;
-    int ix = blockIdx.x * blockDim.x + threadIdx.x;
-    int iy = blockIdx.y;
-    int it = blockIdx.z;
-    if (ix >= nx) return;
-    float acc = fan_pixel_gather(yw, col, view, idY + it * tmp_size, Nv[it], G, ix, iy, nx, ny, na);
-    Store<TX>::st(X + (long long)it * nx * ny + (long long)iy * nx + ix, acc);
+    const int ix0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+    const int iy0 = 2 * blockIdx.y;
+    const int it = blockIdx.z;
+    if (ix0 >= nx) return;
+    float acc[2][2];
+    fan_block_gather<2, 2>(acc, yw, col, view, idY + it * tmp_size, Nv[it], G, ix0, iy0, nx,
+                           ny, na);
+    TX* xf = X + (long long)it * nx * ny;
+#pragma unroll
+    for (int j = 0; j < 2; j++)
+#pragma unroll
+        for (int i = 0; i < 2; i++)
+            if (iy0 + j < ny && ix0 + i < nx)
+                Store<TX>::st(xf + (long long)(iy0 + j) * nx + ix0 + i, acc[j][i]);
 }
 
 // ---------------------------------------------------------------------------
@@ -149,11 +167,15 @@ k_adj_fan(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __re
 // (A_z increasing in k); MODE -1: below, every such ray falls; MODE 0: the run
 // straddles the source plane (general min/max). The other orientation's rays
 // get w <= 0 from the specialised formula, as they miss the run.
-template <int MODE, int TZ>
-__device__ __forceinline__ void adj_rows(float (&acc)[TZ], int nk, int z0, float l, float h,
-                                         float e1, float e2, float s1, float s2,
-                                         const float2* __restrict__ rv,
-                                         const float* __restrict__ ycol, int na, int nb)
+// MIRROR: rows are limited to the walked half (nb here is nb/2) and every
+// weight also carries the mirrored ray (row nb-1-ib, read from ycolm - ib*na)
+// into the mirrored voxel's accumulator accm[k].
+template <int MODE, int TZ, bool MIRROR>
+__device__ __forceinline__ void adj_rows(float (&acc)[TZ], float (&accm)[TZ], int nk, int z0,
+                                         float l, float h, float e1, float e2, float s1,
+                                         float s2, const float2* __restrict__ rv,
+                                         const float* __restrict__ ycol,
+                                         const float* __restrict__ ycolm, int na, int nb)
 {
     float mn = fminf(e1, e2), mx = fmaxf(e1, e2);   // row span at plane k
 #pragma unroll
@@ -168,6 +190,7 @@ __device__ __forceinline__ void adj_rows(float (&acc)[TZ], int nk, int z0, float
         for (int ib = blo; ib <= bhi; ib++) {
             const float2 re = rv[ib];                 // (inv_z, off_z) of row ib
             const float yval = __ldg(ycol + (long long)ib * na);
+            const float ym = MIRROR ? __ldg(ycolm - (long long)ib * na) : 0.0f;
             const float az0 = fmaf(fk0, re.x, re.y);
             const float az1 = fmaf(fk1, re.x, re.y);
             float l2, h2;
@@ -175,13 +198,17 @@ __device__ __forceinline__ void adj_rows(float (&acc)[TZ], int nk, int z0, float
             else if (MODE < 0) { l2 = fmaxf(l, az1); h2 = fminf(h, az0); }
             else { l2 = fmaxf(l, fminf(az0, az1)); h2 = fminf(h, fmaxf(az0, az1)); }
             // w <= 0 (the ray misses voxel k) adds exactly 0 for finite y
-            acc[k] = fmaf(fmaxf(h2 - l2, 0.0f), yval, acc[k]);
+            const float w = fmaxf(h2 - l2, 0.0f);
+            acc[k] = fmaf(w, yval, acc[k]);
+            if (MIRROR) accm[k] = fmaf(w, ym, accm[k]);
         }
     }
 }
 
-template <typename TX, int TZ>
-__global__ void __launch_bounds__(128, 8)
+// MIRROR: the runs cover the lower half z < nz/2 only (the walked rows'
+// rays never reach the upper half); each thread also writes the mirrored run.
+template <typename TX, int TZ, bool MIRROR>
+__global__ void __launch_bounds__(128, MIRROR ? 6 : 8)
 k_adj_cone(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __restrict__ col,
            const float2* __restrict__ rowz, const ViewEntry* __restrict__ view,
            const int* __restrict__ idY, const int* __restrict__ Nv, int tmp_size, DetGrid G,
@@ -193,11 +220,13 @@ k_adj_cone(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __r
     const int iy = blockIdx.y * 4 + threadIdx.y;
     const int zr = blockIdx.z % zruns, it = blockIdx.z / zruns;
     const int z0 = zr * TZ;
-    const int nk = min(TZ, nz - z0);          // voxels of this run inside the volume
+    const int nzw = MIRROR ? nz / 2 : nz;      // voxels gathered directly
+    const int nbw = MIRROR ? nb / 2 : nb;      // rows evaluated
+    const int nk = min(TZ, nzw - z0);          // voxels of this run inside that range
     if (ix >= nx || iy >= ny) return;
-    float acc[TZ];
+    float acc[TZ], accm[TZ];
 #pragma unroll
-    for (int k = 0; k < TZ; k++) acc[k] = 0.0f;
+    for (int k = 0; k < TZ; k++) { acc[k] = 0.0f; accm[k] = 0.0f; }
     const float x0 = (float)(ix - nx / 2), y0 = (float)(iy - ny / 2);
     const float fx0 = (float)ix, fx1 = (float)(ix + 1), fy0 = (float)iy, fy1 = (float)(iy + 1);
     const float inv_dv = 1.0f / G.dv;
@@ -232,15 +261,22 @@ k_adj_cone(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __r
             const float s1 = dz * r1 * inv_dv, s2 = dz * r2 * inv_dv;
             const float e1 = (zr0 * r1 - G.v0) * inv_dv, e2 = (zr0 * r2 - G.v0) * inv_dv;
             const float* ycol = yv + ia;
-            if (mode > 0) adj_rows<1, TZ>(acc, nk, z0, l, h, e1, e2, s1, s2, rv, ycol, na, nb);
-            else if (mode < 0) adj_rows<-1, TZ>(acc, nk, z0, l, h, e1, e2, s1, s2, rv, ycol, na, nb);
-            else adj_rows<0, TZ>(acc, nk, z0, l, h, e1, e2, s1, s2, rv, ycol, na, nb);
+            const float* ycolm = yv + (long long)(nb - 1) * na + ia;
+            if (mode > 0)
+                adj_rows<1, TZ, MIRROR>(acc, accm, nk, z0, l, h, e1, e2, s1, s2, rv, ycol, ycolm, na, nbw);
+            else if (mode < 0)
+                adj_rows<-1, TZ, MIRROR>(acc, accm, nk, z0, l, h, e1, e2, s1, s2, rv, ycol, ycolm, na, nbw);
+            else
+                adj_rows<0, TZ, MIRROR>(acc, accm, nk, z0, l, h, e1, e2, s1, s2, rv, ycol, ycolm, na, nbw);
         }
     }
     const long long base = (long long)it * nx * ny * nz + (long long)iy * nx + ix;
 #pragma unroll
     for (int k = 0; k < TZ; k++)
-        if (k < nk) Store<TX>::st(X + base + (long long)(z0 + k) * nx * ny, acc[k]);
+        if (k < nk) {
+            Store<TX>::st(X + base + (long long)(z0 + k) * nx * ny, acc[k]);
+            if (MIRROR) Store<TX>::st(X + base + (long long)(nz - 1 - z0 - k) * nx * ny, accm[k]);
+        }
 }
 
 DetGrid det_grid(const fl_plan* p)
@@ -256,9 +292,14 @@ void launch_fwd(fl_plan* p, const void* x, void* y, int cr_power, const int* ski
                 const float* xscale, cudaStream_t st)
 {
     const fl_scan& s = p->s;
-    if (s.ndim == 3) {
+    if (s.ndim == 3 && p->zmirror) {
+        dim3 grid(fl_div_up(s.na, 32), fl_div_up(s.nb / 2, 4), s.nv);
+        k_fwd_cone<TX, TY, true><<<grid, dim3(32, 4), 0, st>>>(
+            (const TX*)x, (TY*)y, p->d_col, p->d_colr, p->d_row, p->d_view_frame, s.nx, s.ny,
+            s.nz, s.na, s.nb, p->n_vox_frame, s.scale, cr_power, skip, xscale);
+    } else if (s.ndim == 3) {
         dim3 grid(fl_div_up(s.na, 32), fl_div_up(s.nb, 4), s.nv);
-        k_fwd_cone<TX, TY><<<grid, dim3(32, 4), 0, st>>>(
+        k_fwd_cone<TX, TY, false><<<grid, dim3(32, 4), 0, st>>>(
             (const TX*)x, (TY*)y, p->d_col, p->d_colr, p->d_row, p->d_view_frame, s.nx, s.ny,
             s.nz, s.na, s.nb, p->n_vox_frame, s.scale, cr_power, skip, xscale);
     } else {
@@ -285,13 +326,19 @@ void launch_adj(fl_plan* p, const float* yw, void* x, const int* skip, cudaStrea
     DetGrid G = det_grid(p);
     if (s.ndim == 3) {
         constexpr int TZ = 8;
-        int zruns = (s.nz + TZ - 1) / TZ;
+        const int nzw = p->zmirror ? s.nz / 2 : s.nz;
+        int zruns = (nzw + TZ - 1) / TZ;
         dim3 grid(fl_div_up(s.nx, 32), fl_div_up(s.ny, 4), (unsigned)zruns * s.nt);
-        k_adj_cone<TX, TZ><<<grid, dim3(32, 4), 0, st>>>(
-            (TX*)x, yw, p->d_col, p->d_rowz, p->d_view, p->d_idY, p->d_Nv, p->tmp_size, G, s.nx,
-            s.ny, s.nz, s.na, s.nb, s.dz, zruns, skip);
+        if (p->zmirror)
+            k_adj_cone<TX, TZ, true><<<grid, dim3(32, 4), 0, st>>>(
+                (TX*)x, yw, p->d_col, p->d_rowz, p->d_view, p->d_idY, p->d_Nv, p->tmp_size, G,
+                s.nx, s.ny, s.nz, s.na, s.nb, s.dz, zruns, skip);
+        else
+            k_adj_cone<TX, TZ, false><<<grid, dim3(32, 4), 0, st>>>(
+                (TX*)x, yw, p->d_col, p->d_rowz, p->d_view, p->d_idY, p->d_Nv, p->tmp_size, G,
+                s.nx, s.ny, s.nz, s.na, s.nb, s.dz, zruns, skip);
     } else {
-        dim3 grid(fl_div_up(s.nx, 128), s.ny, s.nt);
+        dim3 grid(fl_div_up(s.nx, 2 * 128), (s.ny + 1) / 2, s.nt);
         k_adj_fan<TX><<<grid, 128, 0, st>>>((TX*)x, yw, p->d_col, p->d_view, p->d_idY,
                                              p->d_Nv, p->tmp_size, G, s.nx, s.ny, s.na, skip);
     }

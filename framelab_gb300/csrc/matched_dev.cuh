@@ -35,10 +35,13 @@ __device__ __forceinline__ int start_slab(float a, float inv, float off, int n)
 // apart for any table fl_plan_create accepts), and the loop leaves as soon as
 // the crossing reaches the exit (or is NaN); the step budget nx+ny+nz+4 is a
 // second, independent bound.
-template <typename TX, bool THREE, bool COUNT>
+// MIRROR: also gathers the z-mirrored voxel (ix, iy, nz-1-iz) of every voxel
+// visited, with the same segment length, into *accm -- the companion ray of a
+// scan that is symmetric about the source plane (fl_plan::zmirror).
+template <typename TX, bool THREE, bool COUNT, bool MIRROR = false>
 __device__ __forceinline__ float walk(const TX* __restrict__ x, float inv_x, float off_x,
                                       float inv_y, float off_y, float inv_z, float off_z,
-                                      int nx, int ny, int nz, int* nseg)
+                                      int nx, int ny, int nz, int* nseg, float* accm = nullptr)
 {
     float ax0 = fmaf(0.0f, inv_x, off_x), ax1 = fmaf((float)nx, inv_x, off_x);
     float ay0 = fmaf(0.0f, inv_y, off_y), ay1 = fmaf((float)ny, inv_y, off_y);
@@ -49,11 +52,17 @@ __device__ __forceinline__ float walk(const TX* __restrict__ x, float inv_x, flo
         a_in = fmaxf(a_in, fminf(az0, az1));
         a_out = fminf(a_out, fmaxf(az0, az1));
     }
-    if (!(a_in < a_out)) { if (COUNT) *nseg = 0; return 0.0f; }
+    if (!(a_in < a_out)) {
+        if (COUNT) *nseg = 0;
+        if (MIRROR) *accm = 0.0f;
+        return 0.0f;
+    }
     const int jx = start_slab(a_in, inv_x, off_x, nx);
     const int jy = start_slab(a_in, inv_y, off_y, ny);
     const int jz = THREE ? start_slab(a_in, inv_z, off_z, nz) : 0;
     int v = (jz * ny + jy) * nx + jx;              // < 2^31 (checked at plan creation)
+    // mirrored voxel index = v + m; m changes only when the walk steps in z
+    int m = MIRROR ? (nz - 1 - 2 * jz) * (nx * ny) : 0;
     const bool px = inv_x > 0.0f, py = inv_y > 0.0f, pz = inv_z > 0.0f;
     float pax = (float)(px ? jx + 1 : jx);
     float pay = (float)(py ? jy + 1 : jy);
@@ -63,11 +72,12 @@ __device__ __forceinline__ float walk(const TX* __restrict__ x, float inv_x, flo
     float nAx = fmaf(pax, inv_x, off_x);
     float nAy = fmaf(pay, inv_y, off_y);
     float nAz = THREE ? fmaf(paz, inv_z, off_z) : 3.0e38f;
-    float cur = a_in, acc = 0.0f;
+    float cur = a_in, acc = 0.0f, am = 0.0f;
     int cnt = 0;
     // the gather of the next voxel is issued as soon as its index is known and
     // consumed one step later, so its latency overlaps the next step's compares
     float xv = COUNT ? 0.0f : ldv(x + v);
+    float xm = MIRROR ? ldv(x + v + m) : 0.0f;
     const int budget = nx + ny + (THREE ? nz : 0) + 4;
     for (int it = 0; it < budget; it += 4) {
 #pragma unroll
@@ -75,22 +85,29 @@ __device__ __forceinline__ float walk(const TX* __restrict__ x, float inv_x, flo
             const float nxt = THREE ? fminf(fminf(nAx, nAy), nAz) : fminf(nAx, nAy);
             const float seg = nxt - cur;
             const bool cont = nxt < a_out;          // false at the exit (and for NaN)
-            float xn = 0.0f;
+            float xn = 0.0f, xmn = 0.0f;
             if (cont) {
                 if (nAx == nxt) { pax += stx; v += dvx; nAx = fmaf(pax, inv_x, off_x); }
                 if (nAy == nxt) { pay += sty; v += dvy; nAy = fmaf(pay, inv_y, off_y); }
-                if (THREE && nAz == nxt) { paz += stz; v += dvz; nAz = fmaf(paz, inv_z, off_z); }
+                if (THREE && nAz == nxt) {
+                    paz += stz; v += dvz; nAz = fmaf(paz, inv_z, off_z);
+                    if (MIRROR) m -= 2 * dvz;
+                }
                 if (!COUNT) xn = ldv(x + v);        // v is inside the volume here
+                if (MIRROR) xmn = ldv(x + v + m);   // and so is its mirror
             }
             if (COUNT) cnt += (seg > 0.0f);
             else acc = fmaf(seg, xv, acc);
+            if (MIRROR) am = fmaf(seg, xm, am);
             if (!cont) goto done;
             xv = xn;
+            xm = xmn;
             cur = nxt;
         }
     }
 done:
     if (COUNT) *nseg = cnt;
+    if (MIRROR) *accm = am;
     return acc;
 }
 
@@ -137,37 +154,59 @@ __device__ __forceinline__ void column_window(const DetGrid& G, float c, float s
     lo = (int)f0; hi = (int)f1;                   // empty when lo > hi
 }
 
-// Fan adjoint of one pixel (ix, iy): sum over the views `views[0..nvf)` of
-// w_rV * yw_r for every ray of the view whose column window covers the pixel,
-// w_rV evaluated from the same crossing table as the forward walk.
-__device__ __forceinline__ float fan_pixel_gather(const float* __restrict__ yw,
-                                                  const ColEntry* __restrict__ col,
-                                                  const ViewEntry* __restrict__ view,
-                                                  const int* __restrict__ views, int nvf,
-                                                  const DetGrid& G, int ix, int iy, int nx,
-                                                  int ny, int na)
+// Fan adjoint of a PX x PY block of pixels with lower corner (ix0, iy0): for
+// every view of `views[0..nvf)` and every ray whose column window covers the
+// block, w_rV * yw_r is added to each pixel the ray crosses, w_rV evaluated
+// from the same crossing table as the forward walk. A pixel's sum runs over
+// the views in order and the columns in increasing order, and only rays with
+// w > 0 add to it, so each pixel's result does not depend on the block shape:
+// the block's window contains every pixel's own window (the corners' column
+// shadow with 0.02 columns of slack is far wider than the FP32 error of w).
+template <int PX, int PY>
+__device__ __forceinline__ void fan_block_gather(float (&acc)[PY][PX],
+                                                 const float* __restrict__ yw,
+                                                 const ColEntry* __restrict__ col,
+                                                 const ViewEntry* __restrict__ view,
+                                                 const int* __restrict__ views, int nvf,
+                                                 const DetGrid& G, int ix0, int iy0, int nx,
+                                                 int ny, int na)
 {
-    float x0 = (float)(ix - nx / 2), y0 = (float)(iy - ny / 2);
-    float fx0 = (float)ix, fx1 = (float)(ix + 1), fy0 = (float)iy, fy1 = (float)(iy + 1);
-    float acc = 0.0f;
-    for (int j = 0; j < nvf; j++) {
-        int iv = views[j];
-        ViewEntry ve = view[iv];
+    const float x0 = (float)(ix0 - nx / 2), y0 = (float)(iy0 - ny / 2);
+    float fx[PX + 1], fy[PY + 1];
+#pragma unroll
+    for (int i = 0; i <= PX; i++) fx[i] = (float)(ix0 + i);
+#pragma unroll
+    for (int j = 0; j <= PY; j++) fy[j] = (float)(iy0 + j);
+#pragma unroll
+    for (int j = 0; j < PY; j++)
+#pragma unroll
+        for (int i = 0; i < PX; i++) acc[j][i] = 0.0f;
+    for (int jv = 0; jv < nvf; jv++) {
+        const int iv = views[jv];
+        const ViewEntry ve = view[iv];
         int lo, hi; float dmin, dmax;
-        column_window(G, ve.c, ve.s, x0, y0, 1.0f, 1.0f, na, lo, hi, dmin, dmax);
+        column_window(G, ve.c, ve.s, x0, y0, (float)PX, (float)PY, na, lo, hi, dmin, dmax);
         const ColEntry* cv = col + (long long)iv * na;
         const float* yv = yw + (long long)iv * na;
         for (int ia = lo; ia <= hi; ia++) {
-            ColEntry ce = cv[ia];
-            float ax0 = fmaf(fx0, ce.inv_x, ce.off_x), ax1 = fmaf(fx1, ce.inv_x, ce.off_x);
-            float ay0 = fmaf(fy0, ce.inv_y, ce.off_y), ay1 = fmaf(fy1, ce.inv_y, ce.off_y);
-            float l = fmaxf(fminf(ax0, ax1), fminf(ay0, ay1));
-            float h = fminf(fmaxf(ax0, ax1), fmaxf(ay0, ay1));
-            float w = h - l;
-            if (w > 0.0f) acc = fmaf(w, __ldg(yv + ia), acc);
+            const ColEntry ce = cv[ia];
+            const float yval = __ldg(yv + ia);
+            float ax[PX + 1], ay[PY + 1];
+#pragma unroll
+            for (int i = 0; i <= PX; i++) ax[i] = fmaf(fx[i], ce.inv_x, ce.off_x);
+#pragma unroll
+            for (int j = 0; j <= PY; j++) ay[j] = fmaf(fy[j], ce.inv_y, ce.off_y);
+#pragma unroll
+            for (int j = 0; j < PY; j++)
+#pragma unroll
+                for (int i = 0; i < PX; i++) {
+                    const float l = fmaxf(fminf(ax[i], ax[i + 1]), fminf(ay[j], ay[j + 1]));
+                    const float h = fminf(fmaxf(ax[i], ax[i + 1]), fmaxf(ay[j], ay[j + 1]));
+                    const float w = h - l;
+                    if (w > 0.0f) acc[j][i] = fmaf(w, yval, acc[j][i]);
+                }
         }
     }
-    return acc;
 }
 
 }  // namespace

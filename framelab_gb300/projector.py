@@ -100,6 +100,18 @@ class Plan:
             self._h = None
 
     @property
+    def z_mirror(self) -> bool:
+        """Whether the matched pair uses the source-plane mirror symmetry
+        (FL_OPT_Z_MIRROR; on by default where the scan allows it)."""
+        v = C.c_int()
+        _lib.check(self._L.fl_plan_query(self._h, _lib.OPT_Z_MIRROR, C.byref(v)))
+        return bool(v.value)
+
+    @z_mirror.setter
+    def z_mirror(self, on: bool):
+        _lib.check(self._L.fl_plan_option(self._h, _lib.OPT_Z_MIRROR, int(bool(on))))
+
+    @property
     def handle(self):
         return self._h
 

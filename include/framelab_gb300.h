@@ -173,6 +173,17 @@ void fl_plan_destroy(fl_plan *plan);
 /* Number of voxels (all frames) and rays of the plan. */
 int fl_plan_sizes(const fl_plan *plan, int64_t *n_vox, int64_t *n_rays);
 
+/* Plan options.
+ * FL_OPT_Z_MIRROR: on by default for a cone scan that is symmetric about the
+ *   source plane (every sd_z = 0, nz and nb even, z_det[nb-1-ib] == -z_det[ib]
+ *   exactly, z_det[0] < 0). The matched pair then walks / weighs only the
+ *   rows ib < nb/2 and gives row nb-1-ib the mirrored values, so both
+ *   kernels do about half the work; the matrix stays exactly transposed.
+ *   Setting 0 selects the general kernels; 1 re-enables it where allowed. */
+enum { FL_OPT_Z_MIRROR = 1 };
+int fl_plan_option(fl_plan *plan, int option, int value);
+int fl_plan_query(const fl_plan *plan, int option, int *value);
+
 /* y = A x on `stream`. x: n_vox elements, y: n_rays elements, device memory. */
 int fl_forward(fl_plan *plan, int model, const void *x, int x_dtype, void *y, int y_dtype,
                void *stream);

@@ -457,3 +457,47 @@ def test_fb_ref_known_answer_disc():
     p, x, ex = fan_disc_beam()
     y = _host(_plan(p).forward(_dev(x), model="fb_ref"))
     assert rel(y, ex) < 5e-3
+
+
+# --------------------------------------------------------------------------
+# source-plane mirror symmetry of the matched pair (FL_OPT_Z_MIRROR)
+# --------------------------------------------------------------------------
+def test_z_mirror_is_detected_only_for_symmetric_scans():
+    assert _plan(_cone_small("circle")).z_mirror
+    assert not _plan(_cone_small("helix")).z_mirror
+    odd = G.cone_para_mm(32, 8, 48, 39, det_pitch_mm=8.0, SO_mm=600.0, SD_mm=1200.0,
+                         voxel_mm=8.0)
+    P = _plan(odd)
+    assert not P.z_mirror
+    P.z_mirror = True                  # not allowed for this geometry: stays off
+    assert not P.z_mirror
+
+
+def test_z_mirror_agrees_with_general_kernels_and_is_exact():
+    torch = _torch()
+    p = _cone_small("circle")
+    n, nb = int(p["nx"]), len(p["z_det"])
+    P = _plan(p)
+    x = PH.ellipsoids_3d(n, seed=9).reshape(-1)
+    rng = np.random.default_rng(3)
+    r = rng.standard_normal(P.n_rays).astype(np.float32)
+    ym, xm = _host(P.forward(_dev(x))), _host(P.adjoint(_dev(r)))
+    P.z_mirror = False
+    yg, xg = _host(P.forward(_dev(x))), _host(P.adjoint(_dev(r)))
+    # the two matrices differ only by the FP32 rounding of the mirrored tables;
+    # the backprojection of a random (zero-mean) sinogram cancels, so its
+    # relative difference is larger (the same bound as against FP64 above)
+    assert _rel(ym, yg) < 2e-6 and _rel(xm, xg) < 2e-5, (_rel(ym, yg), _rel(xm, xg))
+    P.z_mirror = True
+    # by construction: the mirrored rows of A x are the direct rows of A flip_z(x)
+    xf = x.reshape(n, n, n)[::-1].reshape(-1).copy()
+    yf = _host(P.forward(_dev(xf))).reshape(-1, nb, P.na)
+    ym3 = ym.reshape(-1, nb, P.na)
+    assert np.array_equal(ym3[:, nb // 2:, :], yf[:, :nb // 2, :][:, ::-1, :])
+    # and the adjoint stays the exact transpose
+    lhs = np.dot(ym.astype(np.float64), r.astype(np.float64))
+    rhs = np.dot(x.astype(np.float64), xm.astype(np.float64))
+    assert abs(lhs - rhs) / abs(lhs) < 1e-5
+    # half-precision storage goes through the same mirrored kernels
+    y16 = _host(P.forward(_dev(x, torch.float16)))
+    assert _rel(y16, ym) < 2e-3
