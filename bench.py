@@ -79,7 +79,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="cone512", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--only", default="", help="comma list of legs: mixed,plain,e2e,kernels,seq")
+    ap.add_argument("--only", default="",
+                    help="comma list of legs: mixed,plain,e2e,kernels,seq,grad")
     return ap.parse_args()
 
 
@@ -343,7 +344,8 @@ class Ctx:
         self.dev = torch.device("cuda", local)
         self.stream = torch.cuda.current_stream()
         self.K, self.W = a.steps, a.warmup
-        self.legs = set(a.only.split(",")) if a.only else {"mixed", "plain", "e2e", "kernels", "seq"}
+        self.legs = (set(a.only.split(",")) if a.only else
+                     {"mixed", "plain", "e2e", "kernels", "seq", "grad"})
 
     def barrier(self):
         if self.world > 1:
@@ -517,6 +519,18 @@ def run_single(ctx, name, w, p):
             y16 = P.forward(x_true.half())
             detail["fp16_storage_vs_fp32_rel_l2"] = ctx.rel(y16, y32)
             del xr, yr, y32, y16
+    if "grad" in ctx.legs and w["kind"] == "cone":
+        # gradient of 1/2 |A x - b|^2 through the autograd binding (backward =
+        # the exact-transpose backprojector) against central differences on 64
+        # random voxels, h = 1e-3, at the CGLS iterate
+        from framelab_gb300.autograd import fd_gradcheck
+        f = P.forward(x_true)
+        t0 = time.perf_counter()
+        err, _ = fd_gradcheck(P, u_g.reshape(-1), f, n_vox=64, h=1e-3)
+        detail["gradcheck_max_rel_err"] = err
+        detail["gradcheck_voxels"] = 64
+        detail["gradcheck_s"] = time.perf_counter() - t0
+        del f
     return dict(value=world * K / t_g, t_step=t_g / K, e2e=e2e, roofline=roofline,
                 launches=5 * K + 1, detail=detail, clocks=clocks.summary(), unit="iter/s")
 

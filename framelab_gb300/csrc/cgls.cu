@@ -290,11 +290,14 @@ struct fl_cgls {
     const float* cap_u;         // pointers baked into the captured graph
     float* cap_uw;
     float *hb, *hu;             // device copies for the host-buffer entry point
+    int fold;                   // fused forms on a z-mirror plan: vectors kept z-folded
+    float *bf, *uf;             // folded copies of b and u
 };
 
 static void cgls_free(fl_cgls* c)
 {
-    void* ptrs[] = {c->r, c->p, c->q, c->tmp, c->p16, c->S, c->partials, c->hist, c->hb, c->hu};
+    void* ptrs[] = {c->r,    c->p,        c->q,    c->tmp, c->p16, c->S,
+                    c->partials, c->hist, c->hb, c->hu,  c->bf,  c->uf};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     if (c->exec) cudaGraphExecDestroy(c->exec);
@@ -324,6 +327,11 @@ extern "C" int fl_cgls_create(fl_plan* plan, int mode, fl_cgls** out)
     M((void**)&c->r, c->n * 4); M((void**)&c->p, c->n * 4); M((void**)&c->q, c->n * 4);
     M((void**)&c->tmp, c->nr * 4);
     if (mode == FL_CGLS_MIXED) M((void**)&c->p16, c->n * 2);
+    // the fused forms keep every vector z-folded on a z-mirror plan (the
+    // algebra is elementwise, so only b in and u out change layout); whether
+    // the plan uses the mirror is read again at every solve
+    c->fold = (plan->zmirror && mode != FL_CGLS_PLAIN) ? 1 : 0;
+    if (c->fold) { M((void**)&c->bf, c->n * 4); M((void**)&c->uf, c->n * 4); }
     M((void**)&c->S, sizeof(CgScalars));
     M((void**)&c->partials, sizeof(double) * c->grid);
     M((void**)&c->hist, sizeof(double) * c->hist_cap);
@@ -343,13 +351,17 @@ extern "C" void fl_cgls_destroy(fl_cgls* c)
     delete c;
 }
 
-// q = (A^T A + lam I) x with FP32 storage (matched model)
+// q = (A^T A + lam I) x with FP32 storage (matched model); x and q in the
+// workspace's vector layout
 static int normal_apply(fl_cgls* c, const float* x, float* q, float lam, cudaStream_t s)
 {
     fl_plan* P = c->plan;
+    const int lay = c->fold ? FL_LAY_X_FOLDED : 0;
     int st;
-    if ((st = fl_matched_forward(P, x, FL_F32, c->tmp, FL_F32, 2, nullptr, nullptr, s))) return st;
-    if ((st = fl_matched_adjoint_w(P, c->tmp, q, FL_F32, nullptr, s))) return st;
+    if ((st = fl_matched_forward(P, x, FL_F32, c->tmp, FL_F32, 2, nullptr, nullptr,
+                                 lay | FL_LAY_Y_ADJ, s)))
+        return st;
+    if ((st = fl_matched_adjoint_w(P, c->tmp, q, FL_F32, nullptr, lay, s))) return st;
     if (lam != 0.0f) {
         k_axpby<<<c->grid, kThreads, 0, s>>>(q, x, lam, 1.0f, c->n);
         if ((st = fl_check_launch("normal_apply"))) return st;
@@ -365,8 +377,10 @@ extern "C" int fl_normal_apply(fl_plan* plan, const float* x, float* q, float la
     float* w;
     if ((st = fl_plan_work(plan, &w))) return st;
     cudaStream_t s = (cudaStream_t)stream;
-    if ((st = fl_matched_forward(plan, x, FL_F32, w, FL_F32, 2, nullptr, nullptr, s))) return st;
-    if ((st = fl_matched_adjoint_w(plan, w, q, FL_F32, nullptr, s))) return st;
+    if ((st = fl_matched_forward(plan, x, FL_F32, w, FL_F32, 2, nullptr, nullptr, FL_LAY_Y_ADJ,
+                                 s)))
+        return st;
+    if ((st = fl_matched_adjoint_w(plan, w, q, FL_F32, nullptr, 0, s))) return st;
     if (lam != 0.0f) {
         k_axpby<<<grid_for(plan->n_vox), kThreads, 0, s>>>(q, x, lam, 1.0f, plan->n_vox);
         return fl_check_launch("fl_normal_apply");
@@ -429,13 +443,16 @@ static int mixed_iteration(fl_cgls* c, float* u, cudaStream_t s)
 {
     fl_plan* P = c->plan;
     CgScalars* S = c->S;
+    const int lay = c->fold ? FL_LAY_X_FOLDED : 0;
     int st;
     if (c->p16)
-        st = fl_matched_forward(P, c->p16, FL_F16, c->tmp, FL_F32, 2, &S->done, &S->p_unscale, s);
+        st = fl_matched_forward(P, c->p16, FL_F16, c->tmp, FL_F32, 2, &S->done, &S->p_unscale,
+                                lay | FL_LAY_Y_ADJ, s);
     else
-        st = fl_matched_forward(P, c->p, FL_F32, c->tmp, FL_F32, 2, &S->done, nullptr, s);
+        st = fl_matched_forward(P, c->p, FL_F32, c->tmp, FL_F32, 2, &S->done, nullptr,
+                                lay | FL_LAY_Y_ADJ, s);
     if (st) return st;
-    if ((st = fl_matched_adjoint_w(P, c->tmp, c->q, FL_F32, &S->done, s))) return st;
+    if ((st = fl_matched_adjoint_w(P, c->tmp, c->q, FL_F32, &S->done, lay, s))) return st;
     k_cg_pq<<<c->grid, kThreads, 0, s>>>(c->p, c->q, c->n, S, c->partials);
     k_cg_update<<<c->grid, kThreads, 0, s>>>(u, c->r, c->p, c->q, c->n, S, c->partials, c->hist,
                                              c->hist_cap);
@@ -448,26 +465,45 @@ static int solve_mixed(fl_cgls* c, const float* b, float* u, float lam, int iter
 {
     cudaStream_t s = c->cs;
     int st;
+    // layout of the workspace vectors follows the plan's current mirror option
+    const int fold = c->plan->zmirror ? 1 : 0;
+    if (fold && !c->bf) {
+        FL_CUDA(cudaMalloc((void**)&c->bf, c->n * 4));
+        FL_CUDA(cudaMalloc((void**)&c->uf, c->n * 4));
+    }
+    if (fold != c->fold) { c->fold = fold; c->captured = false; }
     FL_CUDA(cudaEventRecord(c->ev0, us));
     FL_CUDA(cudaStreamWaitEvent(s, c->ev0, 0));
     CgScalars init;
     std::memset(&init, 0, sizeof init);
     init.tol = tol; init.lam = lam;
     FL_CUDA(cudaMemcpyAsync(c->S, &init, sizeof init, cudaMemcpyHostToDevice, s));
+    // the user's b and u (standard layout) or their z-folded copies
+    const float* bb = b;
+    float* uu = u;
+    if (c->fold) {
+        if ((st = fl_matched_fold(c->plan, b, c->bf, FL_F32, 0, s))) return st;
+        if (flags & FL_CGLS_ZERO_START)
+            FL_CUDA(cudaMemsetAsync(c->uf, 0, c->n * 4, s));
+        else if ((st = fl_matched_fold(c->plan, u, c->uf, FL_F32, 0, s)))
+            return st;
+        bb = c->bf;
+        uu = c->uf;
+    }
     const float* q0 = nullptr;
     if (!(flags & FL_CGLS_ZERO_START)) {
-        if ((st = normal_apply(c, u, c->q, lam, s))) return st;
+        if ((st = normal_apply(c, uu, c->q, lam, s))) return st;
         q0 = c->q;
     }
-    k_cg_init<<<c->grid, kThreads, 0, s>>>(b, q0, c->r, c->p, c->n, c->S, c->partials);
+    k_cg_init<<<c->grid, kThreads, 0, s>>>(bb, q0, c->r, c->p, c->n, c->S, c->partials);
     if (c->p16) k_cg_p16<<<c->grid, kThreads, 0, s>>>(c->p, c->p16, c->n, c->S);
     if ((st = fl_check_launch("cgls mixed init"))) return st;
 
-    if (!c->captured || c->cap_uw != u) {
+    if (!c->captured || c->cap_uw != uu) {
         if (c->exec) { cudaGraphExecDestroy(c->exec); c->exec = nullptr; }
         cudaGraph_t g;
         FL_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-        int cst = mixed_iteration(c, u, s);
+        int cst = mixed_iteration(c, uu, s);
         cudaError_t e = cudaStreamEndCapture(s, &g);
         if (cst) return cst;
         FL_CUDA(e);
@@ -475,16 +511,17 @@ static int solve_mixed(fl_cgls* c, const float* b, float* u, float lam, int iter
         cudaGraphDestroy(g);
         FL_CUDA(e);
         c->captured = true;
-        c->cap_uw = u;
+        c->cap_uw = uu;
     }
     for (int it = 0; it < iters; it++) {
         FL_CUDA(cudaGraphLaunch(c->exec, s));
         if (c->p16 && refresh > 0 && (it + 1) % refresh == 0 && it + 1 < iters) {
-            if ((st = normal_apply(c, u, c->q, lam, s))) return st;
-            k_cg_refresh<<<c->grid, kThreads, 0, s>>>(b, c->q, c->r, c->n, c->S, c->partials);
+            if ((st = normal_apply(c, uu, c->q, lam, s))) return st;
+            k_cg_refresh<<<c->grid, kThreads, 0, s>>>(bb, c->q, c->r, c->n, c->S, c->partials);
             if ((st = fl_check_launch("cgls refresh"))) return st;
         }
     }
+    if (c->fold && (st = fl_matched_fold(c->plan, c->uf, u, FL_F32, 1, s))) return st;
     CgScalars fin;
     FL_CUDA(cudaMemcpyAsync(&fin, c->S, sizeof fin, cudaMemcpyDeviceToHost, s));
     std::vector<double> h(c->hist_cap);

@@ -28,20 +28,46 @@ __device__ __forceinline__ float fabs_ref(float a) { return fabsf(a); }
 // arithmetic is always f32.
 // ---------------------------------------------------------------------------
 template <typename T> struct Store;
+// ld2/st2: the two adjacent elements p[0], p[1] (p 2-element aligned) as one
+// access -- a voxel and its mirror in the z-folded layout (fl_plan.h).
 template <> struct Store<float> {
     static __device__ __forceinline__ float ld(const float* p) { return __ldg(p); }
     static __device__ __forceinline__ float ld_plain(const float* p) { return *p; }
     static __device__ __forceinline__ void st(float* p, float v) { *p = v; }
+    static __device__ __forceinline__ float2 ld2(const float* p)
+    {
+        return __ldg(reinterpret_cast<const float2*>(p));
+    }
+    static __device__ __forceinline__ void st2(float* p, float a, float b)
+    {
+        *reinterpret_cast<float2*>(p) = make_float2(a, b);
+    }
 };
 template <> struct Store<__half> {
     static __device__ __forceinline__ float ld(const __half* p) { return __half2float(__ldg(p)); }
     static __device__ __forceinline__ float ld_plain(const __half* p) { return __half2float(*p); }
     static __device__ __forceinline__ void st(__half* p, float v) { *p = __float2half_rn(v); }
+    static __device__ __forceinline__ float2 ld2(const __half* p)
+    {
+        return __half22float2(__ldg(reinterpret_cast<const __half2*>(p)));
+    }
+    static __device__ __forceinline__ void st2(__half* p, float a, float b)
+    {
+        *reinterpret_cast<__half2*>(p) = __floats2half2_rn(a, b);
+    }
 };
 template <> struct Store<__nv_bfloat16> {
     static __device__ __forceinline__ float ld(const __nv_bfloat16* p) { return __bfloat162float(__ldg(p)); }
     static __device__ __forceinline__ float ld_plain(const __nv_bfloat16* p) { return __bfloat162float(*p); }
     static __device__ __forceinline__ void st(__nv_bfloat16* p, float v) { *p = __float2bfloat16_rn(v); }
+    static __device__ __forceinline__ float2 ld2(const __nv_bfloat16* p)
+    {
+        return __bfloat1622float2(__ldg(reinterpret_cast<const __nv_bfloat162*>(p)));
+    }
+    static __device__ __forceinline__ void st2(__nv_bfloat16* p, float a, float b)
+    {
+        *reinterpret_cast<__nv_bfloat162*>(p) = __floats2bfloat162_rn(a, b);
+    }
 };
 
 // ---------------------------------------------------------------------------

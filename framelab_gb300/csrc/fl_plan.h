@@ -53,9 +53,23 @@ struct fl_plan {
     // for b < nb/2, so one walk / one weight serves both rays.
     int zmirror_ok;            // the geometry allows it
     int zmirror;               // in use (FL_OPT_Z_MIRROR)
-    // reusable scratch (sinogram-sized f32 for the pre-weighted adjoint input)
+    // reusable scratch: sinogram-sized f32 for the pre-weighted adjoint input,
+    // volume-sized for the z-folded copy of a forward input
     float *d_work;
     size_t work_elems;
+    void *d_vwork;
+    size_t vwork_bytes;
+};
+
+// Layouts of the matched launchers' operands. For a z-mirror plan the
+// z-folded volume stores, per frame, the pairs (voxel (ix, iy, iz),
+// voxel (ix, iy, nz-1-iz)) for iz < nz/2 at pair index (iz*ny + iy)*nx + ix;
+// the adjoint input (pre-weighted sinogram) is always folded the same way:
+// pairs (row ib, row nb-1-ib) for ib < nb/2 at pair index (iv*nb/2 + ib)*na + ia.
+// For other plans both layouts are the standard ones.
+enum {
+    FL_LAY_X_FOLDED = 1,   // the volume operand is z-folded
+    FL_LAY_Y_ADJ = 2       // the forward writes the adjoint-input layout
 };
 
 // internal launchers
@@ -68,10 +82,15 @@ int fl_ref_fb_adjoint(fl_plan* p, const float* y, float* x, cudaStream_t st);
 // (lets a captured CGLS iteration become a no-op after convergence).
 // xscale: optional device factor applied to the gathered sum (scaled storage).
 int fl_matched_forward(fl_plan* p, const void* x, int xt, void* y, int yt, int cr_power,
-                       const int* skip, const float* xscale, cudaStream_t st);
+                       const int* skip, const float* xscale, int layout, cudaStream_t st);
+// yw (adjoint-input layout) = c_r * y (standard layout)
 int fl_matched_weight(fl_plan* p, const void* y, int yt, float* yw, cudaStream_t st);
 int fl_matched_adjoint_w(fl_plan* p, const float* yw, void* x, int xt, const int* skip,
-                         cudaStream_t st);
+                         int layout, cudaStream_t st);
+// volume (all frames) to the z-folded layout, or back with unfold = 1
+int fl_matched_fold(fl_plan* p, const void* src, void* dst, int dtype, int unfold,
+                    cudaStream_t st);
 int fl_plan_work(fl_plan* p, float** w);
+int fl_plan_vwork(fl_plan* p, size_t bytes, void** w);
 int fl_matched_ready(fl_plan* p);
 int fl_matched_count(fl_plan* p, int32_t* counts, cudaStream_t st);

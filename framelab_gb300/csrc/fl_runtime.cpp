@@ -63,7 +63,7 @@ static void free_plan_arrays(fl_plan* p)
                     p->d_sin_phi, p->d_cos_det, p->d_sin_det,   p->d_cphi_f, p->d_sphi_f,
                     p->d_view_frame, p->d_idY, p->d_Nv,        p->d_col,   p->d_colr,
                     p->d_row,    p->d_rowz,   p->d_view,       p->d_work,
-                    p->d_cos_det2, p->d_sin_det2, p->d_fb_edges};
+                    p->d_cos_det2, p->d_sin_det2, p->d_fb_edges, p->d_vwork};
     for (void* q : ptrs)
         if (q) cudaFree(q);
 }
@@ -169,13 +169,17 @@ static int build_tables(fl_plan* p, const std::vector<float>& phi, const float* 
     }
     // z-mirror symmetry (fl_plan.h): exact comparisons, so only a geometry that
     // is symmetric in its FP32 inputs qualifies
+    // (every walked row must descend -- z_det < 0 for ib < nb/2 -- so its ray
+    // stays below the source plane: the z-folded volume holds only that half)
     p->zmirror_ok = 0;
-    if (s.ndim == 3 && s.nz % 2 == 0 && s.nb % 2 == 0 && z_det[0] < 0.0f) {
+    if (s.ndim == 3 && s.nz % 2 == 0 && s.nb % 2 == 0 && s.dz > 0.0f) {
         bool ok = true;
         for (int iv = 0; iv < s.nv && ok; iv++)
             if (sd_z && sd_z[iv] != 0.0f) ok = false;
         for (int ib = 0; ib < s.nb && ok; ib++)
             if (z_det[s.nb - 1 - ib] != -z_det[ib]) ok = false;
+        for (int ib = 0; ib < s.nb / 2 && ok; ib++)
+            if (!(z_det[ib] < 0.0f)) ok = false;
         p->zmirror_ok = ok ? 1 : 0;
     }
     p->zmirror = p->zmirror_ok;
@@ -393,7 +397,7 @@ extern "C" int fl_forward(fl_plan* p, int model, const void* x, int xt, void* y,
     }
     if (model == FL_MODEL_MATCHED) {
         if ((st = fl_matched_ready(p))) return st;
-        return fl_matched_forward(p, x, xt, y, yt, 1, nullptr, nullptr, sm);
+        return fl_matched_forward(p, x, xt, y, yt, 1, nullptr, nullptr, 0, sm);
     }
     if (model == FL_MODEL_GAO_REF) {
         if (xt != FL_F32 || yt != FL_F32)
@@ -409,6 +413,20 @@ extern "C" int fl_forward(fl_plan* p, int model, const void* x, int xt, void* y,
 }
 
 // scratch for the pre-weighted adjoint input, owned by the plan
+int fl_plan_vwork(fl_plan* p, size_t bytes, void** w)
+{
+    if (p->vwork_bytes < bytes) {
+        if (p->d_vwork) cudaFree(p->d_vwork);
+        p->d_vwork = nullptr;
+        p->vwork_bytes = 0;
+        int st = fl_check_cuda(cudaMalloc(&p->d_vwork, bytes), "cudaMalloc(volume scratch)");
+        if (st) return st;
+        p->vwork_bytes = bytes;
+    }
+    *w = p->d_vwork;
+    return FL_OK;
+}
+
 int fl_plan_work(fl_plan* p, float** w)
 {
     size_t need = (size_t)p->n_rays;
@@ -452,7 +470,7 @@ extern "C" int fl_adjoint(fl_plan* p, int model, const void* y, int yt, void* x,
         float* w;
         if ((st = fl_plan_work(p, &w))) return st;
         if ((st = fl_matched_weight(p, y, yt, w, sm))) return st;
-        return fl_matched_adjoint_w(p, w, x, xt, nullptr, sm);
+        return fl_matched_adjoint_w(p, w, x, xt, nullptr, 0, sm);
     }
     return fl_set_error(FL_ERR_UNSUPPORTED, "fl_adjoint: model %d not available", model);
 }

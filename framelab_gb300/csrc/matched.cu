@@ -15,6 +15,8 @@
 // Adjoint: one thread per voxel column gathers over the rays whose detector
 // window covers the column and evaluates the same w_rV from the same table
 // entries -- the exact transpose, with no atomics.
+#include <algorithm>
+
 #include "fl_common.cuh"
 #include "fl_plan.h"
 #include "matched_dev.cuh"
@@ -25,20 +27,21 @@ namespace {
 // Forward kernels. Block (32, 4): 32 adjacent detector columns x 4 rows of one
 // view, so a warp's rays are neighbours and their gathers share cache lines.
 // ---------------------------------------------------------------------------
-// MIRROR (scans symmetric about the source plane, fl_plan::zmirror): the
-// block walks only the rows ib < nb/2 and writes each ray's z-mirrored
-// companion, row nb-1-ib, from the same walk.
+// MIRROR (scans symmetric about the source plane, fl_plan::zmirror): X is
+// z-folded; the block walks only the rows ib < nb/2 and also produces each
+// ray's mirrored companion, row nb-1-ib, from the same walk. yfold selects
+// the folded sinogram layout (pairs of rows ib and nb-1-ib) for the output.
 template <typename TX, typename TY, bool MIRROR>
 __global__ void __launch_bounds__(128, MIRROR ? 12 : 16)
 k_fwd_cone(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restrict__ col,
            const float* __restrict__ colr, const RowEntry* __restrict__ row,
            const int* __restrict__ vframe, int nx, int ny, int nz, int na, int nb,
            long long nper, float scale, int cr_power, const int* __restrict__ skip,
-           const float* __restrict__ xscale)
+           const float* __restrict__ xscale, int yfold)
 {
     if (skip && *skip) return;
-    int ia = blockIdx.x * 32 + threadIdx.x;
-    int ib = blockIdx.y * 4 + threadIdx.y;
+    int ia = blockIdx.x * blockDim.x + threadIdx.x;
+    int ib = blockIdx.y * blockDim.y + threadIdx.y;
     int iv = blockIdx.z;
     if (ia >= na || ib >= (MIRROR ? nb / 2 : nb)) return;
     ColEntry ce = col[(long long)iv * na + ia];
@@ -51,11 +54,17 @@ k_fwd_cone(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restr
     if (xscale) { acc *= *xscale; accm *= *xscale; }
     float out = cr * acc;
     if (cr_power == 2) out = cr * out;
-    Store<TY>::st(y + ((long long)iv * nb + ib) * na + ia, out);
     if (MIRROR) {
         float om = cr * accm;
         if (cr_power == 2) om = cr * om;
-        Store<TY>::st(y + ((long long)iv * nb + (nb - 1 - ib)) * na + ia, om);
+        if (yfold) {
+            Store<TY>::st2(y + 2 * (((long long)iv * (nb / 2) + ib) * na + ia), out, om);
+        } else {
+            Store<TY>::st(y + ((long long)iv * nb + ib) * na + ia, out);
+            Store<TY>::st(y + ((long long)iv * nb + (nb - 1 - ib)) * na + ia, om);
+        }
+    } else {
+        Store<TY>::st(y + ((long long)iv * nb + ib) * na + ia, out);
     }
 }
 
@@ -104,6 +113,49 @@ k_count(int32_t* __restrict__ cnt, const ColEntry* __restrict__ col,
                                  nx, ny, 1, &c);
     }
     cnt[r] = c;
+}
+
+// Folded yw for a z-mirror plan: the pair (c_r y[ib], c_r y[nb-1-ib]) of rows
+// ib < nb/2, both with the walked row's c_r (equal to the mirror's: its d_z is
+// the exact negation).
+template <typename TY>
+__global__ void k_weight_fold(float* __restrict__ yw, const TY* __restrict__ y,
+                              const float* __restrict__ colr, const RowEntry* __restrict__ row,
+                              int na, int nb, long long npairs, float scale)
+{
+    long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= npairs) return;
+    const int nbh = nb / 2;
+    int ia = (int)(r % na);
+    long long q = r / na;
+    int ib = (int)(q % nbh);
+    int iv = (int)(q / nbh);
+    float cr = ray_cr(scale, colr[(long long)iv * na + ia], row[(long long)iv * nb + ib].dz2);
+    float a = Store<TY>::ld_plain(y + ((long long)iv * nb + ib) * na + ia);
+    float b = Store<TY>::ld_plain(y + ((long long)iv * nb + (nb - 1 - ib)) * na + ia);
+    Store<float>::st2(yw + 2 * r, cr * a, cr * b);
+}
+
+// z-fold / unfold of volumes (all frames): pair r = (iz < nz/2, iy, ix) of a
+// frame holds voxel (ix, iy, iz) and its mirror (ix, iy, nz-1-iz).
+template <typename T>
+__global__ void k_fold(const T* __restrict__ src, T* __restrict__ dst, long long nxy, int nz,
+                       long long npairs_frame, long long npairs, int unfold)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < npairs;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long f = i / npairs_frame, r = i % npairs_frame;
+        const long long iz = r / nxy, q = r % nxy;
+        const long long base = f * 2 * npairs_frame;
+        const long long lo = base + iz * nxy + q, hi = base + (nz - 1 - iz) * nxy + q;
+        if (unfold) {
+            const T a = src[base + 2 * r], b = src[base + 2 * r + 1];
+            dst[lo] = a; dst[hi] = b;
+        } else {
+            const T a = src[lo], b = src[hi];
+            dst[base + 2 * r] = a; dst[base + 2 * r + 1] = b;
+        }
+    }
 }
 
 // yw = c_r * y  (the adjoint gathers pre-weighted sinogram values)
@@ -167,15 +219,15 @@ k_adj_fan(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __re
 // (A_z increasing in k); MODE -1: below, every such ray falls; MODE 0: the run
 // straddles the source plane (general min/max). The other orientation's rays
 // get w <= 0 from the specialised formula, as they miss the run.
-// MIRROR: rows are limited to the walked half (nb here is nb/2) and every
-// weight also carries the mirrored ray (row nb-1-ib, read from ycolm - ib*na)
-// into the mirrored voxel's accumulator accm[k].
+// MIRROR: rows are limited to the walked half (nb here is nb/2), ycol points
+// into the folded sinogram (pairs of rows ib and nb-1-ib, row stride 2*na) and
+// every weight also carries the mirrored ray into the mirrored voxel's
+// accumulator accm[k].
 template <int MODE, int TZ, bool MIRROR>
 __device__ __forceinline__ void adj_rows(float (&acc)[TZ], float (&accm)[TZ], int nk, int z0,
                                          float l, float h, float e1, float e2, float s1,
                                          float s2, const float2* __restrict__ rv,
-                                         const float* __restrict__ ycol,
-                                         const float* __restrict__ ycolm, int na, int nb)
+                                         const float* __restrict__ ycol, int na, int nb)
 {
     float mn = fminf(e1, e2), mx = fmaxf(e1, e2);   // row span at plane k
 #pragma unroll
@@ -189,8 +241,13 @@ __device__ __forceinline__ void adj_rows(float (&acc)[TZ], float (&accm)[TZ], in
         const float fk0 = (float)(z0 + k), fk1 = (float)(z0 + k + 1);
         for (int ib = blo; ib <= bhi; ib++) {
             const float2 re = rv[ib];                 // (inv_z, off_z) of row ib
-            const float yval = __ldg(ycol + (long long)ib * na);
-            const float ym = MIRROR ? __ldg(ycolm - (long long)ib * na) : 0.0f;
+            float yval, ym = 0.0f;
+            if (MIRROR) {
+                const float2 t = Store<float>::ld2(ycol + 2 * (long long)ib * na);
+                yval = t.x; ym = t.y;
+            } else {
+                yval = __ldg(ycol + (long long)ib * na);
+            }
             const float az0 = fmaf(fk0, re.x, re.y);
             const float az1 = fmaf(fk1, re.x, re.y);
             float l2, h2;
@@ -205,19 +262,20 @@ __device__ __forceinline__ void adj_rows(float (&acc)[TZ], float (&accm)[TZ], in
     }
 }
 
-// MIRROR: the runs cover the lower half z < nz/2 only (the walked rows'
-// rays never reach the upper half); each thread also writes the mirrored run.
+// MIRROR: yw is the folded sinogram; the runs cover the lower half z < nz/2
+// only (the walked rows' rays never reach the upper half) and each thread also
+// produces the mirrored run, into the folded volume when xfold is set.
 template <typename TX, int TZ, bool MIRROR>
 __global__ void __launch_bounds__(128, MIRROR ? 6 : 8)
 k_adj_cone(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __restrict__ col,
            const float2* __restrict__ rowz, const ViewEntry* __restrict__ view,
            const int* __restrict__ idY, const int* __restrict__ Nv, int tmp_size, DetGrid G,
            int nx, int ny, int nz, int na, int nb, float dz, int zruns,
-           const int* __restrict__ skip)
+           const int* __restrict__ skip, int xfold)
 {
     if (skip && *skip) return;
-    const int ix = blockIdx.x * 32 + threadIdx.x;
-    const int iy = blockIdx.y * 4 + threadIdx.y;
+    const int ix = blockIdx.x * blockDim.x + threadIdx.x;
+    const int iy = blockIdx.y * blockDim.y + threadIdx.y;
     const int zr = blockIdx.z % zruns, it = blockIdx.z / zruns;
     const int z0 = zr * TZ;
     const int nzw = MIRROR ? nz / 2 : nz;      // voxels gathered directly
@@ -238,7 +296,7 @@ k_adj_cone(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __r
         column_window(G, ve.c, ve.s, x0, y0, 1.0f, 1.0f, na, alo, ahi, dmin, dmax);
         const ColEntry* cv = col + (long long)iv * na;
         const float2* rv = rowz + (long long)iv * nb;
-        const float* yv = yw + (long long)iv * nb * na;
+        const float* yv = yw + (long long)iv * nb * na;   // folded: nb/2 rows of pairs
         // run planes relative to the source: lowest and highest
         const float zr0 = (float)(z0 - nz / 2) * dz - ve.sz;
         const float zr1 = (float)(z0 + nk - nz / 2) * dz - ve.sz;
@@ -260,22 +318,28 @@ k_adj_cone(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __r
             const float r1 = __fdividef(1.0f, l + ve.ac), r2 = __fdividef(1.0f, h + ve.ac);
             const float s1 = dz * r1 * inv_dv, s2 = dz * r2 * inv_dv;
             const float e1 = (zr0 * r1 - G.v0) * inv_dv, e2 = (zr0 * r2 - G.v0) * inv_dv;
-            const float* ycol = yv + ia;
-            const float* ycolm = yv + (long long)(nb - 1) * na + ia;
+            const float* ycol = MIRROR ? yv + 2 * ia : yv + ia;
             if (mode > 0)
-                adj_rows<1, TZ, MIRROR>(acc, accm, nk, z0, l, h, e1, e2, s1, s2, rv, ycol, ycolm, na, nbw);
+                adj_rows<1, TZ, MIRROR>(acc, accm, nk, z0, l, h, e1, e2, s1, s2, rv, ycol, na, nbw);
             else if (mode < 0)
-                adj_rows<-1, TZ, MIRROR>(acc, accm, nk, z0, l, h, e1, e2, s1, s2, rv, ycol, ycolm, na, nbw);
+                adj_rows<-1, TZ, MIRROR>(acc, accm, nk, z0, l, h, e1, e2, s1, s2, rv, ycol, na, nbw);
             else
-                adj_rows<0, TZ, MIRROR>(acc, accm, nk, z0, l, h, e1, e2, s1, s2, rv, ycol, ycolm, na, nbw);
+                adj_rows<0, TZ, MIRROR>(acc, accm, nk, z0, l, h, e1, e2, s1, s2, rv, ycol, na, nbw);
         }
     }
-    const long long base = (long long)it * nx * ny * nz + (long long)iy * nx + ix;
+    const long long frame = (long long)it * nx * ny * nz, col_ = (long long)iy * nx + ix;
 #pragma unroll
     for (int k = 0; k < TZ; k++)
         if (k < nk) {
-            Store<TX>::st(X + base + (long long)(z0 + k) * nx * ny, acc[k]);
-            if (MIRROR) Store<TX>::st(X + base + (long long)(nz - 1 - z0 - k) * nx * ny, accm[k]);
+            if (MIRROR && xfold) {
+                Store<TX>::st2(X + frame + 2 * ((long long)(z0 + k) * nx * ny + col_), acc[k],
+                               accm[k]);
+            } else {
+                Store<TX>::st(X + frame + (long long)(z0 + k) * nx * ny + col_, acc[k]);
+                if (MIRROR)
+                    Store<TX>::st(X + frame + (long long)(nz - 1 - z0 - k) * nx * ny + col_,
+                                  accm[k]);
+            }
         }
 }
 
@@ -289,19 +353,19 @@ DetGrid det_grid(const fl_plan* p)
 
 template <typename TX, typename TY>
 void launch_fwd(fl_plan* p, const void* x, void* y, int cr_power, const int* skip,
-                const float* xscale, cudaStream_t st)
+                const float* xscale, int yfold, cudaStream_t st)
 {
     const fl_scan& s = p->s;
     if (s.ndim == 3 && p->zmirror) {
-        dim3 grid(fl_div_up(s.na, 32), fl_div_up(s.nb / 2, 4), s.nv);
-        k_fwd_cone<TX, TY, true><<<grid, dim3(32, 4), 0, st>>>(
+        dim3 grid(fl_div_up(s.na, 16), fl_div_up(s.nb / 2, 8), s.nv);
+        k_fwd_cone<TX, TY, true><<<grid, dim3(16, 8), 0, st>>>(
             (const TX*)x, (TY*)y, p->d_col, p->d_colr, p->d_row, p->d_view_frame, s.nx, s.ny,
-            s.nz, s.na, s.nb, p->n_vox_frame, s.scale, cr_power, skip, xscale);
+            s.nz, s.na, s.nb, p->n_vox_frame, s.scale, cr_power, skip, xscale, yfold);
     } else if (s.ndim == 3) {
         dim3 grid(fl_div_up(s.na, 32), fl_div_up(s.nb, 4), s.nv);
         k_fwd_cone<TX, TY, false><<<grid, dim3(32, 4), 0, st>>>(
             (const TX*)x, (TY*)y, p->d_col, p->d_colr, p->d_row, p->d_view_frame, s.nx, s.ny,
-            s.nz, s.na, s.nb, p->n_vox_frame, s.scale, cr_power, skip, xscale);
+            s.nz, s.na, s.nb, p->n_vox_frame, s.scale, cr_power, skip, xscale, 0);
     } else {
         long long nr = (long long)s.na * s.nv;
         k_fwd_fan<TX, TY><<<fl_div_up(nr, 128), 128, 0, st>>>(
@@ -312,15 +376,16 @@ void launch_fwd(fl_plan* p, const void* x, void* y, int cr_power, const int* ski
 
 template <typename TX>
 void launch_fwd_y(fl_plan* p, const void* x, void* y, int yt, int cr_power, const int* skip,
-                  const float* xscale, cudaStream_t st)
+                  const float* xscale, int yfold, cudaStream_t st)
 {
-    if (yt == FL_F32) launch_fwd<TX, float>(p, x, y, cr_power, skip, xscale, st);
-    else if (yt == FL_F16) launch_fwd<TX, __half>(p, x, y, cr_power, skip, xscale, st);
-    else launch_fwd<TX, __nv_bfloat16>(p, x, y, cr_power, skip, xscale, st);
+    if (yt == FL_F32) launch_fwd<TX, float>(p, x, y, cr_power, skip, xscale, yfold, st);
+    else if (yt == FL_F16) launch_fwd<TX, __half>(p, x, y, cr_power, skip, xscale, yfold, st);
+    else launch_fwd<TX, __nv_bfloat16>(p, x, y, cr_power, skip, xscale, yfold, st);
 }
 
 template <typename TX>
-void launch_adj(fl_plan* p, const float* yw, void* x, const int* skip, cudaStream_t st)
+void launch_adj(fl_plan* p, const float* yw, void* x, const int* skip, int xfold,
+                cudaStream_t st)
 {
     const fl_scan& s = p->s;
     DetGrid G = det_grid(p);
@@ -328,15 +393,17 @@ void launch_adj(fl_plan* p, const float* yw, void* x, const int* skip, cudaStrea
         constexpr int TZ = 8;
         const int nzw = p->zmirror ? s.nz / 2 : s.nz;
         int zruns = (nzw + TZ - 1) / TZ;
-        dim3 grid(fl_div_up(s.nx, 32), fl_div_up(s.ny, 4), (unsigned)zruns * s.nt);
-        if (p->zmirror)
-            k_adj_cone<TX, TZ, true><<<grid, dim3(32, 4), 0, st>>>(
+        if (p->zmirror) {
+            dim3 grid(fl_div_up(s.nx, 16), fl_div_up(s.ny, 8), (unsigned)zruns * s.nt);
+            k_adj_cone<TX, TZ, true><<<grid, dim3(16, 8), 0, st>>>(
                 (TX*)x, yw, p->d_col, p->d_rowz, p->d_view, p->d_idY, p->d_Nv, p->tmp_size, G,
-                s.nx, s.ny, s.nz, s.na, s.nb, s.dz, zruns, skip);
-        else
+                s.nx, s.ny, s.nz, s.na, s.nb, s.dz, zruns, skip, xfold);
+        } else {
+            dim3 grid(fl_div_up(s.nx, 32), fl_div_up(s.ny, 4), (unsigned)zruns * s.nt);
             k_adj_cone<TX, TZ, false><<<grid, dim3(32, 4), 0, st>>>(
                 (TX*)x, yw, p->d_col, p->d_rowz, p->d_view, p->d_idY, p->d_Nv, p->tmp_size, G,
-                s.nx, s.ny, s.nz, s.na, s.nb, s.dz, zruns, skip);
+                s.nx, s.ny, s.nz, s.na, s.nb, s.dz, zruns, skip, 0);
+        }
     } else {
         dim3 grid(fl_div_up(s.nx, 2 * 128), (s.ny + 1) / 2, s.nt);
         k_adj_fan<TX><<<grid, 128, 0, st>>>((TX*)x, yw, p->d_col, p->d_view, p->d_idY,
@@ -344,14 +411,47 @@ void launch_adj(fl_plan* p, const float* yw, void* x, const int* skip, cudaStrea
     }
 }
 
+template <typename T>
+void launch_fold(fl_plan* p, const void* src, void* dst, int unfold, cudaStream_t st)
+{
+    const fl_scan& s = p->s;
+    const long long nxy = (long long)s.nx * s.ny;
+    const long long npf = nxy * (s.nz / 2), np = npf * s.nt;
+    unsigned g = (unsigned)std::min<long long>((np + 255) / 256, 16LL * 152);
+    k_fold<T><<<g, 256, 0, st>>>((const T*)src, (T*)dst, nxy, s.nz, npf, np, unfold);
+}
+
+size_t dtype_bytes(int t) { return t == FL_F32 ? 4 : 2; }
+
 }  // namespace
 
-int fl_matched_forward(fl_plan* p, const void* x, int xt, void* y, int yt, int cr_power,
-                       const int* skip, const float* xscale, cudaStream_t st)
+int fl_matched_fold(fl_plan* p, const void* src, void* dst, int dtype, int unfold,
+                    cudaStream_t st)
 {
-    if (xt == FL_F32) launch_fwd_y<float>(p, x, y, yt, cr_power, skip, xscale, st);
-    else if (xt == FL_F16) launch_fwd_y<__half>(p, x, y, yt, cr_power, skip, xscale, st);
-    else launch_fwd_y<__nv_bfloat16>(p, x, y, yt, cr_power, skip, xscale, st);
+    if (!p->zmirror) return fl_set_error(FL_ERR_INVALID, "fold: plan has no z-mirror layout");
+    if (dtype == FL_F32) launch_fold<float>(p, src, dst, unfold, st);
+    else if (dtype == FL_F16) launch_fold<__half>(p, src, dst, unfold, st);
+    else launch_fold<__nv_bfloat16>(p, src, dst, unfold, st);
+    return fl_check_launch(unfold ? "z-unfold" : "z-fold");
+}
+
+int fl_matched_forward(fl_plan* p, const void* x, int xt, void* y, int yt, int cr_power,
+                       const int* skip, const float* xscale, int layout, cudaStream_t st)
+{
+    int yfold = 0;
+    if (p->s.ndim == 3 && p->zmirror) {
+        if (!(layout & FL_LAY_X_FOLDED)) {
+            void* w;
+            int e = fl_plan_vwork(p, (size_t)p->n_vox * dtype_bytes(xt), &w);
+            if (e) return e;
+            if ((e = fl_matched_fold(p, x, w, xt, 0, st))) return e;
+            x = w;
+        }
+        yfold = (layout & FL_LAY_Y_ADJ) ? 1 : 0;
+    }
+    if (xt == FL_F32) launch_fwd_y<float>(p, x, y, yt, cr_power, skip, xscale, yfold, st);
+    else if (xt == FL_F16) launch_fwd_y<__half>(p, x, y, yt, cr_power, skip, xscale, yfold, st);
+    else launch_fwd_y<__nv_bfloat16>(p, x, y, yt, cr_power, skip, xscale, yfold, st);
     return fl_check_launch("matched forward");
 }
 
@@ -360,6 +460,21 @@ int fl_matched_weight(fl_plan* p, const void* y, int yt, float* yw, cudaStream_t
     const fl_scan& s = p->s;
     long long nr = p->n_rays;
     int three = s.ndim == 3;
+    if (three && p->zmirror) {
+        long long np = (long long)s.nv * (s.nb / 2) * s.na;
+        unsigned g = fl_div_up(np, 256);
+        if (yt == FL_F32)
+            k_weight_fold<float><<<g, 256, 0, st>>>(yw, (const float*)y, p->d_colr, p->d_row,
+                                                    s.na, s.nb, np, s.scale);
+        else if (yt == FL_F16)
+            k_weight_fold<__half><<<g, 256, 0, st>>>(yw, (const __half*)y, p->d_colr, p->d_row,
+                                                     s.na, s.nb, np, s.scale);
+        else
+            k_weight_fold<__nv_bfloat16><<<g, 256, 0, st>>>(yw, (const __nv_bfloat16*)y,
+                                                            p->d_colr, p->d_row, s.na, s.nb, np,
+                                                            s.scale);
+        return fl_check_launch("matched adjoint weighting");
+    }
     unsigned g = fl_div_up(nr, 256);
     if (yt == FL_F32)
         k_weight<float><<<g, 256, 0, st>>>(yw, (const float*)y, p->d_colr, p->d_row, s.na,
@@ -374,11 +489,12 @@ int fl_matched_weight(fl_plan* p, const void* y, int yt, float* yw, cudaStream_t
 }
 
 int fl_matched_adjoint_w(fl_plan* p, const float* yw, void* x, int xt, const int* skip,
-                         cudaStream_t st)
+                         int layout, cudaStream_t st)
 {
-    if (xt == FL_F32) launch_adj<float>(p, yw, x, skip, st);
-    else if (xt == FL_F16) launch_adj<__half>(p, yw, x, skip, st);
-    else launch_adj<__nv_bfloat16>(p, yw, x, skip, st);
+    const int xfold = (p->zmirror && (layout & FL_LAY_X_FOLDED)) ? 1 : 0;
+    if (xt == FL_F32) launch_adj<float>(p, yw, x, skip, xfold, st);
+    else if (xt == FL_F16) launch_adj<__half>(p, yw, x, skip, xfold, st);
+    else launch_adj<__nv_bfloat16>(p, yw, x, skip, xfold, st);
     return fl_check_launch("matched adjoint");
 }
 

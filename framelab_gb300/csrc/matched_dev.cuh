@@ -35,9 +35,12 @@ __device__ __forceinline__ int start_slab(float a, float inv, float off, int n)
 // apart for any table fl_plan_create accepts), and the loop leaves as soon as
 // the crossing reaches the exit (or is NaN); the step budget nx+ny+nz+4 is a
 // second, independent bound.
-// MIRROR: also gathers the z-mirrored voxel (ix, iy, nz-1-iz) of every voxel
-// visited, with the same segment length, into *accm -- the companion ray of a
-// scan that is symmetric about the source plane (fl_plan::zmirror).
+// MIRROR: x is the z-folded volume (pairs of voxel (ix, iy, iz < nz/2) and its
+// mirror (ix, iy, nz-1-iz), fl_plan.h); the ray must descend from the source
+// plane, so it stays in iz < nz/2. Every step gathers the pair: the voxel's
+// value goes to the return value and the mirror's, with the same segment
+// length, to *accm -- the companion ray of a scan symmetric about the source
+// plane (fl_plan::zmirror).
 template <typename TX, bool THREE, bool COUNT, bool MIRROR = false>
 __device__ __forceinline__ float walk(const TX* __restrict__ x, float inv_x, float off_x,
                                       float inv_y, float off_y, float inv_z, float off_z,
@@ -57,12 +60,17 @@ __device__ __forceinline__ float walk(const TX* __restrict__ x, float inv_x, flo
         if (MIRROR) *accm = 0.0f;
         return 0.0f;
     }
+    if (MIRROR && !(inv_z < 0.0f)) {               // not a descending ray: no walk
+        *accm = 0.0f;
+        return 0.0f;
+    }
     const int jx = start_slab(a_in, inv_x, off_x, nx);
     const int jy = start_slab(a_in, inv_y, off_y, ny);
-    const int jz = THREE ? start_slab(a_in, inv_z, off_z, nz) : 0;
+    int jz = THREE ? start_slab(a_in, inv_z, off_z, nz) : 0;
+    // a descending ray enters below the source plane and only steps down, so
+    // the folded index below stays inside the nz/2 stored slices
+    if (MIRROR) jz = min(jz, nz / 2 - 1);
     int v = (jz * ny + jy) * nx + jx;              // < 2^31 (checked at plan creation)
-    // mirrored voxel index = v + m; m changes only when the walk steps in z
-    int m = MIRROR ? (nz - 1 - 2 * jz) * (nx * ny) : 0;
     const bool px = inv_x > 0.0f, py = inv_y > 0.0f, pz = inv_z > 0.0f;
     float pax = (float)(px ? jx + 1 : jx);
     float pay = (float)(py ? jy + 1 : jy);
@@ -76,8 +84,13 @@ __device__ __forceinline__ float walk(const TX* __restrict__ x, float inv_x, flo
     int cnt = 0;
     // the gather of the next voxel is issued as soon as its index is known and
     // consumed one step later, so its latency overlaps the next step's compares
-    float xv = COUNT ? 0.0f : ldv(x + v);
-    float xm = MIRROR ? ldv(x + v + m) : 0.0f;
+    float xv = 0.0f, xm = 0.0f;
+    if (MIRROR) {
+        const float2 t = Store<TX>::ld2(x + 2 * (long long)v);
+        xv = t.x; xm = t.y;
+    } else if (!COUNT) {
+        xv = ldv(x + v);
+    }
     const int budget = nx + ny + (THREE ? nz : 0) + 4;
     for (int it = 0; it < budget; it += 4) {
 #pragma unroll
@@ -89,12 +102,13 @@ __device__ __forceinline__ float walk(const TX* __restrict__ x, float inv_x, flo
             if (cont) {
                 if (nAx == nxt) { pax += stx; v += dvx; nAx = fmaf(pax, inv_x, off_x); }
                 if (nAy == nxt) { pay += sty; v += dvy; nAy = fmaf(pay, inv_y, off_y); }
-                if (THREE && nAz == nxt) {
-                    paz += stz; v += dvz; nAz = fmaf(paz, inv_z, off_z);
-                    if (MIRROR) m -= 2 * dvz;
+                if (THREE && nAz == nxt) { paz += stz; v += dvz; nAz = fmaf(paz, inv_z, off_z); }
+                if (MIRROR) {                        // v is inside the folded volume here
+                    const float2 t = Store<TX>::ld2(x + 2 * (long long)v);
+                    xn = t.x; xmn = t.y;
+                } else if (!COUNT) {
+                    xn = ldv(x + v);                 // v is inside the volume here
                 }
-                if (!COUNT) xn = ldv(x + v);        // v is inside the volume here
-                if (MIRROR) xmn = ldv(x + v + m);   // and so is its mirror
             }
             if (COUNT) cnt += (seg > 0.0f);
             else acc = fmaf(seg, xv, acc);

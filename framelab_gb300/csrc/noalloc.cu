@@ -70,6 +70,6 @@ extern "C" int fl_adjoint_noalloc(fl_plan* p, const void* y, int yt, void* x, in
     if ((st = scratch_for_current_device(&w))) return st;
     cudaStream_t s = (cudaStream_t)stream;
     if ((st = fl_matched_weight(p, y, yt, w, s))) return st;
-    if ((st = fl_matched_adjoint_w(p, w, x, xt, nullptr, s))) return st;
+    if ((st = fl_matched_adjoint_w(p, w, x, xt, nullptr, 0, s))) return st;
     return fl_set_error(FL_OK, "");
 }

@@ -175,10 +175,12 @@ int fl_plan_sizes(const fl_plan *plan, int64_t *n_vox, int64_t *n_rays);
 
 /* Plan options.
  * FL_OPT_Z_MIRROR: on by default for a cone scan that is symmetric about the
- *   source plane (every sd_z = 0, nz and nb even, z_det[nb-1-ib] == -z_det[ib]
- *   exactly, z_det[0] < 0). The matched pair then walks / weighs only the
- *   rows ib < nb/2 and gives row nb-1-ib the mirrored values, so both
- *   kernels do about half the work; the matrix stays exactly transposed.
+ *   source plane (every sd_z = 0, nz and nb even, dz > 0, z_det[nb-1-ib] ==
+ *   -z_det[ib] exactly and z_det[ib] < 0 for ib < nb/2). The matched pair then
+ *   walks / weighs only the rows ib < nb/2 and gives row nb-1-ib the mirrored
+ *   values, with voxel pairs (iz, nz-1-iz) and row pairs stored side by side
+ *   internally, so both kernels do about half the work; the matrix stays
+ *   exactly transposed.
  *   Setting 0 selects the general kernels; 1 re-enables it where allowed. */
 enum { FL_OPT_Z_MIRROR = 1 };
 int fl_plan_option(fl_plan *plan, int option, int value);

@@ -71,3 +71,28 @@ def test_cgls_early_stop_and_warm_start():
     u6 = cg2.solve(bt, lam=1.0, iters=6)
     r = lambda v: np.linalg.norm(v.cpu().numpy())  # noqa: E731
     assert r(u2 - u6) / r(u6) < 0.2     # warm restart lands near the 6-iteration solution
+
+
+@pytest.mark.parametrize("mode", ["graph", "mixed"])
+def test_cgls_z_folded_vectors_follow_the_plan_option(mode):
+    """On a source-plane-symmetric scan the fused forms keep their vectors
+    z-folded; turning the plan's mirror option off between solves on the same
+    workspace switches to the general kernels and standard layout."""
+    import torch
+    from framelab_gb300.projector import Plan
+    from framelab_gb300.solvers import NativeCGLS
+    p, x, b = _setup(16, 8)
+    P = Plan(p)
+    assert P.z_mirror
+    bt = torch.from_numpy(b.astype(np.float32)).cuda()
+    cg = NativeCGLS(P, mode)
+    u_m = cg.solve(bt, lam=0.5, iters=6, refresh=3)
+    P.z_mirror = False
+    u_g = cg.solve(bt, lam=0.5, iters=6, refresh=3)
+    P.z_mirror = True
+    u_m2 = cg.solve(bt, lam=0.5, iters=6, refresh=3)
+    rel = float((u_m - u_g).norm() / u_g.norm())
+    assert rel < (1e-3 if mode == "mixed" else 1e-5), rel
+    assert torch.equal(u_m, u_m2)
+    u64, _ = _oracle_solution(p, b, 0.5, 6)
+    assert np.linalg.norm(u_m.cpu().numpy() - u64) / np.linalg.norm(u64) < 1e-3
