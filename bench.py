@@ -334,6 +334,23 @@ class ClockSampler:
 # --------------------------------------------------------------------------
 # GPU legs
 # --------------------------------------------------------------------------
+def max_over_ranks(t: float, world: int, device) -> float:
+    """The slowest replica's time: the job ends when every rank has."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        x = torch.tensor([t], device=device, dtype=torch.float64)
+        dist.all_reduce(x, op=dist.ReduceOp.MAX)
+        return float(x.item())
+    return t
+
+
+def job_rate(world: int, steps: int, t_max: float) -> float:
+    """Whole-job throughput of independent replicas (weak scaling): every rank
+    does `steps` steps, all of them done after t_max seconds."""
+    return world * steps / t_max
+
+
 class Ctx:
     """Device, stream, replica bookkeeping and the CUDA-event timer."""
 
@@ -353,12 +370,7 @@ class Ctx:
             dist.barrier()
 
     def tmax(self, t):
-        if self.world > 1:
-            import torch.distributed as dist
-            x = self.torch.tensor([t], device=self.dev, dtype=self.torch.float64)
-            dist.all_reduce(x, op=dist.ReduceOp.MAX)
-            return float(x.item())
-        return t
+        return max_over_ranks(t, self.world, self.dev)
 
     def timed(self, fn):
         """Run fn between CUDA events on the launching stream, synchronised and
@@ -531,7 +543,7 @@ def run_single(ctx, name, w, p):
         detail["gradcheck_voxels"] = 64
         detail["gradcheck_s"] = time.perf_counter() - t0
         del f
-    return dict(value=world * K / t_g, t_step=t_g / K, e2e=e2e, roofline=roofline,
+    return dict(value=job_rate(world, K, t_g), t_step=t_g / K, e2e=e2e, roofline=roofline,
                 launches=5 * K + 1, detail=detail, clocks=clocks.summary(), unit="iter/s")
 
 
@@ -599,7 +611,7 @@ def run_batch(ctx, name, w, paras):
         _, ta = ctx.timed(lambda: [B.adjoint(y, out=xo) for _ in range(reps)])
         roofline = projector_roofline(ctx, name, n_isect, B.n_rays, B.n_vox, tf / reps,
                                       ta / reps, detail, "batched matched")
-    return dict(value=world * K / t_b, t_step=t_b / K, e2e=e2e, roofline=roofline,
+    return dict(value=job_rate(world, K, t_b), t_step=t_b / K, e2e=e2e, roofline=roofline,
                 launches=5 * K + 1, detail=detail, clocks=clocks.summary(), unit="iter/s")
 
 
@@ -656,7 +668,7 @@ def run_sb(ctx, name, w, p):
     # warm-start residual (fwd, adj, axpy) + init, inner x (fwd, adj, 3 updates),
     # Bregman analysis + synthesis (3 + 3 per level), |u_k - u_{k-1}| (diff, 2 dots)
     launches = 2 + 3 * w["levels"] + K * (4 + 5 * w["inner"] + 6 * w["levels"] + 3)
-    return dict(value=world * K / t_s, t_step=t_s / K, e2e=e2e, roofline=roofline,
+    return dict(value=job_rate(world, K, t_s), t_step=t_s / K, e2e=e2e, roofline=roofline,
                 launches=launches, detail=detail, clocks=clocks.summary(), unit="iter/s")
 
 

@@ -13,11 +13,12 @@ class Project(torch.autograd.Function):
     @staticmethod
     def forward(ctx, x: torch.Tensor, plan) -> torch.Tensor:
         ctx.plan = plan
+        ctx.x_shape = x.shape
         return plan.forward(x.detach().contiguous())
 
     @staticmethod
     def backward(ctx, gy: torch.Tensor):
-        return ctx.plan.adjoint(gy.detach().contiguous()), None
+        return ctx.plan.adjoint(gy.detach().contiguous()).reshape(ctx.x_shape), None
 
 
 def project(x: torch.Tensor, plan) -> torch.Tensor:

@@ -248,6 +248,15 @@ struct DotScratch {
 DotScratch g_dot[64];
 }
 
+extern "C" int fl_axpby(float* y, const float* x, float a, float b, int64_t n, void* stream)
+{
+    if (!y || (!x && a != 0.0f) || n < 0) return fl_set_error(FL_ERR_INVALID, "fl_axpby: bad argument");
+    if (n == 0) return fl_set_error(FL_OK, "");
+    k_axpby<<<grid_for(n), kThreads, 0, (cudaStream_t)stream>>>(y, x ? x : y, x ? a : 0.0f, b, n);
+    int st = fl_check_launch("fl_axpby");
+    return st ? st : fl_set_error(FL_OK, "");
+}
+
 extern "C" int fl_dot(const float* a, const float* b, int64_t n, double* out, void* stream)
 {
     if (!a || !b || !out || n < 0) return fl_set_error(FL_ERR_INVALID, "fl_dot: bad argument");

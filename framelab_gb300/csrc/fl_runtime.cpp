@@ -219,6 +219,10 @@ extern "C" int fl_plan_create(const fl_scan* scan, fl_plan** out)
         return fl_set_error(FL_ERR_INVALID, "sizes must be positive");
     if ((int64_t)s.nx * s.ny * s.nz >= (int64_t)1 << 31)
         return fl_set_error(FL_ERR_UNSUPPORTED, "a frame must hold fewer than 2^31 voxels");
+    // views, detector rows and image rows index grid dimensions y / z
+    if (s.nv > 65535 || s.nb > 65535 || s.ny > 65535 || s.nt > 65535)
+        return fl_set_error(FL_ERR_UNSUPPORTED,
+                            "at most 65535 views, detector rows, image rows and frames per plan");
     if (!(s.SO > 0) || !(s.OD > -s.SO) || !(s.scale > 0) || !(s.dz > 0))
         return fl_set_error(FL_ERR_INVALID, "SO, SO+OD, scale and dz must be positive");
     if ((!s.sd_phi && !(s.cos_phi && s.sin_phi)) || !s.y_det || (s.ndim == 3 && !s.z_det))

@@ -158,6 +158,20 @@ unsigned grid_for(long long n)
 }  // namespace
 
 // ---------------------------------------------------------------------------
+// out = sign(a) max(|a| - tau, 0) for coefficients outside [keep0, keep1)
+// (the unshrunk low band), out = a inside
+__global__ void k_shrink(const float* __restrict__ a, float* __restrict__ out, long long n,
+                         long long keep0, long long keep1, float tau)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const float v = a[i];
+        if (i >= keep0 && i < keep1) { out[i] = v; continue; }
+        const float m = fmaxf(fabsf(v) - tau, 0.0f);
+        out[i] = v > 0.0f ? m : (v < 0.0f ? -m : 0.0f);
+    }
+}
+
 struct fl_framelet {
     int nx, ny, nz, dim, levels, kind;
     int nf, nbands;                 // filters per axis, bands per level (nf^dim)
@@ -369,5 +383,16 @@ extern "C" int fl_framelet_bregman(fl_framelet* w, const float* u, float* v, flo
     int st = analysis(w, u, v, t, 1, tau, s);
     if (st) return st;
     st = synthesis(w, t, b, Atf, mu, s);
+    return st ? st : fl_set_error(FL_OK, "");
+}
+
+extern "C" int fl_framelet_shrink(fl_framelet* w, const float* coef, float* out, float tau,
+                                  void* stream)
+{
+    if (!w || !coef || !out) return fl_set_error(FL_ERR_INVALID, "fl_framelet_shrink: null argument");
+    const long long n = w->ncoef_bands * w->N;
+    const long long low = w->level_base[w->levels - 1] * w->N;   // band 0 of the last level
+    k_shrink<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(coef, out, n, low, low + w->N, tau);
+    int st = fl_check_launch("framelet shrink");
     return st ? st : fl_set_error(FL_OK, "");
 }

@@ -40,9 +40,12 @@ k_fwd_cone(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restr
            const float* __restrict__ xscale, int yfold)
 {
     if (skip && *skip) return;
+    // grid y = view, grid z = band of detector rows: the blocks that run
+    // together cover all views of one row band, whose rays share a z-slab of
+    // the volume, so the gathers stay in L2
     int ia = blockIdx.x * blockDim.x + threadIdx.x;
-    int ib = blockIdx.y * blockDim.y + threadIdx.y;
-    int iv = blockIdx.z;
+    int iv = blockIdx.y;
+    int ib = blockIdx.z * blockDim.y + threadIdx.y;
     if (ia >= na || ib >= (MIRROR ? nb / 2 : nb)) return;
     ColEntry ce = col[(long long)iv * na + ia];
     RowEntry re = row[(long long)iv * nb + ib];
@@ -179,8 +182,9 @@ __global__ void k_weight(float* __restrict__ yw, const TY* __restrict__ y,
 // ---------------------------------------------------------------------------
 // Fan adjoint: one thread per (pixel, frame).
 // ---------------------------------------------------------------------------
-// Fan adjoint: one thread per 2 x 2 pixel block of one frame.
-template <typename TX>
+// Fan adjoint: one thread per P x P pixel block of one frame (P = 2 for
+// images large enough to fill the GPU, else 1).
+template <typename TX, int P>
 __global__ void __launch_bounds__(128)
 k_adj_fan(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __restrict__ col,
           const ViewEntry* __restrict__ view, const int* __restrict__ idY,
@@ -188,18 +192,18 @@ k_adj_fan(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __re
           const int* __restrict__ skip)
 {
     if (skip && *skip) return;
-    const int ix0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
-    const int iy0 = 2 * blockIdx.y;
+    const int ix0 = P * (blockIdx.x * blockDim.x + threadIdx.x);
+    const int iy0 = P * blockIdx.y;
     const int it = blockIdx.z;
     if (ix0 >= nx) return;
-    float acc[2][2];
-    fan_block_gather<2, 2>(acc, yw, col, view, idY + it * tmp_size, Nv[it], G, ix0, iy0, nx,
+    float acc[P][P];
+    fan_block_gather<P, P>(acc, yw, col, view, idY + it * tmp_size, Nv[it], G, ix0, iy0, nx,
                            ny, na);
     TX* xf = X + (long long)it * nx * ny;
 #pragma unroll
-    for (int j = 0; j < 2; j++)
+    for (int j = 0; j < P; j++)
 #pragma unroll
-        for (int i = 0; i < 2; i++)
+        for (int i = 0; i < P; i++)
             if (iy0 + j < ny && ix0 + i < nx)
                 Store<TX>::st(xf + (long long)(iy0 + j) * nx + ix0 + i, acc[j][i]);
 }
@@ -229,15 +233,28 @@ __device__ __forceinline__ void adj_rows(float (&acc)[TZ], float (&accm)[TZ], in
                                          float s2, const float2* __restrict__ rv,
                                          const float* __restrict__ ycol, int na, int nb)
 {
+    // MIRROR with MODE -1 (every run of the lower half except the one at the
+    // source plane): the rays descend and the row grid rises (dv > 0 for any
+    // z-mirror plan), so e1 <= e2 at every plane and both grow with k; voxel
+    // k's rows are then [e1(k), e2(k + 1)] without per-plane min / max
+    constexpr bool DESC = MIRROR && MODE < 0;
     float mn = fminf(e1, e2), mx = fmaxf(e1, e2);   // row span at plane k
+    float lo_e = e1 - 0.02f, hi_e = e2 + s2 + 0.02f;
 #pragma unroll
     for (int k = 0; k < TZ; k++) {
         if (k >= nk) break;
-        e1 += s1; e2 += s2;
-        const float mn1 = fminf(e1, e2), mx1 = fmaxf(e1, e2);   // plane k + 1
-        const int blo = max(__float2int_ru(fminf(mn, mn1) - 0.02f), 0);
-        const int bhi = min(__float2int_rd(fmaxf(mx, mx1) + 0.02f), nb - 1);
-        mn = mn1; mx = mx1;
+        int blo, bhi;
+        if (DESC) {
+            blo = max(__float2int_ru(lo_e), 0);
+            bhi = min(__float2int_rd(hi_e), nb - 1);
+            lo_e += s1; hi_e += s2;
+        } else {
+            e1 += s1; e2 += s2;
+            const float mn1 = fminf(e1, e2), mx1 = fmaxf(e1, e2);   // plane k + 1
+            blo = max(__float2int_ru(fminf(mn, mn1) - 0.02f), 0);
+            bhi = min(__float2int_rd(fmaxf(mx, mx1) + 0.02f), nb - 1);
+            mn = mn1; mx = mx1;
+        }
         const float fk0 = (float)(z0 + k), fk1 = (float)(z0 + k + 1);
         for (int ib = blo; ib <= bhi; ib++) {
             const float2 re = rv[ib];                 // (inv_z, off_z) of row ib
@@ -266,7 +283,7 @@ __device__ __forceinline__ void adj_rows(float (&acc)[TZ], float (&accm)[TZ], in
 // only (the walked rows' rays never reach the upper half) and each thread also
 // produces the mirrored run, into the folded volume when xfold is set.
 template <typename TX, int TZ, bool MIRROR>
-__global__ void __launch_bounds__(128, MIRROR ? 6 : 8)
+__global__ void __launch_bounds__(128, 8)
 k_adj_cone(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __restrict__ col,
            const float2* __restrict__ rowz, const ViewEntry* __restrict__ view,
            const int* __restrict__ idY, const int* __restrict__ Nv, int tmp_size, DetGrid G,
@@ -357,13 +374,13 @@ void launch_fwd(fl_plan* p, const void* x, void* y, int cr_power, const int* ski
 {
     const fl_scan& s = p->s;
     if (s.ndim == 3 && p->zmirror) {
-        dim3 grid(fl_div_up(s.na, 16), fl_div_up(s.nb / 2, 8), s.nv);
-        k_fwd_cone<TX, TY, true><<<grid, dim3(16, 8), 0, st>>>(
+        dim3 grid(fl_div_up(s.na, 8), s.nv, fl_div_up(s.nb / 2, 16));
+        k_fwd_cone<TX, TY, true><<<grid, dim3(8, 16), 0, st>>>(
             (const TX*)x, (TY*)y, p->d_col, p->d_colr, p->d_row, p->d_view_frame, s.nx, s.ny,
             s.nz, s.na, s.nb, p->n_vox_frame, s.scale, cr_power, skip, xscale, yfold);
     } else if (s.ndim == 3) {
-        dim3 grid(fl_div_up(s.na, 32), fl_div_up(s.nb, 4), s.nv);
-        k_fwd_cone<TX, TY, false><<<grid, dim3(32, 4), 0, st>>>(
+        dim3 grid(fl_div_up(s.na, 8), s.nv, fl_div_up(s.nb, 16));
+        k_fwd_cone<TX, TY, false><<<grid, dim3(8, 16), 0, st>>>(
             (const TX*)x, (TY*)y, p->d_col, p->d_colr, p->d_row, p->d_view_frame, s.nx, s.ny,
             s.nz, s.na, s.nb, p->n_vox_frame, s.scale, cr_power, skip, xscale, 0);
     } else {
@@ -405,9 +422,19 @@ void launch_adj(fl_plan* p, const float* yw, void* x, const int* skip, int xfold
                 s.nx, s.ny, s.nz, s.na, s.nb, s.dz, zruns, skip, 0);
         }
     } else {
-        dim3 grid(fl_div_up(s.nx, 2 * 128), (s.ny + 1) / 2, s.nt);
-        k_adj_fan<TX><<<grid, 128, 0, st>>>((TX*)x, yw, p->d_col, p->d_view, p->d_idY,
-                                             p->d_Nv, p->tmp_size, G, s.nx, s.ny, s.na, skip);
+        // 2 x 2 blocks once there are at least 4 waves of 128-thread blocks
+        const long long blocks2 = (long long)fl_div_up(s.nx, 2 * 128) * ((s.ny + 1) / 2) * s.nt;
+        if (blocks2 >= 4LL * 152) {
+            dim3 grid(fl_div_up(s.nx, 2 * 128), (s.ny + 1) / 2, s.nt);
+            k_adj_fan<TX, 2><<<grid, 128, 0, st>>>((TX*)x, yw, p->d_col, p->d_view, p->d_idY,
+                                                    p->d_Nv, p->tmp_size, G, s.nx, s.ny, s.na,
+                                                    skip);
+        } else {
+            dim3 grid(fl_div_up(s.nx, 128), s.ny, s.nt);
+            k_adj_fan<TX, 1><<<grid, 128, 0, st>>>((TX*)x, yw, p->d_col, p->d_view, p->d_idY,
+                                                    p->d_Nv, p->tmp_size, G, s.nx, s.ny, s.na,
+                                                    skip);
+        }
     }
 }
 

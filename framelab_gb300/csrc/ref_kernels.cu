@@ -738,6 +738,8 @@ int fl_ref_adjoint(fl_plan* p, const float* y, float* x, cudaStream_t st)
             x, y, p->d_cos_phi, p->d_sin_phi, p->d_cos_det, p->d_sin_det, p->d_idY, p->d_Nv,
             p->tmp_size, s.SO, s.OD, s.scale, s.dy_det, s.y_os, s.nx, s.ny, s.na, s.nt);
     } else {
+        if ((long long)s.nz * s.nt > 65535)
+            return fl_set_error(FL_ERR_UNSUPPORTED, "reference backprojector: nz * nt > 65535");
         dim3 grid(fl_div_up(s.nx, 128), s.ny, (unsigned)s.nz * s.nt);
         k_ref_cone_chord_adj<<<grid, 128, 0, st>>>(
             x, y, p->d_cos_phi, p->d_sin_phi, p->d_sd_z, p->d_y_det, p->d_z_det, p->d_idY,

@@ -225,6 +225,10 @@ int fl_adjoint_noalloc(fl_plan *plan, const void *y, int y_dtype, void *x, int x
  * must not share a device. */
 int fl_dot(const float *a, const float *b, int64_t n, double *out, void *stream);
 
+/* y = a*x + b*y on n device floats (x may be NULL: y = b*y). The object
+ * algebra of ObjectData / CTData / FrameletExpansion (plus, minus, mtimes). */
+int fl_axpby(float *y, const float *x, float a, float b, int64_t n, void *stream);
+
 /* q = (A^T A + lam I) x for the matched model, FP32 (the operator
  * A_loc of solveCGLS.m:7). x, q: n_vox device floats. */
 int fl_normal_apply(fl_plan *plan, const float *x, float *q, float lam, void *stream);
