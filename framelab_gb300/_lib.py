@@ -70,7 +70,46 @@ _SIGS = {
                                      _I, _I, _I, _I, _I, _I, _I]),
     "Atx_cone_mf_gpu_new": (None, [_V, _V, _V, _V, _V, _V, _V, _V, _V, _F, _F, _F, _F, _F, _F,
                                    _F, _I, _I, _I, _I, _I, _I, _I, _I, _I]),
+    "fl_adjoint_noalloc": (_I, [_P, _V, _I, _V, _I, _V]),
+    # vector algebra and CGLS
+    "fl_dot": (_I, [_V, _V, _I64, _V, _V]),
+    "fl_axpby": (_I, [_V, _V, _F, _F, _I64, _V]),
+    "fl_normal_apply": (_I, [_P, _V, _V, _F, _V]),
+    "fl_cgls_create": (_I, [_P, _I, C.POINTER(_P)]),
+    "fl_cgls_destroy": (None, [_P]),
+    "fl_cgls_solve": (_I, [_P, _V, _V, _F, _I, _D, _I, _I, _V, C.POINTER(_I), _V]),
+    "fl_cgls_solve_host": (_I, [_P, _V, _V, _F, _I, _D, _I, _I, _V, C.POINTER(_I), _V]),
+    # framelets and split Bregman
+    "fl_framelet_create": (_I, [_I, _I, _I, _I, _I, C.POINTER(_P)]),
+    "fl_framelet_destroy": (None, [_P]),
+    "fl_framelet_ncoef": (_I64, [_P]),
+    "fl_framelet_analysis": (_I, [_P, _V, _V, _V]),
+    "fl_framelet_synthesis": (_I, [_P, _V, _V, _V]),
+    "fl_framelet_bregman": (_I, [_P, _V, _V, _V, _V, _F, _F, _V, _V]),
+    "fl_framelet_shrink": (_I, [_P, _V, _V, _F, _V]),
+    "fl_sb_solve": (_I, [_P, _V, _V, _F, _F, _I, _I, _D, _I, _I, _I, _V, _V]),
+    # batched fan slices
+    "fl_batch_create": (_I, [C.POINTER(_P), C.c_int32, C.POINTER(_P)]),
+    "fl_batch_destroy": (None, [_P]),
+    "fl_batch_layout": (_I, [_P, _V, _V]),
+    "fl_batch_forward": (_I, [_P, _V, _V, _V]),
+    "fl_batch_adjoint": (_I, [_P, _V, _V, _V]),
+    "fl_batch_cgls": (_I, [_P, _V, _V, _F, C.c_int32, _D, C.c_int32, _V, _V, _V]),
 }
+
+
+class _Checked:
+    """The loaded library. Only functions with a signature in _SIGS can be
+    reached: a ctypes call without argtypes would pass 64-bit device
+    pointers as 32-bit C ints."""
+
+    def __init__(self, cdll):
+        self._cdll = cdll
+
+    def __getattr__(self, name):
+        if name not in _SIGS:
+            raise AttributeError(f"{name}: no signature registered in framelab_gb300._lib")
+        return getattr(self._cdll, name)
 
 
 def lib_path() -> str:
@@ -92,7 +131,7 @@ def load(build_if_missing: bool = True):
                 fn = getattr(lib, name)
                 fn.restype = res
                 fn.argtypes = args
-            _lib = lib
+            _lib = _Checked(lib)
         return _lib
 
 
@@ -100,7 +139,7 @@ def declare(name, restype, argtypes):
     """Register the signature of an additional exported symbol."""
     _SIGS[name] = (restype, argtypes)
     if _lib is not None:
-        fn = getattr(_lib, name)
+        fn = getattr(_lib._cdll, name)
         fn.restype = restype
         fn.argtypes = argtypes
 

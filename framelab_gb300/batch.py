@@ -21,15 +21,6 @@ import torch
 from . import _lib
 from .projector import Plan
 
-_lib.declare("fl_batch_create", C.c_int, [C.POINTER(C.c_void_p), C.c_int32,
-                                          C.POINTER(C.c_void_p)])
-_lib.declare("fl_batch_destroy", None, [C.c_void_p])
-_lib.declare("fl_batch_layout", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p])
-_lib.declare("fl_batch_forward", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p])
-_lib.declare("fl_batch_adjoint", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p])
-_lib.declare("fl_batch_cgls", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_int32,
-                                        C.c_double, C.c_int32, C.c_void_p, C.c_void_p,
-                                        C.c_void_p])
 ZERO_START = 1
 
 

@@ -40,10 +40,6 @@ from . import geometry as G
 from .projector import Plan
 from .transforms import FrameletSystem as _NativeFramelets
 
-_lib.declare("fl_axpby", C.c_int, [C.c_void_p, C.c_void_p, C.c_float, C.c_float, C.c_int64,
-                                   C.c_void_p])
-_lib.declare("fl_framelet_shrink", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_float,
-                                             C.c_void_p])
 
 
 def _stream():

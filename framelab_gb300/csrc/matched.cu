@@ -223,48 +223,25 @@ k_adj_fan(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __re
 // (A_z increasing in k); MODE -1: below, every such ray falls; MODE 0: the run
 // straddles the source plane (general min/max). The other orientation's rays
 // get w <= 0 from the specialised formula, as they miss the run.
-// MIRROR: rows are limited to the walked half (nb here is nb/2), ycol points
-// into the folded sinogram (pairs of rows ib and nb-1-ib, row stride 2*na) and
-// every weight also carries the mirrored ray into the mirrored voxel's
-// accumulator accm[k].
-template <int MODE, int TZ, bool MIRROR>
-__device__ __forceinline__ void adj_rows(float (&acc)[TZ], float (&accm)[TZ], int nk, int z0,
-                                         float l, float h, float e1, float e2, float s1,
-                                         float s2, const float2* __restrict__ rv,
+template <int MODE, int TZ>
+__device__ __forceinline__ void adj_rows(float (&acc)[TZ], int nk, int z0, float l, float h,
+                                         float e1, float e2, float s1, float s2,
+                                         const float2* __restrict__ rv,
                                          const float* __restrict__ ycol, int na, int nb)
 {
-    // MIRROR with MODE -1 (every run of the lower half except the one at the
-    // source plane): the rays descend and the row grid rises (dv > 0 for any
-    // z-mirror plan), so e1 <= e2 at every plane and both grow with k; voxel
-    // k's rows are then [e1(k), e2(k + 1)] without per-plane min / max
-    constexpr bool DESC = MIRROR && MODE < 0;
     float mn = fminf(e1, e2), mx = fmaxf(e1, e2);   // row span at plane k
-    float lo_e = e1 - 0.02f, hi_e = e2 + s2 + 0.02f;
 #pragma unroll
     for (int k = 0; k < TZ; k++) {
         if (k >= nk) break;
-        int blo, bhi;
-        if (DESC) {
-            blo = max(__float2int_ru(lo_e), 0);
-            bhi = min(__float2int_rd(hi_e), nb - 1);
-            lo_e += s1; hi_e += s2;
-        } else {
-            e1 += s1; e2 += s2;
-            const float mn1 = fminf(e1, e2), mx1 = fmaxf(e1, e2);   // plane k + 1
-            blo = max(__float2int_ru(fminf(mn, mn1) - 0.02f), 0);
-            bhi = min(__float2int_rd(fmaxf(mx, mx1) + 0.02f), nb - 1);
-            mn = mn1; mx = mx1;
-        }
+        e1 += s1; e2 += s2;
+        const float mn1 = fminf(e1, e2), mx1 = fmaxf(e1, e2);   // plane k + 1
+        const int blo = max(__float2int_ru(fminf(mn, mn1) - 0.02f), 0);
+        const int bhi = min(__float2int_rd(fmaxf(mx, mx1) + 0.02f), nb - 1);
+        mn = mn1; mx = mx1;
         const float fk0 = (float)(z0 + k), fk1 = (float)(z0 + k + 1);
         for (int ib = blo; ib <= bhi; ib++) {
             const float2 re = rv[ib];                 // (inv_z, off_z) of row ib
-            float yval, ym = 0.0f;
-            if (MIRROR) {
-                const float2 t = Store<float>::ld2(ycol + 2 * (long long)ib * na);
-                yval = t.x; ym = t.y;
-            } else {
-                yval = __ldg(ycol + (long long)ib * na);
-            }
+            const float yval = __ldg(ycol + (long long)ib * na);
             const float az0 = fmaf(fk0, re.x, re.y);
             const float az1 = fmaf(fk1, re.x, re.y);
             float l2, h2;
@@ -272,9 +249,54 @@ __device__ __forceinline__ void adj_rows(float (&acc)[TZ], float (&accm)[TZ], in
             else if (MODE < 0) { l2 = fmaxf(l, az1); h2 = fminf(h, az0); }
             else { l2 = fmaxf(l, fminf(az0, az1)); h2 = fminf(h, fmaxf(az0, az1)); }
             // w <= 0 (the ray misses voxel k) adds exactly 0 for finite y
+            acc[k] = fmaf(fmaxf(h2 - l2, 0.0f), yval, acc[k]);
+        }
+    }
+}
+
+// z-mirror form: rows limited to the walked half (nb here is nb/2); ycol
+// points into the folded sinogram (pairs of rows ib and nb-1-ib, row stride
+// 2*na); acc[k] holds the voxel k and its mirror, both updated by one paired
+// FMA (per lane the same rounding as fmaf). MODE -1 (every lower run except
+// the one at the source plane): the rays descend and the row grid rises
+// (dv > 0 for any z-mirror plan), so e1 <= e2 at every plane and both grow
+// with k; voxel k's rows are then [e1(k), e2(k + 1)] without per-plane
+// min / max. MODE 0: the general window. (MODE +1 does not occur: every run
+// of the lower half lies below the source.)
+template <int MODE, int TZ>
+__device__ __forceinline__ void adj_rows_pair(float2 (&acc)[TZ], int nk, int z0, float l,
+                                              float h, float e1, float e2, float s1, float s2,
+                                              const float2* __restrict__ rv,
+                                              const float* __restrict__ ycol, int na, int nb)
+{
+    float mn = fminf(e1, e2), mx = fmaxf(e1, e2);
+    float lo_e = e1 - 0.02f, hi_e = e2 + s2 + 0.02f;
+#pragma unroll
+    for (int k = 0; k < TZ; k++) {
+        if (k >= nk) break;
+        int blo, bhi;
+        if (MODE < 0) {
+            blo = max(__float2int_ru(lo_e), 0);
+            bhi = min(__float2int_rd(hi_e), nb - 1);
+            lo_e += s1; hi_e += s2;
+        } else {
+            e1 += s1; e2 += s2;
+            const float mn1 = fminf(e1, e2), mx1 = fmaxf(e1, e2);
+            blo = max(__float2int_ru(fminf(mn, mn1) - 0.02f), 0);
+            bhi = min(__float2int_rd(fmaxf(mx, mx1) + 0.02f), nb - 1);
+            mn = mn1; mx = mx1;
+        }
+        const float fk0 = (float)(z0 + k), fk1 = (float)(z0 + k + 1);
+        for (int ib = blo; ib <= bhi; ib++) {
+            const float2 re = rv[ib];
+            const float2 t = Store<float>::ld2(ycol + 2 * (long long)ib * na);
+            const float2 az = __ffma2_rn(make_float2(fk0, fk1), make_float2(re.x, re.x),
+                                         make_float2(re.y, re.y));
+            float l2, h2;
+            if (MODE < 0) { l2 = fmaxf(l, az.y); h2 = fminf(h, az.x); }
+            else { l2 = fmaxf(l, fminf(az.x, az.y)); h2 = fminf(h, fmaxf(az.x, az.y)); }
             const float w = fmaxf(h2 - l2, 0.0f);
-            acc[k] = fmaf(w, yval, acc[k]);
-            if (MIRROR) accm[k] = fmaf(w, ym, accm[k]);
+            acc[k] = __ffma2_rn(make_float2(w, w), t, acc[k]);
         }
     }
 }
@@ -299,9 +321,10 @@ k_adj_cone(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __r
     const int nbw = MIRROR ? nb / 2 : nb;      // rows evaluated
     const int nk = min(TZ, nzw - z0);          // voxels of this run inside that range
     if (ix >= nx || iy >= ny) return;
-    float acc[TZ], accm[TZ];
+    float acc[TZ];                 // general form
+    float2 acc2[TZ];               // mirror form: (voxel, mirrored voxel)
 #pragma unroll
-    for (int k = 0; k < TZ; k++) { acc[k] = 0.0f; accm[k] = 0.0f; }
+    for (int k = 0; k < TZ; k++) { acc[k] = 0.0f; acc2[k] = make_float2(0.0f, 0.0f); }
     const float x0 = (float)(ix - nx / 2), y0 = (float)(iy - ny / 2);
     const float fx0 = (float)ix, fx1 = (float)(ix + 1), fy0 = (float)iy, fy1 = (float)(iy + 1);
     const float inv_dv = 1.0f / G.dv;
@@ -335,13 +358,21 @@ k_adj_cone(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __r
             const float r1 = __fdividef(1.0f, l + ve.ac), r2 = __fdividef(1.0f, h + ve.ac);
             const float s1 = dz * r1 * inv_dv, s2 = dz * r2 * inv_dv;
             const float e1 = (zr0 * r1 - G.v0) * inv_dv, e2 = (zr0 * r2 - G.v0) * inv_dv;
-            const float* ycol = MIRROR ? yv + 2 * ia : yv + ia;
-            if (mode > 0)
-                adj_rows<1, TZ, MIRROR>(acc, accm, nk, z0, l, h, e1, e2, s1, s2, rv, ycol, na, nbw);
-            else if (mode < 0)
-                adj_rows<-1, TZ, MIRROR>(acc, accm, nk, z0, l, h, e1, e2, s1, s2, rv, ycol, na, nbw);
-            else
-                adj_rows<0, TZ, MIRROR>(acc, accm, nk, z0, l, h, e1, e2, s1, s2, rv, ycol, na, nbw);
+            if (MIRROR) {
+                const float* ycol = yv + 2 * ia;
+                if (mode < 0)
+                    adj_rows_pair<-1, TZ>(acc2, nk, z0, l, h, e1, e2, s1, s2, rv, ycol, na, nbw);
+                else
+                    adj_rows_pair<0, TZ>(acc2, nk, z0, l, h, e1, e2, s1, s2, rv, ycol, na, nbw);
+            } else {
+                const float* ycol = yv + ia;
+                if (mode > 0)
+                    adj_rows<1, TZ>(acc, nk, z0, l, h, e1, e2, s1, s2, rv, ycol, na, nbw);
+                else if (mode < 0)
+                    adj_rows<-1, TZ>(acc, nk, z0, l, h, e1, e2, s1, s2, rv, ycol, na, nbw);
+                else
+                    adj_rows<0, TZ>(acc, nk, z0, l, h, e1, e2, s1, s2, rv, ycol, na, nbw);
+            }
         }
     }
     const long long frame = (long long)it * nx * ny * nz, col_ = (long long)iy * nx + ix;
@@ -349,13 +380,14 @@ k_adj_cone(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __r
     for (int k = 0; k < TZ; k++)
         if (k < nk) {
             if (MIRROR && xfold) {
-                Store<TX>::st2(X + frame + 2 * ((long long)(z0 + k) * nx * ny + col_), acc[k],
-                               accm[k]);
+                Store<TX>::st2(X + frame + 2 * ((long long)(z0 + k) * nx * ny + col_),
+                               acc2[k].x, acc2[k].y);
+            } else if (MIRROR) {
+                Store<TX>::st(X + frame + (long long)(z0 + k) * nx * ny + col_, acc2[k].x);
+                Store<TX>::st(X + frame + (long long)(nz - 1 - z0 - k) * nx * ny + col_,
+                              acc2[k].y);
             } else {
                 Store<TX>::st(X + frame + (long long)(z0 + k) * nx * ny + col_, acc[k]);
-                if (MIRROR)
-                    Store<TX>::st(X + frame + (long long)(nz - 1 - z0 - k) * nx * ny + col_,
-                                  accm[k]);
             }
         }
 }

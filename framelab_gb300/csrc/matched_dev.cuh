@@ -80,17 +80,15 @@ __device__ __forceinline__ float walk(const TX* __restrict__ x, float inv_x, flo
     float nAx = fmaf(pax, inv_x, off_x);
     float nAy = fmaf(pay, inv_y, off_y);
     float nAz = THREE ? fmaf(paz, inv_z, off_z) : 3.0e38f;
-    float cur = a_in, acc = 0.0f, am = 0.0f;
+    float cur = a_in, acc = 0.0f;
+    float2 acc2 = make_float2(0.0f, 0.0f);   // MIRROR: (voxel, mirror) sums, paired FMA
     int cnt = 0;
     // the gather of the next voxel is issued as soon as its index is known and
     // consumed one step later, so its latency overlaps the next step's compares
-    float xv = 0.0f, xm = 0.0f;
-    if (MIRROR) {
-        const float2 t = Store<TX>::ld2(x + 2 * (long long)v);
-        xv = t.x; xm = t.y;
-    } else if (!COUNT) {
-        xv = ldv(x + v);
-    }
+    float xv = 0.0f;
+    float2 xv2 = make_float2(0.0f, 0.0f);
+    if (MIRROR) xv2 = Store<TX>::ld2(x + 2 * (long long)v);
+    else if (!COUNT) xv = ldv(x + v);
     const int budget = nx + ny + (THREE ? nz : 0) + 4;
     for (int it = 0; it < budget; it += 4) {
 #pragma unroll
@@ -98,30 +96,27 @@ __device__ __forceinline__ float walk(const TX* __restrict__ x, float inv_x, flo
             const float nxt = THREE ? fminf(fminf(nAx, nAy), nAz) : fminf(nAx, nAy);
             const float seg = nxt - cur;
             const bool cont = nxt < a_out;          // false at the exit (and for NaN)
-            float xn = 0.0f, xmn = 0.0f;
+            float xn = 0.0f;
+            float2 xn2 = make_float2(0.0f, 0.0f);
             if (cont) {
                 if (nAx == nxt) { pax += stx; v += dvx; nAx = fmaf(pax, inv_x, off_x); }
                 if (nAy == nxt) { pay += sty; v += dvy; nAy = fmaf(pay, inv_y, off_y); }
                 if (THREE && nAz == nxt) { paz += stz; v += dvz; nAz = fmaf(paz, inv_z, off_z); }
-                if (MIRROR) {                        // v is inside the folded volume here
-                    const float2 t = Store<TX>::ld2(x + 2 * (long long)v);
-                    xn = t.x; xmn = t.y;
-                } else if (!COUNT) {
-                    xn = ldv(x + v);                 // v is inside the volume here
-                }
+                if (MIRROR) xn2 = Store<TX>::ld2(x + 2 * (long long)v);  // inside the folded volume
+                else if (!COUNT) xn = ldv(x + v);                         // inside the volume
             }
             if (COUNT) cnt += (seg > 0.0f);
+            else if (MIRROR) acc2 = __ffma2_rn(make_float2(seg, seg), xv2, acc2);
             else acc = fmaf(seg, xv, acc);
-            if (MIRROR) am = fmaf(seg, xm, am);
             if (!cont) goto done;
             xv = xn;
-            xm = xmn;
+            xv2 = xn2;
             cur = nxt;
         }
     }
 done:
     if (COUNT) *nseg = cnt;
-    if (MIRROR) *accm = am;
+    if (MIRROR) { *accm = acc2.y; return acc2.x; }
     return acc;
 }
 

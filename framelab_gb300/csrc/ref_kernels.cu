@@ -553,12 +553,15 @@ k_ref_fan_gao(const float* __restrict__ X, float* __restrict__ y,
         if (c2 == c1) {
             if (c1 >= 0 && c1 <= ns - 1) acc = fadd(acc, fmul(l, PIX(c1)));
         } else if (c2 > 0 && c2 < ns) {
-            acc = fadd(acc, fmul(fmul(fdiv(fsub((float)c2, p1), d), l), PIX(c1)));
+            // the reference reads x outside the image when the two crossings round
+            // more than a pixel apart (c1 < 0, Ax_fan_mf_cpu_new.cpp:60-63): skipped
+            if (c1 >= 0) acc = fadd(acc, fmul(fmul(fdiv(fsub((float)c2, p1), d), l), PIX(c1)));
             acc = fadd(acc, fmul(fmul(fdiv(fsub(p2, (float)c2), d), l), PIX(c2)));
         } else {
             if (c2 == 0) acc = fadd(acc, fmul(fmul(fdiv(fsub(p2, (float)c2), d), l), PIX(c2)));
             // the reference tests c2 == ny on both branches (Ax_fan_mf_cpu_new.cpp:70,111)
-            if (c2 == ny) acc = fadd(acc, fmul(fmul(fdiv(fsub((float)c2, p1), d), l), PIX(c1)));
+            if (c2 == ny && c1 >= 0 && c1 < ns)
+                acc = fadd(acc, fmul(fmul(fdiv(fsub((float)c2, p1), d), l), PIX(c1)));
         }
 #undef PIX
     }

@@ -15,17 +15,6 @@ import torch
 
 from . import _lib
 
-_lib.declare("fl_dot", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p])
-_lib.declare("fl_normal_apply", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_float,
-                                          C.c_void_p])
-_lib.declare("fl_cgls_create", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)])
-_lib.declare("fl_cgls_destroy", None, [C.c_void_p])
-_lib.declare("fl_cgls_solve", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_int,
-                                        C.c_double, C.c_int, C.c_int, C.c_void_p,
-                                        C.POINTER(C.c_int), C.c_void_p])
-_lib.declare("fl_cgls_solve_host", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_float,
-                                             C.c_int, C.c_double, C.c_int, C.c_int, C.c_void_p,
-                                             C.POINTER(C.c_int), C.c_void_p])
 MODES = {"plain": 0, "mixed": 1, "graph": 2}
 ZERO_START = 1
 

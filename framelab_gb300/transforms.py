@@ -17,15 +17,6 @@ import torch
 from . import _lib
 
 _V = C.c_void_p
-_lib.declare("fl_framelet_create", C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
-                                             C.POINTER(_V)])
-_lib.declare("fl_framelet_destroy", None, [_V])
-_lib.declare("fl_framelet_ncoef", C.c_int64, [_V])
-_lib.declare("fl_framelet_analysis", C.c_int, [_V, _V, _V, _V])
-_lib.declare("fl_framelet_synthesis", C.c_int, [_V, _V, _V, _V])
-_lib.declare("fl_framelet_bregman", C.c_int, [_V, _V, _V, _V, _V, C.c_float, C.c_float, _V, _V])
-_lib.declare("fl_sb_solve", C.c_int, [_V, _V, _V, C.c_float, C.c_float, C.c_int, C.c_int,
-                                      C.c_double, C.c_int, C.c_int, C.c_int, _V, _V])
 KINDS = {"haar": 0, "linear": 1, "cubic": 3}
 
 

@@ -760,14 +760,16 @@ void orc_fan_gao_f32(const float *X, float *y, float SO, float OD, float scale, 
                     }
                 } else if (c2 > 0 && c2 < ns) {
                     float d = p2 - p1, l = sqrtf(d * d + 1);
-                    acc += ((c2 - p1) / d) * l * PIX(c1);
+                    /* c1 < 0 (crossings rounded more than a pixel apart): the
+                       reference reads outside the image here; the term is skipped */
+                    if (c1 >= 0) acc += ((c2 - p1) / d) * l * PIX(c1);
                     acc += ((p2 - c2) / d) * l * PIX(c2);
                 } else {
                     if (c2 == 0) {
                         float d = p2 - p1, l = sqrtf(d * d + 1);
                         acc += ((p2 - c2) / d) * l * PIX(c2);
                     }
-                    if (c2 == (xdom ? ny : nedge)) {
+                    if (c2 == (xdom ? ny : nedge) && c1 >= 0 && c1 < ns) {
                         float d = p2 - p1, l = sqrtf(d * d + 1);
                         acc += ((c2 - p1) / d) * l * PIX(c1);
                     }
