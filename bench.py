@@ -664,6 +664,23 @@ def run_sb(ctx, name, w, p):
         tf, ta, _, _ = time_pair(ctx, P, (u / (u.abs().max() + 1e-30)).contiguous())
         roofline = projector_roofline(ctx, name, n_isect, P.n_rays, P.n_vox, tf, ta, detail,
                                       "matched")
+        # one framelet step of the outer loop (analysis with shrink and Bregman
+        # update, synthesis into b), against its compulsory bytes: u read, b
+        # written, v read and written, t written and read back
+        from framelab_gb300.transforms import FrameletSystem
+        fw = FrameletSystem((w["n"],) * 3, "linear", w["levels"])
+        v = torch.zeros(fw.ncoef, device=ctx.dev)
+        t = torch.empty_like(v)
+        bb = torch.empty_like(u)
+        fw.bregman(u, v, t, None, w["mu"], w["lam"] / w["mu"], bb)
+        reps = 3
+        _, tfw = ctx.timed(lambda: [fw.bregman(u, v, t, None, w["mu"], w["lam"] / w["mu"], bb)
+                                    for _ in range(reps)])
+        tfw /= reps
+        fb = 4 * (2 * P.n_vox + 4 * fw.ncoef)
+        detail.update(framelet_step_ms=tfw * 1e3, framelet_compulsory_GBps=fb / tfw / 1e9,
+                      framelet_ncoef=fw.ncoef)
+        del v, t, bb, fw
     # setup: A^T f (weighting + gather) and W u0 (3 per level); per outer iteration:
     # warm-start residual (fwd, adj, axpy) + init, inner x (fwd, adj, 3 updates),
     # Bregman analysis + synthesis (3 + 3 per level), |u_k - u_{k-1}| (diff, 2 dots)

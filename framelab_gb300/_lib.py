@@ -71,6 +71,8 @@ _SIGS = {
     "Atx_cone_mf_gpu_new": (None, [_V, _V, _V, _V, _V, _V, _V, _V, _V, _F, _F, _F, _F, _F, _F,
                                    _F, _I, _I, _I, _I, _I, _I, _I, _I, _I]),
     "fl_adjoint_noalloc": (_I, [_P, _V, _I, _V, _I, _V]),
+    "fl_debug_bounds": (_I, [C.POINTER(_I64), _I]),
+    "fl_debug_fail_alloc": (None, [_I64]),
     # vector algebra and CGLS
     "fl_dot": (_I, [_V, _V, _I64, _V, _V]),
     "fl_axpby": (_I, [_V, _V, _F, _F, _I64, _V]),
@@ -112,8 +114,13 @@ class _Checked:
         return getattr(self._cdll, name)
 
 
+# FRAMELAB_GB300_VARIANT selects a build variant of the library for this
+# process ("checked": bounds-checked gathers, framelab_gb300.build.VARIANTS)
+_VARIANT = os.environ.get("FRAMELAB_GB300_VARIANT", "")
+
+
 def lib_path() -> str:
-    return _build.OUT
+    return _build.variant_path(_VARIANT)
 
 
 def load(build_if_missing: bool = True):
@@ -121,9 +128,9 @@ def load(build_if_missing: bool = True):
     global _lib
     with _lock:
         if _lib is None:
-            path = _build.OUT
+            path = _build.variant_path(_VARIANT)
             if build_if_missing:
-                path = _build.build()
+                path = _build.build(variant=_VARIANT)
             if not os.path.exists(path):
                 raise FLError(FL_ERR_CUDA, f"{path} not built; run framelab_gb300.build.build()")
             lib = C.CDLL(path)

@@ -48,21 +48,37 @@ def _digest(paths) -> str:
     return h.hexdigest()
 
 
-def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
-    os.makedirs(BUILD, exist_ok=True)
-    stamp = os.path.join(BUILD, "stamp")
+# build variants: name -> (library file, object directory, extra nvcc flags)
+VARIANTS = {
+    "": (OUT, BUILD, ()),
+    # every gather of the fast kernels checks its index, skips an access out of
+    # range and counts it (fl_debug_bounds)
+    "checked": (os.path.join(HERE, "libframelab_gb300_checked.so"), BUILD + "_checked",
+                ("-DFL_BOUNDS_CHECK",)),
+}
+
+
+def variant_path(variant: str = "") -> str:
+    return VARIANTS[variant][0]
+
+
+def build(force: bool = False, verbose: bool = False, extra_flags=(), variant: str = "") -> str:
+    out, bdir, vflags = VARIANTS[variant]
+    extra_flags = (*vflags, *extra_flags)
+    os.makedirs(bdir, exist_ok=True)
+    stamp = os.path.join(bdir, "stamp")
     srcs = _sources()
     dig = _digest(srcs) + ":" + " ".join(extra_flags)
-    if not force and os.path.exists(OUT) and os.path.exists(stamp):
+    if not force and os.path.exists(out) and os.path.exists(stamp):
         with open(stamp) as f:
             if f.read() == dig:
-                return OUT
+                return out
     nvcc = _nvcc()
     common = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC,
               *ARCH, *extra_flags]
 
     def compile_one(src):
-        obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+        obj = os.path.join(bdir, os.path.basename(src) + ".o")
         cmd = [nvcc, *common, "-c", src, "-o", obj]
         if src.endswith(".cu"):
             cmd[1:1] = ["-Xptxas", "-warn-spills", "--expt-relaxed-constexpr"]
@@ -75,16 +91,16 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
 
     with ThreadPoolExecutor(max(1, min(len(srcs), os.cpu_count() or 4))) as ex:
         objs = list(ex.map(compile_one, srcs))
-    tmp = OUT + ".tmp"
+    tmp = out + ".tmp"
     link = [nvcc, "-shared", *ARCH, "-cudart", "shared", "-o", tmp, *objs,
             "-Xlinker", f"-rpath,{_cuda_lib()}"]
     r = subprocess.run(link, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
-    os.replace(tmp, OUT)
+    os.replace(tmp, out)
     with open(stamp, "w") as f:
         f.write(dig)
-    return OUT
+    return out
 
 
 if __name__ == "__main__":

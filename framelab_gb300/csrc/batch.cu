@@ -26,6 +26,7 @@
 #include <numeric>
 #include <vector>
 
+#include "fl_trace.h"
 #include "fl_common.cuh"
 #include "fl_plan.h"
 #include "matched_dev.cuh"
@@ -116,7 +117,8 @@ k_batch_fwd(const float* __restrict__ X, float* __restrict__ Y,
     if (r >= b.na * b.nv) return;
     const ColEntry ce = b.col[r];
     float acc = walk<float, false, false>(X + b.xoff, ce.inv_x, ce.off_x, ce.inv_y, ce.off_y,
-                                          0.0f, 0.0f, b.nx, b.ny, 1, nullptr);
+                                          0.0f, 0.0f, b.nx, b.ny, 1, nullptr, nullptr,
+                                          (long long)b.nx * b.ny);
     float cr = ray_cr(b.scale, b.colr[r], 0.0f);
     float out = cr * acc;
     if (cr_power == 2) out = cr * out;
@@ -300,13 +302,14 @@ static void batch_free(fl_batch* b)
 template <typename T>
 static int upload_vec(T** d, const std::vector<T>& h)
 {
-    FL_CUDA(cudaMalloc((void**)d, sizeof(T) * (h.empty() ? 1 : h.size())));
+    FL_CUDA(fl_malloc((void**)d, sizeof(T) * (h.empty() ? 1 : h.size())));
     if (!h.empty()) FL_CUDA(cudaMemcpy(*d, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice));
     return FL_OK;
 }
 
 extern "C" int fl_batch_create(fl_plan* const* plans, int32_t n_plans, fl_batch** out)
 {
+    FL_RANGE("fl_batch_create");
     if (!plans || !out || n_plans < 1)
         return fl_set_error(FL_ERR_INVALID, "fl_batch_create: bad argument");
     *out = nullptr;
@@ -386,7 +389,7 @@ extern "C" int fl_batch_create(fl_plan* const* plans, int32_t n_plans, fl_batch*
     if (!st) st = upload_vec(&b->d_pix, pix);
     if (!st) st = upload_vec(&b->d_vec, vec);
     auto M = [&](void** ptr, size_t bytes) {
-        if (!st) st = fl_check_cuda(cudaMalloc(ptr, bytes), "cudaMalloc(batch)");
+        if (!st) st = fl_check_cuda(fl_malloc(ptr, bytes), "fl_malloc(batch)");
     };
     M((void**)&b->r, b->n_vox * 4); M((void**)&b->p, b->n_vox * 4); M((void**)&b->q, b->n_vox * 4);
     M((void**)&b->tmp, b->n_rays * 4);
@@ -436,6 +439,7 @@ static int batch_adj_w(fl_batch* b, const float* yw, float* x, const BatchScal* 
 
 extern "C" int fl_batch_forward(fl_batch* b, const float* x, float* y, void* stream)
 {
+    FL_RANGE("fl_batch_forward");
     if (!b || !x || !y) return fl_set_error(FL_ERR_INVALID, "fl_batch_forward: null argument");
     int st = batch_fwd(b, x, y, 1, nullptr, (cudaStream_t)stream);
     return st ? st : fl_set_error(FL_OK, "");
@@ -444,6 +448,7 @@ extern "C" int fl_batch_forward(fl_batch* b, const float* x, float* y, void* str
 // Uses the batch's sinogram scratch: calls on one batch are stream-ordered.
 extern "C" int fl_batch_adjoint(fl_batch* b, const float* y, float* x, void* stream)
 {
+    FL_RANGE("fl_batch_adjoint");
     if (!b || !x || !y) return fl_set_error(FL_ERR_INVALID, "fl_batch_adjoint: null argument");
     cudaStream_t s = (cudaStream_t)stream;
     k_batch_weight<<<b->n_ray_chunks, kRayChunk, 0, s>>>(b->tmp, y, b->d_sl, b->d_rays);
@@ -470,6 +475,7 @@ extern "C" int fl_batch_cgls(fl_batch* b, const float* rhs, float* u, float lam,
                              double tol, int32_t flags, double* gamma_history,
                              int32_t* iters_done, void* stream)
 {
+    FL_RANGE("fl_batch_cgls");
     if (!b || !rhs || !u || iters < 0)
         return fl_set_error(FL_ERR_INVALID, "fl_batch_cgls: bad argument");
     cudaStream_t us = (cudaStream_t)stream, s = b->cs;
@@ -520,3 +526,5 @@ extern "C" int fl_batch_cgls(fl_batch* b, const float* rhs, float* u, float lam,
     }
     return fl_set_error(FL_OK, "");
 }
+
+FL_OOB_ACCESSOR(fl_oob_batch)

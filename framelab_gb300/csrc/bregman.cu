@@ -2,6 +2,7 @@
 // native CGLS and the fused framelet step; everything stays on the device.
 #include <cmath>
 
+#include "fl_trace.h"
 #include "fl_common.cuh"
 #include "fl_plan.h"
 
@@ -24,6 +25,7 @@ extern "C" int fl_sb_solve(fl_plan* plan, const float* f, float* u, float lam, f
                            int outer, int cg_iters, double cg_tol, int levels, int kind, int mode,
                            double* history, void* stream)
 {
+    FL_RANGE("fl_sb_solve");
     if (!plan || !f || !u || outer < 0 || cg_iters < 0 || !(mu > 0))
         return fl_set_error(FL_ERR_INVALID, "fl_sb_solve: bad argument");
     cudaStream_t s = (cudaStream_t)stream;
@@ -37,7 +39,7 @@ extern "C" int fl_sb_solve(fl_plan* plan, const float* f, float* u, float lam, f
     const long long nc = fl_framelet_ncoef(fw);
     DevMem Atf, b, v, t, prev, dsum;
     auto alloc = [&](DevMem& m, size_t bytes) {
-        return st ? st : (st = fl_check_cuda(cudaMalloc(&m.p, bytes), "cudaMalloc(split Bregman)"));
+        return st ? st : (st = fl_check_cuda(fl_malloc(&m.p, bytes), "fl_malloc(split Bregman)"));
     };
     alloc(Atf, n * 4); alloc(b, n * 4); alloc(v, nc * 4); alloc(t, nc * 4); alloc(prev, n * 4);
     alloc(dsum, 2 * sizeof(double));

@@ -18,6 +18,7 @@
 #include <new>
 #include <vector>
 
+#include "fl_trace.h"
 #include "fl_common.cuh"
 #include "fl_plan.h"
 
@@ -269,8 +270,8 @@ extern "C" int fl_dot(const float* a, const float* b, int64_t n, double* out, vo
         if (d.partials) cudaFree(d.partials);
         if (d.ticket) cudaFree(d.ticket);
         d.partials = nullptr; d.ticket = nullptr; d.cap = 0;
-        FL_CUDA(cudaMalloc((void**)&d.partials, sizeof(double) * 4 * sm_count()));
-        FL_CUDA(cudaMalloc((void**)&d.ticket, sizeof(unsigned)));
+        FL_CUDA(fl_malloc((void**)&d.partials, sizeof(double) * 4 * sm_count()));
+        FL_CUDA(fl_malloc((void**)&d.ticket, sizeof(unsigned)));
         FL_CUDA(cudaMemset(d.ticket, 0, sizeof(unsigned)));
         d.cap = 4 * sm_count();
     }
@@ -317,6 +318,7 @@ static void cgls_free(fl_cgls* c)
 
 extern "C" int fl_cgls_create(fl_plan* plan, int mode, fl_cgls** out)
 {
+    FL_RANGE("fl_cgls_create");
     if (!plan || !out) return fl_set_error(FL_ERR_INVALID, "fl_cgls_create: null argument");
     if (mode != FL_CGLS_PLAIN && mode != FL_CGLS_MIXED && mode != FL_CGLS_GRAPH)
         return fl_set_error(FL_ERR_INVALID, "unknown CGLS mode %d", mode);
@@ -331,7 +333,7 @@ extern "C" int fl_cgls_create(fl_plan* plan, int mode, fl_cgls** out)
     c->grid = grid_for(c->n);
     c->hist_cap = 4096;
     auto M = [&](void** ptr, size_t bytes) {
-        return st ? st : (st = fl_check_cuda(cudaMalloc(ptr, bytes), "cudaMalloc(cgls)"));
+        return st ? st : (st = fl_check_cuda(fl_malloc(ptr, bytes), "fl_malloc(cgls)"));
     };
     M((void**)&c->r, c->n * 4); M((void**)&c->p, c->n * 4); M((void**)&c->q, c->n * 4);
     M((void**)&c->tmp, c->nr * 4);
@@ -380,6 +382,7 @@ static int normal_apply(fl_cgls* c, const float* x, float* q, float lam, cudaStr
 
 extern "C" int fl_normal_apply(fl_plan* plan, const float* x, float* q, float lam, void* stream)
 {
+    FL_RANGE("fl_normal_apply");
     if (!plan || !x || !q) return fl_set_error(FL_ERR_INVALID, "fl_normal_apply: null argument");
     int st = fl_matched_ready(plan);
     if (st) return st;
@@ -476,9 +479,15 @@ static int solve_mixed(fl_cgls* c, const float* b, float* u, float lam, int iter
     int st;
     // layout of the workspace vectors follows the plan's current mirror option
     const int fold = c->plan->zmirror ? 1 : 0;
-    if (fold && !c->bf) {
-        FL_CUDA(cudaMalloc((void**)&c->bf, c->n * 4));
-        FL_CUDA(cudaMalloc((void**)&c->uf, c->n * 4));
+    if (fold && (!c->bf || !c->uf)) {        // both folded copies, or neither
+        int e = c->bf ? FL_OK : fl_check_cuda(fl_malloc((void**)&c->bf, c->n * 4), "fl_malloc(cgls)");
+        if (!e && !c->uf) e = fl_check_cuda(fl_malloc((void**)&c->uf, c->n * 4), "fl_malloc(cgls)");
+        if (e) {
+            if (c->bf) cudaFree(c->bf);
+            if (c->uf) cudaFree(c->uf);
+            c->bf = c->uf = nullptr;
+            return e;
+        }
     }
     if (fold != c->fold) { c->fold = fold; c->captured = false; }
     FL_CUDA(cudaEventRecord(c->ev0, us));
@@ -549,6 +558,7 @@ extern "C" int fl_cgls_solve(fl_cgls* c, const float* b, float* u, float lam, in
                              double tol, int refresh, int flags, double* gamma_history,
                              int* iters_done, void* stream)
 {
+    FL_RANGE("fl_cgls_solve");
     if (!c || !b || !u || iters < 0)
         return fl_set_error(FL_ERR_INVALID, "fl_cgls_solve: bad argument");
     int st = (c->mode == FL_CGLS_PLAIN)
@@ -564,12 +574,13 @@ extern "C" int fl_cgls_solve_host(fl_cgls* c, const float* b_host, float* u_host
                                   int iters, double tol, int refresh, int flags,
                                   double* gamma_history, int* iters_done, void* stream)
 {
+    FL_RANGE("fl_cgls_solve_host");
     if (!c || !b_host || !u_host || iters < 0)
         return fl_set_error(FL_ERR_INVALID, "fl_cgls_solve_host: bad argument");
     cudaStream_t s = (cudaStream_t)stream;
     size_t bytes = (size_t)c->n * sizeof(float);
-    if (!c->hb) FL_CUDA(cudaMalloc((void**)&c->hb, bytes));
-    if (!c->hu) FL_CUDA(cudaMalloc((void**)&c->hu, bytes));
+    if (!c->hb) FL_CUDA(fl_malloc((void**)&c->hb, bytes));
+    if (!c->hu) FL_CUDA(fl_malloc((void**)&c->hu, bytes));
     FL_CUDA(cudaMemcpyAsync(c->hb, b_host, bytes, cudaMemcpyHostToDevice, s));
     if (!(flags & FL_CGLS_ZERO_START))
         FL_CUDA(cudaMemcpyAsync(c->hu, u_host, bytes, cudaMemcpyHostToDevice, s));

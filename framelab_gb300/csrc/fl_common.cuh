@@ -71,9 +71,42 @@ template <> struct Store<__nv_bfloat16> {
 };
 
 // ---------------------------------------------------------------------------
+// Bounds-checked builds (-DFL_BOUNDS_CHECK). FL_IN(i, n) is true when
+// 0 <= i < n; otherwise it counts a violation in this translation unit's
+// counter and the caller skips the access. In normal builds it is the
+// constant true and costs nothing. FL_OOB_ACCESSOR(name) defines the host
+// function that reads (and optionally clears) the counter.
+// ---------------------------------------------------------------------------
+#if defined(FL_BOUNDS_CHECK) && defined(__CUDACC__)
+static __device__ unsigned long long fl_oob_count;
+__device__ __forceinline__ bool fl_in(long long i, long long n)
+{
+    if (i >= 0 && i < n) return true;
+    atomicAdd(&fl_oob_count, 1ULL);
+    return false;
+}
+#define FL_IN(i, n) fl_in((long long)(i), (long long)(n))
+#define FL_OOB_ACCESSOR(name)                                                         \
+    extern "C" unsigned long long name(int reset)                                     \
+    {                                                                                 \
+        unsigned long long v = 0, z = 0;                                              \
+        cudaMemcpyFromSymbol(&v, fl_oob_count, sizeof v);                             \
+        if (reset) cudaMemcpyToSymbol(fl_oob_count, &z, sizeof z);                    \
+        return v;                                                                     \
+    }
+#else
+#define FL_IN(i, n) true
+#define FL_OOB_ACCESSOR(name) \
+    extern "C" unsigned long long name(int) { return 0; }
+#endif
+
+// ---------------------------------------------------------------------------
 // Host-side status handling (fl_runtime.cpp).
 // ---------------------------------------------------------------------------
 int fl_set_error(int code, const char* fmt, ...);
+// Every device allocation of the library goes through fl_malloc, so a test can
+// make the n-th one fail (fl_debug_fail_alloc) and check the error paths.
+cudaError_t fl_malloc(void** p, size_t bytes);
 int fl_check_cuda(cudaError_t e, const char* what);
 int fl_check_launch(const char* what);
 #define FL_CUDA(call)                                                     \

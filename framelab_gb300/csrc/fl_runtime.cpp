@@ -1,5 +1,6 @@
 // fl_runtime.cpp -- host runtime: status, plans (geometry -> HBM tables),
 // projector dispatch and the reference-signature drop-ins.
+#include <atomic>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -9,6 +10,7 @@
 #include <new>
 #include <vector>
 
+#include "fl_trace.h"
 #include "fl_plan.h"
 #include "framelab_gb300.h"
 
@@ -39,6 +41,27 @@ int fl_check_cuda(cudaError_t e, const char* what)
 
 int fl_check_launch(const char* what) { return fl_check_cuda(cudaGetLastError(), what); }
 
+// Allocation failure injection: g_fail_countdown = n > 0 makes the n-th next
+// fl_malloc fail as an out-of-memory would (one shot).
+static std::atomic<long long> g_fail_countdown{0};
+
+extern "C" void fl_debug_fail_alloc(int64_t nth) { g_fail_countdown.store(nth > 0 ? nth : 0); }
+
+cudaError_t fl_malloc(void** p, size_t bytes)
+{
+    long long c = g_fail_countdown.load();
+    while (c > 0) {
+        if (g_fail_countdown.compare_exchange_weak(c, c - 1)) {
+            if (c == 1) {
+                *p = nullptr;
+                return cudaErrorMemoryAllocation;
+            }
+            break;
+        }
+    }
+    return cudaMalloc(p, bytes);
+}
+
 extern "C" int fl_last_status(void) { return g_status; }
 extern "C" const char* fl_last_error(void) { return g_msg; }
 extern "C" const char* fl_version(void) { return "framelab_gb300 1.0 (sm_103a)"; }
@@ -51,7 +74,7 @@ static int upload(T** dst, const T* src, size_t n)
 {
     *dst = nullptr;
     if (n == 0) return FL_OK;
-    int st = fl_check_cuda(cudaMalloc((void**)dst, n * sizeof(T)), "cudaMalloc(plan)");
+    int st = fl_check_cuda(fl_malloc((void**)dst, n * sizeof(T)), "fl_malloc(plan)");
     if (st) return st;
     return fl_check_cuda(cudaMemcpy(*dst, src, n * sizeof(T), cudaMemcpyHostToDevice),
                          "cudaMemcpy(plan)");
@@ -208,6 +231,7 @@ extern "C" int fl_plan_query(const fl_plan* p, int option, int* value)
 
 extern "C" int fl_plan_create(const fl_scan* scan, fl_plan** out)
 {
+    FL_RANGE("fl_plan_create");
     if (!scan || !out) return fl_set_error(FL_ERR_INVALID, "fl_plan_create: null argument");
     *out = nullptr;
     fl_scan s = *scan;
@@ -390,6 +414,7 @@ int fl_matched_ready(fl_plan* p)
 extern "C" int fl_forward(fl_plan* p, int model, const void* x, int xt, void* y, int yt,
                           void* stream)
 {
+    FL_RANGE("fl_forward");
     if (!p || !x || !y) return fl_set_error(FL_ERR_INVALID, "fl_forward: null argument");
     int st;
     if ((st = check_dtype(xt)) || (st = check_dtype(yt))) return st;
@@ -423,7 +448,7 @@ int fl_plan_vwork(fl_plan* p, size_t bytes, void** w)
         if (p->d_vwork) cudaFree(p->d_vwork);
         p->d_vwork = nullptr;
         p->vwork_bytes = 0;
-        int st = fl_check_cuda(cudaMalloc(&p->d_vwork, bytes), "cudaMalloc(volume scratch)");
+        int st = fl_check_cuda(fl_malloc(&p->d_vwork, bytes), "fl_malloc(volume scratch)");
         if (st) return st;
         p->vwork_bytes = bytes;
     }
@@ -438,8 +463,8 @@ int fl_plan_work(fl_plan* p, float** w)
         if (p->d_work) cudaFree(p->d_work);
         p->d_work = nullptr;
         p->work_elems = 0;
-        int st = fl_check_cuda(cudaMalloc((void**)&p->d_work, need * sizeof(float)),
-                               "cudaMalloc(adjoint scratch)");
+        int st = fl_check_cuda(fl_malloc((void**)&p->d_work, need * sizeof(float)),
+                               "fl_malloc(adjoint scratch)");
         if (st) return st;
         p->work_elems = need;
     }
@@ -450,6 +475,7 @@ int fl_plan_work(fl_plan* p, float** w)
 extern "C" int fl_adjoint(fl_plan* p, int model, const void* y, int yt, void* x, int xt,
                           void* stream)
 {
+    FL_RANGE("fl_adjoint");
     if (!p || !x || !y) return fl_set_error(FL_ERR_INVALID, "fl_adjoint: null argument");
     int st;
     if ((st = check_dtype(xt)) || (st = check_dtype(yt))) return st;
@@ -481,12 +507,14 @@ extern "C" int fl_adjoint(fl_plan* p, int model, const void* y, int yt, void* x,
 
 extern "C" int fl_forward_gao(fl_plan* p, const float* x, float* y, float* ynorm, void* stream)
 {
+    FL_RANGE("fl_forward_gao");
     if (!p || !x || !y) return fl_set_error(FL_ERR_INVALID, "fl_forward_gao: null argument");
     return fl_ref_gao_forward(p, x, y, ynorm, (cudaStream_t)stream);
 }
 
 extern "C" int fl_count_intersections(fl_plan* p, int32_t* counts, void* stream)
 {
+    FL_RANGE("fl_count_intersections");
     if (!p || !counts) return fl_set_error(FL_ERR_INVALID, "null argument");
     int st = fl_matched_ready(p);
     if (st) return st;
@@ -500,7 +528,7 @@ namespace {
 struct DevBuf {
     void* p = nullptr;
     ~DevBuf() { if (p) cudaFree(p); }
-    int alloc(size_t bytes) { return fl_check_cuda(cudaMalloc(&p, bytes ? bytes : 4), "cudaMalloc"); }
+    int alloc(size_t bytes) { return fl_check_cuda(fl_malloc(&p, bytes ? bytes : 4), "cudaMalloc"); }
 };
 struct PlanGuard {
     fl_plan* p = nullptr;
@@ -571,6 +599,7 @@ extern "C" void Ax_fan_mf_gpu_siddon(float* X, float* y, float SO, float OD, flo
                                      int ny, int nv, float* sd_phi, int nd, float* y_det,
                                      int* id_X, int nt)
 {
+    FL_RANGE("Ax_fan_mf_gpu_siddon");
     fl_scan s;
     std::memset(&s, 0, sizeof s);
     s.ndim = 2; s.nx = nx; s.ny = ny; s.nz = 1; s.nt = nt; s.nv = nv; s.na = nd; s.nb = 1;
@@ -585,6 +614,7 @@ extern "C" void Atx_fan_mf_gpu_new(float* x, float* Y, float SO, float OD, float
                                    float* cos_phi, float* sin_phi, float* cos_det,
                                    float* sin_det)
 {
+    FL_RANGE("Atx_fan_mf_gpu_new");
     fl_scan s;
     std::memset(&s, 0, sizeof s);
     s.ndim = 2; s.nx = nx; s.ny = ny; s.nz = 1; s.nt = nt; s.nv = nv; s.na = nd; s.nb = 1;
@@ -604,6 +634,7 @@ extern "C" void Ax_cone_mf_gpu_siddon(float* X, float* y, float* sd_phi, float* 
                                       float OD, float scale, float dz, int nx, int ny, int nz,
                                       int nt, int na, int nb, int nv, int tmp_size, int nv_block)
 {
+    FL_RANGE("Ax_cone_mf_gpu_siddon");
     (void)nv_block;
     fl_scan s;
     std::memset(&s, 0, sizeof s);
@@ -624,6 +655,7 @@ extern "C" void Atx_cone_mf_gpu_new(float* X, float* y, float* cos_phi, float* s
                                     float dz_det, float dz, int nx, int ny, int nz, int nt,
                                     int na, int nb, int nv, int tmp_size, int nv_block)
 {
+    FL_RANGE("Atx_cone_mf_gpu_new");
     (void)nv_block;
     fl_scan s;
     std::memset(&s, 0, sizeof s);
@@ -643,6 +675,7 @@ extern "C" void Ax_fan_mf_gpu_new(float* X, float* y, float SO, float OD, float 
                                   int ny, int nv, float* sd_phi, int nd, float* y_det,
                                   int* id_X, int nt)
 {
+    FL_RANGE("Ax_fan_mf_gpu_new");
     fl_scan s;
     std::memset(&s, 0, sizeof s);
     s.ndim = 2; s.nx = nx; s.ny = ny; s.nz = 1; s.nt = nt; s.nv = nv; s.na = nd; s.nb = 1;
@@ -656,6 +689,7 @@ extern "C" void Ax_cone_mf_gpu_new(float* X, float* y, float* yNorm, float* sd_p
                                    float OD, float scale, float dz, int nx, int ny, int nz,
                                    int nt, int na, int nb, int nv, int tmp_size, int nv_block)
 {
+    FL_RANGE("Ax_cone_mf_gpu_new");
     (void)nv_block;
     fl_scan s;
     std::memset(&s, 0, sizeof s);
@@ -674,6 +708,7 @@ extern "C" void Ax_fan_mf_gpu_new_fb(float* X, float* y, float SO, float OD, flo
                                      int ny, int nv, float* sd_phi, int nd, float* y_det,
                                      int* id_X, int nt, float dy_det)
 {
+    FL_RANGE("Ax_fan_mf_gpu_new_fb");
     fl_scan s;
     std::memset(&s, 0, sizeof s);
     s.ndim = 2; s.nx = nx; s.ny = ny; s.nz = 1; s.nt = nt; s.nv = nv; s.na = nd; s.nb = 1;
@@ -688,6 +723,7 @@ extern "C" void Atx_fan_mf_gpu_new_fb(float* x, float* Y, float SO, float OD, fl
                                       float* cos_phi, float* sin_phi, float* cos_det,
                                       float* sin_det)
 {
+    FL_RANGE("Atx_fan_mf_gpu_new_fb");
     fl_scan s;
     std::memset(&s, 0, sizeof s);
     s.ndim = 2; s.nx = nx; s.ny = ny; s.nz = 1; s.nt = nt; s.nv = nv; s.na = nd; s.nb = 1;

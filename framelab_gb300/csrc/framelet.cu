@@ -24,6 +24,7 @@
 #include <new>
 #include <vector>
 
+#include "fl_trace.h"
 #include "fl_common.cuh"
 
 namespace {
@@ -221,6 +222,7 @@ static void set_filters(fl_framelet* w, int kind)
 
 extern "C" int fl_framelet_create(int nx, int ny, int nz, int levels, int kind, fl_framelet** out)
 {
+    FL_RANGE("fl_framelet_create");
     if (!out || nx < 1 || ny < 1 || nz < 1 || levels < 1 || levels > 8)
         return fl_set_error(FL_ERR_INVALID, "fl_framelet_create: bad size or levels");
     if (kind != FL_FRAMELET_LINEAR && kind != FL_FRAMELET_HAAR && kind != FL_FRAMELET_CUBIC)
@@ -243,8 +245,8 @@ extern "C" int fl_framelet_create(int nx, int ny, int nz, int levels, int kind, 
     w->ncoef_bands = b;
     long long inter = (w->dim == 3) ? (w->nf + w->nf * w->nf) : w->nf;
     w->work_elems = (inter + 2) * w->N;   // pass intermediates + two low-band volumes
-    int st = fl_check_cuda(cudaMalloc((void**)&w->work, w->work_elems * sizeof(float)),
-                           "cudaMalloc(framelet)");
+    int st = fl_check_cuda(fl_malloc((void**)&w->work, w->work_elems * sizeof(float)),
+                           "fl_malloc(framelet)");
     if (st) { delete w; return st; }
     *out = w;
     return fl_set_error(FL_OK, "");
@@ -362,6 +364,7 @@ static int synthesis(fl_framelet* w, float* coef, float* out, const float* base,
 
 extern "C" int fl_framelet_analysis(fl_framelet* w, const float* u, float* coef, void* stream)
 {
+    FL_RANGE("fl_framelet_analysis");
     if (!w || !u || !coef) return fl_set_error(FL_ERR_INVALID, "fl_framelet_analysis: null argument");
     int st = analysis(w, u, coef, nullptr, 0, 0.0f, (cudaStream_t)stream);
     return st ? st : fl_set_error(FL_OK, "");
@@ -369,6 +372,7 @@ extern "C" int fl_framelet_analysis(fl_framelet* w, const float* u, float* coef,
 
 extern "C" int fl_framelet_synthesis(fl_framelet* w, const float* coef, float* u, void* stream)
 {
+    FL_RANGE("fl_framelet_synthesis");
     if (!w || !u || !coef) return fl_set_error(FL_ERR_INVALID, "fl_framelet_synthesis: null argument");
     int st = synthesis(w, const_cast<float*>(coef), u, nullptr, 1.0f, (cudaStream_t)stream);
     return st ? st : fl_set_error(FL_OK, "");
@@ -377,6 +381,7 @@ extern "C" int fl_framelet_synthesis(fl_framelet* w, const float* coef, float* u
 extern "C" int fl_framelet_bregman(fl_framelet* w, const float* u, float* v, float* t,
                                    const float* Atf, float mu, float tau, float* b, void* stream)
 {
+    FL_RANGE("fl_framelet_bregman");
     if (!w || !u || !v || !t || !b)
         return fl_set_error(FL_ERR_INVALID, "fl_framelet_bregman: null argument");
     cudaStream_t s = (cudaStream_t)stream;

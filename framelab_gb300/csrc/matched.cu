@@ -52,7 +52,8 @@ k_fwd_cone(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restr
     const TX* x = X + (long long)vframe[iv] * nper;
     float accm = 0.0f;
     float acc = walk<TX, true, false, MIRROR>(x, ce.inv_x, ce.off_x, ce.inv_y, ce.off_y,
-                                              re.inv_z, re.off_z, nx, ny, nz, nullptr, &accm);
+                                              re.inv_z, re.off_z, nx, ny, nz, nullptr, &accm,
+                                              nper);
     float cr = ray_cr(scale, colr[(long long)iv * na + ia], re.dz2);
     if (xscale) { acc *= *xscale; accm *= *xscale; }
     float out = cr * acc;
@@ -85,7 +86,7 @@ k_fwd_fan(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restri
     ColEntry ce = col[r];
     const TX* x = X + (long long)vframe[iv] * nper;
     float acc = walk<TX, false, false>(x, ce.inv_x, ce.off_x, ce.inv_y, ce.off_y, 0.0f, 0.0f,
-                                       nx, ny, 1, nullptr);
+                                       nx, ny, 1, nullptr, nullptr, nper);
     float cr = ray_cr(scale, colr[r], 0.0f);
     if (xscale) acc *= *xscale;
     float out = cr * acc;
@@ -240,6 +241,7 @@ __device__ __forceinline__ void adj_rows(float (&acc)[TZ], int nk, int z0, float
         mn = mn1; mx = mx1;
         const float fk0 = (float)(z0 + k), fk1 = (float)(z0 + k + 1);
         for (int ib = blo; ib <= bhi; ib++) {
+            if (!FL_IN(ib, nb)) continue;
             const float2 re = rv[ib];                 // (inv_z, off_z) of row ib
             const float yval = __ldg(ycol + (long long)ib * na);
             const float az0 = fmaf(fk0, re.x, re.y);
@@ -288,6 +290,7 @@ __device__ __forceinline__ void adj_rows_pair(float2 (&acc)[TZ], int nk, int z0,
         }
         const float fk0 = (float)(z0 + k), fk1 = (float)(z0 + k + 1);
         for (int ib = blo; ib <= bhi; ib++) {
+            if (!FL_IN(ib, nb)) continue;
             const float2 re = rv[ib];
             const float2 t = Store<float>::ld2(ycol + 2 * (long long)ib * na);
             const float2 az = __ffma2_rn(make_float2(fk0, fk1), make_float2(re.x, re.x),
@@ -345,6 +348,7 @@ k_adj_cone(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __r
         const float tol = 1e-3f * dz;
         const int mode = (zr0 >= tol) ? 1 : ((zr1 <= -tol) ? -1 : 0);
         for (int ia = alo; ia <= ahi; ia++) {
+            if (!FL_IN(ia, na)) continue;
             const ColEntry ce = cv[ia];
             const float ax0 = fmaf(fx0, ce.inv_x, ce.off_x), ax1 = fmaf(fx1, ce.inv_x, ce.off_x);
             const float ay0 = fmaf(fy0, ce.inv_y, ce.off_y), ay1 = fmaf(fy1, ce.inv_y, ce.off_y);
@@ -564,4 +568,23 @@ int fl_matched_count(fl_plan* p, int32_t* counts, cudaStream_t st)
     k_count<<<fl_div_up(nr, 128), 128, 0, st>>>(counts, p->d_col, p->d_row, s.nx, s.ny, s.nz,
                                                 s.na, s.nb, s.nv, s.ndim == 3);
     return fl_check_launch("intersection count");
+}
+
+// ---------------------------------------------------------------------------
+// Bounds-checked builds: violations counted by the matched and batched kernels
+// ---------------------------------------------------------------------------
+FL_OOB_ACCESSOR(fl_oob_matched)
+extern "C" unsigned long long fl_oob_batch(int reset);
+
+extern "C" int fl_debug_bounds(int64_t* violations, int reset)
+{
+    if (!violations) return fl_set_error(FL_ERR_INVALID, "fl_debug_bounds: null argument");
+#ifdef FL_BOUNDS_CHECK
+    FL_CUDA(cudaDeviceSynchronize());
+    *violations = (int64_t)(fl_oob_matched(reset) + fl_oob_batch(reset));
+    return fl_set_error(FL_OK, "");
+#else
+    *violations = 0;
+    return fl_set_error(FL_ERR_UNSUPPORTED, "library built without FL_BOUNDS_CHECK");
+#endif
 }

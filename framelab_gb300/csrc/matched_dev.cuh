@@ -41,10 +41,12 @@ __device__ __forceinline__ int start_slab(float a, float inv, float off, int n)
 // value goes to the return value and the mirror's, with the same segment
 // length, to *accm -- the companion ray of a scan symmetric about the source
 // plane (fl_plan::zmirror).
+// xlen: elements available at x (checked builds verify every gather index).
 template <typename TX, bool THREE, bool COUNT, bool MIRROR = false>
 __device__ __forceinline__ float walk(const TX* __restrict__ x, float inv_x, float off_x,
                                       float inv_y, float off_y, float inv_z, float off_z,
-                                      int nx, int ny, int nz, int* nseg, float* accm = nullptr)
+                                      int nx, int ny, int nz, int* nseg, float* accm = nullptr,
+                                      long long xlen = 0)
 {
     float ax0 = fmaf(0.0f, inv_x, off_x), ax1 = fmaf((float)nx, inv_x, off_x);
     float ay0 = fmaf(0.0f, inv_y, off_y), ay1 = fmaf((float)ny, inv_y, off_y);
@@ -87,8 +89,8 @@ __device__ __forceinline__ float walk(const TX* __restrict__ x, float inv_x, flo
     // consumed one step later, so its latency overlaps the next step's compares
     float xv = 0.0f;
     float2 xv2 = make_float2(0.0f, 0.0f);
-    if (MIRROR) xv2 = Store<TX>::ld2(x + 2 * (long long)v);
-    else if (!COUNT) xv = ldv(x + v);
+    if (MIRROR) { if (FL_IN(2 * (long long)v + 1, xlen)) xv2 = Store<TX>::ld2(x + 2 * (long long)v); }
+    else if (!COUNT) { if (FL_IN(v, xlen)) xv = ldv(x + v); }
     const int budget = nx + ny + (THREE ? nz : 0) + 4;
     for (int it = 0; it < budget; it += 4) {
 #pragma unroll
@@ -102,8 +104,9 @@ __device__ __forceinline__ float walk(const TX* __restrict__ x, float inv_x, flo
                 if (nAx == nxt) { pax += stx; v += dvx; nAx = fmaf(pax, inv_x, off_x); }
                 if (nAy == nxt) { pay += sty; v += dvy; nAy = fmaf(pay, inv_y, off_y); }
                 if (THREE && nAz == nxt) { paz += stz; v += dvz; nAz = fmaf(paz, inv_z, off_z); }
-                if (MIRROR) xn2 = Store<TX>::ld2(x + 2 * (long long)v);  // inside the folded volume
-                else if (!COUNT) xn = ldv(x + v);                         // inside the volume
+                // v is inside the (folded) volume here
+                if (MIRROR) { if (FL_IN(2 * (long long)v + 1, xlen)) xn2 = Store<TX>::ld2(x + 2 * (long long)v); }
+                else if (!COUNT) { if (FL_IN(v, xlen)) xn = ldv(x + v); }
             }
             if (COUNT) cnt += (seg > 0.0f);
             else if (MIRROR) acc2 = __ffma2_rn(make_float2(seg, seg), xv2, acc2);
@@ -198,6 +201,7 @@ __device__ __forceinline__ void fan_block_gather(float (&acc)[PY][PX],
         const ColEntry* cv = col + (long long)iv * na;
         const float* yv = yw + (long long)iv * na;
         for (int ia = lo; ia <= hi; ia++) {
+            if (!FL_IN(ia, na)) continue;
             const ColEntry ce = cv[ia];
             const float yval = __ldg(yv + ia);
             float ax[PX + 1], ay[PY + 1];

@@ -19,6 +19,7 @@
 // reads, and each call overwrites what the previous call left there.
 #include <mutex>
 
+#include "fl_trace.h"
 #include "fl_common.cuh"
 #include "fl_plan.h"
 
@@ -52,6 +53,7 @@ int scratch_for_current_device(float** out)
 extern "C" int fl_adjoint_noalloc(fl_plan* p, const void* y, int yt, void* x, int xt,
                                   void* stream)
 {
+    FL_RANGE("fl_adjoint_noalloc");
     if (!p || !x || !y) return fl_set_error(FL_ERR_INVALID, "fl_adjoint_noalloc: null argument");
     if ((xt != FL_F32 && xt != FL_F16 && xt != FL_BF16) ||
         (yt != FL_F32 && yt != FL_F16 && yt != FL_BF16))

@@ -323,6 +323,18 @@ int fl_batch_adjoint(fl_batch *b, const float *y, float *x, void *stream);
 int fl_batch_cgls(fl_batch *b, const float *rhs, float *u, float lam, int32_t iters, double tol,
                   int32_t flags, double *gamma_history, int32_t *iters_done, void *stream);
 
+/* Bounds-checked builds only (compiled with -DFL_BOUNDS_CHECK, the
+ * "checked" build variant): *violations = the number of gathers of the
+ * matched and batched kernels whose index fell outside its array since the
+ * last reset (each such access was skipped); reset = 1 clears the count.
+ * Normal builds return FL_ERR_UNSUPPORTED with *violations = 0. */
+int fl_debug_bounds(int64_t *violations, int reset);
+
+/* Failure injection for tests: the nth next device allocation of the library
+ * (1 = the next one) fails as an out-of-memory would, once; 0 disarms it.
+ * Every entry point then returns FL_ERR_ALLOC and releases what it held. */
+void fl_debug_fail_alloc(int64_t nth);
+
 #ifdef __cplusplus
 }
 #endif

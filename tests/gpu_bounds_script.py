@@ -1,0 +1,72 @@
+"""Runs every form of the matched projector pair, the batched fan kernels
+and the fused CGLS through the bounds-checked library (started with
+FRAMELAB_GB300_VARIANT=checked) and prints the number of out-of-range gathers
+the kernels counted. Used by tests/test_gpu_bounds.py."""
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+import torch
+
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+from framelab_gb300 import _lib  # noqa: E402
+from framelab_gb300 import geometry as G  # noqa: E402
+from framelab_gb300.batch import FanBatch  # noqa: E402
+from framelab_gb300.classes import DataTypes, Operators  # noqa: E402
+from framelab_gb300.projector import Plan  # noqa: E402
+from framelab_gb300.solvers import NativeCGLS  # noqa: E402
+
+
+def run_plan(p, rng):
+    P = Plan(p)
+    x = torch.from_numpy(rng.standard_normal(P.n_vox).astype(np.float32)).cuda()
+    y = torch.from_numpy(rng.standard_normal(P.n_rays).astype(np.float32)).cuda()
+    for dt in (torch.float32, torch.float16):
+        P.forward(x.to(dt))
+        P.adjoint(y.to(dt))
+    if P.cone:
+        P.z_mirror = False
+        P.forward(x)
+        P.adjoint(y)
+        P.z_mirror = True
+    for mode in ("graph", "mixed"):
+        NativeCGLS(P, mode).solve(torch.abs(x), lam=0.1, iters=3, refresh=2)
+
+
+def main():
+    L = _lib.load()
+    v = C.c_int64()
+    st = L.fl_debug_bounds(C.byref(v), 1)
+    assert st == _lib.FL_OK, "not a bounds-checked build"
+    rng = np.random.default_rng(0)
+    cases = [
+        G.cone_para_mm(32, 16, 48, 40, det_pitch_mm=8.0, SO_mm=600.0, SD_mm=1200.0,
+                       voxel_mm=8.0),                                  # circle: z-mirror
+        G.cone_para(16, 16, 16, 36, 32, 10, L=(2, 2, 2)),              # short SO, steep rows
+        G.cone_para(20, 18, 14, 30, 26, 0, L=(2, 2, 2), scan="helix", zmax=0.5, rps=1.0,
+                    vtab=1.0, fps=8),                                  # helix: general kernels
+        G.cone_para_mm(24, 12, 40, 33, det_pitch_mm=6.0, SO_mm=500.0, SD_mm=1000.0,
+                       voxel_mm=6.0, nz=17),                           # odd nz and nb
+        G.fan_para(64, 64, 128, 30, L=(1, 1)),                         # fan, 1 x 1 blocks
+        G.fan_para(512, 512, 1024, 60, L=(1, 1)),                      # fan, 2 x 2 blocks
+    ]
+    for p in cases:
+        run_plan(p, rng)
+    sl = [(16, 16, 33, 7), (24, 40, 61, 13), (40, 40, 81, 9)]
+    B = FanBatch([G.fan_para(nx, ny, nd, nv, L=(2.0 * nx / max(nx, ny), 2.0 * ny / max(nx, ny)))
+                  for nx, ny, nd, nv in sl])
+    xb = torch.rand(B.n_vox, device="cuda")
+    B.adjoint(B.forward(xb))
+    B.cgls(B.adjoint(B.forward(xb)), iters=3)
+    # the class mirror's default scanner geometry
+    cb = Operators.ConeBeamScanner("circle", 36, 32, 10, model="matched")
+    u = DataTypes.ObjectData(3, np.ones((16, 16, 16), np.float32), [2, 2, 2])
+    cb.applyAdjoint(cb.apply(u), [16, 16, 16])
+    torch.cuda.synchronize()
+    _lib.check(L.fl_debug_bounds(C.byref(v), 0))
+    print("violations", v.value)
+
+
+if __name__ == "__main__":
+    main()
