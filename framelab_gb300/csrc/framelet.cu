@@ -40,115 +40,164 @@ struct BandPtrs {
     float* p[kMaxBands];   // per band: coefficient array (nullptr: not stored)
 };
 
-__device__ __forceinline__ long long wrap_index(int ix, int iy, int iz, int nx, int ny, int nz)
+// j mod n for a tap index; |j - [0, n)| is almost always below n, so one add
+// or subtract wraps it (the modulo only runs for volumes smaller than a tap
+// offset)
+__device__ __forceinline__ int wrapi(int j, int n)
 {
+    if (j < 0) {
+        j += n;
+        if (j < 0) { j %= n; if (j < 0) j += n; }
+    } else if (j >= n) {
+        j -= n;
+        if (j >= n) j %= n;
+    }
+    return j;
+}
+
+// index of the neighbour at offset d along AXIS (0 x, 1 y, 2 z), circular
+template <int AXIS>
+__device__ __forceinline__ long long nb(int ix, int iy, int iz, int nx, int ny, int nz, int d)
+{
+    if (AXIS == 0) ix = wrapi(ix + d, nx);
+    else if (AXIS == 1) iy = wrapi(iy + d, ny);
+    else iz = wrapi(iz + d, nz);
     return ((long long)iz * ny + iy) * nx + ix;
 }
 
-// Index of the neighbour at offset d along `axis` with circular wrap.
-__device__ __forceinline__ long long nb_index(int ix, int iy, int iz, int nx, int ny, int nz,
-                                              int axis, int d)
-{
-    if (axis == 0) { ix = (ix + d) % nx; if (ix < 0) ix += nx; }
-    else if (axis == 1) { iy = (iy + d) % ny; if (iy < 0) iy += ny; }
-    else { iz = (iz + d) % nz; if (iz < 0) iz += nz; }
-    return wrap_index(ix, iy, iz, nx, ny, nz);
-}
+// Every pass runs on the grid (x in blocks of 128, y, z * channel): no index
+// arithmetic per element beyond the wrap of the taps. NF filters of NT taps.
+constexpr int kPassThreads = 128;
 
-// out[nf*c + f] = F_f (*) in[c] along axis, c < nin   (analysis split pass)
-__global__ void k_split(const float* __restrict__ in, long long in_stride, int nin,
-                        float* __restrict__ out, long long out_stride, int nx, int ny, int nz,
-                        int axis, int step, Filters F)
+// out[NF*c + f] = F_f (*) in[c] along AXIS   (analysis split pass)
+template <int NF, int NT, int AXIS>
+__global__ void __launch_bounds__(kPassThreads)
+k_split(const float* __restrict__ in, long long in_stride, float* __restrict__ out,
+        long long out_stride, int nx, int ny, int nz, int step, Filters F)
 {
-    const long long N = (long long)nx * ny * nz;
-    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < N * nin;
-         p += (long long)gridDim.x * blockDim.x) {
-        const int c = (int)(p / N);
-        const long long q = p - (long long)c * N;
-        const int ix = (int)(q % nx), iy = (int)((q / nx) % ny), iz = (int)(q / ((long long)nx * ny));
-        float v[5];
-        const int ctr = (F.nt - 1) / 2;
-        for (int t = 0; t < F.nt; t++)
-            v[t] = __ldg(in + (long long)c * in_stride +
-                         nb_index(ix, iy, iz, nx, ny, nz, axis, (t - ctr) * step));
-        for (int f = 0; f < F.nf; f++) {
-            float s = 0.0f;
-            for (int t = 0; t < F.nt; t++) s = fmaf(F.f[f][t], v[t], s);
-            out[(long long)(F.nf * c + f) * out_stride + q] = s;
-        }
+    const int ix = blockIdx.x * kPassThreads + threadIdx.x;
+    if (ix >= nx) return;
+    const int iy = blockIdx.y, iz = blockIdx.z % nz, c = blockIdx.z / nz;
+    const long long q = ((long long)iz * ny + iy) * nx + ix;
+    const float* src = in + (long long)c * in_stride;
+    constexpr int ctr = (NT - 1) / 2;
+    float v[NT];
+#pragma unroll
+    for (int t = 0; t < NT; t++) v[t] = __ldg(src + nb<AXIS>(ix, iy, iz, nx, ny, nz, (t - ctr) * step));
+#pragma unroll
+    for (int f = 0; f < NF; f++) {
+        float s = 0.0f;
+#pragma unroll
+        for (int t = 0; t < NT; t++) s = fmaf(F.f[f][t], v[t], s);
+        out[(long long)(NF * c + f) * out_stride + q] = s;
     }
 }
 
-// Last analysis pass. band = nf*c + f. mode 0: coef[band] = w (skipping band 0
+// Last analysis pass. band = NF*c + f. mode 0: coef[band] = w (skipping band 0
 // below the last level, which goes to `low`); mode 1: split-Bregman update on
 // v and t = alpha - v_new with soft threshold tau (no shrink on band 0 of the
 // last level).
-__global__ void k_split_last(const float* __restrict__ in, long long in_stride, int nin,
-                             int nx, int ny, int nz, int axis, int step, Filters F,
-                             BandPtrs coef, BandPtrs tout, float* __restrict__ low, int last,
-                             int mode, float tau)
+template <int NF, int NT, int AXIS>
+__global__ void __launch_bounds__(kPassThreads)
+k_split_last(const float* __restrict__ in, long long in_stride, int nx, int ny, int nz,
+             int step, Filters F, BandPtrs coef, BandPtrs tout, float* __restrict__ low,
+             int last, int mode, float tau)
 {
-    const long long N = (long long)nx * ny * nz;
-    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < N * nin;
-         p += (long long)gridDim.x * blockDim.x) {
-        const int c = (int)(p / N);
-        const long long q = p - (long long)c * N;
-        const int ix = (int)(q % nx), iy = (int)((q / nx) % ny), iz = (int)(q / ((long long)nx * ny));
-        float v[5];
-        const int ctr = (F.nt - 1) / 2;
-        for (int t = 0; t < F.nt; t++)
-            v[t] = __ldg(in + (long long)c * in_stride +
-                         nb_index(ix, iy, iz, nx, ny, nz, axis, (t - ctr) * step));
-        for (int f = 0; f < F.nf; f++) {
-            float w = 0.0f;
-            for (int t = 0; t < F.nt; t++) w = fmaf(F.f[f][t], v[t], w);
-            const int band = F.nf * c + f;
-            if (band == 0 && !last) {
-                if (low) low[q] = w;
-                continue;
+    const int ix = blockIdx.x * kPassThreads + threadIdx.x;
+    if (ix >= nx) return;
+    const int iy = blockIdx.y, iz = blockIdx.z % nz, c = blockIdx.z / nz;
+    const long long q = ((long long)iz * ny + iy) * nx + ix;
+    const float* src = in + (long long)c * in_stride;
+    constexpr int ctr = (NT - 1) / 2;
+    float v[NT];
+#pragma unroll
+    for (int t = 0; t < NT; t++) v[t] = __ldg(src + nb<AXIS>(ix, iy, iz, nx, ny, nz, (t - ctr) * step));
+#pragma unroll
+    for (int f = 0; f < NF; f++) {
+        float w = 0.0f;
+#pragma unroll
+        for (int t = 0; t < NT; t++) w = fmaf(F.f[f][t], v[t], w);
+        const int band = NF * c + f;
+        if (band == 0 && !last) {
+            if (low) low[q] = w;
+            continue;
+        }
+        if (mode == 0) {
+            coef.p[band][q] = w;
+        } else {
+            const float s = coef.p[band][q] + w;           // v + W u
+            float a = s;                                   // alpha
+            if (!(band == 0 && last)) {
+                const float m = fabsf(s) - tau;
+                a = m > 0.0f ? copysignf(m, s) : 0.0f;
             }
-            if (mode == 0) {
-                coef.p[band][q] = w;
-            } else {
-                const float s = coef.p[band][q] + w;           // v + W u
-                float a = s;                                   // alpha
-                if (!(band == 0 && last)) {
-                    const float m = fabsf(s) - tau;
-                    a = m > 0.0f ? copysignf(m, s) : 0.0f;
-                }
-                const float vn = s - a;                        // v + W u - alpha
-                coef.p[band][q] = vn;
-                tout.p[band][q] = a - vn;                      // alpha - v_new
-            }
+            const float vn = s - a;                        // v + W u - alpha
+            coef.p[band][q] = vn;
+            tout.p[band][q] = a - vn;                      // alpha - v_new
         }
     }
 }
 
-// out[c] = sum_f F_f (*) in[nf*c + f] along axis (synthesis merge pass); input
+// out[c] = sum_f F_f (*) in[NF*c + f] along AXIS (synthesis merge pass); input
 // arrays come from `bands` (band pointer per index) -- with band 0 replaced by
 // `low` when non-null. final: out = base + scale * result.
-__global__ void k_merge(BandPtrs bands, const float* __restrict__ low, int nout, float* __restrict__ out,
-                        long long out_stride, int nx, int ny, int nz, int axis, int step,
-                        Filters F, const float* __restrict__ base, float scale, int final_)
+template <int NF, int NT, int AXIS>
+__global__ void __launch_bounds__(kPassThreads)
+k_merge(BandPtrs bands, const float* __restrict__ low, float* __restrict__ out,
+        long long out_stride, int nx, int ny, int nz, int step, Filters F,
+        const float* __restrict__ base, float scale, int final_)
 {
-    const long long N = (long long)nx * ny * nz;
-    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < N * nout;
-         p += (long long)gridDim.x * blockDim.x) {
-        const int c = (int)(p / N);
-        const long long q = p - (long long)c * N;
-        const int ix = (int)(q % nx), iy = (int)((q / nx) % ny), iz = (int)(q / ((long long)nx * ny));
-        const int ctr = (F.nt - 1) / 2;
-        float s = 0.0f;
-        for (int f = 0; f < F.nf; f++) {
-            const int band = F.nf * c + f;
-            const float* src = (band == 0 && low) ? low : bands.p[band];
-            for (int t = 0; t < F.nt; t++)
-                s = fmaf(F.f[f][t], __ldg(src + nb_index(ix, iy, iz, nx, ny, nz, axis, (t - ctr) * step)), s);
-        }
-        if (final_) s = (base ? __ldg(base + q) : 0.0f) + scale * s;
-        out[(long long)c * out_stride + q] = s;
+    const int ix = blockIdx.x * kPassThreads + threadIdx.x;
+    if (ix >= nx) return;
+    const int iy = blockIdx.y, iz = blockIdx.z % nz, c = blockIdx.z / nz;
+    const long long q = ((long long)iz * ny + iy) * nx + ix;
+    constexpr int ctr = (NT - 1) / 2;
+    float s = 0.0f;
+#pragma unroll
+    for (int f = 0; f < NF; f++) {
+        const int band = NF * c + f;
+        const float* src = (band == 0 && low) ? low : bands.p[band];
+#pragma unroll
+        for (int t = 0; t < NT; t++)
+            s = fmaf(F.f[f][t], __ldg(src + nb<AXIS>(ix, iy, iz, nx, ny, nz, (t - ctr) * step)), s);
     }
+    if (final_) s = (base ? __ldg(base + q) : 0.0f) + scale * s;
+    out[(long long)c * out_stride + q] = s;
 }
+
+// launchers: filter bank (NF, NT) and axis as template arguments
+template <int NF, int NT>
+struct Pass {
+    static void split(int axis, dim3 g, cudaStream_t s, const float* in, long long is, float* out,
+                      long long os, int nx, int ny, int nz, int step, const Filters& F)
+    {
+        if (axis == 0) k_split<NF, NT, 0><<<g, kPassThreads, 0, s>>>(in, is, out, os, nx, ny, nz, step, F);
+        else if (axis == 1) k_split<NF, NT, 1><<<g, kPassThreads, 0, s>>>(in, is, out, os, nx, ny, nz, step, F);
+        else k_split<NF, NT, 2><<<g, kPassThreads, 0, s>>>(in, is, out, os, nx, ny, nz, step, F);
+    }
+    static void split_last(int axis, dim3 g, cudaStream_t s, const float* in, long long is,
+                           int nx, int ny, int nz, int step, const Filters& F, const BandPtrs& cb,
+                           const BandPtrs& tb, float* low, int last, int mode, float tau)
+    {
+        if (axis == 0)
+            k_split_last<NF, NT, 0><<<g, kPassThreads, 0, s>>>(in, is, nx, ny, nz, step, F, cb, tb, low, last, mode, tau);
+        else if (axis == 1)
+            k_split_last<NF, NT, 1><<<g, kPassThreads, 0, s>>>(in, is, nx, ny, nz, step, F, cb, tb, low, last, mode, tau);
+        else
+            k_split_last<NF, NT, 2><<<g, kPassThreads, 0, s>>>(in, is, nx, ny, nz, step, F, cb, tb, low, last, mode, tau);
+    }
+    static void merge(int axis, dim3 g, cudaStream_t s, const BandPtrs& b, const float* low,
+                      float* out, long long os, int nx, int ny, int nz, int step,
+                      const Filters& F, const float* base, float scale, int final_)
+    {
+        if (axis == 0)
+            k_merge<NF, NT, 0><<<g, kPassThreads, 0, s>>>(b, low, out, os, nx, ny, nz, step, F, base, scale, final_);
+        else if (axis == 1)
+            k_merge<NF, NT, 1><<<g, kPassThreads, 0, s>>>(b, low, out, os, nx, ny, nz, step, F, base, scale, final_);
+        else
+            k_merge<NF, NT, 2><<<g, kPassThreads, 0, s>>>(b, low, out, os, nx, ny, nz, step, F, base, scale, final_);
+    }
+};
 
 unsigned grid_for(long long n)
 {
@@ -227,6 +276,13 @@ extern "C" int fl_framelet_create(int nx, int ny, int nz, int levels, int kind, 
         return fl_set_error(FL_ERR_INVALID, "fl_framelet_create: bad size or levels");
     if (kind != FL_FRAMELET_LINEAR && kind != FL_FRAMELET_HAAR && kind != FL_FRAMELET_CUBIC)
         return fl_set_error(FL_ERR_INVALID, "fl_framelet_create: unknown filter bank %d", kind);
+    {   // the passes run on the grid (x blocks, y, z * channels)
+        const long long maxch = (kind == FL_FRAMELET_CUBIC ? 25 : 9);
+        if (ny > 65535 || (long long)nz * maxch > 65535)
+            return fl_set_error(FL_ERR_UNSUPPORTED,
+                                "fl_framelet_create: ny must be <= 65535 and nz <= %lld",
+                                65535 / maxch);
+    }
     *out = nullptr;
     fl_framelet* w = new (std::nothrow) fl_framelet;
     if (!w) return fl_set_error(FL_ERR_ALLOC, "out of host memory");
@@ -281,35 +337,84 @@ static BandPtrs level_bands(const fl_framelet* w, float* coef, int l)
     return B;
 }
 
+static dim3 pass_grid(const fl_framelet* w, int channels)
+{
+    return dim3(fl_div_up(w->nx, kPassThreads), w->ny, (unsigned)(w->nz * channels));
+}
+
+// One analysis level: the separable passes along the three (two) axes, the
+// last one fused with the coefficient write or the Bregman update.
+template <int NF, int NT>
+static void analysis_level(fl_framelet* w, const float* in, int step, const BandPtrs& cb,
+                           const BandPtrs& tb, float* low_out, int last, int mode, float tau,
+                           cudaStream_t s)
+{
+    using P = Pass<NF, NT>;
+    const long long N = w->N;
+    float* A = w->work;                          // NF arrays
+    float* Bm = A + (long long)NF * N;           // NF^2 arrays (3-D)
+    if (w->dim == 3) {
+        P::split(w->axes[0], pass_grid(w, 1), s, in, N, A, N, w->nx, w->ny, w->nz, step, w->D);
+        P::split(w->axes[1], pass_grid(w, NF), s, A, N, Bm, N, w->nx, w->ny, w->nz, step, w->D);
+        P::split_last(w->axes[2], pass_grid(w, NF * NF), s, Bm, N, w->nx, w->ny, w->nz, step,
+                      w->D, cb, tb, low_out, last, mode, tau);
+    } else {
+        P::split(w->axes[0], pass_grid(w, 1), s, in, N, A, N, w->nx, w->ny, w->nz, step, w->D);
+        P::split_last(w->axes[1], pass_grid(w, NF), s, A, N, w->nx, w->ny, w->nz, step, w->D,
+                      cb, tb, low_out, last, mode, tau);
+    }
+}
+
+// One synthesis level: the merge passes in reverse axis order, the last one
+// writing dst (= base + scale * result on the final level).
+template <int NF, int NT>
+static void synthesis_level(fl_framelet* w, const BandPtrs& cb, const float* low, float* dst,
+                            int step, const float* base, float scale, int final_, cudaStream_t s)
+{
+    using P = Pass<NF, NT>;
+    const long long N = w->N;
+    float* A = w->work;
+    float* Bm = A + (long long)NF * N;
+    BandPtrs ib, jb;
+    for (int b = 0; b < kMaxBands; b++) ib.p[b] = jb.p[b] = nullptr;
+    if (w->dim == 3) {
+        P::merge(w->axes[2], pass_grid(w, NF * NF), s, cb, low, Bm, N, w->nx, w->ny, w->nz,
+                 step, w->R, nullptr, 1.0f, 0);
+        for (int b = 0; b < NF * NF; b++) ib.p[b] = Bm + (long long)b * N;
+        P::merge(w->axes[1], pass_grid(w, NF), s, ib, nullptr, A, N, w->nx, w->ny, w->nz, step,
+                 w->R, nullptr, 1.0f, 0);
+        for (int b = 0; b < NF; b++) jb.p[b] = A + (long long)b * N;
+        P::merge(w->axes[0], pass_grid(w, 1), s, jb, nullptr, dst, N, w->nx, w->ny, w->nz, step,
+                 w->R, base, scale, final_);
+    } else {
+        P::merge(w->axes[1], pass_grid(w, NF), s, cb, low, A, N, w->nx, w->ny, w->nz, step,
+                 w->R, nullptr, 1.0f, 0);
+        for (int b = 0; b < NF; b++) jb.p[b] = A + (long long)b * N;
+        P::merge(w->axes[0], pass_grid(w, 1), s, jb, nullptr, dst, N, w->nx, w->ny, w->nz, step,
+                 w->R, base, scale, final_);
+    }
+}
+
 // Analysis of all levels. mode 0: coef = W u. mode 1: Bregman update of v
 // (coef argument) writing t = alpha - v_new into tcoef.
 static int analysis(fl_framelet* w, const float* u, float* coef, float* tcoef, int mode,
                     float tau, cudaStream_t s)
 {
     const long long N = w->N;
-    const int nf = w->nf;
-    float* A = w->work;                          // nf arrays
-    float* Bm = A + (long long)nf * N;           // nf^2 arrays (3-D)
     float* low0 = w->work + (w->work_elems - 2 * N);
     float* low1 = low0 + N;
     const float* in = u;
     for (int l = 0; l < w->levels; l++) {
         const int step = 1 << l;
-        const bool last = (l == w->levels - 1);
+        const int last = (l == w->levels - 1) ? 1 : 0;
         float* low_out = last ? nullptr : ((l % 2 == 0) ? low0 : low1);
         BandPtrs cb = level_bands(w, coef, l), tb = level_bands(w, tcoef, l);
-        if (w->dim == 3) {
-            k_split<<<grid_for(N), 256, 0, s>>>(in, N, 1, A, N, w->nx, w->ny, w->nz, w->axes[0], step, w->D);
-            k_split<<<grid_for(N * nf), 256, 0, s>>>(A, N, nf, Bm, N, w->nx, w->ny, w->nz, w->axes[1], step, w->D);
-            k_split_last<<<grid_for(N * nf * nf), 256, 0, s>>>(Bm, N, nf * nf, w->nx, w->ny, w->nz,
-                                                             w->axes[2], step, w->D, cb, tb,
-                                                             low_out, last, mode, tau);
-        } else {
-            k_split<<<grid_for(N), 256, 0, s>>>(in, N, 1, A, N, w->nx, w->ny, w->nz, w->axes[0], step, w->D);
-            k_split_last<<<grid_for(N * nf), 256, 0, s>>>(A, N, nf, w->nx, w->ny, w->nz,
-                                                         w->axes[1], step, w->D, cb, tb, low_out,
-                                                         last, mode, tau);
-        }
+        if (w->kind == FL_FRAMELET_LINEAR)
+            analysis_level<3, 3>(w, in, step, cb, tb, low_out, last, mode, tau, s);
+        else if (w->kind == FL_FRAMELET_CUBIC)
+            analysis_level<5, 5>(w, in, step, cb, tb, low_out, last, mode, tau, s);
+        else
+            analysis_level<2, 3>(w, in, step, cb, tb, low_out, last, mode, tau, s);
         int st = fl_check_launch("framelet analysis");
         if (st) return st;
         in = low_out;
@@ -322,39 +427,22 @@ static int synthesis(fl_framelet* w, float* coef, float* out, const float* base,
                      cudaStream_t s)
 {
     const long long N = w->N;
-    const int nf = w->nf;
-    float* A = w->work;
-    float* Bm = A + (long long)nf * N;
     float* low0 = w->work + (w->work_elems - 2 * N);
     float* low1 = low0 + N;
     const float* low = nullptr;
     for (int l = w->levels - 1; l >= 0; l--) {
         const int step = 1 << l;
-        const bool final_ = (l == 0);
+        const int final_ = (l == 0) ? 1 : 0;
         float* dst = final_ ? out : ((l % 2 == 0) ? low0 : low1);
         BandPtrs cb = level_bands(w, coef, l);
-        BandPtrs ib, jb;
-        for (int b = 0; b < kMaxBands; b++) ib.p[b] = jb.p[b] = nullptr;
-        if (w->dim == 3) {
-            // z merge: nbands -> nf^2 arrays (Bm)
-            k_merge<<<grid_for(N * nf * nf), 256, 0, s>>>(cb, low, nf * nf, Bm, N, w->nx, w->ny,
-                                                        w->nz, w->axes[2], step, w->R, nullptr,
-                                                        1.0f, 0);
-            for (int b = 0; b < nf * nf; b++) ib.p[b] = Bm + (long long)b * N;
-            k_merge<<<grid_for(N * nf), 256, 0, s>>>(ib, nullptr, nf, A, N, w->nx, w->ny, w->nz,
-                                                   w->axes[1], step, w->R, nullptr, 1.0f, 0);
-            for (int b = 0; b < nf; b++) jb.p[b] = A + (long long)b * N;
-            k_merge<<<grid_for(N), 256, 0, s>>>(jb, nullptr, 1, dst, N, w->nx, w->ny, w->nz,
-                                              w->axes[0], step, w->R, final_ ? base : nullptr,
-                                              final_ ? scale : 1.0f, final_ ? 1 : 0);
-        } else {
-            k_merge<<<grid_for(N * nf), 256, 0, s>>>(cb, low, nf, A, N, w->nx, w->ny, w->nz,
-                                                   w->axes[1], step, w->R, nullptr, 1.0f, 0);
-            for (int b = 0; b < nf; b++) jb.p[b] = A + (long long)b * N;
-            k_merge<<<grid_for(N), 256, 0, s>>>(jb, nullptr, 1, dst, N, w->nx, w->ny, w->nz,
-                                              w->axes[0], step, w->R, final_ ? base : nullptr,
-                                              final_ ? scale : 1.0f, final_ ? 1 : 0);
-        }
+        const float* bs = final_ ? base : nullptr;
+        const float sc = final_ ? scale : 1.0f;
+        if (w->kind == FL_FRAMELET_LINEAR)
+            synthesis_level<3, 3>(w, cb, low, dst, step, bs, sc, final_, s);
+        else if (w->kind == FL_FRAMELET_CUBIC)
+            synthesis_level<5, 5>(w, cb, low, dst, step, bs, sc, final_, s);
+        else
+            synthesis_level<2, 3>(w, cb, low, dst, step, bs, sc, final_, s);
         int st = fl_check_launch("framelet synthesis");
         if (st) return st;
         low = dst;
