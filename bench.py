@@ -677,9 +677,15 @@ def run_sb(ctx, name, w, p):
         _, tfw = ctx.timed(lambda: [fw.bregman(u, v, t, None, w["mu"], w["lam"] / w["mu"], bb)
                                     for _ in range(reps)])
         tfw /= reps
+        fw.fused = False                # the separable pass per axis, for comparison
+        fw.bregman(u, v, t, None, w["mu"], w["lam"] / w["mu"], bb)
+        _, tsep = ctx.timed(lambda: [fw.bregman(u, v, t, None, w["mu"], w["lam"] / w["mu"], bb)
+                                     for _ in range(reps)])
+        tsep /= reps
+        fw.fused = True
         fb = 4 * (2 * P.n_vox + 4 * fw.ncoef)
         detail.update(framelet_step_ms=tfw * 1e3, framelet_compulsory_GBps=fb / tfw / 1e9,
-                      framelet_ncoef=fw.ncoef)
+                      framelet_separable_step_ms=tsep * 1e3, framelet_ncoef=fw.ncoef)
         del v, t, bb, fw
     # setup: A^T f (weighting + gather) and W u0 (3 per level); per outer iteration:
     # warm-start residual (fwd, adj, axpy) + init, inner x (fwd, adj, 3 updates),

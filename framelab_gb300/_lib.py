@@ -18,6 +18,7 @@ FL_OK, FL_ERR_INVALID, FL_ERR_UNSUPPORTED, FL_ERR_CUDA, FL_ERR_ALLOC, FL_ERR_TIM
 MODEL_SIDDON_REF, MODEL_CHORD_REF, MODEL_GAO_REF, MODEL_FB_REF, MODEL_MATCHED = 0, 1, 2, 3, 16
 F32, F16, BF16 = 0, 1, 2
 OPT_Z_MIRROR = 1
+FRAMELET_OPT_FUSED = 1
 
 
 class FLError(RuntimeError):
@@ -89,6 +90,7 @@ _SIGS = {
     "fl_framelet_synthesis": (_I, [_P, _V, _V, _V]),
     "fl_framelet_bregman": (_I, [_P, _V, _V, _V, _V, _F, _F, _V, _V]),
     "fl_framelet_shrink": (_I, [_P, _V, _V, _F, _V]),
+    "fl_framelet_option": (_I, [_P, _I, _I]),
     "fl_sb_solve": (_I, [_P, _V, _V, _F, _F, _I, _I, _D, _I, _I, _I, _V, _V]),
     # batched fan slices
     "fl_batch_create": (_I, [C.POINTER(_P), C.c_int32, C.POINTER(_P)]),

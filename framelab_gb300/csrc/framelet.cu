@@ -112,6 +112,10 @@ k_split_last(const float* __restrict__ in, long long in_stride, int nx, int ny, 
     float v[NT];
 #pragma unroll
     for (int t = 0; t < NT; t++) v[t] = __ldg(src + nb<AXIS>(ix, iy, iz, nx, ny, nz, (t - ctr) * step));
+    float vv[NF];                                          // v of every band, read before any store
+#pragma unroll
+    for (int f = 0; f < NF; f++)
+        vv[f] = (mode == 0 || (NF * c + f == 0 && !last)) ? 0.0f : coef.p[NF * c + f][q];
 #pragma unroll
     for (int f = 0; f < NF; f++) {
         float w = 0.0f;
@@ -125,7 +129,7 @@ k_split_last(const float* __restrict__ in, long long in_stride, int nx, int ny, 
         if (mode == 0) {
             coef.p[band][q] = w;
         } else {
-            const float s = coef.p[band][q] + w;           // v + W u
+            const float s = vv[f] + w;                     // v + W u
             float a = s;                                   // alpha
             if (!(band == 0 && last)) {
                 const float m = fabsf(s) - tau;
@@ -199,6 +203,191 @@ struct Pass {
     }
 };
 
+// ---------------------------------------------------------------------------
+// z-streaming 3-D level kernels for the three-tap banks (linear, Haar). A
+// block owns a column tile (warp = one row y, lane = x) and walks the slices
+// z = r, r + s, r + 2s, ... of one residue class r mod s (s = 2^level), up to
+// kSegZ output slices. The z taps of an output slice are the slices z - s, z,
+// z + s of its own class, so each thread keeps the z-pass inputs of its
+// sample in a three-slot register window and every slice is read once per
+// block. Every value is the same fmaf chain as in the separable pass kernels
+// above (taps in order, filters in order), so both forms give identical bits.
+constexpr int kSX = 32, kSY = 8, kST = kSX * kSY;   // column tile, threads per block
+constexpr int kSegZ = 32;                            // output slices of one class per block
+constexpr int kMaxStreamStep = 8;                    // dilations the streaming kernels take
+
+// slices of residue class r in [0, nz): r, r + s, ...
+__host__ __device__ inline int class_len(int nz, int s, int r)
+{
+    return r < nz ? (nz - 1 - r) / s + 1 : 0;
+}
+
+// One analysis level: the y and x passes of each slice in shared memory, the
+// z pass from the register window, fused with the coefficient write (mode 0)
+// or the Bregman update (mode 1) exactly as k_split_last.
+template <int NF, int S>
+__global__ void __launch_bounds__(kST, 2)
+k_ana_stream(const float* __restrict__ in, int nx, int ny, int nz, int nseg, Filters F,
+             BandPtrs coef, BandPtrs tout, float* __restrict__ low, int last, int mode, float tau)
+{
+    constexpr int RX = kSX + 2 * S, RY = kSY + 2 * S;   // in-plane region (halo S)
+    constexpr int XR = RX - 32;                        // lanes holding a second column
+    constexpr int LR = (RY + kSY - 1) / kSY;           // region rows per warp
+    constexpr int NC = NF * NF;                        // channels into the z pass
+    __shared__ float s_in[2][RY][RX];
+    __shared__ float s_p1[2][NF][kSY][RX];
+    const int lane = threadIdx.x & 31, wy = threadIdx.x >> 5;
+    const int x0 = blockIdx.x * kSX, y0 = blockIdx.y * kSY;
+    const int seg = blockIdx.z % nseg, r = blockIdx.z / nseg;
+    const int nfirst = seg * kSegZ, nend = min(nfirst + kSegZ, class_len(nz, S, r));
+    if (nfirst >= nend) return;                        // uniform per block
+    const int xa = wrapi(x0 - S + lane, nx);
+    const int xb = lane < XR ? wrapi(x0 - S + 32 + lane, nx) : 0;
+    int rows[LR];
+#pragma unroll
+    for (int m = 0; m < LR; m++) rows[m] = wrapi(y0 - S + wy + kSY * m, ny);
+    const int x = x0 + lane, y = y0 + wy;
+    const bool ok = x < nx && y < ny;
+    float pa[LR], pb[LR];                              // the next slice's region, in flight
+    auto fetch = [&](int n) {
+        const long long zo = (long long)wrapi(r + S * n, nz) * ny;
+#pragma unroll
+        for (int m = 0; m < LR; m++)
+            if (wy + kSY * m < RY) {
+                const float* row = in + (zo + rows[m]) * nx;
+                pa[m] = __ldg(row + xa);
+                pb[m] = lane < XR ? __ldg(row + xb) : 0.0f;
+            }
+    };
+    float win[3][NC];
+    fetch(nfirst - 1);
+    for (int n = nfirst - 1, it = 0; n <= nend; n++, it++) {
+        const int b = it & 1;
+#pragma unroll
+        for (int m = 0; m < LR; m++)
+            if (wy + kSY * m < RY) {
+                s_in[b][wy + kSY * m][lane] = pa[m];
+                if (lane < XR) s_in[b][wy + kSY * m][32 + lane] = pb[m];
+            }
+        if (n < nend) fetch(n + 1);
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < NF; i++) {                 // y pass (D_i)
+            float s0 = 0.0f;
+#pragma unroll
+            for (int t = 0; t < 3; t++) s0 = fmaf(F.f[i][t], s_in[b][wy + t * S][lane], s0);
+            s_p1[b][i][wy][lane] = s0;
+            if (lane < XR) {
+                float s1 = 0.0f;
+#pragma unroll
+                for (int t = 0; t < 3; t++) s1 = fmaf(F.f[i][t], s_in[b][wy + t * S][32 + lane], s1);
+                s_p1[b][i][wy][32 + lane] = s1;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int c = 0; c < NC; c++) { win[0][c] = win[1][c]; win[1][c] = win[2][c]; }
+#pragma unroll
+        for (int i = 0; i < NF; i++)                   // x pass (D_j) into the newest slot
+#pragma unroll
+            for (int j = 0; j < NF; j++) {
+                float s0 = 0.0f;
+#pragma unroll
+                for (int t = 0; t < 3; t++) s0 = fmaf(F.f[j][t], s_p1[b][i][wy][lane + t * S], s0);
+                win[2][NF * i + j] = s0;
+            }
+        if (n < nfirst + 1 || !ok) continue;           // window filling, or outside the volume
+        const int z = r + S * (n - 1);                 // slots: z - S, z, z + S
+        const long long q = ((long long)z * ny + y) * nx + x;
+        // every v of this sample is read before the first store (the band
+        // pointers may alias as far as the compiler knows), so the loads are
+        // in flight together
+        float vv[NC * NF];
+#pragma unroll
+        for (int band = 0; band < NC * NF; band++)
+            vv[band] = (mode == 0 || (band == 0 && !last)) ? 0.0f : coef.p[band][q];
+#pragma unroll
+        for (int c = 0; c < NC; c++)
+#pragma unroll
+            for (int k = 0; k < NF; k++) {             // z pass (D_k)
+                const int band = NF * c + k;
+                float w = 0.0f;
+#pragma unroll
+                for (int t = 0; t < 3; t++) w = fmaf(F.f[k][t], win[t][c], w);
+                if (band == 0 && !last) {
+                    if (low) low[q] = w;
+                    continue;
+                }
+                if (mode == 0) {
+                    coef.p[band][q] = w;
+                } else {
+                    const float sv = vv[band] + w;         // v + W u
+                    float a = sv;                          // alpha
+                    if (!(band == 0 && last)) {
+                        const float mg = fabsf(sv) - tau;
+                        a = mg > 0.0f ? copysignf(mg, sv) : 0.0f;
+                    }
+                    const float vn = sv - a;               // v + W u - alpha
+                    coef.p[band][q] = vn;
+                    tout.p[band][q] = a - vn;              // alpha - v_new
+                }
+            }
+    }
+}
+
+// The z and x merges of one synthesis level (k_merge along z into NF^2
+// arrays, then along x into the NF arrays A_i), band 0 taken from `low` when
+// non-null. A warp covers one row y: its lanes hold the columns from S before
+// its kSX - 2S outputs to S after them, and the x taps come from the
+// neighbouring lanes. blockIdx.z = seg + nseg (i + NF r).
+template <int NF, int S>
+__global__ void __launch_bounds__(kST)
+k_syn_zx(BandPtrs bands, const float* __restrict__ low, float* __restrict__ A, long long N,
+         int nx, int ny, int nz, int nseg, Filters R)
+{
+    constexpr int OX = kSX - 2 * S, NB = NF * NF;      // outputs per warp, bands per thread
+    const int lane = threadIdx.x & 31;
+    const int y = blockIdx.y * kSY + (threadIdx.x >> 5);
+    const int seg = blockIdx.z % nseg, ir = blockIdx.z / nseg, i = ir % NF, r = ir / NF;
+    const int nfirst = seg * kSegZ, nend = min(nfirst + kSegZ, class_len(nz, S, r));
+    if (nfirst >= nend || y >= ny) return;             // whole warps (no block barrier here)
+    const int xl = blockIdx.x * OX - S + lane;         // this lane's column, unwrapped
+    const long long col = (long long)y * nx + wrapi(xl, nx);
+    const bool out_ok = lane >= S && lane < kSX - S && xl < nx;
+    const long long plane = (long long)ny * nx;
+    auto src = [&](int b) -> const float* {            // b = NF j + k: band NF (NF i + j) + k
+        const int band = NF * NF * i + b;
+        return (band == 0 && low) ? low : bands.p[band];
+    };
+    float win[3][NB], nxt[NB];
+    auto fetch = [&](int n, float (&d)[NB]) {
+        const long long o = (long long)wrapi(r + S * n, nz) * plane + col;
+#pragma unroll
+        for (int b = 0; b < NB; b++) d[b] = __ldg(src(b) + o);
+    };
+    fetch(nfirst - 1, win[1]);
+    fetch(nfirst, win[2]);
+    fetch(nfirst + 1, nxt);
+    for (int n = nfirst + 1; n <= nend; n++) {
+#pragma unroll
+        for (int b = 0; b < NB; b++) { win[0][b] = win[1][b]; win[1][b] = win[2][b]; win[2][b] = nxt[b]; }
+        if (n < nend) fetch(n + 1, nxt);
+        float a = 0.0f;                                // output slice r + S (n - 1)
+#pragma unroll
+        for (int j = 0; j < NF; j++) {
+            float bm = 0.0f;                           // z merge (R_k) of channel NF i + j
+#pragma unroll
+            for (int k = 0; k < NF; k++)
+#pragma unroll
+                for (int t = 0; t < 3; t++) bm = fmaf(R.f[k][t], win[t][NF * j + k], bm);
+#pragma unroll
+            for (int t = 0; t < 3; t++)                // x merge (R_j)
+                a = fmaf(R.f[j][t], __shfl_sync(0xffffffffu, bm, lane + (t - 1) * S), a);
+        }
+        if (out_ok) A[i * N + (long long)(r + S * (n - 1)) * plane + (long long)y * nx + xl] = a;
+    }
+}
+
 unsigned grid_for(long long n)
 {
     long long g = (n + 255) / 256;
@@ -228,6 +417,7 @@ struct fl_framelet {
     long long N;
     Filters D, R;
     int axes[3];                    // analysis pass order
+    int fused;                      // 3-D levels through the z-streaming kernels
     float* work;                    // intermediates: nf^(dim-1) + nf^(dim-2) arrays + low
     long long work_elems;
     std::vector<long long> level_base;   // first coefficient band of each level
@@ -287,7 +477,7 @@ extern "C" int fl_framelet_create(int nx, int ny, int nz, int levels, int kind, 
     fl_framelet* w = new (std::nothrow) fl_framelet;
     if (!w) return fl_set_error(FL_ERR_ALLOC, "out of host memory");
     w->nx = nx; w->ny = ny; w->nz = nz; w->dim = (nz > 1) ? 3 : 2; w->levels = levels;
-    w->kind = kind; w->N = (long long)nx * ny * nz;
+    w->kind = kind; w->N = (long long)nx * ny * nz; w->fused = 1;
     set_filters(w, kind);
     w->nf = w->D.nf;
     w->nbands = w->dim == 3 ? w->nf * w->nf * w->nf : w->nf * w->nf;
@@ -395,6 +585,94 @@ static void synthesis_level(fl_framelet* w, const BandPtrs& cb, const float* low
     }
 }
 
+// z-streaming form of a 3-D level (three-tap banks, dilation up to
+// kMaxStreamStep): analysis in one kernel; synthesis as the z + x merges in
+// one kernel and the y merge (with the final base + scale) as the separable
+// pass. Returns false when the level needs the separable passes.
+static bool stream_ok(const fl_framelet* w, int step)
+{
+    return w->fused && w->dim == 3 && w->D.nt == 3 && step <= kMaxStreamStep;
+}
+
+static int stream_nseg(const fl_framelet* w, int step)
+{
+    return fl_div_up(class_len(w->nz, step, 0), kSegZ);
+}
+
+template <int NF, int S>
+static void ana_stream(fl_framelet* w, const float* in, const BandPtrs& cb, const BandPtrs& tb,
+                       float* low_out, int last, int mode, float tau, cudaStream_t s)
+{
+    const int nseg = stream_nseg(w, S);
+    const dim3 grid(fl_div_up(w->nx, kSX), fl_div_up(w->ny, kSY), (unsigned)(nseg * S));
+    k_ana_stream<NF, S><<<grid, kST, 0, s>>>(in, w->nx, w->ny, w->nz, nseg, w->D, cb, tb,
+                                             low_out, last, mode, tau);
+}
+
+template <int NF, int S>
+static void syn_stream(fl_framelet* w, const BandPtrs& cb, const float* low, float* dst,
+                       const float* base, float scale, int final_, cudaStream_t s)
+{
+    const int nseg = stream_nseg(w, S);
+    const long long N = w->N;
+    float* A = w->work;                                // NF arrays
+    const dim3 grid(fl_div_up(w->nx, kSX - 2 * S), fl_div_up(w->ny, kSY),
+                    (unsigned)(nseg * NF * S));
+    k_syn_zx<NF, S><<<grid, kST, 0, s>>>(cb, low, A, N, w->nx, w->ny, w->nz, nseg, w->R);
+    BandPtrs ab;
+    for (int b = 0; b < kMaxBands; b++) ab.p[b] = b < NF ? A + (long long)b * N : nullptr;
+    Pass<NF, 3>::merge(w->axes[0], pass_grid(w, 1), s, ab, nullptr, dst, N, w->nx, w->ny, w->nz,
+                       S, w->R, base, scale, final_);
+}
+
+template <int NF>
+static void stream_level(fl_framelet* w, int step, bool analysis_pass, const float* in,
+                         const BandPtrs& cb, const BandPtrs& tb, float* low_out, int last,
+                         int mode, float tau, const float* low, float* dst, const float* base,
+                         float scale, int final_, cudaStream_t s)
+{
+    switch (step) {
+#define FL_STREAM_CASE(SS)                                                                   \
+    case SS:                                                                                 \
+        if (analysis_pass) ana_stream<NF, SS>(w, in, cb, tb, low_out, last, mode, tau, s);   \
+        else syn_stream<NF, SS>(w, cb, low, dst, base, scale, final_, s);                    \
+        break;
+        FL_STREAM_CASE(1)
+        FL_STREAM_CASE(2)
+        FL_STREAM_CASE(4)
+        FL_STREAM_CASE(8)
+#undef FL_STREAM_CASE
+    }
+}
+
+template <int NF, int NT>
+static void run_analysis_level(fl_framelet* w, const float* in, int step, const BandPtrs& cb,
+                               const BandPtrs& tb, float* low_out, int last, int mode, float tau,
+                               cudaStream_t s)
+{
+    if constexpr (NT == 3)
+        if (stream_ok(w, step)) {
+            stream_level<NF>(w, step, true, in, cb, tb, low_out, last, mode, tau, nullptr,
+                             nullptr, nullptr, 1.0f, 0, s);
+            return;
+        }
+    analysis_level<NF, NT>(w, in, step, cb, tb, low_out, last, mode, tau, s);
+}
+
+template <int NF, int NT>
+static void run_synthesis_level(fl_framelet* w, const BandPtrs& cb, const float* low, float* dst,
+                                int step, const float* base, float scale, int final_,
+                                cudaStream_t s)
+{
+    if constexpr (NT == 3)
+        if (stream_ok(w, step)) {
+            stream_level<NF>(w, step, false, nullptr, cb, cb, nullptr, 0, 0, 0.0f, low, dst,
+                             base, scale, final_, s);
+            return;
+        }
+    synthesis_level<NF, NT>(w, cb, low, dst, step, base, scale, final_, s);
+}
+
 // Analysis of all levels. mode 0: coef = W u. mode 1: Bregman update of v
 // (coef argument) writing t = alpha - v_new into tcoef.
 static int analysis(fl_framelet* w, const float* u, float* coef, float* tcoef, int mode,
@@ -410,11 +688,11 @@ static int analysis(fl_framelet* w, const float* u, float* coef, float* tcoef, i
         float* low_out = last ? nullptr : ((l % 2 == 0) ? low0 : low1);
         BandPtrs cb = level_bands(w, coef, l), tb = level_bands(w, tcoef, l);
         if (w->kind == FL_FRAMELET_LINEAR)
-            analysis_level<3, 3>(w, in, step, cb, tb, low_out, last, mode, tau, s);
+            run_analysis_level<3, 3>(w, in, step, cb, tb, low_out, last, mode, tau, s);
         else if (w->kind == FL_FRAMELET_CUBIC)
-            analysis_level<5, 5>(w, in, step, cb, tb, low_out, last, mode, tau, s);
+            run_analysis_level<5, 5>(w, in, step, cb, tb, low_out, last, mode, tau, s);
         else
-            analysis_level<2, 3>(w, in, step, cb, tb, low_out, last, mode, tau, s);
+            run_analysis_level<2, 3>(w, in, step, cb, tb, low_out, last, mode, tau, s);
         int st = fl_check_launch("framelet analysis");
         if (st) return st;
         in = low_out;
@@ -438,11 +716,11 @@ static int synthesis(fl_framelet* w, float* coef, float* out, const float* base,
         const float* bs = final_ ? base : nullptr;
         const float sc = final_ ? scale : 1.0f;
         if (w->kind == FL_FRAMELET_LINEAR)
-            synthesis_level<3, 3>(w, cb, low, dst, step, bs, sc, final_, s);
+            run_synthesis_level<3, 3>(w, cb, low, dst, step, bs, sc, final_, s);
         else if (w->kind == FL_FRAMELET_CUBIC)
-            synthesis_level<5, 5>(w, cb, low, dst, step, bs, sc, final_, s);
+            run_synthesis_level<5, 5>(w, cb, low, dst, step, bs, sc, final_, s);
         else
-            synthesis_level<2, 3>(w, cb, low, dst, step, bs, sc, final_, s);
+            run_synthesis_level<2, 3>(w, cb, low, dst, step, bs, sc, final_, s);
         int st = fl_check_launch("framelet synthesis");
         if (st) return st;
         low = dst;
@@ -477,6 +755,15 @@ extern "C" int fl_framelet_bregman(fl_framelet* w, const float* u, float* v, flo
     if (st) return st;
     st = synthesis(w, t, b, Atf, mu, s);
     return st ? st : fl_set_error(FL_OK, "");
+}
+
+extern "C" int fl_framelet_option(fl_framelet* w, int option, int value)
+{
+    if (!w) return fl_set_error(FL_ERR_INVALID, "fl_framelet_option: null framelet");
+    if (option != FL_FRAMELET_OPT_FUSED)
+        return fl_set_error(FL_ERR_INVALID, "fl_framelet_option: unknown option %d", option);
+    w->fused = value ? 1 : 0;
+    return fl_set_error(FL_OK, "");
 }
 
 extern "C" int fl_framelet_shrink(fl_framelet* w, const float* coef, float* out, float tau,

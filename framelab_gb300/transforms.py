@@ -38,6 +38,7 @@ class FrameletSystem:
         h = C.c_void_p()
         _lib.check(L.fl_framelet_create(nx, ny, nz, levels, KINDS[kind], C.byref(h)))
         self._h, self._L = h, L
+        self._fused = True
         self.ncoef = int(L.fl_framelet_ncoef(h))
 
     def __del__(self):
@@ -45,6 +46,16 @@ class FrameletSystem:
         if h is not None and h.value:
             self._L.fl_framelet_destroy(h)
             self._h = None
+
+    @property
+    def fused(self) -> bool:
+        """3-D levels through the fused tile kernels (default) or the separable passes."""
+        return self._fused
+
+    @fused.setter
+    def fused(self, on: bool):
+        _lib.check(self._L.fl_framelet_option(self._h, _lib.FRAMELET_OPT_FUSED, int(bool(on))))
+        self._fused = bool(on)
 
     def forward(self, u: torch.Tensor) -> torch.Tensor:
         out = torch.empty(self.ncoef, device=u.device, dtype=torch.float32)

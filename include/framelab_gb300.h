@@ -271,6 +271,12 @@ void fl_framelet_destroy(fl_framelet *fw);
 /* Floats in a coefficient set: every band of every level except the low band
  * of levels below the last (which the synthesis never reads). */
 int64_t fl_framelet_ncoef(const fl_framelet *fw);
+/* FL_FRAMELET_OPT_FUSED (default 1): each 3-D level of the three-tap banks
+ * (linear, Haar) with dilation up to 8 streams along z: the analysis (with
+ * the Bregman update) is one kernel, the synthesis two; 0 selects the
+ * separable pass per axis. Both forms give identical results. */
+enum { FL_FRAMELET_OPT_FUSED = 1 };
+int fl_framelet_option(fl_framelet *fw, int option, int value);
 /* coef = W u (forwardTransform, FraDecMultiLevel3D.m) */
 int fl_framelet_analysis(fl_framelet *fw, const float *u, float *coef, void *stream);
 /* u = W^T coef (adjointTransform, FraRecMultiLevel3D.m) */

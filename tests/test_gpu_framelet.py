@@ -1,5 +1,7 @@
 """Framelet transform, shrink/Bregman step and split Bregman on the GPU against
 the FP64 restatement (oracle/numerics.py)."""
+import zlib
+
 import numpy as np
 import pytest
 
@@ -123,3 +125,49 @@ def test_split_bregman_matches_oracle():
         rel = np.linalg.norm(u - u64) / np.linalg.norm(u64)
         assert rel < (1e-4 if mode == "plain" else 2e-3), (mode, rel)
         assert np.all(np.isfinite(hist)) and hist.size == outer
+
+
+# z-streaming kernels (3-D levels of the three-tap banks, dilation up to 8)
+# against the separable pass per axis: the same fmaf chains, so identical
+# bits. Shapes cover ragged column tiles, fewer slices than a residue class
+# needs and fewer columns than a warp; level 5 (dilation 16) and the cubic
+# bank take the separable passes in both forms.
+FUSED_SHAPES = [(12, 20, 16), (9, 37, 70), (3, 5, 40), (17, 8, 33)]
+
+
+@pytest.mark.parametrize("shape", FUSED_SHAPES)
+@pytest.mark.parametrize("kind", ["linear", "haar", "cubic"])
+@pytest.mark.parametrize("levels", [1, 2, 4, 5])
+def test_fused_levels_bit_identical_to_separable(shape, kind, levels):
+    import torch
+    from framelab_gb300.transforms import FrameletSystem
+    rng = np.random.default_rng(zlib.crc32(repr((shape, kind, levels)).encode()))
+    u = torch.from_numpy(rng.standard_normal(shape).astype(np.float32)).cuda()
+    Atf = torch.from_numpy(rng.standard_normal(shape).astype(np.float32)).cuda()
+    fs = FrameletSystem(shape, kind, levels)
+    out = {}
+    for fused in (True, False):
+        fs.fused = fused
+        c = fs.forward(u)
+        r = fs.adjoint(c)
+        v = c * 0.5
+        t = torch.empty_like(v)
+        b = torch.empty(shape, device="cuda")
+        fs.bregman(u, v, t, Atf, 0.8, 0.05, b)
+        torch.cuda.synchronize()
+        out[fused] = (c, r, v, t, b)
+    for a, bb, what in zip(out[True], out[False], ("W u", "W^T c", "v", "t", "b")):
+        assert torch.equal(a, bb), what
+
+
+def test_fused_reconstructs_large_volume():
+    import torch
+    from framelab_gb300.transforms import FrameletSystem
+    g = torch.Generator(device="cuda").manual_seed(5)
+    u = torch.randn((96, 160, 128), device="cuda", generator=g)
+    fs = FrameletSystem(tuple(u.shape), "linear", 2)
+    c = fs.forward(u)
+    rec = fs.adjoint(c)
+    assert float((rec - u).norm() / u.norm()) < 1e-6               # W^T W = I
+    fs.fused = False
+    assert torch.equal(fs.forward(u), c)
