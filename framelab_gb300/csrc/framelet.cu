@@ -388,6 +388,47 @@ k_syn_zx(BandPtrs bands, const float* __restrict__ low, float* __restrict__ A, l
     }
 }
 
+// The y merge of one synthesis level (k_merge along y into the output, final
+// = base + scale * result), streaming along y: a thread owns one column
+// (x, z) and walks the rows of one residue class mod S, the three y taps of
+// each output row held in a register window per input array.
+constexpr int kSegY = 32;                            // output rows of one class per thread
+
+template <int NF, int S>
+__global__ void __launch_bounds__(128)
+k_merge_y_stream(const float* __restrict__ A, long long N, float* __restrict__ out, int nx,
+                 int ny, int nz, int nseg, Filters R, const float* __restrict__ base,
+                 float scale, int final_)
+{
+    const int x = blockIdx.x * 128 + threadIdx.x, z = blockIdx.y;
+    const int seg = blockIdx.z % nseg, r = blockIdx.z / nseg;
+    const int nfirst = seg * kSegY, nend = min(nfirst + kSegY, class_len(ny, S, r));
+    if (x >= nx || nfirst >= nend) return;
+    const long long zo = (long long)z * ny * nx + x;
+    float win[3][NF], nxt[NF];
+    auto fetch = [&](int n, float (&d)[NF]) {
+        const long long o = zo + (long long)wrapi(r + S * n, ny) * nx;
+#pragma unroll
+        for (int i = 0; i < NF; i++) d[i] = __ldg(A + i * N + o);
+    };
+    fetch(nfirst - 1, win[1]);
+    fetch(nfirst, win[2]);
+    fetch(nfirst + 1, nxt);
+    for (int n = nfirst + 1; n <= nend; n++) {
+#pragma unroll
+        for (int i = 0; i < NF; i++) { win[0][i] = win[1][i]; win[1][i] = win[2][i]; win[2][i] = nxt[i]; }
+        if (n < nend) fetch(n + 1, nxt);
+        float sum = 0.0f;
+#pragma unroll
+        for (int i = 0; i < NF; i++)
+#pragma unroll
+            for (int t = 0; t < 3; t++) sum = fmaf(R.f[i][t], win[t][i], sum);
+        const long long q = zo + (long long)(r + S * (n - 1)) * nx;
+        if (final_) sum = (base ? __ldg(base + q) : 0.0f) + scale * sum;
+        out[q] = sum;
+    }
+}
+
 unsigned grid_for(long long n)
 {
     long long g = (n + 255) / 256;
@@ -587,8 +628,7 @@ static void synthesis_level(fl_framelet* w, const BandPtrs& cb, const float* low
 
 // z-streaming form of a 3-D level (three-tap banks, dilation up to
 // kMaxStreamStep): analysis in one kernel; synthesis as the z + x merges in
-// one kernel and the y merge (with the final base + scale) as the separable
-// pass. Returns false when the level needs the separable passes.
+// one kernel and the y merge (with the final base + scale) streaming along y.
 static bool stream_ok(const fl_framelet* w, int step)
 {
     return w->fused && w->dim == 3 && w->D.nt == 3 && step <= kMaxStreamStep;
@@ -619,10 +659,10 @@ static void syn_stream(fl_framelet* w, const BandPtrs& cb, const float* low, flo
     const dim3 grid(fl_div_up(w->nx, kSX - 2 * S), fl_div_up(w->ny, kSY),
                     (unsigned)(nseg * NF * S));
     k_syn_zx<NF, S><<<grid, kST, 0, s>>>(cb, low, A, N, w->nx, w->ny, w->nz, nseg, w->R);
-    BandPtrs ab;
-    for (int b = 0; b < kMaxBands; b++) ab.p[b] = b < NF ? A + (long long)b * N : nullptr;
-    Pass<NF, 3>::merge(w->axes[0], pass_grid(w, 1), s, ab, nullptr, dst, N, w->nx, w->ny, w->nz,
-                       S, w->R, base, scale, final_);
+    const int nsegy = fl_div_up(class_len(w->ny, S, 0), kSegY);
+    const dim3 gy(fl_div_up(w->nx, 128), w->nz, (unsigned)(nsegy * S));
+    k_merge_y_stream<NF, S><<<gy, 128, 0, s>>>(A, N, dst, w->nx, w->ny, w->nz, nsegy, w->R, base,
+                                               scale, final_);
 }
 
 template <int NF>
