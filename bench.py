@@ -67,6 +67,9 @@ WORKLOADS = {
     # split Bregman on 256^3 from 90 views, Poisson counts at I0 = 1e5
     "sb256": dict(kind="sb", n=256, nv=90, na=512, nb=384, det_mm=1.0, vox_mm=1.0, SO=600.0,
                   SD=1200.0, I0=1e5, pmax=4.0, lam=0.01, mu=1.0, inner=5, levels=2),
+    # the same solve on 128^3 (small case for ncu captures of the framelet kernels)
+    "sb128": dict(kind="sb", n=128, nv=90, na=256, nb=192, det_mm=2.0, vox_mm=2.0, SO=600.0,
+                  SD=1200.0, I0=1e5, pmax=4.0, lam=0.01, mu=1.0, inner=5, levels=2),
 }
 REFRESH = 10
 
@@ -147,7 +150,8 @@ def describe(name, w, world):
               f"panel @ {w['det_mm']} mm, {w['levels']}-level linear framelet, "
               f"lam {w['lam']}, mu {w['mu']}, {w['inner']} CGLS per outer iteration")
         metric = "split-Bregman outer iter/s (cone-beam, 2-level linear framelet)"
-        l2 = "working set > L2 (framelet coefficients 2 x 3.4 GiB)"
+        nc = 53 * 4 * w["n"] ** 3            # 26 + 27 bands of the 2-level linear framelet
+        l2 = f"working set > L2 (framelet coefficients 2 x {nc / 2**30:.2f} GiB)"
         data = (f"synthetic: seeded 12-ellipsoid phantom scaled to max line integral "
                 f"{w['pmax']}, Poisson counts at I0 = {w['I0']:.0e}")
     config = {"workload": wl, "global_batch": world, "l2": l2,
