@@ -14,7 +14,8 @@ from . import build as _build
 _lock = threading.Lock()
 _lib = None
 
-FL_OK, FL_ERR_INVALID, FL_ERR_UNSUPPORTED, FL_ERR_CUDA, FL_ERR_ALLOC, FL_ERR_TIMEOUT = range(6)
+(FL_OK, FL_ERR_INVALID, FL_ERR_UNSUPPORTED, FL_ERR_CUDA, FL_ERR_ALLOC, FL_ERR_TIMEOUT,
+ FL_ERR_NUMERIC) = range(7)
 MODEL_SIDDON_REF, MODEL_CHORD_REF, MODEL_GAO_REF, MODEL_FB_REF, MODEL_MATCHED = 0, 1, 2, 3, 16
 F32, F16, BF16 = 0, 1, 2
 OPT_Z_MIRROR = 1

@@ -101,9 +101,10 @@ class FanBatch:
         n = len(self.plans)
         hist = np.zeros((n, max(iters, 1)), np.float64)
         done = np.zeros(n, np.int32)
-        _lib.check(self._L.fl_batch_cgls(self._h, rhs.data_ptr(), u.data_ptr(), float(lam),
-                                         int(iters), float(tol), flags, hist.ctypes.data,
-                                         done.ctypes.data, _stream()))
+        st = self._L.fl_batch_cgls(self._h, rhs.data_ptr(), u.data_ptr(), float(lam), int(iters),
+                                   float(tol), flags, hist.ctypes.data, done.ctypes.data,
+                                   _stream())
         self.history = hist[:, :iters]
-        self.iters_done = done
+        self.iters_done = done                # per slice, also when a slice stopped on NaN / Inf
+        _lib.check(st)
         return u

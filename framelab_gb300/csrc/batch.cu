@@ -54,6 +54,7 @@ struct BatchSlice {
 struct BatchScal {
     double gamma, alpha, beta;
     int done, iter;
+    int status;            // 1: stopped by a non-finite gamma or <p, q>
 };
 
 struct VecChunk {
@@ -185,7 +186,8 @@ k_batch_init(const float* __restrict__ bvec, const float* __restrict__ q,
     if (slice_sum(s, c.slice, b.vc0, b.vc1, partials, tickets, tot) && threadIdx.x == 0) {
         BatchScal& z = S[c.slice];
         z.gamma = tot; z.alpha = 0.0; z.beta = 0.0; z.iter = 0;
-        z.done = 0;
+        z.done = 0; z.status = 0;
+        if (!isfinite(tot)) { z.done = 1; z.status = 1; }
     }
 }
 
@@ -210,8 +212,13 @@ k_batch_pq(const float* __restrict__ p, float* __restrict__ q, float lam,
     double tot;
     if (slice_sum(s, c.slice, b.vc0, b.vc1, partials, tickets, tot) && threadIdx.x == 0) {
         BatchScal& z = S[c.slice];
-        if (tot != 0.0) z.alpha = z.gamma / tot;
-        else { z.alpha = 0.0; z.done = 1; }
+        const double a = z.gamma / tot;
+        if (tot > 0.0 && isfinite(a)) {
+            z.alpha = a;
+        } else {
+            z.alpha = 0.0; z.done = 1;
+            if (!isfinite(tot) || !isfinite(z.gamma)) z.status = 1;
+        }
     }
 }
 
@@ -238,6 +245,7 @@ k_batch_update(float* __restrict__ u, float* __restrict__ r, const float* __rest
     double tot;
     if (slice_sum(s, c.slice, b.vc0, b.vc1, partials, tickets, tot) && threadIdx.x == 0) {
         BatchScal& z = S[c.slice];
+        if (!isfinite(tot)) { z.done = 1; z.status = 1; return; }
         z.beta = tot / z.gamma;
         z.gamma = tot;
         if (hist && z.iter < hist_cap) hist[(long long)c.slice * hist_cap + z.iter] = tot;
@@ -524,6 +532,12 @@ extern "C" int fl_batch_cgls(fl_batch* b, const float* rhs, float* u, float lam,
                 gamma_history[(size_t)i * iters + k] =
                     (k < nh && k < fin[i].iter) ? h[(size_t)i * b->hist_cap + k] : 0.0;
     }
+    for (int i = 0; i < b->n; i++)
+        if (fin[i].status)
+            return fl_set_error(FL_ERR_NUMERIC,
+                                "fl_batch_cgls: slice %d stopped on a non-finite residual or "
+                                "curvature after %d iterations (the other slices completed)",
+                                i, fin[i].iter);
     return fl_set_error(FL_OK, "");
 }
 

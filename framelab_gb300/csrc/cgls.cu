@@ -14,6 +14,7 @@
 //    u (r = (A^T A + lam) u - b).
 // Both stop early once gamma < tol, like the reference; in the graph this is a
 // device flag that turns the remaining replays into no-ops.
+#include <cmath>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -29,8 +30,9 @@ struct CgScalars {
     float lam;
     float p_scale;     // p16 = p * p_scale
     float p_unscale;   // 1 / p_scale (forward applies it to the gathered sum)
-    int done;          // 1 once gamma < tol
+    int done;          // 1 once gamma < tol, or at a breakdown (see status)
     int iter;          // iterations completed
+    int status;        // 1: a non-finite gamma or <p, q> (NaN / Inf in b, u0 or A) stopped it
     unsigned ticket;   // last-block detection for the fused reductions
 };
 
@@ -120,6 +122,10 @@ k_cg_init(const float* __restrict__ bvec, const float* __restrict__ q, float* __
         S->gamma = tot;
         S->done = 0;
         S->iter = 0;
+        // a zero residual is already the solution (the reference loop would go
+        // on to 0/0); a non-finite one stops with status 1
+        if (!isfinite(tot)) { S->done = 1; S->status = 1; }
+        else if (tot == 0.0) S->done = 1;
         double rms = sqrt(tot / (double)n);
         S->p_scale = rms > 0 ? (float)(1.0 / (8.0 * rms)) : 1.0f;
         S->p_unscale = 1.0f / S->p_scale;
@@ -153,7 +159,15 @@ k_cg_pq(const float* __restrict__ p, float* __restrict__ q, long long n, CgScala
         s += (double)pi * qi;
     }
     double tot;
-    if (grid_sum(s, partials, &S->ticket, tot) && threadIdx.x == 0) S->alpha = S->gamma / tot;
+    if (grid_sum(s, partials, &S->ticket, tot) && threadIdx.x == 0) {
+        const double a = S->gamma / tot;
+        if (tot > 0.0 && isfinite(a)) {
+            S->alpha = a;
+        } else {                       // breakdown: stop before u is touched
+            S->done = 1;
+            if (!isfinite(tot) || !isfinite(S->gamma)) S->status = 1;
+        }
+    }
 }
 
 // u += alpha p ; r += alpha q ; gamma' = <r, r> ; beta = gamma'/gamma ; stop test
@@ -174,6 +188,7 @@ k_cg_update(float* __restrict__ u, float* __restrict__ r, const float* __restric
     }
     double tot;
     if (grid_sum(s, partials, &S->ticket, tot) && threadIdx.x == 0) {
+        if (!isfinite(tot)) { S->done = 1; S->status = 1; return; }
         S->beta = tot / S->gamma;
         S->gamma = tot;
         if (hist && S->iter < hist_cap) hist[S->iter] = tot;
@@ -213,7 +228,10 @@ k_cg_refresh(const float* __restrict__ bvec, const float* __restrict__ q, float*
         s += (double)ri * ri;
     }
     double tot;
-    if (grid_sum(s, partials, &S->ticket, tot) && threadIdx.x == 0) S->gamma = tot;
+    if (grid_sum(s, partials, &S->ticket, tot) && threadIdx.x == 0) {
+        S->gamma = tot;
+        if (!isfinite(tot)) { S->done = 1; S->status = 1; }
+    }
 }
 
 int sm_count()
@@ -408,6 +426,14 @@ static int plain_dot(fl_cgls* c, const float* a, const float* b, double* host, c
     return fl_check_cuda(cudaStreamSynchronize(s), "cudaStreamSynchronize");
 }
 
+static int nonfinite(int it, int* done_iters)
+{
+    if (done_iters) *done_iters = it;
+    return fl_set_error(FL_ERR_NUMERIC,
+                        "fl_cgls_solve: non-finite residual or curvature after %d iterations "
+                        "(NaN or Inf in b, u0 or the operator)", it);
+}
+
 static int solve_plain(fl_cgls* c, const float* b, float* u, float lam, int iters, double tol,
                        int flags, double* hist, int* done_iters, cudaStream_t s)
 {
@@ -429,16 +455,21 @@ static int solve_plain(fl_cgls* c, const float* b, float* u, float lam, int iter
     double gamma;
     if ((st = plain_dot(c, c->r, c->r, &gamma, s))) return st;
     int it = 0;
+    if (!std::isfinite(gamma)) return nonfinite(0, done_iters);
+    if (gamma == 0.0) iters = 0;                 // u0 already solves it
     while (it < iters) {
-        it++;
         if ((st = normal_apply(c, c->p, c->q, lam, s))) return st;
         double pq;
         if ((st = plain_dot(c, c->p, c->q, &pq, s))) return st;
+        if (!std::isfinite(pq)) return nonfinite(it, done_iters);
+        if (!(pq > 0.0)) break;                  // breakdown: stop before u is touched
+        it++;
         float alpha = (float)(gamma / pq);
         k_axpby<<<g, kThreads, 0, s>>>(u, c->p, alpha, 1.0f, n);
         k_axpby<<<g, kThreads, 0, s>>>(c->r, c->q, alpha, 1.0f, n);
         double gnew;
         if ((st = plain_dot(c, c->r, c->r, &gnew, s))) return st;
+        if (!std::isfinite(gnew)) return nonfinite(it, done_iters);
         float beta = (float)(gnew / gamma);
         k_axpby<<<g, kThreads, 0, s>>>(c->p, c->r, -1.0f, beta, n);
         if ((st = fl_check_launch("cgls iteration"))) return st;
@@ -551,6 +582,7 @@ static int solve_mixed(fl_cgls* c, const float* b, float* u, float lam, int iter
     FL_CUDA(cudaStreamSynchronize(s));
     if (hist) for (int k = 0; k < nh && k < fin.iter; k++) hist[k] = h[k];
     if (done_iters) *done_iters = fin.iter;
+    if (fin.status) return nonfinite(fin.iter, done_iters);
     return FL_OK;
 }
 

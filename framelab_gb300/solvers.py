@@ -66,11 +66,12 @@ class NativeCGLS:
         flags = ZERO_START if zero_start else 0
         hist = np.zeros(max(iters, 1), np.float64)
         nd = C.c_int()
-        _lib.check(self._L.fl_cgls_solve(self._h, b.data_ptr(), u.data_ptr(), float(lam),
-                                         int(iters), float(tol), int(refresh), flags,
-                                         hist.ctypes.data, C.byref(nd), _stream()))
-        self.iters_done = nd.value
+        st = self._L.fl_cgls_solve(self._h, b.data_ptr(), u.data_ptr(), float(lam), int(iters),
+                                   float(tol), int(refresh), flags, hist.ctypes.data,
+                                   C.byref(nd), _stream())
+        self.iters_done = nd.value            # also set when the solve stopped on an error
         self.history = hist[:nd.value].tolist()
+        _lib.check(st)
         return u
 
     def solve_host(self, b: np.ndarray, u: np.ndarray, lam: float = 0.0, iters: int = 20,
@@ -78,10 +79,11 @@ class NativeCGLS:
         """Host-buffer solve (pinned or pageable numpy float32 arrays); u is overwritten."""
         hist = np.zeros(max(iters, 1), np.float64)
         nd = C.c_int()
-        _lib.check(self._L.fl_cgls_solve_host(self._h, b.ctypes.data, u.ctypes.data, float(lam),
-                                              int(iters), float(tol), int(refresh),
-                                              ZERO_START if zero_start else 0, hist.ctypes.data,
-                                              C.byref(nd), _stream()))
+        st = self._L.fl_cgls_solve_host(self._h, b.ctypes.data, u.ctypes.data, float(lam),
+                                        int(iters), float(tol), int(refresh),
+                                        ZERO_START if zero_start else 0, hist.ctypes.data,
+                                        C.byref(nd), _stream())
         self.iters_done = nd.value
         self.history = hist[:nd.value].tolist()
+        _lib.check(st)
         return u

@@ -38,7 +38,8 @@ enum {
     FL_ERR_UNSUPPORTED = 2,  /* valid but not implemented for this case */
     FL_ERR_CUDA = 3,         /* a CUDA runtime call or a kernel failed */
     FL_ERR_ALLOC = 4,        /* device or host allocation failed */
-    FL_ERR_TIMEOUT = 5       /* a bounded device-side wait gave up */
+    FL_ERR_TIMEOUT = 5,      /* a bounded device-side wait gave up */
+    FL_ERR_NUMERIC = 6       /* a solve met NaN / Inf (in its inputs or the operator) */
 };
 
 /* Status of the last call made on this host thread, and its message. */

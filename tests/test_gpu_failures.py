@@ -68,3 +68,57 @@ def test_allocation_failures_are_clean_errors():
     again = _workload(p, x, f, fan)
     for a, r in zip(again, ref):
         assert np.array_equal(a, r)
+
+
+@pytest.mark.parametrize("mode", ["plain", "graph", "mixed"])
+def test_nonfinite_rhs_stops_with_numeric_error(mode):
+    import torch
+    from framelab_gb300 import _lib
+    from framelab_gb300.projector import Plan
+    from framelab_gb300.solvers import NativeCGLS
+    p = G.cone_para_mm(24, 12, 36, 28, det_pitch_mm=8.0, SO_mm=600.0, SD_mm=1200.0,
+                       voxel_mm=8.0)
+    P = Plan(p)
+    x = torch.from_numpy(PH.ellipsoids_3d(24, seed=2).reshape(-1)).cuda()
+    b = P.adjoint(P.forward(x)).reshape(-1).contiguous()
+    cg = NativeCGLS(P, mode)
+    want = cg.solve(b, iters=4).clone()
+    bad = b.clone()
+    bad[1234] = float("nan")
+    with pytest.raises(_lib.FLError) as e:
+        cg.solve(bad, iters=4)
+    assert e.value.code == _lib.FL_ERR_NUMERIC
+    assert cg.iters_done == 0
+    # the workspace is still good: the same solve gives the same bits
+    assert torch.equal(cg.solve(b, iters=4), want)
+
+
+@pytest.mark.parametrize("mode", ["plain", "graph", "mixed"])
+def test_zero_rhs_returns_the_start_without_iterating(mode):
+    import torch
+    from framelab_gb300.projector import Plan
+    from framelab_gb300.solvers import NativeCGLS
+    p = G.cone_para_mm(16, 8, 24, 20, det_pitch_mm=8.0, SO_mm=600.0, SD_mm=1200.0,
+                       voxel_mm=8.0)
+    P = Plan(p)
+    cg = NativeCGLS(P, mode)
+    u = cg.solve(torch.zeros(P.n_vox, device="cuda"), iters=5)
+    assert cg.iters_done == 0
+    assert bool(torch.all(u == 0))
+
+
+def test_batch_nonfinite_slice_is_reported_and_others_complete():
+    import torch
+    from framelab_gb300 import _lib
+    from framelab_gb300.batch import FanBatch
+    paras = [G.fan_para(n, n, 2 * n, v, L=(1, 1)) for n, v in ((24, 9), (32, 12), (20, 7))]
+    B = FanBatch(paras)
+    rhs = B.adjoint(B.forward(torch.ones(B.n_vox, device="cuda")))
+    good = B.cgls(rhs, iters=4).clone()
+    bad = rhs.clone()
+    B.images(bad)[1][3, 4] = float("inf")
+    with pytest.raises(_lib.FLError) as e:
+        B.cgls(bad, iters=4)
+    assert e.value.code == _lib.FL_ERR_NUMERIC and "slice 1" in str(e.value)
+    assert list(B.iters_done) == [4, 0, 4]      # the other slices ran to the end
+    assert torch.equal(B.cgls(rhs, iters=4), good)
