@@ -140,7 +140,8 @@ k_batch_weight(float* __restrict__ YW, const float* __restrict__ Y,
 }
 
 // x = A^T (pre-weighted yw), one block per chunk of 2 image rows x
-// 2*kPixChunk columns, one thread per 2 x 2 pixel block
+// 2*kPixChunk columns, one thread per 2 x 2 pixel block (all view groups in
+// the thread: the single-scan kernel's bits)
 __global__ void __launch_bounds__(kPixChunk)
 k_batch_adj(float* __restrict__ X, const float* __restrict__ YW,
             const BatchSlice* __restrict__ sl, const int4* __restrict__ chunks,
@@ -152,8 +153,8 @@ k_batch_adj(float* __restrict__ X, const float* __restrict__ YW,
     const int ix0 = ch.z + 2 * threadIdx.x, iy0 = ch.y;
     if (ix0 >= b.nx) return;
     float acc[2][2];
-    fan_block_gather<2, 2>(acc, YW + b.yoff, b.col, b.view, b.views, b.nvf, b.G, ix0, iy0,
-                           b.nx, b.ny, b.na);
+    fan_block_gather_all<2, 2>(acc, YW + b.yoff, b.col, b.view, b.views, b.nvf, b.G, ix0, iy0,
+                               b.nx, b.ny, b.na);
     float* xs = X + b.xoff;
 #pragma unroll
     for (int j = 0; j < 2; j++)

@@ -183,23 +183,39 @@ __global__ void k_weight(float* __restrict__ yw, const TY* __restrict__ y,
 // ---------------------------------------------------------------------------
 // Fan adjoint: one thread per (pixel, frame).
 // ---------------------------------------------------------------------------
-// Fan adjoint: one thread per P x P pixel block of one frame (P = 2 for
-// images large enough to fill the GPU, else 1).
-template <typename TX, int P>
+// Fan adjoint of one P x P pixel block of one frame per thread. Small images
+// (GROUPED, P = 1): blocks of kFanX x kFanGroups threads, thread (x, g)
+// gathers view group g and group 0 writes the combined sums, so that four
+// times as many threads share the views. Large images (P = 2): blocks of 128
+// threads, each gathering all groups itself. Both give the same bits.
+constexpr int kFanX = 32;
+
+template <typename TX, int P, bool GROUPED>
 __global__ void __launch_bounds__(128)
 k_adj_fan(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __restrict__ col,
           const ViewEntry* __restrict__ view, const int* __restrict__ idY,
           const int* __restrict__ Nv, int tmp_size, DetGrid G, int nx, int ny, int na,
           const int* __restrict__ skip)
 {
-    if (skip && *skip) return;
+    if (skip && *skip) return;                 // uniform (one flag for the launch)
     const int ix0 = P * (blockIdx.x * blockDim.x + threadIdx.x);
     const int iy0 = P * blockIdx.y;
     const int it = blockIdx.z;
-    if (ix0 >= nx) return;
     float acc[P][P];
-    fan_block_gather<P, P>(acc, yw, col, view, idY + it * tmp_size, Nv[it], G, ix0, iy0, nx,
-                           ny, na);
+    if (GROUPED) {
+#pragma unroll
+        for (int j = 0; j < P; j++)
+#pragma unroll
+            for (int i = 0; i < P; i++) acc[j][i] = 0.0f;
+        if (ix0 < nx)
+            fan_block_gather<P, P>(acc, yw, col, view, idY + it * tmp_size, Nv[it], G, ix0, iy0,
+                                   nx, ny, na, threadIdx.y);
+        if (!fan_combine_groups<P, kFanX>(acc) || ix0 >= nx) return;
+    } else {
+        if (ix0 >= nx) return;
+        fan_block_gather_all<P, P>(acc, yw, col, view, idY + it * tmp_size, Nv[it], G, ix0, iy0,
+                                   nx, ny, na);
+    }
     TX* xf = X + (long long)it * nx * ny;
 #pragma unroll
     for (int j = 0; j < P; j++)
@@ -458,18 +474,19 @@ void launch_adj(fl_plan* p, const float* yw, void* x, const int* skip, int xfold
                 s.nx, s.ny, s.nz, s.na, s.nb, s.dz, zruns, skip, 0);
         }
     } else {
-        // 2 x 2 blocks once there are at least 4 waves of 128-thread blocks
+        // 2 x 2 pixel blocks, one thread each, once there are at least 4 waves
+        // of 128-thread blocks; else one pixel per view group
         const long long blocks2 = (long long)fl_div_up(s.nx, 2 * 128) * ((s.ny + 1) / 2) * s.nt;
         if (blocks2 >= 4LL * 152) {
             dim3 grid(fl_div_up(s.nx, 2 * 128), (s.ny + 1) / 2, s.nt);
-            k_adj_fan<TX, 2><<<grid, 128, 0, st>>>((TX*)x, yw, p->d_col, p->d_view, p->d_idY,
-                                                    p->d_Nv, p->tmp_size, G, s.nx, s.ny, s.na,
-                                                    skip);
+            k_adj_fan<TX, 2, false><<<grid, 128, 0, st>>>((TX*)x, yw, p->d_col, p->d_view,
+                                                           p->d_idY, p->d_Nv, p->tmp_size, G,
+                                                           s.nx, s.ny, s.na, skip);
         } else {
-            dim3 grid(fl_div_up(s.nx, 128), s.ny, s.nt);
-            k_adj_fan<TX, 1><<<grid, 128, 0, st>>>((TX*)x, yw, p->d_col, p->d_view, p->d_idY,
-                                                    p->d_Nv, p->tmp_size, G, s.nx, s.ny, s.na,
-                                                    skip);
+            dim3 grid(fl_div_up(s.nx, kFanX), s.ny, s.nt);
+            k_adj_fan<TX, 1, true><<<grid, dim3(kFanX, kFanGroups), 0, st>>>(
+                (TX*)x, yw, p->d_col, p->d_view, p->d_idY, p->d_Nv, p->tmp_size, G, s.nx, s.ny,
+                s.na, skip);
         }
     }
 }

@@ -167,13 +167,52 @@ __device__ __forceinline__ void column_window(const DetGrid& G, float c, float s
 }
 
 // Fan adjoint of a PX x PY block of pixels with lower corner (ix0, iy0): for
-// every view of `views[0..nvf)` and every ray whose column window covers the
-// block, w_rV * yw_r is added to each pixel the ray crosses, w_rV evaluated
-// from the same crossing table as the forward walk. A pixel's sum runs over
-// the views in order and the columns in increasing order, and only rays with
-// w > 0 add to it, so each pixel's result does not depend on the block shape:
-// the block's window contains every pixel's own window (the corners' column
-// shadow with 0.02 columns of slack is far wider than the FP32 error of w).
+// the views views[g], views[g + kFanGroups], ... (view group g of nvf views)
+// and every ray whose column window covers the block, w_rV * yw_r is added to
+// each pixel the ray crosses, w_rV evaluated from the same crossing table as
+// the forward walk. A group's sum runs over its views in order and the
+// columns in increasing order, and only rays with w > 0 add to it, so each
+// pixel's result does not depend on the block shape: the block's window
+// contains every pixel's own window (the corners' column shadow with 0.02
+// columns of slack is far wider than the FP32 error of w). The groups' sums
+// are then added in the order g = 0, 1, ... (fan_combine_groups).
+constexpr int kFanGroups = 4;
+
+// One view of the fan gather: adds w_rV * yw_r for every ray of view iv whose
+// column window covers the block.
+template <int PX, int PY>
+__device__ __forceinline__ void fan_view_gather(float (&acc)[PY][PX], const float* __restrict__ yw,
+                                                const ColEntry* __restrict__ col,
+                                                const ViewEntry& ve, int iv, const DetGrid& G,
+                                                float x0, float y0, const float (&fx)[PX + 1],
+                                                const float (&fy)[PY + 1], int na)
+{
+    int lo, hi; float dmin, dmax;
+    column_window(G, ve.c, ve.s, x0, y0, (float)PX, (float)PY, na, lo, hi, dmin, dmax);
+    const ColEntry* cv = col + (long long)iv * na;
+    const float* yv = yw + (long long)iv * na;
+    for (int ia = lo; ia <= hi; ia++) {
+        if (!FL_IN(ia, na)) continue;
+        const ColEntry ce = cv[ia];
+        const float yval = __ldg(yv + ia);
+        float ax[PX + 1], ay[PY + 1];
+#pragma unroll
+        for (int i = 0; i <= PX; i++) ax[i] = fmaf(fx[i], ce.inv_x, ce.off_x);
+#pragma unroll
+        for (int j = 0; j <= PY; j++) ay[j] = fmaf(fy[j], ce.inv_y, ce.off_y);
+#pragma unroll
+        for (int j = 0; j < PY; j++)
+#pragma unroll
+            for (int i = 0; i < PX; i++) {
+                const float l = fmaxf(fminf(ax[i], ax[i + 1]), fminf(ay[j], ay[j + 1]));
+                const float h = fminf(fmaxf(ax[i], ax[i + 1]), fmaxf(ay[j], ay[j + 1]));
+                const float w = h - l;
+                if (w > 0.0f) acc[j][i] = fmaf(w, yval, acc[j][i]);
+            }
+    }
+}
+
+// View group g alone (one thread per group; fan_combine_groups adds them).
 template <int PX, int PY>
 __device__ __forceinline__ void fan_block_gather(float (&acc)[PY][PX],
                                                  const float* __restrict__ yw,
@@ -181,7 +220,7 @@ __device__ __forceinline__ void fan_block_gather(float (&acc)[PY][PX],
                                                  const ViewEntry* __restrict__ view,
                                                  const int* __restrict__ views, int nvf,
                                                  const DetGrid& G, int ix0, int iy0, int nx,
-                                                 int ny, int na)
+                                                 int ny, int na, int g)
 {
     const float x0 = (float)(ix0 - nx / 2), y0 = (float)(iy0 - ny / 2);
     float fx[PX + 1], fy[PY + 1];
@@ -193,33 +232,94 @@ __device__ __forceinline__ void fan_block_gather(float (&acc)[PY][PX],
     for (int j = 0; j < PY; j++)
 #pragma unroll
         for (int i = 0; i < PX; i++) acc[j][i] = 0.0f;
+    for (int jv = g; jv < nvf; jv += kFanGroups) {
+        const int iv = views[jv];
+        fan_view_gather<PX, PY>(acc, yw, col, view[iv], iv, G, x0, y0, fx, fy, na);
+    }
+}
+
+// Every view group in one thread: the views in order, each into its group's
+// own sums (register sets rotated once per view), then
+// ((S_0 + S_1) + S_2) + S_3 -- the same bits as one thread per group and
+// fan_combine_groups, without the extra threads (for launches that fill the
+// GPU anyway).
+template <int PX, int PY>
+__device__ __forceinline__ void fan_block_gather_all(float (&acc)[PY][PX],
+                                                     const float* __restrict__ yw,
+                                                     const ColEntry* __restrict__ col,
+                                                     const ViewEntry* __restrict__ view,
+                                                     const int* __restrict__ views, int nvf,
+                                                     const DetGrid& G, int ix0, int iy0, int nx,
+                                                     int ny, int na)
+{
+    const float x0 = (float)(ix0 - nx / 2), y0 = (float)(iy0 - ny / 2);
+    float fx[PX + 1], fy[PY + 1];
+#pragma unroll
+    for (int i = 0; i <= PX; i++) fx[i] = (float)(ix0 + i);
+#pragma unroll
+    for (int j = 0; j <= PY; j++) fy[j] = (float)(iy0 + j);
+    // part[0] always holds the group of the next view: after each view the
+    // groups rotate one place, and after the loop back into group order
+    float part[kFanGroups][PY][PX];
+#pragma unroll
+    for (int g = 0; g < kFanGroups; g++)
+#pragma unroll
+        for (int j = 0; j < PY; j++)
+#pragma unroll
+            for (int i = 0; i < PX; i++) part[g][j][i] = 0.0f;
+    auto rotate = [&]() {
+#pragma unroll
+        for (int j = 0; j < PY; j++)
+#pragma unroll
+            for (int i = 0; i < PX; i++) {
+                const float t = part[0][j][i];
+#pragma unroll
+                for (int g = 0; g < kFanGroups - 1; g++) part[g][j][i] = part[g + 1][j][i];
+                part[kFanGroups - 1][j][i] = t;
+            }
+    };
     for (int jv = 0; jv < nvf; jv++) {
         const int iv = views[jv];
-        const ViewEntry ve = view[iv];
-        int lo, hi; float dmin, dmax;
-        column_window(G, ve.c, ve.s, x0, y0, (float)PX, (float)PY, na, lo, hi, dmin, dmax);
-        const ColEntry* cv = col + (long long)iv * na;
-        const float* yv = yw + (long long)iv * na;
-        for (int ia = lo; ia <= hi; ia++) {
-            if (!FL_IN(ia, na)) continue;
-            const ColEntry ce = cv[ia];
-            const float yval = __ldg(yv + ia);
-            float ax[PX + 1], ay[PY + 1];
-#pragma unroll
-            for (int i = 0; i <= PX; i++) ax[i] = fmaf(fx[i], ce.inv_x, ce.off_x);
-#pragma unroll
-            for (int j = 0; j <= PY; j++) ay[j] = fmaf(fy[j], ce.inv_y, ce.off_y);
-#pragma unroll
-            for (int j = 0; j < PY; j++)
-#pragma unroll
-                for (int i = 0; i < PX; i++) {
-                    const float l = fmaxf(fminf(ax[i], ax[i + 1]), fminf(ay[j], ay[j + 1]));
-                    const float h = fminf(fmaxf(ax[i], ax[i + 1]), fmaxf(ay[j], ay[j + 1]));
-                    const float w = h - l;
-                    if (w > 0.0f) acc[j][i] = fmaf(w, yval, acc[j][i]);
-                }
-        }
+        fan_view_gather<PX, PY>(part[0], yw, col, view[iv], iv, G, x0, y0, fx, fy, na);
+        rotate();
     }
+    for (int k = (kFanGroups - nvf % kFanGroups) % kFanGroups; k > 0; k--) rotate();
+#pragma unroll
+    for (int j = 0; j < PY; j++)
+#pragma unroll
+        for (int i = 0; i < PX; i++) {
+            float s = part[0][j][i];
+#pragma unroll
+            for (int g = 1; g < kFanGroups; g++) s += part[g][j][i];
+            acc[j][i] = s;
+        }
+}
+
+// The kFanGroups view groups of a pixel block are the threads (x, g) of a
+// block of NX x kFanGroups threads; their sums meet in shared memory and
+// group 0 returns true holding ((S_0 + S_1) + S_2) + S_3. Every thread of the
+// block must call it (it synchronises the block).
+template <int P, int NX>
+__device__ __forceinline__ bool fan_combine_groups(float (&acc)[P][P])
+{
+    __shared__ float part[kFanGroups][P * P][NX];
+    const int tx = threadIdx.x, g = threadIdx.y;
+#pragma unroll
+    for (int j = 0; j < P; j++)
+#pragma unroll
+        for (int i = 0; i < P; i++) part[g][j * P + i][tx] = acc[j][i];
+    __syncthreads();
+    if (g != 0) return false;
+#pragma unroll
+    for (int j = 0; j < P; j++)
+#pragma unroll
+        for (int i = 0; i < P; i++) {
+            float s = part[0][j * P + i][tx];
+#pragma unroll
+            for (int k = 1; k < kFanGroups; k++) s += part[k][j * P + i][tx];
+            acc[j][i] = s;
+        }
+    return true;
 }
 
 }  // namespace
