@@ -19,6 +19,7 @@ _lib = None
 MODEL_SIDDON_REF, MODEL_CHORD_REF, MODEL_GAO_REF, MODEL_FB_REF, MODEL_MATCHED = 0, 1, 2, 3, 16
 F32, F16, BF16 = 0, 1, 2
 OPT_Z_MIRROR = 1
+OPT_ROT_MIRROR = 2
 FRAMELET_OPT_FUSED = 1
 
 

@@ -53,6 +53,14 @@ struct fl_plan {
     // for b < nb/2, so one walk / one weight serves both rays.
     int zmirror_ok;            // the geometry allows it
     int zmirror;               // in use (FL_OPT_Z_MIRROR)
+    // half-turn symmetry on top of the z mirror: one frame, an even number of
+    // views with view v + nv/2 opposite view v (sources and detector turned by
+    // pi about the z axis), even nx and ny. The matched model then defines
+    // A[(v + nv/2, a, b), (nx-1-x, ny-1-y, z)] = A[(v, a, b), (x, y, z)] for
+    // v < nv/2 (with c_r of view v), so one walk / one weight serves four
+    // rays: rows b and nb-1-b of views v and v + nv/2.
+    int rot_ok;                // the geometry allows it
+    int rot;                   // in use (FL_OPT_ROT_MIRROR; only with zmirror)
     // reusable scratch: sinogram-sized f32 for the pre-weighted adjoint input,
     // volume-sized for the z-folded copy of a forward input
     float *d_work;

@@ -206,6 +206,21 @@ static int build_tables(fl_plan* p, const std::vector<float>& phi, const float* 
         p->zmirror_ok = ok ? 1 : 0;
     }
     p->zmirror = p->zmirror_ok;
+    // half-turn symmetry (fl_plan.h): view v + nv/2 is view v turned by pi to
+    // within 1e-6 in cos and sin (FP32 angles such as 2 pi k / nv are never
+    // exactly opposite), one frame, even nx and ny
+    p->rot_ok = 0;
+    if (p->zmirror_ok && s.nt == 1 && s.nv % 2 == 0 && s.nx % 2 == 0 && s.ny % 2 == 0) {
+        bool ok = true;
+        const int h = s.nv / 2;
+        for (int iv = 0; iv < h && ok; iv++) {
+            const double c0 = std::cos((double)phi[iv]), s0 = std::sin((double)phi[iv]);
+            const double c1 = std::cos((double)phi[iv + h]), s1 = std::sin((double)phi[iv + h]);
+            if (std::fabs(c0 + c1) > 1e-6 || std::fabs(s0 + s1) > 1e-6) ok = false;
+        }
+        p->rot_ok = ok ? 1 : 0;
+    }
+    p->rot = p->rot_ok;
     return FL_OK;
 }
 
@@ -216,6 +231,10 @@ extern "C" int fl_plan_option(fl_plan* p, int option, int value)
         p->zmirror = (value && p->zmirror_ok) ? 1 : 0;
         return fl_set_error(FL_OK, "");
     }
+    if (option == FL_OPT_ROT_MIRROR) {
+        p->rot = (value && p->rot_ok) ? 1 : 0;
+        return fl_set_error(FL_OK, "");
+    }
     return fl_set_error(FL_ERR_INVALID, "fl_plan_option: unknown option %d", option);
 }
 
@@ -224,6 +243,10 @@ extern "C" int fl_plan_query(const fl_plan* p, int option, int* value)
     if (!p || !value) return fl_set_error(FL_ERR_INVALID, "fl_plan_query: null argument");
     if (option == FL_OPT_Z_MIRROR) {
         *value = p->zmirror;
+        return fl_set_error(FL_OK, "");
+    }
+    if (option == FL_OPT_ROT_MIRROR) {
+        *value = (p->rot && p->zmirror) ? 1 : 0;
         return fl_set_error(FL_OK, "");
     }
     return fl_set_error(FL_ERR_INVALID, "fl_plan_query: unknown option %d", option);

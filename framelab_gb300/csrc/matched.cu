@@ -72,6 +72,47 @@ k_fwd_cone(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restr
     }
 }
 
+// Half-turn form (fl_plan::rot, on a z-mirror plan): the block walks rows
+// ib < nb/2 of views iv < nv/2 only; each walk also yields the rays of view
+// iv + nv/2 at the same column and rows (the turned ray, over the turned
+// voxels), all four with the walked ray's c_r.
+template <typename TX, typename TY>
+__global__ void __launch_bounds__(128, 12)
+k_fwd_quad(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restrict__ col,
+           const float* __restrict__ colr, const RowEntry* __restrict__ row, int nx, int ny,
+           int nz, int na, int nb, int nv, long long nper, float scale, int cr_power,
+           const int* __restrict__ skip, const float* __restrict__ xscale, int yfold)
+{
+    if (skip && *skip) return;
+    const int ia = blockIdx.x * blockDim.x + threadIdx.x;
+    const int iv = blockIdx.y;                      // < nv / 2
+    const int ib = blockIdx.z * blockDim.y + threadIdx.y;
+    const int nbh = nb / 2, hv = nv / 2;
+    if (ia >= na || ib >= nbh) return;
+    const ColEntry ce = col[(long long)iv * na + ia];
+    const RowEntry re = row[(long long)iv * nb + ib];
+    float2 a, r;
+    walk_quad<TX>(X, ce.inv_x, ce.off_x, ce.inv_y, ce.off_y, re.inv_z, re.off_z, nx, ny, nz, &a,
+                  &r, nper);
+    float cr = ray_cr(scale, colr[(long long)iv * na + ia], re.dz2);
+    if (xscale) {
+        const float xs = *xscale;
+        a.x *= xs; a.y *= xs; r.x *= xs; r.y *= xs;
+    }
+    float o[4] = {cr * a.x, cr * a.y, cr * r.x, cr * r.y};
+    if (cr_power == 2)
+        for (int k = 0; k < 4; k++) o[k] = cr * o[k];
+    if (yfold) {
+        Store<TY>::st2(y + 2 * (((long long)iv * nbh + ib) * na + ia), o[0], o[1]);
+        Store<TY>::st2(y + 2 * (((long long)(iv + hv) * nbh + ib) * na + ia), o[2], o[3]);
+    } else {
+        Store<TY>::st(y + ((long long)iv * nb + ib) * na + ia, o[0]);
+        Store<TY>::st(y + ((long long)iv * nb + (nb - 1 - ib)) * na + ia, o[1]);
+        Store<TY>::st(y + ((long long)(iv + hv) * nb + ib) * na + ia, o[2]);
+        Store<TY>::st(y + ((long long)(iv + hv) * nb + (nb - 1 - ib)) * na + ia, o[3]);
+    }
+}
+
 template <typename TX, typename TY>
 __global__ void __launch_bounds__(128, 8)
 k_fwd_fan(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restrict__ col,
@@ -122,10 +163,12 @@ k_count(int32_t* __restrict__ cnt, const ColEntry* __restrict__ col,
 // Folded yw for a z-mirror plan: the pair (c_r y[ib], c_r y[nb-1-ib]) of rows
 // ib < nb/2, both with the walked row's c_r (equal to the mirror's: its d_z is
 // the exact negation).
+// hv > 0 (half-turn plan): the views iv >= hv take c_r of view iv - hv, the
+// ray they are defined by.
 template <typename TY>
 __global__ void k_weight_fold(float* __restrict__ yw, const TY* __restrict__ y,
                               const float* __restrict__ colr, const RowEntry* __restrict__ row,
-                              int na, int nb, long long npairs, float scale)
+                              int na, int nb, long long npairs, float scale, int hv)
 {
     long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= npairs) return;
@@ -134,7 +177,8 @@ __global__ void k_weight_fold(float* __restrict__ yw, const TY* __restrict__ y,
     long long q = r / na;
     int ib = (int)(q % nbh);
     int iv = (int)(q / nbh);
-    float cr = ray_cr(scale, colr[(long long)iv * na + ia], row[(long long)iv * nb + ib].dz2);
+    const int ivc = (hv > 0 && iv >= hv) ? iv - hv : iv;
+    float cr = ray_cr(scale, colr[(long long)ivc * na + ia], row[(long long)ivc * nb + ib].dz2);
     float a = Store<TY>::ld_plain(y + ((long long)iv * nb + ib) * na + ia);
     float b = Store<TY>::ld_plain(y + ((long long)iv * nb + (nb - 1 - ib)) * na + ia);
     Store<float>::st2(yw + 2 * r, cr * a, cr * b);
@@ -320,6 +364,136 @@ __device__ __forceinline__ void adj_rows_pair(float2 (&acc)[TZ], int nk, int z0,
     }
 }
 
+// Half-turn form of adj_rows_pair: every weight also multiplies the folded
+// row pair of view v + nv/2 (ycolr) into the turned voxels' sums accr.
+template <int MODE, int TZ>
+__device__ __forceinline__ void adj_rows_quad(float2 (&acc)[TZ], float2 (&accr)[TZ], int nk,
+                                              int z0, float l, float h, float e1, float e2,
+                                              float s1, float s2, const float2* __restrict__ rv,
+                                              const float* __restrict__ ycol,
+                                              const float* __restrict__ ycolr, int na, int nb)
+{
+    float mn = fminf(e1, e2), mx = fmaxf(e1, e2);
+    float lo_e = e1 - 0.02f, hi_e = e2 + s2 + 0.02f;
+#pragma unroll
+    for (int k = 0; k < TZ; k++) {
+        if (k >= nk) break;
+        int blo, bhi;
+        if (MODE < 0) {
+            blo = max(__float2int_ru(lo_e), 0);
+            bhi = min(__float2int_rd(hi_e), nb - 1);
+            lo_e += s1; hi_e += s2;
+        } else {
+            e1 += s1; e2 += s2;
+            const float mn1 = fminf(e1, e2), mx1 = fmaxf(e1, e2);
+            blo = max(__float2int_ru(fminf(mn, mn1) - 0.02f), 0);
+            bhi = min(__float2int_rd(fmaxf(mx, mx1) + 0.02f), nb - 1);
+            mn = mn1; mx = mx1;
+        }
+        const float fk0 = (float)(z0 + k), fk1 = (float)(z0 + k + 1);
+        for (int ib = blo; ib <= bhi; ib++) {
+            if (!FL_IN(ib, nb)) continue;
+            const float2 re = rv[ib];
+            const float2 t = Store<float>::ld2(ycol + 2 * (long long)ib * na);
+            const float2 tr = Store<float>::ld2(ycolr + 2 * (long long)ib * na);
+            const float2 az = __ffma2_rn(make_float2(fk0, fk1), make_float2(re.x, re.x),
+                                         make_float2(re.y, re.y));
+            float l2, h2;
+            if (MODE < 0) { l2 = fmaxf(l, az.y); h2 = fminf(h, az.x); }
+            else { l2 = fmaxf(l, fminf(az.x, az.y)); h2 = fminf(h, fmaxf(az.x, az.y)); }
+            const float w = fmaxf(h2 - l2, 0.0f);
+            acc[k] = __ffma2_rn(make_float2(w, w), t, acc[k]);
+            accr[k] = __ffma2_rn(make_float2(w, w), tr, accr[k]);
+        }
+    }
+}
+
+// Half-turn + z-mirror backprojection (fl_plan::rot): one thread per voxel
+// column V = (ix, iy < ny/2) and its turned column T = (nx-1-ix, ny-1-iy),
+// with a run of TZ voxels of the lower half and their mirrors; one frame. The
+// thread visits the views iv < nv/2 only. In view iv it evaluates the weights
+// of both columns: a weight of V multiplies the row pair of view iv into V
+// and the row pair of view iv + nv/2 into T (A[(iv + nv/2, r), T] =
+// A[(iv, r), V]); a weight of T, the other way round. yw is the folded
+// sinogram of all views; X the folded volume (xfold) or the standard one.
+template <typename TX, int TZ>
+__global__ void __launch_bounds__(128, 6)
+k_adj_quad(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __restrict__ col,
+           const float2* __restrict__ rowz, const ViewEntry* __restrict__ view, DetGrid G,
+           int nx, int ny, int nz, int na, int nb, int nv, float dz, int zruns,
+           const int* __restrict__ skip, int xfold)
+{
+    if (skip && *skip) return;
+    const int ix = blockIdx.x * blockDim.x + threadIdx.x;
+    const int iy = blockIdx.y * blockDim.y + threadIdx.y;     // < ny / 2
+    const int z0 = blockIdx.z * TZ;
+    const int nzw = nz / 2, nbw = nb / 2, hv = nv / 2;
+    const int nk = min(TZ, nzw - z0);
+    if (ix >= nx || iy >= ny / 2) return;
+    const int tx = nx - 1 - ix, ty = ny - 1 - iy;             // the turned column
+    float2 accV[TZ], accT[TZ];
+#pragma unroll
+    for (int k = 0; k < TZ; k++) { accV[k] = make_float2(0.0f, 0.0f); accT[k] = accV[k]; }
+    const float inv_dv = 1.0f / G.dv;
+    const long long vstride = (long long)nbw * na * 2;        // folded floats per view
+    for (int iv = 0; iv < hv; iv++) {
+        const ViewEntry ve = view[iv];
+        const ColEntry* cv = col + (long long)iv * na;
+        const float2* rv = rowz + (long long)iv * nb;
+        const float* yv = yw + (long long)iv * vstride;
+        const float* yvr = yw + (long long)(iv + hv) * vstride;
+        const float zr0 = (float)(z0 - nz / 2) * dz - ve.sz;
+        const float zr1 = (float)(z0 + nk - nz / 2) * dz - ve.sz;
+        const float tol = 1e-3f * dz;
+        const int mode = (zr1 <= -tol) ? -1 : 0;               // lower half: never above
+        // column (cx, cy) in view iv: its weights go to `own` with view iv and
+        // to `other` with view iv + nv/2
+        auto column = [&](int cx, int cy, float2 (&own)[TZ], float2 (&other)[TZ]) {
+            int alo, ahi; float dmin, dmax;
+            column_window(G, ve.c, ve.s, (float)(cx - nx / 2), (float)(cy - ny / 2), 1.0f, 1.0f,
+                          na, alo, ahi, dmin, dmax);
+            const float fx0 = (float)cx, fx1 = (float)(cx + 1);
+            const float fy0 = (float)cy, fy1 = (float)(cy + 1);
+            for (int ia = alo; ia <= ahi; ia++) {
+                if (!FL_IN(ia, na)) continue;
+                const ColEntry ce = cv[ia];
+                const float ax0 = fmaf(fx0, ce.inv_x, ce.off_x), ax1 = fmaf(fx1, ce.inv_x, ce.off_x);
+                const float ay0 = fmaf(fy0, ce.inv_y, ce.off_y), ay1 = fmaf(fy1, ce.inv_y, ce.off_y);
+                const float l = fmaxf(fminf(ax0, ax1), fminf(ay0, ay1));
+                const float h = fminf(fmaxf(ax0, ax1), fmaxf(ay0, ay1));
+                if (!(l < h)) continue;
+                const float r1 = __fdividef(1.0f, l + ve.ac), r2 = __fdividef(1.0f, h + ve.ac);
+                const float s1 = dz * r1 * inv_dv, s2 = dz * r2 * inv_dv;
+                const float e1 = (zr0 * r1 - G.v0) * inv_dv, e2 = (zr0 * r2 - G.v0) * inv_dv;
+                if (mode < 0)
+                    adj_rows_quad<-1, TZ>(own, other, nk, z0, l, h, e1, e2, s1, s2, rv,
+                                          yv + 2 * ia, yvr + 2 * ia, na, nbw);
+                else
+                    adj_rows_quad<0, TZ>(own, other, nk, z0, l, h, e1, e2, s1, s2, rv,
+                                         yv + 2 * ia, yvr + 2 * ia, na, nbw);
+            }
+        };
+        column(ix, iy, accV, accT);
+        column(tx, ty, accT, accV);
+    }
+    const long long nxy = (long long)nx * ny;
+    const long long cV = (long long)iy * nx + ix, cT = (long long)ty * nx + tx;
+#pragma unroll
+    for (int k = 0; k < TZ; k++)
+        if (k < nk) {
+            const long long zl = (long long)(z0 + k) * nxy, zh = (long long)(nz - 1 - z0 - k) * nxy;
+            if (xfold) {
+                Store<TX>::st2(X + 2 * (zl + cV), accV[k].x, accV[k].y);
+                Store<TX>::st2(X + 2 * (zl + cT), accT[k].x, accT[k].y);
+            } else {
+                Store<TX>::st(X + zl + cV, accV[k].x);
+                Store<TX>::st(X + zh + cV, accV[k].y);
+                Store<TX>::st(X + zl + cT, accT[k].x);
+                Store<TX>::st(X + zh + cT, accT[k].y);
+            }
+        }
+}
+
 // MIRROR: yw is the folded sinogram; the runs cover the lower half z < nz/2
 // only (the walked rows' rays never reach the upper half) and each thread also
 // produces the mirrored run, into the folded volume when xfold is set.
@@ -425,7 +599,12 @@ void launch_fwd(fl_plan* p, const void* x, void* y, int cr_power, const int* ski
                 const float* xscale, int yfold, cudaStream_t st)
 {
     const fl_scan& s = p->s;
-    if (s.ndim == 3 && p->zmirror) {
+    if (s.ndim == 3 && p->zmirror && p->rot) {
+        dim3 grid(fl_div_up(s.na, 8), s.nv / 2, fl_div_up(s.nb / 2, 16));
+        k_fwd_quad<TX, TY><<<grid, dim3(8, 16), 0, st>>>(
+            (const TX*)x, (TY*)y, p->d_col, p->d_colr, p->d_row, s.nx, s.ny, s.nz, s.na, s.nb,
+            s.nv, p->n_vox_frame, s.scale, cr_power, skip, xscale, yfold);
+    } else if (s.ndim == 3 && p->zmirror) {
         dim3 grid(fl_div_up(s.na, 8), s.nv, fl_div_up(s.nb / 2, 16));
         k_fwd_cone<TX, TY, true><<<grid, dim3(8, 16), 0, st>>>(
             (const TX*)x, (TY*)y, p->d_col, p->d_colr, p->d_row, p->d_view_frame, s.nx, s.ny,
@@ -462,7 +641,12 @@ void launch_adj(fl_plan* p, const float* yw, void* x, const int* skip, int xfold
         constexpr int TZ = 8;
         const int nzw = p->zmirror ? s.nz / 2 : s.nz;
         int zruns = (nzw + TZ - 1) / TZ;
-        if (p->zmirror) {
+        if (p->zmirror && p->rot) {
+            dim3 grid(fl_div_up(s.nx, 16), fl_div_up(s.ny / 2, 8), (unsigned)zruns);
+            k_adj_quad<TX, TZ><<<grid, dim3(16, 8), 0, st>>>(
+                (TX*)x, yw, p->d_col, p->d_rowz, p->d_view, G, s.nx, s.ny, s.nz, s.na, s.nb, s.nv,
+                s.dz, zruns, skip, xfold);
+        } else if (p->zmirror) {
             dim3 grid(fl_div_up(s.nx, 16), fl_div_up(s.ny, 8), (unsigned)zruns * s.nt);
             k_adj_cone<TX, TZ, true><<<grid, dim3(16, 8), 0, st>>>(
                 (TX*)x, yw, p->d_col, p->d_rowz, p->d_view, p->d_idY, p->d_Nv, p->tmp_size, G,
@@ -543,16 +727,17 @@ int fl_matched_weight(fl_plan* p, const void* y, int yt, float* yw, cudaStream_t
     if (three && p->zmirror) {
         long long np = (long long)s.nv * (s.nb / 2) * s.na;
         unsigned g = fl_div_up(np, 256);
+        const int hv = p->rot ? s.nv / 2 : 0;
         if (yt == FL_F32)
             k_weight_fold<float><<<g, 256, 0, st>>>(yw, (const float*)y, p->d_colr, p->d_row,
-                                                    s.na, s.nb, np, s.scale);
+                                                    s.na, s.nb, np, s.scale, hv);
         else if (yt == FL_F16)
             k_weight_fold<__half><<<g, 256, 0, st>>>(yw, (const __half*)y, p->d_colr, p->d_row,
-                                                     s.na, s.nb, np, s.scale);
+                                                     s.na, s.nb, np, s.scale, hv);
         else
             k_weight_fold<__nv_bfloat16><<<g, 256, 0, st>>>(yw, (const __nv_bfloat16*)y,
                                                             p->d_colr, p->d_row, s.na, s.nb, np,
-                                                            s.scale);
+                                                            s.scale, hv);
         return fl_check_launch("matched adjoint weighting");
     }
     unsigned g = fl_div_up(nr, 256);

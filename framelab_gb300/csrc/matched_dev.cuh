@@ -123,6 +123,77 @@ done:
     return acc;
 }
 
+// The z-mirror walk of a descending ray with the half-turn partner (plan
+// flag rot): besides the folded pair of voxel (ix, iy, iz) it gathers the
+// pair of voxel (nx-1-ix, ny-1-iy, iz), folded index Kz - v with
+// Kz = (2 iz + 1) nx ny - 1, which the turned ray of view v + nv/2 crosses
+// with the same segment. *acc gets the (voxel, mirror) sums, *accr the turned
+// pair's. Termination as in walk().
+template <typename TX>
+__device__ __forceinline__ void walk_quad(const TX* __restrict__ x, float inv_x, float off_x,
+                                          float inv_y, float off_y, float inv_z, float off_z,
+                                          int nx, int ny, int nz, float2* acc, float2* accr,
+                                          long long xlen)
+{
+    *acc = make_float2(0.0f, 0.0f);
+    *accr = make_float2(0.0f, 0.0f);
+    float ax0 = fmaf(0.0f, inv_x, off_x), ax1 = fmaf((float)nx, inv_x, off_x);
+    float ay0 = fmaf(0.0f, inv_y, off_y), ay1 = fmaf((float)ny, inv_y, off_y);
+    float a_in = fmaxf(fminf(ax0, ax1), fminf(ay0, ay1));
+    float a_out = fminf(fmaxf(ax0, ax1), fmaxf(ay0, ay1));
+    float az0 = fmaf(0.0f, inv_z, off_z), az1 = fmaf((float)nz, inv_z, off_z);
+    a_in = fmaxf(a_in, fminf(az0, az1));
+    a_out = fminf(a_out, fmaxf(az0, az1));
+    if (!(a_in < a_out) || !(inv_z < 0.0f)) return;
+    const int jx = start_slab(a_in, inv_x, off_x, nx);
+    const int jy = start_slab(a_in, inv_y, off_y, ny);
+    const int jz = min(start_slab(a_in, inv_z, off_z, nz), nz / 2 - 1);
+    const int nxy = nx * ny;
+    int v = (jz * ny + jy) * nx + jx;              // < 2^31 (checked at plan creation)
+    int kz = (2 * jz + 1) * nxy - 1;               // turned pair index = kz - v
+    const bool px = inv_x > 0.0f, py = inv_y > 0.0f;
+    float pax = (float)(px ? jx + 1 : jx);
+    float pay = (float)(py ? jy + 1 : jy);
+    float paz = (float)jz;                         // descending: next plane is jz
+    const float stx = px ? 1.0f : -1.0f, sty = py ? 1.0f : -1.0f;
+    const int dvx = px ? 1 : -1, dvy = py ? nx : -nx;
+    float nAx = fmaf(pax, inv_x, off_x);
+    float nAy = fmaf(pay, inv_y, off_y);
+    float nAz = fmaf(paz, inv_z, off_z);
+    float cur = a_in;
+    float2 s2 = make_float2(0.0f, 0.0f), r2 = make_float2(0.0f, 0.0f);
+    float2 xv2 = make_float2(0.0f, 0.0f), xr2 = make_float2(0.0f, 0.0f);
+    if (FL_IN(2 * (long long)v + 1, xlen)) xv2 = Store<TX>::ld2(x + 2 * (long long)v);
+    if (FL_IN(2 * (long long)(kz - v) + 1, xlen)) xr2 = Store<TX>::ld2(x + 2 * (long long)(kz - v));
+    const int budget = nx + ny + nz + 4;
+    for (int it = 0; it < budget; it += 4) {
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const float nxt = fminf(fminf(nAx, nAy), nAz);
+            const float seg = nxt - cur;
+            const bool cont = nxt < a_out;         // false at the exit (and for NaN)
+            float2 xn2 = make_float2(0.0f, 0.0f), xnr2 = make_float2(0.0f, 0.0f);
+            if (cont) {
+                if (nAx == nxt) { pax += stx; v += dvx; nAx = fmaf(pax, inv_x, off_x); }
+                if (nAy == nxt) { pay += sty; v += dvy; nAy = fmaf(pay, inv_y, off_y); }
+                if (nAz == nxt) { paz -= 1.0f; v -= nxy; kz -= 2 * nxy; nAz = fmaf(paz, inv_z, off_z); }
+                if (FL_IN(2 * (long long)v + 1, xlen)) xn2 = Store<TX>::ld2(x + 2 * (long long)v);
+                if (FL_IN(2 * (long long)(kz - v) + 1, xlen))
+                    xnr2 = Store<TX>::ld2(x + 2 * (long long)(kz - v));
+            }
+            s2 = __ffma2_rn(make_float2(seg, seg), xv2, s2);
+            r2 = __ffma2_rn(make_float2(seg, seg), xr2, r2);
+            if (!cont) goto done;
+            xv2 = xn2;
+            xr2 = xnr2;
+            cur = nxt;
+        }
+    }
+done:
+    *acc = s2;
+    *accr = r2;
+}
+
 __device__ __forceinline__ float ray_cr(float scale, float dxy2, float dz2)
 {
     return fmul(scale, fsqrt(fadd(dxy2, dz2)));

@@ -112,6 +112,18 @@ class Plan:
         _lib.check(self._L.fl_plan_option(self._h, _lib.OPT_Z_MIRROR, int(bool(on))))
 
     @property
+    def rot_mirror(self) -> bool:
+        """Whether the matched pair also uses the half-turn symmetry between
+        views v and v + nv/2 (FL_OPT_ROT_MIRROR; needs the z mirror)."""
+        v = C.c_int()
+        _lib.check(self._L.fl_plan_query(self._h, _lib.OPT_ROT_MIRROR, C.byref(v)))
+        return bool(v.value)
+
+    @rot_mirror.setter
+    def rot_mirror(self, on: bool):
+        _lib.check(self._L.fl_plan_option(self._h, _lib.OPT_ROT_MIRROR, int(bool(on))))
+
+    @property
     def handle(self):
         return self._h
 

@@ -384,6 +384,9 @@ def test_multi_frame_views_read_their_frame():
     q["id_Y"], q["Nv"], q["tmp_size"] = idY, np.array([len(v) for v in views], np.uint32), np.uint32(tmp)
     X = rng.standard_normal((2, 16 ** 3)).astype(np.float32)
     P2, P1 = _plan(q), _plan(p)
+    # the one-frame plan's 6 views pair up as opposites; the two-frame plan
+    # cannot use the half turn, so compare against every view's own tables
+    P1.rot_mirror = False
     y2 = _host(P2.forward(_dev(X.reshape(-1)), model="matched")).reshape(6, -1)
     for t in (0, 1):
         y1 = _host(P1.forward(_dev(X[t]), model="matched")).reshape(6, -1)
@@ -478,6 +481,7 @@ def test_z_mirror_agrees_with_general_kernels_and_is_exact():
     p = _cone_small("circle")
     n, nb = int(p["nx"]), len(p["z_det"])
     P = _plan(p)
+    P.rot_mirror = False               # the z mirror alone (the half turn: below)
     x = PH.ellipsoids_3d(n, seed=9).reshape(-1)
     rng = np.random.default_rng(3)
     r = rng.standard_normal(P.n_rays).astype(np.float32)
@@ -501,3 +505,72 @@ def test_z_mirror_agrees_with_general_kernels_and_is_exact():
     # half-precision storage goes through the same mirrored kernels
     y16 = _host(P.forward(_dev(x, torch.float16)))
     assert _rel(y16, ym) < 2e-3
+
+
+def _short_scan(p):
+    """The same scan over half a turn: no view has an opposite partner."""
+    q = dict(p)
+    nv = len(p["sd_phi"])
+    q["sd_phi"] = (np.pi / nv * np.arange(nv)).astype(np.float32)
+    for k, f in (("cos_phi", np.cos), ("sin_phi", np.sin)):
+        if k in q:
+            q[k] = f(q["sd_phi"].astype(np.float64)).astype(np.float32)
+    return q
+
+
+def test_rot_mirror_is_detected_only_for_half_turn_scans():
+    P = _plan(_cone_small("circle"))
+    assert P.z_mirror and P.rot_mirror
+    P.z_mirror = False                 # the half turn rides on the z mirror
+    assert not P.rot_mirror
+    P.z_mirror = True
+    assert P.rot_mirror
+    odd = G.cone_para_mm(32, 15, 48, 40, det_pitch_mm=8.0, SO_mm=600.0, SD_mm=1200.0,
+                         voxel_mm=8.0)
+    Q = _plan(odd)
+    assert Q.z_mirror and not Q.rot_mirror
+    Q.rot_mirror = True                # not allowed for this geometry: stays off
+    assert not Q.rot_mirror
+    S = _plan(_short_scan(_cone_small("circle")))
+    assert S.z_mirror and not S.rot_mirror
+    assert not _plan(_cone_small("helix")).rot_mirror
+
+
+def test_rot_mirror_agrees_with_general_kernels_and_is_exact():
+    torch = _torch()
+    from framelab_gb300.solvers import NativeCGLS
+    p = _cone_small("circle")
+    n, nb, nv = int(p["nx"]), len(p["z_det"]), len(p["sd_phi"])
+    P = _plan(p)
+    x = PH.ellipsoids_3d(n, seed=9).reshape(-1)
+    rng = np.random.default_rng(4)
+    r = rng.standard_normal(P.n_rays).astype(np.float32)
+    yq, xq = _host(P.forward(_dev(x))), _host(P.adjoint(_dev(r)))
+    P.rot_mirror = False
+    ym, xm = _host(P.forward(_dev(x))), _host(P.adjoint(_dev(r)))
+    P.z_mirror = False
+    yg, xg = _host(P.forward(_dev(x))), _host(P.adjoint(_dev(r)))
+    # the turned views use the walked view's tables: the matrices differ by the
+    # FP32 rounding of the turned views' own tables (and their angles, which are
+    # opposite only to within FP32)
+    for yo, xo in ((ym, xm), (yg, xg)):
+        assert _rel(yq, yo) < 1e-5 and _rel(xq, xo) < 1e-4, (_rel(yq, yo), _rel(xq, xo))
+    P.z_mirror = True
+    P.rot_mirror = True
+    # by construction: views v + nv/2 of A x are views v of A turn(x), with
+    # turn(x)[z, y, x] = x[z, ny-1-y, nx-1-x]
+    xt = x.reshape(n, n, n)[:, ::-1, ::-1].reshape(-1).copy()
+    yt = _host(P.forward(_dev(xt))).reshape(nv, nb, -1)
+    assert np.array_equal(yq.reshape(nv, nb, -1)[nv // 2:], yt[:nv // 2])
+    # the adjoint stays the exact transpose
+    lhs = np.dot(yq.astype(np.float64), r.astype(np.float64))
+    rhs = np.dot(x.astype(np.float64), xq.astype(np.float64))
+    assert abs(lhs - rhs) / abs(lhs) < 1e-5
+    # half-precision storage and the fused CGLS go through the same kernels
+    assert _rel(_host(P.forward(_dev(x, torch.float16))), yq) < 2e-3
+    b = P.adjoint(P.forward(_dev(x))).reshape(-1).contiguous()
+    cg = NativeCGLS(P, "graph")
+    uq = cg.solve(b, iters=6).clone()
+    P.rot_mirror = False               # the captured graph follows the option
+    um = cg.solve(b, iters=6)
+    assert _rel(_host(uq), _host(um)) < 1e-4
