@@ -417,7 +417,7 @@ __device__ __forceinline__ void adj_rows_quad(float2 (&acc)[TZ], float2 (&accr)[
 // A[(iv, r), V]); a weight of T, the other way round. yw is the folded
 // sinogram of all views; X the folded volume (xfold) or the standard one.
 template <typename TX, int TZ>
-__global__ void __launch_bounds__(128, 6)
+__global__ void __launch_bounds__(128, 8)
 k_adj_quad(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __restrict__ col,
            const float2* __restrict__ rowz, const ViewEntry* __restrict__ view, DetGrid G,
            int nx, int ny, int nz, int na, int nb, int nv, float dz, int zruns,
@@ -642,8 +642,11 @@ void launch_adj(fl_plan* p, const float* yw, void* x, const int* skip, int xfold
         const int nzw = p->zmirror ? s.nz / 2 : s.nz;
         int zruns = (nzw + TZ - 1) / TZ;
         if (p->zmirror && p->rot) {
+            // runs of 4: the two columns' 16 accumulators keep 8 blocks per SM
+            constexpr int TQ = 4;
+            zruns = (nzw + TQ - 1) / TQ;
             dim3 grid(fl_div_up(s.nx, 16), fl_div_up(s.ny / 2, 8), (unsigned)zruns);
-            k_adj_quad<TX, TZ><<<grid, dim3(16, 8), 0, st>>>(
+            k_adj_quad<TX, TQ><<<grid, dim3(16, 8), 0, st>>>(
                 (TX*)x, yw, p->d_col, p->d_rowz, p->d_view, G, s.nx, s.ny, s.nz, s.na, s.nb, s.nv,
                 s.dz, zruns, skip, xfold);
         } else if (p->zmirror) {
