@@ -20,6 +20,7 @@ MODEL_SIDDON_REF, MODEL_CHORD_REF, MODEL_GAO_REF, MODEL_FB_REF, MODEL_MATCHED = 
 F32, F16, BF16 = 0, 1, 2
 OPT_Z_MIRROR = 1
 OPT_ROT_MIRROR = 2
+OPT_QUARTER_TURN = 3
 FRAMELET_OPT_FUSED = 1
 
 

@@ -61,6 +61,13 @@ struct fl_plan {
     // rays: rows b and nb-1-b of views v and v + nv/2.
     int rot_ok;                // the geometry allows it
     int rot;                   // in use (FL_OPT_ROT_MIRROR; only with zmirror)
+    // quarter turn on top of the half turn: nx == ny, nv a multiple of 4 and
+    // view v + nv/4 view v turned by pi/2. The matched model then defines
+    // A[(v + j nv/4, a, b), R^j (x, y, z)] = A[(v, a, b), (x, y, z)] for
+    // v < nv/4, j = 1..3, R (x, y) = (n-1-y, x), so one walk / one weight
+    // serves eight rays (views v + j nv/4, rows b and nb-1-b).
+    int rot4_ok;
+    int rot4;                  // in use (FL_OPT_QUARTER_TURN; only with rot and zmirror)
     // reusable scratch: sinogram-sized f32 for the pre-weighted adjoint input,
     // volume-sized for the z-folded copy of a forward input
     float *d_work;

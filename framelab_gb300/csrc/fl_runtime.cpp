@@ -221,6 +221,20 @@ static int build_tables(fl_plan* p, const std::vector<float>& phi, const float* 
         p->rot_ok = ok ? 1 : 0;
     }
     p->rot = p->rot_ok;
+    // quarter turn (fl_plan.h): view v + nv/4 is view v turned by pi/2 to
+    // within 1e-6 (cos -> -sin, sin -> cos), square xy grid
+    p->rot4_ok = 0;
+    if (p->rot_ok && s.nv % 4 == 0 && s.nx == s.ny) {
+        bool ok = true;
+        const int q = s.nv / 4;
+        for (int iv = 0; iv < q && ok; iv++) {
+            const double c0 = std::cos((double)phi[iv]), s0 = std::sin((double)phi[iv]);
+            const double c1 = std::cos((double)phi[iv + q]), s1 = std::sin((double)phi[iv + q]);
+            if (std::fabs(c1 + s0) > 1e-6 || std::fabs(s1 - c0) > 1e-6) ok = false;
+        }
+        p->rot4_ok = ok ? 1 : 0;
+    }
+    p->rot4 = p->rot4_ok;
     return FL_OK;
 }
 
@@ -235,6 +249,10 @@ extern "C" int fl_plan_option(fl_plan* p, int option, int value)
         p->rot = (value && p->rot_ok) ? 1 : 0;
         return fl_set_error(FL_OK, "");
     }
+    if (option == FL_OPT_QUARTER_TURN) {
+        p->rot4 = (value && p->rot4_ok) ? 1 : 0;
+        return fl_set_error(FL_OK, "");
+    }
     return fl_set_error(FL_ERR_INVALID, "fl_plan_option: unknown option %d", option);
 }
 
@@ -247,6 +265,10 @@ extern "C" int fl_plan_query(const fl_plan* p, int option, int* value)
     }
     if (option == FL_OPT_ROT_MIRROR) {
         *value = (p->rot && p->zmirror) ? 1 : 0;
+        return fl_set_error(FL_OK, "");
+    }
+    if (option == FL_OPT_QUARTER_TURN) {
+        *value = (p->rot4 && p->rot && p->zmirror) ? 1 : 0;
         return fl_set_error(FL_OK, "");
     }
     return fl_set_error(FL_ERR_INVALID, "fl_plan_query: unknown option %d", option);

@@ -113,6 +113,44 @@ k_fwd_quad(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restr
     }
 }
 
+// Quarter-turn form (fl_plan::rot4): the block walks rows ib < nb/2 of views
+// iv < nv/4; each walk yields the rays of views iv + j nv/4 (j = 0..3) at the
+// same column and rows, all eight with the walked ray's c_r.
+template <typename TX, typename TY>
+__global__ void __launch_bounds__(128, 8)
+k_fwd_oct(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restrict__ col,
+          const float* __restrict__ colr, const RowEntry* __restrict__ row, int n, int nz,
+          int na, int nb, int nv, long long nper, float scale, int cr_power,
+          const int* __restrict__ skip, const float* __restrict__ xscale, int yfold)
+{
+    if (skip && *skip) return;
+    const int ia = blockIdx.x * blockDim.x + threadIdx.x;
+    const int iv = blockIdx.y;                      // < nv / 4
+    const int ib = blockIdx.z * blockDim.y + threadIdx.y;
+    const int nbh = nb / 2, qv = nv / 4;
+    if (ia >= na || ib >= nbh) return;
+    const ColEntry ce = col[(long long)iv * na + ia];
+    const RowEntry re = row[(long long)iv * nb + ib];
+    float2 a[4];
+    walk_oct<TX>(X, ce.inv_x, ce.off_x, ce.inv_y, ce.off_y, re.inv_z, re.off_z, n, nz, a, nper);
+    float cr = ray_cr(scale, colr[(long long)iv * na + ia], re.dz2);
+    const float xs = xscale ? *xscale : 1.0f;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        float o0 = a[j].x, o1 = a[j].y;
+        if (xscale) { o0 *= xs; o1 *= xs; }
+        o0 = cr * o0; o1 = cr * o1;
+        if (cr_power == 2) { o0 = cr * o0; o1 = cr * o1; }
+        const long long vj = iv + (long long)j * qv;
+        if (yfold) {
+            Store<TY>::st2(y + 2 * ((vj * nbh + ib) * na + ia), o0, o1);
+        } else {
+            Store<TY>::st(y + (vj * nb + ib) * na + ia, o0);
+            Store<TY>::st(y + (vj * nb + (nb - 1 - ib)) * na + ia, o1);
+        }
+    }
+}
+
 template <typename TX, typename TY>
 __global__ void __launch_bounds__(128, 8)
 k_fwd_fan(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restrict__ col,
@@ -163,12 +201,13 @@ k_count(int32_t* __restrict__ cnt, const ColEntry* __restrict__ col,
 // Folded yw for a z-mirror plan: the pair (c_r y[ib], c_r y[nb-1-ib]) of rows
 // ib < nb/2, both with the walked row's c_r (equal to the mirror's: its d_z is
 // the exact negation).
-// hv > 0 (half-turn plan): the views iv >= hv take c_r of view iv - hv, the
-// ray they are defined by.
+// pv: the views repeat with period pv (nv, or nv/2 for a half-turn plan, nv/4
+// for a quarter-turn plan): view iv takes c_r of view iv % pv, the ray it is
+// defined by.
 template <typename TY>
 __global__ void k_weight_fold(float* __restrict__ yw, const TY* __restrict__ y,
                               const float* __restrict__ colr, const RowEntry* __restrict__ row,
-                              int na, int nb, long long npairs, float scale, int hv)
+                              int na, int nb, long long npairs, float scale, int pv)
 {
     long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= npairs) return;
@@ -177,7 +216,7 @@ __global__ void k_weight_fold(float* __restrict__ yw, const TY* __restrict__ y,
     long long q = r / na;
     int ib = (int)(q % nbh);
     int iv = (int)(q / nbh);
-    const int ivc = (hv > 0 && iv >= hv) ? iv - hv : iv;
+    const int ivc = iv % pv;
     float cr = ray_cr(scale, colr[(long long)ivc * na + ia], row[(long long)ivc * nb + ib].dz2);
     float a = Store<TY>::ld_plain(y + ((long long)iv * nb + ib) * na + ia);
     float b = Store<TY>::ld_plain(y + ((long long)iv * nb + (nb - 1 - ib)) * na + ia);
@@ -494,6 +533,149 @@ k_adj_quad(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __r
         }
 }
 
+// Quarter-turn form of adj_rows_pair: every weight multiplies the folded row
+// pairs of views v + j nv/4 (y0..y3) into the sums a0..a3.
+template <int MODE, int TZ>
+__device__ __forceinline__ void adj_rows_oct(float2 (&a0)[TZ], float2 (&a1)[TZ],
+                                             float2 (&a2)[TZ], float2 (&a3)[TZ], int nk, int z0,
+                                             float l, float h, float e1, float e2, float s1,
+                                             float s2, const float2* __restrict__ rv,
+                                             const float* __restrict__ y0,
+                                             const float* __restrict__ y1,
+                                             const float* __restrict__ y2,
+                                             const float* __restrict__ y3, int na, int nb)
+{
+    float mn = fminf(e1, e2), mx = fmaxf(e1, e2);
+    float lo_e = e1 - 0.02f, hi_e = e2 + s2 + 0.02f;
+#pragma unroll
+    for (int k = 0; k < TZ; k++) {
+        if (k >= nk) break;
+        int blo, bhi;
+        if (MODE < 0) {
+            blo = max(__float2int_ru(lo_e), 0);
+            bhi = min(__float2int_rd(hi_e), nb - 1);
+            lo_e += s1; hi_e += s2;
+        } else {
+            e1 += s1; e2 += s2;
+            const float mn1 = fminf(e1, e2), mx1 = fmaxf(e1, e2);
+            blo = max(__float2int_ru(fminf(mn, mn1) - 0.02f), 0);
+            bhi = min(__float2int_rd(fmaxf(mx, mx1) + 0.02f), nb - 1);
+            mn = mn1; mx = mx1;
+        }
+        const float fk0 = (float)(z0 + k), fk1 = (float)(z0 + k + 1);
+        for (int ib = blo; ib <= bhi; ib++) {
+            if (!FL_IN(ib, nb)) continue;
+            const float2 re = rv[ib];
+            const long long o = 2 * (long long)ib * na;
+            const float2 t0 = Store<float>::ld2(y0 + o), t1 = Store<float>::ld2(y1 + o);
+            const float2 t2 = Store<float>::ld2(y2 + o), t3 = Store<float>::ld2(y3 + o);
+            const float2 az = __ffma2_rn(make_float2(fk0, fk1), make_float2(re.x, re.x),
+                                         make_float2(re.y, re.y));
+            float l2, h2;
+            if (MODE < 0) { l2 = fmaxf(l, az.y); h2 = fminf(h, az.x); }
+            else { l2 = fmaxf(l, fminf(az.x, az.y)); h2 = fminf(h, fmaxf(az.x, az.y)); }
+            const float2 w2 = make_float2(fmaxf(h2 - l2, 0.0f), fmaxf(h2 - l2, 0.0f));
+            a0[k] = __ffma2_rn(w2, t0, a0[k]);
+            a1[k] = __ffma2_rn(w2, t1, a1[k]);
+            a2[k] = __ffma2_rn(w2, t2, a2[k]);
+            a3[k] = __ffma2_rn(w2, t3, a3[k]);
+        }
+    }
+}
+
+// Quarter-turn + z-mirror backprojection (fl_plan::rot4, nx == ny == n): one
+// thread per voxel column V0 = (x, y) of the quadrant x, y < n/2 and its
+// turns V_j = R^j V0, with a run of TZ voxels of the lower half and their
+// mirrors; one frame. It visits the views iv < nv/4. In view iv a weight of
+// column V_k multiplies the row pairs of view iv + j nv/4 into V_{k+j mod 4}
+// (A[(iv + j nv/4, r), R^j V] = A[(iv, r), V]).
+template <typename TX, int TZ>
+__global__ void __launch_bounds__(128, TZ == 2 ? 8 : 6)
+k_adj_oct(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __restrict__ col,
+          const float2* __restrict__ rowz, const ViewEntry* __restrict__ view, DetGrid G, int n,
+          int nz, int na, int nb, int nv, float dz, const int* __restrict__ skip, int xfold)
+{
+    if (skip && *skip) return;
+    const int ix = blockIdx.x * blockDim.x + threadIdx.x;    // < n / 2
+    const int iy = blockIdx.y * blockDim.y + threadIdx.y;    // < n / 2
+    const int z0 = blockIdx.z * TZ;
+    const int nzw = nz / 2, nbw = nb / 2, qv = nv / 4, h = n / 2;
+    const int nk = min(TZ, nzw - z0);
+    if (ix >= h || iy >= h) return;
+    const int cx[4] = {ix, n - 1 - iy, n - 1 - ix, iy};
+    const int cy[4] = {iy, ix, n - 1 - iy, n - 1 - ix};
+    float2 A0[TZ], A1[TZ], A2[TZ], A3[TZ];
+#pragma unroll
+    for (int k = 0; k < TZ; k++) {
+        A0[k] = make_float2(0.0f, 0.0f); A1[k] = A0[k]; A2[k] = A0[k]; A3[k] = A0[k];
+    }
+    const float inv_dv = 1.0f / G.dv;
+    const long long vstride = (long long)nbw * na * 2;        // folded floats per view
+    for (int iv = 0; iv < qv; iv++) {
+        const ViewEntry ve = view[iv];
+        const ColEntry* cv = col + (long long)iv * na;
+        const float2* rv = rowz + (long long)iv * nb;
+        const float* y0 = yw + (long long)iv * vstride;
+        const float* y1 = y0 + (long long)qv * vstride;
+        const float* y2 = y1 + (long long)qv * vstride;
+        const float* y3 = y2 + (long long)qv * vstride;
+        const float zr0 = (float)(z0 - nz / 2) * dz - ve.sz;
+        const float zr1 = (float)(z0 + nk - nz / 2) * dz - ve.sz;
+        const float tol = 1e-3f * dz;
+        const int mode = (zr1 <= -tol) ? -1 : 0;               // lower half: never above
+        // column (px, py) in view iv: its weights go to b0 with view iv,
+        // b1 with iv + nv/4, b2 with iv + nv/2, b3 with iv + 3 nv/4
+        auto column = [&](int px_, int py_, float2 (&b0)[TZ], float2 (&b1)[TZ],
+                          float2 (&b2)[TZ], float2 (&b3)[TZ]) {
+            int alo, ahi; float dmin, dmax;
+            column_window(G, ve.c, ve.s, (float)(px_ - h), (float)(py_ - h), 1.0f, 1.0f, na, alo,
+                          ahi, dmin, dmax);
+            const float fx0 = (float)px_, fx1 = (float)(px_ + 1);
+            const float fy0 = (float)py_, fy1 = (float)(py_ + 1);
+            for (int ia = alo; ia <= ahi; ia++) {
+                if (!FL_IN(ia, na)) continue;
+                const ColEntry ce = cv[ia];
+                const float ax0 = fmaf(fx0, ce.inv_x, ce.off_x), ax1 = fmaf(fx1, ce.inv_x, ce.off_x);
+                const float ay0 = fmaf(fy0, ce.inv_y, ce.off_y), ay1 = fmaf(fy1, ce.inv_y, ce.off_y);
+                const float l = fmaxf(fminf(ax0, ax1), fminf(ay0, ay1));
+                const float hh = fminf(fmaxf(ax0, ax1), fmaxf(ay0, ay1));
+                if (!(l < hh)) continue;
+                const float r1 = __fdividef(1.0f, l + ve.ac), r2 = __fdividef(1.0f, hh + ve.ac);
+                const float s1 = dz * r1 * inv_dv, s2 = dz * r2 * inv_dv;
+                const float e1 = (zr0 * r1 - G.v0) * inv_dv, e2 = (zr0 * r2 - G.v0) * inv_dv;
+                const int o = 2 * ia;
+                if (mode < 0)
+                    adj_rows_oct<-1, TZ>(b0, b1, b2, b3, nk, z0, l, hh, e1, e2, s1, s2, rv,
+                                         y0 + o, y1 + o, y2 + o, y3 + o, na, nbw);
+                else
+                    adj_rows_oct<0, TZ>(b0, b1, b2, b3, nk, z0, l, hh, e1, e2, s1, s2, rv,
+                                        y0 + o, y1 + o, y2 + o, y3 + o, na, nbw);
+            }
+        };
+        column(cx[0], cy[0], A0, A1, A2, A3);
+        column(cx[1], cy[1], A1, A2, A3, A0);
+        column(cx[2], cy[2], A2, A3, A0, A1);
+        column(cx[3], cy[3], A3, A0, A1, A2);
+    }
+    const long long nn = (long long)n * n;
+#pragma unroll
+    for (int k = 0; k < TZ; k++)
+        if (k < nk) {
+            const long long zl = (long long)(z0 + k) * nn, zh = (long long)(nz - 1 - z0 - k) * nn;
+            const float2* accs[4] = {&A0[k], &A1[k], &A2[k], &A3[k]};
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const long long c = (long long)cy[j] * n + cx[j];
+                if (xfold) {
+                    Store<TX>::st2(X + 2 * (zl + c), accs[j]->x, accs[j]->y);
+                } else {
+                    Store<TX>::st(X + zl + c, accs[j]->x);
+                    Store<TX>::st(X + zh + c, accs[j]->y);
+                }
+            }
+        }
+}
+
 // MIRROR: yw is the folded sinogram; the runs cover the lower half z < nz/2
 // only (the walked rows' rays never reach the upper half) and each thread also
 // produces the mirrored run, into the folded volume when xfold is set.
@@ -599,7 +781,12 @@ void launch_fwd(fl_plan* p, const void* x, void* y, int cr_power, const int* ski
                 const float* xscale, int yfold, cudaStream_t st)
 {
     const fl_scan& s = p->s;
-    if (s.ndim == 3 && p->zmirror && p->rot) {
+    if (s.ndim == 3 && p->zmirror && p->rot && p->rot4) {
+        dim3 grid(fl_div_up(s.na, 8), s.nv / 4, fl_div_up(s.nb / 2, 16));
+        k_fwd_oct<TX, TY><<<grid, dim3(8, 16), 0, st>>>(
+            (const TX*)x, (TY*)y, p->d_col, p->d_colr, p->d_row, s.nx, s.nz, s.na, s.nb, s.nv,
+            p->n_vox_frame, s.scale, cr_power, skip, xscale, yfold);
+    } else if (s.ndim == 3 && p->zmirror && p->rot) {
         dim3 grid(fl_div_up(s.na, 8), s.nv / 2, fl_div_up(s.nb / 2, 16));
         k_fwd_quad<TX, TY><<<grid, dim3(8, 16), 0, st>>>(
             (const TX*)x, (TY*)y, p->d_col, p->d_colr, p->d_row, s.nx, s.ny, s.nz, s.na, s.nb,
@@ -641,7 +828,15 @@ void launch_adj(fl_plan* p, const float* yw, void* x, const int* skip, int xfold
         constexpr int TZ = 8;
         const int nzw = p->zmirror ? s.nz / 2 : s.nz;
         int zruns = (nzw + TZ - 1) / TZ;
-        if (p->zmirror && p->rot) {
+        if (p->zmirror && p->rot && p->rot4) {
+            // runs of 2: the four columns' 16 accumulators keep 8 blocks per SM
+            constexpr int TO = 2;
+            zruns = (nzw + TO - 1) / TO;
+            dim3 grid(fl_div_up(s.nx / 2, 8), fl_div_up(s.ny / 2, 16), (unsigned)zruns);
+            k_adj_oct<TX, TO><<<grid, dim3(8, 16), 0, st>>>(
+                (TX*)x, yw, p->d_col, p->d_rowz, p->d_view, G, s.nx, s.nz, s.na, s.nb, s.nv,
+                s.dz, skip, xfold);
+        } else if (p->zmirror && p->rot) {
             // runs of 4: the two columns' 16 accumulators keep 8 blocks per SM
             constexpr int TQ = 4;
             zruns = (nzw + TQ - 1) / TQ;
@@ -730,7 +925,7 @@ int fl_matched_weight(fl_plan* p, const void* y, int yt, float* yw, cudaStream_t
     if (three && p->zmirror) {
         long long np = (long long)s.nv * (s.nb / 2) * s.na;
         unsigned g = fl_div_up(np, 256);
-        const int hv = p->rot ? s.nv / 2 : 0;
+        const int hv = !p->rot ? s.nv : (p->rot4 ? s.nv / 4 : s.nv / 2);   // view period
         if (yt == FL_F32)
             k_weight_fold<float><<<g, 256, 0, st>>>(yw, (const float*)y, p->d_colr, p->d_row,
                                                     s.na, s.nb, np, s.scale, hv);

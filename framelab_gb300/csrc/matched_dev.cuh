@@ -194,6 +194,100 @@ done:
     *accr = r2;
 }
 
+// The z-mirror walk with all four quarter turns (plan flag rot4, nx == ny ==
+// n): per step it gathers the folded pairs of voxel (ix, iy) and of its turns
+// R^j (ix, iy), R (x, y) = (n-1-y, x), which the ray of view v + j nv/4 at the
+// same column and row crosses with the same segment. The four pair indices
+// move with the walk: an x step by d moves them by (d, d n, -d, -d n), a y
+// step by (d n, -d, -d n, d), a z step by -n^2 each. acc[j] gets the
+// (voxel, mirror) sums of turn j. Termination as in walk().
+template <typename TX>
+__device__ __forceinline__ void walk_oct(const TX* __restrict__ x, float inv_x, float off_x,
+                                         float inv_y, float off_y, float inv_z, float off_z,
+                                         int n, int nz, float2 (&acc)[4], long long xlen)
+{
+#pragma unroll
+    for (int j = 0; j < 4; j++) acc[j] = make_float2(0.0f, 0.0f);
+    float ax0 = fmaf(0.0f, inv_x, off_x), ax1 = fmaf((float)n, inv_x, off_x);
+    float ay0 = fmaf(0.0f, inv_y, off_y), ay1 = fmaf((float)n, inv_y, off_y);
+    float a_in = fmaxf(fminf(ax0, ax1), fminf(ay0, ay1));
+    float a_out = fminf(fmaxf(ax0, ax1), fmaxf(ay0, ay1));
+    float az0 = fmaf(0.0f, inv_z, off_z), az1 = fmaf((float)nz, inv_z, off_z);
+    a_in = fmaxf(a_in, fminf(az0, az1));
+    a_out = fminf(a_out, fmaxf(az0, az1));
+    if (!(a_in < a_out) || !(inv_z < 0.0f)) return;
+    const int jx = start_slab(a_in, inv_x, off_x, n);
+    const int jy = start_slab(a_in, inv_y, off_y, n);
+    const int jz = min(start_slab(a_in, inv_z, off_z, nz), nz / 2 - 1);
+    const int nn = n * n;
+    int q[4];                                      // folded pair index of each turn
+    q[0] = (jz * n + jy) * n + jx;
+    q[1] = (jz * n + jx) * n + (n - 1 - jy);
+    q[2] = (jz * n + (n - 1 - jy)) * n + (n - 1 - jx);
+    q[3] = (jz * n + (n - 1 - jx)) * n + jy;
+    const bool px = inv_x > 0.0f, py = inv_y > 0.0f;
+    float pax = (float)(px ? jx + 1 : jx);
+    float pay = (float)(py ? jy + 1 : jy);
+    float paz = (float)jz;                         // descending: next plane is jz
+    const float stx = px ? 1.0f : -1.0f, sty = py ? 1.0f : -1.0f;
+    const int dx = px ? 1 : -1, dy = py ? 1 : -1;
+    const int mx[4] = {dx, dx * n, -dx, -dx * n}, my[4] = {dy * n, -dy, -dy * n, dy};
+    float nAx = fmaf(pax, inv_x, off_x);
+    float nAy = fmaf(pay, inv_y, off_y);
+    float nAz = fmaf(paz, inv_z, off_z);
+    float cur = a_in;
+    float2 xv[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        xv[j] = make_float2(0.0f, 0.0f);
+        if (FL_IN(2 * (long long)q[j] + 1, xlen)) xv[j] = Store<TX>::ld2(x + 2 * (long long)q[j]);
+    }
+    float2 s[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) s[j] = make_float2(0.0f, 0.0f);
+    const int budget = 2 * n + nz + 4;
+    for (int it = 0; it < budget; it += 2) {
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            const float nxt = fminf(fminf(nAx, nAy), nAz);
+            const float seg = nxt - cur;
+            const bool cont = nxt < a_out;         // false at the exit (and for NaN)
+            float2 xn[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) xn[j] = make_float2(0.0f, 0.0f);
+            if (cont) {
+                if (nAx == nxt) {
+                    pax += stx; nAx = fmaf(pax, inv_x, off_x);
+#pragma unroll
+                    for (int j = 0; j < 4; j++) q[j] += mx[j];
+                }
+                if (nAy == nxt) {
+                    pay += sty; nAy = fmaf(pay, inv_y, off_y);
+#pragma unroll
+                    for (int j = 0; j < 4; j++) q[j] += my[j];
+                }
+                if (nAz == nxt) {
+                    paz -= 1.0f; nAz = fmaf(paz, inv_z, off_z);
+#pragma unroll
+                    for (int j = 0; j < 4; j++) q[j] -= nn;
+                }
+#pragma unroll
+                for (int j = 0; j < 4; j++)
+                    if (FL_IN(2 * (long long)q[j] + 1, xlen)) xn[j] = Store<TX>::ld2(x + 2 * (long long)q[j]);
+            }
+#pragma unroll
+            for (int j = 0; j < 4; j++) s[j] = __ffma2_rn(make_float2(seg, seg), xv[j], s[j]);
+            if (!cont) goto done;
+#pragma unroll
+            for (int j = 0; j < 4; j++) xv[j] = xn[j];
+            cur = nxt;
+        }
+    }
+done:
+#pragma unroll
+    for (int j = 0; j < 4; j++) acc[j] = s[j];
+}
+
 __device__ __forceinline__ float ray_cr(float scale, float dxy2, float dz2)
 {
     return fmul(scale, fsqrt(fadd(dxy2, dz2)));

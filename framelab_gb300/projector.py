@@ -124,6 +124,18 @@ class Plan:
         _lib.check(self._L.fl_plan_option(self._h, _lib.OPT_ROT_MIRROR, int(bool(on))))
 
     @property
+    def quarter_turn(self) -> bool:
+        """Whether the matched pair also uses the quarter-turn symmetry between
+        views v and v + nv/4 (FL_OPT_QUARTER_TURN; needs the half turn)."""
+        v = C.c_int()
+        _lib.check(self._L.fl_plan_query(self._h, _lib.OPT_QUARTER_TURN, C.byref(v)))
+        return bool(v.value)
+
+    @quarter_turn.setter
+    def quarter_turn(self, on: bool):
+        _lib.check(self._L.fl_plan_option(self._h, _lib.OPT_QUARTER_TURN, int(bool(on))))
+
+    @property
     def handle(self):
         return self._h
 

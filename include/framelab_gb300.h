@@ -192,8 +192,14 @@ int fl_plan_sizes(const fl_plan *plan, int64_t *n_vox, int64_t *n_rays);
  *   (x, y, z), with the same length and c_r. One walk or weight serves four
  *   rays; the matrix stays exactly transposed and differs from the general
  *   kernels' by the FP32 rounding of the turned views' own tables.
- *   Queries report 0 while FL_OPT_Z_MIRROR is off. */
-enum { FL_OPT_Z_MIRROR = 1, FL_OPT_ROT_MIRROR = 2 };
+ *   Queries report 0 while FL_OPT_Z_MIRROR is off.
+ * FL_OPT_QUARTER_TURN: on top of FL_OPT_ROT_MIRROR, on by default when
+ *   nx == ny, nv is a multiple of 4 and view v + nv/4 is view v turned by
+ *   pi/2 (to within 1e-6). Ray (v + j nv/4, a, b) is then defined as ray
+ *   (v, a, b) turned by j pi/2, crossing voxel R^j (x, y, z) with
+ *   R (x, y, z) = (n-1-y, x, z): one walk or weight serves eight rays. Queries
+ *   report 0 while either option below it is off. */
+enum { FL_OPT_Z_MIRROR = 1, FL_OPT_ROT_MIRROR = 2, FL_OPT_QUARTER_TURN = 3 };
 int fl_plan_option(fl_plan *plan, int option, int value);
 int fl_plan_query(const fl_plan *plan, int option, int *value);
 

@@ -574,3 +574,44 @@ def test_rot_mirror_agrees_with_general_kernels_and_is_exact():
     P.rot_mirror = False               # the captured graph follows the option
     um = cg.solve(b, iters=6)
     assert _rel(_host(uq), _host(um)) < 1e-4
+
+
+def test_quarter_turn_is_detected_and_exact():
+    torch = _torch()
+    from framelab_gb300.solvers import NativeCGLS
+    p = _cone_small("circle")                          # 32^3, 16 views over a full turn
+    n, nb, nv = int(p["nx"]), len(p["z_det"]), len(p["sd_phi"])
+    P = _plan(p)
+    assert P.z_mirror and P.rot_mirror and P.quarter_turn
+    P.rot_mirror = False                               # rides on the half turn
+    assert not P.quarter_turn
+    P.rot_mirror = True
+    assert P.quarter_turn
+    six = G.cone_para_mm(32, 6, 48, 40, det_pitch_mm=8.0, SO_mm=600.0, SD_mm=1200.0,
+                         voxel_mm=8.0)                 # half turn, but nv/4 not whole
+    Q = _plan(six)
+    assert Q.rot_mirror and not Q.quarter_turn
+    x = PH.ellipsoids_3d(n, seed=11).reshape(-1)
+    rng = np.random.default_rng(6)
+    r = rng.standard_normal(P.n_rays).astype(np.float32)
+    y8, x8 = _host(P.forward(_dev(x))), _host(P.adjoint(_dev(r)))
+    P.quarter_turn = False
+    y4, x4 = _host(P.forward(_dev(x))), _host(P.adjoint(_dev(r)))
+    P.quarter_turn = True
+    assert _rel(y8, y4) < 1e-5 and _rel(x8, x4) < 1e-4, (_rel(y8, y4), _rel(x8, x4))
+    # by construction: views v + nv/4 of A x are views v of A R(x), with
+    # R(x)[z, y, x] = x[z, x, n-1-y] (the voxel turned by pi/2)
+    xr = x.reshape(n, n, n)[:, :, ::-1].transpose(0, 2, 1).reshape(-1).copy()
+    yr = _host(P.forward(_dev(xr))).reshape(nv, nb, -1)
+    assert np.array_equal(y8.reshape(nv, nb, -1)[nv // 4:], yr[:3 * nv // 4])
+    # the adjoint stays the exact transpose
+    lhs = np.dot(y8.astype(np.float64), r.astype(np.float64))
+    rhs = np.dot(x.astype(np.float64), x8.astype(np.float64))
+    assert abs(lhs - rhs) / abs(lhs) < 1e-5
+    # the fused CGLS follows the option (its graph is captured again)
+    b = P.adjoint(P.forward(_dev(x))).reshape(-1).contiguous()
+    cg = NativeCGLS(P, "mixed")
+    u8 = cg.solve(b, iters=6).clone()
+    P.quarter_turn = False
+    u4 = cg.solve(b, iters=6)
+    assert _rel(_host(u8), _host(u4)) < 1e-3
