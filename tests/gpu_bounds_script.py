@@ -25,11 +25,12 @@ def run_plan(p, rng):
     for dt in (torch.float32, torch.float16):
         P.forward(x.to(dt))
         P.adjoint(y.to(dt))
-    if P.cone:
-        P.z_mirror = False
-        P.forward(x)
-        P.adjoint(y)
-        P.z_mirror = True
+    if P.cone:                         # every symmetry level the plan allows
+        for q, r, z in ((False, True, True), (False, False, True), (False, False, False)):
+            P.quarter_turn, P.rot_mirror, P.z_mirror = q, r, z
+            P.forward(x)
+            P.adjoint(y)
+        P.z_mirror, P.rot_mirror, P.quarter_turn = True, True, True
     for mode in ("graph", "mixed"):
         NativeCGLS(P, mode).solve(torch.abs(x), lam=0.1, iters=3, refresh=2)
 
@@ -42,7 +43,9 @@ def main():
     rng = np.random.default_rng(0)
     cases = [
         G.cone_para_mm(32, 16, 48, 40, det_pitch_mm=8.0, SO_mm=600.0, SD_mm=1200.0,
-                       voxel_mm=8.0),                                  # circle: z-mirror
+                       voxel_mm=8.0),                                  # circle: quarter turns
+        G.cone_para_mm(30, 18, 44, 36, det_pitch_mm=8.0, SO_mm=600.0, SD_mm=1200.0,
+                       voxel_mm=8.0),                                  # circle: half turn
         G.cone_para(16, 16, 16, 36, 32, 10, L=(2, 2, 2)),              # short SO, steep rows
         G.cone_para(20, 18, 14, 30, 26, 0, L=(2, 2, 2), scan="helix", zmax=0.5, rps=1.0,
                     vtab=1.0, fps=8),                                  # helix: general kernels
