@@ -348,6 +348,7 @@ extern "C" int fl_batch_create(fl_plan* const* plans, int32_t n_plans, fl_batch*
         b.views = p->d_idY; b.nvf = nvf;
         b.G.kind = p->det_kind; b.G.u0 = p->u0; b.G.du = p->du; b.G.g0 = p->g0; b.G.dg = p->dg;
         b.G.v0 = p->v0; b.G.dv = p->dv; b.G.SO = s.SO; b.G.SD = p->SD;
+        b.G.rdu = 1.0f / p->du; b.G.rdg = p->dg != 0.0f ? 1.0f / p->dg : 0.0f;
         b.nx = s.nx; b.ny = s.ny; b.na = s.na; b.nv = s.nv; b.scale = s.scale;
         xoff[i + 1] = xoff[i] + (long long)s.nx * s.ny;
         yoff[i + 1] = yoff[i] + (long long)s.na * s.nv;

@@ -773,6 +773,8 @@ DetGrid det_grid(const fl_plan* p)
     DetGrid G;
     G.kind = p->det_kind; G.u0 = p->u0; G.du = p->du; G.g0 = p->g0; G.dg = p->dg;
     G.v0 = p->v0; G.dv = p->dv; G.SO = p->s.SO; G.SD = p->SD;
+    G.rdu = p->du != 0.0f ? 1.0f / p->du : 0.0f;
+    G.rdg = p->dg != 0.0f ? 1.0f / p->dg : 0.0f;
     return G;
 }
 
