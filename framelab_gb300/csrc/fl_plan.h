@@ -80,7 +80,10 @@ struct fl_plan {
 // z-folded volume stores, per frame, the pairs (voxel (ix, iy, iz),
 // voxel (ix, iy, nz-1-iz)) for iz < nz/2 at pair index (iz*ny + iy)*nx + ix;
 // the adjoint input (pre-weighted sinogram) is always folded the same way:
-// pairs (row ib, row nb-1-ib) for ib < nb/2 at pair index (iv*nb/2 + ib)*na + ia.
+// pairs (row ib, row nb-1-ib) for ib < nb/2 at pair index (iv*nb/2 + ib)*na + ia,
+// except on a quarter-turn plan (rot4), where the 8 values of views
+// iv + j nv/4 (j = 0..3), rows ib and nb-1-ib, lie side by side at 8 *
+// ((iv*nb/2 + ib)*na + ia) + 2 j for iv < nv/4.
 // For other plans both layouts are the standard ones.
 enum {
     FL_LAY_X_FOLDED = 1,   // the volume operand is z-folded

@@ -115,7 +115,9 @@ k_fwd_quad(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restr
 
 // Quarter-turn form (fl_plan::rot4): the block walks rows ib < nb/2 of views
 // iv < nv/4; each walk yields the rays of views iv + j nv/4 (j = 0..3) at the
-// same column and rows, all eight with the walked ray's c_r.
+// same column and rows, all eight with the walked ray's c_r. yfold writes the
+// backprojection's input layout for these plans: per (iv < nv/4, ib < nb/2,
+// ia) the 8 values (view iv + j nv/4, rows ib / nb-1-ib) side by side.
 template <typename TX, typename TY>
 __global__ void __launch_bounds__(128, 8)
 k_fwd_oct(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restrict__ col,
@@ -142,8 +144,8 @@ k_fwd_oct(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restri
         o0 = cr * o0; o1 = cr * o1;
         if (cr_power == 2) { o0 = cr * o0; o1 = cr * o1; }
         const long long vj = iv + (long long)j * qv;
-        if (yfold) {
-            Store<TY>::st2(y + 2 * ((vj * nbh + ib) * na + ia), o0, o1);
+        if (yfold) {                    // the 8 values of the orbit side by side
+            Store<TY>::st2(y + 8 * (((long long)iv * nbh + ib) * na + ia) + 2 * j, o0, o1);
         } else {
             Store<TY>::st(y + (vj * nb + ib) * na + ia, o0);
             Store<TY>::st(y + (vj * nb + (nb - 1 - ib)) * na + ia, o1);
@@ -221,6 +223,31 @@ __global__ void k_weight_fold(float* __restrict__ yw, const TY* __restrict__ y,
     float a = Store<TY>::ld_plain(y + ((long long)iv * nb + ib) * na + ia);
     float b = Store<TY>::ld_plain(y + ((long long)iv * nb + (nb - 1 - ib)) * na + ia);
     Store<float>::st2(yw + 2 * r, cr * a, cr * b);
+}
+
+// Packed yw of a quarter-turn plan: for r = (iv < nv/4, ib < nb/2, ia) the 8
+// values c_r y of views iv + j nv/4 (j = 0..3), rows ib and nb-1-ib, with c_r
+// of view iv (the ray they are all defined by).
+template <typename TY>
+__global__ void k_weight_oct(float* __restrict__ yw, const TY* __restrict__ y,
+                             const float* __restrict__ colr, const RowEntry* __restrict__ row,
+                             int na, int nb, int nv, long long npack, float scale)
+{
+    long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= npack) return;
+    const int nbh = nb / 2, qv = nv / 4;
+    const int ia = (int)(r % na);
+    const long long q = r / na;
+    const int ib = (int)(q % nbh);
+    const int iv = (int)(q / nbh);
+    const float cr = ray_cr(scale, colr[(long long)iv * na + ia], row[(long long)iv * nb + ib].dz2);
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const long long vj = iv + (long long)j * qv;
+        const float a = Store<TY>::ld_plain(y + (vj * nb + ib) * na + ia);
+        const float b = Store<TY>::ld_plain(y + (vj * nb + (nb - 1 - ib)) * na + ia);
+        Store<float>::st2(yw + 8 * r + 2 * j, cr * a, cr * b);
+    }
 }
 
 // z-fold / unfold of volumes (all frames): pair r = (iz < nz/2, iy, ix) of a
@@ -533,17 +560,15 @@ k_adj_quad(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __r
         }
 }
 
-// Quarter-turn form of adj_rows_pair: every weight multiplies the folded row
-// pairs of views v + j nv/4 (y0..y3) into the sums a0..a3.
+// Quarter-turn form of adj_rows_pair: every weight multiplies the row pairs of
+// views v + j nv/4 into the sums a0..a3; y8 holds them side by side (8 floats
+// per row and column, 32-byte aligned).
 template <int MODE, int TZ>
 __device__ __forceinline__ void adj_rows_oct(float2 (&a0)[TZ], float2 (&a1)[TZ],
                                              float2 (&a2)[TZ], float2 (&a3)[TZ], int nk, int z0,
                                              float l, float h, float e1, float e2, float s1,
                                              float s2, const float2* __restrict__ rv,
-                                             const float* __restrict__ y0,
-                                             const float* __restrict__ y1,
-                                             const float* __restrict__ y2,
-                                             const float* __restrict__ y3, int na, int nb)
+                                             const float* __restrict__ y8, int na, int nb)
 {
     float mn = fminf(e1, e2), mx = fmaxf(e1, e2);
     float lo_e = e1 - 0.02f, hi_e = e2 + s2 + 0.02f;
@@ -566,9 +591,10 @@ __device__ __forceinline__ void adj_rows_oct(float2 (&a0)[TZ], float2 (&a1)[TZ],
         for (int ib = blo; ib <= bhi; ib++) {
             if (!FL_IN(ib, nb)) continue;
             const float2 re = rv[ib];
-            const long long o = 2 * (long long)ib * na;
-            const float2 t0 = Store<float>::ld2(y0 + o), t1 = Store<float>::ld2(y1 + o);
-            const float2 t2 = Store<float>::ld2(y2 + o), t3 = Store<float>::ld2(y3 + o);
+            const float4* q8 = reinterpret_cast<const float4*>(y8 + 8 * (long long)ib * na);
+            const float4 u01 = __ldg(q8), u23 = __ldg(q8 + 1);
+            const float2 t0 = make_float2(u01.x, u01.y), t1 = make_float2(u01.z, u01.w);
+            const float2 t2 = make_float2(u23.x, u23.y), t3 = make_float2(u23.z, u23.w);
             const float2 az = __ffma2_rn(make_float2(fk0, fk1), make_float2(re.x, re.x),
                                          make_float2(re.y, re.y));
             float l2, h2;
@@ -588,7 +614,8 @@ __device__ __forceinline__ void adj_rows_oct(float2 (&a0)[TZ], float2 (&a1)[TZ],
 // turns V_j = R^j V0, with a run of TZ voxels of the lower half and their
 // mirrors; one frame. It visits the views iv < nv/4. In view iv a weight of
 // column V_k multiplies the row pairs of view iv + j nv/4 into V_{k+j mod 4}
-// (A[(iv + j nv/4, r), R^j V] = A[(iv, r), V]).
+// (A[(iv + j nv/4, r), R^j V] = A[(iv, r), V]). yw is the packed sinogram of
+// k_weight_oct / k_fwd_oct (8 values per (iv < nv/4, ib < nb/2, ia)).
 template <typename TX, int TZ>
 __global__ void __launch_bounds__(128, TZ == 2 ? 8 : 6)
 k_adj_oct(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __restrict__ col,
@@ -610,15 +637,12 @@ k_adj_oct(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __re
         A0[k] = make_float2(0.0f, 0.0f); A1[k] = A0[k]; A2[k] = A0[k]; A3[k] = A0[k];
     }
     const float inv_dv = 1.0f / G.dv;
-    const long long vstride = (long long)nbw * na * 2;        // folded floats per view
+    const long long vstride = (long long)nbw * na * 8;        // packed floats per view
     for (int iv = 0; iv < qv; iv++) {
         const ViewEntry ve = view[iv];
         const ColEntry* cv = col + (long long)iv * na;
         const float2* rv = rowz + (long long)iv * nb;
-        const float* y0 = yw + (long long)iv * vstride;
-        const float* y1 = y0 + (long long)qv * vstride;
-        const float* y2 = y1 + (long long)qv * vstride;
-        const float* y3 = y2 + (long long)qv * vstride;
+        const float* yv = yw + (long long)iv * vstride;
         const float zr0 = (float)(z0 - nz / 2) * dz - ve.sz;
         const float zr1 = (float)(z0 + nk - nz / 2) * dz - ve.sz;
         const float tol = 1e-3f * dz;
@@ -643,13 +667,13 @@ k_adj_oct(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __re
                 const float r1 = __fdividef(1.0f, l + ve.ac), r2 = __fdividef(1.0f, hh + ve.ac);
                 const float s1 = dz * r1 * inv_dv, s2 = dz * r2 * inv_dv;
                 const float e1 = (zr0 * r1 - G.v0) * inv_dv, e2 = (zr0 * r2 - G.v0) * inv_dv;
-                const int o = 2 * ia;
+                const float* y8 = yv + 8 * ia;
                 if (mode < 0)
-                    adj_rows_oct<-1, TZ>(b0, b1, b2, b3, nk, z0, l, hh, e1, e2, s1, s2, rv,
-                                         y0 + o, y1 + o, y2 + o, y3 + o, na, nbw);
+                    adj_rows_oct<-1, TZ>(b0, b1, b2, b3, nk, z0, l, hh, e1, e2, s1, s2, rv, y8,
+                                         na, nbw);
                 else
-                    adj_rows_oct<0, TZ>(b0, b1, b2, b3, nk, z0, l, hh, e1, e2, s1, s2, rv,
-                                        y0 + o, y1 + o, y2 + o, y3 + o, na, nbw);
+                    adj_rows_oct<0, TZ>(b0, b1, b2, b3, nk, z0, l, hh, e1, e2, s1, s2, rv, y8,
+                                        na, nbw);
             }
         };
         column(cx[0], cy[0], A0, A1, A2, A3);
@@ -924,6 +948,21 @@ int fl_matched_weight(fl_plan* p, const void* y, int yt, float* yw, cudaStream_t
     const fl_scan& s = p->s;
     long long nr = p->n_rays;
     int three = s.ndim == 3;
+    if (three && p->zmirror && p->rot && p->rot4) {
+        long long npk = (long long)(s.nv / 4) * (s.nb / 2) * s.na;
+        unsigned g = fl_div_up(npk, 256);
+        if (yt == FL_F32)
+            k_weight_oct<float><<<g, 256, 0, st>>>(yw, (const float*)y, p->d_colr, p->d_row, s.na,
+                                                   s.nb, s.nv, npk, s.scale);
+        else if (yt == FL_F16)
+            k_weight_oct<__half><<<g, 256, 0, st>>>(yw, (const __half*)y, p->d_colr, p->d_row,
+                                                    s.na, s.nb, s.nv, npk, s.scale);
+        else
+            k_weight_oct<__nv_bfloat16><<<g, 256, 0, st>>>(yw, (const __nv_bfloat16*)y, p->d_colr,
+                                                           p->d_row, s.na, s.nb, s.nv, npk,
+                                                           s.scale);
+        return fl_check_launch("matched adjoint weighting");
+    }
     if (three && p->zmirror) {
         long long np = (long long)s.nv * (s.nb / 2) * s.na;
         unsigned g = fl_div_up(np, 256);
