@@ -222,9 +222,10 @@ static int build_tables(fl_plan* p, const std::vector<float>& phi, const float* 
     }
     p->rot = p->rot_ok;
     // quarter turn (fl_plan.h): view v + nv/4 is view v turned by pi/2 to
-    // within 1e-6 (cos -> -sin, sin -> cos), square xy grid
+    // within 1e-6 (cos -> -sin, sin -> cos), square xy grid of a multiple of 4
+    // (the folded volume is then tiled in 4 x 4 columns)
     p->rot4_ok = 0;
-    if (p->rot_ok && s.nv % 4 == 0 && s.nx == s.ny) {
+    if (p->rot_ok && s.nv % 4 == 0 && s.nx == s.ny && s.nx % 4 == 0) {
         bool ok = true;
         const int q = s.nv / 4;
         for (int iv = 0; iv < q && ok; iv++) {

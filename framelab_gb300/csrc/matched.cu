@@ -272,6 +272,31 @@ __global__ void k_fold(const T* __restrict__ src, T* __restrict__ dst, long long
     }
 }
 
+// Fold / unfold of a quarter-turn plan's volume (one frame, n x n x nz): the
+// tiled pair r (fl_plan.h) holds voxel (x, y, z) and its mirror (x, y, nz-1-z).
+template <typename T>
+__global__ void k_fold_tiled(const T* __restrict__ src, T* __restrict__ dst, int n, int nz,
+                             long long npairs, int unfold)
+{
+    const long long nn = (long long)n * n;
+    const int n4 = n >> 2;
+    for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < npairs;
+         r += (long long)gridDim.x * blockDim.x) {
+        const long long z = r / nn;
+        const int rem = (int)(r - z * nn), tile = rem >> 4, w = rem & 15;
+        const int y = (tile / n4) * 4 + (w >> 2), x = (tile % n4) * 4 + (w & 3);
+        const long long lo = z * nn + (long long)y * n + x;
+        const long long hi = (nz - 1 - z) * nn + (long long)y * n + x;
+        if (unfold) {
+            const T a = src[2 * r], b = src[2 * r + 1];
+            dst[lo] = a; dst[hi] = b;
+        } else {
+            const T a = src[lo], b = src[hi];
+            dst[2 * r] = a; dst[2 * r + 1] = b;
+        }
+    }
+}
+
 // yw = c_r * y  (the adjoint gathers pre-weighted sinogram values)
 template <typename TY>
 __global__ void k_weight(float* __restrict__ yw, const TY* __restrict__ y,
@@ -615,7 +640,8 @@ __device__ __forceinline__ void adj_rows_oct(float2 (&a0)[TZ], float2 (&a1)[TZ],
 // mirrors; one frame. It visits the views iv < nv/4. In view iv a weight of
 // column V_k multiplies the row pairs of view iv + j nv/4 into V_{k+j mod 4}
 // (A[(iv + j nv/4, r), R^j V] = A[(iv, r), V]). yw is the packed sinogram of
-// k_weight_oct / k_fwd_oct (8 values per (iv < nv/4, ib < nb/2, ia)).
+// k_weight_oct / k_fwd_oct (8 values per (iv < nv/4, ib < nb/2, ia)); X the
+// tiled folded volume (xfold) or the standard one.
 template <typename TX, int TZ>
 __global__ void __launch_bounds__(128, TZ == 2 ? 8 : 6)
 k_adj_oct(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __restrict__ col,
@@ -690,8 +716,9 @@ k_adj_oct(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __re
 #pragma unroll
             for (int j = 0; j < 4; j++) {
                 const long long c = (long long)cy[j] * n + cx[j];
-                if (xfold) {
-                    Store<TX>::st2(X + 2 * (zl + c), accs[j]->x, accs[j]->y);
+                if (xfold) {                  // the tiled folded volume
+                    const long long t = tiled_pair(cx[j], cy[j], (int)zl, n >> 2);
+                    Store<TX>::st2(X + 2 * t, accs[j]->x, accs[j]->y);
                 } else {
                     Store<TX>::st(X + zl + c, accs[j]->x);
                     Store<TX>::st(X + zh + c, accs[j]->y);
@@ -906,7 +933,10 @@ void launch_fold(fl_plan* p, const void* src, void* dst, int unfold, cudaStream_
     const long long nxy = (long long)s.nx * s.ny;
     const long long npf = nxy * (s.nz / 2), np = npf * s.nt;
     unsigned g = (unsigned)std::min<long long>((np + 255) / 256, 16LL * 152);
-    k_fold<T><<<g, 256, 0, st>>>((const T*)src, (T*)dst, nxy, s.nz, npf, np, unfold);
+    if (p->rot && p->rot4)      // tiled (one frame)
+        k_fold_tiled<T><<<g, 256, 0, st>>>((const T*)src, (T*)dst, s.nx, s.nz, npf, unfold);
+    else
+        k_fold<T><<<g, 256, 0, st>>>((const T*)src, (T*)dst, nxy, s.nz, npf, np, unfold);
 }
 
 size_t dtype_bytes(int t) { return t == FL_F32 ? 4 : 2; }

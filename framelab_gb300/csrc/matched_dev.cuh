@@ -194,13 +194,19 @@ done:
     *accr = r2;
 }
 
+// Folded pair index of voxel (x, y, z) in the 4 x 4 tiled volume of a
+// quarter-turn plan (fl_plan.h); zb = z * n * n, n4 = n / 4.
+__device__ __forceinline__ int tiled_pair(int x, int y, int zb, int n4)
+{
+    return zb + (((y >> 2) * n4 + (x >> 2)) << 4) + ((y & 3) << 2) + (x & 3);
+}
+
 // The z-mirror walk with all four quarter turns (plan flag rot4, nx == ny ==
-// n): per step it gathers the folded pairs of voxel (ix, iy) and of its turns
-// R^j (ix, iy), R (x, y) = (n-1-y, x), which the ray of view v + j nv/4 at the
-// same column and row crosses with the same segment. The four pair indices
-// move with the walk: an x step by d moves them by (d, d n, -d, -d n), a y
-// step by (d n, -d, -d n, d), a z step by -n^2 each. acc[j] gets the
-// (voxel, mirror) sums of turn j. Termination as in walk().
+// n, a multiple of 4): per step it gathers the folded pairs of voxel (ix, iy)
+// and of its turns R^j (ix, iy), R (x, y) = (n-1-y, x), which the ray of view
+// v + j nv/4 at the same column and row crosses with the same segment. x is
+// the tiled folded volume. acc[j] gets the (voxel, mirror) sums of turn j.
+// Termination as in walk().
 template <typename TX>
 __device__ __forceinline__ void walk_oct(const TX* __restrict__ x, float inv_x, float off_x,
                                          float inv_y, float off_y, float inv_z, float off_z,
@@ -219,19 +225,22 @@ __device__ __forceinline__ void walk_oct(const TX* __restrict__ x, float inv_x, 
     const int jx = start_slab(a_in, inv_x, off_x, n);
     const int jy = start_slab(a_in, inv_y, off_y, n);
     const int jz = min(start_slab(a_in, inv_z, off_z, nz), nz / 2 - 1);
-    const int nn = n * n;
+    const int nn = n * n, n4 = n >> 2;
+    int cx = jx, cy = jy, zb = jz * nn;            // voxel of turn 0; z base of all turns
     int q[4];                                      // folded pair index of each turn
-    q[0] = (jz * n + jy) * n + jx;
-    q[1] = (jz * n + jx) * n + (n - 1 - jy);
-    q[2] = (jz * n + (n - 1 - jy)) * n + (n - 1 - jx);
-    q[3] = (jz * n + (n - 1 - jx)) * n + jy;
+    auto turns = [&]() {
+        q[0] = tiled_pair(cx, cy, zb, n4);
+        q[1] = tiled_pair(n - 1 - cy, cx, zb, n4);
+        q[2] = tiled_pair(n - 1 - cx, n - 1 - cy, zb, n4);
+        q[3] = tiled_pair(cy, n - 1 - cx, zb, n4);
+    };
+    turns();
     const bool px = inv_x > 0.0f, py = inv_y > 0.0f;
     float pax = (float)(px ? jx + 1 : jx);
     float pay = (float)(py ? jy + 1 : jy);
     float paz = (float)jz;                         // descending: next plane is jz
     const float stx = px ? 1.0f : -1.0f, sty = py ? 1.0f : -1.0f;
     const int dx = px ? 1 : -1, dy = py ? 1 : -1;
-    const int mx[4] = {dx, dx * n, -dx, -dx * n}, my[4] = {dy * n, -dy, -dy * n, dy};
     float nAx = fmaf(pax, inv_x, off_x);
     float nAy = fmaf(pay, inv_y, off_y);
     float nAz = fmaf(paz, inv_z, off_z);
@@ -256,21 +265,10 @@ __device__ __forceinline__ void walk_oct(const TX* __restrict__ x, float inv_x, 
 #pragma unroll
             for (int j = 0; j < 4; j++) xn[j] = make_float2(0.0f, 0.0f);
             if (cont) {
-                if (nAx == nxt) {
-                    pax += stx; nAx = fmaf(pax, inv_x, off_x);
-#pragma unroll
-                    for (int j = 0; j < 4; j++) q[j] += mx[j];
-                }
-                if (nAy == nxt) {
-                    pay += sty; nAy = fmaf(pay, inv_y, off_y);
-#pragma unroll
-                    for (int j = 0; j < 4; j++) q[j] += my[j];
-                }
-                if (nAz == nxt) {
-                    paz -= 1.0f; nAz = fmaf(paz, inv_z, off_z);
-#pragma unroll
-                    for (int j = 0; j < 4; j++) q[j] -= nn;
-                }
+                if (nAx == nxt) { pax += stx; nAx = fmaf(pax, inv_x, off_x); cx += dx; }
+                if (nAy == nxt) { pay += sty; nAy = fmaf(pay, inv_y, off_y); cy += dy; }
+                if (nAz == nxt) { paz -= 1.0f; nAz = fmaf(paz, inv_z, off_z); zb -= nn; }
+                turns();
 #pragma unroll
                 for (int j = 0; j < 4; j++)
                     if (FL_IN(2 * (long long)q[j] + 1, xlen)) xn[j] = Store<TX>::ld2(x + 2 * (long long)q[j]);
