@@ -55,13 +55,13 @@ struct fl_plan {
     int zmirror;               // in use (FL_OPT_Z_MIRROR)
     // half-turn symmetry on top of the z mirror: one frame, an even number of
     // views with view v + nv/2 opposite view v (sources and detector turned by
-    // pi about the z axis), even nx and ny. The matched model then defines
+    // pi about the z axis), nx and ny multiples of 4. The matched model then defines
     // A[(v + nv/2, a, b), (nx-1-x, ny-1-y, z)] = A[(v, a, b), (x, y, z)] for
     // v < nv/2 (with c_r of view v), so one walk / one weight serves four
     // rays: rows b and nb-1-b of views v and v + nv/2.
     int rot_ok;                // the geometry allows it
     int rot;                   // in use (FL_OPT_ROT_MIRROR; only with zmirror)
-    // quarter turn on top of the half turn: nx == ny a multiple of 4, nv a multiple of 4 and
+    // quarter turn on top of the half turn: nx == ny, nv a multiple of 4 and
     // view v + nv/4 view v turned by pi/2. The matched model then defines
     // A[(v + j nv/4, a, b), R^j (x, y, z)] = A[(v, a, b), (x, y, z)] for
     // v < nv/4, j = 1..3, R (x, y) = (n-1-y, x), so one walk / one weight
@@ -84,10 +84,10 @@ struct fl_plan {
 // except on a quarter-turn plan (rot4), where the 8 values of views
 // iv + j nv/4 (j = 0..3), rows ib and nb-1-ib, lie side by side at 8 *
 // ((iv*nb/2 + ib)*na + ia) + 2 j for iv < nv/4.
-// A quarter-turn plan's folded volume is tiled in xy: the pair of voxel
-// (x, y, z < nz/2) is at z*n*n + 16*((y/4)*(n/4) + x/4) + 4*(y%4) + x%4, so
-// one 128-byte line holds a 4 x 4 patch of pairs (the gathers of a warp's
-// neighbouring rays share lines whatever the ray direction).
+// A half- or quarter-turn plan's folded volume is tiled in xy: the pair of
+// voxel (x, y, z < nz/2) is at z*nx*ny + 16*((y/4)*(nx/4) + x/4) + 4*(y%4) +
+// x%4, so one 128-byte line holds a 4 x 4 patch of pairs (the gathers of a
+// warp's neighbouring rays share lines whatever the ray direction).
 // For other plans both layouts are the standard ones.
 enum {
     FL_LAY_X_FOLDED = 1,   // the volume operand is z-folded

@@ -208,9 +208,10 @@ static int build_tables(fl_plan* p, const std::vector<float>& phi, const float* 
     p->zmirror = p->zmirror_ok;
     // half-turn symmetry (fl_plan.h): view v + nv/2 is view v turned by pi to
     // within 1e-6 in cos and sin (FP32 angles such as 2 pi k / nv are never
-    // exactly opposite), one frame, even nx and ny
+    // exactly opposite), one frame, nx and ny multiples of 4 (the folded volume
+    // is tiled in 4 x 4 columns)
     p->rot_ok = 0;
-    if (p->zmirror_ok && s.nt == 1 && s.nv % 2 == 0 && s.nx % 2 == 0 && s.ny % 2 == 0) {
+    if (p->zmirror_ok && s.nt == 1 && s.nv % 2 == 0 && s.nx % 4 == 0 && s.ny % 4 == 0) {
         bool ok = true;
         const int h = s.nv / 2;
         for (int iv = 0; iv < h && ok; iv++) {
@@ -222,8 +223,7 @@ static int build_tables(fl_plan* p, const std::vector<float>& phi, const float* 
     }
     p->rot = p->rot_ok;
     // quarter turn (fl_plan.h): view v + nv/4 is view v turned by pi/2 to
-    // within 1e-6 (cos -> -sin, sin -> cos), square xy grid of a multiple of 4
-    // (the folded volume is then tiled in 4 x 4 columns)
+    // within 1e-6 (cos -> -sin, sin -> cos), square xy grid
     p->rot4_ok = 0;
     if (p->rot_ok && s.nv % 4 == 0 && s.nx == s.ny && s.nx % 4 == 0) {
         bool ok = true;

@@ -272,21 +272,22 @@ __global__ void k_fold(const T* __restrict__ src, T* __restrict__ dst, long long
     }
 }
 
-// Fold / unfold of a quarter-turn plan's volume (one frame, n x n x nz): the
-// tiled pair r (fl_plan.h) holds voxel (x, y, z) and its mirror (x, y, nz-1-z).
+// Fold / unfold of a half- or quarter-turn plan's volume (one frame,
+// nx x ny x nz, nx and ny multiples of 4): the tiled pair r (fl_plan.h) holds
+// voxel (x, y, z) and its mirror (x, y, nz-1-z).
 template <typename T>
-__global__ void k_fold_tiled(const T* __restrict__ src, T* __restrict__ dst, int n, int nz,
-                             long long npairs, int unfold)
+__global__ void k_fold_tiled(const T* __restrict__ src, T* __restrict__ dst, int nx, int ny,
+                             int nz, long long npairs, int unfold)
 {
-    const long long nn = (long long)n * n;
-    const int n4 = n >> 2;
+    const long long nn = (long long)nx * ny;
+    const int nx4 = nx >> 2;
     for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < npairs;
          r += (long long)gridDim.x * blockDim.x) {
         const long long z = r / nn;
         const int rem = (int)(r - z * nn), tile = rem >> 4, w = rem & 15;
-        const int y = (tile / n4) * 4 + (w >> 2), x = (tile % n4) * 4 + (w & 3);
-        const long long lo = z * nn + (long long)y * n + x;
-        const long long hi = (nz - 1 - z) * nn + (long long)y * n + x;
+        const int y = (tile / nx4) * 4 + (w >> 2), x = (tile % nx4) * 4 + (w & 3);
+        const long long lo = z * nn + (long long)y * nx + x;
+        const long long hi = (nz - 1 - z) * nn + (long long)y * nx + x;
         if (unfold) {
             const T a = src[2 * r], b = src[2 * r + 1];
             dst[lo] = a; dst[hi] = b;
@@ -506,7 +507,7 @@ __device__ __forceinline__ void adj_rows_quad(float2 (&acc)[TZ], float2 (&accr)[
 // of both columns: a weight of V multiplies the row pair of view iv into V
 // and the row pair of view iv + nv/2 into T (A[(iv + nv/2, r), T] =
 // A[(iv, r), V]); a weight of T, the other way round. yw is the folded
-// sinogram of all views; X the folded volume (xfold) or the standard one.
+// sinogram of all views; X the tiled folded volume (xfold) or the standard one.
 template <typename TX, int TZ>
 __global__ void __launch_bounds__(128, 8)
 k_adj_quad(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __restrict__ col,
@@ -573,9 +574,11 @@ k_adj_quad(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __r
     for (int k = 0; k < TZ; k++)
         if (k < nk) {
             const long long zl = (long long)(z0 + k) * nxy, zh = (long long)(nz - 1 - z0 - k) * nxy;
-            if (xfold) {
-                Store<TX>::st2(X + 2 * (zl + cV), accV[k].x, accV[k].y);
-                Store<TX>::st2(X + 2 * (zl + cT), accT[k].x, accT[k].y);
+            if (xfold) {                      // the tiled folded volume
+                const int tV = tiled_pair(ix, iy, (int)zl, nx >> 2);
+                const int tT = tiled_pair(tx, ty, (int)zl, nx >> 2);
+                Store<TX>::st2(X + 2 * (long long)tV, accV[k].x, accV[k].y);
+                Store<TX>::st2(X + 2 * (long long)tT, accT[k].x, accT[k].y);
             } else {
                 Store<TX>::st(X + zl + cV, accV[k].x);
                 Store<TX>::st(X + zh + cV, accV[k].y);
@@ -933,8 +936,9 @@ void launch_fold(fl_plan* p, const void* src, void* dst, int unfold, cudaStream_
     const long long nxy = (long long)s.nx * s.ny;
     const long long npf = nxy * (s.nz / 2), np = npf * s.nt;
     unsigned g = (unsigned)std::min<long long>((np + 255) / 256, 16LL * 152);
-    if (p->rot && p->rot4)      // tiled (one frame)
-        k_fold_tiled<T><<<g, 256, 0, st>>>((const T*)src, (T*)dst, s.nx, s.nz, npf, unfold);
+    if (p->rot)                 // half- or quarter-turn plan: tiled (one frame)
+        k_fold_tiled<T><<<g, 256, 0, st>>>((const T*)src, (T*)dst, s.nx, s.ny, s.nz, npf,
+                                           unfold);
     else
         k_fold<T><<<g, 256, 0, st>>>((const T*)src, (T*)dst, nxy, s.nz, npf, np, unfold);
 }

@@ -123,11 +123,18 @@ done:
     return acc;
 }
 
+// Folded pair index of voxel (x, y, z) in the 4 x 4 tiled volume of a
+// half- or quarter-turn plan (fl_plan.h); zb = z * nx * ny, nx4 = nx / 4.
+__device__ __forceinline__ int tiled_pair(int x, int y, int zb, int nx4)
+{
+    return zb + (((y >> 2) * nx4 + (x >> 2)) << 4) + ((y & 3) << 2) + (x & 3);
+}
+
 // The z-mirror walk of a descending ray with the half-turn partner (plan
 // flag rot): besides the folded pair of voxel (ix, iy, iz) it gathers the
-// pair of voxel (nx-1-ix, ny-1-iy, iz), folded index Kz - v with
-// Kz = (2 iz + 1) nx ny - 1, which the turned ray of view v + nv/2 crosses
-// with the same segment. *acc gets the (voxel, mirror) sums, *accr the turned
+// pair of voxel (nx-1-ix, ny-1-iy, iz), which the turned ray of view v + nv/2
+// crosses with the same segment. x is the tiled folded volume (nx, ny
+// multiples of 4). *acc gets the (voxel, mirror) sums, *accr the turned
 // pair's. Termination as in walk().
 template <typename TX>
 __device__ __forceinline__ void walk_quad(const TX* __restrict__ x, float inv_x, float off_x,
@@ -148,15 +155,15 @@ __device__ __forceinline__ void walk_quad(const TX* __restrict__ x, float inv_x,
     const int jx = start_slab(a_in, inv_x, off_x, nx);
     const int jy = start_slab(a_in, inv_y, off_y, ny);
     const int jz = min(start_slab(a_in, inv_z, off_z, nz), nz / 2 - 1);
-    const int nxy = nx * ny;
-    int v = (jz * ny + jy) * nx + jx;              // < 2^31 (checked at plan creation)
-    int kz = (2 * jz + 1) * nxy - 1;               // turned pair index = kz - v
+    const int nxy = nx * ny, nx4 = nx >> 2;
+    int cx = jx, cy = jy, zb = jz * nxy;           // < 2^31 (checked at plan creation)
+    int v = tiled_pair(cx, cy, zb, nx4), vr = tiled_pair(nx - 1 - cx, ny - 1 - cy, zb, nx4);
     const bool px = inv_x > 0.0f, py = inv_y > 0.0f;
     float pax = (float)(px ? jx + 1 : jx);
     float pay = (float)(py ? jy + 1 : jy);
     float paz = (float)jz;                         // descending: next plane is jz
     const float stx = px ? 1.0f : -1.0f, sty = py ? 1.0f : -1.0f;
-    const int dvx = px ? 1 : -1, dvy = py ? nx : -nx;
+    const int dx = px ? 1 : -1, dy = py ? 1 : -1;
     float nAx = fmaf(pax, inv_x, off_x);
     float nAy = fmaf(pay, inv_y, off_y);
     float nAz = fmaf(paz, inv_z, off_z);
@@ -164,7 +171,7 @@ __device__ __forceinline__ void walk_quad(const TX* __restrict__ x, float inv_x,
     float2 s2 = make_float2(0.0f, 0.0f), r2 = make_float2(0.0f, 0.0f);
     float2 xv2 = make_float2(0.0f, 0.0f), xr2 = make_float2(0.0f, 0.0f);
     if (FL_IN(2 * (long long)v + 1, xlen)) xv2 = Store<TX>::ld2(x + 2 * (long long)v);
-    if (FL_IN(2 * (long long)(kz - v) + 1, xlen)) xr2 = Store<TX>::ld2(x + 2 * (long long)(kz - v));
+    if (FL_IN(2 * (long long)vr + 1, xlen)) xr2 = Store<TX>::ld2(x + 2 * (long long)vr);
     const int budget = nx + ny + nz + 4;
     for (int it = 0; it < budget; it += 4) {
 #pragma unroll
@@ -174,12 +181,13 @@ __device__ __forceinline__ void walk_quad(const TX* __restrict__ x, float inv_x,
             const bool cont = nxt < a_out;         // false at the exit (and for NaN)
             float2 xn2 = make_float2(0.0f, 0.0f), xnr2 = make_float2(0.0f, 0.0f);
             if (cont) {
-                if (nAx == nxt) { pax += stx; v += dvx; nAx = fmaf(pax, inv_x, off_x); }
-                if (nAy == nxt) { pay += sty; v += dvy; nAy = fmaf(pay, inv_y, off_y); }
-                if (nAz == nxt) { paz -= 1.0f; v -= nxy; kz -= 2 * nxy; nAz = fmaf(paz, inv_z, off_z); }
+                if (nAx == nxt) { pax += stx; cx += dx; nAx = fmaf(pax, inv_x, off_x); }
+                if (nAy == nxt) { pay += sty; cy += dy; nAy = fmaf(pay, inv_y, off_y); }
+                if (nAz == nxt) { paz -= 1.0f; zb -= nxy; nAz = fmaf(paz, inv_z, off_z); }
+                v = tiled_pair(cx, cy, zb, nx4);
+                vr = tiled_pair(nx - 1 - cx, ny - 1 - cy, zb, nx4);
                 if (FL_IN(2 * (long long)v + 1, xlen)) xn2 = Store<TX>::ld2(x + 2 * (long long)v);
-                if (FL_IN(2 * (long long)(kz - v) + 1, xlen))
-                    xnr2 = Store<TX>::ld2(x + 2 * (long long)(kz - v));
+                if (FL_IN(2 * (long long)vr + 1, xlen)) xnr2 = Store<TX>::ld2(x + 2 * (long long)vr);
             }
             s2 = __ffma2_rn(make_float2(seg, seg), xv2, s2);
             r2 = __ffma2_rn(make_float2(seg, seg), xr2, r2);
@@ -194,12 +202,6 @@ done:
     *accr = r2;
 }
 
-// Folded pair index of voxel (x, y, z) in the 4 x 4 tiled volume of a
-// quarter-turn plan (fl_plan.h); zb = z * n * n, n4 = n / 4.
-__device__ __forceinline__ int tiled_pair(int x, int y, int zb, int n4)
-{
-    return zb + (((y >> 2) * n4 + (x >> 2)) << 4) + ((y & 3) << 2) + (x & 3);
-}
 
 // The z-mirror walk with all four quarter turns (plan flag rot4, nx == ny ==
 // n, a multiple of 4): per step it gathers the folded pairs of voxel (ix, iy)

@@ -186,10 +186,11 @@ int fl_plan_sizes(const fl_plan *plan, int64_t *n_vox, int64_t *n_rays);
  * FL_OPT_ROT_MIRROR: on top of FL_OPT_Z_MIRROR, on by default for a scan of
  *   one frame with an even number of views where view v + nv/2 is view v
  *   turned by pi about the z axis (cos and sin of the angles opposite to
- *   within 1e-6) and even nx, ny. The matched pair then walks / weighs only
- *   views v < nv/2: ray (v + nv/2, a, b) is defined as ray (v, a, b) turned by
- *   pi, crossing voxel (nx-1-x, ny-1-y, z) where ray (v, a, b) crosses
- *   (x, y, z), with the same length and c_r. One walk or weight serves four
+ *   within 1e-6) and nx, ny multiples of 4. The matched pair then walks /
+ *   weighs only views v < nv/2: ray (v + nv/2, a, b) is defined as ray
+ *   (v, a, b) turned by pi, crossing voxel (nx-1-x, ny-1-y, z) where ray
+ *   (v, a, b) crosses (x, y, z), with the same length and c_r. One walk or
+ *   weight serves four
  *   rays; the matrix stays exactly transposed and differs from the general
  *   kernels' by the FP32 rounding of the turned views' own tables.
  *   Queries report 0 while FL_OPT_Z_MIRROR is off.

@@ -44,7 +44,7 @@ def main():
     cases = [
         G.cone_para_mm(32, 16, 48, 40, det_pitch_mm=8.0, SO_mm=600.0, SD_mm=1200.0,
                        voxel_mm=8.0),                                  # circle: quarter turns
-        G.cone_para_mm(30, 18, 44, 36, det_pitch_mm=8.0, SO_mm=600.0, SD_mm=1200.0,
+        G.cone_para_mm(28, 18, 44, 36, det_pitch_mm=8.0, SO_mm=600.0, SD_mm=1200.0,
                        voxel_mm=8.0),                                  # circle: half turn
         G.cone_para(16, 16, 16, 36, 32, 10, L=(2, 2, 2)),              # short SO, steep rows
         G.cone_para(20, 18, 14, 30, 26, 0, L=(2, 2, 2), scan="helix", zmax=0.5, rps=1.0,

@@ -615,3 +615,23 @@ def test_quarter_turn_is_detected_and_exact():
     P.quarter_turn = False
     u4 = cg.solve(b, iters=6)
     assert _rel(_host(u8), _host(u4)) < 1e-3
+
+
+def test_turn_plans_need_columns_of_four():
+    """The half- and quarter-turn forms keep the folded volume in 4 x 4 tiles:
+    sizes that are not multiples of 4 keep the z mirror alone."""
+    p = G.cone_para_mm(30, 16, 44, 36, det_pitch_mm=8.0, SO_mm=600.0, SD_mm=1200.0,
+                       voxel_mm=8.0)
+    P = _plan(p)
+    assert P.z_mirror and not P.rot_mirror and not P.quarter_turn
+    q = G.cone_para(32, 28, 16, 44, 36, 16, L=(2, 28 / 16, 1))   # rectangular: half turn only
+    Q = _plan(q)
+    assert Q.rot_mirror and not Q.quarter_turn
+    x = np.random.default_rng(2).standard_normal(Q.n_vox).astype(np.float32)
+    y = np.random.default_rng(3).standard_normal(Q.n_rays).astype(np.float32)
+    lhs = np.dot(_host(Q.forward(_dev(x))).astype(np.float64), y.astype(np.float64))
+    rhs = np.dot(x.astype(np.float64), _host(Q.adjoint(_dev(y))).astype(np.float64))
+    assert abs(lhs - rhs) / abs(lhs) < 1e-5
+    yq = _host(Q.forward(_dev(x)))
+    Q.rot_mirror = False
+    assert _rel(yq, _host(Q.forward(_dev(x)))) < 1e-5
