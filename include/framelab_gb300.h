@@ -190,9 +190,9 @@ int fl_plan_sizes(const fl_plan *plan, int64_t *n_vox, int64_t *n_rays);
  *   weighs only views v < nv/2: ray (v + nv/2, a, b) is defined as ray
  *   (v, a, b) turned by pi, crossing voxel (nx-1-x, ny-1-y, z) where ray
  *   (v, a, b) crosses (x, y, z), with the same length and c_r. One walk or
- *   weight serves four
- *   rays; the matrix stays exactly transposed and differs from the general
- *   kernels' by the FP32 rounding of the turned views' own tables.
+ *   weight serves four rays; the matrix stays exactly transposed and differs
+ *   from the general kernels' by the FP32 rounding of the turned views' own
+ *   tables.
  *   Queries report 0 while FL_OPT_Z_MIRROR is off.
  * FL_OPT_QUARTER_TURN: on top of FL_OPT_ROT_MIRROR, on by default when
  *   nx == ny, nv is a multiple of 4 and view v + nv/4 is view v turned by
