@@ -125,6 +125,7 @@ done:
 
 // Folded pair index of voxel (x, y, z) in the 4 x 4 tiled volume of a
 // half- or quarter-turn plan (fl_plan.h); zb = z * nx * ny, nx4 = nx / 4.
+// The voxel turned by pi, (nx-1-x, ny-1-y, z), is at 2 zb + nx ny - 1 minus it.
 __device__ __forceinline__ int tiled_pair(int x, int y, int zb, int nx4)
 {
     return zb + (((y >> 2) * nx4 + (x >> 2)) << 4) + ((y & 3) << 2) + (x & 3);
@@ -157,7 +158,7 @@ __device__ __forceinline__ void walk_quad(const TX* __restrict__ x, float inv_x,
     const int jz = min(start_slab(a_in, inv_z, off_z, nz), nz / 2 - 1);
     const int nxy = nx * ny, nx4 = nx >> 2;
     int cx = jx, cy = jy, zb = jz * nxy;           // < 2^31 (checked at plan creation)
-    int v = tiled_pair(cx, cy, zb, nx4), vr = tiled_pair(nx - 1 - cx, ny - 1 - cy, zb, nx4);
+    int v = tiled_pair(cx, cy, zb, nx4), vr = 2 * zb + nxy - 1 - v;
     const bool px = inv_x > 0.0f, py = inv_y > 0.0f;
     float pax = (float)(px ? jx + 1 : jx);
     float pay = (float)(py ? jy + 1 : jy);
@@ -185,7 +186,7 @@ __device__ __forceinline__ void walk_quad(const TX* __restrict__ x, float inv_x,
                 if (nAy == nxt) { pay += sty; cy += dy; nAy = fmaf(pay, inv_y, off_y); }
                 if (nAz == nxt) { paz -= 1.0f; zb -= nxy; nAz = fmaf(paz, inv_z, off_z); }
                 v = tiled_pair(cx, cy, zb, nx4);
-                vr = tiled_pair(nx - 1 - cx, ny - 1 - cy, zb, nx4);
+                vr = 2 * zb + nxy - 1 - v;
                 if (FL_IN(2 * (long long)v + 1, xlen)) xn2 = Store<TX>::ld2(x + 2 * (long long)v);
                 if (FL_IN(2 * (long long)vr + 1, xlen)) xnr2 = Store<TX>::ld2(x + 2 * (long long)vr);
             }
@@ -230,11 +231,11 @@ __device__ __forceinline__ void walk_oct(const TX* __restrict__ x, float inv_x, 
     const int nn = n * n, n4 = n >> 2;
     int cx = jx, cy = jy, zb = jz * nn;            // voxel of turn 0; z base of all turns
     int q[4];                                      // folded pair index of each turn
-    auto turns = [&]() {
+    auto turns = [&]() {                           // turns 2, 3 are turns 0, 1 by pi
         q[0] = tiled_pair(cx, cy, zb, n4);
         q[1] = tiled_pair(n - 1 - cy, cx, zb, n4);
-        q[2] = tiled_pair(n - 1 - cx, n - 1 - cy, zb, n4);
-        q[3] = tiled_pair(cy, n - 1 - cx, zb, n4);
+        q[2] = 2 * zb + nn - 1 - q[0];
+        q[3] = 2 * zb + nn - 1 - q[1];
     };
     turns();
     const bool px = inv_x > 0.0f, py = inv_y > 0.0f;
