@@ -81,9 +81,9 @@ struct fl_plan {
 // voxel (ix, iy, nz-1-iz)) for iz < nz/2 at pair index (iz*ny + iy)*nx + ix;
 // the adjoint input (pre-weighted sinogram) is always folded the same way:
 // pairs (row ib, row nb-1-ib) for ib < nb/2 at pair index (iv*nb/2 + ib)*na + ia,
-// except on a quarter-turn plan (rot4), where the 8 values of views
-// iv + j nv/4 (j = 0..3), rows ib and nb-1-ib, lie side by side at 8 *
-// ((iv*nb/2 + ib)*na + ia) + 2 j for iv < nv/4.
+// except on a half- (G = 2) or quarter-turn (G = 4) plan, where the 2 G values
+// of views iv + j nv/G (j < G), rows ib and nb-1-ib, lie side by side at
+// 2 G ((iv*nb/2 + ib)*na + ia) + 2 j for iv < nv/G.
 // A half- or quarter-turn plan's folded volume is tiled in xy: the pair of
 // voxel (x, y, z < nz/2) is at z*nx*ny + 16*((y/4)*(nx/4) + x/4) + 4*(y%4) +
 // x%4, so one 128-byte line holds a 4 x 4 patch of pairs (the gathers of a

@@ -75,7 +75,10 @@ k_fwd_cone(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restr
 // Half-turn form (fl_plan::rot, on a z-mirror plan): the block walks rows
 // ib < nb/2 of views iv < nv/2 only; each walk also yields the rays of view
 // iv + nv/2 at the same column and rows (the turned ray, over the turned
-// voxels), all four with the walked ray's c_r.
+// voxels), all four with the walked ray's c_r. yfold writes the
+// backprojection's input layout for these plans: per (iv < nv/2, ib < nb/2,
+// ia) the 4 values (views iv, iv + nv/2; rows ib, nb-1-ib) side by side
+// (k_weight_packed<TY, 2>).
 template <typename TX, typename TY>
 __global__ void __launch_bounds__(128, 12)
 k_fwd_quad(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restrict__ col,
@@ -102,9 +105,10 @@ k_fwd_quad(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restr
     float o[4] = {cr * a.x, cr * a.y, cr * r.x, cr * r.y};
     if (cr_power == 2)
         for (int k = 0; k < 4; k++) o[k] = cr * o[k];
-    if (yfold) {
-        Store<TY>::st2(y + 2 * (((long long)iv * nbh + ib) * na + ia), o[0], o[1]);
-        Store<TY>::st2(y + 2 * (((long long)(iv + hv) * nbh + ib) * na + ia), o[2], o[3]);
+    if (yfold) {                        // the 4 values of the pair of views side by side
+        const long long u = 4 * (((long long)iv * nbh + ib) * na + ia);
+        Store<TY>::st2(y + u, o[0], o[1]);
+        Store<TY>::st2(y + u + 2, o[2], o[3]);
     } else {
         Store<TY>::st(y + ((long long)iv * nb + ib) * na + ia, o[0]);
         Store<TY>::st(y + ((long long)iv * nb + (nb - 1 - ib)) * na + ia, o[1]);
@@ -117,7 +121,8 @@ k_fwd_quad(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restr
 // iv < nv/4; each walk yields the rays of views iv + j nv/4 (j = 0..3) at the
 // same column and rows, all eight with the walked ray's c_r. yfold writes the
 // backprojection's input layout for these plans: per (iv < nv/4, ib < nb/2,
-// ia) the 8 values (view iv + j nv/4, rows ib / nb-1-ib) side by side.
+// ia) the 8 values (view iv + j nv/4, rows ib / nb-1-ib) side by side
+// (k_weight_packed<TY, 4>).
 template <typename TX, typename TY>
 __global__ void __launch_bounds__(128, 8)
 k_fwd_oct(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restrict__ col,
@@ -203,9 +208,8 @@ k_count(int32_t* __restrict__ cnt, const ColEntry* __restrict__ col,
 // Folded yw for a z-mirror plan: the pair (c_r y[ib], c_r y[nb-1-ib]) of rows
 // ib < nb/2, both with the walked row's c_r (equal to the mirror's: its d_z is
 // the exact negation).
-// pv: the views repeat with period pv (nv, or nv/2 for a half-turn plan, nv/4
-// for a quarter-turn plan): view iv takes c_r of view iv % pv, the ray it is
-// defined by.
+// pv: view iv takes c_r of view iv % pv, the ray it is defined by (pv = nv:
+// turn plans pack their input with k_weight_packed instead).
 template <typename TY>
 __global__ void k_weight_fold(float* __restrict__ yw, const TY* __restrict__ y,
                               const float* __restrict__ colr, const RowEntry* __restrict__ row,
@@ -225,28 +229,29 @@ __global__ void k_weight_fold(float* __restrict__ yw, const TY* __restrict__ y,
     Store<float>::st2(yw + 2 * r, cr * a, cr * b);
 }
 
-// Packed yw of a quarter-turn plan: for r = (iv < nv/4, ib < nb/2, ia) the 8
-// values c_r y of views iv + j nv/4 (j = 0..3), rows ib and nb-1-ib, with c_r
-// of view iv (the ray they are all defined by).
-template <typename TY>
-__global__ void k_weight_oct(float* __restrict__ yw, const TY* __restrict__ y,
-                             const float* __restrict__ colr, const RowEntry* __restrict__ row,
-                             int na, int nb, int nv, long long npack, float scale)
+// Packed yw of a half- (G = 2) or quarter-turn (G = 4) plan: for
+// r = (iv < nv/G, ib < nb/2, ia) the 2 G values c_r y of views iv + j nv/G
+// (j < G), rows ib and nb-1-ib, with c_r of view iv (the ray they are all
+// defined by).
+template <typename TY, int G>
+__global__ void k_weight_packed(float* __restrict__ yw, const TY* __restrict__ y,
+                                const float* __restrict__ colr, const RowEntry* __restrict__ row,
+                                int na, int nb, int nv, long long npack, float scale)
 {
     long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= npack) return;
-    const int nbh = nb / 2, qv = nv / 4;
+    const int nbh = nb / 2, pv = nv / G;
     const int ia = (int)(r % na);
     const long long q = r / na;
     const int ib = (int)(q % nbh);
     const int iv = (int)(q / nbh);
     const float cr = ray_cr(scale, colr[(long long)iv * na + ia], row[(long long)iv * nb + ib].dz2);
 #pragma unroll
-    for (int j = 0; j < 4; j++) {
-        const long long vj = iv + (long long)j * qv;
+    for (int j = 0; j < G; j++) {
+        const long long vj = iv + (long long)j * pv;
         const float a = Store<TY>::ld_plain(y + (vj * nb + ib) * na + ia);
         const float b = Store<TY>::ld_plain(y + (vj * nb + (nb - 1 - ib)) * na + ia);
-        Store<float>::st2(yw + 8 * r + 2 * j, cr * a, cr * b);
+        Store<float>::st2(yw + 2 * G * r + 2 * j, cr * a, cr * b);
     }
 }
 
@@ -456,14 +461,14 @@ __device__ __forceinline__ void adj_rows_pair(float2 (&acc)[TZ], int nk, int z0,
     }
 }
 
-// Half-turn form of adj_rows_pair: every weight also multiplies the folded
-// row pair of view v + nv/2 (ycolr) into the turned voxels' sums accr.
+// Half-turn form of adj_rows_pair: every weight also multiplies the row pair
+// of view v + nv/2 into the turned voxels' sums accr; y4 holds both row pairs
+// side by side (4 floats per row and column, 16-byte aligned).
 template <int MODE, int TZ>
 __device__ __forceinline__ void adj_rows_quad(float2 (&acc)[TZ], float2 (&accr)[TZ], int nk,
                                               int z0, float l, float h, float e1, float e2,
                                               float s1, float s2, const float2* __restrict__ rv,
-                                              const float* __restrict__ ycol,
-                                              const float* __restrict__ ycolr, int na, int nb)
+                                              const float* __restrict__ y4, int na, int nb)
 {
     float mn = fminf(e1, e2), mx = fmaxf(e1, e2);
     float lo_e = e1 - 0.02f, hi_e = e2 + s2 + 0.02f;
@@ -486,8 +491,8 @@ __device__ __forceinline__ void adj_rows_quad(float2 (&acc)[TZ], float2 (&accr)[
         for (int ib = blo; ib <= bhi; ib++) {
             if (!FL_IN(ib, nb)) continue;
             const float2 re = rv[ib];
-            const float2 t = Store<float>::ld2(ycol + 2 * (long long)ib * na);
-            const float2 tr = Store<float>::ld2(ycolr + 2 * (long long)ib * na);
+            const float4 u = __ldg(reinterpret_cast<const float4*>(y4 + 4 * (long long)ib * na));
+            const float2 t = make_float2(u.x, u.y), tr = make_float2(u.z, u.w);
             const float2 az = __ffma2_rn(make_float2(fk0, fk1), make_float2(re.x, re.x),
                                          make_float2(re.y, re.y));
             float l2, h2;
@@ -506,8 +511,9 @@ __device__ __forceinline__ void adj_rows_quad(float2 (&acc)[TZ], float2 (&accr)[
 // thread visits the views iv < nv/2 only. In view iv it evaluates the weights
 // of both columns: a weight of V multiplies the row pair of view iv into V
 // and the row pair of view iv + nv/2 into T (A[(iv + nv/2, r), T] =
-// A[(iv, r), V]); a weight of T, the other way round. yw is the folded
-// sinogram of all views; X the tiled folded volume (xfold) or the standard one.
+// A[(iv, r), V]); a weight of T, the other way round. yw is the packed
+// sinogram of k_weight_packed / k_fwd_quad (4 values per (iv < nv/2,
+// ib < nb/2, ia)); X the tiled folded volume (xfold) or the standard one.
 template <typename TX, int TZ>
 __global__ void __launch_bounds__(128, 8)
 k_adj_quad(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __restrict__ col,
@@ -527,13 +533,12 @@ k_adj_quad(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __r
 #pragma unroll
     for (int k = 0; k < TZ; k++) { accV[k] = make_float2(0.0f, 0.0f); accT[k] = accV[k]; }
     const float inv_dv = 1.0f / G.dv;
-    const long long vstride = (long long)nbw * na * 2;        // folded floats per view
+    const long long vstride = (long long)nbw * na * 4;        // packed floats per view pair
     for (int iv = 0; iv < hv; iv++) {
         const ViewEntry ve = view[iv];
         const ColEntry* cv = col + (long long)iv * na;
         const float2* rv = rowz + (long long)iv * nb;
         const float* yv = yw + (long long)iv * vstride;
-        const float* yvr = yw + (long long)(iv + hv) * vstride;
         const float zr0 = (float)(z0 - nz / 2) * dz - ve.sz;
         const float zr1 = (float)(z0 + nk - nz / 2) * dz - ve.sz;
         const float tol = 1e-3f * dz;
@@ -559,10 +564,10 @@ k_adj_quad(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __r
                 const float e1 = (zr0 * r1 - G.v0) * inv_dv, e2 = (zr0 * r2 - G.v0) * inv_dv;
                 if (mode < 0)
                     adj_rows_quad<-1, TZ>(own, other, nk, z0, l, h, e1, e2, s1, s2, rv,
-                                          yv + 2 * ia, yvr + 2 * ia, na, nbw);
+                                          yv + 4 * ia, na, nbw);
                 else
                     adj_rows_quad<0, TZ>(own, other, nk, z0, l, h, e1, e2, s1, s2, rv,
-                                         yv + 2 * ia, yvr + 2 * ia, na, nbw);
+                                         yv + 4 * ia, na, nbw);
             }
         };
         column(ix, iy, accV, accT);
@@ -643,7 +648,7 @@ __device__ __forceinline__ void adj_rows_oct(float2 (&a0)[TZ], float2 (&a1)[TZ],
 // mirrors; one frame. It visits the views iv < nv/4. In view iv a weight of
 // column V_k multiplies the row pairs of view iv + j nv/4 into V_{k+j mod 4}
 // (A[(iv + j nv/4, r), R^j V] = A[(iv, r), V]). yw is the packed sinogram of
-// k_weight_oct / k_fwd_oct (8 values per (iv < nv/4, ib < nb/2, ia)); X the
+// k_weight_packed / k_fwd_oct (8 values per (iv < nv/4, ib < nb/2, ia)); X the
 // tiled folded volume (xfold) or the standard one.
 template <typename TX, int TZ>
 __global__ void __launch_bounds__(128, TZ == 2 ? 8 : 6)
@@ -945,6 +950,24 @@ void launch_fold(fl_plan* p, const void* src, void* dst, int unfold, cudaStream_
 
 size_t dtype_bytes(int t) { return t == FL_F32 ? 4 : 2; }
 
+template <int G>
+void launch_weight_packed(fl_plan* p, const void* y, int yt, float* yw, cudaStream_t st)
+{
+    const fl_scan& s = p->s;
+    const long long npk = (long long)(s.nv / G) * (s.nb / 2) * s.na;
+    const unsigned g = fl_div_up(npk, 256);
+    if (yt == FL_F32)
+        k_weight_packed<float, G><<<g, 256, 0, st>>>(yw, (const float*)y, p->d_colr, p->d_row,
+                                                     s.na, s.nb, s.nv, npk, s.scale);
+    else if (yt == FL_F16)
+        k_weight_packed<__half, G><<<g, 256, 0, st>>>(yw, (const __half*)y, p->d_colr, p->d_row,
+                                                      s.na, s.nb, s.nv, npk, s.scale);
+    else
+        k_weight_packed<__nv_bfloat16, G><<<g, 256, 0, st>>>(yw, (const __nv_bfloat16*)y,
+                                                             p->d_colr, p->d_row, s.na, s.nb,
+                                                             s.nv, npk, s.scale);
+}
+
 }  // namespace
 
 int fl_matched_fold(fl_plan* p, const void* src, void* dst, int dtype, int unfold,
@@ -982,25 +1005,15 @@ int fl_matched_weight(fl_plan* p, const void* y, int yt, float* yw, cudaStream_t
     const fl_scan& s = p->s;
     long long nr = p->n_rays;
     int three = s.ndim == 3;
-    if (three && p->zmirror && p->rot && p->rot4) {
-        long long npk = (long long)(s.nv / 4) * (s.nb / 2) * s.na;
-        unsigned g = fl_div_up(npk, 256);
-        if (yt == FL_F32)
-            k_weight_oct<float><<<g, 256, 0, st>>>(yw, (const float*)y, p->d_colr, p->d_row, s.na,
-                                                   s.nb, s.nv, npk, s.scale);
-        else if (yt == FL_F16)
-            k_weight_oct<__half><<<g, 256, 0, st>>>(yw, (const __half*)y, p->d_colr, p->d_row,
-                                                    s.na, s.nb, s.nv, npk, s.scale);
-        else
-            k_weight_oct<__nv_bfloat16><<<g, 256, 0, st>>>(yw, (const __nv_bfloat16*)y, p->d_colr,
-                                                           p->d_row, s.na, s.nb, s.nv, npk,
-                                                           s.scale);
+    if (three && p->zmirror && p->rot) {
+        if (p->rot4) launch_weight_packed<4>(p, y, yt, yw, st);
+        else launch_weight_packed<2>(p, y, yt, yw, st);
         return fl_check_launch("matched adjoint weighting");
     }
     if (three && p->zmirror) {
         long long np = (long long)s.nv * (s.nb / 2) * s.na;
         unsigned g = fl_div_up(np, 256);
-        const int hv = !p->rot ? s.nv : (p->rot4 ? s.nv / 4 : s.nv / 2);   // view period
+        const int hv = s.nv;            // view period: every view has its own rays here
         if (yt == FL_F32)
             k_weight_fold<float><<<g, 256, 0, st>>>(yw, (const float*)y, p->d_colr, p->d_row,
                                                     s.na, s.nb, np, s.scale, hv);
