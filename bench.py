@@ -624,7 +624,7 @@ def run_sb(ctx, name, w, p):
     torch = ctx.torch
     from framelab_gb300 import phantoms as PH
     from framelab_gb300.projector import Plan
-    from framelab_gb300.transforms import split_bregman
+    from framelab_gb300.transforms import SplitBregmanSolver
     K, W, world = ctx.K, ctx.W, ctx.world
     P = Plan(p)
     x = torch.from_numpy(PH.ellipsoids_3d(w["n"], seed=5).reshape(-1)).to(ctx.dev)
@@ -636,14 +636,17 @@ def run_sb(ctx, name, w, p):
     f = -torch.log(counts.clamp(min=1.0) / w["I0"])
     del proj, counts
     u0 = torch.zeros(P.n_vox, device=ctx.dev)
-    kw = dict(lam=w["lam"], mu=w["mu"], cg_iters=w["inner"], levels=w["levels"], kind="linear",
-              mode="graph")
+    kw = dict(lam=w["lam"], mu=w["mu"], cg_iters=w["inner"])
+    # the workspace (framelet, CGLS, coefficient sets) is allocated once, as
+    # for the CGLS workloads; each step is one outer iteration of solve()
+    sbs = SplitBregmanSolver(P, levels=w["levels"], kind="linear", mode="graph")
     detail = {}
     if W:
-        split_bregman(P, f, u0, outer=W, **kw)
+        sbs.solve(f, u0, outer=W, **kw)
     clocks = ClockSampler(ctx.local)
     with clocks:
-        (u, hist), t_s = ctx.timed(lambda: split_bregman(P, f, u0, outer=K, **kw))
+        u, t_s = ctx.timed(lambda: sbs.solve(f, u0, outer=K, **kw))
+    hist = sbs.history
     detail["vs_truth_rel_l2"] = ctx.rel(u, x_phys)
     detail["last_relative_update"] = float(hist[-1]) if len(hist) else None
     e2e = None
@@ -654,11 +657,11 @@ def run_sb(ctx, name, w, p):
 
         def host_solve():
             fd = fh.to(ctx.dev, non_blocking=True).view_as(f)
-            uh.copy_(split_bregman(P, fd, u0, outer=K, **kw)[0], non_blocking=True)
+            uh.copy_(sbs.solve(fd, u0, outer=K, **kw), non_blocking=True)
         _, t_e = ctx.timed(host_solve)
         e2e = {"value": world * K / t_e, "unit": "iter/s",
                "h2d_bytes_per_step": f.numel() * 4 / K, "d2h_bytes_per_step": P.n_vox * 4 / K,
-               "call": f"split_bregman (fl_sb_solve), {K} outer iterations per call: "
+               "call": f"SplitBregmanSolver.solve (fl_sb_run), {K} outer iterations per call: "
                        "sinogram in (pinned host), volume out"}
     roofline = None
     if "kernels" in ctx.legs:

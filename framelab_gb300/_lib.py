@@ -95,6 +95,9 @@ _SIGS = {
     "fl_framelet_shrink": (_I, [_P, _V, _V, _F, _V]),
     "fl_framelet_option": (_I, [_P, _I, _I]),
     "fl_sb_solve": (_I, [_P, _V, _V, _F, _F, _I, _I, _D, _I, _I, _I, _V, _V]),
+    "fl_sb_create": (_I, [_P, _I, _I, _I, C.POINTER(_P)]),
+    "fl_sb_run": (_I, [_P, _V, _V, _F, _F, _I, _I, _D, _V, _V]),
+    "fl_sb_destroy": (None, [_P]),
     # batched fan slices
     "fl_batch_create": (_I, [C.POINTER(_P), C.c_int32, C.POINTER(_P)]),
     "fl_batch_destroy": (None, [_P]),

@@ -75,6 +75,36 @@ class FrameletSystem:
         return b
 
 
+class SplitBregmanSolver:
+    """Device split Bregman on one plan with a persistent workspace
+    (fl_sb_create / fl_sb_run): the framelet, CGLS workspace and coefficient
+    sets are allocated once and reused by every solve."""
+
+    def __init__(self, plan, levels: int = 2, kind: str = "linear", mode: str = "mixed"):
+        from .solvers import MODES
+        L = _lib.load()
+        h = C.c_void_p()
+        _lib.check(L.fl_sb_create(plan.handle, int(levels), KINDS[kind], MODES[mode], C.byref(h)))
+        self.plan, self._h, self._L = plan, h, L
+        self.history = None
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            self._L.fl_sb_destroy(h)
+            self._h = None
+
+    def solve(self, f: torch.Tensor, u0: torch.Tensor, lam: float, mu: float, outer: int = 30,
+              cg_iters: int = 5, cg_tol: float = 1e-10) -> torch.Tensor:
+        u = u0.clone()
+        hist = np.zeros(max(outer, 1), np.float64)
+        _lib.check(self._L.fl_sb_run(self._h, f.data_ptr(), u.data_ptr(), float(lam), float(mu),
+                                     int(outer), int(cg_iters), float(cg_tol), hist.ctypes.data,
+                                     _stream()))
+        self.history = hist[:outer]
+        return u
+
+
 def split_bregman(plan, f: torch.Tensor, u0: torch.Tensor, lam: float, mu: float,
                   outer: int = 30, cg_iters: int = 5, cg_tol: float = 1e-10, levels: int = 2,
                   kind: str = "linear", mode: str = "mixed"):

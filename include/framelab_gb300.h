@@ -315,6 +315,15 @@ int fl_sb_solve(fl_plan *plan, const float *f, float *u, float lam, float mu, in
                 int cg_iters, double cg_tol, int levels, int kind, int mode, double *history,
                 void *stream);
 
+/* Persistent form of fl_sb_solve: the framelet, the CGLS workspace and the
+ * coefficient sets of one plan (about 2 * 53 volumes for a 2-level linear
+ * framelet) are allocated once and reused by every fl_sb_run. */
+typedef struct fl_sb fl_sb;
+int fl_sb_create(fl_plan *plan, int levels, int kind, int mode, fl_sb **sb);
+int fl_sb_run(fl_sb *sb, const float *f, float *u, float lam, float mu, int outer,
+              int cg_iters, double cg_tol, double *history, void *stream);
+void fl_sb_destroy(fl_sb *sb);
+
 /* The same solve with host buffers (the mex-style boundary): b and u0 are
  * copied to the device (u0 skipped with FL_CGLS_ZERO_START), the result is
  * copied back into u. Device copies are kept in the workspace for reuse. */

@@ -171,3 +171,25 @@ def test_fused_reconstructs_large_volume():
     assert float((rec - u).norm() / u.norm()) < 1e-6               # W^T W = I
     fs.fused = False
     assert torch.equal(fs.forward(u), c)
+
+
+def test_persistent_split_bregman_matches_one_shot():
+    import torch
+    from framelab_gb300 import geometry as G, phantoms as PH
+    from framelab_gb300.projector import Plan
+    from framelab_gb300.transforms import SplitBregmanSolver, split_bregman
+    n = 24
+    p = G.cone_para_mm(n, 16, 36, 30, det_pitch_mm=12.0, SO_mm=600.0, SD_mm=1200.0,
+                       voxel_mm=12.0)
+    P = Plan(p)
+    x = torch.from_numpy(PH.ellipsoids_3d(n, seed=4).reshape(-1)).cuda()
+    f = P.forward(x)
+    u0 = torch.zeros(P.n_vox, device="cuda")
+    kw = dict(lam=0.02, mu=1.0, outer=3, cg_iters=3)
+    one, hist = split_bregman(P, f, u0, levels=2, mode="graph", **kw)
+    S = SplitBregmanSolver(P, levels=2, kind="linear", mode="graph")
+    a = S.solve(f, u0, **kw)
+    b = S.solve(f, u0, **kw)                   # the workspace is reused
+    torch.cuda.synchronize()
+    assert torch.equal(a, one) and torch.equal(b, one)
+    assert np.array_equal(S.history, hist)
