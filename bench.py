@@ -548,7 +548,8 @@ def run_single(ctx, name, w, p):
         detail["gradcheck_s"] = time.perf_counter() - t0
         del f
     return dict(value=job_rate(world, K, t_g), t_step=t_g / K, e2e=e2e, roofline=roofline,
-                launches=5 * K + 1, detail=detail, clocks=clocks.summary(), unit="iter/s")
+                launches=5 * K + 1 + (2 if P.z_mirror else 0), detail=detail,
+                clocks=clocks.summary(), unit="iter/s")
 
 
 def run_batch(ctx, name, w, paras):
@@ -694,10 +695,11 @@ def run_sb(ctx, name, w, p):
         detail.update(framelet_step_ms=tfw * 1e3, framelet_compulsory_GBps=fb / tfw / 1e9,
                       framelet_separable_step_ms=tsep * 1e3, framelet_ncoef=fw.ncoef)
         del v, t, bb, fw
-    # setup: A^T f (weighting + gather) and W u0 (3 per level); per outer iteration:
-    # warm-start residual (fwd, adj, axpy) + init, inner x (fwd, adj, 3 updates),
-    # Bregman analysis + synthesis (3 + 3 per level), |u_k - u_{k-1}| (diff, 2 dots)
-    launches = 2 + 3 * w["levels"] + K * (4 + 5 * w["inner"] + 6 * w["levels"] + 3)
+    # setup: A^T f (packing + gather) and W u0 (1 per level); per outer iteration:
+    # fold b and u, warm-start residual (fwd, adj) + init, inner x (fwd, adj,
+    # 3 updates), unfold u; Bregman analysis + synthesis (1 + 2 per level);
+    # |u_k - u_{k-1}| (diff, 2 dots)
+    launches = 2 + w["levels"] + K * (6 + 5 * w["inner"] + 3 * w["levels"] + 3)
     return dict(value=job_rate(world, K, t_s), t_step=t_s / K, e2e=e2e, roofline=roofline,
                 launches=launches, detail=detail, clocks=clocks.summary(), unit="iter/s")
 
