@@ -548,7 +548,7 @@ def run_single(ctx, name, w, p):
         detail["gradcheck_s"] = time.perf_counter() - t0
         del f
     return dict(value=job_rate(world, K, t_g), t_step=t_g / K, e2e=e2e, roofline=roofline,
-                launches=5 * K + 1 + (2 if P.z_mirror else 0), detail=detail,
+                launches=5 * K + 1 + (2 if P.z_mirror else 0), detail=detail,   # ncu-checked
                 clocks=clocks.summary(), unit="iter/s")
 
 
@@ -696,10 +696,11 @@ def run_sb(ctx, name, w, p):
                       framelet_separable_step_ms=tsep * 1e3, framelet_ncoef=fw.ncoef)
         del v, t, bb, fw
     # setup: A^T f (packing + gather) and W u0 (1 per level); per outer iteration:
-    # fold b and u, warm-start residual (fwd, adj) + init, inner x (fwd, adj,
-    # 3 updates), unfold u; Bregman analysis + synthesis (1 + 2 per level);
-    # |u_k - u_{k-1}| (diff, 2 dots)
-    launches = 2 + w["levels"] + K * (6 + 5 * w["inner"] + 3 * w["levels"] + 3)
+    # fold b and u, warm-start residual (fwd, adj, + mu u) + init, inner x (fwd,
+    # adj, 3 updates), unfold u; Bregman analysis + synthesis (1 + 2 per level);
+    # |u_k - u_{k-1}| (diff, 2 dots). Checked against an ncu launch list of one
+    # call (sb128, 4 outer iterations: 168 launches).
+    launches = 2 + w["levels"] + K * (7 + 5 * w["inner"] + 3 * w["levels"] + 3)
     return dict(value=job_rate(world, K, t_s), t_step=t_s / K, e2e=e2e, roofline=roofline,
                 launches=launches, detail=detail, clocks=clocks.summary(), unit="iter/s")
 
