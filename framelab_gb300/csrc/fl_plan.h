@@ -68,6 +68,11 @@ struct fl_plan {
     // serves eight rays (views v + j nv/4, rows b and nb-1-b).
     int rot4_ok;
     int rot4;                  // in use (FL_OPT_QUARTER_TURN; only with rot and zmirror)
+    // fan plans take both turns without a mirror: the half turn with ny even,
+    // the quarter turn with nx == ny even (A[(v + j nv/G, a), R^j (x, y)] =
+    // A[(v, a), (x, y)], one walk / one weight serving G rays).
+    // Every turn form needs one frame whose view list is 0, 1, ..., nv-1.
+    int views_natural;
     // reusable scratch: sinogram-sized f32 for the pre-weighted adjoint input,
     // volume-sized for the z-folded copy of a forward input
     float *d_work;
@@ -76,6 +81,15 @@ struct fl_plan {
     size_t vwork_bytes;
 };
 
+// Rays served by one walk or weight of the matched kernels in use, over the
+// views: 4 (quarter turn), 2 (half turn) or 1. A cone plan's turn forms also
+// need the z mirror.
+inline int fl_plan_turns(const fl_plan* p)
+{
+    if (!p->rot || (p->s.ndim == 3 && !p->zmirror)) return 1;
+    return p->rot4 ? 4 : 2;
+}
+
 // Layouts of the matched launchers' operands. For a z-mirror plan the
 // z-folded volume stores, per frame, the pairs (voxel (ix, iy, iz),
 // voxel (ix, iy, nz-1-iz)) for iz < nz/2 at pair index (iz*ny + iy)*nx + ix;
@@ -83,7 +97,9 @@ struct fl_plan {
 // pairs (row ib, row nb-1-ib) for ib < nb/2 at pair index (iv*nb/2 + ib)*na + ia,
 // except on a half- (G = 2) or quarter-turn (G = 4) plan, where the 2 G values
 // of views iv + j nv/G (j < G), rows ib and nb-1-ib, lie side by side at
-// 2 G ((iv*nb/2 + ib)*na + ia) + 2 j for iv < nv/G.
+// 2 G ((iv*nb/2 + ib)*na + ia) + 2 j for iv < nv/G. A fan plan with turns
+// (G = 2 or 4) packs the G values of views iv + j nv/G side by side at
+// G (iv*na + ia) + j.
 // A half- or quarter-turn plan's folded volume is tiled in xy: the pair of
 // voxel (x, y, z < nz/2) is at z*nx*ny + 16*((y/4)*(nx/4) + x/4) + 4*(y%4) +
 // x%4, so one 128-byte line holds a 4 x 4 patch of pairs (the gathers of a

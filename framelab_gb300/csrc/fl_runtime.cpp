@@ -210,8 +210,11 @@ static int build_tables(fl_plan* p, const std::vector<float>& phi, const float* 
     // within 1e-6 in cos and sin (FP32 angles such as 2 pi k / nv are never
     // exactly opposite), one frame, nx and ny multiples of 4 (the folded volume
     // is tiled in 4 x 4 columns)
+    // fan plans: no mirror, ny even (the rows y < ny/2 are the primary half)
     p->rot_ok = 0;
-    if (p->zmirror_ok && s.nt == 1 && s.nv % 2 == 0 && s.nx % 4 == 0 && s.ny % 4 == 0) {
+    const bool cone_turn = s.ndim == 3 && p->zmirror_ok && s.nx % 4 == 0 && s.ny % 4 == 0;
+    const bool fan_turn = s.ndim == 2 && s.ny % 2 == 0;
+    if ((cone_turn || fan_turn) && s.nt == 1 && p->views_natural && s.nv % 2 == 0) {
         bool ok = true;
         const int h = s.nv / 2;
         for (int iv = 0; iv < h && ok; iv++) {
@@ -225,7 +228,7 @@ static int build_tables(fl_plan* p, const std::vector<float>& phi, const float* 
     // quarter turn (fl_plan.h): view v + nv/4 is view v turned by pi/2 to
     // within 1e-6 (cos -> -sin, sin -> cos), square xy grid
     p->rot4_ok = 0;
-    if (p->rot_ok && s.nv % 4 == 0 && s.nx == s.ny && s.nx % 4 == 0) {
+    if (p->rot_ok && s.nv % 4 == 0 && s.nx == s.ny && s.nx % (s.ndim == 3 ? 4 : 2) == 0) {
         bool ok = true;
         const int q = s.nv / 4;
         for (int iv = 0; iv < q && ok; iv++) {
@@ -265,11 +268,11 @@ extern "C" int fl_plan_query(const fl_plan* p, int option, int* value)
         return fl_set_error(FL_OK, "");
     }
     if (option == FL_OPT_ROT_MIRROR) {
-        *value = (p->rot && p->zmirror) ? 1 : 0;
+        *value = fl_plan_turns(p) >= 2 ? 1 : 0;
         return fl_set_error(FL_OK, "");
     }
     if (option == FL_OPT_QUARTER_TURN) {
-        *value = (p->rot4 && p->rot && p->zmirror) ? 1 : 0;
+        *value = fl_plan_turns(p) == 4 ? 1 : 0;
         return fl_set_error(FL_OK, "");
     }
     return fl_set_error(FL_ERR_INVALID, "fl_plan_query: unknown option %d", option);
@@ -392,6 +395,9 @@ extern "C" int fl_plan_create(const fl_scan* scan, fl_plan** out)
     }
     if (tmp < 1) tmp = 1, idY.resize((size_t)nt, 0);
     p->tmp_size = tmp;
+    p->views_natural = nt == 1 && Nvv[0] == nv;
+    for (int j = 0; j < Nvv[0] && p->views_natural; j++)
+        if (idY[j] != j) p->views_natural = 0;
 
     int st = FL_OK;
     if (!st) st = upload(&p->d_sd_phi, phi.data(), nv);

@@ -171,13 +171,77 @@ k_fwd_fan(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restri
     int iv = (int)(r / na);
     ColEntry ce = col[r];
     const TX* x = X + (long long)vframe[iv] * nper;
-    float acc = walk<TX, false, false>(x, ce.inv_x, ce.off_x, ce.inv_y, ce.off_y, 0.0f, 0.0f,
-                                       nx, ny, 1, nullptr, nullptr, nper);
+    float a1[1];
+    walk_fan<TX, 1>(x, ce.inv_x, ce.off_x, ce.inv_y, ce.off_y, nx, ny, a1, nper);
+    float acc = a1[0];
     float cr = ray_cr(scale, colr[r], 0.0f);
     if (xscale) acc *= *xscale;
     float out = cr * acc;
     if (cr_power == 2) out = cr * out;
     Store<TY>::st(y + r, out);
+}
+
+// Fan forward of a turn plan (G = 2 or 4, one frame): kFanLanes threads per
+// ray (iv < nv/G, ia), each walking one part of it (walk_fan), their sums
+// added in lane order; the walk also yields the rays of views iv + j nv/G at
+// the same column, all with the walked ray's c_r. ypack writes the
+// adjoint-input layout of these plans: the G values of ray (iv, ia)'s orbit
+// side by side at G (iv na + ia) + j (k_weight_fan_packed). Fan launches
+// have few rays: the parts give the GPU kFanLanes times the threads, each
+// with that fraction of the walk.
+constexpr int kFanLanes = 8;
+
+template <typename TX, typename TY, int G>
+__global__ void __launch_bounds__(128, 8)
+k_fwd_fan_turn(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restrict__ col,
+               const float* __restrict__ colr, int nx, int ny, int na, int nv, float scale,
+               int cr_power, const int* __restrict__ skip, const float* __restrict__ xscale,
+               int ypack)
+{
+    if (skip && *skip) return;                 // uniform (one flag for the launch)
+    const int gv = nv / G;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long r = t / kFanLanes;
+    const int lane = (int)(t % kFanLanes);
+    const bool ray = r < (long long)na * gv;
+    float acc[G];
+#pragma unroll
+    for (int j = 0; j < G; j++) acc[j] = 0.0f;
+    if (ray) {
+        const ColEntry ce = col[r];
+        walk_fan<TX, G, kFanLanes>(X, ce.inv_x, ce.off_x, ce.inv_y, ce.off_y, nx, ny, acc,
+                                   (long long)nx * ny, lane);
+    }
+    // the parts of a ray are consecutive lanes of one warp: lane 0 adds them
+    const int base = (threadIdx.x & 31) & ~(kFanLanes - 1);
+#pragma unroll
+    for (int j = 0; j < G; j++) {
+        float part[kFanLanes];
+#pragma unroll
+        for (int k = 0; k < kFanLanes; k++) part[k] = __shfl_sync(0xffffffffu, acc[j], base + k);
+        float sum = part[0];
+#pragma unroll
+        for (int k = 1; k < kFanLanes; k++) sum += part[k];
+        acc[j] = sum;
+    }
+    if (!ray || lane != 0) return;
+    const int iv = (int)(r / na), ia = (int)(r - (long long)iv * na);
+    const float cr = ray_cr(scale, colr[r], 0.0f);
+    float o[G];
+#pragma unroll
+    for (int j = 0; j < G; j++) {
+        float a = acc[j];
+        if (xscale) a *= *xscale;
+        o[j] = cr * a;
+        if (cr_power == 2) o[j] = cr * o[j];
+    }
+    if (ypack) {
+#pragma unroll
+        for (int j = 0; j < G; j += 2) Store<TY>::st2(y + G * r + j, o[j], o[j + 1]);
+    } else {
+#pragma unroll
+        for (int j = 0; j < G; j++) Store<TY>::st(y + ((long long)iv + (long long)j * gv) * na + ia, o[j]);
+    }
 }
 
 __global__ void __launch_bounds__(128)
@@ -253,6 +317,23 @@ __global__ void k_weight_packed(float* __restrict__ yw, const TY* __restrict__ y
         const float b = Store<TY>::ld_plain(y + (vj * nb + (nb - 1 - ib)) * na + ia);
         Store<float>::st2(yw + 2 * G * r + 2 * j, cr * a, cr * b);
     }
+}
+
+// Packed yw of a fan turn plan (G = 2 or 4): for r = (iv < nv/G, ia) the G
+// values c_r y of views iv + j nv/G at column ia, with c_r of view iv.
+template <typename TY, int G>
+__global__ void k_weight_fan_packed(float* __restrict__ yw, const TY* __restrict__ y,
+                                    const float* __restrict__ colr, int na, int nv,
+                                    long long npack, float scale)
+{
+    const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= npack) return;
+    const int gv = nv / G;
+    const int iv = (int)(r / na), ia = (int)(r - (long long)iv * na);
+    const float cr = ray_cr(scale, colr[r], 0.0f);
+#pragma unroll
+    for (int j = 0; j < G; j++)
+        yw[G * r + j] = cr * Store<TY>::ld_plain(y + ((long long)iv + (long long)j * gv) * na + ia);
 }
 
 // z-fold / unfold of volumes (all frames): pair r = (iz < nz/2, iy, ix) of a
@@ -364,6 +445,42 @@ k_adj_fan(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __re
         for (int i = 0; i < P; i++)
             if (iy0 + j < ny && ix0 + i < nx)
                 Store<TX>::st(xf + (long long)(iy0 + j) * nx + ix0 + i, acc[j][i]);
+}
+
+// Fan adjoint of a turn plan (G = 2 or 4, one frame): thread (x, g) of a
+// block of kFanX x NG threads takes the primary pixel (ix, iy) -- G = 2:
+// iy < ny/2; G = 4: ix, iy < n/2 -- with its turns, over view group g of the
+// views iv < nv/G (fan_turn_gather). The NG groups' sums meet in shared
+// memory and are added in the order g = 0, 1, ...; group 0 stores the G
+// pixels.
+template <typename TX, int G, int NG>
+__global__ void __launch_bounds__(kFanX * NG)
+k_adj_fan_turn(TX* __restrict__ X, const float* __restrict__ ywp,
+               const ColEntry* __restrict__ col, const ViewEntry* __restrict__ view, DetGrid D,
+               int nx, int ny, int na, int nv, const int* __restrict__ skip)
+{
+    if (skip && *skip) return;                 // uniform (one flag for the launch)
+    const int hx = G == 2 ? nx : nx / 2;
+    const int ix = blockIdx.x * kFanX + threadIdx.x, iy = blockIdx.y;
+    const int tx = threadIdx.x, g = threadIdx.y;
+    float acc[G];
+#pragma unroll
+    for (int j = 0; j < G; j++) acc[j] = 0.0f;
+    if (ix < hx) fan_turn_gather<G>(acc, ywp, col, view, D, ix, iy, nx, ny, na, nv, g, NG);
+    __shared__ float part[NG][G][kFanX];
+#pragma unroll
+    for (int j = 0; j < G; j++) part[g][j][tx] = acc[j];
+    __syncthreads();
+    if (g != 0 || ix >= hx) return;
+    int px[G], py[G];
+    fan_turn_pixels<G>(ix, iy, nx, ny, px, py);
+#pragma unroll
+    for (int j = 0; j < G; j++) {
+        float sum = part[0][j][tx];
+#pragma unroll
+        for (int k = 1; k < NG; k++) sum += part[k][j][tx];
+        Store<TX>::st(X + (long long)py[j] * nx + px[j], sum);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -862,6 +979,17 @@ void launch_fwd(fl_plan* p, const void* x, void* y, int cr_power, const int* ski
         k_fwd_cone<TX, TY, false><<<grid, dim3(8, 16), 0, st>>>(
             (const TX*)x, (TY*)y, p->d_col, p->d_colr, p->d_row, p->d_view_frame, s.nx, s.ny,
             s.nz, s.na, s.nb, p->n_vox_frame, s.scale, cr_power, skip, xscale, 0);
+    } else if (fl_plan_turns(p) > 1) {
+        const int G = fl_plan_turns(p);
+        const long long nt = (long long)s.na * (s.nv / G) * kFanLanes;
+        if (G == 4)
+            k_fwd_fan_turn<TX, TY, 4><<<fl_div_up(nt, 128), 128, 0, st>>>(
+                (const TX*)x, (TY*)y, p->d_col, p->d_colr, s.nx, s.ny, s.na, s.nv, s.scale,
+                cr_power, skip, xscale, yfold);
+        else
+            k_fwd_fan_turn<TX, TY, 2><<<fl_div_up(nt, 128), 128, 0, st>>>(
+                (const TX*)x, (TY*)y, p->d_col, p->d_colr, s.nx, s.ny, s.na, s.nv, s.scale,
+                cr_power, skip, xscale, yfold);
     } else {
         long long nr = (long long)s.na * s.nv;
         k_fwd_fan<TX, TY><<<fl_div_up(nr, 128), 128, 0, st>>>(
@@ -916,6 +1044,14 @@ void launch_adj(fl_plan* p, const float* yw, void* x, const int* skip, int xfold
                 (TX*)x, yw, p->d_col, p->d_rowz, p->d_view, p->d_idY, p->d_Nv, p->tmp_size, G,
                 s.nx, s.ny, s.nz, s.na, s.nb, s.dz, zruns, skip, 0);
         }
+    } else if (fl_plan_turns(p) == 4) {
+        dim3 grid(fl_div_up(s.nx / 2, kFanX), s.ny / 2);
+        k_adj_fan_turn<TX, 4, kTurnGroups><<<grid, dim3(kFanX, kTurnGroups), 0, st>>>(
+            (TX*)x, yw, p->d_col, p->d_view, G, s.nx, s.ny, s.na, s.nv, skip);
+    } else if (fl_plan_turns(p) == 2) {
+        dim3 grid(fl_div_up(s.nx, kFanX), s.ny / 2);
+        k_adj_fan_turn<TX, 2, kTurnGroups><<<grid, dim3(kFanX, kTurnGroups), 0, st>>>(
+            (TX*)x, yw, p->d_col, p->d_view, G, s.nx, s.ny, s.na, s.nv, skip);
     } else {
         // 2 x 2 pixel blocks, one thread each, once there are at least 4 waves
         // of 128-thread blocks; else one pixel per view group
@@ -968,6 +1104,23 @@ void launch_weight_packed(fl_plan* p, const void* y, int yt, float* yw, cudaStre
                                                              s.nv, npk, s.scale);
 }
 
+template <int G>
+void launch_weight_fan_packed(fl_plan* p, const void* y, int yt, float* yw, cudaStream_t st)
+{
+    const fl_scan& s = p->s;
+    const long long npk = (long long)s.na * (s.nv / G);
+    const unsigned g = fl_div_up(npk, 256);
+    if (yt == FL_F32)
+        k_weight_fan_packed<float, G><<<g, 256, 0, st>>>(yw, (const float*)y, p->d_colr, s.na,
+                                                         s.nv, npk, s.scale);
+    else if (yt == FL_F16)
+        k_weight_fan_packed<__half, G><<<g, 256, 0, st>>>(yw, (const __half*)y, p->d_colr, s.na,
+                                                          s.nv, npk, s.scale);
+    else
+        k_weight_fan_packed<__nv_bfloat16, G><<<g, 256, 0, st>>>(
+            yw, (const __nv_bfloat16*)y, p->d_colr, s.na, s.nv, npk, s.scale);
+}
+
 }  // namespace
 
 int fl_matched_fold(fl_plan* p, const void* src, void* dst, int dtype, int unfold,
@@ -993,6 +1146,8 @@ int fl_matched_forward(fl_plan* p, const void* x, int xt, void* y, int yt, int c
             x = w;
         }
         yfold = (layout & FL_LAY_Y_ADJ) ? 1 : 0;
+    } else if (p->s.ndim == 2 && fl_plan_turns(p) > 1) {
+        yfold = (layout & FL_LAY_Y_ADJ) ? 1 : 0;      // the packed fan layout
     }
     if (xt == FL_F32) launch_fwd_y<float>(p, x, y, yt, cr_power, skip, xscale, yfold, st);
     else if (xt == FL_F16) launch_fwd_y<__half>(p, x, y, yt, cr_power, skip, xscale, yfold, st);
@@ -1008,6 +1163,11 @@ int fl_matched_weight(fl_plan* p, const void* y, int yt, float* yw, cudaStream_t
     if (three && p->zmirror && p->rot) {
         if (p->rot4) launch_weight_packed<4>(p, y, yt, yw, st);
         else launch_weight_packed<2>(p, y, yt, yw, st);
+        return fl_check_launch("matched adjoint weighting");
+    }
+    if (!three && fl_plan_turns(p) > 1) {
+        if (fl_plan_turns(p) == 4) launch_weight_fan_packed<4>(p, y, yt, yw, st);
+        else launch_weight_fan_packed<2>(p, y, yt, yw, st);
         return fl_check_launch("matched adjoint weighting");
     }
     if (three && p->zmirror) {

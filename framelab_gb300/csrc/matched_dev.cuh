@@ -289,6 +289,119 @@ done:
     for (int j = 0; j < 4; j++) acc[j] = s[j];
 }
 
+// The fan walk in batches of kFanBatch steps: the crossings of a batch are
+// found first (they do not depend on the image), then its gathers are issued
+// together and the segments added in walk order. The sums are the same as
+// walk()'s, bit for bit, but a batch waits for its gathers once instead of
+// once per step.
+// G = 1: the ray's own pixels (acc[0]). G = 2 or 4 (a turn plan, one frame):
+// per step also the turns R^j (ix, iy) of the pixel -- G = 2: R (x, y) =
+// (nx-1-x, ny-1-y); G = 4 (nx == ny == n): R (x, y) = (n-1-y, x) -- which
+// the ray of view v + j nv/G at the same column crosses with the same
+// segment; acc[j] gets turn j's sum.
+// L > 1: the ray is cut into L parts and this call walks part `lane`. Part k
+// runs from crossing c_k to crossing c_{k+1}, where c_k (0 < k < L) is the
+// first crossing after a_in + k (a_out - a_in) / L (c_0 = a_in, c_L =
+// a_out). Every lane computes the cuts from the same expressions, and a cut
+// is a crossing of the ray's own table, so each segment -- each matrix
+// entry -- lies whole in one part and is the walk's own; only the order of
+// the additions changes (the caller adds the parts in lane order).
+// Termination as in walk().
+constexpr int kFanBatch = 4;
+
+template <typename TX, int G, int L = 1>
+__device__ __forceinline__ void walk_fan(const TX* __restrict__ x, float inv_x, float off_x,
+                                         float inv_y, float off_y, int nx, int ny,
+                                         float (&acc)[G], long long xlen, int lane = 0)
+{
+    static_assert(G == 1 || G == 2 || G == 4, "one, two or four turns");
+#pragma unroll
+    for (int j = 0; j < G; j++) acc[j] = 0.0f;
+    float ax0 = fmaf(0.0f, inv_x, off_x), ax1 = fmaf((float)nx, inv_x, off_x);
+    float ay0 = fmaf(0.0f, inv_y, off_y), ay1 = fmaf((float)ny, inv_y, off_y);
+    const float a_in = fmaxf(fminf(ax0, ax1), fminf(ay0, ay1));
+    const float a_out = fminf(fmaxf(ax0, ax1), fmaxf(ay0, ay1));
+    if (!(a_in < a_out)) return;
+    const bool px = inv_x > 0.0f, py = inv_y > 0.0f;
+    // the crossing that ends the slab pair (jx, jy)
+    auto next_x = [&](int j) { return fmaf((float)(px ? j + 1 : j), inv_x, off_x); };
+    auto next_y = [&](int j) { return fmaf((float)(py ? j + 1 : j), inv_y, off_y); };
+    float cur = a_in, end = a_out;
+    int jx, jy;
+    if (L > 1 && lane > 0) {
+        const float t = fmaf((float)lane, (a_out - a_in) * (1.0f / L), a_in);
+        jx = start_slab(t, inv_x, off_x, nx);
+        jy = start_slab(t, inv_y, off_y, ny);
+        const float cx = next_x(jx), cy = next_y(jy), c = fminf(cx, cy);
+        if (!(c < a_out)) return;                  // the cut falls at the exit: nothing left
+        if (cx == c) jx += px ? 1 : -1;
+        if (cy == c) jy += py ? 1 : -1;
+        cur = c;
+    } else {
+        jx = start_slab(a_in, inv_x, off_x, nx);
+        jy = start_slab(a_in, inv_y, off_y, ny);
+    }
+    if (L > 1 && lane + 1 < L) {
+        const float t = fmaf((float)(lane + 1), (a_out - a_in) * (1.0f / L), a_in);
+        const int ex = start_slab(t, inv_x, off_x, nx), ey = start_slab(t, inv_y, off_y, ny);
+        end = fminf(fminf(next_x(ex), next_y(ey)), a_out);
+        if (!(cur < end)) return;                  // an empty part
+    }
+    const int nxy = nx * ny;                       // < 2^31 (checked at plan creation)
+    // q0: the pixel; q1 (G = 4): its quarter turn x * n + n-1-y; the turns by
+    // pi of both are nxy - 1 minus them
+    int q0 = jy * nx + jx, q1 = jx * nx + (nx - 1 - jy);
+    float pax = (float)(px ? jx + 1 : jx);
+    float pay = (float)(py ? jy + 1 : jy);
+    const float stx = px ? 1.0f : -1.0f, sty = py ? 1.0f : -1.0f;
+    const int dq0x = px ? 1 : -1, dq0y = py ? nx : -nx;
+    const int dq1x = px ? nx : -nx, dq1y = py ? -1 : 1;
+    float nAx = fmaf(pax, inv_x, off_x);
+    float nAy = fmaf(pay, inv_y, off_y);
+    float s[G];
+#pragma unroll
+    for (int j = 0; j < G; j++) s[j] = 0.0f;
+    bool in = true;                                // the walk is at a pixel of the part
+    const int budget = nx + ny + 4;
+    for (int it = 0; it < budget && in; it += kFanBatch) {
+        float seg[kFanBatch];
+        int i0[kFanBatch], i1[kFanBatch];
+        bool live[kFanBatch];
+#pragma unroll
+        for (int u = 0; u < kFanBatch; u++) {
+            const float nxt = fminf(nAx, nAy);
+            const bool cont = nxt < end;           // false at the part's end (and for NaN)
+            live[u] = in;
+            seg[u] = nxt - cur;
+            i0[u] = q0; i1[u] = q1;
+            if (in && cont) {
+                if (nAx == nxt) { pax += stx; nAx = fmaf(pax, inv_x, off_x); q0 += dq0x; q1 += dq1x; }
+                if (nAy == nxt) { pay += sty; nAy = fmaf(pay, inv_y, off_y); q0 += dq0y; q1 += dq1y; }
+                cur = nxt;
+            }
+            in = in && cont;
+        }
+        float v[kFanBatch][G];
+#pragma unroll
+        for (int u = 0; u < kFanBatch; u++) {
+            const int q[4] = {i0[u], G == 4 ? i1[u] : nxy - 1 - i0[u], nxy - 1 - i0[u],
+                              nxy - 1 - i1[u]};
+#pragma unroll
+            for (int j = 0; j < G; j++) {
+                v[u][j] = 0.0f;
+                if (live[u] && FL_IN(q[j], xlen)) v[u][j] = ldv(x + q[j]);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kFanBatch; u++)
+#pragma unroll
+            for (int j = 0; j < G; j++)
+                if (live[u]) s[j] = fmaf(seg[u], v[u][j], s[j]);
+    }
+#pragma unroll
+    for (int j = 0; j < G; j++) acc[j] = s[j];
+}
+
 __device__ __forceinline__ float ray_cr(float scale, float dxy2, float dz2)
 {
     return fmul(scale, fsqrt(fadd(dxy2, dz2)));
@@ -460,6 +573,78 @@ __device__ __forceinline__ void fan_block_gather_all(float (&acc)[PY][PX],
             for (int g = 1; g < kFanGroups; g++) s += part[g][j][i];
             acc[j][i] = s;
         }
+}
+
+// Pixel p0 = (ix, iy) of a fan turn plan and its turns p_k = R^k p0
+// (walk_fan's R).
+template <int G>
+__device__ __forceinline__ void fan_turn_pixels(int ix, int iy, int nx, int ny, int (&px)[G],
+                                                int (&py)[G])
+{
+    px[0] = ix; py[0] = iy;
+    if (G == 2) {
+        px[1] = nx - 1 - ix; py[1] = ny - 1 - iy;
+    } else {
+        px[1] = nx - 1 - iy; py[1] = ix;
+        px[2] = nx - 1 - ix; py[2] = nx - 1 - iy;
+        px[3] = iy;          py[3] = nx - 1 - ix;
+    }
+}
+
+// View groups of the fan turn adjoint (k_adj_fan_turn).
+constexpr int kTurnGroups = 8;
+
+// Fan adjoint of a turn plan (G = 2 or 4, one frame): pixel p0 = (ix, iy)
+// and its turns p_k over the views iv = g, g + NG, ... < nv/G of view group
+// g. In view iv the weight of p_k and ray (iv, ia), from the same crossing
+// table as the walk, multiplies the value of ray (iv + j nv/G, ia) into
+// p_{k+j mod G}: A[(iv + j nv/G, a), R^j p] = A[(iv, a), p]. ywp is the
+// packed sinogram (G values per (iv < nv/G, ia)). A pixel's sum runs over the
+// group's views in order, per view over k = 0, 1, ... and the columns in
+// increasing order; only rays with w > 0 add to it.
+template <int G>
+__device__ __forceinline__ void fan_turn_gather(float (&acc)[G], const float* __restrict__ ywp,
+                                                const ColEntry* __restrict__ col,
+                                                const ViewEntry* __restrict__ view,
+                                                const DetGrid& D, int ix, int iy, int nx, int ny,
+                                                int na, int nv, int g, int NG)
+{
+    int px[G], py[G];
+    fan_turn_pixels<G>(ix, iy, nx, ny, px, py);
+    const int gv = nv / G;
+    for (int iv = g; iv < gv; iv += NG) {
+        const ViewEntry ve = view[iv];
+        const ColEntry* cv = col + (long long)iv * na;
+        const float* yv = ywp + (long long)G * iv * na;
+#pragma unroll
+        for (int k = 0; k < G; k++) {
+            int lo, hi; float dmin, dmax;
+            column_window(D, ve.c, ve.s, (float)(px[k] - nx / 2), (float)(py[k] - ny / 2), 1.0f,
+                          1.0f, na, lo, hi, dmin, dmax);
+            const float fx0 = (float)px[k], fx1 = (float)(px[k] + 1);
+            const float fy0 = (float)py[k], fy1 = (float)(py[k] + 1);
+            for (int ia = lo; ia <= hi; ia++) {
+                if (!FL_IN(ia, na)) continue;
+                const ColEntry ce = cv[ia];
+                const float ax0 = fmaf(fx0, ce.inv_x, ce.off_x), ax1 = fmaf(fx1, ce.inv_x, ce.off_x);
+                const float ay0 = fmaf(fy0, ce.inv_y, ce.off_y), ay1 = fmaf(fy1, ce.inv_y, ce.off_y);
+                const float l = fmaxf(fminf(ax0, ax1), fminf(ay0, ay1));
+                const float h = fminf(fmaxf(ax0, ax1), fmaxf(ay0, ay1));
+                const float w = h - l;
+                if (!(w > 0.0f)) continue;
+                float t[G];
+                if constexpr (G == 4) {
+                    const float4 u = __ldg(reinterpret_cast<const float4*>(yv + 4 * ia));
+                    t[0] = u.x; t[1] = u.y; t[2] = u.z; t[3] = u.w;
+                } else {
+                    const float2 u = __ldg(reinterpret_cast<const float2*>(yv + 2 * ia));
+                    t[0] = u.x; t[1] = u.y;
+                }
+#pragma unroll
+                for (int j = 0; j < G; j++) acc[(k + j) % G] = fmaf(w, t[j], acc[(k + j) % G]);
+            }
+        }
+    }
 }
 
 // The kFanGroups view groups of a pixel block are the threads (x, g) of a

@@ -114,7 +114,8 @@ class Plan:
     @property
     def rot_mirror(self) -> bool:
         """Whether the matched pair also uses the half-turn symmetry between
-        views v and v + nv/2 (FL_OPT_ROT_MIRROR; needs the z mirror)."""
+        views v and v + nv/2 (FL_OPT_ROT_MIRROR; a cone plan needs the z
+        mirror for it, a fan plan an even ny)."""
         v = C.c_int()
         _lib.check(self._L.fl_plan_query(self._h, _lib.OPT_ROT_MIRROR, C.byref(v)))
         return bool(v.value)

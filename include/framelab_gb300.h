@@ -193,13 +193,21 @@ int fl_plan_sizes(const fl_plan *plan, int64_t *n_vox, int64_t *n_rays);
  *   weight serves four rays; the matrix stays exactly transposed and differs
  *   from the general kernels' by the FP32 rounding of the turned views' own
  *   tables.
- *   Queries report 0 while FL_OPT_Z_MIRROR is off.
+ *   Queries report 0 while FL_OPT_Z_MIRROR is off. Fan-beam plans take the
+ *   half turn without a mirror (one frame, ny even, the same view test):
+ *   ray (v + nv/2, a) crosses pixel (nx-1-x, ny-1-y) where ray (v, a) crosses
+ *   (x, y), one walk or weight serving two rays.
  * FL_OPT_QUARTER_TURN: on top of FL_OPT_ROT_MIRROR, on by default when
  *   nx == ny, nv is a multiple of 4 and view v + nv/4 is view v turned by
  *   pi/2 (to within 1e-6). Ray (v + j nv/4, a, b) is then defined as ray
  *   (v, a, b) turned by j pi/2, crossing voxel R^j (x, y, z) with
- *   R (x, y, z) = (n-1-y, x, z): one walk or weight serves eight rays. Queries
- *   report 0 while either option below it is off. */
+ *   R (x, y, z) = (n-1-y, x, z): one walk or weight serves eight rays (four
+ *   on a fan plan, R (x, y) = (n-1-y, x), nx == ny even). Queries report 0
+ *   while either option below it is off.
+ *   A ray that runs exactly along a pixel boundary (the central ray of an
+ *   odd detector at a view angle of exactly 0) has no unique discretisation:
+ *   on the turn forms its turned copies take the walked view's choice, which
+ *   can differ from the general kernels' at O(1) for that ray alone. */
 enum { FL_OPT_Z_MIRROR = 1, FL_OPT_ROT_MIRROR = 2, FL_OPT_QUARTER_TURN = 3 };
 int fl_plan_option(fl_plan *plan, int option, int value);
 int fl_plan_query(const fl_plan *plan, int option, int *value);

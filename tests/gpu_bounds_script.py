@@ -31,6 +31,12 @@ def run_plan(p, rng):
             P.forward(x)
             P.adjoint(y)
         P.z_mirror, P.rot_mirror, P.quarter_turn = True, True, True
+    else:                              # fan: half turn, then the general kernels
+        for q, r in ((False, True), (False, False)):
+            P.quarter_turn, P.rot_mirror = q, r
+            P.forward(x)
+            P.adjoint(y)
+        P.rot_mirror, P.quarter_turn = True, True
     for mode in ("graph", "mixed"):
         NativeCGLS(P, mode).solve(torch.abs(x), lam=0.1, iters=3, refresh=2)
 
@@ -53,6 +59,7 @@ def main():
                        voxel_mm=6.0, nz=17),                           # odd nz and nb
         G.fan_para(64, 64, 128, 30, L=(1, 1)),                         # fan, 1 x 1 blocks
         G.fan_para(512, 512, 1024, 60, L=(1, 1)),                      # fan, 2 x 2 blocks
+        G.fan_para(48, 36, 97, 42, L=(1, 0.75), SO=3.0, OD=3.0, Ly=3.0),  # fan, rectangular
     ]
     for p in cases:
         run_plan(p, rng)

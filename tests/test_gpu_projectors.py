@@ -617,6 +617,105 @@ def test_quarter_turn_is_detected_and_exact():
     assert _rel(_host(u8), _host(u4)) < 1e-3
 
 
+def _fan_turn_para(n=48, ny=None, nv=40, phi=None, nd=96):
+    return G.fan_para(n, ny or n, nd, nv, L=(1.0, (ny or n) / n), SO=3.0, OD=3.0, Ly=3.0,
+                      sd_phi=phi)
+
+
+def test_fan_turns_are_detected_only_for_turn_scans():
+    """Fan plans take the half turn (ny even) and the quarter turn (nx == ny,
+    even, nv a multiple of 4) with no mirror."""
+    P = _plan(_fan_turn_para())
+    assert not P.z_mirror and P.rot_mirror and P.quarter_turn
+    P.rot_mirror = False                               # the quarter turn rides on it
+    assert not P.quarter_turn
+    P.rot_mirror = True
+    assert P.quarter_turn
+    H = _plan(_fan_turn_para(nv=42))                   # nv/4 not whole
+    assert H.rot_mirror and not H.quarter_turn
+    R = _plan(_fan_turn_para(n=48, ny=36))             # rectangular: half turn only
+    assert R.rot_mirror and not R.quarter_turn
+    O1 = _plan(_fan_turn_para(n=48, ny=37))            # odd ny: no primary half
+    assert not O1.rot_mirror
+    O1.rot_mirror = True
+    assert not O1.rot_mirror
+    phi = np.sort(np.random.default_rng(0).uniform(0, 2 * np.pi, 40)).astype(np.float32)
+    assert not _plan(_fan_turn_para(phi=phi)).rot_mirror
+    short = (np.pi / 40 * np.arange(40)).astype(np.float32)   # half a turn of views
+    assert not _plan(_fan_turn_para(phi=short)).rot_mirror
+
+
+@pytest.mark.parametrize("shape", [(48, 48, 40, 96), (48, 36, 42, 96), (40, 40, 38, 96),
+                                   (48, 48, 40, 97)])
+def test_fan_turns_agree_with_general_kernels_and_are_exact(shape):
+    torch = _torch()
+    from framelab_gb300.solvers import NativeCGLS
+    n, ny, nv, nd = shape
+    p = _fan_turn_para(n, ny, nv, nd=nd)
+    P = _plan(p)
+    G4 = P.quarter_turn
+    assert P.rot_mirror and G4 == (n == ny and nv % 4 == 0)
+    X = PH.ellipses_2d(max(n, ny), seed=5)[:ny, :n]
+    x = np.ascontiguousarray(X).reshape(-1).astype(np.float32)
+    rng = np.random.default_rng(7)
+    r = rng.standard_normal((nv, nd)).astype(np.float32)
+    # An odd detector has a central ray through the isocentre. At view 0
+    # (angle exactly 0) it runs exactly along the pixel boundary y = 0, and
+    # its length goes to one row. The turned views' own angles are a float
+    # rounding off the axes, so their central rays cross that boundary at the
+    # isocentre. The turned copy of view 0's ray therefore assigns half its
+    # length to the other neighbouring row or column. The two discretisations
+    # of this one degenerate ray differ at O(1), so the comparison with the
+    # general kernels and the FP64 model leaves that column out.
+    keep = np.ones(nd, bool)
+    if nd % 2:
+        keep[nd // 2] = False
+        r[:, nd // 2] = 0.0
+    r = r.reshape(-1)
+    yt, xt = _host(P.forward(_dev(x))), _host(P.adjoint(_dev(r)))
+    P.rot_mirror = False
+    yg, xg = _host(P.forward(_dev(x))), _host(P.adjoint(_dev(r)))
+    P.rot_mirror = True
+    # the turned views use the walked view's tables: the matrices differ by the
+    # FP32 rounding of the turned views' own tables and angles
+    yk, gk = yt.reshape(nv, nd)[:, keep], yg.reshape(nv, nd)[:, keep]
+    assert _rel(yk, gk) < 1e-5 and _rel(xt, xg) < 1e-4, (_rel(yk, gk), _rel(xt, xg))
+    assert _rel(yk, O.exact_forward(x, p).reshape(nv, nd)[:, keep]) < 1e-5
+    assert _rel(xt, O.exact_adjoint(r, p)) < 1e-4
+    if G4:
+        # views v + nv/4 of A x are views v of A R(x): R(x)[y, x] = x[x, n-1-y]
+        xr = X[:, ::-1].T.reshape(-1).astype(np.float32).copy()
+        yr = _host(P.forward(_dev(xr))).reshape(nv, nd)
+        assert np.array_equal(yt.reshape(nv, nd)[nv // 4:], yr[:3 * nv // 4])
+    else:
+        # views v + nv/2 of A x are views v of A of the image turned by pi
+        xh = X[::-1, ::-1].reshape(-1).astype(np.float32).copy()
+        yh = _host(P.forward(_dev(xh))).reshape(nv, nd)
+        assert np.array_equal(yt.reshape(nv, nd)[nv // 2:], yh[:nv // 2])
+    # the adjoint stays the exact transpose
+    lhs = np.dot(yt.astype(np.float64), r.astype(np.float64))
+    rhs = np.dot(x.astype(np.float64), xt.astype(np.float64))
+    assert abs(lhs - rhs) / abs(lhs) < 1e-5, (lhs, rhs)
+    # low-precision storage goes through the same kernels
+    assert _rel(_host(P.forward(_dev(x, torch.float16))), yt) < 2e-3
+    xb = _host(P.adjoint(_dev(r, torch.bfloat16)))
+    assert _rel(xb, _host(P.adjoint(_dev(r.astype(np.float32))))) < 2e-2
+    # every CGLS form goes through them and follows the option (with an odd
+    # detector the two matrices differ on the central ray, and so do the
+    # solutions)
+    b = P.adjoint(P.forward(_dev(x))).reshape(-1).contiguous()
+    for mode in ("plain", "graph", "mixed"):
+        cg = NativeCGLS(P, mode)
+        ut = cg.solve(b, iters=6).clone()
+        P.rot_mirror = False
+        ug = cg.solve(b, iters=6).clone()
+        P.rot_mirror = True
+        tol = 1e-3 if mode == "mixed" else 1e-4
+        assert np.all(np.isfinite(_host(ut)))
+        if nd % 2 == 0:
+            assert _rel(_host(ut), _host(ug)) < tol, (mode, _rel(_host(ut), _host(ug)))
+
+
 def test_turn_plans_need_columns_of_four():
     """The half- and quarter-turn forms keep the folded volume in 4 x 4 tiles:
     sizes that are not multiples of 4 keep the z mirror alone."""
