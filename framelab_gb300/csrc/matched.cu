@@ -183,16 +183,18 @@ k_fwd_fan(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restri
 
 // Fan forward of a turn plan (G = 2 or 4, one frame): kFanLanes threads per
 // ray (iv < nv/G, ia), each walking one part of it (walk_fan), their sums
-// added in lane order; the walk also yields the rays of views iv + j nv/G at
+// added in part order; the walk also yields the rays of views iv + j nv/G at
 // the same column, all with the walked ray's c_r. ypack writes the
 // adjoint-input layout of these plans: the G values of ray (iv, ia)'s orbit
 // side by side at G (iv na + ia) + j (k_weight_fan_packed). Fan launches
 // have few rays: the parts give the GPU kFanLanes times the threads, each
-// with that fraction of the walk.
+// with that fraction of the walk. A block is 32 neighbouring rays x
+// kFanLanes parts, part k in warp k, so a warp's gathers follow 32
+// neighbouring rays.
 constexpr int kFanLanes = 8;
 
 template <typename TX, typename TY, int G>
-__global__ void __launch_bounds__(128, 8)
+__global__ void __launch_bounds__(32 * kFanLanes, 4)
 k_fwd_fan_turn(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restrict__ col,
                const float* __restrict__ colr, int nx, int ny, int na, int nv, float scale,
                int cr_power, const int* __restrict__ skip, const float* __restrict__ xscale,
@@ -200,9 +202,8 @@ k_fwd_fan_turn(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __r
 {
     if (skip && *skip) return;                 // uniform (one flag for the launch)
     const int gv = nv / G;
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long r = t / kFanLanes;
-    const int lane = (int)(t % kFanLanes);
+    const int tx = threadIdx.x, lane = threadIdx.y;
+    const long long r = (long long)blockIdx.x * 32 + tx;
     const bool ray = r < (long long)na * gv;
     float acc[G];
 #pragma unroll
@@ -212,19 +213,19 @@ k_fwd_fan_turn(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __r
         walk_fan<TX, G, kFanLanes>(X, ce.inv_x, ce.off_x, ce.inv_y, ce.off_y, nx, ny, acc,
                                    (long long)nx * ny, lane);
     }
-    // the parts of a ray are consecutive lanes of one warp: lane 0 adds them
-    const int base = (threadIdx.x & 31) & ~(kFanLanes - 1);
+    // part k of ray tx is warp k's lane tx: warp 0 adds them in order
+    __shared__ float part[kFanLanes][G][32];
+#pragma unroll
+    for (int j = 0; j < G; j++) part[lane][j][tx] = acc[j];
+    __syncthreads();
+    if (!ray || lane != 0) return;
 #pragma unroll
     for (int j = 0; j < G; j++) {
-        float part[kFanLanes];
+        float sum = part[0][j][tx];
 #pragma unroll
-        for (int k = 0; k < kFanLanes; k++) part[k] = __shfl_sync(0xffffffffu, acc[j], base + k);
-        float sum = part[0];
-#pragma unroll
-        for (int k = 1; k < kFanLanes; k++) sum += part[k];
+        for (int k = 1; k < kFanLanes; k++) sum += part[k][j][tx];
         acc[j] = sum;
     }
-    if (!ray || lane != 0) return;
     const int iv = (int)(r / na), ia = (int)(r - (long long)iv * na);
     const float cr = ray_cr(scale, colr[r], 0.0f);
     float o[G];
@@ -981,13 +982,14 @@ void launch_fwd(fl_plan* p, const void* x, void* y, int cr_power, const int* ski
             s.nz, s.na, s.nb, p->n_vox_frame, s.scale, cr_power, skip, xscale, 0);
     } else if (fl_plan_turns(p) > 1) {
         const int G = fl_plan_turns(p);
-        const long long nt = (long long)s.na * (s.nv / G) * kFanLanes;
+        const long long nr = (long long)s.na * (s.nv / G);
+        const dim3 blk(32, kFanLanes);
         if (G == 4)
-            k_fwd_fan_turn<TX, TY, 4><<<fl_div_up(nt, 128), 128, 0, st>>>(
+            k_fwd_fan_turn<TX, TY, 4><<<fl_div_up(nr, 32), blk, 0, st>>>(
                 (const TX*)x, (TY*)y, p->d_col, p->d_colr, s.nx, s.ny, s.na, s.nv, s.scale,
                 cr_power, skip, xscale, yfold);
         else
-            k_fwd_fan_turn<TX, TY, 2><<<fl_div_up(nt, 128), 128, 0, st>>>(
+            k_fwd_fan_turn<TX, TY, 2><<<fl_div_up(nr, 32), blk, 0, st>>>(
                 (const TX*)x, (TY*)y, p->d_col, p->d_colr, s.nx, s.ny, s.na, s.nv, s.scale,
                 cr_power, skip, xscale, yfold);
     } else {
