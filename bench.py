@@ -553,7 +553,8 @@ def run_single(ctx, name, w, p):
 
 
 def run_batch(ctx, name, w, paras):
-    """fanbatch: batched CGLS over uneven fan slices (one launch per operator)."""
+    """fanbatch: batched CGLS over uneven fan slices (one launch per operator and
+    kind of slice: general, or half / quarter turn)."""
     torch = ctx.torch
     from framelab_gb300 import phantoms as PH
     from framelab_gb300.batch import FanBatch
@@ -569,7 +570,8 @@ def run_batch(ctx, name, w, paras):
     rhs = B.adjoint(sino)
     del sino
     torch.cuda.synchronize()
-    detail = {"slices": len(B), "n_vox": B.n_vox, "n_rays": B.n_rays}
+    detail = {"slices": len(B), "n_vox": B.n_vox, "n_rays": B.n_rays,
+              "slices_by_turns": {str(t): B.turns.count(t) for t in (1, 2, 4)}}
     if W:
         B.cgls(rhs, iters=W)
     clocks = ClockSampler(ctx.local)
@@ -617,7 +619,8 @@ def run_batch(ctx, name, w, paras):
         roofline = projector_roofline(ctx, name, n_isect, B.n_rays, B.n_vox, tf / reps,
                                       ta / reps, detail, "batched matched")
     return dict(value=job_rate(world, K, t_b), t_step=t_b / K, e2e=e2e, roofline=roofline,
-                launches=5 * K + 1, detail=detail, clocks=clocks.summary(), unit="iter/s")
+                launches=B.launches_per_iteration * K + 1, detail=detail,
+                clocks=clocks.summary(), unit="iter/s")
 
 
 def run_sb(ctx, name, w, p):

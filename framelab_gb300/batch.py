@@ -5,8 +5,11 @@ detector widths and view counts), builds a :class:`~framelab_gb300.projector.Pla
 per slice and one native batch over them. Images and sinograms of all slices
 live concatenated in one device tensor each (slice ``i`` at
 ``vox_offsets[i]:vox_offsets[i+1]`` / ``ray_offsets[i]:ray_offsets[i+1]``), and
-every operator is one kernel launch for the whole batch. The per-slice results
-equal the slice plan's own matched forward/adjoint bit for bit.
+every operator is one kernel launch for the whole batch, or two when some
+slices use the half or quarter turn of their plan (they run the plan's turn
+kernels). The per-slice results equal the slice plan's own matched
+forward/adjoint bit for bit, with the plan's turn options as they were when
+the batch was created.
 
 This is the reference's per-slice loop over ``FanBeamScanner.apply`` /
 ``applyAdjoint`` and ``solveCGLS`` (``solveCGLS.m:6-31``) as one batched solve.
@@ -31,12 +34,18 @@ def _stream():
 class FanBatch:
     """Many single-frame fan-beam scans projected and solved together."""
 
-    def __init__(self, paras):
+    def __init__(self, paras, turns: bool = True):
+        """``turns=False`` keeps every slice on the general kernels (each
+        plan's half / quarter turn switched off before the batch is built)."""
         L = _lib.load()
         self.plans = [Plan(p) for p in paras]
         for i, P in enumerate(self.plans):
             if P.cone:
                 raise ValueError(f"slice {i} is not a fan-beam scan")
+            if not turns:
+                P.rot_mirror = False
+        # rays served per walk of each slice (4 quarter turn, 2 half turn, 1)
+        self.turns = [4 if P.quarter_turn else (2 if P.rot_mirror else 1) for P in self.plans]
         n = len(self.plans)
         handles = (C.c_void_p * n)(*[P.handle.value for P in self.plans])
         h = C.c_void_p()
@@ -52,6 +61,14 @@ class FanBatch:
 
     def __len__(self):
         return len(self.plans)
+
+    @property
+    def launches_per_iteration(self) -> int:
+        """Kernel launches of one CGLS iteration: forward and adjoint for the
+        general and for the turn slices, plus the three algebra kernels."""
+        general = any(t == 1 for t in self.turns)
+        turned = any(t > 1 for t in self.turns)
+        return 3 + 2 * int(general) + 2 * int(turned)
 
     def __del__(self):
         h = getattr(self, "_h", None)

@@ -11,15 +11,20 @@
 // count) so the largest slices start first and the tail is made of the
 // cheapest chunks. The forward and adjoint are the matched model of the
 // single-scan kernels (the same device code, matched_dev.cuh), so each slice's
-// result is bit-identical to its own plan's.
+// result is bit-identical to its own plan's. A slice whose plan uses the half
+// or quarter turn (fl_plan_turns when the batch is created) goes through the
+// plan's turn kernels instead, on two more lists (32 rays of the views
+// iv < nv/G; 32 primary pixels); its adjoint input is packed per orbit, as
+// the plan's.
 //
 // CGLS (solveCGLS.m:6-31) runs per slice, all slices in lockstep: every slice
 // has its own FP64 gamma/alpha/beta and stop flag, the inner products are
 // segmented by slice (per-chunk FP64 partials; the last chunk of a slice to
 // finish sums that slice's partials in a fixed order, so results do not depend
 // on scheduling). One iteration = 5 launches (forward with c_r^2, adjoint,
-// q += lam p with <p,q>, updates with <r,r>, direction), captured once as a
-// CUDA graph and replayed. A stopped slice's chunks return at once.
+// q += lam p with <p,q>, updates with <r,r>, direction; 7 when both general
+// and turn slices are present), captured once as a CUDA graph and replayed.
+// A stopped slice's chunks return at once.
 #include <algorithm>
 #include <cstring>
 #include <new>
@@ -46,8 +51,12 @@ struct BatchSlice {
     int nvf;               // its length (Nv[0])
     DetGrid G;
     int nx, ny, na, nv;
+    int turns;             // fl_plan_turns of the slice's plan at batch creation
+    int lanes;             // parts per walked ray (fan_turn_lanes)
     float scale;
     long long xoff, yoff;  // offsets of the slice in the concatenated image / sinogram
+    long long woff;        // its offset in the batch's sinogram scratch (a multiple of
+                           // 4 floats: turn slices' packed orbits are read as vectors)
     int vc0, vc1;          // its vector chunks [vc0, vc1)
 };
 
@@ -109,7 +118,7 @@ __device__ bool slice_sum(double v, int slice, int c0, int c1, double* partials,
 __global__ void __launch_bounds__(kRayChunk, 8)
 k_batch_fwd(const float* __restrict__ X, float* __restrict__ Y,
             const BatchSlice* __restrict__ sl, const int2* __restrict__ chunks, int cr_power,
-            const BatchScal* __restrict__ S)
+            int scratch, const BatchScal* __restrict__ S)
 {
     const int2 ch = chunks[blockIdx.x];
     if (S && S[ch.x].done) return;
@@ -123,10 +132,35 @@ k_batch_fwd(const float* __restrict__ X, float* __restrict__ Y,
     float cr = ray_cr(b.scale, b.colr[r], 0.0f);
     float out = cr * acc;
     if (cr_power == 2) out = cr * out;
-    Y[b.yoff + r] = out;
+    Y[(scratch ? b.woff : b.yoff) + r] = out;
 }
 
-// yw = c_r * y over the ray chunks (input of the stand-alone adjoint)
+// Turn slices: the plan's turn forward, one block of kFanBlock threads per
+// chunk (slice, r0) of the rays iv < nv/G (kFanBlock / lanes rays). ypack:
+// into the batch's scratch (woff), packed per orbit; else the standard
+// layout at yoff.
+__global__ void __launch_bounds__(kFanBlock, 4)
+k_batch_fwd_turn(const float* __restrict__ X, float* __restrict__ Y,
+                 const BatchSlice* __restrict__ sl, const int2* __restrict__ chunks,
+                 int cr_power, int ypack, const BatchScal* __restrict__ S)
+{
+    const int2 ch = chunks[blockIdx.x];
+    if (S && S[ch.x].done) return;            // uniform in the block
+    const BatchSlice& b = sl[ch.x];
+    float* y = Y + (ypack ? b.woff : b.yoff);
+#define FL_BATCH_TURN(GG, LL)                                                                  \
+    fan_turn_forward_block<float, float, GG, LL>(X + b.xoff, y, b.col, b.colr, b.nx, b.ny, b.na, \
+                                                 b.nv, b.scale, cr_power, nullptr, ypack, ch.y)
+    if (b.turns == 4 && b.lanes > 1) FL_BATCH_TURN(4, kFanLanes);
+    else if (b.turns == 4) FL_BATCH_TURN(4, 1);
+    else if (b.lanes > 1) FL_BATCH_TURN(2, kFanLanes);
+    else FL_BATCH_TURN(2, 1);
+#undef FL_BATCH_TURN
+}
+
+// yw = c_r * y over the ray chunks of all slices (input of the stand-alone
+// adjoint, in the batch's scratch); a turn slice's yw is packed per orbit
+// with c_r of view iv < nv/G (the single plan's k_weight_fan_packed values)
 __global__ void __launch_bounds__(kRayChunk)
 k_batch_weight(float* __restrict__ YW, const float* __restrict__ Y,
                const BatchSlice* __restrict__ sl, const int2* __restrict__ chunks)
@@ -135,8 +169,33 @@ k_batch_weight(float* __restrict__ YW, const float* __restrict__ Y,
     const BatchSlice& b = sl[ch.x];
     const int r = ch.y + threadIdx.x;
     if (r >= b.na * b.nv) return;
+    if (b.turns > 1) {
+        const int gv = b.nv / b.turns, iv = r / b.na, ia = r - iv * b.na;
+        const int rp = (iv % gv) * b.na + ia;
+        const float cr = ray_cr(b.scale, b.colr[rp], 0.0f);
+        YW[b.woff + (long long)b.turns * rp + iv / gv] = cr * Y[b.yoff + r];
+        return;
+    }
     float cr = ray_cr(b.scale, b.colr[r], 0.0f);
-    YW[b.yoff + r] = cr * Y[b.yoff + r];
+    YW[b.woff + r] = cr * Y[b.yoff + r];
+}
+
+// Turn slices: the plan's turn backprojection, one block of 32 blocks of 2 x 2
+// primary pixels x kTurnGroups view groups per chunk (slice, iy0, ix0).
+__global__ void __launch_bounds__(kFanX * kTurnGroups)
+k_batch_adj_turn(float* __restrict__ X, const float* __restrict__ YW,
+                 const BatchSlice* __restrict__ sl, const int4* __restrict__ chunks,
+                 const BatchScal* __restrict__ S)
+{
+    const int4 ch = chunks[blockIdx.x];       // (slice, iy, ix0, -)
+    if (S && S[ch.x].done) return;            // uniform in the block
+    const BatchSlice& b = sl[ch.x];
+    if (b.turns == 4)
+        fan_turn_adjoint_block<float, 4, 2>(X + b.xoff, YW + b.woff, b.col, b.view, b.G, b.nx,
+                                            b.ny, b.na, b.nv, ch.z, ch.y);
+    else
+        fan_turn_adjoint_block<float, 2, 2>(X + b.xoff, YW + b.woff, b.col, b.view, b.G, b.nx,
+                                            b.ny, b.na, b.nv, ch.z, ch.y);
 }
 
 // x = A^T (pre-weighted yw), one block per chunk of 2 image rows x
@@ -153,7 +212,7 @@ k_batch_adj(float* __restrict__ X, const float* __restrict__ YW,
     const int ix0 = ch.z + 2 * threadIdx.x, iy0 = ch.y;
     if (ix0 >= b.nx) return;
     float acc[2][2];
-    fan_block_gather_all<2, 2>(acc, YW + b.yoff, b.col, b.view, b.views, b.nvf, b.G, ix0, iy0,
+    fan_block_gather_all<2, 2>(acc, YW + b.woff, b.col, b.view, b.views, b.nvf, b.G, ix0, iy0,
                                b.nx, b.ny, b.na);
     float* xs = X + b.xoff;
 #pragma unroll
@@ -279,8 +338,11 @@ struct fl_batch {
     long long n_vox, n_rays;
     std::vector<long long> xoff, yoff;   // [n + 1]
     BatchSlice* d_sl;
-    int2* d_rays;  int n_ray_chunks;
-    int4* d_pix;   int n_pix_chunks;
+    int2* d_rays;  int n_ray_chunks;       // general slices' rays (forward)
+    int2* d_rays_t; int n_ray_t_chunks;    // turn slices' walked rays (forward)
+    int2* d_wrays; int n_wray_chunks;      // every slice's rays (weighting)
+    int4* d_pix;   int n_pix_chunks;       // general slices' pixel blocks
+    int4* d_pix_t; int n_pix_t_chunks;     // turn slices' primary pixels
     VecChunk* d_vec; int n_vec_chunks;
     float *r, *p, *q, *tmp;
     BatchScal* S;
@@ -298,8 +360,8 @@ struct fl_batch {
 
 static void batch_free(fl_batch* b)
 {
-    void* ptrs[] = {b->d_sl, b->d_rays, b->d_pix, b->d_vec, b->r, b->p, b->q, b->tmp,
-                    b->S, b->partials, b->tickets, b->hist};
+    void* ptrs[] = {b->d_sl, b->d_rays, b->d_rays_t, b->d_wrays, b->d_pix, b->d_pix_t, b->d_vec,
+                    b->r, b->p, b->q, b->tmp, b->S, b->partials, b->tickets, b->hist};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     if (b->exec) cudaGraphExecDestroy(b->exec);
@@ -323,7 +385,7 @@ extern "C" int fl_batch_create(fl_plan* const* plans, int32_t n_plans, fl_batch*
         return fl_set_error(FL_ERR_INVALID, "fl_batch_create: bad argument");
     *out = nullptr;
     std::vector<BatchSlice> sl(n_plans);
-    std::vector<long long> xoff(n_plans + 1, 0), yoff(n_plans + 1, 0);
+    std::vector<long long> xoff(n_plans + 1, 0), yoff(n_plans + 1, 0), woff(n_plans + 1, 0);
     for (int i = 0; i < n_plans; i++) {
         fl_plan* p = plans[i];
         if (!p) return fl_set_error(FL_ERR_INVALID, "fl_batch_create: plan %d is null", i);
@@ -350,9 +412,12 @@ extern "C" int fl_batch_create(fl_plan* const* plans, int32_t n_plans, fl_batch*
         b.G.v0 = p->v0; b.G.dv = p->dv; b.G.SO = s.SO; b.G.SD = p->SD;
         b.G.rdu = 1.0f / p->du; b.G.rdg = p->dg != 0.0f ? 1.0f / p->dg : 0.0f;
         b.nx = s.nx; b.ny = s.ny; b.na = s.na; b.nv = s.nv; b.scale = s.scale;
+        b.turns = fl_plan_turns(p);
+        b.lanes = b.turns > 1 ? fan_turn_lanes((long long)s.na * (s.nv / b.turns)) : 1;
         xoff[i + 1] = xoff[i] + (long long)s.nx * s.ny;
         yoff[i + 1] = yoff[i] + (long long)s.na * s.nv;
-        b.xoff = xoff[i]; b.yoff = yoff[i];
+        woff[i + 1] = woff[i] + ((long long)s.na * s.nv + 3) / 4 * 4;
+        b.xoff = xoff[i]; b.yoff = yoff[i]; b.woff = woff[i];
     }
     // work lists, costliest slices first
     std::vector<int> by_walk(n_plans), by_views(n_plans);
@@ -364,14 +429,29 @@ extern "C" int fl_batch_create(fl_plan* const* plans, int32_t n_plans, fl_batch*
     std::stable_sort(by_views.begin(), by_views.end(), [&](int a, int c) {
         return sl[a].nvf > sl[c].nvf;
     });
-    std::vector<int2> rays;
-    for (int i : by_walk)
-        for (int r = 0; r < sl[i].na * sl[i].nv; r += kRayChunk) rays.push_back(make_int2(i, r));
-    std::vector<int4> pix;
-    for (int i : by_views)
-        for (int iy = 0; iy < sl[i].ny; iy += 2)
-            for (int ix = 0; ix < sl[i].nx; ix += 2 * kPixChunk)
-                pix.push_back(make_int4(i, iy, ix, 0));
+    std::vector<int2> rays, rays_t, wrays;
+    for (int i : by_walk) {
+        const BatchSlice& c = sl[i];
+        for (int r = 0; r < c.na * c.nv; r += kRayChunk) wrays.push_back(make_int2(i, r));
+        if (c.turns == 1)
+            for (int r = 0; r < c.na * c.nv; r += kRayChunk) rays.push_back(make_int2(i, r));
+        else
+            for (int r = 0; r < c.na * (c.nv / c.turns); r += kFanBlock / c.lanes)
+                rays_t.push_back(make_int2(i, r));
+    }
+    std::vector<int4> pix, pix_t;
+    for (int i : by_views) {
+        const BatchSlice& c = sl[i];
+        if (c.turns == 1) {
+            for (int iy = 0; iy < c.ny; iy += 2)
+                for (int ix = 0; ix < c.nx; ix += 2 * kPixChunk)
+                    pix.push_back(make_int4(i, iy, ix, 0));
+        } else {                          // the primary pixels: rows y < ny/2 (and x < nx/2)
+            const int hx = c.turns == 2 ? c.nx : c.nx / 2;
+            for (int iy = 0; iy < c.ny / 2; iy += 2)
+                for (int ix = 0; ix < hx; ix += 2 * kFanX) pix_t.push_back(make_int4(i, iy, ix, 0));
+        }
+    }
     std::vector<VecChunk> vec;
     for (int i = 0; i < n_plans; i++) {
         sl[i].vc0 = (int)vec.size();
@@ -380,7 +460,8 @@ extern "C" int fl_batch_create(fl_plan* const* plans, int32_t n_plans, fl_batch*
             vec.push_back(VecChunk{i, (int)k, (int)std::min<long long>(kVecChunk, n - k), 0});
         sl[i].vc1 = (int)vec.size();
     }
-    if (rays.size() > 0x7fffffffu || pix.size() > 0x7fffffffu || vec.size() > 0x7fffffffu)
+    if (wrays.size() > 0x7fffffffu || pix.size() + pix_t.size() > 0x7fffffffu ||
+        vec.size() > 0x7fffffffu)
         return fl_set_error(FL_ERR_UNSUPPORTED, "fl_batch_create: batch too large");
 
     fl_batch* b = new (std::nothrow) fl_batch;
@@ -388,21 +469,27 @@ extern "C" int fl_batch_create(fl_plan* const* plans, int32_t n_plans, fl_batch*
     b->n = n_plans; b->n_vox = xoff[n_plans]; b->n_rays = yoff[n_plans];
     b->xoff = xoff; b->yoff = yoff;
     b->d_sl = nullptr; b->d_rays = nullptr; b->d_pix = nullptr; b->d_vec = nullptr;
+    b->d_rays_t = nullptr; b->d_wrays = nullptr; b->d_pix_t = nullptr;
     b->r = b->p = b->q = b->tmp = nullptr; b->S = nullptr; b->partials = nullptr;
     b->tickets = nullptr; b->hist = nullptr; b->hist_cap = 4096;
     b->cs = nullptr; b->ev0 = b->ev1 = nullptr; b->exec = nullptr; b->cap_u = nullptr;
     b->cap_lam = 0.0f; b->cap_tol = 0.0;
     b->n_ray_chunks = (int)rays.size(); b->n_pix_chunks = (int)pix.size();
+    b->n_ray_t_chunks = (int)rays_t.size(); b->n_wray_chunks = (int)wrays.size();
+    b->n_pix_t_chunks = (int)pix_t.size();
     b->n_vec_chunks = (int)vec.size();
     int st = upload_vec(&b->d_sl, sl);
     if (!st) st = upload_vec(&b->d_rays, rays);
+    if (!st) st = upload_vec(&b->d_rays_t, rays_t);
+    if (!st) st = upload_vec(&b->d_wrays, wrays);
     if (!st) st = upload_vec(&b->d_pix, pix);
+    if (!st) st = upload_vec(&b->d_pix_t, pix_t);
     if (!st) st = upload_vec(&b->d_vec, vec);
     auto M = [&](void** ptr, size_t bytes) {
         if (!st) st = fl_check_cuda(fl_malloc(ptr, bytes), "fl_malloc(batch)");
     };
     M((void**)&b->r, b->n_vox * 4); M((void**)&b->p, b->n_vox * 4); M((void**)&b->q, b->n_vox * 4);
-    M((void**)&b->tmp, b->n_rays * 4);
+    M((void**)&b->tmp, woff[n_plans] * 4);
     M((void**)&b->S, sizeof(BatchScal) * n_plans);
     M((void**)&b->partials, sizeof(double) * b->n_vec_chunks);
     M((void**)&b->tickets, sizeof(unsigned) * n_plans);
@@ -434,16 +521,27 @@ extern "C" int fl_batch_layout(const fl_batch* b, int64_t* vox_offsets, int64_t*
     return fl_set_error(FL_OK, "");
 }
 
-static int batch_fwd(fl_batch* b, const float* x, float* y, int cr_power, const BatchScal* S,
-                     cudaStream_t s)
+// ypack: y is the batch's scratch (slice offsets woff), turn slices packed per
+// orbit, as batch_adj_w reads it; else the caller's sinogram (offsets yoff)
+static int batch_fwd(fl_batch* b, const float* x, float* y, int cr_power, int ypack,
+                     const BatchScal* S, cudaStream_t s)
 {
-    k_batch_fwd<<<b->n_ray_chunks, kRayChunk, 0, s>>>(x, y, b->d_sl, b->d_rays, cr_power, S);
+    if (b->n_ray_chunks)
+        k_batch_fwd<<<b->n_ray_chunks, kRayChunk, 0, s>>>(x, y, b->d_sl, b->d_rays, cr_power,
+                                                          ypack, S);
+    if (b->n_ray_t_chunks)
+        k_batch_fwd_turn<<<b->n_ray_t_chunks, kFanBlock, 0, s>>>(
+            x, y, b->d_sl, b->d_rays_t, cr_power, ypack, S);
     return fl_check_launch("batched forward");
 }
 
 static int batch_adj_w(fl_batch* b, const float* yw, float* x, const BatchScal* S, cudaStream_t s)
 {
-    k_batch_adj<<<b->n_pix_chunks, kPixChunk, 0, s>>>(x, yw, b->d_sl, b->d_pix, S);
+    if (b->n_pix_chunks)
+        k_batch_adj<<<b->n_pix_chunks, kPixChunk, 0, s>>>(x, yw, b->d_sl, b->d_pix, S);
+    if (b->n_pix_t_chunks)
+        k_batch_adj_turn<<<b->n_pix_t_chunks, dim3(kFanX, kTurnGroups), 0, s>>>(
+            x, yw, b->d_sl, b->d_pix_t, S);
     return fl_check_launch("batched adjoint");
 }
 
@@ -451,7 +549,7 @@ extern "C" int fl_batch_forward(fl_batch* b, const float* x, float* y, void* str
 {
     FL_RANGE("fl_batch_forward");
     if (!b || !x || !y) return fl_set_error(FL_ERR_INVALID, "fl_batch_forward: null argument");
-    int st = batch_fwd(b, x, y, 1, nullptr, (cudaStream_t)stream);
+    int st = batch_fwd(b, x, y, 1, 0, nullptr, (cudaStream_t)stream);
     return st ? st : fl_set_error(FL_OK, "");
 }
 
@@ -461,7 +559,7 @@ extern "C" int fl_batch_adjoint(fl_batch* b, const float* y, float* x, void* str
     FL_RANGE("fl_batch_adjoint");
     if (!b || !x || !y) return fl_set_error(FL_ERR_INVALID, "fl_batch_adjoint: null argument");
     cudaStream_t s = (cudaStream_t)stream;
-    k_batch_weight<<<b->n_ray_chunks, kRayChunk, 0, s>>>(b->tmp, y, b->d_sl, b->d_rays);
+    k_batch_weight<<<b->n_wray_chunks, kRayChunk, 0, s>>>(b->tmp, y, b->d_sl, b->d_wrays);
     int st = fl_check_launch("batched weighting");
     if (!st) st = batch_adj_w(b, b->tmp, x, nullptr, s);
     return st ? st : fl_set_error(FL_OK, "");
@@ -469,7 +567,7 @@ extern "C" int fl_batch_adjoint(fl_batch* b, const float* y, float* x, void* str
 
 static int batch_iteration(fl_batch* b, float* u, float lam, double tol, cudaStream_t s)
 {
-    int st = batch_fwd(b, b->p, b->tmp, 2, b->S, s);
+    int st = batch_fwd(b, b->p, b->tmp, 2, 1, b->S, s);
     if (!st) st = batch_adj_w(b, b->tmp, b->q, b->S, s);
     if (st) return st;
     const int g = b->n_vec_chunks;
@@ -494,7 +592,7 @@ extern "C" int fl_batch_cgls(fl_batch* b, const float* rhs, float* u, float lam,
     FL_CUDA(cudaStreamWaitEvent(s, b->ev0, 0));
     const float* q0 = nullptr;
     if (!(flags & FL_CGLS_ZERO_START)) {
-        if ((st = batch_fwd(b, u, b->tmp, 2, nullptr, s))) return st;
+        if ((st = batch_fwd(b, u, b->tmp, 2, 1, nullptr, s))) return st;
         if ((st = batch_adj_w(b, b->tmp, b->q, nullptr, s))) return st;
         q0 = b->q;
     }

@@ -181,68 +181,18 @@ k_fwd_fan(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restri
     Store<TY>::st(y + r, out);
 }
 
-// Fan forward of a turn plan (G = 2 or 4, one frame): kFanLanes threads per
-// ray (iv < nv/G, ia), each walking one part of it (walk_fan), their sums
-// added in part order; the walk also yields the rays of views iv + j nv/G at
-// the same column, all with the walked ray's c_r. ypack writes the
-// adjoint-input layout of these plans: the G values of ray (iv, ia)'s orbit
-// side by side at G (iv na + ia) + j (k_weight_fan_packed). Fan launches
-// have few rays: the parts give the GPU kFanLanes times the threads, each
-// with that fraction of the walk. A block is 32 neighbouring rays x
-// kFanLanes parts, part k in warp k, so a warp's gathers follow 32
-// neighbouring rays.
-constexpr int kFanLanes = 8;
-
-template <typename TX, typename TY, int G>
-__global__ void __launch_bounds__(32 * kFanLanes, 4)
+// Fan forward of a turn plan (G = 2 or 4, one frame): blocks of kFanBlock
+// threads, L parts per ray (fan_turn_forward_block, fan_turn_lanes).
+template <typename TX, typename TY, int G, int L>
+__global__ void __launch_bounds__(kFanBlock, 4)
 k_fwd_fan_turn(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restrict__ col,
                const float* __restrict__ colr, int nx, int ny, int na, int nv, float scale,
                int cr_power, const int* __restrict__ skip, const float* __restrict__ xscale,
                int ypack)
 {
     if (skip && *skip) return;                 // uniform (one flag for the launch)
-    const int gv = nv / G;
-    const int tx = threadIdx.x, lane = threadIdx.y;
-    const long long r = (long long)blockIdx.x * 32 + tx;
-    const bool ray = r < (long long)na * gv;
-    float acc[G];
-#pragma unroll
-    for (int j = 0; j < G; j++) acc[j] = 0.0f;
-    if (ray) {
-        const ColEntry ce = col[r];
-        walk_fan<TX, G, kFanLanes>(X, ce.inv_x, ce.off_x, ce.inv_y, ce.off_y, nx, ny, acc,
-                                   (long long)nx * ny, lane);
-    }
-    // part k of ray tx is warp k's lane tx: warp 0 adds them in order
-    __shared__ float part[kFanLanes][G][32];
-#pragma unroll
-    for (int j = 0; j < G; j++) part[lane][j][tx] = acc[j];
-    __syncthreads();
-    if (!ray || lane != 0) return;
-#pragma unroll
-    for (int j = 0; j < G; j++) {
-        float sum = part[0][j][tx];
-#pragma unroll
-        for (int k = 1; k < kFanLanes; k++) sum += part[k][j][tx];
-        acc[j] = sum;
-    }
-    const int iv = (int)(r / na), ia = (int)(r - (long long)iv * na);
-    const float cr = ray_cr(scale, colr[r], 0.0f);
-    float o[G];
-#pragma unroll
-    for (int j = 0; j < G; j++) {
-        float a = acc[j];
-        if (xscale) a *= *xscale;
-        o[j] = cr * a;
-        if (cr_power == 2) o[j] = cr * o[j];
-    }
-    if (ypack) {
-#pragma unroll
-        for (int j = 0; j < G; j += 2) Store<TY>::st2(y + G * r + j, o[j], o[j + 1]);
-    } else {
-#pragma unroll
-        for (int j = 0; j < G; j++) Store<TY>::st(y + ((long long)iv + (long long)j * gv) * na + ia, o[j]);
-    }
+    fan_turn_forward_block<TX, TY, G, L>(X, y, col, colr, nx, ny, na, nv, scale, cr_power,
+                                         xscale, ypack, (long long)blockIdx.x * (kFanBlock / L));
 }
 
 __global__ void __launch_bounds__(128)
@@ -411,7 +361,6 @@ __global__ void k_weight(float* __restrict__ yw, const TY* __restrict__ y,
 // gathers view group g and group 0 writes the combined sums, so that four
 // times as many threads share the views. Large images (P = 2): blocks of 128
 // threads, each gathering all groups itself. Both give the same bits.
-constexpr int kFanX = 32;
 
 template <typename TX, int P, bool GROUPED>
 __global__ void __launch_bounds__(128)
@@ -448,40 +397,18 @@ k_adj_fan(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __re
                 Store<TX>::st(xf + (long long)(iy0 + j) * nx + ix0 + i, acc[j][i]);
 }
 
-// Fan adjoint of a turn plan (G = 2 or 4, one frame): thread (x, g) of a
-// block of kFanX x NG threads takes the primary pixel (ix, iy) -- G = 2:
-// iy < ny/2; G = 4: ix, iy < n/2 -- with its turns, over view group g of the
-// views iv < nv/G (fan_turn_gather). The NG groups' sums meet in shared
-// memory and are added in the order g = 0, 1, ...; group 0 stores the G
-// pixels.
-template <typename TX, int G, int NG>
-__global__ void __launch_bounds__(kFanX * NG)
+// Fan adjoint of a turn plan (G = 2 or 4, one frame): blocks of kFanX P x P
+// blocks of primary pixels x kTurnGroups view groups (fan_turn_adjoint_block;
+// the bits do not depend on P).
+template <typename TX, int G, int P>
+__global__ void __launch_bounds__(kFanX * kTurnGroups)
 k_adj_fan_turn(TX* __restrict__ X, const float* __restrict__ ywp,
                const ColEntry* __restrict__ col, const ViewEntry* __restrict__ view, DetGrid D,
                int nx, int ny, int na, int nv, const int* __restrict__ skip)
 {
     if (skip && *skip) return;                 // uniform (one flag for the launch)
-    const int hx = G == 2 ? nx : nx / 2;
-    const int ix = blockIdx.x * kFanX + threadIdx.x, iy = blockIdx.y;
-    const int tx = threadIdx.x, g = threadIdx.y;
-    float acc[G];
-#pragma unroll
-    for (int j = 0; j < G; j++) acc[j] = 0.0f;
-    if (ix < hx) fan_turn_gather<G>(acc, ywp, col, view, D, ix, iy, nx, ny, na, nv, g, NG);
-    __shared__ float part[NG][G][kFanX];
-#pragma unroll
-    for (int j = 0; j < G; j++) part[g][j][tx] = acc[j];
-    __syncthreads();
-    if (g != 0 || ix >= hx) return;
-    int px[G], py[G];
-    fan_turn_pixels<G>(ix, iy, nx, ny, px, py);
-#pragma unroll
-    for (int j = 0; j < G; j++) {
-        float sum = part[0][j][tx];
-#pragma unroll
-        for (int k = 1; k < NG; k++) sum += part[k][j][tx];
-        Store<TX>::st(X + (long long)py[j] * nx + px[j], sum);
-    }
+    fan_turn_adjoint_block<TX, G, P>(X, ywp, col, view, D, nx, ny, na, nv,
+                                     blockIdx.x * kFanX * P, blockIdx.y * P);
 }
 
 // ---------------------------------------------------------------------------
@@ -983,15 +910,17 @@ void launch_fwd(fl_plan* p, const void* x, void* y, int cr_power, const int* ski
     } else if (fl_plan_turns(p) > 1) {
         const int G = fl_plan_turns(p);
         const long long nr = (long long)s.na * (s.nv / G);
-        const dim3 blk(32, kFanLanes);
-        if (G == 4)
-            k_fwd_fan_turn<TX, TY, 4><<<fl_div_up(nr, 32), blk, 0, st>>>(
-                (const TX*)x, (TY*)y, p->d_col, p->d_colr, s.nx, s.ny, s.na, s.nv, s.scale,
-                cr_power, skip, xscale, yfold);
-        else
-            k_fwd_fan_turn<TX, TY, 2><<<fl_div_up(nr, 32), blk, 0, st>>>(
-                (const TX*)x, (TY*)y, p->d_col, p->d_colr, s.nx, s.ny, s.na, s.nv, s.scale,
-                cr_power, skip, xscale, yfold);
+        const bool split = fan_turn_lanes(nr) > 1;
+        const unsigned g = fl_div_up(nr, split ? kFanBlock / kFanLanes : kFanBlock);
+#define FL_FAN_TURN(GG, LL)                                                                  \
+    k_fwd_fan_turn<TX, TY, GG, LL><<<g, kFanBlock, 0, st>>>(                                 \
+        (const TX*)x, (TY*)y, p->d_col, p->d_colr, s.nx, s.ny, s.na, s.nv, s.scale, cr_power, \
+        skip, xscale, yfold)
+        if (G == 4 && split) FL_FAN_TURN(4, kFanLanes);
+        else if (G == 4) FL_FAN_TURN(4, 1);
+        else if (split) FL_FAN_TURN(2, kFanLanes);
+        else FL_FAN_TURN(2, 1);
+#undef FL_FAN_TURN
     } else {
         long long nr = (long long)s.na * s.nv;
         k_fwd_fan<TX, TY><<<fl_div_up(nr, 128), 128, 0, st>>>(
@@ -1046,14 +975,26 @@ void launch_adj(fl_plan* p, const float* yw, void* x, const int* skip, int xfold
                 (TX*)x, yw, p->d_col, p->d_rowz, p->d_view, p->d_idY, p->d_Nv, p->tmp_size, G,
                 s.nx, s.ny, s.nz, s.na, s.nb, s.dz, zruns, skip, 0);
         }
-    } else if (fl_plan_turns(p) == 4) {
-        dim3 grid(fl_div_up(s.nx / 2, kFanX), s.ny / 2);
-        k_adj_fan_turn<TX, 4, kTurnGroups><<<grid, dim3(kFanX, kTurnGroups), 0, st>>>(
-            (TX*)x, yw, p->d_col, p->d_view, G, s.nx, s.ny, s.na, s.nv, skip);
-    } else if (fl_plan_turns(p) == 2) {
-        dim3 grid(fl_div_up(s.nx, kFanX), s.ny / 2);
-        k_adj_fan_turn<TX, 2, kTurnGroups><<<grid, dim3(kFanX, kTurnGroups), 0, st>>>(
-            (TX*)x, yw, p->d_col, p->d_view, G, s.nx, s.ny, s.na, s.nv, skip);
+    } else if (fl_plan_turns(p) > 1) {
+        // 2 x 2 primary blocks once there are at least 4 waves of them, else
+        // one primary pixel per thread (the same bits)
+        const int T = fl_plan_turns(p);
+        const int hx = T == 2 ? s.nx : s.nx / 2, hy = s.ny / 2;
+        const dim3 blk(kFanX, kTurnGroups);
+        const dim3 g2(fl_div_up(hx, 2 * kFanX), fl_div_up(hy, 2)), g1(fl_div_up(hx, kFanX), hy);
+        const bool two = (long long)g2.x * g2.y >= 4LL * 152;
+        if (T == 4 && two)
+            k_adj_fan_turn<TX, 4, 2><<<g2, blk, 0, st>>>((TX*)x, yw, p->d_col, p->d_view, G, s.nx,
+                                                         s.ny, s.na, s.nv, skip);
+        else if (T == 4)
+            k_adj_fan_turn<TX, 4, 1><<<g1, blk, 0, st>>>((TX*)x, yw, p->d_col, p->d_view, G, s.nx,
+                                                         s.ny, s.na, s.nv, skip);
+        else if (two)
+            k_adj_fan_turn<TX, 2, 2><<<g2, blk, 0, st>>>((TX*)x, yw, p->d_col, p->d_view, G, s.nx,
+                                                         s.ny, s.na, s.nv, skip);
+        else
+            k_adj_fan_turn<TX, 2, 1><<<g1, blk, 0, st>>>((TX*)x, yw, p->d_col, p->d_view, G, s.nx,
+                                                         s.ny, s.na, s.nv, skip);
     } else {
         // 2 x 2 pixel blocks, one thread each, once there are at least 4 waves
         // of 128-thread blocks; else one pixel per view group

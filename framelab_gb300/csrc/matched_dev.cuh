@@ -594,23 +594,55 @@ __device__ __forceinline__ void fan_turn_pixels(int ix, int iy, int nx, int ny, 
 // View groups of the fan turn adjoint (k_adj_fan_turn).
 constexpr int kTurnGroups = 8;
 
-// Fan adjoint of a turn plan (G = 2 or 4, one frame): pixel p0 = (ix, iy)
-// and its turns p_k over the views iv = g, g + NG, ... < nv/G of view group
-// g. In view iv the weight of p_k and ray (iv, ia), from the same crossing
-// table as the walk, multiplies the value of ray (iv + j nv/G, ia) into
-// p_{k+j mod G}: A[(iv + j nv/G, a), R^j p] = A[(iv, a), p]. ywp is the
-// packed sinogram (G values per (iv < nv/G, ia)). A pixel's sum runs over the
-// group's views in order, per view over k = 0, 1, ... and the columns in
-// increasing order; only rays with w > 0 add to it.
-template <int G>
-__device__ __forceinline__ void fan_turn_gather(float (&acc)[G], const float* __restrict__ ywp,
+// Turn k of a P x P block of primary pixels with lower corner (ix0, iy0):
+// R^k maps the block onto the P x P block with lower corner (X0, Y0) (the
+// turns of walk_fan's R), and primary pixel (ix0 + i, iy0 + j) onto that
+// block's pixel (X0 + a, Y0 + b). turn_local gives (i, j) for (a, b).
+template <int G, int P>
+__device__ __forceinline__ void turn_corner(int k, int ix0, int iy0, int nx, int ny, int& X0,
+                                            int& Y0)
+{
+    if (k == 0) { X0 = ix0; Y0 = iy0; }
+    else if (G == 2 || k == 2) { X0 = nx - ix0 - P; Y0 = ny - iy0 - P; }
+    else if (k == 1) { X0 = nx - iy0 - P; Y0 = ix0; }
+    else { X0 = iy0; Y0 = nx - ix0 - P; }
+}
+
+template <int G, int P>
+__host__ __device__ constexpr int turn_local_i(int k, int a, int b)
+{
+    return k == 0 ? a : (G == 2 || k == 2) ? P - 1 - a : k == 1 ? b : P - 1 - b;
+}
+
+template <int G, int P>
+__host__ __device__ constexpr int turn_local_j(int k, int a, int b)
+{
+    return k == 0 ? b : (G == 2 || k == 2) ? P - 1 - b : k == 1 ? P - 1 - a : a;
+}
+
+// Fan adjoint of a turn plan (G = 2 or 4, one frame): the P x P block of
+// primary pixels at (ix0, iy0) and its turns, over the views iv = g, g + NG,
+// ... < nv/G of view group g. In view iv the weight of a turned pixel R^k p
+// and ray (iv, ia), from the same crossing table as the walk, multiplies the
+// value of ray (iv + j nv/G, ia) into R^{k+j mod G} p: A[(iv + j nv/G, a),
+// R^j p] = A[(iv, a), p]. acc[m][j][i] collects turn m of primary pixel
+// (ix0 + i, iy0 + j). ywp is the packed sinogram (G values per
+// (iv < nv/G, ia)). A pixel's sum runs over the group's views in order, per
+// view over k = 0, 1, ... and the columns in increasing order; only rays
+// with w > 0 add to it. The turned block's column window contains each of
+// its pixels' own windows (0.02 columns of slack against the FP32 error of
+// w), so the sums do not depend on P.
+template <int G, int P>
+__device__ __forceinline__ void fan_turn_gather(float (&acc)[G][P][P],
+                                                const float* __restrict__ ywp,
                                                 const ColEntry* __restrict__ col,
                                                 const ViewEntry* __restrict__ view,
-                                                const DetGrid& D, int ix, int iy, int nx, int ny,
-                                                int na, int nv, int g, int NG)
+                                                const DetGrid& D, int ix0, int iy0, int nx,
+                                                int ny, int na, int nv, int g, int NG)
 {
-    int px[G], py[G];
-    fan_turn_pixels<G>(ix, iy, nx, ny, px, py);
+    int X0[G], Y0[G];
+#pragma unroll
+    for (int k = 0; k < G; k++) turn_corner<G, P>(k, ix0, iy0, nx, ny, X0[k], Y0[k]);
     const int gv = nv / G;
     for (int iv = g; iv < gv; iv += NG) {
         const ViewEntry ve = view[iv];
@@ -619,19 +651,20 @@ __device__ __forceinline__ void fan_turn_gather(float (&acc)[G], const float* __
 #pragma unroll
         for (int k = 0; k < G; k++) {
             int lo, hi; float dmin, dmax;
-            column_window(D, ve.c, ve.s, (float)(px[k] - nx / 2), (float)(py[k] - ny / 2), 1.0f,
-                          1.0f, na, lo, hi, dmin, dmax);
-            const float fx0 = (float)px[k], fx1 = (float)(px[k] + 1);
-            const float fy0 = (float)py[k], fy1 = (float)(py[k] + 1);
+            column_window(D, ve.c, ve.s, (float)(X0[k] - nx / 2), (float)(Y0[k] - ny / 2),
+                          (float)P, (float)P, na, lo, hi, dmin, dmax);
+            float fx[P + 1], fy[P + 1];
+#pragma unroll
+            for (int q = 0; q <= P; q++) { fx[q] = (float)(X0[k] + q); fy[q] = (float)(Y0[k] + q); }
             for (int ia = lo; ia <= hi; ia++) {
                 if (!FL_IN(ia, na)) continue;
                 const ColEntry ce = cv[ia];
-                const float ax0 = fmaf(fx0, ce.inv_x, ce.off_x), ax1 = fmaf(fx1, ce.inv_x, ce.off_x);
-                const float ay0 = fmaf(fy0, ce.inv_y, ce.off_y), ay1 = fmaf(fy1, ce.inv_y, ce.off_y);
-                const float l = fmaxf(fminf(ax0, ax1), fminf(ay0, ay1));
-                const float h = fminf(fmaxf(ax0, ax1), fmaxf(ay0, ay1));
-                const float w = h - l;
-                if (!(w > 0.0f)) continue;
+                float ax[P + 1], ay[P + 1];
+#pragma unroll
+                for (int q = 0; q <= P; q++) {
+                    ax[q] = fmaf(fx[q], ce.inv_x, ce.off_x);
+                    ay[q] = fmaf(fy[q], ce.inv_y, ce.off_y);
+                }
                 float t[G];
                 if constexpr (G == 4) {
                     const float4 u = __ldg(reinterpret_cast<const float4*>(yv + 4 * ia));
@@ -641,10 +674,157 @@ __device__ __forceinline__ void fan_turn_gather(float (&acc)[G], const float* __
                     t[0] = u.x; t[1] = u.y;
                 }
 #pragma unroll
-                for (int j = 0; j < G; j++) acc[(k + j) % G] = fmaf(w, t[j], acc[(k + j) % G]);
+                for (int b = 0; b < P; b++)
+#pragma unroll
+                    for (int a = 0; a < P; a++) {
+                        const float l = fmaxf(fminf(ax[a], ax[a + 1]), fminf(ay[b], ay[b + 1]));
+                        const float h = fminf(fmaxf(ax[a], ax[a + 1]), fmaxf(ay[b], ay[b + 1]));
+                        const float w = h - l;
+                        if (!(w > 0.0f)) continue;
+                        const int i = turn_local_i<G, P>(k, a, b), j = turn_local_j<G, P>(k, a, b);
+#pragma unroll
+                        for (int m = 0; m < G; m++)
+                            acc[(k + m) % G][j][i] = fmaf(w, t[m], acc[(k + m) % G][j][i]);
+                    }
             }
         }
     }
+}
+
+// Pixels per block row of the grouped fan backprojections.
+constexpr int kFanX = 32;
+// Parts per ray of the fan turn forward: kFanLanes for scans with fewer
+// than kFanSplitWalks walks (nv/G views x na columns), else 1. A function of
+// the scan alone, so a plan and a batch holding it choose alike.
+constexpr int kFanLanes = 8;
+constexpr long long kFanSplitWalks = 1LL << 16;
+constexpr int kFanBlock = 256;       // threads per block of the fan turn forward
+
+__host__ __device__ inline int fan_turn_lanes(long long walks)
+{
+    return walks < kFanSplitWalks ? kFanLanes : 1;
+}
+
+// One block of kFanBlock threads of the fan turn forward (G = 2 or 4, one
+// frame): L threads per ray (iv < nv/G, ia), each walking one part of it
+// (walk_fan), their sums added in part order; the walk also yields the rays
+// of views iv + j nv/G at the same column, all with the walked ray's c_r.
+// The block holds the rays r0, r0 + 1, ... : with L parts, kFanBlock / L
+// rays, part k in warp(s) k, so a warp's gathers follow neighbouring rays.
+// Small fan launches have few rays: the parts give the GPU L times the
+// threads, each with that fraction of the walk. ypack writes the
+// adjoint-input layout of these plans: the G values of ray (iv, ia)'s orbit
+// side by side at G (iv na + ia) + j. Every thread of the block must call it
+// (it synchronises the block).
+template <typename TX, typename TY, int G, int L>
+__device__ __forceinline__ void fan_turn_forward_block(const TX* __restrict__ X,
+                                                       TY* __restrict__ y,
+                                                       const ColEntry* __restrict__ col,
+                                                       const float* __restrict__ colr, int nx,
+                                                       int ny, int na, int nv, float scale,
+                                                       int cr_power,
+                                                       const float* __restrict__ xscale,
+                                                       int ypack, long long r0)
+{
+    constexpr int NR = kFanBlock / L;          // rays per block
+    const int gv = nv / G;
+    const int tx = threadIdx.x % NR, lane = threadIdx.x / NR;
+    const long long r = r0 + tx;
+    const bool ray = r < (long long)na * gv;
+    float acc[G];
+#pragma unroll
+    for (int j = 0; j < G; j++) acc[j] = 0.0f;
+    if (ray) {
+        const ColEntry ce = col[r];
+        walk_fan<TX, G, L>(X, ce.inv_x, ce.off_x, ce.inv_y, ce.off_y, nx, ny, acc,
+                           (long long)nx * ny, lane);
+    }
+    if constexpr (L > 1) {
+        // part k of ray tx is thread k NR + tx: the first NR threads add them in order
+        __shared__ float part[L][G][NR];
+#pragma unroll
+        for (int j = 0; j < G; j++) part[lane][j][tx] = acc[j];
+        __syncthreads();
+        if (lane != 0) return;
+#pragma unroll
+        for (int j = 0; j < G; j++) {
+            float sum = part[0][j][tx];
+#pragma unroll
+            for (int k = 1; k < L; k++) sum += part[k][j][tx];
+            acc[j] = sum;
+        }
+    }
+    if (!ray) return;
+    const int iv = (int)(r / na), ia = (int)(r - (long long)iv * na);
+    const float cr = ray_cr(scale, colr[r], 0.0f);
+    float o[G];
+#pragma unroll
+    for (int j = 0; j < G; j++) {
+        float a = acc[j];
+        if (xscale) a *= *xscale;
+        o[j] = cr * a;
+        if (cr_power == 2) o[j] = cr * o[j];
+    }
+    if (ypack) {
+#pragma unroll
+        for (int j = 0; j < G; j += 2) Store<TY>::st2(y + G * r + j, o[j], o[j + 1]);
+    } else {
+#pragma unroll
+        for (int j = 0; j < G; j++)
+            Store<TY>::st(y + ((long long)iv + (long long)j * gv) * na + ia, o[j]);
+    }
+}
+
+// One block of the fan turn backprojection (G = 2 or 4, one frame): thread
+// (x, g) of a block of kFanX x kTurnGroups threads takes the P x P block of
+// primary pixels at (ix0 + P x, iy0) -- G = 2: rows y < ny/2; G = 4: x, y <
+// n/2 -- with its turns, over view group g of the views iv < nv/G
+// (fan_turn_gather). The groups' sums meet in shared memory and are added in
+// the order g = 0, 1, ...; group 0 stores the pixels. Every thread of the
+// block must call it (it synchronises the block).
+template <typename TX, int G, int P>
+__device__ __forceinline__ void fan_turn_adjoint_block(TX* __restrict__ X,
+                                                       const float* __restrict__ ywp,
+                                                       const ColEntry* __restrict__ col,
+                                                       const ViewEntry* __restrict__ view,
+                                                       const DetGrid& D, int nx, int ny, int na,
+                                                       int nv, int ix0, int iy0)
+{
+    const int hx = G == 2 ? nx : nx / 2, hy = ny / 2;
+    const int tx = threadIdx.x, g = threadIdx.y, bx = ix0 + P * tx;
+    float acc[G][P][P];
+#pragma unroll
+    for (int m = 0; m < G; m++)
+#pragma unroll
+        for (int j = 0; j < P; j++)
+#pragma unroll
+            for (int i = 0; i < P; i++) acc[m][j][i] = 0.0f;
+    if (bx < hx)
+        fan_turn_gather<G, P>(acc, ywp, col, view, D, bx, iy0, nx, ny, na, nv, g, kTurnGroups);
+    __shared__ float part[kTurnGroups][G * P * P][kFanX];
+#pragma unroll
+    for (int m = 0; m < G; m++)
+#pragma unroll
+        for (int j = 0; j < P; j++)
+#pragma unroll
+            for (int i = 0; i < P; i++) part[g][(m * P + j) * P + i][tx] = acc[m][j][i];
+    __syncthreads();
+    if (g != 0) return;
+#pragma unroll
+    for (int j = 0; j < P; j++)
+#pragma unroll
+        for (int i = 0; i < P; i++) {
+            if (bx + i >= hx || iy0 + j >= hy) continue;      // not a primary pixel
+            int px[G], py[G];
+            fan_turn_pixels<G>(bx + i, iy0 + j, nx, ny, px, py);
+#pragma unroll
+            for (int m = 0; m < G; m++) {
+                float sum = part[0][(m * P + j) * P + i][tx];
+#pragma unroll
+                for (int k = 1; k < kTurnGroups; k++) sum += part[k][(m * P + j) * P + i][tx];
+                Store<TX>::st(X + (long long)py[m] * nx + px[m], sum);
+            }
+        }
 }
 
 // The kFanGroups view groups of a pixel block are the threads (x, g) of a

@@ -69,6 +69,14 @@ def main():
     xb = torch.rand(B.n_vox, device="cuda")
     B.adjoint(B.forward(xb))
     B.cgls(B.adjoint(B.forward(xb)), iters=3)
+    # a batch with half- and quarter-turn slices (views evenly over a full turn)
+    sl = [(32, 32, 64, 20), (24, 40, 61, 14), (40, 40, 81, 9), (20, 36, 41, 12)]
+    B = FanBatch([G.fan_para(nx, ny, nd, nv, L=(2.0 * nx / max(nx, ny), 2.0 * ny / max(nx, ny)))
+                  for nx, ny, nd, nv in sl])
+    assert B.turns == [4, 2, 1, 2], B.turns
+    xb = torch.rand(B.n_vox, device="cuda")
+    B.adjoint(B.forward(xb))
+    B.cgls(B.adjoint(B.forward(xb)), iters=3)
     # the class mirror's default scanner geometry
     cb = Operators.ConeBeamScanner("circle", 36, 32, 10, model="matched")
     u = DataTypes.ObjectData(3, np.ones((16, 16, 16), np.float32), [2, 2, 2])
