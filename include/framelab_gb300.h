@@ -343,8 +343,11 @@ int fl_cgls_solve_host(fl_cgls *cg, const float *b_host, float *u_host, float la
  * A batch projects and solves many independent single-frame fan-beam scans of
  * different sizes at once (matched model): images and sinograms of all slices
  * are concatenated in plan order (offsets from fl_batch_layout) and every
- * operator is one launch over all slices. Each slice's forward/adjoint result
- * is bit-identical to its own plan's. The plans must outlive the batch.
+ * operator is one launch over all slices (two when some slices' plans use
+ * FL_OPT_ROT_MIRROR / FL_OPT_QUARTER_TURN: those run the turn kernels). Each
+ * slice's forward/adjoint result is bit-identical to its own plan's, with the
+ * plan's options as they were at fl_batch_create. The plans must outlive the
+ * batch.
  * Replaces looping the reference's per-slice Ax_fan_mf / Atx_fan_mf calls
  * (FanBeamScanner/apply.m:11-20, applyAdjoint.m:21-29) and solveCGLS.m:6-31
  * over the slices. */
@@ -360,7 +363,8 @@ int fl_batch_adjoint(fl_batch *b, const float *y, float *x, void *stream);
  * guess in (ignored with FL_CGLS_ZERO_START), result out (device).
  * gamma_history (host, optional): [n_plans * iters], row i = slice i's gamma
  * after each iteration (0 after it stopped); iters_done (host, optional):
- * [n_plans]. One iteration is a replayed CUDA graph of 5 launches. */
+ * [n_plans]. One iteration is a replayed CUDA graph of 5 launches (7 when
+ * the batch mixes turn and general slices). */
 int fl_batch_cgls(fl_batch *b, const float *rhs, float *u, float lam, int32_t iters, double tol,
                   int32_t flags, double *gamma_history, int32_t *iters_done, void *stream);
 
