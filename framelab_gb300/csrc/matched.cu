@@ -669,10 +669,12 @@ __device__ __forceinline__ void adj_rows_oct(float2 (&a0)[TZ], float2 (&a1)[TZ],
         for (int ib = blo; ib <= bhi; ib++) {
             if (!FL_IN(ib, nb)) continue;
             const float2 re = rv[ib];
-            const float4* q8 = reinterpret_cast<const float4*>(y8 + 8 * (long long)ib * na);
-            const float4 u01 = __ldg(q8), u23 = __ldg(q8 + 1);
-            const float2 t0 = make_float2(u01.x, u01.y), t1 = make_float2(u01.z, u01.w);
-            const float2 t2 = make_float2(u23.x, u23.y), t3 = make_float2(u23.z, u23.w);
+            // the orbit's 8 values in one 32-byte load (orbits are 32-byte aligned)
+            float2 t0, t1, t2, t3;
+            asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                : "=f"(t0.x), "=f"(t0.y), "=f"(t1.x), "=f"(t1.y), "=f"(t2.x), "=f"(t2.y),
+                  "=f"(t3.x), "=f"(t3.y)
+                : "l"(y8 + 8 * (long long)ib * na));
             const float2 az = __ffma2_rn(make_float2(fk0, fk1), make_float2(re.x, re.x),
                                          make_float2(re.y, re.y));
             float l2, h2;
