@@ -83,7 +83,7 @@ def parse():
     ap.add_argument("--workload", default="cone512", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--only", default="",
-                    help="comma list of legs: mixed,plain,e2e,kernels,seq,grad")
+                    help="comma list of legs: mixed,plain,hostplain,e2e,kernels,seq,grad")
     return ap.parse_args()
 
 
@@ -366,7 +366,7 @@ class Ctx:
         self.stream = torch.cuda.current_stream()
         self.K, self.W = a.steps, a.warmup
         self.legs = (set(a.only.split(",")) if a.only else
-                     {"mixed", "plain", "e2e", "kernels", "seq", "grad"})
+                     {"mixed", "plain", "hostplain", "e2e", "kernels", "seq", "grad"})
 
     def barrier(self):
         if self.world > 1:
@@ -456,6 +456,53 @@ def time_pair(ctx, P, x, reps=3):
     return tf / reps, ta / reps, y, xo
 
 
+def host_structure_cgls(ctx, P, b, lam, cg_g, detail, iters=2):
+    """The reference's plain FP32 GPU structure with this library's projectors:
+    solveCGLS.m (u0 = 0) with its algebra on host FP32 arrays (FP32 inner
+    products, as MATLAB's on single arrays), and every A / A^T call through
+    host buffers -- its input copied to the device and its output back, as
+    the reference's mex GPU projectors do for MATLAB arrays. Timed over
+    `iters` iterations after one untimed."""
+    import time
+    torch = ctx.torch
+    bh = b.cpu().numpy().astype(np.float32)
+
+    def normal(v):
+        y = P.forward(torch.from_numpy(v).to(ctx.dev)).cpu()
+        q = P.adjoint(y.to(ctx.dev)).reshape(-1).cpu().numpy()
+        return q + np.float32(lam) * v if lam else q
+
+    def cgls(n):
+        u = np.zeros_like(bh)
+        r = bh.copy()
+        p = r.copy()
+        gamma = float(np.dot(r, r))
+        for _ in range(n):
+            q = normal(p)
+            alpha = gamma / float(np.dot(p, q))
+            u += np.float32(alpha) * p
+            r -= np.float32(alpha) * q
+            g1 = float(np.dot(r, r))
+            p = r + np.float32(g1 / gamma) * p
+            gamma = g1
+        return u
+
+    cgls(1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    u = cgls(iters)
+    torch.cuda.synchronize()
+    t = (time.perf_counter() - t0) / iters
+    u_ref = cg_g.solve(b, lam=lam, iters=iters).reshape(-1).cpu().numpy()
+    out = {"host_structure_iter_per_s": 1.0 / t,
+           "host_structure_vs_graph_rel_l2": float(np.linalg.norm(u - u_ref) /
+                                                   max(np.linalg.norm(u_ref), 1e-30)),
+           "graph_over_host_structure": detail["graph_iter_per_s_per_gpu"] * t}
+    if "mixed_iter_per_s" in detail:
+        out["mixed_over_host_structure"] = detail["mixed_iter_per_s"] * t
+    return out
+
+
 def run_single(ctx, name, w, p):
     """cone / fan: CGLS on one scan (graph headline, mixed, plain, e2e, kernels)."""
     torch = ctx.torch
@@ -500,6 +547,8 @@ def run_single(ctx, name, w, p):
                                       if "mixed_iter_per_s" in detail else None)
         detail["graph_vs_plain_rel_l2"] = ctx.rel(u_g, u_p)
         del cg_p, u_p
+    if "hostplain" in ctx.legs:
+        detail.update(host_structure_cgls(ctx, P, b, lam, cg_g, detail))
     e2e = None
     if "e2e" in ctx.legs:
         bh = torch.empty(b.numel(), dtype=torch.float32, pin_memory=True)
