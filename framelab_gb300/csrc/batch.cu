@@ -352,6 +352,8 @@ struct fl_batch {
     int hist_cap;
     cudaStream_t cs;
     cudaEvent_t ev0, ev1;
+    cudaStream_t cs2;                  // the turn slices' branch of a forward / adjoint
+    cudaEvent_t evf, evj;              // its fork and join
     cudaGraphExec_t exec;
     float* cap_u;
     float cap_lam;
@@ -366,6 +368,9 @@ static void batch_free(fl_batch* b)
         if (q) cudaFree(q);
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->cs) cudaStreamDestroy(b->cs);
+    if (b->cs2) cudaStreamDestroy(b->cs2);
+    if (b->evf) cudaEventDestroy(b->evf);
+    if (b->evj) cudaEventDestroy(b->evj);
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
 }
@@ -473,6 +478,7 @@ extern "C" int fl_batch_create(fl_plan* const* plans, int32_t n_plans, fl_batch*
     b->r = b->p = b->q = b->tmp = nullptr; b->S = nullptr; b->partials = nullptr;
     b->tickets = nullptr; b->hist = nullptr; b->hist_cap = 4096;
     b->cs = nullptr; b->ev0 = b->ev1 = nullptr; b->exec = nullptr; b->cap_u = nullptr;
+    b->cs2 = nullptr; b->evf = b->evj = nullptr;
     b->cap_lam = 0.0f; b->cap_tol = 0.0;
     b->n_ray_chunks = (int)rays.size(); b->n_pix_chunks = (int)pix.size();
     b->n_ray_t_chunks = (int)rays_t.size(); b->n_wray_chunks = (int)wrays.size();
@@ -499,6 +505,9 @@ extern "C" int fl_batch_create(fl_plan* const* plans, int32_t n_plans, fl_batch*
     if (!st) st = fl_check_cuda(cudaStreamCreateWithFlags(&b->cs, cudaStreamNonBlocking), "stream");
     if (!st) st = fl_check_cuda(cudaEventCreateWithFlags(&b->ev0, cudaEventDisableTiming), "event");
     if (!st) st = fl_check_cuda(cudaEventCreateWithFlags(&b->ev1, cudaEventDisableTiming), "event");
+    if (!st) st = fl_check_cuda(cudaStreamCreateWithFlags(&b->cs2, cudaStreamNonBlocking), "stream");
+    if (!st) st = fl_check_cuda(cudaEventCreateWithFlags(&b->evf, cudaEventDisableTiming), "event");
+    if (!st) st = fl_check_cuda(cudaEventCreateWithFlags(&b->evj, cudaEventDisableTiming), "event");
     if (st) { batch_free(b); delete b; return st; }
     *out = b;
     return fl_set_error(FL_OK, "");
@@ -523,26 +532,50 @@ extern "C" int fl_batch_layout(const fl_batch* b, int64_t* vox_offsets, int64_t*
 
 // ypack: y is the batch's scratch (slice offsets woff), turn slices packed per
 // orbit, as batch_adj_w reads it; else the caller's sinogram (offsets yoff)
+// With both kinds of slices, the turn slices' launch runs on a second stream
+// forked from s and joined back (two branches of a captured graph): the two
+// write different slices, and each fills the other's tail.
+static cudaStream_t fork(fl_batch* b, cudaStream_t s)
+{
+    if (cudaEventRecord(b->evf, s) != cudaSuccess || cudaStreamWaitEvent(b->cs2, b->evf, 0) != cudaSuccess)
+        return s;
+    return b->cs2;
+}
+
+static int join(fl_batch* b, cudaStream_t s, cudaStream_t s2)
+{
+    if (s2 == s) return FL_OK;
+    FL_CUDA(cudaEventRecord(b->evj, s2));
+    FL_CUDA(cudaStreamWaitEvent(s, b->evj, 0));
+    return FL_OK;
+}
+
 static int batch_fwd(fl_batch* b, const float* x, float* y, int cr_power, int ypack,
                      const BatchScal* S, cudaStream_t s)
 {
+    const cudaStream_t s2 = (b->n_ray_chunks && b->n_ray_t_chunks) ? fork(b, s) : s;
+    if (b->n_ray_t_chunks)
+        k_batch_fwd_turn<<<b->n_ray_t_chunks, kFanBlock, 0, s2>>>(
+            x, y, b->d_sl, b->d_rays_t, cr_power, ypack, S);
     if (b->n_ray_chunks)
         k_batch_fwd<<<b->n_ray_chunks, kRayChunk, 0, s>>>(x, y, b->d_sl, b->d_rays, cr_power,
                                                           ypack, S);
-    if (b->n_ray_t_chunks)
-        k_batch_fwd_turn<<<b->n_ray_t_chunks, kFanBlock, 0, s>>>(
-            x, y, b->d_sl, b->d_rays_t, cr_power, ypack, S);
-    return fl_check_launch("batched forward");
+    int st = fl_check_launch("batched forward");
+    if (!st) st = join(b, s, s2);
+    return st;
 }
 
 static int batch_adj_w(fl_batch* b, const float* yw, float* x, const BatchScal* S, cudaStream_t s)
 {
+    const cudaStream_t s2 = (b->n_pix_chunks && b->n_pix_t_chunks) ? fork(b, s) : s;
+    if (b->n_pix_t_chunks)
+        k_batch_adj_turn<<<b->n_pix_t_chunks, dim3(kFanX, kTurnGroups), 0, s2>>>(
+            x, yw, b->d_sl, b->d_pix_t, S);
     if (b->n_pix_chunks)
         k_batch_adj<<<b->n_pix_chunks, kPixChunk, 0, s>>>(x, yw, b->d_sl, b->d_pix, S);
-    if (b->n_pix_t_chunks)
-        k_batch_adj_turn<<<b->n_pix_t_chunks, dim3(kFanX, kTurnGroups), 0, s>>>(
-            x, yw, b->d_sl, b->d_pix_t, S);
-    return fl_check_launch("batched adjoint");
+    int st = fl_check_launch("batched adjoint");
+    if (!st) st = join(b, s, s2);
+    return st;
 }
 
 extern "C" int fl_batch_forward(fl_batch* b, const float* x, float* y, void* stream)
