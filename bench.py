@@ -511,6 +511,7 @@ def run_single(ctx, name, w, p):
     from framelab_gb300.solvers import NativeCGLS, dot
     K, W, world = ctx.K, ctx.W, ctx.world
     P = Plan(p)
+    shapes = P.autotune()                 # launch shapes for this geometry (untimed)
     n = w["n"]
     img = PH.ellipsoids_3d(n, seed=5) if w["kind"] == "cone" else PH.ellipses_2d(n, seed=5)
     x_true = torch.from_numpy(img.reshape(-1)).to(ctx.dev)
@@ -519,7 +520,7 @@ def run_single(ctx, name, w, p):
     del f
     torch.cuda.synchronize()
     lam = w["lam"]
-    detail = {}
+    detail = {"launch_shapes": shapes}
     cg_g = NativeCGLS(P, "graph")
     if W:
         cg_g.solve(b, lam=lam, iters=W)
@@ -680,6 +681,7 @@ def run_sb(ctx, name, w, p):
     from framelab_gb300.transforms import SplitBregmanSolver
     K, W, world = ctx.K, ctx.W, ctx.world
     P = Plan(p)
+    shapes = P.autotune()                 # launch shapes for this geometry (untimed)
     x = torch.from_numpy(PH.ellipsoids_3d(w["n"], seed=5).reshape(-1)).to(ctx.dev)
     proj = P.forward(x)
     s = w["pmax"] / float(proj.max())
@@ -693,7 +695,7 @@ def run_sb(ctx, name, w, p):
     # the workspace (framelet, CGLS, coefficient sets) is allocated once, as
     # for the CGLS workloads; each step is one outer iteration of solve()
     sbs = SplitBregmanSolver(P, levels=w["levels"], kind="linear", mode="graph")
-    detail = {}
+    detail = {"launch_shapes": shapes}
     if W:
         sbs.solve(f, u0, outer=W, **kw)
     clocks = ClockSampler(ctx.local)

@@ -57,6 +57,7 @@ _SIGS = {
     "fl_plan_sizes": (_I, [_P, C.POINTER(_I64), C.POINTER(_I64)]),
     "fl_plan_option": (_I, [_P, _I, _I]),
     "fl_plan_query": (_I, [_P, _I, C.POINTER(_I)]),
+    "fl_plan_autotune": (_I, [_P, _P, _P]),
     "fl_forward": (_I, [_P, _I, _V, _I, _V, _I, _V]),
     "fl_adjoint": (_I, [_P, _I, _V, _I, _V, _I, _V]),
     "fl_count_intersections": (_I, [_P, _V, _V]),

@@ -73,6 +73,10 @@ struct fl_plan {
     // A[(v, a), (x, y)], one walk / one weight serving G rays).
     // Every turn form needs one frame whose view list is 0, 1, ..., nv-1.
     int views_natural;
+    // launch shapes (threads in x and y, x * y = 128) of the cone projector
+    // kernels; 0 keeps each kernel's built-in shape (set by fl_plan_autotune;
+    // every thread's result is independent of the shape)
+    int fwd_bx, fwd_by, adj_bx, adj_by;
     // reusable scratch: sinogram-sized f32 for the pre-weighted adjoint input,
     // volume-sized for the z-folded copy of a forward input
     float *d_work;

@@ -17,6 +17,7 @@
 // entries -- the exact transpose, with no atomics.
 #include <algorithm>
 
+#include "fl_trace.h"
 #include "fl_common.cuh"
 #include "fl_plan.h"
 #include "matched_dev.cuh"
@@ -889,24 +890,25 @@ void launch_fwd(fl_plan* p, const void* x, void* y, int cr_power, const int* ski
                 const float* xscale, int yfold, cudaStream_t st)
 {
     const fl_scan& s = p->s;
+    const dim3 fb = p->fwd_bx ? dim3(p->fwd_bx, p->fwd_by) : dim3(8, 16);
     if (s.ndim == 3 && p->zmirror && p->rot && p->rot4) {
-        dim3 grid(fl_div_up(s.na, 8), s.nv / 4, fl_div_up(s.nb / 2, 16));
-        k_fwd_oct<TX, TY><<<grid, dim3(8, 16), 0, st>>>(
+        dim3 grid(fl_div_up(s.na, fb.x), s.nv / 4, fl_div_up(s.nb / 2, fb.y));
+        k_fwd_oct<TX, TY><<<grid, fb, 0, st>>>(
             (const TX*)x, (TY*)y, p->d_col, p->d_colr, p->d_row, s.nx, s.nz, s.na, s.nb, s.nv,
             p->n_vox_frame, s.scale, cr_power, skip, xscale, yfold);
     } else if (s.ndim == 3 && p->zmirror && p->rot) {
-        dim3 grid(fl_div_up(s.na, 8), s.nv / 2, fl_div_up(s.nb / 2, 16));
-        k_fwd_quad<TX, TY><<<grid, dim3(8, 16), 0, st>>>(
+        dim3 grid(fl_div_up(s.na, fb.x), s.nv / 2, fl_div_up(s.nb / 2, fb.y));
+        k_fwd_quad<TX, TY><<<grid, fb, 0, st>>>(
             (const TX*)x, (TY*)y, p->d_col, p->d_colr, p->d_row, s.nx, s.ny, s.nz, s.na, s.nb,
             s.nv, p->n_vox_frame, s.scale, cr_power, skip, xscale, yfold);
     } else if (s.ndim == 3 && p->zmirror) {
-        dim3 grid(fl_div_up(s.na, 8), s.nv, fl_div_up(s.nb / 2, 16));
-        k_fwd_cone<TX, TY, true><<<grid, dim3(8, 16), 0, st>>>(
+        dim3 grid(fl_div_up(s.na, fb.x), s.nv, fl_div_up(s.nb / 2, fb.y));
+        k_fwd_cone<TX, TY, true><<<grid, fb, 0, st>>>(
             (const TX*)x, (TY*)y, p->d_col, p->d_colr, p->d_row, p->d_view_frame, s.nx, s.ny,
             s.nz, s.na, s.nb, p->n_vox_frame, s.scale, cr_power, skip, xscale, yfold);
     } else if (s.ndim == 3) {
-        dim3 grid(fl_div_up(s.na, 8), s.nv, fl_div_up(s.nb, 16));
-        k_fwd_cone<TX, TY, false><<<grid, dim3(8, 16), 0, st>>>(
+        dim3 grid(fl_div_up(s.na, fb.x), s.nv, fl_div_up(s.nb, fb.y));
+        k_fwd_cone<TX, TY, false><<<grid, fb, 0, st>>>(
             (const TX*)x, (TY*)y, p->d_col, p->d_colr, p->d_row, p->d_view_frame, s.nx, s.ny,
             s.nz, s.na, s.nb, p->n_vox_frame, s.scale, cr_power, skip, xscale, 0);
     } else if (fl_plan_turns(p) > 1) {
@@ -954,26 +956,30 @@ void launch_adj(fl_plan* p, const float* yw, void* x, const int* skip, int xfold
             // runs of 2: the four columns' 16 accumulators keep 8 blocks per SM
             constexpr int TO = 2;
             zruns = (nzw + TO - 1) / TO;
-            dim3 grid(fl_div_up(s.nx / 2, 8), fl_div_up(s.ny / 2, 16), (unsigned)zruns);
-            k_adj_oct<TX, TO><<<grid, dim3(8, 16), 0, st>>>(
+            const dim3 ab = p->adj_bx ? dim3(p->adj_bx, p->adj_by) : dim3(8, 16);
+            dim3 grid(fl_div_up(s.nx / 2, ab.x), fl_div_up(s.ny / 2, ab.y), (unsigned)zruns);
+            k_adj_oct<TX, TO><<<grid, ab, 0, st>>>(
                 (TX*)x, yw, p->d_col, p->d_rowz, p->d_view, G, s.nx, s.nz, s.na, s.nb, s.nv,
                 s.dz, skip, xfold);
         } else if (p->zmirror && p->rot) {
             // runs of 4: the two columns' 16 accumulators keep 8 blocks per SM
             constexpr int TQ = 4;
             zruns = (nzw + TQ - 1) / TQ;
-            dim3 grid(fl_div_up(s.nx, 16), fl_div_up(s.ny / 2, 8), (unsigned)zruns);
-            k_adj_quad<TX, TQ><<<grid, dim3(16, 8), 0, st>>>(
+            const dim3 ab = p->adj_bx ? dim3(p->adj_bx, p->adj_by) : dim3(16, 8);
+            dim3 grid(fl_div_up(s.nx, ab.x), fl_div_up(s.ny / 2, ab.y), (unsigned)zruns);
+            k_adj_quad<TX, TQ><<<grid, ab, 0, st>>>(
                 (TX*)x, yw, p->d_col, p->d_rowz, p->d_view, G, s.nx, s.ny, s.nz, s.na, s.nb, s.nv,
                 s.dz, zruns, skip, xfold);
         } else if (p->zmirror) {
-            dim3 grid(fl_div_up(s.nx, 16), fl_div_up(s.ny, 8), (unsigned)zruns * s.nt);
-            k_adj_cone<TX, TZ, true><<<grid, dim3(16, 8), 0, st>>>(
+            const dim3 ab = p->adj_bx ? dim3(p->adj_bx, p->adj_by) : dim3(16, 8);
+            dim3 grid(fl_div_up(s.nx, ab.x), fl_div_up(s.ny, ab.y), (unsigned)zruns * s.nt);
+            k_adj_cone<TX, TZ, true><<<grid, ab, 0, st>>>(
                 (TX*)x, yw, p->d_col, p->d_rowz, p->d_view, p->d_idY, p->d_Nv, p->tmp_size, G,
                 s.nx, s.ny, s.nz, s.na, s.nb, s.dz, zruns, skip, xfold);
         } else {
-            dim3 grid(fl_div_up(s.nx, 32), fl_div_up(s.ny, 4), (unsigned)zruns * s.nt);
-            k_adj_cone<TX, TZ, false><<<grid, dim3(32, 4), 0, st>>>(
+            const dim3 ab = p->adj_bx ? dim3(p->adj_bx, p->adj_by) : dim3(32, 4);
+            dim3 grid(fl_div_up(s.nx, ab.x), fl_div_up(s.ny, ab.y), (unsigned)zruns * s.nt);
+            k_adj_cone<TX, TZ, false><<<grid, ab, 0, st>>>(
                 (TX*)x, yw, p->d_col, p->d_rowz, p->d_view, p->d_idY, p->d_Nv, p->tmp_size, G,
                 s.nx, s.ny, s.nz, s.na, s.nb, s.dz, zruns, skip, 0);
         }
@@ -1152,6 +1158,74 @@ int fl_matched_adjoint_w(fl_plan* p, const float* yw, void* x, int xt, const int
     else if (xt == FL_F16) launch_adj<__half>(p, yw, x, skip, xfold, st);
     else launch_adj<__nv_bfloat16>(p, yw, x, skip, xfold, st);
     return fl_check_launch("matched adjoint");
+}
+
+// Launch-shape autotuner of the cone projector kernels: each 128-thread shape
+// below is timed (CUDA events, one launch after one untimed) on the plan's own
+// geometry, with the plan's scratch as input and output, and the fastest kept
+// for the forward and for the backprojection. A thread's result does not
+// depend on the shape, so neither do the projections. Fan plans keep theirs.
+extern "C" int fl_plan_autotune(fl_plan* p, void* stream, int32_t* shapes)
+{
+    FL_RANGE("fl_plan_autotune");
+    if (!p) return fl_set_error(FL_ERR_INVALID, "fl_plan_autotune: null plan");
+    int st = fl_matched_ready(p);
+    if (st) return st;
+    if (p->s.ndim == 3 && p->det_kind >= 0) {
+        cudaStream_t s = (cudaStream_t)stream;
+        float* y = nullptr;
+        void* x = nullptr;
+        if ((st = fl_plan_work(p, &y))) return st;
+        if ((st = fl_plan_vwork(p, (size_t)p->n_vox * sizeof(float), &x))) return st;
+        FL_CUDA(cudaMemsetAsync(y, 0, (size_t)p->n_rays * sizeof(float), s));
+        FL_CUDA(cudaMemsetAsync(x, 0, (size_t)p->n_vox * sizeof(float), s));
+        const int lay = p->zmirror ? FL_LAY_X_FOLDED : 0;
+        static const int cand[4][2] = {{8, 16}, {16, 8}, {32, 4}, {4, 32}};
+        cudaEvent_t e0, e1;
+        FL_CUDA(cudaEventCreate(&e0));
+        if (cudaEventCreate(&e1) != cudaSuccess) {
+            cudaEventDestroy(e0);
+            return fl_set_error(FL_ERR_CUDA, "fl_plan_autotune: cudaEventCreate failed");
+        }
+        auto timed = [&](bool fwd, float& ms) -> int {
+            for (int rep = 0; rep < 2; rep++) {
+                if (rep == 1 && cudaEventRecord(e0, s) != cudaSuccess) return FL_ERR_CUDA;
+                int e = fwd ? fl_matched_forward(p, x, FL_F32, y, FL_F32, 2, nullptr, nullptr,
+                                                 lay | FL_LAY_Y_ADJ, s)
+                            : fl_matched_adjoint_w(p, y, x, FL_F32, nullptr, lay, s);
+                if (e) return e;
+            }
+            if (cudaEventRecord(e1, s) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
+                return fl_set_error(FL_ERR_CUDA, "fl_plan_autotune: timing failed");
+            return FL_OK;
+        };
+        for (int pass = 0; pass < 2 && !st; pass++) {
+            const bool fwd = pass == 0;
+            float best = 3.0e38f;
+            int bi = 0;
+            for (int c = 0; c < 4 && !st; c++) {
+                if (fwd) { p->fwd_bx = cand[c][0]; p->fwd_by = cand[c][1]; }
+                else     { p->adj_bx = cand[c][0]; p->adj_by = cand[c][1]; }
+                float ms = 0.0f;
+                st = timed(fwd, ms);
+                if (!st && ms < best) { best = ms; bi = c; }
+            }
+            if (fwd) { p->fwd_bx = cand[bi][0]; p->fwd_by = cand[bi][1]; }
+            else     { p->adj_bx = cand[bi][0]; p->adj_by = cand[bi][1]; }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (st) {                         // keep the built-in shapes after a failure
+            p->fwd_bx = p->fwd_by = p->adj_bx = p->adj_by = 0;
+            return st;
+        }
+    }
+    if (shapes) {
+        shapes[0] = p->fwd_bx; shapes[1] = p->fwd_by;
+        shapes[2] = p->adj_bx; shapes[3] = p->adj_by;
+    }
+    return fl_set_error(FL_OK, "");
 }
 
 int fl_matched_count(fl_plan* p, int32_t* counts, cudaStream_t st)

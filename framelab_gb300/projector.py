@@ -189,6 +189,17 @@ class Plan:
                                           _stream(stream)))
         return (y, yn) if yn is not None else y
 
+    def autotune(self, stream=None) -> dict:
+        """Times the block shapes of this cone plan's matched projector kernels
+        on its own geometry and keeps the fastest (``fl_plan_autotune``; the
+        projections do not change). Returns the chosen shapes; fan plans
+        report ``None`` and keep theirs."""
+        sh = (C.c_int32 * 4)()
+        _lib.check(self._L.fl_plan_autotune(self._h, _stream(stream), sh))
+        if not sh[0]:
+            return {"forward": None, "adjoint": None}
+        return {"forward": (sh[0], sh[1]), "adjoint": (sh[2], sh[3])}
+
     def count_intersections(self, stream=None) -> torch.Tensor:
         c = torch.empty(self.sino_shape, device="cuda", dtype=torch.int32)
         _lib.check(self._L.fl_count_intersections(self._h, c.data_ptr(), _stream(stream)))

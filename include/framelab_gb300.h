@@ -211,6 +211,14 @@ int fl_plan_sizes(const fl_plan *plan, int64_t *n_vox, int64_t *n_rays);
 enum { FL_OPT_Z_MIRROR = 1, FL_OPT_ROT_MIRROR = 2, FL_OPT_QUARTER_TURN = 3 };
 int fl_plan_option(fl_plan *plan, int option, int value);
 int fl_plan_query(const fl_plan *plan, int option, int *value);
+/* Launch-shape autotuner for a cone plan's matched projector kernels: times
+ * each 128-thread block shape (8x16, 16x8, 32x4, 4x32) on the plan's own
+ * geometry, one launch each on `stream` after one untimed, and keeps the
+ * fastest for the forward and for the backprojection. The results of the
+ * projectors do not depend on the shape. Synchronises `stream`; uses the
+ * plan's scratch buffers. shapes (optional, [4]): the chosen forward x, y and
+ * backprojection x, y (0 for fan plans, which keep their shapes). */
+int fl_plan_autotune(fl_plan *plan, void *stream, int32_t *shapes);
 
 /* y = A x on `stream`. x: n_vox elements, y: n_rays elements, device memory. */
 int fl_forward(fl_plan *plan, int model, const void *x, int x_dtype, void *y, int y_dtype,

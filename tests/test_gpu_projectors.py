@@ -716,6 +716,27 @@ def test_fan_turns_agree_with_general_kernels_and_are_exact(shape):
             assert _rel(_host(ut), _host(ug)) < tol, (mode, _rel(_host(ut), _host(ug)))
 
 
+@pytest.mark.parametrize("zm", [True, False])
+def test_autotune_keeps_the_projections(zm):
+    """The launch-shape autotuner picks one of its 128-thread shapes for each
+    kernel; every thread's result is independent of the shape, so the
+    projections stay bit for bit."""
+    p = _cone_small("circle")
+    P = _plan(p)
+    P.z_mirror = zm
+    rng = np.random.default_rng(12)
+    x = _dev(rng.standard_normal(P.n_vox).astype(np.float32))
+    r = _dev(rng.standard_normal(P.n_rays).astype(np.float32))
+    y0, x0 = _host(P.forward(x)), _host(P.adjoint(r))
+    sh = P.autotune()
+    shapes = {(8, 16), (16, 8), (32, 4), (4, 32)}
+    assert sh["forward"] in shapes and sh["adjoint"] in shapes, sh
+    assert np.array_equal(_host(P.forward(x)), y0)
+    assert np.array_equal(_host(P.adjoint(r)), x0)
+    assert _plan(G.fan_para(32, 32, 64, 20, L=(1, 1))).autotune() == {"forward": None,
+                                                                       "adjoint": None}
+
+
 def test_turn_plans_need_columns_of_four():
     """The half- and quarter-turn forms keep the folded volume in 4 x 4 tiles:
     sizes that are not multiples of 4 keep the z mirror alone."""
