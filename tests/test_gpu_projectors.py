@@ -737,6 +737,47 @@ def test_autotune_keeps_the_projections(zm):
                                                                        "adjoint": None}
 
 
+# degenerate and small sizes: one view, one detector column or row, a 1-pixel
+# wide image, a 2-slice volume, a detector much wider than the field (most
+# rays miss). Each runs the kernel form its symmetries select. Odd detectors
+# are shifted off the isocentre (y_os): a central ray along a pixel boundary
+# has no unique discretisation.
+SMALL = [
+    ("fan", dict(nx=2, ny=2, nd=3, nv=1, y_os=0.013)),      # general, one view
+    ("fan", dict(nx=1, ny=2, nd=1, nv=2, y_os=0.013)),      # half turn, one column
+    ("fan", dict(nx=2, ny=2, nd=2, nv=4)),                  # quarter turn, 2 x 2
+    ("fan", dict(nx=6, ny=4, nd=64, nv=6, Ly=40.0)),        # most rays miss
+    ("cone", dict(nx=4, ny=4, nz=2, na=1, nb=2, nv=4, y_os=0.013)),  # quarter turn + mirror
+    ("cone", dict(nx=4, ny=8, nz=2, na=3, nb=2, nv=2, y_os=0.013)),  # half turn + mirror
+    ("cone", dict(nx=3, ny=2, nz=1, na=2, nb=1, nv=3)),     # general
+]
+
+
+@pytest.mark.parametrize("kind,sz", SMALL)
+def test_small_and_degenerate_sizes_match_fp64(kind, sz):
+    sz = dict(sz)
+    if kind == "fan":
+        p = G.fan_para(sz["nx"], sz["ny"], sz["nd"], sz["nv"], L=(1.0, sz["ny"] / sz["nx"]),
+                       SO=3.0, OD=3.0, Ly=sz.get("Ly", 3.0), y_os=sz.get("y_os", 0.0))
+    else:
+        p = G.cone_para(sz["nx"], sz["ny"], sz["nz"], sz["na"], sz["nb"], sz["nv"],
+                        L=(1.0, sz["ny"] / sz["nx"], sz["nz"] / sz["nx"]), SO=3.0, OD=3.0,
+                        Ly=3.0, Lz=2.0, y_os=sz.get("y_os", 0.0))
+    P = _plan(p)
+    rng = np.random.default_rng(13)
+    x = rng.uniform(0.5, 1.5, P.n_vox).astype(np.float32)
+    r = rng.standard_normal(P.n_rays).astype(np.float32)
+    y, xa = _host(P.forward(_dev(x))), _host(P.adjoint(_dev(r)))
+    e, ea = O.exact_forward(x, p), O.exact_adjoint(r, p)
+    assert np.all(np.isfinite(y)) and np.all(np.isfinite(xa))
+    # small problems: compare in absolute terms against the largest value
+    assert np.max(np.abs(y - e)) <= 1e-5 * max(np.max(np.abs(e)), 1e-30), (kind, sz)
+    assert np.max(np.abs(xa - ea)) <= 1e-4 * max(np.max(np.abs(ea)), 1e-30), (kind, sz)
+    lhs = np.dot(y.astype(np.float64), r.astype(np.float64))
+    rhs = np.dot(x.astype(np.float64), xa.astype(np.float64))
+    assert abs(lhs - rhs) <= 1e-5 * max(abs(lhs), 1e-30)
+
+
 def test_turn_plans_need_columns_of_four():
     """The half- and quarter-turn forms keep the folded volume in 4 x 4 tiles:
     sizes that are not multiples of 4 keep the z mirror alone."""
