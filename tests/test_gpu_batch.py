@@ -100,6 +100,34 @@ def test_batch_turn_slices_bit_identical_to_single_plans():
         assert float((a - b).norm() / b.norm()) < 1e-5, i
 
 
+def test_batch_tiny_slices_of_every_kind_bit_identical():
+    """Degenerate slices in one batch: one view (general), a one-pixel-wide
+    image and a single detector column (half turn), a 2 x 2 image (quarter
+    turn), beside a normal slice."""
+    import torch
+    from framelab_gb300.batch import FanBatch
+    paras = [G.fan_para(2, 2, 3, 1, L=(1.0, 1.0), SO=3.0, OD=3.0, Ly=3.0, y_os=0.013),
+             G.fan_para(1, 2, 1, 2, L=(1.0, 2.0), SO=3.0, OD=3.0, Ly=3.0, y_os=0.013),
+             G.fan_para(2, 2, 2, 4, L=(1.0, 1.0), SO=3.0, OD=3.0, Ly=3.0),
+             G.fan_para(24, 24, 48, 12, L=(1.0, 1.0), SO=3.0, OD=3.0, Ly=3.0)]
+    B = FanBatch(paras)
+    assert B.turns == [1, 2, 4, 4]
+    rng = np.random.default_rng(14)
+    x = torch.from_numpy(rng.standard_normal(B.n_vox).astype(np.float32)).cuda()
+    y = torch.from_numpy(rng.standard_normal(B.n_rays).astype(np.float32)).cuda()
+    yb, xb = B.forward(x), B.adjoint(y)
+    torch.cuda.synchronize()
+    for i, P in enumerate(B.plans):
+        xi = B.images(x)[i].reshape(-1).contiguous()
+        yi = B.sinograms(y)[i].reshape(-1).contiguous()
+        assert torch.equal(B.sinograms(yb)[i].reshape(-1),
+                           P.forward(xi, model="matched").reshape(-1)), i
+        assert torch.equal(B.images(xb)[i].reshape(-1),
+                           P.adjoint(yi, model="matched").reshape(-1)), i
+    u = B.cgls(B.adjoint(B.forward(torch.abs(x))), lam=0.1, iters=3)
+    assert bool(torch.isfinite(u).all())
+
+
 def test_batch_turn_slices_cgls_agree_with_single_slice_solver():
     import torch
     from framelab_gb300.batch import FanBatch
