@@ -60,6 +60,7 @@ def main():
         G.fan_para(64, 64, 128, 30, L=(1, 1)),                         # fan, 1 x 1 blocks
         G.fan_para(512, 512, 1024, 60, L=(1, 1)),                      # fan, 2 x 2 blocks
         G.fan_para(48, 36, 97, 42, L=(1, 0.75), SO=3.0, OD=3.0, Ly=3.0),  # fan, rectangular
+        G.fan_para(640, 480, 64, 6, L=(1, 0.75), SO=3.0, OD=3.0, Ly=3.0),  # fan, 2 x 2 turn blocks
     ]
     for p in cases:
         run_plan(p, rng)

@@ -716,6 +716,32 @@ def test_fan_turns_agree_with_general_kernels_and_are_exact(shape):
             assert _rel(_host(ut), _host(ug)) < tol, (mode, _rel(_host(ut), _host(ug)))
 
 
+@pytest.mark.parametrize("shape", [(640, 480, 64, 6), (1152, 1152, 32, 4)])
+def test_fan_turn_large_images_use_2x2_blocks(shape):
+    """Images with at least 4 waves of 2 x 2 primary blocks take the 2 x 2
+    form of the turn backprojection (half turn, quarter turn): against the
+    FP64 oracle and by the dot test."""
+    nx, ny, nd, nv = shape
+    p = G.fan_para(nx, ny, nd, nv, L=(1.0, ny / nx), SO=3.0, OD=3.0, Ly=3.0)
+    P = _plan(p)
+    assert P.rot_mirror and P.quarter_turn == (nx == ny)
+    hx, hy = (nx // 2 if nx == ny else nx), ny // 2
+    assert -(-hx // 64) * -(-hy // 2) >= 4 * 152           # the 2 x 2 form
+    rng = np.random.default_rng(15)
+    x = rng.uniform(0, 1, P.n_vox).astype(np.float32)
+    r = rng.standard_normal(P.n_rays).astype(np.float32)
+    y, xa = _host(P.forward(_dev(x))), _host(P.adjoint(_dev(r)))
+    assert _rel(y, O.exact_forward(x, p)) < 1e-5
+    # each weight is a difference of FP32 crossing parameters centred on the
+    # isocentre: their ulp at the image edge (about 6e-8 n/2 pixel) bounds a
+    # weight's error, which the adjoint of a random sinogram shows directly
+    # (1.9e-4 at 1152^2), while the forward averages it along the ray
+    assert _rel(xa, O.exact_adjoint(r, p)) < 2.5e-7 * max(nx, ny) + 5e-5
+    lhs = np.dot(y.astype(np.float64), r.astype(np.float64))
+    rhs = np.dot(x.astype(np.float64), xa.astype(np.float64))
+    assert abs(lhs - rhs) / abs(lhs) < 1e-5
+
+
 @pytest.mark.parametrize("zm", [True, False])
 def test_autotune_keeps_the_projections(zm):
     """The launch-shape autotuner picks one of its 128-thread shapes for each
