@@ -82,6 +82,9 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="cone512", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--symmetry", default="all", choices=["all", "mirror", "none"],
+                    help="kernel forms a cone plan may use: every symmetry its scan has "
+                         "(default), the z mirror alone, or none (general kernels)")
     ap.add_argument("--only", default="",
                     help="comma list of legs: mixed,plain,hostplain,e2e,kernels,seq,grad")
     return ap.parse_args()
@@ -503,6 +506,15 @@ def host_structure_cgls(ctx, P, b, lam, cg_g, detail, iters=2):
     return out
 
 
+def restrict_symmetry(ctx, P):
+    """--symmetry: keep the plan to the z mirror alone, or to the general
+    kernels (the default uses every symmetry the scan has)."""
+    if ctx.a.symmetry in ("mirror", "none"):
+        P.rot_mirror = False
+    if ctx.a.symmetry == "none":
+        P.z_mirror = False
+
+
 def run_single(ctx, name, w, p):
     """cone / fan: CGLS on one scan (graph headline, mixed, plain, e2e, kernels)."""
     torch = ctx.torch
@@ -511,6 +523,7 @@ def run_single(ctx, name, w, p):
     from framelab_gb300.solvers import NativeCGLS, dot
     K, W, world = ctx.K, ctx.W, ctx.world
     P = Plan(p)
+    restrict_symmetry(ctx, P)
     shapes = P.autotune()                 # launch shapes for this geometry (untimed)
     n = w["n"]
     img = PH.ellipsoids_3d(n, seed=5) if w["kind"] == "cone" else PH.ellipses_2d(n, seed=5)
@@ -681,6 +694,7 @@ def run_sb(ctx, name, w, p):
     from framelab_gb300.transforms import SplitBregmanSolver
     K, W, world = ctx.K, ctx.W, ctx.world
     P = Plan(p)
+    restrict_symmetry(ctx, P)
     shapes = P.autotune()                 # launch shapes for this geometry (untimed)
     x = torch.from_numpy(PH.ellipsoids_3d(w["n"], seed=5).reshape(-1)).to(ctx.dev)
     proj = P.forward(x)
@@ -767,6 +781,8 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     w = WORKLOADS[a.workload]
     metric, config, data = describe(a.workload, w, world)
+    if a.symmetry != "all":
+        config["symmetry"] = a.symmetry
 
     if a.impl == "reference":
         if rank != 0:
