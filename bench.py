@@ -83,8 +83,9 @@ def parse():
     ap.add_argument("--workload", default="cone512", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--symmetry", default="all", choices=["all", "mirror", "none"],
-                    help="kernel forms a cone plan may use: every symmetry its scan has "
-                         "(default), the z mirror alone, or none (general kernels)")
+                    help="kernel forms a plan may use: every symmetry its scan has "
+                         "(default), the z mirror alone (no half or quarter turn), or none "
+                         "(general kernels)")
     ap.add_argument("--only", default="",
                     help="comma list of legs: mixed,plain,hostplain,e2e,kernels,seq,grad")
     return ap.parse_args()
