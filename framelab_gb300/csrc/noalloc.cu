@@ -11,12 +11,18 @@
 // allocator. fl_adjoint_noalloc runs the same two kernels with the scratch in
 // a fixed array compiled into this library instead.
 //
-// The array holds FL_ADJOINT_NOALLOC_MAX_RAYS floats (8 MiB) on every GPU that
-// loads the library, until the process exits. All calls share it, so calls
-// whose work can overlap on the GPU (different streams, or different host
-// threads) race on it and must be serialised by the caller. Nothing in it has
-// to start at zero: the weighting kernel writes every element the gather
-// reads, and each call overwrites what the previous call left there.
+// The array holds FL_ADJOINT_NOALLOC_MAX_RAYS floats (8 MiB) per GPU, until the
+// process exits. With CUDA's default lazy module loading it is placed on a GPU
+// when the first call on that GPU looks up its address: that first call takes
+// the 8 MiB, so it belongs before the caller's pool allocator takes the GPU's
+// memory and before any stream capture. Later calls allocate nothing. All
+// calls share the array, so calls whose work can overlap on the GPU
+// (different streams, or different host threads) race on it and must be
+// serialised by the caller. Nothing in it has to start at zero: the weighting
+// kernel writes every element the gather reads, and each call overwrites what
+// the previous call left there. The stream must belong to the current device
+// (the array's address is the current device's); a stream of another device
+// is refused.
 #include <mutex>
 
 #include "fl_trace.h"
@@ -68,9 +74,18 @@ extern "C" int fl_adjoint_noalloc(fl_plan* p, const void* y, int yt, void* x, in
     if (p->det_kind < 0 || (p->det_kind == 1 && p->s.ndim == 3))
         return fl_set_error(FL_ERR_UNSUPPORTED,
                             "matched adjoint needs a uniform flat or (fan) equiangular detector");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (s) {
+        int dev = 0, sdev = 0;
+        FL_CUDA(cudaGetDevice(&dev));
+        FL_CUDA(cudaStreamGetDevice(s, &sdev));
+        if (sdev != dev)
+            return fl_set_error(FL_ERR_INVALID,
+                                "fl_adjoint_noalloc: the stream belongs to device %d, the "
+                                "current device is %d", sdev, dev);
+    }
     float* w = nullptr;
     if ((st = scratch_for_current_device(&w))) return st;
-    cudaStream_t s = (cudaStream_t)stream;
     if ((st = fl_matched_weight(p, y, yt, w, s))) return st;
     if ((st = fl_matched_adjoint_w(p, w, x, xt, nullptr, 0, s))) return st;
     return fl_set_error(FL_OK, "");

@@ -6,10 +6,17 @@ detector grids are pixel-centred, and the frame bookkeeping (``id_X``, ``id_Y``,
 ``Nv``, ``tmp_size``) describes a single frame (``nt = 1``), as the reference's
 classes always do.
 
-Arithmetic follows MATLAB's ``single`` rules: an expression mixing ``double``
-and ``single`` operands is evaluated in single precision. MATLAB's own
-single-precision ``cos``/``sin``/``atan2`` are not available here; they are
-taken as the double-precision result rounded to single.
+Arithmetic follows MATLAB's class rules operation by operation:
+* both operands ``single`` (the scanner's ``SO``, ``OD``, ``Ly``, ``Lz`` and
+  ``y_os`` properties, ``ConeBeamScanner.m:10-16``, ``FanBeamScanner.m:5-10``,
+  and ``scale``): the operation is a single-precision one;
+* one operand ``double`` (the counts ``na``, ``nb``, ``nd``, the helix step
+  ``h``, index ranges): the operation is carried out in double and its result
+  rounded to ``single``;
+* an all-``double`` expression wrapped in ``single(...)`` is rounded once.
+Each field below cites the ``setPara.m`` line whose order it follows.
+MATLAB's own single-precision ``cos``/``sin``/``atan2`` are not available
+here; they are taken as the double-precision result rounded to single.
 
 Field names and dtypes are those the mex gateways read (``Ax_fan_mf.cpp:28-41``,
 ``Atx_fan_mf.cpp:29-63``, ``Ax_cone_mf.cpp:31-52``, ``Atx_cone_mf.cpp:31-55``) and
@@ -29,10 +36,30 @@ def _single_trig(fn, x):
     return fn(np.asarray(x, dtype=np.float64)).astype(np.float32)
 
 
+def _mixed(a_double, b_single) -> np.ndarray:
+    """One MATLAB operation ``double * single``: computed in double, rounded
+    to single."""
+    return (np.asarray(a_double, np.float64) * np.float64(b_single)).astype(np.float32) \
+        if np.ndim(b_single) == 0 else \
+        (np.float64(a_double) * np.asarray(b_single, np.float32).astype(np.float64)).astype(
+            np.float32)
+
+
+def _pitch(L_single, n: int) -> np.float32:
+    """``L/n`` with ``L`` a single property and ``n`` a double count
+    (``FanBeamScanner/setPara.m:10``, ``ConeBeamScanner/setPara.m:10-11``):
+    the division runs in double and rounds to single."""
+    return f32(np.float64(f32(L_single)) / np.float64(n))
+
+
 def _centred_grid(n: int, pitch: np.float32, offset: np.float32) -> np.ndarray:
-    """single(((-n/2:n/2-1)+0.5)*pitch + offset): pixel-centred detector grid."""
-    k = (-n / 2.0 + np.arange(n, dtype=np.float64) + 0.5).astype(np.float32)
-    return (k * f32(pitch) + f32(offset)).astype(np.float32)
+    """``single(((-n/2:n/2-1)+0.5)*pitch + offset)``
+    (``FanBeamScanner/setPara.m:23``, ``ConeBeamScanner/setPara.m:53-54``):
+    the double index vector times the single pitch is one mixed operation
+    (double product, exact here, rounded to single), then a single + single
+    addition of the offset."""
+    k = -n / 2.0 + np.arange(n, dtype=np.float64) + 0.5
+    return (_mixed(k, f32(pitch)) + f32(offset)).astype(np.float32)
 
 
 def _frame_tables(nv: int):
@@ -51,9 +78,9 @@ def fan_para(nx: int, ny: int, nd: int, nv: int, L=(10.0, 10.0), SO=5.0, OD=5.0,
     Ly = 6, ``FanBeamScanner.m:4-11``); ``sd_phi`` overrides the uniform 2*pi
     source angles.
     """
-    scale = f32(L[0] / nx)
-    SOs, ODs = f32(SO) / scale, f32(OD) / scale
-    dy_det = f32(f32(Ly) / f32(nd))
+    scale = f32(L[0] / nx)                          # single(object.Dx(1))  (setPara.m:5)
+    SOs, ODs = f32(SO) / scale, f32(OD) / scale     # single / single       (setPara.m:8-9)
+    dy_det = _pitch(Ly, nd)                         # Ly / nd               (setPara.m:10)
     if sd_phi is None:
         sd_phi = (2 * math.pi / nv * np.arange(nv)).astype(np.float32)
     sd_phi = np.asarray(sd_phi, dtype=np.float32)
@@ -110,12 +137,12 @@ def cone_para(nx: int, ny: int, nz: int, na: int, nb: int, nv: int = 128,
     ``scan`` is ``'circle'``, ``'helix'`` or ``'multiHelix'``; for the helical
     scans the view count follows ``ConeBeamScanner.m:53-58``.
     """
-    scale = f32(L[0] / nx)
-    dzv = f32(f32(L[2] / nz) / scale)
-    SOs, ODs = f32(SO) / scale, f32(OD) / scale
-    dy_det = f32(f32(Ly) / f32(na))
-    dz_det = f32(f32(Lz) / f32(nb))
-    pdy, pdz = f32(dy_det / scale), f32(dz_det / scale)
+    scale = f32(L[0] / nx)                          # single(object.Dx(1))      (setPara.m:5)
+    dzv = f32(f32(L[2] / nz) / scale)               # single(object.Dx(3))/scale (setPara.m:22)
+    SOs, ODs = f32(SO) / scale, f32(OD) / scale     # single / single           (setPara.m:8-9)
+    dy_det = _pitch(Ly, na)                         # Ly / na                   (setPara.m:10)
+    dz_det = _pitch(Lz, nb)                         # Lz / nb                   (setPara.m:11)
+    pdy, pdz = f32(dy_det / scale), f32(dz_det / scale)   # single / single   (setPara.m:12-13)
     if scan == "circle":
         sd_phi = (2 * math.pi / nv * np.arange(nv)).astype(np.float32)
         sd_z = (np.zeros(nv, dtype=np.float32) / scale).astype(np.float32)
@@ -126,10 +153,17 @@ def cone_para(nx: int, ny: int, nz: int, na: int, nb: int, nv: int = 128,
         base = -phi_max / 2 + dphi * np.arange(nper)
         h = vtab / (2 * math.pi * rps)
         shifts = [0.0] if scan == "helix" else list(phase_shift)[:n_helix]
+        # single((-phiMax/2:dphi:phiMax/2) + phaseShift(i))  (setPara.m:32, 42)
         phis = [(base + s).astype(np.float32) for s in shifts]
         sd_phi = np.concatenate(phis).astype(np.float32)
-        zs = [((f32(h) * base.astype(np.float32)).astype(np.float32) / scale).astype(np.float32)
-              for _ in shifts]
+        if scan == "helix":
+            # single(h*sd_phi)/scale: double h times the single sd_phi is a
+            # mixed operation (double product rounded to single)  (setPara.m:35)
+            zs = [(_mixed(h, sd_phi) / scale).astype(np.float32)]
+        else:
+            # single(h*(-phiMax/2:dphi:phiMax/2))/scale: all double, rounded
+            # once, the same z for every helix  (setPara.m:49)
+            zs = [((h * base).astype(np.float32) / scale).astype(np.float32) for _ in shifts]
         sd_z = np.concatenate(zs).astype(np.float32)
     else:
         raise ValueError("circle, helix and multiHelix are only valid types")

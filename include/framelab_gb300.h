@@ -240,11 +240,15 @@ int fl_count_intersections(fl_plan *plan, int32_t *counts, void *stream);
  * host application whose own pool allocator owns the GPU's memory, a loop
  * that must not block on the allocator. The sinogram pre-weighting scratch
  * that fl_adjoint allocates in the plan is instead a fixed array of
- * FL_ADJOINT_NOALLOC_MAX_RAYS floats (8 MiB) inside the library, held on every
- * GPU that loads it until the process exits; plans with more rays are refused
- * with FL_ERR_INVALID. The first call on each device looks up that array's
- * device address once (make it before any stream capture). All calls share the
- * array: calls that can overlap on the GPU race and must be serialised. */
+ * FL_ADJOINT_NOALLOC_MAX_RAYS floats (8 MiB) inside the library; plans with
+ * more rays are refused with FL_ERR_INVALID. The first call on each device
+ * looks up that array's device address, and with CUDA's lazy module loading
+ * that is when the 8 MiB are placed on the device: make that first call
+ * before any stream capture and before a pool allocator takes the GPU's
+ * memory. Later calls allocate nothing; the array stays until the process
+ * exits. The stream must belong to the current device (another device's
+ * stream is refused). All calls share the array: calls that can overlap on
+ * the GPU race and must be serialised. */
 #define FL_ADJOINT_NOALLOC_MAX_RAYS (1 << 21)
 int fl_adjoint_noalloc(fl_plan *plan, const void *y, int y_dtype, void *x, int x_dtype,
                        void *stream);

@@ -340,6 +340,90 @@ def exact_count(p, views=None):
 
 
 # --------------------------------------------------------------------------
+# subsets: a list of rays or voxels at full problem size
+# --------------------------------------------------------------------------
+def _i64(a):
+    return np.ascontiguousarray(np.asarray(a, dtype=np.int64).reshape(-1))
+
+
+def _chunks(n, threads):
+    return _split(n, threads * 4 if threads > 1 else 1)
+
+
+def exact_forward_rays(X, p, rays, threads=1):
+    """FP64 exact forward of the rays ``rays`` (id iv*na*nb + ib*na + ia)."""
+    L = lib()
+    sd, sz, yd, zd, nz, dz = _exact_args(p)
+    X = _d(X); rays = _i64(rays)
+    y = np.zeros(rays.size, np.float64)
+
+    def go(a, b):
+        L.orc_exact_forward_rays(P(X), y[a:].ctypes.data_as(dp), D(float(p["SO"])),
+                                 D(float(p["OD"])), D(float(p["scale"])), I(int(p["nx"])),
+                                 I(int(p["ny"])), I(nz), D(dz), P(sd), P(sz), I(len(yd)),
+                                 I(len(zd)), P(yd), P(zd), rays[a:].ctypes.data_as(i64p),
+                                 C.c_long(b - a))
+    _run(go, _chunks(rays.size, threads), threads)
+    return y
+
+
+def cone_siddon_rays(X, p, rays, threads=1):
+    """Ax_cone_mf_cpu_siddon (Ax_cone_mf_cpu_siddon.cpp:19-134) for the rays
+    ``rays``: each value is the one ``cone_siddon_f32`` writes, bit for bit."""
+    L = lib()
+    X = _f(X); sd = _f(p["sd_phi"]); sz = _f(p["sd_z"]); yd = _f(p["y_det"])
+    zd = _f(p["z_det"]); idx = _i(p["id_X"]); rays = _i64(rays)
+    y = np.zeros(rays.size, np.float32)
+
+    def go(a, b):
+        L.orc_cone_siddon_rays(P(X), y[a:].ctypes.data_as(fp), F(p["SO"]), F(p["OD"]),
+                               F(p["scale"]), I(int(p["nx"])), I(int(p["ny"])), I(int(p["nz"])),
+                               P(sd), P(sz), I(len(yd)), I(len(zd)), P(yd), P(zd), P(idx),
+                               F(p["dz"]), rays[a:].ctypes.data_as(i64p), C.c_long(b - a))
+    _run(go, _chunks(rays.size, threads), threads)
+    return y
+
+
+def exact_adjoint_vox(Y, p, vox, threads=1):
+    """FP64 exact transpose of the FP32 sinogram ``Y`` at the voxels ``vox``
+    (frame 0): the FP64 chord of every ray through each voxel, times the ray's
+    value, summed in FP64."""
+    L = lib()
+    sd, sz, yd, zd, nz, dz = _exact_args(p)
+    Y = _f(Y); vox = _i64(vox)
+    x = np.zeros(vox.size, np.float64)
+
+    def go(a, b):
+        L.orc_exact_adjoint_vox(x[a:].ctypes.data_as(dp), P(Y), D(float(p["SO"])),
+                                D(float(p["OD"])), D(float(p["scale"])), I(int(p["nx"])),
+                                I(int(p["ny"])), I(nz), D(dz), I(0), I(len(sd)), P(sd), P(sz),
+                                I(len(yd)), I(len(zd)), P(yd), P(zd),
+                                vox[a:].ctypes.data_as(i64p), C.c_long(b - a))
+    _run(go, _chunks(vox.size, threads), threads)
+    return x
+
+
+def cone_adj_vox(Y, p, vox, threads=1):
+    """Atx_cone_mf_cpu_new (Atx_cone_mf_cpu_new.cpp:23-85) at the voxels ``vox``
+    (frame 0): each value is the one ``cone_adj_f32`` writes, bit for bit."""
+    L = lib()
+    Y = _f(Y); cp = _f(p["cos_phi"]); sp = _f(p["sin_phi"]); sz = _f(p["sd_z"])
+    yd = _f(p["y_det"]); zd = _f(p["z_det"]); idY = _i(np.asarray(p["id_Y"]).T.reshape(-1))
+    Nv = _i(p["Nv"]); vox = _i64(vox)
+    nx, ny, nz = int(p["nx"]), int(p["ny"]), int(p["nz"])
+    x = np.zeros(vox.size, np.float32)
+
+    def go(a, b):
+        L.orc_cone_adj_vox(x[a:].ctypes.data_as(fp), P(Y), F(p["SO"]), F(p["OD"]),
+                           F(p["scale"]), I(nx), I(ny), I(nz), P(sz), P(yd), P(zd),
+                           F(p["dy_det"]), F(p["y_os"]), F(p["dz_det"]), F(p["dz"]), P(idY),
+                           P(Nv), I(int(p["tmp_size"])), P(cp), P(sp), I(len(yd)), I(len(zd)),
+                           vox[a:].ctypes.data_as(i64p), C.c_long(b - a))
+    _run(go, _chunks(vox.size, threads), threads)
+    return x
+
+
+# --------------------------------------------------------------------------
 # dominant-axis forward (version 1), FP32 restatement
 # --------------------------------------------------------------------------
 def cone_gao_f32(X, p, threads=1, views=None):

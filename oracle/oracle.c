@@ -142,6 +142,52 @@ void orc_fan_siddon_f32(const float *X, float *y, float SO, float OD, float scal
 }
 
 /*
+ * One ray of the cone-beam Siddon projection: source angle trig (cphi, sphi),
+ * source z `sz`, detector point (ydet, zdet). The float operations and their
+ * order are those of Ax_cone_mf_cpu_siddon.cpp:35-131 for that ray.
+ */
+static float orc_cone_siddon_ray(const float *x, float SO, float OD, float scale, int nx,
+                                 int ny, int nz, float cphi, float sphi, float sz, float ydet,
+                                 float zdet, float dz0)
+{
+    int nx2 = nx / 2, ny2 = ny / 2, nz2 = nz / 2;
+    float x1 = cphi * (-SO), y1 = sphi * (-SO), z1 = sz;
+    float x2 = cphi * OD - sphi * ydet;
+    float y2 = sphi * OD + cphi * ydet;
+    float z2 = zdet + sz;
+    float dx = x2 - x1, dy = y2 - y1, dz = z2 - z1;
+    orc_axis ax[3];
+    orc_axis_init(&ax[0], x1, x2, nx, 0, 1.0f);
+    orc_axis_init(&ax[1], y1, y2, ny, 0, 1.0f);
+    orc_axis_init(&ax[2], z1, z2, nz, 1, dz0);
+    float total = (float)sqrt(dx * dx + dy * dy + dz * dz);
+    float acc = 0.0f;
+    int k = orc_pick(ax, 3);
+    if (k >= 0) {
+        float prev = ax[k].head;
+        orc_axis_pop(&ax[k]);
+        while ((k = orc_pick(ax, 3)) >= 0) {
+            float next = ax[k].head;
+            orc_axis_pop(&ax[k]);
+            float ac = (prev + next) / 2;
+            int tx = (int)floorf(x1 + ac * dx + (float)nx2);
+            if (tx >= 0 && tx < nx) {
+                int ty = (int)floorf(y1 + ac * dy + (float)ny2);
+                if (ty >= 0 && ty < ny) {
+                    int tz = (int)floorf((z1 + ac * dz) / dz0 + (float)nz2);
+                    if (tz >= 0 && tz < nz) {
+                        float seg = (next - prev) * total;
+                        acc += seg * x[((long)tz * ny + ty) * nx + tx];
+                    }
+                }
+            }
+            prev = next;
+        }
+    }
+    return acc * scale;
+}
+
+/*
  * Cone-beam Siddon projection of views [v0, v1).
  * Restates Ax_cone_mf_cpu_siddon (Ax_cone_mf_cpu_siddon.cpp:19-134).
  */
@@ -150,50 +196,36 @@ void orc_cone_siddon_f32(const float *X, float *y, float SO, float OD, float sca
                          const float *sd_z, int na, int nb, const float *y_det,
                          const float *z_det, const int *id_X, float dz0)
 {
-    int nx2 = nx / 2, ny2 = ny / 2, nz2 = nz / 2;
     long n = (long)nx * ny * nz, nd = (long)na * nb;
     for (int iv = v0; iv < v1; iv++) {
         const float *x = X + (long)id_X[iv] * n;
         /* C++ <math.h> resolves cos(float) to the float overload (cosf) */
         float cphi = cosf(sd_phi[iv]), sphi = sinf(sd_phi[iv]);
-        float x1 = cphi * (-SO), y1 = sphi * (-SO), z1 = sd_z[iv];
-        for (int ib = 0; ib < nb; ib++) {
-            for (int ia = 0; ia < na; ia++) {
-                float x2 = cphi * OD - sphi * y_det[ia];
-                float y2 = sphi * OD + cphi * y_det[ia];
-                float z2 = z_det[ib] + sd_z[iv];
-                float dx = x2 - x1, dy = y2 - y1, dz = z2 - z1;
-                orc_axis ax[3];
-                orc_axis_init(&ax[0], x1, x2, nx, 0, 1.0f);
-                orc_axis_init(&ax[1], y1, y2, ny, 0, 1.0f);
-                orc_axis_init(&ax[2], z1, z2, nz, 1, dz0);
-                float total = (float)sqrt(dx * dx + dy * dy + dz * dz);
-                float acc = 0.0f;
-                int k = orc_pick(ax, 3);
-                if (k >= 0) {
-                    float prev = ax[k].head;
-                    orc_axis_pop(&ax[k]);
-                    while ((k = orc_pick(ax, 3)) >= 0) {
-                        float next = ax[k].head;
-                        orc_axis_pop(&ax[k]);
-                        float ac = (prev + next) / 2;
-                        int tx = (int)floorf(x1 + ac * dx + (float)nx2);
-                        if (tx >= 0 && tx < nx) {
-                            int ty = (int)floorf(y1 + ac * dy + (float)ny2);
-                            if (ty >= 0 && ty < ny) {
-                                int tz = (int)floorf((z1 + ac * dz) / dz0 + (float)nz2);
-                                if (tz >= 0 && tz < nz) {
-                                    float seg = (next - prev) * total;
-                                    acc += seg * x[((long)tz * ny + ty) * nx + tx];
-                                }
-                            }
-                        }
-                        prev = next;
-                    }
-                }
-                y[(long)iv * nd + (long)ib * na + ia] = acc * scale;
-            }
-        }
+        for (int ib = 0; ib < nb; ib++)
+            for (int ia = 0; ia < na; ia++)
+                y[(long)iv * nd + (long)ib * na + ia] =
+                    orc_cone_siddon_ray(x, SO, OD, scale, nx, ny, nz, cphi, sphi, sd_z[iv],
+                                        y_det[ia], z_det[ib], dz0);
+    }
+}
+
+/*
+ * The same projection for a list of rays (ray id iv*na*nb + ib*na + ia);
+ * y[k] is ray rays[k]. Each value is the one orc_cone_siddon_f32 writes.
+ */
+void orc_cone_siddon_rays(const float *X, float *y, float SO, float OD, float scale, int nx,
+                          int ny, int nz, const float *sd_phi, const float *sd_z, int na,
+                          int nb, const float *y_det, const float *z_det, const int *id_X,
+                          float dz0, const int64_t *rays, long nr)
+{
+    long n = (long)nx * ny * nz, nd = (long)na * nb;
+    for (long k = 0; k < nr; k++) {
+        int iv = (int)(rays[k] / nd);
+        long r = rays[k] - (long)iv * nd;
+        int ib = (int)(r / na), ia = (int)(r - (long)ib * na);
+        float cphi = cosf(sd_phi[iv]), sphi = sinf(sd_phi[iv]);
+        y[k] = orc_cone_siddon_ray(X + (long)id_X[iv] * n, SO, OD, scale, nx, ny, nz, cphi,
+                                   sphi, sd_z[iv], y_det[ia], z_det[ib], dz0);
     }
 }
 
@@ -360,10 +392,60 @@ void orc_fan_adj_f32(float *x, const float *Y, float SO, float OD, float scale, 
 }
 
 /*
+ * One voxel (ix, iy, iz) of frame `it` of the cone-beam chord backprojection:
+ * the float operations and their order are those of
+ * Atx_cone_mf_cpu_new.cpp:38-81 for that voxel, including its unit-cube chord
+ * (it passes voxel size 1,1,1 whatever dz is) and its z window half-width
+ * sqrt(1 + dz^2/2).
+ */
+static float orc_cone_adj_voxel(const float *Y, float SO, float OD, float scale, int nx,
+                                int ny, int nz, const float *sd_z, const float *y_det,
+                                const float *z_det, float dy_det, float y_os, float dz_det,
+                                float dz, const int *id_Y, const int *Nv, int tmp_size,
+                                const float *cos_phi, const float *sin_phi, int na, int nb,
+                                int ix, int iy, int iz, int it)
+{
+    float SD = SO + OD;
+    int na2 = na / 2, nb2 = nb / 2, nx2 = nx / 2, ny2 = ny / 2, nz2 = nz / 2;
+    long nd = (long)na * nb;
+    float d = (float)sqrt(1 + dz * dz / 2);
+    float zc = (float)(iz + 0.5 - nz2) * dz;
+    float yc = (float)(iy + 0.5 - ny2);
+    float xc = (float)(ix + 0.5 - nx2);
+    float acc = 0.0f;
+    for (int j = 0; j < Nv[it]; j++) {
+        int iv = id_Y[it * tmp_size + j];
+        const float *yv = Y + (long)iv * nd;
+        float c = cos_phi[iv], s = sin_phi[iv];
+        float xr = c * xc + s * yc;
+        float yr = -s * xc + c * yc;
+        float g = SD / ((xr + SO) * dy_det);
+        int amax = (int)floor((yr + 1) * g - y_os + na2);
+        int amin = (int)floor((yr - 1) * g - y_os + na2);
+        g = SD / ((xr + SO) * dz_det);
+        int bmax = (int)floor((zc + d) * g + nb2);
+        int bmin = (int)floor((zc - d) * g + nb2);
+        if (amin < 0) amin = 0;
+        if (amax > na - 1) amax = na - 1;
+        if (bmin < 0) bmin = 0;
+        if (bmax > nb - 1) bmax = nb - 1;
+        for (int ib = bmin; ib <= bmax; ib++) {
+            for (int ia = amin; ia <= amax; ia++) {
+                float x1 = c * (-SO), y1 = s * (-SO), z1 = sd_z[iv];
+                float x2 = c * OD - s * y_det[ia];
+                float y2 = s * OD + c * y_det[ia];
+                float z2 = z_det[ib] + sd_z[iv];
+                float l = orc_chord_box(x1, y1, z1, x2, y2, z2, 1.0f, 1.0f, 1.0f, xc, yc, zc);
+                acc += l * yv[(long)ib * na + ia];
+            }
+        }
+    }
+    return acc * scale;
+}
+
+/*
  * Cone-beam backprojection for volume slices [iz0, iz1).
- * Restates Atx_cone_mf_cpu_new (Atx_cone_mf_cpu_new.cpp:23-85), including its
- * unit-cube chord (it passes voxel size 1,1,1 whatever dz is) and its
- * z window half-width sqrt(1 + dz^2/2).
+ * Restates Atx_cone_mf_cpu_new (Atx_cone_mf_cpu_new.cpp:23-85).
  */
 void orc_cone_adj_f32(float *x, const float *Y, float SO, float OD, float scale, int nx,
                       int ny, int nz, const float *sd_z, const float *y_det,
@@ -372,51 +454,35 @@ void orc_cone_adj_f32(float *x, const float *Y, float SO, float OD, float scale,
                       const float *cos_phi, const float *sin_phi, int na, int nb, int iz0,
                       int iz1)
 {
-    float SD = SO + OD;
-    int na2 = na / 2, nb2 = nb / 2, nx2 = nx / 2, ny2 = ny / 2, nz2 = nz / 2;
-    long n = (long)nx * ny * nz, nd = (long)na * nb;
-    float d = (float)sqrt(1 + dz * dz / 2);
-    for (int iz = iz0; iz < iz1; iz++) {
-        float zc = (float)(iz + 0.5 - nz2) * dz;
-        for (int iy = 0; iy < ny; iy++) {
-            float yc = (float)(iy + 0.5 - ny2);
-            for (int ix = 0; ix < nx; ix++) {
-                float xc = (float)(ix + 0.5 - nx2);
-                long idx = ((long)iz * ny + iy) * nx + ix;
-                for (int it = 0; it < nt; it++) {
-                    float acc = 0.0f;
-                    for (int j = 0; j < Nv[it]; j++) {
-                        int iv = id_Y[it * tmp_size + j];
-                        const float *yv = Y + (long)iv * nd;
-                        float c = cos_phi[iv], s = sin_phi[iv];
-                        float xr = c * xc + s * yc;
-                        float yr = -s * xc + c * yc;
-                        float g = SD / ((xr + SO) * dy_det);
-                        int amax = (int)floor((yr + 1) * g - y_os + na2);
-                        int amin = (int)floor((yr - 1) * g - y_os + na2);
-                        g = SD / ((xr + SO) * dz_det);
-                        int bmax = (int)floor((zc + d) * g + nb2);
-                        int bmin = (int)floor((zc - d) * g + nb2);
-                        if (amin < 0) amin = 0;
-                        if (amax > na - 1) amax = na - 1;
-                        if (bmin < 0) bmin = 0;
-                        if (bmax > nb - 1) bmax = nb - 1;
-                        for (int ib = bmin; ib <= bmax; ib++) {
-                            for (int ia = amin; ia <= amax; ia++) {
-                                float x1 = c * (-SO), y1 = s * (-SO), z1 = sd_z[iv];
-                                float x2 = c * OD - s * y_det[ia];
-                                float y2 = s * OD + c * y_det[ia];
-                                float z2 = z_det[ib] + sd_z[iv];
-                                float l = orc_chord_box(x1, y1, z1, x2, y2, z2, 1.0f, 1.0f,
-                                                        1.0f, xc, yc, zc);
-                                acc += l * yv[(long)ib * na + ia];
-                            }
-                        }
-                    }
-                    x[it * n + idx] = acc * scale;
-                }
-            }
-        }
+    long n = (long)nx * ny * nz;
+    for (int iz = iz0; iz < iz1; iz++)
+        for (int iy = 0; iy < ny; iy++)
+            for (int ix = 0; ix < nx; ix++)
+                for (int it = 0; it < nt; it++)
+                    x[it * n + ((long)iz * ny + iy) * nx + ix] = orc_cone_adj_voxel(
+                        Y, SO, OD, scale, nx, ny, nz, sd_z, y_det, z_det, dy_det, y_os, dz_det,
+                        dz, id_Y, Nv, tmp_size, cos_phi, sin_phi, na, nb, ix, iy, iz, it);
+}
+
+/*
+ * The same backprojection for a list of voxels of frame 0 (index
+ * iz*ny*nx + iy*nx + ix); x[k] is voxel vox[k]. Each value is the one
+ * orc_cone_adj_f32 writes.
+ */
+void orc_cone_adj_vox(float *x, const float *Y, float SO, float OD, float scale, int nx,
+                      int ny, int nz, const float *sd_z, const float *y_det,
+                      const float *z_det, float dy_det, float y_os, float dz_det, float dz,
+                      const int *id_Y, const int *Nv, int tmp_size, const float *cos_phi,
+                      const float *sin_phi, int na, int nb, const int64_t *vox, long nvx)
+{
+    for (long k = 0; k < nvx; k++) {
+        long v = vox[k];
+        int iz = (int)(v / ((long)nx * ny));
+        long r = v - (long)iz * nx * ny;
+        int iy = (int)(r / nx), ix = (int)(r - (long)iy * nx);
+        x[k] = orc_cone_adj_voxel(Y, SO, OD, scale, nx, ny, nz, sd_z, y_det, z_det, dy_det,
+                                  y_os, dz_det, dz, id_Y, Nv, tmp_size, cos_phi, sin_phi, na,
+                                  nb, ix, iy, iz, 0);
     }
 }
 
@@ -594,6 +660,133 @@ void orc_exact_count(int64_t *cnt, double SO, double OD, int nx, int ny, int nz,
                     orc_exact_walk(&g, S, D, NULL, NULL);
             }
         }
+    }
+}
+
+/* Exact forward for a list of rays (ray id iv*na*nb + ib*na + ia): y[k] is
+ * ray rays[k], as orc_exact_forward_f64 computes it. */
+void orc_exact_forward_rays(const double *X, double *y, double SO, double OD, double scale,
+                            int nx, int ny, int nz, double dz, const float *sd_phi,
+                            const float *sd_z, int na, int nb, const float *y_det,
+                            const float *z_det, const int64_t *rays, long nr)
+{
+    orc_grid g = {nx, ny, nz, dz};
+    long nd = (long)na * nb;
+    for (long k = 0; k < nr; k++) {
+        int iv = (int)(rays[k] / nd);
+        long r = rays[k] - (long)iv * nd;
+        int ib = (int)(r / na), ia = (int)(r - (long)ib * na);
+        double S[3], D[3];
+        orc_ray_points(SO, OD, (double)sd_phi[iv], sd_z ? (double)sd_z[iv] : 0.0,
+                       (double)y_det[ia], z_det ? (double)z_det[ib] : 0.0, S, D);
+        orc_fwd_ctx f = {X, 0.0};
+        orc_exact_walk(&g, S, D, orc_fwd_visit, &f);
+        y[k] = scale * f.acc;
+    }
+}
+
+/* Length of the segment S->D inside the box [lo, hi] (FP64 slab method). */
+static double orc_box_chord(const double S[3], const double D[3], const double lo[3],
+                            const double hi[3])
+{
+    double t0 = 0.0, t1 = 1.0, len2 = 0.0;
+    for (int a = 0; a < 3; a++) {
+        double d = D[a] - S[a];
+        len2 += d * d;
+        if (d == 0.0) {
+            if (S[a] < lo[a] || S[a] >= hi[a]) return 0.0;
+            continue;
+        }
+        double u = (lo[a] - S[a]) / d, v = (hi[a] - S[a]) / d;
+        if (u > v) { double t = u; u = v; v = t; }
+        if (u > t0) t0 = u;
+        if (v < t1) t1 = v;
+    }
+    return t1 > t0 ? (t1 - t0) * sqrt(len2) : 0.0;
+}
+
+/* Indices [*i0, *i1] of a monotonic grid g[0..n) whose values lie in [lo, hi],
+ * widened by one index on each side (the whole grid when it is not monotonic). */
+static void orc_grid_range(const float *g, int n, double lo, double hi, int *i0, int *i1)
+{
+    int asc = 1, desc = 1;
+    if (n > 1) { asc = g[n - 1] >= g[0]; desc = !asc; }
+    for (int k = 1; k < n && (asc || desc); k++) {
+        if (g[k] < g[k - 1]) asc = 0;
+        if (g[k] > g[k - 1]) desc = 0;
+    }
+    if (!asc && !desc) { *i0 = 0; *i1 = n - 1; return; }
+    /* first index whose value is >= lo (ascending) / <= hi (descending) */
+    int a = 0, b = n;
+    while (a < b) {
+        int m = (a + b) / 2;
+        int before = asc ? (double)g[m] < lo : (double)g[m] > hi;
+        if (before) a = m + 1; else b = m;
+    }
+    int first = a;
+    a = 0; b = n;
+    while (a < b) {
+        int m = (a + b) / 2;
+        int inside_or_before = asc ? (double)g[m] <= hi : (double)g[m] >= lo;
+        if (inside_or_before) a = m + 1; else b = m;
+    }
+    int last = a - 1;
+    *i0 = first - 1 < 0 ? 0 : first - 1;
+    *i1 = last + 1 > n - 1 ? n - 1 : last + 1;
+}
+
+/*
+ * Exact transpose for a list of voxels of one frame (index iz*ny*nx + iy*nx +
+ * ix) of an FP32 sinogram y: x[k] = scale * sum over the rays of views
+ * [v0, v1) of len * y, in FP64, with len the FP64
+ * chord of each ray through voxel vox[k]. Per view, only the detector cells
+ * inside the projection of the voxel's eight corners (plus one cell on each
+ * side) are visited; every other ray misses the voxel. A fan is nz = 1,
+ * nb = 1, z_det = {0}, dz = 1.
+ */
+void orc_exact_adjoint_vox(double *x, const float *y, double SO, double OD, double scale,
+                           int nx, int ny, int nz, double dz, int v0, int v1,
+                           const float *sd_phi, const float *sd_z, int na, int nb,
+                           const float *y_det, const float *z_det, const int64_t *vox,
+                           long nvx)
+{
+    long nd = (long)na * nb;
+    double SD = SO + OD;
+    for (long k = 0; k < nvx; k++) {
+        long v = vox[k];
+        int iz = (int)(v / ((long)nx * ny));
+        long r = v - (long)iz * nx * ny;
+        int iy = (int)(r / nx), ix = (int)(r - (long)iy * nx);
+        double lo[3] = {(double)(ix - nx / 2), (double)(iy - ny / 2), (iz - nz / 2) * dz};
+        double hi[3] = {lo[0] + 1.0, lo[1] + 1.0, lo[2] + dz};
+        double acc = 0.0;
+        for (int iv = v0; iv < v1; iv++) {
+            double c = cos((double)sd_phi[iv]), s = sin((double)sd_phi[iv]);
+            double sz = sd_z ? (double)sd_z[iv] : 0.0;
+            double umin = INFINITY, umax = -INFINITY, wmin = INFINITY, wmax = -INFINITY;
+            for (int q = 0; q < 8; q++) {
+                double px = (q & 1) ? hi[0] : lo[0], py = (q & 2) ? hi[1] : lo[1];
+                double pz = (q & 4) ? hi[2] : lo[2];
+                double depth = SO + c * px + s * py, lat = -s * px + c * py;
+                double u = SD * lat / depth, w = SD * (pz - sz) / depth;
+                if (u < umin) umin = u;
+                if (u > umax) umax = u;
+                if (w < wmin) wmin = w;
+                if (w > wmax) wmax = w;
+            }
+            int a0, a1, b0 = 0, b1 = 0;
+            orc_grid_range(y_det, na, umin, umax, &a0, &a1);
+            if (z_det) orc_grid_range(z_det, nb, wmin, wmax, &b0, &b1);
+            for (int ib = b0; ib <= b1; ib++)
+                for (int ia = a0; ia <= a1; ia++) {
+                    double S[3], D[3];
+                    orc_ray_points(SO, OD, (double)sd_phi[iv], sz, (double)y_det[ia],
+                                   z_det ? (double)z_det[ib] : 0.0, S, D);
+                    double l = orc_box_chord(S, D, lo, hi);
+                    if (l > 0.0) acc += l * (double)y[(long)iv * nd + (long)ib * na + ia];
+                }
+        }
+        x[k] = scale * acc;
     }
 }
 

@@ -1,0 +1,85 @@
+"""Parity of a projector pair at a configuration's own size (test infrastructure).
+
+TEST INFRASTRUCTURE ONLY: used by ``tests/`` and by the parity leg of
+``bench.py`` as the checker of GPU results. It never runs on the product path.
+
+The GPU side is passed in as two callables on host arrays, ``forward(x) -> y``
+and ``adjoint(y) -> x`` (full sinogram / full volume, FP32). Three numbers are
+reported for each operator, as relative L2 errors over the sampled entries:
+
+* ``matched_vs_fp64``: the GPU result against the FP64 exact Siddon model
+  (exact intersection lengths of the same rays);
+* ``reference_vs_fp64``: the reference's own FP32 CPU kernel against the same
+  FP64 model (``Ax_*_mf_cpu_siddon`` forward, ``Atx_*_mf_cpu_new`` chord
+  backprojector), i.e. the reference's own error;
+* ``matched_vs_reference``: the GPU result against the reference kernel.
+
+The fan is checked in full. A cone volume is checked on seeded random
+subsets: the forward on a set of rays, the backprojection on a set of voxels,
+each subset value computed by the oracle exactly as the full function would
+(``tests/test_oracle_pin.py`` pins the subset functions to the full ones).
+Two sinograms feed the backprojectors: the GPU forward projection of the
+phantom (the sinogram a reconstruction sees) and N(0, 1) noise (every matrix
+entry's error shows, none averages out).
+"""
+from __future__ import annotations
+
+import os
+
+import numpy as np
+
+from . import (cone_adj_vox, cone_siddon_rays, exact_adjoint, exact_adjoint_vox,
+               exact_forward, exact_forward_rays, fan_adj_f32, fan_siddon_f32)
+
+
+def rel(a, b) -> float:
+    a = np.asarray(a, np.float64).reshape(-1)
+    b = np.asarray(b, np.float64).reshape(-1)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def _three(gpu, ref, exact) -> dict:
+    return {"matched_vs_fp64": rel(gpu, exact), "reference_vs_fp64": rel(ref, exact),
+            "matched_vs_reference": rel(gpu, ref)}
+
+
+def _threads(threads):
+    return threads or max(1, os.cpu_count() or 1)
+
+
+def fan_parity(para, x, forward, adjoint, seed=0, threads=None) -> dict:
+    """Full fan-beam check: every ray, every pixel."""
+    t = _threads(threads)
+    x = np.ascontiguousarray(x, np.float32).reshape(-1)
+    y = np.asarray(forward(x), np.float32).reshape(-1)
+    out = {"forward": dict(rays=int(y.size), **_three(y, fan_siddon_f32(x, para, threads=t),
+                                                     exact_forward(x, para, threads=t)))}
+    rng = np.random.default_rng(seed)
+    for name, sino in (("phantom", y), ("random", rng.standard_normal(y.size).astype(np.float32))):
+        xa = np.asarray(adjoint(sino), np.float32).reshape(-1)
+        out[f"adjoint_{name}_sino"] = dict(
+            voxels=int(xa.size), **_three(xa, fan_adj_f32(sino, para, threads=t),
+                                          exact_adjoint(sino, para, threads=t)))
+    return out
+
+
+def cone_parity(para, x, forward, adjoint, n_rays=20000, n_vox=4000, seed=0,
+                threads=None) -> dict:
+    """Cone-beam check on ``n_rays`` random rays and ``n_vox`` random voxels."""
+    t = _threads(threads)
+    rng = np.random.default_rng(seed)
+    x = np.ascontiguousarray(x, np.float32).reshape(-1)
+    y = np.asarray(forward(x), np.float32).reshape(-1)
+    rays = np.sort(rng.choice(y.size, min(n_rays, y.size), replace=False))
+    out = {"forward": dict(rays=int(rays.size), **_three(
+        y[rays], cone_siddon_rays(x, para, rays, threads=t),
+        exact_forward_rays(x, para, rays, threads=t)))}
+    vox = np.sort(rng.choice(x.size, min(n_vox, x.size), replace=False))
+    for name in ("phantom", "random"):
+        sino = y if name == "phantom" else rng.standard_normal(y.size).astype(np.float32)
+        xa = np.asarray(adjoint(sino), np.float32).reshape(-1)
+        out[f"adjoint_{name}_sino"] = dict(voxels=int(vox.size), **_three(
+            xa[vox], cone_adj_vox(sino, para, vox, threads=t),
+            exact_adjoint_vox(sino, para, vox, threads=t)))
+        del sino
+    return out

@@ -15,7 +15,7 @@ def test_gradient_matches_central_differences():
     x = torch.from_numpy(PH.ellipsoids_3d(48, seed=1)).cuda().reshape(P.vol_shape)
     b = project(x * 1.1 + 0.05, P).detach()
     err, idx = fd_gradcheck(P, x, b, n_vox=64, h=1e-3)
-    assert err < 2e-2, err
+    assert err < 1e-3, err
 
 
 def test_backward_is_the_adjoint():

@@ -107,3 +107,25 @@ def test_restatement_matches_golden(path):
     else:
         pytest.skip(f"no restatement for {kind}")
     assert np.array_equal(out, case["y"]), kind
+
+
+@pytest.mark.parametrize("scan", ["circle", "helix"])
+def test_subset_functions_equal_the_full_ones(scan):
+    """The ray- and voxel-subset oracles used for parity at full problem size
+    return, at every sampled entry, exactly what the full functions write
+    (FP32 restatements bit for bit; the FP64 voxel chord sum to FP64
+    rounding against the FP64 Siddon transpose)."""
+    rng = np.random.default_rng(11)
+    p = _rand_cone(rng, 20, 36, 28, 10, scan)
+    X = rng.standard_normal(20 ** 3).astype(np.float32)
+    y = O.cone_siddon_f32(X, p)
+    rays = rng.choice(y.size, 400, replace=False)
+    assert np.array_equal(O.cone_siddon_rays(X, p, rays, threads=2), y[rays])
+    e = O.exact_forward(X, p)
+    assert np.array_equal(O.exact_forward_rays(X, p, rays, threads=2), e[rays])
+    Y = rng.standard_normal(y.size).astype(np.float32)
+    vox = rng.choice(X.size, 300, replace=False)
+    assert np.array_equal(O.cone_adj_vox(Y, p, vox, threads=2), O.cone_adj_f32(Y, p)[vox])
+    ea = O.exact_adjoint(Y, p)
+    got = O.exact_adjoint_vox(Y, p, vox, threads=2)
+    assert np.max(np.abs(got - ea[vox])) <= 1e-12 * np.max(np.abs(ea))
