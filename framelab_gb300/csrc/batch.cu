@@ -125,10 +125,8 @@ k_batch_fwd(const float* __restrict__ X, float* __restrict__ Y,
     const BatchSlice& b = sl[ch.x];
     const int r = ch.y + threadIdx.x;
     if (r >= b.na * b.nv) return;
-    const ColEntry ce = b.col[r];
-    float acc = walk<float, false, false>(X + b.xoff, ce.inv_x, ce.off_x, ce.inv_y, ce.off_y,
-                                          0.0f, 0.0f, b.nx, b.ny, 1, nullptr, nullptr,
-                                          (long long)b.nx * b.ny);
+    float acc = walk<float, false, false>(X + b.xoff, b.col + r, &b.col[r].y, b.nx, b.ny, 1,
+                                          nullptr, nullptr, (long long)b.nx * b.ny);
     float cr = ray_cr(b.scale, b.colr[r], 0.0f);
     float out = cr * acc;
     if (cr_power == 2) out = cr * out;

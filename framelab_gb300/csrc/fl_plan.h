@@ -5,17 +5,37 @@
 
 #include "framelab_gb300.h"
 
-// Per-ray parameters of the matched Siddon model. A ray's plane crossings are
-// A_a(k) = fmaf(k, inv_a, off_a) for plane index k on axis a (x, y: planes at
-// k - n/2; z: planes at (k - nz/2)*dz), an affine re-parameterisation
-// A = alpha - alpha_c(view) of the source->detector parameter alpha, centred
-// near the isocentre for precision. The forward walk and the adjoint gather
-// read the same FP32 table entries, so both see identical crossings.
+// Per-ray parameters of the matched Siddon model, one AxisEntry per axis.
+// The ray crosses plane k of an axis (x, y: planes at k - n/2; z: planes at
+// (k - nz/2)*dz) at A(k) = alpha(k) - alpha_c(view), the source->detector
+// parameter measured from the isocentre crossing, with
+//     A(k) = (k - kq) * (ih + il) + c,
+// where kq is a quantised plane coordinate of the ray's isocentre crossing
+// (its quantum makes k - kq exact in FP32 for every plane the kernels use),
+// ih + il the FP64 pitch/d rounded to a pair of floats and c the rest of
+// the quantisation. Built in FP64 on the host, rounded once per field.
+//
+// The kernels never use an A(k) on its own: a ray's path is cut into
+// segments of 2^SH planes of its dominant xy axis (the one with the
+// smaller |ih|), and within segment s every crossing is taken relative to
+// the anchor B_s = A_D(kA) of the dominant axis D at the segment's middle
+// plane kA, held as bh + be (make_anchor, matched_dev.cuh):
+//     t(k) = fma(m, ih, -bh) + fma(m, il, c - be),   m = k - kq.
+// t is a small number (a few voxels of path), so the difference of two
+// crossings -- the weight -- carries FP32 rounding of t, not of A: the
+// weight's relative error stays near 1e-7 whatever the size of the volume.
+// The forward walk and the backprojection gather evaluate this same
+// expression from the same table entries, so both see identical crossings.
+struct AxisEntry {
+    float kq, ih, il, c;
+};
 struct ColEntry {   // per (view, detector column): x and y axes
-    float inv_x, off_x, inv_y, off_y;
+    AxisEntry x, y;
 };
 struct RowEntry {   // per (view, detector row): z axis (cone only)
-    float inv_z, off_z, rinv_z, dz2;   // dz2 = fl(d_z^2)
+    AxisEntry z;
+    float dz2;        // fl(d_z^2), for c_r
+    float pad[3];
 };
 struct ViewEntry {  // per view, for the adjoint's detector windows
     float c, s;       // cos/sin of the source angle
@@ -38,7 +58,7 @@ struct fl_plan {
     ColEntry *d_col;           // [nv*na]
     float *d_colr;             // [nv*na] fl(d_x^2 + d_y^2)
     RowEntry *d_row;           // [nv*nb]
-    float2 *d_rowz;            // [nv*nb] (inv_z, off_z): the backprojector's 8-byte copy
+    AxisEntry *d_rowz;         // [nv*nb] z axes: the backprojector's 16-byte copy
     ViewEntry *d_view;         // [nv]
     // detector grid for the adjoint windows (matched model)
     int det_kind;              // 0 flat uniform, 1 equiangular (fan), -1 irregular

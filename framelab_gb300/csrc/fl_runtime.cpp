@@ -100,6 +100,34 @@ static double nudge(double d, double len)
     return d;
 }
 
+// One axis of a ray (fl_plan.h): crossings A(k) = (k - K) * inv for plane
+// index k in [0, n], with K the plane coordinate of the ray's isocentre
+// crossing. K is quantised to kq, a multiple of a power of two chosen so that
+// every k - kq the kernels form (k in [-1, n + 1]) has at most 24 significant
+// bits, i.e. is exact in FP32; c carries the quantisation remainder.
+static AxisEntry axis_entry(double K, double inv, int n)
+{
+    double span = std::fmax(std::fabs(K + 1.0), std::fabs((double)n + 1.0 - K)) + 2.0;
+    int e = 0;
+    std::frexp(span, &e);                        // span < 2^e
+    double q = std::ldexp(1.0, e - 23);          // |k - kq| / q < 2^23 + ...
+    double kq = std::nearbyint(K / q) * q;
+    AxisEntry a;
+    a.kq = (float)kq;                            // exact: 24 significant bits at most
+    a.ih = (float)inv;
+    a.il = (float)(inv - (double)a.ih);
+    a.c = (float)((kq - K) * inv);
+    return a;
+}
+
+// Finite, and kq within 2^22 planes (its quantum is then at most 1, so every
+// k - kq of an integer k is exact).
+static bool axis_finite(const AxisEntry& a)
+{
+    return std::isfinite(a.kq) && std::isfinite(a.ih) && std::isfinite(a.il) &&
+           std::isfinite(a.c) && a.ih != 0.0f && std::fabs(a.kq) < 4194304.0f;
+}
+
 static int build_tables(fl_plan* p, const std::vector<float>& phi, const float* sd_z,
                         const float* y_det, const float* z_det)
 {
@@ -120,22 +148,20 @@ static int build_tables(fl_plan* p, const std::vector<float>& phi, const float* 
             double dx = (OD * c - u * sn) - Sx, dy = (OD * sn + u * c) - Sy;
             double len = std::sqrt(dx * dx + dy * dy);
             dx = nudge(dx, len); dy = nudge(dy, len);
+            // the ray's isocentre crossing P = S + ac d, in plane coordinates
             ColEntry e;
-            e.inv_x = (float)(1.0 / dx);
-            e.off_x = (float)((-nx2 - Sx) / dx - ac);
-            e.inv_y = (float)(1.0 / dy);
-            e.off_y = (float)((-ny2 - Sy) / dy - ac);
+            e.x = axis_entry(nx2 + (Sx + ac * dx), 1.0 / dx, s.nx);
+            e.y = axis_entry(ny2 + (Sy + ac * dy), 1.0 / dy, s.ny);
             col[(size_t)iv * s.na + ia] = e;
             colr[(size_t)iv * s.na + ia] = (float)(dx * dx + dy * dy);
         }
         for (int ib = 0; ib < s.nb; ib++) {
-            RowEntry r{0.0f, 0.0f, 0.0f, 0.0f};
+            RowEntry r{};
+            r.z = AxisEntry{0.0f, 1.0f, 0.0f, 0.0f};
             if (s.ndim == 3) {
                 double dzr = nudge((double)z_det[ib], SD);   // detector z - source z
                 double pitch = s.dz;
-                r.inv_z = (float)(pitch / dzr);
-                r.off_z = (float)((-nz2 * pitch - Sz) / dzr - ac);
-                r.rinv_z = (float)(dzr / pitch);
+                r.z = axis_entry(nz2 + (Sz + ac * dzr) / pitch, pitch / dzr, s.nz);
                 r.dz2 = (float)(dzr * dzr);
             }
             row[(size_t)iv * s.nb + ib] = r;
@@ -143,18 +169,17 @@ static int build_tables(fl_plan* p, const std::vector<float>& phi, const float* 
     }
     // every crossing parameter the kernels read must be finite
     for (const ColEntry& e : col)
-        if (!std::isfinite(e.inv_x) || !std::isfinite(e.off_x) || !std::isfinite(e.inv_y) ||
-            !std::isfinite(e.off_y))
+        if (!axis_finite(e.x) || !axis_finite(e.y))
             return fl_set_error(FL_ERR_INVALID, "geometry gives a non-finite ray parameter");
     for (const RowEntry& r : row)
-        if (!std::isfinite(r.inv_z) || !std::isfinite(r.off_z) || !std::isfinite(r.rinv_z))
+        if (!axis_finite(r.z))
             return fl_set_error(FL_ERR_INVALID, "geometry gives a non-finite ray parameter");
     int st;
     if ((st = upload(&p->d_col, col.data(), col.size()))) return st;
     if ((st = upload(&p->d_colr, colr.data(), colr.size()))) return st;
     if ((st = upload(&p->d_row, row.data(), row.size()))) return st;
-    std::vector<float2> rowz(row.size());
-    for (size_t i = 0; i < row.size(); i++) rowz[i] = make_float2(row[i].inv_z, row[i].off_z);
+    std::vector<AxisEntry> rowz(row.size());
+    for (size_t i = 0; i < row.size(); i++) rowz[i] = row[i].z;
     if ((st = upload(&p->d_rowz, rowz.data(), rowz.size()))) return st;
     if ((st = upload(&p->d_view, view.data(), view.size()))) return st;
 
@@ -213,7 +238,9 @@ static int build_tables(fl_plan* p, const std::vector<float>& phi, const float* 
     // fan plans: no mirror, ny even (the rows y < ny/2 are the primary half)
     p->rot_ok = 0;
     const bool cone_turn = s.ndim == 3 && p->zmirror_ok && s.nx % 4 == 0 && s.ny % 4 == 0;
-    const bool fan_turn = s.ndim == 2 && s.ny % 2 == 0;
+    // fan turn plans: even nx and ny, so a turned 2 x 2 pixel block starts at
+    // even coordinates and lies in one segment of the matched model's frames
+    const bool fan_turn = s.ndim == 2 && s.ny % 2 == 0 && s.nx % 2 == 0;
     if ((cone_turn || fan_turn) && s.nt == 1 && p->views_natural && s.nv % 2 == 0) {
         bool ok = true;
         const int h = s.nv / 2;

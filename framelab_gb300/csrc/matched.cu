@@ -2,19 +2,20 @@
 //
 // Matrix. For ray r and voxel V = (ix, iy, iz) the entry is
 //     A[r,V] = c_r * w_rV,   c_r = scale * |D - S|,
-//     w_rV   = fl( min_a max(A_a(i_a), A_a(i_a+1)) - max_a min(A_a(i_a), A_a(i_a+1)) )
-// when positive, where A_a(k) = fmaf(k, inv_a, off_a) are the FP32 plane
-// crossings of the ray (fl_plan.h). This is the exact Siddon intersection
-// length evaluated with FP32 crossing parameters.
+//     w_rV   = fl( min_a U_a(V) - max_a L_a(V) )
+// when positive, where L_a / U_a are the crossings of the planes at which the
+// ray enters / leaves V's slab on axis a, evaluated in the frame of the
+// segment of the ray's dominant axis that holds V (fl_plan.h,
+// matched_dev.cuh). This is the exact Siddon intersection length with FP32
+// arithmetic on small, anchored crossing parameters.
 //
-// Forward: one thread per ray walks the crossings in increasing order (an
-// incremental Siddon walk: three candidate crossings, step the smallest). The
-// segment it accumulates inside V is exactly w_rV above: its start is the
-// latest crossing behind V, its end the earliest crossing ahead.
+// Forward: one thread per ray walks each segment's sub-box, stepping the
+// smallest next crossing (an incremental Siddon walk); the segment it
+// accumulates inside V is exactly w_rV above.
 //
 // Adjoint: one thread per voxel column gathers over the rays whose detector
 // window covers the column and evaluates the same w_rV from the same table
-// entries -- the exact transpose, with no atomics.
+// entries in the same frame -- the exact transpose, with no atomics.
 #include <algorithm>
 
 #include "fl_trace.h"
@@ -33,7 +34,7 @@ namespace {
 // ray's mirrored companion, row nb-1-ib, from the same walk. yfold selects
 // the folded sinogram layout (pairs of rows ib and nb-1-ib) for the output.
 template <typename TX, typename TY, bool MIRROR>
-__global__ void __launch_bounds__(128, MIRROR ? 12 : 16)
+__global__ void __launch_bounds__(128, 8)
 k_fwd_cone(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restrict__ col,
            const float* __restrict__ colr, const RowEntry* __restrict__ row,
            const int* __restrict__ vframe, int nx, int ny, int nz, int na, int nb,
@@ -48,14 +49,13 @@ k_fwd_cone(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restr
     int iv = blockIdx.y;
     int ib = blockIdx.z * blockDim.y + threadIdx.y;
     if (ia >= na || ib >= (MIRROR ? nb / 2 : nb)) return;
-    ColEntry ce = col[(long long)iv * na + ia];
-    RowEntry re = row[(long long)iv * nb + ib];
+    const ColEntry* ce = col + (long long)iv * na + ia;
+    const RowEntry* re = row + (long long)iv * nb + ib;
     const TX* x = X + (long long)vframe[iv] * nper;
     float accm = 0.0f;
-    float acc = walk<TX, true, false, MIRROR>(x, ce.inv_x, ce.off_x, ce.inv_y, ce.off_y,
-                                              re.inv_z, re.off_z, nx, ny, nz, nullptr, &accm,
-                                              nper);
-    float cr = ray_cr(scale, colr[(long long)iv * na + ia], re.dz2);
+    float acc = walk<TX, true, false, MIRROR>(x, ce, &re->z, nx, ny, nz, nullptr,
+                                              &accm, nper);
+    float cr = ray_cr(scale, colr[(long long)iv * na + ia], __ldg(&re->dz2));
     if (xscale) { acc *= *xscale; accm *= *xscale; }
     float out = cr * acc;
     if (cr_power == 2) out = cr * out;
@@ -81,7 +81,7 @@ k_fwd_cone(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restr
 // ia) the 4 values (views iv, iv + nv/2; rows ib, nb-1-ib) side by side
 // (k_weight_packed<TY, 2>).
 template <typename TX, typename TY>
-__global__ void __launch_bounds__(128, 12)
+__global__ void __launch_bounds__(128, 8)
 k_fwd_quad(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restrict__ col,
            const float* __restrict__ colr, const RowEntry* __restrict__ row, int nx, int ny,
            int nz, int na, int nb, int nv, long long nper, float scale, int cr_power,
@@ -93,12 +93,11 @@ k_fwd_quad(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restr
     const int ib = blockIdx.z * blockDim.y + threadIdx.y;
     const int nbh = nb / 2, hv = nv / 2;
     if (ia >= na || ib >= nbh) return;
-    const ColEntry ce = col[(long long)iv * na + ia];
-    const RowEntry re = row[(long long)iv * nb + ib];
+    const ColEntry* ce = col + (long long)iv * na + ia;
+    const RowEntry* re = row + (long long)iv * nb + ib;
     float2 a, r;
-    walk_quad<TX>(X, ce.inv_x, ce.off_x, ce.inv_y, ce.off_y, re.inv_z, re.off_z, nx, ny, nz, &a,
-                  &r, nper);
-    float cr = ray_cr(scale, colr[(long long)iv * na + ia], re.dz2);
+    walk_quad<TX>(X, ce, &re->z, nx, ny, nz, &a, &r, nper);
+    float cr = ray_cr(scale, colr[(long long)iv * na + ia], __ldg(&re->dz2));
     if (xscale) {
         const float xs = *xscale;
         a.x *= xs; a.y *= xs; r.x *= xs; r.y *= xs;
@@ -137,11 +136,11 @@ k_fwd_oct(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restri
     const int ib = blockIdx.z * blockDim.y + threadIdx.y;
     const int nbh = nb / 2, qv = nv / 4;
     if (ia >= na || ib >= nbh) return;
-    const ColEntry ce = col[(long long)iv * na + ia];
-    const RowEntry re = row[(long long)iv * nb + ib];
+    const ColEntry* ce = col + (long long)iv * na + ia;
+    const RowEntry* re = row + (long long)iv * nb + ib;
     float2 a[4];
-    walk_oct<TX>(X, ce.inv_x, ce.off_x, ce.inv_y, ce.off_y, re.inv_z, re.off_z, n, nz, a, nper);
-    float cr = ray_cr(scale, colr[(long long)iv * na + ia], re.dz2);
+    walk_oct<TX>(X, ce, &re->z, n, nz, a, nper);
+    float cr = ray_cr(scale, colr[(long long)iv * na + ia], __ldg(&re->dz2));
     const float xs = xscale ? *xscale : 1.0f;
 #pragma unroll
     for (int j = 0; j < 4; j++) {
@@ -170,10 +169,9 @@ k_fwd_fan(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restri
     long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= (long long)na * nv) return;
     int iv = (int)(r / na);
-    ColEntry ce = col[r];
     const TX* x = X + (long long)vframe[iv] * nper;
     float a1[1];
-    walk_fan<TX, 1>(x, ce.inv_x, ce.off_x, ce.inv_y, ce.off_y, nx, ny, a1, nper);
+    walk_fan<TX, 1>(x, &col[r].x, &col[r].y, nx, ny, a1, nper);
     float acc = a1[0];
     float cr = ray_cr(scale, colr[r], 0.0f);
     if (xscale) acc *= *xscale;
@@ -208,15 +206,13 @@ k_count(int32_t* __restrict__ cnt, const ColEntry* __restrict__ col,
     long long q = r / na;
     int ib = (int)(q % nb);
     int iv = (int)(q / nb);
-    ColEntry ce = col[(long long)iv * na + ia];
+    const ColEntry* ce = col + (long long)iv * na + ia;
     int c = 0;
     if (three) {
-        RowEntry re = row[(long long)iv * nb + ib];
-        walk<float, true, true>(nullptr, ce.inv_x, ce.off_x, ce.inv_y, ce.off_y, re.inv_z,
-                                re.off_z, nx, ny, nz, &c);
+        const RowEntry* re = row + (long long)iv * nb + ib;
+        walk<float, true, true>(nullptr, ce, &re->z, nx, ny, nz, &c);
     } else {
-        walk<float, false, true>(nullptr, ce.inv_x, ce.off_x, ce.inv_y, ce.off_y, 0.0f, 0.0f,
-                                 nx, ny, 1, &c);
+        walk<float, false, true>(nullptr, ce, &ce->y, nx, ny, 1, &c);
     }
     cnt[r] = c;
 }
@@ -430,7 +426,7 @@ k_adj_fan_turn(TX* __restrict__ X, const float* __restrict__ ywp,
 template <int MODE, int TZ>
 __device__ __forceinline__ void adj_rows(float (&acc)[TZ], int nk, int z0, float l, float h,
                                          float e1, float e2, float s1, float s2,
-                                         const float2* __restrict__ rv,
+                                         const AxisEntry* __restrict__ rv, float bh, float be,
                                          const float* __restrict__ ycol, int na, int nb)
 {
     float mn = fminf(e1, e2), mx = fmaxf(e1, e2);   // row span at plane k
@@ -445,10 +441,10 @@ __device__ __forceinline__ void adj_rows(float (&acc)[TZ], int nk, int z0, float
         const float fk0 = (float)(z0 + k), fk1 = (float)(z0 + k + 1);
         for (int ib = blo; ib <= bhi; ib++) {
             if (!FL_IN(ib, nb)) continue;
-            const float2 re = rv[ib];                 // (inv_z, off_z) of row ib
+            const AxisEntry re = rv[ib];                 // (inv_z, off_z) of row ib
             const float yval = __ldg(ycol + (long long)ib * na);
-            const float az0 = fmaf(fk0, re.x, re.y);
-            const float az1 = fmaf(fk1, re.x, re.y);
+            const float2 azp = row_planes(re, fk0, fk1, bh, be);
+            const float az0 = azp.x, az1 = azp.y;
             float l2, h2;
             if (MODE > 0)      { l2 = fmaxf(l, az0); h2 = fminf(h, az1); }
             else if (MODE < 0) { l2 = fmaxf(l, az1); h2 = fminf(h, az0); }
@@ -471,7 +467,7 @@ __device__ __forceinline__ void adj_rows(float (&acc)[TZ], int nk, int z0, float
 template <int MODE, int TZ>
 __device__ __forceinline__ void adj_rows_pair(float2 (&acc)[TZ], int nk, int z0, float l,
                                               float h, float e1, float e2, float s1, float s2,
-                                              const float2* __restrict__ rv,
+                                              const AxisEntry* __restrict__ rv, float bh, float be,
                                               const float* __restrict__ ycol, int na, int nb)
 {
     float mn = fminf(e1, e2), mx = fmaxf(e1, e2);
@@ -494,10 +490,9 @@ __device__ __forceinline__ void adj_rows_pair(float2 (&acc)[TZ], int nk, int z0,
         const float fk0 = (float)(z0 + k), fk1 = (float)(z0 + k + 1);
         for (int ib = blo; ib <= bhi; ib++) {
             if (!FL_IN(ib, nb)) continue;
-            const float2 re = rv[ib];
+            const AxisEntry re = rv[ib];
             const float2 t = Store<float>::ld2(ycol + 2 * (long long)ib * na);
-            const float2 az = __ffma2_rn(make_float2(fk0, fk1), make_float2(re.x, re.x),
-                                         make_float2(re.y, re.y));
+            const float2 az = row_planes(re, fk0, fk1, bh, be);
             float l2, h2;
             if (MODE < 0) { l2 = fmaxf(l, az.y); h2 = fminf(h, az.x); }
             else { l2 = fmaxf(l, fminf(az.x, az.y)); h2 = fminf(h, fmaxf(az.x, az.y)); }
@@ -513,7 +508,7 @@ __device__ __forceinline__ void adj_rows_pair(float2 (&acc)[TZ], int nk, int z0,
 template <int MODE, int TZ>
 __device__ __forceinline__ void adj_rows_quad(float2 (&acc)[TZ], float2 (&accr)[TZ], int nk,
                                               int z0, float l, float h, float e1, float e2,
-                                              float s1, float s2, const float2* __restrict__ rv,
+                                              float s1, float s2, const AxisEntry* __restrict__ rv, float bh, float be,
                                               const float* __restrict__ y4, int na, int nb)
 {
     float mn = fminf(e1, e2), mx = fmaxf(e1, e2);
@@ -536,11 +531,10 @@ __device__ __forceinline__ void adj_rows_quad(float2 (&acc)[TZ], float2 (&accr)[
         const float fk0 = (float)(z0 + k), fk1 = (float)(z0 + k + 1);
         for (int ib = blo; ib <= bhi; ib++) {
             if (!FL_IN(ib, nb)) continue;
-            const float2 re = rv[ib];
+            const AxisEntry re = rv[ib];
             const float4 u = __ldg(reinterpret_cast<const float4*>(y4 + 4 * (long long)ib * na));
             const float2 t = make_float2(u.x, u.y), tr = make_float2(u.z, u.w);
-            const float2 az = __ffma2_rn(make_float2(fk0, fk1), make_float2(re.x, re.x),
-                                         make_float2(re.y, re.y));
+            const float2 az = row_planes(re, fk0, fk1, bh, be);
             float l2, h2;
             if (MODE < 0) { l2 = fmaxf(l, az.y); h2 = fminf(h, az.x); }
             else { l2 = fmaxf(l, fminf(az.x, az.y)); h2 = fminf(h, fmaxf(az.x, az.y)); }
@@ -563,7 +557,7 @@ __device__ __forceinline__ void adj_rows_quad(float2 (&acc)[TZ], float2 (&accr)[
 template <typename TX, int TZ>
 __global__ void __launch_bounds__(128, 8)
 k_adj_quad(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __restrict__ col,
-           const float2* __restrict__ rowz, const ViewEntry* __restrict__ view, DetGrid G,
+           const AxisEntry* __restrict__ rowz, const ViewEntry* __restrict__ view, DetGrid G,
            int nx, int ny, int nz, int na, int nb, int nv, float dz, int zruns,
            const int* __restrict__ skip, int xfold)
 {
@@ -583,7 +577,7 @@ k_adj_quad(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __r
     for (int iv = 0; iv < hv; iv++) {
         const ViewEntry ve = view[iv];
         const ColEntry* cv = col + (long long)iv * na;
-        const float2* rv = rowz + (long long)iv * nb;
+        const AxisEntry* rv = rowz + (long long)iv * nb;
         const float* yv = yw + (long long)iv * vstride;
         const float zr0 = (float)(z0 - nz / 2) * dz - ve.sz;
         const float zr1 = (float)(z0 + nk - nz / 2) * dz - ve.sz;
@@ -595,24 +589,21 @@ k_adj_quad(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __r
             int alo, ahi; float dmin, dmax;
             column_window(G, ve.c, ve.s, (float)(cx - nx / 2), (float)(cy - ny / 2), 1.0f, 1.0f,
                           na, alo, ahi, dmin, dmax);
-            const float fx0 = (float)cx, fx1 = (float)(cx + 1);
-            const float fy0 = (float)cy, fy1 = (float)(cy + 1);
             for (int ia = alo; ia <= ahi; ia++) {
                 if (!FL_IN(ia, na)) continue;
                 const ColEntry ce = cv[ia];
-                const float ax0 = fmaf(fx0, ce.inv_x, ce.off_x), ax1 = fmaf(fx1, ce.inv_x, ce.off_x);
-                const float ay0 = fmaf(fy0, ce.inv_y, ce.off_y), ay1 = fmaf(fy1, ce.inv_y, ce.off_y);
-                const float l = fmaxf(fminf(ax0, ax1), fminf(ay0, ay1));
-                const float h = fminf(fmaxf(ax0, ax1), fmaxf(ay0, ay1));
-                if (!(l < h)) continue;
-                const float r1 = __fdividef(1.0f, l + ve.ac), r2 = __fdividef(1.0f, h + ve.ac);
+                float bh, be, l, h;
+                if (!cone_column(ce, cx, cy, nx, ny, bh, be, l, h)) continue;
+                // absolute parameters of the column's ends (row windows only)
+                const float r1 = __fdividef(1.0f, __fadd_rn(bh, l) + ve.ac);
+                const float r2 = __fdividef(1.0f, __fadd_rn(bh, h) + ve.ac);
                 const float s1 = dz * r1 * inv_dv, s2 = dz * r2 * inv_dv;
                 const float e1 = (zr0 * r1 - G.v0) * inv_dv, e2 = (zr0 * r2 - G.v0) * inv_dv;
                 if (mode < 0)
-                    adj_rows_quad<-1, TZ>(own, other, nk, z0, l, h, e1, e2, s1, s2, rv,
+                    adj_rows_quad<-1, TZ>(own, other, nk, z0, l, h, e1, e2, s1, s2, rv, bh, be,
                                           yv + 4 * ia, na, nbw);
                 else
-                    adj_rows_quad<0, TZ>(own, other, nk, z0, l, h, e1, e2, s1, s2, rv,
+                    adj_rows_quad<0, TZ>(own, other, nk, z0, l, h, e1, e2, s1, s2, rv, bh, be,
                                          yv + 4 * ia, na, nbw);
             }
         };
@@ -646,7 +637,7 @@ template <int MODE, int TZ>
 __device__ __forceinline__ void adj_rows_oct(float2 (&a0)[TZ], float2 (&a1)[TZ],
                                              float2 (&a2)[TZ], float2 (&a3)[TZ], int nk, int z0,
                                              float l, float h, float e1, float e2, float s1,
-                                             float s2, const float2* __restrict__ rv,
+                                             float s2, const AxisEntry* __restrict__ rv, float bh, float be,
                                              const float* __restrict__ y8, int na, int nb)
 {
     float mn = fminf(e1, e2), mx = fmaxf(e1, e2);
@@ -669,15 +660,14 @@ __device__ __forceinline__ void adj_rows_oct(float2 (&a0)[TZ], float2 (&a1)[TZ],
         const float fk0 = (float)(z0 + k), fk1 = (float)(z0 + k + 1);
         for (int ib = blo; ib <= bhi; ib++) {
             if (!FL_IN(ib, nb)) continue;
-            const float2 re = rv[ib];
+            const AxisEntry re = rv[ib];
             // the orbit's 8 values in one 32-byte load (orbits are 32-byte aligned)
             float2 t0, t1, t2, t3;
             asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
                 : "=f"(t0.x), "=f"(t0.y), "=f"(t1.x), "=f"(t1.y), "=f"(t2.x), "=f"(t2.y),
                   "=f"(t3.x), "=f"(t3.y)
                 : "l"(y8 + 8 * (long long)ib * na));
-            const float2 az = __ffma2_rn(make_float2(fk0, fk1), make_float2(re.x, re.x),
-                                         make_float2(re.y, re.y));
+            const float2 az = row_planes(re, fk0, fk1, bh, be);
             float l2, h2;
             if (MODE < 0) { l2 = fmaxf(l, az.y); h2 = fminf(h, az.x); }
             else { l2 = fmaxf(l, fminf(az.x, az.y)); h2 = fminf(h, fmaxf(az.x, az.y)); }
@@ -701,7 +691,7 @@ __device__ __forceinline__ void adj_rows_oct(float2 (&a0)[TZ], float2 (&a1)[TZ],
 template <typename TX, int TZ>
 __global__ void __launch_bounds__(128, TZ == 2 ? 8 : 6)
 k_adj_oct(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __restrict__ col,
-          const float2* __restrict__ rowz, const ViewEntry* __restrict__ view, DetGrid G, int n,
+          const AxisEntry* __restrict__ rowz, const ViewEntry* __restrict__ view, DetGrid G, int n,
           int nz, int na, int nb, int nv, float dz, const int* __restrict__ skip, int xfold)
 {
     if (skip && *skip) return;
@@ -723,7 +713,7 @@ k_adj_oct(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __re
     for (int iv = 0; iv < qv; iv++) {
         const ViewEntry ve = view[iv];
         const ColEntry* cv = col + (long long)iv * na;
-        const float2* rv = rowz + (long long)iv * nb;
+        const AxisEntry* rv = rowz + (long long)iv * nb;
         const float* yv = yw + (long long)iv * vstride;
         const float zr0 = (float)(z0 - nz / 2) * dz - ve.sz;
         const float zr1 = (float)(z0 + nk - nz / 2) * dz - ve.sz;
@@ -736,25 +726,22 @@ k_adj_oct(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __re
             int alo, ahi; float dmin, dmax;
             column_window(G, ve.c, ve.s, (float)(px_ - h), (float)(py_ - h), 1.0f, 1.0f, na, alo,
                           ahi, dmin, dmax);
-            const float fx0 = (float)px_, fx1 = (float)(px_ + 1);
-            const float fy0 = (float)py_, fy1 = (float)(py_ + 1);
             for (int ia = alo; ia <= ahi; ia++) {
                 if (!FL_IN(ia, na)) continue;
                 const ColEntry ce = cv[ia];
-                const float ax0 = fmaf(fx0, ce.inv_x, ce.off_x), ax1 = fmaf(fx1, ce.inv_x, ce.off_x);
-                const float ay0 = fmaf(fy0, ce.inv_y, ce.off_y), ay1 = fmaf(fy1, ce.inv_y, ce.off_y);
-                const float l = fmaxf(fminf(ax0, ax1), fminf(ay0, ay1));
-                const float hh = fminf(fmaxf(ax0, ax1), fmaxf(ay0, ay1));
-                if (!(l < hh)) continue;
-                const float r1 = __fdividef(1.0f, l + ve.ac), r2 = __fdividef(1.0f, hh + ve.ac);
+                float bh, be, l, hh;
+                if (!cone_column(ce, px_, py_, n, n, bh, be, l, hh)) continue;
+                // absolute parameters of the column's ends (row windows only)
+                const float r1 = __fdividef(1.0f, __fadd_rn(bh, l) + ve.ac);
+                const float r2 = __fdividef(1.0f, __fadd_rn(bh, hh) + ve.ac);
                 const float s1 = dz * r1 * inv_dv, s2 = dz * r2 * inv_dv;
                 const float e1 = (zr0 * r1 - G.v0) * inv_dv, e2 = (zr0 * r2 - G.v0) * inv_dv;
                 const float* y8 = yv + 8 * ia;
                 if (mode < 0)
-                    adj_rows_oct<-1, TZ>(b0, b1, b2, b3, nk, z0, l, hh, e1, e2, s1, s2, rv, y8,
+                    adj_rows_oct<-1, TZ>(b0, b1, b2, b3, nk, z0, l, hh, e1, e2, s1, s2, rv, bh, be, y8,
                                          na, nbw);
                 else
-                    adj_rows_oct<0, TZ>(b0, b1, b2, b3, nk, z0, l, hh, e1, e2, s1, s2, rv, y8,
+                    adj_rows_oct<0, TZ>(b0, b1, b2, b3, nk, z0, l, hh, e1, e2, s1, s2, rv, bh, be, y8,
                                         na, nbw);
             }
         };
@@ -789,7 +776,7 @@ k_adj_oct(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __re
 template <typename TX, int TZ, bool MIRROR>
 __global__ void __launch_bounds__(128, 8)
 k_adj_cone(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __restrict__ col,
-           const float2* __restrict__ rowz, const ViewEntry* __restrict__ view,
+           const AxisEntry* __restrict__ rowz, const ViewEntry* __restrict__ view,
            const int* __restrict__ idY, const int* __restrict__ Nv, int tmp_size, DetGrid G,
            int nx, int ny, int nz, int na, int nb, float dz, int zruns,
            const int* __restrict__ skip, int xfold)
@@ -808,7 +795,6 @@ k_adj_cone(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __r
 #pragma unroll
     for (int k = 0; k < TZ; k++) { acc[k] = 0.0f; acc2[k] = make_float2(0.0f, 0.0f); }
     const float x0 = (float)(ix - nx / 2), y0 = (float)(iy - ny / 2);
-    const float fx0 = (float)ix, fx1 = (float)(ix + 1), fy0 = (float)iy, fy1 = (float)(iy + 1);
     const float inv_dv = 1.0f / G.dv;
     const int nvf = Nv[it];
     for (int j = 0; j < nvf; j++) {
@@ -817,7 +803,7 @@ k_adj_cone(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __r
         int alo, ahi; float dmin, dmax;
         column_window(G, ve.c, ve.s, x0, y0, 1.0f, 1.0f, na, alo, ahi, dmin, dmax);
         const ColEntry* cv = col + (long long)iv * na;
-        const float2* rv = rowz + (long long)iv * nb;
+        const AxisEntry* rv = rowz + (long long)iv * nb;
         const float* yv = yw + (long long)iv * nb * na;   // folded: nb/2 rows of pairs
         // run planes relative to the source: lowest and highest
         const float zr0 = (float)(z0 - nz / 2) * dz - ve.sz;
@@ -829,32 +815,30 @@ k_adj_cone(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __r
         for (int ia = alo; ia <= ahi; ia++) {
             if (!FL_IN(ia, na)) continue;
             const ColEntry ce = cv[ia];
-            const float ax0 = fmaf(fx0, ce.inv_x, ce.off_x), ax1 = fmaf(fx1, ce.inv_x, ce.off_x);
-            const float ay0 = fmaf(fy0, ce.inv_y, ce.off_y), ay1 = fmaf(fy1, ce.inv_y, ce.off_y);
-            const float l = fmaxf(fminf(ax0, ax1), fminf(ay0, ay1));
-            const float h = fminf(fmaxf(ax0, ax1), fmaxf(ay0, ay1));
-            if (!(l < h)) continue;
+            float bh, be, l, h;
+            if (!cone_column(ce, ix, iy, nx, ny, bh, be, l, h)) continue;
             // A ray of row ib is at z = sz + (A + ac) * d_ib, d_ib ~ v0 + ib * dv. It is
             // inside voxel k somewhere in [l, h] iff d_ib lies between the plane
             // heights over (A + ac) at the two ends: in detector-row units the
             // rows [e(k), e(k+1)], stepping by dz/(A + ac)/dv per plane.
-            const float r1 = __fdividef(1.0f, l + ve.ac), r2 = __fdividef(1.0f, h + ve.ac);
+            const float r1 = __fdividef(1.0f, __fadd_rn(bh, l) + ve.ac);
+            const float r2 = __fdividef(1.0f, __fadd_rn(bh, h) + ve.ac);
             const float s1 = dz * r1 * inv_dv, s2 = dz * r2 * inv_dv;
             const float e1 = (zr0 * r1 - G.v0) * inv_dv, e2 = (zr0 * r2 - G.v0) * inv_dv;
             if (MIRROR) {
                 const float* ycol = yv + 2 * ia;
                 if (mode < 0)
-                    adj_rows_pair<-1, TZ>(acc2, nk, z0, l, h, e1, e2, s1, s2, rv, ycol, na, nbw);
+                    adj_rows_pair<-1, TZ>(acc2, nk, z0, l, h, e1, e2, s1, s2, rv, bh, be, ycol, na, nbw);
                 else
-                    adj_rows_pair<0, TZ>(acc2, nk, z0, l, h, e1, e2, s1, s2, rv, ycol, na, nbw);
+                    adj_rows_pair<0, TZ>(acc2, nk, z0, l, h, e1, e2, s1, s2, rv, bh, be, ycol, na, nbw);
             } else {
                 const float* ycol = yv + ia;
                 if (mode > 0)
-                    adj_rows<1, TZ>(acc, nk, z0, l, h, e1, e2, s1, s2, rv, ycol, na, nbw);
+                    adj_rows<1, TZ>(acc, nk, z0, l, h, e1, e2, s1, s2, rv, bh, be, ycol, na, nbw);
                 else if (mode < 0)
-                    adj_rows<-1, TZ>(acc, nk, z0, l, h, e1, e2, s1, s2, rv, ycol, na, nbw);
+                    adj_rows<-1, TZ>(acc, nk, z0, l, h, e1, e2, s1, s2, rv, bh, be, ycol, na, nbw);
                 else
-                    adj_rows<0, TZ>(acc, nk, z0, l, h, e1, e2, s1, s2, rv, ycol, na, nbw);
+                    adj_rows<0, TZ>(acc, nk, z0, l, h, e1, e2, s1, s2, rv, bh, be, ycol, na, nbw);
             }
         }
     }

@@ -11,116 +11,286 @@ namespace {
 template <typename T>
 __device__ __forceinline__ float ldv(const T* p) { return Store<T>::ld(p); }
 
-// Slab index of the ray at parameter a on one axis, consistent with the FP32
-// crossings: inv > 0 -> A(j) <= a < A(j+1); inv < 0 -> A(j+1) <= a < A(j).
-__device__ __forceinline__ int start_slab(float a, float inv, float off, int n)
+// ---------------------------------------------------------------------------
+// Crossings in a segment frame (the model is described in fl_plan.h).
+// ---------------------------------------------------------------------------
+constexpr int kSegCone = 6;    // 3-D rays: segments of 64 planes of the dominant axis
+constexpr int kSegFan = 4;     // fan rays: segments of 16 planes
+
+// Crossing of the plane with m = k - kq relative to the anchor bh + be,
+// cb = c - be: the expression both projectors evaluate.
+__device__ __forceinline__ float xrel(const AxisEntry& a, float m, float bh, float cb)
 {
-    float t = floorf(__fdividef(a - off, inv));
-    t = fminf(fmaxf(t, 0.0f), (float)(n - 1));   // NaN -> 0
-    int j = (int)t;
-    if (inv > 0.0f) {
-        while (j < n - 1 && fmaf((float)(j + 1), inv, off) <= a) j++;
-        while (j > 0 && fmaf((float)j, inv, off) > a) j--;
+    return __fadd_rn(__fmaf_rn(m, a.ih, -bh), __fmaf_rn(m, a.il, cb));
+}
+
+// Both planes of a pair at once (m2 = (k0 - kq, k1 - kq)); per lane the same
+// roundings as xrel.
+__device__ __forceinline__ float2 xrel2(const AxisEntry& a, float2 m2, float bh, float cb)
+{
+    return __fadd2_rn(__ffma2_rn(m2, make_float2(a.ih, a.ih), make_float2(-bh, -bh)),
+                      __ffma2_rn(m2, make_float2(a.il, a.il), make_float2(cb, cb)));
+}
+
+// Absolute crossing of plane k, hi part only: for estimates (which segments a
+// ray meets, first guesses of its voxels) and detector windows, never a weight.
+__device__ __forceinline__ float xabs(const AxisEntry& a, float k)
+{
+    return __fmul_rn(__fsub_rn(k, a.kq), a.ih);
+}
+
+// A ray's dominant xy axis, which its segments are cut along: the one with
+// the smaller |ih| (the larger direction component).
+__device__ __forceinline__ bool x_dominant(const AxisEntry& X, const AxisEntry& Y)
+{
+    return fabsf(X.ih) <= fabsf(Y.ih);
+}
+
+// Anchor of segment s of a ray (dominant axis D of nD planes): the crossing of
+// the segment's middle plane (clamped to the volume) as bh + be, be holding
+// the rounding of bh exactly and the table's low parts.
+template <int SH>
+__device__ __forceinline__ void make_anchor(const AxisEntry& D, int s, int nD, float& bh,
+                                            float& be)
+{
+    const float m = __fsub_rn((float)min((s << SH) + (1 << (SH - 1)), nD), D.kq);
+    bh = __fmul_rn(m, D.ih);
+    be = __fadd_rn(__fmaf_rn(m, D.il, __fmaf_rn(m, D.ih, -bh)), D.c);
+}
+
+// First guess of the slab of an axis holding the absolute parameter a.
+__device__ __forceinline__ int slab_guess(const AxisEntry& ax, float a, int n)
+{
+    float k = floorf(__fadd_rn(ax.kq, __fdividef(a, ax.ih)));
+    k = fminf(fmaxf(k, 0.0f), (float)(n - 1));      // NaN -> 0
+    return (int)k;
+}
+
+// Slab j in [lo, hi) of an axis holding the parameter v of a frame: a
+// positive axis (ih > 0) t(j) <= v < t(j+1), a negative one t(j+1) <= v <
+// t(j), found from the guess j (clamped into the range). Each loop moves one
+// way and is bounded by the range.
+__device__ __forceinline__ int slab_at(const AxisEntry& a, bool pos, int j, int lo, int hi,
+                                       float v, float bh, float cb)
+{
+    j = min(max(j, lo), hi - 1);
+    if (pos) {
+        while (j + 1 < hi && xrel(a, __fsub_rn((float)(j + 1), a.kq), bh, cb) <= v) j++;
+        while (j > lo && xrel(a, __fsub_rn((float)j, a.kq), bh, cb) > v) j--;
     } else {
-        while (j > 0 && fmaf((float)j, inv, off) <= a) j--;
-        while (j < n - 1 && fmaf((float)(j + 1), inv, off) > a) j++;
+        while (j > lo && xrel(a, __fsub_rn((float)j, a.kq), bh, cb) <= v) j--;
+        while (j + 1 < hi && xrel(a, __fsub_rn((float)(j + 1), a.kq), bh, cb) > v) j++;
     }
     return j;
 }
 
-// Walk one ray through an nx*ny*nz volume (nz == 1 with no z axis for 2-D).
-// Returns sum over voxels of w * x; *nseg counts segments with w > 0.
-// Termination: every step advances at least one axis to a strictly larger
-// crossing (consecutive FP32 crossings of one axis are thousands of ulps
-// apart for any table fl_plan_create accepts), and the loop leaves as soon as
-// the crossing reaches the exit (or is NaN); the step budget nx+ny+nz+4 is a
-// second, independent bound.
-// MIRROR: x is the z-folded volume (pairs of voxel (ix, iy, iz < nz/2) and its
-// mirror (ix, iy, nz-1-iz), fl_plan.h); the ray must descend from the source
-// plane, so it stays in iz < nz/2. Every step gathers the pair: the voxel's
-// value goes to the return value and the mirror's, with the same segment
-// length, to *accm -- the companion ray of a scan symmetric about the source
-// plane (fl_plan::zmirror).
-// xlen: elements available at x (checked builds verify every gather index).
-template <typename TX, bool THREE, bool COUNT, bool MIRROR = false>
-__device__ __forceinline__ float walk(const TX* __restrict__ x, float inv_x, float off_x,
-                                      float inv_y, float off_y, float inv_z, float off_z,
-                                      int nx, int ny, int nz, int* nseg, float* accm = nullptr,
-                                      long long xlen = 0)
+// Which segments of its dominant axis a ray can cross: from the box's entry
+// and exit parameters (absolute hi parts), with one plane of margin on each
+// side (a segment it does not cross is found empty in its own frame). Returns
+// false for a ray that misses the box by more than the estimate's rounding.
+template <int SH>
+__device__ __forceinline__ bool seg_range(const AxisEntry& D, int nD, float a_in, float a_out,
+                                          int& s1, int& s2)
 {
-    float ax0 = fmaf(0.0f, inv_x, off_x), ax1 = fmaf((float)nx, inv_x, off_x);
-    float ay0 = fmaf(0.0f, inv_y, off_y), ay1 = fmaf((float)ny, inv_y, off_y);
-    float a_in = fmaxf(fminf(ax0, ax1), fminf(ay0, ay1));
-    float a_out = fminf(fmaxf(ax0, ax1), fmaxf(ay0, ay1));
-    if (THREE) {
-        float az0 = fmaf(0.0f, inv_z, off_z), az1 = fmaf((float)nz, inv_z, off_z);
-        a_in = fmaxf(a_in, fminf(az0, az1));
-        a_out = fminf(a_out, fmaxf(az0, az1));
-    }
-    if (!(a_in < a_out)) {
-        if (COUNT) *nseg = 0;
-        if (MIRROR) *accm = 0.0f;
-        return 0.0f;
-    }
-    if (MIRROR && !(inv_z < 0.0f)) {               // not a descending ray: no walk
-        *accm = 0.0f;
-        return 0.0f;
-    }
-    const int jx = start_slab(a_in, inv_x, off_x, nx);
-    const int jy = start_slab(a_in, inv_y, off_y, ny);
-    int jz = THREE ? start_slab(a_in, inv_z, off_z, nz) : 0;
-    // a descending ray enters below the source plane and only steps down, so
-    // the folded index below stays inside the nz/2 stored slices
-    if (MIRROR) jz = min(jz, nz / 2 - 1);
-    int v = (jz * ny + jy) * nx + jx;              // < 2^31 (checked at plan creation)
-    const bool px = inv_x > 0.0f, py = inv_y > 0.0f, pz = inv_z > 0.0f;
-    float pax = (float)(px ? jx + 1 : jx);
-    float pay = (float)(py ? jy + 1 : jy);
-    float paz = (float)(pz ? jz + 1 : jz);
-    const float stx = px ? 1.0f : -1.0f, sty = py ? 1.0f : -1.0f, stz = pz ? 1.0f : -1.0f;
-    const int dvx = px ? 1 : -1, dvy = py ? nx : -nx, dvz = pz ? nx * ny : -(nx * ny);
-    float nAx = fmaf(pax, inv_x, off_x);
-    float nAy = fmaf(pay, inv_y, off_y);
-    float nAz = THREE ? fmaf(paz, inv_z, off_z) : 3.0e38f;
-    float cur = a_in, acc = 0.0f;
-    float2 acc2 = make_float2(0.0f, 0.0f);   // MIRROR: (voxel, mirror) sums, paired FMA
-    int cnt = 0;
-    // the gather of the next voxel is issued as soon as its index is known and
-    // consumed one step later, so its latency overlaps the next step's compares
-    float xv = 0.0f;
-    float2 xv2 = make_float2(0.0f, 0.0f);
-    if (MIRROR) { if (FL_IN(2 * (long long)v + 1, xlen)) xv2 = Store<TX>::ld2(x + 2 * (long long)v); }
-    else if (!COUNT) { if (FL_IN(v, xlen)) xv = ldv(x + v); }
-    const int budget = nx + ny + (THREE ? nz : 0) + 4;
-    for (int it = 0; it < budget; it += 4) {
-#pragma unroll
-        for (int u = 0; u < 4; u++) {
-            const float nxt = THREE ? fminf(fminf(nAx, nAy), nAz) : fminf(nAx, nAy);
-            const float seg = nxt - cur;
-            const bool cont = nxt < a_out;          // false at the exit (and for NaN)
-            float xn = 0.0f;
-            float2 xn2 = make_float2(0.0f, 0.0f);
-            if (cont) {
-                if (nAx == nxt) { pax += stx; v += dvx; nAx = fmaf(pax, inv_x, off_x); }
-                if (nAy == nxt) { pay += sty; v += dvy; nAy = fmaf(pay, inv_y, off_y); }
-                if (THREE && nAz == nxt) { paz += stz; v += dvz; nAz = fmaf(paz, inv_z, off_z); }
-                // v is inside the (folded) volume here
-                if (MIRROR) { if (FL_IN(2 * (long long)v + 1, xlen)) xn2 = Store<TX>::ld2(x + 2 * (long long)v); }
-                else if (!COUNT) { if (FL_IN(v, xlen)) xn = ldv(x + v); }
+    const float tol = 4e-7f * fmaxf(fabsf(a_in), fabsf(a_out)) + 1e-30f;
+    if (!(a_in < a_out + tol)) return false;
+    const float k1 = __fadd_rn(D.kq, __fdividef(a_in, D.ih));
+    const float k2 = __fadd_rn(D.kq, __fdividef(a_out, D.ih));
+    const float lo = fmaxf(floorf(fminf(k1, k2)) - 1.0f, 0.0f);          // NaN -> 0
+    const float hi = fminf(floorf(fmaxf(k1, k2)) + 1.0f, (float)(nD - 1));
+    if (!(lo <= hi)) return false;
+    s1 = (int)lo >> SH;
+    s2 = (int)hi >> SH;
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// The forward walk. A ray's matrix entries are, per segment s of its
+// dominant axis, the weights
+//   w_rV = fl(min_a U_a(V) - max_a L_a(V))    (entry c_r w_rV when positive)
+// of the voxels V whose dominant index lies in the segment, with L_a / U_a
+// the crossings (in segment s's frame) of the planes where the ray enters /
+// leaves V's slab on axis a. Segments are independent: the walk visits them
+// in the ray's order and walks each one's sub-box (the segment's dominant
+// slabs times the other axes' full ranges) from its entry v_in, stepping the
+// axes whose next crossing is the smallest (all tied axes at once). Every
+// visited voxel's segment is then exactly its w_rV: it starts at the latest
+// crossing behind the voxel and ends at the earliest ahead, and the voxels it
+// skips have w_rV <= 0. The backprojection evaluates the same expression per
+// (voxel, ray) in the voxel's own segment.
+//
+// The axis entries are read from global memory (kq and c again at every
+// segment start, so they hold no registers during the steps).
+// Body (the gathers of one kernel form):
+//   at(jx, jy, jz)        load the value(s) of voxel (jx, jy, jz)
+//   take(seg, more, jx, jy, jz)
+//                         if more, load the value(s) of the new current voxel
+//                         (jx, jy, jz); then add seg times the value(s) of
+//                         the voxel just left
+// Termination: each step advances at least one axis inside a finite
+// sub-box; the step budget is a second, independent bound.
+// ---------------------------------------------------------------------------
+// One dominant axis (XD: x, else y), the segments [s1, s2] in the ray's order.
+template <bool THREE, bool XD, typename Body>
+__device__ __forceinline__ void seg_walk_dom(const ColEntry* __restrict__ ce,
+                                             const AxisEntry* __restrict__ pZ, int nx, int ny,
+                                             int nzr, int s1, int s2, int jx, int jy, int jz,
+                                             Body& body)
+{
+    constexpr int SH = THREE ? kSegCone : kSegFan;
+    const float ihx = __ldg(&ce->x.ih), ilx = __ldg(&ce->x.il);
+    const float ihy = __ldg(&ce->y.ih), ily = __ldg(&ce->y.il);
+    const float ihz = THREE ? __ldg(&pZ->ih) : 1.0f, ilz = THREE ? __ldg(&pZ->il) : 0.0f;
+    const bool px = ihx > 0.0f, py = ihy > 0.0f, pz = ihz > 0.0f;
+    const bool pd = XD ? px : py;
+    const int nD = XD ? nx : ny;
+    const int nseg = s2 - s1;
+    for (int q = 0; q <= nseg; q++) {
+        const int s = pd ? s1 + q : s2 - q;
+        const AxisEntry X{__ldg(&ce->x.kq), ihx, ilx, __ldg(&ce->x.c)};
+        const AxisEntry Y{__ldg(&ce->y.kq), ihy, ily, __ldg(&ce->y.c)};
+        const AxisEntry Z{THREE ? __ldg(&pZ->kq) : 0.0f, ihz, ilz, THREE ? __ldg(&pZ->c) : 0.0f};
+        float bh, be;
+        make_anchor<SH>(XD ? X : Y, s, nD, bh, be);
+        const float cbx = __fsub_rn(X.c, be), cby = __fsub_rn(Y.c, be);
+        const float cbz = THREE ? __fsub_rn(Z.c, be) : 0.0f;
+        const int dlo = s << SH, dhi = min((s + 1) << SH, nD);
+        // the sub-box's entry and exit in this frame
+        const float tx0 = xrel(X, __fsub_rn((float)(XD ? dlo : 0), X.kq), bh, cbx);
+        const float tx1 = xrel(X, __fsub_rn((float)(XD ? dhi : nx), X.kq), bh, cbx);
+        const float ty0 = xrel(Y, __fsub_rn((float)(XD ? 0 : dlo), Y.kq), bh, cby);
+        const float ty1 = xrel(Y, __fsub_rn((float)(XD ? ny : dhi), Y.kq), bh, cby);
+        float v_in = fmaxf(fminf(tx0, tx1), fminf(ty0, ty1));
+        float v_out = fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1));
+        if (THREE) {
+            const float tz0 = xrel(Z, __fsub_rn(0.0f, Z.kq), bh, cbz);
+            const float tz1 = xrel(Z, __fsub_rn((float)nzr, Z.kq), bh, cbz);
+            v_in = fmaxf(v_in, fminf(tz0, tz1));
+            v_out = fminf(v_out, fmaxf(tz0, tz1));
+        }
+        if (!(v_in < v_out)) continue;
+        jx = slab_at(X, px, jx, XD ? dlo : 0, XD ? dhi : nx, v_in, bh, cbx);
+        jy = slab_at(Y, py, jy, XD ? 0 : dlo, XD ? ny : dhi, v_in, bh, cby);
+        if (THREE) jz = slab_at(Z, pz, jz, 0, nzr, v_in, bh, cbz);
+        float mx = __fsub_rn((float)(px ? jx + 1 : jx), X.kq);
+        float my = __fsub_rn((float)(py ? jy + 1 : jy), Y.kq);
+        float mz = THREE ? __fsub_rn((float)(pz ? jz + 1 : jz), Z.kq) : 0.0f;
+        float Ux = xrel(X, mx, bh, cbx), Uy = xrel(Y, my, bh, cby);
+        float Uz = THREE ? xrel(Z, mz, bh, cbz) : 3.0e38f;
+        body.at(jx, jy, jz);
+        float cur = v_in;
+        // The voxel being left is the sub-box's last exactly when the next
+        // crossing reaches the sub-box's exit: every voxel inside has its
+        // next crossings at or before the exit planes', and the exit plane's
+        // crossing is computed from the same m as v_out.
+        const int budget = (dhi - dlo) + (XD ? ny : nx) + (THREE ? nzr : 0) + 2;
+#pragma unroll 2
+        for (int it = 0; it < budget; it++) {
+            const float nxt = THREE ? fminf(fminf(Ux, Uy), Uz) : fminf(Ux, Uy);
+            const float seg = __fsub_rn(nxt, cur);
+            const bool more = nxt < v_out;             // false at the exit (and for NaN)
+            if (Ux == nxt) {
+                jx += px ? 1 : -1;
+                mx = __fadd_rn(mx, px ? 1.0f : -1.0f); Ux = xrel(X, mx, bh, cbx);
             }
-            if (COUNT) cnt += (seg > 0.0f);
-            else if (MIRROR) acc2 = __ffma2_rn(make_float2(seg, seg), xv2, acc2);
-            else acc = fmaf(seg, xv, acc);
-            if (!cont) goto done;
-            xv = xn;
-            xv2 = xn2;
+            if (Uy == nxt) {
+                jy += py ? 1 : -1;
+                my = __fadd_rn(my, py ? 1.0f : -1.0f); Uy = xrel(Y, my, bh, cby);
+            }
+            if (THREE && Uz == nxt) {
+                jz += pz ? 1 : -1;
+                mz = __fadd_rn(mz, pz ? 1.0f : -1.0f); Uz = xrel(Z, mz, bh, cbz);
+            }
+            body.take(seg, more, jx, jy, jz);
+            if (!more) break;
             cur = nxt;
         }
     }
-done:
-    if (COUNT) *nseg = cnt;
-    if (MIRROR) { *accm = acc2.y; return acc2.x; }
-    return acc;
+}
+
+// The walk of ray (ce, pZ) through an nx x ny (x nzr) box: finds the segments
+// it can cross and its first slabs, then walks them along its dominant axis.
+template <bool THREE, typename Body>
+__device__ __forceinline__ void seg_walk(const ColEntry* __restrict__ ce,
+                                         const AxisEntry* __restrict__ pZ, int nx, int ny,
+                                         int nzr, Body& body)
+{
+    constexpr int SH = THREE ? kSegCone : kSegFan;
+    const AxisEntry X = ce->x, Y = ce->y;
+    float a_in = fmaxf(fminf(xabs(X, 0.0f), xabs(X, (float)nx)),
+                       fminf(xabs(Y, 0.0f), xabs(Y, (float)ny)));
+    float a_out = fminf(fmaxf(xabs(X, 0.0f), xabs(X, (float)nx)),
+                        fmaxf(xabs(Y, 0.0f), xabs(Y, (float)ny)));
+    int jz = 0;
+    if (THREE) {
+        const AxisEntry Z = *pZ;
+        const float z0 = xabs(Z, 0.0f), z1 = xabs(Z, (float)nzr);
+        a_in = fmaxf(a_in, fminf(z0, z1));
+        a_out = fminf(a_out, fmaxf(z0, z1));
+        jz = slab_guess(Z, a_in, nzr);
+    }
+    const bool xd = x_dominant(X, Y);
+    int s1, s2;
+    if (!seg_range<SH>(xd ? X : Y, xd ? nx : ny, a_in, a_out, s1, s2)) return;
+    const int jx = slab_guess(X, a_in, nx), jy = slab_guess(Y, a_in, ny);
+    if (xd) seg_walk_dom<THREE, true>(ce, pZ, nx, ny, nzr, s1, s2, jx, jy, jz, body);
+    else seg_walk_dom<THREE, false>(ce, pZ, nx, ny, nzr, s1, s2, jx, jy, jz, body);
+}
+
+// Body of the general forward and the count: the standard volume, or with
+// MIRROR the z-folded one (pairs of voxel (ix, iy, iz) and its mirror (ix,
+// iy, nz-1-iz) at pair index (iz*ny + iy)*nx + ix; acc gets the voxel's sum,
+// accm the mirror's -- the companion ray of a scan symmetric about the
+// source plane). COUNT: counts the voxels with w > 0, no loads. xlen:
+// elements available at x (checked builds verify every gather index).
+template <typename TX, bool COUNT, bool MIRROR>
+struct GenBody {
+    const TX* __restrict__ x;
+    long long xlen;
+    int nx, ny;
+    int cnt = 0;
+    float acc = 0.0f, xv = 0.0f;
+    float2 acc2 = make_float2(0.0f, 0.0f), xv2 = make_float2(0.0f, 0.0f);
+    __device__ __forceinline__ void load(int jx, int jy, int jz, float& s, float2& s2) const
+    {
+        if (COUNT) return;
+        const int v = (jz * ny + jy) * nx + jx;      // < 2^31 (checked at plan creation)
+        if (MIRROR) {
+            s2 = make_float2(0.0f, 0.0f);
+            if (FL_IN(2 * (long long)v + 1, xlen)) s2 = Store<TX>::ld2(x + 2 * (long long)v);
+        } else {
+            s = 0.0f;
+            if (FL_IN(v, xlen)) s = ldv(x + v);
+        }
+    }
+    __device__ __forceinline__ void at(int jx, int jy, int jz) { load(jx, jy, jz, xv, xv2); }
+    __device__ __forceinline__ void take(float seg, bool more, int jx, int jy, int jz)
+    {
+        float xn = 0.0f;
+        float2 xn2 = make_float2(0.0f, 0.0f);
+        if (more) load(jx, jy, jz, xn, xn2);
+        if (COUNT) cnt += seg > 0.0f;
+        else if (MIRROR) acc2 = __ffma2_rn(make_float2(seg, seg), xv2, acc2);
+        else acc = fmaf(seg, xv, acc);
+        xv = xn;
+        xv2 = xn2;
+    }
+};
+
+// The general walk (2-D with THREE = false; z-folded volume with MIRROR: the
+// ray must descend from the source plane, so it stays in iz < nz/2).
+// Returns sum over voxels of w * x; *nseg counts segments with w > 0.
+template <typename TX, bool THREE, bool COUNT, bool MIRROR = false>
+__device__ __forceinline__ float walk(const TX* __restrict__ x, const ColEntry* ce,
+                                      const AxisEntry* pZ, int nx, int ny, int nz, int* nseg,
+                                      float* accm = nullptr, long long xlen = 0)
+{
+    GenBody<TX, COUNT, MIRROR> b{x, xlen, nx, ny};
+    if (!(MIRROR && !(__ldg(&pZ->ih) < 0.0f)))      // the folded walk takes descending rays
+        seg_walk<THREE>(ce, pZ, nx, ny, THREE ? (MIRROR ? nz / 2 : nz) : 1, b);
+    if (COUNT) *nseg = b.cnt;
+    if (MIRROR) { *accm = b.acc2.y; return b.acc2.x; }
+    return b.acc;
 }
 
 // Folded pair index of voxel (x, y, z) in the 4 x 4 tiled volume of a
@@ -135,271 +305,252 @@ __device__ __forceinline__ int tiled_pair(int x, int y, int zb, int nx4)
 // flag rot): besides the folded pair of voxel (ix, iy, iz) it gathers the
 // pair of voxel (nx-1-ix, ny-1-iy, iz), which the turned ray of view v + nv/2
 // crosses with the same segment. x is the tiled folded volume (nx, ny
-// multiples of 4). *acc gets the (voxel, mirror) sums, *accr the turned
-// pair's. Termination as in walk().
+// multiples of 4). acc gets the (voxel, mirror) sums, accr the turned pair's.
 template <typename TX>
-__device__ __forceinline__ void walk_quad(const TX* __restrict__ x, float inv_x, float off_x,
-                                          float inv_y, float off_y, float inv_z, float off_z,
-                                          int nx, int ny, int nz, float2* acc, float2* accr,
-                                          long long xlen)
-{
-    *acc = make_float2(0.0f, 0.0f);
-    *accr = make_float2(0.0f, 0.0f);
-    float ax0 = fmaf(0.0f, inv_x, off_x), ax1 = fmaf((float)nx, inv_x, off_x);
-    float ay0 = fmaf(0.0f, inv_y, off_y), ay1 = fmaf((float)ny, inv_y, off_y);
-    float a_in = fmaxf(fminf(ax0, ax1), fminf(ay0, ay1));
-    float a_out = fminf(fmaxf(ax0, ax1), fmaxf(ay0, ay1));
-    float az0 = fmaf(0.0f, inv_z, off_z), az1 = fmaf((float)nz, inv_z, off_z);
-    a_in = fmaxf(a_in, fminf(az0, az1));
-    a_out = fminf(a_out, fmaxf(az0, az1));
-    if (!(a_in < a_out) || !(inv_z < 0.0f)) return;
-    const int jx = start_slab(a_in, inv_x, off_x, nx);
-    const int jy = start_slab(a_in, inv_y, off_y, ny);
-    const int jz = min(start_slab(a_in, inv_z, off_z, nz), nz / 2 - 1);
-    const int nxy = nx * ny, nx4 = nx >> 2;
-    int cx = jx, cy = jy, zb = jz * nxy;           // < 2^31 (checked at plan creation)
-    int v = tiled_pair(cx, cy, zb, nx4), vr = 2 * zb + nxy - 1 - v;
-    const bool px = inv_x > 0.0f, py = inv_y > 0.0f;
-    float pax = (float)(px ? jx + 1 : jx);
-    float pay = (float)(py ? jy + 1 : jy);
-    float paz = (float)jz;                         // descending: next plane is jz
-    const float stx = px ? 1.0f : -1.0f, sty = py ? 1.0f : -1.0f;
-    const int dx = px ? 1 : -1, dy = py ? 1 : -1;
-    float nAx = fmaf(pax, inv_x, off_x);
-    float nAy = fmaf(pay, inv_y, off_y);
-    float nAz = fmaf(paz, inv_z, off_z);
-    float cur = a_in;
-    float2 s2 = make_float2(0.0f, 0.0f), r2 = make_float2(0.0f, 0.0f);
-    float2 xv2 = make_float2(0.0f, 0.0f), xr2 = make_float2(0.0f, 0.0f);
-    if (FL_IN(2 * (long long)v + 1, xlen)) xv2 = Store<TX>::ld2(x + 2 * (long long)v);
-    if (FL_IN(2 * (long long)vr + 1, xlen)) xr2 = Store<TX>::ld2(x + 2 * (long long)vr);
-    const int budget = nx + ny + nz + 4;
-    for (int it = 0; it < budget; it += 4) {
-#pragma unroll
-        for (int u = 0; u < 4; u++) {
-            const float nxt = fminf(fminf(nAx, nAy), nAz);
-            const float seg = nxt - cur;
-            const bool cont = nxt < a_out;         // false at the exit (and for NaN)
-            float2 xn2 = make_float2(0.0f, 0.0f), xnr2 = make_float2(0.0f, 0.0f);
-            if (cont) {
-                if (nAx == nxt) { pax += stx; cx += dx; nAx = fmaf(pax, inv_x, off_x); }
-                if (nAy == nxt) { pay += sty; cy += dy; nAy = fmaf(pay, inv_y, off_y); }
-                if (nAz == nxt) { paz -= 1.0f; zb -= nxy; nAz = fmaf(paz, inv_z, off_z); }
-                v = tiled_pair(cx, cy, zb, nx4);
-                vr = 2 * zb + nxy - 1 - v;
-                if (FL_IN(2 * (long long)v + 1, xlen)) xn2 = Store<TX>::ld2(x + 2 * (long long)v);
-                if (FL_IN(2 * (long long)vr + 1, xlen)) xnr2 = Store<TX>::ld2(x + 2 * (long long)vr);
-            }
-            s2 = __ffma2_rn(make_float2(seg, seg), xv2, s2);
-            r2 = __ffma2_rn(make_float2(seg, seg), xr2, r2);
-            if (!cont) goto done;
-            xv2 = xn2;
-            xr2 = xnr2;
-            cur = nxt;
-        }
+struct QuadBody {
+    const TX* __restrict__ x;
+    long long xlen;
+    int nxy, nx4;
+    float2 acc = make_float2(0.0f, 0.0f), accr = make_float2(0.0f, 0.0f);
+    float2 xv = make_float2(0.0f, 0.0f), xr = make_float2(0.0f, 0.0f);
+    __device__ __forceinline__ void load(int jx, int jy, int jz, float2& a, float2& r) const
+    {
+        const int zb = jz * nxy;                     // < 2^31 (checked at plan creation)
+        const int t = tiled_pair(jx, jy, zb, nx4), tr = 2 * zb + nxy - 1 - t;
+        a = make_float2(0.0f, 0.0f); r = a;
+        if (FL_IN(2 * (long long)t + 1, xlen)) a = Store<TX>::ld2(x + 2 * (long long)t);
+        if (FL_IN(2 * (long long)tr + 1, xlen)) r = Store<TX>::ld2(x + 2 * (long long)tr);
     }
-done:
-    *acc = s2;
-    *accr = r2;
-}
+    __device__ __forceinline__ void at(int jx, int jy, int jz) { load(jx, jy, jz, xv, xr); }
+    __device__ __forceinline__ void take(float seg, bool more, int jx, int jy, int jz)
+    {
+        float2 xn = make_float2(0.0f, 0.0f), xnr = xn;
+        if (more) load(jx, jy, jz, xn, xnr);
+        acc = __ffma2_rn(make_float2(seg, seg), xv, acc);
+        accr = __ffma2_rn(make_float2(seg, seg), xr, accr);
+        xv = xn;
+        xr = xnr;
+    }
+};
 
+template <typename TX>
+__device__ __forceinline__ void walk_quad(const TX* __restrict__ x, const ColEntry* ce,
+                                          const AxisEntry* pZ, int nx, int ny, int nz,
+                                          float2* acc, float2* accr, long long xlen)
+{
+    QuadBody<TX> b{x, xlen, nx * ny, nx >> 2};
+    if (__ldg(&pZ->ih) < 0.0f) seg_walk<true>(ce, pZ, nx, ny, nz / 2, b);
+    *acc = b.acc;
+    *accr = b.accr;
+}
 
 // The z-mirror walk with all four quarter turns (plan flag rot4, nx == ny ==
 // n, a multiple of 4): per step it gathers the folded pairs of voxel (ix, iy)
 // and of its turns R^j (ix, iy), R (x, y) = (n-1-y, x), which the ray of view
 // v + j nv/4 at the same column and row crosses with the same segment. x is
 // the tiled folded volume. acc[j] gets the (voxel, mirror) sums of turn j.
-// Termination as in walk().
 template <typename TX>
-__device__ __forceinline__ void walk_oct(const TX* __restrict__ x, float inv_x, float off_x,
-                                         float inv_y, float off_y, float inv_z, float off_z,
-                                         int n, int nz, float2 (&acc)[4], long long xlen)
-{
-#pragma unroll
-    for (int j = 0; j < 4; j++) acc[j] = make_float2(0.0f, 0.0f);
-    float ax0 = fmaf(0.0f, inv_x, off_x), ax1 = fmaf((float)n, inv_x, off_x);
-    float ay0 = fmaf(0.0f, inv_y, off_y), ay1 = fmaf((float)n, inv_y, off_y);
-    float a_in = fmaxf(fminf(ax0, ax1), fminf(ay0, ay1));
-    float a_out = fminf(fmaxf(ax0, ax1), fmaxf(ay0, ay1));
-    float az0 = fmaf(0.0f, inv_z, off_z), az1 = fmaf((float)nz, inv_z, off_z);
-    a_in = fmaxf(a_in, fminf(az0, az1));
-    a_out = fminf(a_out, fmaxf(az0, az1));
-    if (!(a_in < a_out) || !(inv_z < 0.0f)) return;
-    const int jx = start_slab(a_in, inv_x, off_x, n);
-    const int jy = start_slab(a_in, inv_y, off_y, n);
-    const int jz = min(start_slab(a_in, inv_z, off_z, nz), nz / 2 - 1);
-    const int nn = n * n, n4 = n >> 2;
-    int cx = jx, cy = jy, zb = jz * nn;            // voxel of turn 0; z base of all turns
-    int q[4];                                      // folded pair index of each turn
-    auto turns = [&]() {                           // turns 2, 3 are turns 0, 1 by pi
-        q[0] = tiled_pair(cx, cy, zb, n4);
-        q[1] = tiled_pair(n - 1 - cy, cx, zb, n4);
+struct OctBody {
+    const TX* __restrict__ x;
+    long long xlen;
+    int n, nn, n4;
+    float2 acc[4], xv[4];
+    __device__ __forceinline__ void load(int jx, int jy, int jz, float2 (&o)[4]) const
+    {
+        const int zb = jz * nn;
+        int q[4];                                    // turns 2, 3 are turns 0, 1 by pi
+        q[0] = tiled_pair(jx, jy, zb, n4);
+        q[1] = tiled_pair(n - 1 - jy, jx, zb, n4);
         q[2] = 2 * zb + nn - 1 - q[0];
         q[3] = 2 * zb + nn - 1 - q[1];
-    };
-    turns();
-    const bool px = inv_x > 0.0f, py = inv_y > 0.0f;
-    float pax = (float)(px ? jx + 1 : jx);
-    float pay = (float)(py ? jy + 1 : jy);
-    float paz = (float)jz;                         // descending: next plane is jz
-    const float stx = px ? 1.0f : -1.0f, sty = py ? 1.0f : -1.0f;
-    const int dx = px ? 1 : -1, dy = py ? 1 : -1;
-    float nAx = fmaf(pax, inv_x, off_x);
-    float nAy = fmaf(pay, inv_y, off_y);
-    float nAz = fmaf(paz, inv_z, off_z);
-    float cur = a_in;
-    float2 xv[4];
 #pragma unroll
-    for (int j = 0; j < 4; j++) {
-        xv[j] = make_float2(0.0f, 0.0f);
-        if (FL_IN(2 * (long long)q[j] + 1, xlen)) xv[j] = Store<TX>::ld2(x + 2 * (long long)q[j]);
-    }
-    float2 s[4];
-#pragma unroll
-    for (int j = 0; j < 4; j++) s[j] = make_float2(0.0f, 0.0f);
-    const int budget = 2 * n + nz + 4;
-    for (int it = 0; it < budget; it += 2) {
-#pragma unroll
-        for (int u = 0; u < 2; u++) {
-            const float nxt = fminf(fminf(nAx, nAy), nAz);
-            const float seg = nxt - cur;
-            const bool cont = nxt < a_out;         // false at the exit (and for NaN)
-            float2 xn[4];
-#pragma unroll
-            for (int j = 0; j < 4; j++) xn[j] = make_float2(0.0f, 0.0f);
-            if (cont) {
-                if (nAx == nxt) { pax += stx; nAx = fmaf(pax, inv_x, off_x); cx += dx; }
-                if (nAy == nxt) { pay += sty; nAy = fmaf(pay, inv_y, off_y); cy += dy; }
-                if (nAz == nxt) { paz -= 1.0f; nAz = fmaf(paz, inv_z, off_z); zb -= nn; }
-                turns();
-#pragma unroll
-                for (int j = 0; j < 4; j++)
-                    if (FL_IN(2 * (long long)q[j] + 1, xlen)) xn[j] = Store<TX>::ld2(x + 2 * (long long)q[j]);
-            }
-#pragma unroll
-            for (int j = 0; j < 4; j++) s[j] = __ffma2_rn(make_float2(seg, seg), xv[j], s[j]);
-            if (!cont) goto done;
-#pragma unroll
-            for (int j = 0; j < 4; j++) xv[j] = xn[j];
-            cur = nxt;
+        for (int j = 0; j < 4; j++) {
+            o[j] = make_float2(0.0f, 0.0f);
+            if (FL_IN(2 * (long long)q[j] + 1, xlen)) o[j] = Store<TX>::ld2(x + 2 * (long long)q[j]);
         }
     }
-done:
+    __device__ __forceinline__ void at(int jx, int jy, int jz) { load(jx, jy, jz, xv); }
+    __device__ __forceinline__ void take(float seg, bool more, int jx, int jy, int jz)
+    {
+        float2 xn[4];
 #pragma unroll
-    for (int j = 0; j < 4; j++) acc[j] = s[j];
+        for (int j = 0; j < 4; j++) xn[j] = make_float2(0.0f, 0.0f);
+        if (more) load(jx, jy, jz, xn);
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            acc[j] = __ffma2_rn(make_float2(seg, seg), xv[j], acc[j]);
+            xv[j] = xn[j];
+        }
+    }
+};
+
+template <typename TX>
+__device__ __forceinline__ void walk_oct(const TX* __restrict__ x, const ColEntry* ce,
+                                         const AxisEntry* pZ, int n, int nz, float2 (&acc)[4],
+                                         long long xlen)
+{
+    OctBody<TX> b;
+    b.x = x; b.xlen = xlen; b.n = n; b.nn = n * n; b.n4 = n >> 2;
+#pragma unroll
+    for (int j = 0; j < 4; j++) { b.acc[j] = make_float2(0.0f, 0.0f); b.xv[j] = b.acc[j]; }
+    if (__ldg(&pZ->ih) < 0.0f) seg_walk<true>(ce, pZ, n, n, nz / 2, b);
+#pragma unroll
+    for (int j = 0; j < 4; j++) acc[j] = b.acc[j];
 }
 
 // The fan walk in batches of kFanBatch steps: the crossings of a batch are
 // found first (they do not depend on the image), then its gathers are issued
-// together and the segments added in walk order. The sums are the same as
-// walk()'s, bit for bit, but a batch waits for its gathers once instead of
-// once per step.
+// together and the segments added in walk order -- the same sums as the
+// general walk, bit for bit, waiting for the gathers once per batch.
 // G = 1: the ray's own pixels (acc[0]). G = 2 or 4 (a turn plan, one frame):
 // per step also the turns R^j (ix, iy) of the pixel -- G = 2: R (x, y) =
 // (nx-1-x, ny-1-y); G = 4 (nx == ny == n): R (x, y) = (n-1-y, x) -- which
 // the ray of view v + j nv/G at the same column crosses with the same
 // segment; acc[j] gets turn j's sum.
-// L > 1: the ray is cut into L parts and this call walks part `lane`. Part k
-// runs from crossing c_k to crossing c_{k+1}, where c_k (0 < k < L) is the
-// first crossing after a_in + k (a_out - a_in) / L (c_0 = a_in, c_L =
-// a_out). Every lane computes the cuts from the same expressions, and a cut
-// is a crossing of the ray's own table, so each segment -- each matrix
-// entry -- lies whole in one part and is the walk's own; only the order of
-// the additions changes (the caller adds the parts in lane order).
-// Termination as in walk().
+// L > 1: the ray's segments (in walk order) are dealt to L parts, part k
+// taking those with index q in [k S / L, (k+1) S / L) of the S it can cross;
+// this call walks part `lane`. Segments are independent, so every matrix
+// entry lies whole in one part and is the walk's own; only the order of the
+// additions changes (the caller adds the parts in lane order).
 constexpr int kFanBatch = 4;
 
 template <typename TX, int G, int L = 1>
-__device__ __forceinline__ void walk_fan(const TX* __restrict__ x, float inv_x, float off_x,
-                                         float inv_y, float off_y, int nx, int ny,
-                                         float (&acc)[G], long long xlen, int lane = 0)
+__device__ __forceinline__ void walk_fan(const TX* __restrict__ x, const AxisEntry* pX,
+                                         const AxisEntry* pY, int nx, int ny, float (&acc)[G],
+                                         long long xlen, int lane = 0)
 {
+    const AxisEntry X = *pX, Y = *pY;
     static_assert(G == 1 || G == 2 || G == 4, "one, two or four turns");
+    constexpr int SH = kSegFan;
 #pragma unroll
     for (int j = 0; j < G; j++) acc[j] = 0.0f;
-    float ax0 = fmaf(0.0f, inv_x, off_x), ax1 = fmaf((float)nx, inv_x, off_x);
-    float ay0 = fmaf(0.0f, inv_y, off_y), ay1 = fmaf((float)ny, inv_y, off_y);
-    const float a_in = fmaxf(fminf(ax0, ax1), fminf(ay0, ay1));
-    const float a_out = fminf(fmaxf(ax0, ax1), fmaxf(ay0, ay1));
-    if (!(a_in < a_out)) return;
-    const bool px = inv_x > 0.0f, py = inv_y > 0.0f;
-    // the crossing that ends the slab pair (jx, jy)
-    auto next_x = [&](int j) { return fmaf((float)(px ? j + 1 : j), inv_x, off_x); };
-    auto next_y = [&](int j) { return fmaf((float)(py ? j + 1 : j), inv_y, off_y); };
-    float cur = a_in, end = a_out;
-    int jx, jy;
-    if (L > 1 && lane > 0) {
-        const float t = fmaf((float)lane, (a_out - a_in) * (1.0f / L), a_in);
-        jx = start_slab(t, inv_x, off_x, nx);
-        jy = start_slab(t, inv_y, off_y, ny);
-        const float cx = next_x(jx), cy = next_y(jy), c = fminf(cx, cy);
-        if (!(c < a_out)) return;                  // the cut falls at the exit: nothing left
-        if (cx == c) jx += px ? 1 : -1;
-        if (cy == c) jy += py ? 1 : -1;
-        cur = c;
-    } else {
-        jx = start_slab(a_in, inv_x, off_x, nx);
-        jy = start_slab(a_in, inv_y, off_y, ny);
+    const float a_in = fmaxf(fminf(xabs(X, 0.0f), xabs(X, (float)nx)),
+                             fminf(xabs(Y, 0.0f), xabs(Y, (float)ny)));
+    const float a_out = fminf(fmaxf(xabs(X, 0.0f), xabs(X, (float)nx)),
+                              fmaxf(xabs(Y, 0.0f), xabs(Y, (float)ny)));
+    const bool xd = x_dominant(X, Y);
+    const AxisEntry D = xd ? X : Y;
+    const int nD = xd ? nx : ny;
+    int s1, s2;
+    if (!seg_range<SH>(D, nD, a_in, a_out, s1, s2)) return;
+    const bool px = X.ih > 0.0f, py = Y.ih > 0.0f, pd = xd ? px : py;
+    const int S = s2 - s1 + 1;
+    const int q0 = L > 1 ? (lane * S) / L : 0, q1 = L > 1 ? ((lane + 1) * S) / L : S;
+    if (q0 >= q1) return;
+    // first guesses at the entry of this part's first segment
+    float ag = a_in;
+    if (L > 1 && q0 > 0) {
+        const int s = pd ? s1 + q0 : s2 - q0;
+        ag = fmaxf(a_in, xabs(D, (float)(pd ? (s << SH) : min((s + 1) << SH, nD))));
     }
-    if (L > 1 && lane + 1 < L) {
-        const float t = fmaf((float)(lane + 1), (a_out - a_in) * (1.0f / L), a_in);
-        const int ex = start_slab(t, inv_x, off_x, nx), ey = start_slab(t, inv_y, off_y, ny);
-        end = fminf(fminf(next_x(ex), next_y(ey)), a_out);
-        if (!(cur < end)) return;                  // an empty part
-    }
+    int jx = slab_guess(X, ag, nx), jy = slab_guess(Y, ag, ny);
     const int nxy = nx * ny;                       // < 2^31 (checked at plan creation)
-    // q0: the pixel; q1 (G = 4): its quarter turn x * n + n-1-y; the turns by
-    // pi of both are nxy - 1 minus them
-    int q0 = jy * nx + jx, q1 = jx * nx + (nx - 1 - jy);
-    float pax = (float)(px ? jx + 1 : jx);
-    float pay = (float)(py ? jy + 1 : jy);
-    const float stx = px ? 1.0f : -1.0f, sty = py ? 1.0f : -1.0f;
     const int dq0x = px ? 1 : -1, dq0y = py ? nx : -nx;
     const int dq1x = px ? nx : -nx, dq1y = py ? -1 : 1;
-    float nAx = fmaf(pax, inv_x, off_x);
-    float nAy = fmaf(pay, inv_y, off_y);
-    float s[G];
+    const float stx = px ? 1.0f : -1.0f, sty = py ? 1.0f : -1.0f;
+    float sacc[G];
 #pragma unroll
-    for (int j = 0; j < G; j++) s[j] = 0.0f;
-    bool in = true;                                // the walk is at a pixel of the part
-    const int budget = nx + ny + 4;
-    for (int it = 0; it < budget && in; it += kFanBatch) {
-        float seg[kFanBatch];
-        int i0[kFanBatch], i1[kFanBatch];
-        bool live[kFanBatch];
+    for (int j = 0; j < G; j++) sacc[j] = 0.0f;
+    for (int q = q0; q < q1; q++) {
+        const int s = pd ? s1 + q : s2 - q;
+        float bh, be;
+        make_anchor<SH>(D, s, nD, bh, be);
+        const float cbx = __fsub_rn(X.c, be), cby = __fsub_rn(Y.c, be);
+        const int dlo = s << SH, dhi = min((s + 1) << SH, nD);
+        const int lox = xd ? dlo : 0, hix = xd ? dhi : nx;
+        const int loy = xd ? 0 : dlo, hiy = xd ? ny : dhi;
+        const float tx0 = xrel(X, __fsub_rn((float)lox, X.kq), bh, cbx);
+        const float tx1 = xrel(X, __fsub_rn((float)hix, X.kq), bh, cbx);
+        const float ty0 = xrel(Y, __fsub_rn((float)loy, Y.kq), bh, cby);
+        const float ty1 = xrel(Y, __fsub_rn((float)hiy, Y.kq), bh, cby);
+        const float v_in = fmaxf(fminf(tx0, tx1), fminf(ty0, ty1));
+        const float v_out = fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1));
+        if (!(v_in < v_out)) continue;
+        jx = slab_at(X, px, jx, lox, hix, v_in, bh, cbx);
+        jy = slab_at(Y, py, jy, loy, hiy, v_in, bh, cby);
+        float mx = __fsub_rn((float)(px ? jx + 1 : jx), X.kq);
+        float my = __fsub_rn((float)(py ? jy + 1 : jy), Y.kq);
+        float Ux = xrel(X, mx, bh, cbx), Uy = xrel(Y, my, bh, cby);
+        // p0: the pixel; p1 (G = 4): its quarter turn x * n + n-1-y; the turns
+        // by pi of both are nxy - 1 minus them
+        int p0 = jy * nx + jx, p1 = jx * nx + (nx - 1 - jy);
+        float cur = v_in;
+        bool in = true;
+        const int budget = (hix - lox) + (hiy - loy) + 2;
+        for (int it = 0; it < budget && in; it += kFanBatch) {
+            float seg[kFanBatch];
+            int i0[kFanBatch], i1[kFanBatch];
+            bool live[kFanBatch];
 #pragma unroll
-        for (int u = 0; u < kFanBatch; u++) {
-            const float nxt = fminf(nAx, nAy);
-            const bool cont = nxt < end;           // false at the part's end (and for NaN)
-            live[u] = in;
-            seg[u] = nxt - cur;
-            i0[u] = q0; i1[u] = q1;
-            if (in && cont) {
-                if (nAx == nxt) { pax += stx; nAx = fmaf(pax, inv_x, off_x); q0 += dq0x; q1 += dq1x; }
-                if (nAy == nxt) { pay += sty; nAy = fmaf(pay, inv_y, off_y); q0 += dq0y; q1 += dq1y; }
-                cur = nxt;
+            for (int u = 0; u < kFanBatch; u++) {
+                const float nxt = fminf(Ux, Uy);
+                live[u] = in;
+                seg[u] = __fsub_rn(nxt, cur);
+                i0[u] = p0; i1[u] = p1;
+                if (in) {
+                    // the last voxel of the sub-box: its next crossing is the exit
+                    const bool more = nxt < v_out;
+                    if (Ux == nxt) {
+                        jx += px ? 1 : -1;
+                        mx = __fadd_rn(mx, stx); Ux = xrel(X, mx, bh, cbx);
+                        p0 += dq0x; p1 += dq1x;
+                    }
+                    if (Uy == nxt) {
+                        jy += py ? 1 : -1;
+                        my = __fadd_rn(my, sty); Uy = xrel(Y, my, bh, cby);
+                        p0 += dq0y; p1 += dq1y;
+                    }
+                    cur = nxt;
+                    in = more;
+                }
             }
-            in = in && cont;
-        }
-        float v[kFanBatch][G];
+            float vv[kFanBatch][G];
 #pragma unroll
-        for (int u = 0; u < kFanBatch; u++) {
-            const int q[4] = {i0[u], G == 4 ? i1[u] : nxy - 1 - i0[u], nxy - 1 - i0[u],
-                              nxy - 1 - i1[u]};
+            for (int u = 0; u < kFanBatch; u++) {
+                const int qq[4] = {i0[u], G == 4 ? i1[u] : nxy - 1 - i0[u], nxy - 1 - i0[u],
+                                   nxy - 1 - i1[u]};
 #pragma unroll
-            for (int j = 0; j < G; j++) {
-                v[u][j] = 0.0f;
-                if (live[u] && FL_IN(q[j], xlen)) v[u][j] = ldv(x + q[j]);
+                for (int j = 0; j < G; j++) {
+                    vv[u][j] = 0.0f;
+                    if (live[u] && FL_IN(qq[j], xlen)) vv[u][j] = ldv(x + qq[j]);
+                }
             }
+#pragma unroll
+            for (int u = 0; u < kFanBatch; u++)
+#pragma unroll
+                for (int j = 0; j < G; j++)
+                    if (live[u]) sacc[j] = fmaf(seg[u], vv[u][j], sacc[j]);
         }
-#pragma unroll
-        for (int u = 0; u < kFanBatch; u++)
-#pragma unroll
-            for (int j = 0; j < G; j++)
-                if (live[u]) s[j] = fmaf(seg[u], v[u][j], s[j]);
     }
 #pragma unroll
-    for (int j = 0; j < G; j++) acc[j] = s[j];
+    for (int j = 0; j < G; j++) acc[j] = sacc[j];
+}
+
+// The xy part of a cone ray's crossings with the voxel column (cx, cy): the
+// frame of the column's segment (anchor bh + be) and the column's entry l and
+// exit h in it, the crossings the forward walk computes for the column's
+// planes. Returns false when the ray misses the column (l >= h).
+__device__ __forceinline__ bool cone_column(const ColEntry& ce, int cx, int cy, int nx, int ny,
+                                            float& bh, float& be, float& l, float& h)
+{
+    const bool xd = x_dominant(ce.x, ce.y);
+    make_anchor<kSegCone>(xd ? ce.x : ce.y, (xd ? cx : cy) >> kSegCone, xd ? nx : ny, bh, be);
+    const float mx = __fsub_rn((float)cx, ce.x.kq), my = __fsub_rn((float)cy, ce.y.kq);
+    const float2 tx = xrel2(ce.x, make_float2(mx, __fadd_rn(mx, 1.0f)), bh,
+                            __fsub_rn(ce.x.c, be));
+    const float2 ty = xrel2(ce.y, make_float2(my, __fadd_rn(my, 1.0f)), bh,
+                            __fsub_rn(ce.y.c, be));
+    l = fmaxf(fminf(tx.x, tx.y), fminf(ty.x, ty.y));
+    h = fminf(fmaxf(tx.x, tx.y), fmaxf(ty.x, ty.y));
+    return l < h;
+}
+
+// Crossings of z planes k0 and k1 of row re in the frame bh + be.
+__device__ __forceinline__ float2 row_planes(const AxisEntry& re, float k0, float k1, float bh,
+                                             float be)
+{
+    return xrel2(re, make_float2(__fsub_rn(k0, re.kq), __fsub_rn(k1, re.kq)), bh,
+                 __fsub_rn(re.c, be));
 }
 
 __device__ __forceinline__ float ray_cr(float scale, float dxy2, float dz2)
@@ -458,17 +609,38 @@ __device__ __forceinline__ void column_window(const DetGrid& G, float c, float s
 // are then added in the order g = 0, 1, ... (fan_combine_groups).
 constexpr int kFanGroups = 4;
 
+// The crossings of the planes ix0 .. ix0 + PX (x) and iy0 .. iy0 + PY (y) of
+// fan ray ce, relative to the anchor of the segment holding the block (the
+// block lies in one segment of either axis: PX, PY <= 2 and ix0, iy0
+// multiples of them). These are the crossings the forward walk computes for
+// the same planes in the same segment.
+template <int PX, int PY>
+__device__ __forceinline__ void fan_block_crossings(const ColEntry& ce, int ix0, int iy0, int nx,
+                                                    int ny, float (&ax)[PX + 1],
+                                                    float (&ay)[PY + 1])
+{
+    const bool xd = x_dominant(ce.x, ce.y);
+    float bh, be;
+    make_anchor<kSegFan>(xd ? ce.x : ce.y, (xd ? ix0 : iy0) >> kSegFan, xd ? nx : ny, bh, be);
+    const float cbx = __fsub_rn(ce.x.c, be), cby = __fsub_rn(ce.y.c, be);
+    const float mx = __fsub_rn((float)ix0, ce.x.kq), my = __fsub_rn((float)iy0, ce.y.kq);
+#pragma unroll
+    for (int i = 0; i <= PX; i++) ax[i] = xrel(ce.x, __fadd_rn(mx, (float)i), bh, cbx);
+#pragma unroll
+    for (int j = 0; j <= PY; j++) ay[j] = xrel(ce.y, __fadd_rn(my, (float)j), bh, cby);
+}
+
 // One view of the fan gather: adds w_rV * yw_r for every ray of view iv whose
-// column window covers the block.
+// column window covers the block with lower corner (ix0, iy0).
 template <int PX, int PY>
 __device__ __forceinline__ void fan_view_gather(float (&acc)[PY][PX], const float* __restrict__ yw,
                                                 const ColEntry* __restrict__ col,
                                                 const ViewEntry& ve, int iv, const DetGrid& G,
-                                                float x0, float y0, const float (&fx)[PX + 1],
-                                                const float (&fy)[PY + 1], int na)
+                                                int ix0, int iy0, int nx, int ny, int na)
 {
     int lo, hi; float dmin, dmax;
-    column_window(G, ve.c, ve.s, x0, y0, (float)PX, (float)PY, na, lo, hi, dmin, dmax);
+    column_window(G, ve.c, ve.s, (float)(ix0 - nx / 2), (float)(iy0 - ny / 2), (float)PX,
+                  (float)PY, na, lo, hi, dmin, dmax);
     const ColEntry* cv = col + (long long)iv * na;
     const float* yv = yw + (long long)iv * na;
     for (int ia = lo; ia <= hi; ia++) {
@@ -476,10 +648,7 @@ __device__ __forceinline__ void fan_view_gather(float (&acc)[PY][PX], const floa
         const ColEntry ce = cv[ia];
         const float yval = __ldg(yv + ia);
         float ax[PX + 1], ay[PY + 1];
-#pragma unroll
-        for (int i = 0; i <= PX; i++) ax[i] = fmaf(fx[i], ce.inv_x, ce.off_x);
-#pragma unroll
-        for (int j = 0; j <= PY; j++) ay[j] = fmaf(fy[j], ce.inv_y, ce.off_y);
+        fan_block_crossings<PX, PY>(ce, ix0, iy0, nx, ny, ax, ay);
 #pragma unroll
         for (int j = 0; j < PY; j++)
 #pragma unroll
@@ -502,19 +671,13 @@ __device__ __forceinline__ void fan_block_gather(float (&acc)[PY][PX],
                                                  const DetGrid& G, int ix0, int iy0, int nx,
                                                  int ny, int na, int g)
 {
-    const float x0 = (float)(ix0 - nx / 2), y0 = (float)(iy0 - ny / 2);
-    float fx[PX + 1], fy[PY + 1];
-#pragma unroll
-    for (int i = 0; i <= PX; i++) fx[i] = (float)(ix0 + i);
-#pragma unroll
-    for (int j = 0; j <= PY; j++) fy[j] = (float)(iy0 + j);
 #pragma unroll
     for (int j = 0; j < PY; j++)
 #pragma unroll
         for (int i = 0; i < PX; i++) acc[j][i] = 0.0f;
     for (int jv = g; jv < nvf; jv += kFanGroups) {
         const int iv = views[jv];
-        fan_view_gather<PX, PY>(acc, yw, col, view[iv], iv, G, x0, y0, fx, fy, na);
+        fan_view_gather<PX, PY>(acc, yw, col, view[iv], iv, G, ix0, iy0, nx, ny, na);
     }
 }
 
@@ -532,12 +695,6 @@ __device__ __forceinline__ void fan_block_gather_all(float (&acc)[PY][PX],
                                                      const DetGrid& G, int ix0, int iy0, int nx,
                                                      int ny, int na)
 {
-    const float x0 = (float)(ix0 - nx / 2), y0 = (float)(iy0 - ny / 2);
-    float fx[PX + 1], fy[PY + 1];
-#pragma unroll
-    for (int i = 0; i <= PX; i++) fx[i] = (float)(ix0 + i);
-#pragma unroll
-    for (int j = 0; j <= PY; j++) fy[j] = (float)(iy0 + j);
     // part[0] always holds the group of the next view: after each view the
     // groups rotate one place, and after the loop back into group order
     float part[kFanGroups][PY][PX];
@@ -560,7 +717,7 @@ __device__ __forceinline__ void fan_block_gather_all(float (&acc)[PY][PX],
     };
     for (int jv = 0; jv < nvf; jv++) {
         const int iv = views[jv];
-        fan_view_gather<PX, PY>(part[0], yw, col, view[iv], iv, G, x0, y0, fx, fy, na);
+        fan_view_gather<PX, PY>(part[0], yw, col, view[iv], iv, G, ix0, iy0, nx, ny, na);
         rotate();
     }
     for (int k = (kFanGroups - nvf % kFanGroups) % kFanGroups; k > 0; k--) rotate();
@@ -653,18 +810,11 @@ __device__ __forceinline__ void fan_turn_gather(float (&acc)[G][P][P],
             int lo, hi; float dmin, dmax;
             column_window(D, ve.c, ve.s, (float)(X0[k] - nx / 2), (float)(Y0[k] - ny / 2),
                           (float)P, (float)P, na, lo, hi, dmin, dmax);
-            float fx[P + 1], fy[P + 1];
-#pragma unroll
-            for (int q = 0; q <= P; q++) { fx[q] = (float)(X0[k] + q); fy[q] = (float)(Y0[k] + q); }
             for (int ia = lo; ia <= hi; ia++) {
                 if (!FL_IN(ia, na)) continue;
                 const ColEntry ce = cv[ia];
                 float ax[P + 1], ay[P + 1];
-#pragma unroll
-                for (int q = 0; q <= P; q++) {
-                    ax[q] = fmaf(fx[q], ce.inv_x, ce.off_x);
-                    ay[q] = fmaf(fy[q], ce.inv_y, ce.off_y);
-                }
+                fan_block_crossings<P, P>(ce, X0[k], Y0[k], nx, ny, ax, ay);
                 float t[G];
                 if constexpr (G == 4) {
                     const float4 u = __ldg(reinterpret_cast<const float4*>(yv + 4 * ia));
@@ -735,9 +885,7 @@ __device__ __forceinline__ void fan_turn_forward_block(const TX* __restrict__ X,
 #pragma unroll
     for (int j = 0; j < G; j++) acc[j] = 0.0f;
     if (ray) {
-        const ColEntry ce = col[r];
-        walk_fan<TX, G, L>(X, ce.inv_x, ce.off_x, ce.inv_y, ce.off_y, nx, ny, acc,
-                           (long long)nx * ny, lane);
+        walk_fan<TX, G, L>(X, &col[r].x, &col[r].y, nx, ny, acc, (long long)nx * ny, lane);
     }
     if constexpr (L > 1) {
         // part k of ray tx is thread k NR + tx: the first NR threads add them in order

@@ -275,7 +275,11 @@ def ref_cone_adj(Y, p):
 # --------------------------------------------------------------------------
 
 def _exact_args(p):
-    sd = _f(p["sd_phi"]); yd = _f(p["y_det"])
+    """FP64 model inputs: the source angles in FP64 (the FP32 sd_phi, or an
+    explicit "phi64" array, e.g. views snapped to exact turns), the other
+    geometry as the FP32 para holds it."""
+    sd = _d(p["phi64"]) if "phi64" in p else _d(_f(p["sd_phi"]))
+    yd = _f(p["y_det"])
     cone = "nz" in p
     sz = _f(p["sd_z"]) if cone else np.zeros(len(sd), np.float32)
     zd = _f(p["z_det"]) if cone else np.zeros(1, np.float32)

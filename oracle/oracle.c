@@ -600,7 +600,7 @@ static void orc_ray_points(double SO, double OD, double phi, double sz, double y
  */
 void orc_exact_forward_f64(const double *X, double *y, double SO, double OD, double scale,
                            int nx, int ny, int nz, double dz, int v0, int v1,
-                           const float *sd_phi, const float *sd_z, int na, int nb,
+                           const double *phi, const float *sd_z, int na, int nb,
                            const float *y_det, const float *z_det)
 {
     orc_grid g = {nx, ny, nz, dz};
@@ -610,7 +610,7 @@ void orc_exact_forward_f64(const double *X, double *y, double SO, double OD, dou
         for (int ib = 0; ib < nb; ib++) {
             for (int ia = 0; ia < na; ia++) {
                 double S[3], D[3];
-                orc_ray_points(SO, OD, (double)sd_phi[iv], sz, (double)y_det[ia],
+                orc_ray_points(SO, OD, phi[iv], sz, (double)y_det[ia],
                                z_det ? (double)z_det[ib] : 0.0, S, D);
                 orc_fwd_ctx f = {X, 0.0};
                 orc_exact_walk(&g, S, D, orc_fwd_visit, &f);
@@ -623,7 +623,7 @@ void orc_exact_forward_f64(const double *X, double *y, double SO, double OD, dou
 /* Exact transpose: X += scale * sum over rays of views [v0, v1) (len * y). */
 void orc_exact_adjoint_f64(double *X, const double *y, double SO, double OD, double scale,
                            int nx, int ny, int nz, double dz, int v0, int v1,
-                           const float *sd_phi, const float *sd_z, int na, int nb,
+                           const double *phi, const float *sd_z, int na, int nb,
                            const float *y_det, const float *z_det)
 {
     orc_grid g = {nx, ny, nz, dz};
@@ -633,7 +633,7 @@ void orc_exact_adjoint_f64(double *X, const double *y, double SO, double OD, dou
         for (int ib = 0; ib < nb; ib++) {
             for (int ia = 0; ia < na; ia++) {
                 double S[3], D[3];
-                orc_ray_points(SO, OD, (double)sd_phi[iv], sz, (double)y_det[ia],
+                orc_ray_points(SO, OD, phi[iv], sz, (double)y_det[ia],
                                z_det ? (double)z_det[ib] : 0.0, S, D);
                 orc_adj_ctx f = {X, scale * y[(long)iv * nd + (long)ib * na + ia]};
                 orc_exact_walk(&g, S, D, orc_adj_visit, &f);
@@ -644,7 +644,7 @@ void orc_exact_adjoint_f64(double *X, const double *y, double SO, double OD, dou
 
 /* Number of voxels crossed with positive length, per ray of views [v0, v1). */
 void orc_exact_count(int64_t *cnt, double SO, double OD, int nx, int ny, int nz, double dz,
-                     int v0, int v1, const float *sd_phi, const float *sd_z, int na, int nb,
+                     int v0, int v1, const double *phi, const float *sd_z, int na, int nb,
                      const float *y_det, const float *z_det)
 {
     orc_grid g = {nx, ny, nz, dz};
@@ -654,7 +654,7 @@ void orc_exact_count(int64_t *cnt, double SO, double OD, int nx, int ny, int nz,
         for (int ib = 0; ib < nb; ib++) {
             for (int ia = 0; ia < na; ia++) {
                 double S[3], D[3];
-                orc_ray_points(SO, OD, (double)sd_phi[iv], sz, (double)y_det[ia],
+                orc_ray_points(SO, OD, phi[iv], sz, (double)y_det[ia],
                                z_det ? (double)z_det[ib] : 0.0, S, D);
                 cnt[(long)(iv - v0) * nd + (long)ib * na + ia] =
                     orc_exact_walk(&g, S, D, NULL, NULL);
@@ -666,7 +666,7 @@ void orc_exact_count(int64_t *cnt, double SO, double OD, int nx, int ny, int nz,
 /* Exact forward for a list of rays (ray id iv*na*nb + ib*na + ia): y[k] is
  * ray rays[k], as orc_exact_forward_f64 computes it. */
 void orc_exact_forward_rays(const double *X, double *y, double SO, double OD, double scale,
-                            int nx, int ny, int nz, double dz, const float *sd_phi,
+                            int nx, int ny, int nz, double dz, const double *phi,
                             const float *sd_z, int na, int nb, const float *y_det,
                             const float *z_det, const int64_t *rays, long nr)
 {
@@ -677,7 +677,7 @@ void orc_exact_forward_rays(const double *X, double *y, double SO, double OD, do
         long r = rays[k] - (long)iv * nd;
         int ib = (int)(r / na), ia = (int)(r - (long)ib * na);
         double S[3], D[3];
-        orc_ray_points(SO, OD, (double)sd_phi[iv], sd_z ? (double)sd_z[iv] : 0.0,
+        orc_ray_points(SO, OD, phi[iv], sd_z ? (double)sd_z[iv] : 0.0,
                        (double)y_det[ia], z_det ? (double)z_det[ib] : 0.0, S, D);
         orc_fwd_ctx f = {X, 0.0};
         orc_exact_walk(&g, S, D, orc_fwd_visit, &f);
@@ -746,7 +746,7 @@ static void orc_grid_range(const float *g, int n, double lo, double hi, int *i0,
  */
 void orc_exact_adjoint_vox(double *x, const float *y, double SO, double OD, double scale,
                            int nx, int ny, int nz, double dz, int v0, int v1,
-                           const float *sd_phi, const float *sd_z, int na, int nb,
+                           const double *phi, const float *sd_z, int na, int nb,
                            const float *y_det, const float *z_det, const int64_t *vox,
                            long nvx)
 {
@@ -761,7 +761,7 @@ void orc_exact_adjoint_vox(double *x, const float *y, double SO, double OD, doub
         double hi[3] = {lo[0] + 1.0, lo[1] + 1.0, lo[2] + dz};
         double acc = 0.0;
         for (int iv = v0; iv < v1; iv++) {
-            double c = cos((double)sd_phi[iv]), s = sin((double)sd_phi[iv]);
+            double c = cos(phi[iv]), s = sin(phi[iv]);
             double sz = sd_z ? (double)sd_z[iv] : 0.0;
             double umin = INFINITY, umax = -INFINITY, wmin = INFINITY, wmax = -INFINITY;
             for (int q = 0; q < 8; q++) {
@@ -780,7 +780,7 @@ void orc_exact_adjoint_vox(double *x, const float *y, double SO, double OD, doub
             for (int ib = b0; ib <= b1; ib++)
                 for (int ia = a0; ia <= a1; ia++) {
                     double S[3], D[3];
-                    orc_ray_points(SO, OD, (double)sd_phi[iv], sz, (double)y_det[ia],
+                    orc_ray_points(SO, OD, phi[iv], sz, (double)y_det[ia],
                                    z_det ? (double)z_det[ib] : 0.0, S, D);
                     double l = orc_box_chord(S, D, lo, hi);
                     if (l > 0.0) acc += l * (double)y[(long)iv * nd + (long)ib * na + ia];

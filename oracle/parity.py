@@ -21,6 +21,14 @@ each subset value computed by the oracle exactly as the full function would
 Two sinograms feed the backprojectors: the GPU forward projection of the
 phantom (the sinogram a reconstruction sees) and N(0, 1) noise (every matrix
 entry's error shows, none averages out).
+
+A plan that uses the half or quarter turn (G = 2 or 4 views per walk) defines
+view v + j nv/G as view v turned by exactly j 2 pi / G. FP32 source angles
+single(2 pi k / nv) are not exact turns of each other (up to 2.4e-7 rad
+apart), so such a plan projects a scan whose angles are snapped to exact
+turns. ``snapped(para, G)`` is that scan for the FP64 model (FP64 angles
+phi_v + j 2 pi / G); ``matched_vs_fp64_snapped`` measures the kernels'
+arithmetic on their own geometry, ``matched_vs_fp64`` includes the snap.
 """
 from __future__ import annotations
 
@@ -38,48 +46,70 @@ def rel(a, b) -> float:
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
 
-def _three(gpu, ref, exact) -> dict:
-    return {"matched_vs_fp64": rel(gpu, exact), "reference_vs_fp64": rel(ref, exact),
-            "matched_vs_reference": rel(gpu, ref)}
+def _three(gpu, ref, exact, exact_snapped=None) -> dict:
+    out = {"matched_vs_fp64": rel(gpu, exact), "reference_vs_fp64": rel(ref, exact),
+           "matched_vs_reference": rel(gpu, ref)}
+    if exact_snapped is not None:
+        out["matched_vs_fp64_snapped"] = rel(gpu, exact_snapped)
+    return out
+
+
+def snapped(para, turns: int) -> dict:
+    """The scan a plan with `turns` views per walk projects: FP64 angles
+    phi[v + j nv/turns] = phi[v] + j 2 pi / turns for v < nv/turns (the FP32
+    angles of the walked views, turned exactly)."""
+    if turns <= 1:
+        return para
+    phi = np.asarray(para["sd_phi"], np.float32).astype(np.float64)
+    q = phi.size // turns
+    p64 = np.concatenate([phi[:q] + j * (2.0 * np.pi / turns) for j in range(turns)])
+    out = dict(para)
+    out["phi64"] = p64
+    return out
 
 
 def _threads(threads):
     return threads or max(1, os.cpu_count() or 1)
 
 
-def fan_parity(para, x, forward, adjoint, seed=0, threads=None) -> dict:
+def fan_parity(para, x, forward, adjoint, seed=0, threads=None, turns=1) -> dict:
     """Full fan-beam check: every ray, every pixel."""
     t = _threads(threads)
+    ps = snapped(para, turns) if turns > 1 else None
     x = np.ascontiguousarray(x, np.float32).reshape(-1)
     y = np.asarray(forward(x), np.float32).reshape(-1)
-    out = {"forward": dict(rays=int(y.size), **_three(y, fan_siddon_f32(x, para, threads=t),
-                                                     exact_forward(x, para, threads=t)))}
+    out = {"forward": dict(rays=int(y.size), **_three(
+        y, fan_siddon_f32(x, para, threads=t), exact_forward(x, para, threads=t),
+        exact_forward(x, ps, threads=t) if ps else None))}
     rng = np.random.default_rng(seed)
     for name, sino in (("phantom", y), ("random", rng.standard_normal(y.size).astype(np.float32))):
         xa = np.asarray(adjoint(sino), np.float32).reshape(-1)
-        out[f"adjoint_{name}_sino"] = dict(
-            voxels=int(xa.size), **_three(xa, fan_adj_f32(sino, para, threads=t),
-                                          exact_adjoint(sino, para, threads=t)))
+        out[f"adjoint_{name}_sino"] = dict(voxels=int(xa.size), **_three(
+            xa, fan_adj_f32(sino, para, threads=t), exact_adjoint(sino, para, threads=t),
+            exact_adjoint(sino, ps, threads=t) if ps else None))
     return out
 
 
 def cone_parity(para, x, forward, adjoint, n_rays=20000, n_vox=4000, seed=0,
-                threads=None) -> dict:
+                threads=None, turns=1) -> dict:
     """Cone-beam check on ``n_rays`` random rays and ``n_vox`` random voxels."""
     t = _threads(threads)
+    ps = snapped(para, turns) if turns > 1 else None
     rng = np.random.default_rng(seed)
     x = np.ascontiguousarray(x, np.float32).reshape(-1)
     y = np.asarray(forward(x), np.float32).reshape(-1)
     rays = np.sort(rng.choice(y.size, min(n_rays, y.size), replace=False))
     out = {"forward": dict(rays=int(rays.size), **_three(
         y[rays], cone_siddon_rays(x, para, rays, threads=t),
-        exact_forward_rays(x, para, rays, threads=t)))}
+        exact_forward_rays(x, para, rays, threads=t),
+        exact_forward_rays(x, ps, rays, threads=t) if ps else None))}
     vox = np.sort(rng.choice(x.size, min(n_vox, x.size), replace=False))
     for name in ("phantom", "random"):
         sino = y if name == "phantom" else rng.standard_normal(y.size).astype(np.float32)
         xa = np.asarray(adjoint(sino), np.float32).reshape(-1)
         out[f"adjoint_{name}_sino"] = dict(voxels=int(vox.size), **_three(
             xa[vox], cone_adj_vox(sino, para, vox, threads=t),
-            exact_adjoint_vox(sino, para, vox, threads=t)))
+            exact_adjoint_vox(sino, para, vox, threads=t),
+            exact_adjoint_vox(sino, ps, vox, threads=t) if ps else None))
         del sino
     return out

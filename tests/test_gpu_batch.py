@@ -102,16 +102,18 @@ def test_batch_turn_slices_bit_identical_to_single_plans():
 
 def test_batch_tiny_slices_of_every_kind_bit_identical():
     """Degenerate slices in one batch: one view (general), a one-pixel-wide
-    image and a single detector column (half turn), a 2 x 2 image (quarter
-    turn), beside a normal slice."""
+    image (general: the turns need even nx and ny), a single detector column
+    over a 2 x 2 image (half turn), a 2 x 2 image (quarter turn), beside a
+    normal slice."""
     import torch
     from framelab_gb300.batch import FanBatch
     paras = [G.fan_para(2, 2, 3, 1, L=(1.0, 1.0), SO=3.0, OD=3.0, Ly=3.0, y_os=0.013),
              G.fan_para(1, 2, 1, 2, L=(1.0, 2.0), SO=3.0, OD=3.0, Ly=3.0, y_os=0.013),
+             G.fan_para(2, 2, 1, 2, L=(1.0, 1.0), SO=3.0, OD=3.0, Ly=3.0, y_os=0.013),
              G.fan_para(2, 2, 2, 4, L=(1.0, 1.0), SO=3.0, OD=3.0, Ly=3.0),
              G.fan_para(24, 24, 48, 12, L=(1.0, 1.0), SO=3.0, OD=3.0, Ly=3.0)]
     B = FanBatch(paras)
-    assert B.turns == [1, 2, 4, 4]
+    assert B.turns == [1, 1, 2, 4, 4]
     rng = np.random.default_rng(14)
     x = torch.from_numpy(rng.standard_normal(B.n_vox).astype(np.float32)).cuda()
     y = torch.from_numpy(rng.standard_normal(B.n_rays).astype(np.float32)).cuda()

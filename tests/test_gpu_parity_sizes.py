@@ -10,13 +10,21 @@ oracle evaluating each sampled entry exactly as its full function would.
 For every operator three relative L2 errors are measured (oracle/parity.py):
 the GPU result against the FP64 exact model, the reference's own FP32 CPU
 kernel against the FP64 model, and the GPU result against the reference.
-The matched pair must be within 1e-5 of the FP64 model everywhere, for the
-backprojection of the phantom's sinogram and of N(0, 1) noise alike. Against
-the reference it must be within 1e-5 or, where the reference is itself
-further than that from the FP64 model (its FP32 Siddon at SO = 128,000
-pixels; its chord backprojector, Atx_cone_mf_cpu_new.cpp:23-85 with
+Each configuration runs twice. With the half and quarter turns off (the
+general and z-mirror kernels) the matched pair must be within 1e-5 of the
+FP64 model everywhere, for the backprojection of the phantom's sinogram and
+of N(0, 1) noise alike. With the turns on (the default) it projects the scan
+whose turned views are exact turns of the walked ones (oracle/parity.py,
+``snapped``): there it must be within 1e-5 of that scan's FP64 model
+everywhere, and within 1e-5 of the nominal model for the forward and the
+phantom's sinogram; the backprojection of noise then shows the angle snap
+(up to 2.4e-7 rad at radius r), bounded here by 3e-4.
+Against the reference the pair must be within 1e-5 or, where the reference
+is itself further than that from the FP64 model (its FP32 Siddon at SO =
+128,000 pixels; its chord backprojector, Atx_cone_mf_cpu_new.cpp:23-85 with
 find_l_3d.cpp:94-182, drops the chords of rays that leave a voxel within a
-rounding of an edge), within the reference's own error plus 1e-5.
+rounding of an edge), within the reference's own error plus 1e-5 -- plus
+the snap's own difference for the turn plans.
 """
 import math
 
@@ -39,23 +47,46 @@ def _ops(P):
     return fwd, adj
 
 
-def _check(res):
+def _turns(P):
+    return 4 if P.quarter_turn else (2 if P.rot_mirror else 1)
+
+
+def _check(res, turns):
     for op, r in res.items():
-        assert r["matched_vs_fp64"] < TOL, (op, r)
-        assert r["matched_vs_reference"] < max(TOL, r["reference_vs_fp64"] + TOL), (op, r)
+        if turns == 1:
+            assert r["matched_vs_fp64"] < TOL, (op, r)
+            assert r["matched_vs_reference"] < max(TOL, r["reference_vs_fp64"] + TOL), (op, r)
+        else:
+            assert r["matched_vs_fp64_snapped"] < TOL, (op, r)
+            snap = 3e-4 if op == "adjoint_random_sino" else TOL
+            assert r["matched_vs_fp64"] < snap, (op, r)
+            assert r["matched_vs_reference"] < max(snap, r["reference_vs_fp64"] + snap), (op, r)
+
+
+def _plans(p):
+    from framelab_gb300.projector import Plan
+    for turns_on in (True, False):
+        P = Plan(p)
+        if not turns_on:
+            P.quarter_turn = False
+            P.rot_mirror = False
+        yield P
 
 
 @pytest.mark.parametrize("field_mm", [256.0, 1.0])
 def test_fan256_full(field_mm):
     import oracle.parity as PAR
     from framelab_gb300 import geometry as G, phantoms as PH
-    from framelab_gb300.projector import Plan
     L = field_mm
     p = G.fan_para(256, 256, 512, 360, L=(L, L), SO=500.0, OD=500.0,
                    Ly=2.0 * math.sqrt(2.0) * L)
-    P = Plan(p)
-    res = PAR.fan_parity(p, PH.ellipses_2d(256, seed=1), *_ops(P))
-    _check(res)
+    x = PH.ellipses_2d(256, seed=1)
+    forms = []
+    for P in _plans(p):
+        t = _turns(P)
+        forms.append(t)
+        _check(PAR.fan_parity(p, x, *_ops(P), turns=t), t)
+    assert forms == [4, 1]
 
 
 @pytest.mark.parametrize("n", [256, 512])
@@ -63,16 +94,20 @@ def test_cone_config_sizes_on_subsets(n):
     import torch
     import oracle.parity as PAR
     from framelab_gb300 import geometry as G, phantoms as PH
-    from framelab_gb300.projector import Plan
     if n == 256:
         p = G.cone_para_mm(256, 360, 512, 384, det_pitch_mm=1.0, SO_mm=600.0, SD_mm=1200.0,
                            voxel_mm=1.0)
     else:
         p = G.cone_para_mm(512, 720, 1024, 768, det_pitch_mm=0.5, SO_mm=600.0, SD_mm=1200.0,
                            voxel_mm=0.5)
-    P = Plan(p)
-    res = PAR.cone_parity(p, PH.ellipsoids_3d(n, seed=1), *_ops(P), n_rays=20000,
-                          n_vox=4000 if n == 256 else 2000)
-    del P
-    torch.cuda.empty_cache()
-    _check(res)
+    x = PH.ellipsoids_3d(n, seed=1)
+    forms = []
+    for P in _plans(p):
+        t = _turns(P)
+        forms.append(t)
+        res = PAR.cone_parity(p, x, *_ops(P), n_rays=20000, n_vox=4000 if n == 256 else 2000,
+                              turns=t)
+        del P
+        torch.cuda.empty_cache()
+        _check(res, t)
+    assert forms == [4, 1]
