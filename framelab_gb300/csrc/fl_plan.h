@@ -26,13 +26,14 @@
 // weight's relative error stays near 1e-7 whatever the size of the volume.
 // The forward walk and the backprojection gather evaluate this same
 // expression from the same table entries, so both see identical crossings.
-struct AxisEntry {
+// 16- and 32-byte aligned, so each entry is read with vector loads
+struct alignas(16) AxisEntry {
     float kq, ih, il, c;
 };
-struct ColEntry {   // per (view, detector column): x and y axes
+struct alignas(32) ColEntry {   // per (view, detector column): x and y axes
     AxisEntry x, y;
 };
-struct RowEntry {   // per (view, detector row): z axis (cone only)
+struct alignas(32) RowEntry {   // per (view, detector row): z axis (cone only)
     AxisEntry z;
     float dz2;        // fl(d_z^2), for c_r
     float pad[3];

@@ -14,7 +14,7 @@ __device__ __forceinline__ float ldv(const T* p) { return Store<T>::ld(p); }
 // ---------------------------------------------------------------------------
 // Crossings in a segment frame (the model is described in fl_plan.h).
 // ---------------------------------------------------------------------------
-constexpr int kSegCone = 6;    // 3-D rays: segments of 64 planes of the dominant axis
+constexpr int kSegCone = 7;    // 3-D rays: segments of 128 planes of the dominant axis
 constexpr int kSegFan = 4;     // fan rays: segments of 16 planes
 
 // Crossing of the plane with m = k - kq relative to the anchor bh + be,
