@@ -8,10 +8,13 @@
 //  * FL_CGLS_GRAPH: FP32 storage; axpy/dot work fused into three kernels that
 //    keep alpha, beta and gamma in device memory; one iteration captured as a
 //    CUDA graph and replayed.
-//  * FL_CGLS_MIXED: as FL_CGLS_GRAPH, and the search direction is also kept as
-//    scaled FP16 for the projector's gathers (FP32 accumulation along each
-//    ray). Every `refresh` iterations the residual is recomputed in FP32 from
-//    u (r = (A^T A + lam) u - b).
+//  * FL_CGLS_MIXED: as FL_CGLS_GRAPH, with FP16 storage of the two operands
+//    the projectors read: the search direction (scaled, gathered along each
+//    ray with FP32 accumulation) and, on a cone plan, the forward projection
+//    that feeds the backprojection (scaled by the plan's y16_scale, gathered
+//    with FP32 accumulation). u, r and the step lengths stay FP32 / FP64, so
+//    the residual is updated in FP32 every iteration; every `refresh`
+//    iterations it is recomputed in FP32 from u (r = (A^T A + lam) u - b).
 // Both stop early once gamma < tol, like the reference; in the graph this is a
 // device flag that turns the remaining replays into no-ops.
 #include <cmath>
@@ -29,7 +32,10 @@ struct CgScalars {
     double tol;
     float lam;
     float p_scale;     // p16 = p * p_scale
-    float p_unscale;   // 1 / p_scale (forward applies it to the gathered sum)
+    float p_unscale;   // 1 / p_scale
+    float y_scale;     // mixed: scale of the FP16 forward projection (plan y16_scale, or 1)
+    float q_unscale;   // mixed: q = q_unscale * (the backprojection of it); else 1
+    int mixed;         // the direction is read in FP16
     int done;          // 1 once gamma < tol, or at a breakdown (see status)
     int iter;          // iterations completed
     int status;        // 1: a non-finite gamma or <p, q> (NaN / Inf in b, u0 or A) stopped it
@@ -129,6 +135,7 @@ k_cg_init(const float* __restrict__ bvec, const float* __restrict__ q, float* __
         double rms = sqrt(tot / (double)n);
         S->p_scale = rms > 0 ? (float)(1.0 / (8.0 * rms)) : 1.0f;
         S->p_unscale = 1.0f / S->p_scale;
+        S->q_unscale = S->mixed ? S->p_unscale / S->y_scale : 1.0f;
     }
 }
 
@@ -143,18 +150,19 @@ __global__ void k_cg_p16(const float* __restrict__ p, __half* __restrict__ p16, 
         p16[i] = __float2half_rn(p[i] * sc);
 }
 
-// q += lam p ; alpha = gamma / <p, q>
+// q = q_unscale q + lam p ; alpha = gamma / <p, q>  (q_unscale = 1 outside
+// the mixed form: the same bits as q + lam p)
 __global__ void __launch_bounds__(kThreads)
 k_cg_pq(const float* __restrict__ p, float* __restrict__ q, long long n, CgScalars* S,
         double* partials)
 {
     if (S->done) return;
-    float lam = S->lam;
+    float lam = S->lam, qs = S->q_unscale;
     double s = 0.0;
     for (long long i = (long long)blockIdx.x * kThreads + threadIdx.x; i < n;
          i += (long long)gridDim.x * kThreads) {
         float pi = p[i];
-        float qi = fmaf(lam, pi, q[i]);
+        float qi = fmaf(lam, pi, q[i] * qs);
         q[i] = qi;
         s += (double)pi * qi;
     }
@@ -196,6 +204,7 @@ k_cg_update(float* __restrict__ u, float* __restrict__ r, const float* __restric
         double rms = sqrt(tot / (double)n);
         S->p_scale = rms > 0 ? (float)(1.0 / (8.0 * rms)) : 1.0f;
         S->p_unscale = 1.0f / S->p_scale;
+        S->q_unscale = S->mixed ? S->p_unscale / S->y_scale : 1.0f;
         if (tot < S->tol) S->done = 1;
     }
 }
@@ -304,8 +313,9 @@ struct fl_cgls {
     fl_plan* plan;
     int mode;
     long long n, nr;
-    float *r, *p, *q, *tmp;     // tmp: sinogram (C^2 W p in the mixed driver)
+    float *r, *p, *q, *tmp;     // tmp: sinogram (C^2 W p in the fused drivers)
     __half* p16;
+    __half* tmp16;              // mixed form on a cone plan: the FP16 sinogram
     CgScalars* S;
     double* partials;
     double* hist;
@@ -325,7 +335,7 @@ struct fl_cgls {
 
 static void cgls_free(fl_cgls* c)
 {
-    void* ptrs[] = {c->r,    c->p,        c->q,    c->tmp, c->p16, c->S,
+    void* ptrs[] = {c->r,    c->p,        c->q,    c->tmp, c->p16, c->tmp16, c->S,
                     c->partials, c->hist, c->hb, c->hu,  c->bf,  c->uf};
     for (void* q : ptrs)
         if (q) cudaFree(q);
@@ -357,6 +367,7 @@ extern "C" int fl_cgls_create(fl_plan* plan, int mode, fl_cgls** out)
     M((void**)&c->r, c->n * 4); M((void**)&c->p, c->n * 4); M((void**)&c->q, c->n * 4);
     M((void**)&c->tmp, c->nr * 4);
     if (mode == FL_CGLS_MIXED) M((void**)&c->p16, c->n * 2);
+    if (mode == FL_CGLS_MIXED && plan->s.ndim == 3) M((void**)&c->tmp16, c->nr * 2);
     // the fused forms keep every vector z-folded on a z-mirror plan (the
     // algebra is elementwise, so only b in and u out change layout); whether
     // the plan uses the mirror is read again at every solve
@@ -490,14 +501,22 @@ static int mixed_iteration(fl_cgls* c, float* u, cudaStream_t s)
     CgScalars* S = c->S;
     const int lay = c->fold ? FL_LAY_X_FOLDED : 0;
     int st;
-    if (c->p16)
-        st = fl_matched_forward(P, c->p16, FL_F16, c->tmp, FL_F32, 2, &S->done, &S->p_unscale,
+    if (c->p16) {
+        // y = y_scale C^2 W p16 (FP16 on a cone plan), q' = W^T y; k_cg_pq
+        // rescales q' by p_unscale / y_scale
+        void* y = c->tmp16 ? (void*)c->tmp16 : (void*)c->tmp;
+        const int yt = c->tmp16 ? FL_F16 : FL_F32;
+        st = fl_matched_forward(P, c->p16, FL_F16, y, yt, 2, &S->done, &S->y_scale,
                                 lay | FL_LAY_Y_ADJ, s);
-    else
+        if (st) return st;
+        st = fl_matched_adjoint_wt(P, y, yt, c->q, FL_F32, &S->done, lay, s);
+    } else {
         st = fl_matched_forward(P, c->p, FL_F32, c->tmp, FL_F32, 2, &S->done, nullptr,
                                 lay | FL_LAY_Y_ADJ, s);
+        if (st) return st;
+        st = fl_matched_adjoint_w(P, c->tmp, c->q, FL_F32, &S->done, lay, s);
+    }
     if (st) return st;
-    if ((st = fl_matched_adjoint_w(P, c->tmp, c->q, FL_F32, &S->done, lay, s))) return st;
     k_cg_pq<<<c->grid, kThreads, 0, s>>>(c->p, c->q, c->n, S, c->partials);
     k_cg_update<<<c->grid, kThreads, 0, s>>>(u, c->r, c->p, c->q, c->n, S, c->partials, c->hist,
                                              c->hist_cap);
@@ -530,6 +549,9 @@ static int solve_mixed(fl_cgls* c, const float* b, float* u, float lam, int iter
     CgScalars init;
     std::memset(&init, 0, sizeof init);
     init.tol = tol; init.lam = lam;
+    init.mixed = c->p16 ? 1 : 0;
+    init.y_scale = c->tmp16 ? c->plan->y16_scale : 1.0f;
+    init.q_unscale = 1.0f;
     FL_CUDA(cudaMemcpyAsync(c->S, &init, sizeof init, cudaMemcpyHostToDevice, s));
     // the user's b and u (standard layout) or their z-folded copies
     const float* bb = b;

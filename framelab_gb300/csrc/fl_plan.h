@@ -98,6 +98,10 @@ struct fl_plan {
     // kernels; 0 keeps each kernel's built-in shape (set by fl_plan_autotune;
     // every thread's result is independent of the shape)
     int fwd_bx, fwd_by, adj_bx, adj_by;
+    // scale of an FP16 backprojection input (the mixed CGLS form): the largest
+    // power of two with y16_scale * c_r^2 <= 1 for every ray, so c_r^2 * (a
+    // ray's sum of w p) stays within FP16's range whenever |p| does
+    float y16_scale;
     // reusable scratch: sinogram-sized f32 for the pre-weighted adjoint input,
     // volume-sized for the z-folded copy of a forward input
     float *d_work;
@@ -150,6 +154,9 @@ int fl_matched_forward(fl_plan* p, const void* x, int xt, void* y, int yt, int c
 int fl_matched_weight(fl_plan* p, const void* y, int yt, float* yw, cudaStream_t st);
 int fl_matched_adjoint_w(fl_plan* p, const float* yw, void* x, int xt, const int* skip,
                          int layout, cudaStream_t st);
+// the same with the input in FP32 or (cone plans) FP16, wt = FL_F32 / FL_F16
+int fl_matched_adjoint_wt(fl_plan* p, const void* yw, int wt, void* x, int xt, const int* skip,
+                          int layout, cudaStream_t st);
 // volume (all frames) to the z-folded layout, or back with unfold = 1
 int fl_matched_fold(fl_plan* p, const void* src, void* dst, int dtype, int unfold,
                     cudaStream_t st);

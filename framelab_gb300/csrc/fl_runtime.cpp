@@ -167,6 +167,21 @@ static int build_tables(fl_plan* p, const std::vector<float>& phi, const float* 
             row[(size_t)iv * s.nb + ib] = r;
         }
     }
+    // FP16 backprojection input scale: 2^-ceil(log2(max c_r^2))
+    {
+        double cr2max = 0.0, sc = (double)s.scale * (double)s.scale;
+        for (int iv = 0; iv < s.nv; iv++) {      // c_r^2 = scale^2 (|d_xy|^2 + d_z^2)
+            double mxy = 0.0, mz = 0.0;
+            for (int ia = 0; ia < s.na; ia++)
+                mxy = std::fmax(mxy, (double)colr[(size_t)iv * s.na + ia]);
+            for (int ib = 0; ib < s.nb; ib++)
+                mz = std::fmax(mz, (double)row[(size_t)iv * s.nb + ib].dz2);
+            cr2max = std::fmax(cr2max, sc * (mxy + mz));
+        }
+        int e = 0;
+        std::frexp(cr2max > 0.0 ? cr2max : 1.0, &e);        // cr2max < 2^e
+        p->y16_scale = (float)std::ldexp(1.0, -e);
+    }
     // every crossing parameter the kernels read must be finite
     for (const ColEntry& e : col)
         if (!axis_finite(e.x) || !axis_finite(e.y))

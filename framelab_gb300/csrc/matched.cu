@@ -418,16 +418,79 @@ k_adj_fan_turn(TX* __restrict__ X, const float* __restrict__ ywp,
 // with w_rV evaluated exactly as in the forward walk. The TZ accumulators are
 // registers (k is a compile-time index).
 // ---------------------------------------------------------------------------
+// The backprojection input (pre-weighted sinogram) is FP32, or FP16 in the
+// mixed CGLS form. ld_in<TW, N> reads N consecutive values of one orbit from
+// an address aligned to N elements, as one vector load, and widens them.
+template <typename TW, int N>
+__device__ __forceinline__ void ld_in(const TW* __restrict__ p, float (&v)[N]);
+
+template <>
+__device__ __forceinline__ void ld_in<float, 1>(const float* __restrict__ p, float (&v)[1])
+{
+    v[0] = __ldg(p);
+}
+template <>
+__device__ __forceinline__ void ld_in<float, 2>(const float* __restrict__ p, float (&v)[2])
+{
+    const float2 u = __ldg(reinterpret_cast<const float2*>(p));
+    v[0] = u.x; v[1] = u.y;
+}
+template <>
+__device__ __forceinline__ void ld_in<float, 4>(const float* __restrict__ p, float (&v)[4])
+{
+    const float4 u = __ldg(reinterpret_cast<const float4*>(p));
+    v[0] = u.x; v[1] = u.y; v[2] = u.z; v[3] = u.w;
+}
+template <>
+__device__ __forceinline__ void ld_in<float, 8>(const float* __restrict__ p, float (&v)[8])
+{
+    // one 32-byte load (sm_100 and later; orbits are 32-byte aligned)
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]),
+          "=f"(v[7])
+        : "l"(p));
+}
+template <>
+__device__ __forceinline__ void ld_in<__half, 1>(const __half* __restrict__ p, float (&v)[1])
+{
+    v[0] = __half2float(__ldg(p));
+}
+template <>
+__device__ __forceinline__ void ld_in<__half, 2>(const __half* __restrict__ p, float (&v)[2])
+{
+    const float2 a = __half22float2(__ldg(reinterpret_cast<const __half2*>(p)));
+    v[0] = a.x; v[1] = a.y;
+}
+template <>
+__device__ __forceinline__ void ld_in<__half, 4>(const __half* __restrict__ p, float (&v)[4])
+{
+    const uint2 u = __ldg(reinterpret_cast<const uint2*>(p));
+    const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&u.x));
+    const float2 b = __half22float2(*reinterpret_cast<const __half2*>(&u.y));
+    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+}
+template <>
+__device__ __forceinline__ void ld_in<__half, 8>(const __half* __restrict__ p, float (&v)[8])
+{
+    const uint4 u = __ldg(reinterpret_cast<const uint4*>(p));
+    const unsigned w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&w[k]));
+        v[2 * k] = a.x; v[2 * k + 1] = a.y;
+    }
+}
+
 // Candidate rays of one detector column for the TZ voxels of a run. MODE +1:
 // the run lies above the source plane, so every ray that reaches it rises
 // (A_z increasing in k); MODE -1: below, every such ray falls; MODE 0: the run
 // straddles the source plane (general min/max). The other orientation's rays
 // get w <= 0 from the specialised formula, as they miss the run.
-template <int MODE, int TZ>
+template <int MODE, int TZ, typename TW>
 __device__ __forceinline__ void adj_rows(float (&acc)[TZ], int nk, int z0, float l, float h,
                                          float e1, float e2, float s1, float s2,
                                          const AxisEntry* __restrict__ rv, float bh, float be,
-                                         const float* __restrict__ ycol, int na, int nb)
+                                         const TW* __restrict__ ycol, int na, int nb)
 {
     float mn = fminf(e1, e2), mx = fmaxf(e1, e2);   // row span at plane k
 #pragma unroll
@@ -442,7 +505,9 @@ __device__ __forceinline__ void adj_rows(float (&acc)[TZ], int nk, int z0, float
         for (int ib = blo; ib <= bhi; ib++) {
             if (!FL_IN(ib, nb)) continue;
             const AxisEntry re = rv[ib];                 // (inv_z, off_z) of row ib
-            const float yval = __ldg(ycol + (long long)ib * na);
+            float yv1[1];
+            ld_in<TW, 1>(ycol + (long long)ib * na, yv1);
+            const float yval = yv1[0];
             const float2 azp = row_planes(re, fk0, fk1, bh, be);
             const float az0 = azp.x, az1 = azp.y;
             float l2, h2;
@@ -464,11 +529,11 @@ __device__ __forceinline__ void adj_rows(float (&acc)[TZ], int nk, int z0, float
 // with k; voxel k's rows are then [e1(k), e2(k + 1)] without per-plane
 // min / max. MODE 0: the general window. (MODE +1 does not occur: every run
 // of the lower half lies below the source.)
-template <int MODE, int TZ>
+template <int MODE, int TZ, typename TW>
 __device__ __forceinline__ void adj_rows_pair(float2 (&acc)[TZ], int nk, int z0, float l,
                                               float h, float e1, float e2, float s1, float s2,
                                               const AxisEntry* __restrict__ rv, float bh, float be,
-                                              const float* __restrict__ ycol, int na, int nb)
+                                              const TW* __restrict__ ycol, int na, int nb)
 {
     float mn = fminf(e1, e2), mx = fmaxf(e1, e2);
     float lo_e = e1 - 0.02f, hi_e = e2 + s2 + 0.02f;
@@ -491,7 +556,9 @@ __device__ __forceinline__ void adj_rows_pair(float2 (&acc)[TZ], int nk, int z0,
         for (int ib = blo; ib <= bhi; ib++) {
             if (!FL_IN(ib, nb)) continue;
             const AxisEntry re = rv[ib];
-            const float2 t = Store<float>::ld2(ycol + 2 * (long long)ib * na);
+            float tv[2];
+            ld_in<TW, 2>(ycol + 2 * (long long)ib * na, tv);
+            const float2 t = make_float2(tv[0], tv[1]);
             const float2 az = row_planes(re, fk0, fk1, bh, be);
             float l2, h2;
             if (MODE < 0) { l2 = fmaxf(l, az.y); h2 = fminf(h, az.x); }
@@ -505,11 +572,11 @@ __device__ __forceinline__ void adj_rows_pair(float2 (&acc)[TZ], int nk, int z0,
 // Half-turn form of adj_rows_pair: every weight also multiplies the row pair
 // of view v + nv/2 into the turned voxels' sums accr; y4 holds both row pairs
 // side by side (4 floats per row and column, 16-byte aligned).
-template <int MODE, int TZ>
+template <int MODE, int TZ, typename TW>
 __device__ __forceinline__ void adj_rows_quad(float2 (&acc)[TZ], float2 (&accr)[TZ], int nk,
                                               int z0, float l, float h, float e1, float e2,
                                               float s1, float s2, const AxisEntry* __restrict__ rv, float bh, float be,
-                                              const float* __restrict__ y4, int na, int nb)
+                                              const TW* __restrict__ y4, int na, int nb)
 {
     float mn = fminf(e1, e2), mx = fmaxf(e1, e2);
     float lo_e = e1 - 0.02f, hi_e = e2 + s2 + 0.02f;
@@ -532,8 +599,9 @@ __device__ __forceinline__ void adj_rows_quad(float2 (&acc)[TZ], float2 (&accr)[
         for (int ib = blo; ib <= bhi; ib++) {
             if (!FL_IN(ib, nb)) continue;
             const AxisEntry re = rv[ib];
-            const float4 u = __ldg(reinterpret_cast<const float4*>(y4 + 4 * (long long)ib * na));
-            const float2 t = make_float2(u.x, u.y), tr = make_float2(u.z, u.w);
+            float u[4];
+            ld_in<TW, 4>(y4 + 4 * (long long)ib * na, u);
+            const float2 t = make_float2(u[0], u[1]), tr = make_float2(u[2], u[3]);
             const float2 az = row_planes(re, fk0, fk1, bh, be);
             float l2, h2;
             if (MODE < 0) { l2 = fmaxf(l, az.y); h2 = fminf(h, az.x); }
@@ -554,9 +622,9 @@ __device__ __forceinline__ void adj_rows_quad(float2 (&acc)[TZ], float2 (&accr)[
 // A[(iv, r), V]); a weight of T, the other way round. yw is the packed
 // sinogram of k_weight_packed / k_fwd_quad (4 values per (iv < nv/2,
 // ib < nb/2, ia)); X the tiled folded volume (xfold) or the standard one.
-template <typename TX, int TZ>
+template <typename TX, int TZ, typename TW>
 __global__ void __launch_bounds__(128, 8)
-k_adj_quad(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __restrict__ col,
+k_adj_quad(TX* __restrict__ X, const TW* __restrict__ yw, const ColEntry* __restrict__ col,
            const AxisEntry* __restrict__ rowz, const ViewEntry* __restrict__ view, DetGrid G,
            int nx, int ny, int nz, int na, int nb, int nv, float dz, int zruns,
            const int* __restrict__ skip, int xfold)
@@ -578,7 +646,7 @@ k_adj_quad(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __r
         const ViewEntry ve = view[iv];
         const ColEntry* cv = col + (long long)iv * na;
         const AxisEntry* rv = rowz + (long long)iv * nb;
-        const float* yv = yw + (long long)iv * vstride;
+        const TW* yv = yw + (long long)iv * vstride;
         const float zr0 = (float)(z0 - nz / 2) * dz - ve.sz;
         const float zr1 = (float)(z0 + nk - nz / 2) * dz - ve.sz;
         const float tol = 1e-3f * dz;
@@ -600,10 +668,10 @@ k_adj_quad(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __r
                 const float s1 = dz * r1 * inv_dv, s2 = dz * r2 * inv_dv;
                 const float e1 = (zr0 * r1 - G.v0) * inv_dv, e2 = (zr0 * r2 - G.v0) * inv_dv;
                 if (mode < 0)
-                    adj_rows_quad<-1, TZ>(own, other, nk, z0, l, h, e1, e2, s1, s2, rv, bh, be,
+                    adj_rows_quad<-1, TZ, TW>(own, other, nk, z0, l, h, e1, e2, s1, s2, rv, bh, be,
                                           yv + 4 * ia, na, nbw);
                 else
-                    adj_rows_quad<0, TZ>(own, other, nk, z0, l, h, e1, e2, s1, s2, rv, bh, be,
+                    adj_rows_quad<0, TZ, TW>(own, other, nk, z0, l, h, e1, e2, s1, s2, rv, bh, be,
                                          yv + 4 * ia, na, nbw);
             }
         };
@@ -633,12 +701,12 @@ k_adj_quad(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __r
 // Quarter-turn form of adj_rows_pair: every weight multiplies the row pairs of
 // views v + j nv/4 into the sums a0..a3; y8 holds them side by side (8 floats
 // per row and column, 32-byte aligned).
-template <int MODE, int TZ>
+template <int MODE, int TZ, typename TW>
 __device__ __forceinline__ void adj_rows_oct(float2 (&a0)[TZ], float2 (&a1)[TZ],
                                              float2 (&a2)[TZ], float2 (&a3)[TZ], int nk, int z0,
                                              float l, float h, float e1, float e2, float s1,
                                              float s2, const AxisEntry* __restrict__ rv, float bh, float be,
-                                             const float* __restrict__ y8, int na, int nb)
+                                             const TW* __restrict__ y8, int na, int nb)
 {
     float mn = fminf(e1, e2), mx = fmaxf(e1, e2);
     float lo_e = e1 - 0.02f, hi_e = e2 + s2 + 0.02f;
@@ -661,12 +729,11 @@ __device__ __forceinline__ void adj_rows_oct(float2 (&a0)[TZ], float2 (&a1)[TZ],
         for (int ib = blo; ib <= bhi; ib++) {
             if (!FL_IN(ib, nb)) continue;
             const AxisEntry re = rv[ib];
-            // the orbit's 8 values in one 32-byte load (orbits are 32-byte aligned)
-            float2 t0, t1, t2, t3;
-            asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-                : "=f"(t0.x), "=f"(t0.y), "=f"(t1.x), "=f"(t1.y), "=f"(t2.x), "=f"(t2.y),
-                  "=f"(t3.x), "=f"(t3.y)
-                : "l"(y8 + 8 * (long long)ib * na));
+            // the orbit's 8 values in one vector load (32 bytes FP32, 16 bytes FP16)
+            float o8[8];
+            ld_in<TW, 8>(y8 + 8 * (long long)ib * na, o8);
+            const float2 t0 = make_float2(o8[0], o8[1]), t1 = make_float2(o8[2], o8[3]);
+            const float2 t2 = make_float2(o8[4], o8[5]), t3 = make_float2(o8[6], o8[7]);
             const float2 az = row_planes(re, fk0, fk1, bh, be);
             float l2, h2;
             if (MODE < 0) { l2 = fmaxf(l, az.y); h2 = fminf(h, az.x); }
@@ -688,9 +755,9 @@ __device__ __forceinline__ void adj_rows_oct(float2 (&a0)[TZ], float2 (&a1)[TZ],
 // (A[(iv + j nv/4, r), R^j V] = A[(iv, r), V]). yw is the packed sinogram of
 // k_weight_packed / k_fwd_oct (8 values per (iv < nv/4, ib < nb/2, ia)); X the
 // tiled folded volume (xfold) or the standard one.
-template <typename TX, int TZ>
+template <typename TX, int TZ, typename TW>
 __global__ void __launch_bounds__(128, TZ == 2 ? 8 : 6)
-k_adj_oct(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __restrict__ col,
+k_adj_oct(TX* __restrict__ X, const TW* __restrict__ yw, const ColEntry* __restrict__ col,
           const AxisEntry* __restrict__ rowz, const ViewEntry* __restrict__ view, DetGrid G, int n,
           int nz, int na, int nb, int nv, float dz, const int* __restrict__ skip, int xfold)
 {
@@ -714,7 +781,7 @@ k_adj_oct(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __re
         const ViewEntry ve = view[iv];
         const ColEntry* cv = col + (long long)iv * na;
         const AxisEntry* rv = rowz + (long long)iv * nb;
-        const float* yv = yw + (long long)iv * vstride;
+        const TW* yv = yw + (long long)iv * vstride;
         const float zr0 = (float)(z0 - nz / 2) * dz - ve.sz;
         const float zr1 = (float)(z0 + nk - nz / 2) * dz - ve.sz;
         const float tol = 1e-3f * dz;
@@ -736,12 +803,12 @@ k_adj_oct(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __re
                 const float r2 = __fdividef(1.0f, __fadd_rn(bh, hh) + ve.ac);
                 const float s1 = dz * r1 * inv_dv, s2 = dz * r2 * inv_dv;
                 const float e1 = (zr0 * r1 - G.v0) * inv_dv, e2 = (zr0 * r2 - G.v0) * inv_dv;
-                const float* y8 = yv + 8 * ia;
+                const TW* y8 = yv + 8 * ia;
                 if (mode < 0)
-                    adj_rows_oct<-1, TZ>(b0, b1, b2, b3, nk, z0, l, hh, e1, e2, s1, s2, rv, bh, be, y8,
+                    adj_rows_oct<-1, TZ, TW>(b0, b1, b2, b3, nk, z0, l, hh, e1, e2, s1, s2, rv, bh, be, y8,
                                          na, nbw);
                 else
-                    adj_rows_oct<0, TZ>(b0, b1, b2, b3, nk, z0, l, hh, e1, e2, s1, s2, rv, bh, be, y8,
+                    adj_rows_oct<0, TZ, TW>(b0, b1, b2, b3, nk, z0, l, hh, e1, e2, s1, s2, rv, bh, be, y8,
                                         na, nbw);
             }
         };
@@ -773,9 +840,9 @@ k_adj_oct(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __re
 // MIRROR: yw is the folded sinogram; the runs cover the lower half z < nz/2
 // only (the walked rows' rays never reach the upper half) and each thread also
 // produces the mirrored run, into the folded volume when xfold is set.
-template <typename TX, int TZ, bool MIRROR>
+template <typename TX, int TZ, bool MIRROR, typename TW>
 __global__ void __launch_bounds__(128, 8)
-k_adj_cone(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __restrict__ col,
+k_adj_cone(TX* __restrict__ X, const TW* __restrict__ yw, const ColEntry* __restrict__ col,
            const AxisEntry* __restrict__ rowz, const ViewEntry* __restrict__ view,
            const int* __restrict__ idY, const int* __restrict__ Nv, int tmp_size, DetGrid G,
            int nx, int ny, int nz, int na, int nb, float dz, int zruns,
@@ -804,7 +871,7 @@ k_adj_cone(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __r
         column_window(G, ve.c, ve.s, x0, y0, 1.0f, 1.0f, na, alo, ahi, dmin, dmax);
         const ColEntry* cv = col + (long long)iv * na;
         const AxisEntry* rv = rowz + (long long)iv * nb;
-        const float* yv = yw + (long long)iv * nb * na;   // folded: nb/2 rows of pairs
+        const TW* yv = yw + (long long)iv * nb * na;      // folded: nb/2 rows of pairs
         // run planes relative to the source: lowest and highest
         const float zr0 = (float)(z0 - nz / 2) * dz - ve.sz;
         const float zr1 = (float)(z0 + nk - nz / 2) * dz - ve.sz;
@@ -826,19 +893,19 @@ k_adj_cone(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __r
             const float s1 = dz * r1 * inv_dv, s2 = dz * r2 * inv_dv;
             const float e1 = (zr0 * r1 - G.v0) * inv_dv, e2 = (zr0 * r2 - G.v0) * inv_dv;
             if (MIRROR) {
-                const float* ycol = yv + 2 * ia;
+                const TW* ycol = yv + 2 * ia;
                 if (mode < 0)
-                    adj_rows_pair<-1, TZ>(acc2, nk, z0, l, h, e1, e2, s1, s2, rv, bh, be, ycol, na, nbw);
+                    adj_rows_pair<-1, TZ, TW>(acc2, nk, z0, l, h, e1, e2, s1, s2, rv, bh, be, ycol, na, nbw);
                 else
-                    adj_rows_pair<0, TZ>(acc2, nk, z0, l, h, e1, e2, s1, s2, rv, bh, be, ycol, na, nbw);
+                    adj_rows_pair<0, TZ, TW>(acc2, nk, z0, l, h, e1, e2, s1, s2, rv, bh, be, ycol, na, nbw);
             } else {
-                const float* ycol = yv + ia;
+                const TW* ycol = yv + ia;
                 if (mode > 0)
-                    adj_rows<1, TZ>(acc, nk, z0, l, h, e1, e2, s1, s2, rv, bh, be, ycol, na, nbw);
+                    adj_rows<1, TZ, TW>(acc, nk, z0, l, h, e1, e2, s1, s2, rv, bh, be, ycol, na, nbw);
                 else if (mode < 0)
-                    adj_rows<-1, TZ>(acc, nk, z0, l, h, e1, e2, s1, s2, rv, bh, be, ycol, na, nbw);
+                    adj_rows<-1, TZ, TW>(acc, nk, z0, l, h, e1, e2, s1, s2, rv, bh, be, ycol, na, nbw);
                 else
-                    adj_rows<0, TZ>(acc, nk, z0, l, h, e1, e2, s1, s2, rv, bh, be, ycol, na, nbw);
+                    adj_rows<0, TZ, TW>(acc, nk, z0, l, h, e1, e2, s1, s2, rv, bh, be, ycol, na, nbw);
             }
         }
     }
@@ -926,13 +993,14 @@ void launch_fwd_y(fl_plan* p, const void* x, void* y, int yt, int cr_power, cons
     else launch_fwd<TX, __nv_bfloat16>(p, x, y, cr_power, skip, xscale, yfold, st);
 }
 
-template <typename TX>
-void launch_adj(fl_plan* p, const float* yw, void* x, const int* skip, int xfold,
-                cudaStream_t st)
+// The cone backprojections, input TW (FP32, or FP16 in the mixed CGLS form).
+template <typename TX, typename TW>
+void launch_adj_cone(fl_plan* p, const TW* yw, void* x, const int* skip, int xfold,
+                     cudaStream_t st)
 {
     const fl_scan& s = p->s;
     DetGrid G = det_grid(p);
-    if (s.ndim == 3) {
+    {
         constexpr int TZ = 8;
         const int nzw = p->zmirror ? s.nz / 2 : s.nz;
         int zruns = (nzw + TZ - 1) / TZ;
@@ -942,7 +1010,7 @@ void launch_adj(fl_plan* p, const float* yw, void* x, const int* skip, int xfold
             zruns = (nzw + TO - 1) / TO;
             const dim3 ab = p->adj_bx ? dim3(p->adj_bx, p->adj_by) : dim3(8, 16);
             dim3 grid(fl_div_up(s.nx / 2, ab.x), fl_div_up(s.ny / 2, ab.y), (unsigned)zruns);
-            k_adj_oct<TX, TO><<<grid, ab, 0, st>>>(
+            k_adj_oct<TX, TO, TW><<<grid, ab, 0, st>>>(
                 (TX*)x, yw, p->d_col, p->d_rowz, p->d_view, G, s.nx, s.nz, s.na, s.nb, s.nv,
                 s.dz, skip, xfold);
         } else if (p->zmirror && p->rot) {
@@ -951,22 +1019,33 @@ void launch_adj(fl_plan* p, const float* yw, void* x, const int* skip, int xfold
             zruns = (nzw + TQ - 1) / TQ;
             const dim3 ab = p->adj_bx ? dim3(p->adj_bx, p->adj_by) : dim3(16, 8);
             dim3 grid(fl_div_up(s.nx, ab.x), fl_div_up(s.ny / 2, ab.y), (unsigned)zruns);
-            k_adj_quad<TX, TQ><<<grid, ab, 0, st>>>(
+            k_adj_quad<TX, TQ, TW><<<grid, ab, 0, st>>>(
                 (TX*)x, yw, p->d_col, p->d_rowz, p->d_view, G, s.nx, s.ny, s.nz, s.na, s.nb, s.nv,
                 s.dz, zruns, skip, xfold);
         } else if (p->zmirror) {
             const dim3 ab = p->adj_bx ? dim3(p->adj_bx, p->adj_by) : dim3(16, 8);
             dim3 grid(fl_div_up(s.nx, ab.x), fl_div_up(s.ny, ab.y), (unsigned)zruns * s.nt);
-            k_adj_cone<TX, TZ, true><<<grid, ab, 0, st>>>(
+            k_adj_cone<TX, TZ, true, TW><<<grid, ab, 0, st>>>(
                 (TX*)x, yw, p->d_col, p->d_rowz, p->d_view, p->d_idY, p->d_Nv, p->tmp_size, G,
                 s.nx, s.ny, s.nz, s.na, s.nb, s.dz, zruns, skip, xfold);
         } else {
             const dim3 ab = p->adj_bx ? dim3(p->adj_bx, p->adj_by) : dim3(32, 4);
             dim3 grid(fl_div_up(s.nx, ab.x), fl_div_up(s.ny, ab.y), (unsigned)zruns * s.nt);
-            k_adj_cone<TX, TZ, false><<<grid, ab, 0, st>>>(
+            k_adj_cone<TX, TZ, false, TW><<<grid, ab, 0, st>>>(
                 (TX*)x, yw, p->d_col, p->d_rowz, p->d_view, p->d_idY, p->d_Nv, p->tmp_size, G,
                 s.nx, s.ny, s.nz, s.na, s.nb, s.dz, zruns, skip, 0);
         }
+    }
+}
+
+template <typename TX>
+void launch_adj(fl_plan* p, const float* yw, void* x, const int* skip, int xfold,
+                cudaStream_t st)
+{
+    const fl_scan& s = p->s;
+    DetGrid G = det_grid(p);
+    if (s.ndim == 3) {
+        launch_adj_cone<TX, float>(p, yw, x, skip, xfold, st);
     } else if (fl_plan_turns(p) > 1) {
         // 2 x 2 primary blocks once there are at least 4 waves of them, else
         // one primary pixel per thread (the same bits)
@@ -1142,6 +1221,21 @@ int fl_matched_adjoint_w(fl_plan* p, const float* yw, void* x, int xt, const int
     else if (xt == FL_F16) launch_adj<__half>(p, yw, x, skip, xfold, st);
     else launch_adj<__nv_bfloat16>(p, yw, x, skip, xfold, st);
     return fl_check_launch("matched adjoint");
+}
+
+int fl_matched_adjoint_wt(fl_plan* p, const void* yw, int wt, void* x, int xt, const int* skip,
+                          int layout, cudaStream_t st)
+{
+    if (wt == FL_F32) return fl_matched_adjoint_w(p, (const float*)yw, x, xt, skip, layout, st);
+    if (wt != FL_F16 || p->s.ndim != 3)
+        return fl_set_error(FL_ERR_UNSUPPORTED,
+                            "matched adjoint: FP16 input is for cone plans only");
+    const int xfold = (p->zmirror && (layout & FL_LAY_X_FOLDED)) ? 1 : 0;
+    const __half* w = (const __half*)yw;
+    if (xt == FL_F32) launch_adj_cone<float, __half>(p, w, x, skip, xfold, st);
+    else if (xt == FL_F16) launch_adj_cone<__half, __half>(p, w, x, skip, xfold, st);
+    else launch_adj_cone<__nv_bfloat16, __half>(p, w, x, skip, xfold, st);
+    return fl_check_launch("matched adjoint (FP16 input)");
 }
 
 // Launch-shape autotuner of the cone projector kernels: each 128-thread shape
