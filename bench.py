@@ -87,7 +87,8 @@ def parse():
                          "(default), the z mirror alone (no half or quarter turn), or none "
                          "(general kernels)")
     ap.add_argument("--only", default="",
-                    help="comma list of legs: mixed,plain,hostplain,e2e,kernels,seq,grad")
+                    help="comma list of legs: mixed,plain,hostplain,e2e,kernels,seq,grad,"
+                         "parity,dropin")
     return ap.parse_args()
 
 
@@ -370,7 +371,8 @@ class Ctx:
         self.stream = torch.cuda.current_stream()
         self.K, self.W = a.steps, a.warmup
         self.legs = (set(a.only.split(",")) if a.only else
-                     {"mixed", "plain", "hostplain", "e2e", "kernels", "seq", "grad"})
+                     {"mixed", "plain", "hostplain", "e2e", "kernels", "seq", "grad", "parity",
+                      "dropin"})
 
     def barrier(self):
         if self.world > 1:
@@ -507,6 +509,93 @@ def host_structure_cgls(ctx, P, b, lam, cg_g, detail, iters=2):
     return out
 
 
+def parity_block(ctx, w, p):
+    """Parity of the matched pair on this workload's own geometry (the oracle
+    as the checker, untimed): the plan with its half / quarter turns and the
+    plan without them, each against the FP64 exact model, beside the
+    reference's own FP32 CPU kernels against the same model. Cone volumes on
+    seeded subsets (20,000 rays; 2,000 or 4,000 voxels), fans in full
+    (oracle/parity.py)."""
+    torch = ctx.torch
+    import oracle.parity as PAR
+    from framelab_gb300 import phantoms as PH
+    from framelab_gb300.projector import Plan
+    n = w["n"]
+    x = PH.ellipsoids_3d(n, seed=1) if w["kind"] == "cone" else PH.ellipses_2d(n, seed=1)
+    out = {}
+    for form in ("turns", "precise"):
+        P = Plan(p)
+        if form == "precise":
+            P.quarter_turn = False
+            P.rot_mirror = False
+        t = 4 if P.quarter_turn else (2 if P.rot_mirror else 1)
+
+        def fwd(v, P=P):
+            return P.forward(torch.from_numpy(np.ascontiguousarray(v)).to(ctx.dev)).cpu().numpy()
+
+        def adj(v, P=P):
+            return P.adjoint(torch.from_numpy(np.ascontiguousarray(v)).to(ctx.dev)).cpu().numpy()
+        t0 = time.perf_counter()
+        if w["kind"] == "cone":
+            r = PAR.cone_parity(p, x, fwd, adj, n_rays=20000, n_vox=2000 if n >= 512 else 4000,
+                                turns=t)
+        else:
+            r = PAR.fan_parity(p, x, fwd, adj, turns=t)
+        r["views_per_walk"] = t
+        r["seconds"] = time.perf_counter() - t0
+        out[form] = r
+        del P
+        torch.cuda.empty_cache()
+    return out
+
+
+def dropin_pair(ctx, w, p):
+    """The MATLAB classes' path: version 1 (ConeBeamScanner/setPara.m:82), i.e.
+    Ax_cone_mf_gpu_new + Atx_cone_mf_gpu_new through host pointers, as
+    ConeBeamScanner/apply.m and applyAdjoint.m call them -- each call copies
+    its input to the device and its output back (the bit-exact replicas of
+    the reference's CPU kernels). Wall-clock seconds of one call each, after
+    one untimed pair."""
+    import ctypes as C
+    from framelab_gb300 import _lib
+    L = _lib.load()
+    n, na, nb = w["n"], w["na"], w["nb"]
+    nv = len(p["sd_phi"])
+    rng = np.random.default_rng(0)
+    X = rng.random(n ** 3, dtype=np.float32)
+    y = np.zeros(nv * na * nb, np.float32)
+    yn = np.zeros_like(y)
+    Y = rng.random(nv * na * nb, dtype=np.float32)
+    xo = np.zeros(n ** 3, np.float32)
+    a = {k: np.ascontiguousarray(p[k], np.float32)
+         for k in ("sd_phi", "sd_z", "y_det", "z_det", "cos_phi", "sin_phi")}
+    idY = np.ascontiguousarray(np.asarray(p["id_Y"]).T.reshape(-1).astype(np.int32))
+    Nv = np.ascontiguousarray(p["Nv"].astype(np.int32))
+    P_ = lambda v: v.ctypes.data_as(C.c_void_p)
+    nvb, ts = int(p["nv_block"]), int(p["tmp_size"])
+
+    def fwd():
+        L.Ax_cone_mf_gpu_new(P_(X), P_(y), P_(yn), P_(a["sd_phi"]), P_(a["sd_z"]), P_(a["y_det"]),
+                             P_(a["z_det"]), P_(idY), P_(Nv), float(p["SO"]), float(p["OD"]),
+                             float(p["scale"]), float(p["dz"]), n, n, n, 1, na, nb, nv, ts, nvb)
+        _lib.check_last()
+
+    def adj():
+        L.Atx_cone_mf_gpu_new(P_(xo), P_(Y), P_(a["cos_phi"]), P_(a["sin_phi"]), P_(a["sd_z"]),
+                              P_(a["y_det"]), P_(a["z_det"]), P_(idY), P_(Nv), float(p["SO"]),
+                              float(p["OD"]), float(p["scale"]), float(p["dy_det"]),
+                              float(p["y_os"]), float(p["dz_det"]), float(p["dz"]), n, n, n, 1,
+                              na, nb, nv, ts, nvb)
+        _lib.check_last()
+    fwd(); adj()
+    ctx.torch.cuda.synchronize()
+    t0 = time.perf_counter(); fwd(); t1 = time.perf_counter(); adj(); t2 = time.perf_counter()
+    return {"dropin_iter_per_s": 1.0 / (t2 - t0), "dropin_forward_s": t1 - t0,
+            "dropin_adjoint_s": t2 - t1,
+            "dropin_call": "Ax_cone_mf_gpu_new + Atx_cone_mf_gpu_new (host pointers, version 1)",
+            "dropin_bytes_copied_per_iter": 4 * (2 * n ** 3 + 3 * nv * na * nb)}
+
+
 def restrict_symmetry(ctx, P):
     """--symmetry: keep the plan to the z mirror alone, or to the general
     kernels (the default uses every symmetry the scan has)."""
@@ -599,6 +688,10 @@ def run_single(ctx, name, w, p):
             y16 = P.forward(x_true.half())
             detail["fp16_storage_vs_fp32_rel_l2"] = ctx.rel(y16, y32)
             del xr, yr, y32, y16
+    if "parity" in ctx.legs:
+        detail["parity"] = parity_block(ctx, w, p)
+    if "dropin" in ctx.legs and w["kind"] == "cone":
+        detail.update(dropin_pair(ctx, w, p))
     if "grad" in ctx.legs and w["kind"] == "cone":
         # gradient of 1/2 |A x - b|^2 through the autograd binding (backward =
         # the exact-transpose backprojector) against central differences on 64

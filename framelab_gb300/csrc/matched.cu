@@ -675,8 +675,17 @@ k_adj_quad(TX* __restrict__ X, const TW* __restrict__ yw, const ColEntry* __rest
                                          yv + 4 * ia, na, nbw);
             }
         };
-        column(ix, iy, accV, accT);
-        column(tx, ty, accT, accV);
+        // both columns in one rolled loop (one copy of the row code); the two
+        // sets swap after each column and are back in order after the second
+#pragma unroll 1
+        for (int k = 0; k < 2; k++) {
+            column(k ? tx : ix, k ? ty : iy, accV, accT);
+#pragma unroll
+            for (int z = 0; z < TZ; z++) {
+                const float2 t = accV[z];
+                accV[z] = accT[z]; accT[z] = t;
+            }
+        }
     }
     const long long nxy = (long long)nx * ny;
     const long long cV = (long long)iy * nx + ix, cT = (long long)ty * nx + tx;
@@ -812,10 +821,20 @@ k_adj_oct(TX* __restrict__ X, const TW* __restrict__ yw, const ColEntry* __restr
                                         na, nbw);
             }
         };
-        column(cx[0], cy[0], A0, A1, A2, A3);
-        column(cx[1], cy[1], A1, A2, A3, A0);
-        column(cx[2], cy[2], A2, A3, A0, A1);
-        column(cx[3], cy[3], A3, A0, A1, A2);
+        // the four turns in one rolled loop (one copy of the row code: the
+        // unrolled form overflowed the instruction cache): turn k's weights go
+        // to A_{k+j} with view iv + j nv/4, so the sets rotate one place after
+        // each turn and are back in order after the fourth
+#pragma unroll 1
+        for (int k = 0; k < 4; k++) {
+            column(k == 0 ? cx[0] : k == 1 ? cx[1] : k == 2 ? cx[2] : cx[3],
+                   k == 0 ? cy[0] : k == 1 ? cy[1] : k == 2 ? cy[2] : cy[3], A0, A1, A2, A3);
+#pragma unroll
+            for (int z = 0; z < TZ; z++) {
+                const float2 t = A0[z];
+                A0[z] = A1[z]; A1[z] = A2[z]; A2[z] = A3[z]; A3[z] = t;
+            }
+        }
     }
     const long long nn = (long long)n * n;
 #pragma unroll
