@@ -410,18 +410,27 @@ def hbm_peak():
         return 6800.0, "fallback"
 
 
-def traffic_of(workload, dom):
-    tpath = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tpath):
-        with open(tpath) as fh:
-            ent = json.load(fh).get(workload, {}).get(dom)
-        if ent:
-            return ent.get("bytes_per_launch")
-    return None
+def roofline_model():
+    try:
+        with open(os.path.join(ROOT, "profiles", "roofline_model.json")) as fh:
+            return json.load(fh)
+    except OSError:
+        return None
 
 
-def projector_roofline(ctx, workload, n_isect, n_rays, n_vox, t_fwd, t_adj, detail, label):
-    """Dominant projector kernel: algorithmic bytes over CUDA-event time."""
+def projector_roofline(ctx, workload, n_isect, n_rays, n_vox, t_fwd, t_adj, detail, label,
+                       sm_mhz=None, l1_model=True):
+    """The dominant projector kernel against the bound it runs into.
+
+    The matched projectors gather every voxel / sinogram value a ray or voxel
+    needs through L1 (the algorithmic bytes below move at 1.3-1.9x the HBM
+    copy rate, so they are L1/L2 hits, not DRAM traffic). With l1_model the
+    roofline is the L1 data pipe: wavefronts per intersection from the ncu
+    capture of the current kernels (profiles/roofline_model.json) times this
+    workload's intersections, over the CUDA-event time, against 1 wavefront
+    per SM-cycle at the SM clock sampled during the run. Issue slots and the
+    HBM fraction of the compulsory bytes (input read once, output written
+    once) stand beside it; so does the algorithmic-bytes figure."""
     b_fwd = n_isect * 4 + n_rays * 4      # f32 voxel gathers + f32 sinogram writes
     b_adj = n_isect * 4 + n_vox * 4       # f32 sinogram gathers + f32 voxel writes
     peak, src = hbm_peak()
@@ -430,12 +439,40 @@ def projector_roofline(ctx, workload, n_isect, n_rays, n_vox, t_fwd, t_adj, deta
                   fwd_alg_GBps=b_fwd / t_fwd / 1e9, adj_alg_GBps=b_adj / t_adj / 1e9,
                   fwd_rays_per_s=n_rays / t_fwd, adj_voxel_updates_per_s=n_isect / t_adj)
     dom = "adjoint" if t_adj > t_fwd else "forward"
-    ach = (b_adj / t_adj if dom == "adjoint" else b_fwd / t_fwd) / 1e9
-    return {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
-            "frac": ach / peak if peak else None, "traffic": traffic_of(workload, dom),
-            "kernel": f"{label} {dom} (f32 storage)", "peak_source": src,
-            "bytes_definition": "sum over rays of voxels crossed x element bytes + "
-                                "one element per ray (forward) / per voxel (adjoint)"}
+    t = t_adj if dom == "adjoint" else t_fwd
+    compulsory = 4 * (n_rays + n_vox)     # one pass over the input and the output
+    alg = (b_adj if dom == "adjoint" else b_fwd)
+    hbm = {"bound": "hbm", "unit": "GB/s", "peak": peak, "peak_source": src,
+           "compulsory_GBps": compulsory / t / 1e9,
+           "compulsory_frac": compulsory / t / 1e9 / peak if peak else None,
+           "algorithmic_GBps": alg / t / 1e9,
+           "algorithmic_frac": alg / t / 1e9 / peak if peak else None}
+    m = roofline_model() if l1_model else None
+    if not m:
+        return {"bound": "hbm", "achieved": alg / t / 1e9, "peak": peak, "unit": "GB/s",
+                "frac": alg / t / 1e9 / peak if peak else None, "traffic": None,
+                "kernel": f"{label} {dom} (f32 storage)", "peak_source": src,
+                "bytes_definition": "sum over rays of voxels crossed x element bytes + "
+                                    "one element per ray (forward) / per voxel (adjoint)"}
+    k = m[dom]
+    f = (sm_mhz or 2070.0) * 1e6
+    sms = m["sms"]
+    ach = k["l1_wavefronts_per_isect"] * n_isect / t
+    pk = m["l1_wavefronts_per_sm_cycle"] * sms * f
+    iss = k["warp_inst_per_isect"] * n_isect / t
+    ipk = m["issue_per_sm_cycle"] * sms * f
+    return {"bound": "l1", "achieved": ach, "peak": pk, "unit": "wavefronts/s",
+            "frac": ach / pk, "traffic": k["dram_bytes_per_isect"] * n_isect,
+            "kernel": f"{label} {dom} ({k['kernel']})",
+            "peak_source": f"1 L1 data-pipe wavefront per SM-cycle x {sms} SMs x "
+                           f"{f / 1e6:.0f} MHz (SM clock sampled in this run)",
+            "model": "ncu per-intersection counts of the current kernels at cone256 "
+                     "(profiles/roofline_model.json) x this workload's intersections; "
+                     "traffic likewise scaled (a lower bound at larger sizes, where L2 "
+                     "reuse across views falls)",
+            "issue": {"achieved": iss, "peak": ipk, "unit": "warp-instructions/s",
+                      "frac": iss / ipk},
+            "hbm": hbm}
 
 
 def time_pair(ctx, P, x, reps=3):
@@ -674,8 +711,9 @@ def run_single(ctx, name, w, p):
         p32 = (u_g / (u_g.abs().max() + 1e-30)).contiguous()
         tf, ta, y, xo = time_pair(ctx, P, p32)
         roofline = projector_roofline(ctx, name, n_isect, P.n_rays, P.n_vox, tf, ta, detail,
-                                      "matched")
-        if name == "cone256":
+                                      "matched", clocks.summary().get("sm_mhz"),
+                                      l1_model=w["kind"] == "cone" and P.quarter_turn)
+        if w["kind"] == "cone":
             # dot-product identity <A x, y> = <x, A^T y> on N(0,1) vectors (FP64 dots)
             g = torch.Generator(device=ctx.dev).manual_seed(11)
             xr = torch.randn(P.n_vox, device=ctx.dev, generator=g)
@@ -774,7 +812,7 @@ def run_batch(ctx, name, w, paras):
         _, tf = ctx.timed(lambda: [B.forward(xs, out=y) for _ in range(reps)])
         _, ta = ctx.timed(lambda: [B.adjoint(y, out=xo) for _ in range(reps)])
         roofline = projector_roofline(ctx, name, n_isect, B.n_rays, B.n_vox, tf / reps,
-                                      ta / reps, detail, "batched matched")
+                                      ta / reps, detail, "batched matched", l1_model=False)
     return dict(value=job_rate(world, K, t_b), t_step=t_b / K, e2e=e2e, roofline=roofline,
                 launches=B.launches_per_iteration * K + 1, detail=detail,
                 clocks=clocks.summary(), unit="iter/s")
@@ -833,7 +871,7 @@ def run_sb(ctx, name, w, p):
         del cnt
         tf, ta, _, _ = time_pair(ctx, P, (u / (u.abs().max() + 1e-30)).contiguous())
         roofline = projector_roofline(ctx, name, n_isect, P.n_rays, P.n_vox, tf, ta, detail,
-                                      "matched")
+                                      "matched", l1_model=False)
         # one framelet step of the outer loop (analysis with shrink and Bregman
         # update, synthesis into b), against its compulsory bytes: u read, b
         # written, v read and written, t written and read back
