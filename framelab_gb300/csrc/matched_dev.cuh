@@ -230,8 +230,21 @@ __device__ __forceinline__ void seg_walk(const ColEntry* __restrict__ ce,
         jz = slab_guess(Z, a_in, nzr);
     }
     const bool xd = x_dominant(X, Y);
-    int s1, s2;
-    if (!seg_range<SH>(xd ? X : Y, xd ? nx : ny, a_in, a_out, s1, s2)) return;
+    int s1 = 0, s2 = -1;
+    const bool hit = seg_range<SH>(xd ? X : Y, xd ? nx : ny, a_in, a_out, s1, s2);
+    // Warp alignment: when the warp's rays share their dominant axis and its
+    // direction (all but the warps at a 45-degree switch), every lane walks
+    // the warp's whole range of segments, so that all lanes work on the same
+    // segment at the same time instead of drifting a segment apart (a lane's
+    // first segment depends on where its ray enters). A segment a ray does
+    // not cross is empty in its own frame and costs the lane only the test.
+    const unsigned am = __activemask();
+    const bool pd = xd ? X.ih > 0.0f : Y.ih > 0.0f;
+    const int key = (xd ? 2 : 0) | (pd ? 1 : 0);
+    const int lo = __reduce_min_sync(am, hit ? s1 : 0x7fffffff);
+    const int hi = __reduce_max_sync(am, hit ? s2 : -1);
+    if (!hit) return;
+    if (__match_any_sync(am, key) == am) { s1 = lo; s2 = hi; }
     const int jx = slab_guess(X, a_in, nx), jy = slab_guess(Y, a_in, ny);
     if (xd) seg_walk_dom<THREE, true>(ce, pZ, nx, ny, nzr, s1, s2, jx, jy, jz, body);
     else seg_walk_dom<THREE, false>(ce, pZ, nx, ny, nzr, s1, s2, jx, jy, jz, body);
