@@ -80,3 +80,75 @@ def test_soft_shrink_known_answers():
     assert np.array_equal(out[0][(0, 0, 0)], a)                       # low-pass kept
     for key in ((1, 0, 0), (0, 2, 1)):
         assert np.array_equal(out[0][key].ravel(), [-1.0, 0.0, 0.0, 0.0, 1.0])
+
+
+# --------------------------------------------------------------------------
+# Impulse responses written out by hand from the MATLAB sources
+# --------------------------------------------------------------------------
+# ConvSymAsym3D.m:19-24 places filter M at every 2^(L-1)-th tap of a column
+# kernel and calls imfilter(A, ker, 'circular'): correlation (imfilter's
+# default), 'same' size, kernel centre at its middle tap. For an impulse at
+# index p that gives C(p - d * 2^(L-1)) = M(c + d) (c the middle tap): the
+# filter read backwards around p, wrapped around the array's ends.
+# FraDecMultiLevel3D.m:35-44: filter D{i} runs along MATLAB dimension 2 (y),
+# D{j} along dimension 1 (x), D{k} along dimension 3 (z); here (z, y, x) is
+# numpy's (axis 0, 1, 2). Linear filters, GenerateFrameletFilter.m:10-12:
+#   D1 = [1 2 1]/4, D2 = -[1 0 -1]/4*sqrt(2) = [-s, 0, s] with s = sqrt(2)/4,
+#   D3 = [-1 2 -1]/4.
+S4 = np.sqrt(2.0) / 4
+RESP = {  # offset d -> value, the filter read backwards (offset -1 holds the last tap)
+    0: {-1: 0.25, 0: 0.5, 1: 0.25},
+    1: {-1: S4, 0: 0.0, 1: -S4},
+    2: {-1: -0.25, 0: 0.5, 1: -0.25},
+}
+
+
+def _impulse(shape, at):
+    a = np.zeros(shape)
+    a[at] = 1.0
+    return a
+
+
+@pytest.mark.parametrize("band", [(1, 0, 0), (0, 1, 2), (2, 2, 1), (1, 1, 1)])
+def test_level1_impulse_response_is_the_reversed_tensor_filter(band):
+    shape, at = (7, 8, 9), (3, 4, 5)
+    c = N.frame_dec_level(_impulse(shape, at), N.filters("linear")[0], 1)[band]
+    i, j, k = band                    # along y, x, z
+    want = np.zeros(shape)
+    for dz, vz in RESP[k].items():
+        for dy, vy in RESP[i].items():
+            for dx, vx in RESP[j].items():
+                want[at[0] + dz, at[1] + dy, at[2] + dx] = vz * vy * vx
+    assert np.allclose(c, want, atol=1e-15, rtol=0)
+
+
+def test_level2_taps_are_two_apart():
+    """ConvSymAsym3D.m:16-20: at level 2 the kernel is [M1 0 M2 0 M3]."""
+    shape, at = (5, 11, 6), (2, 5, 3)
+    c = N.frame_dec_level(_impulse(shape, at), N.filters("linear")[0], 2)[(1, 0, 0)]
+    line = c[at[0], :, at[2]] / (0.5 * 0.5)        # D1 centre taps along x and z
+    want = np.zeros(11)
+    want[at[1] - 2], want[at[1] + 2] = S4, -S4
+    assert np.allclose(line, want, atol=1e-15, rtol=0)
+
+
+def test_circular_boundary_wraps_the_response():
+    """imfilter(..., 'circular') (ConvSymAsym3D.m:24): an impulse at the first
+    index reaches the last one."""
+    shape = (4, 6, 5)
+    c = N.frame_dec_level(_impulse(shape, (0, 0, 0)), N.filters("linear")[0], 1)[(0, 1, 0)]
+    # D2 along x: offset -1 -> index nx-1 holds +s, offset +1 -> index 1 holds -s
+    assert c[0, 0, 4] == pytest.approx(S4 * 0.5 * 0.5)
+    assert c[0, 0, 1] == pytest.approx(-S4 * 0.5 * 0.5)
+    assert c[3, 5, 4] == pytest.approx(S4 * 0.25 * 0.25)
+
+
+def test_haar_filters_are_one_sided():
+    """GenerateFrameletFilter.m:3-4: D1 = [0 1 1]/2, D2 = -[0 1 -1]/2: the
+    response of an impulse at p sits at p and p - 1 only."""
+    shape, at = (4, 4, 6), (1, 2, 3)
+    c = N.frame_dec_level(_impulse(shape, at), N.filters("haar")[0], 1)[(0, 1, 0)]
+    line = c[at[0], at[1], :] / (0.5 * 0.5)
+    want = np.zeros(6)
+    want[at[2]], want[at[2] - 1] = -0.5, 0.5        # D2 = [0, -1/2, 1/2] read backwards
+    assert np.allclose(line, want, atol=1e-15, rtol=0)
