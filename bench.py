@@ -171,36 +171,39 @@ def _threads():
     return max(1, os.cpu_count() or 1)
 
 
-def cone_pair_seconds(w, p, row_step=16, av=4):
+def cone_pair_seconds(w, p, row_step=16, av=16):
     """Seconds for one forward (Ax_cone_mf_cpu_siddon) + one backprojection
     (Atx_cone_mf_cpu_new) of the oracle's bit-exact restatement with all host
-    threads, from a bounded sample extrapolated linearly.
-    Forward sample: one view per thread, every `row_step`-th detector row (a ray
-    depends only on its view, column and row, so these are rays of the full
-    scan). Backprojection sample: one slice per thread, spread over z, x `av`
-    views."""
+    threads, from a bounded sample (several seconds of CPU work) extrapolated
+    linearly.
+    Forward sample: four views per thread, spread over the scan, every
+    `row_step`-th detector row (a ray depends only on its view, column and
+    row, so these are rays of the full scan). Backprojection sample: one slice
+    per thread, spread over z, x `av` views spread over the scan."""
     import concurrent.futures as cf
     import oracle as O
     threads = _threads()
     n, nv, nb = w["n"], len(p["sd_phi"]), w["nb"]
     rng = np.random.default_rng(0)
     x = rng.random(n ** 3, dtype=np.float32)
-    fv = min(nv, threads)
+    fv = min(nv, 4 * threads)
+    fsel = np.linspace(0, nv - 1, fv).astype(int)
     rows = np.arange(0, nb, row_step)
     q = dict(p)
-    q["sd_phi"] = p["sd_phi"][:fv]
-    q["sd_z"] = p["sd_z"][:fv]
+    q["sd_phi"] = p["sd_phi"][fsel]
+    q["sd_z"] = p["sd_z"][fsel]
     q["z_det"] = p["z_det"][rows]
-    q["id_X"] = p["id_X"][:fv]
+    q["id_X"] = p["id_X"][fsel]
     t0 = time.perf_counter()
     O.cone_siddon_f32(x, q, threads=threads)
     t_f = time.perf_counter() - t0
     fwd_full = t_f * (nv / fv) * (nb / len(rows))
     av = min(av, nv)
+    asel = np.linspace(0, nv - 1, av).astype(int)
     y = rng.random(av * w["na"] * nb, dtype=np.float32)
     r = dict(p)
     for k in ("cos_phi", "sin_phi", "sd_phi", "sd_z"):
-        r[k] = p[k][:av]
+        r[k] = p[k][asel]
     r["id_Y"] = np.arange(av, dtype=np.uint32).reshape(av, 1)
     r["Nv"] = np.array([av], np.uint32)
     r["tmp_size"] = np.uint32(av)
