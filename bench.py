@@ -413,23 +413,30 @@ def hbm_peak():
         return 6800.0, "fallback"
 
 
-def roofline_model():
+def roofline_model(form):
+    """Per-intersection counts of one kernel form's pair ("hex": quarter turns
+    with the reflection, "oct": quarter turns), or None."""
     try:
         with open(os.path.join(ROOT, "profiles", "roofline_model.json")) as fh:
-            return json.load(fh)
+            m = json.load(fh)
     except OSError:
         return None
+    k = m.get("forms", {}).get(form)
+    if not k:
+        return None
+    return dict(k, sms=m["sms"], l1_wavefronts_per_sm_cycle=m["l1_wavefronts_per_sm_cycle"],
+                issue_per_sm_cycle=m["issue_per_sm_cycle"])
 
 
 def projector_roofline(ctx, workload, n_isect, n_rays, n_vox, t_fwd, t_adj, detail, label,
-                       sm_mhz=None, l1_model=True):
+                       sm_mhz=None, l1_form=None):
     """The dominant projector kernel against the bound it runs into.
 
     The matched projectors gather every voxel / sinogram value a ray or voxel
     needs through L1 (the algorithmic bytes below move at 1.3-1.9x the HBM
-    copy rate, so they are L1/L2 hits, not DRAM traffic). With l1_model the
+    copy rate, so they are L1/L2 hits, not DRAM traffic). With l1_form the
     roofline is the L1 data pipe: wavefronts per intersection from the ncu
-    capture of the current kernels (profiles/roofline_model.json) times this
+    capture of the kernel form in use (profiles/roofline_model.json) times this
     workload's intersections, over the CUDA-event time, against 1 wavefront
     per SM-cycle at the SM clock sampled during the run. Issue slots and the
     HBM fraction of the compulsory bytes (input read once, output written
@@ -450,7 +457,7 @@ def projector_roofline(ctx, workload, n_isect, n_rays, n_vox, t_fwd, t_adj, deta
            "compulsory_frac": compulsory / t / 1e9 / peak if peak else None,
            "algorithmic_GBps": alg / t / 1e9,
            "algorithmic_frac": alg / t / 1e9 / peak if peak else None}
-    m = roofline_model() if l1_model else None
+    m = roofline_model(l1_form) if l1_form else None
     if not m:
         return {"bound": "hbm", "achieved": alg / t / 1e9, "peak": peak, "unit": "GB/s",
                 "frac": alg / t / 1e9 / peak if peak else None, "traffic": None,
@@ -469,7 +476,7 @@ def projector_roofline(ctx, workload, n_isect, n_rays, n_vox, t_fwd, t_adj, deta
             "kernel": f"{label} {dom} ({k['kernel']})",
             "peak_source": f"1 L1 data-pipe wavefront per SM-cycle x {sms} SMs x "
                            f"{f / 1e6:.0f} MHz (SM clock sampled in this run)",
-            "model": "ncu per-intersection counts of the current kernels at cone256 "
+            "model": "ncu per-intersection counts of the kernel form in use at cone256 "
                      "(profiles/roofline_model.json) x this workload's intersections; "
                      "traffic likewise scaled (a lower bound at larger sizes, where L2 "
                      "reuse across views falls)",
@@ -568,7 +575,7 @@ def parity_block(ctx, w, p):
         if form == "precise":
             P.quarter_turn = False
             P.rot_mirror = False
-        t = 4 if P.quarter_turn else (2 if P.rot_mirror else 1)
+        t = P.views_per_walk
 
         def fwd(v, P=P):
             return P.forward(torch.from_numpy(np.ascontiguousarray(v)).to(ctx.dev)).cpu().numpy()
@@ -715,7 +722,8 @@ def run_single(ctx, name, w, p):
         tf, ta, y, xo = time_pair(ctx, P, p32)
         roofline = projector_roofline(ctx, name, n_isect, P.n_rays, P.n_vox, tf, ta, detail,
                                       "matched", clocks.summary().get("sm_mhz"),
-                                      l1_model=w["kind"] == "cone" and P.quarter_turn)
+                                      l1_form={8: "hex", 4: "oct"}.get(P.views_per_walk)
+                                      if w["kind"] == "cone" else None)
         if w["kind"] == "cone":
             # dot-product identity <A x, y> = <x, A^T y> on N(0,1) vectors (FP64 dots)
             g = torch.Generator(device=ctx.dev).manual_seed(11)
@@ -815,7 +823,7 @@ def run_batch(ctx, name, w, paras):
         _, tf = ctx.timed(lambda: [B.forward(xs, out=y) for _ in range(reps)])
         _, ta = ctx.timed(lambda: [B.adjoint(y, out=xo) for _ in range(reps)])
         roofline = projector_roofline(ctx, name, n_isect, B.n_rays, B.n_vox, tf / reps,
-                                      ta / reps, detail, "batched matched", l1_model=False)
+                                      ta / reps, detail, "batched matched")
     return dict(value=job_rate(world, K, t_b), t_step=t_b / K, e2e=e2e, roofline=roofline,
                 launches=B.launches_per_iteration * K + 1, detail=detail,
                 clocks=clocks.summary(), unit="iter/s")
@@ -874,7 +882,7 @@ def run_sb(ctx, name, w, p):
         del cnt
         tf, ta, _, _ = time_pair(ctx, P, (u / (u.abs().max() + 1e-30)).contiguous())
         roofline = projector_roofline(ctx, name, n_isect, P.n_rays, P.n_vox, tf, ta, detail,
-                                      "matched", l1_model=False)
+                                      "matched")
         # one framelet step of the outer loop (analysis with shrink and Bregman
         # update, synthesis into b), against its compulsory bytes: u read, b
         # written, v read and written, t written and read back

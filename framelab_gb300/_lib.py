@@ -21,6 +21,8 @@ F32, F16, BF16 = 0, 1, 2
 OPT_Z_MIRROR = 1
 OPT_ROT_MIRROR = 2
 OPT_QUARTER_TURN = 3
+OPT_REFLECT = 4
+QUERY_ADJ_RUN = 16
 FRAMELET_OPT_FUSED = 1
 
 

@@ -135,13 +135,19 @@ static int build_tables(fl_plan* p, const std::vector<float>& phi, const float* 
     const double SO = s.SO, OD = s.OD, SD = SO + OD;
     const double ac = SO / SD;   // alpha at the isocentre plane: A = alpha - ac
     const int nx2 = s.nx / 2, ny2 = s.ny / 2, nz2 = s.nz / 2;
-    std::vector<ColEntry> col((size_t)s.nv * s.na);
-    std::vector<float> colr((size_t)s.nv * s.na);
-    std::vector<RowEntry> row((size_t)s.nv * s.nb);
-    std::vector<ViewEntry> view(s.nv);
-    for (int iv = 0; iv < s.nv; iv++) {
-        double c = std::cos((double)phi[iv]), sn = std::sin((double)phi[iv]);
-        double Sx = -SO * c, Sy = -SO * sn, Sz = sd_z ? (double)sd_z[iv] : 0.0;
+    // views 0 .. nv-1, then row nv: view nv/8 at the exact diagonal angle
+    // pi/4 (the reflection form walks it there; a copy of view 0 otherwise)
+    const int nvt = s.nv + 1;
+    std::vector<ColEntry> col((size_t)nvt * s.na);
+    std::vector<float> colr((size_t)nvt * s.na);
+    std::vector<RowEntry> row((size_t)nvt * s.nb);
+    std::vector<ViewEntry> view(nvt);
+    const bool diag = s.nv % 8 == 0;
+    for (int iv = 0; iv < nvt; iv++) {
+        const int src = iv < s.nv ? iv : (diag ? s.nv / 8 : 0);
+        double c = std::cos((double)phi[src]), sn = std::sin((double)phi[src]);
+        if (iv == s.nv && diag) c = sn = std::sqrt(0.5);
+        double Sx = -SO * c, Sy = -SO * sn, Sz = sd_z ? (double)sd_z[src] : 0.0;
         view[iv] = ViewEntry{(float)c, (float)sn, (float)Sz, (float)ac};
         for (int ia = 0; ia < s.na; ia++) {
             double u = y_det[ia];
@@ -281,6 +287,24 @@ static int build_tables(fl_plan* p, const std::vector<float>& phi, const float* 
         p->rot4_ok = ok ? 1 : 0;
     }
     p->rot4 = p->rot4_ok;
+    // reflection (fl_plan.h): cone plans with the quarter turn, nv a multiple
+    // of 8, view nv - v the mirror image of view v about the x axis to within
+    // 1e-6 (cos equal, sin opposite) and an exactly symmetric detector
+    p->rot8_ok = 0;
+    if (p->rot4_ok && s.ndim == 3 && diag && s.na % 2 == 0) {
+        bool ok = true;
+        for (int ia = 0; ia < s.na / 2 && ok; ia++)
+            if (y_det[s.na - 1 - ia] != -y_det[ia]) ok = false;
+        for (int iv = 1; iv < s.nv && ok; iv++) {
+            const double c0 = std::cos((double)phi[iv]), s0 = std::sin((double)phi[iv]);
+            const int m = s.nv - iv;
+            const double c1 = std::cos((double)phi[m]), s1 = std::sin((double)phi[m]);
+            if (std::fabs(c0 - c1) > 1e-6 || std::fabs(s0 + s1) > 1e-6) ok = false;
+        }
+        if (phi[0] != 0.0f) ok = false;             // view 0 is its own mirror image
+        p->rot8_ok = ok ? 1 : 0;
+    }
+    p->rot8 = p->rot8_ok;
     return FL_OK;
 }
 
@@ -299,6 +323,10 @@ extern "C" int fl_plan_option(fl_plan* p, int option, int value)
         p->rot4 = (value && p->rot4_ok) ? 1 : 0;
         return fl_set_error(FL_OK, "");
     }
+    if (option == FL_OPT_REFLECT) {
+        p->rot8 = (value && p->rot8_ok) ? 1 : 0;
+        return fl_set_error(FL_OK, "");
+    }
     return fl_set_error(FL_ERR_INVALID, "fl_plan_option: unknown option %d", option);
 }
 
@@ -314,7 +342,15 @@ extern "C" int fl_plan_query(const fl_plan* p, int option, int* value)
         return fl_set_error(FL_OK, "");
     }
     if (option == FL_OPT_QUARTER_TURN) {
-        *value = fl_plan_turns(p) == 4 ? 1 : 0;
+        *value = fl_plan_turns(p) >= 4 ? 1 : 0;
+        return fl_set_error(FL_OK, "");
+    }
+    if (option == FL_OPT_REFLECT) {
+        *value = fl_plan_turns(p) == 8 ? 1 : 0;
+        return fl_set_error(FL_OK, "");
+    }
+    if (option == FL_QUERY_ADJ_RUN) {
+        *value = p->adj_run == 1 ? 1 : 2;
         return fl_set_error(FL_OK, "");
     }
     return fl_set_error(FL_ERR_INVALID, "fl_plan_query: unknown option %d", option);

@@ -158,6 +158,64 @@ k_fwd_oct(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restri
     }
 }
 
+// View and column of the ray that image k of a walked ray (v, a) is, on a
+// reflection plan: k < 4 the turn R^k (view v + k nv/4, column a), k >= 4 the
+// reflection R^(k-4) M (view (k-4) nv/4 - v, column na-1-a).
+__device__ __forceinline__ void hex_image(int k, int v, int a, int na, int nv, long long& vk,
+                                          int& ak)
+{
+    const int qv = nv / 4;
+    if (k < 4) { vk = v + (long long)k * qv; ak = a; }
+    else { vk = ((long long)(k - 4) * qv - v + nv) % nv; ak = na - 1 - a; }
+}
+
+// Reflection form (fl_plan::rot8): the block walks rows ib < nb/2 of the
+// slots s < nv/8 (hex_slot: the walked views 0 .. nv/8); each walk yields the
+// rays of its sixteen images (hex_image, rows ib and nb-1-ib), all with the
+// walked ray's c_r. yfold writes the backprojection's input layout for these
+// plans: per (s, ib < nb/2, ia) the 8 values of the turn images side by side
+// in the first plane, the 8 of the reflected images in the second
+// (k_weight_packed_hex).
+template <typename TX, typename TY>
+__global__ void __launch_bounds__(128, 6)
+k_fwd_hex(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restrict__ col,
+          const float* __restrict__ colr, const RowEntry* __restrict__ row, int n, int nz,
+          int na, int nb, int nv, long long nper, float scale, int cr_power,
+          const int* __restrict__ skip, const float* __restrict__ xscale, int yfold)
+{
+    if (skip && *skip) return;
+    const int ia = blockIdx.x * blockDim.x + threadIdx.x;
+    const int sl = blockIdx.y;                      // < nv / 8
+    const int ib = blockIdx.z * blockDim.y + threadIdx.y;
+    const int nbh = nb / 2;
+    if (ia >= na || ib >= nbh) return;
+    int v, vt, a;
+    hex_slot(sl, ia, na, nv, v, vt, a);
+    const ColEntry* ce = col + (long long)vt * na + a;
+    const RowEntry* re = row + (long long)vt * nb + ib;
+    float2 acc[8];
+    walk_hex<TX>(X, ce, &re->z, n, nz, acc, nper);
+    const float cr = ray_cr(scale, colr[(long long)vt * na + a], __ldg(&re->dz2));
+    const float xs = xscale ? *xscale : 1.0f;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        float o0 = acc[k].x, o1 = acc[k].y;
+        if (xscale) { o0 *= xs; o1 *= xs; }
+        o0 = cr * o0; o1 = cr * o1;
+        if (cr_power == 2) { o0 = cr * o0; o1 = cr * o1; }
+        if (yfold) {                    // the orbit's two planes of 8 values
+            const long long half = (long long)(nv / 8) * nbh * na * 8;
+            Store<TY>::st2(y + (k < 4 ? 0 : half) + 8 * (((long long)sl * nbh + ib) * na + ia) +
+                               2 * (k & 3), o0, o1);
+        } else {
+            long long vk; int ak;
+            hex_image(k, v, a, na, nv, vk, ak);
+            Store<TY>::st(y + (vk * nb + ib) * na + ak, o0);
+            Store<TY>::st(y + (vk * nb + (nb - 1 - ib)) * na + ak, o1);
+        }
+    }
+}
+
 template <typename TX, typename TY>
 __global__ void __launch_bounds__(128, 8)
 k_fwd_fan(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restrict__ col,
@@ -264,6 +322,36 @@ __global__ void k_weight_packed(float* __restrict__ yw, const TY* __restrict__ y
         const float a = Store<TY>::ld_plain(y + (vj * nb + ib) * na + ia);
         const float b = Store<TY>::ld_plain(y + (vj * nb + (nb - 1 - ib)) * na + ia);
         Store<float>::st2(yw + 2 * G * r + 2 * j, cr * a, cr * b);
+    }
+}
+
+// Packed yw of a reflection plan: for r = (s < nv/8, ib < nb/2, ia) the 16
+// values c_r y of the walked ray's images (hex_image, rows ib and nb-1-ib),
+// with c_r of the walked ray (hex_slot): images 0..3 at 8 r + 2 k, images
+// 4..7 in the second plane, at npack * 8 + 8 r + 2 (k - 4).
+template <typename TY>
+__global__ void k_weight_packed_hex(float* __restrict__ yw, const TY* __restrict__ y,
+                                    const float* __restrict__ colr,
+                                    const RowEntry* __restrict__ row, int na, int nb, int nv,
+                                    long long npack, float scale)
+{
+    long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= npack) return;
+    const int nbh = nb / 2;
+    const int ia = (int)(r % na);
+    const long long q = r / na;
+    const int ib = (int)(q % nbh);
+    const int sl = (int)(q / nbh);
+    int v, vt, a;
+    hex_slot(sl, ia, na, nv, v, vt, a);
+    const float cr = ray_cr(scale, colr[(long long)vt * na + a], row[(long long)vt * nb + ib].dz2);
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        long long vk; int ak;
+        hex_image(k, v, a, na, nv, vk, ak);
+        const float p0 = Store<TY>::ld_plain(y + (vk * nb + ib) * na + ak);
+        const float p1 = Store<TY>::ld_plain(y + (vk * nb + (nb - 1 - ib)) * na + ak);
+        Store<float>::st2(yw + (k < 4 ? 0 : 8 * npack) + 8 * r + 2 * (k & 3), cr * p0, cr * p1);
     }
 }
 
@@ -856,6 +944,202 @@ k_adj_oct(TX* __restrict__ X, const TW* __restrict__ yw, const ColEntry* __restr
         }
 }
 
+// Reflection form of adj_rows_oct: every weight multiplies the row pairs of
+// the walked ray's eight images into the sums P[j] (turn images) and Q[j]
+// (reflected images); yt / yr hold them side by side (8 values per row and
+// column in each plane, 32-byte aligned), so each is one vector load whose
+// lanes read neighbouring columns' orbits.
+template <int MODE, int TZ, typename TW>
+__device__ __forceinline__ void adj_rows_hex(float2 (&P)[4][TZ], float2 (&Q)[4][TZ], int nk,
+                                             int z0, float l, float h, float e1, float e2,
+                                             float s1, float s2,
+                                             const AxisEntry* __restrict__ rv, float bh,
+                                             float be, const TW* __restrict__ yt,
+                                             const TW* __restrict__ yr, int na, int nb)
+{
+    float mn = fminf(e1, e2), mx = fmaxf(e1, e2);
+    float lo_e = e1 - 0.02f, hi_e = e2 + s2 + 0.02f;
+#pragma unroll
+    for (int k = 0; k < TZ; k++) {
+        if (k >= nk) break;
+        int blo, bhi;
+        if (MODE < 0) {
+            blo = max(__float2int_ru(lo_e), 0);
+            bhi = min(__float2int_rd(hi_e), nb - 1);
+            lo_e += s1; hi_e += s2;
+        } else {
+            e1 += s1; e2 += s2;
+            const float mn1 = fminf(e1, e2), mx1 = fmaxf(e1, e2);
+            blo = max(__float2int_ru(fminf(mn, mn1) - 0.02f), 0);
+            bhi = min(__float2int_rd(fmaxf(mx, mx1) + 0.02f), nb - 1);
+            mn = mn1; mx = mx1;
+        }
+        const float fk0 = (float)(z0 + k), fk1 = (float)(z0 + k + 1);
+        for (int ib = blo; ib <= bhi; ib++) {
+            if (!FL_IN(ib, nb)) continue;
+            const AxisEntry re = rv[ib];
+            float o[16];
+            ld_in<TW, 8>(yt + 8 * (long long)ib * na, *reinterpret_cast<float(*)[8]>(o));
+            ld_in<TW, 8>(yr + 8 * (long long)ib * na, *reinterpret_cast<float(*)[8]>(o + 8));
+            const float2 az = row_planes(re, fk0, fk1, bh, be);
+            float l2, h2;
+            if (MODE < 0) { l2 = fmaxf(l, az.y); h2 = fminf(h, az.x); }
+            else { l2 = fmaxf(l, fminf(az.x, az.y)); h2 = fminf(h, fmaxf(az.x, az.y)); }
+            const float w = fmaxf(h2 - l2, 0.0f);
+            const float2 w2 = make_float2(w, w);
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                P[j][k] = __ffma2_rn(w2, make_float2(o[2 * j], o[2 * j + 1]), P[j][k]);
+                Q[j][k] = __ffma2_rn(w2, make_float2(o[8 + 2 * j], o[9 + 2 * j]), Q[j][k]);
+            }
+        }
+    }
+}
+
+// Reflection + quarter-turn + z-mirror backprojection (fl_plan::rot8, nx == ny
+// == n): one thread per voxel column V0 = (x, y) of the octant x <= y < n/2
+// with its images C_k = R^k V0 and D_k = R^k M V0 (k < 4; for x == y, D_k =
+// C_{k+3} and only the C_k are visited), a run of TZ voxels of the lower half
+// and their mirrors; one frame. It visits the walked views v = 0 .. nv/8
+// (view nv/8 from table row nv; views 0 and nv/8 on columns a < na/2). In view
+// v a weight of column C_k multiplies turn slot j (view v + j nv/4) into
+// C_{k+j} and reflected slot j (view j nv/4 - v, column na-1-a) into D_{j-k};
+// a weight of D_k, turn slot j into D_{k+j} and reflected slot j into C_{j-k}.
+// One weight thus feeds sixteen (voxel, ray) pairs. yw is the packed input
+// of k_weight_packed_hex / k_fwd_hex (two planes); X the tiled folded volume
+// (xfold) or the standard one.
+template <typename TX, int TZ, typename TW>
+__global__ void __launch_bounds__(128, TZ == 1 ? 8 : 6)
+k_adj_hex(TX* __restrict__ X, const TW* __restrict__ yw, const ColEntry* __restrict__ col,
+          const AxisEntry* __restrict__ rowz, const ViewEntry* __restrict__ view, DetGrid G, int n,
+          int nz, int na, int nb, int nv, float dz, const int* __restrict__ skip, int xfold)
+{
+    if (skip && *skip) return;
+    const int ix = blockIdx.x * blockDim.x + threadIdx.x;    // < n / 2
+    const int iy = blockIdx.y * blockDim.y + threadIdx.y;    // < n / 2
+    const int z0 = blockIdx.z * TZ;
+    const int nzw = nz / 2, nbw = nb / 2, ov = nv / 8, h = n / 2;
+    const int nk = min(TZ, nzw - z0);
+    if (ix >= h || iy >= h || ix > iy) return;
+    const bool diag = ix == iy;
+    // P: the sums the turn slots feed, Q: the reflected slots' (rotated one
+    // place per column, in opposite directions; exchanged between the C and
+    // the D columns)
+    float2 P[4][TZ], Q[4][TZ];
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+#pragma unroll
+        for (int k = 0; k < TZ; k++) { P[j][k] = make_float2(0.0f, 0.0f); Q[j][k] = P[j][k]; }
+    const float inv_dv = 1.0f / G.dv;
+    const long long vstride = (long long)nbw * na * 8;       // values per slot and plane
+    const long long half = (long long)ov * vstride;          // the reflected images' plane
+    const int nsteps = diag ? 4 : 8;
+    for (int w = 0; w <= ov; w++) {
+        const bool last = w == ov;
+        const int vt = last ? nv : w;                          // table row
+        const int alim = (w == 0 || last) ? na / 2 : na;       // walked columns
+        const ViewEntry ve = view[vt];
+        const ColEntry* cv = col + (long long)vt * na;
+        const AxisEntry* rv = rowz + (long long)vt * nb;
+        const TW* yv = yw + (last ? 8LL * (na / 2) : (long long)w * vstride);
+        const float zr0 = (float)(z0 - nz / 2) * dz - ve.sz;
+        const float zr1 = (float)(z0 + nk - nz / 2) * dz - ve.sz;
+        const float tol = 1e-3f * dz;
+        const int mode = (zr1 <= -tol) ? -1 : 0;               // lower half: never above
+        int px = ix, py = iy;                                  // C_0
+#pragma unroll 1
+        for (int k = 0; k < nsteps; k++) {
+            if (k == 4) {                                      // the D columns: D_0 = M V0
+                px = ix; py = n - 1 - iy;
+#pragma unroll
+                for (int j = 0; j < 4; j++)
+#pragma unroll
+                    for (int z = 0; z < TZ; z++) {
+                        const float2 t = P[j][z];
+                        P[j][z] = Q[j][z]; Q[j][z] = t;
+                    }
+            }
+            int alo, ahi; float dmin, dmax;
+            column_window(G, ve.c, ve.s, (float)(px - h), (float)(py - h), 1.0f, 1.0f, na, alo,
+                          ahi, dmin, dmax);
+            ahi = min(ahi, alim - 1);
+            for (int ia = alo; ia <= ahi; ia++) {
+                if (!FL_IN(ia, na)) continue;
+                const ColEntry ce = cv[ia];
+                float bh, be, l, hh;
+                if (!cone_column(ce, px, py, n, n, bh, be, l, hh)) continue;
+                // absolute parameters of the column's ends (row windows only)
+                const float r1 = __fdividef(1.0f, __fadd_rn(bh, l) + ve.ac);
+                const float r2 = __fdividef(1.0f, __fadd_rn(bh, hh) + ve.ac);
+                const float s1 = dz * r1 * inv_dv, s2 = dz * r2 * inv_dv;
+                const float e1 = (zr0 * r1 - G.v0) * inv_dv, e2 = (zr0 * r2 - G.v0) * inv_dv;
+                const TW* yt = yv + 8 * ia;
+                if (mode < 0)
+                    adj_rows_hex<-1, TZ, TW>(P, Q, nk, z0, l, hh, e1, e2, s1, s2, rv, bh, be, yt,
+                                             yt + half, na, nbw);
+                else
+                    adj_rows_hex<0, TZ, TW>(P, Q, nk, z0, l, hh, e1, e2, s1, s2, rv, bh, be, yt,
+                                            yt + half, na, nbw);
+            }
+            // next column R (px, py); P rotates back one place, Q forward one
+            const int t = px;
+            px = n - 1 - py; py = t;
+#pragma unroll
+            for (int z = 0; z < TZ; z++) {
+                const float2 a = P[0][z];
+                P[0][z] = P[1][z]; P[1][z] = P[2][z]; P[2][z] = P[3][z]; P[3][z] = a;
+                const float2 b = Q[3][z];
+                Q[3][z] = Q[2][z]; Q[2][z] = Q[1][z]; Q[1][z] = Q[0][z]; Q[0][z] = b;
+            }
+        }
+        if (!diag) {                                           // C sums back into P
+#pragma unroll
+            for (int j = 0; j < 4; j++)
+#pragma unroll
+                for (int z = 0; z < TZ; z++) {
+                    const float2 t = P[j][z];
+                    P[j][z] = Q[j][z]; Q[j][z] = t;
+                }
+        }
+    }
+    // C_j = R^j V0 holds P[j] (and, on the diagonal, Q[j + 1], the sums of
+    // D_{j+1} = C_j); D_j = R^j M V0 holds Q[j]
+    const long long nn = (long long)n * n;
+    const int cx[4] = {ix, n - 1 - iy, n - 1 - ix, iy};
+    const int cy[4] = {iy, ix, n - 1 - iy, n - 1 - ix};
+    const int dxs[4] = {ix, iy, n - 1 - ix, n - 1 - iy};
+    const int dys[4] = {n - 1 - iy, ix, iy, n - 1 - ix};
+#pragma unroll
+    for (int k = 0; k < TZ; k++)
+        if (k < nk) {
+            const long long zl = (long long)(z0 + k) * nn, zh = (long long)(nz - 1 - z0 - k) * nn;
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                if (diag && j >= 4) break;
+                float2 a;
+                int qx, qy;
+                if (j < 4) {
+                    a = P[j][k];
+                    if (diag) {
+                        const float2 b = Q[(j + 1) & 3][k];
+                        a.x += b.x; a.y += b.y;
+                    }
+                    qx = cx[j]; qy = cy[j];
+                } else {
+                    a = Q[j - 4][k]; qx = dxs[j - 4]; qy = dys[j - 4];
+                }
+                if (xfold) {                  // the tiled folded volume
+                    const long long t = tiled_pair(qx, qy, (int)zl, n >> 2);
+                    Store<TX>::st2(X + 2 * t, a.x, a.y);
+                } else {
+                    const long long c = (long long)qy * n + qx;
+                    Store<TX>::st(X + zl + c, a.x);
+                    Store<TX>::st(X + zh + c, a.y);
+                }
+            }
+        }
+}
+
 // MIRROR: yw is the folded sinogram; the runs cover the lower half z < nz/2
 // only (the walked rows' rays never reach the upper half) and each thread also
 // produces the mirrored run, into the folded volume when xfold is set.
@@ -961,7 +1245,12 @@ void launch_fwd(fl_plan* p, const void* x, void* y, int cr_power, const int* ski
 {
     const fl_scan& s = p->s;
     const dim3 fb = p->fwd_bx ? dim3(p->fwd_bx, p->fwd_by) : dim3(8, 16);
-    if (s.ndim == 3 && p->zmirror && p->rot && p->rot4) {
+    if (s.ndim == 3 && fl_plan_turns(p) == 8) {
+        dim3 grid(fl_div_up(s.na, fb.x), s.nv / 8, fl_div_up(s.nb / 2, fb.y));
+        k_fwd_hex<TX, TY><<<grid, fb, 0, st>>>(
+            (const TX*)x, (TY*)y, p->d_col, p->d_colr, p->d_row, s.nx, s.nz, s.na, s.nb, s.nv,
+            p->n_vox_frame, s.scale, cr_power, skip, xscale, yfold);
+    } else if (s.ndim == 3 && p->zmirror && p->rot && p->rot4) {
         dim3 grid(fl_div_up(s.na, fb.x), s.nv / 4, fl_div_up(s.nb / 2, fb.y));
         k_fwd_oct<TX, TY><<<grid, fb, 0, st>>>(
             (const TX*)x, (TY*)y, p->d_col, p->d_colr, p->d_row, s.nx, s.nz, s.na, s.nb, s.nv,
@@ -1023,7 +1312,22 @@ void launch_adj_cone(fl_plan* p, const TW* yw, void* x, const int* skip, int xfo
         constexpr int TZ = 8;
         const int nzw = p->zmirror ? s.nz / 2 : s.nz;
         int zruns = (nzw + TZ - 1) / TZ;
-        if (p->zmirror && p->rot && p->rot4) {
+        if (fl_plan_turns(p) == 8) {
+            // runs of 2 voxels (the eight columns' 32 accumulators, 6 blocks per
+            // SM) or of 1 (16 accumulators, 8 blocks per SM): fl_plan_autotune
+            const int run = p->adj_run == 1 ? 1 : 2;
+            zruns = (nzw + run - 1) / run;
+            const dim3 ab = p->adj_bx ? dim3(p->adj_bx, p->adj_by) : dim3(8, 16);
+            dim3 grid(fl_div_up(s.nx / 2, ab.x), fl_div_up(s.ny / 2, ab.y), (unsigned)zruns);
+            if (run == 1)
+                k_adj_hex<TX, 1, TW><<<grid, ab, 0, st>>>(
+                    (TX*)x, yw, p->d_col, p->d_rowz, p->d_view, G, s.nx, s.nz, s.na, s.nb, s.nv,
+                    s.dz, skip, xfold);
+            else
+                k_adj_hex<TX, 2, TW><<<grid, ab, 0, st>>>(
+                    (TX*)x, yw, p->d_col, p->d_rowz, p->d_view, G, s.nx, s.nz, s.na, s.nb, s.nv,
+                    s.dz, skip, xfold);
+        } else if (p->zmirror && p->rot && p->rot4) {
             // runs of 2: the four columns' 16 accumulators keep 8 blocks per SM
             constexpr int TO = 2;
             zruns = (nzw + TO - 1) / TO;
@@ -1193,6 +1497,23 @@ int fl_matched_weight(fl_plan* p, const void* y, int yt, float* yw, cudaStream_t
     const fl_scan& s = p->s;
     long long nr = p->n_rays;
     int three = s.ndim == 3;
+    if (three && fl_plan_turns(p) == 8) {
+        const long long npk = (long long)(s.nv / 8) * (s.nb / 2) * s.na;
+        const unsigned g = fl_div_up(npk, 256);
+        if (yt == FL_F32)
+            k_weight_packed_hex<float><<<g, 256, 0, st>>>(yw, (const float*)y, p->d_colr,
+                                                          p->d_row, s.na, s.nb, s.nv, npk,
+                                                          s.scale);
+        else if (yt == FL_F16)
+            k_weight_packed_hex<__half><<<g, 256, 0, st>>>(yw, (const __half*)y, p->d_colr,
+                                                           p->d_row, s.na, s.nb, s.nv, npk,
+                                                           s.scale);
+        else
+            k_weight_packed_hex<__nv_bfloat16><<<g, 256, 0, st>>>(
+                yw, (const __nv_bfloat16*)y, p->d_colr, p->d_row, s.na, s.nb, s.nv, npk,
+                s.scale);
+        return fl_check_launch("matched adjoint weighting");
+    }
     if (three && p->zmirror && p->rot) {
         if (p->rot4) launch_weight_packed<4>(p, y, yt, yw, st);
         else launch_weight_packed<2>(p, y, yt, yw, st);
@@ -1260,8 +1581,10 @@ int fl_matched_adjoint_wt(fl_plan* p, const void* yw, int wt, void* x, int xt, c
 // Launch-shape autotuner of the cone projector kernels: each 128-thread shape
 // below is timed (CUDA events, one launch after one untimed) on the plan's own
 // geometry, with the plan's scratch as input and output, and the fastest kept
-// for the forward and for the backprojection. A thread's result does not
-// depend on the shape, so neither do the projections. Fan plans keep theirs.
+// for the forward and for the backprojection (for the reflection
+// backprojection, with runs of 1 or 2 voxels per thread). A thread's result
+// does not depend on the shape or the run, so neither do the projections. Fan
+// plans keep theirs.
 extern "C" int fl_plan_autotune(fl_plan* p, void* stream, int32_t* shapes)
 {
     FL_RANGE("fl_plan_autotune");
@@ -1297,24 +1620,27 @@ extern "C" int fl_plan_autotune(fl_plan* p, void* stream, int32_t* shapes)
                 return fl_set_error(FL_ERR_CUDA, "fl_plan_autotune: timing failed");
             return FL_OK;
         };
+        // the reflection backprojection also tries both voxel runs per thread
+        const int nruns = fl_plan_turns(p) == 8 ? 2 : 1;
         for (int pass = 0; pass < 2 && !st; pass++) {
             const bool fwd = pass == 0;
             float best = 3.0e38f;
-            int bi = 0;
-            for (int c = 0; c < 4 && !st; c++) {
-                if (fwd) { p->fwd_bx = cand[c][0]; p->fwd_by = cand[c][1]; }
-                else     { p->adj_bx = cand[c][0]; p->adj_by = cand[c][1]; }
-                float ms = 0.0f;
-                st = timed(fwd, ms);
-                if (!st && ms < best) { best = ms; bi = c; }
-            }
+            int bi = 0, br = 0;
+            for (int c = 0; c < 4 && !st; c++)
+                for (int r = 0; r < (fwd ? 1 : nruns) && !st; r++) {
+                    if (fwd) { p->fwd_bx = cand[c][0]; p->fwd_by = cand[c][1]; }
+                    else { p->adj_bx = cand[c][0]; p->adj_by = cand[c][1]; p->adj_run = 2 - r; }
+                    float ms = 0.0f;
+                    st = timed(fwd, ms);
+                    if (!st && ms < best) { best = ms; bi = c; br = r; }
+                }
             if (fwd) { p->fwd_bx = cand[bi][0]; p->fwd_by = cand[bi][1]; }
-            else     { p->adj_bx = cand[bi][0]; p->adj_by = cand[bi][1]; }
+            else { p->adj_bx = cand[bi][0]; p->adj_by = cand[bi][1]; p->adj_run = 2 - br; }
         }
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         if (st) {                         // keep the built-in shapes after a failure
-            p->fwd_bx = p->fwd_by = p->adj_bx = p->adj_by = 0;
+            p->fwd_bx = p->fwd_by = p->adj_bx = p->adj_by = p->adj_run = 0;
             return st;
         }
     }

@@ -411,6 +411,75 @@ __device__ __forceinline__ void walk_oct(const TX* __restrict__ x, const ColEntr
     for (int j = 0; j < 4; j++) acc[j] = b.acc[j];
 }
 
+// The z-mirror walk with the quarter turns and the reflection (plan flag
+// rot8): per step the folded pairs of the voxel's eight images under the
+// square's symmetries, g_k = R^k (k < 4) and R^(k-4) M (k >= 4), M (x, y) =
+// (x, n-1-y), R (x, y) = (n-1-y, x); R M (x, y) = (y, x). acc[k] gets the
+// (voxel, mirror) sums of image k, the sums of the ray g_k takes the walked
+// ray to.
+template <typename TX>
+struct HexBody {
+    const TX* __restrict__ x;
+    long long xlen;
+    int n, nn, n4;
+    float2 acc[8], xv[8];
+    __device__ __forceinline__ void load(int jx, int jy, int jz, float2 (&o)[8]) const
+    {
+        const int zb = jz * nn, pi2 = 2 * zb + nn - 1;   // q -> pi2 - q: the turn by pi
+        int q[8];
+        q[0] = tiled_pair(jx, jy, zb, n4);
+        q[1] = tiled_pair(n - 1 - jy, jx, zb, n4);
+        q[4] = tiled_pair(jx, n - 1 - jy, zb, n4);
+        q[5] = tiled_pair(jy, jx, zb, n4);
+        q[2] = pi2 - q[0];
+        q[3] = pi2 - q[1];
+        q[6] = pi2 - q[4];
+        q[7] = pi2 - q[5];
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            o[j] = make_float2(0.0f, 0.0f);
+            if (FL_IN(2 * (long long)q[j] + 1, xlen)) o[j] = Store<TX>::ld2(x + 2 * (long long)q[j]);
+        }
+    }
+    __device__ __forceinline__ void at(int jx, int jy, int jz) { load(jx, jy, jz, xv); }
+    __device__ __forceinline__ void take(float seg, bool more, int jx, int jy, int jz)
+    {
+        float2 xn[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) xn[j] = make_float2(0.0f, 0.0f);
+        if (more) load(jx, jy, jz, xn);
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            acc[j] = __ffma2_rn(make_float2(seg, seg), xv[j], acc[j]);
+            xv[j] = xn[j];
+        }
+    }
+};
+
+template <typename TX>
+__device__ __forceinline__ void walk_hex(const TX* __restrict__ x, const ColEntry* ce,
+                                         const AxisEntry* pZ, int n, int nz, float2 (&acc)[8],
+                                         long long xlen)
+{
+    HexBody<TX> b;
+    b.x = x; b.xlen = xlen; b.n = n; b.nn = n * n; b.n4 = n >> 2;
+#pragma unroll
+    for (int j = 0; j < 8; j++) { b.acc[j] = make_float2(0.0f, 0.0f); b.xv[j] = b.acc[j]; }
+    if (__ldg(&pZ->ih) < 0.0f) seg_walk<true>(ce, pZ, n, n, nz / 2, b);
+#pragma unroll
+    for (int j = 0; j < 8; j++) acc[j] = b.acc[j];
+}
+
+// Walked view, table row and column of slot (s, ia) of a reflection plan
+// (fl_plan.h): slot s in [1, nv/8) is view s at column ia; slot 0 holds view
+// 0 at columns ia < na/2 and view nv/8 (its tables in row nv, the exact
+// diagonal angle) at columns ia - na/2.
+__device__ __forceinline__ void hex_slot(int s, int ia, int na, int nv, int& v, int& vt, int& a)
+{
+    v = s; vt = s; a = ia;
+    if (s == 0 && ia >= na / 2) { v = nv / 8; vt = nv; a = ia - na / 2; }
+}
+
 // The fan walk in batches of kFanBatch steps: the crossings of a batch are
 // found first (they do not depend on the image), then its gathers are issued
 // together and the segments added in walk order -- the same sums as the

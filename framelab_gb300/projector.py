@@ -137,6 +137,29 @@ class Plan:
         _lib.check(self._L.fl_plan_option(self._h, _lib.OPT_QUARTER_TURN, int(bool(on))))
 
     @property
+    def reflect(self) -> bool:
+        """Whether the matched pair also uses the reflection between views v
+        and nv - v about the x axis (FL_OPT_REFLECT; cone plans, needs the
+        quarter turn and a detector symmetric about its centre)."""
+        v = C.c_int()
+        _lib.check(self._L.fl_plan_query(self._h, _lib.OPT_REFLECT, C.byref(v)))
+        return bool(v.value)
+
+    @reflect.setter
+    def reflect(self, on: bool):
+        _lib.check(self._L.fl_plan_option(self._h, _lib.OPT_REFLECT, int(bool(on))))
+
+    @property
+    def views_per_walk(self) -> int:
+        """Views one walk or weight of the matched kernels in use serves: 8
+        (quarter turns and the reflection), 4, 2 or 1."""
+        if self.reflect:
+            return 8
+        if self.quarter_turn:
+            return 4
+        return 2 if self.rot_mirror else 1
+
+    @property
     def handle(self):
         return self._h
 
@@ -192,13 +215,19 @@ class Plan:
     def autotune(self, stream=None) -> dict:
         """Times the block shapes of this cone plan's matched projector kernels
         on its own geometry and keeps the fastest (``fl_plan_autotune``; the
-        projections do not change). Returns the chosen shapes; fan plans
+        projections do not change). Returns the chosen shapes (and, on a
+        reflection plan, the backprojection's voxels per thread); fan plans
         report ``None`` and keep theirs."""
         sh = (C.c_int32 * 4)()
         _lib.check(self._L.fl_plan_autotune(self._h, _stream(stream), sh))
         if not sh[0]:
             return {"forward": None, "adjoint": None}
-        return {"forward": (sh[0], sh[1]), "adjoint": (sh[2], sh[3])}
+        out = {"forward": (sh[0], sh[1]), "adjoint": (sh[2], sh[3])}
+        if self.reflect:
+            v = C.c_int()
+            _lib.check(self._L.fl_plan_query(self._h, _lib.QUERY_ADJ_RUN, C.byref(v)))
+            out["adjoint_voxels_per_thread"] = v.value
+        return out
 
     def count_intersections(self, stream=None) -> torch.Tensor:
         c = torch.empty(self.sino_shape, device="cuda", dtype=torch.int32)

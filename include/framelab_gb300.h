@@ -208,17 +208,31 @@ int fl_plan_sizes(const fl_plan *plan, int64_t *n_vox, int64_t *n_rays);
  *   odd detector at a view angle of exactly 0) has no unique discretisation:
  *   on the turn forms its turned copies take the walked view's choice, which
  *   can differ from the general kernels' at O(1) for that ray alone. */
-enum { FL_OPT_Z_MIRROR = 1, FL_OPT_ROT_MIRROR = 2, FL_OPT_QUARTER_TURN = 3 };
+/* FL_OPT_REFLECT: on top of FL_OPT_QUARTER_TURN (cone plans), on by default
+ *   when nv is a multiple of 8, view nv - v is the mirror image of view v
+ *   about the x axis (to within 1e-6) and the detector is symmetric about its
+ *   centre (y_det[na-1-a] == -y_det[a], na even). Ray (j nv/4 - v, na-1-a, b)
+ *   is then defined as ray (v, a, b) reflected by M (x, y, z) = (x, n-1-y, z)
+ *   and turned by j pi/2, for the walked views v = 0 .. nv/8 (views 0 and
+ *   nv/8 walk their columns a < na/2, the other half being their mirror
+ *   images; view nv/8 is walked at the exact angle pi/4): one walk or weight
+ *   serves sixteen rays. Queries report 0 while any option below it is off. */
+enum { FL_OPT_Z_MIRROR = 1, FL_OPT_ROT_MIRROR = 2, FL_OPT_QUARTER_TURN = 3,
+       FL_OPT_REFLECT = 4 };
 int fl_plan_option(fl_plan *plan, int option, int value);
 int fl_plan_query(const fl_plan *plan, int option, int *value);
 /* Launch-shape autotuner for a cone plan's matched projector kernels: times
  * each 128-thread block shape (8x16, 16x8, 32x4, 4x32) on the plan's own
  * geometry, one launch each on `stream` after one untimed, and keeps the
  * fastest for the forward and for the backprojection. The results of the
- * projectors do not depend on the shape. Synchronises `stream`; uses the
+ * projectors do not depend on the shape (nor on the voxel run of the
+ * reflection backprojection, which it tunes too). Synchronises `stream`; uses the
  * plan's scratch buffers. shapes (optional, [4]): the chosen forward x, y and
  * backprojection x, y (0 for fan plans, which keep their shapes). */
 int fl_plan_autotune(fl_plan *plan, void *stream, int32_t *shapes);
+/* fl_plan_query(plan, FL_QUERY_ADJ_RUN, &v): voxels per thread of the
+ * reflection backprojection (1 or 2; fl_plan_autotune times both). */
+enum { FL_QUERY_ADJ_RUN = 16 };
 
 /* y = A x on `stream`. x: n_vox elements, y: n_rays elements, device memory. */
 int fl_forward(fl_plan *plan, int model, const void *x, int x_dtype, void *y, int y_dtype,

@@ -23,7 +23,8 @@ phantom (the sinogram a reconstruction sees) and N(0, 1) noise (every matrix
 entry's error shows, none averages out).
 
 A plan that uses the half or quarter turn (G = 2 or 4 views per walk) defines
-view v + j nv/G as view v turned by exactly j 2 pi / G. FP32 source angles
+view v + j nv/G as view v turned by exactly j 2 pi / G (with the reflection,
+G = 8, also view j nv/4 - v as view v reflected about the x axis and turned). FP32 source angles
 single(2 pi k / nv) are not exact turns of each other (up to 2.4e-7 rad
 apart), so such a plan projects a scan whose angles are snapped to exact
 turns. ``snapped(para, G)`` is that scan for the FP64 model (FP64 angles
@@ -57,12 +58,25 @@ def _three(gpu, ref, exact, exact_snapped=None) -> dict:
 def snapped(para, turns: int) -> dict:
     """The scan a plan with `turns` views per walk projects: FP64 angles
     phi[v + j nv/turns] = phi[v] + j 2 pi / turns for v < nv/turns (the FP32
-    angles of the walked views, turned exactly)."""
+    angles of the walked views, turned exactly). turns = 8 is the quarter
+    turns with the reflection about the x axis: the walked views v = 0 ..
+    nv/8 (view nv/8 at exactly pi/4) turned by j pi/2 and reflected, view
+    j nv/4 - v at angle j pi/2 - phi[v]."""
     if turns <= 1:
         return para
     phi = np.asarray(para["sd_phi"], np.float32).astype(np.float64)
-    q = phi.size // turns
-    p64 = np.concatenate([phi[:q] + j * (2.0 * np.pi / turns) for j in range(turns)])
+    if turns == 8:
+        nv = phi.size
+        q, o = nv // 4, nv // 8
+        base = np.concatenate([phi[:o], [np.pi / 4]])          # walked views 0 .. nv/8
+        u = np.arange(nv)
+        j, v = u // q, u % q
+        refl = v > o
+        vv = np.where(refl, q - v, v)
+        p64 = np.where(refl, (j + 1) * (np.pi / 2) - base[vv], base[vv] + j * (np.pi / 2))
+    else:
+        q = phi.size // turns
+        p64 = np.concatenate([phi[:q] + j * (2.0 * np.pi / turns) for j in range(turns)])
     out = dict(para)
     out["phi64"] = p64
     return out

@@ -10,8 +10,8 @@ oracle evaluating each sampled entry exactly as its full function would.
 For every operator three relative L2 errors are measured (oracle/parity.py):
 the GPU result against the FP64 exact model, the reference's own FP32 CPU
 kernel against the FP64 model, and the GPU result against the reference.
-Each configuration runs twice. With the half and quarter turns off (the
-general and z-mirror kernels) the matched pair must be within 1e-5 of the
+Each configuration runs twice. With the half and quarter turns (and the
+reflection) off (the general and z-mirror kernels) the matched pair must be within 1e-5 of the
 FP64 model everywhere, for the backprojection of the phantom's sinogram and
 of N(0, 1) noise alike. With the turns on (the default) it projects the scan
 whose turned views are exact turns of the walked ones (oracle/parity.py,
@@ -48,7 +48,7 @@ def _ops(P):
 
 
 def _turns(P):
-    return 4 if P.quarter_turn else (2 if P.rot_mirror else 1)
+    return P.views_per_walk
 
 
 def _check(res, turns):
@@ -110,4 +110,4 @@ def test_cone_config_sizes_on_subsets(n):
         del P
         torch.cuda.empty_cache()
         _check(res, t)
-    assert forms == [4, 1]
+    assert forms == [8, 1]

@@ -617,6 +617,65 @@ def test_quarter_turn_is_detected_and_exact():
     assert _rel(_host(u8), _host(u4)) < 1e-3
 
 
+def test_reflection_is_detected_and_exact():
+    torch = _torch()
+    from framelab_gb300.solvers import NativeCGLS
+    import oracle.parity as PAR
+    p = _cone_small("circle")                          # 32^3, 16 views, 48 x 40 panel
+    n, nb, nv, na = int(p["nx"]), len(p["z_det"]), len(p["sd_phi"]), len(p["y_det"])
+    P = _plan(p)
+    assert P.reflect and P.views_per_walk == 8
+    P.quarter_turn = False                             # rides on the quarter turn
+    assert not P.reflect and P.views_per_walk == 2
+    P.quarter_turn = True
+    assert P.reflect
+    twelve = G.cone_para_mm(32, 12, 48, 40, det_pitch_mm=8.0, SO_mm=600.0, SD_mm=1200.0,
+                            voxel_mm=8.0)              # quarter turns, nv/8 not whole
+    Q = _plan(twelve)
+    assert Q.quarter_turn and not Q.reflect
+    off = G.cone_para(32, 32, 32, 48, 40, 16, L=(2, 2, 2), y_os=0.01)   # off-centre panel
+    R = _plan(off)
+    assert R.quarter_turn and not R.reflect
+    x = PH.ellipsoids_3d(n, seed=12).reshape(-1)
+    rng = np.random.default_rng(8)
+    r = rng.standard_normal(P.n_rays).astype(np.float32)
+    y16, x16 = _host(P.forward(_dev(x))), _host(P.adjoint(_dev(r)))
+    P.reflect = False
+    y8, x8 = _host(P.forward(_dev(x))), _host(P.adjoint(_dev(r)))
+    P.reflect = True
+    assert _rel(y16, y8) < 1e-5 and _rel(x16, x8) < 1e-4, (_rel(y16, y8), _rel(x16, x8))
+    # by construction: view nv - v (mod nv), column na-1-a of A x is view v,
+    # column a of A M(x), with M(x)[z, y, x] = x[z, n-1-y, x]
+    xm = x.reshape(n, n, n)[:, ::-1, :].reshape(-1).copy()
+    ym = _host(P.forward(_dev(xm))).reshape(nv, nb, na)
+    idx = (nv - np.arange(nv)) % nv
+    assert np.array_equal(y16.reshape(nv, nb, na)[idx][:, :, ::-1], ym)
+    # and the quarter turns still hold bit for bit
+    xr = x.reshape(n, n, n)[:, :, ::-1].transpose(0, 2, 1).reshape(-1).copy()
+    yr = _host(P.forward(_dev(xr))).reshape(nv, nb, -1)
+    assert np.array_equal(y16.reshape(nv, nb, -1)[nv // 4:], yr[:3 * nv // 4])
+    # the adjoint stays the exact transpose
+    lhs = np.dot(y16.astype(np.float64), r.astype(np.float64))
+    rhs = np.dot(x.astype(np.float64), x16.astype(np.float64))
+    assert abs(lhs - rhs) / abs(lhs) < 1e-5
+    # the scan it projects (views snapped to the square's symmetries) to FP64
+    ps = PAR.snapped(p, 8)
+    assert _rel(y16, O.exact_forward(x, ps)) < 2e-6
+    assert _rel(x16, O.exact_adjoint(r, ps)) < 5e-6
+    # half-precision storage; the stand-alone backprojection of FP16 input
+    assert _rel(_host(P.forward(_dev(x, torch.float16))), y16) < 2e-3
+    assert _rel(_host(P.adjoint(_dev(r, torch.float16))), x16) < 2e-3
+    # the fused CGLS forms follow the option (their graphs are captured again)
+    b = P.adjoint(P.forward(_dev(x))).reshape(-1).contiguous()
+    for mode, tol in (("graph", 1e-4), ("mixed", 1e-3)):
+        cg = NativeCGLS(P, mode)
+        u16 = cg.solve(b, iters=6).clone()
+        P.reflect = False
+        u8 = cg.solve(b, iters=6)
+        P.reflect = True
+        assert _rel(_host(u16), _host(u8)) < tol, (mode, _rel(_host(u16), _host(u8)))
+
+
 def _fan_turn_para(n=48, ny=None, nv=40, phi=None, nd=96):
     return G.fan_para(n, ny or n, nd, nv, L=(1.0, (ny or n) / n), SO=3.0, OD=3.0, Ly=3.0,
                       sd_phi=phi)
