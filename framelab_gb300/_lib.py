@@ -22,7 +22,8 @@ OPT_Z_MIRROR = 1
 OPT_ROT_MIRROR = 2
 OPT_QUARTER_TURN = 3
 OPT_REFLECT = 4
-QUERY_ADJ_RUN = 16
+TUNE_ADJ_RUN = 16
+TUNE_ADJ_ROWS = 17
 FRAMELET_OPT_FUSED = 1
 
 

@@ -114,8 +114,9 @@ struct fl_plan {
     // kernels; 0 keeps each kernel's built-in shape (set by fl_plan_autotune;
     // every thread's result is independent of the shape)
     int fwd_bx, fwd_by, adj_bx, adj_by;
-    // voxels per thread of the reflection backprojection (1 or 2; 0 = 2)
-    int adj_run;
+    // voxels per thread of the reflection backprojection (1 or 2; 0 = 2) and
+    // detector rows per iteration of its row loop (1 or 2; 0 = 1)
+    int adj_run, adj_rows;
     // scale of an FP16 backprojection input (the mixed CGLS form): the largest
     // power of two with y16_scale * c_r^2 <= 1 for every ray, so c_r^2 * (a
     // ray's sum of w p) stays within FP16's range whenever |p| does

@@ -327,6 +327,12 @@ extern "C" int fl_plan_option(fl_plan* p, int option, int value)
         p->rot8 = (value && p->rot8_ok) ? 1 : 0;
         return fl_set_error(FL_OK, "");
     }
+    if (option == FL_TUNE_ADJ_RUN || option == FL_TUNE_ADJ_ROWS) {
+        if (value != 1 && value != 2)
+            return fl_set_error(FL_ERR_INVALID, "fl_plan_option: %d is not 1 or 2", value);
+        (option == FL_TUNE_ADJ_RUN ? p->adj_run : p->adj_rows) = value;
+        return fl_set_error(FL_OK, "");
+    }
     return fl_set_error(FL_ERR_INVALID, "fl_plan_option: unknown option %d", option);
 }
 
@@ -349,8 +355,12 @@ extern "C" int fl_plan_query(const fl_plan* p, int option, int* value)
         *value = fl_plan_turns(p) == 8 ? 1 : 0;
         return fl_set_error(FL_OK, "");
     }
-    if (option == FL_QUERY_ADJ_RUN) {
+    if (option == FL_TUNE_ADJ_RUN) {
         *value = p->adj_run == 1 ? 1 : 2;
+        return fl_set_error(FL_OK, "");
+    }
+    if (option == FL_TUNE_ADJ_ROWS) {
+        *value = p->adj_rows == 2 ? 2 : 1;
         return fl_set_error(FL_OK, "");
     }
     return fl_set_error(FL_ERR_INVALID, "fl_plan_query: unknown option %d", option);

@@ -948,8 +948,10 @@ k_adj_oct(TX* __restrict__ X, const TW* __restrict__ yw, const ColEntry* __restr
 // the walked ray's eight images into the sums P[j] (turn images) and Q[j]
 // (reflected images); yt / yr hold them side by side (8 values per row and
 // column in each plane, 32-byte aligned), so each is one vector load whose
-// lanes read neighbouring columns' orbits.
-template <int MODE, int TZ, typename TW>
+// lanes read neighbouring columns' orbits. RU rows per iteration: RU = 2
+// issues the loads of two rows before either's arithmetic (more loads in
+// flight per thread); the rows are still added in order.
+template <int MODE, int TZ, int RU, typename TW>
 __device__ __forceinline__ void adj_rows_hex(float2 (&P)[4][TZ], float2 (&Q)[4][TZ], int nk,
                                              int z0, float l, float h, float e1, float e2,
                                              float s1, float s2,
@@ -975,22 +977,33 @@ __device__ __forceinline__ void adj_rows_hex(float2 (&P)[4][TZ], float2 (&Q)[4][
             mn = mn1; mx = mx1;
         }
         const float fk0 = (float)(z0 + k), fk1 = (float)(z0 + k + 1);
-        for (int ib = blo; ib <= bhi; ib++) {
-            if (!FL_IN(ib, nb)) continue;
-            const AxisEntry re = rv[ib];
-            float o[16];
-            ld_in<TW, 8>(yt + 8 * (long long)ib * na, *reinterpret_cast<float(*)[8]>(o));
-            ld_in<TW, 8>(yr + 8 * (long long)ib * na, *reinterpret_cast<float(*)[8]>(o + 8));
-            const float2 az = row_planes(re, fk0, fk1, bh, be);
-            float l2, h2;
-            if (MODE < 0) { l2 = fmaxf(l, az.y); h2 = fminf(h, az.x); }
-            else { l2 = fmaxf(l, fminf(az.x, az.y)); h2 = fminf(h, fmaxf(az.x, az.y)); }
-            const float w = fmaxf(h2 - l2, 0.0f);
-            const float2 w2 = make_float2(w, w);
+        for (int ib = blo; ib <= bhi; ib += RU) {
+            AxisEntry re[RU];
+            float o[RU][16];
+            bool on[RU];
 #pragma unroll
-            for (int j = 0; j < 4; j++) {
-                P[j][k] = __ffma2_rn(w2, make_float2(o[2 * j], o[2 * j + 1]), P[j][k]);
-                Q[j][k] = __ffma2_rn(w2, make_float2(o[8 + 2 * j], o[9 + 2 * j]), Q[j][k]);
+            for (int u = 0; u < RU; u++) {
+                on[u] = ib + u <= bhi && FL_IN(ib + u, nb);
+                const long long r = on[u] ? ib + u : min(max(ib, 0), nb - 1);   // one that exists
+                re[u] = rv[r];
+                ld_in<TW, 8>(yt + 8 * r * na, *reinterpret_cast<float(*)[8]>(o[u]));
+                ld_in<TW, 8>(yr + 8 * r * na, *reinterpret_cast<float(*)[8]>(o[u] + 8));
+            }
+#pragma unroll
+            for (int u = 0; u < RU; u++) {
+                const float2 az = row_planes(re[u], fk0, fk1, bh, be);
+                float l2, h2;
+                if (MODE < 0) { l2 = fmaxf(l, az.y); h2 = fminf(h, az.x); }
+                else { l2 = fmaxf(l, fminf(az.x, az.y)); h2 = fminf(h, fmaxf(az.x, az.y)); }
+                if (!on[u]) continue;
+                const float w = fmaxf(h2 - l2, 0.0f);
+                const float2 w2 = make_float2(w, w);
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    P[j][k] = __ffma2_rn(w2, make_float2(o[u][2 * j], o[u][2 * j + 1]), P[j][k]);
+                    Q[j][k] = __ffma2_rn(w2, make_float2(o[u][8 + 2 * j], o[u][9 + 2 * j]),
+                                         Q[j][k]);
+                }
             }
         }
     }
@@ -1008,8 +1021,8 @@ __device__ __forceinline__ void adj_rows_hex(float2 (&P)[4][TZ], float2 (&Q)[4][
 // One weight thus feeds sixteen (voxel, ray) pairs. yw is the packed input
 // of k_weight_packed_hex / k_fwd_hex (two planes); X the tiled folded volume
 // (xfold) or the standard one.
-template <typename TX, int TZ, typename TW>
-__global__ void __launch_bounds__(128, TZ == 1 ? 8 : 6)
+template <typename TX, int TZ, int RU, typename TW>
+__global__ void __launch_bounds__(128, TZ == 1 ? (RU == 1 ? 8 : 6) : (RU == 1 ? 6 : 5))
 k_adj_hex(TX* __restrict__ X, const TW* __restrict__ yw, const ColEntry* __restrict__ col,
           const AxisEntry* __restrict__ rowz, const ViewEntry* __restrict__ view, DetGrid G, int n,
           int nz, int na, int nb, int nv, float dz, const int* __restrict__ skip, int xfold)
@@ -1075,11 +1088,11 @@ k_adj_hex(TX* __restrict__ X, const TW* __restrict__ yw, const ColEntry* __restr
                 const float e1 = (zr0 * r1 - G.v0) * inv_dv, e2 = (zr0 * r2 - G.v0) * inv_dv;
                 const TW* yt = yv + 8 * ia;
                 if (mode < 0)
-                    adj_rows_hex<-1, TZ, TW>(P, Q, nk, z0, l, hh, e1, e2, s1, s2, rv, bh, be, yt,
-                                             yt + half, na, nbw);
+                    adj_rows_hex<-1, TZ, RU, TW>(P, Q, nk, z0, l, hh, e1, e2, s1, s2, rv, bh, be,
+                                                 yt, yt + half, na, nbw);
                 else
-                    adj_rows_hex<0, TZ, TW>(P, Q, nk, z0, l, hh, e1, e2, s1, s2, rv, bh, be, yt,
-                                            yt + half, na, nbw);
+                    adj_rows_hex<0, TZ, RU, TW>(P, Q, nk, z0, l, hh, e1, e2, s1, s2, rv, bh, be,
+                                                yt, yt + half, na, nbw);
             }
             // next column R (px, py); P rotates back one place, Q forward one
             const int t = px;
@@ -1313,20 +1326,21 @@ void launch_adj_cone(fl_plan* p, const TW* yw, void* x, const int* skip, int xfo
         const int nzw = p->zmirror ? s.nz / 2 : s.nz;
         int zruns = (nzw + TZ - 1) / TZ;
         if (fl_plan_turns(p) == 8) {
-            // runs of 2 voxels (the eight columns' 32 accumulators, 6 blocks per
-            // SM) or of 1 (16 accumulators, 8 blocks per SM): fl_plan_autotune
-            const int run = p->adj_run == 1 ? 1 : 2;
+            // runs of 2 voxels (the eight columns' 32 accumulators) or of 1 (16
+            // accumulators), one or two rows per iteration: fl_plan_autotune
+            const int run = p->adj_run == 1 ? 1 : 2, ru = p->adj_rows == 2 ? 2 : 1;
             zruns = (nzw + run - 1) / run;
             const dim3 ab = p->adj_bx ? dim3(p->adj_bx, p->adj_by) : dim3(8, 16);
             dim3 grid(fl_div_up(s.nx / 2, ab.x), fl_div_up(s.ny / 2, ab.y), (unsigned)zruns);
-            if (run == 1)
-                k_adj_hex<TX, 1, TW><<<grid, ab, 0, st>>>(
-                    (TX*)x, yw, p->d_col, p->d_rowz, p->d_view, G, s.nx, s.nz, s.na, s.nb, s.nv,
-                    s.dz, skip, xfold);
-            else
-                k_adj_hex<TX, 2, TW><<<grid, ab, 0, st>>>(
-                    (TX*)x, yw, p->d_col, p->d_rowz, p->d_view, G, s.nx, s.nz, s.na, s.nb, s.nv,
-                    s.dz, skip, xfold);
+#define FL_ADJ_HEX(TZ_, RU_)                                                                  \
+    k_adj_hex<TX, TZ_, RU_, TW><<<grid, ab, 0, st>>>((TX*)x, yw, p->d_col, p->d_rowz, p->d_view, \
+                                                     G, s.nx, s.nz, s.na, s.nb, s.nv, s.dz,     \
+                                                     skip, xfold)
+            if (run == 1 && ru == 1) FL_ADJ_HEX(1, 1);
+            else if (run == 1) FL_ADJ_HEX(1, 2);
+            else if (ru == 1) FL_ADJ_HEX(2, 1);
+            else FL_ADJ_HEX(2, 2);
+#undef FL_ADJ_HEX
         } else if (p->zmirror && p->rot && p->rot4) {
             // runs of 2: the four columns' 16 accumulators keep 8 blocks per SM
             constexpr int TO = 2;
@@ -1582,9 +1596,9 @@ int fl_matched_adjoint_wt(fl_plan* p, const void* yw, int wt, void* x, int xt, c
 // below is timed (CUDA events, one launch after one untimed) on the plan's own
 // geometry, with the plan's scratch as input and output, and the fastest kept
 // for the forward and for the backprojection (for the reflection
-// backprojection, with runs of 1 or 2 voxels per thread). A thread's result
-// does not depend on the shape or the run, so neither do the projections. Fan
-// plans keep theirs.
+// backprojection, with runs of 1 or 2 voxels per thread and 1 or 2 rows per
+// iteration). A thread's result does not depend on these, so neither do the
+// projections. Fan plans keep theirs.
 extern "C" int fl_plan_autotune(fl_plan* p, void* stream, int32_t* shapes)
 {
     FL_RANGE("fl_plan_autotune");
@@ -1620,27 +1634,35 @@ extern "C" int fl_plan_autotune(fl_plan* p, void* stream, int32_t* shapes)
                 return fl_set_error(FL_ERR_CUDA, "fl_plan_autotune: timing failed");
             return FL_OK;
         };
-        // the reflection backprojection also tries both voxel runs per thread
-        const int nruns = fl_plan_turns(p) == 8 ? 2 : 1;
+        // the reflection backprojection also tries voxel runs of 2 and 1 per
+        // thread and one or two rows per iteration (variant r: run 2 - r % 2,
+        // rows 1 + r / 2)
+        const int nvar = fl_plan_turns(p) == 8 ? 4 : 1;
         for (int pass = 0; pass < 2 && !st; pass++) {
             const bool fwd = pass == 0;
             float best = 3.0e38f;
             int bi = 0, br = 0;
             for (int c = 0; c < 4 && !st; c++)
-                for (int r = 0; r < (fwd ? 1 : nruns) && !st; r++) {
+                for (int r = 0; r < (fwd ? 1 : nvar) && !st; r++) {
                     if (fwd) { p->fwd_bx = cand[c][0]; p->fwd_by = cand[c][1]; }
-                    else { p->adj_bx = cand[c][0]; p->adj_by = cand[c][1]; p->adj_run = 2 - r; }
+                    else {
+                        p->adj_bx = cand[c][0]; p->adj_by = cand[c][1];
+                        p->adj_run = 2 - r % 2; p->adj_rows = 1 + r / 2;
+                    }
                     float ms = 0.0f;
                     st = timed(fwd, ms);
                     if (!st && ms < best) { best = ms; bi = c; br = r; }
                 }
             if (fwd) { p->fwd_bx = cand[bi][0]; p->fwd_by = cand[bi][1]; }
-            else { p->adj_bx = cand[bi][0]; p->adj_by = cand[bi][1]; p->adj_run = 2 - br; }
+            else {
+                p->adj_bx = cand[bi][0]; p->adj_by = cand[bi][1];
+                p->adj_run = 2 - br % 2; p->adj_rows = 1 + br / 2;
+            }
         }
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         if (st) {                         // keep the built-in shapes after a failure
-            p->fwd_bx = p->fwd_by = p->adj_bx = p->adj_by = p->adj_run = 0;
+            p->fwd_bx = p->fwd_by = p->adj_bx = p->adj_by = p->adj_run = p->adj_rows = 0;
             return st;
         }
     }

@@ -225,8 +225,10 @@ class Plan:
         out = {"forward": (sh[0], sh[1]), "adjoint": (sh[2], sh[3])}
         if self.reflect:
             v = C.c_int()
-            _lib.check(self._L.fl_plan_query(self._h, _lib.QUERY_ADJ_RUN, C.byref(v)))
+            _lib.check(self._L.fl_plan_query(self._h, _lib.TUNE_ADJ_RUN, C.byref(v)))
             out["adjoint_voxels_per_thread"] = v.value
+            _lib.check(self._L.fl_plan_query(self._h, _lib.TUNE_ADJ_ROWS, C.byref(v)))
+            out["adjoint_rows_per_iteration"] = v.value
         return out
 
     def count_intersections(self, stream=None) -> torch.Tensor:

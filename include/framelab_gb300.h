@@ -230,9 +230,12 @@ int fl_plan_query(const fl_plan *plan, int option, int *value);
  * plan's scratch buffers. shapes (optional, [4]): the chosen forward x, y and
  * backprojection x, y (0 for fan plans, which keep their shapes). */
 int fl_plan_autotune(fl_plan *plan, void *stream, int32_t *shapes);
-/* fl_plan_query(plan, FL_QUERY_ADJ_RUN, &v): voxels per thread of the
- * reflection backprojection (1 or 2; fl_plan_autotune times both). */
-enum { FL_QUERY_ADJ_RUN = 16 };
+/* FL_TUNE_ADJ_RUN: voxels per thread of the reflection backprojection (1 or
+ * 2); FL_TUNE_ADJ_ROWS: detector rows per iteration of its row loop (1 or 2).
+ * fl_plan_autotune times each pair and keeps the fastest; fl_plan_option sets
+ * them (other values are refused), fl_plan_query reads them. The results do
+ * not depend on them. */
+enum { FL_TUNE_ADJ_RUN = 16, FL_TUNE_ADJ_ROWS = 17 };
 
 /* y = A x on `stream`. x: n_vox elements, y: n_rays elements, device memory. */
 int fl_forward(fl_plan *plan, int model, const void *x, int x_dtype, void *y, int y_dtype,
