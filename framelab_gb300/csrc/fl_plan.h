@@ -115,7 +115,8 @@ struct fl_plan {
     // every thread's result is independent of the shape)
     int fwd_bx, fwd_by, adj_bx, adj_by;
     // voxels per thread of the reflection backprojection (1 or 2; 0 = 2) and
-    // detector rows per iteration of its row loop (1 or 2; 0 = 1)
+    // its row loop: 1 or 2 rows per iteration, 3 one pass over the run's rows
+    // (runs of 2; 0 = 1)
     int adj_run, adj_rows;
     // scale of an FP16 backprojection input (the mixed CGLS form): the largest
     // power of two with y16_scale * c_r^2 <= 1 for every ray, so c_r^2 * (a

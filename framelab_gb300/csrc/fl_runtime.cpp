@@ -328,8 +328,9 @@ extern "C" int fl_plan_option(fl_plan* p, int option, int value)
         return fl_set_error(FL_OK, "");
     }
     if (option == FL_TUNE_ADJ_RUN || option == FL_TUNE_ADJ_ROWS) {
-        if (value != 1 && value != 2)
-            return fl_set_error(FL_ERR_INVALID, "fl_plan_option: %d is not 1 or 2", value);
+        const int top = option == FL_TUNE_ADJ_RUN ? 2 : 3;
+        if (value < 1 || value > top)
+            return fl_set_error(FL_ERR_INVALID, "fl_plan_option: %d is not in 1..%d", value, top);
         (option == FL_TUNE_ADJ_RUN ? p->adj_run : p->adj_rows) = value;
         return fl_set_error(FL_OK, "");
     }
@@ -360,7 +361,7 @@ extern "C" int fl_plan_query(const fl_plan* p, int option, int* value)
         return fl_set_error(FL_OK, "");
     }
     if (option == FL_TUNE_ADJ_ROWS) {
-        *value = p->adj_rows == 2 ? 2 : 1;
+        *value = p->adj_rows ? p->adj_rows : 1;
         return fl_set_error(FL_OK, "");
     }
     return fl_set_error(FL_ERR_INVALID, "fl_plan_query: unknown option %d", option);

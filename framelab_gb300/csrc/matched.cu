@@ -961,6 +961,60 @@ __device__ __forceinline__ void adj_rows_hex(float2 (&P)[4][TZ], float2 (&Q)[4][
 {
     float mn = fminf(e1, e2), mx = fmaxf(e1, e2);
     float lo_e = e1 - 0.02f, hi_e = e2 + s2 + 0.02f;
+    if constexpr (RU == 0) {
+        // the run's rows once: each row in the union of the voxels' windows
+        // is loaded once and adds to every voxel whose window holds it (the
+        // same terms in the same order as one pass per voxel)
+        int blo[TZ], bhi[TZ];
+        int ulo = nb, uhi = -1;
+#pragma unroll
+        for (int k = 0; k < TZ; k++) {
+            if (MODE < 0) {
+                blo[k] = max(__float2int_ru(lo_e), 0);
+                bhi[k] = min(__float2int_rd(hi_e), nb - 1);
+                lo_e += s1; hi_e += s2;
+            } else {
+                e1 += s1; e2 += s2;
+                const float mn1 = fminf(e1, e2), mx1 = fmaxf(e1, e2);
+                blo[k] = max(__float2int_ru(fminf(mn, mn1) - 0.02f), 0);
+                bhi[k] = min(__float2int_rd(fmaxf(mx, mx1) + 0.02f), nb - 1);
+                mn = mn1; mx = mx1;
+            }
+            if (k >= nk) { blo[k] = nb; bhi[k] = -1; }
+            ulo = min(ulo, blo[k]); uhi = max(uhi, bhi[k]);
+        }
+        for (int ib = ulo; ib <= uhi; ib++) {
+            if (!FL_IN(ib, nb)) continue;
+            const AxisEntry re = rv[ib];
+            float o[16];
+            ld_in<TW, 8>(yt + 8 * (long long)ib * na, *reinterpret_cast<float(*)[8]>(o));
+            ld_in<TW, 8>(yr + 8 * (long long)ib * na, *reinterpret_cast<float(*)[8]>(o + 8));
+            const float cb = __fsub_rn(re.c, be);
+            float az[TZ + 1];
+#pragma unroll
+            for (int k = 0; k <= TZ; k++)
+                az[k] = xrel(re, __fsub_rn((float)(z0 + k), re.kq), bh, cb);
+#pragma unroll
+            for (int k = 0; k < TZ; k++) {
+                if (ib < blo[k] || ib > bhi[k]) continue;
+                float l2, h2;
+                if (MODE < 0) { l2 = fmaxf(l, az[k + 1]); h2 = fminf(h, az[k]); }
+                else {
+                    l2 = fmaxf(l, fminf(az[k], az[k + 1]));
+                    h2 = fminf(h, fmaxf(az[k], az[k + 1]));
+                }
+                const float w = fmaxf(h2 - l2, 0.0f);
+                const float2 w2 = make_float2(w, w);
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    P[j][k] = __ffma2_rn(w2, make_float2(o[2 * j], o[2 * j + 1]), P[j][k]);
+                    Q[j][k] = __ffma2_rn(w2, make_float2(o[8 + 2 * j], o[9 + 2 * j]), Q[j][k]);
+                }
+            }
+        }
+        return;
+    }
+    constexpr int RN = RU > 0 ? RU : 1;          // rows per iteration below
 #pragma unroll
     for (int k = 0; k < TZ; k++) {
         if (k >= nk) break;
@@ -977,12 +1031,12 @@ __device__ __forceinline__ void adj_rows_hex(float2 (&P)[4][TZ], float2 (&Q)[4][
             mn = mn1; mx = mx1;
         }
         const float fk0 = (float)(z0 + k), fk1 = (float)(z0 + k + 1);
-        for (int ib = blo; ib <= bhi; ib += RU) {
-            AxisEntry re[RU];
-            float o[RU][16];
-            bool on[RU];
+        for (int ib = blo; ib <= bhi; ib += RN) {
+            AxisEntry re[RN];
+            float o[RN][16];
+            bool on[RN];
 #pragma unroll
-            for (int u = 0; u < RU; u++) {
+            for (int u = 0; u < RN; u++) {
                 on[u] = ib + u <= bhi && FL_IN(ib + u, nb);
                 const long long r = on[u] ? ib + u : min(max(ib, 0), nb - 1);   // one that exists
                 re[u] = rv[r];
@@ -990,7 +1044,7 @@ __device__ __forceinline__ void adj_rows_hex(float2 (&P)[4][TZ], float2 (&Q)[4][
                 ld_in<TW, 8>(yr + 8 * r * na, *reinterpret_cast<float(*)[8]>(o[u] + 8));
             }
 #pragma unroll
-            for (int u = 0; u < RU; u++) {
+            for (int u = 0; u < RN; u++) {
                 const float2 az = row_planes(re[u], fk0, fk1, bh, be);
                 float l2, h2;
                 if (MODE < 0) { l2 = fmaxf(l, az.y); h2 = fminf(h, az.x); }
@@ -1022,7 +1076,7 @@ __device__ __forceinline__ void adj_rows_hex(float2 (&P)[4][TZ], float2 (&Q)[4][
 // of k_weight_packed_hex / k_fwd_hex (two planes); X the tiled folded volume
 // (xfold) or the standard one.
 template <typename TX, int TZ, int RU, typename TW>
-__global__ void __launch_bounds__(128, TZ == 1 ? (RU == 1 ? 8 : 6) : (RU == 1 ? 6 : 5))
+__global__ void __launch_bounds__(128, TZ == 1 ? (RU == 2 ? 6 : 8) : (RU == 1 ? 6 : 5))
 k_adj_hex(TX* __restrict__ X, const TW* __restrict__ yw, const ColEntry* __restrict__ col,
           const AxisEntry* __restrict__ rowz, const ViewEntry* __restrict__ view, DetGrid G, int n,
           int nz, int na, int nb, int nv, float dz, const int* __restrict__ skip, int xfold)
@@ -1327,8 +1381,10 @@ void launch_adj_cone(fl_plan* p, const TW* yw, void* x, const int* skip, int xfo
         int zruns = (nzw + TZ - 1) / TZ;
         if (fl_plan_turns(p) == 8) {
             // runs of 2 voxels (the eight columns' 32 accumulators) or of 1 (16
-            // accumulators), one or two rows per iteration: fl_plan_autotune
-            const int run = p->adj_run == 1 ? 1 : 2, ru = p->adj_rows == 2 ? 2 : 1;
+            // accumulators); one or two rows per iteration, or (runs of 2) one
+            // pass over the run's rows: fl_plan_autotune
+            const int run = p->adj_run == 1 ? 1 : 2;
+            const int ru = p->adj_rows == 2 ? 2 : (p->adj_rows == 3 && run == 2 ? 0 : 1);
             zruns = (nzw + run - 1) / run;
             const dim3 ab = p->adj_bx ? dim3(p->adj_bx, p->adj_by) : dim3(8, 16);
             dim3 grid(fl_div_up(s.nx / 2, ab.x), fl_div_up(s.ny / 2, ab.y), (unsigned)zruns);
@@ -1339,7 +1395,8 @@ void launch_adj_cone(fl_plan* p, const TW* yw, void* x, const int* skip, int xfo
             if (run == 1 && ru == 1) FL_ADJ_HEX(1, 1);
             else if (run == 1) FL_ADJ_HEX(1, 2);
             else if (ru == 1) FL_ADJ_HEX(2, 1);
-            else FL_ADJ_HEX(2, 2);
+            else if (ru == 2) FL_ADJ_HEX(2, 2);
+            else FL_ADJ_HEX(2, 0);
 #undef FL_ADJ_HEX
         } else if (p->zmirror && p->rot && p->rot4) {
             // runs of 2: the four columns' 16 accumulators keep 8 blocks per SM
@@ -1597,8 +1654,8 @@ int fl_matched_adjoint_wt(fl_plan* p, const void* yw, int wt, void* x, int xt, c
 // geometry, with the plan's scratch as input and output, and the fastest kept
 // for the forward and for the backprojection (for the reflection
 // backprojection, with runs of 1 or 2 voxels per thread and 1 or 2 rows per
-// iteration). A thread's result does not depend on these, so neither do the
-// projections. Fan plans keep theirs.
+// iteration or one pass over a run's rows). A thread's result does not depend
+// on these, so neither do the projections. Fan plans keep theirs.
 extern "C" int fl_plan_autotune(fl_plan* p, void* stream, int32_t* shapes)
 {
     FL_RANGE("fl_plan_autotune");
@@ -1635,9 +1692,10 @@ extern "C" int fl_plan_autotune(fl_plan* p, void* stream, int32_t* shapes)
             return FL_OK;
         };
         // the reflection backprojection also tries voxel runs of 2 and 1 per
-        // thread and one or two rows per iteration (variant r: run 2 - r % 2,
-        // rows 1 + r / 2)
-        const int nvar = fl_plan_turns(p) == 8 ? 4 : 1;
+        // thread with one or two rows per iteration, and runs of 2 in one pass
+        // over their rows (variant r: run, rows)
+        static const int var[5][2] = {{2, 1}, {1, 1}, {2, 2}, {1, 2}, {2, 3}};
+        const int nvar = fl_plan_turns(p) == 8 ? 5 : 1;
         for (int pass = 0; pass < 2 && !st; pass++) {
             const bool fwd = pass == 0;
             float best = 3.0e38f;
@@ -1647,7 +1705,7 @@ extern "C" int fl_plan_autotune(fl_plan* p, void* stream, int32_t* shapes)
                     if (fwd) { p->fwd_bx = cand[c][0]; p->fwd_by = cand[c][1]; }
                     else {
                         p->adj_bx = cand[c][0]; p->adj_by = cand[c][1];
-                        p->adj_run = 2 - r % 2; p->adj_rows = 1 + r / 2;
+                        p->adj_run = var[r][0]; p->adj_rows = var[r][1];
                     }
                     float ms = 0.0f;
                     st = timed(fwd, ms);
@@ -1656,7 +1714,7 @@ extern "C" int fl_plan_autotune(fl_plan* p, void* stream, int32_t* shapes)
             if (fwd) { p->fwd_bx = cand[bi][0]; p->fwd_by = cand[bi][1]; }
             else {
                 p->adj_bx = cand[bi][0]; p->adj_by = cand[bi][1];
-                p->adj_run = 2 - br % 2; p->adj_rows = 1 + br / 2;
+                p->adj_run = var[br][0]; p->adj_rows = var[br][1];
             }
         }
         cudaEventDestroy(e0);

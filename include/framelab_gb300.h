@@ -231,10 +231,11 @@ int fl_plan_query(const fl_plan *plan, int option, int *value);
  * backprojection x, y (0 for fan plans, which keep their shapes). */
 int fl_plan_autotune(fl_plan *plan, void *stream, int32_t *shapes);
 /* FL_TUNE_ADJ_RUN: voxels per thread of the reflection backprojection (1 or
- * 2); FL_TUNE_ADJ_ROWS: detector rows per iteration of its row loop (1 or 2).
- * fl_plan_autotune times each pair and keeps the fastest; fl_plan_option sets
- * them (other values are refused), fl_plan_query reads them. The results do
- * not depend on them. */
+ * 2); FL_TUNE_ADJ_ROWS: its row loop, 1 or 2 detector rows per iteration, or
+ * 3: one pass over a run's rows, each row loaded once for all the run's
+ * voxels (runs of 2; with runs of 1 it is 1). fl_plan_autotune times the
+ * pairs and keeps the fastest; fl_plan_option sets them (other values are
+ * refused), fl_plan_query reads them. The results do not depend on them. */
 enum { FL_TUNE_ADJ_RUN = 16, FL_TUNE_ADJ_ROWS = 17 };
 
 /* y = A x on `stream`. x: n_vox elements, y: n_rays elements, device memory. */

@@ -826,11 +826,12 @@ def test_autotune_keeps_the_projections(zm):
         from framelab_gb300 import _lib
         L = _lib.load()
         for run in (1, 2):
-            for rows in (1, 2):
+            for rows in (1, 2, 3):
                 assert L.fl_plan_option(P.handle, _lib.TUNE_ADJ_RUN, run) == _lib.FL_OK
                 assert L.fl_plan_option(P.handle, _lib.TUNE_ADJ_ROWS, rows) == _lib.FL_OK
                 assert np.array_equal(_host(P.adjoint(r)), x0), (run, rows)
         assert L.fl_plan_option(P.handle, _lib.TUNE_ADJ_RUN, 3) == _lib.FL_ERR_INVALID
+        assert L.fl_plan_option(P.handle, _lib.TUNE_ADJ_ROWS, 4) == _lib.FL_ERR_INVALID
 
 
 # degenerate and small sizes: one view, one detector column or row, a 1-pixel
