@@ -598,9 +598,9 @@ def parity_block(ctx, w, p):
         t0 = time.perf_counter()
         if w["kind"] == "cone":
             r = PAR.cone_parity(p, x, fwd, adj, n_rays=20000, n_vox=2000 if n >= 512 else 4000,
-                                turns=t)
+                                turns=P.rotations, reflect=P.reflect)
         else:
-            r = PAR.fan_parity(p, x, fwd, adj, turns=t)
+            r = PAR.fan_parity(p, x, fwd, adj, turns=P.rotations, reflect=P.reflect)
         r["views_per_walk"] = t
         r["seconds"] = time.perf_counter() - t0
         out[form] = r
@@ -736,8 +736,9 @@ def run_single(ctx, name, w, p):
         tf, ta, y, xo = time_pair(ctx, P, p32)
         roofline = projector_roofline(ctx, name, n_isect, P.n_rays, P.n_vox, tf, ta, detail,
                                       "matched", clocks.summary().get("sm_mhz"),
-                                      l1_form={8: "hex", 4: "oct"}.get(P.views_per_walk)
-                                      if w["kind"] == "cone" else None)
+                                      l1_form=({(4, True): "hex", (4, False): "oct"}
+                                               .get((P.rotations, P.reflect))
+                                               if w["kind"] == "cone" else None))
         if w["kind"] == "cone":
             # dot-product identity <A x, y> = <x, A^T y> on N(0,1) vectors (FP64 dots)
             g = torch.Generator(device=ctx.dev).manual_seed(11)

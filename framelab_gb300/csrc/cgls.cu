@@ -329,7 +329,7 @@ struct fl_cgls {
     float* cap_uw;
     float *hb, *hu;             // device copies for the host-buffer entry point
     int fold;                   // fused forms on a z-mirror plan: vectors kept z-folded
-    int rot;                    // fl_plan_turns when the graph was captured (1, 2, 4)
+    int rot;                    // fl_plan_form when the graph was captured
     float *bf, *uf;             // folded copies of b and u
 };
 
@@ -372,7 +372,7 @@ extern "C" int fl_cgls_create(fl_plan* plan, int mode, fl_cgls** out)
     // algebra is elementwise, so only b in and u out change layout); whether
     // the plan uses the mirror is read again at every solve
     c->fold = (plan->zmirror && mode != FL_CGLS_PLAIN) ? 1 : 0;
-    c->rot = fl_plan_turns(plan);
+    c->rot = fl_plan_form(plan);
     if (c->fold) { M((void**)&c->bf, c->n * 4); M((void**)&c->uf, c->n * 4); }
     M((void**)&c->S, sizeof(CgScalars));
     M((void**)&c->partials, sizeof(double) * c->grid);
@@ -542,7 +542,7 @@ static int solve_mixed(fl_cgls* c, const float* b, float* u, float lam, int iter
         }
     }
     if (fold != c->fold) { c->fold = fold; c->captured = false; }
-    const int rot = fl_plan_turns(c->plan);               // kernels in the graph
+    const int rot = fl_plan_form(c->plan);                // kernels in the graph
     if (rot != c->rot) { c->rot = rot; c->captured = false; }
     FL_CUDA(cudaEventRecord(c->ev0, us));
     FL_CUDA(cudaStreamWaitEvent(s, c->ev0, 0));

@@ -55,13 +55,14 @@ struct fl_plan {
     float *d_cos_det2, *d_sin_det2; // [na+1] bin-edge trig (finite-beam backprojector)
     float *d_fb_edges;             // [nv*na*6] finite-beam edge lines (Px, Py, Pd) x 2
     int32_t *d_view_frame, *d_idY, *d_Nv;
-    // matched-model tables (device); row nv (one extra view) holds view nv/8
-    // at the exact angle pi/4 for the reflection form (rot8)
-    ColEntry *d_col;           // [(nv+1)*na]
-    float *d_colr;             // [(nv+1)*na] fl(d_x^2 + d_y^2)
-    RowEntry *d_row;           // [(nv+1)*nb]
-    AxisEntry *d_rowz;         // [(nv+1)*nb] z axes: the backprojector's 16-byte copy
-    ViewEntry *d_view;         // [nv+1]
+    // matched-model tables (device); rows nv and nv + 1 (two extra views) hold
+    // view nv/8 at the exact angle pi/4 and view nv/4 at the exact angle pi/2
+    // for the reflection forms
+    ColEntry *d_col;           // [(nv+2)*na]
+    float *d_colr;             // [(nv+2)*na] fl(d_x^2 + d_y^2)
+    RowEntry *d_row;           // [(nv+2)*nb]
+    AxisEntry *d_rowz;         // [(nv+2)*nb] z axes: the backprojector's 16-byte copy
+    ViewEntry *d_view;         // [nv+2]
     // detector grid for the adjoint windows (matched model)
     int det_kind;              // 0 flat uniform, 1 equiangular (fan), -1 irregular
     float u0, du, g0, dg;      // flat: u = u0 + ia*du ; arc: gamma = g0 + ia*dg
@@ -90,21 +91,24 @@ struct fl_plan {
     // serves eight rays (views v + j nv/4, rows b and nb-1-b).
     int rot4_ok;
     int rot4;                  // in use (FL_OPT_QUARTER_TURN; only with rot and zmirror)
-    // reflection on top of the quarter turn (cone plans): nv a multiple of 8,
-    // view nv - v the mirror image of view v about the x axis (to within
-    // 1e-6) and a detector symmetric about its centre (y_det[na-1-a] ==
-    // -y_det[a] exactly, na even). With M (x, y) = (x, n-1-y) the matched
-    // model then defines, for the walked views v = 0 .. nv/8 (views 0 and
-    // nv/8 on their columns a < na/2 only, the other half being their
-    // mirror images),
-    //   A[(v + j nv/4, a, b), R^j V] = A[(j nv/4 - v, na-1-a, b), R^j M V]
+    // reflection on top of the half or the quarter turn (cone plans): view nv
+    // - v the mirror image of view v about the x axis (to within 1e-6), view 0
+    // at angle 0 and a detector symmetric about its centre (y_det[na-1-a] ==
+    // -y_det[a] exactly, na even). With M (x, y) = (x, ny-1-y) and S = R (the
+    // quarter turn, NR = 4 rotations; nv a multiple of 8) or S = R^2 (the half
+    // turn, NR = 2), the matched model defines, for the walked views v = 0 ..
+    // ov (ov = nv/8, or floor(nv/4)),
+    //   A[(v + j nv/NR, a, b), S^j V] = A[(j nv/NR - v, na-1-a, b), S^j M V]
     //     = A[(v, a, b), V],
-    // so one walk / one weight serves sixteen rays (the dihedral group of the
-    // square times the z mirror). View nv/8's walked rays use the tables of
-    // the exact diagonal angle pi/4 (extra table row nv), so the scan the
-    // plan projects has every view at an angle of the group's orbit.
-    int rot8_ok;
-    int rot8;                  // in use (FL_OPT_REFLECT; only with rot4)
+    // so one walk / one weight serves 4 NR rays (the symmetries of the square,
+    // or of the rectangle, times the z mirror). View 0, and view ov where it
+    // is its own mirror image (NR = 4; NR = 2 with nv a multiple of 4), walk
+    // their columns a < na/2 only, the other half being their mirror images;
+    // view ov is then walked from table row nv (NR = 4: the exact diagonal
+    // angle pi/4) or nv + 1 (NR = 2: the exact angle pi/2), so the scan the
+    // plan projects has every view at an angle of its orbit.
+    int refl4_ok, refl2_ok;    // the geometry allows it with the quarter / half turn
+    int refl;                  // wanted (FL_OPT_REFLECT); used where the turn in use allows
     // fan plans take both turns without a mirror: the half turn with ny even,
     // the quarter turn with nx == ny even (A[(v + j nv/G, a), R^j (x, y)] =
     // A[(v, a), (x, y)], one walk / one weight serving G rays).
@@ -130,14 +134,44 @@ struct fl_plan {
     size_t vwork_bytes;
 };
 
-// Rays served by one walk or weight of the matched kernels in use, over the
-// views: 8 (quarter turns and the reflection), 4 (quarter turn), 2 (half turn)
-// or 1. A cone plan's turn forms also need the z mirror.
+// The matched kernel form a plan uses (its options within what its geometry
+// allows). A cone plan's turn forms also need the z mirror.
+enum {
+    FL_FORM_GENERAL = 0,      // general kernels (fan: no turn; cone: no mirror)
+    FL_FORM_MIRROR,           // cone: z mirror
+    FL_FORM_HALF,             // half turn (cone: with the z mirror)
+    FL_FORM_QUARTER,          // quarter turns (cone: with the z mirror)
+    FL_FORM_HALF_REFL,        // cone: half turn, reflection, z mirror
+    FL_FORM_QUARTER_REFL      // cone: quarter turns, reflection, z mirror
+};
+
+inline int fl_plan_form(const fl_plan* p)
+{
+    if (p->s.ndim == 3 && !p->zmirror) return FL_FORM_GENERAL;
+    if (!p->rot) return p->s.ndim == 3 ? FL_FORM_MIRROR : FL_FORM_GENERAL;
+    if (p->rot4)
+        return (p->s.ndim == 3 && p->refl && p->refl4_ok) ? FL_FORM_QUARTER_REFL : FL_FORM_QUARTER;
+    return (p->s.ndim == 3 && p->refl && p->refl2_ok) ? FL_FORM_HALF_REFL : FL_FORM_HALF;
+}
+
+// Views one walk or weight of the matched kernels in use serves: 8 (quarter
+// turns and the reflection), 4 (quarter turns, or the half turn and the
+// reflection), 2 (half turn) or 1.
 inline int fl_plan_turns(const fl_plan* p)
 {
-    if (!p->rot || (p->s.ndim == 3 && !p->zmirror)) return 1;
-    if (!p->rot4) return 2;
-    return p->rot8 ? 8 : 4;
+    switch (fl_plan_form(p)) {
+    case FL_FORM_QUARTER_REFL: return 8;
+    case FL_FORM_QUARTER: case FL_FORM_HALF_REFL: return 4;
+    case FL_FORM_HALF: return 2;
+    default: return 1;
+    }
+}
+
+// Rotations of a reflection form (4 or 2), or 0.
+inline int fl_plan_refl(const fl_plan* p)
+{
+    const int f = fl_plan_form(p);
+    return f == FL_FORM_QUARTER_REFL ? 4 : (f == FL_FORM_HALF_REFL ? 2 : 0);
 }
 
 // Layouts of the matched launchers' operands. For a z-mirror plan the
@@ -147,14 +181,10 @@ inline int fl_plan_turns(const fl_plan* p)
 // pairs (row ib, row nb-1-ib) for ib < nb/2 at pair index (iv*nb/2 + ib)*na + ia,
 // except on a half- (G = 2) or quarter-turn (G = 4) plan, where the 2 G values
 // of views iv + j nv/G (j < G), rows ib and nb-1-ib, lie side by side at
-// 2 G ((iv*nb/2 + ib)*na + ia) + 2 j for iv < nv/G. A reflection plan (G = 8)
-// packs the 16 values of a walked ray's orbit in two planes of nv*nb*na/2
-// values: at 8 ((s*nb/2 + ib)*na + ia) + 2 k the rows of view v + k nv/4 at
-// column a (k < 4), and at the same place in the second plane those of view
-// k nv/4 - v at column na-1-a, where slot s in [1, nv/8) is the walked view
-// v = s at column a = ia, and slot 0 holds view 0 at columns a = ia < na/2
-// and view nv/8 at columns a = ia - na/2 (both walk half their columns), so
-// the packed input has exactly nv*nb*na values. A fan plan with turns
+// 2 G ((iv*nb/2 + ib)*na + ia) + 2 j for iv < nv/G. A reflection form packs
+// the 4 NR values of a walked ray's orbit in two planes of nv*nb*na/2 values
+// (the turn images' rows, then the reflected images'; ReflGeom in
+// matched_dev.cuh), exactly nv*nb*na values in all. A fan plan with turns
 // (G = 2 or 4) packs the G values of views iv + j nv/G side by side at
 // G (iv*na + ia) + j.
 // A half- or quarter-turn plan's folded volume is tiled in xy: the pair of

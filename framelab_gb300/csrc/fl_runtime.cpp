@@ -136,17 +136,21 @@ static int build_tables(fl_plan* p, const std::vector<float>& phi, const float* 
     const double ac = SO / SD;   // alpha at the isocentre plane: A = alpha - ac
     const int nx2 = s.nx / 2, ny2 = s.ny / 2, nz2 = s.nz / 2;
     // views 0 .. nv-1, then row nv: view nv/8 at the exact diagonal angle
-    // pi/4 (the reflection form walks it there; a copy of view 0 otherwise)
-    const int nvt = s.nv + 1;
+    // pi/4, row nv + 1: view nv/4 at the exact angle pi/2 (the reflection
+    // forms walk them there; copies of view 0 where nv/8 or nv/4 is no view)
+    const int nvt = s.nv + 2;
     std::vector<ColEntry> col((size_t)nvt * s.na);
     std::vector<float> colr((size_t)nvt * s.na);
     std::vector<RowEntry> row((size_t)nvt * s.nb);
     std::vector<ViewEntry> view(nvt);
-    const bool diag = s.nv % 8 == 0;
+    const bool diag = s.nv % 8 == 0, side = s.nv % 4 == 0;
     for (int iv = 0; iv < nvt; iv++) {
-        const int src = iv < s.nv ? iv : (diag ? s.nv / 8 : 0);
+        int src = iv;
+        if (iv == s.nv) src = diag ? s.nv / 8 : 0;
+        if (iv == s.nv + 1) src = side ? s.nv / 4 : 0;
         double c = std::cos((double)phi[src]), sn = std::sin((double)phi[src]);
         if (iv == s.nv && diag) c = sn = std::sqrt(0.5);
+        if (iv == s.nv + 1 && side) { c = 0.0; sn = 1.0; }
         double Sx = -SO * c, Sy = -SO * sn, Sz = sd_z ? (double)sd_z[src] : 0.0;
         view[iv] = ViewEntry{(float)c, (float)sn, (float)Sz, (float)ac};
         for (int ia = 0; ia < s.na; ia++) {
@@ -287,11 +291,12 @@ static int build_tables(fl_plan* p, const std::vector<float>& phi, const float* 
         p->rot4_ok = ok ? 1 : 0;
     }
     p->rot4 = p->rot4_ok;
-    // reflection (fl_plan.h): cone plans with the quarter turn, nv a multiple
-    // of 8, view nv - v the mirror image of view v about the x axis to within
-    // 1e-6 (cos equal, sin opposite) and an exactly symmetric detector
-    p->rot8_ok = 0;
-    if (p->rot4_ok && s.ndim == 3 && diag && s.na % 2 == 0) {
+    // reflection (fl_plan.h): cone plans with the half turn (and, for the
+    // quarter-turn form, the quarter turn and nv a multiple of 8), view nv - v
+    // the mirror image of view v about the x axis to within 1e-6 (cos equal,
+    // sin opposite) and an exactly symmetric detector
+    p->refl2_ok = p->refl4_ok = 0;
+    if (p->rot_ok && s.ndim == 3 && s.na % 2 == 0) {
         bool ok = true;
         for (int ia = 0; ia < s.na / 2 && ok; ia++)
             if (y_det[s.na - 1 - ia] != -y_det[ia]) ok = false;
@@ -302,9 +307,10 @@ static int build_tables(fl_plan* p, const std::vector<float>& phi, const float* 
             if (std::fabs(c0 - c1) > 1e-6 || std::fabs(s0 + s1) > 1e-6) ok = false;
         }
         if (phi[0] != 0.0f) ok = false;             // view 0 is its own mirror image
-        p->rot8_ok = ok ? 1 : 0;
+        p->refl2_ok = ok ? 1 : 0;
+        p->refl4_ok = (ok && p->rot4_ok && diag) ? 1 : 0;
     }
-    p->rot8 = p->rot8_ok;
+    p->refl = 1;
     return FL_OK;
 }
 
@@ -324,7 +330,7 @@ extern "C" int fl_plan_option(fl_plan* p, int option, int value)
         return fl_set_error(FL_OK, "");
     }
     if (option == FL_OPT_REFLECT) {
-        p->rot8 = (value && p->rot8_ok) ? 1 : 0;
+        p->refl = value ? 1 : 0;
         return fl_set_error(FL_OK, "");
     }
     if (option == FL_TUNE_ADJ_RUN || option == FL_TUNE_ADJ_ROWS) {
@@ -344,16 +350,17 @@ extern "C" int fl_plan_query(const fl_plan* p, int option, int* value)
         *value = p->zmirror;
         return fl_set_error(FL_OK, "");
     }
+    const int form = fl_plan_form(p);
     if (option == FL_OPT_ROT_MIRROR) {
-        *value = fl_plan_turns(p) >= 2 ? 1 : 0;
+        *value = form >= FL_FORM_HALF ? 1 : 0;
         return fl_set_error(FL_OK, "");
     }
     if (option == FL_OPT_QUARTER_TURN) {
-        *value = fl_plan_turns(p) >= 4 ? 1 : 0;
+        *value = (form == FL_FORM_QUARTER || form == FL_FORM_QUARTER_REFL) ? 1 : 0;
         return fl_set_error(FL_OK, "");
     }
     if (option == FL_OPT_REFLECT) {
-        *value = fl_plan_turns(p) == 8 ? 1 : 0;
+        *value = fl_plan_refl(p) ? 1 : 0;
         return fl_set_error(FL_OK, "");
     }
     if (option == FL_TUNE_ADJ_RUN) {

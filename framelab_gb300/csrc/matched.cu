@@ -159,57 +159,59 @@ k_fwd_oct(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restri
 }
 
 // View and column of the ray that image k of a walked ray (v, a) is, on a
-// reflection plan: k < 4 the turn R^k (view v + k nv/4, column a), k >= 4 the
-// reflection R^(k-4) M (view (k-4) nv/4 - v, column na-1-a).
-__device__ __forceinline__ void hex_image(int k, int v, int a, int na, int nv, long long& vk,
-                                          int& ak)
+// reflection form (NR = 4 or 2): k < NR the turn R^(4k/NR) (view v + k nv/NR,
+// column a), k >= NR the reflection R^(4(k-NR)/NR) M (view (k-NR) nv/NR - v,
+// column na-1-a).
+template <int NR>
+__device__ __forceinline__ void refl_image(int k, int v, int a, int na, int nv, long long& vk,
+                                           int& ak)
 {
-    const int qv = nv / 4;
-    if (k < 4) { vk = v + (long long)k * qv; ak = a; }
-    else { vk = ((long long)(k - 4) * qv - v + nv) % nv; ak = na - 1 - a; }
+    const int sv = nv / NR;
+    if (k < NR) { vk = v + (long long)k * sv; ak = a; }
+    else { vk = ((long long)(k - NR) * sv - v + nv) % nv; ak = na - 1 - a; }
 }
 
-// Reflection form (fl_plan::rot8): the block walks rows ib < nb/2 of the
-// slots s < nv/8 (hex_slot: the walked views 0 .. nv/8); each walk yields the
-// rays of its sixteen images (hex_image, rows ib and nb-1-ib), all with the
-// walked ray's c_r. yfold writes the backprojection's input layout for these
-// plans: per (s, ib < nb/2, ia) the 8 values of the turn images side by side
-// in the first plane, the 8 of the reflected images in the second
-// (k_weight_packed_hex).
-template <typename TX, typename TY>
-__global__ void __launch_bounds__(128, 6)
-k_fwd_hex(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restrict__ col,
-          const float* __restrict__ colr, const RowEntry* __restrict__ row, int n, int nz,
-          int na, int nb, int nv, long long nper, float scale, int cr_power,
-          const int* __restrict__ skip, const float* __restrict__ xscale, int yfold)
+// Reflection forms (fl_plan::refl; NR = 4: quarter turns, square grid; NR =
+// 2: half turn): the block walks rows ib < nb/2 of the slots s (refl_slot:
+// the walked views 0 .. ov); each walk yields the rays of its 4 NR images
+// (refl_image, rows ib and nb-1-ib), all with the walked ray's c_r. yfold
+// writes the backprojection's input layout for these plans (two planes,
+// ReflGeom; k_weight_packed_refl).
+template <typename TX, typename TY, int NR>
+__global__ void __launch_bounds__(128, NR == 4 ? 6 : 8)
+k_fwd_refl(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restrict__ col,
+           const float* __restrict__ colr, const RowEntry* __restrict__ row, int nx, int ny,
+           int nz, int na, int nb, int nv, long long nper, float scale, int cr_power,
+           const int* __restrict__ skip, const float* __restrict__ xscale, int yfold)
 {
     if (skip && *skip) return;
+    const ReflGeom g = refl_geom(NR, nv, na, nb);
     const int ia = blockIdx.x * blockDim.x + threadIdx.x;
-    const int sl = blockIdx.y;                      // < nv / 8
+    const int sl = blockIdx.y;                      // < g.slots
     const int ib = blockIdx.z * blockDim.y + threadIdx.y;
-    const int nbh = nb / 2;
-    if (ia >= na || ib >= nbh) return;
-    int v, vt, a;
-    hex_slot(sl, ia, na, nv, v, vt, a);
+    if (ia >= na || ib >= g.nbh) return;
+    int v, vt, a, stride;
+    long long off;
+    if (!refl_slot(g, sl, ia, v, vt, a, off, stride)) return;
     const ColEntry* ce = col + (long long)vt * na + a;
     const RowEntry* re = row + (long long)vt * nb + ib;
-    float2 acc[8];
-    walk_hex<TX>(X, ce, &re->z, n, nz, acc, nper);
+    float2 acc[2 * NR];
+    walk_refl<TX, NR>(X, ce, &re->z, nx, ny, nz, acc, nper);
     const float cr = ray_cr(scale, colr[(long long)vt * na + a], __ldg(&re->dz2));
     const float xs = xscale ? *xscale : 1.0f;
 #pragma unroll
-    for (int k = 0; k < 8; k++) {
+    for (int k = 0; k < 2 * NR; k++) {
         float o0 = acc[k].x, o1 = acc[k].y;
         if (xscale) { o0 *= xs; o1 *= xs; }
         o0 = cr * o0; o1 = cr * o1;
         if (cr_power == 2) { o0 = cr * o0; o1 = cr * o1; }
-        if (yfold) {                    // the orbit's two planes of 8 values
-            const long long half = (long long)(nv / 8) * nbh * na * 8;
-            Store<TY>::st2(y + (k < 4 ? 0 : half) + 8 * (((long long)sl * nbh + ib) * na + ia) +
-                               2 * (k & 3), o0, o1);
+        if (yfold) {                    // the orbit's two planes of 2 NR values
+            Store<TY>::st2(y + (k < NR ? 0 : g.plane) + off +
+                               (long long)g.vpr * ((long long)ib * stride + ia) + 2 * (k % NR),
+                           o0, o1);
         } else {
             long long vk; int ak;
-            hex_image(k, v, a, na, nv, vk, ak);
+            refl_image<NR>(k, v, a, na, nv, vk, ak);
             Store<TY>::st(y + (vk * nb + ib) * na + ak, o0);
             Store<TY>::st(y + (vk * nb + (nb - 1 - ib)) * na + ak, o1);
         }
@@ -325,33 +327,34 @@ __global__ void k_weight_packed(float* __restrict__ yw, const TY* __restrict__ y
     }
 }
 
-// Packed yw of a reflection plan: for r = (s < nv/8, ib < nb/2, ia) the 16
-// values c_r y of the walked ray's images (hex_image, rows ib and nb-1-ib),
-// with c_r of the walked ray (hex_slot): images 0..3 at 8 r + 2 k, images
-// 4..7 in the second plane, at npack * 8 + 8 r + 2 (k - 4).
-template <typename TY>
-__global__ void k_weight_packed_hex(float* __restrict__ yw, const TY* __restrict__ y,
-                                    const float* __restrict__ colr,
-                                    const RowEntry* __restrict__ row, int na, int nb, int nv,
-                                    long long npack, float scale)
+// Packed yw of a reflection form: for each walked ray (refl_slot) and row ib
+// < nb/2 the 4 NR values c_r y of its images (refl_image, rows ib and
+// nb-1-ib), with c_r of the walked ray, in the two planes of ReflGeom.
+template <typename TY, int NR>
+__global__ void k_weight_packed_refl(float* __restrict__ yw, const TY* __restrict__ y,
+                                     const float* __restrict__ colr,
+                                     const RowEntry* __restrict__ row, int na, int nb, int nv,
+                                     long long npack, float scale)
 {
     long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= npack) return;
-    const int nbh = nb / 2;
+    if (r >= npack) return;                         // npack = slots * nb/2 * na
+    const ReflGeom g = refl_geom(NR, nv, na, nb);
     const int ia = (int)(r % na);
     const long long q = r / na;
-    const int ib = (int)(q % nbh);
-    const int sl = (int)(q / nbh);
-    int v, vt, a;
-    hex_slot(sl, ia, na, nv, v, vt, a);
+    const int ib = (int)(q % g.nbh);
+    const int sl = (int)(q / g.nbh);
+    int v, vt, a, stride;
+    long long off;
+    if (!refl_slot(g, sl, ia, v, vt, a, off, stride)) return;
     const float cr = ray_cr(scale, colr[(long long)vt * na + a], row[(long long)vt * nb + ib].dz2);
+    const long long at = off + (long long)g.vpr * ((long long)ib * stride + ia);
 #pragma unroll
-    for (int k = 0; k < 8; k++) {
+    for (int k = 0; k < 2 * NR; k++) {
         long long vk; int ak;
-        hex_image(k, v, a, na, nv, vk, ak);
+        refl_image<NR>(k, v, a, na, nv, vk, ak);
         const float p0 = Store<TY>::ld_plain(y + (vk * nb + ib) * na + ak);
         const float p1 = Store<TY>::ld_plain(y + (vk * nb + (nb - 1 - ib)) * na + ak);
-        Store<float>::st2(yw + (k < 4 ? 0 : 8 * npack) + 8 * r + 2 * (k & 3), cr * p0, cr * p1);
+        Store<float>::st2(yw + (k < NR ? 0 : g.plane) + at + 2 * (k % NR), cr * p0, cr * p1);
     }
 }
 
@@ -944,20 +947,21 @@ k_adj_oct(TX* __restrict__ X, const TW* __restrict__ yw, const ColEntry* __restr
         }
 }
 
-// Reflection form of adj_rows_oct: every weight multiplies the row pairs of
-// the walked ray's eight images into the sums P[j] (turn images) and Q[j]
-// (reflected images); yt / yr hold them side by side (8 values per row and
-// column in each plane, 32-byte aligned), so each is one vector load whose
-// lanes read neighbouring columns' orbits. RU rows per iteration: RU = 2
-// issues the loads of two rows before either's arithmetic (more loads in
-// flight per thread); the rows are still added in order.
-template <int MODE, int TZ, int RU, typename TW>
-__device__ __forceinline__ void adj_rows_hex(float2 (&P)[4][TZ], float2 (&Q)[4][TZ], int nk,
-                                             int z0, float l, float h, float e1, float e2,
-                                             float s1, float s2,
-                                             const AxisEntry* __restrict__ rv, float bh,
-                                             float be, const TW* __restrict__ yt,
-                                             const TW* __restrict__ yr, int na, int nb)
+// Reflection forms of adj_rows_oct: every weight multiplies the row pairs of
+// the walked ray's 2 NR images into the sums P[j] (turn images) and Q[j]
+// (reflected images); yt / yr hold them side by side (2 NR values per row and
+// column in each plane, rows rs columns apart), so each is one vector load
+// whose lanes read neighbouring columns' orbits. RU rows per iteration: RU =
+// 2 issues the loads of two rows before either's arithmetic (more loads in
+// flight per thread); RU = 0 loads each row of the run once for all its
+// voxels; the rows are added in order either way.
+template <int MODE, int TZ, int RU, typename TW, int NR>
+__device__ __forceinline__ void adj_rows_refl(float2 (&P)[NR][TZ], float2 (&Q)[NR][TZ], int nk,
+                                              int z0, float l, float h, float e1, float e2,
+                                              float s1, float s2,
+                                              const AxisEntry* __restrict__ rv, float bh,
+                                              float be, const TW* __restrict__ yt,
+                                              const TW* __restrict__ yr, int rs, int nb)
 {
     float mn = fminf(e1, e2), mx = fmaxf(e1, e2);
     float lo_e = e1 - 0.02f, hi_e = e2 + s2 + 0.02f;
@@ -986,9 +990,11 @@ __device__ __forceinline__ void adj_rows_hex(float2 (&P)[4][TZ], float2 (&Q)[4][
         for (int ib = ulo; ib <= uhi; ib++) {
             if (!FL_IN(ib, nb)) continue;
             const AxisEntry re = rv[ib];
-            float o[16];
-            ld_in<TW, 8>(yt + 8 * (long long)ib * na, *reinterpret_cast<float(*)[8]>(o));
-            ld_in<TW, 8>(yr + 8 * (long long)ib * na, *reinterpret_cast<float(*)[8]>(o + 8));
+            float o[4 * NR];
+            ld_in<TW, 2 * NR>(yt + 2 * NR * (long long)ib * rs,
+                              *reinterpret_cast<float(*)[2 * NR]>(o));
+            ld_in<TW, 2 * NR>(yr + 2 * NR * (long long)ib * rs,
+                              *reinterpret_cast<float(*)[2 * NR]>(o + 2 * NR));
             const float cb = __fsub_rn(re.c, be);
             float az[TZ + 1];
 #pragma unroll
@@ -1006,9 +1012,10 @@ __device__ __forceinline__ void adj_rows_hex(float2 (&P)[4][TZ], float2 (&Q)[4][
                 const float w = fmaxf(h2 - l2, 0.0f);
                 const float2 w2 = make_float2(w, w);
 #pragma unroll
-                for (int j = 0; j < 4; j++) {
+                for (int j = 0; j < NR; j++) {
                     P[j][k] = __ffma2_rn(w2, make_float2(o[2 * j], o[2 * j + 1]), P[j][k]);
-                    Q[j][k] = __ffma2_rn(w2, make_float2(o[8 + 2 * j], o[9 + 2 * j]), Q[j][k]);
+                    Q[j][k] = __ffma2_rn(w2, make_float2(o[2 * NR + 2 * j], o[2 * NR + 2 * j + 1]),
+                                         Q[j][k]);
                 }
             }
         }
@@ -1033,15 +1040,16 @@ __device__ __forceinline__ void adj_rows_hex(float2 (&P)[4][TZ], float2 (&Q)[4][
         const float fk0 = (float)(z0 + k), fk1 = (float)(z0 + k + 1);
         for (int ib = blo; ib <= bhi; ib += RN) {
             AxisEntry re[RN];
-            float o[RN][16];
+            float o[RN][4 * NR];
             bool on[RN];
 #pragma unroll
             for (int u = 0; u < RN; u++) {
                 on[u] = ib + u <= bhi && FL_IN(ib + u, nb);
                 const long long r = on[u] ? ib + u : min(max(ib, 0), nb - 1);   // one that exists
                 re[u] = rv[r];
-                ld_in<TW, 8>(yt + 8 * r * na, *reinterpret_cast<float(*)[8]>(o[u]));
-                ld_in<TW, 8>(yr + 8 * r * na, *reinterpret_cast<float(*)[8]>(o[u] + 8));
+                ld_in<TW, 2 * NR>(yt + 2 * NR * r * rs, *reinterpret_cast<float(*)[2 * NR]>(o[u]));
+                ld_in<TW, 2 * NR>(yr + 2 * NR * r * rs,
+                                  *reinterpret_cast<float(*)[2 * NR]>(o[u] + 2 * NR));
             }
 #pragma unroll
             for (int u = 0; u < RN; u++) {
@@ -1053,62 +1061,63 @@ __device__ __forceinline__ void adj_rows_hex(float2 (&P)[4][TZ], float2 (&Q)[4][
                 const float w = fmaxf(h2 - l2, 0.0f);
                 const float2 w2 = make_float2(w, w);
 #pragma unroll
-                for (int j = 0; j < 4; j++) {
+                for (int j = 0; j < NR; j++) {
                     P[j][k] = __ffma2_rn(w2, make_float2(o[u][2 * j], o[u][2 * j + 1]), P[j][k]);
-                    Q[j][k] = __ffma2_rn(w2, make_float2(o[u][8 + 2 * j], o[u][9 + 2 * j]),
-                                         Q[j][k]);
+                    Q[j][k] = __ffma2_rn(
+                        w2, make_float2(o[u][2 * NR + 2 * j], o[u][2 * NR + 2 * j + 1]), Q[j][k]);
                 }
             }
         }
     }
 }
 
-// Reflection + quarter-turn + z-mirror backprojection (fl_plan::rot8, nx == ny
-// == n): one thread per voxel column V0 = (x, y) of the octant x <= y < n/2
-// with its images C_k = R^k V0 and D_k = R^k M V0 (k < 4; for x == y, D_k =
-// C_{k+3} and only the C_k are visited), a run of TZ voxels of the lower half
-// and their mirrors; one frame. It visits the walked views v = 0 .. nv/8
-// (view nv/8 from table row nv; views 0 and nv/8 on columns a < na/2). In view
-// v a weight of column C_k multiplies turn slot j (view v + j nv/4) into
-// C_{k+j} and reflected slot j (view j nv/4 - v, column na-1-a) into D_{j-k};
-// a weight of D_k, turn slot j into D_{k+j} and reflected slot j into C_{j-k}.
-// One weight thus feeds sixteen (voxel, ray) pairs. yw is the packed input
-// of k_weight_packed_hex / k_fwd_hex (two planes); X the tiled folded volume
+// Reflection + z-mirror backprojections (fl_plan::refl). NR = 4 (quarter
+// turns, nx == ny == n): one thread per voxel column V0 = (x, y) of the octant
+// x <= y < n/2; NR = 2 (half turn): of the quadrant x < nx/2, y < ny/2. With
+// S = R^(4/NR) the thread owns the images C_k = S^k V0 and D_k = S^k M V0 (k
+// < NR; for NR = 4 and x == y, D_k = C_{k+3} and only the C_k are visited),
+// a run of TZ voxels of the lower half and their mirrors; one frame. It
+// visits the walked views w = 0 .. ov (refl_view). In view w a weight of
+// column C_k multiplies turn slot j (view w + j nv/NR) into C_{k+j} and
+// reflected slot j (view j nv/NR - w, column na-1-a) into D_{j-k}; a weight of
+// D_k, turn slot j into D_{k+j} and reflected slot j into C_{j-k}. One weight
+// thus feeds 4 NR (voxel, ray) pairs. yw is the packed input of
+// k_weight_packed_refl / k_fwd_refl (two planes); X the tiled folded volume
 // (xfold) or the standard one.
-template <typename TX, int TZ, int RU, typename TW>
+template <typename TX, int TZ, int RU, typename TW, int NR>
 __global__ void __launch_bounds__(128, TZ == 1 ? (RU == 2 ? 6 : 8) : (RU == 1 ? 6 : 5))
-k_adj_hex(TX* __restrict__ X, const TW* __restrict__ yw, const ColEntry* __restrict__ col,
-          const AxisEntry* __restrict__ rowz, const ViewEntry* __restrict__ view, DetGrid G, int n,
-          int nz, int na, int nb, int nv, float dz, const int* __restrict__ skip, int xfold)
+k_adj_refl(TX* __restrict__ X, const TW* __restrict__ yw, const ColEntry* __restrict__ col,
+           const AxisEntry* __restrict__ rowz, const ViewEntry* __restrict__ view, DetGrid G,
+           int nx, int ny, int nz, int na, int nb, int nv, float dz,
+           const int* __restrict__ skip, int xfold)
 {
     if (skip && *skip) return;
-    const int ix = blockIdx.x * blockDim.x + threadIdx.x;    // < n / 2
-    const int iy = blockIdx.y * blockDim.y + threadIdx.y;    // < n / 2
+    const ReflGeom g = refl_geom(NR, nv, na, nb);
+    const int ix = blockIdx.x * blockDim.x + threadIdx.x;    // < nx / 2
+    const int iy = blockIdx.y * blockDim.y + threadIdx.y;    // < ny / 2
     const int z0 = blockIdx.z * TZ;
-    const int nzw = nz / 2, nbw = nb / 2, ov = nv / 8, h = n / 2;
+    const int nzw = nz / 2, hx = nx / 2, hy = ny / 2;
     const int nk = min(TZ, nzw - z0);
-    if (ix >= h || iy >= h || ix > iy) return;
-    const bool diag = ix == iy;
+    if (ix >= hx || iy >= hy || (NR == 4 && ix > iy)) return;
+    const bool diag = NR == 4 && ix == iy;
     // P: the sums the turn slots feed, Q: the reflected slots' (rotated one
     // place per column, in opposite directions; exchanged between the C and
     // the D columns)
-    float2 P[4][TZ], Q[4][TZ];
+    float2 P[NR][TZ], Q[NR][TZ];
 #pragma unroll
-    for (int j = 0; j < 4; j++)
+    for (int j = 0; j < NR; j++)
 #pragma unroll
         for (int k = 0; k < TZ; k++) { P[j][k] = make_float2(0.0f, 0.0f); Q[j][k] = P[j][k]; }
     const float inv_dv = 1.0f / G.dv;
-    const long long vstride = (long long)nbw * na * 8;       // values per slot and plane
-    const long long half = (long long)ov * vstride;          // the reflected images' plane
-    const int nsteps = diag ? 4 : 8;
-    for (int w = 0; w <= ov; w++) {
-        const bool last = w == ov;
-        const int vt = last ? nv : w;                          // table row
-        const int alim = (w == 0 || last) ? na / 2 : na;       // walked columns
+    const int nsteps = diag ? NR : 2 * NR;
+    for (int w = 0; w <= g.ov; w++) {
+        int vt, rs, alim;
+        long long base;
+        refl_view(g, w, vt, base, rs, alim);
         const ViewEntry ve = view[vt];
         const ColEntry* cv = col + (long long)vt * na;
         const AxisEntry* rv = rowz + (long long)vt * nb;
-        const TW* yv = yw + (last ? 8LL * (na / 2) : (long long)w * vstride);
+        const TW* yv = yw + base;
         const float zr0 = (float)(z0 - nz / 2) * dz - ve.sz;
         const float zr1 = (float)(z0 + nk - nz / 2) * dz - ve.sz;
         const float tol = 1e-3f * dz;
@@ -1116,10 +1125,10 @@ k_adj_hex(TX* __restrict__ X, const TW* __restrict__ yw, const ColEntry* __restr
         int px = ix, py = iy;                                  // C_0
 #pragma unroll 1
         for (int k = 0; k < nsteps; k++) {
-            if (k == 4) {                                      // the D columns: D_0 = M V0
-                px = ix; py = n - 1 - iy;
+            if (k == NR) {                                     // the D columns: D_0 = M V0
+                px = ix; py = ny - 1 - iy;
 #pragma unroll
-                for (int j = 0; j < 4; j++)
+                for (int j = 0; j < NR; j++)
 #pragma unroll
                     for (int z = 0; z < TZ; z++) {
                         const float2 t = P[j][z];
@@ -1127,41 +1136,49 @@ k_adj_hex(TX* __restrict__ X, const TW* __restrict__ yw, const ColEntry* __restr
                     }
             }
             int alo, ahi; float dmin, dmax;
-            column_window(G, ve.c, ve.s, (float)(px - h), (float)(py - h), 1.0f, 1.0f, na, alo,
+            column_window(G, ve.c, ve.s, (float)(px - hx), (float)(py - hy), 1.0f, 1.0f, na, alo,
                           ahi, dmin, dmax);
             ahi = min(ahi, alim - 1);
             for (int ia = alo; ia <= ahi; ia++) {
                 if (!FL_IN(ia, na)) continue;
                 const ColEntry ce = cv[ia];
                 float bh, be, l, hh;
-                if (!cone_column(ce, px, py, n, n, bh, be, l, hh)) continue;
+                if (!cone_column(ce, px, py, nx, ny, bh, be, l, hh)) continue;
                 // absolute parameters of the column's ends (row windows only)
                 const float r1 = __fdividef(1.0f, __fadd_rn(bh, l) + ve.ac);
                 const float r2 = __fdividef(1.0f, __fadd_rn(bh, hh) + ve.ac);
                 const float s1 = dz * r1 * inv_dv, s2 = dz * r2 * inv_dv;
                 const float e1 = (zr0 * r1 - G.v0) * inv_dv, e2 = (zr0 * r2 - G.v0) * inv_dv;
-                const TW* yt = yv + 8 * ia;
+                const TW* yt = yv + g.vpr * ia;
                 if (mode < 0)
-                    adj_rows_hex<-1, TZ, RU, TW>(P, Q, nk, z0, l, hh, e1, e2, s1, s2, rv, bh, be,
-                                                 yt, yt + half, na, nbw);
+                    adj_rows_refl<-1, TZ, RU, TW, NR>(P, Q, nk, z0, l, hh, e1, e2, s1, s2, rv, bh,
+                                                      be, yt, yt + g.plane, rs, g.nbh);
                 else
-                    adj_rows_hex<0, TZ, RU, TW>(P, Q, nk, z0, l, hh, e1, e2, s1, s2, rv, bh, be,
-                                                yt, yt + half, na, nbw);
+                    adj_rows_refl<0, TZ, RU, TW, NR>(P, Q, nk, z0, l, hh, e1, e2, s1, s2, rv, bh,
+                                                     be, yt, yt + g.plane, rs, g.nbh);
             }
-            // next column R (px, py); P rotates back one place, Q forward one
-            const int t = px;
-            px = n - 1 - py; py = t;
+            // next column S (px, py); P rotates back one place, Q forward one
+            if (NR == 4) {
+                const int t = px;
+                px = nx - 1 - py; py = t;
+            } else {
+                px = nx - 1 - px; py = ny - 1 - py;
+            }
 #pragma unroll
             for (int z = 0; z < TZ; z++) {
                 const float2 a = P[0][z];
-                P[0][z] = P[1][z]; P[1][z] = P[2][z]; P[2][z] = P[3][z]; P[3][z] = a;
-                const float2 b = Q[3][z];
-                Q[3][z] = Q[2][z]; Q[2][z] = Q[1][z]; Q[1][z] = Q[0][z]; Q[0][z] = b;
+#pragma unroll
+                for (int j = 0; j + 1 < NR; j++) P[j][z] = P[j + 1][z];
+                P[NR - 1][z] = a;
+                const float2 b = Q[NR - 1][z];
+#pragma unroll
+                for (int j = NR - 1; j > 0; j--) Q[j][z] = Q[j - 1][z];
+                Q[0][z] = b;
             }
         }
         if (!diag) {                                           // C sums back into P
 #pragma unroll
-            for (int j = 0; j < 4; j++)
+            for (int j = 0; j < NR; j++)
 #pragma unroll
                 for (int z = 0; z < TZ; z++) {
                     const float2 t = P[j][z];
@@ -1169,37 +1186,43 @@ k_adj_hex(TX* __restrict__ X, const TW* __restrict__ yw, const ColEntry* __restr
                 }
         }
     }
-    // C_j = R^j V0 holds P[j] (and, on the diagonal, Q[j + 1], the sums of
-    // D_{j+1} = C_j); D_j = R^j M V0 holds Q[j]
-    const long long nn = (long long)n * n;
-    const int cx[4] = {ix, n - 1 - iy, n - 1 - ix, iy};
-    const int cy[4] = {iy, ix, n - 1 - iy, n - 1 - ix};
-    const int dxs[4] = {ix, iy, n - 1 - ix, n - 1 - iy};
-    const int dys[4] = {n - 1 - iy, ix, iy, n - 1 - ix};
+    // C_j = S^j V0 holds P[j] (and, on the diagonal of NR = 4, Q[j + 1], the
+    // sums of D_{j+1} = C_j); D_j = S^j M V0 holds Q[j]
+    const long long nxy = (long long)nx * ny;
+    int cx[NR], cy[NR], dxs[NR], dys[NR];
+    if (NR == 4) {
+        cx[0] = ix; cx[1] = nx - 1 - iy; cx[2] = nx - 1 - ix; cx[3] = iy;
+        cy[0] = iy; cy[1] = ix; cy[2] = ny - 1 - iy; cy[3] = ny - 1 - ix;
+        dxs[0] = ix; dxs[1] = iy; dxs[2] = nx - 1 - ix; dxs[3] = nx - 1 - iy;
+        dys[0] = ny - 1 - iy; dys[1] = ix; dys[2] = iy; dys[3] = ny - 1 - ix;
+    } else {
+        cx[0] = ix; cx[1] = nx - 1 - ix; cy[0] = iy; cy[1] = ny - 1 - iy;
+        dxs[0] = ix; dxs[1] = nx - 1 - ix; dys[0] = ny - 1 - iy; dys[1] = iy;
+    }
 #pragma unroll
     for (int k = 0; k < TZ; k++)
         if (k < nk) {
-            const long long zl = (long long)(z0 + k) * nn, zh = (long long)(nz - 1 - z0 - k) * nn;
+            const long long zl = (long long)(z0 + k) * nxy, zh = (long long)(nz - 1 - z0 - k) * nxy;
 #pragma unroll
-            for (int j = 0; j < 8; j++) {
-                if (diag && j >= 4) break;
+            for (int j = 0; j < 2 * NR; j++) {
+                if (diag && j >= NR) break;
                 float2 a;
                 int qx, qy;
-                if (j < 4) {
+                if (j < NR) {
                     a = P[j][k];
                     if (diag) {
-                        const float2 b = Q[(j + 1) & 3][k];
+                        const float2 b = Q[(j + 1) % NR][k];
                         a.x += b.x; a.y += b.y;
                     }
                     qx = cx[j]; qy = cy[j];
                 } else {
-                    a = Q[j - 4][k]; qx = dxs[j - 4]; qy = dys[j - 4];
+                    a = Q[j - NR][k]; qx = dxs[j - NR]; qy = dys[j - NR];
                 }
                 if (xfold) {                  // the tiled folded volume
-                    const long long t = tiled_pair(qx, qy, (int)zl, n >> 2);
+                    const long long t = tiled_pair(qx, qy, (int)zl, nx >> 2);
                     Store<TX>::st2(X + 2 * t, a.x, a.y);
                 } else {
-                    const long long c = (long long)qy * n + qx;
+                    const long long c = (long long)qy * nx + qx;
                     Store<TX>::st(X + zl + c, a.x);
                     Store<TX>::st(X + zh + c, a.y);
                 }
@@ -1312,11 +1335,17 @@ void launch_fwd(fl_plan* p, const void* x, void* y, int cr_power, const int* ski
 {
     const fl_scan& s = p->s;
     const dim3 fb = p->fwd_bx ? dim3(p->fwd_bx, p->fwd_by) : dim3(8, 16);
-    if (s.ndim == 3 && fl_plan_turns(p) == 8) {
-        dim3 grid(fl_div_up(s.na, fb.x), s.nv / 8, fl_div_up(s.nb / 2, fb.y));
-        k_fwd_hex<TX, TY><<<grid, fb, 0, st>>>(
-            (const TX*)x, (TY*)y, p->d_col, p->d_colr, p->d_row, s.nx, s.nz, s.na, s.nb, s.nv,
-            p->n_vox_frame, s.scale, cr_power, skip, xscale, yfold);
+    if (s.ndim == 3 && fl_plan_refl(p)) {
+        const int NR = fl_plan_refl(p);
+        const ReflGeom g = refl_geom(NR, s.nv, s.na, s.nb);
+        dim3 grid(fl_div_up(s.na, fb.x), g.slots, fl_div_up(s.nb / 2, fb.y));
+#define FL_FWD_REFL(NR_)                                                                     \
+    k_fwd_refl<TX, TY, NR_><<<grid, fb, 0, st>>>(                                            \
+        (const TX*)x, (TY*)y, p->d_col, p->d_colr, p->d_row, s.nx, s.ny, s.nz, s.na, s.nb, s.nv, \
+        p->n_vox_frame, s.scale, cr_power, skip, xscale, yfold)
+        if (NR == 4) FL_FWD_REFL(4);
+        else FL_FWD_REFL(2);
+#undef FL_FWD_REFL
     } else if (s.ndim == 3 && p->zmirror && p->rot && p->rot4) {
         dim3 grid(fl_div_up(s.na, fb.x), s.nv / 4, fl_div_up(s.nb / 2, fb.y));
         k_fwd_oct<TX, TY><<<grid, fb, 0, st>>>(
@@ -1379,25 +1408,31 @@ void launch_adj_cone(fl_plan* p, const TW* yw, void* x, const int* skip, int xfo
         constexpr int TZ = 8;
         const int nzw = p->zmirror ? s.nz / 2 : s.nz;
         int zruns = (nzw + TZ - 1) / TZ;
-        if (fl_plan_turns(p) == 8) {
-            // runs of 2 voxels (the eight columns' 32 accumulators) or of 1 (16
-            // accumulators); one or two rows per iteration, or (runs of 2) one
-            // pass over the run's rows: fl_plan_autotune
+        if (fl_plan_refl(p)) {
+            // runs of 2 voxels or of 1; one or two rows per iteration, or (runs
+            // of 2) one pass over the run's rows: fl_plan_autotune
+            const int NR = fl_plan_refl(p);
             const int run = p->adj_run == 1 ? 1 : 2;
             const int ru = p->adj_rows == 2 ? 2 : (p->adj_rows == 3 && run == 2 ? 0 : 1);
             zruns = (nzw + run - 1) / run;
             const dim3 ab = p->adj_bx ? dim3(p->adj_bx, p->adj_by) : dim3(8, 16);
             dim3 grid(fl_div_up(s.nx / 2, ab.x), fl_div_up(s.ny / 2, ab.y), (unsigned)zruns);
-#define FL_ADJ_HEX(TZ_, RU_)                                                                  \
-    k_adj_hex<TX, TZ_, RU_, TW><<<grid, ab, 0, st>>>((TX*)x, yw, p->d_col, p->d_rowz, p->d_view, \
-                                                     G, s.nx, s.nz, s.na, s.nb, s.nv, s.dz,     \
-                                                     skip, xfold)
-            if (run == 1 && ru == 1) FL_ADJ_HEX(1, 1);
-            else if (run == 1) FL_ADJ_HEX(1, 2);
-            else if (ru == 1) FL_ADJ_HEX(2, 1);
-            else if (ru == 2) FL_ADJ_HEX(2, 2);
-            else FL_ADJ_HEX(2, 0);
-#undef FL_ADJ_HEX
+#define FL_ADJ_REFL(TZ_, RU_, NR_)                                                             \
+    k_adj_refl<TX, TZ_, RU_, TW, NR_><<<grid, ab, 0, st>>>(                                     \
+        (TX*)x, yw, p->d_col, p->d_rowz, p->d_view, G, s.nx, s.ny, s.nz, s.na, s.nb, s.nv, s.dz, \
+        skip, xfold)
+#define FL_ADJ_REFL_NR(NR_)                                                                    \
+    do {                                                                                       \
+        if (run == 1 && ru == 1) FL_ADJ_REFL(1, 1, NR_);                                      \
+        else if (run == 1) FL_ADJ_REFL(1, 2, NR_);                                            \
+        else if (ru == 1) FL_ADJ_REFL(2, 1, NR_);                                             \
+        else if (ru == 2) FL_ADJ_REFL(2, 2, NR_);                                             \
+        else FL_ADJ_REFL(2, 0, NR_);                                                          \
+    } while (0)
+            if (NR == 4) FL_ADJ_REFL_NR(4);
+            else FL_ADJ_REFL_NR(2);
+#undef FL_ADJ_REFL_NR
+#undef FL_ADJ_REFL
         } else if (p->zmirror && p->rot && p->rot4) {
             // runs of 2: the four columns' 16 accumulators keep 8 blocks per SM
             constexpr int TO = 2;
@@ -1512,6 +1547,26 @@ void launch_weight_packed(fl_plan* p, const void* y, int yt, float* yw, cudaStre
                                                              s.nv, npk, s.scale);
 }
 
+template <int NR>
+void launch_weight_packed_refl(fl_plan* p, const void* y, int yt, float* yw, cudaStream_t st)
+{
+    const fl_scan& s = p->s;
+    const ReflGeom gm = refl_geom(NR, s.nv, s.na, s.nb);
+    const long long npk = (long long)gm.slots * gm.nbh * s.na;
+    const unsigned g = fl_div_up(npk, 256);
+    if (yt == FL_F32)
+        k_weight_packed_refl<float, NR><<<g, 256, 0, st>>>(yw, (const float*)y, p->d_colr,
+                                                           p->d_row, s.na, s.nb, s.nv, npk,
+                                                           s.scale);
+    else if (yt == FL_F16)
+        k_weight_packed_refl<__half, NR><<<g, 256, 0, st>>>(yw, (const __half*)y, p->d_colr,
+                                                            p->d_row, s.na, s.nb, s.nv, npk,
+                                                            s.scale);
+    else
+        k_weight_packed_refl<__nv_bfloat16, NR><<<g, 256, 0, st>>>(
+            yw, (const __nv_bfloat16*)y, p->d_colr, p->d_row, s.na, s.nb, s.nv, npk, s.scale);
+}
+
 template <int G>
 void launch_weight_fan_packed(fl_plan* p, const void* y, int yt, float* yw, cudaStream_t st)
 {
@@ -1568,21 +1623,9 @@ int fl_matched_weight(fl_plan* p, const void* y, int yt, float* yw, cudaStream_t
     const fl_scan& s = p->s;
     long long nr = p->n_rays;
     int three = s.ndim == 3;
-    if (three && fl_plan_turns(p) == 8) {
-        const long long npk = (long long)(s.nv / 8) * (s.nb / 2) * s.na;
-        const unsigned g = fl_div_up(npk, 256);
-        if (yt == FL_F32)
-            k_weight_packed_hex<float><<<g, 256, 0, st>>>(yw, (const float*)y, p->d_colr,
-                                                          p->d_row, s.na, s.nb, s.nv, npk,
-                                                          s.scale);
-        else if (yt == FL_F16)
-            k_weight_packed_hex<__half><<<g, 256, 0, st>>>(yw, (const __half*)y, p->d_colr,
-                                                           p->d_row, s.na, s.nb, s.nv, npk,
-                                                           s.scale);
-        else
-            k_weight_packed_hex<__nv_bfloat16><<<g, 256, 0, st>>>(
-                yw, (const __nv_bfloat16*)y, p->d_colr, p->d_row, s.na, s.nb, s.nv, npk,
-                s.scale);
+    if (three && fl_plan_refl(p)) {
+        if (fl_plan_refl(p) == 4) launch_weight_packed_refl<4>(p, y, yt, yw, st);
+        else launch_weight_packed_refl<2>(p, y, yt, yw, st);
         return fl_check_launch("matched adjoint weighting");
     }
     if (three && p->zmirror && p->rot) {
@@ -1695,7 +1738,7 @@ extern "C" int fl_plan_autotune(fl_plan* p, void* stream, int32_t* shapes)
         // thread with one or two rows per iteration, and runs of 2 in one pass
         // over their rows (variant r: run, rows)
         static const int var[5][2] = {{2, 1}, {1, 1}, {2, 2}, {1, 2}, {2, 3}};
-        const int nvar = fl_plan_turns(p) == 8 ? 5 : 1;
+        const int nvar = fl_plan_refl(p) ? 5 : 1;
         for (int pass = 0; pass < 2 && !st; pass++) {
             const bool fwd = pass == 0;
             float best = 3.0e38f;

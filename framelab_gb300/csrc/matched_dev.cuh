@@ -411,32 +411,40 @@ __device__ __forceinline__ void walk_oct(const TX* __restrict__ x, const ColEntr
     for (int j = 0; j < 4; j++) acc[j] = b.acc[j];
 }
 
-// The z-mirror walk with the quarter turns and the reflection (plan flag
-// rot8): per step the folded pairs of the voxel's eight images under the
-// square's symmetries, g_k = R^k (k < 4) and R^(k-4) M (k >= 4), M (x, y) =
-// (x, n-1-y), R (x, y) = (n-1-y, x); R M (x, y) = (y, x). acc[k] gets the
-// (voxel, mirror) sums of image k, the sums of the ray g_k takes the walked
-// ray to.
-template <typename TX>
-struct HexBody {
+// The z-mirror walk of a reflection form (fl_plan.h): NR = 4, the quarter
+// turns and the reflection (square grid); NR = 2, the half turn and the
+// reflection. Per step the folded pairs of the voxel's 2 NR images g_k =
+// R^(4k/NR) (k < NR) and R^(4(k-NR)/NR) M (k >= NR), with M (x, y) = (x,
+// ny-1-y), R (x, y) = (n-1-y, x), R^2 (x, y) = (nx-1-x, ny-1-y); R M (x, y) =
+// (y, x). acc[k] gets the (voxel, mirror) sums of image k, the sums of the ray
+// g_k takes the walked ray to.
+template <typename TX, int NR>
+struct ReflBody {
     const TX* __restrict__ x;
     long long xlen;
-    int n, nn, n4;
-    float2 acc[8], xv[8];
-    __device__ __forceinline__ void load(int jx, int jy, int jz, float2 (&o)[8]) const
+    int nx, ny, nxy, nx4;
+    float2 acc[2 * NR], xv[2 * NR];
+    __device__ __forceinline__ void load(int jx, int jy, int jz, float2 (&o)[2 * NR]) const
     {
-        const int zb = jz * nn, pi2 = 2 * zb + nn - 1;   // q -> pi2 - q: the turn by pi
-        int q[8];
-        q[0] = tiled_pair(jx, jy, zb, n4);
-        q[1] = tiled_pair(n - 1 - jy, jx, zb, n4);
-        q[4] = tiled_pair(jx, n - 1 - jy, zb, n4);
-        q[5] = tiled_pair(jy, jx, zb, n4);
-        q[2] = pi2 - q[0];
-        q[3] = pi2 - q[1];
-        q[6] = pi2 - q[4];
-        q[7] = pi2 - q[5];
+        const int zb = jz * nxy, pi2 = 2 * zb + nxy - 1;  // q -> pi2 - q: the turn by pi
+        int q[2 * NR];
+        if (NR == 4) {
+            q[0] = tiled_pair(jx, jy, zb, nx4);
+            q[1] = tiled_pair(nx - 1 - jy, jx, zb, nx4);
+            q[4] = tiled_pair(jx, ny - 1 - jy, zb, nx4);
+            q[5] = tiled_pair(jy, jx, zb, nx4);
+            q[2] = pi2 - q[0];
+            q[3] = pi2 - q[1];
+            q[6] = pi2 - q[4];
+            q[7] = pi2 - q[5];
+        } else {
+            q[0] = tiled_pair(jx, jy, zb, nx4);
+            q[2] = tiled_pair(jx, ny - 1 - jy, zb, nx4);
+            q[1] = pi2 - q[0];
+            q[3] = pi2 - q[2];
+        }
 #pragma unroll
-        for (int j = 0; j < 8; j++) {
+        for (int j = 0; j < 2 * NR; j++) {
             o[j] = make_float2(0.0f, 0.0f);
             if (FL_IN(2 * (long long)q[j] + 1, xlen)) o[j] = Store<TX>::ld2(x + 2 * (long long)q[j]);
         }
@@ -444,42 +452,103 @@ struct HexBody {
     __device__ __forceinline__ void at(int jx, int jy, int jz) { load(jx, jy, jz, xv); }
     __device__ __forceinline__ void take(float seg, bool more, int jx, int jy, int jz)
     {
-        float2 xn[8];
+        float2 xn[2 * NR];
 #pragma unroll
-        for (int j = 0; j < 8; j++) xn[j] = make_float2(0.0f, 0.0f);
+        for (int j = 0; j < 2 * NR; j++) xn[j] = make_float2(0.0f, 0.0f);
         if (more) load(jx, jy, jz, xn);
 #pragma unroll
-        for (int j = 0; j < 8; j++) {
+        for (int j = 0; j < 2 * NR; j++) {
             acc[j] = __ffma2_rn(make_float2(seg, seg), xv[j], acc[j]);
             xv[j] = xn[j];
         }
     }
 };
 
-template <typename TX>
-__device__ __forceinline__ void walk_hex(const TX* __restrict__ x, const ColEntry* ce,
-                                         const AxisEntry* pZ, int n, int nz, float2 (&acc)[8],
-                                         long long xlen)
+template <typename TX, int NR>
+__device__ __forceinline__ void walk_refl(const TX* __restrict__ x, const ColEntry* ce,
+                                          const AxisEntry* pZ, int nx, int ny, int nz,
+                                          float2 (&acc)[2 * NR], long long xlen)
 {
-    HexBody<TX> b;
-    b.x = x; b.xlen = xlen; b.n = n; b.nn = n * n; b.n4 = n >> 2;
+    ReflBody<TX, NR> b;
+    b.x = x; b.xlen = xlen; b.nx = nx; b.ny = ny; b.nxy = nx * ny; b.nx4 = nx >> 2;
 #pragma unroll
-    for (int j = 0; j < 8; j++) { b.acc[j] = make_float2(0.0f, 0.0f); b.xv[j] = b.acc[j]; }
-    if (__ldg(&pZ->ih) < 0.0f) seg_walk<true>(ce, pZ, n, n, nz / 2, b);
+    for (int j = 0; j < 2 * NR; j++) { b.acc[j] = make_float2(0.0f, 0.0f); b.xv[j] = b.acc[j]; }
+    if (__ldg(&pZ->ih) < 0.0f) seg_walk<true>(ce, pZ, nx, ny, nz / 2, b);
 #pragma unroll
-    for (int j = 0; j < 8; j++) acc[j] = b.acc[j];
+    for (int j = 0; j < 2 * NR; j++) acc[j] = b.acc[j];
 }
 
-// Walked view, table row and column of slot (s, ia) of a reflection plan
-// (fl_plan.h): slot s in [1, nv/8) is view s at column ia; slot 0 holds view
-// 0 at columns ia < na/2 and view nv/8 (its tables in row nv, the exact
-// diagonal angle) at columns ia - na/2.
-__device__ __forceinline__ void hex_slot(int s, int ia, int na, int nv, int& v, int& vt, int& a)
+// Views and input layout of a reflection form (fl_plan.h). The walked views
+// are w = 0 .. ov (ov = nv/8 for NR = 4, floor(nv/4) for NR = 2). View 0 walks
+// its columns a < na/2; so does view ov when it is its own mirror image ("end":
+// NR = 4, or NR = 2 with nv a multiple of 4), walked from table row endrow
+// (nv: the exact angle pi/4; nv + 1: the exact angle pi/2). The backprojection
+// input has two planes of nv nb na / 2 values (the turn images, the reflected
+// images), vpr = 2 NR values per walked ray and plane (NR images x two rows).
+// Per plane: with an end view, slots s < ov of nb/2 rows x na columns, slot 0
+// holding view 0 at columns < na/2 and view ov at columns >= na/2, slot s
+// view s; without one, slot s < ov holds view s + 1 and a half slot at the end
+// (rows of na/2 columns) view 0.
+struct ReflGeom {
+    int nv, na, nbh, ov, end, endrow, vpr, slots;   // slots: forward grid (whole and half)
+    long long slot, plane;                          // values per slot / per plane
+};
+
+__host__ __device__ inline ReflGeom refl_geom(int NR, int nv, int na, int nb)
 {
-    v = s; vt = s; a = ia;
-    if (s == 0 && ia >= na / 2) { v = nv / 8; vt = nv; a = ia - na / 2; }
+    ReflGeom g;
+    g.nv = nv; g.na = na; g.nbh = nb / 2;
+    g.ov = NR == 4 ? nv / 8 : nv / 4;
+    g.end = NR == 4 || nv % 4 == 0;
+    g.endrow = NR == 4 ? nv : nv + 1;
+    g.vpr = 2 * NR;
+    g.slots = g.end ? g.ov : g.ov + 1;
+    g.slot = (long long)g.nbh * na * g.vpr;
+    g.plane = (long long)nv * nb * na / 2;
+    return g;
 }
 
+// Forward slot (s, column ia) of a reflection form: the walked view v, its
+// table row vt and column a, and where its values go in each plane (offset
+// off + vpr (ib stride + ia) + 2 k for row ib, image k mod NR). False for the
+// unused half of the last slot.
+__device__ __forceinline__ bool refl_slot(const ReflGeom& g, int s, int ia, int& v, int& vt,
+                                          int& a, long long& off, int& stride)
+{
+    const int h = g.na / 2;
+    a = ia; stride = g.na;
+    if (g.end) {
+        off = s * g.slot;
+        v = vt = s;
+        if (s == 0 && ia >= h) { v = g.ov; vt = g.endrow; a = ia - h; }
+        return true;
+    }
+    if (s == g.ov) {
+        if (ia >= h) return false;
+        v = vt = 0; off = g.ov * g.slot; stride = h;
+        return true;
+    }
+    v = vt = s + 1; off = s * g.slot;
+    return true;
+}
+
+// Backprojection view w of a reflection form: table row, the plane offset of
+// its values (column ia, row ib at base + vpr (ib stride + ia)), and the
+// number of its walked columns.
+__device__ __forceinline__ void refl_view(const ReflGeom& g, int w, int& vt, long long& base,
+                                          int& stride, int& alim)
+{
+    const int h = g.na / 2;
+    stride = g.na; alim = g.na; vt = w;
+    if (g.end) {
+        base = w * g.slot;
+        if (w == 0) alim = h;
+        else if (w == g.ov) { vt = g.endrow; base = (long long)g.vpr * h; alim = h; }
+        return;
+    }
+    if (w == 0) { base = g.ov * g.slot; stride = h; alim = h; }
+    else base = (w - 1) * g.slot;
+}
 // The fan walk in batches of kFanBatch steps: the crossings of a batch are
 // found first (they do not depend on the image), then its gathers are issued
 // together and the segments added in walk order -- the same sums as the

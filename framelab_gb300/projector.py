@@ -139,8 +139,8 @@ class Plan:
     @property
     def reflect(self) -> bool:
         """Whether the matched pair also uses the reflection between views v
-        and nv - v about the x axis (FL_OPT_REFLECT; cone plans, needs the
-        quarter turn and a detector symmetric about its centre)."""
+        and nv - v about the x axis (FL_OPT_REFLECT; cone plans, with the half
+        or the quarter turn and a detector symmetric about its centre)."""
         v = C.c_int()
         _lib.check(self._L.fl_plan_query(self._h, _lib.OPT_REFLECT, C.byref(v)))
         return bool(v.value)
@@ -150,14 +150,18 @@ class Plan:
         _lib.check(self._L.fl_plan_option(self._h, _lib.OPT_REFLECT, int(bool(on))))
 
     @property
-    def views_per_walk(self) -> int:
-        """Views one walk or weight of the matched kernels in use serves: 8
-        (quarter turns and the reflection), 4, 2 or 1."""
-        if self.reflect:
-            return 8
+    def rotations(self) -> int:
+        """Turns of the matched kernels in use: 4 (quarter turns), 2 (half
+        turn) or 1."""
         if self.quarter_turn:
             return 4
         return 2 if self.rot_mirror else 1
+
+    @property
+    def views_per_walk(self) -> int:
+        """Views one walk or weight of the matched kernels in use serves: the
+        rotations, twice that with the reflection (8, 4, 2 or 1)."""
+        return self.rotations * (2 if self.reflect else 1)
 
     @property
     def handle(self):

@@ -55,27 +55,34 @@ def _three(gpu, ref, exact, exact_snapped=None) -> dict:
     return out
 
 
-def snapped(para, turns: int) -> dict:
-    """The scan a plan with `turns` views per walk projects: FP64 angles
-    phi[v + j nv/turns] = phi[v] + j 2 pi / turns for v < nv/turns (the FP32
-    angles of the walked views, turned exactly). turns = 8 is the quarter
-    turns with the reflection about the x axis: the walked views v = 0 ..
-    nv/8 (view nv/8 at exactly pi/4) turned by j pi/2 and reflected, view
-    j nv/4 - v at angle j pi/2 - phi[v]."""
+def snapped(para, turns: int, reflect: bool = False) -> dict:
+    """The scan a plan with `turns` views per rotation orbit projects: FP64
+    angles phi[v + j nv/turns] = phi[v] + j 2 pi / turns for v < nv/turns (the
+    FP32 angles of the walked views, turned exactly). With the reflection
+    about the x axis (reflect, or turns = 8 for the quarter turns with it),
+    the walked views are v = 0 .. floor(nv / (2 turns)) -- the last one at
+    exactly pi/turns where it is its own mirror image (nv a multiple of
+    2 turns) -- and view j nv/turns - v is view v reflected and turned, at
+    angle j 2 pi / turns - phi[v]."""
+    if turns == 8:
+        turns, reflect = 4, True
     if turns <= 1:
         return para
     phi = np.asarray(para["sd_phi"], np.float32).astype(np.float64)
-    if turns == 8:
-        nv = phi.size
-        q, o = nv // 4, nv // 8
-        base = np.concatenate([phi[:o], [np.pi / 4]])          # walked views 0 .. nv/8
+    nv = phi.size
+    q = nv // turns
+    if reflect:
+        ov = q // 2
+        base = phi[:ov + 1].copy()
+        if q % 2 == 0:
+            base[ov] = np.pi / turns                  # the end view, its own mirror image
         u = np.arange(nv)
-        j, v = u // q, u % q
-        refl = v > o
-        vv = np.where(refl, q - v, v)
-        p64 = np.where(refl, (j + 1) * (np.pi / 2) - base[vv], base[vv] + j * (np.pi / 2))
+        j, r = u // q, u % q
+        refl = r > ov
+        vv = np.where(refl, q - r, r)
+        step = 2.0 * np.pi / turns
+        p64 = np.where(refl, (j + 1) * step - base[vv], base[vv] + j * step)
     else:
-        q = phi.size // turns
         p64 = np.concatenate([phi[:q] + j * (2.0 * np.pi / turns) for j in range(turns)])
     out = dict(para)
     out["phi64"] = p64
@@ -86,10 +93,11 @@ def _threads(threads):
     return threads or max(1, os.cpu_count() or 1)
 
 
-def fan_parity(para, x, forward, adjoint, seed=0, threads=None, turns=1) -> dict:
+def fan_parity(para, x, forward, adjoint, seed=0, threads=None, turns=1,
+               reflect=False) -> dict:
     """Full fan-beam check: every ray, every pixel."""
     t = _threads(threads)
-    ps = snapped(para, turns) if turns > 1 else None
+    ps = snapped(para, turns, reflect) if turns > 1 else None
     x = np.ascontiguousarray(x, np.float32).reshape(-1)
     y = np.asarray(forward(x), np.float32).reshape(-1)
     out = {"forward": dict(rays=int(y.size), **_three(
@@ -105,10 +113,10 @@ def fan_parity(para, x, forward, adjoint, seed=0, threads=None, turns=1) -> dict
 
 
 def cone_parity(para, x, forward, adjoint, n_rays=20000, n_vox=4000, seed=0,
-                threads=None, turns=1) -> dict:
+                threads=None, turns=1, reflect=False) -> dict:
     """Cone-beam check on ``n_rays`` random rays and ``n_vox`` random voxels."""
     t = _threads(threads)
-    ps = snapped(para, turns) if turns > 1 else None
+    ps = snapped(para, turns, reflect) if turns > 1 else None
     rng = np.random.default_rng(seed)
     x = np.ascontiguousarray(x, np.float32).reshape(-1)
     y = np.asarray(forward(x), np.float32).reshape(-1)

@@ -26,11 +26,13 @@ def run_plan(p, rng):
         P.forward(x.to(dt))
         P.adjoint(y.to(dt))
     if P.cone:                         # every symmetry level the plan allows
-        for f, q, r, z in ((False, True, True, True), (False, False, True, True),
-                           (False, False, False, True), (False, False, False, False)):
+        for f, q, r, z in ((False, True, True, True), (True, False, True, True),
+                           (False, False, True, True), (False, False, False, True),
+                           (False, False, False, False)):
             P.reflect, P.quarter_turn, P.rot_mirror, P.z_mirror = f, q, r, z
             P.forward(x)
             P.adjoint(y)
+            P.adjoint(y.half())
         P.z_mirror, P.rot_mirror, P.quarter_turn, P.reflect = True, True, True, True
     else:                              # fan: half turn, then the general kernels
         for q, r in ((False, True), (False, False)):
@@ -55,6 +57,7 @@ def main():
                        voxel_mm=8.0),                                  # reflection, nv = 8
         G.cone_para_mm(32, 12, 48, 40, det_pitch_mm=8.0, SO_mm=600.0, SD_mm=1200.0,
                        voxel_mm=8.0),                                  # quarter turns
+        G.cone_para(32, 24, 16, 40, 36, 18, L=(2.0, 1.5, 1.0)),        # half turn, reflection
         G.cone_para_mm(28, 18, 44, 36, det_pitch_mm=8.0, SO_mm=600.0, SD_mm=1200.0,
                        voxel_mm=8.0),                                  # circle: half turn
         G.cone_para(16, 16, 16, 36, 32, 10, L=(2, 2, 2)),              # short SO, steep rows

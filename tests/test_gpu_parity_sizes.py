@@ -85,7 +85,7 @@ def test_fan256_full(field_mm):
     for P in _plans(p):
         t = _turns(P)
         forms.append(t)
-        _check(PAR.fan_parity(p, x, *_ops(P), turns=t), t)
+        _check(PAR.fan_parity(p, x, *_ops(P), turns=P.rotations, reflect=P.reflect), t)
     assert forms == [4, 1]
 
 
@@ -106,7 +106,7 @@ def test_cone_config_sizes_on_subsets(n):
         t = _turns(P)
         forms.append(t)
         res = PAR.cone_parity(p, x, *_ops(P), n_rays=20000, n_vox=4000 if n == 256 else 2000,
-                              turns=t)
+                              turns=P.rotations, reflect=P.reflect)
         del P
         torch.cuda.empty_cache()
         _check(res, t)

@@ -625,14 +625,19 @@ def test_reflection_is_detected_and_exact():
     n, nb, nv, na = int(p["nx"]), len(p["z_det"]), len(p["sd_phi"]), len(p["y_det"])
     P = _plan(p)
     assert P.reflect and P.views_per_walk == 8
-    P.quarter_turn = False                             # rides on the quarter turn
-    assert not P.reflect and P.views_per_walk == 2
+    P.quarter_turn = False                             # then with the half turn
+    assert P.reflect and P.views_per_walk == 4
+    P.rot_mirror = False                               # rides on a turn
+    assert not P.reflect and P.views_per_walk == 1
+    P.rot_mirror = True
     P.quarter_turn = True
-    assert P.reflect
+    assert P.reflect and P.views_per_walk == 8
     twelve = G.cone_para_mm(32, 12, 48, 40, det_pitch_mm=8.0, SO_mm=600.0, SD_mm=1200.0,
                             voxel_mm=8.0)              # quarter turns, nv/8 not whole
     Q = _plan(twelve)
     assert Q.quarter_turn and not Q.reflect
+    Q.quarter_turn = False                             # the half turn takes it
+    assert Q.reflect and Q.views_per_walk == 4
     off = G.cone_para(32, 32, 32, 48, 40, 16, L=(2, 2, 2), y_os=0.01)   # off-centre panel
     R = _plan(off)
     assert R.quarter_turn and not R.reflect
@@ -674,6 +679,51 @@ def test_reflection_is_detected_and_exact():
         u8 = cg.solve(b, iters=6)
         P.reflect = True
         assert _rel(_host(u16), _host(u8)) < tol, (mode, _rel(_host(u16), _host(u8)))
+
+
+@pytest.mark.parametrize("nx,ny,nv,quarter_off", [(32, 32, 18, False), (32, 32, 12, True),
+                                                  (32, 24, 14, False), (24, 32, 16, True)])
+def test_half_turn_reflection_is_exact(nx, ny, nv, quarter_off):
+    """The half turn with the reflection (eight rays per walk): nv = 18 and 14
+    have no end view (nv/4 not whole), 12 and 16 walk view nv/4 at exactly
+    pi/2; rectangular grids take it too."""
+    torch = _torch()
+    from framelab_gb300.solvers import NativeCGLS
+    import oracle.parity as PAR
+    nz, na, nb = 32, 48, 40
+    p = G.cone_para(nx, ny, nz, na, nb, nv, L=(2.0 * nx / 32, 2.0 * ny / 32, 2.0))
+    P = _plan(p)
+    if quarter_off:
+        P.quarter_turn = False
+    assert P.rot_mirror and not P.quarter_turn and P.reflect and P.views_per_walk == 4
+    rng = np.random.default_rng(nv)
+    x = rng.standard_normal(nx * ny * nz).astype(np.float32)
+    r = rng.standard_normal(P.n_rays).astype(np.float32)
+    y4, x4 = _host(P.forward(_dev(x))), _host(P.adjoint(_dev(r)))
+    P.reflect = False
+    y2, x2 = _host(P.forward(_dev(x))), _host(P.adjoint(_dev(r)))
+    P.reflect = True
+    assert _rel(y4, y2) < 1e-5 and _rel(x4, x2) < 1e-4, (_rel(y4, y2), _rel(x4, x2))
+    xv = x.reshape(nz, ny, nx)
+    # view nv - v (mod nv), column na-1-a of A x is view v, column a of A M(x)
+    ym = _host(P.forward(_dev(xv[:, ::-1, :].reshape(-1).copy()))).reshape(nv, nb, na)
+    idx = (nv - np.arange(nv)) % nv
+    assert np.array_equal(y4.reshape(nv, nb, na)[idx][:, :, ::-1], ym)
+    # views v + nv/2 of A x are views v of A turn(x), turn(x)[z, y, x] = x[z, ny-1-y, nx-1-x]
+    yt = _host(P.forward(_dev(xv[:, ::-1, ::-1].reshape(-1).copy()))).reshape(nv, nb, na)
+    assert np.array_equal(y4.reshape(nv, nb, na)[nv // 2:], yt[:nv // 2])
+    lhs = np.dot(y4.astype(np.float64), r.astype(np.float64))
+    rhs = np.dot(x.astype(np.float64), x4.astype(np.float64))
+    assert abs(lhs - rhs) / abs(lhs) < 1e-5
+    ps = PAR.snapped(p, 2, True)
+    assert _rel(y4, O.exact_forward(x, ps)) < 2e-6
+    assert _rel(x4, O.exact_adjoint(r, ps)) < 5e-6
+    b = P.adjoint(P.forward(_dev(np.abs(x)))).reshape(-1).contiguous()
+    cg = NativeCGLS(P, "graph")
+    u4 = cg.solve(b, iters=6).clone()
+    P.reflect = False
+    u2 = cg.solve(b, iters=6)
+    assert _rel(_host(u4), _host(u2)) < 1e-4
 
 
 def _fan_turn_para(n=48, ny=None, nv=40, phi=None, nd=96):
