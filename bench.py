@@ -427,7 +427,7 @@ def hbm_peak():
 
 
 def roofline_model(form):
-    """Per-intersection counts of one kernel form's pair ("hex": quarter turns
+    """Per-intersection counts of one kernel form's pair ("refl4": quarter turns
     with the reflection, "oct": quarter turns), or None."""
     try:
         with open(os.path.join(ROOT, "profiles", "roofline_model.json")) as fh:
@@ -736,7 +736,7 @@ def run_single(ctx, name, w, p):
         tf, ta, y, xo = time_pair(ctx, P, p32)
         roofline = projector_roofline(ctx, name, n_isect, P.n_rays, P.n_vox, tf, ta, detail,
                                       "matched", clocks.summary().get("sm_mhz"),
-                                      l1_form=({(4, True): "hex", (4, False): "oct"}
+                                      l1_form=({(4, True): "refl4", (4, False): "oct"}
                                                .get((P.rotations, P.reflect))
                                                if w["kind"] == "cone" else None))
         if w["kind"] == "cone":
