@@ -997,7 +997,7 @@ constexpr int kFanX = 32;
 // Parts per ray of the fan turn forward: kFanLanes for scans with fewer
 // than kFanSplitWalks walks (nv/G views x na columns), else 1. A function of
 // the scan alone, so a plan and a batch holding it choose alike.
-constexpr int kFanLanes = 8;
+constexpr int kFanLanes = 16;
 constexpr long long kFanSplitWalks = 1LL << 16;
 constexpr int kFanBlock = 256;       // threads per block of the fan turn forward
 
