@@ -782,6 +782,7 @@ def run_batch(ctx, name, w, paras):
     from framelab_gb300.solvers import NativeCGLS
     K, W, world = ctx.K, ctx.W, ctx.world
     B = FanBatch(paras)
+    parts = B.autotune()                  # parts per walked ray of the turn slices (untimed)
     x_true = B.concat_images([PH.ellipses_2d(P.nx, seed=100 + i)
                               for i, P in enumerate(B.plans)]).to(ctx.dev)
     sino = B.forward(x_true)
@@ -792,7 +793,8 @@ def run_batch(ctx, name, w, paras):
     del sino
     torch.cuda.synchronize()
     detail = {"slices": len(B), "n_vox": B.n_vox, "n_rays": B.n_rays,
-              "slices_by_turns": {str(t): B.turns.count(t) for t in (1, 2, 4)}}
+              "slices_by_turns": {str(t): B.turns.count(t) for t in (1, 2, 4)},
+              "turn_parts_per_ray": parts}
     if W:
         B.cgls(rhs, iters=W)
     clocks = ClockSampler(ctx.local)

@@ -24,6 +24,8 @@ OPT_QUARTER_TURN = 3
 OPT_REFLECT = 4
 TUNE_ADJ_RUN = 16
 TUNE_ADJ_ROWS = 17
+TUNE_FAN_PARTS = 18
+TUNE_FAN_BLOCK = 19
 FRAMELET_OPT_FUSED = 1
 
 
@@ -109,6 +111,7 @@ _SIGS = {
     "fl_batch_forward": (_I, [_P, _V, _V, _V]),
     "fl_batch_adjoint": (_I, [_P, _V, _V, _V]),
     "fl_batch_cgls": (_I, [_P, _V, _V, _F, C.c_int32, _D, C.c_int32, _V, _V, _V]),
+    "fl_batch_autotune": (_I, [_P, _V, _V]),
 }
 
 

@@ -34,9 +34,11 @@ def _stream():
 class FanBatch:
     """Many single-frame fan-beam scans projected and solved together."""
 
-    def __init__(self, paras, turns: bool = True):
+    def __init__(self, paras, turns: bool = True, fan_parts: int | None = None):
         """``turns=False`` keeps every slice on the general kernels (each
-        plan's half / quarter turn switched off before the batch is built)."""
+        plan's half / quarter turn switched off before the batch is built).
+        ``fan_parts`` (1, 4, 16) sets the parts per walked ray of every turn
+        slice's plan first (``Plan.set_tuning("fan_parts", ...)``)."""
         L = _lib.load()
         self.plans = [Plan(p) for p in paras]
         for i, P in enumerate(self.plans):
@@ -44,6 +46,8 @@ class FanBatch:
                 raise ValueError(f"slice {i} is not a fan-beam scan")
             if not turns:
                 P.rot_mirror = False
+            if fan_parts is not None:
+                P.set_tuning("fan_parts", fan_parts)
         # rays served per walk of each slice (4 quarter turn, 2 half turn, 1)
         self.turns = [4 if P.quarter_turn else (2 if P.rot_mirror else 1) for P in self.plans]
         n = len(self.plans)
@@ -61,6 +65,15 @@ class FanBatch:
 
     def __len__(self):
         return len(self.plans)
+
+    def autotune(self) -> int:
+        """Times the parts per walked ray of the turn slices (1, 4, 16) on this
+        batch's forward and keeps the fastest for all of them
+        (``fl_batch_autotune``); returns it (0 without turn slices). The
+        batch's forward then equals its plans' with that count set."""
+        v = C.c_int32()
+        _lib.check(self._L.fl_batch_autotune(self._h, _stream(), C.byref(v)))
+        return v.value
 
     @property
     def launches_per_iteration(self) -> int:

@@ -52,7 +52,7 @@ struct BatchSlice {
     DetGrid G;
     int nx, ny, na, nv;
     int turns;             // fl_plan_turns of the slice's plan at batch creation
-    int lanes;             // parts per walked ray (fan_turn_lanes)
+    int lanes;             // parts per walked ray (fl_plan_fan_lanes of the slice's plan)
     float scale;
     long long xoff, yoff;  // offsets of the slice in the concatenated image / sinogram
     long long woff;        // its offset in the batch's sinogram scratch (a multiple of
@@ -149,9 +149,11 @@ k_batch_fwd_turn(const float* __restrict__ X, float* __restrict__ Y,
 #define FL_BATCH_TURN(GG, LL)                                                                  \
     fan_turn_forward_block<float, float, GG, LL>(X + b.xoff, y, b.col, b.colr, b.nx, b.ny, b.na, \
                                                  b.nv, b.scale, cr_power, nullptr, ypack, ch.y)
-    if (b.turns == 4 && b.lanes > 1) FL_BATCH_TURN(4, kFanLanes);
+    if (b.turns == 4 && b.lanes == kFanLanes) FL_BATCH_TURN(4, kFanLanes);
+    else if (b.turns == 4 && b.lanes == 4) FL_BATCH_TURN(4, 4);
     else if (b.turns == 4) FL_BATCH_TURN(4, 1);
-    else if (b.lanes > 1) FL_BATCH_TURN(2, kFanLanes);
+    else if (b.lanes == kFanLanes) FL_BATCH_TURN(2, kFanLanes);
+    else if (b.lanes == 4) FL_BATCH_TURN(2, 4);
     else FL_BATCH_TURN(2, 1);
 #undef FL_BATCH_TURN
 }
@@ -356,7 +358,24 @@ struct fl_batch {
     float* cap_u;
     float cap_lam;
     double cap_tol;
+    std::vector<BatchSlice> h_sl;      // host copy of d_sl
+    std::vector<int> by_walk;          // slices, costliest walks first
+    int cap_rays_t;                    // capacity of d_rays_t (chunks)
 };
+
+// Chunks (slice, r0) of the turn slices' walked rays, kFanBlock / lanes rays each.
+static std::vector<int2> turn_ray_chunks(const std::vector<BatchSlice>& sl,
+                                         const std::vector<int>& by_walk)
+{
+    std::vector<int2> rays_t;
+    for (int i : by_walk) {
+        const BatchSlice& c = sl[i];
+        if (c.turns > 1)
+            for (int r = 0; r < c.na * (c.nv / c.turns); r += kFanBlock / c.lanes)
+                rays_t.push_back(make_int2(i, r));
+    }
+    return rays_t;
+}
 
 static void batch_free(fl_batch* b)
 {
@@ -416,7 +435,7 @@ extern "C" int fl_batch_create(fl_plan* const* plans, int32_t n_plans, fl_batch*
         b.G.rdu = 1.0f / p->du; b.G.rdg = p->dg != 0.0f ? 1.0f / p->dg : 0.0f;
         b.nx = s.nx; b.ny = s.ny; b.na = s.na; b.nv = s.nv; b.scale = s.scale;
         b.turns = fl_plan_turns(p);
-        b.lanes = b.turns > 1 ? fan_turn_lanes((long long)s.na * (s.nv / b.turns)) : 1;
+        b.lanes = b.turns > 1 ? fl_plan_fan_lanes(p) : 1;
         xoff[i + 1] = xoff[i] + (long long)s.nx * s.ny;
         yoff[i + 1] = yoff[i] + (long long)s.na * s.nv;
         woff[i + 1] = woff[i] + ((long long)s.na * s.nv + 3) / 4 * 4;
@@ -432,15 +451,22 @@ extern "C" int fl_batch_create(fl_plan* const* plans, int32_t n_plans, fl_batch*
     std::stable_sort(by_views.begin(), by_views.end(), [&](int a, int c) {
         return sl[a].nvf > sl[c].nvf;
     });
-    std::vector<int2> rays, rays_t, wrays;
+    std::vector<int2> rays, wrays;
     for (int i : by_walk) {
         const BatchSlice& c = sl[i];
         for (int r = 0; r < c.na * c.nv; r += kRayChunk) wrays.push_back(make_int2(i, r));
         if (c.turns == 1)
             for (int r = 0; r < c.na * c.nv; r += kRayChunk) rays.push_back(make_int2(i, r));
-        else
-            for (int r = 0; r < c.na * (c.nv / c.turns); r += kFanBlock / c.lanes)
-                rays_t.push_back(make_int2(i, r));
+    }
+    // room for the largest turn-ray list (16 parts per ray), which
+    // fl_batch_autotune may choose
+    std::vector<int2> rays_t = turn_ray_chunks(sl, by_walk);
+    size_t cap_t = rays_t.size();
+    {
+        std::vector<BatchSlice> s16 = sl;
+        for (BatchSlice& c : s16)
+            if (c.turns > 1) c.lanes = kFanLanes;
+        cap_t = std::max(cap_t, turn_ray_chunks(s16, by_walk).size());
     }
     std::vector<int4> pix, pix_t;
     for (int i : by_views) {
@@ -464,7 +490,7 @@ extern "C" int fl_batch_create(fl_plan* const* plans, int32_t n_plans, fl_batch*
         sl[i].vc1 = (int)vec.size();
     }
     if (wrays.size() > 0x7fffffffu || pix.size() + pix_t.size() > 0x7fffffffu ||
-        vec.size() > 0x7fffffffu)
+        vec.size() > 0x7fffffffu || cap_t > 0x7fffffffu)
         return fl_set_error(FL_ERR_UNSUPPORTED, "fl_batch_create: batch too large");
 
     fl_batch* b = new (std::nothrow) fl_batch;
@@ -478,13 +504,20 @@ extern "C" int fl_batch_create(fl_plan* const* plans, int32_t n_plans, fl_batch*
     b->cs = nullptr; b->ev0 = b->ev1 = nullptr; b->exec = nullptr; b->cap_u = nullptr;
     b->cs2 = nullptr; b->evf = b->evj = nullptr;
     b->cap_lam = 0.0f; b->cap_tol = 0.0;
+    b->h_sl = sl; b->by_walk = by_walk; b->cap_rays_t = (int)cap_t;
     b->n_ray_chunks = (int)rays.size(); b->n_pix_chunks = (int)pix.size();
     b->n_ray_t_chunks = (int)rays_t.size(); b->n_wray_chunks = (int)wrays.size();
     b->n_pix_t_chunks = (int)pix_t.size();
     b->n_vec_chunks = (int)vec.size();
     int st = upload_vec(&b->d_sl, sl);
     if (!st) st = upload_vec(&b->d_rays, rays);
-    if (!st) st = upload_vec(&b->d_rays_t, rays_t);
+    if (!st) {
+        st = fl_check_cuda(fl_malloc((void**)&b->d_rays_t, sizeof(int2) * (cap_t ? cap_t : 1)),
+                           "fl_malloc(batch)");
+        if (!st && !rays_t.empty())
+            st = fl_check_cuda(cudaMemcpy(b->d_rays_t, rays_t.data(), sizeof(int2) * rays_t.size(),
+                                          cudaMemcpyHostToDevice), "upload");
+    }
     if (!st) st = upload_vec(&b->d_wrays, wrays);
     if (!st) st = upload_vec(&b->d_pix, pix);
     if (!st) st = upload_vec(&b->d_pix_t, pix_t);
@@ -594,6 +627,70 @@ extern "C" int fl_batch_adjoint(fl_batch* b, const float* y, float* x, void* str
     int st = fl_check_launch("batched weighting");
     if (!st) st = batch_adj_w(b, b->tmp, x, nullptr, s);
     return st ? st : fl_set_error(FL_OK, "");
+}
+
+// Sets every turn slice's parts per walked ray to L and rebuilds the turn
+// forward's work list (kFanBlock / L rays per chunk).
+static int batch_set_lanes(fl_batch* b, int L, cudaStream_t s)
+{
+    for (BatchSlice& c : b->h_sl)
+        if (c.turns > 1) c.lanes = L;
+    const std::vector<int2> rays_t = turn_ray_chunks(b->h_sl, b->by_walk);
+    if ((long long)rays_t.size() > b->cap_rays_t)
+        return fl_set_error(FL_ERR_INVALID, "fl_batch_autotune: work list beyond its room");
+    FL_CUDA(cudaMemcpyAsync(b->d_sl, b->h_sl.data(), sizeof(BatchSlice) * b->h_sl.size(),
+                            cudaMemcpyHostToDevice, s));
+    if (!rays_t.empty())
+        FL_CUDA(cudaMemcpyAsync(b->d_rays_t, rays_t.data(), sizeof(int2) * rays_t.size(),
+                                cudaMemcpyHostToDevice, s));
+    FL_CUDA(cudaStreamSynchronize(s));         // the host vectors go out of scope
+    b->n_ray_t_chunks = (int)rays_t.size();
+    if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }   // recaptured
+    return FL_OK;
+}
+
+// Parts per walked ray of the batch's turn slices: each count (1, 4, 16) is
+// timed on the batch's own forward of a CGLS iteration (CUDA events, one
+// launch after one untimed; the batch's q and scratch as input and output)
+// and the fastest kept for every turn slice. Alone, a small scan needs parts
+// to fill the GPU; in a batch its neighbours may already fill it.
+extern "C" int fl_batch_autotune(fl_batch* b, void* stream, int32_t* parts)
+{
+    FL_RANGE("fl_batch_autotune");
+    if (!b) return fl_set_error(FL_ERR_INVALID, "fl_batch_autotune: null batch");
+    bool any = false;
+    for (const BatchSlice& c : b->h_sl) any |= c.turns > 1;
+    if (parts) *parts = 0;
+    if (!any) return fl_set_error(FL_OK, "");
+    cudaStream_t s = (cudaStream_t)stream;
+    FL_CUDA(cudaMemsetAsync(b->q, 0, sizeof(float) * b->n_vox, s));
+    cudaEvent_t e0, e1;
+    FL_CUDA(cudaEventCreate(&e0));
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return fl_set_error(FL_ERR_CUDA, "fl_batch_autotune: cudaEventCreate failed");
+    }
+    static const int cand[3] = {1, 4, kFanLanes};
+    float best = 3.0e38f;
+    int bi = -1, st = FL_OK;
+    for (int c = 0; c < 3 && !st; c++) {
+        if ((st = batch_set_lanes(b, cand[c], s))) break;
+        for (int rep = 0; rep < 2 && !st; rep++) {
+            if (rep == 1 && cudaEventRecord(e0, s) != cudaSuccess) st = FL_ERR_CUDA;
+            if (!st) st = batch_fwd(b, b->q, b->tmp, 2, 1, nullptr, s);
+        }
+        float ms = 0.0f;
+        if (!st && (cudaEventRecord(e1, s) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                    cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))
+            st = fl_set_error(FL_ERR_CUDA, "fl_batch_autotune: timing failed");
+        if (!st && ms < best) { best = ms; bi = c; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st) return st;
+    if ((st = batch_set_lanes(b, cand[bi], s))) return st;
+    if (parts) *parts = cand[bi];
+    return fl_set_error(FL_OK, "");
 }
 
 static int batch_iteration(fl_batch* b, float* u, float lam, double tol, cudaStream_t s)

@@ -122,6 +122,10 @@ struct fl_plan {
     // its row loop: 1 or 2 rows per iteration, 3 one pass over the run's rows
     // (runs of 2; 0 = 1)
     int adj_run, adj_rows;
+    // fan plans: parts per walked ray of the turn forward (1, 4 or 16; 0 =
+    // the scan's default, fl_plan_fan_lanes) and pixels per thread side of
+    // the backprojections (1 or 2; 0 = 2 once there are 4 waves of blocks)
+    int fan_lanes, fan_block;
     // scale of an FP16 backprojection input (the mixed CGLS form): the largest
     // power of two with y16_scale * c_r^2 <= 1 for every ray, so c_r^2 * (a
     // ray's sum of w p) stays within FP16's range whenever |p| does
@@ -196,6 +200,15 @@ enum {
     FL_LAY_X_FOLDED = 1,   // the volume operand is z-folded
     FL_LAY_Y_ADJ = 2       // the forward writes the adjoint-input layout
 };
+
+// Parts per walked ray of a fan turn plan's forward: the plan's setting
+// (FL_TUNE_FAN_PARTS), else 16 for scans of fewer than 65,536 walks and 1
+// above (a batch takes its slices' values when it is built).
+int fl_plan_fan_lanes(const fl_plan* p);
+// Pixels per thread side of a fan plan's backprojection (1 or 2): the plan's
+// setting (FL_TUNE_FAN_BLOCK), else 2 once the 2 x 2 blocks make four waves
+// of thread blocks on 152 SMs.
+int fl_plan_fan_block(const fl_plan* p);
 
 // internal launchers
 int fl_ref_forward(fl_plan* p, const float* x, float* y, cudaStream_t st);

@@ -340,6 +340,18 @@ extern "C" int fl_plan_option(fl_plan* p, int option, int value)
         (option == FL_TUNE_ADJ_RUN ? p->adj_run : p->adj_rows) = value;
         return fl_set_error(FL_OK, "");
     }
+    if (option == FL_TUNE_FAN_PARTS) {
+        if (value != 1 && value != 4 && value != 16)
+            return fl_set_error(FL_ERR_INVALID, "fl_plan_option: %d parts (1, 4 or 16)", value);
+        p->fan_lanes = value;
+        return fl_set_error(FL_OK, "");
+    }
+    if (option == FL_TUNE_FAN_BLOCK) {
+        if (value != 1 && value != 2)
+            return fl_set_error(FL_ERR_INVALID, "fl_plan_option: pixel block %d (1 or 2)", value);
+        p->fan_block = value;
+        return fl_set_error(FL_OK, "");
+    }
     return fl_set_error(FL_ERR_INVALID, "fl_plan_option: unknown option %d", option);
 }
 
@@ -369,6 +381,14 @@ extern "C" int fl_plan_query(const fl_plan* p, int option, int* value)
     }
     if (option == FL_TUNE_ADJ_ROWS) {
         *value = p->adj_rows ? p->adj_rows : 1;
+        return fl_set_error(FL_OK, "");
+    }
+    if (option == FL_TUNE_FAN_PARTS) {
+        *value = fl_plan_fan_lanes(p);
+        return fl_set_error(FL_OK, "");
+    }
+    if (option == FL_TUNE_FAN_BLOCK) {
+        *value = fl_plan_fan_block(p);
         return fl_set_error(FL_OK, "");
     }
     return fl_set_error(FL_ERR_INVALID, "fl_plan_query: unknown option %d", option);

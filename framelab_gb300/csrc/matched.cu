@@ -1329,6 +1329,33 @@ DetGrid det_grid(const fl_plan* p)
     return G;
 }
 
+}  // namespace
+
+// Tunables of fan plans (fl_plan.h).
+int fl_plan_fan_lanes(const fl_plan* p)
+{
+    if (p->fan_lanes) return p->fan_lanes;
+    const int G = fl_plan_turns(p);
+    return G > 1 ? fan_turn_lanes((long long)p->s.na * (p->s.nv / G)) : 1;
+}
+
+int fl_plan_fan_block(const fl_plan* p)
+{
+    if (p->fan_block) return p->fan_block;
+    const fl_scan& s = p->s;
+    const int T = fl_plan_turns(p);
+    long long blocks2;
+    if (T > 1) {
+        const int hx = T == 2 ? s.nx : s.nx / 2, hy = s.ny / 2;
+        blocks2 = (long long)fl_div_up(hx, 2 * kFanX) * fl_div_up(hy, 2);
+    } else {
+        blocks2 = (long long)fl_div_up(s.nx, 2 * 128) * ((s.ny + 1) / 2) * s.nt;
+    }
+    return blocks2 >= 4LL * 152 ? 2 : 1;
+}
+
+namespace {
+
 template <typename TX, typename TY>
 void launch_fwd(fl_plan* p, const void* x, void* y, int cr_power, const int* skip,
                 const float* xscale, int yfold, cudaStream_t st)
@@ -1369,15 +1396,17 @@ void launch_fwd(fl_plan* p, const void* x, void* y, int cr_power, const int* ski
     } else if (fl_plan_turns(p) > 1) {
         const int G = fl_plan_turns(p);
         const long long nr = (long long)s.na * (s.nv / G);
-        const bool split = fan_turn_lanes(nr) > 1;
-        const unsigned g = fl_div_up(nr, split ? kFanBlock / kFanLanes : kFanBlock);
+        const int lanes = fl_plan_fan_lanes(p);
+        const unsigned g = fl_div_up(nr, kFanBlock / lanes);
 #define FL_FAN_TURN(GG, LL)                                                                  \
     k_fwd_fan_turn<TX, TY, GG, LL><<<g, kFanBlock, 0, st>>>(                                 \
         (const TX*)x, (TY*)y, p->d_col, p->d_colr, s.nx, s.ny, s.na, s.nv, s.scale, cr_power, \
         skip, xscale, yfold)
-        if (G == 4 && split) FL_FAN_TURN(4, kFanLanes);
+        if (G == 4 && lanes == kFanLanes) FL_FAN_TURN(4, kFanLanes);
+        else if (G == 4 && lanes == 4) FL_FAN_TURN(4, 4);
         else if (G == 4) FL_FAN_TURN(4, 1);
-        else if (split) FL_FAN_TURN(2, kFanLanes);
+        else if (lanes == kFanLanes) FL_FAN_TURN(2, kFanLanes);
+        else if (lanes == 4) FL_FAN_TURN(2, 4);
         else FL_FAN_TURN(2, 1);
 #undef FL_FAN_TURN
     } else {
@@ -1482,7 +1511,7 @@ void launch_adj(fl_plan* p, const float* yw, void* x, const int* skip, int xfold
         const int hx = T == 2 ? s.nx : s.nx / 2, hy = s.ny / 2;
         const dim3 blk(kFanX, kTurnGroups);
         const dim3 g2(fl_div_up(hx, 2 * kFanX), fl_div_up(hy, 2)), g1(fl_div_up(hx, kFanX), hy);
-        const bool two = (long long)g2.x * g2.y >= 4LL * 152;
+        const bool two = fl_plan_fan_block(p) == 2;
         if (T == 4 && two)
             k_adj_fan_turn<TX, 4, 2><<<g2, blk, 0, st>>>((TX*)x, yw, p->d_col, p->d_view, G, s.nx,
                                                          s.ny, s.na, s.nv, skip);
@@ -1498,8 +1527,7 @@ void launch_adj(fl_plan* p, const float* yw, void* x, const int* skip, int xfold
     } else {
         // 2 x 2 pixel blocks, one thread each, once there are at least 4 waves
         // of 128-thread blocks; else one pixel per view group
-        const long long blocks2 = (long long)fl_div_up(s.nx, 2 * 128) * ((s.ny + 1) / 2) * s.nt;
-        if (blocks2 >= 4LL * 152) {
+        if (fl_plan_fan_block(p) == 2) {
             dim3 grid(fl_div_up(s.nx, 2 * 128), (s.ny + 1) / 2, s.nt);
             k_adj_fan<TX, 2, false><<<grid, 128, 0, st>>>((TX*)x, yw, p->d_col, p->d_view,
                                                            p->d_idY, p->d_Nv, p->tmp_size, G,
@@ -1692,48 +1720,57 @@ int fl_matched_adjoint_wt(fl_plan* p, const void* yw, int wt, void* x, int xt, c
     return fl_check_launch("matched adjoint (FP16 input)");
 }
 
-// Launch-shape autotuner of the cone projector kernels: each 128-thread shape
+// Launch-shape autotuner of the matched projector kernels: each candidate
 // below is timed (CUDA events, one launch after one untimed) on the plan's own
 // geometry, with the plan's scratch as input and output, and the fastest kept
-// for the forward and for the backprojection (for the reflection
-// backprojection, with runs of 1 or 2 voxels per thread and 1 or 2 rows per
-// iteration or one pass over a run's rows). A thread's result does not depend
-// on these, so neither do the projections. Fan plans keep theirs.
+// for the forward and for the backprojection.
+// * Cone plans: the 128-thread block shapes of both kernels, and for the
+//   reflection backprojection runs of 1 or 2 voxels per thread with 1 or 2
+//   rows per iteration or one pass over a run's rows. A thread's result does
+//   not depend on these, so neither do the projections.
+// * Fan plans: the parts per walked ray of the turn forward (1, 4, 16: the
+//   order of a ray's additions, within FP32 rounding) and the pixel block of
+//   the backprojections (1 or 2: the same bits).
 extern "C" int fl_plan_autotune(fl_plan* p, void* stream, int32_t* shapes)
 {
     FL_RANGE("fl_plan_autotune");
     if (!p) return fl_set_error(FL_ERR_INVALID, "fl_plan_autotune: null plan");
     int st = fl_matched_ready(p);
     if (st) return st;
-    if (p->s.ndim == 3 && p->det_kind >= 0) {
-        cudaStream_t s = (cudaStream_t)stream;
-        float* y = nullptr;
-        void* x = nullptr;
-        if ((st = fl_plan_work(p, &y))) return st;
-        if ((st = fl_plan_vwork(p, (size_t)p->n_vox * sizeof(float), &x))) return st;
-        FL_CUDA(cudaMemsetAsync(y, 0, (size_t)p->n_rays * sizeof(float), s));
-        FL_CUDA(cudaMemsetAsync(x, 0, (size_t)p->n_vox * sizeof(float), s));
-        const int lay = p->zmirror ? FL_LAY_X_FOLDED : 0;
-        static const int cand[4][2] = {{8, 16}, {16, 8}, {32, 4}, {4, 32}};
-        cudaEvent_t e0, e1;
-        FL_CUDA(cudaEventCreate(&e0));
-        if (cudaEventCreate(&e1) != cudaSuccess) {
-            cudaEventDestroy(e0);
-            return fl_set_error(FL_ERR_CUDA, "fl_plan_autotune: cudaEventCreate failed");
+    const bool cone = p->s.ndim == 3;
+    if (p->det_kind < 0 || (cone && p->det_kind == 1)) {   // no matched backprojection
+        if (shapes) shapes[0] = shapes[1] = shapes[2] = shapes[3] = 0;
+        return fl_set_error(FL_OK, "");
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    float* y = nullptr;
+    void* x = nullptr;
+    if ((st = fl_plan_work(p, &y))) return st;
+    if ((st = fl_plan_vwork(p, (size_t)p->n_vox * sizeof(float), &x))) return st;
+    FL_CUDA(cudaMemsetAsync(y, 0, (size_t)p->n_rays * sizeof(float), s));
+    FL_CUDA(cudaMemsetAsync(x, 0, (size_t)p->n_vox * sizeof(float), s));
+    const int lay = p->zmirror ? FL_LAY_X_FOLDED : 0;
+    cudaEvent_t e0, e1;
+    FL_CUDA(cudaEventCreate(&e0));
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return fl_set_error(FL_ERR_CUDA, "fl_plan_autotune: cudaEventCreate failed");
+    }
+    auto timed = [&](bool fwd, float& ms) -> int {
+        for (int rep = 0; rep < 2; rep++) {
+            if (rep == 1 && cudaEventRecord(e0, s) != cudaSuccess) return FL_ERR_CUDA;
+            int e = fwd ? fl_matched_forward(p, x, FL_F32, y, FL_F32, 2, nullptr, nullptr,
+                                             lay | FL_LAY_Y_ADJ, s)
+                        : fl_matched_adjoint_w(p, y, x, FL_F32, nullptr, lay, s);
+            if (e) return e;
         }
-        auto timed = [&](bool fwd, float& ms) -> int {
-            for (int rep = 0; rep < 2; rep++) {
-                if (rep == 1 && cudaEventRecord(e0, s) != cudaSuccess) return FL_ERR_CUDA;
-                int e = fwd ? fl_matched_forward(p, x, FL_F32, y, FL_F32, 2, nullptr, nullptr,
-                                                 lay | FL_LAY_Y_ADJ, s)
-                            : fl_matched_adjoint_w(p, y, x, FL_F32, nullptr, lay, s);
-                if (e) return e;
-            }
-            if (cudaEventRecord(e1, s) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
-                cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
-                return fl_set_error(FL_ERR_CUDA, "fl_plan_autotune: timing failed");
-            return FL_OK;
-        };
+        if (cudaEventRecord(e1, s) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+            cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
+            return fl_set_error(FL_ERR_CUDA, "fl_plan_autotune: timing failed");
+        return FL_OK;
+    };
+    if (cone) {
+        static const int cand[4][2] = {{8, 16}, {16, 8}, {32, 4}, {4, 32}};
         // the reflection backprojection also tries voxel runs of 2 and 1 per
         // thread with one or two rows per iteration, and runs of 2 in one pass
         // over their rows (variant r: run, rows)
@@ -1760,16 +1797,38 @@ extern "C" int fl_plan_autotune(fl_plan* p, void* stream, int32_t* shapes)
                 p->adj_run = var[br][0]; p->adj_rows = var[br][1];
             }
         }
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
-        if (st) {                         // keep the built-in shapes after a failure
-            p->fwd_bx = p->fwd_by = p->adj_bx = p->adj_by = p->adj_run = p->adj_rows = 0;
-            return st;
+        if (st) p->fwd_bx = p->fwd_by = p->adj_bx = p->adj_by = p->adj_run = p->adj_rows = 0;
+    } else {
+        static const int parts[3] = {1, 4, 16};
+        const bool turn = fl_plan_turns(p) > 1;
+        for (int pass = 0; pass < 2 && !st; pass++) {
+            const bool fwd = pass == 0;
+            if (fwd && !turn) continue;            // the general forward has no parts
+            float best = 3.0e38f;
+            int bi = 0;
+            for (int c = 0; c < (fwd ? 3 : 2) && !st; c++) {
+                if (fwd) p->fan_lanes = parts[c];
+                else p->fan_block = c + 1;
+                float ms = 0.0f;
+                st = timed(fwd, ms);
+                if (!st && ms < best) { best = ms; bi = c; }
+            }
+            if (fwd) p->fan_lanes = parts[bi];
+            else p->fan_block = bi + 1;
         }
+        if (st) p->fan_lanes = p->fan_block = 0;
     }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st) return st;                    // the built-in shapes are kept after a failure
     if (shapes) {
-        shapes[0] = p->fwd_bx; shapes[1] = p->fwd_by;
-        shapes[2] = p->adj_bx; shapes[3] = p->adj_by;
+        if (cone) {
+            shapes[0] = p->fwd_bx; shapes[1] = p->fwd_by;
+            shapes[2] = p->adj_bx; shapes[3] = p->adj_by;
+        } else {
+            shapes[0] = fl_plan_fan_lanes(p); shapes[1] = 0;
+            shapes[2] = fl_plan_fan_block(p); shapes[3] = 0;
+        }
     }
     return fl_set_error(FL_OK, "");
 }

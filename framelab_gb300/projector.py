@@ -163,6 +163,20 @@ class Plan:
         rotations, twice that with the reflection (8, 4, 2 or 1)."""
         return self.rotations * (2 if self.reflect else 1)
 
+    # launch variants fl_plan_autotune chooses among (fl_plan_option values)
+    TUNABLES = {"adj_run": _lib.TUNE_ADJ_RUN, "adj_rows": _lib.TUNE_ADJ_ROWS,
+                "fan_parts": _lib.TUNE_FAN_PARTS, "fan_block": _lib.TUNE_FAN_BLOCK}
+
+    def tuning(self, name: str) -> int:
+        """The value in effect of a launch variant (``TUNABLES``)."""
+        v = C.c_int()
+        _lib.check(self._L.fl_plan_query(self._h, self.TUNABLES[name], C.byref(v)))
+        return v.value
+
+    def set_tuning(self, name: str, value: int):
+        """Sets a launch variant (``TUNABLES``); values outside its set raise."""
+        _lib.check(self._L.fl_plan_option(self._h, self.TUNABLES[name], int(value)))
+
     @property
     def handle(self):
         return self._h
@@ -217,15 +231,20 @@ class Plan:
         return (y, yn) if yn is not None else y
 
     def autotune(self, stream=None) -> dict:
-        """Times the block shapes of this cone plan's matched projector kernels
-        on its own geometry and keeps the fastest (``fl_plan_autotune``; the
-        projections do not change). Returns the chosen shapes (and, on a
-        reflection plan, the backprojection's voxels per thread); fan plans
-        report ``None`` and keep theirs."""
+        """Times the launch variants of this plan's matched projector kernels
+        on its own geometry and keeps the fastest (``fl_plan_autotune``).
+        Cone plans: the block shapes (and, on a reflection plan, the
+        backprojection's voxels per thread and row loop); the projections do
+        not change. Fan plans: the parts per walked ray of the turn forward
+        (the order of a ray's additions) and the backprojection's pixel block
+        (the same bits). Plans without a matched backprojection report
+        ``None``."""
         sh = (C.c_int32 * 4)()
         _lib.check(self._L.fl_plan_autotune(self._h, _stream(stream), sh))
         if not sh[0]:
             return {"forward": None, "adjoint": None}
+        if not self.cone:
+            return {"forward_parts_per_ray": sh[0], "adjoint_pixel_block": sh[2]}
         out = {"forward": (sh[0], sh[1]), "adjoint": (sh[2], sh[3])}
         if self.reflect:
             v = C.c_int()

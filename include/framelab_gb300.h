@@ -221,14 +221,18 @@ enum { FL_OPT_Z_MIRROR = 1, FL_OPT_ROT_MIRROR = 2, FL_OPT_QUARTER_TURN = 3,
        FL_OPT_REFLECT = 4 };
 int fl_plan_option(fl_plan *plan, int option, int value);
 int fl_plan_query(const fl_plan *plan, int option, int *value);
-/* Launch-shape autotuner for a cone plan's matched projector kernels: times
- * each 128-thread block shape (8x16, 16x8, 32x4, 4x32) on the plan's own
- * geometry, one launch each on `stream` after one untimed, and keeps the
- * fastest for the forward and for the backprojection. The results of the
- * projectors do not depend on the shape (nor on the voxel run of the
- * reflection backprojection, which it tunes too). Synchronises `stream`; uses the
- * plan's scratch buffers. shapes (optional, [4]): the chosen forward x, y and
- * backprojection x, y (0 for fan plans, which keep their shapes). */
+/* Launch-shape autotuner for a plan's matched projector kernels: times each
+ * candidate on the plan's own geometry, one launch each on `stream` after one
+ * untimed, and keeps the fastest for the forward and for the backprojection.
+ * Cone plans: the 128-thread block shapes (8x16, 16x8, 32x4, 4x32) of both
+ * kernels and, on reflection plans, the backprojection's voxel run and row
+ * loop (FL_TUNE_ADJ_RUN / _ROWS). Fan plans: the parts per walked ray of the
+ * turn forward (FL_TUNE_FAN_PARTS: 1, 4, 16; turn plans) and the pixel block
+ * of the backprojections (FL_TUNE_FAN_BLOCK: 1 or 2). Only the fan parts
+ * count changes any bit of a result (the order of a ray's additions, not its
+ * matrix). Synchronises `stream`; uses the plan's scratch buffers. shapes
+ * (optional, [4]): the chosen forward x, y and backprojection x, y of a cone
+ * plan; for a fan plan the parts count, 0, the pixel block, 0. */
 int fl_plan_autotune(fl_plan *plan, void *stream, int32_t *shapes);
 /* FL_TUNE_ADJ_RUN: voxels per thread of the reflection backprojection (1 or
  * 2); FL_TUNE_ADJ_ROWS: its row loop, 1 or 2 detector rows per iteration, or
@@ -237,6 +241,18 @@ int fl_plan_autotune(fl_plan *plan, void *stream, int32_t *shapes);
  * pairs and keeps the fastest; fl_plan_option sets them (other values are
  * refused), fl_plan_query reads them. The results do not depend on them. */
 enum { FL_TUNE_ADJ_RUN = 16, FL_TUNE_ADJ_ROWS = 17 };
+/* Fan plans. FL_TUNE_FAN_PARTS: threads per walked ray of the half- or
+ * quarter-turn forward (1, 4 or 16), each walking a run of the ray's segments,
+ * their sums added in order; by default 16 for scans of fewer than 65,536
+ * walks (nv/G views x na columns), else 1. It sets the order of a ray's
+ * additions: the forward's bits (within FP32 rounding), not its matrix. A batch
+ * takes each turn slice's count when it is created, so batched and single-plan
+ * results stay equal bit for bit. FL_TUNE_FAN_BLOCK: pixels per thread side of
+ * the fan backprojections, 1 (one pixel, view groups over threads) or 2 (a 2x2
+ * block); by default 2 once there are four waves of blocks. The results do not
+ * depend on it. fl_plan_option sets them (other values are refused),
+ * fl_plan_query reads the values in effect. */
+enum { FL_TUNE_FAN_PARTS = 18, FL_TUNE_FAN_BLOCK = 19 };
 
 /* y = A x on `stream`. x: n_vox elements, y: n_rays elements, device memory. */
 int fl_forward(fl_plan *plan, int model, const void *x, int x_dtype, void *y, int y_dtype,
@@ -397,6 +413,17 @@ int fl_batch_adjoint(fl_batch *b, const float *y, float *x, void *stream);
  * the batch mixes turn and general slices). */
 int fl_batch_cgls(fl_batch *b, const float *rhs, float *u, float lam, int32_t iters, double tol,
                   int32_t flags, double *gamma_history, int32_t *iters_done, void *stream);
+/* Launch tuner of a batch: times the parts per walked ray of its half- and
+ * quarter-turn slices (1, 4, 16; FL_TUNE_FAN_PARTS) on the batch's own
+ * forward, one launch each on `stream` after one untimed, and keeps the
+ * fastest for every turn slice (a small scan needs parts to fill the GPU
+ * alone, not always beside other slices). The count sets the order of a
+ * ray's additions, so the batch's forward then equals its slice plans' with
+ * that count set. Synchronises `stream`; clobbers the batch's CGLS scratch
+ * (not the solution). parts (optional): the count chosen, 0 when the batch
+ * has no turn slice. Replaces nothing in the reference (its slices run one
+ * by one). */
+int fl_batch_autotune(fl_batch *b, void *stream, int32_t *parts);
 
 /* Bounds-checked builds only (compiled with -DFL_BOUNDS_CHECK, the
  * "checked" build variant): *violations = the number of gathers of the

@@ -100,6 +100,48 @@ def test_batch_turn_slices_bit_identical_to_single_plans():
         assert float((a - b).norm() / b.norm()) < 1e-5, i
 
 
+def test_batch_autotune_and_parts_keep_batch_equal_to_plans():
+    """A batch takes its turn slices' parts per walked ray from their plans
+    (here set to 4), and its own tuner sets one count for all of them; either
+    way each slice's forward equals its plan's with that count, bit for bit,
+    and the backprojection is unchanged."""
+    import torch
+    from framelab_gb300.batch import FanBatch
+    paras = _turn_paras()
+    B = FanBatch(paras, fan_parts=4)
+    rng = np.random.default_rng(9)
+    x = torch.from_numpy(rng.standard_normal(B.n_vox).astype(np.float32)).cuda()
+    y = torch.from_numpy(rng.standard_normal(B.n_rays).astype(np.float32)).cuda()
+
+    def check():
+        yb, xb = B.forward(x), B.adjoint(y)
+        torch.cuda.synchronize()
+        for i, P in enumerate(B.plans):
+            xi = B.images(x)[i].reshape(-1).contiguous()
+            yi = B.sinograms(y)[i].reshape(-1).contiguous()
+            assert torch.equal(B.sinograms(yb)[i].reshape(-1),
+                               P.forward(xi, model="matched").reshape(-1)), i
+            assert torch.equal(B.images(xb)[i].reshape(-1),
+                               P.adjoint(yi, model="matched").reshape(-1)), i
+
+    assert [P.tuning("fan_parts") for P, t in zip(B.plans, B.turns) if t > 1] == [4] * 4
+    check()
+    b = torch.from_numpy(rng.standard_normal(B.n_vox).astype(np.float32)).cuda()
+    B.cgls(b, iters=3)                    # captures its graph with 4 parts
+    parts = B.autotune()
+    assert parts in (1, 4, 16)
+    for P, t in zip(B.plans, B.turns):
+        if t > 1:
+            P.set_tuning("fan_parts", parts)
+    check()
+    # the CUDA-graph CGLS is recaptured with the new work list
+    u1 = B.cgls(b, iters=3)
+    B2 = FanBatch(paras, fan_parts=parts)
+    u2 = B2.cgls(b, iters=3)
+    assert torch.equal(u1, u2)
+    assert FanBatch(paras, turns=False).autotune() == 0
+
+
 def test_batch_tiny_slices_of_every_kind_bit_identical():
     """Degenerate slices in one batch: one view (general), a one-pixel-wide
     image (general: the turns need even nx and ny), a single detector column

@@ -868,8 +868,6 @@ def test_autotune_keeps_the_projections(zm):
     assert sh["forward"] in shapes and sh["adjoint"] in shapes, sh
     assert np.array_equal(_host(P.forward(x)), y0)
     assert np.array_equal(_host(P.adjoint(r)), x0)
-    assert _plan(G.fan_para(32, 32, 64, 20, L=(1, 1))).autotune() == {"forward": None,
-                                                                       "adjoint": None}
     if zm:
         # the reflection backprojection's voxel runs and rows per iteration
         assert P.reflect and sh["adjoint_voxels_per_thread"] in (1, 2)
@@ -882,6 +880,39 @@ def test_autotune_keeps_the_projections(zm):
                 assert np.array_equal(_host(P.adjoint(r)), x0), (run, rows)
         assert L.fl_plan_option(P.handle, _lib.TUNE_ADJ_RUN, 3) == _lib.FL_ERR_INVALID
         assert L.fl_plan_option(P.handle, _lib.TUNE_ADJ_ROWS, 4) == _lib.FL_ERR_INVALID
+
+
+@pytest.mark.parametrize("nv", [20, 18, 9])
+def test_fan_autotune_parts_and_pixel_block(nv):
+    """Fan plans: the tuner picks the parts per walked ray of the turn forward
+    (quarter turn at nv = 20, half turn at 18; the general plan at 9 has no
+    parts) and the backprojection's pixel block. The pixel block keeps every
+    bit; the parts change only the order of a ray's additions."""
+    from framelab_gb300 import _lib
+    P = _plan(G.fan_para(64, 64, 128, nv, L=(1, 1), SO=3.0, OD=3.0, Ly=3.0))
+    rng = np.random.default_rng(nv)
+    x = _dev(rng.standard_normal(P.n_vox).astype(np.float32))
+    r = _dev(rng.standard_normal(P.n_rays).astype(np.float32))
+    y0, x0 = _host(P.forward(x)), _host(P.adjoint(r))
+    sh = P.autotune()
+    assert sh["adjoint_pixel_block"] in (1, 2), sh
+    assert sh["forward_parts_per_ray"] == (1 if nv == 9 else P.tuning("fan_parts")), sh
+    assert sh["forward_parts_per_ray"] in (1, 4, 16)
+    assert np.array_equal(_host(P.adjoint(r)), x0)
+    for blk in (1, 2):
+        P.set_tuning("fan_block", blk)
+        assert P.tuning("fan_block") == blk
+        assert np.array_equal(_host(P.adjoint(r)), x0), blk
+    ys = {}
+    for parts in (1, 4, 16):
+        P.set_tuning("fan_parts", parts)
+        ys[parts] = _host(P.forward(x))
+        assert np.linalg.norm(ys[parts] - y0) <= 1e-6 * np.linalg.norm(y0), parts
+    if nv == 9:                          # the general forward walks each ray whole
+        assert all(np.array_equal(v, y0) for v in ys.values())
+    L = _lib.load()
+    assert L.fl_plan_option(P.handle, _lib.TUNE_FAN_PARTS, 2) == _lib.FL_ERR_INVALID
+    assert L.fl_plan_option(P.handle, _lib.TUNE_FAN_BLOCK, 3) == _lib.FL_ERR_INVALID
 
 
 # degenerate and small sizes: one view, one detector column or row, a 1-pixel
