@@ -588,6 +588,7 @@ def parity_block(ctx, w, p):
         if form == "precise":
             P.quarter_turn = False
             P.rot_mirror = False
+            P.reflect = False
         t = P.views_per_walk
 
         def fwd(v, P=P):
@@ -793,7 +794,8 @@ def run_batch(ctx, name, w, paras):
     del sino
     torch.cuda.synchronize()
     detail = {"slices": len(B), "n_vox": B.n_vox, "n_rays": B.n_rays,
-              "slices_by_turns": {str(t): B.turns.count(t) for t in (1, 2, 4)},
+              "slices_by_rays_per_walk": {str(t): B.turns.count(t) for t in (1, 2, 4, 8)},
+              "reflection_slices": sum(B.reflect),
               "turn_parts_per_ray": parts}
     if W:
         B.cgls(rhs, iters=W)

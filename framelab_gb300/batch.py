@@ -34,9 +34,14 @@ def _stream():
 class FanBatch:
     """Many single-frame fan-beam scans projected and solved together."""
 
-    def __init__(self, paras, turns: bool = True, fan_parts: int | None = None):
+    def __init__(self, paras, turns: bool = True, fan_parts: int | None = None,
+                 reflect: bool = True):
         """``turns=False`` keeps every slice on the general kernels (each
-        plan's half / quarter turn switched off before the batch is built).
+        plan's half / quarter turn and reflection switched off before the
+        batch is built). ``reflect`` (default on) asks every slice's plan for
+        the reflection about the x axis where its scan allows it: many slices
+        fill the GPU together, so the batch gains what a single small scan
+        would not.
         ``fan_parts`` (1, 4, 16) sets the parts per walked ray of every turn
         slice's plan first (``Plan.set_tuning("fan_parts", ...)``)."""
         L = _lib.load()
@@ -44,12 +49,16 @@ class FanBatch:
         for i, P in enumerate(self.plans):
             if P.cone:
                 raise ValueError(f"slice {i} is not a fan-beam scan")
+            P.reflect = reflect and turns
             if not turns:
                 P.rot_mirror = False
             if fan_parts is not None:
                 P.set_tuning("fan_parts", fan_parts)
-        # rays served per walk of each slice (4 quarter turn, 2 half turn, 1)
-        self.turns = [4 if P.quarter_turn else (2 if P.rot_mirror else 1) for P in self.plans]
+        # rays served per walk of each slice: 8 (quarter turns and the
+        # reflection), 4 (quarter turns, or the half turn and the reflection),
+        # 2 (half turn, or the reflection alone), 1
+        self.turns = [P.views_per_walk for P in self.plans]
+        self.reflect = [P.reflect for P in self.plans]
         n = len(self.plans)
         handles = (C.c_void_p * n)(*[P.handle.value for P in self.plans])
         h = C.c_void_p()
@@ -77,11 +86,13 @@ class FanBatch:
 
     @property
     def launches_per_iteration(self) -> int:
-        """Kernel launches of one CGLS iteration: forward and adjoint for the
-        general and for the turn slices, plus the three algebra kernels."""
+        """Kernel launches of one CGLS iteration: forward and adjoint for each
+        kind of slice present (general, turn, reflection), plus the three
+        algebra kernels."""
         general = any(t == 1 for t in self.turns)
-        turned = any(t > 1 for t in self.turns)
-        return 3 + 2 * int(general) + 2 * int(turned)
+        turned = any(t > 1 and not r for t, r in zip(self.turns, self.reflect))
+        mirrored = any(self.reflect)
+        return 3 + 2 * (int(general) + int(turned) + int(mirrored))
 
     def __del__(self):
         h = getattr(self, "_h", None)

@@ -15,15 +15,17 @@
 // or quarter turn (fl_plan_turns when the batch is created) goes through the
 // plan's turn kernels instead, on two more lists (32 rays of the views
 // iv < nv/G; 32 primary pixels); its adjoint input is packed per orbit, as
-// the plan's.
+// the plan's. So does a slice whose plan uses a reflection form (with or
+// without a turn): walked rays and primary pixels of that form.
 //
 // CGLS (solveCGLS.m:6-31) runs per slice, all slices in lockstep: every slice
 // has its own FP64 gamma/alpha/beta and stop flag, the inner products are
 // segmented by slice (per-chunk FP64 partials; the last chunk of a slice to
 // finish sums that slice's partials in a fixed order, so results do not depend
-// on scheduling). One iteration = 5 launches (forward with c_r^2, adjoint,
-// q += lam p with <p,q>, updates with <r,r>, direction; 7 when both general
-// and turn slices are present), captured once as a CUDA graph and replayed.
+// on scheduling). One iteration = 3 launches (q += lam p with <p,q>, updates
+// with <r,r>, direction) plus a forward with c_r^2 and an adjoint for each
+// kind of slice present (general, turn, reflection; parallel branches),
+// captured once as a CUDA graph and replayed.
 // A stopped slice's chunks return at once.
 #include <algorithm>
 #include <cstring>
@@ -52,6 +54,8 @@ struct BatchSlice {
     DetGrid G;
     int nx, ny, na, nv;
     int turns;             // fl_plan_turns of the slice's plan at batch creation
+    int refl;              // fl_plan_refl of it (1, 2, 4: a fan reflection form; 0: none)
+    int pblk;              // its backprojection's pixel block side (fan_refl_pblock)
     int lanes;             // parts per walked ray (fl_plan_fan_lanes of the slice's plan)
     float scale;
     long long xoff, yoff;  // offsets of the slice in the concatenated image / sinogram
@@ -158,6 +162,27 @@ k_batch_fwd_turn(const float* __restrict__ X, float* __restrict__ Y,
 #undef FL_BATCH_TURN
 }
 
+// Reflection slices: the plan's reflection forward (fan_refl_forward_block),
+// one block of kFanBlock threads per chunk (slice, r0) of the walked rays
+// (slots x columns of FanReflGeom; kFanBlock / lanes rays). ypack as above.
+__global__ void __launch_bounds__(kFanBlock, 3)
+k_batch_fwd_refl(const float* __restrict__ X, float* __restrict__ Y,
+                 const BatchSlice* __restrict__ sl, const int2* __restrict__ chunks,
+                 int cr_power, int ypack, const BatchScal* __restrict__ S)
+{
+    const int2 ch = chunks[blockIdx.x];
+    if (S && S[ch.x].done) return;            // uniform in the block
+    const BatchSlice& b = sl[ch.x];
+    float* y = Y + (ypack ? b.woff : b.yoff);
+#define FL_BATCH_REFL(NN)                                                                      \
+    fan_refl_forward_block<float, float, NN>(X + b.xoff, y, b.col, b.colr, b.nx, b.ny, b.na, b.nv, \
+                                             b.scale, cr_power, nullptr, ypack, ch.y, b.lanes)
+    if (b.refl == 4) FL_BATCH_REFL(4);
+    else if (b.refl == 2) FL_BATCH_REFL(2);
+    else FL_BATCH_REFL(1);
+#undef FL_BATCH_REFL
+}
+
 // yw = c_r * y over the ray chunks of all slices (input of the stand-alone
 // adjoint, in the batch's scratch); a turn slice's yw is packed per orbit
 // with c_r of view iv < nv/G (the single plan's k_weight_fan_packed values)
@@ -169,6 +194,23 @@ k_batch_weight(float* __restrict__ YW, const float* __restrict__ Y,
     const BatchSlice& b = sl[ch.x];
     const int r = ch.y + threadIdx.x;
     if (r >= b.na * b.nv) return;
+    if (b.refl) {                             // r: a walked ray (slot, column)
+        const int NR = b.refl;
+        const FanReflGeom g = fan_refl_geom(NR, b.nv, b.na);
+        const int s = r / b.na, ia = r - s * b.na;
+        int v, vt, a, stride;
+        long long off;
+        if (s >= g.slots || !refl_slot(g, s, ia, v, vt, a, off, stride)) return;
+        const float cr = ray_cr(b.scale, b.colr[(long long)vt * b.na + a], 0.0f);
+        for (int k = 0; k < 2 * NR; k++) {
+            long long vk; int ak;
+            if (NR == 4) refl_image<4>(k, v, a, b.na, b.nv, vk, ak);
+            else if (NR == 2) refl_image<2>(k, v, a, b.na, b.nv, vk, ak);
+            else refl_image<1>(k, v, a, b.na, b.nv, vk, ak);
+            YW[b.woff + off + (long long)(2 * NR) * ia + k] = cr * Y[b.yoff + vk * b.na + ak];
+        }
+        return;
+    }
     if (b.turns > 1) {
         const int gv = b.nv / b.turns, iv = r / b.na, ia = r - iv * b.na;
         const int rp = (iv % gv) * b.na + ia;
@@ -196,6 +238,30 @@ k_batch_adj_turn(float* __restrict__ X, const float* __restrict__ YW,
     else
         fan_turn_adjoint_block<float, 2, 2>(X + b.xoff, YW + b.woff, b.col, b.view, b.G, b.nx,
                                             b.ny, b.na, b.nv, ch.z, ch.y);
+}
+
+// Reflection slices: the plan's reflection backprojection, one block of
+// kFanX primary pixel blocks of one block row x kTurnGroups view groups per
+// chunk (slice, block row, first block column).
+__global__ void __launch_bounds__(kFanX * kTurnGroups)
+k_batch_adj_refl(float* __restrict__ X, const float* __restrict__ YW,
+                 const BatchSlice* __restrict__ sl, const int4* __restrict__ chunks,
+                 const BatchScal* __restrict__ S)
+{
+    const int4 ch = chunks[blockIdx.x];       // (slice, iy, ix0, -)
+    if (S && S[ch.x].done) return;            // uniform in the block
+    const BatchSlice& b = sl[ch.x];
+    __shared__ float smem[kFanReflShared];
+#define FL_BATCH_ADJ_REFL(NN, PP)                                                              \
+    fan_refl_adjoint_block<float, NN, PP>(X + b.xoff, YW + b.woff, b.col, b.view, b.G, b.nx, b.ny, \
+                                          b.na, b.nv, ch.z, ch.y, smem)
+    if (b.refl == 4 && b.pblk == 2) FL_BATCH_ADJ_REFL(4, 2);
+    else if (b.refl == 4) FL_BATCH_ADJ_REFL(4, 1);
+    else if (b.refl == 2 && b.pblk == 2) FL_BATCH_ADJ_REFL(2, 2);
+    else if (b.refl == 2) FL_BATCH_ADJ_REFL(2, 1);
+    else if (b.pblk == 2) FL_BATCH_ADJ_REFL(1, 2);
+    else FL_BATCH_ADJ_REFL(1, 1);
+#undef FL_BATCH_ADJ_REFL
 }
 
 // x = A^T (pre-weighted yw), one block per chunk of 2 image rows x
@@ -343,6 +409,8 @@ struct fl_batch {
     int2* d_wrays; int n_wray_chunks;      // every slice's rays (weighting)
     int4* d_pix;   int n_pix_chunks;       // general slices' pixel blocks
     int4* d_pix_t; int n_pix_t_chunks;     // turn slices' primary pixels
+    int2* d_rays_r; int n_ray_r_chunks;    // reflection slices' walked rays (forward)
+    int4* d_pix_r; int n_pix_r_chunks;     // reflection slices' primary pixels
     VecChunk* d_vec; int n_vec_chunks;
     float *r, *p, *q, *tmp;
     BatchScal* S;
@@ -354,25 +422,30 @@ struct fl_batch {
     cudaEvent_t ev0, ev1;
     cudaStream_t cs2;                  // the turn slices' branch of a forward / adjoint
     cudaEvent_t evf, evj;              // its fork and join
+    cudaStream_t cs3;                  // the reflection slices' branch
+    cudaEvent_t evf3, evj3;
     cudaGraphExec_t exec;
     float* cap_u;
     float cap_lam;
     double cap_tol;
     std::vector<BatchSlice> h_sl;      // host copy of d_sl
     std::vector<int> by_walk;          // slices, costliest walks first
-    int cap_rays_t;                    // capacity of d_rays_t (chunks)
+    int cap_rays_t, cap_rays_r;        // capacities of d_rays_t, d_rays_r (chunks)
 };
 
-// Chunks (slice, r0) of the turn slices' walked rays, kFanBlock / lanes rays each.
+// Chunks (slice, r0) of the walked rays of the turn slices (refl false) or of
+// the reflection slices (refl true), kFanBlock / lanes rays each.
 static std::vector<int2> turn_ray_chunks(const std::vector<BatchSlice>& sl,
-                                         const std::vector<int>& by_walk)
+                                         const std::vector<int>& by_walk, bool refl)
 {
     std::vector<int2> rays_t;
     for (int i : by_walk) {
         const BatchSlice& c = sl[i];
-        if (c.turns > 1)
-            for (int r = 0; r < c.na * (c.nv / c.turns); r += kFanBlock / c.lanes)
-                rays_t.push_back(make_int2(i, r));
+        if (c.turns > 1 && (c.refl != 0) == refl) {
+            const int walks = c.refl ? c.na * fan_refl_geom(c.refl, c.nv, c.na).slots
+                                     : c.na * (c.nv / c.turns);
+            for (int r = 0; r < walks; r += kFanBlock / c.lanes) rays_t.push_back(make_int2(i, r));
+        }
     }
     return rays_t;
 }
@@ -380,6 +453,7 @@ static std::vector<int2> turn_ray_chunks(const std::vector<BatchSlice>& sl,
 static void batch_free(fl_batch* b)
 {
     void* ptrs[] = {b->d_sl, b->d_rays, b->d_rays_t, b->d_wrays, b->d_pix, b->d_pix_t, b->d_vec,
+                    b->d_rays_r, b->d_pix_r,
                     b->r, b->p, b->q, b->tmp, b->S, b->partials, b->tickets, b->hist};
     for (void* q : ptrs)
         if (q) cudaFree(q);
@@ -388,6 +462,9 @@ static void batch_free(fl_batch* b)
     if (b->cs2) cudaStreamDestroy(b->cs2);
     if (b->evf) cudaEventDestroy(b->evf);
     if (b->evj) cudaEventDestroy(b->evj);
+    if (b->cs3) cudaStreamDestroy(b->cs3);
+    if (b->evf3) cudaEventDestroy(b->evf3);
+    if (b->evj3) cudaEventDestroy(b->evj3);
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
 }
@@ -435,6 +512,8 @@ extern "C" int fl_batch_create(fl_plan* const* plans, int32_t n_plans, fl_batch*
         b.G.rdu = 1.0f / p->du; b.G.rdg = p->dg != 0.0f ? 1.0f / p->dg : 0.0f;
         b.nx = s.nx; b.ny = s.ny; b.na = s.na; b.nv = s.nv; b.scale = s.scale;
         b.turns = fl_plan_turns(p);
+        b.refl = fl_plan_refl(p);
+        b.pblk = b.refl ? fan_refl_pblock(b.refl, s.nx, s.ny) : 0;
         b.lanes = b.turns > 1 ? fl_plan_fan_lanes(p) : 1;
         xoff[i + 1] = xoff[i] + (long long)s.nx * s.ny;
         yoff[i + 1] = yoff[i] + (long long)s.na * s.nv;
@@ -458,23 +537,30 @@ extern "C" int fl_batch_create(fl_plan* const* plans, int32_t n_plans, fl_batch*
         if (c.turns == 1)
             for (int r = 0; r < c.na * c.nv; r += kRayChunk) rays.push_back(make_int2(i, r));
     }
-    // room for the largest turn-ray list (16 parts per ray), which
+    // room for the largest walked-ray lists (16 parts per ray), which
     // fl_batch_autotune may choose
-    std::vector<int2> rays_t = turn_ray_chunks(sl, by_walk);
-    size_t cap_t = rays_t.size();
+    std::vector<int2> rays_t = turn_ray_chunks(sl, by_walk, false);
+    std::vector<int2> rays_r = turn_ray_chunks(sl, by_walk, true);
+    size_t cap_t = rays_t.size(), cap_r = rays_r.size();
     {
         std::vector<BatchSlice> s16 = sl;
         for (BatchSlice& c : s16)
             if (c.turns > 1) c.lanes = kFanLanes;
-        cap_t = std::max(cap_t, turn_ray_chunks(s16, by_walk).size());
+        cap_t = std::max(cap_t, turn_ray_chunks(s16, by_walk, false).size());
+        cap_r = std::max(cap_r, turn_ray_chunks(s16, by_walk, true).size());
     }
-    std::vector<int4> pix, pix_t;
+    std::vector<int4> pix, pix_t, pix_r;
     for (int i : by_views) {
         const BatchSlice& c = sl[i];
         if (c.turns == 1) {
             for (int iy = 0; iy < c.ny; iy += 2)
                 for (int ix = 0; ix < c.nx; ix += 2 * kPixChunk)
                     pix.push_back(make_int4(i, iy, ix, 0));
+        } else if (c.refl) {              // kFanX primary pixel blocks per chunk (block units)
+            const int hxb = (c.refl == 1 ? c.nx : c.nx / 2) / c.pblk, hyb = (c.ny / 2) / c.pblk;
+            for (int by = 0; by < hyb; by++)
+                for (int bx = 0; bx < hxb && (c.refl != 4 || bx <= by); bx += kFanX)
+                    pix_r.push_back(make_int4(i, by, bx, 0));
         } else {                          // the primary pixels: rows y < ny/2 (and x < nx/2)
             const int hx = c.turns == 2 ? c.nx : c.nx / 2;
             for (int iy = 0; iy < c.ny / 2; iy += 2)
@@ -489,8 +575,8 @@ extern "C" int fl_batch_create(fl_plan* const* plans, int32_t n_plans, fl_batch*
             vec.push_back(VecChunk{i, (int)k, (int)std::min<long long>(kVecChunk, n - k), 0});
         sl[i].vc1 = (int)vec.size();
     }
-    if (wrays.size() > 0x7fffffffu || pix.size() + pix_t.size() > 0x7fffffffu ||
-        vec.size() > 0x7fffffffu || cap_t > 0x7fffffffu)
+    if (wrays.size() > 0x7fffffffu || pix.size() + pix_t.size() + pix_r.size() > 0x7fffffffu ||
+        vec.size() > 0x7fffffffu || cap_t + cap_r > 0x7fffffffu)
         return fl_set_error(FL_ERR_UNSUPPORTED, "fl_batch_create: batch too large");
 
     fl_batch* b = new (std::nothrow) fl_batch;
@@ -503,21 +589,27 @@ extern "C" int fl_batch_create(fl_plan* const* plans, int32_t n_plans, fl_batch*
     b->tickets = nullptr; b->hist = nullptr; b->hist_cap = 4096;
     b->cs = nullptr; b->ev0 = b->ev1 = nullptr; b->exec = nullptr; b->cap_u = nullptr;
     b->cs2 = nullptr; b->evf = b->evj = nullptr;
+    b->cs3 = nullptr; b->evf3 = b->evj3 = nullptr;
+    b->d_rays_r = nullptr; b->d_pix_r = nullptr;
     b->cap_lam = 0.0f; b->cap_tol = 0.0;
-    b->h_sl = sl; b->by_walk = by_walk; b->cap_rays_t = (int)cap_t;
+    b->h_sl = sl; b->by_walk = by_walk; b->cap_rays_t = (int)cap_t; b->cap_rays_r = (int)cap_r;
+    b->n_ray_r_chunks = (int)rays_r.size(); b->n_pix_r_chunks = (int)pix_r.size();
     b->n_ray_chunks = (int)rays.size(); b->n_pix_chunks = (int)pix.size();
     b->n_ray_t_chunks = (int)rays_t.size(); b->n_wray_chunks = (int)wrays.size();
     b->n_pix_t_chunks = (int)pix_t.size();
     b->n_vec_chunks = (int)vec.size();
     int st = upload_vec(&b->d_sl, sl);
     if (!st) st = upload_vec(&b->d_rays, rays);
-    if (!st) {
-        st = fl_check_cuda(fl_malloc((void**)&b->d_rays_t, sizeof(int2) * (cap_t ? cap_t : 1)),
-                           "fl_malloc(batch)");
-        if (!st && !rays_t.empty())
-            st = fl_check_cuda(cudaMemcpy(b->d_rays_t, rays_t.data(), sizeof(int2) * rays_t.size(),
+    auto upload_room = [&](int2** d, const std::vector<int2>& h, size_t cap) {
+        if (st) return;
+        st = fl_check_cuda(fl_malloc((void**)d, sizeof(int2) * (cap ? cap : 1)), "fl_malloc(batch)");
+        if (!st && !h.empty())
+            st = fl_check_cuda(cudaMemcpy(*d, h.data(), sizeof(int2) * h.size(),
                                           cudaMemcpyHostToDevice), "upload");
-    }
+    };
+    upload_room(&b->d_rays_t, rays_t, cap_t);
+    upload_room(&b->d_rays_r, rays_r, cap_r);
+    if (!st) st = upload_vec(&b->d_pix_r, pix_r);
     if (!st) st = upload_vec(&b->d_wrays, wrays);
     if (!st) st = upload_vec(&b->d_pix, pix);
     if (!st) st = upload_vec(&b->d_pix_t, pix_t);
@@ -539,6 +631,9 @@ extern "C" int fl_batch_create(fl_plan* const* plans, int32_t n_plans, fl_batch*
     if (!st) st = fl_check_cuda(cudaStreamCreateWithFlags(&b->cs2, cudaStreamNonBlocking), "stream");
     if (!st) st = fl_check_cuda(cudaEventCreateWithFlags(&b->evf, cudaEventDisableTiming), "event");
     if (!st) st = fl_check_cuda(cudaEventCreateWithFlags(&b->evj, cudaEventDisableTiming), "event");
+    if (!st) st = fl_check_cuda(cudaStreamCreateWithFlags(&b->cs3, cudaStreamNonBlocking), "stream");
+    if (!st) st = fl_check_cuda(cudaEventCreateWithFlags(&b->evf3, cudaEventDisableTiming), "event");
+    if (!st) st = fl_check_cuda(cudaEventCreateWithFlags(&b->evj3, cudaEventDisableTiming), "event");
     if (st) { batch_free(b); delete b; return st; }
     *out = b;
     return fl_set_error(FL_OK, "");
@@ -561,51 +656,65 @@ extern "C" int fl_batch_layout(const fl_batch* b, int64_t* vox_offsets, int64_t*
     return fl_set_error(FL_OK, "");
 }
 
-// ypack: y is the batch's scratch (slice offsets woff), turn slices packed per
-// orbit, as batch_adj_w reads it; else the caller's sinogram (offsets yoff)
-// With both kinds of slices, the turn slices' launch runs on a second stream
-// forked from s and joined back (two branches of a captured graph): the two
-// write different slices, and each fills the other's tail.
-static cudaStream_t fork(fl_batch* b, cudaStream_t s)
+// ypack: y is the batch's scratch (slice offsets woff), turn and reflection
+// slices packed per orbit, as batch_adj_w reads it; else the caller's
+// sinogram (offsets yoff).
+// Each kind of slice present (general, turn, reflection) is one launch; the
+// first present runs on s, every further one on a stream of its own forked
+// from s and joined back (branches of a captured graph): they write
+// different slices, and each fills the others' tails.
+static cudaStream_t fork_to(cudaStream_t s, cudaStream_t cs, cudaEvent_t ev)
 {
-    if (cudaEventRecord(b->evf, s) != cudaSuccess || cudaStreamWaitEvent(b->cs2, b->evf, 0) != cudaSuccess)
+    if (cudaEventRecord(ev, s) != cudaSuccess || cudaStreamWaitEvent(cs, ev, 0) != cudaSuccess)
         return s;
-    return b->cs2;
+    return cs;
 }
 
-static int join(fl_batch* b, cudaStream_t s, cudaStream_t s2)
+static int join_from(cudaStream_t s, cudaStream_t s2, cudaEvent_t ev)
 {
     if (s2 == s) return FL_OK;
-    FL_CUDA(cudaEventRecord(b->evj, s2));
-    FL_CUDA(cudaStreamWaitEvent(s, b->evj, 0));
+    FL_CUDA(cudaEventRecord(ev, s2));
+    FL_CUDA(cudaStreamWaitEvent(s, ev, 0));
     return FL_OK;
 }
 
 static int batch_fwd(fl_batch* b, const float* x, float* y, int cr_power, int ypack,
                      const BatchScal* S, cudaStream_t s)
 {
-    const cudaStream_t s2 = (b->n_ray_chunks && b->n_ray_t_chunks) ? fork(b, s) : s;
-    if (b->n_ray_t_chunks)
+    const bool g = b->n_ray_chunks, t = b->n_ray_t_chunks, r = b->n_ray_r_chunks;
+    const cudaStream_t s2 = (t && g) ? fork_to(s, b->cs2, b->evf) : s;
+    const cudaStream_t s3 = (r && (g || t)) ? fork_to(s, b->cs3, b->evf3) : s;
+    if (r)
+        k_batch_fwd_refl<<<b->n_ray_r_chunks, kFanBlock, 0, s3>>>(
+            x, y, b->d_sl, b->d_rays_r, cr_power, ypack, S);
+    if (t)
         k_batch_fwd_turn<<<b->n_ray_t_chunks, kFanBlock, 0, s2>>>(
             x, y, b->d_sl, b->d_rays_t, cr_power, ypack, S);
-    if (b->n_ray_chunks)
+    if (g)
         k_batch_fwd<<<b->n_ray_chunks, kRayChunk, 0, s>>>(x, y, b->d_sl, b->d_rays, cr_power,
                                                           ypack, S);
     int st = fl_check_launch("batched forward");
-    if (!st) st = join(b, s, s2);
+    if (!st) st = join_from(s, s2, b->evj);
+    if (!st) st = join_from(s, s3, b->evj3);
     return st;
 }
 
 static int batch_adj_w(fl_batch* b, const float* yw, float* x, const BatchScal* S, cudaStream_t s)
 {
-    const cudaStream_t s2 = (b->n_pix_chunks && b->n_pix_t_chunks) ? fork(b, s) : s;
-    if (b->n_pix_t_chunks)
+    const bool g = b->n_pix_chunks, t = b->n_pix_t_chunks, r = b->n_pix_r_chunks;
+    const cudaStream_t s2 = (t && g) ? fork_to(s, b->cs2, b->evf) : s;
+    const cudaStream_t s3 = (r && (g || t)) ? fork_to(s, b->cs3, b->evf3) : s;
+    if (r)
+        k_batch_adj_refl<<<b->n_pix_r_chunks, dim3(kFanX, kTurnGroups), 0, s3>>>(
+            x, yw, b->d_sl, b->d_pix_r, S);
+    if (t)
         k_batch_adj_turn<<<b->n_pix_t_chunks, dim3(kFanX, kTurnGroups), 0, s2>>>(
             x, yw, b->d_sl, b->d_pix_t, S);
-    if (b->n_pix_chunks)
+    if (g)
         k_batch_adj<<<b->n_pix_chunks, kPixChunk, 0, s>>>(x, yw, b->d_sl, b->d_pix, S);
     int st = fl_check_launch("batched adjoint");
-    if (!st) st = join(b, s, s2);
+    if (!st) st = join_from(s, s2, b->evj);
+    if (!st) st = join_from(s, s3, b->evj3);
     return st;
 }
 
@@ -635,16 +744,21 @@ static int batch_set_lanes(fl_batch* b, int L, cudaStream_t s)
 {
     for (BatchSlice& c : b->h_sl)
         if (c.turns > 1) c.lanes = L;
-    const std::vector<int2> rays_t = turn_ray_chunks(b->h_sl, b->by_walk);
-    if ((long long)rays_t.size() > b->cap_rays_t)
+    const std::vector<int2> rays_t = turn_ray_chunks(b->h_sl, b->by_walk, false);
+    const std::vector<int2> rays_r = turn_ray_chunks(b->h_sl, b->by_walk, true);
+    if ((long long)rays_t.size() > b->cap_rays_t || (long long)rays_r.size() > b->cap_rays_r)
         return fl_set_error(FL_ERR_INVALID, "fl_batch_autotune: work list beyond its room");
     FL_CUDA(cudaMemcpyAsync(b->d_sl, b->h_sl.data(), sizeof(BatchSlice) * b->h_sl.size(),
                             cudaMemcpyHostToDevice, s));
     if (!rays_t.empty())
         FL_CUDA(cudaMemcpyAsync(b->d_rays_t, rays_t.data(), sizeof(int2) * rays_t.size(),
                                 cudaMemcpyHostToDevice, s));
+    if (!rays_r.empty())
+        FL_CUDA(cudaMemcpyAsync(b->d_rays_r, rays_r.data(), sizeof(int2) * rays_r.size(),
+                                cudaMemcpyHostToDevice, s));
     FL_CUDA(cudaStreamSynchronize(s));         // the host vectors go out of scope
     b->n_ray_t_chunks = (int)rays_t.size();
+    b->n_ray_r_chunks = (int)rays_r.size();
     if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }   // recaptured
     return FL_OK;
 }

@@ -111,7 +111,11 @@ struct fl_plan {
     int refl;                  // wanted (FL_OPT_REFLECT); used where the turn in use allows
     // fan plans take both turns without a mirror: the half turn with ny even,
     // the quarter turn with nx == ny even (A[(v + j nv/G, a), R^j (x, y)] =
-    // A[(v, a), (x, y)], one walk / one weight serving G rays).
+    // A[(v, a), (x, y)], one walk / one weight serving G rays), and the
+    // reflection with either (one walk / weight serving 2 G rays; the quarter
+    // turns with nv a multiple of 8) or alone for odd view counts (two rays:
+    // S = identity, walked views 0 .. (nv-1)/2; FanReflGeom in matched_dev.cuh)
+    int refl1_ok;              // fan: the reflection alone (odd nv)
     // Every turn form needs one frame whose view list is 0, 1, ..., nv-1.
     int views_natural;
     // launch shapes (threads in x and y, x * y = 128) of the cone projector
@@ -145,37 +149,45 @@ enum {
     FL_FORM_MIRROR,           // cone: z mirror
     FL_FORM_HALF,             // half turn (cone: with the z mirror)
     FL_FORM_QUARTER,          // quarter turns (cone: with the z mirror)
-    FL_FORM_HALF_REFL,        // cone: half turn, reflection, z mirror
-    FL_FORM_QUARTER_REFL      // cone: quarter turns, reflection, z mirror
+    FL_FORM_HALF_REFL,        // half turn and reflection (cone: with the z mirror)
+    FL_FORM_QUARTER_REFL,     // quarter turns and reflection (cone: with the z mirror)
+    FL_FORM_REFL              // fan: the reflection alone (odd nv)
 };
 
 inline int fl_plan_form(const fl_plan* p)
 {
     if (p->s.ndim == 3 && !p->zmirror) return FL_FORM_GENERAL;
-    if (!p->rot) return p->s.ndim == 3 ? FL_FORM_MIRROR : FL_FORM_GENERAL;
-    if (p->rot4)
-        return (p->s.ndim == 3 && p->refl && p->refl4_ok) ? FL_FORM_QUARTER_REFL : FL_FORM_QUARTER;
-    return (p->s.ndim == 3 && p->refl && p->refl2_ok) ? FL_FORM_HALF_REFL : FL_FORM_HALF;
+    if (!p->rot) {
+        if (p->s.ndim == 3) return FL_FORM_MIRROR;
+        return (p->refl && p->refl1_ok) ? FL_FORM_REFL : FL_FORM_GENERAL;
+    }
+    if (p->rot4) return (p->refl && p->refl4_ok) ? FL_FORM_QUARTER_REFL : FL_FORM_QUARTER;
+    return (p->refl && p->refl2_ok) ? FL_FORM_HALF_REFL : FL_FORM_HALF;
 }
 
 // Views one walk or weight of the matched kernels in use serves: 8 (quarter
 // turns and the reflection), 4 (quarter turns, or the half turn and the
-// reflection), 2 (half turn) or 1.
+// reflection), 2 (half turn, or the reflection alone) or 1.
 inline int fl_plan_turns(const fl_plan* p)
 {
     switch (fl_plan_form(p)) {
     case FL_FORM_QUARTER_REFL: return 8;
     case FL_FORM_QUARTER: case FL_FORM_HALF_REFL: return 4;
-    case FL_FORM_HALF: return 2;
+    case FL_FORM_HALF: case FL_FORM_REFL: return 2;
     default: return 1;
     }
 }
 
-// Rotations of a reflection form (4 or 2), or 0.
+// Rotations of a reflection form (4, 2, or 1 for the fan's reflection
+// alone), or 0.
 inline int fl_plan_refl(const fl_plan* p)
 {
-    const int f = fl_plan_form(p);
-    return f == FL_FORM_QUARTER_REFL ? 4 : (f == FL_FORM_HALF_REFL ? 2 : 0);
+    switch (fl_plan_form(p)) {
+    case FL_FORM_QUARTER_REFL: return 4;
+    case FL_FORM_HALF_REFL: return 2;
+    case FL_FORM_REFL: return 1;
+    default: return 0;
+    }
 }
 
 // Layouts of the matched launchers' operands. For a z-mirror plan the

@@ -291,12 +291,17 @@ static int build_tables(fl_plan* p, const std::vector<float>& phi, const float* 
         p->rot4_ok = ok ? 1 : 0;
     }
     p->rot4 = p->rot4_ok;
-    // reflection (fl_plan.h): cone plans with the half turn (and, for the
-    // quarter-turn form, the quarter turn and nv a multiple of 8), view nv - v
-    // the mirror image of view v about the x axis to within 1e-6 (cos equal,
-    // sin opposite) and an exactly symmetric detector
-    p->refl2_ok = p->refl4_ok = 0;
-    if (p->rot_ok && s.ndim == 3 && s.na % 2 == 0) {
+    // reflection (fl_plan.h): plans with the half turn (and, for the
+    // quarter-turn form, the quarter turn and nv a multiple of 8), or fan
+    // plans of one frame, natural view order, an odd view count and ny even
+    // (the reflection alone), with view nv - v the mirror image of view v
+    // about the x axis to within 1e-6 (cos equal, sin opposite), view 0 at
+    // angle 0 and an exactly symmetric detector of even width; fan plans also
+    // need the uniform detector of their backprojection
+    p->refl2_ok = p->refl4_ok = p->refl1_ok = 0;
+    const bool fan_alone = s.ndim == 2 && s.nt == 1 && p->views_natural && s.nv % 2 == 1 &&
+                           s.ny % 2 == 0;
+    if ((p->rot_ok || fan_alone) && s.na % 2 == 0 && (s.ndim == 3 || p->det_kind >= 0)) {
         bool ok = true;
         for (int ia = 0; ia < s.na / 2 && ok; ia++)
             if (y_det[s.na - 1 - ia] != -y_det[ia]) ok = false;
@@ -307,10 +312,14 @@ static int build_tables(fl_plan* p, const std::vector<float>& phi, const float* 
             if (std::fabs(c0 - c1) > 1e-6 || std::fabs(s0 + s1) > 1e-6) ok = false;
         }
         if (phi[0] != 0.0f) ok = false;             // view 0 is its own mirror image
-        p->refl2_ok = ok ? 1 : 0;
+        p->refl2_ok = (ok && p->rot_ok) ? 1 : 0;
         p->refl4_ok = (ok && p->rot4_ok && diag) ? 1 : 0;
+        p->refl1_ok = (ok && fan_alone) ? 1 : 0;
     }
-    p->refl = 1;
+    // cone plans take the reflection by default; fan plans when asked: the
+    // octant of a single fan image of a few hundred pixels has too few pixel
+    // blocks to fill the GPU with it, while a batch of many slices gains
+    p->refl = s.ndim == 3 ? 1 : 0;
     return FL_OK;
 }
 
@@ -364,7 +373,7 @@ extern "C" int fl_plan_query(const fl_plan* p, int option, int* value)
     }
     const int form = fl_plan_form(p);
     if (option == FL_OPT_ROT_MIRROR) {
-        *value = form >= FL_FORM_HALF ? 1 : 0;
+        *value = (form >= FL_FORM_HALF && form != FL_FORM_REFL) ? 1 : 0;
         return fl_set_error(FL_OK, "");
     }
     if (option == FL_OPT_QUARTER_TURN) {

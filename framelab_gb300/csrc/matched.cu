@@ -158,19 +158,6 @@ k_fwd_oct(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restri
     }
 }
 
-// View and column of the ray that image k of a walked ray (v, a) is, on a
-// reflection form (NR = 4 or 2): k < NR the turn R^(4k/NR) (view v + k nv/NR,
-// column a), k >= NR the reflection R^(4(k-NR)/NR) M (view (k-NR) nv/NR - v,
-// column na-1-a).
-template <int NR>
-__device__ __forceinline__ void refl_image(int k, int v, int a, int na, int nv, long long& vk,
-                                           int& ak)
-{
-    const int sv = nv / NR;
-    if (k < NR) { vk = v + (long long)k * sv; ak = a; }
-    else { vk = ((long long)(k - NR) * sv - v + nv) % nv; ak = na - 1 - a; }
-}
-
 // Reflection forms (fl_plan::refl; NR = 4: quarter turns, square grid; NR =
 // 2: half turn): the block walks rows ib < nb/2 of the slots s (refl_slot:
 // the walked views 0 .. ov); each walk yields the rays of its 4 NR images
@@ -252,6 +239,34 @@ k_fwd_fan_turn(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __r
     if (skip && *skip) return;                 // uniform (one flag for the launch)
     fan_turn_forward_block<TX, TY, G, L>(X, y, col, colr, nx, ny, na, nv, scale, cr_power,
                                          xscale, ypack, (long long)blockIdx.x * (kFanBlock / L));
+}
+
+// Fan reflection forms (NR = 1, 2 or 4, one frame): forward blocks of
+// kFanBlock threads, L parts per walked ray (fan_refl_forward_block).
+template <typename TX, typename TY, int NR>
+__global__ void __launch_bounds__(kFanBlock, 3)
+k_fwd_fan_refl(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restrict__ col,
+               const float* __restrict__ colr, int nx, int ny, int na, int nv, float scale,
+               int cr_power, const int* __restrict__ skip, const float* __restrict__ xscale,
+               int ypack, int L)
+{
+    if (skip && *skip) return;                 // uniform (one flag for the launch)
+    fan_refl_forward_block<TX, TY, NR>(X, y, col, colr, nx, ny, na, nv, scale, cr_power, xscale,
+                                       ypack, (long long)blockIdx.x * (kFanBlock / L), L);
+}
+
+// Fan reflection backprojection: blocks of kFanX PB x PB pixel blocks of one
+// block row x kTurnGroups view groups (fan_refl_adjoint_block).
+template <typename TX, int NR, int PB>
+__global__ void __launch_bounds__(kFanX * kTurnGroups)
+k_adj_fan_refl(TX* __restrict__ X, const float* __restrict__ ywp,
+               const ColEntry* __restrict__ col, const ViewEntry* __restrict__ view, DetGrid G,
+               int nx, int ny, int na, int nv, const int* __restrict__ skip)
+{
+    if (skip && *skip) return;
+    __shared__ float smem[kTurnGroups * 2 * NR * PB * PB * kFanX];
+    fan_refl_adjoint_block<TX, NR, PB>(X, ywp, col, view, G, nx, ny, na, nv, blockIdx.x * kFanX,
+                                       blockIdx.y, smem);
 }
 
 __global__ void __launch_bounds__(128)
@@ -373,6 +388,30 @@ __global__ void k_weight_fan_packed(float* __restrict__ yw, const TY* __restrict
 #pragma unroll
     for (int j = 0; j < G; j++)
         yw[G * r + j] = cr * Store<TY>::ld_plain(y + ((long long)iv + (long long)j * gv) * na + ia);
+}
+
+// Packed yw of a fan reflection form (NR = 1, 2, 4): for each walked ray
+// (refl_slot of FanReflGeom) the 2 NR values c_r y of its images
+// (refl_image), with c_r of the walked ray.
+template <typename TY, int NR>
+__global__ void k_weight_fan_refl(float* __restrict__ yw, const TY* __restrict__ y,
+                                  const float* __restrict__ colr, int na, int nv,
+                                  long long nslot, float scale)
+{
+    const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nslot) return;                         // nslot = slots * na
+    const FanReflGeom g = fan_refl_geom(NR, nv, na);
+    const int sl = (int)(r / na), ia = (int)(r - (long long)sl * na);
+    int v, vt, a, stride;
+    long long off;
+    if (!refl_slot(g, sl, ia, v, vt, a, off, stride)) return;
+    const float cr = ray_cr(scale, colr[(long long)vt * na + a], 0.0f);
+#pragma unroll
+    for (int k = 0; k < 2 * NR; k++) {
+        long long vk; int ak;
+        refl_image<NR>(k, v, a, na, nv, vk, ak);
+        yw[off + (long long)(2 * NR) * ia + k] = cr * Store<TY>::ld_plain(y + vk * na + ak);
+    }
 }
 
 // z-fold / unfold of volumes (all frames): pair r = (iz < nz/2, iy, ix) of a
@@ -1336,7 +1375,10 @@ int fl_plan_fan_lanes(const fl_plan* p)
 {
     if (p->fan_lanes) return p->fan_lanes;
     const int G = fl_plan_turns(p);
-    return G > 1 ? fan_turn_lanes((long long)p->s.na * (p->s.nv / G)) : 1;
+    if (G <= 1 || p->s.ndim != 2) return 1;
+    if (const int NR = fl_plan_refl(p))           // walked rays: slots x columns
+        return fan_turn_lanes((long long)p->s.na * fan_refl_geom(NR, p->s.nv, p->s.na).slots);
+    return fan_turn_lanes((long long)p->s.na * (p->s.nv / G));
 }
 
 int fl_plan_fan_block(const fl_plan* p)
@@ -1393,6 +1435,19 @@ void launch_fwd(fl_plan* p, const void* x, void* y, int cr_power, const int* ski
         k_fwd_cone<TX, TY, false><<<grid, fb, 0, st>>>(
             (const TX*)x, (TY*)y, p->d_col, p->d_colr, p->d_row, p->d_view_frame, s.nx, s.ny,
             s.nz, s.na, s.nb, p->n_vox_frame, s.scale, cr_power, skip, xscale, 0);
+    } else if (fl_plan_refl(p)) {
+        const int NR = fl_plan_refl(p);
+        const long long nr = (long long)s.na * fan_refl_geom(NR, s.nv, s.na).slots;
+        const int lanes = fl_plan_fan_lanes(p);
+        const unsigned g = fl_div_up(nr, kFanBlock / lanes);
+#define FL_FAN_REFL(NN)                                                                      \
+    k_fwd_fan_refl<TX, TY, NN><<<g, kFanBlock, 0, st>>>(                                     \
+        (const TX*)x, (TY*)y, p->d_col, p->d_colr, s.nx, s.ny, s.na, s.nv, s.scale, cr_power, \
+        skip, xscale, yfold, lanes)
+        if (NR == 4) FL_FAN_REFL(4);
+        else if (NR == 2) FL_FAN_REFL(2);
+        else FL_FAN_REFL(1);
+#undef FL_FAN_REFL
     } else if (fl_plan_turns(p) > 1) {
         const int G = fl_plan_turns(p);
         const long long nr = (long long)s.na * (s.nv / G);
@@ -1504,6 +1559,23 @@ void launch_adj(fl_plan* p, const float* yw, void* x, const int* skip, int xfold
     DetGrid G = det_grid(p);
     if (s.ndim == 3) {
         launch_adj_cone<TX, float>(p, yw, x, skip, xfold, st);
+    } else if (fl_plan_refl(p)) {
+        // one PB x PB block of primary pixels per thread (fan_refl_pblock); the
+        // octant's blocks right of the diagonal have no primary block and return
+        const int NR = fl_plan_refl(p);
+        const int PB = fan_refl_pblock(NR, s.nx, s.ny);
+        const int hxb = (NR == 1 ? s.nx : s.nx / 2) / PB, hyb = (s.ny / 2) / PB;
+        const dim3 blk(kFanX, kTurnGroups), g1(fl_div_up(hxb, kFanX), hyb);
+#define FL_ADJ_FAN_REFL(NN, PP)                                                              \
+    k_adj_fan_refl<TX, NN, PP><<<g1, blk, 0, st>>>((TX*)x, yw, p->d_col, p->d_view, G, s.nx, \
+                                                   s.ny, s.na, s.nv, skip)
+        if (NR == 4 && PB == 2) FL_ADJ_FAN_REFL(4, 2);
+        else if (NR == 4) FL_ADJ_FAN_REFL(4, 1);
+        else if (NR == 2 && PB == 2) FL_ADJ_FAN_REFL(2, 2);
+        else if (NR == 2) FL_ADJ_FAN_REFL(2, 1);
+        else if (PB == 2) FL_ADJ_FAN_REFL(1, 2);
+        else FL_ADJ_FAN_REFL(1, 1);
+#undef FL_ADJ_FAN_REFL
     } else if (fl_plan_turns(p) > 1) {
         // 2 x 2 primary blocks once there are at least 4 waves of them, else
         // one primary pixel per thread (the same bits)
@@ -1612,6 +1684,23 @@ void launch_weight_fan_packed(fl_plan* p, const void* y, int yt, float* yw, cuda
             yw, (const __nv_bfloat16*)y, p->d_colr, s.na, s.nv, npk, s.scale);
 }
 
+template <int NR>
+void launch_weight_fan_refl(fl_plan* p, const void* y, int yt, float* yw, cudaStream_t st)
+{
+    const fl_scan& s = p->s;
+    const long long ns = (long long)s.na * fan_refl_geom(NR, s.nv, s.na).slots;
+    const unsigned g = fl_div_up(ns, 256);
+    if (yt == FL_F32)
+        k_weight_fan_refl<float, NR><<<g, 256, 0, st>>>(yw, (const float*)y, p->d_colr, s.na,
+                                                        s.nv, ns, s.scale);
+    else if (yt == FL_F16)
+        k_weight_fan_refl<__half, NR><<<g, 256, 0, st>>>(yw, (const __half*)y, p->d_colr, s.na,
+                                                         s.nv, ns, s.scale);
+    else
+        k_weight_fan_refl<__nv_bfloat16, NR><<<g, 256, 0, st>>>(
+            yw, (const __nv_bfloat16*)y, p->d_colr, s.na, s.nv, ns, s.scale);
+}
+
 }  // namespace
 
 int fl_matched_fold(fl_plan* p, const void* src, void* dst, int dtype, int unfold,
@@ -1659,6 +1748,12 @@ int fl_matched_weight(fl_plan* p, const void* y, int yt, float* yw, cudaStream_t
     if (three && p->zmirror && p->rot) {
         if (p->rot4) launch_weight_packed<4>(p, y, yt, yw, st);
         else launch_weight_packed<2>(p, y, yt, yw, st);
+        return fl_check_launch("matched adjoint weighting");
+    }
+    if (!three && fl_plan_refl(p)) {
+        if (fl_plan_refl(p) == 4) launch_weight_fan_refl<4>(p, y, yt, yw, st);
+        else if (fl_plan_refl(p) == 2) launch_weight_fan_refl<2>(p, y, yt, yw, st);
+        else launch_weight_fan_refl<1>(p, y, yt, yw, st);
         return fl_check_launch("matched adjoint weighting");
     }
     if (!three && fl_plan_turns(p) > 1) {

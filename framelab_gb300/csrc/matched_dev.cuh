@@ -508,11 +508,43 @@ __host__ __device__ inline ReflGeom refl_geom(int NR, int nv, int na, int nb)
     return g;
 }
 
+// Fan reflection forms (fl_plan::refl on a fan plan, NR = 1, 2 or 4): with
+// M (x, y) = (x, ny-1-y), S = the identity (NR = 1), the half turn R^2 (NR =
+// 2) or the quarter turn R (NR = 4) and q = nv/NR, the walked views v = 0 ..
+// ov (ov = floor(q/2)) define
+//   A[(v + j q, a), S^j p] = A[(j q - v, na-1-a), S^j M p] = A[(v, a), p].
+// View 0, and view ov where q is even (then its own mirror image), walk their
+// columns a < na/2 only; view ov is walked from table row nv (NR = 4: the
+// exact angle pi/4) or nv + 1 (NR = 2: the exact angle pi/2). NR = 1 takes
+// odd view counts (no end view). The packed input holds the 2 NR values of a
+// walked ray's orbit side by side (the turn images', then the reflected
+// images'), in slots of na columns laid out as the cone's (refl_slot /
+// refl_view with one row): nv * na values in all.
+struct FanReflGeom {
+    int nv, na, ov, end, endrow, vpr, slots;
+    long long slot;                                 // values per slot
+};
+
+__host__ __device__ inline FanReflGeom fan_refl_geom(int NR, int nv, int na)
+{
+    FanReflGeom g;
+    g.nv = nv; g.na = na;
+    const int q = nv / NR;
+    g.ov = q / 2;
+    g.end = q % 2 == 0;
+    g.endrow = NR == 4 ? nv : nv + 1;
+    g.vpr = 2 * NR;
+    g.slots = g.end ? g.ov : g.ov + 1;
+    g.slot = (long long)na * g.vpr;
+    return g;
+}
+
 // Forward slot (s, column ia) of a reflection form: the walked view v, its
 // table row vt and column a, and where its values go in each plane (offset
 // off + vpr (ib stride + ia) + 2 k for row ib, image k mod NR). False for the
-// unused half of the last slot.
-__device__ __forceinline__ bool refl_slot(const ReflGeom& g, int s, int ia, int& v, int& vt,
+// unused half of the last slot. (Geo: ReflGeom, or FanReflGeom with one row.)
+template <typename Geo>
+__device__ __forceinline__ bool refl_slot(const Geo& g, int s, int ia, int& v, int& vt,
                                           int& a, long long& off, int& stride)
 {
     const int h = g.na / 2;
@@ -532,10 +564,24 @@ __device__ __forceinline__ bool refl_slot(const ReflGeom& g, int s, int ia, int&
     return true;
 }
 
+// View and column of the ray that image k of a walked ray (v, a) is, on a
+// reflection form (NR = 4, 2 or 1): k < NR the turn S^k (view v + k nv/NR,
+// column a), k >= NR the reflection S^(k-NR) M (view (k-NR) nv/NR - v,
+// column na-1-a).
+template <int NR>
+__device__ __forceinline__ void refl_image(int k, int v, int a, int na, int nv, long long& vk,
+                                           int& ak)
+{
+    const int sv = nv / NR;
+    if (k < NR) { vk = v + (long long)k * sv; ak = a; }
+    else { vk = ((long long)(k - NR) * sv - v + nv) % nv; ak = na - 1 - a; }
+}
+
 // Backprojection view w of a reflection form: table row, the plane offset of
 // its values (column ia, row ib at base + vpr (ib stride + ia)), and the
 // number of its walked columns.
-__device__ __forceinline__ void refl_view(const ReflGeom& g, int w, int& vt, long long& base,
+template <typename Geo>
+__device__ __forceinline__ void refl_view(const Geo& g, int w, int& vt, long long& base,
                                           int& stride, int& alim)
 {
     const int h = g.na / 2;
@@ -563,18 +609,40 @@ __device__ __forceinline__ void refl_view(const ReflGeom& g, int w, int& vt, lon
 // this call walks part `lane`. Segments are independent, so every matrix
 // entry lies whole in one part and is the walk's own; only the order of the
 // additions changes (the caller adds the parts in lane order).
+// RF (a fan reflection form, G = NR = 1, 2 or 4): per step also the images
+// S^j M (ix, iy) of the pixel, M (x, y) = (x, ny-1-y), into acc[G + j].
 constexpr int kFanBatch = 4;
 
-template <typename TX, int G, int L = 1>
+// walk_fan_parts: the same walk with the parts count L a run-time value.
+template <typename TX, int G, bool RF>
+__device__ __forceinline__ void walk_fan_parts(const TX* __restrict__ x, const AxisEntry* pX,
+                                               const AxisEntry* pY, int nx, int ny,
+                                               float (&acc)[RF ? 2 * G : G], long long xlen,
+                                               int lane, int L);
+
+template <typename TX, int G, int L = 1, bool RF = false>
 __device__ __forceinline__ void walk_fan(const TX* __restrict__ x, const AxisEntry* pX,
-                                         const AxisEntry* pY, int nx, int ny, float (&acc)[G],
-                                         long long xlen, int lane = 0)
+                                         const AxisEntry* pY, int nx, int ny,
+                                         float (&acc)[RF ? 2 * G : G], long long xlen,
+                                         int lane = 0)
+{
+    walk_fan_parts<TX, G, RF>(x, pX, pY, nx, ny, acc, xlen, lane, L);
+}
+
+template <typename TX, int G, bool RF>
+__device__ __forceinline__ void walk_fan_parts(const TX* __restrict__ x, const AxisEntry* pX,
+                                               const AxisEntry* pY, int nx, int ny,
+                                               float (&acc)[RF ? 2 * G : G], long long xlen,
+                                               int lane, int L)
 {
     const AxisEntry X = *pX, Y = *pY;
     static_assert(G == 1 || G == 2 || G == 4, "one, two or four turns");
     constexpr int SH = kSegFan;
+    constexpr int NI = RF ? 2 * G : G;             // images per step
+    // steps batched per gather round (eight images: two, within the registers)
+    constexpr int NB = NI > 4 ? 2 : kFanBatch;
 #pragma unroll
-    for (int j = 0; j < G; j++) acc[j] = 0.0f;
+    for (int j = 0; j < NI; j++) acc[j] = 0.0f;
     const float a_in = fmaxf(fminf(xabs(X, 0.0f), xabs(X, (float)nx)),
                              fminf(xabs(Y, 0.0f), xabs(Y, (float)ny)));
     const float a_out = fminf(fmaxf(xabs(X, 0.0f), xabs(X, (float)nx)),
@@ -599,9 +667,9 @@ __device__ __forceinline__ void walk_fan(const TX* __restrict__ x, const AxisEnt
     const int dq0x = px ? 1 : -1, dq0y = py ? nx : -nx;
     const int dq1x = px ? nx : -nx, dq1y = py ? -1 : 1;
     const float stx = px ? 1.0f : -1.0f, sty = py ? 1.0f : -1.0f;
-    float sacc[G];
+    float sacc[NI];
 #pragma unroll
-    for (int j = 0; j < G; j++) sacc[j] = 0.0f;
+    for (int j = 0; j < NI; j++) sacc[j] = 0.0f;
     for (int q = q0; q < q1; q++) {
         const int s = pd ? s1 + q : s2 - q;
         float bh, be;
@@ -623,21 +691,24 @@ __device__ __forceinline__ void walk_fan(const TX* __restrict__ x, const AxisEnt
         float my = __fsub_rn((float)(py ? jy + 1 : jy), Y.kq);
         float Ux = xrel(X, mx, bh, cbx), Uy = xrel(Y, my, bh, cby);
         // p0: the pixel; p1 (G = 4): its quarter turn x * n + n-1-y; the turns
-        // by pi of both are nxy - 1 minus them
+        // by pi of both are nxy - 1 minus them. m0, m1 (RF): the same for the
+        // mirror image M p = (x, ny-1-y) (index (ny-1-y) nx + x) and its
+        // quarter turn (y, x) (index x n + y)
         int p0 = jy * nx + jx, p1 = jx * nx + (nx - 1 - jy);
+        int m0 = (ny - 1 - jy) * nx + jx, m1 = jx * nx + jy;
         float cur = v_in;
         bool in = true;
         const int budget = (hix - lox) + (hiy - loy) + 2;
-        for (int it = 0; it < budget && in; it += kFanBatch) {
-            float seg[kFanBatch];
-            int i0[kFanBatch], i1[kFanBatch];
-            bool live[kFanBatch];
+        for (int it = 0; it < budget && in; it += NB) {
+            float seg[NB];
+            int i0[NB], i1[NB], k0[NB], k1[NB];
+            bool live[NB];
 #pragma unroll
-            for (int u = 0; u < kFanBatch; u++) {
+            for (int u = 0; u < NB; u++) {
                 const float nxt = fminf(Ux, Uy);
                 live[u] = in;
                 seg[u] = __fsub_rn(nxt, cur);
-                i0[u] = p0; i1[u] = p1;
+                i0[u] = p0; i1[u] = p1; k0[u] = m0; k1[u] = m1;
                 if (in) {
                     // the last voxel of the sub-box: its next crossing is the exit
                     const bool more = nxt < v_out;
@@ -645,36 +716,41 @@ __device__ __forceinline__ void walk_fan(const TX* __restrict__ x, const AxisEnt
                         jx += px ? 1 : -1;
                         mx = __fadd_rn(mx, stx); Ux = xrel(X, mx, bh, cbx);
                         p0 += dq0x; p1 += dq1x;
+                        if (RF) { m0 += dq0x; m1 += dq1x; }
                     }
                     if (Uy == nxt) {
                         jy += py ? 1 : -1;
                         my = __fadd_rn(my, sty); Uy = xrel(Y, my, bh, cby);
                         p0 += dq0y; p1 += dq1y;
+                        if (RF) { m0 -= dq0y; m1 -= dq1y; }
                     }
                     cur = nxt;
                     in = more;
                 }
             }
-            float vv[kFanBatch][G];
+            float vv[NB][NI];
 #pragma unroll
-            for (int u = 0; u < kFanBatch; u++) {
-                const int qq[4] = {i0[u], G == 4 ? i1[u] : nxy - 1 - i0[u], nxy - 1 - i0[u],
-                                   nxy - 1 - i1[u]};
+            for (int u = 0; u < NB; u++) {
+                const int qq[8] = {i0[u], G == 4 ? i1[u] : nxy - 1 - i0[u], nxy - 1 - i0[u],
+                                   nxy - 1 - i1[u],
+                                   k0[u], G == 4 ? k1[u] : nxy - 1 - k0[u], nxy - 1 - k0[u],
+                                   nxy - 1 - k1[u]};
 #pragma unroll
-                for (int j = 0; j < G; j++) {
+                for (int j = 0; j < NI; j++) {
+                    const int q = j < G ? qq[j] : qq[4 + j - G];
                     vv[u][j] = 0.0f;
-                    if (live[u] && FL_IN(qq[j], xlen)) vv[u][j] = ldv(x + qq[j]);
+                    if (live[u] && FL_IN(q, xlen)) vv[u][j] = ldv(x + q);
                 }
             }
 #pragma unroll
-            for (int u = 0; u < kFanBatch; u++)
+            for (int u = 0; u < NB; u++)
 #pragma unroll
-                for (int j = 0; j < G; j++)
+                for (int j = 0; j < NI; j++)
                     if (live[u]) sacc[j] = fmaf(seg[u], vv[u][j], sacc[j]);
         }
     }
 #pragma unroll
-    for (int j = 0; j < G; j++) acc[j] = sacc[j];
+    for (int j = 0; j < NI; j++) acc[j] = sacc[j];
 }
 
 // The xy part of a cone ray's crossings with the voxel column (cx, cy): the
@@ -1122,6 +1198,345 @@ __device__ __forceinline__ void fan_turn_adjoint_block(TX* __restrict__ X,
 #pragma unroll
                 for (int k = 1; k < kTurnGroups; k++) sum += part[k][(m * P + j) * P + i][tx];
                 Store<TX>::st(X + (long long)py[m] * nx + px[m], sum);
+            }
+        }
+}
+
+// One block of kFanBlock threads of a fan reflection form's forward (NR = 1,
+// 2 or 4; FanReflGeom): L (1, 4 or 16, uniform in the launch) threads per
+// walked ray r = (slot, column) of the r0, r0 + 1, ... (kFanBlock / L
+// rays), each walking one part of it (walk_fan with the reflected images),
+// their sums added in part order. The walk yields the rays of the 2 NR images
+// (refl_image) of the walked ray, all with its c_r. ypack writes the packed
+// input of the backprojection (the 2 NR values at off + 2 NR ia of
+// refl_slot). Every thread of the block must call it (it synchronises the
+// block).
+template <typename TX, typename TY, int NR>
+__device__ __forceinline__ void fan_refl_forward_block(const TX* __restrict__ X,
+                                                       TY* __restrict__ y,
+                                                       const ColEntry* __restrict__ col,
+                                                       const float* __restrict__ colr, int nx,
+                                                       int ny, int na, int nv, float scale,
+                                                       int cr_power,
+                                                       const float* __restrict__ xscale,
+                                                       int ypack, long long r0, int L)
+{
+    constexpr int NI = 2 * NR;
+    const int nry = kFanBlock / L;             // rays per block
+    const FanReflGeom g = fan_refl_geom(NR, nv, na);
+    const int tx = threadIdx.x % nry, lane = threadIdx.x / nry;
+    const long long r = r0 + tx;
+    int v = 0, vt = 0, a = 0, stride = 0;
+    long long off = 0;
+    const int sl = (int)(r / na), ia = (int)(r - (long long)sl * na);
+    const bool ray = r < (long long)g.slots * na && refl_slot(g, sl, ia, v, vt, a, off, stride);
+    float acc[NI];
+#pragma unroll
+    for (int j = 0; j < NI; j++) acc[j] = 0.0f;
+    const long long rr = (long long)vt * na + a;      // the walked ray's table entry
+    if (ray) walk_fan_parts<TX, NR, true>(X, &col[rr].x, &col[rr].y, nx, ny, acc,
+                                          (long long)nx * ny, lane, L);
+    if (L > 1) {
+        // part k of ray tx is thread k nry + tx: the first nry threads add them in order
+        __shared__ float part[NI][kFanBlock];
+#pragma unroll
+        for (int j = 0; j < NI; j++) part[j][threadIdx.x] = acc[j];
+        __syncthreads();
+        if (lane != 0) return;
+#pragma unroll
+        for (int j = 0; j < NI; j++) {
+            float sum = part[j][tx];
+            for (int k = 1; k < L; k++) sum += part[j][k * nry + tx];
+            acc[j] = sum;
+        }
+    }
+    if (!ray) return;
+    const float cr = ray_cr(scale, colr[rr], 0.0f);
+    float o[NI];
+#pragma unroll
+    for (int j = 0; j < NI; j++) {
+        float t = acc[j];
+        if (xscale) t *= *xscale;
+        o[j] = cr * t;
+        if (cr_power == 2) o[j] = cr * o[j];
+    }
+    if (ypack) {
+#pragma unroll
+        for (int j = 0; j < NI; j += 2) Store<TY>::st2(y + off + (long long)NI * ia + j, o[j], o[j + 1]);
+    } else {
+#pragma unroll
+        for (int k = 0; k < NI; k++) {
+            long long vk; int ak;
+            refl_image<NR>(k, v, a, na, nv, vk, ak);
+            Store<TY>::st(y + vk * na + ak, o[k]);
+        }
+    }
+}
+
+// Primary pixels of a fan reflection form (NR = 4: the octant x <= y < n/2;
+// 2: the quadrant x < nx/2, y < ny/2; 1: the rows y < ny/2) and their images
+// C_k = S^k p, D_k = S^k M p (k < NR), as (x, y).
+template <int NR>
+__host__ __device__ inline bool fan_refl_primary(int ix, int iy, int nx, int ny)
+{
+    if (NR == 4) return ix <= iy && iy < ny / 2;
+    if (NR == 2) return ix < nx / 2 && iy < ny / 2;
+    return ix < nx && iy < ny / 2;
+}
+
+template <int NR>
+__device__ __forceinline__ void fan_refl_images(int ix, int iy, int nx, int ny, int (&cx)[NR],
+                                                int (&cy)[NR], int (&dx)[NR], int (&dy)[NR])
+{
+    if (NR == 4) {
+        cx[0] = ix; cx[1 % NR] = nx - 1 - iy; cx[2 % NR] = nx - 1 - ix; cx[3 % NR] = iy;
+        cy[0] = iy; cy[1 % NR] = ix; cy[2 % NR] = ny - 1 - iy; cy[3 % NR] = ny - 1 - ix;
+        dx[0] = ix; dx[1 % NR] = iy; dx[2 % NR] = nx - 1 - ix; dx[3 % NR] = nx - 1 - iy;
+        dy[0] = ny - 1 - iy; dy[1 % NR] = ix; dy[2 % NR] = iy; dy[3 % NR] = ny - 1 - ix;
+    } else if (NR == 2) {
+        cx[0] = ix; cx[1 % NR] = nx - 1 - ix; cy[0] = iy; cy[1 % NR] = ny - 1 - iy;
+        dx[0] = ix; dx[1 % NR] = nx - 1 - ix; dy[0] = ny - 1 - iy; dy[1 % NR] = iy;
+    } else {
+        cx[0] = ix; cy[0] = iy; dx[0] = ix; dy[0] = ny - 1 - iy;
+    }
+}
+
+// Pixel block of a fan reflection backprojection: PB x PB (1, or 2 where the
+// primary domain tiles into 2 x 2 blocks: NR = 4, n a multiple of 4; NR = 2,
+// nx and ny multiples of 4; NR = 1, nx even and ny a multiple of 4). A
+// function of the geometry alone, so a plan and a batch holding it choose
+// alike.
+__host__ __device__ inline int fan_refl_pblock(int NR, int nx, int ny)
+{
+    if (NR == 4) return nx % 4 == 0 ? 2 : 1;
+    if (NR == 2) return (nx % 4 == 0 && ny % 4 == 0) ? 2 : 1;
+    return (nx % 2 == 0 && ny % 4 == 0) ? 2 : 1;
+}
+
+// Fan reflection backprojection of the primary PB x PB block with lower corner
+// (X0, Y0) over the walked views w = g, g + NG, ... <= ov (FanReflGeom). The
+// thread visits the block's images C_0 .. C_{NR-1} (S^k of the block) and
+// D_0 .. D_{NR-1} (S^k M of it) in one rolled loop. In view w a weight of a
+// pixel of C_k (from the same crossing table as the walk) multiplies turn
+// slot j (view w + j q) into C_{k+j} and reflected slot j (view j q - w,
+// column na-1-a) into D_{j-k}; a weight of a pixel of D_k, turn slot j into
+// D_{k+j} and reflected slot j into C_{j-k}. P holds the turn slots' sums, Q
+// the reflected ones', rotated one place per block image in opposite
+// directions and exchanged between the C and the D images; their pixel index
+// follows the image block's own pixel order (re-indexed by S and M at each
+// step), so at the end P[j][b][a] is C_j's sum and Q[j][b][a] D_j's for the
+// primary pixel (X0 + a, Y0 + b). On the diagonal blocks of NR = 4 (X0 ==
+// Y0) D_k = C_{k+3} T with T the transpose within the block: only the C_k
+// are visited, and C_j of pixel p sums P[j][p] + Q[(j+1) % NR][T p]. Per
+// pixel the sums run over the group's views in order, per view over the
+// images in order and the columns in increasing order; only rays with w > 0
+// add (the block's column window contains each pixel's own).
+template <int NR, int PB>
+__device__ __forceinline__ void fan_refl_gather(float (&P)[NR][PB][PB], float (&Q)[NR][PB][PB],
+                                                const float* __restrict__ ywp,
+                                                const ColEntry* __restrict__ col,
+                                                const ViewEntry* __restrict__ view,
+                                                const DetGrid& D, int X0, int Y0, int nx, int ny,
+                                                int na, int nv, int g, int NG)
+{
+    const FanReflGeom geo = fan_refl_geom(NR, nv, na);
+    const bool diag = NR == 4 && X0 == Y0;
+    const int nsteps = diag ? NR : 2 * NR;
+    // re-index the pixel dimension of P and Q: T[b][a] <- T[f(b, a)]
+    auto turn_px = [&](float (&A)[NR][PB][PB]) {          // the block turned by S
+        if (PB == 1 || NR == 1) return;
+#pragma unroll
+        for (int j = 0; j < NR; j++) {
+            float o[PB][PB];
+#pragma unroll
+            for (int b = 0; b < PB; b++)
+#pragma unroll
+                for (int a = 0; a < PB; a++) o[b][a] = A[j][b][a];
+#pragma unroll
+            for (int b = 0; b < PB; b++)
+#pragma unroll
+                for (int a = 0; a < PB; a++)
+                    // R: new (a, b) holds old (b, PB-1-a); R^2: old (PB-1-a, PB-1-b)
+                    A[j][b][a] = NR == 4 ? o[PB - 1 - a][b] : o[PB - 1 - b][PB - 1 - a];
+        }
+    };
+    auto mirror_px = [&](float (&A)[NR][PB][PB]) {        // M: (a, b) <- (a, PB-1-b)
+        if (PB == 1) return;
+#pragma unroll
+        for (int j = 0; j < NR; j++)
+#pragma unroll
+            for (int a = 0; a < PB; a++) {
+                const float t = A[j][0][a]; A[j][0][a] = A[j][PB - 1][a]; A[j][PB - 1][a] = t;
+            }
+    };
+    for (int w = g; w <= geo.ov; w += NG) {
+        int vt, rs, alim;
+        long long base;
+        refl_view(geo, w, vt, base, rs, alim);
+        const ViewEntry ve = view[vt];
+        const ColEntry* cv = col + (long long)vt * na;
+        const float* yv = ywp + base;
+        int bx = X0, by = Y0;                          // C_0
+#pragma unroll 1
+        for (int k = 0; k < nsteps; k++) {
+            if (k == NR) {                             // the D images: D_0 = M block
+                bx = X0; by = ny - Y0 - PB;
+#pragma unroll
+                for (int j = 0; j < NR; j++)
+#pragma unroll
+                    for (int b = 0; b < PB; b++)
+#pragma unroll
+                        for (int a = 0; a < PB; a++) {
+                            const float t = P[j][b][a]; P[j][b][a] = Q[j][b][a]; Q[j][b][a] = t;
+                        }
+                mirror_px(P);
+                mirror_px(Q);
+            }
+            int lo, hi; float dmin, dmax;
+            column_window(D, ve.c, ve.s, (float)(bx - nx / 2), (float)(by - ny / 2), (float)PB,
+                          (float)PB, na, lo, hi, dmin, dmax);
+            hi = min(hi, alim - 1);
+            for (int ia = lo; ia <= hi; ia++) {
+                if (!FL_IN(ia, na)) continue;
+                const ColEntry ce = cv[ia];
+                float ax[PB + 1], ay[PB + 1];
+                fan_block_crossings<PB, PB>(ce, bx, by, nx, ny, ax, ay);
+                float t[2 * NR];
+                const float* yo = yv + (long long)(2 * NR) * ia;
+                if constexpr (NR == 4) {
+                    const float4 u0 = __ldg(reinterpret_cast<const float4*>(yo));
+                    const float4 u1 = __ldg(reinterpret_cast<const float4*>(yo) + 1);
+                    t[0] = u0.x; t[1] = u0.y; t[2] = u0.z; t[3] = u0.w;
+                    t[4] = u1.x; t[5] = u1.y; t[6] = u1.z; t[7] = u1.w;
+                } else if constexpr (NR == 2) {
+                    const float4 u = __ldg(reinterpret_cast<const float4*>(yo));
+                    t[0] = u.x; t[1] = u.y; t[2] = u.z; t[3] = u.w;
+                } else {
+                    const float2 u = __ldg(reinterpret_cast<const float2*>(yo));
+                    t[0] = u.x; t[1] = u.y;
+                }
+#pragma unroll
+                for (int b = 0; b < PB; b++)
+#pragma unroll
+                    for (int a = 0; a < PB; a++) {
+                        const float l = fmaxf(fminf(ax[a], ax[a + 1]), fminf(ay[b], ay[b + 1]));
+                        const float h = fminf(fmaxf(ax[a], ax[a + 1]), fmaxf(ay[b], ay[b + 1]));
+                        const float wt = h - l;
+                        if (!(wt > 0.0f)) continue;
+#pragma unroll
+                        for (int j = 0; j < NR; j++) {
+                            P[j][b][a] = fmaf(wt, t[j], P[j][b][a]);
+                            Q[j][b][a] = fmaf(wt, t[NR + j], Q[j][b][a]);
+                        }
+                    }
+            }
+            // next image S (block); P rotates back one place, Q forward one;
+            // the pixel index follows the turned block
+            if (NR == 4) {
+                const int tt = bx;
+                bx = nx - by - PB; by = tt;
+            } else if (NR == 2) {
+                bx = nx - bx - PB; by = ny - by - PB;
+            }
+            if (NR > 1) {
+#pragma unroll
+                for (int b = 0; b < PB; b++)
+#pragma unroll
+                    for (int a = 0; a < PB; a++) {
+                        const float a0 = P[0][b][a];
+#pragma unroll
+                        for (int j = 0; j + 1 < NR; j++) P[j][b][a] = P[j + 1][b][a];
+                        P[NR - 1][b][a] = a0;
+                        const float b0 = Q[NR - 1][b][a];
+#pragma unroll
+                        for (int j = NR - 1; j > 0; j--) Q[j][b][a] = Q[j - 1][b][a];
+                        Q[0][b][a] = b0;
+                    }
+                turn_px(P);
+                turn_px(Q);
+            }
+        }
+        if (!diag) {                                   // back to the C order
+            mirror_px(P);
+            mirror_px(Q);
+#pragma unroll
+            for (int j = 0; j < NR; j++)
+#pragma unroll
+                for (int b = 0; b < PB; b++)
+#pragma unroll
+                    for (int a = 0; a < PB; a++) {
+                        const float t = P[j][b][a]; P[j][b][a] = Q[j][b][a]; Q[j][b][a] = t;
+                    }
+        }
+    }
+}
+
+// Shared floats fan_refl_adjoint_block needs (the largest form: NR = 4,
+// 2 x 2 blocks).
+constexpr int kFanReflShared = kTurnGroups * 2 * 4 * 4 * kFanX;
+
+// One block of a fan reflection backprojection: thread (x, g) of a block of
+// kFanX x kTurnGroups threads takes the PB x PB block of primary pixels with
+// lower corner (PB (bx0 + x), PB by) where it is a primary block (in block
+// units: x < the domain's width; NR = 4: x <= by) over view group g of the
+// walked views (fan_refl_gather). The groups' sums meet in shared memory
+// (smem: kFanReflShared floats) and are added in the order g = 0, 1, ...;
+// group 0 stores the images. Every thread of the block must call it (it
+// synchronises the block).
+template <typename TX, int NR, int PB>
+__device__ __forceinline__ void fan_refl_adjoint_block(TX* __restrict__ X,
+                                                       const float* __restrict__ ywp,
+                                                       const ColEntry* __restrict__ col,
+                                                       const ViewEntry* __restrict__ view,
+                                                       const DetGrid& D, int nx, int ny, int na,
+                                                       int nv, int bx0, int by, float* smem)
+{
+    constexpr int NV = NR * PB * PB;
+    const int tx = threadIdx.x, g = threadIdx.y, bx = bx0 + tx;
+    const int hxb = (NR == 1 ? nx : nx / 2) / PB, hyb = (ny / 2) / PB;
+    const bool prim = bx < hxb && by < hyb && (NR != 4 || bx <= by);
+    const int X0 = PB * bx, Y0 = PB * by;
+    float P[NR][PB][PB], Q[NR][PB][PB];
+#pragma unroll
+    for (int j = 0; j < NR; j++)
+#pragma unroll
+        for (int b = 0; b < PB; b++)
+#pragma unroll
+            for (int a = 0; a < PB; a++) { P[j][b][a] = 0.0f; Q[j][b][a] = 0.0f; }
+    if (prim)
+        fan_refl_gather<NR, PB>(P, Q, ywp, col, view, D, X0, Y0, nx, ny, na, nv, g, kTurnGroups);
+    static_assert(kTurnGroups * 2 * NV * kFanX <= kFanReflShared, "shared buffer");
+    float(*part)[2 * NV][kFanX] = reinterpret_cast<float(*)[2 * NV][kFanX]>(smem);
+#pragma unroll
+    for (int j = 0; j < NR; j++)
+#pragma unroll
+        for (int b = 0; b < PB; b++)
+#pragma unroll
+            for (int a = 0; a < PB; a++) {
+                part[g][(j * PB + b) * PB + a][tx] = P[j][b][a];
+                part[g][NV + (j * PB + b) * PB + a][tx] = Q[j][b][a];
+            }
+    __syncthreads();
+    if (g != 0 || !prim) return;
+    auto sum = [&](int k) {
+        float t = part[0][k][tx];
+#pragma unroll
+        for (int m = 1; m < kTurnGroups; m++) t += part[m][k][tx];
+        return t;
+    };
+    const bool diag = NR == 4 && X0 == Y0;
+#pragma unroll
+    for (int b = 0; b < PB; b++)
+#pragma unroll
+        for (int a = 0; a < PB; a++) {
+            int cx[NR], cy[NR], dx[NR], dy[NR];
+            fan_refl_images<NR>(X0 + a, Y0 + b, nx, ny, cx, cy, dx, dy);
+#pragma unroll
+            for (int j = 0; j < NR; j++) {
+                float c = sum((j * PB + b) * PB + a);
+                if (diag) c += sum(NV + (((j + 1) % NR) * PB + a) * PB + b);   // Q[j+1][T p]
+                Store<TX>::st(X + (long long)cy[j] * nx + cx[j], c);
+                if (!diag) Store<TX>::st(X + (long long)dy[j] * nx + dx[j], sum(NV + (j * PB + b) * PB + a));
             }
         }
 }

@@ -139,8 +139,10 @@ class Plan:
     @property
     def reflect(self) -> bool:
         """Whether the matched pair also uses the reflection between views v
-        and nv - v about the x axis (FL_OPT_REFLECT; cone plans, with the half
-        or the quarter turn and a detector symmetric about its centre)."""
+        and nv - v about the x axis (FL_OPT_REFLECT; with the half or the
+        quarter turn and a detector symmetric about its centre, or, on a fan
+        plan of an odd view count, alone). On by default for cone plans; fan
+        plans take it when it is set (FanBatch sets it for its slices)."""
         v = C.c_int()
         _lib.check(self._L.fl_plan_query(self._h, _lib.OPT_REFLECT, C.byref(v)))
         return bool(v.value)

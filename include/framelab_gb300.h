@@ -208,15 +208,25 @@ int fl_plan_sizes(const fl_plan *plan, int64_t *n_vox, int64_t *n_rays);
  *   odd detector at a view angle of exactly 0) has no unique discretisation:
  *   on the turn forms its turned copies take the walked view's choice, which
  *   can differ from the general kernels' at O(1) for that ray alone. */
-/* FL_OPT_REFLECT: on top of FL_OPT_QUARTER_TURN (cone plans), on by default
- *   when nv is a multiple of 8, view nv - v is the mirror image of view v
- *   about the x axis (to within 1e-6) and the detector is symmetric about its
- *   centre (y_det[na-1-a] == -y_det[a], na even). Ray (j nv/4 - v, na-1-a, b)
- *   is then defined as ray (v, a, b) reflected by M (x, y, z) = (x, n-1-y, z)
- *   and turned by j pi/2, for the walked views v = 0 .. nv/8 (views 0 and
- *   nv/8 walk their columns a < na/2, the other half being their mirror
- *   images; view nv/8 is walked at the exact angle pi/4): one walk or weight
- *   serves sixteen rays. Queries report 0 while any option below it is off. */
+/* FL_OPT_REFLECT: on by default for cone plans, and taken by fan plans when
+ *   set (a single small fan scan has too few walked rays and pixel blocks to
+ *   fill the GPU with it: 256^2, 360 views, 6107 against 6851 CGLS it/s;
+ *   batches of many slices gain: 64 uneven slices, 61.9 against 51.9 it/s),
+ *   where view 0 is at angle 0, view nv - v is
+ *   the mirror image of view v about the x axis (to within 1e-6) and the
+ *   detector is symmetric about its centre (y_det[na-1-a] == -y_det[a], na
+ *   even), on top of the quarter turns (with nv a multiple of 8) or of the
+ *   half turn; fan plans of one frame with an odd view count and ny even
+ *   also take it alone. With M (x, y) = (x, ny-1-y), S the quarter turn R,
+ *   the half turn R^2 or (alone) the identity, NR = 4, 2, 1 its order and q =
+ *   nv/NR, ray (j q - v, na-1-a, b) is defined as ray (v, a, b) reflected by
+ *   M and turned by S^j, for the walked views v = 0 .. floor(q/2). View 0,
+ *   and view q/2 where q is even (then its own mirror image), walk their
+ *   columns a < na/2, the other half being their mirror images; view q/2 is
+ *   walked at the exact angle pi/NR (cone: the quarter or half turn; fan:
+ *   the same). One walk or weight serves sixteen (cone, quarter turns),
+ *   eight (cone, half turn; fan, quarter turns), four (fan, half turn) or two
+ *   (fan, alone) rays. Queries report 0 while an option it rides on is off. */
 enum { FL_OPT_Z_MIRROR = 1, FL_OPT_ROT_MIRROR = 2, FL_OPT_QUARTER_TURN = 3,
        FL_OPT_REFLECT = 4 };
 int fl_plan_option(fl_plan *plan, int option, int value);
@@ -389,8 +399,10 @@ int fl_cgls_solve_host(fl_cgls *cg, const float *b_host, float *u_host, float la
  * A batch projects and solves many independent single-frame fan-beam scans of
  * different sizes at once (matched model): images and sinograms of all slices
  * are concatenated in plan order (offsets from fl_batch_layout) and every
- * operator is one launch over all slices (two when some slices' plans use
- * FL_OPT_ROT_MIRROR / FL_OPT_QUARTER_TURN: those run the turn kernels). Each
+ * operator is one launch over all slices of a kind: general slices, slices
+ * whose plans use a turn alone (FL_OPT_ROT_MIRROR / FL_OPT_QUARTER_TURN) and
+ * slices whose plans use a reflection form (FL_OPT_REFLECT) run those
+ * plans' kernels, as parallel branches of the stream. Each
  * slice's forward/adjoint result is bit-identical to its own plan's, with the
  * plan's options as they were at fl_batch_create. The plans must outlive the
  * batch.
@@ -409,8 +421,9 @@ int fl_batch_adjoint(fl_batch *b, const float *y, float *x, void *stream);
  * guess in (ignored with FL_CGLS_ZERO_START), result out (device).
  * gamma_history (host, optional): [n_plans * iters], row i = slice i's gamma
  * after each iteration (0 after it stopped); iters_done (host, optional):
- * [n_plans]. One iteration is a replayed CUDA graph of 5 launches (7 when
- * the batch mixes turn and general slices). */
+ * [n_plans]. One iteration is a replayed CUDA graph of 3 launches plus a
+ * forward and a backprojection for each kind of slice present (general,
+ * turn, reflection; the kinds run as parallel branches). */
 int fl_batch_cgls(fl_batch *b, const float *rhs, float *u, float lam, int32_t iters, double tol,
                   int32_t flags, double *gamma_history, int32_t *iters_done, void *stream);
 /* Launch tuner of a batch: times the parts per walked ray of its half- and

@@ -59,15 +59,17 @@ def snapped(para, turns: int, reflect: bool = False) -> dict:
     """The scan a plan with `turns` views per rotation orbit projects: FP64
     angles phi[v + j nv/turns] = phi[v] + j 2 pi / turns for v < nv/turns (the
     FP32 angles of the walked views, turned exactly). With the reflection
-    about the x axis (reflect, or turns = 8 for the quarter turns with it),
-    the walked views are v = 0 .. floor(nv / (2 turns)) -- the last one at
-    exactly pi/turns where it is its own mirror image (nv a multiple of
-    2 turns) -- and view j nv/turns - v is view v reflected and turned, at
-    angle j 2 pi / turns - phi[v]."""
+    about the x axis (reflect, or turns = 8 for the quarter turns with it;
+    turns = 1 for a fan's reflection alone, odd nv), the walked views are
+    v = 0 .. floor(nv / (2 turns)) -- the last one at exactly pi/turns where
+    it is its own mirror image (nv a multiple of 2 turns) -- and view
+    j nv/turns - v is view v reflected and turned, at angle
+    j 2 pi / turns - phi[v]."""
     if turns == 8:
         turns, reflect = 4, True
-    if turns <= 1:
+    if turns <= 1 and not reflect:
         return para
+    turns = max(turns, 1)
     phi = np.asarray(para["sd_phi"], np.float32).astype(np.float64)
     nv = phi.size
     q = nv // turns
@@ -97,7 +99,7 @@ def fan_parity(para, x, forward, adjoint, seed=0, threads=None, turns=1,
                reflect=False) -> dict:
     """Full fan-beam check: every ray, every pixel."""
     t = _threads(threads)
-    ps = snapped(para, turns, reflect) if turns > 1 else None
+    ps = snapped(para, turns, reflect) if (turns > 1 or reflect) else None
     x = np.ascontiguousarray(x, np.float32).reshape(-1)
     y = np.asarray(forward(x), np.float32).reshape(-1)
     out = {"forward": dict(rays=int(y.size), **_three(
@@ -116,7 +118,7 @@ def cone_parity(para, x, forward, adjoint, n_rays=20000, n_vox=4000, seed=0,
                 threads=None, turns=1, reflect=False) -> dict:
     """Cone-beam check on ``n_rays`` random rays and ``n_vox`` random voxels."""
     t = _threads(threads)
-    ps = snapped(para, turns, reflect) if turns > 1 else None
+    ps = snapped(para, turns, reflect) if (turns > 1 or reflect) else None
     rng = np.random.default_rng(seed)
     x = np.ascontiguousarray(x, np.float32).reshape(-1)
     y = np.asarray(forward(x), np.float32).reshape(-1)

@@ -34,12 +34,13 @@ def run_plan(p, rng):
             P.adjoint(y)
             P.adjoint(y.half())
         P.z_mirror, P.rot_mirror, P.quarter_turn, P.reflect = True, True, True, True
-    else:                              # fan: half turn, then the general kernels
-        for q, r in ((False, True), (False, False)):
-            P.quarter_turn, P.rot_mirror = q, r
+    else:                              # fan: every form the plan allows
+        for f, q, r in ((False, True, True), (True, False, True), (False, False, True),
+                        (True, False, False), (False, False, False)):
+            P.reflect, P.quarter_turn, P.rot_mirror = f, q, r
             P.forward(x)
             P.adjoint(y)
-        P.rot_mirror, P.quarter_turn = True, True
+        P.rot_mirror, P.quarter_turn, P.reflect = True, True, True
     for mode in ("graph", "mixed"):
         NativeCGLS(P, mode).solve(torch.abs(x), lam=0.1, iters=3, refresh=2)
 
@@ -69,6 +70,10 @@ def main():
         G.fan_para(512, 512, 1024, 60, L=(1, 1)),                      # fan, 2 x 2 blocks
         G.fan_para(48, 36, 97, 42, L=(1, 0.75), SO=3.0, OD=3.0, Ly=3.0),  # fan, rectangular
         G.fan_para(640, 480, 64, 6, L=(1, 0.75), SO=3.0, OD=3.0, Ly=3.0),  # fan, 2 x 2 turn blocks
+        G.fan_para(64, 64, 128, 31, L=(1, 1)),                         # fan, reflection alone
+        G.fan_para(64, 64, 128, 32, L=(1, 1)),                         # fan, quarter turns + refl.
+        G.fan_para(48, 36, 96, 40, L=(1, 0.75), SO=3.0, OD=3.0, Ly=3.0),  # half turn + refl., end view
+        G.fan_para(512, 512, 1024, 61, L=(1, 1)),                      # reflection alone, large
     ]
     for p in cases:
         run_plan(p, rng)
@@ -85,6 +90,21 @@ def main():
     assert B.turns == [4, 2, 1, 2], B.turns
     xb = torch.rand(B.n_vox, device="cuda")
     B.adjoint(B.forward(xb))
+    B.cgls(B.adjoint(B.forward(xb)), iters=3)
+    # a batch with reflection slices of every form beside turn and general ones
+    sl = [(32, 32, 64, 37), (32, 32, 64, 40), (24, 40, 62, 14), (40, 24, 80, 12),
+          (32, 32, 64, 44), (20, 20, 41, 11), (16, 16, 32, 1)]
+    B = FanBatch([G.fan_para(nx, ny, nd, nv, L=(1.0, ny / nx), SO=3.0, OD=3.0, Ly=3.0)
+                  for nx, ny, nd, nv in sl])
+    assert B.turns == [2, 8, 4, 4, 4, 1, 2], B.turns
+    xb = torch.rand(B.n_vox, device="cuda")
+    B.adjoint(B.forward(xb))
+    B.cgls(B.adjoint(B.forward(xb)), iters=3)
+    for parts in (1, 4, 16):
+        Bp = FanBatch([G.fan_para(nx, ny, nd, nv, L=(1.0, ny / nx), SO=3.0, OD=3.0, Ly=3.0)
+                       for nx, ny, nd, nv in sl], fan_parts=parts)
+        Bp.adjoint(Bp.forward(xb))
+    B.autotune()
     B.cgls(B.adjoint(B.forward(xb)), iters=3)
     # the class mirror's default scanner geometry
     cb = Operators.ConeBeamScanner("circle", 36, 32, 10, model="matched")

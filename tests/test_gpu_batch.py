@@ -100,6 +100,60 @@ def test_batch_turn_slices_bit_identical_to_single_plans():
         assert float((a - b).norm() / b.norm()) < 1e-5, i
 
 
+# views evenly over a full turn with symmetric detectors of even width: the
+# reflection alone (odd nv, and a single view), with the quarter turns (nv a
+# multiple of 8), with the half turn (with and without an end view), beside a
+# quarter-turn slice (nv = 4 mod 8) and a general one (odd detector width)
+REFL_SLICES = [(32, 32, 64, 37), (32, 32, 64, 40), (24, 40, 62, 14), (40, 24, 80, 12),
+               (32, 32, 64, 44), (20, 20, 41, 11), (16, 16, 32, 1)]
+
+
+def test_batch_reflection_slices_bit_identical_to_single_plans():
+    """Slices whose plans use a reflection form run those forms' kernels in
+    the batch (a third branch beside the turn and the general slices): each
+    slice's forward and backprojection equal its plan's bit for bit, and the
+    batched CGLS equals the single-slice graph solver's bits too."""
+    import torch
+    from framelab_gb300.batch import FanBatch
+    from framelab_gb300.solvers import NativeCGLS
+    rng = np.random.default_rng(3)
+    paras = [G.fan_para(nx, ny, nd, nv, L=(1.0, ny / nx), SO=rng.uniform(3, 6),
+                        OD=rng.uniform(3, 6), Ly=rng.uniform(5, 8))
+             for nx, ny, nd, nv in REFL_SLICES]
+    B = FanBatch(paras)
+    assert B.turns == [2, 8, 4, 4, 4, 1, 2], B.turns
+    assert B.reflect == [True, True, True, True, False, False, True]
+    assert B.launches_per_iteration == 9
+    x = torch.from_numpy(rng.standard_normal(B.n_vox).astype(np.float32)).cuda()
+    y = torch.from_numpy(rng.standard_normal(B.n_rays).astype(np.float32)).cuda()
+    yb, xb = B.forward(x), B.adjoint(y)
+    torch.cuda.synchronize()
+    for i, P in enumerate(B.plans):
+        xi = B.images(x)[i].reshape(-1).contiguous()
+        yi = B.sinograms(y)[i].reshape(-1).contiguous()
+        assert torch.equal(B.sinograms(yb)[i].reshape(-1),
+                           P.forward(xi, model="matched").reshape(-1)), i
+        assert torch.equal(B.images(xb)[i].reshape(-1),
+                           P.adjoint(yi, model="matched").reshape(-1)), i
+    b = B.adjoint(B.forward(x))
+    ub = B.cgls(b, iters=4)
+    for i, P in enumerate(B.plans):
+        bi = B.images(b)[i].reshape(-1).contiguous()
+        ui = NativeCGLS(P, "graph").solve(bi, iters=4)
+        assert float((B.images(ub)[i].reshape(-1) - ui).norm() / ui.norm()) < 1e-5, i
+    # the batch tuner covers the reflection slices' parts too
+    parts = B.autotune()
+    assert parts in (1, 4, 16)
+    for P, t in zip(B.plans, B.turns):
+        if t > 1:
+            P.set_tuning("fan_parts", parts)
+    yb = B.forward(x)
+    for i, P in enumerate(B.plans):
+        xi = B.images(x)[i].reshape(-1).contiguous()
+        assert torch.equal(B.sinograms(yb)[i].reshape(-1),
+                           P.forward(xi, model="matched").reshape(-1)), i
+
+
 def test_batch_autotune_and_parts_keep_batch_equal_to_plans():
     """A batch takes its turn slices' parts per walked ray from their plans
     (here set to 4), and its own tuner sets one count for all of them; either
@@ -146,16 +200,20 @@ def test_batch_tiny_slices_of_every_kind_bit_identical():
     """Degenerate slices in one batch: one view (general), a one-pixel-wide
     image (general: the turns need even nx and ny), a single detector column
     over a 2 x 2 image (half turn), a 2 x 2 image (quarter turn), beside a
-    normal slice."""
+    normal slice, and 2 x 2 images with the reflection alone (3 views) and
+    with the quarter turns (8 views: the one primary pixel is on the
+    diagonal)."""
     import torch
     from framelab_gb300.batch import FanBatch
     paras = [G.fan_para(2, 2, 3, 1, L=(1.0, 1.0), SO=3.0, OD=3.0, Ly=3.0, y_os=0.013),
              G.fan_para(1, 2, 1, 2, L=(1.0, 2.0), SO=3.0, OD=3.0, Ly=3.0, y_os=0.013),
              G.fan_para(2, 2, 1, 2, L=(1.0, 1.0), SO=3.0, OD=3.0, Ly=3.0, y_os=0.013),
              G.fan_para(2, 2, 2, 4, L=(1.0, 1.0), SO=3.0, OD=3.0, Ly=3.0),
-             G.fan_para(24, 24, 48, 12, L=(1.0, 1.0), SO=3.0, OD=3.0, Ly=3.0)]
+             G.fan_para(24, 24, 48, 12, L=(1.0, 1.0), SO=3.0, OD=3.0, Ly=3.0),
+             G.fan_para(2, 2, 2, 3, L=(1.0, 1.0), SO=3.0, OD=3.0, Ly=3.0),
+             G.fan_para(2, 2, 2, 8, L=(1.0, 1.0), SO=3.0, OD=3.0, Ly=3.0)]
     B = FanBatch(paras)
-    assert B.turns == [1, 1, 2, 4, 4]
+    assert B.turns == [1, 1, 2, 4, 4, 2, 8]
     rng = np.random.default_rng(14)
     x = torch.from_numpy(rng.standard_normal(B.n_vox).astype(np.float32)).cuda()
     y = torch.from_numpy(rng.standard_normal(B.n_rays).astype(np.float32)).cuda()

@@ -63,13 +63,18 @@ def _check(res, turns):
             assert r["matched_vs_reference"] < max(snap, r["reference_vs_fp64"] + snap), (op, r)
 
 
-def _plans(p):
+def _plans(p, fan_reflect=False):
+    """The default plan, the plan without its turns (and reflection) and, for a
+    fan scan with fan_reflect, the plan with the reflection taken."""
     from framelab_gb300.projector import Plan
-    for turns_on in (True, False):
+    for form in ("default", "general") + (("reflect",) if fan_reflect else ()):
         P = Plan(p)
-        if not turns_on:
+        if form == "general":
             P.quarter_turn = False
             P.rot_mirror = False
+            P.reflect = False
+        elif form == "reflect":
+            P.reflect = True
         yield P
 
 
@@ -82,11 +87,11 @@ def test_fan256_full(field_mm):
                    Ly=2.0 * math.sqrt(2.0) * L)
     x = PH.ellipses_2d(256, seed=1)
     forms = []
-    for P in _plans(p):
+    for P in _plans(p, fan_reflect=True):
         t = _turns(P)
         forms.append(t)
         _check(PAR.fan_parity(p, x, *_ops(P), turns=P.rotations, reflect=P.reflect), t)
-    assert forms == [4, 1]
+    assert forms == [4, 1, 8]
 
 
 @pytest.mark.parametrize("n", [256, 512])

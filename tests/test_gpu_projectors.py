@@ -762,6 +762,7 @@ def test_fan_turns_agree_with_general_kernels_and_are_exact(shape):
     n, ny, nv, nd = shape
     p = _fan_turn_para(n, ny, nv, nd=nd)
     P = _plan(p)
+    P.reflect = False                  # the turns alone (the reflection: below)
     G4 = P.quarter_turn
     assert P.rot_mirror and G4 == (n == ny and nv % 4 == 0)
     X = PH.ellipses_2d(max(n, ny), seed=5)[:ny, :n]
@@ -833,6 +834,7 @@ def test_fan_turn_large_images_use_2x2_blocks(shape):
     nx, ny, nd, nv = shape
     p = G.fan_para(nx, ny, nd, nv, L=(1.0, ny / nx), SO=3.0, OD=3.0, Ly=3.0)
     P = _plan(p)
+    P.reflect = False
     assert P.rot_mirror and P.quarter_turn == (nx == ny)
     hx, hy = (nx // 2 if nx == ny else nx), ny // 2
     assert -(-hx // 64) * -(-hy // 2) >= 4 * 152           # the 2 x 2 form
@@ -849,6 +851,112 @@ def test_fan_turn_large_images_use_2x2_blocks(shape):
     lhs = np.dot(y.astype(np.float64), r.astype(np.float64))
     rhs = np.dot(x.astype(np.float64), xa.astype(np.float64))
     assert abs(lhs - rhs) / abs(lhs) < 1e-5
+
+
+# fan reflection forms: (nx, ny, nd, nv) -> views per walk. The reflection
+# alone (odd nv), with the half turn (nv even; with an end view at pi/2 when
+# nv is a multiple of 4 on a rectangle), with the quarter turns (square, nv a
+# multiple of 8). The backprojection takes 2 x 2 pixel blocks where the
+# primary domain tiles into them (sizes multiples of 4; the octant's diagonal
+# blocks through the transpose), single pixels otherwise (the last three).
+FAN_REFL = [((40, 40, 96, 37), 2), ((36, 48, 80, 9), 2), ((48, 36, 96, 42), 4),
+            ((48, 36, 96, 40), 4), ((48, 48, 96, 48), 8), ((48, 48, 96, 1), 2),
+            ((42, 42, 96, 48), 8), ((38, 38, 80, 37), 2), ((44, 38, 96, 42), 4)]
+
+
+def test_fan_reflection_is_detected_only_for_mirror_scans():
+    """The reflection needs view 0 at angle 0, views nv - v mirror images of
+    views v, a detector symmetric about its centre (even width) and, alone, an
+    odd view count and ny even; with the quarter turns nv a multiple of 8."""
+    def plan(nx, ny, nd, nv, **kw):
+        P = _plan(G.fan_para(nx, ny, nd, nv, L=(1.0, ny / nx), SO=3.0, OD=3.0, Ly=3.0, **kw))
+        assert not P.reflect                      # fan plans take it when asked
+        P.reflect = True
+        return P
+    Q = plan(40, 40, 64, 44)                      # nv = 4 mod 8: the quarter turns alone
+    assert Q.quarter_turn and not Q.reflect and Q.views_per_walk == 4
+    assert not plan(40, 40, 65, 37).reflect       # odd detector width
+    assert not plan(40, 40, 64, 37, y_os=0.1).reflect   # detector off centre
+    assert not plan(40, 39, 64, 37).reflect       # odd ny: no primary half
+    phi = (2 * np.pi / 37 * np.arange(37) + 0.01).astype(np.float32)
+    assert not plan(40, 40, 64, 37, sd_phi=phi).reflect   # view 0 not at angle 0
+    R = plan(40, 40, 64, 37)
+    assert R.reflect and not R.rot_mirror and R.views_per_walk == 2
+    R.reflect = False
+    assert not R.reflect and R.views_per_walk == 1
+
+
+@pytest.mark.parametrize("shape,vpw", FAN_REFL)
+def test_fan_reflection_forms_are_exact(shape, vpw):
+    """Fan reflection forms: view nv - v, column nd-1-a of A x equals view v,
+    column a of A M(x) (M (x, y) = (x, ny-1-y)) bit for bit, and the turns
+    still hold bit for bit; the pair stays the exact transpose (dot test);
+    both operators are within 2e-6 (forward) and 5e-6 (backprojection of
+    noise) of the FP64 model of the scan the plan projects (the reflected and
+    turned views at their exact angles, oracle/parity.py snapped); FP16
+    storage goes through the same kernels; the CUDA-graph CGLS follows the
+    option."""
+    import oracle.parity as PAR
+    from framelab_gb300.solvers import NativeCGLS
+    torch = _torch()
+    nx, ny, nd, nv = shape
+    p = G.fan_para(nx, ny, nd, nv, L=(1.0, ny / nx), SO=3.0, OD=3.0, Ly=3.0)
+    P = _plan(p)
+    P.reflect = True
+    assert P.reflect and P.views_per_walk == vpw, (P.reflect, P.views_per_walk)
+    rng = np.random.default_rng(nv)
+    X = rng.uniform(0, 1, (ny, nx)).astype(np.float32)
+    x = X.reshape(-1).copy()
+    r = rng.standard_normal(P.n_rays).astype(np.float32)
+    yt, xt = _host(P.forward(_dev(x))), _host(P.adjoint(_dev(r)))
+    Y = yt.reshape(nv, nd)
+    # the reflection: view (nv - v) mod nv, column nd-1-a of A x = view v,
+    # column a of A M(x)
+    ym = _host(P.forward(_dev(X[::-1, :].reshape(-1).copy()))).reshape(nv, nd)
+    assert np.array_equal(Y[(-np.arange(nv)) % nv, ::-1], ym)
+    # the turns
+    if P.quarter_turn:
+        yr = _host(P.forward(_dev(X[:, ::-1].T.reshape(-1).copy()))).reshape(nv, nd)
+        assert np.array_equal(Y[(np.arange(nv) + nv // 4) % nv], yr)
+    elif P.rot_mirror:
+        yh = _host(P.forward(_dev(X[::-1, ::-1].reshape(-1).copy()))).reshape(nv, nd)
+        assert np.array_equal(Y[(np.arange(nv) + nv // 2) % nv], yh)
+    lhs = np.dot(yt.astype(np.float64), r.astype(np.float64))
+    rhs = np.dot(x.astype(np.float64), xt.astype(np.float64))
+    assert abs(lhs - rhs) / abs(lhs) < 1e-5, (lhs, rhs)
+    ps = PAR.snapped(p, P.rotations, True)
+    assert _rel(yt, O.exact_forward(x, ps)) < 2e-6
+    assert _rel(xt, O.exact_adjoint(r, ps)) < 5e-6
+    # the nominal scan differs from it by the angle snap only
+    assert _rel(yt, O.exact_forward(x, p)) < 1e-5
+    assert _rel(_host(P.forward(_dev(x, torch.float16))), yt) < 2e-3
+    b = P.adjoint(P.forward(_dev(x))).reshape(-1).contiguous()
+    cg = NativeCGLS(P, "graph")
+    u1 = _host(cg.solve(b, iters=5).clone())
+    P.reflect = False
+    u0 = _host(cg.solve(b, iters=5).clone())
+    P.reflect = True
+    u2 = _host(cg.solve(b, iters=5).clone())
+    assert np.array_equal(u1, u2) and _rel(u1, u0) < 1e-4
+
+
+def test_fan_reflection_large_image():
+    """A 512 x 512 quarter-turn scan with the reflection (720 views, 1024
+    bins): within 2e-6 / 5e-6 of the FP64 model of its scan, at the size
+    where the pixel count per thread block and the parts per ray matter."""
+    import oracle.parity as PAR
+    p = G.fan_para(512, 512, 1024, 720, L=(1.0, 1.0), SO=3.0, OD=3.0, Ly=3.0)
+    P = _plan(p)
+    P.reflect = True
+    assert P.views_per_walk == 8
+    rng = np.random.default_rng(3)
+    x = rng.uniform(0, 1, P.n_vox).astype(np.float32)
+    r = rng.standard_normal(P.n_rays).astype(np.float32)
+    y, xa = _host(P.forward(_dev(x))), _host(P.adjoint(_dev(r)))
+    ps = PAR.snapped(p, 4, True)
+    th = os.cpu_count() or 1
+    assert _rel(y, O.exact_forward(x, ps, threads=th)) < 2e-6
+    assert _rel(xa, O.exact_adjoint(r, ps, threads=th)) < 5e-6
 
 
 @pytest.mark.parametrize("zm", [True, False])
@@ -882,21 +990,27 @@ def test_autotune_keeps_the_projections(zm):
         assert L.fl_plan_option(P.handle, _lib.TUNE_ADJ_ROWS, 4) == _lib.FL_ERR_INVALID
 
 
-@pytest.mark.parametrize("nv", [20, 18, 9])
-def test_fan_autotune_parts_and_pixel_block(nv):
-    """Fan plans: the tuner picks the parts per walked ray of the turn forward
-    (quarter turn at nv = 20, half turn at 18; the general plan at 9 has no
-    parts) and the backprojection's pixel block. The pixel block keeps every
-    bit; the parts change only the order of a ray's additions."""
+@pytest.mark.parametrize("nv,refl", [(20, True), (18, False), (18, True), (9, False),
+                                     (9, True)])
+def test_fan_autotune_parts_and_pixel_block(nv, refl):
+    """Fan plans: the tuner picks the parts per walked ray of the turn and
+    reflection forwards (quarter turn at nv = 20; half turn at 18, with the
+    reflection or not; at 9 the reflection alone, or the general plan, which
+    has no parts) and the backprojection's pixel block. The pixel block keeps
+    every bit; the parts change only the order of a ray's additions."""
     from framelab_gb300 import _lib
     P = _plan(G.fan_para(64, 64, 128, nv, L=(1, 1), SO=3.0, OD=3.0, Ly=3.0))
+    P.reflect = refl
+    assert P.views_per_walk == {(20, True): 4, (18, False): 2, (18, True): 4, (9, False): 1,
+                                (9, True): 2}[(nv, refl)]
     rng = np.random.default_rng(nv)
     x = _dev(rng.standard_normal(P.n_vox).astype(np.float32))
     r = _dev(rng.standard_normal(P.n_rays).astype(np.float32))
     y0, x0 = _host(P.forward(x)), _host(P.adjoint(r))
     sh = P.autotune()
     assert sh["adjoint_pixel_block"] in (1, 2), sh
-    assert sh["forward_parts_per_ray"] == (1 if nv == 9 else P.tuning("fan_parts")), sh
+    general = P.views_per_walk == 1
+    assert sh["forward_parts_per_ray"] == (1 if general else P.tuning("fan_parts")), sh
     assert sh["forward_parts_per_ray"] in (1, 4, 16)
     assert np.array_equal(_host(P.adjoint(r)), x0)
     for blk in (1, 2):
@@ -908,7 +1022,7 @@ def test_fan_autotune_parts_and_pixel_block(nv):
         P.set_tuning("fan_parts", parts)
         ys[parts] = _host(P.forward(x))
         assert np.linalg.norm(ys[parts] - y0) <= 1e-6 * np.linalg.norm(y0), parts
-    if nv == 9:                          # the general forward walks each ray whole
+    if general:                          # the general forward walks each ray whole
         assert all(np.array_equal(v, y0) for v in ys.values())
     L = _lib.load()
     assert L.fl_plan_option(P.handle, _lib.TUNE_FAN_PARTS, 2) == _lib.FL_ERR_INVALID
