@@ -770,7 +770,9 @@ def run_single(ctx, name, w, p):
         detail["gradcheck_s"] = time.perf_counter() - t0
         del f
     return dict(value=job_rate(world, K, t_g), t_step=t_g / K, e2e=e2e, roofline=roofline,
-                launches=5 * K + 1 + (2 if P.z_mirror else 0), detail=detail,   # ncu-checked
+                # ncu-checked: 5 per iteration (a fan plan's forward adds its
+                # transposed copy: 6), the start, and the z fold / unfold
+                launches=(5 if P.cone else 6) * K + 1 + (2 if P.z_mirror else 0), detail=detail,
                 clocks=clocks.summary(), unit="iter/s")
 
 

@@ -24,8 +24,9 @@
 // finish sums that slice's partials in a fixed order, so results do not depend
 // on scheduling). One iteration = 3 launches (q += lam p with <p,q>, updates
 // with <r,r>, direction) plus a forward with c_r^2 and an adjoint for each
-// kind of slice present (general, turn, reflection; parallel branches),
-// captured once as a CUDA graph and replayed.
+// kind of slice present (general, turn, reflection; parallel branches) and,
+// with turn or reflection slices, the transposed copy of the direction their
+// forward reads, captured once as a CUDA graph and replayed.
 // A stopped slice's chunks return at once.
 #include <algorithm>
 #include <cstring>
@@ -141,8 +142,8 @@ k_batch_fwd(const float* __restrict__ X, float* __restrict__ Y,
 // chunk (slice, r0) of the rays iv < nv/G (kFanBlock / lanes rays). ypack:
 // into the batch's scratch (woff), packed per orbit; else the standard
 // layout at yoff.
-__global__ void __launch_bounds__(kFanBlock, 4)
-k_batch_fwd_turn(const float* __restrict__ X, float* __restrict__ Y,
+__global__ void __launch_bounds__(kFanBlock, 3)
+k_batch_fwd_turn(const float* __restrict__ X, const float* __restrict__ XT, float* __restrict__ Y,
                  const BatchSlice* __restrict__ sl, const int2* __restrict__ chunks,
                  int cr_power, int ypack, const BatchScal* __restrict__ S)
 {
@@ -150,23 +151,37 @@ k_batch_fwd_turn(const float* __restrict__ X, float* __restrict__ Y,
     if (S && S[ch.x].done) return;            // uniform in the block
     const BatchSlice& b = sl[ch.x];
     float* y = Y + (ypack ? b.woff : b.yoff);
-#define FL_BATCH_TURN(GG, LL)                                                                  \
-    fan_turn_forward_block<float, float, GG, LL>(X + b.xoff, y, b.col, b.colr, b.nx, b.ny, b.na, \
-                                                 b.nv, b.scale, cr_power, nullptr, ypack, ch.y)
-    if (b.turns == 4 && b.lanes == kFanLanes) FL_BATCH_TURN(4, kFanLanes);
-    else if (b.turns == 4 && b.lanes == 4) FL_BATCH_TURN(4, 4);
-    else if (b.turns == 4) FL_BATCH_TURN(4, 1);
-    else if (b.lanes == kFanLanes) FL_BATCH_TURN(2, kFanLanes);
-    else if (b.lanes == 4) FL_BATCH_TURN(2, 4);
-    else FL_BATCH_TURN(2, 1);
-#undef FL_BATCH_TURN
+    if (b.turns == 4)
+        fan_turn_forward_block<float, float, 4>(X + b.xoff, XT + b.xoff, y, b.col, b.colr, b.nx,
+                                                b.ny, b.na, b.nv, b.scale, cr_power, nullptr,
+                                                ypack, ch.y, b.lanes);
+    else
+        fan_turn_forward_block<float, float, 2>(X + b.xoff, XT + b.xoff, y, b.col, b.colr, b.nx,
+                                                b.ny, b.na, b.nv, b.scale, cr_power, nullptr,
+                                                ypack, ch.y, b.lanes);
+}
+
+// Transposed copy of every slice's image (XT[xoff + x ny + y] = X[xoff + y nx
+// + x]) over the vector chunks, for the turn and reflection forwards
+// (walk_fan).
+__global__ void __launch_bounds__(kVecThreads)
+k_batch_transpose(const float* __restrict__ X, float* __restrict__ XT,
+                  const BatchSlice* __restrict__ sl, const VecChunk* __restrict__ chunks)
+{
+    const VecChunk ch = chunks[blockIdx.x];
+    const BatchSlice& b = sl[ch.slice];
+    if (b.turns == 1) return;                 // the general forward reads X alone
+    for (int k = threadIdx.x; k < ch.len; k += kVecThreads) {
+        const int i = ch.start + k, iy = i / b.nx, ix = i - iy * b.nx;
+        XT[b.xoff + (long long)ix * b.ny + iy] = X[b.xoff + i];
+    }
 }
 
 // Reflection slices: the plan's reflection forward (fan_refl_forward_block),
 // one block of kFanBlock threads per chunk (slice, r0) of the walked rays
 // (slots x columns of FanReflGeom; kFanBlock / lanes rays). ypack as above.
 __global__ void __launch_bounds__(kFanBlock, 3)
-k_batch_fwd_refl(const float* __restrict__ X, float* __restrict__ Y,
+k_batch_fwd_refl(const float* __restrict__ X, const float* __restrict__ XT, float* __restrict__ Y,
                  const BatchSlice* __restrict__ sl, const int2* __restrict__ chunks,
                  int cr_power, int ypack, const BatchScal* __restrict__ S)
 {
@@ -175,8 +190,9 @@ k_batch_fwd_refl(const float* __restrict__ X, float* __restrict__ Y,
     const BatchSlice& b = sl[ch.x];
     float* y = Y + (ypack ? b.woff : b.yoff);
 #define FL_BATCH_REFL(NN)                                                                      \
-    fan_refl_forward_block<float, float, NN>(X + b.xoff, y, b.col, b.colr, b.nx, b.ny, b.na, b.nv, \
-                                             b.scale, cr_power, nullptr, ypack, ch.y, b.lanes)
+    fan_refl_forward_block<float, float, NN>(X + b.xoff, XT + b.xoff, y, b.col, b.colr, b.nx,    \
+                                             b.ny, b.na, b.nv, b.scale, cr_power, nullptr, ypack, \
+                                             ch.y, b.lanes)
     if (b.refl == 4) FL_BATCH_REFL(4);
     else if (b.refl == 2) FL_BATCH_REFL(2);
     else FL_BATCH_REFL(1);
@@ -243,7 +259,7 @@ k_batch_adj_turn(float* __restrict__ X, const float* __restrict__ YW,
 // Reflection slices: the plan's reflection backprojection, one block of
 // kFanX primary pixel blocks of one block row x kTurnGroups view groups per
 // chunk (slice, block row, first block column).
-__global__ void __launch_bounds__(kFanX * kTurnGroups)
+__global__ void __launch_bounds__(kFanX * kTurnGroups, 3)
 k_batch_adj_refl(float* __restrict__ X, const float* __restrict__ YW,
                  const BatchSlice* __restrict__ sl, const int4* __restrict__ chunks,
                  const BatchScal* __restrict__ S)
@@ -413,6 +429,7 @@ struct fl_batch {
     int4* d_pix_r; int n_pix_r_chunks;     // reflection slices' primary pixels
     VecChunk* d_vec; int n_vec_chunks;
     float *r, *p, *q, *tmp;
+    float* xt;                         // transposed copies of a forward's input (walk_fan)
     BatchScal* S;
     double* partials;
     unsigned* tickets;
@@ -454,7 +471,7 @@ static void batch_free(fl_batch* b)
 {
     void* ptrs[] = {b->d_sl, b->d_rays, b->d_rays_t, b->d_wrays, b->d_pix, b->d_pix_t, b->d_vec,
                     b->d_rays_r, b->d_pix_r,
-                    b->r, b->p, b->q, b->tmp, b->S, b->partials, b->tickets, b->hist};
+                    b->r, b->p, b->q, b->tmp, b->xt, b->S, b->partials, b->tickets, b->hist};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     if (b->exec) cudaGraphExecDestroy(b->exec);
@@ -585,7 +602,7 @@ extern "C" int fl_batch_create(fl_plan* const* plans, int32_t n_plans, fl_batch*
     b->xoff = xoff; b->yoff = yoff;
     b->d_sl = nullptr; b->d_rays = nullptr; b->d_pix = nullptr; b->d_vec = nullptr;
     b->d_rays_t = nullptr; b->d_wrays = nullptr; b->d_pix_t = nullptr;
-    b->r = b->p = b->q = b->tmp = nullptr; b->S = nullptr; b->partials = nullptr;
+    b->r = b->p = b->q = b->tmp = b->xt = nullptr; b->S = nullptr; b->partials = nullptr;
     b->tickets = nullptr; b->hist = nullptr; b->hist_cap = 4096;
     b->cs = nullptr; b->ev0 = b->ev1 = nullptr; b->exec = nullptr; b->cap_u = nullptr;
     b->cs2 = nullptr; b->evf = b->evj = nullptr;
@@ -619,6 +636,7 @@ extern "C" int fl_batch_create(fl_plan* const* plans, int32_t n_plans, fl_batch*
     };
     M((void**)&b->r, b->n_vox * 4); M((void**)&b->p, b->n_vox * 4); M((void**)&b->q, b->n_vox * 4);
     M((void**)&b->tmp, woff[n_plans] * 4);
+    M((void**)&b->xt, b->n_vox * 4);
     M((void**)&b->S, sizeof(BatchScal) * n_plans);
     M((void**)&b->partials, sizeof(double) * b->n_vec_chunks);
     M((void**)&b->tickets, sizeof(unsigned) * n_plans);
@@ -682,14 +700,16 @@ static int batch_fwd(fl_batch* b, const float* x, float* y, int cr_power, int yp
                      const BatchScal* S, cudaStream_t s)
 {
     const bool g = b->n_ray_chunks, t = b->n_ray_t_chunks, r = b->n_ray_r_chunks;
+    if (t || r)
+        k_batch_transpose<<<b->n_vec_chunks, kVecThreads, 0, s>>>(x, b->xt, b->d_sl, b->d_vec);
     const cudaStream_t s2 = (t && g) ? fork_to(s, b->cs2, b->evf) : s;
     const cudaStream_t s3 = (r && (g || t)) ? fork_to(s, b->cs3, b->evf3) : s;
     if (r)
         k_batch_fwd_refl<<<b->n_ray_r_chunks, kFanBlock, 0, s3>>>(
-            x, y, b->d_sl, b->d_rays_r, cr_power, ypack, S);
+            x, b->xt, y, b->d_sl, b->d_rays_r, cr_power, ypack, S);
     if (t)
         k_batch_fwd_turn<<<b->n_ray_t_chunks, kFanBlock, 0, s2>>>(
-            x, y, b->d_sl, b->d_rays_t, cr_power, ypack, S);
+            x, b->xt, y, b->d_sl, b->d_rays_t, cr_power, ypack, S);
     if (g)
         k_batch_fwd<<<b->n_ray_chunks, kRayChunk, 0, s>>>(x, y, b->d_sl, b->d_rays, cr_power,
                                                           ypack, S);

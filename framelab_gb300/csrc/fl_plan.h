@@ -140,6 +140,9 @@ struct fl_plan {
     size_t work_elems;
     void *d_vwork;
     size_t vwork_bytes;
+    // fan plans: the forward's transposed copy of its input (n_vox elements
+    // of up to 4 bytes; allocated with the plan)
+    void *d_xt;
 };
 
 // The matched kernel form a plan uses (its options within what its geometry

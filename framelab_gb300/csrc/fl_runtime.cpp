@@ -86,7 +86,7 @@ static void free_plan_arrays(fl_plan* p)
                     p->d_sin_phi, p->d_cos_det, p->d_sin_det,   p->d_cphi_f, p->d_sphi_f,
                     p->d_view_frame, p->d_idY, p->d_Nv,        p->d_col,   p->d_colr,
                     p->d_row,    p->d_rowz,   p->d_view,       p->d_work,
-                    p->d_cos_det2, p->d_sin_det2, p->d_fb_edges, p->d_vwork};
+                    p->d_cos_det2, p->d_sin_det2, p->d_fb_edges, p->d_vwork, p->d_xt};
     for (void* q : ptrs)
         if (q) cudaFree(q);
 }
@@ -547,6 +547,10 @@ extern "C" int fl_plan_create(const fl_scan* scan, fl_plan** out)
     p->s.cos_phi = p->s.sin_phi = p->s.cos_det = p->s.sin_det = nullptr;
     p->s.view_frame = p->s.id_Y = p->s.Nv = nullptr;
     p->s.cos_det2 = p->s.sin_det2 = nullptr;
+    // fan plans: the forward's transposed copy of its input (matched.cu)
+    if (!st && s.ndim == 2)
+        st = fl_check_cuda(fl_malloc(&p->d_xt, (size_t)p->n_vox * sizeof(float)),
+                           "fl_malloc(plan)");
     if (st) {
         free_plan_arrays(p);
         delete p;

@@ -207,18 +207,20 @@ k_fwd_refl(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restr
 
 template <typename TX, typename TY>
 __global__ void __launch_bounds__(128, 8)
-k_fwd_fan(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restrict__ col,
-          const float* __restrict__ colr, const int* __restrict__ vframe, int nx, int ny,
-          int na, int nv, long long nper, float scale, int cr_power,
-          const int* __restrict__ skip, const float* __restrict__ xscale)
+k_fwd_fan(const TX* __restrict__ X, const TX* __restrict__ XT, TY* __restrict__ y,
+          const ColEntry* __restrict__ col, const float* __restrict__ colr,
+          const int* __restrict__ vframe, int nx, int ny, int na, int nv, long long nper,
+          float scale, int cr_power, const int* __restrict__ skip,
+          const float* __restrict__ xscale)
 {
     if (skip && *skip) return;
     long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= (long long)na * nv) return;
     int iv = (int)(r / na);
     const TX* x = X + (long long)vframe[iv] * nper;
+    const TX* xt = XT + (long long)vframe[iv] * nper;
     float a1[1];
-    walk_fan<TX, 1>(x, &col[r].x, &col[r].y, nx, ny, a1, nper);
+    walk_fan<TX, 1>(x, xt, &col[r].x, &col[r].y, nx, ny, a1, nper);
     float acc = a1[0];
     float cr = ray_cr(scale, colr[r], 0.0f);
     if (xscale) acc *= *xscale;
@@ -228,30 +230,31 @@ k_fwd_fan(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restri
 }
 
 // Fan forward of a turn plan (G = 2 or 4, one frame): blocks of kFanBlock
-// threads, L parts per ray (fan_turn_forward_block, fan_turn_lanes).
-template <typename TX, typename TY, int G, int L>
-__global__ void __launch_bounds__(kFanBlock, 4)
-k_fwd_fan_turn(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restrict__ col,
-               const float* __restrict__ colr, int nx, int ny, int na, int nv, float scale,
-               int cr_power, const int* __restrict__ skip, const float* __restrict__ xscale,
-               int ypack)
+// threads, L parts per ray (fan_turn_forward_block, fl_plan_fan_lanes).
+template <typename TX, typename TY, int G>
+__global__ void __launch_bounds__(kFanBlock, 3)
+k_fwd_fan_turn(const TX* __restrict__ X, const TX* __restrict__ XT, TY* __restrict__ y,
+               const ColEntry* __restrict__ col, const float* __restrict__ colr, int nx, int ny,
+               int na, int nv, float scale, int cr_power, const int* __restrict__ skip,
+               const float* __restrict__ xscale, int ypack, int L)
 {
     if (skip && *skip) return;                 // uniform (one flag for the launch)
-    fan_turn_forward_block<TX, TY, G, L>(X, y, col, colr, nx, ny, na, nv, scale, cr_power,
-                                         xscale, ypack, (long long)blockIdx.x * (kFanBlock / L));
+    fan_turn_forward_block<TX, TY, G>(X, XT, y, col, colr, nx, ny, na, nv, scale, cr_power,
+                                      xscale, ypack, (long long)blockIdx.x * (kFanBlock / L), L);
 }
 
 // Fan reflection forms (NR = 1, 2 or 4, one frame): forward blocks of
 // kFanBlock threads, L parts per walked ray (fan_refl_forward_block).
 template <typename TX, typename TY, int NR>
 __global__ void __launch_bounds__(kFanBlock, 3)
-k_fwd_fan_refl(const TX* __restrict__ X, TY* __restrict__ y, const ColEntry* __restrict__ col,
+k_fwd_fan_refl(const TX* __restrict__ X, const TX* __restrict__ XT, TY* __restrict__ y,
+               const ColEntry* __restrict__ col,
                const float* __restrict__ colr, int nx, int ny, int na, int nv, float scale,
                int cr_power, const int* __restrict__ skip, const float* __restrict__ xscale,
                int ypack, int L)
 {
     if (skip && *skip) return;                 // uniform (one flag for the launch)
-    fan_refl_forward_block<TX, TY, NR>(X, y, col, colr, nx, ny, na, nv, scale, cr_power, xscale,
+    fan_refl_forward_block<TX, TY, NR>(X, XT, y, col, colr, nx, ny, na, nv, scale, cr_power, xscale,
                                        ypack, (long long)blockIdx.x * (kFanBlock / L), L);
 }
 
@@ -267,6 +270,27 @@ k_adj_fan_refl(TX* __restrict__ X, const float* __restrict__ ywp,
     __shared__ float smem[kTurnGroups * 2 * NR * PB * PB * kFanX];
     fan_refl_adjoint_block<TX, NR, PB>(X, ywp, col, view, G, nx, ny, na, nv, blockIdx.x * kFanX,
                                        blockIdx.y, smem);
+}
+
+// Transposed copy of fan images (all frames): xt[f nper + x ny + y] =
+// x[f nper + y nx + x], through a 32 x 32 tile in shared memory.
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_transpose_fan(const T* __restrict__ x, T* __restrict__ xt, int nx, int ny, long long nper)
+{
+    __shared__ T tile[32][33];
+    const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
+    const T* src = x + (long long)blockIdx.z * nper;
+    T* dst = xt + (long long)blockIdx.z * nper;
+    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+        const int yy = by + k, xx = bx + threadIdx.x;
+        if (yy < ny && xx < nx) tile[k][threadIdx.x] = src[(long long)yy * nx + xx];
+    }
+    __syncthreads();
+    for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+        const int xx = bx + k, yy = by + threadIdx.x;
+        if (xx < nx && yy < ny) dst[(long long)xx * ny + yy] = tile[threadIdx.x][k];
+    }
 }
 
 __global__ void __launch_bounds__(128)
@@ -1398,6 +1422,19 @@ int fl_plan_fan_block(const fl_plan* p)
 
 namespace {
 
+// The fan forward's transposed copy of its input (walk_fan), in the plan's
+// buffer (allocated with the plan: nothing is allocated here, so a forward
+// can be captured in a CUDA graph).
+template <typename TX>
+const TX* fan_transposed(fl_plan* p, const void* x, cudaStream_t st)
+{
+    const fl_scan& s = p->s;
+    const dim3 grid(fl_div_up(s.nx, 32), fl_div_up(s.ny, 32), s.nt);
+    k_transpose_fan<TX><<<grid, dim3(32, 8), 0, st>>>((const TX*)x, (TX*)p->d_xt, s.nx, s.ny,
+                                                      p->n_vox_frame);
+    return (const TX*)p->d_xt;
+}
+
 template <typename TX, typename TY>
 void launch_fwd(fl_plan* p, const void* x, void* y, int cr_power, const int* skip,
                 const float* xscale, int yfold, cudaStream_t st)
@@ -1436,39 +1473,38 @@ void launch_fwd(fl_plan* p, const void* x, void* y, int cr_power, const int* ski
             (const TX*)x, (TY*)y, p->d_col, p->d_colr, p->d_row, p->d_view_frame, s.nx, s.ny,
             s.nz, s.na, s.nb, p->n_vox_frame, s.scale, cr_power, skip, xscale, 0);
     } else if (fl_plan_refl(p)) {
+        const TX* xt = fan_transposed<TX>(p, x, st);
         const int NR = fl_plan_refl(p);
         const long long nr = (long long)s.na * fan_refl_geom(NR, s.nv, s.na).slots;
         const int lanes = fl_plan_fan_lanes(p);
         const unsigned g = fl_div_up(nr, kFanBlock / lanes);
 #define FL_FAN_REFL(NN)                                                                      \
     k_fwd_fan_refl<TX, TY, NN><<<g, kFanBlock, 0, st>>>(                                     \
-        (const TX*)x, (TY*)y, p->d_col, p->d_colr, s.nx, s.ny, s.na, s.nv, s.scale, cr_power, \
-        skip, xscale, yfold, lanes)
+        (const TX*)x, xt, (TY*)y, p->d_col, p->d_colr, s.nx, s.ny, s.na, s.nv, s.scale,         \
+        cr_power, skip, xscale, yfold, lanes)
         if (NR == 4) FL_FAN_REFL(4);
         else if (NR == 2) FL_FAN_REFL(2);
         else FL_FAN_REFL(1);
 #undef FL_FAN_REFL
     } else if (fl_plan_turns(p) > 1) {
+        const TX* xt = fan_transposed<TX>(p, x, st);
         const int G = fl_plan_turns(p);
         const long long nr = (long long)s.na * (s.nv / G);
         const int lanes = fl_plan_fan_lanes(p);
         const unsigned g = fl_div_up(nr, kFanBlock / lanes);
-#define FL_FAN_TURN(GG, LL)                                                                  \
-    k_fwd_fan_turn<TX, TY, GG, LL><<<g, kFanBlock, 0, st>>>(                                 \
-        (const TX*)x, (TY*)y, p->d_col, p->d_colr, s.nx, s.ny, s.na, s.nv, s.scale, cr_power, \
-        skip, xscale, yfold)
-        if (G == 4 && lanes == kFanLanes) FL_FAN_TURN(4, kFanLanes);
-        else if (G == 4 && lanes == 4) FL_FAN_TURN(4, 4);
-        else if (G == 4) FL_FAN_TURN(4, 1);
-        else if (lanes == kFanLanes) FL_FAN_TURN(2, kFanLanes);
-        else if (lanes == 4) FL_FAN_TURN(2, 4);
-        else FL_FAN_TURN(2, 1);
+#define FL_FAN_TURN(GG)                                                                      \
+    k_fwd_fan_turn<TX, TY, GG><<<g, kFanBlock, 0, st>>>(                                     \
+        (const TX*)x, xt, (TY*)y, p->d_col, p->d_colr, s.nx, s.ny, s.na, s.nv, s.scale,         \
+        cr_power, skip, xscale, yfold, lanes)
+        if (G == 4) FL_FAN_TURN(4);
+        else FL_FAN_TURN(2);
 #undef FL_FAN_TURN
     } else {
         long long nr = (long long)s.na * s.nv;
+        const TX* xt = fan_transposed<TX>(p, x, st);
         k_fwd_fan<TX, TY><<<fl_div_up(nr, 128), 128, 0, st>>>(
-            (const TX*)x, (TY*)y, p->d_col, p->d_colr, p->d_view_frame, s.nx, s.ny, s.na, s.nv,
-            p->n_vox_frame, s.scale, cr_power, skip, xscale);
+            (const TX*)x, xt, (TY*)y, p->d_col, p->d_colr, p->d_view_frame, s.nx, s.ny, s.na,
+            s.nv, p->n_vox_frame, s.scale, cr_power, skip, xscale);
     }
 }
 

@@ -613,24 +613,31 @@ __device__ __forceinline__ void refl_view(const Geo& g, int w, int& vt, long lon
 // S^j M (ix, iy) of the pixel, M (x, y) = (x, ny-1-y), into acc[G + j].
 constexpr int kFanBatch = 4;
 
+// xt (optional): the same image transposed, xt[x ny + y] = x[y nx + x]. A
+// warp's rays at one step lie along the detector, across the direction they
+// travel: for an image ray that travels mostly along x they sit in one
+// column of pixels, consecutive in xt, so its gathers read xt; the others
+// read x. The values, and so the sums, are the same either way.
 // walk_fan_parts: the same walk with the parts count L a run-time value.
 template <typename TX, int G, bool RF>
-__device__ __forceinline__ void walk_fan_parts(const TX* __restrict__ x, const AxisEntry* pX,
+__device__ __forceinline__ void walk_fan_parts(const TX* __restrict__ x,
+                                               const TX* __restrict__ xt, const AxisEntry* pX,
                                                const AxisEntry* pY, int nx, int ny,
                                                float (&acc)[RF ? 2 * G : G], long long xlen,
                                                int lane, int L);
 
 template <typename TX, int G, int L = 1, bool RF = false>
-__device__ __forceinline__ void walk_fan(const TX* __restrict__ x, const AxisEntry* pX,
-                                         const AxisEntry* pY, int nx, int ny,
-                                         float (&acc)[RF ? 2 * G : G], long long xlen,
+__device__ __forceinline__ void walk_fan(const TX* __restrict__ x, const TX* __restrict__ xt,
+                                         const AxisEntry* pX, const AxisEntry* pY, int nx,
+                                         int ny, float (&acc)[RF ? 2 * G : G], long long xlen,
                                          int lane = 0)
 {
-    walk_fan_parts<TX, G, RF>(x, pX, pY, nx, ny, acc, xlen, lane, L);
+    walk_fan_parts<TX, G, RF>(x, xt, pX, pY, nx, ny, acc, xlen, lane, L);
 }
 
 template <typename TX, int G, bool RF>
-__device__ __forceinline__ void walk_fan_parts(const TX* __restrict__ x, const AxisEntry* pX,
+__device__ __forceinline__ void walk_fan_parts(const TX* __restrict__ x,
+                                               const TX* __restrict__ xt, const AxisEntry* pX,
                                                const AxisEntry* pY, int nx, int ny,
                                                float (&acc)[RF ? 2 * G : G], long long xlen,
                                                int lane, int L)
@@ -665,7 +672,12 @@ __device__ __forceinline__ void walk_fan_parts(const TX* __restrict__ x, const A
     int jx = slab_guess(X, ag, nx), jy = slab_guess(Y, ag, ny);
     const int nxy = nx * ny;                       // < 2^31 (checked at plan creation)
     const int dq0x = px ? 1 : -1, dq0y = py ? nx : -nx;
-    const int dq1x = px ? nx : -nx, dq1y = py ? -1 : 1;
+    const int dq1x = px ? ny : -ny, dq1y = py ? -1 : 1;
+    // image j read from xt: its ray travels mostly along x (a quarter turn
+    // swaps the axes of the odd images of G = 4)
+    bool useT[NI];
+#pragma unroll
+    for (int j = 0; j < NI; j++) useT[j] = xt != nullptr && (xd != (G == 4 && (j % G) % 2 == 1));
     const float stx = px ? 1.0f : -1.0f, sty = py ? 1.0f : -1.0f;
     float sacc[NI];
 #pragma unroll
@@ -690,12 +702,13 @@ __device__ __forceinline__ void walk_fan_parts(const TX* __restrict__ x, const A
         float mx = __fsub_rn((float)(px ? jx + 1 : jx), X.kq);
         float my = __fsub_rn((float)(py ? jy + 1 : jy), Y.kq);
         float Ux = xrel(X, mx, bh, cbx), Uy = xrel(Y, my, bh, cby);
-        // p0: the pixel; p1 (G = 4): its quarter turn x * n + n-1-y; the turns
-        // by pi of both are nxy - 1 minus them. m0, m1 (RF): the same for the
-        // mirror image M p = (x, ny-1-y) (index (ny-1-y) nx + x) and its
-        // quarter turn (y, x) (index x n + y)
-        int p0 = jy * nx + jx, p1 = jx * nx + (nx - 1 - jy);
-        int m0 = (ny - 1 - jy) * nx + jx, m1 = jx * nx + jy;
+        // p0: the pixel's index in x, y nx + x; m0: its mirror image M p =
+        // (x, ny-1-y) in x. p1 = x ny + ny-1-y and m1 = x ny + y: in x the
+        // quarter turns (n-1-y, x) and (y, x) = R M p of the pixel (G = 4,
+        // nx == ny), in xt the mirror image and the pixel. The turns by pi of
+        // all are nxy - 1 minus them, in either array.
+        int p0 = jy * nx + jx, p1 = jx * ny + (ny - 1 - jy);
+        int m0 = (ny - 1 - jy) * nx + jx, m1 = jx * ny + jy;
         float cur = v_in;
         bool in = true;
         const int budget = (hix - lox) + (hiy - loy) + 2;
@@ -715,14 +728,12 @@ __device__ __forceinline__ void walk_fan_parts(const TX* __restrict__ x, const A
                     if (Ux == nxt) {
                         jx += px ? 1 : -1;
                         mx = __fadd_rn(mx, stx); Ux = xrel(X, mx, bh, cbx);
-                        p0 += dq0x; p1 += dq1x;
-                        if (RF) { m0 += dq0x; m1 += dq1x; }
+                        p0 += dq0x; p1 += dq1x; m0 += dq0x; m1 += dq1x;
                     }
                     if (Uy == nxt) {
                         jy += py ? 1 : -1;
                         my = __fadd_rn(my, sty); Uy = xrel(Y, my, bh, cby);
-                        p0 += dq0y; p1 += dq1y;
-                        if (RF) { m0 -= dq0y; m1 -= dq1y; }
+                        p0 += dq0y; p1 += dq1y; m0 -= dq0y; m1 -= dq1y;
                     }
                     cur = nxt;
                     in = more;
@@ -731,15 +742,22 @@ __device__ __forceinline__ void walk_fan_parts(const TX* __restrict__ x, const A
             float vv[NB][NI];
 #pragma unroll
             for (int u = 0; u < NB; u++) {
+                // the images C_0 .. C_{G-1}, then (RF) D_0 .. D_{G-1}: index in x ...
                 const int qq[8] = {i0[u], G == 4 ? i1[u] : nxy - 1 - i0[u], nxy - 1 - i0[u],
                                    nxy - 1 - i1[u],
                                    k0[u], G == 4 ? k1[u] : nxy - 1 - k0[u], nxy - 1 - k0[u],
                                    nxy - 1 - k1[u]};
+                // ... and in xt
+                const int qt[8] = {k1[u], G == 4 ? k0[u] : nxy - 1 - k1[u], nxy - 1 - k1[u],
+                                   nxy - 1 - k0[u],
+                                   i1[u], G == 4 ? i0[u] : nxy - 1 - i1[u], nxy - 1 - i1[u],
+                                   nxy - 1 - i0[u]};
 #pragma unroll
                 for (int j = 0; j < NI; j++) {
-                    const int q = j < G ? qq[j] : qq[4 + j - G];
+                    const int q = useT[j] ? (j < G ? qt[j] : qt[4 + j - G])
+                                          : (j < G ? qq[j] : qq[4 + j - G]);
                     vv[u][j] = 0.0f;
-                    if (live[u] && FL_IN(q, xlen)) vv[u][j] = ldv(x + q);
+                    if (live[u] && FL_IN(q, xlen)) vv[u][j] = ldv((useT[j] ? xt : x) + q);
                 }
             }
 #pragma unroll
@@ -1083,7 +1101,8 @@ __host__ __device__ inline int fan_turn_lanes(long long walks)
 }
 
 // One block of kFanBlock threads of the fan turn forward (G = 2 or 4, one
-// frame): L threads per ray (iv < nv/G, ia), each walking one part of it
+// frame; XT the transposed image, walk_fan): L (1, 4 or 16, uniform in the
+// launch) threads per ray (iv < nv/G, ia), each walking one part of it
 // (walk_fan), their sums added in part order; the walk also yields the rays
 // of views iv + j nv/G at the same column, all with the walked ray's c_r.
 // The block holds the rays r0, r0 + 1, ... : with L parts, kFanBlock / L
@@ -1093,39 +1112,39 @@ __host__ __device__ inline int fan_turn_lanes(long long walks)
 // adjoint-input layout of these plans: the G values of ray (iv, ia)'s orbit
 // side by side at G (iv na + ia) + j. Every thread of the block must call it
 // (it synchronises the block).
-template <typename TX, typename TY, int G, int L>
+template <typename TX, typename TY, int G>
 __device__ __forceinline__ void fan_turn_forward_block(const TX* __restrict__ X,
+                                                       const TX* __restrict__ XT,
                                                        TY* __restrict__ y,
                                                        const ColEntry* __restrict__ col,
                                                        const float* __restrict__ colr, int nx,
                                                        int ny, int na, int nv, float scale,
                                                        int cr_power,
                                                        const float* __restrict__ xscale,
-                                                       int ypack, long long r0)
+                                                       int ypack, long long r0, int L)
 {
-    constexpr int NR = kFanBlock / L;          // rays per block
+    const int nry = kFanBlock / L;             // rays per block
     const int gv = nv / G;
-    const int tx = threadIdx.x % NR, lane = threadIdx.x / NR;
+    const int tx = threadIdx.x % nry, lane = threadIdx.x / nry;
     const long long r = r0 + tx;
     const bool ray = r < (long long)na * gv;
     float acc[G];
 #pragma unroll
     for (int j = 0; j < G; j++) acc[j] = 0.0f;
-    if (ray) {
-        walk_fan<TX, G, L>(X, &col[r].x, &col[r].y, nx, ny, acc, (long long)nx * ny, lane);
-    }
-    if constexpr (L > 1) {
-        // part k of ray tx is thread k NR + tx: the first NR threads add them in order
-        __shared__ float part[L][G][NR];
+    if (ray)
+        walk_fan_parts<TX, G, false>(X, XT, &col[r].x, &col[r].y, nx, ny, acc,
+                                     (long long)nx * ny, lane, L);
+    if (L > 1) {
+        // part k of ray tx is thread k nry + tx: the first nry threads add them in order
+        __shared__ float part[G][kFanBlock];
 #pragma unroll
-        for (int j = 0; j < G; j++) part[lane][j][tx] = acc[j];
+        for (int j = 0; j < G; j++) part[j][threadIdx.x] = acc[j];
         __syncthreads();
         if (lane != 0) return;
 #pragma unroll
         for (int j = 0; j < G; j++) {
-            float sum = part[0][j][tx];
-#pragma unroll
-            for (int k = 1; k < L; k++) sum += part[k][j][tx];
+            float sum = part[j][tx];
+            for (int k = 1; k < L; k++) sum += part[j][k * nry + tx];
             acc[j] = sum;
         }
     }
@@ -1203,7 +1222,7 @@ __device__ __forceinline__ void fan_turn_adjoint_block(TX* __restrict__ X,
 }
 
 // One block of kFanBlock threads of a fan reflection form's forward (NR = 1,
-// 2 or 4; FanReflGeom): L (1, 4 or 16, uniform in the launch) threads per
+// 2 or 4; FanReflGeom; XT the transposed image, walk_fan): L (1, 4 or 16, uniform in the launch) threads per
 // walked ray r = (slot, column) of the r0, r0 + 1, ... (kFanBlock / L
 // rays), each walking one part of it (walk_fan with the reflected images),
 // their sums added in part order. The walk yields the rays of the 2 NR images
@@ -1213,6 +1232,7 @@ __device__ __forceinline__ void fan_turn_adjoint_block(TX* __restrict__ X,
 // block).
 template <typename TX, typename TY, int NR>
 __device__ __forceinline__ void fan_refl_forward_block(const TX* __restrict__ X,
+                                                       const TX* __restrict__ XT,
                                                        TY* __restrict__ y,
                                                        const ColEntry* __restrict__ col,
                                                        const float* __restrict__ colr, int nx,
@@ -1234,7 +1254,7 @@ __device__ __forceinline__ void fan_refl_forward_block(const TX* __restrict__ X,
 #pragma unroll
     for (int j = 0; j < NI; j++) acc[j] = 0.0f;
     const long long rr = (long long)vt * na + a;      // the walked ray's table entry
-    if (ray) walk_fan_parts<TX, NR, true>(X, &col[rr].x, &col[rr].y, nx, ny, acc,
+    if (ray) walk_fan_parts<TX, NR, true>(X, XT, &col[rr].x, &col[rr].y, nx, ny, acc,
                                           (long long)nx * ny, lane, L);
     if (L > 1) {
         // part k of ray tx is thread k nry + tx: the first nry threads add them in order

@@ -423,7 +423,8 @@ int fl_batch_adjoint(fl_batch *b, const float *y, float *x, void *stream);
  * after each iteration (0 after it stopped); iters_done (host, optional):
  * [n_plans]. One iteration is a replayed CUDA graph of 3 launches plus a
  * forward and a backprojection for each kind of slice present (general,
- * turn, reflection; the kinds run as parallel branches). */
+ * turn, reflection; the kinds run as parallel branches) and, with turn or
+ * reflection slices, a transposed copy of the direction they read. */
 int fl_batch_cgls(fl_batch *b, const float *rhs, float *u, float lam, int32_t iters, double tol,
                   int32_t flags, double *gamma_history, int32_t *iters_done, void *stream);
 /* Launch tuner of a batch: times the parts per walked ray of its half- and

@@ -67,7 +67,7 @@ def test_batch_turn_slices_bit_identical_to_single_plans():
     from framelab_gb300.batch import FanBatch
     paras = _turn_paras()
     B = FanBatch(paras)
-    assert B.turns == [4, 2, 1, 4, 2] and B.launches_per_iteration == 7
+    assert B.turns == [4, 2, 1, 4, 2] and B.launches_per_iteration == 8
     rng = np.random.default_rng(8)
     x = torch.from_numpy(rng.standard_normal(B.n_vox).astype(np.float32)).cuda()
     y = torch.from_numpy(rng.standard_normal(B.n_rays).astype(np.float32)).cuda()
@@ -123,7 +123,7 @@ def test_batch_reflection_slices_bit_identical_to_single_plans():
     B = FanBatch(paras)
     assert B.turns == [2, 8, 4, 4, 4, 1, 2], B.turns
     assert B.reflect == [True, True, True, True, False, False, True]
-    assert B.launches_per_iteration == 9
+    assert B.launches_per_iteration == 10
     x = torch.from_numpy(rng.standard_normal(B.n_vox).astype(np.float32)).cuda()
     y = torch.from_numpy(rng.standard_normal(B.n_rays).astype(np.float32)).cuda()
     yb, xb = B.forward(x), B.adjoint(y)
