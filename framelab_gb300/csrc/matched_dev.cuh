@@ -613,11 +613,11 @@ __device__ __forceinline__ void refl_view(const Geo& g, int w, int& vt, long lon
 // S^j M (ix, iy) of the pixel, M (x, y) = (x, ny-1-y), into acc[G + j].
 constexpr int kFanBatch = 4;
 
-// xt (optional): the same image transposed, xt[x ny + y] = x[y nx + x]. A
-// warp's rays at one step lie along the detector, across the direction they
-// travel: for an image ray that travels mostly along x they sit in one
-// column of pixels, consecutive in xt, so its gathers read xt; the others
-// read x. The values, and so the sums, are the same either way.
+// xt: the same image transposed, xt[x ny + y] = x[y nx + x]. A warp's rays
+// at one step lie along the detector, across the direction they travel: for
+// an image ray that travels mostly along x they sit in one column of pixels,
+// consecutive in xt, so its gathers read xt; the others read x. The values,
+// and so the sums, are the same either way.
 // walk_fan_parts: the same walk with the parts count L a run-time value.
 template <typename TX, int G, bool RF>
 __device__ __forceinline__ void walk_fan_parts(const TX* __restrict__ x,
@@ -671,13 +671,18 @@ __device__ __forceinline__ void walk_fan_parts(const TX* __restrict__ x,
     }
     int jx = slab_guess(X, ag, nx), jy = slab_guess(Y, ag, ny);
     const int nxy = nx * ny;                       // < 2^31 (checked at plan creation)
-    const int dq0x = px ? 1 : -1, dq0y = py ? nx : -nx;
-    const int dq1x = px ? ny : -ny, dq1y = py ? -1 : 1;
-    // image j read from xt: its ray travels mostly along x (a quarter turn
-    // swaps the axes of the odd images of G = 4)
-    bool useT[NI];
-#pragma unroll
-    for (int j = 0; j < NI; j++) useT[j] = xt != nullptr && (xd != (G == 4 && (j % G) % 2 == 1));
+    // The array the walked ray's own direction reads (xt when it travels
+    // mostly along x, else x) is E, the other O. Two running indices a, b
+    // address every image: in E, a the pixel and b its mirror image M p
+    // (x-dominant: x ny + y and x ny + ny-1-y in xt; else y nx + x and
+    // (ny-1-y) nx + x in x). With G = 4 the odd images (quarter turns) travel
+    // across, and read O, where b is the quarter turn C_1 and a the image
+    // D_1 = R M p (x n + n-1-y and x n + y in x, or (n-1-y) n + x and y n + x
+    // in xt). The turns by pi are nxy - 1 minus these, in either array.
+    const TX* E = xd ? xt : x;
+    const TX* O = xd ? x : xt;
+    const int sx = xd ? ny : 1, sy = xd ? 1 : nx;   // a's steps in x and y
+    const int dax = px ? sx : -sx, day = py ? sy : -sy;
     const float stx = px ? 1.0f : -1.0f, sty = py ? 1.0f : -1.0f;
     float sacc[NI];
 #pragma unroll
@@ -702,38 +707,33 @@ __device__ __forceinline__ void walk_fan_parts(const TX* __restrict__ x,
         float mx = __fsub_rn((float)(px ? jx + 1 : jx), X.kq);
         float my = __fsub_rn((float)(py ? jy + 1 : jy), Y.kq);
         float Ux = xrel(X, mx, bh, cbx), Uy = xrel(Y, my, bh, cby);
-        // p0: the pixel's index in x, y nx + x; m0: its mirror image M p =
-        // (x, ny-1-y) in x. p1 = x ny + ny-1-y and m1 = x ny + y: in x the
-        // quarter turns (n-1-y, x) and (y, x) = R M p of the pixel (G = 4,
-        // nx == ny), in xt the mirror image and the pixel. The turns by pi of
-        // all are nxy - 1 minus them, in either array.
-        int p0 = jy * nx + jx, p1 = jx * ny + (ny - 1 - jy);
-        int m0 = (ny - 1 - jy) * nx + jx, m1 = jx * ny + jy;
+        int a = xd ? jx * ny + jy : jy * nx + jx;
+        int b = xd ? jx * ny + (ny - 1 - jy) : (ny - 1 - jy) * nx + jx;
         float cur = v_in;
         bool in = true;
         const int budget = (hix - lox) + (hiy - loy) + 2;
         for (int it = 0; it < budget && in; it += NB) {
             float seg[NB];
-            int i0[NB], i1[NB], k0[NB], k1[NB];
+            int ia[NB], ib[NB];
             bool live[NB];
 #pragma unroll
             for (int u = 0; u < NB; u++) {
                 const float nxt = fminf(Ux, Uy);
                 live[u] = in;
                 seg[u] = __fsub_rn(nxt, cur);
-                i0[u] = p0; i1[u] = p1; k0[u] = m0; k1[u] = m1;
+                ia[u] = a; ib[u] = b;
                 if (in) {
                     // the last voxel of the sub-box: its next crossing is the exit
                     const bool more = nxt < v_out;
                     if (Ux == nxt) {
                         jx += px ? 1 : -1;
                         mx = __fadd_rn(mx, stx); Ux = xrel(X, mx, bh, cbx);
-                        p0 += dq0x; p1 += dq1x; m0 += dq0x; m1 += dq1x;
+                        a += dax; b += dax;
                     }
                     if (Uy == nxt) {
                         jy += py ? 1 : -1;
                         my = __fadd_rn(my, sty); Uy = xrel(Y, my, bh, cby);
-                        p0 += dq0y; p1 += dq1y; m0 -= dq0y; m1 -= dq1y;
+                        a += day; b -= day;
                     }
                     cur = nxt;
                     in = more;
@@ -742,22 +742,17 @@ __device__ __forceinline__ void walk_fan_parts(const TX* __restrict__ x,
             float vv[NB][NI];
 #pragma unroll
             for (int u = 0; u < NB; u++) {
-                // the images C_0 .. C_{G-1}, then (RF) D_0 .. D_{G-1}: index in x ...
-                const int qq[8] = {i0[u], G == 4 ? i1[u] : nxy - 1 - i0[u], nxy - 1 - i0[u],
-                                   nxy - 1 - i1[u],
-                                   k0[u], G == 4 ? k1[u] : nxy - 1 - k0[u], nxy - 1 - k0[u],
-                                   nxy - 1 - k1[u]};
-                // ... and in xt
-                const int qt[8] = {k1[u], G == 4 ? k0[u] : nxy - 1 - k1[u], nxy - 1 - k1[u],
-                                   nxy - 1 - k0[u],
-                                   i1[u], G == 4 ? i0[u] : nxy - 1 - i1[u], nxy - 1 - i1[u],
-                                   nxy - 1 - i0[u]};
+                // images C_0 .. C_{G-1}, then (RF) D_0 .. D_{G-1}
+                const int A = ia[u], B = ib[u], A2 = nxy - 1 - A, B2 = nxy - 1 - B;
+                const int q4[8] = {A, B, A2, B2, B, A, B2, A2};       // G = 4: odd ones in O
+                const int q2[4] = {A, A2, B, B2};                      // G = 2
+                const int q1[2] = {A, B};                              // G = 1
 #pragma unroll
                 for (int j = 0; j < NI; j++) {
-                    const int q = useT[j] ? (j < G ? qt[j] : qt[4 + j - G])
-                                          : (j < G ? qq[j] : qq[4 + j - G]);
+                    const int q = G == 4 ? q4[j] : (G == 2 ? q2[j] : q1[j]);
+                    const TX* arr = (G == 4 && (j & 1)) ? O : E;
                     vv[u][j] = 0.0f;
-                    if (live[u] && FL_IN(q, xlen)) vv[u][j] = ldv((useT[j] ? xt : x) + q);
+                    if (live[u] && FL_IN(q, xlen)) vv[u][j] = ldv(arr + q);
                 }
             }
 #pragma unroll
