@@ -130,6 +130,9 @@ struct fl_plan {
     // the scan's default, fl_plan_fan_lanes) and pixels per thread side of
     // the backprojections (1 or 2; 0 = 2 once there are 4 waves of blocks)
     int fan_lanes, fan_block;
+    // fan plans: view groups of the turn and reflection backprojections (8
+    // or 16; 0 = 8)
+    int fan_groups;
     // scale of an FP16 backprojection input (the mixed CGLS form): the largest
     // power of two with y16_scale * c_r^2 <= 1 for every ray, so c_r^2 * (a
     // ray's sum of w p) stays within FP16's range whenever |p| does
@@ -224,6 +227,9 @@ int fl_plan_fan_lanes(const fl_plan* p);
 // setting (FL_TUNE_FAN_BLOCK), else 2 once the 2 x 2 blocks make four waves
 // of thread blocks on 152 SMs.
 int fl_plan_fan_block(const fl_plan* p);
+// View groups of a fan plan's turn and reflection backprojections (8 or 16):
+// the plan's setting (FL_TUNE_FAN_GROUPS), else 8.
+int fl_plan_fan_groups(const fl_plan* p);
 
 // internal launchers
 int fl_ref_forward(fl_plan* p, const float* x, float* y, cudaStream_t st);

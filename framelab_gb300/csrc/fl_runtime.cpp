@@ -361,6 +361,12 @@ extern "C" int fl_plan_option(fl_plan* p, int option, int value)
         p->fan_block = value;
         return fl_set_error(FL_OK, "");
     }
+    if (option == FL_TUNE_FAN_GROUPS) {
+        if (value != 8 && value != 16)
+            return fl_set_error(FL_ERR_INVALID, "fl_plan_option: %d view groups (8 or 16)", value);
+        p->fan_groups = value;
+        return fl_set_error(FL_OK, "");
+    }
     return fl_set_error(FL_ERR_INVALID, "fl_plan_option: unknown option %d", option);
 }
 
@@ -398,6 +404,10 @@ extern "C" int fl_plan_query(const fl_plan* p, int option, int* value)
     }
     if (option == FL_TUNE_FAN_BLOCK) {
         *value = fl_plan_fan_block(p);
+        return fl_set_error(FL_OK, "");
+    }
+    if (option == FL_TUNE_FAN_GROUPS) {
+        *value = fl_plan_fan_groups(p);
         return fl_set_error(FL_OK, "");
     }
     return fl_set_error(FL_ERR_INVALID, "fl_plan_query: unknown option %d", option);

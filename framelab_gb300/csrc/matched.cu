@@ -260,16 +260,16 @@ k_fwd_fan_refl(const TX* __restrict__ X, const TX* __restrict__ XT, TY* __restri
 
 // Fan reflection backprojection: blocks of kFanX PB x PB pixel blocks of one
 // block row x kTurnGroups view groups (fan_refl_adjoint_block).
-template <typename TX, int NR, int PB>
-__global__ void __launch_bounds__(kFanX * kTurnGroups)
+template <typename TX, int NR, int PB, int NG>
+__global__ void __launch_bounds__(kFanX * NG)
 k_adj_fan_refl(TX* __restrict__ X, const float* __restrict__ ywp,
                const ColEntry* __restrict__ col, const ViewEntry* __restrict__ view, DetGrid G,
                int nx, int ny, int na, int nv, const int* __restrict__ skip)
 {
     if (skip && *skip) return;
-    __shared__ float smem[kTurnGroups * 2 * NR * PB * PB * kFanX];
-    fan_refl_adjoint_block<TX, NR, PB>(X, ywp, col, view, G, nx, ny, na, nv, blockIdx.x * kFanX,
-                                       blockIdx.y, smem);
+    __shared__ float smem[NG * 2 * NR * PB * PB * kFanX];
+    fan_refl_adjoint_block<TX, NR, PB, NG>(X, ywp, col, view, G, nx, ny, na, nv,
+                                           blockIdx.x * kFanX, blockIdx.y, smem);
 }
 
 // Transposed copy of fan images (all frames): xt[f nper + x ny + y] =
@@ -551,15 +551,15 @@ k_adj_fan(TX* __restrict__ X, const float* __restrict__ yw, const ColEntry* __re
 // Fan adjoint of a turn plan (G = 2 or 4, one frame): blocks of kFanX P x P
 // blocks of primary pixels x kTurnGroups view groups (fan_turn_adjoint_block;
 // the bits do not depend on P).
-template <typename TX, int G, int P>
-__global__ void __launch_bounds__(kFanX * kTurnGroups)
+template <typename TX, int G, int P, int NG>
+__global__ void __launch_bounds__(kFanX * NG)
 k_adj_fan_turn(TX* __restrict__ X, const float* __restrict__ ywp,
                const ColEntry* __restrict__ col, const ViewEntry* __restrict__ view, DetGrid D,
                int nx, int ny, int na, int nv, const int* __restrict__ skip)
 {
     if (skip && *skip) return;                 // uniform (one flag for the launch)
-    fan_turn_adjoint_block<TX, G, P>(X, ywp, col, view, D, nx, ny, na, nv,
-                                     blockIdx.x * kFanX * P, blockIdx.y * P);
+    fan_turn_adjoint_block<TX, G, P, NG>(X, ywp, col, view, D, nx, ny, na, nv,
+                                         blockIdx.x * kFanX * P, blockIdx.y * P);
 }
 
 // ---------------------------------------------------------------------------
@@ -1405,6 +1405,15 @@ int fl_plan_fan_lanes(const fl_plan* p)
     return fan_turn_lanes((long long)p->s.na * (p->s.nv / G));
 }
 
+int fl_plan_fan_groups(const fl_plan* p)
+{
+    // the quarter-turn reflection backprojection with 2 x 2 blocks keeps 8
+    // (16 would need 64 KB of shared memory per thread block)
+    const int NR = p->s.ndim == 2 ? fl_plan_refl(p) : 0;
+    if (NR == 4 && fan_refl_pblock(NR, p->s.nx, p->s.ny) == 2) return kTurnGroups;
+    return p->fan_groups ? p->fan_groups : kTurnGroups;
+}
+
 int fl_plan_fan_block(const fl_plan* p)
 {
     if (p->fan_block) return p->fan_block;
@@ -1601,37 +1610,47 @@ void launch_adj(fl_plan* p, const float* yw, void* x, const int* skip, int xfold
         const int NR = fl_plan_refl(p);
         const int PB = fan_refl_pblock(NR, s.nx, s.ny);
         const int hxb = (NR == 1 ? s.nx : s.nx / 2) / PB, hyb = (s.ny / 2) / PB;
-        const dim3 blk(kFanX, kTurnGroups), g1(fl_div_up(hxb, kFanX), hyb);
-#define FL_ADJ_FAN_REFL(NN, PP)                                                              \
-    k_adj_fan_refl<TX, NN, PP><<<g1, blk, 0, st>>>((TX*)x, yw, p->d_col, p->d_view, G, s.nx, \
-                                                   s.ny, s.na, s.nv, skip)
-        if (NR == 4 && PB == 2) FL_ADJ_FAN_REFL(4, 2);
-        else if (NR == 4) FL_ADJ_FAN_REFL(4, 1);
-        else if (NR == 2 && PB == 2) FL_ADJ_FAN_REFL(2, 2);
-        else if (NR == 2) FL_ADJ_FAN_REFL(2, 1);
-        else if (PB == 2) FL_ADJ_FAN_REFL(1, 2);
-        else FL_ADJ_FAN_REFL(1, 1);
+        const int NG = fl_plan_fan_groups(p);
+        const dim3 blk(kFanX, NG), g1(fl_div_up(hxb, kFanX), hyb);
+#define FL_ADJ_FAN_REFL(NN, PP, GG)                                                          \
+    k_adj_fan_refl<TX, NN, PP, GG><<<g1, blk, 0, st>>>((TX*)x, yw, p->d_col, p->d_view, G,   \
+                                                       s.nx, s.ny, s.na, s.nv, skip)
+#define FL_ADJ_FAN_REFL_G(NN, PP)                                                            \
+    do {                                                                                     \
+        if (NG == 16) FL_ADJ_FAN_REFL(NN, PP, 16);                                           \
+        else FL_ADJ_FAN_REFL(NN, PP, kTurnGroups);                                           \
+    } while (0)
+        if (NR == 4 && PB == 2) FL_ADJ_FAN_REFL(4, 2, kTurnGroups);   // fl_plan_fan_groups
+        else if (NR == 4) FL_ADJ_FAN_REFL_G(4, 1);
+        else if (NR == 2 && PB == 2) FL_ADJ_FAN_REFL_G(2, 2);
+        else if (NR == 2) FL_ADJ_FAN_REFL_G(2, 1);
+        else if (PB == 2) FL_ADJ_FAN_REFL_G(1, 2);
+        else FL_ADJ_FAN_REFL_G(1, 1);
+#undef FL_ADJ_FAN_REFL_G
 #undef FL_ADJ_FAN_REFL
     } else if (fl_plan_turns(p) > 1) {
         // 2 x 2 primary blocks once there are at least 4 waves of them, else
         // one primary pixel per thread (the same bits)
         const int T = fl_plan_turns(p);
         const int hx = T == 2 ? s.nx : s.nx / 2, hy = s.ny / 2;
-        const dim3 blk(kFanX, kTurnGroups);
+        const int NG = fl_plan_fan_groups(p);
+        const dim3 blk(kFanX, NG);
         const dim3 g2(fl_div_up(hx, 2 * kFanX), fl_div_up(hy, 2)), g1(fl_div_up(hx, kFanX), hy);
         const bool two = fl_plan_fan_block(p) == 2;
-        if (T == 4 && two)
-            k_adj_fan_turn<TX, 4, 2><<<g2, blk, 0, st>>>((TX*)x, yw, p->d_col, p->d_view, G, s.nx,
-                                                         s.ny, s.na, s.nv, skip);
-        else if (T == 4)
-            k_adj_fan_turn<TX, 4, 1><<<g1, blk, 0, st>>>((TX*)x, yw, p->d_col, p->d_view, G, s.nx,
-                                                         s.ny, s.na, s.nv, skip);
-        else if (two)
-            k_adj_fan_turn<TX, 2, 2><<<g2, blk, 0, st>>>((TX*)x, yw, p->d_col, p->d_view, G, s.nx,
-                                                         s.ny, s.na, s.nv, skip);
-        else
-            k_adj_fan_turn<TX, 2, 1><<<g1, blk, 0, st>>>((TX*)x, yw, p->d_col, p->d_view, G, s.nx,
-                                                         s.ny, s.na, s.nv, skip);
+#define FL_ADJ_FAN_TURN(TT, PP, GG)                                                          \
+    k_adj_fan_turn<TX, TT, PP, GG><<<PP == 2 ? g2 : g1, blk, 0, st>>>(                       \
+        (TX*)x, yw, p->d_col, p->d_view, G, s.nx, s.ny, s.na, s.nv, skip)
+#define FL_ADJ_FAN_TURN_G(TT, PP)                                                            \
+    do {                                                                                     \
+        if (NG == 16) FL_ADJ_FAN_TURN(TT, PP, 16);                                           \
+        else FL_ADJ_FAN_TURN(TT, PP, kTurnGroups);                                           \
+    } while (0)
+        if (T == 4 && two) FL_ADJ_FAN_TURN_G(4, 2);
+        else if (T == 4) FL_ADJ_FAN_TURN_G(4, 1);
+        else if (two) FL_ADJ_FAN_TURN_G(2, 2);
+        else FL_ADJ_FAN_TURN_G(2, 1);
+#undef FL_ADJ_FAN_TURN_G
+#undef FL_ADJ_FAN_TURN
     } else {
         // 2 x 2 pixel blocks, one thread each, once there are at least 4 waves
         // of 128-thread blocks; else one pixel per view group
@@ -1937,17 +1956,20 @@ extern "C" int fl_plan_autotune(fl_plan* p, void* stream, int32_t* shapes)
             if (fwd && !turn) continue;            // the general forward has no parts
             float best = 3.0e38f;
             int bi = 0;
-            for (int c = 0; c < (fwd ? 3 : 2) && !st; c++) {
+            // backprojection: pixel block 1 or 2 x view groups 8 or 16 (turn
+            // and reflection forms; the general one has its own groups)
+            const int nc = fwd ? 3 : (turn ? 4 : 2);
+            for (int c = 0; c < nc && !st; c++) {
                 if (fwd) p->fan_lanes = parts[c];
-                else p->fan_block = c + 1;
+                else { p->fan_block = c % 2 + 1; p->fan_groups = c < 2 ? kTurnGroups : 16; }
                 float ms = 0.0f;
                 st = timed(fwd, ms);
                 if (!st && ms < best) { best = ms; bi = c; }
             }
             if (fwd) p->fan_lanes = parts[bi];
-            else p->fan_block = bi + 1;
+            else { p->fan_block = bi % 2 + 1; p->fan_groups = bi < 2 ? kTurnGroups : 16; }
         }
-        if (st) p->fan_lanes = p->fan_block = 0;
+        if (st) p->fan_lanes = p->fan_block = p->fan_groups = 0;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -1958,7 +1980,7 @@ extern "C" int fl_plan_autotune(fl_plan* p, void* stream, int32_t* shapes)
             shapes[2] = p->adj_bx; shapes[3] = p->adj_by;
         } else {
             shapes[0] = fl_plan_fan_lanes(p); shapes[1] = 0;
-            shapes[2] = fl_plan_fan_block(p); shapes[3] = 0;
+            shapes[2] = fl_plan_fan_block(p); shapes[3] = fl_plan_fan_groups(p);
         }
     }
     return fl_set_error(FL_OK, "");

@@ -988,7 +988,9 @@ __device__ __forceinline__ void fan_turn_pixels(int ix, int iy, int nx, int ny, 
     }
 }
 
-// View groups of the fan turn adjoint (k_adj_fan_turn).
+// View groups of the fan turn and reflection backprojections: 8 in batches
+// and by default; a plan may take 16 (FL_TUNE_FAN_GROUPS), which changes the
+// order of a pixel's additions.
 constexpr int kTurnGroups = 8;
 
 // Turn k of a P x P block of primary pixels with lower corner (ix0, iy0):
@@ -1171,7 +1173,7 @@ __device__ __forceinline__ void fan_turn_forward_block(const TX* __restrict__ X,
 // (fan_turn_gather). The groups' sums meet in shared memory and are added in
 // the order g = 0, 1, ...; group 0 stores the pixels. Every thread of the
 // block must call it (it synchronises the block).
-template <typename TX, int G, int P>
+template <typename TX, int G, int P, int NG = kTurnGroups>
 __device__ __forceinline__ void fan_turn_adjoint_block(TX* __restrict__ X,
                                                        const float* __restrict__ ywp,
                                                        const ColEntry* __restrict__ col,
@@ -1189,8 +1191,8 @@ __device__ __forceinline__ void fan_turn_adjoint_block(TX* __restrict__ X,
 #pragma unroll
             for (int i = 0; i < P; i++) acc[m][j][i] = 0.0f;
     if (bx < hx)
-        fan_turn_gather<G, P>(acc, ywp, col, view, D, bx, iy0, nx, ny, na, nv, g, kTurnGroups);
-    __shared__ float part[kTurnGroups][G * P * P][kFanX];
+        fan_turn_gather<G, P>(acc, ywp, col, view, D, bx, iy0, nx, ny, na, nv, g, NG);
+    __shared__ float part[NG][G * P * P][kFanX];
 #pragma unroll
     for (int m = 0; m < G; m++)
 #pragma unroll
@@ -1210,7 +1212,7 @@ __device__ __forceinline__ void fan_turn_adjoint_block(TX* __restrict__ X,
             for (int m = 0; m < G; m++) {
                 float sum = part[0][(m * P + j) * P + i][tx];
 #pragma unroll
-                for (int k = 1; k < kTurnGroups; k++) sum += part[k][(m * P + j) * P + i][tx];
+                for (int k = 1; k < NG; k++) sum += part[k][(m * P + j) * P + i][tx];
                 Store<TX>::st(X + (long long)py[m] * nx + px[m], sum);
             }
         }
@@ -1495,10 +1497,10 @@ constexpr int kFanReflShared = kTurnGroups * 2 * 4 * 4 * kFanX;
 // lower corner (PB (bx0 + x), PB by) where it is a primary block (in block
 // units: x < the domain's width; NR = 4: x <= by) over view group g of the
 // walked views (fan_refl_gather). The groups' sums meet in shared memory
-// (smem: kFanReflShared floats) and are added in the order g = 0, 1, ...;
+// (smem: NG 2 NR PB^2 kFanX floats) and are added in the order g = 0, 1, ...;
 // group 0 stores the images. Every thread of the block must call it (it
 // synchronises the block).
-template <typename TX, int NR, int PB>
+template <typename TX, int NR, int PB, int NG = kTurnGroups>
 __device__ __forceinline__ void fan_refl_adjoint_block(TX* __restrict__ X,
                                                        const float* __restrict__ ywp,
                                                        const ColEntry* __restrict__ col,
@@ -1519,8 +1521,7 @@ __device__ __forceinline__ void fan_refl_adjoint_block(TX* __restrict__ X,
 #pragma unroll
             for (int a = 0; a < PB; a++) { P[j][b][a] = 0.0f; Q[j][b][a] = 0.0f; }
     if (prim)
-        fan_refl_gather<NR, PB>(P, Q, ywp, col, view, D, X0, Y0, nx, ny, na, nv, g, kTurnGroups);
-    static_assert(kTurnGroups * 2 * NV * kFanX <= kFanReflShared, "shared buffer");
+        fan_refl_gather<NR, PB>(P, Q, ywp, col, view, D, X0, Y0, nx, ny, na, nv, g, NG);
     float(*part)[2 * NV][kFanX] = reinterpret_cast<float(*)[2 * NV][kFanX]>(smem);
 #pragma unroll
     for (int j = 0; j < NR; j++)
@@ -1536,7 +1537,7 @@ __device__ __forceinline__ void fan_refl_adjoint_block(TX* __restrict__ X,
     auto sum = [&](int k) {
         float t = part[0][k][tx];
 #pragma unroll
-        for (int m = 1; m < kTurnGroups; m++) t += part[m][k][tx];
+        for (int m = 1; m < NG; m++) t += part[m][k][tx];
         return t;
     };
     const bool diag = NR == 4 && X0 == Y0;

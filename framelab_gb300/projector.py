@@ -167,7 +167,8 @@ class Plan:
 
     # launch variants fl_plan_autotune chooses among (fl_plan_option values)
     TUNABLES = {"adj_run": _lib.TUNE_ADJ_RUN, "adj_rows": _lib.TUNE_ADJ_ROWS,
-                "fan_parts": _lib.TUNE_FAN_PARTS, "fan_block": _lib.TUNE_FAN_BLOCK}
+                "fan_parts": _lib.TUNE_FAN_PARTS, "fan_block": _lib.TUNE_FAN_BLOCK,
+                "fan_groups": _lib.TUNE_FAN_GROUPS}
 
     def tuning(self, name: str) -> int:
         """The value in effect of a launch variant (``TUNABLES``)."""
@@ -246,7 +247,8 @@ class Plan:
         if not sh[0]:
             return {"forward": None, "adjoint": None}
         if not self.cone:
-            return {"forward_parts_per_ray": sh[0], "adjoint_pixel_block": sh[2]}
+            return {"forward_parts_per_ray": sh[0], "adjoint_pixel_block": sh[2],
+                    "adjoint_view_groups": sh[3]}
         out = {"forward": (sh[0], sh[1]), "adjoint": (sh[2], sh[3])}
         if self.reflect:
             v = C.c_int()

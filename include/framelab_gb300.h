@@ -237,12 +237,14 @@ int fl_plan_query(const fl_plan *plan, int option, int *value);
  * Cone plans: the 128-thread block shapes (8x16, 16x8, 32x4, 4x32) of both
  * kernels and, on reflection plans, the backprojection's voxel run and row
  * loop (FL_TUNE_ADJ_RUN / _ROWS). Fan plans: the parts per walked ray of the
- * turn forward (FL_TUNE_FAN_PARTS: 1, 4, 16; turn plans) and the pixel block
- * of the backprojections (FL_TUNE_FAN_BLOCK: 1 or 2). Only the fan parts
- * count changes any bit of a result (the order of a ray's additions, not its
- * matrix). Synchronises `stream`; uses the plan's scratch buffers. shapes
- * (optional, [4]): the chosen forward x, y and backprojection x, y of a cone
- * plan; for a fan plan the parts count, 0, the pixel block, 0. */
+ * turn and reflection forwards (FL_TUNE_FAN_PARTS: 1, 4, 16), the pixel block
+ * of the backprojections (FL_TUNE_FAN_BLOCK: 1 or 2) and the view groups of
+ * the turn and reflection backprojections (FL_TUNE_FAN_GROUPS: 8 or 16). Only
+ * the fan parts and groups change any bit of a result (the order of a ray's
+ * or a pixel's additions, not the matrix). Synchronises `stream`; uses the
+ * plan's scratch buffers. shapes (optional, [4]): the chosen forward x, y and
+ * backprojection x, y of a cone plan; for a fan plan the parts count, 0, the
+ * pixel block and the view groups. */
 int fl_plan_autotune(fl_plan *plan, void *stream, int32_t *shapes);
 /* FL_TUNE_ADJ_RUN: voxels per thread of the reflection backprojection (1 or
  * 2); FL_TUNE_ADJ_ROWS: its row loop, 1 or 2 detector rows per iteration, or
@@ -263,6 +265,15 @@ enum { FL_TUNE_ADJ_RUN = 16, FL_TUNE_ADJ_ROWS = 17 };
  * depend on it. fl_plan_option sets them (other values are refused),
  * fl_plan_query reads the values in effect. */
 enum { FL_TUNE_FAN_PARTS = 18, FL_TUNE_FAN_BLOCK = 19 };
+/* FL_TUNE_FAN_GROUPS: view groups of a fan plan's turn and reflection
+ * backprojections, 8 (the default) or 16: each thread block's threads split a
+ * pixel block's views into that many interleaved groups, added in order at
+ * the end. It sets the order of a pixel's additions (its bits within FP32
+ * rounding); batches take 8, so batched and single-plan results are equal bit
+ * for bit with 8. The quarter-turn reflection form with 2 x 2 pixel blocks
+ * always takes 8 (fl_plan_query reports the value in effect).
+ * fl_plan_autotune times both on turn and reflection plans. */
+enum { FL_TUNE_FAN_GROUPS = 20 };
 
 /* y = A x on `stream`. x: n_vox elements, y: n_rays elements, device memory. */
 int fl_forward(fl_plan *plan, int model, const void *x, int x_dtype, void *y, int y_dtype,

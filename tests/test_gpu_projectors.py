@@ -996,8 +996,9 @@ def test_fan_autotune_parts_and_pixel_block(nv, refl):
     """Fan plans: the tuner picks the parts per walked ray of the turn and
     reflection forwards (quarter turn at nv = 20; half turn at 18, with the
     reflection or not; at 9 the reflection alone, or the general plan, which
-    has no parts) and the backprojection's pixel block. The pixel block keeps
-    every bit; the parts change only the order of a ray's additions."""
+    has no parts), the backprojection's pixel block and its view groups. The
+    pixel block keeps every bit; the parts and the groups change only the
+    order of a ray's or a pixel's additions."""
     from framelab_gb300 import _lib
     P = _plan(G.fan_para(64, 64, 128, nv, L=(1, 1), SO=3.0, OD=3.0, Ly=3.0))
     P.reflect = refl
@@ -1012,6 +1013,12 @@ def test_fan_autotune_parts_and_pixel_block(nv, refl):
     general = P.views_per_walk == 1
     assert sh["forward_parts_per_ray"] == (1 if general else P.tuning("fan_parts")), sh
     assert sh["forward_parts_per_ray"] in (1, 4, 16)
+    assert sh["adjoint_view_groups"] == P.tuning("fan_groups") in ((8,) if general else (8, 16))
+    # 16 view groups add a pixel's views in another order
+    P.set_tuning("fan_groups", 16)
+    x16 = _host(P.adjoint(r))
+    assert np.linalg.norm(x16 - x0) <= 1e-6 * np.linalg.norm(x0)
+    P.set_tuning("fan_groups", 8)
     assert np.array_equal(_host(P.adjoint(r)), x0)
     for blk in (1, 2):
         P.set_tuning("fan_block", blk)
@@ -1027,6 +1034,7 @@ def test_fan_autotune_parts_and_pixel_block(nv, refl):
     L = _lib.load()
     assert L.fl_plan_option(P.handle, _lib.TUNE_FAN_PARTS, 2) == _lib.FL_ERR_INVALID
     assert L.fl_plan_option(P.handle, _lib.TUNE_FAN_BLOCK, 3) == _lib.FL_ERR_INVALID
+    assert L.fl_plan_option(P.handle, _lib.TUNE_FAN_GROUPS, 12) == _lib.FL_ERR_INVALID
 
 
 # degenerate and small sizes: one view, one detector column or row, a 1-pixel
