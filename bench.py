@@ -472,11 +472,20 @@ def projector_roofline(ctx, workload, n_isect, n_rays, n_vox, t_fwd, t_adj, deta
            "algorithmic_frac": alg / t / 1e9 / peak if peak else None}
     m = roofline_model(l1_form) if l1_form else None
     if not m:
-        return {"bound": "hbm", "achieved": alg / t / 1e9, "peak": peak, "unit": "GB/s",
-                "frac": alg / t / 1e9 / peak if peak else None, "traffic": None,
+        # no per-intersection L1 model for this kernel form: the DRAM view of
+        # the compulsory bytes, with the gather bytes (served by L1 / L2)
+        # beside it -- those exceed what HBM could deliver, so they are no
+        # roofline
+        return {"bound": "hbm", "achieved": compulsory / t / 1e9, "peak": peak, "unit": "GB/s",
+                "frac": compulsory / t / 1e9 / peak if peak else None, "traffic": None,
                 "kernel": f"{label} {dom} (f32 storage)", "peak_source": src,
-                "bytes_definition": "sum over rays of voxels crossed x element bytes + "
-                                    "one element per ray (forward) / per voxel (adjoint)"}
+                "bytes_definition": "compulsory: one element per ray and per voxel "
+                                    "(input read once, output written once)",
+                "gathers_served_by_l1_l2": {
+                    "GBps": alg / t / 1e9,
+                    "bytes_definition": "sum over rays of voxels crossed x element bytes + "
+                                        "one element per ray (forward) / per voxel (adjoint)"},
+                "note": "latency / issue / L1 bound (profiles/ for the counters)"}
     k = m[dom]
     f = (sm_mhz or 2070.0) * 1e6
     sms = m["sms"]

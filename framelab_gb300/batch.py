@@ -88,12 +88,12 @@ class FanBatch:
     def launches_per_iteration(self) -> int:
         """Kernel launches of one CGLS iteration: forward and adjoint for each
         kind of slice present (general, turn, reflection), the transposed
-        copy of the direction the turn and reflection forwards read, and the
-        three algebra kernels."""
+        copy of the direction the forwards read, and the three algebra
+        kernels."""
         general = any(t == 1 for t in self.turns)
         turned = any(t > 1 and not r for t, r in zip(self.turns, self.reflect))
         mirrored = any(self.reflect)
-        return 3 + 2 * (int(general) + int(turned) + int(mirrored)) + int(turned or mirrored)
+        return 4 + 2 * (int(general) + int(turned) + int(mirrored))
 
     def __del__(self):
         h = getattr(self, "_h", None)

@@ -24,9 +24,9 @@
 // finish sums that slice's partials in a fixed order, so results do not depend
 // on scheduling). One iteration = 3 launches (q += lam p with <p,q>, updates
 // with <r,r>, direction) plus a forward with c_r^2 and an adjoint for each
-// kind of slice present (general, turn, reflection; parallel branches) and,
-// with turn or reflection slices, the transposed copy of the direction their
-// forward reads, captured once as a CUDA graph and replayed.
+// kind of slice present (general, turn, reflection; parallel branches) and
+// the transposed copy of the direction the forwards read, captured once as a
+// CUDA graph and replayed.
 // A stopped slice's chunks return at once.
 #include <algorithm>
 #include <cstring>
@@ -121,7 +121,7 @@ __device__ bool slice_sum(double v, int slice, int c0, int c1, double* partials,
 
 // y = c_r^cr_power * (sum of w x along each ray), one block per ray chunk
 __global__ void __launch_bounds__(kRayChunk, 8)
-k_batch_fwd(const float* __restrict__ X, float* __restrict__ Y,
+k_batch_fwd(const float* __restrict__ X, const float* __restrict__ XT, float* __restrict__ Y,
             const BatchSlice* __restrict__ sl, const int2* __restrict__ chunks, int cr_power,
             int scratch, const BatchScal* __restrict__ S)
 {
@@ -130,8 +130,10 @@ k_batch_fwd(const float* __restrict__ X, float* __restrict__ Y,
     const BatchSlice& b = sl[ch.x];
     const int r = ch.y + threadIdx.x;
     if (r >= b.na * b.nv) return;
-    float acc = walk<float, false, false>(X + b.xoff, b.col + r, &b.col[r].y, b.nx, b.ny, 1,
-                                          nullptr, nullptr, (long long)b.nx * b.ny);
+    float a1[1];
+    walk_fan<float, 1>(X + b.xoff, XT + b.xoff, &b.col[r].x, &b.col[r].y, b.nx, b.ny, a1,
+                       (long long)b.nx * b.ny);
+    const float acc = a1[0];
     float cr = ray_cr(b.scale, b.colr[r], 0.0f);
     float out = cr * acc;
     if (cr_power == 2) out = cr * out;
@@ -162,15 +164,13 @@ k_batch_fwd_turn(const float* __restrict__ X, const float* __restrict__ XT, floa
 }
 
 // Transposed copy of every slice's image (XT[xoff + x ny + y] = X[xoff + y nx
-// + x]) over the vector chunks, for the turn and reflection forwards
-// (walk_fan).
+// + x]) over the vector chunks, for the forwards (walk_fan).
 __global__ void __launch_bounds__(kVecThreads)
 k_batch_transpose(const float* __restrict__ X, float* __restrict__ XT,
                   const BatchSlice* __restrict__ sl, const VecChunk* __restrict__ chunks)
 {
     const VecChunk ch = chunks[blockIdx.x];
     const BatchSlice& b = sl[ch.slice];
-    if (b.turns == 1) return;                 // the general forward reads X alone
     for (int k = threadIdx.x; k < ch.len; k += kVecThreads) {
         const int i = ch.start + k, iy = i / b.nx, ix = i - iy * b.nx;
         XT[b.xoff + (long long)ix * b.ny + iy] = X[b.xoff + i];
@@ -700,8 +700,7 @@ static int batch_fwd(fl_batch* b, const float* x, float* y, int cr_power, int yp
                      const BatchScal* S, cudaStream_t s)
 {
     const bool g = b->n_ray_chunks, t = b->n_ray_t_chunks, r = b->n_ray_r_chunks;
-    if (t || r)
-        k_batch_transpose<<<b->n_vec_chunks, kVecThreads, 0, s>>>(x, b->xt, b->d_sl, b->d_vec);
+    k_batch_transpose<<<b->n_vec_chunks, kVecThreads, 0, s>>>(x, b->xt, b->d_sl, b->d_vec);
     const cudaStream_t s2 = (t && g) ? fork_to(s, b->cs2, b->evf) : s;
     const cudaStream_t s3 = (r && (g || t)) ? fork_to(s, b->cs3, b->evf3) : s;
     if (r)
@@ -711,8 +710,8 @@ static int batch_fwd(fl_batch* b, const float* x, float* y, int cr_power, int yp
         k_batch_fwd_turn<<<b->n_ray_t_chunks, kFanBlock, 0, s2>>>(
             x, b->xt, y, b->d_sl, b->d_rays_t, cr_power, ypack, S);
     if (g)
-        k_batch_fwd<<<b->n_ray_chunks, kRayChunk, 0, s>>>(x, y, b->d_sl, b->d_rays, cr_power,
-                                                          ypack, S);
+        k_batch_fwd<<<b->n_ray_chunks, kRayChunk, 0, s>>>(x, b->xt, y, b->d_sl, b->d_rays,
+                                                          cr_power, ypack, S);
     int st = fl_check_launch("batched forward");
     if (!st) st = join_from(s, s2, b->evj);
     if (!st) st = join_from(s, s3, b->evj3);

@@ -275,11 +275,18 @@ enum { FL_TUNE_FAN_PARTS = 18, FL_TUNE_FAN_BLOCK = 19 };
  * fl_plan_autotune times both on turn and reflection plans. */
 enum { FL_TUNE_FAN_GROUPS = 20 };
 
-/* y = A x on `stream`. x: n_vox elements, y: n_rays elements, device memory. */
+/* y = A x on `stream`. x: n_vox elements, y: n_rays elements, device memory.
+ * The matched model works in buffers the plan owns: a z-mirror cone plan
+ * folds x into its volume scratch, a fan plan writes the transposed copy of
+ * x its walks read (allocated with the plan). Matched forwards and
+ * backprojections of one plan are therefore ordered on one stream: calls of
+ * one plan that overlap on the GPU (different streams) race; different
+ * plans do not share buffers. */
 int fl_forward(fl_plan *plan, int model, const void *x, int x_dtype, void *y, int y_dtype,
                void *stream);
 /* x = A^T y on `stream`. For FL_MODEL_MATCHED this is the exact transpose of
- * fl_forward's matrix; FL_MODEL_CHORD_REF is the reference's backprojector. */
+ * fl_forward's matrix (it weights y into the plan's sinogram scratch first);
+ * FL_MODEL_CHORD_REF is the reference's backprojector. */
 int fl_adjoint(fl_plan *plan, int model, const void *y, int y_dtype, void *x, int x_dtype,
                void *stream);
 /* Version-1 forward with the cone-beam normalised output (ynorm may be NULL;
@@ -434,8 +441,8 @@ int fl_batch_adjoint(fl_batch *b, const float *y, float *x, void *stream);
  * after each iteration (0 after it stopped); iters_done (host, optional):
  * [n_plans]. One iteration is a replayed CUDA graph of 3 launches plus a
  * forward and a backprojection for each kind of slice present (general,
- * turn, reflection; the kinds run as parallel branches) and, with turn or
- * reflection slices, a transposed copy of the direction they read. */
+ * turn, reflection; the kinds run as parallel branches) and a transposed
+ * copy of the direction the forwards read. */
 int fl_batch_cgls(fl_batch *b, const float *rhs, float *u, float lam, int32_t iters, double tol,
                   int32_t flags, double *gamma_history, int32_t *iters_done, void *stream);
 /* Launch tuner of a batch: times the parts per walked ray of its half- and

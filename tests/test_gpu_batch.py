@@ -82,7 +82,7 @@ def test_batch_turn_slices_bit_identical_to_single_plans():
                            P.adjoint(yi, model="matched").reshape(-1)), i
     # without the turns every slice takes the general kernels, still bit for bit
     B1 = FanBatch(paras, turns=False)
-    assert B1.turns == [1] * 5 and B1.launches_per_iteration == 5
+    assert B1.turns == [1] * 5 and B1.launches_per_iteration == 6
     yb1 = B1.forward(x)
     for i, P in enumerate(B1.plans):
         xi = B1.images(x)[i].reshape(-1).contiguous()
