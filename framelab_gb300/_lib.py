@@ -27,6 +27,7 @@ TUNE_ADJ_ROWS = 17
 TUNE_FAN_PARTS = 18
 TUNE_FAN_BLOCK = 19
 TUNE_FAN_GROUPS = 20
+TUNE_ADJ_CHUNKS = 21
 FRAMELET_OPT_FUSED = 1
 
 

@@ -126,6 +126,12 @@ struct fl_plan {
     // its row loop: 1 or 2 rows per iteration, 3 one pass over the run's rows
     // (runs of 2; 0 = 1)
     int adj_run, adj_rows;
+    // launches over consecutive view chunks of the reflection backprojection
+    // (FP32 output; 0 or 1: one launch), and the diagonal columns'
+    // second sums between them ((nx/2) (nz/2) 4 float2, allocated with
+    // quarter-turn reflection plans)
+    int adj_chunks;
+    float2 *d_dq;
     // fan plans: parts per walked ray of the turn forward (1, 4 or 16; 0 =
     // the scan's default, fl_plan_fan_lanes) and pixels per thread side of
     // the backprojections (1 or 2; 0 = 2 once there are 4 waves of blocks)
@@ -230,6 +236,9 @@ int fl_plan_fan_block(const fl_plan* p);
 // View groups of a fan plan's turn and reflection backprojections (8 or 16):
 // the plan's setting (FL_TUNE_FAN_GROUPS), else 8.
 int fl_plan_fan_groups(const fl_plan* p);
+// View chunks of a cone plan's reflection backprojection: the plan's setting
+// (FL_TUNE_ADJ_CHUNKS) where the output is FP32, else 1.
+int fl_plan_adj_chunks(const fl_plan* p, bool f32_out);
 
 // internal launchers
 int fl_ref_forward(fl_plan* p, const float* x, float* y, cudaStream_t st);

@@ -86,7 +86,8 @@ static void free_plan_arrays(fl_plan* p)
                     p->d_sin_phi, p->d_cos_det, p->d_sin_det,   p->d_cphi_f, p->d_sphi_f,
                     p->d_view_frame, p->d_idY, p->d_Nv,        p->d_col,   p->d_colr,
                     p->d_row,    p->d_rowz,   p->d_view,       p->d_work,
-                    p->d_cos_det2, p->d_sin_det2, p->d_fb_edges, p->d_vwork, p->d_xt};
+                    p->d_cos_det2, p->d_sin_det2, p->d_fb_edges, p->d_vwork, p->d_xt,
+                    p->d_dq};
     for (void* q : ptrs)
         if (q) cudaFree(q);
 }
@@ -361,6 +362,12 @@ extern "C" int fl_plan_option(fl_plan* p, int option, int value)
         p->fan_block = value;
         return fl_set_error(FL_OK, "");
     }
+    if (option == FL_TUNE_ADJ_CHUNKS) {
+        if (value < 1 || value > 64)
+            return fl_set_error(FL_ERR_INVALID, "fl_plan_option: %d view chunks (1 .. 64)", value);
+        p->adj_chunks = value;
+        return fl_set_error(FL_OK, "");
+    }
     if (option == FL_TUNE_FAN_GROUPS) {
         if (value != 8 && value != 16)
             return fl_set_error(FL_ERR_INVALID, "fl_plan_option: %d view groups (8 or 16)", value);
@@ -408,6 +415,10 @@ extern "C" int fl_plan_query(const fl_plan* p, int option, int* value)
     }
     if (option == FL_TUNE_FAN_GROUPS) {
         *value = fl_plan_fan_groups(p);
+        return fl_set_error(FL_OK, "");
+    }
+    if (option == FL_TUNE_ADJ_CHUNKS) {
+        *value = fl_plan_refl(p) && p->s.ndim == 3 ? fl_plan_adj_chunks(p, true) : 1;
         return fl_set_error(FL_OK, "");
     }
     return fl_set_error(FL_ERR_INVALID, "fl_plan_query: unknown option %d", option);
@@ -560,6 +571,12 @@ extern "C" int fl_plan_create(const fl_scan* scan, fl_plan** out)
     // fan plans: the forward's transposed copy of its input (matched.cu)
     if (!st && s.ndim == 2)
         st = fl_check_cuda(fl_malloc(&p->d_xt, (size_t)p->n_vox * sizeof(float)),
+                           "fl_malloc(plan)");
+    // quarter-turn reflection plans: the diagonal columns' second sums
+    // between view chunks of the backprojection (matched.cu)
+    if (!st && s.ndim == 3 && p->refl4_ok)
+        st = fl_check_cuda(fl_malloc((void**)&p->d_dq, (size_t)(s.nx / 2) * (s.nz / 2) * 4 *
+                                                           sizeof(float2)),
                            "fl_malloc(plan)");
     if (st) {
         free_plan_arrays(p);

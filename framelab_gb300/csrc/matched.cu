@@ -18,6 +18,8 @@
 // entries in the same frame -- the exact transpose, with no atomics.
 #include <algorithm>
 
+#include <type_traits>
+
 #include "fl_trace.h"
 #include "fl_common.cuh"
 #include "fl_plan.h"
@@ -1147,12 +1149,20 @@ __device__ __forceinline__ void adj_rows_refl(float2 (&P)[NR][TZ], float2 (&Q)[N
 // thus feeds 4 NR (voxel, ray) pairs. yw is the packed input of
 // k_weight_packed_refl / k_fwd_refl (two planes); X the tiled folded volume
 // (xfold) or the standard one.
+// View chunks: the walked views w0 .. w1 only. A launch that is not the
+// first continues the sums it finds in X (FP32, either layout) and one that
+// is not the last leaves them there, so a sequence of launches over
+// consecutive chunks adds every term in the order one launch would: the bits
+// are the same. On the diagonal (NR = 4, x == y) P and Q are carried apart
+// between chunks, P in X and Q in dq (dq[((x * dqz + z) * NR + j)] for the
+// voxel pair at height z < nz/2), and combined by the last.
 template <typename TX, int TZ, int RU, typename TW, int NR>
 __global__ void __launch_bounds__(128, TZ == 1 ? (RU == 2 ? 6 : 8) : (RU == 1 ? 6 : 5))
 k_adj_refl(TX* __restrict__ X, const TW* __restrict__ yw, const ColEntry* __restrict__ col,
            const AxisEntry* __restrict__ rowz, const ViewEntry* __restrict__ view, DetGrid G,
            int nx, int ny, int nz, int na, int nb, int nv, float dz,
-           const int* __restrict__ skip, int xfold)
+           const int* __restrict__ skip, int xfold, int w0, int w1, int first, int last,
+           float2* __restrict__ dq, int dqz)
 {
     if (skip && *skip) return;
     const ReflGeom g = refl_geom(NR, nv, na, nb);
@@ -1173,7 +1183,44 @@ k_adj_refl(TX* __restrict__ X, const TW* __restrict__ yw, const ColEntry* __rest
         for (int k = 0; k < TZ; k++) { P[j][k] = make_float2(0.0f, 0.0f); Q[j][k] = P[j][k]; }
     const float inv_dv = 1.0f / G.dv;
     const int nsteps = diag ? NR : 2 * NR;
-    for (int w = 0; w <= g.ov; w++) {
+    // C_j = S^j V0 and D_j = S^j M V0 of the thread's column (the stores
+    // below; the loads of a chunk after the first)
+    const long long nxy = (long long)nx * ny;
+    int cx[NR], cy[NR], dxs[NR], dys[NR];
+    if (NR == 4) {
+        cx[0] = ix; cx[1 % NR] = nx - 1 - iy; cx[2 % NR] = nx - 1 - ix; cx[3 % NR] = iy;
+        cy[0] = iy; cy[1 % NR] = ix; cy[2 % NR] = ny - 1 - iy; cy[3 % NR] = ny - 1 - ix;
+        dxs[0] = ix; dxs[1 % NR] = iy; dxs[2 % NR] = nx - 1 - ix; dxs[3 % NR] = nx - 1 - iy;
+        dys[0] = ny - 1 - iy; dys[1 % NR] = ix; dys[2 % NR] = iy; dys[3 % NR] = ny - 1 - ix;
+    } else {
+        cx[0] = ix; cx[1 % NR] = nx - 1 - ix; cy[0] = iy; cy[1 % NR] = ny - 1 - iy;
+        dxs[0] = ix; dxs[1 % NR] = nx - 1 - ix; dys[0] = ny - 1 - iy; dys[1 % NR] = iy;
+    }
+    if (!first) {                                    // continue the chunk before
+#pragma unroll
+        for (int k = 0; k < TZ; k++)
+            if (k < nk) {
+                const int zl = (z0 + k) * (int)nxy;
+#pragma unroll
+                for (int j = 0; j < 2 * NR; j++) {
+                    if (diag && j >= NR) {
+                        Q[j - NR][k] = dq[((long long)ix * dqz + z0 + k) * NR + (j - NR)];
+                        continue;
+                    }
+                    const int qx = j < NR ? cx[j] : dxs[j - NR], qy = j < NR ? cy[j] : dys[j - NR];
+                    const float* Xf = (const float*)X;
+                    float2 a;
+                    if (xfold) {
+                        a = Store<float>::ld2(Xf + 2 * tiled_pair(qx, qy, zl, nx >> 2));
+                    } else {
+                        const long long c = (long long)qy * nx + qx;
+                        a = make_float2(Xf[zl + c], Xf[(long long)(nz - 1 - z0 - k) * nxy + c]);
+                    }
+                    if (j < NR) P[j][k] = a; else Q[j - NR][k] = a;
+                }
+            }
+    }
+    for (int w = w0; w <= min(w1, g.ov); w++) {
         int vt, rs, alim;
         long long base;
         refl_view(g, w, vt, base, rs, alim);
@@ -1250,30 +1297,23 @@ k_adj_refl(TX* __restrict__ X, const TW* __restrict__ yw, const ColEntry* __rest
         }
     }
     // C_j = S^j V0 holds P[j] (and, on the diagonal of NR = 4, Q[j + 1], the
-    // sums of D_{j+1} = C_j); D_j = S^j M V0 holds Q[j]
-    const long long nxy = (long long)nx * ny;
-    int cx[NR], cy[NR], dxs[NR], dys[NR];
-    if (NR == 4) {
-        cx[0] = ix; cx[1] = nx - 1 - iy; cx[2] = nx - 1 - ix; cx[3] = iy;
-        cy[0] = iy; cy[1] = ix; cy[2] = ny - 1 - iy; cy[3] = ny - 1 - ix;
-        dxs[0] = ix; dxs[1] = iy; dxs[2] = nx - 1 - ix; dxs[3] = nx - 1 - iy;
-        dys[0] = ny - 1 - iy; dys[1] = ix; dys[2] = iy; dys[3] = ny - 1 - ix;
-    } else {
-        cx[0] = ix; cx[1] = nx - 1 - ix; cy[0] = iy; cy[1] = ny - 1 - iy;
-        dxs[0] = ix; dxs[1] = nx - 1 - ix; dys[0] = ny - 1 - iy; dys[1] = iy;
-    }
+    // sums of D_{j+1} = C_j; before the last chunk they stay apart, Q in dq);
+    // D_j = S^j M V0 holds Q[j]
 #pragma unroll
     for (int k = 0; k < TZ; k++)
         if (k < nk) {
             const long long zl = (long long)(z0 + k) * nxy, zh = (long long)(nz - 1 - z0 - k) * nxy;
 #pragma unroll
             for (int j = 0; j < 2 * NR; j++) {
-                if (diag && j >= NR) break;
+                if (diag && j >= NR) {
+                    if (!last) dq[((long long)ix * dqz + z0 + k) * NR + (j - NR)] = Q[j - NR][k];
+                    continue;
+                }
                 float2 a;
                 int qx, qy;
                 if (j < NR) {
                     a = P[j][k];
-                    if (diag) {
+                    if (diag && last) {
                         const float2 b = Q[(j + 1) % NR][k];
                         a.x += b.x; a.y += b.y;
                     }
@@ -1403,6 +1443,13 @@ int fl_plan_fan_lanes(const fl_plan* p)
     if (const int NR = fl_plan_refl(p))           // walked rays: slots x columns
         return fan_turn_lanes((long long)p->s.na * fan_refl_geom(NR, p->s.nv, p->s.na).slots);
     return fan_turn_lanes((long long)p->s.na * (p->s.nv / G));
+}
+
+int fl_plan_adj_chunks(const fl_plan* p, bool f32_out)
+{
+    if (!f32_out || p->adj_chunks < 2) return 1;
+    if (fl_plan_refl(p) == 4 && !p->d_dq) return 1;        // no room for the diagonal's sums
+    return p->adj_chunks;
 }
 
 int fl_plan_fan_groups(const fl_plan* p)
@@ -1546,10 +1593,17 @@ void launch_adj_cone(fl_plan* p, const TW* yw, void* x, const int* skip, int xfo
             zruns = (nzw + run - 1) / run;
             const dim3 ab = p->adj_bx ? dim3(p->adj_bx, p->adj_by) : dim3(8, 16);
             dim3 grid(fl_div_up(s.nx / 2, ab.x), fl_div_up(s.ny / 2, ab.y), (unsigned)zruns);
+            // view chunks (fl_plan_adj_chunks): launches over consecutive
+            // walked views, so the blocks resident together read the same
+            // views' rows from L2; FP32 output only
+            const int nch = fl_plan_adj_chunks(p, std::is_same<TX, float>::value);
+            const int wper = (refl_geom(NR, s.nv, s.na, s.nb).ov + nch) / nch;
 #define FL_ADJ_REFL(TZ_, RU_, NR_)                                                             \
-    k_adj_refl<TX, TZ_, RU_, TW, NR_><<<grid, ab, 0, st>>>(                                     \
-        (TX*)x, yw, p->d_col, p->d_rowz, p->d_view, G, s.nx, s.ny, s.nz, s.na, s.nb, s.nv, s.dz, \
-        skip, xfold)
+    for (int c = 0; c < nch; c++)                                                             \
+        k_adj_refl<TX, TZ_, RU_, TW, NR_><<<grid, ab, 0, st>>>(                                 \
+            (TX*)x, yw, p->d_col, p->d_rowz, p->d_view, G, s.nx, s.ny, s.nz, s.na, s.nb, s.nv,   \
+            s.dz, skip, xfold, c * wper, c * wper + wper - 1, c == 0, c == nch - 1, p->d_dq,    \
+            s.nz / 2)
 #define FL_ADJ_REFL_NR(NR_)                                                                    \
     do {                                                                                       \
         if (run == 1 && ru == 1) FL_ADJ_REFL(1, 1, NR_);                                      \
@@ -1947,7 +2001,22 @@ extern "C" int fl_plan_autotune(fl_plan* p, void* stream, int32_t* shapes)
                 p->adj_run = var[br][0]; p->adj_rows = var[br][1];
             }
         }
-        if (st) p->fwd_bx = p->fwd_by = p->adj_bx = p->adj_by = p->adj_run = p->adj_rows = 0;
+        // then the view chunks of the reflection backprojection (FP32 output)
+        if (!st && fl_plan_refl(p) && p->zmirror) {
+            static const int chunks[4] = {1, 4, 8, 16};
+            float best = 3.0e38f;
+            int bi = 0;
+            for (int c = 0; c < 4 && !st; c++) {
+                p->adj_chunks = chunks[c];
+                float ms = 0.0f;
+                st = timed(false, ms);
+                if (!st && ms < best) { best = ms; bi = c; }
+            }
+            p->adj_chunks = chunks[bi];
+        }
+        if (st)
+            p->fwd_bx = p->fwd_by = p->adj_bx = p->adj_by = p->adj_run = p->adj_rows =
+                p->adj_chunks = 0;
     } else {
         static const int parts[3] = {1, 4, 16};
         const bool turn = fl_plan_turns(p) > 1;

@@ -168,7 +168,7 @@ class Plan:
     # launch variants fl_plan_autotune chooses among (fl_plan_option values)
     TUNABLES = {"adj_run": _lib.TUNE_ADJ_RUN, "adj_rows": _lib.TUNE_ADJ_ROWS,
                 "fan_parts": _lib.TUNE_FAN_PARTS, "fan_block": _lib.TUNE_FAN_BLOCK,
-                "fan_groups": _lib.TUNE_FAN_GROUPS}
+                "fan_groups": _lib.TUNE_FAN_GROUPS, "adj_chunks": _lib.TUNE_ADJ_CHUNKS}
 
     def tuning(self, name: str) -> int:
         """The value in effect of a launch variant (``TUNABLES``)."""
@@ -256,6 +256,8 @@ class Plan:
             out["adjoint_voxels_per_thread"] = v.value
             _lib.check(self._L.fl_plan_query(self._h, _lib.TUNE_ADJ_ROWS, C.byref(v)))
             out["adjoint_rows_per_iteration"] = v.value
+            _lib.check(self._L.fl_plan_query(self._h, _lib.TUNE_ADJ_CHUNKS, C.byref(v)))
+            out["adjoint_view_chunks"] = v.value
         return out
 
     def count_intersections(self, stream=None) -> torch.Tensor:

@@ -274,6 +274,15 @@ enum { FL_TUNE_FAN_PARTS = 18, FL_TUNE_FAN_BLOCK = 19 };
  * always takes 8 (fl_plan_query reports the value in effect).
  * fl_plan_autotune times both on turn and reflection plans. */
 enum { FL_TUNE_FAN_GROUPS = 20 };
+/* FL_TUNE_ADJ_CHUNKS: the reflection backprojection of a cone plan runs as
+ * this many launches over consecutive chunks of its walked views (1 .. 64;
+ * default 1), each continuing the sums the one before left in the output, so
+ * the blocks resident together read the same views' detector rows and L2
+ * serves them (512^3, 720 views: 16 chunks, 264 -> 256 ms per CGLS iteration).
+ * The sums are added in the same order: the results do not depend on it. It
+ * applies where the backprojection writes FP32 (FP16 / BF16 outputs take one
+ * launch). fl_plan_autotune times 1, 4, 8, 16. */
+enum { FL_TUNE_ADJ_CHUNKS = 21 };
 
 /* y = A x on `stream`. x: n_vox elements, y: n_rays elements, device memory.
  * The matched model works in buffers the plan owns: a z-mirror cone plan

@@ -617,6 +617,37 @@ def test_quarter_turn_is_detected_and_exact():
     assert _rel(_host(u8), _host(u4)) < 1e-3
 
 
+@pytest.mark.parametrize("geom", ["circle16", "circle24"])
+def test_reflection_view_chunks_keep_the_bits(geom):
+    """The reflection backprojection run as launches over view chunks
+    (FL_TUNE_ADJ_CHUNKS, FP32 output in either layout) continues each sum
+    where the chunk before left it, the diagonal columns' second sums in
+    their own buffer: the public backprojection (standard layout) and every
+    CGLS iterate (folded layout) are the same bit for bit for 1, 2, 3, 4 and
+    16 chunks (more chunks than walked views included), quarter turns
+    (diagonal columns) and half turn alike."""
+    from framelab_gb300.solvers import NativeCGLS
+    torch = _torch()
+    nv = 16 if geom == "circle16" else 24
+    p = G.cone_para_mm(32, nv, 48, 40, det_pitch_mm=8.0, SO_mm=600.0, SD_mm=1200.0,
+                       voxel_mm=8.0)
+    for quarter in (True, False):
+        P = _plan(p)
+        P.quarter_turn = quarter
+        assert P.reflect and P.views_per_walk == (8 if quarter else 4)
+        b = P.adjoint(P.forward(_dev(PH.ellipsoids_3d(32, seed=3).reshape(-1)))).reshape(-1)
+        r = _dev(np.random.default_rng(4).standard_normal(P.n_rays).astype(np.float32))
+        us, xs = [], []
+        for ch in (1, 2, 3, 4, 16):
+            P.set_tuning("adj_chunks", ch)
+            assert P.tuning("adj_chunks") == ch
+            us.append(_host(NativeCGLS(P, "graph").solve(b.contiguous(), iters=4)))
+            xs.append(_host(P.adjoint(r)))
+        for ch, u, xa in zip((2, 3, 4, 16), us[1:], xs[1:]):
+            assert np.array_equal(u, us[0]), (quarter, ch)
+            assert np.array_equal(xa, xs[0]), (quarter, ch)
+
+
 def test_reflection_is_detected_and_exact():
     torch = _torch()
     from framelab_gb300.solvers import NativeCGLS
@@ -986,6 +1017,8 @@ def test_autotune_keeps_the_projections(zm):
                 assert L.fl_plan_option(P.handle, _lib.TUNE_ADJ_RUN, run) == _lib.FL_OK
                 assert L.fl_plan_option(P.handle, _lib.TUNE_ADJ_ROWS, rows) == _lib.FL_OK
                 assert np.array_equal(_host(P.adjoint(r)), x0), (run, rows)
+        assert sh["adjoint_view_chunks"] in (1, 4, 8, 16)
+        assert L.fl_plan_option(P.handle, _lib.TUNE_ADJ_CHUNKS, 0) == _lib.FL_ERR_INVALID
         assert L.fl_plan_option(P.handle, _lib.TUNE_ADJ_RUN, 3) == _lib.FL_ERR_INVALID
         assert L.fl_plan_option(P.handle, _lib.TUNE_ADJ_ROWS, 4) == _lib.FL_ERR_INVALID
 
