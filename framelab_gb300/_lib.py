@@ -28,6 +28,8 @@ TUNE_FAN_PARTS = 18
 TUNE_FAN_BLOCK = 19
 TUNE_FAN_GROUPS = 20
 TUNE_ADJ_CHUNKS = 21
+TUNE_FAN_TMA = 22
+DEBUG_TMA_TIMEOUTS = 23
 FRAMELET_OPT_FUSED = 1
 
 

@@ -150,8 +150,11 @@ struct fl_plan {
     void *d_vwork;
     size_t vwork_bytes;
     // fan plans: the forward's transposed copy of its input (n_vox elements
-    // of up to 4 bytes; allocated with the plan)
+    // of up to 4 bytes; allocated with the plan), made by TMA where possible
+    // (fan_tma.cu; FL_TUNE_FAN_TMA, default on) with its timeout flag
     void *d_xt;
+    int fan_tma_ok;
+    int *d_tma_err;
 };
 
 // The matched kernel form a plan uses (its options within what its geometry
@@ -239,6 +242,12 @@ int fl_plan_fan_groups(const fl_plan* p);
 // View chunks of a cone plan's reflection backprojection: the plan's setting
 // (FL_TUNE_ADJ_CHUNKS) where the output is FP32, else 1.
 int fl_plan_adj_chunks(const fl_plan* p, bool f32_out);
+
+// The fan forward's transposed copy of x by TMA (fan_tma.cu): false, with
+// nothing launched, where the plan, the input address or the row sizes do
+// not allow it.
+bool fl_fan_transpose_tma(fl_plan* p, const void* x, int dtype, cudaStream_t st);
+bool fl_tma_available();
 
 // internal launchers
 int fl_ref_forward(fl_plan* p, const float* x, float* y, cudaStream_t st);

@@ -87,7 +87,7 @@ static void free_plan_arrays(fl_plan* p)
                     p->d_view_frame, p->d_idY, p->d_Nv,        p->d_col,   p->d_colr,
                     p->d_row,    p->d_rowz,   p->d_view,       p->d_work,
                     p->d_cos_det2, p->d_sin_det2, p->d_fb_edges, p->d_vwork, p->d_xt,
-                    p->d_dq};
+                    p->d_dq, p->d_tma_err};
     for (void* q : ptrs)
         if (q) cudaFree(q);
 }
@@ -362,6 +362,12 @@ extern "C" int fl_plan_option(fl_plan* p, int option, int value)
         p->fan_block = value;
         return fl_set_error(FL_OK, "");
     }
+    if (option == FL_TUNE_FAN_TMA) {
+        if (value != 0 && value != 1)
+            return fl_set_error(FL_ERR_INVALID, "fl_plan_option: %d (0 or 1)", value);
+        p->fan_tma_ok = p->s.ndim == 2 && value && fl_tma_available() ? 1 : 0;
+        return fl_set_error(FL_OK, "");
+    }
     if (option == FL_TUNE_ADJ_CHUNKS) {
         if (value < 1 || value > 64)
             return fl_set_error(FL_ERR_INVALID, "fl_plan_option: %d view chunks (1 .. 64)", value);
@@ -419,6 +425,20 @@ extern "C" int fl_plan_query(const fl_plan* p, int option, int* value)
     }
     if (option == FL_TUNE_ADJ_CHUNKS) {
         *value = fl_plan_refl(p) && p->s.ndim == 3 ? fl_plan_adj_chunks(p, true) : 1;
+        return fl_set_error(FL_OK, "");
+    }
+    if (option == FL_TUNE_FAN_TMA) {
+        *value = p->fan_tma_ok;
+        return fl_set_error(FL_OK, "");
+    }
+    if (option == FL_DEBUG_TMA_TIMEOUTS) {          // and clears the flag
+        *value = 0;
+        if (p->d_tma_err) {
+            int st = fl_check_cuda(
+                cudaMemcpy(value, p->d_tma_err, sizeof(int), cudaMemcpyDeviceToHost), "cudaMemcpy");
+            if (!st) st = fl_check_cuda(cudaMemset(p->d_tma_err, 0, sizeof(int)), "cudaMemset");
+            if (st) return st;
+        }
         return fl_set_error(FL_OK, "");
     }
     return fl_set_error(FL_ERR_INVALID, "fl_plan_query: unknown option %d", option);
@@ -572,6 +592,11 @@ extern "C" int fl_plan_create(const fl_scan* scan, fl_plan** out)
     if (!st && s.ndim == 2)
         st = fl_check_cuda(fl_malloc(&p->d_xt, (size_t)p->n_vox * sizeof(float)),
                            "fl_malloc(plan)");
+    if (!st && s.ndim == 2) {
+        st = fl_check_cuda(fl_malloc((void**)&p->d_tma_err, sizeof(int)), "fl_malloc(plan)");
+        if (!st) st = fl_check_cuda(cudaMemset(p->d_tma_err, 0, sizeof(int)), "cudaMemset(plan)");
+        p->fan_tma_ok = fl_tma_available() ? 1 : 0;
+    }
     // quarter-turn reflection plans: the diagonal columns' second sums
     // between view chunks of the backprojection (matched.cu)
     if (!st && s.ndim == 3 && p->refl4_ok)

@@ -1480,11 +1480,16 @@ namespace {
 
 // The fan forward's transposed copy of its input (walk_fan), in the plan's
 // buffer (allocated with the plan: nothing is allocated here, so a forward
-// can be captured in a CUDA graph).
+// can be captured in a CUDA graph): by TMA where it applies, else by a
+// shared-memory tile transpose.
 template <typename TX>
 const TX* fan_transposed(fl_plan* p, const void* x, cudaStream_t st)
 {
     const fl_scan& s = p->s;
+    const int dt = std::is_same<TX, float>::value    ? FL_F32
+                   : std::is_same<TX, __half>::value ? FL_F16
+                                                     : FL_BF16;
+    if (fl_fan_transpose_tma(p, x, dt, st)) return (const TX*)p->d_xt;   // fan_tma.cu
     const dim3 grid(fl_div_up(s.nx, 32), fl_div_up(s.ny, 32), s.nt);
     k_transpose_fan<TX><<<grid, dim3(32, 8), 0, st>>>((const TX*)x, (TX*)p->d_xt, s.nx, s.ny,
                                                       p->n_vox_frame);

@@ -168,7 +168,8 @@ class Plan:
     # launch variants fl_plan_autotune chooses among (fl_plan_option values)
     TUNABLES = {"adj_run": _lib.TUNE_ADJ_RUN, "adj_rows": _lib.TUNE_ADJ_ROWS,
                 "fan_parts": _lib.TUNE_FAN_PARTS, "fan_block": _lib.TUNE_FAN_BLOCK,
-                "fan_groups": _lib.TUNE_FAN_GROUPS, "adj_chunks": _lib.TUNE_ADJ_CHUNKS}
+                "fan_groups": _lib.TUNE_FAN_GROUPS, "adj_chunks": _lib.TUNE_ADJ_CHUNKS,
+                "fan_tma": _lib.TUNE_FAN_TMA}
 
     def tuning(self, name: str) -> int:
         """The value in effect of a launch variant (``TUNABLES``)."""

@@ -283,6 +283,17 @@ enum { FL_TUNE_FAN_GROUPS = 20 };
  * applies where the backprojection writes FP32 (FP16 / BF16 outputs take one
  * launch). fl_plan_autotune times 1, 4, 8, 16. */
 enum { FL_TUNE_ADJ_CHUNKS = 21 };
+/* FL_TUNE_FAN_TMA: a fan plan's forward makes the transposed copy of its
+ * input that its walks read with the tensor memory accelerator (tiled
+ * cp.async.bulk.tensor loads and stores of 32 x 32 tiles through shared
+ * memory; 1, the default) or with plain loads and stores (0). The copy, and
+ * so every result, is the same either way. TMA needs the input on a 16-byte
+ * boundary and image rows of a multiple of 16 bytes (nx, ny multiples of 4 in
+ * FP32, 8 in FP16 / BF16); elsewhere the plain copy runs.
+ * FL_DEBUG_TMA_TIMEOUTS (query only): 1 if a TMA tile of this plan did not
+ * arrive within its bounded wait since the last query (the copy was then
+ * incomplete); the query clears it. */
+enum { FL_TUNE_FAN_TMA = 22, FL_DEBUG_TMA_TIMEOUTS = 23 };
 
 /* y = A x on `stream`. x: n_vox elements, y: n_rays elements, device memory.
  * The matched model works in buffers the plan owns: a z-mirror cone plan

@@ -1129,3 +1129,51 @@ def test_turn_plans_need_columns_of_four():
     yq = _host(Q.forward(_dev(x)))
     Q.rot_mirror = False
     assert _rel(yq, _host(Q.forward(_dev(x)))) < 1e-5
+
+
+@pytest.mark.parametrize("nx,ny,nt,dtype", [(64, 64, 1, "f32"), (100, 36, 1, "f32"),
+                                            (96, 64, 2, "f16"), (64, 48, 1, "bf16"),
+                                            (100, 36, 1, "f16"), (33, 31, 1, "f32")])
+def test_fan_transposed_copy_by_tma_keeps_the_bits(nx, ny, nt, dtype):
+    """The fan forward's transposed copy of its input is moved by TMA (tiled
+    bulk tensor loads and stores, 32 x 32 tiles) where the input starts on a
+    16-byte boundary and both row lengths are multiples of 16 bytes, else by
+    the plain tile transpose: the forwards agree bit for bit either way, for
+    every frame, in every storage type, and no tile times out. The ragged
+    sizes (100 x 36 FP16 rows of 72 bytes, 33 x 31) and an input one element
+    off the boundary take the plain copy."""
+    torch = _torch()
+    from framelab_gb300 import _lib
+    p = G.fan_para(nx, ny, 2 * max(nx, ny), 20, L=(1, ny / nx), SO=3.0, OD=3.0, Ly=3.0)
+    if nt > 1:
+        frames = np.arange(20, dtype=np.uint32) % nt
+        q = dict(p)
+        q["nt"] = np.uint32(nt)
+        q["id_X"] = frames
+        views = [np.where(frames == t)[0] for t in range(nt)]
+        tmp = max(len(v) for v in views)
+        idY = np.zeros((tmp, nt), np.uint32)
+        for t in range(nt):
+            idY[:len(views[t]), t] = views[t]
+        q["id_Y"], q["Nv"] = idY, np.array([len(v) for v in views], np.uint32)
+        q["tmp_size"] = np.uint32(tmp)
+        p = q
+    P = _plan(p)
+    assert P.tuning("fan_tma") == 1
+    td = {"f32": torch.float32, "f16": torch.float16, "bf16": torch.bfloat16}[dtype]
+    rng = np.random.default_rng(nx * ny + nt)
+    xs = rng.standard_normal(P.n_vox + 8).astype(np.float32)
+    x = _dev(xs, td)
+    for refl in (False, True):
+        P.reflect = refl
+        for xin in (x[:P.n_vox], x[1:P.n_vox + 1]):     # on and off the 16-byte boundary
+            P.set_tuning("fan_tma", 1)
+            y1 = _host(P.forward(xin))
+            P.set_tuning("fan_tma", 0)
+            assert P.tuning("fan_tma") == 0
+            y0 = _host(P.forward(xin))
+            assert np.array_equal(y1, y0), (refl, xin.data_ptr() % 16)
+    v = C.c_int(-1)
+    _lib.check(_lib.load().fl_plan_query(P.handle, _lib.DEBUG_TMA_TIMEOUTS, C.byref(v)))
+    assert v.value == 0
+    assert _lib.load().fl_plan_option(P.handle, _lib.TUNE_FAN_TMA, 2) == _lib.FL_ERR_INVALID
