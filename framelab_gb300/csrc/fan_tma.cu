@@ -29,12 +29,15 @@
 namespace {
 
 constexpr int kTile = 32;
+// rows of threads per block: 4 (128 threads, 8 KB of tiles) lets 16 blocks,
+// so 16 tile loads of 4 KB (FP32), be in flight per SM
+constexpr int kRows = 4;
 // mbarrier polls before a block gives up on its tile (a 4 KB load takes
 // microseconds; this is seconds): it then records the timeout and returns
 constexpr int kTmaPolls = 1 << 24;
 
 template <typename T>
-__global__ void __launch_bounds__(kTile * 8)
+__global__ void __launch_bounds__(kTile * kRows)
 k_transpose_tma(const __grid_constant__ CUtensorMap src, const __grid_constant__ CUtensorMap dst,
                 int* __restrict__ err)
 {
@@ -76,7 +79,7 @@ k_transpose_tma(const __grid_constant__ CUtensorMap src, const __grid_constant__
     // thread tx moves element (y = (k + tx) mod 32, x = tx), and the 32 lanes
     // of a warp read and write 32 different banks (FP32).
 #pragma unroll
-    for (int k = ty; k < kTile; k += 8) {
+    for (int k = ty; k < kTile; k += kRows) {
         const int c = (k + tx) & (kTile - 1);
         tout[tx * kTile + c] = tin[c * kTile + tx];
     }
@@ -143,7 +146,7 @@ bool fl_fan_transpose_tma(fl_plan* p, const void* x, int dtype, cudaStream_t st)
     if (!encode(&src, t, es, const_cast<void*>(x), s.nx, s.ny, s.nt) ||
         !encode(&dst, t, es, p->d_xt, s.ny, s.nx, s.nt))
         return false;
-    const dim3 grid(fl_div_up(s.nx, kTile), fl_div_up(s.ny, kTile), s.nt), blk(kTile, 8);
+    const dim3 grid(fl_div_up(s.nx, kTile), fl_div_up(s.ny, kTile), s.nt), blk(kTile, kRows);
     if (dtype == FL_F32) k_transpose_tma<float><<<grid, blk, 0, st>>>(src, dst, p->d_tma_err);
     else if (dtype == FL_F16) k_transpose_tma<__half><<<grid, blk, 0, st>>>(src, dst, p->d_tma_err);
     else k_transpose_tma<__nv_bfloat16><<<grid, blk, 0, st>>>(src, dst, p->d_tma_err);
