@@ -52,3 +52,26 @@ def test_plan_rejects_bad_geometry_without_touching_the_gpu():
     assert b"ndim" in L.fl_last_error()
     s.ndim = 3; s.nx = s.ny = s.nz = 8; s.nv = 0; s.na = s.nb = 4
     assert L.fl_plan_create(C.byref(s), C.byref(h)) == _lib.FL_ERR_INVALID
+
+
+def test_python_constants_match_the_header_enums():
+    """Every enumerator of include/*.h that the Python binding also names
+    (with or without the FL_ prefix) has the same value there, and the
+    plan options, tunables and status codes are all named."""
+    values = {}
+    for f in os.listdir(os.path.join(ROOT, "include")):
+        if not f.endswith(".h"):
+            continue
+        src = re.sub(r"/\*.*?\*/", "", open(os.path.join(ROOT, "include", f)).read(), flags=re.S)
+        for body in re.findall(r"\benum\s*\{(.*?)\}", src, flags=re.S):
+            for m in re.finditer(r"\b(FL_\w+)\s*=\s*(\d+)", body):
+                values[m.group(1)] = int(m.group(2))
+    assert len(values) >= 30
+    matched = {}
+    for name, v in values.items():
+        for py in (name, name[3:]):
+            if hasattr(_lib, py):
+                assert getattr(_lib, py) == v, (name, py)
+                matched[name] = py
+    must = [n for n in values if n.startswith(("FL_OPT_", "FL_TUNE_", "FL_ERR_", "FL_DEBUG_"))]
+    assert not [n for n in must if n not in matched], must
