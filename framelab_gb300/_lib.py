@@ -30,6 +30,7 @@ TUNE_FAN_GROUPS = 20
 TUNE_ADJ_CHUNKS = 21
 TUNE_FAN_TMA = 22
 DEBUG_TMA_TIMEOUTS = 23
+DEBUG_TMA_STALL = 24
 FRAMELET_OPT_FUSED = 1
 
 

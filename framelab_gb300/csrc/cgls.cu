@@ -624,6 +624,10 @@ extern "C" int fl_cgls_solve(fl_cgls* c, const float* b, float* u, float lam, in
                                (cudaStream_t)stream)
                  : solve_mixed(c, b, u, lam, iters, tol, refresh, flags, gamma_history, iters_done,
                                (cudaStream_t)stream);
+    if (!st || st == FL_ERR_NUMERIC) {   // a forward's TMA wait gave up: the cause of any NaN
+        const int t = fl_plan_take_timeouts(c->plan, (cudaStream_t)stream);
+        if (t) return t;
+    }
     if (st) return st;
     return fl_set_error(FL_OK, "");
 }

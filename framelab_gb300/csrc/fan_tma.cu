@@ -35,11 +35,14 @@ constexpr int kRows = 4;
 // mbarrier polls before a block gives up on its tile (a 4 KB load takes
 // microseconds; this is seconds): it then records the timeout and returns
 constexpr int kTmaPolls = 1 << 24;
+// stall > 0 (FL_DEBUG_TMA_STALL, tests only): no load is issued and the block
+// waits, for stall polls, on a phase that nothing completes, so the timeout
+// path runs with no copy in flight.
 
 template <typename T>
 __global__ void __launch_bounds__(kTile * kRows)
 k_transpose_tma(const __grid_constant__ CUtensorMap src, const __grid_constant__ CUtensorMap dst,
-                int* __restrict__ err)
+                int* __restrict__ err, int stall)
 {
     __shared__ alignas(128) T tin[kTile * kTile];
     __shared__ alignas(128) T tout[kTile * kTile];
@@ -52,18 +55,21 @@ k_transpose_tma(const __grid_constant__ CUtensorMap src, const __grid_constant__
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sbar) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
-                     ::"r"(sbar), "r"((unsigned)(kTile * kTile * sizeof(T)))
-                     : "memory");
-        asm volatile(
-            "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
-            " [%0], [%1, {%2, %3, %4}], [%5];"
-            ::"r"(sin), "l"(&src), "r"(x0), "r"(y0), "r"(f), "r"(sbar)
-            : "memory");
+        if (!stall) {
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                         ::"r"(sbar), "r"((unsigned)(kTile * kTile * sizeof(T)))
+                         : "memory");
+            asm volatile(
+                "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+                " [%0], [%1, {%2, %3, %4}], [%5];"
+                ::"r"(sin), "l"(&src), "r"(x0), "r"(y0), "r"(f), "r"(sbar)
+                : "memory");
+        }
     }
     __syncthreads();                       // the barrier is set up before anyone waits
     unsigned done = 0;
-    for (int i = 0; i < kTmaPolls && !done; i++)
+    const int polls = stall ? stall : kTmaPolls;
+    for (int i = 0; i < polls && !done; i++)
         asm volatile(
             "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;"
             " selp.u32 %0, 1, 0, p; }"
@@ -147,8 +153,10 @@ bool fl_fan_transpose_tma(fl_plan* p, const void* x, int dtype, cudaStream_t st)
         !encode(&dst, t, es, p->d_xt, s.ny, s.nx, s.nt))
         return false;
     const dim3 grid(fl_div_up(s.nx, kTile), fl_div_up(s.ny, kTile), s.nt), blk(kTile, kRows);
-    if (dtype == FL_F32) k_transpose_tma<float><<<grid, blk, 0, st>>>(src, dst, p->d_tma_err);
-    else if (dtype == FL_F16) k_transpose_tma<__half><<<grid, blk, 0, st>>>(src, dst, p->d_tma_err);
-    else k_transpose_tma<__nv_bfloat16><<<grid, blk, 0, st>>>(src, dst, p->d_tma_err);
+    int* e = p->d_tma_err;
+    const int z = p->tma_stall;
+    if (dtype == FL_F32) k_transpose_tma<float><<<grid, blk, 0, st>>>(src, dst, e, z);
+    else if (dtype == FL_F16) k_transpose_tma<__half><<<grid, blk, 0, st>>>(src, dst, e, z);
+    else k_transpose_tma<__nv_bfloat16><<<grid, blk, 0, st>>>(src, dst, e, z);
     return true;
 }

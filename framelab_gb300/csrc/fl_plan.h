@@ -155,6 +155,7 @@ struct fl_plan {
     void *d_xt;
     int fan_tma_ok;
     int *d_tma_err;
+    int tma_stall;   // FL_DEBUG_TMA_STALL (tests): polls of a wait nothing ends
 };
 
 // The matched kernel form a plan uses (its options within what its geometry
@@ -248,6 +249,10 @@ int fl_plan_adj_chunks(const fl_plan* p, bool f32_out);
 // not allow it.
 bool fl_fan_transpose_tma(fl_plan* p, const void* x, int dtype, cudaStream_t st);
 bool fl_tma_available();
+// FL_ERR_TIMEOUT (and the flag cleared) if a TMA tile load of one of the
+// plan's forwards gave up its bounded wait since the last check; reads the
+// flag after synchronising the stream. FL_OK for plans without the flag.
+int fl_plan_take_timeouts(fl_plan* p, cudaStream_t s);
 
 // internal launchers
 int fl_ref_forward(fl_plan* p, const float* x, float* y, cudaStream_t st);

@@ -362,6 +362,12 @@ extern "C" int fl_plan_option(fl_plan* p, int option, int value)
         p->fan_block = value;
         return fl_set_error(FL_OK, "");
     }
+    if (option == FL_DEBUG_TMA_STALL) {
+        if (value < 0 || value > (1 << 20))
+            return fl_set_error(FL_ERR_INVALID, "fl_plan_option: %d polls (0 .. 2^20)", value);
+        p->tma_stall = value;
+        return fl_set_error(FL_OK, "");
+    }
     if (option == FL_TUNE_FAN_TMA) {
         if (value != 0 && value != 1)
             return fl_set_error(FL_ERR_INVALID, "fl_plan_option: %d (0 or 1)", value);
@@ -432,16 +438,33 @@ extern "C" int fl_plan_query(const fl_plan* p, int option, int* value)
         return fl_set_error(FL_OK, "");
     }
     if (option == FL_DEBUG_TMA_TIMEOUTS) {          // and clears the flag
-        *value = 0;
-        if (p->d_tma_err) {
-            int st = fl_check_cuda(
-                cudaMemcpy(value, p->d_tma_err, sizeof(int), cudaMemcpyDeviceToHost), "cudaMemcpy");
-            if (!st) st = fl_check_cuda(cudaMemset(p->d_tma_err, 0, sizeof(int)), "cudaMemset");
-            if (st) return st;
-        }
+        const int st = fl_plan_take_timeouts(const_cast<fl_plan*>(p), nullptr);
+        *value = st == FL_ERR_TIMEOUT;
+        if (st && st != FL_ERR_TIMEOUT) return st;
+        return fl_set_error(FL_OK, "");
+    }
+    if (option == FL_DEBUG_TMA_STALL) {
+        *value = p->tma_stall;
         return fl_set_error(FL_OK, "");
     }
     return fl_set_error(FL_ERR_INVALID, "fl_plan_query: unknown option %d", option);
+}
+
+int fl_plan_take_timeouts(fl_plan* p, cudaStream_t s)
+{
+    if (!p || !p->d_tma_err) return FL_OK;
+    int v = 0;
+    int st = fl_check_cuda(cudaMemcpyAsync(&v, p->d_tma_err, sizeof v, cudaMemcpyDeviceToHost, s),
+                           "cudaMemcpyAsync");
+    if (!st) st = fl_check_cuda(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    if (st || !v) return st;
+    st = fl_check_cuda(cudaMemsetAsync(p->d_tma_err, 0, sizeof v, s), "cudaMemsetAsync");
+    if (!st) st = fl_check_cuda(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    if (st) return st;
+    return fl_set_error(FL_ERR_TIMEOUT,
+                        "a TMA tile load of the fan forward's transposed copy did not arrive "
+                        "within its bounded wait: the projections since the last check are "
+                        "incomplete");
 }
 
 extern "C" int fl_plan_create(const fl_scan* scan, fl_plan** out)

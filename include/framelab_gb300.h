@@ -294,6 +294,13 @@ enum { FL_TUNE_ADJ_CHUNKS = 21 };
  * arrive within its bounded wait since the last query (the copy was then
  * incomplete); the query clears it. */
 enum { FL_TUNE_FAN_TMA = 22, FL_DEBUG_TMA_TIMEOUTS = 23 };
+/* FL_DEBUG_TMA_STALL (tests only; 0, the default, is off): the plan's TMA
+ * copy issues no load and each block waits N polls on a barrier phase that
+ * nothing completes, then records the timeout and returns, with no copy in
+ * flight. fl_cgls_solve (and so fl_cgls_solve_host and the split-Bregman
+ * solves) then return FL_ERR_TIMEOUT, and clear the flag, when a forward of
+ * the solve timed out. N in 0 .. 2^20. */
+enum { FL_DEBUG_TMA_STALL = 24 };
 
 /* y = A x on `stream`. x: n_vox elements, y: n_rays elements, device memory.
  * The matched model works in buffers the plan owns: a z-mirror cone plan

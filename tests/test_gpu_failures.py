@@ -122,3 +122,45 @@ def test_batch_nonfinite_slice_is_reported_and_others_complete():
     assert e.value.code == _lib.FL_ERR_NUMERIC and "slice 1" in str(e.value)
     assert list(B.iters_done) == [4, 0, 4]      # the other slices ran to the end
     assert torch.equal(B.cgls(rhs, iters=4), good)
+
+
+def test_tma_wait_that_runs_out_is_reported_and_the_context_stays_usable():
+    """The fan forward's TMA copy waits on an mbarrier for a bounded number of
+    polls. FL_DEBUG_TMA_STALL makes that wait run out with nothing in flight
+    (no load is issued; the phase it waits on is never completed): the plan's
+    flag reads 1 once and is then cleared, a solve whose forwards timed out
+    returns FL_ERR_TIMEOUT, and with the hook off the same plan and context
+    give the same bits as before."""
+    import ctypes as C
+    import torch
+    from framelab_gb300 import _lib
+    from framelab_gb300.projector import Plan
+    from framelab_gb300.solvers import NativeCGLS
+    L = _lib.load()
+    P = Plan(G.fan_para(64, 64, 128, 20, L=(1, 1), SO=3.0, OD=3.0, Ly=3.0))
+    assert P.tuning("fan_tma") == 1
+    x = torch.from_numpy(PH.ellipses_2d(64, seed=3).reshape(-1)).cuda()
+    y = P.forward(x).clone()
+    b = P.adjoint(y).reshape(-1).contiguous()
+    want = NativeCGLS(P, "plain").solve(b, iters=3).clone()
+
+    def flag():
+        v = C.c_int(-1)
+        _lib.check(L.fl_plan_query(P.handle, _lib.DEBUG_TMA_TIMEOUTS, C.byref(v)))
+        return v.value
+
+    assert flag() == 0
+    assert L.fl_plan_option(P.handle, _lib.DEBUG_TMA_STALL, -1) == _lib.FL_ERR_INVALID
+    _lib.check(L.fl_plan_option(P.handle, _lib.DEBUG_TMA_STALL, 1000))
+    P.forward(x)
+    torch.cuda.synchronize()
+    assert flag() == 1 and flag() == 0            # read once, then cleared
+    cg = NativeCGLS(P, "plain")
+    with pytest.raises(_lib.FLError) as e:
+        cg.solve(b, iters=3)
+    assert e.value.code == _lib.FL_ERR_TIMEOUT
+    assert flag() == 0
+    _lib.check(L.fl_plan_option(P.handle, _lib.DEBUG_TMA_STALL, 0))
+    assert torch.equal(P.forward(x), y)
+    assert torch.equal(NativeCGLS(P, "plain").solve(b, iters=3), want)
+    assert flag() == 0
