@@ -435,7 +435,11 @@ void fl_sb_destroy(fl_sb *sb);
 
 /* The same solve with host buffers (the mex-style boundary): b and u0 are
  * copied to the device (u0 skipped with FL_CGLS_ZERO_START), the result is
- * copied back into u. Device copies are kept in the workspace for reuse. */
+ * copied back into u. Device copies are kept in the workspace for reuse.
+ * Exception, same results: with a z-mirror plan in the graph or mixed form,
+ * b and u pinned (cudaHostAlloc) or registered (cudaHostRegister), the
+ * solve's fold reads b (and u0) and its unfold writes u in host memory
+ * directly, with no staging copies. Returns once u holds the result. */
 int fl_cgls_solve_host(fl_cgls *cg, const float *b_host, float *u_host, float lam, int iters,
                        double tol, int refresh, int flags, double *gamma_history,
                        int *iters_done, void *stream);

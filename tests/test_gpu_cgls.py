@@ -96,3 +96,33 @@ def test_cgls_z_folded_vectors_follow_the_plan_option(mode):
     assert torch.equal(u_m, u_m2)
     u64, _ = _oracle_solution(p, b, 0.5, 6)
     assert np.linalg.norm(u_m.cpu().numpy() - u64) / np.linalg.norm(u64) < 1e-3
+
+
+@pytest.mark.parametrize("mode", ["plain", "graph", "mixed"])
+def test_host_buffer_solve_equals_the_device_solve(mode):
+    """fl_cgls_solve_host gives the device solve's bits, from pageable numpy
+    buffers (staged copies) and from pinned ones (a z-mirror plan in the
+    graph and mixed forms reads b and writes u in host memory directly), with
+    a zero start and with a given u0 (read in place too)."""
+    import torch
+    from framelab_gb300.projector import Plan
+    from framelab_gb300.solvers import NativeCGLS
+    p = G.cone_para_mm(24, 20, 36, 28, det_pitch_mm=8.0, SO_mm=600.0, SD_mm=1200.0,
+                       voxel_mm=8.0)
+    P = Plan(p)
+    assert P.z_mirror
+    x = torch.from_numpy(PH.ellipsoids_3d(24, seed=5).reshape(-1)).cuda()
+    b = P.adjoint(P.forward(x)).reshape(-1).contiguous()
+    cg = NativeCGLS(P, mode)
+    want = cg.solve(b, iters=4).cpu().numpy()
+    u0 = (0.5 * x).contiguous()
+    want0 = cg.solve(b, u0=u0, iters=3, zero_start=False).cpu().numpy()
+    for pinned in (False, True):
+        bh = torch.empty(b.numel(), dtype=torch.float32, pin_memory=pinned)
+        uh = torch.full((b.numel(),), 7.0, dtype=torch.float32, pin_memory=pinned)
+        bh.copy_(b.cpu())
+        got = cg.solve_host(bh.numpy(), uh.numpy(), iters=4)
+        assert np.array_equal(got, want), (mode, pinned)
+        uh.copy_(u0.cpu())
+        got0 = cg.solve_host(bh.numpy(), uh.numpy(), iters=3, zero_start=False)
+        assert np.array_equal(got0, want0), (mode, pinned)
