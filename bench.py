@@ -736,7 +736,8 @@ def run_single(ctx, name, w, p):
         e2e = {"value": world * K / t_e, "unit": "iter/s",
                "h2d_bytes_per_step": nb / K, "d2h_bytes_per_step": nb / K,
                "call": f"fl_cgls_solve_host, {K} iterations per call: b in, u out "
-                       "(u0 = 0 needs no copy)"}
+                       "(pinned host buffers, read and written in place by the fold "
+                       "kernels over the host link; u0 = 0 needs no transfer)"}
     roofline = None
     if "kernels" in ctx.legs:
         cnt = P.count_intersections()
