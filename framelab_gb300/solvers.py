@@ -76,7 +76,10 @@ class NativeCGLS:
 
     def solve_host(self, b: np.ndarray, u: np.ndarray, lam: float = 0.0, iters: int = 20,
                    tol: float = 1e-14, refresh: int = 10, zero_start: bool = True) -> np.ndarray:
-        """Host-buffer solve (pinned or pageable numpy float32 arrays); u is overwritten."""
+        """Host-buffer solve (pinned or pageable numpy float32 arrays); u is overwritten.
+        Pinned arrays (e.g. ``torch.empty(n, pin_memory=True).numpy()``) with a
+        z-mirror plan in the graph or mixed form are read and written in place
+        by the solve's fold kernels; other arrays are copied."""
         hist = np.zeros(max(iters, 1), np.float64)
         nd = C.c_int()
         st = self._L.fl_cgls_solve_host(self._h, b.ctypes.data, u.ctypes.data, float(lam),
