@@ -83,7 +83,7 @@ k_transpose_tma(const __grid_constant__ CUtensorMap src, const __grid_constant__
     // tin[y][x] (x fastest) -> tout[x][y] (y fastest). Both tiles stay dense
     // (the TMA boxes), so the order is skewed instead of padded: at step k,
     // thread tx moves element (y = (k + tx) mod 32, x = tx), and the 32 lanes
-    // of a warp read and write 32 different banks (FP32).
+    // of a warp address 32 different banks on both sides (FP32).
 #pragma unroll
     for (int k = ty; k < kTile; k += kRows) {
         const int c = (k + tx) & (kTile - 1);
