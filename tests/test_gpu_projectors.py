@@ -1141,7 +1141,8 @@ def test_fan_transposed_copy_by_tma_keeps_the_bits(nx, ny, nt, dtype):
     the plain tile transpose: the forwards agree bit for bit either way, for
     every frame, in every storage type, and no tile times out. The ragged
     sizes (100 x 36 FP16 rows of 72 bytes, 33 x 31) and an input one element
-    off the boundary take the plain copy."""
+    off the boundary take the plain copy; the stall hook (FL_DEBUG_TMA_STALL,
+    whose timeout only the TMA kernel reports) shows which copy ran."""
     torch = _torch()
     from framelab_gb300 import _lib
     p = G.fan_para(nx, ny, 2 * max(nx, ny), 20, L=(1, ny / nx), SO=3.0, OD=3.0, Ly=3.0)
@@ -1173,7 +1174,26 @@ def test_fan_transposed_copy_by_tma_keeps_the_bits(nx, ny, nt, dtype):
             assert P.tuning("fan_tma") == 0
             y0 = _host(P.forward(xin))
             assert np.array_equal(y1, y0), (refl, xin.data_ptr() % 16)
-    v = C.c_int(-1)
-    _lib.check(_lib.load().fl_plan_query(P.handle, _lib.DEBUG_TMA_TIMEOUTS, C.byref(v)))
-    assert v.value == 0
-    assert _lib.load().fl_plan_option(P.handle, _lib.TUNE_FAN_TMA, 2) == _lib.FL_ERR_INVALID
+    L = _lib.load()
+
+    def timed_out():
+        v = C.c_int(-1)
+        _lib.check(L.fl_plan_query(P.handle, _lib.DEBUG_TMA_TIMEOUTS, C.byref(v)))
+        return v.value
+
+    assert timed_out() == 0
+
+    def took_tma(xin):
+        # with the stall hook only the TMA kernel raises the timeout flag
+        P.set_tuning("fan_tma", 1)
+        _lib.check(L.fl_plan_option(P.handle, _lib.DEBUG_TMA_STALL, 16))
+        P.forward(xin)
+        torch.cuda.synchronize()
+        _lib.check(L.fl_plan_option(P.handle, _lib.DEBUG_TMA_STALL, 0))
+        return timed_out() == 1
+
+    es = 4 if dtype == "f32" else 2
+    assert took_tma(x[:P.n_vox]) == ((nx * es) % 16 == 0 and (ny * es) % 16 == 0)
+    assert not took_tma(x[1:P.n_vox + 1])
+    assert timed_out() == 0
+    assert L.fl_plan_option(P.handle, _lib.TUNE_FAN_TMA, 2) == _lib.FL_ERR_INVALID
