@@ -317,6 +317,57 @@ __device__ float chord_box(float px, float py, float pz, float qx, float qy, flo
     return fsqrt(fadd(fadd(fmul(ex, ex), fmul(ey, ey)), fmul(ez, ez)));
 }
 
+// chord_box for a unit cube (w = h = t = 1) when the in-plane direction
+// (a, b) has no zero component, with the x- and y-face families' in-plane
+// crossings u0x, u1x (the b / a family) and u0y, u1y (the a / b family)
+// computed by the caller once per detector column. Every value is the same
+// float expression chord_box evaluates, so the result has the same bits.
+__device__ float chord_box_col(float a, float b, float c, float u0x, float u1x, float u0y,
+                               float u1y, float rx, float ry, float rz)
+{
+    const float hw = 0.5f, hh = 0.5f, ht = 0.5f;          // fdiv(1, 2), exact
+    float P0[3] = {0, 0, 0}, P1[3] = {0, 0, 0};
+    int nh = 0;
+    int f0 = (fabs_ref(a) > fabs_ref(b)) ? 0 : 1;
+#pragma unroll
+    for (int pass = 0; pass < 3; pass++) {
+        if (pass > 0 && nh >= 2) break;
+        int fam = (pass == 0) ? f0 : (pass == 1 ? 1 - f0 : 2);
+        float u0, u1, v0, v1, lim0, lim1;
+        if (fam == 0) {
+            u0 = u0x; u1 = u1x;
+            float s = fdiv(c, a); v0 = fadd(fmul(s, -rx), rz); v1 = fmul(s, hw);
+            lim0 = hh; lim1 = ht;
+        } else if (fam == 1) {
+            u0 = u0y; u1 = u1y;
+            float s = fdiv(c, b); v0 = fadd(fmul(s, -ry), rz); v1 = fmul(s, hh);
+            lim0 = hw; lim1 = ht;
+        } else {
+            float s = fdiv(a, c); u0 = fadd(fmul(s, -rz), rx); u1 = fmul(s, ht);
+            s = fdiv(b, c);       v0 = fadd(fmul(s, -rz), ry); v1 = fmul(s, ht);
+            lim0 = hw; lim1 = hh;
+        }
+#pragma unroll
+        for (int side = 0; side < 2; side++) {
+            if (pass > 0 && side == 1 && nh >= 2) break;
+            float uu = side ? fadd(u0, u1) : fsub(u0, u1);
+            float vv = side ? fadd(v0, v1) : fsub(v0, v1);
+            if (fabs_ref(uu) <= lim0 && fabs_ref(vv) <= lim1) {
+                float q0, q1, q2;
+                if (fam == 0)      { q0 = side ? hw : -hw; q1 = uu; q2 = vv; }
+                else if (fam == 1) { q0 = uu; q1 = side ? hh : -hh; q2 = vv; }
+                else               { q0 = uu; q1 = vv; q2 = side ? ht : -ht; }
+                if (nh == 0) { P0[0] = q0; P0[1] = q1; P0[2] = q2; }
+                else         { P1[0] = q0; P1[1] = q1; P1[2] = q2; }
+                nh++;
+            }
+        }
+    }
+    if (nh != 2) return 0.0f;
+    float ex = fsub(P1[0], P0[0]), ey = fsub(P1[1], P0[1]), ez = fsub(P1[2], P0[2]);
+    return fsqrt(fadd(fadd(fmul(ex, ex), fmul(ey, ey)), fmul(ez, ez)));
+}
+
 // Fan-beam chord backprojection, restating Atx_fan_mf_cpu_new.cpp:21-63.
 // One thread per (pixel, frame).
 __global__ void __launch_bounds__(128)
@@ -362,7 +413,13 @@ k_ref_fan_chord_adj(float* __restrict__ x, const float* __restrict__ Y,
 }
 
 // Cone-beam chord backprojection, restating Atx_cone_mf_cpu_new.cpp:23-85
-// (unit-cube chord, z window half-width sqrt(1 + dz^2/2)).
+// (unit-cube chord, z window half-width sqrt(1 + dz^2/2)). Per view, the
+// detector columns of a voxel's window (up to kChordCols of them) get their
+// row-independent find_l_3d terms once, in shared memory (one slot per
+// thread), and every row of the window reuses them; wider windows take the
+// plain per-(column, row) evaluation. The sums run in the reference's order.
+constexpr int kChordCols = 8;
+
 __global__ void __launch_bounds__(128)
 k_ref_cone_chord_adj(float* __restrict__ x, const float* __restrict__ Y,
                      const float* __restrict__ cos_phi, const float* __restrict__ sin_phi,
@@ -376,6 +433,9 @@ k_ref_cone_chord_adj(float* __restrict__ x, const float* __restrict__ Y,
     int iy = blockIdx.y;
     int izt = blockIdx.z;            // iz + nz * it
     int iz = izt % nz, it = izt / nz;
+    // the window columns' row-independent terms, one slot per thread
+    __shared__ float cols[6][kChordCols][128];
+    const int t = threadIdx.x;
     if (ix >= nx) return;
     float SD = fadd(SO, OD);
     int na2 = na / 2, nb2 = nb / 2, nx2 = nx / 2, ny2 = ny / 2, nz2 = nz / 2;
@@ -402,6 +462,42 @@ k_ref_cone_chord_adj(float* __restrict__ x, const float* __restrict__ Y,
         bmin = max(bmin, 0); bmax = min(bmax, nb - 1);
         float x1 = fmul(c, -SO), y1 = fmul(s, -SO), z1 = sdz[iv];
         float cOD = fmul(c, OD), sOD = fmul(s, OD);
+        const int W = amax - amin + 1;
+        if (W >= 1 && W <= kChordCols) {
+            // chord_box's offsets of the source from the voxel centre
+            const float rx = fsub(x1, xc), ry = fsub(y1, yc), rz = fsub(z1, zc);
+            for (int k = 0; k < W; k++) {
+                const float u = __ldg(ydet + amin + k);
+                const float x2 = fsub(cOD, fmul(s, u)), y2 = fadd(sOD, fmul(c, u));
+                const float a = fsub(x2, x1), b = fsub(y2, y1);
+                float u0x = 0.0f, u1x = 0.0f, u0y = 0.0f, u1y = 0.0f;
+                if (a != 0.0f && b != 0.0f) {
+                    float q = fdiv(b, a);
+                    u0x = fadd(fmul(q, -rx), ry); u1x = fmul(q, 0.5f);
+                    q = fdiv(a, b);
+                    u0y = fadd(fmul(q, -ry), rx); u1y = fmul(q, 0.5f);
+                }
+                cols[0][k][t] = x2; cols[1][k][t] = y2;
+                cols[2][k][t] = u0x; cols[3][k][t] = u1x;
+                cols[4][k][t] = u0y; cols[5][k][t] = u1y;
+            }
+            for (int ib = bmin; ib <= bmax; ib++) {
+                const float z2 = fadd(__ldg(zdet + ib), z1);
+                const float cz = fsub(z2, z1);
+                const float* yr_ = yv + (long long)ib * na + amin;
+                for (int k = 0; k < W; k++) {
+                    const float x2 = cols[0][k][t], y2 = cols[1][k][t];
+                    const float a = fsub(x2, x1), b = fsub(y2, y1);
+                    const float l =
+                        (a == 0.0f || b == 0.0f)
+                            ? chord_box(x1, y1, z1, x2, y2, z2, 1.0f, 1.0f, 1.0f, xc, yc, zc)
+                            : chord_box_col(a, b, cz, cols[2][k][t], cols[3][k][t],
+                                            cols[4][k][t], cols[5][k][t], rx, ry, rz);
+                    acc = fadd(acc, fmul(l, __ldg(yr_ + k)));
+                }
+            }
+            continue;
+        }
         for (int ib = bmin; ib <= bmax; ib++) {
             float z2 = fadd(__ldg(zdet + ib), z1);
             for (int ia = amin; ia <= amax; ia++) {

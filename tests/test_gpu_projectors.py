@@ -112,6 +112,20 @@ def test_chord_ref_random_geometries_bit_exact(seed):
     assert np.array_equal(xc, O.cone_adj_f32(yc, pc))
 
 
+def test_chord_ref_narrow_and_wide_windows_bit_exact():
+    """The cone chord backprojector takes the row-independent find_l_3d terms
+    of a voxel's window columns from a per-thread cache when the window has
+    at most 8 columns, and evaluates every (column, row) when it is wider:
+    both give the reference's bits (coarse panel: narrow windows; medium:
+    6 to 13 columns, both paths in one volume; fine: 16 to 34 columns)."""
+    rng = np.random.default_rng(31)
+    for na, Ly in ((14, 6.0), (48, 4.0), (96, 3.0)):
+        pc = G.cone_para(12, 12, 12, na, 16, 5, L=(2, 2, 2), SO=4.0, OD=4.0, Ly=Ly, Lz=4.0)
+        yc = rng.standard_normal(na * 16 * 5).astype(np.float32)
+        xc = _host(_plan(pc).adjoint(_dev(yc), model="chord_ref"))
+        assert np.array_equal(xc, O.cone_adj_f32(yc, pc)), na
+
+
 # --------------------------------------------------------------------------
 # drop-in entry points through the C ABI, host pointers (the mex boundary)
 # --------------------------------------------------------------------------
